@@ -1,0 +1,228 @@
+/*
+ * vedo_gpu.h - C ABI of the GB300 DEM time-step engine.
+ *
+ * The engine replaces, behind one handle, the container-level loops that the
+ * reference drives once per time step from SimMediator::Run()
+ * (src/vedo/framework/SimMediator.cpp:714-842):
+ *   IactContainer::CalculateImpact    (IactContainer.cpp:33-37)  impact solving
+ *   DOContainer::AddFieldImpact       (DOContainer.cpp:20-27)    field impulse
+ *   DOContainer::AddConstrainedImpact (DOContainer.cpp:47-50)    external force
+ *   DOContainer::Response             (DOContainer.cpp:52-55)    integration
+ *   IactContainer::CheckContactStatus (IactContainer.cpp:47-50)  narrow phase
+ *   Consultant::NextStep / Reset      (NBSConsultant.cpp:35-316) broad phase,
+ *   RebuildIactRecordTab + Initiate   (NBSConsultant.cpp:376-395,
+ *                                      SimMediator.cpp:640-712)  history carry
+ * The reference has no FFI of its own: its plugin surface is the C++ class
+ * hierarchy (ContactDetector::Detect, ContactDetector.h:50; ImpactSolver::
+ * NextStep, ImpactSolver.h:22-23; DiscreteObject::Response,
+ * DiscreteObject.h:107; Consultant, Consultant.h:87-154) selected through the
+ * factories registered in CreateNewAssembler (ModuleList.h:42-77).  These entry
+ * points are what a SimMediator-level binding calls instead; every argument is
+ * a plain pointer or size, and every function returns a status code instead of
+ * calling exit() as the reference does on bad input.
+ *
+ * Units and layouts follow the reference: FP64 everywhere, 3-vectors as
+ * [n][3] row-major double arrays, object indices are the DOWorld indices
+ * (uint32, the reference's _INT32 build).
+ */
+#ifndef VEDO_GPU_H
+#define VEDO_GPU_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes ------------------------------------------------------ */
+enum {
+    VEDO_OK = 0,
+    VEDO_ERR_INVALID_ARGUMENT = 1,  /* NULL handle/pointer, size mismatch            */
+    VEDO_ERR_INVALID_SCENE = 2,     /* unknown model, bad index, empty world          */
+    VEDO_ERR_UNSUPPORTED_MODEL = 3, /* no detector/solver for a shape pair or
+                                       equation type (the factories' null result,
+                                       Assembler.cpp:72-85), or a feature the engine
+                                       does not implement (e.g. periodic boundary)   */
+    VEDO_ERR_OUT_OF_MEMORY = 4,     /* device allocation failed / admission rejected  */
+    VEDO_ERR_CUDA = 5,              /* any other CUDA runtime error                   */
+    VEDO_ERR_DEVICE_TIMEOUT = 6,    /* a bounded device wait gave up                  */
+    VEDO_ERR_BAD_IDO = 7,           /* unreadable, truncated or inconsistent .ido     */
+    VEDO_ERR_IO = 8                 /* output file could not be written               */
+};
+
+/* ---- enums mirrored from DOModel.h:25-27 (C++11 build) ------------------ */
+enum { VEDO_SHAPE_SPHERE = 1, VEDO_SHAPE_QUASI_CYLINDER = 6, VEDO_SHAPE_QUASI_PLATE = 7 };
+enum { VEDO_CONSTRAINED = 1, VEDO_FIXED = 2, VEDO_MOBILE = 3, VEDO_ORBITAL = 4 };
+enum { VEDO_SCOPE_GLOBAL = 1, VEDO_SCOPE_LOCAL = 2 };
+
+/* ---- scene description (what DOWorld holds, DOWorld.h) ----------------- */
+typedef struct vedo_do_model {
+    const char* name;          /* DOModel name                                     */
+    const char* group;         /* DOGroup; interaction models are found by group   */
+    uint32_t behavior;         /* VEDO_CONSTRAINED/FIXED/MOBILE/ORBITAL            */
+    uint32_t scope;            /* VEDO_SCOPE_GLOBAL/LOCAL                          */
+    uint32_t shape;            /* VEDO_SHAPE_*                                     */
+    uint32_t reserved;
+    double density;
+    double density_factor;
+    double external_force[3];
+    double attrs[10];          /* DOShapeAttributes union: sphere {radius};
+                                  quasicylinder {radius, height};
+                                  quasiplate {width, height, length}               */
+} vedo_do_model;
+
+typedef struct vedo_iact_model {
+    const char* master_group;
+    const char* slave_group;
+    const char* equation_type;               /* "ISwBSDBF", "ISwHertz", ...       */
+    uint32_t num_mechanisms;
+    const char* const* mechanism_names;      /* e.g. "NormalStiffness"            */
+    const double* mechanism_values;
+} vedo_iact_model;
+
+typedef struct vedo_scene_desc {
+    /* SystemParameter (SystemParameter.h) */
+    double time_start, time_stop, time_interval, time_current;
+    double field_acceleration[3];
+    double safety_factor;                    /* aries::Constants SafetyFactor     */
+    uint8_t zoi_switch[3], pbc_switch[3];
+    uint8_t reserved[2];
+    double zoi_lower[3], zoi_upper[3];
+    double pbc_lower[3], pbc_upper[3];
+    uint32_t max_id_of_do;
+    /* models */
+    uint32_t num_models;
+    const vedo_do_model* models;
+    uint32_t num_iact_models;
+    const vedo_iact_model* iact_models;
+    /* DOStatus, one entry per discrete object, [n][3] doubles each */
+    uint32_t num_objects;
+    const uint32_t* object_model;            /* index into models                 */
+    const uint32_t* object_id;               /* DOStatus ulID (may be NULL)       */
+    const double* position;
+    const double* velocity;
+    const double* orientation_x;
+    const double* orientation_z;
+    const double* angular_velocity;
+    const double* impact;                    /* may be NULL (zeros)               */
+    const double* angular_impact;            /* may be NULL (zeros)               */
+    /* IactRecordTab (IactRecordTab.cpp:346-530): shear history to re-attach */
+    uint32_t num_records;
+    const uint32_t* record_first;            /* lower object index                */
+    const uint32_t* record_second;           /* higher object index               */
+    const uint8_t* record_contact;
+    const uint8_t* record_bond;
+    const double* record_kn;
+    const double* record_initial_velocity;
+    const double* record_shear;              /* [n][3]                            */
+} vedo_scene_desc;
+
+/* ---- engine options ---------------------------------------------------- */
+enum { VEDO_PRECISION_FP64 = 0, VEDO_PRECISION_MIXED = 1 };
+
+typedef struct vedo_engine_opts {
+    uint32_t up_iact;         /* candidate-list rebuild interval in steps (anne
+                                 <UpIact>, NBSConsultant::ISReset, NBSConsultant.cpp:80-83) */
+    uint32_t record;          /* IDO record interval in steps (anne <Record>);
+                                 0 = never                                          */
+    uint32_t precision;       /* VEDO_PRECISION_FP64 (the drop-in) or _MIXED       */
+    int32_t device;           /* CUDA device ordinal                               */
+    const char* output_prefix;/* "<prefix>_NNNNNNN.ido" records and terminate.ido are
+                                 written when non-NULL, as Consultant::RecordIDO
+                                 (Consultant.cpp:217-230) and NBSConsultant::NextStep
+                                 (NBSConsultant.cpp:63-76) do; NULL writes nothing  */
+    uint32_t reserved[4];
+} vedo_engine_opts;
+
+typedef struct vedo_gpu_engine vedo_gpu_engine;
+
+/* Default options: up_iact 1, record 0, FP64, device 0, no files. */
+void vedo_gpu_default_opts(vedo_engine_opts* opts);
+
+/* Build an engine from a scene.  Replaces DOWorld + NBSConsultant +
+ * SimMediator construction (Anne.cpp:83-119, SimMediator.cpp:83-137): the
+ * first candidate list is built, interactions are created with the
+ * Assembler's slave/master and model-selection rules (Assembler.cpp:15-87,
+ * CDFactory.h:66-95, ISFactory.h:45-48) and the IactRecordTab history is
+ * re-attached.  The scene's host arrays are copied; the caller keeps them. */
+int vedo_gpu_create(const vedo_scene_desc* scene, const vedo_engine_opts* opts, vedo_gpu_engine** out);
+
+/* Same, reading a reference .ido file (DOWorld::ReadIDO, DOWorld_RWIDO.cpp:9-55). */
+int vedo_gpu_create_from_ido(const char* path, const vedo_engine_opts* opts, vedo_gpu_engine** out);
+
+/* Advance nsteps time steps, each one SimMediator::Run() (SimMediator.cpp:714-842).
+ * *keep_running (may be NULL) receives the last step's return value,
+ * t_current < t_stop (SimMediator.cpp:839-841). */
+int vedo_gpu_run(vedo_gpu_engine* e, uint32_t nsteps, int* keep_running);
+
+/* Object state, [n][3] doubles per array; any pointer may be NULL.  impact /
+ * angular_impact are the impulses the last Response consumed, as DOStatus
+ * holds them after DiscreteObject::ClearImpact (DiscreteObject.cpp:141-147). */
+typedef struct vedo_state_view {
+    double* position;
+    double* velocity;
+    double* angular_velocity;
+    double* orientation_x;
+    double* orientation_z;
+    double* impact;
+    double* angular_impact;
+} vedo_state_view;
+
+uint32_t vedo_gpu_num_objects(const vedo_gpu_engine* e);
+int vedo_gpu_get_state(vedo_gpu_engine* e, const vedo_state_view* out);
+/* Overwrite the object state (DOContainer::SetDOStatus, DOContainer.h:55-58). */
+int vedo_gpu_set_state(vedo_gpu_engine* e, const vedo_state_view* in);
+
+/* Interaction list in candidate-list order (the reference's IactContainer order).
+ * first < second are object indices (the IactRecordTab key); slave/master is
+ * the Assembler orientation; active = ContactInfo::bActive of the last
+ * narrow-phase pass; shear/kn/contact = the solver's ImpactStatus.  Any
+ * pointer may be NULL. */
+typedef struct vedo_contact_view {
+    uint32_t* first;
+    uint32_t* second;
+    uint32_t* slave;
+    uint32_t* master;
+    uint8_t* active;
+    double* shear;             /* [n][3] */
+    double* kn;
+    uint8_t* contact;
+} vedo_contact_view;
+
+int vedo_gpu_num_interactions(vedo_gpu_engine* e, uint32_t* n);
+int vedo_gpu_get_interactions(vedo_gpu_engine* e, const vedo_contact_view* out);
+
+/* System observables as DOWorld::CalculateSystemEnergy computes them
+ * (DOWorld.cpp:481-660) over the current state, mobile objects only:
+ * out[0..8] = potential, translational, rotational energy, v min, v max,
+ * omega min, omega max, momentum norm, angular-momentum norm;
+ * out[9] = number of active contacts, out[10] = mass-weighted centre of mass x,
+ * out[11] = y, out[12] = z. */
+int vedo_gpu_get_observables(vedo_gpu_engine* e, double out[13]);
+
+/* Simulated time (SystemParameter::GetTimeCurrent) and step counter. */
+double vedo_gpu_time(const vedo_gpu_engine* e);
+uint64_t vedo_gpu_step_count(const vedo_gpu_engine* e);
+
+/* Write world + active-contact records as a reference .ido
+ * (DOWorld::WriteIDO, DOWorld_RWIDO.cpp:149-202). */
+int vedo_gpu_write_ido(vedo_gpu_engine* e, const char* path);
+
+/* Per-stage device time of the last vedo_gpu_run call in milliseconds:
+ * out[0] = pair kernel (detect + impact solve), out[1] = object kernel
+ * (gather + integrate), out[2] = broad phase rebuild; returns the number of
+ * kernel launches of that call. */
+uint64_t vedo_gpu_last_run_profile(const vedo_gpu_engine* e, double out[3]);
+
+const char* vedo_gpu_last_error(const vedo_gpu_engine* e);
+void vedo_gpu_destroy(vedo_gpu_engine* e);
+
+/* Library version string. */
+const char* vedo_gpu_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* VEDO_GPU_H */

@@ -1,0 +1,321 @@
+"""Seeded synthetic scenes with the shapes of the DEM workloads this engine is measured on.
+
+All scenes are built from numpy's PCG64 generator (bit-identical on x86_64 and
+aarch64) and are plain :class:`~vedo_gb300.scene.Scene` objects, so the same
+scene can be written as a reference ``.ido`` file and run by the reference CPU
+code, the C oracle and the GPU engine.
+
+* :func:`lsd_box` - 8,000 monodisperse spheres (r = 1 mm, 2500 kg/m^3) on a
+  jittered 20x20x20 lattice (2.2 mm spacing, U(+-0.05 mm) jitter, N(0, 0.05 m/s)
+  velocities) falling under g = 9.81 into an open box of 5 fixed plates 50 mm
+  wide and 60 mm tall; linear spring-dashpot ``ISwBSDBF`` with kn = 1e4 N/m,
+  ks = 0.8 kn, restitution 0.8, friction 0.5; dt = 1e-6 s.
+* :func:`hertz_drum` - polydisperse Hertz spheres (lognormal radii binned into K
+  classes, one DOModel per class) in a horizontal drum of R = 0.15 m, L = 0.3 m
+  whose shell is a static polygon of fixed plates and whose two end plates are
+  orbital plates turning at 30 rpm; 35 % fill by seeded random sequential
+  placement.
+* :func:`cluster` - small random clusters used by the parity tests (every
+  solver, plates, cylinders, orbital walls).
+"""
+from __future__ import annotations
+
+import math
+from typing import List, Optional, Sequence, Tuple
+
+import numpy as np
+
+from .scene import (CONSTRAINED, FIXED, GLOBAL, LOCAL, MOBILE, ORBITAL, QUASI_CYLINDER, QUASI_PLATE, SPHERE,
+                    Boundary, DOModel, IactModel, Scene, SystemParameter)
+
+
+def damping_ratio(e: float) -> float:
+    """Viscous damping ratio zeta of a linear spring-dashpot with restitution e."""
+    le = math.log(e)
+    return -le / math.sqrt(math.pi * math.pi + le * le)
+
+
+def lsd_mechanisms(kn: float, ks: float, beta_n: float, beta_s: float, mu: float) -> List[Tuple[str, float]]:
+    """Mechanism list read by ISwBSDBF's constructor (ISwBSDBF.cpp:10-18)."""
+    return [("NormalStiffness", kn), ("ShearStiffness", ks), ("NormalDampingRatio", beta_n),
+            ("ShearDampingRatio", beta_s), ("NormalBondStrength", 0.0), ("ShearBondStrength", 0.0),
+            ("FrictionCoefficient", mu)]
+
+
+def time_control(steps: int, dt: float) -> SystemParameter:
+    """t_stop = (steps - 1/2) dt: the reference loop runs while t_current < t_stop after each
+    step (SimMediator.cpp:839-841), so exactly `steps` steps run despite FP accumulation of t."""
+    return SystemParameter(time_start=0.0, time_stop=(steps - 0.5) * dt, time_interval=dt, time_current=0.0)
+
+
+def box_walls(width: float, height: float, thickness: float, depth_z0: float = 0.0):
+    """Five fixed quasi-plates forming an open box: floor top surface at z = z0, inner side
+    faces at x, y = +-width/2, walls `height` tall.  A plate's normal is OrientationZ, its
+    width runs along OrientationX and its length along Oz x Ox (CDSphere2QuasiPlate.cpp:29-65)."""
+    h = thickness
+    L = width + 2 * h
+    floor = DOModel("Floor", "Wall", FIXED, GLOBAL, 0.0, 1.0, QUASI_PLATE, (L, h, L))
+    side = DOModel("Sides", "Wall", FIXED, GLOBAL, 0.0, 1.0, QUASI_PLATE, (height, h, L))
+    pos = [(0.0, 0.0, depth_z0 - 0.5 * h)]
+    ox = [(1.0, 0.0, 0.0)]
+    oz = [(0.0, 0.0, 1.0)]
+    zc = depth_z0 + 0.5 * height
+    for sx, sy in ((1, 0), (-1, 0), (0, 1), (0, -1)):
+        pos.append((sx * (0.5 * width + 0.5 * h), sy * (0.5 * width + 0.5 * h), zc))
+        ox.append((0.0, 0.0, 1.0))
+        oz.append((float(sx), float(sy), 0.0))
+    return [floor, side], [0, 1, 1, 1, 1], np.array(pos), np.array(ox), np.array(oz)
+
+
+def lsd_box(n_side: int = 20, seed: int = 12345, steps: int = 20000, dt: float = 1e-6, radius: float = 1e-3,
+            density: float = 2500.0, spacing: float = 2.2e-3, jitter: float = 5e-5, vel_sigma: float = 0.05,
+            kn: float = 1e4, ks_ratio: float = 0.8, restitution: float = 0.8, mu: float = 0.5,
+            box_width: float = 0.05, box_height: float = 0.06, wall_thickness: float = 2e-3) -> Scene:
+    """The plain FP64 linear spring-dashpot box (8,000 spheres at n_side = 20)."""
+    rng = np.random.default_rng(seed)
+    i, j, k = np.meshgrid(np.arange(n_side), np.arange(n_side), np.arange(n_side), indexing="ij")
+    grid = np.stack([i.ravel(), j.ravel(), k.ravel()], axis=1).astype(np.float64)
+    pos = np.empty_like(grid)
+    pos[:, 0] = (grid[:, 0] - 0.5 * (n_side - 1)) * spacing
+    pos[:, 1] = (grid[:, 1] - 0.5 * (n_side - 1)) * spacing
+    pos[:, 2] = grid[:, 2] * spacing + 2.0 * radius
+    pos += rng.uniform(-jitter, jitter, size=pos.shape)
+    vel = rng.normal(0.0, vel_sigma, size=pos.shape)
+    n = pos.shape[0]
+    zeta = damping_ratio(restitution)
+    # VEDO damps with the mean mass 1/2(ma+mb) (ISwModels.cpp:88-108): for equal spheres that is
+    # m, twice the reduced mass, so beta = zeta/sqrt(2) gives the intended restitution; against a
+    # wall (SudoMass 0) the sphere mass is the reduced mass and beta = zeta.
+    ball = DOModel("Ball", "Ball", MOBILE, LOCAL, density, 1.0, SPHERE, (radius,))
+    wmodels, widx, wpos, wox, woz = box_walls(box_width, box_height, wall_thickness)
+    models = [ball] + wmodels
+    iacts = [IactModel("Ball", "Ball", "ISwBSDBF", lsd_mechanisms(kn, ks_ratio * kn, zeta / math.sqrt(2.0),
+                                                                  zeta / math.sqrt(2.0), mu)),
+             IactModel("Wall", "Ball", "ISwBSDBF", lsd_mechanisms(kn, ks_ratio * kn, zeta, zeta, mu))]
+    model_index = np.concatenate([np.zeros(n, np.uint32), 1 + np.array(widx, np.uint32)])
+    P = np.concatenate([pos, wpos])
+    V = np.concatenate([vel, np.zeros((len(widx), 3))])
+    OX = np.concatenate([np.tile([1.0, 0.0, 0.0], (n, 1)), wox])
+    OZ = np.concatenate([np.tile([0.0, 0.0, 1.0], (n, 1)), woz])
+    return Scene(time_control(steps, dt), models, iacts, model_index, P, V, OX, OZ)
+
+
+# ---------------------------------------------------------------------------------------------
+def hertz_constants(E: float, nu: float, r_a: float, r_b: Optional[float], rho: float):
+    """kn = 4/3 E* sqrt(R*) for the ISwHertz normal law (ISwModels.cpp:127-132); r_b None = wall."""
+    Es = E / (2.0 * (1.0 - nu * nu)) if r_b is not None else E / (1.0 - nu * nu)
+    Rs = r_a * r_b / (r_a + r_b) if r_b is not None else r_a
+    return 4.0 / 3.0 * Es * math.sqrt(Rs)
+
+
+def _sequential_placement(rng, radii: np.ndarray, inside, lo: np.ndarray, hi: np.ndarray, max_tries: int = 60):
+    """Seeded random sequential placement: candidates drawn uniformly in [lo, hi]; a sphere is
+    kept when `inside(p, r)` holds and it overlaps no sphere placed before (cell grid check)."""
+    rmax = float(radii.max())
+    cell = 2.0 * rmax
+    dims = np.maximum(1, np.ceil((hi - lo) / cell).astype(np.int64))
+    grid = {}
+    out = np.full((radii.shape[0], 3), np.nan)
+    placed = 0
+    for idx in range(radii.shape[0]):
+        r = radii[idx]
+        for _ in range(max_tries):
+            p = lo + rng.random(3) * (hi - lo)
+            if not inside(p, r):
+                continue
+            c = np.floor((p - lo) / cell).astype(np.int64)
+            ok = True
+            for dx in (-1, 0, 1):
+                for dy in (-1, 0, 1):
+                    for dz in (-1, 0, 1):
+                        for q in grid.get((c[0] + dx, c[1] + dy, c[2] + dz), ()):
+                            d = p - out[q]
+                            if d @ d < (r + radii[q]) ** 2:
+                                ok = False
+                                break
+                        if not ok:
+                            break
+                    if not ok:
+                        break
+                if not ok:
+                    break
+            if ok:
+                out[idx] = p
+                grid.setdefault((c[0], c[1], c[2]), []).append(idx)
+                placed += 1
+                break
+    keep = ~np.isnan(out[:, 0])
+    return out[keep], keep
+
+
+def cluster(n: int = 64, seed: int = 7, solver: str = "ISwBSDBF", walls: str = "box", steps: int = 200,
+            dt: float = 1e-6, radius: float = 1e-3, polydisperse: bool = False, density: float = 2500.0,
+            vel_sigma: float = 0.2, orbital: bool = False, cylinders: int = 0, spacing: float = 2.05e-3,
+            friction: float = 0.5) -> Scene:
+    """Small jittered lattice of spheres close enough to collide within a few hundred steps,
+    in a box of plates (optionally with orbital walls and vertical cylinders)."""
+    rng = np.random.default_rng(seed)
+    side = int(math.ceil(n ** (1.0 / 3.0)))
+    g = np.stack(np.meshgrid(*(np.arange(side),) * 3, indexing="ij"), -1).reshape(-1, 3)[:n].astype(float)
+    pos = (g - 0.5 * (side - 1)) * spacing
+    pos[:, 2] += 0.5 * side * spacing + 1.5 * radius
+    pos += rng.uniform(-0.02 * spacing, 0.02 * spacing, size=pos.shape)
+    vel = rng.normal(0.0, vel_sigma, size=pos.shape)
+    avel = rng.normal(0.0, 20.0, size=pos.shape)
+    models: List[DOModel] = []
+    if polydisperse:
+        radii = np.array([0.8, 0.9, 1.0]) * radius
+        for k, r in enumerate(radii):
+            models.append(DOModel(f"Ball{k}", f"B{k}", MOBILE, LOCAL, density, 1.0, SPHERE, (float(r),)))
+        midx = rng.integers(0, 3, size=n).astype(np.uint32)
+    else:
+        models.append(DOModel("Ball", "B0", MOBILE, LOCAL, density, 1.0, SPHERE, (radius,)))
+        midx = np.zeros(n, np.uint32)
+    groups = sorted({m.group for m in models})
+    extent = side * spacing + 4 * radius
+    P, V, OX, OZ, AV = [pos], [vel], [np.tile([1.0, 0, 0], (n, 1))], [np.tile([0, 0, 1.0], (n, 1))], [avel]
+    wall_groups = []
+    if walls == "box":
+        base = len(models)
+        wm, widx, wp, wox, woz = box_walls(extent, extent + 4 * radius, 1e-3)
+        if orbital:
+            wm[1] = DOModel("Sides", "Wall", ORBITAL, GLOBAL, 0.0, 1.0, QUASI_PLATE, wm[1].attrs)
+        models += wm
+        midx = np.concatenate([midx, base + np.array(widx, np.uint32)])
+        P.append(wp); V.append(np.zeros_like(wp)); OX.append(wox); OZ.append(woz)
+        wav = np.zeros_like(wp)
+        if orbital:
+            wav[1:, 2] = 3.0   # side plates spin slowly about the vertical axis through their own centres
+        AV.append(wav)
+        wall_groups.append("Wall")
+    if cylinders:
+        base = len(models)
+        models.append(DOModel("Rod", "Rod", FIXED, GLOBAL, 0.0, 1.0, QUASI_CYLINDER, (0.6 * radius, extent)))
+        cp = np.zeros((cylinders, 3))
+        ang = np.arange(cylinders) * 2 * math.pi / cylinders
+        cp[:, 0] = 0.3 * extent * np.cos(ang)
+        cp[:, 1] = 0.3 * extent * np.sin(ang)
+        cp[:, 2] = 0.5 * extent
+        midx = np.concatenate([midx, np.full(cylinders, base, np.uint32)])
+        P.append(cp); V.append(np.zeros_like(cp)); OX.append(np.tile([1.0, 0, 0], (cylinders, 1)))
+        OZ.append(np.tile([0, 0, 1.0], (cylinders, 1))); AV.append(np.zeros_like(cp))
+        wall_groups.append("Rod")
+    iacts = []
+    e = 0.7
+    zeta = damping_ratio(e)
+    for ga in groups + wall_groups:
+        for gb in groups:
+            if ga in wall_groups or ga <= gb:
+                iacts.append(IactModel(ga, gb, solver, _mechanisms(solver, zeta, friction)))
+    sc = Scene(time_control(steps, dt), models, iacts, midx, np.concatenate(P), np.concatenate(V),
+               np.concatenate(OX), np.concatenate(OZ), np.concatenate(AV))
+    return sc
+
+
+def _mechanisms(solver: str, zeta: float, mu: float):
+    if solver in ("ISwBSDBF", "ISwBtSDBF", "ISwBSDB2F"):
+        return lsd_mechanisms(1e4, 8e3, zeta, zeta, mu)
+    if solver == "ISwHertz":
+        return [("NormalStiffness", 5e7), ("NormalDampingCoefficient", 2e-2)]
+    if solver == "ISwH":
+        return [("HertzNormalStiffness", 5e7), ("EquivalentMass", 5e-6), ("ShearStiffnessCoefficient1", 2.0),
+                ("ShearStiffnessCoefficient2", 3e3), ("DampingRatio", zeta), ("KineticFrictionCoefficient", mu)]
+    raise ValueError(solver)
+
+
+# ---------------------------------------------------------------------------------------------
+def hertz_drum(n: int = 1_000_000, seed: int = 2024, steps: int = 10000, dt: float = 5e-7, K: int = 32,
+               median_r: float = 1e-3, sigma_log: float = 0.2, r_lo: float = 0.5e-3, r_hi: float = 2e-3,
+               E: float = 70e9, nu: float = 0.25, restitution: float = 0.7, mu: float = 0.4,
+               density: float = 2500.0, R: float = 0.15, L: float = 0.3, rpm: float = 30.0,
+               fill: float = 0.35, facets: int = 64, solver: str = "ISwH") -> Scene:
+    """Polydisperse Hertz drum.  Radii lognormal(median, sigma_log) clipped to [r_lo, r_hi],
+    binned into K log-spaced classes (one DOModel and one group per class; K(K+1)/2 + K
+    interaction models).  The shell is `facets` fixed plates on a circle of radius R; the two
+    end plates are orbital plates spinning at `rpm` about the drum axis (x).  The bottom
+    `fill` fraction of the drum volume is filled by seeded placement on a jittered cubic
+    lattice (one site per sphere of the largest class, shuffled), which stands in for random
+    sequential placement at this size."""
+    rng = np.random.default_rng(seed)
+    edges = np.exp(np.linspace(math.log(r_lo), math.log(r_hi), K + 1))
+    centres = np.sqrt(edges[:-1] * edges[1:])
+    r = np.clip(median_r * np.exp(sigma_log * rng.standard_normal(n)), r_lo, r_hi)
+    cls = np.clip(np.searchsorted(edges, r, side="right") - 1, 0, K - 1).astype(np.uint32)
+    radii = centres[cls]
+    # lattice sites inside the lower part of the drum cross-section (axis along x)
+    rmax = float(radii.max())
+    a = 2.0 * rmax * 1.02
+    h_fill = R * (2.0 * fill - 1.0) * 1.35   # fill level (z) giving roughly `fill` of the cross-section
+    xs = np.arange(-0.5 * L + a, 0.5 * L - a, a)
+    ys = np.arange(-R + a, R - a, a)
+    zs = np.arange(-R + a, R - a, a)
+    X, Y, Z = np.meshgrid(xs, ys, zs, indexing="ij")
+    sites = np.stack([X.ravel(), Y.ravel(), Z.ravel()], 1)
+    ok = (sites[:, 1] ** 2 + sites[:, 2] ** 2) < (R - a) ** 2
+    sites = sites[ok]
+    order = np.argsort(sites[:, 2], kind="stable")
+    sites = sites[order]
+    if sites.shape[0] < n:
+        raise ValueError(f"drum holds {sites.shape[0]} lattice sites < {n} spheres; enlarge the drum")
+    sites = sites[:n]
+    sites += rng.uniform(-0.005 * a, 0.005 * a, size=sites.shape)
+    pos = sites
+    vel = np.zeros_like(pos)
+    models: List[DOModel] = []
+    for k in range(K):
+        models.append(DOModel(f"B{k:03d}", f"B{k:03d}", MOBILE, LOCAL, density, 1.0, SPHERE, (float(centres[k]),)))
+    thick = 4e-3
+    fw = 2.0 * R * math.sin(math.pi / facets) * 1.05
+    shell = DOModel("Shell", "Wall", FIXED, GLOBAL, 0.0, 1.0, QUASI_PLATE, (L + 2 * thick, thick, fw))
+    endp = DOModel("End", "Wall", ORBITAL, GLOBAL, 0.0, 1.0, QUASI_PLATE, (2.2 * R, thick, 2.2 * R))
+    models += [shell, endp]
+    wp, wox, woz, wav, widx = [], [], [], [], []
+    for f in range(facets):
+        th = 2.0 * math.pi * (f + 0.5) / facets
+        nrm = np.array([0.0, math.cos(th), math.sin(th)])
+        wp.append(nrm * (R + 0.5 * thick))
+        woz.append(-nrm)
+        wox.append([1.0, 0.0, 0.0])
+        wav.append([0.0, 0.0, 0.0])
+        widx.append(K)
+    omega = rpm * 2.0 * math.pi / 60.0
+    for sx in (-1.0, 1.0):
+        wp.append([sx * (0.5 * L + 0.5 * thick), 0.0, 0.0])
+        woz.append([-sx, 0.0, 0.0])
+        wox.append([0.0, 1.0, 0.0])
+        wav.append([omega, 0.0, 0.0])
+        widx.append(K + 1)
+    iacts = []
+    zeta = damping_ratio(restitution)
+    m_of = lambda rr: density * 4.0 / 3.0 * math.pi * rr ** 3
+    for ka in range(K):
+        for kb in range(ka, K):
+            iacts.append(IactModel(models[ka].group, models[kb].group, solver,
+                                   _hertz_mech(solver, E, nu, centres[ka], centres[kb], m_of, zeta, mu)))
+    for ka in range(K):
+        iacts.append(IactModel("Wall", models[ka].group, solver,
+                               _hertz_mech(solver, E, nu, centres[ka], None, m_of, zeta, mu)))
+    model_index = np.concatenate([cls, np.array(widx, np.uint32)])
+    P = np.concatenate([pos, np.array(wp)])
+    V = np.concatenate([vel, np.zeros((len(widx), 3))])
+    OX = np.concatenate([np.tile([1.0, 0, 0], (n, 1)), np.array(wox)])
+    OZ = np.concatenate([np.tile([0, 0, 1.0], (n, 1)), np.array(woz)])
+    AV = np.concatenate([np.zeros((n, 3)), np.array(wav)])
+    return Scene(time_control(steps, dt), models, iacts, model_index, P, V, OX, OZ, AV)
+
+
+def _hertz_mech(solver, E, nu, ra, rb, m_of, zeta, mu):
+    kn = hertz_constants(E, nu, ra, rb, 0.0)
+    meff = m_of(ra) if rb is None else m_of(ra) * m_of(rb) / (m_of(ra) + m_of(rb))
+    if solver == "ISwHertz":
+        cn = 2.0 * zeta * math.sqrt(meff * kn * math.sqrt(1e-6))   # damping at 1 um overlap
+        return [("NormalStiffness", kn), ("NormalDampingCoefficient", cn)]
+    # ISwH: ks = ksc1 (ksc2 |kn delta|)^(1/3) (ISwH.cpp:213) is Mindlin's kt = 8 G* a with the
+    # Hertz contact radius a = (3 F R* / (4 E*))^(1/3): ksc1 = 8 G*, ksc2 = 3 R* / (4 E*).
+    G = E / (2.0 * (1.0 + nu))
+    Gs = G / (2.0 * (2.0 - nu)) if rb is not None else G / (2.0 - nu)
+    Es = E / (2.0 * (1.0 - nu * nu)) if rb is not None else E / (1.0 - nu * nu)
+    Rs = ra if rb is None else ra * rb / (ra + rb)
+    return [("HertzNormalStiffness", kn), ("EquivalentMass", meff),
+            ("ShearStiffnessCoefficient1", 8.0 * Gs), ("ShearStiffnessCoefficient2", 3.0 * Rs / (4.0 * Es)),
+            ("DampingRatio", zeta), ("KineticFrictionCoefficient", mu)]
