@@ -215,6 +215,12 @@ int vedo_gpu_write_ido(vedo_gpu_engine* e, const char* path);
  * kernel launches of that call. */
 uint64_t vedo_gpu_last_run_profile(const vedo_gpu_engine* e, double out[3]);
 
+/* Enable per-phase CUDA-event timing for vedo_gpu_last_run_profile (adds one host
+ * synchronisation per step; off by default). */
+void vedo_gpu_set_profiling(vedo_gpu_engine* e, int on);
+
+/* Message of the last failure of e; with e == NULL, of the last failed create call
+ * on this thread. */
 const char* vedo_gpu_last_error(const vedo_gpu_engine* e);
 void vedo_gpu_destroy(vedo_gpu_engine* e);
 

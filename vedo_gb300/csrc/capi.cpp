@@ -1,0 +1,129 @@
+// capi.cpp - extern "C" entry points of include/vedo_gpu.h over vedo::Engine.
+#include <cstring>
+#include <new>
+#include <string>
+
+#include "../../include/vedo_gpu.h"
+#include "engine.h"
+
+struct vedo_gpu_engine {
+    vedo::Engine eng;
+};
+
+namespace {
+thread_local std::string g_create_error;
+
+int create_common(const vedo::HScene& s, const vedo_engine_opts* opts, vedo_gpu_engine** out) {
+    vedo_engine_opts o;
+    vedo_gpu_default_opts(&o);
+    if (opts) o = *opts;
+    vedo_gpu_engine* e = new (std::nothrow) vedo_gpu_engine();
+    if (!e) return VEDO_ERR_OUT_OF_MEMORY;
+    int rc = e->eng.init(s, o);
+    if (rc != VEDO_OK) {
+        g_create_error = e->eng.error();
+        delete e;
+        *out = nullptr;
+        return rc;
+    }
+    *out = e;
+    return VEDO_OK;
+}
+}  // namespace
+
+extern "C" {
+
+void vedo_gpu_default_opts(vedo_engine_opts* o) {
+    if (!o) return;
+    std::memset(o, 0, sizeof(*o));
+    o->up_iact = 1;
+    o->record = 0;
+    o->precision = VEDO_PRECISION_FP64;
+    o->device = 0;
+    o->output_prefix = nullptr;
+}
+
+int vedo_gpu_create(const vedo_scene_desc* scene, const vedo_engine_opts* opts, vedo_gpu_engine** out) {
+    if (!scene || !out) return VEDO_ERR_INVALID_ARGUMENT;
+    *out = nullptr;
+    vedo::HScene s;
+    std::string err;
+    if (!vedo::scene_from_desc(scene, s, err)) {
+        g_create_error = err;
+        return VEDO_ERR_INVALID_SCENE;
+    }
+    return create_common(s, opts, out);
+}
+
+int vedo_gpu_create_from_ido(const char* path, const vedo_engine_opts* opts, vedo_gpu_engine** out) {
+    if (!path || !out) return VEDO_ERR_INVALID_ARGUMENT;
+    *out = nullptr;
+    vedo::HScene s;
+    std::string err;
+    if (!vedo::read_ido(path, s, err)) {
+        g_create_error = err;
+        return VEDO_ERR_BAD_IDO;
+    }
+    return create_common(s, opts, out);
+}
+
+int vedo_gpu_run(vedo_gpu_engine* e, uint32_t nsteps, int* keep_running) {
+    if (!e) return VEDO_ERR_INVALID_ARGUMENT;
+    return e->eng.run(nsteps, keep_running);
+}
+
+uint32_t vedo_gpu_num_objects(const vedo_gpu_engine* e) { return e ? e->eng.num_objects() : 0u; }
+
+int vedo_gpu_get_state(vedo_gpu_engine* e, const vedo_state_view* out) {
+    if (!e || !out) return VEDO_ERR_INVALID_ARGUMENT;
+    return e->eng.get_state(*out);
+}
+
+int vedo_gpu_set_state(vedo_gpu_engine* e, const vedo_state_view* in) {
+    if (!e || !in) return VEDO_ERR_INVALID_ARGUMENT;
+    return e->eng.set_state(*in);
+}
+
+int vedo_gpu_num_interactions(vedo_gpu_engine* e, uint32_t* n) {
+    if (!e || !n) return VEDO_ERR_INVALID_ARGUMENT;
+    return e->eng.num_interactions(n);
+}
+
+int vedo_gpu_get_interactions(vedo_gpu_engine* e, const vedo_contact_view* out) {
+    if (!e || !out) return VEDO_ERR_INVALID_ARGUMENT;
+    return e->eng.get_interactions(*out);
+}
+
+int vedo_gpu_get_observables(vedo_gpu_engine* e, double out[13]) {
+    if (!e || !out) return VEDO_ERR_INVALID_ARGUMENT;
+    return e->eng.get_observables(out);
+}
+
+double vedo_gpu_time(const vedo_gpu_engine* e) { return e ? e->eng.time() : 0.0; }
+
+uint64_t vedo_gpu_step_count(const vedo_gpu_engine* e) { return e ? e->eng.steps() : 0u; }
+
+int vedo_gpu_write_ido(vedo_gpu_engine* e, const char* path) {
+    if (!e || !path) return VEDO_ERR_INVALID_ARGUMENT;
+    return e->eng.write_ido(path);
+}
+
+uint64_t vedo_gpu_last_run_profile(const vedo_gpu_engine* e, double out[3]) {
+    if (!e || !out) return 0;
+    return e->eng.last_profile(out);
+}
+
+void vedo_gpu_set_profiling(vedo_gpu_engine* e, int on) {
+    if (e) e->eng.set_profiling(on != 0);
+}
+
+const char* vedo_gpu_last_error(const vedo_gpu_engine* e) {
+    if (!e) return g_create_error.c_str();
+    return e->eng.error().c_str();
+}
+
+void vedo_gpu_destroy(vedo_gpu_engine* e) { delete e; }
+
+const char* vedo_gpu_version(void) { return "vedo-gb300 0.1.0 (sm_103a)"; }
+
+}  // extern "C"

@@ -1,0 +1,91 @@
+// dem_common.cuh - device-side data layout and FP64 vector arithmetic of the DEM engine.
+//
+// The FP64 helpers restate aries::Vector3d (aries/utility/Vector3d.h) operation by
+// operation.  Translation units that include them are compiled with -fmad=false, so
+// every product and sum is rounded separately, exactly as the reference's host build
+// (no -mfma, no -ffast-math, src/Makefile.in:73-77) evaluates them.
+#pragma once
+
+#include <cmath>
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace vedo {
+
+// ---- enums (DOModel.h:25-27) and engine-internal codes -------------------------------
+enum : int { SHAPE_SPHERE = 1, SHAPE_CYL = 6, SHAPE_PLATE = 7 };
+enum : int { BEH_CONSTRAINED = 1, BEH_FIXED = 2, BEH_MOBILE = 3, BEH_ORBITAL = 4 };
+enum : int { SCOPE_GLOBAL = 1, SCOPE_LOCAL = 2 };
+enum : int { CD_SS = 1, CD_SP = 2, CD_SC = 3 };
+enum : int { IS_BSDBF = 1, IS_BTSDBF = 2, IS_BSDB2F = 3, IS_HERTZ = 4, IS_H = 5 };
+
+// Per-model constants (DOModel::Analysis, DOModel.cpp:17-149, plus the dSudoMass the
+// DiscreteObject subclass of each shape/behaviour uses).
+struct ModelDev {
+    int shape, behavior, scope, group;
+    double range;         // DOModel::GetRange
+    double mass;          // DOModel::GetMass (energies)
+    double sudo;          // DiscreteObject::dSudoMass of this shape/behaviour
+    double density;
+    double a0, a1, a2;    // shape attributes: sphere r | cylinder r, h | plate w, h, l
+    double ix, iy, iz;    // mass moment of inertia
+    double ext[3];        // external force
+};
+
+// Interaction constants of one (slave model, master model) pair, as the ImpactSolver
+// constructors compute them (ISwBSDBF.cpp:7-19 etc.).  cd == 0 means "no interaction".
+struct PairParam {
+    int cd, is, iact, pad;
+    double c[8];
+};
+
+// Per-pair status flags (ImpactStatus bContact/bLastContact/bBond/bLastBond).
+enum : uint8_t { ST_CONTACT = 1, ST_LAST_CONTACT = 2, ST_BOND = 4, ST_LAST_BOND = 8 };
+// Default-constructed ImpactStatus has bLastContact = bLastBond = true (ImpactStatus.cpp:8-9).
+constexpr uint8_t ST_DEFAULT = ST_LAST_CONTACT | ST_LAST_BOND;
+
+// Error bits raised by kernels and read by the host after a rebuild.
+enum : int { ERR_UNSUPPORTED_PAIR = 1, ERR_CAPACITY = 2, ERR_BAD_SHAPE_PAIR = 4 };
+
+struct d3 { double x, y, z; };
+
+__host__ __device__ __forceinline__ d3 mk(double x, double y, double z) { d3 r; r.x = x; r.y = y; r.z = z; return r; }
+__host__ __device__ __forceinline__ d3 add(d3 a, d3 b) { return mk(a.x + b.x, a.y + b.y, a.z + b.z); }
+__host__ __device__ __forceinline__ d3 sub(d3 a, d3 b) { return mk(a.x - b.x, a.y - b.y, a.z - b.z); }
+__host__ __device__ __forceinline__ d3 smul(double s, d3 a) { return mk(s * a.x, s * a.y, s * a.z); }
+__host__ __device__ __forceinline__ d3 muls(d3 a, double s) { return mk(a.x * s, a.y * s, a.z * s); }
+__host__ __device__ __forceinline__ d3 neg(d3 a) { return mk(-a.x, -a.y, -a.z); }
+__host__ __device__ __forceinline__ double dot(d3 a, d3 b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
+__host__ __device__ __forceinline__ double len(d3 a) { return sqrt(a.x * a.x + a.y * a.y + a.z * a.z); }
+// Vector3d::direction (Vector3d.h:117-126).  The reference leaves the result
+// uninitialised for a zero vector; every use multiplies it by zero, so (0,0,0) here.
+__host__ __device__ __forceinline__ d3 dir(d3 a) {
+    double l = len(a);
+    if (l != 0) return mk(a.x / l, a.y / l, a.z / l);
+    return mk(0.0, 0.0, 0.0);
+}
+__host__ __device__ __forceinline__ d3 cross(d3 a, d3 b) {
+    return mk(a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x);
+}
+__host__ __device__ __forceinline__ d3 project_on(d3 a, d3 v) { return smul(dot(a, v) / len(v), dir(v)); }
+#ifdef __CUDACC__
+// Vector3d::rotate_around (Vector3d.h:152-178)
+__device__ __forceinline__ d3 rotate_around(d3 p, d3 va) {
+    d3 u = dir(va);
+    double a = len(va);
+    double s = cos(0.5 * a);
+    double t = sin(0.5 * a);
+    d3 v = muls(u, t);
+    d3 r = add(smul(s * s, p), smul(dot(p, v), v));
+    r = add(r, smul(2.0 * s, cross(v, p)));
+    return add(r, cross(v, cross(v, p)));
+}
+
+__device__ __forceinline__ d3 ld(const double4_32a* p, uint32_t i) {
+    double4_32a v = p[i];
+    return mk(v.x, v.y, v.z);
+}
+__device__ __forceinline__ void st(double4_32a* p, uint32_t i, d3 a, double w) { p[i] = make_double4_32a(a.x, a.y, a.z, w); }
+#endif
+
+}  // namespace vedo

@@ -1,0 +1,1150 @@
+// engine.cu - FP64 DEM time step and NBS broad phase on the GPU.
+//
+// Built with -fmad=false: the FP64 arithmetic below reproduces the reference's IEEE
+// operation sequence (see dem_physics.cuh).  Per time step (SimMediator::Run,
+// SimMediator.cpp:714-842) two kernels run:
+//   k_pair  - one thread per candidate pair: narrow phase at the current positions
+//             (the ContactInfo the reference computed at the end of the previous
+//             step) + impact solver + status update; the impulses go to a per-pair
+//             output record.
+//   k_obj   - one thread per local object: the pair impulses in candidate-list order
+//             (the reference's IactContainer order), the field impulse, the external
+//             force and DiscreteObject::Response.  Scope-global objects (walls) are
+//             summed by one warp each in k_obj_global (ordered, warp-cooperative loads).
+// Every UpIact steps the candidate list is rebuilt with NBSConsultant's rule
+// (NBSConsultant.cpp:85-374): cell keys, a stable radix sort, cell ranges, then a count
+// and a fill pass over (object, neighbour slot) tasks laid out in the reference's
+// traversal order, so the new list equals the reference's list element for element.
+#include "engine.h"
+
+#include <algorithm>
+#include <cfloat>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+
+#include "dem_physics.cuh"
+
+namespace vedo {
+
+namespace {
+
+constexpr int TPB = 256;
+inline unsigned blocks_for(uint64_t n, int tpb = TPB) { return (unsigned)((n + tpb - 1) / tpb); }
+
+// Neighbour visiting order of NBSConsultant::Reset (NBSConsultant.cpp:202-270):
+// 12 = the cell itself (i < j), 13 = all scope-global objects.
+__constant__ int c_slot[15][3] = {{-1, -1, -1}, {-1, -1, 0}, {-1, -1, 1}, {0, -1, -1}, {0, -1, 0},
+                                  {0, -1, 1},   {1, -1, -1}, {1, -1, 0},  {1, -1, 1},  {-1, 0, -1},
+                                  {-1, 0, 0},   {0, 0, -1},  {0, 0, 0},   {0, 0, 0},   {1, 0, -1}};
+constexpr int SLOT_SELF = 12;
+constexpr int SLOT_GLOBAL = 13;
+constexpr int NSLOT = 15;
+
+// order-preserving map of doubles to unsigned 64-bit integers (for exact atomic min/max)
+__host__ __device__ inline unsigned long long ord_of(double d) {
+    unsigned long long b;
+    memcpy(&b, &d, 8);
+    return (b >> 63) ? ~b : (b | 0x8000000000000000ull);
+}
+__host__ __device__ inline double dbl_of(unsigned long long o) {
+    unsigned long long b = (o >> 63) ? (o & 0x7fffffffffffffffull) : ~o;
+    double d;
+    memcpy(&d, &b, 8);
+    return d;
+}
+
+// ------------------------------------------------------------------------------------
+// time step
+__global__ void __launch_bounds__(TPB) k_pair(uint32_t np, const uint2* __restrict__ sm,
+                                              const uint32_t* __restrict__ param, const PairParam* __restrict__ params,
+                                              const double4_32a* __restrict__ geom, const double4_32a* __restrict__ pos,
+                                              const double4_32a* __restrict__ vel, const double4_32a* __restrict__ av,
+                                              const double4_32a* __restrict__ ox, const double4_32a* __restrict__ oz,
+                                              double4_32a* __restrict__ hist, double* __restrict__ v0,
+                                              uint8_t* __restrict__ flags, double* __restrict__ out, double dt,
+                                              int backup) {
+    const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= np) return;
+    const uint2 p = sm[k];
+    const uint32_t pi = param[k];
+    const int cd = params[pi].cd, is = params[pi].is;
+    const double4_32a gg = geom[pi];
+    const PairGeom g{gg.x, gg.y, gg.z, gg.w};
+    const d3 Ps = ld(pos, p.x), Pm = ld(pos, p.y);
+    double depth;
+    d3 n, point;
+    detect_pair(cd, g, Ps, Pm, ox, oz, p.y, depth, n, point);
+    const bool active = depth > 0.0;
+    const uint8_t f0 = flags[k];
+    PairStatus st;
+    st.f = f0 & (PF_STATUS | PF_NONZERO);
+    if (backup) {                                             // ImpactStatus::Backup (ImpactStatus.h:174-178)
+        uint8_t s2 = st.f & (uint8_t)~(ST_LAST_CONTACT | ST_LAST_BOND);
+        if (st.f & ST_CONTACT) s2 |= ST_LAST_CONTACT;
+        if (st.f & ST_BOND) s2 |= ST_LAST_BOND;
+        st.f = s2;
+    }
+    const double* c = params[pi].c;
+    const bool bonded = (is == IS_BSDBF || is == IS_BTSDBF || is == IS_BSDB2F) && normal_bond(c[0], c[4], depth);
+    if (!active && !bonded) {                                 // ImpactStatus::Clean, nothing added
+        if (st.f & PF_NONZERO) {
+            hist[k] = make_double4_32a(0.0, 0.0, 0.0, 0.0);
+            v0[k] = 0.0;
+        }
+        if (f0 != 0) flags[k] = 0;
+        return;
+    }
+    if (st.f & PF_NONZERO) {
+        double4_32a h = hist[k];
+        st.shear = mk(h.x, h.y, h.z);
+        st.kn = h.w;
+        st.v0 = v0[k];
+    } else {
+        st.shear = mk(0.0, 0.0, 0.0);
+        st.kn = 0.0;
+        st.v0 = 0.0;
+    }
+    const d3 Va = ld(vel, p.x), Vb = ld(vel, p.y), AVa = ld(av, p.x), AVb = ld(av, p.y);
+    d3 J, tA, tB;
+    const uint8_t app = solve_pair(is, c, active, depth, n, point, Ps, Pm, Va, Vb, AVa, AVb, dt, st, J, tA, tB);
+    if (st.f & PF_NONZERO) {
+        hist[k] = make_double4_32a(st.shear.x, st.shear.y, st.shear.z, st.kn);
+        v0[k] = st.v0;
+    }
+    flags[k] = st.f | app | (active ? PF_ACTIVE : 0);
+    if (app) {
+        double* o = out + 9 * (size_t)k;
+        o[0] = J.x; o[1] = J.y; o[2] = J.z;
+        o[3] = tA.x; o[4] = tA.y; o[5] = tA.z;
+        o[6] = tB.x; o[7] = tB.y; o[8] = tB.z;
+    }
+}
+
+__device__ __forceinline__ void add_entry(uint32_t ent, uint8_t f, const double* __restrict__ out, d3& J, d3& JA) {
+    if (!(f & PF_APPLIED)) return;
+    const double* o = out + 9 * (size_t)(ent >> 1);
+    const d3 Jk = mk(o[0], o[1], o[2]);
+    if (ent & 1) {                                            // master: B->AddImpact(-1.0 * ImpactA, tB)
+        J = add(J, neg(Jk));
+        if (f & PF_ANGULAR) JA = add(JA, mk(o[6], o[7], o[8]));
+    } else {                                                  // slave: A->AddImpact(ImpactA, tA)
+        J = add(J, Jk);
+        if (f & PF_ANGULAR) JA = add(JA, mk(o[3], o[4], o[5]));
+    }
+}
+
+__device__ __forceinline__ void finish_object(uint32_t i, const ModelDev& m, d3 J, d3 JA, double dt, d3 fimp,
+                                              double4_32a* __restrict__ pos, double4_32a* __restrict__ vel,
+                                              double4_32a* __restrict__ av, double4_32a* __restrict__ ox,
+                                              double4_32a* __restrict__ oz, double4_32a* __restrict__ imp,
+                                              double4_32a* __restrict__ aimp, int write_imp) {
+    J = add(J, muls(fimp, m.sudo));                           // DOContainer::AddFieldImpact (DOContainer.cpp:25)
+    J = add(J, smul(dt, mk(m.ext[0], m.ext[1], m.ext[2])));   // DiscreteObject::AddConstrainedImpact (:160-163)
+    if (m.behavior != BEH_FIXED) {
+        d3 P = ld(pos, i), V = ld(vel, i), AV = ld(av, i), Ox = ld(ox, i), Oz = ld(oz, i);
+        respond_object(m, dt, J, JA, P, V, AV, Ox, Oz);
+        st(pos, i, P, 0.0);
+        st(ox, i, Ox, 0.0);
+        st(oz, i, Oz, 0.0);
+        if (m.behavior != BEH_ORBITAL) {
+            st(vel, i, V, 0.0);
+            st(av, i, AV, 0.0);
+        }
+    }
+    if (write_imp) {                                          // DiscreteObject::ClearImpact (:141-147)
+        st(imp, i, J, 0.0);
+        st(aimp, i, JA, 0.0);
+    }
+}
+
+__global__ void __launch_bounds__(TPB) k_obj(uint32_t n, const uint32_t* __restrict__ model_of,
+                                             const ModelDev* __restrict__ models, double4_32a* __restrict__ pos,
+                                             double4_32a* __restrict__ vel, double4_32a* __restrict__ av,
+                                             double4_32a* __restrict__ ox, double4_32a* __restrict__ oz,
+                                             double4_32a* __restrict__ imp, double4_32a* __restrict__ aimp,
+                                             const uint32_t* __restrict__ csr_ptr, const uint32_t* __restrict__ csr_ent,
+                                             const uint8_t* __restrict__ flags, const double* __restrict__ out,
+                                             double dt, d3 fimp, int write_imp) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const ModelDev& m = models[model_of[i]];
+    if (m.scope == SCOPE_GLOBAL) return;
+    d3 J = mk(0.0, 0.0, 0.0), JA = mk(0.0, 0.0, 0.0);
+    const uint32_t e1 = csr_ptr[i + 1];
+    for (uint32_t e = csr_ptr[i]; e < e1; ++e) {
+        const uint32_t ent = csr_ent[e];
+        add_entry(ent, flags[ent >> 1], out, J, JA);
+    }
+    finish_object(i, m, J, JA, dt, fimp, pos, vel, av, ox, oz, imp, aimp, write_imp);
+}
+
+// One warp per scope-global object: lanes load 32 entries at a time, then every lane adds
+// them in order (shuffle broadcast), which keeps the reference's summation order.
+__global__ void k_obj_global(uint32_t nglob, const uint32_t* __restrict__ glob, const uint32_t* __restrict__ model_of,
+                             const ModelDev* __restrict__ models, double4_32a* __restrict__ pos,
+                             double4_32a* __restrict__ vel, double4_32a* __restrict__ av, double4_32a* __restrict__ ox,
+                             double4_32a* __restrict__ oz, double4_32a* __restrict__ imp, double4_32a* __restrict__ aimp,
+                             const uint32_t* __restrict__ csr_ptr, const uint32_t* __restrict__ csr_ent,
+                             const uint8_t* __restrict__ flags, const double* __restrict__ out, double dt, d3 fimp,
+                             int write_imp) {
+    const uint32_t w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int lane = threadIdx.x & 31;
+    if (w >= nglob) return;
+    const uint32_t i = glob[w];
+    const ModelDev& m = models[model_of[i]];
+    d3 J = mk(0.0, 0.0, 0.0), JA = mk(0.0, 0.0, 0.0);
+    const bool need_sum = write_imp || m.behavior == BEH_MOBILE || m.behavior == BEH_CONSTRAINED;
+    if (need_sum) {
+        const uint32_t e0 = csr_ptr[i], e1 = csr_ptr[i + 1];
+        for (uint32_t base = e0; base < e1; base += 32) {
+            const uint32_t e = base + lane;
+            double jx = 0, jy = 0, jz = 0, ax = 0, ay = 0, az = 0;
+            int app = 0;
+            if (e < e1) {
+                const uint32_t ent = csr_ent[e];
+                const uint8_t f = flags[ent >> 1];
+                if (f & PF_APPLIED) {
+                    const double* o = out + 9 * (size_t)(ent >> 1);
+                    app = 1;
+                    if (ent & 1) {
+                        jx = -o[0]; jy = -o[1]; jz = -o[2];
+                        if (f & PF_ANGULAR) { ax = o[6]; ay = o[7]; az = o[8]; app = 2; }
+                    } else {
+                        jx = o[0]; jy = o[1]; jz = o[2];
+                        if (f & PF_ANGULAR) { ax = o[3]; ay = o[4]; az = o[5]; app = 2; }
+                    }
+                }
+            }
+            const uint32_t cnt = min(32u, e1 - base);
+            for (uint32_t q = 0; q < cnt; ++q) {
+                const int a = __shfl_sync(0xffffffffu, app, q);
+                const double bx = __shfl_sync(0xffffffffu, jx, q), by = __shfl_sync(0xffffffffu, jy, q),
+                             bz = __shfl_sync(0xffffffffu, jz, q);
+                const double cx = __shfl_sync(0xffffffffu, ax, q), cy = __shfl_sync(0xffffffffu, ay, q),
+                             cz = __shfl_sync(0xffffffffu, az, q);
+                if (a) J = add(J, mk(bx, by, bz));
+                if (a == 2) JA = add(JA, mk(cx, cy, cz));
+            }
+        }
+    }
+    if (lane == 0) finish_object(i, m, J, JA, dt, fimp, pos, vel, av, ox, oz, imp, aimp, write_imp);
+}
+
+// Narrow phase only: PF_ACTIVE of every pair at the current positions (the IsActive()
+// that NBSConsultant::RebuildIactRecordTab reads, NBSConsultant.cpp:384).
+__global__ void __launch_bounds__(TPB) k_detect_active(uint32_t np, const uint2* __restrict__ sm,
+                                                       const uint32_t* __restrict__ param,
+                                                       const PairParam* __restrict__ params,
+                                                       const double4_32a* __restrict__ geom,
+                                                       const double4_32a* __restrict__ pos, const double4_32a* __restrict__ ox,
+                                                       const double4_32a* __restrict__ oz, uint8_t* __restrict__ flags) {
+    const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= np) return;
+    const uint2 p = sm[k];
+    const uint32_t pi = param[k];
+    const double4_32a gg = geom[pi];
+    const PairGeom g{gg.x, gg.y, gg.z, gg.w};
+    double depth;
+    d3 n, point;
+    detect_pair(params[pi].cd, g, ld(pos, p.x), ld(pos, p.y), ox, oz, p.y, depth, n, point);
+    const uint8_t f = flags[k];
+    const uint8_t nf = depth > 0.0 ? (uint8_t)(f | PF_ACTIVE) : (uint8_t)(f & ~PF_ACTIVE);
+    if (nf != f) flags[k] = nf;
+}
+
+// ------------------------------------------------------------------------------------
+// broad phase (NBSConsultant::Reset, NBSConsultant.cpp:85-316)
+__global__ void __launch_bounds__(TPB) k_safe(uint32_t n, const uint32_t* __restrict__ model_of,
+                                              const ModelDev* __restrict__ models, const double4_32a* __restrict__ pos,
+                                              const double4_32a* __restrict__ vel, double sf, double dtu, double glen,
+                                              double* __restrict__ safe, unsigned long long* __restrict__ red) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    unsigned long long mn[3] = {~0ull, ~0ull, ~0ull}, mx[3] = {0, 0, 0}, vm = 0, last = 0;
+    if (i < n) {
+        const ModelDev& m = models[model_of[i]];
+        const double vl = len(ld(vel, i));
+        safe[i] = sf * (2.0 * m.range + dtu * vl + 0.5 * dtu * dtu * glen);   // :127-129
+        if (m.scope == SCOPE_LOCAL) {                                          // :131-141
+            const double4_32a p = pos[i];
+            mn[0] = mx[0] = ord_of(p.x);
+            mn[1] = mx[1] = ord_of(p.y);
+            mn[2] = mx[2] = ord_of(p.z);
+            vm = ord_of(vl);
+            last = (unsigned long long)i + 1;
+        }
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+#pragma unroll
+        for (int q = 0; q < 3; ++q) {
+            mn[q] = min(mn[q], __shfl_xor_sync(0xffffffffu, mn[q], o));
+            mx[q] = max(mx[q], __shfl_xor_sync(0xffffffffu, mx[q], o));
+        }
+        vm = max(vm, __shfl_xor_sync(0xffffffffu, vm, o));
+        last = max(last, __shfl_xor_sync(0xffffffffu, last, o));
+    }
+    if ((threadIdx.x & 31) == 0) {
+        for (int q = 0; q < 3; ++q) {
+            atomicMin(&red[2 * q], mn[q]);
+            atomicMax(&red[2 * q + 1], mx[q]);
+        }
+        atomicMax(&red[6], vm);
+        atomicMax(&red[7], last);
+    }
+}
+
+__global__ void __launch_bounds__(TPB) k_cellkey(uint32_t n, const uint32_t* __restrict__ model_of,
+                                                 const ModelDev* __restrict__ models, const double4_32a* __restrict__ pos,
+                                                 double xmin, double ymin, double zmin, double zone, uint64_t ny1,
+                                                 uint64_t nz1, uint64_t sentinel, uint64_t* __restrict__ key,
+                                                 uint32_t* __restrict__ sid) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    uint64_t k = sentinel;
+    if (models[model_of[i]].scope == SCOPE_LOCAL) {          // :163-178
+        const double4_32a p = pos[i];
+        const uint64_t cx = (uint32_t)((p.x - xmin) / zone);
+        const uint64_t cy = (uint32_t)((p.y - ymin) / zone);
+        const uint64_t cz = (uint32_t)((p.z - zmin) / zone);
+        k = (cx * ny1 + cy) * nz1 + cz;
+    }
+    key[i] = k;
+    sid[i] = i;
+}
+
+__global__ void __launch_bounds__(TPB) k_cell_flags(uint32_t nloc, const uint64_t* __restrict__ key,
+                                                    uint32_t* __restrict__ flag) {
+    const uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= nloc) return;
+    flag[p] = (p == 0 || key[p] != key[p - 1]) ? 1u : 0u;
+}
+
+__global__ void __launch_bounds__(TPB) k_cell_fill(uint32_t nloc, const uint64_t* __restrict__ key,
+                                                   const uint32_t* __restrict__ flag_excl,
+                                                   uint64_t* __restrict__ cell_key, uint32_t* __restrict__ cell_start,
+                                                   uint32_t* __restrict__ cellof, const uint32_t* __restrict__ ncells) {
+    const uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= nloc) return;
+    const bool head = (p == 0 || key[p] != key[p - 1]);
+    const uint32_t c = head ? flag_excl[p] : flag_excl[p] - 1u;   // index of p's cell
+    cellof[p] = c;
+    if (head) {
+        cell_key[c] = key[p];
+        cell_start[c] = p;
+    }
+    if (p == nloc - 1) cell_start[*ncells] = nloc;
+}
+
+template <bool FILL>
+__global__ void __launch_bounds__(TPB) k_pairs(uint32_t nloc, const uint32_t* __restrict__ sid,
+                                               const uint64_t* __restrict__ cell_key,
+                                               const uint32_t* __restrict__ cell_start,
+                                               const uint32_t* __restrict__ ncells_p, const uint32_t* __restrict__ cellof,
+                                               const uint32_t* __restrict__ glob, uint32_t nglob,
+                                               const uint32_t* __restrict__ model_of, const ModelDev* __restrict__ models,
+                                               const int* __restrict__ group_iact, int G,
+                                               const double4_32a* __restrict__ pos, const double4_32a* __restrict__ ox,
+                                               const double4_32a* __restrict__ oz, const double* __restrict__ safe,
+                                               uint32_t ncx, uint32_t ncy, uint32_t ncz, uint64_t ny1, uint64_t nz1,
+                                               uint32_t* __restrict__ task, uint32_t* __restrict__ first,
+                                               uint32_t* __restrict__ second, int* __restrict__ err) {
+    const uint64_t t = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= (uint64_t)nloc * NSLOT) return;
+    const uint32_t P = (uint32_t)(t / NSLOT);
+    const int s = (int)(t % NSLOT);
+    const uint32_t c = cellof[P];
+    const uint64_t key = cell_key[c];
+    const uint32_t cz = (uint32_t)(key % nz1);
+    const uint64_t rest = key / nz1;
+    const uint32_t cy = (uint32_t)(rest % ny1);
+    const uint32_t cx = (uint32_t)(rest / ny1);
+    const uint32_t cs = cell_start[c], csize = cell_start[c + 1] - cs;
+    const uint64_t tid = (uint64_t)cs * NSLOT + (uint64_t)s * csize + (P - cs);
+    if (cx >= ncx || cy >= ncy || cz >= ncz) {                // only cells inside the loops are primary (:186-190)
+        if (!FILL) task[tid] = 0;
+        return;
+    }
+    const uint32_t* js = nullptr;
+    uint32_t jn = 0;
+    if (s == SLOT_SELF) {                                     // BuildIactTab(v), :347-374
+        js = sid + P + 1;
+        jn = cs + csize - (P + 1);
+    } else if (s == SLOT_GLOBAL) {                            // BuildIactTab(v, GlobalElement), :266
+        js = glob;
+        jn = nglob;
+    } else {
+        const int dx = c_slot[s][0], dy = c_slot[s][1], dz = c_slot[s][2];
+        if (!((cx == 0 && dx < 0) || (cy == 0 && dy < 0) || (cz == 0 && dz < 0))) {
+            const uint64_t nk = ((uint64_t)(cx + dx) * ny1 + (uint64_t)(cy + dy)) * nz1 + (uint64_t)(cz + dz);
+            uint32_t lo = 0, hi = *ncells_p;
+            while (lo < hi) {
+                const uint32_t mid = (lo + hi) >> 1;
+                if (cell_key[mid] < nk) lo = mid + 1; else hi = mid;
+            }
+            if (lo < *ncells_p && cell_key[lo] == nk) {
+                js = sid + cell_start[lo];
+                jn = cell_start[lo + 1] - cell_start[lo];
+            }
+        }
+    }
+    const uint32_t i = sid[P];
+    const ModelDev& mi = models[model_of[i]];
+    const double si = safe[i];
+    const int gi = mi.group;
+    uint32_t cnt = 0;
+    const uint32_t off = FILL ? task[tid] : 0u;
+    for (uint32_t q = 0; q < jn; ++q) {                       // BuildIactTab(v1, v2), :318-345
+        const uint32_t j = js[q];
+        const ModelDev& mj = models[model_of[j]];
+        if (group_iact[gi * G + mj.group] < 0) continue;
+        bool ok;
+        const double d = cal_distance(mi, mj, i, j, pos, ox, oz, ok);
+        if (!ok) {
+            atomicOr(err, ERR_BAD_SHAPE_PAIR);
+            continue;
+        }
+        if (d > (si + safe[j])) continue;
+        if (FILL) {
+            first[off + cnt] = i < j ? i : j;
+            second[off + cnt] = i < j ? j : i;
+        }
+        ++cnt;
+    }
+    if (!FILL) task[tid] = cnt;
+}
+
+// Assembler::CreateInteraction orientation and model selection (Assembler.cpp:15-87)
+__global__ void __launch_bounds__(TPB) k_setup(uint32_t np, const uint32_t* __restrict__ first,
+                                               const uint32_t* __restrict__ second,
+                                               const uint32_t* __restrict__ model_of,
+                                               const ModelDev* __restrict__ models,
+                                               const PairParam* __restrict__ params, uint32_t nm,
+                                               uint2* __restrict__ sm, uint32_t* __restrict__ param,
+                                               int* __restrict__ err) {
+    const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= np) return;
+    const uint32_t a = first[k], b = second[k];
+    const uint32_t ma = model_of[a], mb = model_of[b];
+    const ModelDev& A = models[ma];
+    const ModelDev& B = models[mb];
+    uint32_t sl = a, ms = b;
+    bool bad = (B.density < 0.0 || A.density < 0.0) || (B.density == 0.0 && A.density == 0.0);
+    if (A.shape > B.shape) { sl = b; ms = a; }
+    else if (A.shape < B.shape) { sl = a; ms = b; }
+    else if (A.density == 0.0) { sl = b; ms = a; }
+    else if (B.density == 0.0) { sl = a; ms = b; }
+    const uint32_t pi = model_of[sl] * nm + model_of[ms];
+    if (bad || params[pi].cd == 0) {
+        atomicOr(err, ERR_UNSUPPORTED_PAIR);
+        sm[k] = make_uint2(a, b);
+        param[k] = 0;
+        return;
+    }
+    sm[k] = make_uint2(sl, ms);
+    param[k] = pi;
+}
+
+// History carry: a new pair takes the status of the same (first, second) pair of the old
+// list when that pair was active (RebuildIactRecordTab + Initiate, NBSConsultant.cpp:376-395,
+// SimMediator.cpp:690-707); otherwise a default-constructed ImpactStatus.
+__global__ void __launch_bounds__(TPB) k_history_old(uint32_t np, const uint32_t* __restrict__ first,
+                                                     const uint32_t* __restrict__ second,
+                                                     const uint32_t* __restrict__ o_ptr,
+                                                     const uint32_t* __restrict__ o_ent,
+                                                     const uint32_t* __restrict__ o_first,
+                                                     const uint32_t* __restrict__ o_second,
+                                                     const uint8_t* __restrict__ o_flags,
+                                                     const double4_32a* __restrict__ o_hist,
+                                                     const double* __restrict__ o_v0, double4_32a* __restrict__ hist,
+                                                     double* __restrict__ v0, uint8_t* __restrict__ flags) {
+    const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= np) return;
+    const uint32_t a = first[k], b = second[k];
+    uint8_t f = ST_DEFAULT;
+    double4_32a h = make_double4_32a(0.0, 0.0, 0.0, 0.0);
+    double vv = 0.0;
+    const uint32_t e1 = o_ptr[a + 1];
+    for (uint32_t e = o_ptr[a]; e < e1; ++e) {
+        const uint32_t ko = o_ent[e] >> 1;
+        if (o_first[ko] == a && o_second[ko] == b) {
+            const uint8_t of = o_flags[ko];
+            if (of & PF_ACTIVE) {
+                f = of & (PF_STATUS | PF_NONZERO);
+                if (of & PF_NONZERO) {
+                    h = o_hist[ko];
+                    vv = o_v0[ko];
+                }
+            }
+            break;
+        }
+    }
+    hist[k] = h;
+    v0[k] = vv;
+    flags[k] = f;
+}
+
+// History from the IactRecordTab read with the scene (IactRecordTab::GetImpactStatus,
+// IactRecordTab.cpp:20-25); records are sorted by (first << 32 | second).
+__global__ void __launch_bounds__(TPB) k_history_rec(uint32_t np, const uint32_t* __restrict__ first,
+                                                     const uint32_t* __restrict__ second,
+                                                     const uint64_t* __restrict__ rkey, uint32_t nrec,
+                                                     const double4_32a* __restrict__ rhist, const double* __restrict__ rv0,
+                                                     const uint8_t* __restrict__ rflags, double4_32a* __restrict__ hist,
+                                                     double* __restrict__ v0, uint8_t* __restrict__ flags) {
+    const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= np) return;
+    const uint64_t key = ((uint64_t)first[k] << 32) | second[k];
+    uint32_t lo = 0, hi = nrec;
+    while (lo < hi) {
+        const uint32_t mid = (lo + hi) >> 1;
+        if (rkey[mid] < key) lo = mid + 1; else hi = mid;
+    }
+    if (lo < nrec && rkey[lo] == key) {
+        hist[k] = rhist[lo];
+        v0[k] = rv0[lo];
+        flags[k] = rflags[lo];
+    } else {
+        hist[k] = make_double4_32a(0.0, 0.0, 0.0, 0.0);
+        v0[k] = 0.0;
+        flags[k] = ST_DEFAULT;
+    }
+}
+
+__global__ void __launch_bounds__(TPB) k_csr_keys(uint32_t np, const uint2* __restrict__ sm, uint32_t* __restrict__ key,
+                                                  uint32_t* __restrict__ val) {
+    const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= np) return;
+    const uint2 p = sm[k];
+    key[2 * k] = p.x;
+    val[2 * k] = 2 * k;
+    key[2 * k + 1] = p.y;
+    val[2 * k + 1] = 2 * k + 1;
+}
+
+__global__ void __launch_bounds__(TPB) k_csr_ptr(uint32_t n, const uint32_t* __restrict__ key, uint32_t m,
+                                                 uint32_t* __restrict__ ptr) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i > n) return;
+    uint32_t lo = 0, hi = m;
+    while (lo < hi) {
+        const uint32_t mid = (lo + hi) >> 1;
+        if (key[mid] < i) lo = mid + 1; else hi = mid;
+    }
+    ptr[i] = lo;
+}
+
+// ------------------------------------------------------------------------------------
+// observables (DOWorld::CalculateSystemEnergy, DOWorld.cpp:481-660), mobile objects only;
+// fixed-shape tree reductions, so results are deterministic run to run.
+constexpr int OBS_A = 16;
+__global__ void __launch_bounds__(TPB) k_obs_a(uint32_t n, const uint32_t* __restrict__ model_of,
+                                               const ModelDev* __restrict__ models, const double4_32a* __restrict__ pos,
+                                               const double4_32a* __restrict__ vel, const double4_32a* __restrict__ av,
+                                               d3 g, double* __restrict__ part) {
+    __shared__ double s[OBS_A][TPB];
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    double v[OBS_A];
+    for (int q = 0; q < OBS_A; ++q) v[q] = 0.0;
+    v[12] = DBL_MAX; v[13] = -DBL_MAX; v[14] = DBL_MAX; v[15] = -DBL_MAX;
+    if (i < n) {
+        const ModelDev& m = models[model_of[i]];
+        if (m.behavior == BEH_MOBILE) {
+            const d3 V = ld(vel, i), AV = ld(av, i), P = ld(pos, i);
+            const double vl = len(V), al = len(AV);
+            const d3 I = mk(m.ix, m.iy, m.iz);
+            v[0] = -m.mass * dot(g, P);
+            v[1] = 0.5 * m.mass * vl * vl;
+            v[2] = 0.5 * (I.x * AV.x * AV.x + I.y * AV.y * AV.y + I.z * AV.z * AV.z);
+            const d3 mo = smul(m.mass, V), am = cross(I, AV);
+            v[3] = mo.x; v[4] = mo.y; v[5] = mo.z;
+            v[6] = am.x; v[7] = am.y; v[8] = am.z;
+            v[9] = 1.0;
+            v[10] = m.mass;
+            v[11] = 0.0;
+            v[12] = vl; v[13] = vl; v[14] = al; v[15] = al;
+        }
+    }
+    for (int q = 0; q < OBS_A; ++q) s[q][threadIdx.x] = v[q];
+    __syncthreads();
+    for (int w = TPB / 2; w > 0; w >>= 1) {
+        if (threadIdx.x < w) {
+            for (int q = 0; q < 12; ++q) s[q][threadIdx.x] += s[q][threadIdx.x + w];
+            s[12][threadIdx.x] = fmin(s[12][threadIdx.x], s[12][threadIdx.x + w]);
+            s[13][threadIdx.x] = fmax(s[13][threadIdx.x], s[13][threadIdx.x + w]);
+            s[14][threadIdx.x] = fmin(s[14][threadIdx.x], s[14][threadIdx.x + w]);
+            s[15][threadIdx.x] = fmax(s[15][threadIdx.x], s[15][threadIdx.x + w]);
+        }
+        __syncthreads();
+    }
+    if (threadIdx.x < OBS_A) part[(size_t)blockIdx.x * OBS_A + threadIdx.x] = s[threadIdx.x][0];
+}
+
+__global__ void k_obs_reduce(uint32_t nb, int width, const double* __restrict__ part, double* __restrict__ res,
+                             int nmin_from) {
+    // one thread per field, sequential over blocks (deterministic order)
+    const int q = threadIdx.x;
+    if (q >= width) return;
+    double acc = part[q];
+    for (uint32_t b = 1; b < nb; ++b) {
+        const double x = part[(size_t)b * width + q];
+        if (q < nmin_from) acc += x;
+        else if (((q - nmin_from) & 1) == 0) acc = fmin(acc, x);
+        else acc = fmax(acc, x);
+    }
+    res[q] = acc;
+}
+
+__global__ void __launch_bounds__(TPB) k_obs_b(uint32_t n, const uint32_t* __restrict__ model_of,
+                                               const ModelDev* __restrict__ models, const double4_32a* __restrict__ pos,
+                                               const double4_32a* __restrict__ vel, const double4_32a* __restrict__ av,
+                                               const double* __restrict__ res, uint32_t nact_words,
+                                               const uint8_t* __restrict__ flags, uint32_t np,
+                                               double* __restrict__ part) {
+    __shared__ double s[6][TPB];
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    double v[6] = {0, 0, 0, 0, 0, 0};
+    const double cnt = res[9];
+    const d3 mmean = smul(1.0 / cnt, mk(res[3], res[4], res[5]));
+    const d3 amean = smul(1.0 / cnt, mk(res[6], res[7], res[8]));
+    if (i < n) {
+        const ModelDev& m = models[model_of[i]];
+        if (m.behavior == BEH_MOBILE) {
+            const d3 V = ld(vel, i), AV = ld(av, i), P = ld(pos, i);
+            v[0] = len(sub(smul(m.mass, V), mmean));
+            v[1] = len(sub(cross(mk(m.ix, m.iy, m.iz), AV), amean));
+            v[2] = m.mass * P.x; v[3] = m.mass * P.y; v[4] = m.mass * P.z;
+        }
+    }
+    for (uint32_t k = i; k < np; k += gridDim.x * blockDim.x) v[5] += (flags[k] & PF_ACTIVE) ? 1.0 : 0.0;
+    for (int q = 0; q < 6; ++q) s[q][threadIdx.x] = v[q];
+    __syncthreads();
+    for (int w = TPB / 2; w > 0; w >>= 1) {
+        if (threadIdx.x < w)
+            for (int q = 0; q < 6; ++q) s[q][threadIdx.x] += s[q][threadIdx.x + w];
+        __syncthreads();
+    }
+    if (threadIdx.x < 6) part[(size_t)blockIdx.x * 6 + threadIdx.x] = s[threadIdx.x][0];
+}
+
+}  // namespace
+
+// ====================================================================================
+#define CK(call)                                                  \
+    do {                                                          \
+        cudaError_t _e = (call);                                  \
+        if (_e != cudaSuccess) return cuda_fail(_e, #call);       \
+    } while (0)
+
+int Engine::cuda_fail(cudaError_t e, const char* where) {
+    err_ = std::string("CUDA error ") + cudaGetErrorString(e) + " at " + where;
+    return e == cudaErrorMemoryAllocation ? VEDO_ERR_OUT_OF_MEMORY : VEDO_ERR_CUDA;
+}
+
+template <class T>
+static cudaError_t dalloc(T** p, size_t count) {
+    *p = nullptr;
+    if (count == 0) count = 1;
+    return cudaMalloc((void**)p, sizeof(T) * count);
+}
+
+void Engine::free_list(PairList& L) {
+    cudaFree(L.first); cudaFree(L.second); cudaFree(L.sm); cudaFree(L.param); cudaFree(L.hist); cudaFree(L.v0);
+    cudaFree(L.flags); cudaFree(L.out); cudaFree(L.csr_ent); cudaFree(L.csr_ptr);
+    L = PairList{};
+}
+
+int Engine::ensure_list(PairList& L, uint32_t cap) {
+    if (L.csr_ptr == nullptr) CK(dalloc(&L.csr_ptr, (size_t)n_ + 1));
+    if (cap <= L.cap && L.first) return VEDO_OK;
+    uint32_t* ptr = L.csr_ptr;
+    L.csr_ptr = nullptr;
+    free_list(L);
+    L.csr_ptr = ptr;
+    uint64_t c = std::max<uint64_t>(1024, (uint64_t)cap + cap / 4);
+    if (c > 0x7fffffffull) c = 0x7fffffffull;
+    L.cap = (uint32_t)c;
+    CK(dalloc(&L.first, c)); CK(dalloc(&L.second, c)); CK(dalloc(&L.sm, c)); CK(dalloc(&L.param, c));
+    CK(dalloc(&L.hist, c)); CK(dalloc(&L.v0, c)); CK(dalloc(&L.flags, c)); CK(dalloc(&L.out, 9 * c));
+    CK(dalloc(&L.csr_ent, 2 * c));
+    return VEDO_OK;
+}
+
+Engine::~Engine() {
+    if (stream_) cudaStreamSynchronize(stream_);
+    free_list(cur_);
+    free_list(old_);
+    void* ptrs[] = {d_models_, d_params_, d_geom_, d_group_iact_, d_model_of_, d_err_, d_pos_, d_vel_, d_av_, d_ox_,
+                    d_oz_, d_imp_, d_aimp_, d_global_, d_safe_, d_red_, d_key_, d_key_alt_, d_cell_key_, d_sid_,
+                    d_sid_alt_, d_cell_start_, d_cellof_, d_flag_, d_task_, d_total_, d_ck_, d_cv_, d_ck_alt_,
+                    d_cv_alt_, d_cnt_, d_rec_key_, d_rec_hist_, d_rec_v0_, d_rec_flags_, d_obs_};
+    for (void* p : ptrs) if (p) cudaFree(p);
+    for (auto& e : ev_) if (e) cudaEventDestroy(e);
+    if (stream_) cudaStreamDestroy(stream_);
+}
+
+static void upload3(std::vector<double4_32a>& tmp, const std::vector<double>& v, uint32_t n) {
+    tmp.resize(n);
+    for (uint32_t i = 0; i < n; ++i) tmp[i] = make_double4_32a(v[3 * i], v[3 * i + 1], v[3 * i + 2], 0.0);
+}
+
+int Engine::init(const HScene& scene, const vedo_engine_opts& opts) {
+    host_ = scene;
+    opts_ = opts;
+    if (opts_.up_iact == 0) opts_.up_iact = 1;
+    out_prefix_ = opts.output_prefix ? opts.output_prefix : "";
+    std::string msg;
+    int rc = build_tables(host_, tab_, msg);
+    if (rc != VEDO_OK) return fail(rc, msg);
+    n_ = host_.n;
+    nm_ = (uint32_t)tab_.models.size();
+    dt_ = host_.time_interval;
+    t_ = host_.time_current;
+    t_stop_ = host_.time_stop;
+    sf_ = host_.safety_factor;
+    for (int k = 0; k < 3; ++k) g_[k] = host_.g[k];
+    device_ = opts.device;
+    CK(cudaSetDevice(device_));
+    CK(cudaStreamCreateWithFlags(&stream_, cudaStreamNonBlocking));
+    for (auto& e : ev_) CK(cudaEventCreate(&e));
+    // constant tables
+    CK(dalloc(&d_models_, nm_));
+    CK(cudaMemcpy(d_models_, tab_.models.data(), sizeof(ModelDev) * nm_, cudaMemcpyHostToDevice));
+    CK(dalloc(&d_params_, (size_t)nm_ * nm_));
+    CK(cudaMemcpy(d_params_, tab_.params.data(), sizeof(PairParam) * nm_ * nm_, cudaMemcpyHostToDevice));
+    std::vector<double4_32a> geo((size_t)nm_ * nm_);
+    for (size_t q = 0; q < geo.size(); ++q)
+        geo[q] = make_double4_32a(tab_.geom[4 * q], tab_.geom[4 * q + 1], tab_.geom[4 * q + 2], tab_.geom[4 * q + 3]);
+    CK(dalloc(&d_geom_, geo.size()));
+    CK(cudaMemcpy(d_geom_, geo.data(), sizeof(double4_32a) * geo.size(), cudaMemcpyHostToDevice));
+    const int G = tab_.ngroups;
+    CK(dalloc(&d_group_iact_, (size_t)G * G));
+    CK(cudaMemcpy(d_group_iact_, tab_.group_iact.data(), sizeof(int) * G * G, cudaMemcpyHostToDevice));
+    CK(dalloc(&d_model_of_, n_));
+    CK(cudaMemcpy(d_model_of_, host_.model_of.data(), sizeof(uint32_t) * n_, cudaMemcpyHostToDevice));
+    CK(dalloc(&d_err_, 1));
+    CK(cudaMemset(d_err_, 0, sizeof(int)));
+    // objects
+    std::vector<double4_32a> tmp;
+    double4_32a** dst[] = {&d_pos_, &d_vel_, &d_av_, &d_ox_, &d_oz_, &d_imp_, &d_aimp_};
+    const std::vector<double>* src[] = {&host_.pos, &host_.vel, &host_.av, &host_.ox, &host_.oz, &host_.imp, &host_.aimp};
+    for (int k = 0; k < 7; ++k) {
+        CK(dalloc(dst[k], n_));
+        upload3(tmp, *src[k], n_);
+        CK(cudaMemcpy(*dst[k], tmp.data(), sizeof(double4_32a) * n_, cudaMemcpyHostToDevice));
+    }
+    for (uint32_t i = 0; i < n_; ++i)
+        if (tab_.models[host_.model_of[i]].scope != SCOPE_LOCAL) global_ids_.push_back(i);
+    CK(dalloc(&d_global_, global_ids_.size()));
+    if (!global_ids_.empty())
+        CK(cudaMemcpy(d_global_, global_ids_.data(), sizeof(uint32_t) * global_ids_.size(), cudaMemcpyHostToDevice));
+    // broad-phase scratch
+    CK(dalloc(&d_safe_, n_)); CK(dalloc(&d_red_, 8)); CK(dalloc(&d_key_, n_)); CK(dalloc(&d_key_alt_, n_));
+    CK(dalloc(&d_cell_key_, n_)); CK(dalloc(&d_sid_, n_)); CK(dalloc(&d_sid_alt_, n_));
+    CK(dalloc(&d_cell_start_, (size_t)n_ + 1)); CK(dalloc(&d_cellof_, n_)); CK(dalloc(&d_flag_, n_));
+    CK(dalloc(&d_total_, 4));
+    CK(dalloc(&d_obs_, (size_t)(blocks_for(n_) + 2) * 16 + 64));
+    // IDO records, sorted by key, first of equal keys kept (std::map::insert)
+    const HRecords& R = host_.rec;
+    if (R.size()) {
+        std::vector<uint32_t> ord(R.size());
+        for (uint32_t q = 0; q < ord.size(); ++q) ord[q] = q;
+        auto key = [&](uint32_t q) { return ((uint64_t)R.first[q] << 32) | R.second[q]; };
+        std::stable_sort(ord.begin(), ord.end(), [&](uint32_t a, uint32_t b) { return key(a) < key(b); });
+        std::vector<uint64_t> rk;
+        std::vector<double4_32a> rh;
+        std::vector<double> rv;
+        std::vector<uint8_t> rf;
+        for (uint32_t q : ord) {
+            if (!rk.empty() && rk.back() == key(q)) continue;
+            rk.push_back(key(q));
+            rh.push_back(make_double4_32a(R.shear[3 * q], R.shear[3 * q + 1], R.shear[3 * q + 2], R.kn[q]));
+            rv.push_back(R.v0[q]);
+            // default-constructed ImpactStatus + setters (IactRecordTab.cpp:432-530)
+            rf.push_back((uint8_t)(ST_DEFAULT | (R.contact[q] ? ST_CONTACT : 0) | (R.bond[q] ? ST_BOND : 0) | PF_NONZERO));
+        }
+        nrec_ = (uint32_t)rk.size();
+        CK(dalloc(&d_rec_key_, nrec_)); CK(dalloc(&d_rec_hist_, nrec_)); CK(dalloc(&d_rec_v0_, nrec_));
+        CK(dalloc(&d_rec_flags_, nrec_));
+        CK(cudaMemcpy(d_rec_key_, rk.data(), 8 * nrec_, cudaMemcpyHostToDevice));
+        CK(cudaMemcpy(d_rec_hist_, rh.data(), sizeof(double4_32a) * nrec_, cudaMemcpyHostToDevice));
+        CK(cudaMemcpy(d_rec_v0_, rv.data(), 8 * nrec_, cudaMemcpyHostToDevice));
+        CK(cudaMemcpy(d_rec_flags_, rf.data(), nrec_, cudaMemcpyHostToDevice));
+    }
+    // first candidate list (NBSConsultant constructor) + Initiate
+    rc = rebuild(true);
+    if (rc != VEDO_OK) return rc;
+    CK(cudaStreamSynchronize(stream_));
+    backup_pending_ = false;
+    return VEDO_OK;
+}
+
+int Engine::rebuild(bool from_records) {
+    const uint64_t l0 = g_sort_scan_launches;
+    uint64_t own = 0;
+    // IsActive() of the current interactions at the current positions
+    if (!from_records && cur_.np) {
+        k_detect_active<<<blocks_for(cur_.np), TPB, 0, stream_>>>(cur_.np, cur_.sm, cur_.param, d_params_, d_geom_,
+                                                                  d_pos_, d_ox_, d_oz_, cur_.flags);
+        ++own;
+    }
+    std::swap(cur_, old_);
+    // 1. safe lengths and bounds (:120-146)
+    const double dtu = (double)opts_.up_iact * dt_;
+    const double glen = len(mk(g_[0], g_[1], g_[2]));
+    unsigned long long red0[8] = {ord_of(DBL_MAX), ord_of(DBL_MIN), ord_of(DBL_MAX), ord_of(DBL_MIN),
+                                  ord_of(DBL_MAX), ord_of(DBL_MIN), ord_of(0.0), 0ull};
+    CK(cudaMemcpyAsync(d_red_, red0, sizeof(red0), cudaMemcpyHostToDevice, stream_));
+    k_safe<<<blocks_for(n_), TPB, 0, stream_>>>(n_, d_model_of_, d_models_, d_pos_, d_vel_, sf_, dtu, glen, d_safe_,
+                                                d_red_);
+    ++own;
+    unsigned long long red[8];
+    CK(cudaMemcpyAsync(red, d_red_, sizeof(red), cudaMemcpyDeviceToHost, stream_));
+    CK(cudaStreamSynchronize(stream_));
+    const double xmin = dbl_of(red[0]), xmax = dbl_of(red[1]), ymin = dbl_of(red[2]), ymax = dbl_of(red[3]);
+    const double zmin = dbl_of(red[4]), zmax = dbl_of(red[5]), vmax = dbl_of(red[6]);
+    const uint32_t nloc = n_ - (uint32_t)global_ids_.size();
+    double rmax = 0.0;
+    if (red[7]) rmax = tab_.models[host_.model_of[red[7] - 1]].range;     // the last local DO (:140)
+    const double zone = sf_ * (2.0 * rmax + dtu * vmax + 0.5 * dtu * dtu * glen);   // :146
+    auto ncel = [&](double lo, double hi) {
+        uint32_t c = (uint32_t)std::ceil((hi - lo) / zone);
+        return std::max(c, (uint32_t)1);
+    };
+    const uint32_t ncx = ncel(xmin, xmax), ncy = ncel(ymin, ymax), ncz = ncel(zmin, zmax);
+    const uint64_t ny1 = (uint64_t)ncy + 1, nz1 = (uint64_t)ncz + 1;
+    const uint64_t sentinel = ((uint64_t)ncx + 1) * ny1 * nz1;
+    int bits = 1;
+    while (bits < 64 && (sentinel >> bits)) ++bits;
+    // 2. cell keys, stable sort (locals by cell, ids ascending within a cell)
+    k_cellkey<<<blocks_for(n_), TPB, 0, stream_>>>(n_, d_model_of_, d_models_, d_pos_, xmin, ymin, zmin, zone, ny1,
+                                                   nz1, sentinel, d_key_, d_sid_);
+    ++own;
+    CK(radix_sort_u64(d_key_, d_sid_, d_key_alt_, d_sid_alt_, n_, 0, bits, scratch_, stream_));
+    // 3. cell ranges
+    uint32_t np = 0;
+    if (nloc) {
+        k_cell_flags<<<blocks_for(nloc), TPB, 0, stream_>>>(nloc, d_key_, d_flag_);
+        CK(exclusive_scan_u32(d_flag_, d_flag_, nloc, d_total_, scratch_, stream_));
+        k_cell_fill<<<blocks_for(nloc), TPB, 0, stream_>>>(nloc, d_key_, d_flag_, d_cell_key_, d_cell_start_,
+                                                           d_cellof_, d_total_);
+        own += 2;
+        // 4. count pass over (object, slot) tasks, scan, fill pass
+        const uint64_t ntask = (uint64_t)nloc * NSLOT;
+        if (ntask + 1 > task_cap_) {
+            if (d_task_) cudaFree(d_task_);
+            task_cap_ = (uint32_t)(ntask + 1);
+            CK(dalloc(&d_task_, task_cap_));
+        }
+        CK(cudaMemsetAsync(d_err_, 0, sizeof(int), stream_));
+        k_pairs<false><<<blocks_for(ntask), TPB, 0, stream_>>>(
+            nloc, d_sid_, d_cell_key_, d_cell_start_, d_total_, d_cellof_, d_global_, (uint32_t)global_ids_.size(),
+            d_model_of_, d_models_, d_group_iact_, tab_.ngroups, d_pos_, d_ox_, d_oz_, d_safe_, ncx, ncy, ncz, ny1,
+            nz1, d_task_, nullptr, nullptr, d_err_);
+        ++own;
+        CK(exclusive_scan_u32(d_task_, d_task_, (uint32_t)ntask, d_total_ + 1, scratch_, stream_));
+        CK(cudaMemcpyAsync(&np, d_total_ + 1, sizeof(uint32_t), cudaMemcpyDeviceToHost, stream_));
+        CK(cudaStreamSynchronize(stream_));
+        int rc = ensure_list(cur_, np);
+        if (rc != VEDO_OK) return rc;
+        k_pairs<true><<<blocks_for(ntask), TPB, 0, stream_>>>(
+            nloc, d_sid_, d_cell_key_, d_cell_start_, d_total_, d_cellof_, d_global_, (uint32_t)global_ids_.size(),
+            d_model_of_, d_models_, d_group_iact_, tab_.ngroups, d_pos_, d_ox_, d_oz_, d_safe_, ncx, ncy, ncz, ny1,
+            nz1, d_task_, cur_.first, cur_.second, d_err_);
+        ++own;
+    } else {
+        int rc = ensure_list(cur_, 0);
+        if (rc != VEDO_OK) return rc;
+    }
+    cur_.np = np;
+    // 5. interactions: orientation and model selection
+    if (np) {
+        k_setup<<<blocks_for(np), TPB, 0, stream_>>>(np, cur_.first, cur_.second, d_model_of_, d_models_, d_params_,
+                                                     nm_, cur_.sm, cur_.param, d_err_);
+        ++own;
+        // 6. history
+        if (from_records) {
+            k_history_rec<<<blocks_for(np), TPB, 0, stream_>>>(np, cur_.first, cur_.second, d_rec_key_, nrec_,
+                                                               d_rec_hist_, d_rec_v0_, d_rec_flags_, cur_.hist,
+                                                               cur_.v0, cur_.flags);
+        } else {
+            k_history_old<<<blocks_for(np), TPB, 0, stream_>>>(np, cur_.first, cur_.second, old_.csr_ptr,
+                                                               old_.csr_ent, old_.first, old_.second, old_.flags,
+                                                               old_.hist, old_.v0, cur_.hist, cur_.v0, cur_.flags);
+        }
+        ++own;
+    }
+    // 7. per-object contact entries in ascending pair index (stable radix sort by object)
+    const uint32_t m = 2 * np;
+    if (m > csr_cap_) {
+        for (uint32_t** p : {&d_ck_, &d_ck_alt_, &d_cv_alt_}) {
+            if (*p) cudaFree(*p);
+            *p = nullptr;
+        }
+        csr_cap_ = std::max<uint32_t>(m + m / 4, 2048);
+        CK(dalloc(&d_ck_, csr_cap_)); CK(dalloc(&d_ck_alt_, csr_cap_)); CK(dalloc(&d_cv_alt_, csr_cap_));
+    }
+    if (np) {
+        k_csr_keys<<<blocks_for(np), TPB, 0, stream_>>>(np, cur_.sm, d_ck_, cur_.csr_ent);
+        ++own;
+        int obits = 1;
+        while (obits < 32 && ((n_ - 1) >> obits)) ++obits;
+        CK(radix_sort_u32(d_ck_, cur_.csr_ent, d_ck_alt_, d_cv_alt_, m, 0, obits, scratch_, stream_));
+    }
+    k_csr_ptr<<<blocks_for((uint64_t)n_ + 1), TPB, 0, stream_>>>(n_, d_ck_, m, cur_.csr_ptr);
+    ++own;
+    int herr = 0;
+    CK(cudaMemcpyAsync(&herr, d_err_, sizeof(int), cudaMemcpyDeviceToHost, stream_));
+    CK(cudaStreamSynchronize(stream_));
+    CK(cudaGetLastError());
+    launches_ += own + (g_sort_scan_launches - l0);
+    if (herr & ERR_BAD_SHAPE_PAIR)
+        return fail(VEDO_ERR_UNSUPPORTED_MODEL, "broad phase met a shape pair DOMap::CalDistance does not handle");
+    if (herr & ERR_UNSUPPORTED_PAIR)
+        return fail(VEDO_ERR_UNSUPPORTED_MODEL,
+                    "a candidate pair has no detector/solver (the reference would drop it and misalign its "
+                    "interaction records)");
+    backup_pending_ = false;
+    return VEDO_OK;
+}
+
+int Engine::step_once(bool write_impulses) {
+    const double dt = dt_;
+    const bool prof = profiling_;
+    // CalculateImpact
+    if (prof) CK(cudaEventRecord(ev_[0], stream_));
+    if (cur_.np) {
+        k_pair<<<blocks_for(cur_.np), TPB, 0, stream_>>>(cur_.np, cur_.sm, cur_.param, d_params_, d_geom_, d_pos_,
+                                                         d_vel_, d_av_, d_ox_, d_oz_, cur_.hist, cur_.v0, cur_.flags,
+                                                         cur_.out, dt, backup_pending_ ? 1 : 0);
+        ++launches_;
+    }
+    if (prof) CK(cudaEventRecord(ev_[1], stream_));
+    // AddFieldImpact + AddConstrainedImpact + Response (+ CheckContactStatus in the next k_pair)
+    const d3 fimp = muls(mk(g_[0], g_[1], g_[2]), dt);    // csp->GetFieldAcceleration() * dt (SimMediator.cpp:738)
+    k_obj<<<blocks_for(n_), TPB, 0, stream_>>>(n_, d_model_of_, d_models_, d_pos_, d_vel_, d_av_, d_ox_, d_oz_,
+                                               d_imp_, d_aimp_, cur_.csr_ptr, cur_.csr_ent, cur_.flags, cur_.out, dt,
+                                               fimp, write_impulses ? 1 : 0);
+    ++launches_;
+    if (!global_ids_.empty()) {
+        k_obj_global<<<blocks_for((uint64_t)global_ids_.size() * 32), TPB, 0, stream_>>>(
+            (uint32_t)global_ids_.size(), d_global_, d_model_of_, d_models_, d_pos_, d_vel_, d_av_, d_ox_, d_oz_,
+            d_imp_, d_aimp_, cur_.csr_ptr, cur_.csr_ent, cur_.flags, cur_.out, dt, fimp, write_impulses ? 1 : 0);
+        ++launches_;
+    }
+    if (prof) CK(cudaEventRecord(ev_[2], stream_));
+    backup_pending_ = true;
+    // NBSConsultant::NextStep (NBSConsultant.cpp:35-78)
+    ++round_;
+    t_ += dt;                                              // SystemParameter::NextStep (SystemParameter.h:113-116)
+    if (round_ % opts_.up_iact == 0) {
+        if (prof) CK(cudaEventRecord(ev_[3], stream_));
+        int rc = rebuild(false);
+        if (rc != VEDO_OK) return rc;
+        if (prof) {
+            CK(cudaEventRecord(ev_[4], stream_));
+            CK(cudaEventSynchronize(ev_[4]));
+            float ms = 0;
+            cudaEventElapsedTime(&ms, ev_[3], ev_[4]);
+            prof_ms_[2] += ms;
+        }
+    }
+    if (prof) {
+        float a = 0, b = 0;
+        CK(cudaEventSynchronize(ev_[2]));
+        cudaEventElapsedTime(&a, ev_[0], ev_[1]);
+        cudaEventElapsedTime(&b, ev_[1], ev_[2]);
+        prof_ms_[0] += a;
+        prof_ms_[1] += b;
+    }
+    if (opts_.record && round_ % opts_.record == 0 && !out_prefix_.empty()) {
+        int rc = record_ido();
+        if (rc != VEDO_OK) return rc;
+    }
+    if (t_ >= t_stop_ && !out_prefix_.empty()) {         // NBSConsultant.cpp:65-76
+        std::string dir = out_prefix_;
+        size_t slash = dir.find_last_of('/');
+        dir = slash == std::string::npos ? std::string() : dir.substr(0, slash + 1);
+        int rc = write_ido((dir + "terminate.ido").c_str());
+        if (rc != VEDO_OK) return rc;
+    }
+    return VEDO_OK;
+}
+
+int Engine::run(uint32_t nsteps, int* keep_running) {
+    prof_ms_[0] = prof_ms_[1] = prof_ms_[2] = 0;
+    launches_ = 0;
+    CK(cudaSetDevice(device_));
+    for (uint32_t s = 0; s < nsteps; ++s) {
+        int rc = step_once(s + 1 == nsteps);
+        if (rc != VEDO_OK) return rc;
+    }
+    CK(cudaStreamSynchronize(stream_));
+    CK(cudaGetLastError());
+    if (keep_running) *keep_running = t_ < t_stop_ ? 1 : 0;   // SimMediator.cpp:839-841
+    return VEDO_OK;
+}
+
+uint64_t Engine::last_profile(double out[3]) const {
+    for (int k = 0; k < 3; ++k) out[k] = prof_ms_[k];
+    return launches_;
+}
+
+// ------------------------------------------------------------------------------------
+static void download3(double* dst, const double4_32a* src_dev, uint32_t n, std::vector<double4_32a>& tmp, cudaStream_t s) {
+    tmp.resize(n);
+    cudaMemcpyAsync(tmp.data(), src_dev, sizeof(double4_32a) * n, cudaMemcpyDeviceToHost, s);
+    cudaStreamSynchronize(s);
+    for (uint32_t i = 0; i < n; ++i) {
+        dst[3 * i] = tmp[i].x;
+        dst[3 * i + 1] = tmp[i].y;
+        dst[3 * i + 2] = tmp[i].z;
+    }
+}
+
+int Engine::get_state(const vedo_state_view& v) {
+    std::vector<double4_32a> tmp;
+    double* dst[] = {v.position, v.velocity, v.angular_velocity, v.orientation_x, v.orientation_z, v.impact,
+                     v.angular_impact};
+    const double4_32a* src[] = {d_pos_, d_vel_, d_av_, d_ox_, d_oz_, d_imp_, d_aimp_};
+    for (int k = 0; k < 7; ++k)
+        if (dst[k]) download3(dst[k], src[k], n_, tmp, stream_);
+    CK(cudaGetLastError());
+    return VEDO_OK;
+}
+
+int Engine::set_state(const vedo_state_view& v) {
+    std::vector<double4_32a> tmp(n_);
+    const double* srcs[] = {v.position, v.velocity, v.angular_velocity, v.orientation_x, v.orientation_z, v.impact,
+                            v.angular_impact};
+    double4_32a* dst[] = {d_pos_, d_vel_, d_av_, d_ox_, d_oz_, d_imp_, d_aimp_};
+    for (int k = 0; k < 7; ++k) {
+        if (!srcs[k]) continue;
+        for (uint32_t i = 0; i < n_; ++i)
+            tmp[i] = make_double4_32a(srcs[k][3 * i], srcs[k][3 * i + 1], srcs[k][3 * i + 2], 0.0);
+        CK(cudaMemcpyAsync(dst[k], tmp.data(), sizeof(double4_32a) * n_, cudaMemcpyHostToDevice, stream_));
+        CK(cudaStreamSynchronize(stream_));
+    }
+    return VEDO_OK;
+}
+
+int Engine::num_interactions(uint32_t* n) {
+    *n = cur_.np;
+    return VEDO_OK;
+}
+
+int Engine::get_interactions(const vedo_contact_view& v) {
+    const uint32_t np = cur_.np;
+    if (!np) return VEDO_OK;
+    // ContactInfo::bActive of the last narrow phase = detection at the current positions
+    k_detect_active<<<blocks_for(np), TPB, 0, stream_>>>(np, cur_.sm, cur_.param, d_params_, d_geom_, d_pos_, d_ox_,
+                                                         d_oz_, cur_.flags);
+    std::vector<uint2> sm(np);
+    std::vector<uint8_t> fl(np);
+    std::vector<double4_32a> h(np);
+    if (v.first) CK(cudaMemcpyAsync(v.first, cur_.first, 4 * np, cudaMemcpyDeviceToHost, stream_));
+    if (v.second) CK(cudaMemcpyAsync(v.second, cur_.second, 4 * np, cudaMemcpyDeviceToHost, stream_));
+    CK(cudaMemcpyAsync(sm.data(), cur_.sm, sizeof(uint2) * np, cudaMemcpyDeviceToHost, stream_));
+    CK(cudaMemcpyAsync(fl.data(), cur_.flags, np, cudaMemcpyDeviceToHost, stream_));
+    CK(cudaMemcpyAsync(h.data(), cur_.hist, sizeof(double4_32a) * np, cudaMemcpyDeviceToHost, stream_));
+    CK(cudaStreamSynchronize(stream_));
+    for (uint32_t k = 0; k < np; ++k) {
+        const bool nz = fl[k] & PF_NONZERO;
+        if (v.slave) v.slave[k] = sm[k].x;
+        if (v.master) v.master[k] = sm[k].y;
+        if (v.active) v.active[k] = (fl[k] & PF_ACTIVE) ? 1 : 0;
+        if (v.contact) v.contact[k] = (fl[k] & ST_CONTACT) ? 1 : 0;
+        if (v.kn) v.kn[k] = nz ? h[k].w : 0.0;
+        if (v.shear) {
+            v.shear[3 * k] = nz ? h[k].x : 0.0;
+            v.shear[3 * k + 1] = nz ? h[k].y : 0.0;
+            v.shear[3 * k + 2] = nz ? h[k].z : 0.0;
+        }
+    }
+    return VEDO_OK;
+}
+
+int Engine::get_observables(double out[13]) {
+    const unsigned nb = std::max(1u, blocks_for(n_));
+    double* part = d_obs_;
+    double* res = d_obs_ + (size_t)nb * 16 + 16;
+    const d3 g = mk(g_[0], g_[1], g_[2]);
+    k_obs_a<<<nb, TPB, 0, stream_>>>(n_, d_model_of_, d_models_, d_pos_, d_vel_, d_av_, g, part);
+    k_obs_reduce<<<1, 32, 0, stream_>>>(nb, 16, part, res, 12);
+    if (cur_.np)
+        k_detect_active<<<blocks_for(cur_.np), TPB, 0, stream_>>>(cur_.np, cur_.sm, cur_.param, d_params_, d_geom_,
+                                                                  d_pos_, d_ox_, d_oz_, cur_.flags);
+    k_obs_b<<<nb, TPB, 0, stream_>>>(n_, d_model_of_, d_models_, d_pos_, d_vel_, d_av_, res, 0, cur_.flags, cur_.np,
+                                     part);
+    k_obs_reduce<<<1, 32, 0, stream_>>>(nb, 6, part, res + 16, 6);
+    double r[22];
+    CK(cudaMemcpyAsync(r, res, sizeof(r), cudaMemcpyDeviceToHost, stream_));
+    CK(cudaStreamSynchronize(stream_));
+    const bool any = r[9] > 0;
+    out[0] = r[0]; out[1] = r[1]; out[2] = r[2];
+    out[3] = any ? r[12] : 0.0; out[4] = any ? r[13] : 0.0; out[5] = any ? r[14] : 0.0; out[6] = any ? r[15] : 0.0;
+    out[7] = r[16]; out[8] = r[17];
+    out[9] = r[21];
+    const double msum = r[10];
+    out[10] = msum > 0 ? r[18] / msum : 0.0;
+    out[11] = msum > 0 ? r[19] / msum : 0.0;
+    out[12] = msum > 0 ? r[20] / msum : 0.0;
+    return VEDO_OK;
+}
+
+int Engine::sync_host_state() {
+    vedo_state_view v{host_.pos.data(), host_.vel.data(), host_.av.data(), host_.ox.data(), host_.oz.data(),
+                      host_.imp.data(), host_.aimp.data()};
+    return get_state(v);
+}
+
+int Engine::write_ido(const char* path) {
+    int rc = sync_host_state();
+    if (rc != VEDO_OK) return rc;
+    host_.time_current = t_;
+    // IactRecordTab = the active interactions (NBSConsultant::RebuildIactRecordTab)
+    const uint32_t np = cur_.np;
+    std::vector<uint32_t> a(np), b(np);
+    std::vector<uint8_t> act(np), con(np);
+    std::vector<double> sh(3 * (size_t)np), kn(np);
+    vedo_contact_view cv{a.data(), b.data(), nullptr, nullptr, act.data(), sh.data(), kn.data(), con.data()};
+    rc = get_interactions(cv);
+    if (rc != VEDO_OK) return rc;
+    std::vector<double> v0(np);
+    if (np) {
+        CK(cudaMemcpyAsync(v0.data(), cur_.v0, 8 * np, cudaMemcpyDeviceToHost, stream_));
+        CK(cudaStreamSynchronize(stream_));
+    }
+    HRecords R;
+    std::vector<uint32_t> idx;
+    for (uint32_t k = 0; k < np; ++k)
+        if (act[k]) idx.push_back(k);
+    std::sort(idx.begin(), idx.end(), [&](uint32_t x, uint32_t y) {
+        return a[x] != a[y] ? a[x] < a[y] : b[x] < b[y];
+    });
+    for (uint32_t k : idx) {
+        R.first.push_back(a[k]); R.second.push_back(b[k]);
+        R.contact.push_back(con[k]); R.bond.push_back(0);
+        R.kn.push_back(kn[k]); R.v0.push_back(v0[k]);
+        for (int q = 0; q < 3; ++q) {
+            R.shear.push_back(sh[3 * k + q]);
+            R.point.push_back(0.0); R.dirn.push_back(0.0); R.imp.push_back(0.0); R.aimp.push_back(0.0);
+        }
+        R.overlap.push_back(0.0);
+    }
+    HScene copy_rec = host_;
+    copy_rec.rec = R;
+    std::string msg;
+    if (!vedo::write_ido(path, copy_rec, msg)) return fail(VEDO_ERR_IO, msg);
+    return VEDO_OK;
+}
+
+int Engine::record_ido() {                                 // Consultant::RecordIDO (Consultant.cpp:217-230)
+    char num[32];
+    snprintf(num, sizeof(num), "%d", (int)(10000001 + record_count_));
+    std::string file = out_prefix_ + "_" + (record_count_ < 11000001 ? std::string(num + 2) : std::string(num)) + ".ido";
+    ++record_count_;
+    return write_ido(file.c_str());
+}
+
+}  // namespace vedo

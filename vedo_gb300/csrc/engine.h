@@ -1,0 +1,126 @@
+// engine.h - the GB300 DEM engine object behind the C ABI (include/vedo_gpu.h).
+//
+// One engine = one scene on one GPU, driven on its own CUDA stream.  Device layout:
+//   objects  (n):  pos/vel/av/ox/oz/imp/aimp as double4_32a (x, y, z, pad) - one 32-byte
+//                  sector per gathered vector; model index per object.
+//   pairs    (P):  candidate list in the reference's NBS order: key (first < second),
+//                  oriented (slave, master), parameter index, status (shear + kn as
+//                  double4_32a, v0, flag byte), impulse output (J, tA, tB: 9 doubles).
+//   CSR     (2P):  for each object, its pair entries (k << 1 | side) in ascending k, so
+//                  the per-object impulse sum follows the reference's IactContainer order.
+#pragma once
+
+#include <cstdint>
+#include <string>
+#include <vector>
+
+#include <cuda_runtime.h>
+
+#include "../../include/vedo_gpu.h"
+#include "dem_common.cuh"
+#include "scene_host.h"
+#include "sort_scan.h"
+
+namespace vedo {
+
+struct PairList {
+    uint32_t np = 0, cap = 0;
+    uint32_t* first = nullptr;
+    uint32_t* second = nullptr;
+    uint2* sm = nullptr;
+    uint32_t* param = nullptr;
+    double4_32a* hist = nullptr;     // shear (x, y, z), kn
+    double* v0 = nullptr;
+    uint8_t* flags = nullptr;    // ST_* | PF_* bits (dem_physics.cuh)
+    double* out = nullptr;       // [cap][9]: J, tA, tB of the last solve
+    uint32_t* csr_ent = nullptr; // [2*cap]
+    uint32_t* csr_ptr = nullptr; // [n+1]
+};
+
+class Engine {
+public:
+    Engine() = default;
+    ~Engine();
+
+    int init(const HScene& scene, const vedo_engine_opts& opts);
+    int run(uint32_t nsteps, int* keep_running);
+    int get_state(const vedo_state_view& v);
+    int set_state(const vedo_state_view& v);
+    int num_interactions(uint32_t* n);
+    int get_interactions(const vedo_contact_view& v);
+    int get_observables(double out[13]);
+    int write_ido(const char* path);
+
+    double time() const { return t_; }
+    uint64_t steps() const { return round_; }
+    uint32_t num_objects() const { return n_; }
+    uint64_t last_profile(double out[3]) const;
+    void set_profiling(bool on) { profiling_ = on; }
+    const std::string& error() const { return err_; }
+
+private:
+    int fail(int code, const std::string& msg) { err_ = msg; return code; }
+    int cuda_fail(cudaError_t e, const char* where);
+    int rebuild(bool from_records);
+    int ensure_list(PairList& L, uint32_t cap);
+    void free_list(PairList& L);
+    int step_once(bool write_impulses);
+    int record_ido();
+    int sync_host_state();
+
+    // scene and options
+    HScene host_;
+    Tables tab_;
+    vedo_engine_opts opts_{};
+    std::string out_prefix_;
+    std::string err_;
+    uint32_t n_ = 0, nm_ = 0;
+    double dt_ = 0, t_ = 0, t_stop_ = 0, sf_ = 1.1;
+    double g_[3] = {0, 0, 0};
+    uint64_t round_ = 0;
+    uint64_t record_count_ = 0;
+    bool backup_pending_ = false;   // ImpactStatus::Backup owed before the next solve
+    int device_ = 0;
+    cudaStream_t stream_ = nullptr;
+
+    // device: constants
+    ModelDev* d_models_ = nullptr;
+    PairParam* d_params_ = nullptr;
+    double4_32a* d_geom_ = nullptr;     // per (slave model, master model): ra, b0, b1, b2
+    int* d_group_iact_ = nullptr;
+    uint32_t* d_model_of_ = nullptr;
+    int* d_err_ = nullptr;
+    // device: objects
+    double4_32a *d_pos_ = nullptr, *d_vel_ = nullptr, *d_av_ = nullptr, *d_ox_ = nullptr, *d_oz_ = nullptr;
+    double4_32a *d_imp_ = nullptr, *d_aimp_ = nullptr;
+    // device: pair lists (current and previous)
+    PairList cur_, old_;
+    std::vector<uint32_t> global_ids_;   // host copy of the scope-global objects
+    uint32_t* d_global_ = nullptr;
+    // device: broad-phase scratch
+    Scratch scratch_;
+    double* d_safe_ = nullptr;
+    unsigned long long* d_red_ = nullptr;
+    uint64_t *d_key_ = nullptr, *d_key_alt_ = nullptr, *d_cell_key_ = nullptr;
+    uint32_t *d_sid_ = nullptr, *d_sid_alt_ = nullptr, *d_cell_start_ = nullptr, *d_cellof_ = nullptr;
+    uint32_t *d_flag_ = nullptr, *d_task_ = nullptr, *d_total_ = nullptr;
+    uint32_t task_cap_ = 0;
+    uint32_t *d_ck_ = nullptr, *d_cv_ = nullptr, *d_ck_alt_ = nullptr, *d_cv_alt_ = nullptr;
+    uint32_t csr_cap_ = 0;
+    uint32_t* d_cnt_ = nullptr;
+    // records from the .ido (creation only)
+    uint64_t* d_rec_key_ = nullptr;
+    uint32_t nrec_ = 0;
+    double4_32a* d_rec_hist_ = nullptr;
+    double* d_rec_v0_ = nullptr;
+    uint8_t* d_rec_flags_ = nullptr;
+    // observables scratch
+    double* d_obs_ = nullptr;
+    // profiling of the last run()
+    cudaEvent_t ev_[8] = {};
+    bool profiling_ = false;       // per-phase CUDA-event timing (adds a host sync per step)
+    double prof_ms_[3] = {0, 0, 0};
+    uint64_t launches_ = 0;
+};
+
+}  // namespace vedo

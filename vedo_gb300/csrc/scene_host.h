@@ -1,0 +1,70 @@
+// scene_host.h - host-side scene (what the reference's DOWorld holds), the reference
+// .ido reader/writer, and the flattening of models into the engine's device tables.
+#pragma once
+
+#include <cstdint>
+#include <string>
+#include <utility>
+#include <vector>
+
+#include "../../include/vedo_gpu.h"
+#include "dem_common.cuh"
+
+namespace vedo {
+
+struct HModel {
+    std::string name, group;
+    uint32_t behavior = 0, scope = 0, shape = 0, color = 0;
+    double density = 0, density_factor = 0;
+    double ext[3] = {0, 0, 0};
+    double attrs[10] = {0};
+    std::vector<std::pair<std::string, double>> materials;
+};
+
+struct HIact {
+    std::string master_group, slave_group, equation_type;
+    std::vector<std::pair<std::string, double>> mech;
+};
+
+struct HRecords {
+    std::vector<uint32_t> first, second;
+    std::vector<uint8_t> contact, bond;
+    std::vector<double> kn, v0, overlap;
+    std::vector<double> shear, point, dirn, imp, aimp;   // [n][3]
+    size_t size() const { return first.size(); }
+};
+
+struct HScene {
+    double time_start = 0, time_stop = 0, time_interval = 0, time_current = 0;
+    double g[3] = {0, 0, 0};
+    double safety_factor = 1.1;
+    uint8_t zoi_switch[3] = {0, 0, 0}, pbc_switch[3] = {0, 0, 0};
+    double zoi_lower[3] = {0, 0, 0}, zoi_upper[3] = {0, 0, 0}, pbc_lower[3] = {0, 0, 0}, pbc_upper[3] = {0, 0, 0};
+    uint32_t num_udd_do = 0, num_udd_impact = 0, max_id_of_do = 0;
+    std::vector<HModel> models;
+    std::vector<HIact> iacts;
+    uint32_t n = 0;
+    std::vector<uint32_t> model_of, ids;
+    std::vector<double> pos, vel, ox, oz, av, imp, aimp;   // [n][3]
+    HRecords rec;
+};
+
+// Reference .ido format (DOWorld_RWIDO.cpp:9-202); returns false with a message on error.
+bool read_ido(const std::string& path, HScene& s, std::string& err);
+bool write_ido(const std::string& path, const HScene& s, std::string& err);
+bool scene_from_desc(const vedo_scene_desc* d, HScene& s, std::string& err);
+
+// Flattened constants for the device.
+struct Tables {
+    std::vector<ModelDev> models;
+    int ngroups = 0;
+    std::vector<int> group_iact;          // [ngroups*ngroups] -> interaction model index or -1
+    std::vector<PairParam> params;        // [nmodels*nmodels], (slave model, master model)
+    std::vector<double> geom;             // [nmodels*nmodels][4]: slave radius, master attrs a0..a2
+};
+
+// DOModel::Analysis + DOcf selection + ImpactSolver constructor constants.  Fails with
+// VEDO_ERR_UNSUPPORTED_MODEL / VEDO_ERR_INVALID_SCENE and a message.
+int build_tables(const HScene& s, Tables& t, std::string& err);
+
+}  // namespace vedo

@@ -1,0 +1,182 @@
+"""ctypes binding of the GPU engine (``vedo_gb300/_build/libvedogpu.so``, C ABI of include/vedo_gpu.h).
+
+:class:`GpuEngine` is the host-side mirror of the reference's ``SimMediator``
+(src/vedo/framework/SimMediator.h:22-36): construct it from a scene (or an ``.ido``
+file, as ``anne`` does) and call :meth:`Run` once per time step, or :meth:`run` for
+many steps at a time.  There is no CPU fallback: if the CUDA library is missing or no
+GPU is present, construction raises.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+from typing import Dict, Optional
+
+import numpy as np
+
+from . import _abi
+from ._abi import ContactView, EngineOpts, StateView, dptr, scene_to_desc
+from .scene import Scene
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "_build", "libvedogpu.so")
+
+_lib = None
+
+
+class EngineError(RuntimeError):
+    def __init__(self, code: int, msg: str):
+        super().__init__(f"{_abi.STATUS_NAMES.get(code, code)}: {msg}")
+        self.code = code
+
+
+def lib() -> C.CDLL:
+    """Load the engine library (fails loudly when it has not been built)."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            raise RuntimeError(f"{LIB_PATH} is missing: build it with `python -m vedo_gb300.build`")
+        L = C.CDLL(LIB_PATH)
+        vp = C.c_void_p
+        L.vedo_gpu_default_opts.argtypes = [C.POINTER(EngineOpts)]
+        L.vedo_gpu_create.argtypes = [C.POINTER(_abi.SceneDesc), C.POINTER(EngineOpts), C.POINTER(vp)]
+        L.vedo_gpu_create_from_ido.argtypes = [C.c_char_p, C.POINTER(EngineOpts), C.POINTER(vp)]
+        L.vedo_gpu_run.argtypes = [vp, C.c_uint32, C.POINTER(C.c_int)]
+        L.vedo_gpu_num_objects.argtypes = [vp]
+        L.vedo_gpu_num_objects.restype = C.c_uint32
+        L.vedo_gpu_get_state.argtypes = [vp, C.POINTER(StateView)]
+        L.vedo_gpu_set_state.argtypes = [vp, C.POINTER(StateView)]
+        L.vedo_gpu_num_interactions.argtypes = [vp, C.POINTER(C.c_uint32)]
+        L.vedo_gpu_get_interactions.argtypes = [vp, C.POINTER(ContactView)]
+        L.vedo_gpu_get_observables.argtypes = [vp, C.POINTER(C.c_double)]
+        L.vedo_gpu_time.argtypes = [vp]
+        L.vedo_gpu_time.restype = C.c_double
+        L.vedo_gpu_step_count.argtypes = [vp]
+        L.vedo_gpu_step_count.restype = C.c_uint64
+        L.vedo_gpu_write_ido.argtypes = [vp, C.c_char_p]
+        L.vedo_gpu_last_run_profile.argtypes = [vp, C.POINTER(C.c_double)]
+        L.vedo_gpu_last_run_profile.restype = C.c_uint64
+        L.vedo_gpu_set_profiling.argtypes = [vp, C.c_int]
+        L.vedo_gpu_last_error.argtypes = [vp]
+        L.vedo_gpu_last_error.restype = C.c_char_p
+        L.vedo_gpu_destroy.argtypes = [vp]
+        L.vedo_gpu_version.restype = C.c_char_p
+        _lib = L
+    return _lib
+
+
+STATE_FIELDS = ("position", "velocity", "angular_velocity", "orientation_x", "orientation_z", "impact",
+                "angular_impact")
+
+
+class GpuEngine:
+    """One scene on one GPU.
+
+    Parameters mirror ``anne analysis <ido> nbs <Record> <UpIact>`` (Anne.cpp:38-128):
+    `up_iact` is the candidate-list rebuild interval, `record` the IDO record interval
+    (0 = never) and `output_prefix` where record/terminate IDO files go (None = none).
+    """
+
+    def __init__(self, scene, up_iact: int = 1, record: int = 0, precision: int = _abi.PRECISION_FP64,
+                 device: int = 0, output_prefix: Optional[str] = None):
+        L = lib()
+        opts = EngineOpts()
+        L.vedo_gpu_default_opts(C.byref(opts))
+        opts.up_iact, opts.record, opts.precision, opts.device = up_iact, record, precision, device
+        self._prefix = output_prefix.encode() if output_prefix else None
+        opts.output_prefix = self._prefix
+        h = C.c_void_p()
+        if isinstance(scene, (str, bytes, os.PathLike)):
+            rc = L.vedo_gpu_create_from_ido(os.fsencode(scene), C.byref(opts), C.byref(h))
+        else:
+            desc, keep = scene_to_desc(scene)
+            rc = L.vedo_gpu_create(C.byref(desc), C.byref(opts), C.byref(h))
+            del keep
+        if rc != 0:
+            raise EngineError(rc, L.vedo_gpu_last_error(None).decode())
+        self.h = h
+        self.n = L.vedo_gpu_num_objects(h)
+
+    def _check(self, rc: int):
+        if rc != 0:
+            raise EngineError(rc, lib().vedo_gpu_last_error(self.h).decode())
+
+    # SimMediator::Run (SimMediator.cpp:714-842): one step, returns t < t_stop
+    def Run(self) -> bool:
+        return self.run(1)
+
+    def run(self, nsteps: int) -> bool:
+        keep = C.c_int(0)
+        self._check(lib().vedo_gpu_run(self.h, nsteps, C.byref(keep)))
+        return bool(keep.value)
+
+    def state(self, fields=STATE_FIELDS) -> Dict[str, np.ndarray]:
+        out = {f: np.zeros((self.n, 3)) for f in fields}
+        v = StateView()
+        for f in fields:
+            setattr(v, f, dptr(out[f]))
+        self._check(lib().vedo_gpu_get_state(self.h, C.byref(v)))
+        return out
+
+    def set_state(self, **arrays):
+        v = StateView()
+        keep = []
+        for f, a in arrays.items():
+            a = np.ascontiguousarray(a, dtype=np.float64).reshape(self.n, 3)
+            keep.append(a)
+            setattr(v, f, dptr(a))
+        self._check(lib().vedo_gpu_set_state(self.h, C.byref(v)))
+
+    def interactions(self) -> Dict[str, np.ndarray]:
+        n = C.c_uint32(0)
+        self._check(lib().vedo_gpu_num_interactions(self.h, C.byref(n)))
+        m = n.value
+        out = dict(first=np.zeros(m, np.uint32), second=np.zeros(m, np.uint32), slave=np.zeros(m, np.uint32),
+                   master=np.zeros(m, np.uint32), active=np.zeros(m, np.uint8), shear=np.zeros((m, 3)),
+                   kn=np.zeros(m), contact=np.zeros(m, np.uint8))
+        v = ContactView()
+        for k in ("first", "second", "slave", "master"):
+            setattr(v, k, _abi.uptr(out[k]))
+        v.active, v.contact = _abi.bptr(out["active"]), _abi.bptr(out["contact"])
+        v.shear, v.kn = dptr(out["shear"]), dptr(out["kn"])
+        self._check(lib().vedo_gpu_get_interactions(self.h, C.byref(v)))
+        return out
+
+    def observables(self) -> np.ndarray:
+        o = np.zeros(13)
+        self._check(lib().vedo_gpu_get_observables(self.h, dptr(o)))
+        return o
+
+    def time(self) -> float:
+        return lib().vedo_gpu_time(self.h)
+
+    def step_count(self) -> int:
+        return lib().vedo_gpu_step_count(self.h)
+
+    def write_ido(self, path: str):
+        self._check(lib().vedo_gpu_write_ido(self.h, os.fsencode(path)))
+
+    def set_profiling(self, on: bool):
+        lib().vedo_gpu_set_profiling(self.h, 1 if on else 0)
+
+    def last_run_profile(self):
+        o = np.zeros(3)
+        launches = lib().vedo_gpu_last_run_profile(self.h, dptr(o))
+        return {"pair_ms": o[0], "object_ms": o[1], "rebuild_ms": o[2], "launches": int(launches)}
+
+    def close(self):
+        if getattr(self, "h", None):
+            lib().vedo_gpu_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
