@@ -1,0 +1,327 @@
+#!/usr/bin/env python3
+"""DEM time-step throughput on GB300: particle-steps/s on the 1,000,000-sphere polydisperse
+Hertz drum (radii lognormal median 1 mm, sigma_log 0.2, clipped to [0.5, 2] mm, 32 classes;
+E = 70 GPa, nu = 0.25, e = 0.7, mu = 0.4 via the frictional Hertz-family law ISwH;
+drum R = 0.15 m, L = 0.3 m, polygon shell of 64 fixed plates, end plates at 30 rpm;
+dt = 5e-7 s).  Synthetic seeded scene (vedo_gb300.scenes.hertz_drum).
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+One step = one DEM time step of the whole scene (SimMediator::Run).  `value` is measured
+with CUDA events on the engine's stream around exactly K steps with the scene resident in
+HBM; `e2e` goes through the C ABI with host buffers (state uploaded from pinned memory,
+stepped, read back, every `--sync` steps).  Under torchrun (N > 1) every rank runs an
+independent replica of the scene (no collective on the data path) and `value` is the
+particle-steps of all ranks over the slowest rank's time.  `--impl reference` times the
+reference algorithm on the host cores (the C restatement of the reference step; the
+reference's own build cannot run on this host).
+"""
+import argparse
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "particle-steps/s on 1 GB300 (mixed vs FP64 at stated error); serving p50/p99 ms"
+UNIT = "particle-steps/s"
+WORKLOAD = "hertz_drum_1M"
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=100)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--n", type=int, default=1_000_000, help="spheres in the drum")
+    ap.add_argument("--up-iact", type=int, default=20, help="candidate-list rebuild interval")
+    ap.add_argument("--sync", type=int, default=20, help="e2e: steps between host state round trips")
+    ap.add_argument("--e2e-iters", type=int, default=3)
+    ap.add_argument("--cpu-sample-steps", type=int, default=20)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-profile-pass", action="store_true")
+    return ap.parse_args()
+
+
+# ------------------------------------------------------------------------------------------
+class Dist:
+    def __init__(self):
+        self.world = int(os.environ.get("WORLD_SIZE", "1"))
+        self.rank = int(os.environ.get("RANK", "0"))
+        self.local = int(os.environ.get("LOCAL_RANK", "0"))
+        self.pg = None
+        if self.world > 1:
+            import torch.distributed as dist
+            dist.init_process_group(backend="gloo")
+            self.pg = dist
+
+    def barrier(self):
+        if self.pg:
+            self.pg.barrier()
+
+    def reduce(self, x: float, op: str) -> float:
+        if not self.pg:
+            return x
+        import torch
+        t = torch.tensor([x], dtype=torch.float64)
+        self.pg.all_reduce(t, op=self.pg.ReduceOp.MAX if op == "max" else self.pg.ReduceOp.SUM)
+        return float(t.item())
+
+    def close(self):
+        if self.pg:
+            self.pg.destroy_process_group()
+
+
+class Clocks:
+    """nvidia-smi samples during the timed region (clocks, power, throttle reasons)."""
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu: int):
+        self.gpu = gpu
+        self.proc = None
+        self.path = None
+
+    def start(self):
+        try:
+            fd, self.path = tempfile.mkstemp(suffix=".csv")
+            os.close(fd)
+            self.f = open(self.path, "w")
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.FIELDS}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"], stdout=self.f,
+                                         stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+
+    def stop(self):
+        if not self.proc:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        self.f.close()
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in open(self.path):
+            p = [x.strip() for x in line.split(",")]
+            if len(p) < 9:
+                continue
+            try:
+                sm.append(float(p[1]))
+                mx.append(float(p[2]))
+            except ValueError:
+                continue
+            for k, nm in enumerate(names):
+                if p[5 + k].lower().startswith("active"):
+                    reasons.add(nm)
+        os.unlink(self.path)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+def emit(d):
+    print(json.dumps(d), flush=True)
+
+
+# ------------------------------------------------------------------------------------------
+def cpu_rate(scene, up_iact, steps):
+    """The reference step restated in C (oracle/dem_oracle.c), single thread, on this host."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle
+    oracle.build_port()
+    from oracle import PortWorld
+    w = PortWorld(scene, up_iact=up_iact)
+    t0 = time.perf_counter()
+    w.run(steps)
+    t1 = time.perf_counter()
+    w.close()
+    return scene_particles(scene) * steps / (t1 - t0), t1 - t0
+
+
+def scene_particles(scene):
+    from vedo_gb300.scene import SPHERE
+    sph = [k for k, m in enumerate(scene.models) if m.shape == SPHERE]
+    import numpy as np
+    return int(np.isin(scene.model_index, sph).sum())
+
+
+def reference_arm(args, dist):
+    if dist.rank != 0:
+        return
+    from vedo_gb300 import scenes
+    scene = scenes.hertz_drum(n=args.n)
+    n = scene_particles(scene)
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle
+    oracle.build_port()
+    from oracle import PortWorld
+    w = PortWorld(scene, up_iact=args.up_iact)
+    w.run(max(0, args.warmup))
+    # bound the timed part to about two minutes of CPU work
+    t0 = time.perf_counter()
+    w.run(1)
+    one = time.perf_counter() - t0
+    k = max(1, min(args.steps - 1, int(120.0 / max(one, 1e-6))))
+    t0 = time.perf_counter()
+    w.run(k)
+    dt = time.perf_counter() - t0 + one
+    k += 1
+    value = n * k / dt
+    emit({"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus, "steps": k, "warmup": args.warmup,
+          "ms_per_step": 1e3 * dt / k, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+          "dtype": "f64", "data": "synthetic (seeded hertz_drum scene)", "impl": "reference",
+          "config": {"workload": WORKLOAD, "particles": n, "up_iact": args.up_iact,
+                     "steps_timed": k, "steps_requested": args.steps},
+          "cpu_baseline": {"value": value, "unit": UNIT, "cores": 1, "kind": "port",
+                           "sample": f"{k} full time steps of the {n}-sphere drum after {args.warmup} warm-up "
+                                     f"steps, single thread (the reference step is sequential)"},
+          "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}})
+
+
+# ------------------------------------------------------------------------------------------
+def ours(args, dist):
+    import numpy as np
+    import torch
+    from vedo_gb300 import build as vbuild
+    if dist.local == 0 or dist.world == 1:
+        vbuild.build()
+    dist.barrier()
+    vbuild.build()
+    from vedo_gb300 import scenes
+    from vedo_gb300.engine import GpuEngine
+
+    dev = dist.local
+    torch.cuda.set_device(dev)
+    scene = scenes.hertz_drum(n=args.n, seed=2024 + dist.rank)
+    n = scene_particles(scene)
+    cpu = None
+    if dist.rank == 0 and dist.world == 1 and not args.no_cpu_baseline:
+        rate, secs = cpu_rate(scene, args.up_iact, args.cpu_sample_steps)
+        cpu = {"value": rate, "unit": UNIT, "cores": 1, "kind": "port",
+               "sample": f"first {args.cpu_sample_steps} time steps (one candidate-list rebuild) of the same "
+                         f"{n}-sphere drum, single thread, {secs:.1f} s"}
+    eng = GpuEngine(scene, up_iact=args.up_iact, device=dev)
+    eng.run(args.warmup)
+    dist.barrier()
+    torch.cuda.synchronize()
+    clocks = Clocks(dev)
+    clocks.start()
+    eng.run(args.steps)
+    prof = eng.last_run_profile()
+    clocks_rec = clocks.stop()
+    dist.barrier()
+    t_ms = dist.reduce(prof["total_ms"], "max")
+    total_particles = dist.reduce(float(n), "sum")
+    value = total_particles * args.steps / (t_ms * 1e-3)
+    launches = prof["launches"]
+    it = eng.interactions()
+    n_pairs = len(it["first"])
+    n_active = int(it["active"].sum())
+
+    # per-kernel split for the roofline (profiled pass: adds a host sync per step)
+    kern = None
+    if not args.no_profile_pass:
+        eng.set_profiling(True)
+        eng.run(args.up_iact)
+        kp = eng.last_run_profile()
+        eng.set_profiling(False)
+        kern = kp
+    # e2e through the C ABI with pinned host buffers
+    fields = ("position", "velocity", "angular_velocity", "orientation_x", "orientation_z")
+    st = eng.state(fields)
+    pinned = {f: torch.empty((eng.n, 3), dtype=torch.float64, pin_memory=True) for f in fields}
+    host = {f: pinned[f].numpy() for f in fields}
+    for f in fields:
+        host[f][:] = st[f]
+    e2e_t = 0.0
+    e2e_steps = 0
+    for _ in range(args.e2e_iters):
+        t0 = time.perf_counter()
+        eng.set_state(**host)
+        eng.run(args.sync)
+        out = eng.state(fields)
+        t1 = time.perf_counter()
+        for f in fields:
+            host[f][:] = out[f]
+        e2e_t += t1 - t0
+        e2e_steps += args.sync
+    e2e_t = dist.reduce(e2e_t, "max")
+    e2e_value = total_particles * e2e_steps / e2e_t
+    xfer = 24 * eng.n * len(fields)
+
+    # algorithmic bytes per particle-step (FP64 form): state x, v, w + orientation Ox, Oz
+    # (integrated) read and written, per active contact the ISwH history (shear + kn) read
+    # and written plus the pair index, plus the per-particle radius (polydisperse)
+    s_state = 72 + 48
+    s_hist = 32
+    z_pp = n_active / n
+    b_alg = 2 * s_state + z_pp * (2 * s_hist + 8) + 8
+    peak, peak_kind = peaks()
+    roof = None
+    if kern and kern["pair_ms"] + kern["object_ms"] > 0:
+        steps_k = args.up_iact
+        t_pair = kern["pair_ms"] / steps_k
+        t_obj = kern["object_ms"] / steps_k
+        if t_pair >= t_obj:
+            name, t_k, bytes_k = "k_pair", t_pair, n_active * (2 * s_hist + 8)
+        else:
+            name, t_k, bytes_k = "k_obj", t_obj, n * (2 * s_state + 8)
+        ach = bytes_k / (t_k * 1e-3) / 1e9
+        roof = {"kernel": name, "bound": "hbm", "achieved": ach, "peak": peak, "unit": "GB/s",
+                "frac": ach / peak, "peak_source": peak_kind, "traffic": None,
+                "ms_per_launch": t_k, "alg_bytes_per_launch": bytes_k,
+                "step_split_ms": {"pair": t_pair, "object": t_obj, "rebuild_per_step": kern["rebuild_ms"] / steps_k}}
+    res = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": dist.world, "steps": args.steps,
+           "warmup": args.warmup, "ms_per_step": t_ms / args.steps, "higher_is_better": True, "scaling": "weak",
+           "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded hertz_drum scene, no dataset)",
+           "config": {"workload": WORKLOAD, "particles_per_gpu": n, "objects_per_gpu": eng.n,
+                      "form": "plain FP64 (drop-in, bit-exact order of operations)", "up_iact": args.up_iact,
+                      "candidate_pairs": n_pairs, "active_contacts": n_active, "z_pp": z_pp,
+                      "alg_bytes_per_particle_step": b_alg,
+                      "l2": "working set larger than L2 (state + candidate list > 129 MB)",
+                      "parallelism": f"replicas x{dist.world}", "window": f"steps {args.warmup}.."
+                      f"{args.warmup + args.steps} of the configured 10000-step run"},
+           "clocks": clocks_rec, "gpu_launches": launches,
+           "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": xfer / args.sync,
+                   "d2h_bytes_per_step": xfer / args.sync,
+                   "note": f"vedo_gpu_set_state + vedo_gpu_run({args.sync}) + vedo_gpu_get_state per "
+                           f"{args.sync} steps, pinned host buffers"},
+           "roofline": roof, "cpu_baseline": cpu}
+    eng.close()
+    if dist.rank == 0:
+        emit(res)
+
+
+def main():
+    args = parse()
+    dist = Dist()
+    try:
+        if args.impl == "reference":
+            reference_arm(args, dist)
+        else:
+            ours(args, dist)
+    finally:
+        dist.close()
+
+
+if __name__ == "__main__":
+    main()

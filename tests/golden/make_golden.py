@@ -1,0 +1,56 @@
+"""Generate the golden fixtures of tests/golden/ from the reference itself.
+
+Runs the reference DEM CPU path (compiled from the reference sources by
+``make -C oracle ref``; needs the reference checkout, default /root/reference or
+$VEDO_REFERENCE) on small seeded scenes and stores, per case, the scene as the
+reference reads it (.ido bytes), the run parameters and the reference's results:
+final object state, candidate list (IactPairTab order), interaction list
+(slave/master, active flag, shear history, kn, contact flag) and energies.
+
+    python tests/golden/make_golden.py
+"""
+import os
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+sys.path[:0] = [ROOT, os.path.join(ROOT, "oracle")]
+
+from vedo_gb300 import scenes  # noqa: E402
+
+
+def cases():
+    """(name, scene, steps, up_iact) of every fixture."""
+    yield "box_lsd", scenes.lsd_box(n_side=5, steps=3000, vel_sigma=0.3, seed=11), 2500, 10
+    for solver in ("ISwBSDBF", "ISwBtSDBF", "ISwBSDB2F", "ISwHertz", "ISwH"):
+        yield f"cluster_{solver}", scenes.cluster(n=48, solver=solver, steps=400, seed=5), 300, 5
+    yield "cluster_poly_orbital_cyl", scenes.cluster(n=48, solver="ISwH", polydisperse=True, orbital=True,
+                                                     cylinders=3, steps=300, seed=9), 200, 3
+    yield "cluster_bsdbf_upiact1", scenes.cluster(n=27, solver="ISwBSDBF", steps=200, seed=2), 150, 1
+
+
+def main():
+    import oracle
+    oracle.build_ref()
+    from oracle import RefWorld
+    for name, sc, steps, up in cases():
+        ido = sc.to_ido()
+        w = RefWorld(sc, up_iact=up)
+        cf0, cs0 = w.candidates()
+        w.run(steps)
+        st = w.state()
+        cf, cs = w.candidates()
+        it = w.interactions()
+        np.savez_compressed(os.path.join(HERE, f"{name}.npz"), ido=np.frombuffer(ido, np.uint8), steps=steps,
+                            up_iact=up, cand0_first=cf0, cand0_second=cs0, cand_first=cf, cand_second=cs,
+                            time=w.time(), energy=w.energy(),
+                            **{f"state_{k}": v for k, v in st.items()},
+                            **{f"iact_{k}": v for k, v in it.items()})
+        print(name, sc.num_objects, "objects", len(cf), "candidates", int(it["active"].sum()), "active")
+        w.close()
+
+
+if __name__ == "__main__":
+    main()

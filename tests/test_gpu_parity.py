@@ -1,0 +1,200 @@
+"""GPU parity tests: the CUDA engine, called through the C ABI, against the reference's golden
+vectors (tests/golden, produced by the reference itself) and against the C oracle.
+
+Tolerances: the linear spring-dashpot laws with fixed walls use only IEEE-rounded +,-,*,/
+and sqrt, evaluated in the reference's order without FMA, so the engine must agree bit for
+bit.  Hertz and ISwH call pow(), orbital walls call cos()/sin(); CUDA's and glibc's results
+may differ in the last ulp, so those cases use rtol 1e-9 on short runs (per-step forces agree
+to ~1e-15 relative); the contact set and history pairing stay exact."""
+import glob
+import os
+
+import numpy as np
+import pytest
+
+from vedo_gb300 import scenes
+from vedo_gb300.scene import Scene
+
+pytestmark = pytest.mark.gpu
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+GOLDEN = sorted(glob.glob(os.path.join(ROOT, "tests", "golden", "*.npz")))
+EXACT_CASES = ("box_lsd", "cluster_ISwBSDBF", "cluster_ISwBtSDBF", "cluster_ISwBSDB2F", "cluster_bsdbf_upiact1")
+STATE = ("position", "velocity", "angular_velocity", "impact", "angular_impact", "orientation_x", "orientation_z")
+
+
+def _name(p):
+    return os.path.splitext(os.path.basename(p))[0]
+
+
+@pytest.mark.parametrize("path", GOLDEN, ids=[_name(p) for p in GOLDEN])
+def test_engine_matches_reference_golden(path, engine_lib):
+    g = np.load(path)
+    sc = Scene.from_ido(g["ido"].tobytes())
+    e = engine_lib.GpuEngine(sc, up_iact=int(g["up_iact"]))
+    it0 = e.interactions()
+    assert np.array_equal(it0["first"], g["cand0_first"]) and np.array_equal(it0["second"], g["cand0_second"])
+    e.run(int(g["steps"]))
+    it = e.interactions()
+    assert np.array_equal(it["first"], g["cand_first"]) and np.array_equal(it["second"], g["cand_second"])
+    assert np.array_equal(it["active"], g["iact_active"])
+    assert np.array_equal(it["slave"], g["iact_slave"]) and np.array_equal(it["master"], g["iact_master"])
+    assert np.array_equal(it["contact"], g["iact_contact"])
+    st = e.state()
+    exact = _name(path) in EXACT_CASES
+    for k in STATE:
+        ref = g[f"state_{k}"]
+        if exact and not k.startswith("orientation"):
+            np.testing.assert_array_equal(st[k], ref, err_msg=k)
+        else:
+            np.testing.assert_allclose(st[k], ref, rtol=1e-9, atol=1e-12 * (np.abs(ref).max() + 1e-300), err_msg=k)
+    if exact:
+        np.testing.assert_array_equal(it["shear"], g["iact_shear"])
+    else:
+        np.testing.assert_allclose(it["shear"], g["iact_shear"], rtol=1e-8, atol=1e-14)
+    assert e.time() == float(g["time"])
+    e.close()
+
+
+@pytest.mark.parametrize("solver", ["ISwBSDBF", "ISwBtSDBF", "ISwBSDB2F", "ISwHertz", "ISwH"])
+def test_per_step_impulses_at_identical_state(solver, engine_lib, port_lib):
+    """From identical state, one step: per-object impulse and angular impulse agree with the
+    oracle within 1e-10 relative (exactly for the linear laws)."""
+    from oracle import PortWorld
+    sc = scenes.cluster(n=64, solver=solver, steps=500, seed=21)
+    e = engine_lib.GpuEngine(sc, up_iact=4)
+    p = PortWorld(sc, up_iact=4)
+    e.run(120)
+    p.run(120)
+    s = p.state()
+    sc2 = sc.copy()
+    for k in ("position", "velocity", "angular_velocity", "orientation_x", "orientation_z"):
+        setattr(sc2, k, s[k])
+    e2 = engine_lib.GpuEngine(sc2, up_iact=4)
+    p2 = PortWorld(sc2, up_iact=4)
+    e2.run(1)
+    p2.run(1)
+    a, b = e2.state(), p2.state()
+    for k in ("impact", "angular_impact"):
+        scale = np.abs(b[k]).max() + 1e-300
+        if solver in ("ISwHertz", "ISwH"):
+            np.testing.assert_allclose(a[k], b[k], rtol=1e-10, atol=1e-10 * scale, err_msg=k)
+        else:
+            np.testing.assert_array_equal(a[k], b[k], err_msg=k)
+    ia, ib = e2.interactions(), p2.interactions()
+    assert np.array_equal(ia["active"], ib["active"].astype(np.uint8))
+    assert ia["active"].sum() > 0
+
+
+def test_lsd_box_full_size_bitexact(engine_lib, port_lib):
+    """The 8,000-sphere box: 600 steps with rebuilds every 20, bit for bit against the oracle."""
+    from oracle import PortWorld
+    sc = scenes.lsd_box()
+    e = engine_lib.GpuEngine(sc, up_iact=20)
+    p = PortWorld(sc, up_iact=20)
+    e.run(600)
+    p.run(600)
+    a, b = e.state(), p.state()
+    for k in ("position", "velocity", "angular_velocity", "impact", "angular_impact"):
+        np.testing.assert_array_equal(a[k], b[k], err_msg=k)
+    ia = e.interactions()
+    f, s = p.candidates()
+    assert np.array_equal(ia["first"], f) and np.array_equal(ia["second"], s)
+
+
+def test_first_100_steps_pointwise_hertz_drum_small(engine_lib, port_lib):
+    """Polydisperse ISwH drum (orbital end plates, polygon shell), 20k spheres: pointwise agreement
+    for the first 100 steps (1e-9 relative), exact contact set."""
+    from oracle import PortWorld
+    sc = scenes.hertz_drum(n=20000, seed=5, steps=200)
+    e = engine_lib.GpuEngine(sc, up_iact=10)
+    p = PortWorld(sc, up_iact=10)
+    for _ in range(4):
+        e.run(25)
+        p.run(25)
+        a, b = e.state(), p.state()
+        for k in ("position", "velocity"):
+            np.testing.assert_allclose(a[k], b[k], rtol=1e-9, atol=1e-12 * np.abs(b[k]).max() + 1e-300, err_msg=k)
+    ia, ib = e.interactions(), p.interactions()
+    f, s = p.candidates()
+    assert np.array_equal(ia["first"], f) and np.array_equal(ia["second"], s)
+    assert np.array_equal(ia["active"], ib["active"].astype(np.uint8))
+
+
+def test_create_from_ido_equals_create(engine_lib, tmp_path):
+    sc = scenes.cluster(n=40, solver="ISwH", polydisperse=True, cylinders=2, seed=4)
+    path = tmp_path / "s.ido"
+    sc.to_ido(str(path))
+    a = engine_lib.GpuEngine(sc, up_iact=3)
+    b = engine_lib.GpuEngine(str(path), up_iact=3)
+    a.run(150)
+    b.run(150)
+    sa, sb = a.state(), b.state()
+    for k in sa:
+        np.testing.assert_array_equal(sa[k], sb[k])
+
+
+def test_history_survives_ido_restart(engine_lib, tmp_path):
+    """run(2k) == run(k) + write_ido + reload + run(k): the IDO carries the shear history."""
+    sc = scenes.cluster(n=64, solver="ISwBSDBF", steps=1000, seed=8)
+    a = engine_lib.GpuEngine(sc, up_iact=5)
+    a.run(300)
+    assert a.interactions()["active"].sum() > 0
+    path = tmp_path / "mid.ido"
+    a.write_ido(str(path))
+    a.run(300)
+    b = engine_lib.GpuEngine(str(path), up_iact=5)
+    b.run(300)
+    sa, sb = a.state(), b.state()
+    for k in ("position", "velocity", "angular_velocity"):
+        np.testing.assert_array_equal(sa[k], sb[k])
+
+
+def test_deterministic_reruns(engine_lib):
+    sc = scenes.hertz_drum(n=30000, seed=2, steps=100)
+    r = []
+    for _ in range(2):
+        e = engine_lib.GpuEngine(sc, up_iact=10)
+        e.run(60)
+        r.append(e.state())
+        e.close()
+    for k in r[0]:
+        assert np.array_equal(r[0][k], r[1][k])
+
+
+def test_observables_match_oracle(engine_lib, port_lib):
+    from oracle import PortWorld
+    sc = scenes.lsd_box(n_side=10)
+    e = engine_lib.GpuEngine(sc, up_iact=10)
+    p = PortWorld(sc, up_iact=10)
+    e.run(200)
+    p.run(200)
+    o, q = e.observables(), p.energy()
+    np.testing.assert_allclose(o[:9], q, rtol=1e-12)
+
+
+def test_unsupported_model_is_an_error(engine_lib):
+    sc = scenes.cluster(n=8)
+    sc.iact_models[0].equation_type = "ISwNoSuchLaw"
+    with pytest.raises(engine_lib.EngineError) as ex:
+        engine_lib.GpuEngine(sc)
+    assert ex.value.code == 3
+
+
+def test_missing_mechanism_is_an_error(engine_lib):
+    sc = scenes.cluster(n=8)
+    sc.iact_models[0].mechanisms = [m for m in sc.iact_models[0].mechanisms if m[0] != "ShearStiffness"]
+    with pytest.raises(engine_lib.EngineError) as ex:
+        engine_lib.GpuEngine(sc)
+    assert ex.value.code == 2
+
+
+def test_engine_native_library_is_the_one_loaded(engine_lib):
+    """The product path is the in-tree CUDA library: no fallback exists."""
+    import ctypes
+    e = engine_lib.GpuEngine(scenes.cluster(n=8))
+    e.run(2)
+    assert engine_lib._lib is not None and engine_lib._lib._name.endswith("libvedogpu.so")
+    prof = e.last_run_profile()
+    assert prof["launches"] >= 4
+    del ctypes

@@ -1,0 +1,163 @@
+"""CPU tests: the C oracle against the reference's golden vectors, the .ido format, the
+scene generators and the C ABI library's exported symbols.  No GPU needed."""
+import ctypes
+import glob
+import os
+import re
+
+import numpy as np
+import pytest
+
+from vedo_gb300 import scenes
+from vedo_gb300.scene import Scene
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+GOLDEN = sorted(glob.glob(os.path.join(ROOT, "tests", "golden", "*.npz")))
+EXACT_CASES = ("box_lsd", "cluster_ISwBSDBF", "cluster_ISwBtSDBF", "cluster_ISwBSDB2F", "cluster_bsdbf_upiact1")
+
+
+def _name(p):
+    return os.path.splitext(os.path.basename(p))[0]
+
+
+@pytest.mark.parametrize("path", GOLDEN, ids=[_name(p) for p in GOLDEN])
+def test_port_matches_reference_golden(path, port_lib):
+    """The C restatement reproduces the reference's own outputs: candidate list (order included),
+    active set and shear-history pairing exactly; state bit for bit for the linear laws with fixed
+    walls, and within 1e-9 relative where libm pow/cos/sin enter (Hertz, ISwH, orbital walls)."""
+    from oracle import PortWorld
+    g = np.load(path)
+    sc = Scene.from_ido(g["ido"].tobytes())
+    w = PortWorld(sc, up_iact=int(g["up_iact"]))
+    f0, s0 = w.candidates()
+    assert np.array_equal(f0, g["cand0_first"]) and np.array_equal(s0, g["cand0_second"])
+    w.run(int(g["steps"]))
+    f, s = w.candidates()
+    assert np.array_equal(f, g["cand_first"]) and np.array_equal(s, g["cand_second"])
+    it = w.interactions()
+    assert np.array_equal(it["active"], g["iact_active"])
+    assert np.array_equal(it["slave"], g["iact_slave"]) and np.array_equal(it["master"], g["iact_master"])
+    assert np.array_equal(it["contact"], g["iact_contact"])
+    st = w.state()
+    exact = _name(path) in EXACT_CASES
+    for k in ("position", "velocity", "angular_velocity", "impact", "angular_impact", "orientation_x",
+              "orientation_z"):
+        ref = g[f"state_{k}"]
+        if exact:
+            np.testing.assert_array_equal(st[k], ref, err_msg=k)
+        else:
+            np.testing.assert_allclose(st[k], ref, rtol=1e-9, atol=1e-12 * (np.abs(ref).max() + 1e-300), err_msg=k)
+    if exact:
+        np.testing.assert_array_equal(it["shear"], g["iact_shear"])
+    else:
+        np.testing.assert_allclose(it["shear"], g["iact_shear"], rtol=1e-8, atol=1e-14)
+    assert w.time() == float(g["time"])
+
+
+def test_port_energy_matches_reference(port_lib):
+    """DOWorld::CalculateSystemEnergy restated (the reference computes it at the last reset)."""
+    from oracle import PortWorld
+    g = np.load(os.path.join(ROOT, "tests", "golden", "box_lsd.npz"))
+    w = PortWorld(Scene.from_ido(g["ido"].tobytes()), up_iact=int(g["up_iact"]))
+    w.run(int(g["steps"]))
+    np.testing.assert_array_equal(w.energy(), g["energy"])
+
+
+def test_ido_roundtrip_bytes():
+    """Scene -> .ido -> Scene -> .ido is byte-identical (records included)."""
+    sc = scenes.cluster(n=20, solver="ISwH", polydisperse=True, cylinders=2)
+    from vedo_gb300.scene import Records
+    m = 3
+    sc.records = Records(np.array([0, 1, 2], np.uint32), np.array([5, 6, 7], np.uint32),
+                         np.array([1, 0, 1], bool), np.array([0, 0, 1], bool), np.arange(m) * 1.5,
+                         np.arange(m) * 0.25, np.arange(9.0).reshape(3, 3), np.ones((3, 3)), np.zeros((3, 3)),
+                         np.full((3, 3), 2.0), np.full((3, 3), -1.0), np.arange(m) * 1e-6)
+    b1 = sc.to_ido()
+    sc2 = Scene.from_ido(b1)
+    assert sc2.to_ido() == b1
+    assert len(sc2.records) == 3 and sc2.records.contact.tolist() == [True, False, True]
+
+
+def test_golden_ido_parses():
+    """Every fixture's .ido (written by our writer, read by the reference when the fixtures were
+    made) parses back into the same object count and models."""
+    for p in GOLDEN:
+        g = np.load(p)
+        sc = Scene.from_ido(g["ido"].tobytes())
+        assert sc.num_objects == g["state_position"].shape[0]
+        assert sc.to_ido() == g["ido"].tobytes()
+
+
+def test_truncated_ido_rejected():
+    b = scenes.cluster(n=8).to_ido()
+    with pytest.raises(ValueError):
+        Scene.from_ido(b[: len(b) // 2])
+
+
+def test_time_control_runs_exact_step_count(port_lib):
+    """t_stop = (steps - 1/2) dt makes Run() return false exactly after `steps` steps."""
+    from oracle import PortWorld
+    sc = scenes.cluster(n=8, steps=37)
+    w = PortWorld(sc, up_iact=4)
+    conts = [w.run(1) for _ in range(37)]
+    assert all(conts[:-1]) and not conts[-1]
+
+
+def test_generators_are_deterministic():
+    a, b = scenes.lsd_box(n_side=6), scenes.lsd_box(n_side=6)
+    assert a.to_ido() == b.to_ido()
+    d1 = scenes.hertz_drum(n=20000, seed=3)
+    d2 = scenes.hertz_drum(n=20000, seed=3)
+    assert np.array_equal(d1.position, d2.position) and np.array_equal(d1.model_index, d2.model_index)
+
+
+def test_drum_has_no_initial_overlap():
+    sc = scenes.hertz_drum(n=30000, seed=1)
+    p = sc.position[: 30000]
+    r = np.array([m.attrs[0] for m in sc.models])[sc.model_index[:30000]]
+    from scipy.spatial import cKDTree
+    pairs = cKDTree(p).query_pairs(2 * r.max(), output_type="ndarray")
+    d = np.linalg.norm(p[pairs[:, 0]] - p[pairs[:, 1]], axis=1)
+    assert np.all(d > r[pairs[:, 0]] + r[pairs[:, 1]])
+
+
+def test_lsd_box_matches_stated_config():
+    sc = scenes.lsd_box()
+    n = 8000
+    assert sc.num_objects == n + 5
+    assert sc.models[0].attrs[0] == 1e-3 and sc.models[0].density == 2500.0
+    assert abs(sc.velocity[:n].std() - 0.05) < 0.002
+    assert sc.iact_models[0].get("NormalStiffness") == 1e4 and sc.iact_models[0].get("ShearStiffness") == 8e3
+    assert sc.iact_models[0].get("FrictionCoefficient") == 0.5
+    assert sc.sp.time_interval == 1e-6
+
+
+def test_abi_library_exports_every_declared_symbol(engine_lib):
+    """libvedogpu.so loads without a GPU and exports every function include/vedo_gpu.h declares."""
+    hdr = open(os.path.join(ROOT, "include", "vedo_gpu.h")).read()
+    names = sorted(set(re.findall(r"\b(vedo_gpu_\w+)\s*\(", hdr)))
+    assert len(names) >= 15
+    lib = ctypes.CDLL(engine_lib.LIB_PATH)
+    missing = [n for n in names if not hasattr(lib, n)]
+    assert not missing, missing
+    lib.vedo_gpu_version.restype = ctypes.c_char_p
+    assert b"sm_103a" in lib.vedo_gpu_version()
+
+
+def test_abi_rejects_null_arguments(engine_lib):
+    """Status codes instead of exit(): NULL handles and paths are INVALID_ARGUMENT (no GPU touched)."""
+    lib = engine_lib.lib()
+    assert lib.vedo_gpu_run(None, 1, None) == 1
+    assert lib.vedo_gpu_create_from_ido(None, None, ctypes.byref(ctypes.c_void_p())) == 1
+    assert lib.vedo_gpu_get_observables(None, None) == 1
+
+
+def test_abi_bad_ido_is_reported(engine_lib, tmp_path):
+    """A truncated .ido is BAD_IDO before any device work."""
+    p = tmp_path / "bad.ido"
+    p.write_bytes(scenes.cluster(n=8).to_ido()[:100])
+    lib = engine_lib.lib()
+    h = ctypes.c_void_p()
+    rc = lib.vedo_gpu_create_from_ido(str(p).encode(), None, ctypes.byref(h))
+    assert rc == 7
+    assert b"truncated" in lib.vedo_gpu_last_error(None)

@@ -108,7 +108,7 @@ int vedo_gpu_write_ido(vedo_gpu_engine* e, const char* path) {
     return e->eng.write_ido(path);
 }
 
-uint64_t vedo_gpu_last_run_profile(const vedo_gpu_engine* e, double out[3]) {
+uint64_t vedo_gpu_last_run_profile(const vedo_gpu_engine* e, double out[4]) {
     if (!e || !out) return 0;
     return e->eng.last_profile(out);
 }

@@ -677,7 +677,7 @@ Engine::~Engine() {
     void* ptrs[] = {d_models_, d_params_, d_geom_, d_group_iact_, d_model_of_, d_err_, d_pos_, d_vel_, d_av_, d_ox_,
                     d_oz_, d_imp_, d_aimp_, d_global_, d_safe_, d_red_, d_key_, d_key_alt_, d_cell_key_, d_sid_,
                     d_sid_alt_, d_cell_start_, d_cellof_, d_flag_, d_task_, d_total_, d_ck_, d_cv_, d_ck_alt_,
-                    d_cv_alt_, d_cnt_, d_rec_key_, d_rec_hist_, d_rec_v0_, d_rec_flags_, d_obs_};
+                    d_cv_alt_, d_cnt_, d_rec_key_, d_rec_hist_, d_rec_v0_, d_rec_flags_, d_obs_, d_stage_};
     for (void* p : ptrs) if (p) cudaFree(p);
     for (auto& e : ev_) if (e) cudaEventDestroy(e);
     if (stream_) cudaStreamDestroy(stream_);
@@ -972,59 +972,85 @@ int Engine::step_once(bool write_impulses) {
 }
 
 int Engine::run(uint32_t nsteps, int* keep_running) {
-    prof_ms_[0] = prof_ms_[1] = prof_ms_[2] = 0;
+    prof_ms_[0] = prof_ms_[1] = prof_ms_[2] = prof_ms_[3] = 0;
     launches_ = 0;
     CK(cudaSetDevice(device_));
+    CK(cudaEventRecord(ev_[5], stream_));
     for (uint32_t s = 0; s < nsteps; ++s) {
         int rc = step_once(s + 1 == nsteps);
         if (rc != VEDO_OK) return rc;
     }
+    CK(cudaEventRecord(ev_[6], stream_));
     CK(cudaStreamSynchronize(stream_));
     CK(cudaGetLastError());
+    float tot = 0;
+    cudaEventElapsedTime(&tot, ev_[5], ev_[6]);
+    prof_ms_[3] = tot;
     if (keep_running) *keep_running = t_ < t_stop_ ? 1 : 0;   // SimMediator.cpp:839-841
     return VEDO_OK;
 }
 
-uint64_t Engine::last_profile(double out[3]) const {
-    for (int k = 0; k < 3; ++k) out[k] = prof_ms_[k];
+uint64_t Engine::last_profile(double out[4]) const {
+    for (int k = 0; k < 4; ++k) out[k] = prof_ms_[k];
     return launches_;
 }
 
 // ------------------------------------------------------------------------------------
-static void download3(double* dst, const double4_32a* src_dev, uint32_t n, std::vector<double4_32a>& tmp, cudaStream_t s) {
-    tmp.resize(n);
-    cudaMemcpyAsync(tmp.data(), src_dev, sizeof(double4_32a) * n, cudaMemcpyDeviceToHost, s);
-    cudaStreamSynchronize(s);
-    for (uint32_t i = 0; i < n; ++i) {
-        dst[3 * i] = tmp[i].x;
-        dst[3 * i + 1] = tmp[i].y;
-        dst[3 * i + 2] = tmp[i].z;
+// state I/O: host [n][3] arrays <-> device double4 (x, y, z, pad); the repacking runs on the
+// device, the host side is one contiguous copy per array.
+namespace {
+__global__ void k_pack3(uint32_t n, const double* __restrict__ src, double4_32a* __restrict__ dst) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) dst[i] = make_double4_32a(src[3 * (size_t)i], src[3 * (size_t)i + 1], src[3 * (size_t)i + 2], 0.0);
+}
+__global__ void k_unpack3(uint32_t n, const double4_32a* __restrict__ src, double* __restrict__ dst) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) {
+        const double4_32a v = src[i];
+        dst[3 * (size_t)i] = v.x;
+        dst[3 * (size_t)i + 1] = v.y;
+        dst[3 * (size_t)i + 2] = v.z;
     }
+}
+}  // namespace
+
+int Engine::ensure_stage() {
+    if (d_stage_) return VEDO_OK;
+    CK(dalloc(&d_stage_, 7 * 3 * (size_t)n_));
+    return VEDO_OK;
 }
 
 int Engine::get_state(const vedo_state_view& v) {
-    std::vector<double4_32a> tmp;
+    int rc = ensure_stage();
+    if (rc != VEDO_OK) return rc;
     double* dst[] = {v.position, v.velocity, v.angular_velocity, v.orientation_x, v.orientation_z, v.impact,
                      v.angular_impact};
     const double4_32a* src[] = {d_pos_, d_vel_, d_av_, d_ox_, d_oz_, d_imp_, d_aimp_};
-    for (int k = 0; k < 7; ++k)
-        if (dst[k]) download3(dst[k], src[k], n_, tmp, stream_);
+    for (int k = 0; k < 7; ++k) {
+        if (!dst[k]) continue;
+        double* st = d_stage_ + (size_t)k * 3 * n_;
+        k_unpack3<<<blocks_for(n_), TPB, 0, stream_>>>(n_, src[k], st);
+        CK(cudaMemcpyAsync(dst[k], st, 24 * (size_t)n_, cudaMemcpyDeviceToHost, stream_));
+    }
+    CK(cudaStreamSynchronize(stream_));
     CK(cudaGetLastError());
     return VEDO_OK;
 }
 
 int Engine::set_state(const vedo_state_view& v) {
-    std::vector<double4_32a> tmp(n_);
+    int rc = ensure_stage();
+    if (rc != VEDO_OK) return rc;
     const double* srcs[] = {v.position, v.velocity, v.angular_velocity, v.orientation_x, v.orientation_z, v.impact,
                             v.angular_impact};
     double4_32a* dst[] = {d_pos_, d_vel_, d_av_, d_ox_, d_oz_, d_imp_, d_aimp_};
     for (int k = 0; k < 7; ++k) {
         if (!srcs[k]) continue;
-        for (uint32_t i = 0; i < n_; ++i)
-            tmp[i] = make_double4_32a(srcs[k][3 * i], srcs[k][3 * i + 1], srcs[k][3 * i + 2], 0.0);
-        CK(cudaMemcpyAsync(dst[k], tmp.data(), sizeof(double4_32a) * n_, cudaMemcpyHostToDevice, stream_));
-        CK(cudaStreamSynchronize(stream_));
+        double* st = d_stage_ + (size_t)k * 3 * n_;
+        CK(cudaMemcpyAsync(st, srcs[k], 24 * (size_t)n_, cudaMemcpyHostToDevice, stream_));
+        k_pack3<<<blocks_for(n_), TPB, 0, stream_>>>(n_, st, dst[k]);
     }
+    CK(cudaStreamSynchronize(stream_));
+    CK(cudaGetLastError());
     return VEDO_OK;
 }
 

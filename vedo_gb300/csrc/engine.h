@@ -54,7 +54,7 @@ public:
     double time() const { return t_; }
     uint64_t steps() const { return round_; }
     uint32_t num_objects() const { return n_; }
-    uint64_t last_profile(double out[3]) const;
+    uint64_t last_profile(double out[4]) const;
     void set_profiling(bool on) { profiling_ = on; }
     const std::string& error() const { return err_; }
 
@@ -67,6 +67,7 @@ private:
     int step_once(bool write_impulses);
     int record_ido();
     int sync_host_state();
+    int ensure_stage();
 
     // scene and options
     HScene host_;
@@ -114,12 +115,13 @@ private:
     double4_32a* d_rec_hist_ = nullptr;
     double* d_rec_v0_ = nullptr;
     uint8_t* d_rec_flags_ = nullptr;
-    // observables scratch
+    // observables scratch and state I/O staging ([7][n][3] doubles)
     double* d_obs_ = nullptr;
+    double* d_stage_ = nullptr;
     // profiling of the last run()
     cudaEvent_t ev_[8] = {};
     bool profiling_ = false;       // per-phase CUDA-event timing (adds a host sync per step)
-    double prof_ms_[3] = {0, 0, 0};
+    double prof_ms_[4] = {0, 0, 0, 0};
     uint64_t launches_ = 0;
 };
 

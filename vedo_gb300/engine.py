@@ -160,9 +160,10 @@ class GpuEngine:
         lib().vedo_gpu_set_profiling(self.h, 1 if on else 0)
 
     def last_run_profile(self):
-        o = np.zeros(3)
+        o = np.zeros(4)
         launches = lib().vedo_gpu_last_run_profile(self.h, dptr(o))
-        return {"pair_ms": o[0], "object_ms": o[1], "rebuild_ms": o[2], "launches": int(launches)}
+        return {"pair_ms": float(o[0]), "object_ms": float(o[1]), "rebuild_ms": float(o[2]),
+                "total_ms": float(o[3]), "launches": int(launches)}
 
     def close(self):
         if getattr(self, "h", None):

@@ -228,46 +228,56 @@ def hertz_drum(n: int = 1_000_000, seed: int = 2024, steps: int = 10000, dt: flo
                median_r: float = 1e-3, sigma_log: float = 0.2, r_lo: float = 0.5e-3, r_hi: float = 2e-3,
                E: float = 70e9, nu: float = 0.25, restitution: float = 0.7, mu: float = 0.4,
                density: float = 2500.0, R: float = 0.15, L: float = 0.3, rpm: float = 30.0,
-               fill: float = 0.35, facets: int = 64, solver: str = "ISwH") -> Scene:
-    """Polydisperse Hertz drum.  Radii lognormal(median, sigma_log) clipped to [r_lo, r_hi],
-    binned into K log-spaced classes (one DOModel and one group per class; K(K+1)/2 + K
-    interaction models).  The shell is `facets` fixed plates on a circle of radius R; the two
-    end plates are orbital plates spinning at `rpm` about the drum axis (x).  The bottom
-    `fill` fraction of the drum volume is filled by seeded placement on a jittered cubic
-    lattice (one site per sphere of the largest class, shuffled), which stands in for random
-    sequential placement at this size."""
+               facets: int = 64, gap: float = 0.01, solver: str = "ISwH") -> Scene:
+    """Polydisperse Hertz drum.
+
+    Radii are lognormal(median_r, sigma_log) clipped to [r_lo, r_hi] and binned into K
+    log-spaced classes; each class is one DOModel and one group, with K(K+1)/2 sphere-sphere
+    and K sphere-wall interaction models (Hertz stiffness from E, nu and the class radii).
+    The shell is `facets` fixed quasi-plates on a circle of radius R around the x axis; the
+    two end plates are orbital plates spinning at `rpm` about x.  The spheres fill the drum
+    from the bottom in horizontal lattice layers, largest first, each layer's spacing set by
+    its largest sphere plus a `gap` fraction, which leaves no initial overlap and packs the
+    1,000,000 default spheres into about 40 % of the drum volume."""
     rng = np.random.default_rng(seed)
     edges = np.exp(np.linspace(math.log(r_lo), math.log(r_hi), K + 1))
     centres = np.sqrt(edges[:-1] * edges[1:])
     r = np.clip(median_r * np.exp(sigma_log * rng.standard_normal(n)), r_lo, r_hi)
     cls = np.clip(np.searchsorted(edges, r, side="right") - 1, 0, K - 1).astype(np.uint32)
+    cls = np.sort(cls)[::-1].copy()            # largest classes first (bottom layers)
     radii = centres[cls]
-    # lattice sites inside the lower part of the drum cross-section (axis along x)
-    rmax = float(radii.max())
-    a = 2.0 * rmax * 1.02
-    h_fill = R * (2.0 * fill - 1.0) * 1.35   # fill level (z) giving roughly `fill` of the cross-section
-    xs = np.arange(-0.5 * L + a, 0.5 * L - a, a)
-    ys = np.arange(-R + a, R - a, a)
-    zs = np.arange(-R + a, R - a, a)
-    X, Y, Z = np.meshgrid(xs, ys, zs, indexing="ij")
-    sites = np.stack([X.ravel(), Y.ravel(), Z.ravel()], 1)
-    ok = (sites[:, 1] ** 2 + sites[:, 2] ** 2) < (R - a) ** 2
-    sites = sites[ok]
-    order = np.argsort(sites[:, 2], kind="stable")
-    sites = sites[order]
-    if sites.shape[0] < n:
-        raise ValueError(f"drum holds {sites.shape[0]} lattice sites < {n} spheres; enlarge the drum")
-    sites = sites[:n]
-    sites += rng.uniform(-0.005 * a, 0.005 * a, size=sites.shape)
-    pos = sites
+    pos = np.zeros((n, 3))
+    z = -R
+    placed = 0
+    while placed < n:
+        rl = radii[placed]                       # largest radius of this layer (sorted descending)
+        a = 2.0 * rl * (1.0 + gap)
+        zc = z + a * 0.5 + 0.5 * gap * rl
+        half = math.sqrt(max(0.0, (R - 0.5 * a) ** 2 - zc * zc)) if abs(zc) < R - 0.5 * a else 0.0
+        if half < a:
+            if zc > 0.0:
+                raise ValueError(f"drum full after {placed} of {n} spheres")
+            z += a
+            continue
+        ys = np.arange(-half + 0.5 * a, half - 0.5 * a + 1e-12, a)
+        xs = np.arange(-0.5 * L + 0.5 * a, 0.5 * L - 0.5 * a + 1e-12, a)
+        X, Y = np.meshgrid(xs, ys, indexing="ij")
+        sites = np.stack([X.ravel(), Y.ravel(), np.full(X.size, zc)], 1)
+        take = min(n - placed, sites.shape[0])
+        pos[placed:placed + take] = sites[:take]
+        placed += take
+        z += a
+    pos += rng.uniform(-0.25 * gap, 0.25 * gap, size=pos.shape) * radii[:, None]
+    perm = rng.permutation(n)                  # object order independent of the layer order
+    pos, cls = pos[perm], cls[perm]
     vel = np.zeros_like(pos)
     models: List[DOModel] = []
     for k in range(K):
         models.append(DOModel(f"B{k:03d}", f"B{k:03d}", MOBILE, LOCAL, density, 1.0, SPHERE, (float(centres[k]),)))
     thick = 4e-3
-    fw = 2.0 * R * math.sin(math.pi / facets) * 1.05
+    fw = 2.0 * R * math.tan(math.pi / facets) * 1.02
     shell = DOModel("Shell", "Wall", FIXED, GLOBAL, 0.0, 1.0, QUASI_PLATE, (L + 2 * thick, thick, fw))
-    endp = DOModel("End", "Wall", ORBITAL, GLOBAL, 0.0, 1.0, QUASI_PLATE, (2.2 * R, thick, 2.2 * R))
+    endp = DOModel("EndPl", "Wall", ORBITAL, GLOBAL, 0.0, 1.0, QUASI_PLATE, (2.2 * R, thick, 2.2 * R))
     models += [shell, endp]
     wp, wox, woz, wav, widx = [], [], [], [], []
     for f in range(facets):
