@@ -30,6 +30,8 @@ struct ModelDev {
     double a0, a1, a2;    // shape attributes: sphere r | cylinder r, h | plate w, h, l
     double ix, iy, iz;    // mass moment of inertia
     double ext[3];        // external force
+    double inv_sudo;      // 1.0 / sudo, as DOSphere::Response evaluates it (DOSphere.cpp:30)
+    double rot_coef;      // 2.5 / sudo / r / r (DOSphere.cpp:39), spheres only
 };
 
 // Interaction constants of one (slave model, master model) pair, as the ImpactSolver

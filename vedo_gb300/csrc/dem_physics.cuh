@@ -195,9 +195,8 @@ __device__ __forceinline__ void respond_object(const ModelDev& m, double dt, d3 
                                                d3& Oz) {
     if (m.behavior == BEH_FIXED) return;                      // DOFixedQuasiPlate.h:16-19
     if (m.shape == SHAPE_SPHERE) {                            // DOSphere.cpp:21-48
-        const double sm = m.sudo, R = m.a0;
-        d3 dv = smul(1.0 / sm, J);
-        d3 dav = smul(2.5 / sm / R / R, JA);
+        d3 dv = smul(m.inv_sudo, J);                          // 1.0 / dSudoMass * vImpact
+        d3 dav = smul(m.rot_coef, JA);                         // 2.5 / dSudoMass / Radius / Radius * ...
         d3 dp = smul(dt, add(V, smul(0.5, dv)));
         d3 dw = smul(dt, add(AV, smul(0.5, dav)));
         P = add(P, dp);
@@ -212,7 +211,7 @@ __device__ __forceinline__ void respond_object(const ModelDev& m, double dt, d3 
         Ox = rotate_around(Ox, dw);
         Oz = rotate_around(Oz, dw);
     } else if (m.behavior == BEH_CONSTRAINED) {               // DOConstrainedQuasiPlate.cpp:18-35
-        d3 dv = smul(1.0 / m.sudo, smul(dot(J, Oz), dir(Oz)));
+        d3 dv = smul(m.inv_sudo, smul(dot(J, Oz), dir(Oz)));
         d3 dp = smul(dt, add(V, smul(0.5, dv)));
         d3 dw = muls(AV, dt);
         P = add(P, dp);
@@ -220,7 +219,7 @@ __device__ __forceinline__ void respond_object(const ModelDev& m, double dt, d3 
         Oz = rotate_around(Oz, dw);
         V = add(V, dv);
     } else {                                                  // DOQuasiPlate.cpp:20-41, DOQuasiCylinder.cpp
-        d3 dv = smul(1.0 / m.sudo, J);
+        d3 dv = smul(m.inv_sudo, J);
         d3 dav = mk(dot(JA, Ox) / m.ix, dot(JA, cross(Oz, Ox)) / m.iy, dot(JA, Oz) / m.iz);
         d3 dp = smul(dt, add(V, smul(0.5, dv)));
         d3 dw = smul(dt, add(AV, smul(0.5, dav)));

@@ -24,6 +24,7 @@
 #include <cstring>
 
 #include "dem_physics.cuh"
+#include "prefilter.cuh"
 
 namespace vedo {
 
@@ -58,9 +59,11 @@ __host__ __device__ inline double dbl_of(unsigned long long o) {
 // time step
 __global__ void __launch_bounds__(TPB) k_pair(uint32_t np, const uint2* __restrict__ sm,
                                               const uint32_t* __restrict__ param, const PairParam* __restrict__ params,
-                                              const double4_32a* __restrict__ geom, const double4_32a* __restrict__ pos,
+                                              const double4_32a* __restrict__ geom, const float* __restrict__ reach,
+                                              const double4_32a* __restrict__ pos,
                                               const double4_32a* __restrict__ vel, const double4_32a* __restrict__ av,
                                               const double4_32a* __restrict__ ox, const double4_32a* __restrict__ oz,
+                                              const float4* __restrict__ pos32, const float4* __restrict__ wall32,
                                               double4_32a* __restrict__ hist, double* __restrict__ v0,
                                               uint8_t* __restrict__ flags, double* __restrict__ out, double dt,
                                               int backup) {
@@ -69,6 +72,17 @@ __global__ void __launch_bounds__(TPB) k_pair(uint32_t np, const uint2* __restri
     const uint2 p = sm[k];
     const uint32_t pi = param[k];
     const int cd = params[pi].cd, is = params[pi].is;
+    // Pairs that are certainly apart and carry no normal bond: ImpactStatus::Clean, no impulse.
+    const bool bondable = (is == IS_BSDBF || is == IS_BTSDBF || is == IS_BSDB2F) && params[pi].c[4] != 0.0;
+    if (!bondable && certainly_apart(cd, pos32[p.x], pos32[p.y], wall32[p.y], reach[pi])) {
+        const uint8_t f0 = flags[k];
+        if (f0 & PF_NONZERO) {
+            hist[k] = make_double4_32a(0.0, 0.0, 0.0, 0.0);
+            v0[k] = 0.0;
+        }
+        if (f0 != 0) flags[k] = 0;
+        return;
+    }
     const double4_32a gg = geom[pi];
     const PairGeom g{gg.x, gg.y, gg.z, gg.w};
     const d3 Ps = ld(pos, p.x), Pm = ld(pos, p.y);
@@ -134,11 +148,27 @@ __device__ __forceinline__ void add_entry(uint32_t ent, uint8_t f, const double*
     }
 }
 
+// FP32 copies used by the prefilters: position relative to `origin`, and for plates and
+// cylinders the unit axis with a validity flag (plates need an orthogonal Ox/Oz frame for
+// the plane bound).
+__device__ __forceinline__ void write32(uint32_t i, int shape, d3 P, d3 Ox, d3 Oz, d3 origin,
+                                        float4* __restrict__ pos32, float4* __restrict__ wall32) {
+    pos32[i] = make_float4((float)(P.x - origin.x), (float)(P.y - origin.y), (float)(P.z - origin.z), 0.0f);
+    if (shape != SHAPE_SPHERE) {
+        const double lz = len(Oz), lx = len(Ox);
+        bool ok = lz > 0.0;
+        if (shape == SHAPE_PLATE) ok = ok && lx > 0.0 && fabs(dot(Ox, Oz)) <= 1e-9 * lx * lz;
+        wall32[i] = ok ? make_float4((float)(Oz.x / lz), (float)(Oz.y / lz), (float)(Oz.z / lz), 1.0f)
+                       : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+    }
+}
+
 __device__ __forceinline__ void finish_object(uint32_t i, const ModelDev& m, d3 J, d3 JA, double dt, d3 fimp,
                                               double4_32a* __restrict__ pos, double4_32a* __restrict__ vel,
                                               double4_32a* __restrict__ av, double4_32a* __restrict__ ox,
                                               double4_32a* __restrict__ oz, double4_32a* __restrict__ imp,
-                                              double4_32a* __restrict__ aimp, int write_imp) {
+                                              double4_32a* __restrict__ aimp, int write_imp, d3 origin,
+                                              float4* __restrict__ pos32, float4* __restrict__ wall32) {
     J = add(J, muls(fimp, m.sudo));                           // DOContainer::AddFieldImpact (DOContainer.cpp:25)
     J = add(J, smul(dt, mk(m.ext[0], m.ext[1], m.ext[2])));   // DiscreteObject::AddConstrainedImpact (:160-163)
     if (m.behavior != BEH_FIXED) {
@@ -151,6 +181,7 @@ __device__ __forceinline__ void finish_object(uint32_t i, const ModelDev& m, d3 
             st(vel, i, V, 0.0);
             st(av, i, AV, 0.0);
         }
+        write32(i, m.shape, P, Ox, Oz, origin, pos32, wall32);
     }
     if (write_imp) {                                          // DiscreteObject::ClearImpact (:141-147)
         st(imp, i, J, 0.0);
@@ -165,7 +196,8 @@ __global__ void __launch_bounds__(TPB) k_obj(uint32_t n, const uint32_t* __restr
                                              double4_32a* __restrict__ imp, double4_32a* __restrict__ aimp,
                                              const uint32_t* __restrict__ csr_ptr, const uint32_t* __restrict__ csr_ent,
                                              const uint8_t* __restrict__ flags, const double* __restrict__ out,
-                                             double dt, d3 fimp, int write_imp) {
+                                             double dt, d3 fimp, int write_imp, d3 origin, float4* __restrict__ pos32,
+                                             float4* __restrict__ wall32) {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     const ModelDev& m = models[model_of[i]];
@@ -176,7 +208,7 @@ __global__ void __launch_bounds__(TPB) k_obj(uint32_t n, const uint32_t* __restr
         const uint32_t ent = csr_ent[e];
         add_entry(ent, flags[ent >> 1], out, J, JA);
     }
-    finish_object(i, m, J, JA, dt, fimp, pos, vel, av, ox, oz, imp, aimp, write_imp);
+    finish_object(i, m, J, JA, dt, fimp, pos, vel, av, ox, oz, imp, aimp, write_imp, origin, pos32, wall32);
 }
 
 // One warp per scope-global object: lanes load 32 entries at a time, then every lane adds
@@ -187,7 +219,7 @@ __global__ void k_obj_global(uint32_t nglob, const uint32_t* __restrict__ glob, 
                              double4_32a* __restrict__ oz, double4_32a* __restrict__ imp, double4_32a* __restrict__ aimp,
                              const uint32_t* __restrict__ csr_ptr, const uint32_t* __restrict__ csr_ent,
                              const uint8_t* __restrict__ flags, const double* __restrict__ out, double dt, d3 fimp,
-                             int write_imp) {
+                             int write_imp, d3 origin, float4* __restrict__ pos32, float4* __restrict__ wall32) {
     const uint32_t w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const int lane = threadIdx.x & 31;
     if (w >= nglob) return;
@@ -228,7 +260,8 @@ __global__ void k_obj_global(uint32_t nglob, const uint32_t* __restrict__ glob, 
             }
         }
     }
-    if (lane == 0) finish_object(i, m, J, JA, dt, fimp, pos, vel, av, ox, oz, imp, aimp, write_imp);
+    if (lane == 0)
+        finish_object(i, m, J, JA, dt, fimp, pos, vel, av, ox, oz, imp, aimp, write_imp, origin, pos32, wall32);
 }
 
 // Narrow phase only: PF_ACTIVE of every pair at the current positions (the IsActive()
@@ -237,18 +270,23 @@ __global__ void __launch_bounds__(TPB) k_detect_active(uint32_t np, const uint2*
                                                        const uint32_t* __restrict__ param,
                                                        const PairParam* __restrict__ params,
                                                        const double4_32a* __restrict__ geom,
+                                                       const float* __restrict__ reach,
                                                        const double4_32a* __restrict__ pos, const double4_32a* __restrict__ ox,
-                                                       const double4_32a* __restrict__ oz, uint8_t* __restrict__ flags) {
+                                                       const double4_32a* __restrict__ oz,
+                                                       const float4* __restrict__ pos32,
+                                                       const float4* __restrict__ wall32, uint8_t* __restrict__ flags) {
     const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
     if (k >= np) return;
     const uint2 p = sm[k];
     const uint32_t pi = param[k];
-    const double4_32a gg = geom[pi];
-    const PairGeom g{gg.x, gg.y, gg.z, gg.w};
-    double depth;
-    d3 n, point;
-    detect_pair(params[pi].cd, g, ld(pos, p.x), ld(pos, p.y), ox, oz, p.y, depth, n, point);
     const uint8_t f = flags[k];
+    double depth = -1.0;
+    if (!certainly_apart(params[pi].cd, pos32[p.x], pos32[p.y], wall32[p.y], reach[pi])) {
+        const double4_32a gg = geom[pi];
+        const PairGeom g{gg.x, gg.y, gg.z, gg.w};
+        d3 n, point;
+        detect_pair(params[pi].cd, g, ld(pos, p.x), ld(pos, p.y), ox, oz, p.y, depth, n, point);
+    }
     const uint8_t nf = depth > 0.0 ? (uint8_t)(f | PF_ACTIVE) : (uint8_t)(f & ~PF_ACTIVE);
     if (nf != f) flags[k] = nf;
 }
@@ -336,23 +374,64 @@ __global__ void __launch_bounds__(TPB) k_cell_fill(uint32_t nloc, const uint64_t
     if (p == nloc - 1) cell_start[*ncells] = nloc;
 }
 
+// Candidate test of BuildIactTab (NBSConsultant.cpp:318-345): DOMap::CalDistance <= safe_i +
+// safe_j, decided from FP32 bounds where they are conclusive and in exact FP64 otherwise.
+__device__ __forceinline__ bool candidate(const ModelDev& mi, const ModelDev& mj, uint32_t i, uint32_t j, double si,
+                                          double sj, float si32, float sj32, const double4_32a* __restrict__ pos,
+                                          const double4_32a* __restrict__ ox, const double4_32a* __restrict__ oz,
+                                          const float4* __restrict__ pos32, const float4* __restrict__ wall32,
+                                          int* __restrict__ err) {
+    const float thr = si32 + sj32;                     // float sums of the rounded-to-float safe lengths
+    const float tlo = thr * (1.0f - 4.0f * PF_ARITH_EPS), thi = thr * (1.0f + 4.0f * PF_ARITH_EPS);
+    if (mi.shape == SHAPE_SPHERE && mj.shape == SHAPE_SPHERE) {
+        float e;
+        const float d = dist32(pos32[i], pos32[j], e);
+        if (d - e > thi) return false;
+        if (d + e < tlo) return true;
+    } else {
+        const bool ip = mi.shape != SHAPE_SPHERE;      // the non-sphere member
+        const uint32_t w = ip ? i : j, sp = ip ? j : i;
+        const int wshape = ip ? mi.shape : mj.shape;
+        const float4 wl = wall32[w];
+        if (wl.w != 0.0f && (wshape == SHAPE_PLATE || wshape == SHAPE_CYL) &&
+            (ip ? mj.shape : mi.shape) == SHAPE_SPHERE) {
+            float e;
+            const float d = wshape == SHAPE_PLATE ? plane_dist32(pos32[sp], pos32[w], wl, e)
+                                                  : line_dist32(pos32[sp], pos32[w], wl, e);
+            if (d - e > thi) return false;
+        }
+    }
+    bool ok;
+    const double d = cal_distance(mi, mj, i, j, pos, ox, oz, ok);
+    if (!ok) {
+        atomicOr(err, ERR_BAD_SHAPE_PAIR);
+        return false;
+    }
+    return !(d > (si + sj));
+}
+
+// One thread per (slot, object) task, slot-major so that a warp works on one slot.  Tasks
+// are numbered in the reference's traversal order: cell by cell (ix, iy, iz lexicographic),
+// within a cell by slot, within a slot by the object's position in the cell (ascending id).
 template <bool FILL>
 __global__ void __launch_bounds__(TPB) k_pairs(uint32_t nloc, const uint32_t* __restrict__ sid,
                                                const uint64_t* __restrict__ cell_key,
                                                const uint32_t* __restrict__ cell_start,
                                                const uint32_t* __restrict__ ncells_p, const uint32_t* __restrict__ cellof,
+                                               const uint32_t* __restrict__ grid, uint64_t grid_cells,
                                                const uint32_t* __restrict__ glob, uint32_t nglob,
                                                const uint32_t* __restrict__ model_of, const ModelDev* __restrict__ models,
                                                const int* __restrict__ group_iact, int G,
                                                const double4_32a* __restrict__ pos, const double4_32a* __restrict__ ox,
-                                               const double4_32a* __restrict__ oz, const double* __restrict__ safe,
+                                               const double4_32a* __restrict__ oz, const float4* __restrict__ pos32,
+                                               const float4* __restrict__ wall32, const double* __restrict__ safe,
                                                uint32_t ncx, uint32_t ncy, uint32_t ncz, uint64_t ny1, uint64_t nz1,
                                                uint32_t* __restrict__ task, uint32_t* __restrict__ first,
                                                uint32_t* __restrict__ second, int* __restrict__ err) {
     const uint64_t t = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= (uint64_t)nloc * NSLOT) return;
-    const uint32_t P = (uint32_t)(t / NSLOT);
-    const int s = (int)(t % NSLOT);
+    const int s = (int)(t / nloc);
+    const uint32_t P = (uint32_t)(t % nloc);
     const uint32_t c = cellof[P];
     const uint64_t key = cell_key[c];
     const uint32_t cz = (uint32_t)(key % nz1);
@@ -377,34 +456,37 @@ __global__ void __launch_bounds__(TPB) k_pairs(uint32_t nloc, const uint32_t* __
         const int dx = c_slot[s][0], dy = c_slot[s][1], dz = c_slot[s][2];
         if (!((cx == 0 && dx < 0) || (cy == 0 && dy < 0) || (cz == 0 && dz < 0))) {
             const uint64_t nk = ((uint64_t)(cx + dx) * ny1 + (uint64_t)(cy + dy)) * nz1 + (uint64_t)(cz + dz);
-            uint32_t lo = 0, hi = *ncells_p;
-            while (lo < hi) {
-                const uint32_t mid = (lo + hi) >> 1;
-                if (cell_key[mid] < nk) lo = mid + 1; else hi = mid;
+            uint32_t c2 = 0xffffffffu;
+            if (grid) {
+                if (nk < grid_cells) c2 = grid[nk];
+            } else {
+                const uint32_t nc = *ncells_p;
+                uint32_t lo = 0, hi = nc;
+                while (lo < hi) {
+                    const uint32_t mid = (lo + hi) >> 1;
+                    if (cell_key[mid] < nk) lo = mid + 1; else hi = mid;
+                }
+                if (lo < nc && cell_key[lo] == nk) c2 = lo;
             }
-            if (lo < *ncells_p && cell_key[lo] == nk) {
-                js = sid + cell_start[lo];
-                jn = cell_start[lo + 1] - cell_start[lo];
+            if (c2 != 0xffffffffu) {
+                js = sid + cell_start[c2];
+                jn = cell_start[c2 + 1] - cell_start[c2];
             }
         }
     }
     const uint32_t i = sid[P];
     const ModelDev& mi = models[model_of[i]];
     const double si = safe[i];
+    const float si32 = (float)si;
     const int gi = mi.group;
     uint32_t cnt = 0;
     const uint32_t off = FILL ? task[tid] : 0u;
-    for (uint32_t q = 0; q < jn; ++q) {                       // BuildIactTab(v1, v2), :318-345
+    for (uint32_t q = 0; q < jn; ++q) {
         const uint32_t j = js[q];
         const ModelDev& mj = models[model_of[j]];
         if (group_iact[gi * G + mj.group] < 0) continue;
-        bool ok;
-        const double d = cal_distance(mi, mj, i, j, pos, ox, oz, ok);
-        if (!ok) {
-            atomicOr(err, ERR_BAD_SHAPE_PAIR);
-            continue;
-        }
-        if (d > (si + safe[j])) continue;
+        const double sj = safe[j];
+        if (!candidate(mi, mj, i, j, si, sj, si32, (float)sj, pos, ox, oz, pos32, wall32, err)) continue;
         if (FILL) {
             first[off + cnt] = i < j ? i : j;
             second[off + cnt] = i < j ? j : i;
@@ -412,6 +494,23 @@ __global__ void __launch_bounds__(TPB) k_pairs(uint32_t nloc, const uint32_t* __
         ++cnt;
     }
     if (!FILL) task[tid] = cnt;
+}
+
+__global__ void __launch_bounds__(TPB) k_grid_fill(const uint32_t* __restrict__ ncells_p,
+                                                   const uint64_t* __restrict__ cell_key, uint32_t* __restrict__ grid) {
+    const uint32_t c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c < *ncells_p) grid[cell_key[c]] = c;
+}
+
+__global__ void __launch_bounds__(TPB) k_refresh32(uint32_t n, const uint32_t* __restrict__ model_of,
+                                                   const ModelDev* __restrict__ models,
+                                                   const double4_32a* __restrict__ pos,
+                                                   const double4_32a* __restrict__ ox,
+                                                   const double4_32a* __restrict__ oz, d3 origin,
+                                                   float4* __restrict__ pos32, float4* __restrict__ wall32) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    write32(i, models[model_of[i]].shape, ld(pos, i), ld(ox, i), ld(oz, i), origin, pos32, wall32);
 }
 
 // Assembler::CreateInteraction orientation and model selection (Assembler.cpp:15-87)
@@ -450,6 +549,11 @@ __global__ void __launch_bounds__(TPB) k_setup(uint32_t np, const uint32_t* __re
 // SimMediator.cpp:690-707); otherwise a default-constructed ImpactStatus.
 __global__ void __launch_bounds__(TPB) k_history_old(uint32_t np, const uint32_t* __restrict__ first,
                                                      const uint32_t* __restrict__ second,
+                                                     const uint2* __restrict__ sm, const uint32_t* __restrict__ param,
+                                                     const PairParam* __restrict__ params,
+                                                     const float* __restrict__ reach,
+                                                     const float4* __restrict__ pos32,
+                                                     const float4* __restrict__ wall32,
                                                      const uint32_t* __restrict__ o_ptr,
                                                      const uint32_t* __restrict__ o_ent,
                                                      const uint32_t* __restrict__ o_first,
@@ -464,8 +568,12 @@ __global__ void __launch_bounds__(TPB) k_history_old(uint32_t np, const uint32_t
     uint8_t f = ST_DEFAULT;
     double4_32a h = make_double4_32a(0.0, 0.0, 0.0, 0.0);
     double vv = 0.0;
-    const uint32_t e1 = o_ptr[a + 1];
-    for (uint32_t e = o_ptr[a]; e < e1; ++e) {
+    const uint2 p = sm[k];
+    const uint32_t pi = param[k];
+    // a pair certainly apart now was not active at this position in the old list either
+    const bool maybe = !certainly_apart(params[pi].cd, pos32[p.x], pos32[p.y], wall32[p.y], reach[pi]);
+    const uint32_t e1 = maybe ? o_ptr[a + 1] : 0u;
+    for (uint32_t e = maybe ? o_ptr[a] : 0u; e < e1; ++e) {
         const uint32_t ko = o_ent[e] >> 1;
         if (o_first[ko] == a && o_second[ko] == b) {
             const uint8_t of = o_flags[ko];
@@ -677,7 +785,8 @@ Engine::~Engine() {
     void* ptrs[] = {d_models_, d_params_, d_geom_, d_group_iact_, d_model_of_, d_err_, d_pos_, d_vel_, d_av_, d_ox_,
                     d_oz_, d_imp_, d_aimp_, d_global_, d_safe_, d_red_, d_key_, d_key_alt_, d_cell_key_, d_sid_,
                     d_sid_alt_, d_cell_start_, d_cellof_, d_flag_, d_task_, d_total_, d_ck_, d_cv_, d_ck_alt_,
-                    d_cv_alt_, d_cnt_, d_rec_key_, d_rec_hist_, d_rec_v0_, d_rec_flags_, d_obs_, d_stage_};
+                    d_cv_alt_, d_cnt_, d_rec_key_, d_rec_hist_, d_rec_v0_, d_rec_flags_, d_obs_, d_stage_,
+                    d_pos32_, d_wall32_, d_reach_, d_grid_};
     for (void* p : ptrs) if (p) cudaFree(p);
     for (auto& e : ev_) if (e) cudaEventDestroy(e);
     if (stream_) cudaStreamDestroy(stream_);
@@ -735,6 +844,34 @@ int Engine::init(const HScene& scene, const vedo_engine_opts& opts) {
     }
     for (uint32_t i = 0; i < n_; ++i)
         if (tab_.models[host_.model_of[i]].scope != SCOPE_LOCAL) global_ids_.push_back(i);
+    // FP32 prefilter copies: origin at the centre of the initial bounding box
+    {
+        double lo[3] = {DBL_MAX, DBL_MAX, DBL_MAX}, hi[3] = {-DBL_MAX, -DBL_MAX, -DBL_MAX};
+        for (uint32_t i = 0; i < n_; ++i)
+            for (int k = 0; k < 3; ++k) {
+                lo[k] = std::min(lo[k], host_.pos[3 * i + k]);
+                hi[k] = std::max(hi[k], host_.pos[3 * i + k]);
+            }
+        for (int k = 0; k < 3; ++k) origin_[k] = 0.5 * (lo[k] + hi[k]);
+        CK(dalloc(&d_pos32_, n_));
+        CK(dalloc(&d_wall32_, n_));
+        CK(cudaMemset(d_wall32_, 0, sizeof(float4) * n_));
+        std::vector<float> reach((size_t)nm_ * nm_, 0.0f);
+        for (size_t q = 0; q < reach.size(); ++q) {
+            const double* gq = &tab_.geom[4 * q];   // ra, b0, b1, b2
+            double r = 0.0;
+            if (tab_.params[q].cd == CD_SS) r = gq[0] + gq[1];
+            else if (tab_.params[q].cd == CD_SP) r = gq[0] + 0.5 * gq[2];
+            else if (tab_.params[q].cd == CD_SC) r = gq[0] + gq[1];
+            reach[q] = (float)r * (1.0f + 1e-6f);
+        }
+        CK(dalloc(&d_reach_, reach.size()));
+        CK(cudaMemcpy(d_reach_, reach.data(), sizeof(float) * reach.size(), cudaMemcpyHostToDevice));
+        k_refresh32<<<blocks_for(n_), TPB>>>(n_, d_model_of_, d_models_, d_pos_, d_ox_, d_oz_,
+                                             mk(origin_[0], origin_[1], origin_[2]), d_pos32_, d_wall32_);
+        CK(cudaGetLastError());
+        CK(cudaDeviceSynchronize());
+    }
     CK(dalloc(&d_global_, global_ids_.size()));
     if (!global_ids_.empty())
         CK(cudaMemcpy(d_global_, global_ids_.data(), sizeof(uint32_t) * global_ids_.size(), cudaMemcpyHostToDevice));
@@ -785,7 +922,8 @@ int Engine::rebuild(bool from_records) {
     // IsActive() of the current interactions at the current positions
     if (!from_records && cur_.np) {
         k_detect_active<<<blocks_for(cur_.np), TPB, 0, stream_>>>(cur_.np, cur_.sm, cur_.param, d_params_, d_geom_,
-                                                                  d_pos_, d_ox_, d_oz_, cur_.flags);
+                                                                  d_reach_, d_pos_, d_ox_, d_oz_, d_pos32_,
+                                                                  d_wall32_, cur_.flags);
         ++own;
     }
     std::swap(cur_, old_);
@@ -837,10 +975,25 @@ int Engine::rebuild(bool from_records) {
             CK(dalloc(&d_task_, task_cap_));
         }
         CK(cudaMemsetAsync(d_err_, 0, sizeof(int), stream_));
+        // dense cell map when the grid is small compared with the object count
+        uint32_t* grid = nullptr;
+        const uint64_t gcells = sentinel;
+        if (gcells <= std::max<uint64_t>(8ull * n_, 1ull << 22) && gcells < (1ull << 31)) {
+            if (gcells > grid_cap_) {
+                if (d_grid_) cudaFree(d_grid_);
+                d_grid_ = nullptr;
+                grid_cap_ = gcells + gcells / 4;
+                CK(dalloc(&d_grid_, grid_cap_));
+            }
+            CK(cudaMemsetAsync(d_grid_, 0xff, sizeof(uint32_t) * gcells, stream_));
+            k_grid_fill<<<blocks_for(nloc), TPB, 0, stream_>>>(d_total_, d_cell_key_, d_grid_);
+            ++own;
+            grid = d_grid_;
+        }
         k_pairs<false><<<blocks_for(ntask), TPB, 0, stream_>>>(
-            nloc, d_sid_, d_cell_key_, d_cell_start_, d_total_, d_cellof_, d_global_, (uint32_t)global_ids_.size(),
-            d_model_of_, d_models_, d_group_iact_, tab_.ngroups, d_pos_, d_ox_, d_oz_, d_safe_, ncx, ncy, ncz, ny1,
-            nz1, d_task_, nullptr, nullptr, d_err_);
+            nloc, d_sid_, d_cell_key_, d_cell_start_, d_total_, d_cellof_, grid, gcells, d_global_,
+            (uint32_t)global_ids_.size(), d_model_of_, d_models_, d_group_iact_, tab_.ngroups, d_pos_, d_ox_, d_oz_,
+            d_pos32_, d_wall32_, d_safe_, ncx, ncy, ncz, ny1, nz1, d_task_, nullptr, nullptr, d_err_);
         ++own;
         CK(exclusive_scan_u32(d_task_, d_task_, (uint32_t)ntask, d_total_ + 1, scratch_, stream_));
         CK(cudaMemcpyAsync(&np, d_total_ + 1, sizeof(uint32_t), cudaMemcpyDeviceToHost, stream_));
@@ -848,9 +1001,9 @@ int Engine::rebuild(bool from_records) {
         int rc = ensure_list(cur_, np);
         if (rc != VEDO_OK) return rc;
         k_pairs<true><<<blocks_for(ntask), TPB, 0, stream_>>>(
-            nloc, d_sid_, d_cell_key_, d_cell_start_, d_total_, d_cellof_, d_global_, (uint32_t)global_ids_.size(),
-            d_model_of_, d_models_, d_group_iact_, tab_.ngroups, d_pos_, d_ox_, d_oz_, d_safe_, ncx, ncy, ncz, ny1,
-            nz1, d_task_, cur_.first, cur_.second, d_err_);
+            nloc, d_sid_, d_cell_key_, d_cell_start_, d_total_, d_cellof_, grid, gcells, d_global_,
+            (uint32_t)global_ids_.size(), d_model_of_, d_models_, d_group_iact_, tab_.ngroups, d_pos_, d_ox_, d_oz_,
+            d_pos32_, d_wall32_, d_safe_, ncx, ncy, ncz, ny1, nz1, d_task_, cur_.first, cur_.second, d_err_);
         ++own;
     } else {
         int rc = ensure_list(cur_, 0);
@@ -868,7 +1021,8 @@ int Engine::rebuild(bool from_records) {
                                                                d_rec_hist_, d_rec_v0_, d_rec_flags_, cur_.hist,
                                                                cur_.v0, cur_.flags);
         } else {
-            k_history_old<<<blocks_for(np), TPB, 0, stream_>>>(np, cur_.first, cur_.second, old_.csr_ptr,
+            k_history_old<<<blocks_for(np), TPB, 0, stream_>>>(np, cur_.first, cur_.second, cur_.sm, cur_.param,
+                                                               d_params_, d_reach_, d_pos32_, d_wall32_, old_.csr_ptr,
                                                                old_.csr_ent, old_.first, old_.second, old_.flags,
                                                                old_.hist, old_.v0, cur_.hist, cur_.v0, cur_.flags);
         }
@@ -914,22 +1068,25 @@ int Engine::step_once(bool write_impulses) {
     // CalculateImpact
     if (prof) CK(cudaEventRecord(ev_[0], stream_));
     if (cur_.np) {
-        k_pair<<<blocks_for(cur_.np), TPB, 0, stream_>>>(cur_.np, cur_.sm, cur_.param, d_params_, d_geom_, d_pos_,
-                                                         d_vel_, d_av_, d_ox_, d_oz_, cur_.hist, cur_.v0, cur_.flags,
-                                                         cur_.out, dt, backup_pending_ ? 1 : 0);
+        k_pair<<<blocks_for(cur_.np), TPB, 0, stream_>>>(cur_.np, cur_.sm, cur_.param, d_params_, d_geom_, d_reach_,
+                                                         d_pos_, d_vel_, d_av_, d_ox_, d_oz_, d_pos32_, d_wall32_,
+                                                         cur_.hist, cur_.v0, cur_.flags, cur_.out, dt,
+                                                         backup_pending_ ? 1 : 0);
         ++launches_;
     }
     if (prof) CK(cudaEventRecord(ev_[1], stream_));
     // AddFieldImpact + AddConstrainedImpact + Response (+ CheckContactStatus in the next k_pair)
     const d3 fimp = muls(mk(g_[0], g_[1], g_[2]), dt);    // csp->GetFieldAcceleration() * dt (SimMediator.cpp:738)
+    const d3 org = mk(origin_[0], origin_[1], origin_[2]);
     k_obj<<<blocks_for(n_), TPB, 0, stream_>>>(n_, d_model_of_, d_models_, d_pos_, d_vel_, d_av_, d_ox_, d_oz_,
                                                d_imp_, d_aimp_, cur_.csr_ptr, cur_.csr_ent, cur_.flags, cur_.out, dt,
-                                               fimp, write_impulses ? 1 : 0);
+                                               fimp, write_impulses ? 1 : 0, org, d_pos32_, d_wall32_);
     ++launches_;
     if (!global_ids_.empty()) {
         k_obj_global<<<blocks_for((uint64_t)global_ids_.size() * 32), TPB, 0, stream_>>>(
             (uint32_t)global_ids_.size(), d_global_, d_model_of_, d_models_, d_pos_, d_vel_, d_av_, d_ox_, d_oz_,
-            d_imp_, d_aimp_, cur_.csr_ptr, cur_.csr_ent, cur_.flags, cur_.out, dt, fimp, write_impulses ? 1 : 0);
+            d_imp_, d_aimp_, cur_.csr_ptr, cur_.csr_ent, cur_.flags, cur_.out, dt, fimp, write_impulses ? 1 : 0, org,
+            d_pos32_, d_wall32_);
         ++launches_;
     }
     if (prof) CK(cudaEventRecord(ev_[2], stream_));
@@ -1049,6 +1206,8 @@ int Engine::set_state(const vedo_state_view& v) {
         CK(cudaMemcpyAsync(st, srcs[k], 24 * (size_t)n_, cudaMemcpyHostToDevice, stream_));
         k_pack3<<<blocks_for(n_), TPB, 0, stream_>>>(n_, st, dst[k]);
     }
+    k_refresh32<<<blocks_for(n_), TPB, 0, stream_>>>(n_, d_model_of_, d_models_, d_pos_, d_ox_, d_oz_,
+                                                     mk(origin_[0], origin_[1], origin_[2]), d_pos32_, d_wall32_);
     CK(cudaStreamSynchronize(stream_));
     CK(cudaGetLastError());
     return VEDO_OK;
@@ -1063,8 +1222,8 @@ int Engine::get_interactions(const vedo_contact_view& v) {
     const uint32_t np = cur_.np;
     if (!np) return VEDO_OK;
     // ContactInfo::bActive of the last narrow phase = detection at the current positions
-    k_detect_active<<<blocks_for(np), TPB, 0, stream_>>>(np, cur_.sm, cur_.param, d_params_, d_geom_, d_pos_, d_ox_,
-                                                         d_oz_, cur_.flags);
+    k_detect_active<<<blocks_for(np), TPB, 0, stream_>>>(np, cur_.sm, cur_.param, d_params_, d_geom_, d_reach_, d_pos_,
+                                                         d_ox_, d_oz_, d_pos32_, d_wall32_, cur_.flags);
     std::vector<uint2> sm(np);
     std::vector<uint8_t> fl(np);
     std::vector<double4_32a> h(np);
@@ -1099,7 +1258,8 @@ int Engine::get_observables(double out[13]) {
     k_obs_reduce<<<1, 32, 0, stream_>>>(nb, 16, part, res, 12);
     if (cur_.np)
         k_detect_active<<<blocks_for(cur_.np), TPB, 0, stream_>>>(cur_.np, cur_.sm, cur_.param, d_params_, d_geom_,
-                                                                  d_pos_, d_ox_, d_oz_, cur_.flags);
+                                                                  d_reach_, d_pos_, d_ox_, d_oz_, d_pos32_,
+                                                                  d_wall32_, cur_.flags);
     k_obs_b<<<nb, TPB, 0, stream_>>>(n_, d_model_of_, d_models_, d_pos_, d_vel_, d_av_, res, 0, cur_.flags, cur_.np,
                                      part);
     k_obs_reduce<<<1, 32, 0, stream_>>>(nb, 6, part, res + 16, 6);

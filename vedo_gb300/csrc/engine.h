@@ -115,6 +115,15 @@ private:
     double4_32a* d_rec_hist_ = nullptr;
     double* d_rec_v0_ = nullptr;
     uint8_t* d_rec_flags_ = nullptr;
+    // FP32 prefilter copies (prefilter.cuh): position offsets from origin_, unit wall axes,
+    // and per (slave model, master model) the contact reach rounded up to float
+    float4* d_pos32_ = nullptr;
+    float4* d_wall32_ = nullptr;
+    float* d_reach_ = nullptr;
+    double origin_[3] = {0, 0, 0};
+    // dense cell -> cell-index map of the broad phase when the grid is small enough
+    uint32_t* d_grid_ = nullptr;
+    uint64_t grid_cap_ = 0;
     // observables scratch and state I/O staging ([7][n][3] doubles)
     double* d_obs_ = nullptr;
     double* d_stage_ = nullptr;

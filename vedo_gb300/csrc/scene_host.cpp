@@ -100,6 +100,10 @@ bool analyse(const HModel& m, ModelDev& o) {
         default: return false;
         }
     }
+    // the per-object divisions of Response depend only on the model: evaluated once here
+    // with the same IEEE operations (1.0 / m, then ((2.5 / m) / r) / r)
+    o.inv_sudo = 1.0 / o.sudo;
+    o.rot_coef = (m.shape == SHAPE_SPHERE) ? 2.5 / o.sudo / o.a0 / o.a0 : 0.0;
     return true;
 }
 

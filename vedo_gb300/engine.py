@@ -110,8 +110,14 @@ class GpuEngine:
         self._check(lib().vedo_gpu_run(self.h, nsteps, C.byref(keep)))
         return bool(keep.value)
 
-    def state(self, fields=STATE_FIELDS) -> Dict[str, np.ndarray]:
-        out = {f: np.zeros((self.n, 3)) for f in fields}
+    def state(self, fields=STATE_FIELDS, out: Optional[Dict[str, np.ndarray]] = None) -> Dict[str, np.ndarray]:
+        """Copy object state to host arrays ([n][3] float64); `out` may supply (pinned) buffers."""
+        if out is None:
+            out = {f: np.zeros((self.n, 3)) for f in fields}
+        for f in fields:
+            a = out[f]
+            if a.dtype != np.float64 or not a.flags.c_contiguous or a.shape != (self.n, 3):
+                raise ValueError(f"out[{f!r}] must be a C-contiguous float64 array of shape ({self.n}, 3)")
         v = StateView()
         for f in fields:
             setattr(v, f, dptr(out[f]))
