@@ -198,6 +198,22 @@ def reference_arm(args, dist):
 
 
 # ------------------------------------------------------------------------------------------
+def time_form(eng, args, dist, clocks=None):
+    """W warm-up steps, then exactly K timed steps (CUDA events on the engine stream, max over
+    ranks); returns (ms for K steps, kernel launches in the timed region)."""
+    import torch
+    eng.run(args.warmup)
+    dist.barrier()
+    torch.cuda.synchronize()
+    if clocks:
+        clocks.start()
+    eng.run(args.steps)
+    prof = eng.last_run_profile()
+    rec = clocks.stop() if clocks else None
+    dist.barrier()
+    return dist.reduce(prof["total_ms"], "max"), prof["launches"], rec
+
+
 def ours(args, dist):
     import numpy as np
     import torch
@@ -219,39 +235,62 @@ def ours(args, dist):
         cpu = {"value": rate, "unit": UNIT, "cores": 1, "kind": "port",
                "sample": f"first {args.cpu_sample_steps} time steps (one candidate-list rebuild) of the same "
                          f"{n}-sphere drum, single thread, {secs:.1f} s"}
-    eng = GpuEngine(scene, up_iact=args.up_iact, device=dev)
-    eng.run(args.warmup)
-    dist.barrier()
-    torch.cuda.synchronize()
-    clocks = Clocks(dev)
-    clocks.start()
-    eng.run(args.steps)
-    prof = eng.last_run_profile()
-    clocks_rec = clocks.stop()
-    dist.barrier()
-    t_ms = dist.reduce(prof["total_ms"], "max")
     total_particles = dist.reduce(float(n), "sum")
-    value = total_particles * args.steps / (t_ms * 1e-3)
-    launches = prof["launches"]
-    it = eng.interactions()
-    n_pairs = len(it["first"])
-    n_active = int(it["active"].sum())
 
-    # per-kernel split for the roofline (profiled pass: adds a host sync per step)
+    # plain FP64 form (the drop-in): same scene, same window
+    f64 = GpuEngine(scene, up_iact=args.up_iact, device=dev)
+    t64, l64, _ = time_form(f64, args, dist)
+    fp64_value = total_particles * args.steps / (t64 * 1e-3)
+    it64 = f64.interactions()
+    n_active = int(it64["active"].sum())
+
+    # mixed form (the headline): FP32 pair forces, FP64 integration, compensated sums
+    eng = GpuEngine(scene, up_iact=args.up_iact, device=dev, precision=1)
+    clocks = Clocks(dev)
+    t_ms, launches, clocks_rec = time_form(eng, args, dist, clocks)
+    value = total_particles * args.steps / (t_ms * 1e-3)
+
+    # error of the mixed form against the FP64 engine on this window: end-of-window energy and
+    # the impulses of one step from the FP64 engine's state (restarted through an .ido so both
+    # forms start from identical positions, velocities and shear history)
+    o64, omx = f64.observables(), eng.observables()
+    e64, emx = o64[0] + o64[1] + o64[2], omx[0] + omx[1] + omx[2]
+    errors = {"energy_rel": abs(e64 - emx) / max(abs(e64), 1e-300),
+              "kinetic_rel": abs(o64[1] - omx[1]) / max(abs(o64[1]), 1e-300),
+              "contacts_fp64": int(o64[9]), "contacts_mixed": int(omx[9])}
+    if args.n <= 2_000_000 and not args.no_profile_pass:
+        with tempfile.TemporaryDirectory() as td:
+            path = os.path.join(td, "w.ido")
+            f64.write_ido(path)
+            a = GpuEngine(path, up_iact=args.up_iact, device=dev)
+            b = GpuEngine(path, up_iact=args.up_iact, device=dev, precision=1)
+            a.run(1)
+            b.run(1)
+            sa, sb = a.state(("impact", "angular_impact")), b.state(("impact", "angular_impact"))
+            ia, ib = a.interactions(), b.interactions()
+            A = set(zip(ia["first"][ia["active"] == 1].tolist(), ia["second"][ia["active"] == 1].tolist()))
+            B = set(zip(ib["first"][ib["active"] == 1].tolist(), ib["second"][ib["active"] == 1].tolist()))
+            for k in ("impact", "angular_impact"):
+                d = sa[k] - sb[k]
+                errors[f"step_{k}_rel_l2"] = float(np.linalg.norm(d) / max(np.linalg.norm(sa[k]), 1e-300))
+            errors["contact_set_identical"] = A == B
+            a.close()
+            b.close()
+    f64.close()
+
+    # per-kernel split of the mixed form (tick = fused detect-force-integrate) from one
+    # profiled window
     kern = None
     if not args.no_profile_pass:
         eng.set_profiling(True)
         eng.run(args.up_iact)
-        kp = eng.last_run_profile()
+        kern = eng.last_run_profile()
         eng.set_profiling(False)
-        kern = kp
     # e2e through the C ABI with pinned host buffers
     fields = ("position", "velocity", "angular_velocity", "orientation_x", "orientation_z")
-    st = eng.state(fields)
     pinned = {f: torch.empty((eng.n, 3), dtype=torch.float64, pin_memory=True) for f in fields}
     host = {f: pinned[f].numpy() for f in fields}
-    for f in fields:
-        host[f][:] = st[f]
+    eng.state(fields, out=host)
     e2e_t = 0.0
     e2e_steps = 0
     for _ in range(args.e2e_iters):
@@ -266,43 +305,43 @@ def ours(args, dist):
     e2e_value = total_particles * e2e_steps / e2e_t if e2e_t > 0 else None
     xfer = 24 * eng.n * len(fields)
 
-    # algorithmic bytes per particle-step (FP64 form): state x, v, w + orientation Ox, Oz
-    # (integrated) read and written, per active contact the ISwH history (shear + kn) read
-    # and written plus the pair index, plus the per-particle radius (polydisperse)
-    s_state = 72 + 48
-    s_hist = 32
+    # algorithmic bytes per particle-step of the mixed form: x, v, w (FP64) read + written
+    # (sphere orientation is not integrated in this form), per active contact the FP32 history
+    # (shear + kn, 16 B) read + written plus the pair index, plus the per-particle radius
+    s_state = 72
+    s_hist = 16
     z_pp = n_active / n
     b_alg = 2 * s_state + z_pp * (2 * s_hist + 8) + 8
     peak, peak_kind = peaks()
     roof = None
-    if kern and kern["pair_ms"] + kern["object_ms"] > 0:
-        steps_k = args.up_iact
-        t_pair = kern["pair_ms"] / steps_k
-        t_obj = kern["object_ms"] / steps_k
-        if t_pair >= t_obj:
-            name, t_k, bytes_k = "k_pair", t_pair, n_active * (2 * s_hist + 8)
-        else:
-            name, t_k, bytes_k = "k_obj", t_obj, n * (2 * s_state + 8)
-        ach = bytes_k / (t_k * 1e-3) / 1e9
-        roof = {"kernel": name, "bound": "hbm", "achieved": ach, "peak": peak, "unit": "GB/s",
-                "frac": ach / peak, "peak_source": peak_kind, "traffic": None,
-                "ms_per_launch": t_k, "alg_bytes_per_launch": bytes_k,
-                "step_split_ms": {"pair": t_pair, "object": t_obj, "rebuild_per_step": kern["rebuild_ms"] / steps_k}}
+    if kern and kern["total_ms"] > 0:
+        t_step = t_ms / args.steps
+        ach = b_alg * n / (t_step * 1e-3) / 1e9
+        roof = {"kernel": "k_tick (fused narrow phase + forces + integration, one launch per step)",
+                "bound": "hbm", "achieved": ach, "peak": peak, "unit": "GB/s", "frac": ach / peak,
+                "peak_source": peak_kind, "traffic": None, "ms_per_step": t_step,
+                "alg_bytes_per_step": b_alg * n}
     res = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": dist.world, "steps": args.steps,
            "warmup": args.warmup, "ms_per_step": t_ms / args.steps, "higher_is_better": True, "scaling": "weak",
-           "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded hertz_drum scene, no dataset)",
+           "vs_baseline": None, "dtype": "f32 forces + f64 state (mixed)",
+           "data": "synthetic (seeded hertz_drum scene, no dataset)",
            "config": {"workload": WORKLOAD, "particles_per_gpu": n, "objects_per_gpu": eng.n,
-                      "form": "plain FP64 (drop-in, bit-exact order of operations)", "up_iact": args.up_iact,
-                      "candidate_pairs": n_pairs, "active_contacts": n_active, "z_pp": z_pp,
+                      "form": "mixed (FP32 pair-local forces, FP64 overlap numerator and integration, "
+                              "Kahan sums; sphere orientation not integrated)",
+                      "up_iact_fp64": args.up_iact, "active_contacts": n_active, "z_pp": z_pp,
                       "alg_bytes_per_particle_step": b_alg,
-                      "l2": "working set larger than L2 (state + candidate list > 129 MB)",
-                      "parallelism": f"replicas x{dist.world}", "window": f"steps {args.warmup}.."
-                      f"{args.warmup + args.steps} of the configured 10000-step run"},
+                      "l2": "working set larger than L2 (state + lists > 129 MB)",
+                      "parallelism": f"replicas x{dist.world}",
+                      "window": f"steps {args.warmup}..{args.warmup + args.steps} of the configured 10000-step run"},
+           "fp64": {"value": fp64_value, "ms_per_step": t64 / args.steps, "gpu_launches": l64,
+                    "form": "plain FP64 drop-in, bit-exact operation order"},
+           "mixed_over_fp64": value / fp64_value,
+           "errors_mixed_vs_fp64": errors,
            "clocks": clocks_rec, "gpu_launches": launches,
            "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": xfer / args.sync,
                    "d2h_bytes_per_step": xfer / args.sync,
                    "note": f"vedo_gpu_set_state + vedo_gpu_run({args.sync}) + vedo_gpu_get_state per "
-                           f"{args.sync} steps, pinned host buffers"},
+                           f"{args.sync} steps, pinned host buffers, mixed form"},
            "roofline": roof, "cpu_baseline": cpu}
     eng.close()
     if dist.rank == 0:

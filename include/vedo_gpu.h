@@ -119,6 +119,11 @@ typedef struct vedo_scene_desc {
 } vedo_scene_desc;
 
 /* ---- engine options ---------------------------------------------------- */
+/* FP64: the drop-in; every FP64 operation in the reference's order, results bit-identical
+ *       to the reference for the linear laws (see the design doc of the engine).
+ * MIXED: contact forces in FP32 in pair-local coordinates, FP64 positions, velocities and
+ *       overlap numerators, FP32 compensated sums per object; contact sets identical to
+ *       FP64 at identical positions; sphere orientations are not integrated. */
 enum { VEDO_PRECISION_FP64 = 0, VEDO_PRECISION_MIXED = 1 };
 
 typedef struct vedo_engine_opts {
@@ -132,7 +137,11 @@ typedef struct vedo_engine_opts {
                                  written when non-NULL, as Consultant::RecordIDO
                                  (Consultant.cpp:217-230) and NBSConsultant::NextStep
                                  (NBSConsultant.cpp:63-76) do; NULL writes nothing  */
-    uint32_t reserved[4];
+    float skin;               /* MIXED only: neighbour-list skin as a fraction of the
+                                 largest sphere radius (default 0.15); the list is rebuilt
+                                 when any sphere may have moved half of it             */
+    uint32_t check_interval;  /* MIXED only: steps between displacement checks (10)   */
+    uint32_t reserved[2];
 } vedo_engine_opts;
 
 typedef struct vedo_gpu_engine vedo_gpu_engine;

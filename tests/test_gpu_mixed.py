@@ -1,0 +1,125 @@
+"""GPU tests of the mixed-precision form (VEDO_PRECISION_MIXED) against the FP64 engine, whose
+results are pinned to the reference by test_gpu_parity.py.
+
+Bars (from the engine's contract): the contact set at identical positions is identical;
+per-step impulses from identical state (positions, velocities, shear history) agree within
+1e-5 relative (L2 over all objects); energy after 2,000 steps within 1 %; runs are
+deterministic."""
+import os
+
+import numpy as np
+import pytest
+
+from vedo_gb300 import scenes
+
+pytestmark = pytest.mark.gpu
+
+
+def _settled(engine_lib, tmp_path, scene, steps, name):
+    e = engine_lib.GpuEngine(scene, up_iact=20)
+    e.run(steps)
+    p = str(tmp_path / f"{name}.ido")
+    e.write_ido(p)
+    e.close()
+    return p
+
+
+def _active_set(it):
+    a = it["active"] == 1
+    return set(zip(it["first"][a].tolist(), it["second"][a].tolist()))
+
+
+@pytest.fixture(scope="module")
+def box_ido(engine_lib, tmp_path_factory):
+    sc = scenes.lsd_box(n_side=12, vel_sigma=0.3, spacing=2.05e-3)
+    return _settled(engine_lib, tmp_path_factory.mktemp("mx"), sc, 4000, "box")
+
+
+@pytest.fixture(scope="module")
+def drum_ido(engine_lib, tmp_path_factory):
+    sc = scenes.hertz_drum(n=40000, seed=3, steps=100, gap=0.002, vel_sigma=0.05)
+    return _settled(engine_lib, tmp_path_factory.mktemp("mx"), sc, 3000, "drum")
+
+
+@pytest.mark.parametrize("which", ["box", "drum"])
+def test_mixed_contact_set_equals_fp64(which, box_ido, drum_ido, engine_lib):
+    path = box_ido if which == "box" else drum_ido
+    a = engine_lib.GpuEngine(path, up_iact=20)
+    b = engine_lib.GpuEngine(path, up_iact=20, precision=1)
+    A, B = _active_set(a.interactions()), _active_set(b.interactions())
+    assert len(A) > 10
+    assert A == B
+
+
+@pytest.mark.parametrize("which", ["box", "drum"])
+def test_mixed_per_step_impulse_error(which, box_ido, drum_ido, engine_lib):
+    path = box_ido if which == "box" else drum_ido
+    a = engine_lib.GpuEngine(path, up_iact=20)
+    b = engine_lib.GpuEngine(path, up_iact=20, precision=1)
+    a.run(1)
+    b.run(1)
+    sa, sb = a.state(), b.state()
+    for k in ("impact", "angular_impact"):
+        ref = np.linalg.norm(sa[k])
+        assert ref > 0, k
+        err = np.linalg.norm(sa[k] - sb[k]) / ref
+        assert err <= 1e-5, (k, err)
+
+
+def test_mixed_energy_within_one_percent(box_ido, engine_lib):
+    a = engine_lib.GpuEngine(box_ido, up_iact=20)
+    b = engine_lib.GpuEngine(box_ido, up_iact=20, precision=1)
+    a.run(2000)
+    b.run(2000)
+    oa, ob = a.observables(), b.observables()
+    ea, eb = oa[0] + oa[1] + oa[2], ob[0] + ob[1] + ob[2]
+    assert abs(ea - eb) <= 0.01 * abs(ea)
+    assert abs(oa[1] - ob[1]) <= 0.01 * oa[1]
+
+
+def test_mixed_deterministic(drum_ido, engine_lib):
+    r = []
+    for _ in range(2):
+        e = engine_lib.GpuEngine(drum_ido, up_iact=20, precision=1)
+        e.run(300)
+        r.append(e.state())
+        e.close()
+    for k in r[0]:
+        assert np.array_equal(r[0][k], r[1][k]), k
+
+
+def test_mixed_rebuilds_keep_history(box_ido, engine_lib):
+    """A tiny skin forces a rebuild every few steps; the shear history must survive them
+    (results stay within the FP32 tolerance of a run with a large skin)."""
+    a = engine_lib.GpuEngine(box_ido, precision=1)
+    b = engine_lib.GpuEngine(box_ido, precision=1, skin=0.002, check_interval=1)
+    a.run(400)
+    b.run(400)
+    sa, sb = a.state(), b.state()
+    err = np.linalg.norm(sa["velocity"] - sb["velocity"]) / np.linalg.norm(sa["velocity"])
+    assert err < 1e-4, err
+
+
+def test_mixed_matches_oracle_trajectory_start(engine_lib, port_lib):
+    """Mixed vs the C oracle (= the reference) for the first 100 steps of a colliding cluster."""
+    from oracle import PortWorld
+    sc = scenes.cluster(n=64, solver="ISwBSDBF", steps=500, seed=21)
+    e = engine_lib.GpuEngine(sc, up_iact=5, precision=1)
+    p = PortWorld(sc, up_iact=5)
+    e.run(100)
+    p.run(100)
+    a, b = e.state(), p.state()
+    assert np.linalg.norm(a["velocity"] - b["velocity"]) <= 1e-5 * np.linalg.norm(b["velocity"])
+    assert np.abs(a["position"] - b["position"]).max() <= 1e-9
+
+
+def test_mixed_rejects_mobile_walls(engine_lib):
+    from vedo_gb300.scene import MOBILE
+    sc = scenes.cluster(n=8)
+    for m in sc.models:
+        if m.group == "Wall":
+            m.behavior = MOBILE
+            m.density = 1000.0
+    with pytest.raises(engine_lib.EngineError) as ex:
+        engine_lib.GpuEngine(sc, precision=1)
+    assert ex.value.code == 3

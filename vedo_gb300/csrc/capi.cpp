@@ -4,10 +4,11 @@
 #include <string>
 
 #include "../../include/vedo_gpu.h"
-#include "engine.h"
+#include "engine_base.h"
 
 struct vedo_gpu_engine {
-    vedo::Engine eng;
+    vedo::EngineBase* p = nullptr;
+    ~vedo_gpu_engine() { delete p; }
 };
 
 namespace {
@@ -17,11 +18,20 @@ int create_common(const vedo::HScene& s, const vedo_engine_opts* opts, vedo_gpu_
     vedo_engine_opts o;
     vedo_gpu_default_opts(&o);
     if (opts) o = *opts;
+    if (o.precision != VEDO_PRECISION_FP64 && o.precision != VEDO_PRECISION_MIXED) {
+        g_create_error = "unknown precision form";
+        return VEDO_ERR_INVALID_ARGUMENT;
+    }
     vedo_gpu_engine* e = new (std::nothrow) vedo_gpu_engine();
     if (!e) return VEDO_ERR_OUT_OF_MEMORY;
-    int rc = e->eng.init(s, o);
+    e->p = o.precision == VEDO_PRECISION_MIXED ? vedo::make_mixed_engine() : vedo::make_fp64_engine();
+    if (!e->p) {
+        delete e;
+        return VEDO_ERR_OUT_OF_MEMORY;
+    }
+    int rc = e->p->init(s, o);
     if (rc != VEDO_OK) {
-        g_create_error = e->eng.error();
+        g_create_error = e->p->error();
         delete e;
         *out = nullptr;
         return rc;
@@ -41,6 +51,8 @@ void vedo_gpu_default_opts(vedo_engine_opts* o) {
     o->precision = VEDO_PRECISION_FP64;
     o->device = 0;
     o->output_prefix = nullptr;
+    o->skin = 0.15f;
+    o->check_interval = 10;
 }
 
 int vedo_gpu_create(const vedo_scene_desc* scene, const vedo_engine_opts* opts, vedo_gpu_engine** out) {
@@ -69,57 +81,57 @@ int vedo_gpu_create_from_ido(const char* path, const vedo_engine_opts* opts, ved
 
 int vedo_gpu_run(vedo_gpu_engine* e, uint32_t nsteps, int* keep_running) {
     if (!e) return VEDO_ERR_INVALID_ARGUMENT;
-    return e->eng.run(nsteps, keep_running);
+    return e->p->run(nsteps, keep_running);
 }
 
-uint32_t vedo_gpu_num_objects(const vedo_gpu_engine* e) { return e ? e->eng.num_objects() : 0u; }
+uint32_t vedo_gpu_num_objects(const vedo_gpu_engine* e) { return e ? e->p->num_objects() : 0u; }
 
 int vedo_gpu_get_state(vedo_gpu_engine* e, const vedo_state_view* out) {
     if (!e || !out) return VEDO_ERR_INVALID_ARGUMENT;
-    return e->eng.get_state(*out);
+    return e->p->get_state(*out);
 }
 
 int vedo_gpu_set_state(vedo_gpu_engine* e, const vedo_state_view* in) {
     if (!e || !in) return VEDO_ERR_INVALID_ARGUMENT;
-    return e->eng.set_state(*in);
+    return e->p->set_state(*in);
 }
 
 int vedo_gpu_num_interactions(vedo_gpu_engine* e, uint32_t* n) {
     if (!e || !n) return VEDO_ERR_INVALID_ARGUMENT;
-    return e->eng.num_interactions(n);
+    return e->p->num_interactions(n);
 }
 
 int vedo_gpu_get_interactions(vedo_gpu_engine* e, const vedo_contact_view* out) {
     if (!e || !out) return VEDO_ERR_INVALID_ARGUMENT;
-    return e->eng.get_interactions(*out);
+    return e->p->get_interactions(*out);
 }
 
 int vedo_gpu_get_observables(vedo_gpu_engine* e, double out[13]) {
     if (!e || !out) return VEDO_ERR_INVALID_ARGUMENT;
-    return e->eng.get_observables(out);
+    return e->p->get_observables(out);
 }
 
-double vedo_gpu_time(const vedo_gpu_engine* e) { return e ? e->eng.time() : 0.0; }
+double vedo_gpu_time(const vedo_gpu_engine* e) { return e ? e->p->time() : 0.0; }
 
-uint64_t vedo_gpu_step_count(const vedo_gpu_engine* e) { return e ? e->eng.steps() : 0u; }
+uint64_t vedo_gpu_step_count(const vedo_gpu_engine* e) { return e ? e->p->steps() : 0u; }
 
 int vedo_gpu_write_ido(vedo_gpu_engine* e, const char* path) {
     if (!e || !path) return VEDO_ERR_INVALID_ARGUMENT;
-    return e->eng.write_ido(path);
+    return e->p->write_ido(path);
 }
 
 uint64_t vedo_gpu_last_run_profile(const vedo_gpu_engine* e, double out[4]) {
     if (!e || !out) return 0;
-    return e->eng.last_profile(out);
+    return e->p->last_profile(out);
 }
 
 void vedo_gpu_set_profiling(vedo_gpu_engine* e, int on) {
-    if (e) e->eng.set_profiling(on != 0);
+    if (e) e->p->set_profiling(on != 0);
 }
 
 const char* vedo_gpu_last_error(const vedo_gpu_engine* e) {
     if (!e) return g_create_error.c_str();
-    return e->eng.error().c_str();
+    return e->p->error().c_str();
 }
 
 void vedo_gpu_destroy(vedo_gpu_engine* e) { delete e; }

@@ -18,6 +18,7 @@
 
 #include "../../include/vedo_gpu.h"
 #include "dem_common.cuh"
+#include "engine_base.h"
 #include "scene_host.h"
 #include "sort_scan.h"
 
@@ -37,26 +38,26 @@ struct PairList {
     uint32_t* csr_ptr = nullptr; // [n+1]
 };
 
-class Engine {
+class Engine : public EngineBase {
 public:
     Engine() = default;
-    ~Engine();
+    ~Engine() override;
 
-    int init(const HScene& scene, const vedo_engine_opts& opts);
-    int run(uint32_t nsteps, int* keep_running);
-    int get_state(const vedo_state_view& v);
-    int set_state(const vedo_state_view& v);
-    int num_interactions(uint32_t* n);
-    int get_interactions(const vedo_contact_view& v);
-    int get_observables(double out[13]);
-    int write_ido(const char* path);
+    int init(const HScene& scene, const vedo_engine_opts& opts) override;
+    int run(uint32_t nsteps, int* keep_running) override;
+    int get_state(const vedo_state_view& v) override;
+    int set_state(const vedo_state_view& v) override;
+    int num_interactions(uint32_t* n) override;
+    int get_interactions(const vedo_contact_view& v) override;
+    int get_observables(double out[13]) override;
+    int write_ido(const char* path) override;
 
-    double time() const { return t_; }
-    uint64_t steps() const { return round_; }
-    uint32_t num_objects() const { return n_; }
-    uint64_t last_profile(double out[4]) const;
-    void set_profiling(bool on) { profiling_ = on; }
-    const std::string& error() const { return err_; }
+    double time() const override { return t_; }
+    uint64_t steps() const override { return round_; }
+    uint32_t num_objects() const override { return n_; }
+    uint64_t last_profile(double out[4]) const override;
+    void set_profiling(bool on) override { profiling_ = on; }
+    const std::string& error() const override { return err_; }
 
 private:
     int fail(int code, const std::string& msg) { err_ = msg; return code; }

@@ -1,0 +1,34 @@
+// engine_base.h - the interface both engine forms implement behind the C ABI.
+#pragma once
+
+#include <cstdint>
+#include <string>
+
+#include "../../include/vedo_gpu.h"
+#include "scene_host.h"
+
+namespace vedo {
+
+class EngineBase {
+public:
+    virtual ~EngineBase() = default;
+    virtual int init(const HScene& scene, const vedo_engine_opts& opts) = 0;
+    virtual int run(uint32_t nsteps, int* keep_running) = 0;
+    virtual int get_state(const vedo_state_view& v) = 0;
+    virtual int set_state(const vedo_state_view& v) = 0;
+    virtual int num_interactions(uint32_t* n) = 0;
+    virtual int get_interactions(const vedo_contact_view& v) = 0;
+    virtual int get_observables(double out[13]) = 0;
+    virtual int write_ido(const char* path) = 0;
+    virtual double time() const = 0;
+    virtual uint64_t steps() const = 0;
+    virtual uint32_t num_objects() const = 0;
+    virtual uint64_t last_profile(double out[4]) const = 0;
+    virtual void set_profiling(bool on) = 0;
+    virtual const std::string& error() const = 0;
+};
+
+EngineBase* make_fp64_engine();
+EngineBase* make_mixed_engine();
+
+}  // namespace vedo

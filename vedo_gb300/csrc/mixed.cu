@@ -1,0 +1,1518 @@
+// mixed.cu - mixed-precision DEM engine: one fused tick kernel per time step.
+//
+// Each sphere thread walks its full neighbour list (both directions) and, for every
+// neighbour, evaluates the pair in canonical (slave, master) orientation (the reference's
+// Assembler rule, Assembler.cpp:43-67) from inputs both members read identically: the
+// previous step's positions (FP64), FP32 velocity copies and the pair's history.  Both
+// members therefore obtain bit-identical impulses and Newton's third law holds exactly; the
+// history owner (the lower index, or the sphere of a sphere-wall pair) writes the updated
+// history into the other buffer.  Impulses are summed per sphere in FP32 with Kahan
+// compensation, in the (deterministic) neighbour-list order, and the sphere is integrated
+// in FP64 (positions, velocities, angular velocities).
+//
+// Precision split (per pair): the relative displacement d = x_master - x_slave and the
+// overlap numerator R^2 - |d|^2 are FP64 (the overlap of stiff contacts is 1e-9..1e-6 of the
+// radius, beyond FP32's reach); the overlap itself, the normal, relative velocities, forces
+// and torques are FP32 in pair-local coordinates.  The contact decision (overlap > 0) is the
+// FP64 decision: where |R^2 - |d|^2| is within 1e-9 R^2 the reference's own FP64 formula
+// (rounded intrinsics, no contraction) decides, so contact sets equal the FP64 engine's.
+// Sphere-wall pairs use the reference's FP64 detectors for the geometry.
+//
+// Broad phase: uniform cell list of edge 2 r_max + skin, stable radix sort on cell key,
+// full neighbour lists within r_i + r_j + skin (a conservative FP32 test: a superset), walls
+// by a plane/axis lower bound.  The list is rebuilt when the accumulated bound on any
+// sphere's displacement, sum over steps of dt * max|v|, may exceed half the skin.
+#include <algorithm>
+#include <cfloat>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <new>
+#include <string>
+#include <vector>
+
+#include <cuda_runtime.h>
+
+#include "dem_common.cuh"
+#include "engine_base.h"
+#include "observables.cuh"
+#include "prefilter.cuh"
+#include "scene_host.h"
+#include "sort_scan.h"
+
+namespace vedo {
+namespace {
+
+constexpr int TPB = 256;
+inline unsigned nblk(uint64_t n, int tpb = TPB) { return (unsigned)((n + tpb - 1) / tpb); }
+
+constexpr uint32_t WALL_BIT = 0x80000000u;
+constexpr uint8_t PF_ACTIVE_BIT = 64;
+// history flag bit: the status just became clean and the other buffer still holds the old one
+constexpr uint8_t HF_PENDING = 16;
+
+// ---- exact FP64 (rounded intrinsics: never contracted into FMA) -----------------------
+__device__ __forceinline__ d3 xadd(d3 a, d3 b) { return mk(__dadd_rn(a.x, b.x), __dadd_rn(a.y, b.y), __dadd_rn(a.z, b.z)); }
+__device__ __forceinline__ d3 xsub(d3 a, d3 b) { return mk(__dsub_rn(a.x, b.x), __dsub_rn(a.y, b.y), __dsub_rn(a.z, b.z)); }
+__device__ __forceinline__ d3 xsmul(double s, d3 a) { return mk(__dmul_rn(s, a.x), __dmul_rn(s, a.y), __dmul_rn(s, a.z)); }
+__device__ __forceinline__ double xdot(d3 a, d3 b) {
+    return __dadd_rn(__dadd_rn(__dmul_rn(a.x, b.x), __dmul_rn(a.y, b.y)), __dmul_rn(a.z, b.z));
+}
+__device__ __forceinline__ double xlen(d3 a) { return __dsqrt_rn(xdot(a, a)); }
+__device__ __forceinline__ d3 xdir(d3 a) {
+    const double l = xlen(a);
+    if (l != 0) return mk(__ddiv_rn(a.x, l), __ddiv_rn(a.y, l), __ddiv_rn(a.z, l));
+    return mk(0.0, 0.0, 0.0);
+}
+__device__ __forceinline__ d3 xcross(d3 a, d3 b) {
+    return mk(__dsub_rn(__dmul_rn(a.y, b.z), __dmul_rn(a.z, b.y)), __dsub_rn(__dmul_rn(a.z, b.x), __dmul_rn(a.x, b.z)),
+              __dsub_rn(__dmul_rn(a.x, b.y), __dmul_rn(a.y, b.x)));
+}
+__device__ __forceinline__ d3 xproject_on(d3 a, d3 v) { return xsmul(__ddiv_rn(xdot(a, v), xlen(v)), xdir(v)); }
+
+// The reference's sphere-plate / sphere-cylinder detectors (CDSphere2QuasiPlate.cpp:15-97,
+// CDSphere2QuasiCylinder.cpp:16-80) in exact FP64: depth, unit normal, impact point.
+__device__ __forceinline__ double wall_detect(int cd, double ra, double b0, double b1, double b2, d3 Ps, d3 Pm, d3 Ox,
+                                              d3 Oz, d3& n, d3& point) {
+    double depth;
+    if (cd == CD_SP) {
+        const d3 Oy = xcross(Oz, Ox);
+        const d3 Cap = xsub(Ps, xproject_on(xsub(Ps, Pm), Oz));
+        const double hh = __dmul_rn(0.5, b1), hw = __dmul_rn(0.5, b0), hl = __dmul_rn(0.5, b2);
+        double dx = xdot(xsub(Cap, Pm), Ox);
+        if (dx < -hw) dx = -hw; else if (dx > hw) dx = hw;
+        double dy = xdot(xsub(Cap, Pm), Oy);
+        if (dy < -hl) dy = -hl; else if (dy > hl) dy = hl;
+        const d3 Caps = xadd(xadd(xsmul(dx, Ox), xsmul(dy, Oy)), Pm);
+        const d3 vIm = xsub(Caps, Ps);
+        depth = __dsub_rn(__dadd_rn(ra, hh), xlen(vIm));
+        n = xdir(vIm);
+    } else {
+        const double hh = __dmul_rn(0.5, b1);
+        double dap = xdot(xsub(Ps, Pm), Oz);
+        if (dap < -hh) dap = -hh; else if (dap > hh) dap = hh;
+        const d3 Caps = xadd(Pm, xsmul(dap, Oz));
+        const d3 vIm = xsub(Caps, Ps);
+        depth = __dsub_rn(__dadd_rn(ra, b0), xlen(vIm));
+        n = xdir(vIm);
+    }
+    point = xadd(Ps, xsmul(__dsub_rn(ra, __dmul_rn(0.5, depth)), n));
+    return depth;
+}
+
+// ---- FP32 vectors ----------------------------------------------------------------------
+struct f3 { float x, y, z; };
+__device__ __forceinline__ f3 fm(float x, float y, float z) { f3 r; r.x = x; r.y = y; r.z = z; return r; }
+__device__ __forceinline__ f3 operator+(f3 a, f3 b) { return fm(a.x + b.x, a.y + b.y, a.z + b.z); }
+__device__ __forceinline__ f3 operator-(f3 a, f3 b) { return fm(a.x - b.x, a.y - b.y, a.z - b.z); }
+__device__ __forceinline__ f3 operator*(float s, f3 a) { return fm(s * a.x, s * a.y, s * a.z); }
+__device__ __forceinline__ f3 operator-(f3 a) { return fm(-a.x, -a.y, -a.z); }
+__device__ __forceinline__ float fdot(f3 a, f3 b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
+__device__ __forceinline__ float flen(f3 a) { return sqrtf(fdot(a, a)); }
+__device__ __forceinline__ f3 fdir(f3 a) {
+    const float l = flen(a);
+    return l != 0.0f ? (1.0f / l) * a : fm(0.0f, 0.0f, 0.0f);
+}
+__device__ __forceinline__ f3 fcross(f3 a, f3 b) {
+    return fm(a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x);
+}
+__device__ __forceinline__ f3 f4to3(float4 v) { return fm(v.x, v.y, v.z); }
+
+// Kahan-compensated FP32 sum of 3-vectors
+struct K3 {
+    f3 s{0.0f, 0.0f, 0.0f}, c{0.0f, 0.0f, 0.0f};
+    __device__ __forceinline__ void add1(float& sum, float& comp, float x) {
+        const float y = x - comp;
+        const float t = sum + y;
+        comp = (t - sum) - y;
+        sum = t;
+    }
+    __device__ __forceinline__ void add(f3 v) {
+        add1(s.x, c.x, v.x);
+        add1(s.y, c.y, v.y);
+        add1(s.z, c.z, v.z);
+    }
+    __device__ __forceinline__ d3 value() const {
+        return mk((double)s.x - (double)c.x, (double)s.y - (double)c.y, (double)s.z - (double)c.z);
+    }
+};
+
+// ---- the five laws in FP32 (same control flow as the reference's NextStep) -------------
+enum : uint8_t { HF_CONTACT = 1, HF_LAST_CONTACT = 2, HF_BOND = 4, HF_LAST_BOND = 8 };
+
+__device__ __forceinline__ f3 shear_rot(f3 F, f3 vs) {                    // ISwModels.cpp:263-273
+    return fdot(F, vs) <= 0.0f ? (-flen(F)) * fdir(vs) : flen(F) * fdir(vs);
+}
+
+// returns 0 (nothing added), 1 (impulse only) or 2 (impulse + torques).  LAW != 0 fixes the
+// equation type at compile time (scenes with a single law), LAW == 0 dispatches on `is`.
+template <int LAW>
+__device__ __forceinline__ int solve32(int is_rt, const float* __restrict__ c, bool active, float depth, f3 n, f3 rA, f3 rB,
+                                      f3 va, f3 vb, f3 wa, f3 wb, float dt, uint8_t& f, float4& h, f3& J, f3& tA,
+                                      f3& tB) {
+    const int is = LAW ? LAW : is_rt;
+    const f3 Z = fm(0.0f, 0.0f, 0.0f);
+    const bool lsd = is == IS_BSDBF || is == IS_BTSDBF || is == IS_BSDB2F;
+    const bool bond = lsd && (depth <= 0.0f) && (c[0] != 0.0f) && (c[4] != 0.0f) && (-depth * c[0] < c[4]);
+    if (!active && !bond) {                                                // ImpactStatus::Clean
+        f = 0;
+        h = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+        return 0;
+    }
+    f3 Fn = Z, Fs = Z;
+    if (depth > 0.0f) {
+        const f3 vRel = (va - vb) + fcross(wa, rA) - fcross(wb, rB);
+        const f3 vRn = fdot(vRel, n) * n;
+        const f3 vRs = vRel - vRn;
+        const f3 sh = fm(h.x, h.y, h.z);
+        if (is == IS_BSDBF || is == IS_BSDB2F || is == IS_BTSDBF) {        // ISwBSDBF.cpp:61-112
+            const float kn = c[0], ks = c[1], cn = c[2], cs = c[3], bs = c[5], fc = c[6];
+            Fn = (-kn * depth) * n - cn * vRn;
+            Fs = (is == IS_BTSDBF) ? (-ks * dt) * vRs - cs * vRs : shear_rot(sh, vRs) - (ks * dt) * vRs;
+            const float fmax = fc * kn * depth;
+            const bool slide = (bs == 0.0f) ? (flen(Fs) > fmax) : (flen(Fs) > bs);
+            Fs = slide ? fmax * fdir(Fs) : Fs - cs * vRs;
+            if (is != IS_BTSDBF) h = make_float4(Fs.x, Fs.y, Fs.z, h.w);
+            f |= HF_CONTACT;
+        } else if (is == IS_HERTZ) {                                       // ISwHertz.cpp:53-78
+            f |= HF_CONTACT;
+            Fn = (-c[0] * depth * sqrtf(depth)) * n - c[1] * vRn;
+        } else {                                                           // ISwH.cpp:159-231
+            const float knH = c[0], Meff = c[1], ksc1 = c[2], ksc2 = c[3], betan = c[4], fk = c[5];
+            float kn;
+            if (!(f & HF_CONTACT)) {
+                const float vnl = flen(vRn);
+                if (vnl == 0.0f) kn = knH;
+                else if (betan < 0.99f)
+                    kn = 0.957832746294131f / (1.0f - betan * betan) * powf(Meff, 0.2f) * powf(knH, 0.8f) *
+                         powf(vnl, 0.4f);
+                else
+                    kn = 479.155951122633f * powf(Meff, 0.2f) * powf(knH, 0.8f) * powf(vnl, 0.4f);
+                f |= HF_CONTACT;
+            } else {
+                kn = h.w;
+            }
+            const float ncd = 2.0f * sqrtf(Meff * kn);
+            const float ks = ksc1 * cbrtf(ksc2 * fabsf(kn * depth));
+            Fn = (-kn * depth) * n - (ncd * betan) * vRn;
+            const float ff = fk * kn * depth;
+            Fs = shear_rot(sh, vRs) - (ks * dt) * vRs;
+            if (flen(Fs) >= ff) Fs = ff * fdir(Fs);
+            h = make_float4(Fs.x, Fs.y, Fs.z, kn);
+        }
+    } else {                                                               // normal bond at depth <= 0
+        const f3 vRel = va - vb;
+        const f3 vRn = fdot(vRel, n) * n;
+        bool clean = true;
+        if (is == IS_BSDB2F && !(f & HF_LAST_BOND)) {
+            clean = false;
+        } else if (is == IS_BTSDBF) {
+            Fn = (-c[0] * depth) * n - c[2] * vRn;
+        } else {
+            Fn = fdot(vRn, n) < 0.0f ? (-c[0] * depth) * n - c[2] * vRn : (-c[2]) * vRn;
+        }
+        if (clean) {
+            uint8_t nf = 0;
+            if (f & HF_CONTACT) nf |= HF_LAST_CONTACT;
+            if (f & HF_BOND) nf |= HF_LAST_BOND;
+            f = nf;
+            h = make_float4(0.0f, 0.0f, 0.0f, h.w);
+        }
+    }
+    if (is == IS_HERTZ) {
+        J = dt * Fn;
+        return 1;
+    }
+    const f3 F = Fn + Fs;
+    J = dt * F;
+    tA = dt * fcross(rA, F);
+    tB = (-dt) * fcross(rB, F);
+    return 2;
+}
+
+// ---- tick ------------------------------------------------------------------------------
+struct TickArgs {
+    uint32_t n, nm;
+    const uint32_t* model_of;
+    const ModelDev* models;
+    const PairParam* params;
+    const float* pc32;             // [nm*nm][8] float constants
+    const double4_32a* geom;       // [nm*nm]: ra, b0, b1, b2
+    const double4_32a* xA;
+    double4_32a* xB;
+    double4_32a* v64;
+    double4_32a* w64;
+    const float4* v32A;
+    float4* v32B;
+    const float4* w32A;
+    float4* w32B;
+    const double4_32a* ox;
+    const double4_32a* oz;
+    const uint32_t* nptr;
+    const uint32_t* nent;
+    const uint32_t* nslot;
+    const float4* hA;
+    float4* hB;
+    const uint8_t* fA;
+    uint8_t* fB;
+    double4_32a* imp;
+    double4_32a* aimp;
+    int write_imp;
+    double dt;
+    d3 fimp;
+    unsigned* vmax_bits;
+    const float4* pos32;           // positions at the last rebuild (FP32 offsets)
+    const float* disp;             // bound on any sphere's displacement since the last rebuild
+    const float* reach;
+    const float4* wall32;
+    float* wimp;                   // [ne][6] impulse and angular impulse on the wall of a wall entry
+    const double4_32a* rr;         // [nm*nm] sphere-sphere: R = ra + rb, R^2, tie-band half width 1e-9 R^2
+    const float4* mf;              // [nm][2]: field + external impulse per step, 1/m~; 2.5/(m~ r^2)
+};
+
+template <int LAW>
+__global__ void __launch_bounds__(TPB) k_tick(TickArgs a) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    float vmax_local = 0.0f;
+    if (i < a.n) {
+        const uint32_t mi = a.model_of[i];
+        const ModelDev& M = a.models[mi];
+        if (M.scope == SCOPE_LOCAL) {
+            const d3 Pi = ld(a.xA, i);
+            const float dtf = (float)a.dt;
+            const float disp = *a.disp;
+            K3 J, JA;
+            const uint32_t e1 = a.nptr[i + 1];
+            for (uint32_t e = a.nptr[i]; e < e1; ++e) {
+                const uint32_t ent = a.nent[e];
+                const uint32_t j = ent & ~WALL_BIT;
+                const bool wall = ent & WALL_BIT;
+                const uint32_t mj = a.model_of[j];
+                // canonical orientation (Assembler.cpp:43-67); sphere-wall: the sphere is the slave
+                bool i_slave;
+                if (wall) {
+                    i_slave = true;
+                } else {
+                    const ModelDev& N = a.models[mj];
+                    if (M.density == 0.0 && N.density != 0.0) i_slave = false;
+                    else if (N.density == 0.0 && M.density != 0.0) i_slave = true;
+                    else i_slave = i < j;
+                }
+                const uint32_t s = i_slave ? i : j, m = i_slave ? j : i;
+                const uint32_t pi = (i_slave ? mi : mj) * a.nm + (i_slave ? mj : mi);
+                const PairParam& P = a.params[pi];
+                if (P.cd == 0) continue;
+                const uint32_t slot = a.nslot[e];
+                const int is = LAW ? LAW : P.is;
+                const bool bondable = (is == IS_BSDBF || is == IS_BTSDBF || is == IS_BSDB2F) && P.c[4] != 0.0;
+                if (!bondable) {
+                    // certainly apart: rebuild-time distance minus both spheres' travel since then
+                    const float4 ws = wall ? a.wall32[m] : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+                    if (certainly_apart(P.cd, a.pos32[s], a.pos32[m], ws, a.reach[pi] + 2.0f * disp)) {
+                        if (wall && a.write_imp) {
+                            float* o = a.wimp + 6 * (size_t)e;
+                            o[0] = o[1] = o[2] = o[3] = o[4] = o[5] = 0.0f;
+                        }
+                        if (e == slot) {
+                            const uint8_t f0 = a.fA[slot];
+                            if (f0 & 15) {                 // ImpactStatus::Clean
+                                a.hB[slot] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+                                a.fB[slot] = HF_PENDING;
+                            } else if (f0 & HF_PENDING) {
+                                a.hB[slot] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+                                a.fB[slot] = 0;
+                            }
+                        }
+                        continue;
+                    }
+                }
+                const double4_32a gg = a.geom[pi];
+                const d3 Pj = ld(a.xA, j);
+                const d3 Ps = i_slave ? Pi : Pj, Pm = i_slave ? Pj : Pi;
+                bool active;
+                float depth;
+                f3 n, rA, rB;
+                if (P.cd == CD_SS) {
+                    const d3 d = sub(Pm, Ps);
+                    const double s2 = fma(d.z, d.z, fma(d.y, d.y, d.x * d.x));
+                    const double4_32a rq = a.rr[pi];          // R, R^2, band
+                    const double num = rq.y - s2;
+                    if (num < -rq.z) {
+                        active = false;
+                        depth = (float)num / ((float)rq.x + sqrtf((float)s2));
+                    } else if (num > rq.z) {
+                        active = true;
+                        depth = (float)num / ((float)rq.x + sqrtf((float)s2));
+                    } else {                               // tie band: the reference's formula decides
+                        const double dex = __dsub_rn(__dadd_rn(gg.x, gg.y), xlen(d));
+                        active = dex > 0.0;
+                        depth = (float)dex;
+                    }
+                    const f3 df = fm((float)d.x, (float)d.y, (float)d.z);
+                    n = fdir(df);
+                    rA = ((float)gg.x - 0.5f * depth) * n;
+                    rB = rA - df;
+                } else {
+                    d3 nd, pt;
+                    const double dex = wall_detect(P.cd, gg.x, gg.y, gg.z, gg.w, Ps, Pm, ld(a.ox, m), ld(a.oz, m), nd,
+                                                   pt);
+                    active = dex > 0.0;
+                    depth = (float)dex;
+                    n = fm((float)nd.x, (float)nd.y, (float)nd.z);
+                    const d3 ra = sub(pt, Ps), rb = sub(pt, Pm);
+                    rA = fm((float)ra.x, (float)ra.y, (float)ra.z);
+                    rB = fm((float)rb.x, (float)rb.y, (float)rb.z);
+                }
+                const uint8_t f0 = a.fA[slot];
+                uint8_t f = f0 & 15;
+                float4 h = (f != 0 || active) ? a.hA[slot] : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+                f3 Jp = fm(0.0f, 0.0f, 0.0f), tA = Jp, tB = Jp;
+                const int app = solve32<LAW>(P.is, a.pc32 + 8 * (size_t)pi, active, depth, n, rA, rB,
+                                        f4to3(a.v32A[s]), f4to3(a.v32A[m]), f4to3(a.w32A[s]), f4to3(a.w32A[m]), dtf, f,
+                                        h, Jp, tA, tB);
+                if (e == slot) {                           // history owner writes the new status
+                    if (f != 0 || (f0 & 15) != 0) {
+                        a.hB[slot] = h;
+                        a.fB[slot] = (uint8_t)(f | ((f == 0) ? HF_PENDING : 0));
+                    } else if (f0 & HF_PENDING) {
+                        a.hB[slot] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+                        a.fB[slot] = 0;
+                    }
+                }
+                if (app) {
+                    if (i_slave) {
+                        J.add(Jp);
+                        if (app == 2) JA.add(tA);
+                    } else {
+                        J.add(-Jp);
+                        if (app == 2) JA.add(tB);
+                    }
+                }
+                if (wall && a.write_imp) {                 // the wall's share, summed per wall later
+                    float* o = a.wimp + 6 * (size_t)e;
+                    o[0] = app ? -Jp.x : 0.0f; o[1] = app ? -Jp.y : 0.0f; o[2] = app ? -Jp.z : 0.0f;
+                    o[3] = app == 2 ? tB.x : 0.0f; o[4] = app == 2 ? tB.y : 0.0f; o[5] = app == 2 ? tB.z : 0.0f;
+                }
+            }
+            // field and external impulse (DOContainer.cpp:20-27, DiscreteObject.cpp:160-163) join the
+            // compensated sum; the increments dv, dw are FP32, the state update FP64
+            const float4 mf0 = a.mf[2 * mi], mf1 = a.mf[2 * mi + 1];
+            J.add(fm(mf0.x, mf0.y, mf0.z));
+            if (a.write_imp) {
+                st(a.imp, i, J.value(), 0.0);
+                st(a.aimp, i, JA.value(), 0.0);
+            }
+            if (M.behavior == BEH_MOBILE) {
+                const f3 Jf = fm(J.s.x - J.c.x, J.s.y - J.c.y, J.s.z - J.c.z);
+                const f3 JAf = fm(JA.s.x - JA.c.x, JA.s.y - JA.c.y, JA.s.z - JA.c.z);
+                const f3 dv = mf0.w * Jf, dw = mf1.x * JAf;
+                const d3 V = ld(a.v64, i), W = ld(a.w64, i);
+                const d3 dvd = mk((double)dv.x, (double)dv.y, (double)dv.z);
+                const d3 P2 = mk(fma(a.dt, fma(0.5, dvd.x, V.x), Pi.x), fma(a.dt, fma(0.5, dvd.y, V.y), Pi.y),
+                                 fma(a.dt, fma(0.5, dvd.z, V.z), Pi.z));
+                const d3 V2 = add(V, dvd);
+                const d3 W2 = add(W, mk((double)dw.x, (double)dw.y, (double)dw.z));
+                st(a.xB, i, P2, 0.0);
+                st(a.v64, i, V2, 0.0);
+                st(a.w64, i, W2, 0.0);
+                const float4 vo = a.v32A[i];
+                const float4 vn = make_float4((float)V2.x, (float)V2.y, (float)V2.z, 0.0f);
+                a.v32B[i] = vn;
+                a.w32B[i] = make_float4((float)W2.x, (float)W2.y, (float)W2.z, 0.0f);
+                vmax_local = fmaxf(sqrtf(vo.x * vo.x + vo.y * vo.y + vo.z * vo.z),
+                                   sqrtf(vn.x * vn.x + vn.y * vn.y + vn.z * vn.z));
+            } else {
+                st(a.xB, i, Pi, 0.0);
+                a.v32B[i] = a.v32A[i];
+                a.w32B[i] = a.w32A[i];
+            }
+        }
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) vmax_local = fmaxf(vmax_local, __shfl_xor_sync(0xffffffffu, vmax_local, o));
+    if ((threadIdx.x & 31) == 0 && vmax_local > 0.0f) atomicMax(a.vmax_bits, __float_as_uint(vmax_local * 1.0001f));
+}
+
+// Scope-global objects (walls): fixed ones keep their state, orbital ones move with their
+// prescribed V and omega (DOOrbitalQuasiPlate.cpp:18-34).  Thread 0 also accumulates the
+// displacement bound of the step.
+__global__ void k_walls(uint32_t nglob, const uint32_t* __restrict__ glob, const uint32_t* __restrict__ model_of,
+                        const ModelDev* __restrict__ models, const double4_32a* __restrict__ xA,
+                        double4_32a* __restrict__ xB, const double4_32a* __restrict__ v64,
+                        const double4_32a* __restrict__ w64, const float4* __restrict__ v32A,
+                        float4* __restrict__ v32B, const float4* __restrict__ w32A, float4* __restrict__ w32B,
+                        double4_32a* __restrict__ ox, double4_32a* __restrict__ oz, double dt,
+                        unsigned* __restrict__ vmax_bits, float* __restrict__ disp_bound, float4* __restrict__ wall32) {
+    const uint32_t q = blockIdx.x * blockDim.x + threadIdx.x;
+    if (q == 0) {
+        *disp_bound += (float)dt * __uint_as_float(*vmax_bits);
+        *vmax_bits = 0u;
+    }
+    if (q >= nglob) return;
+    const uint32_t w = glob[q];
+    const ModelDev& M = models[model_of[w]];
+    d3 P = ld(xA, w);
+    if (M.behavior == BEH_ORBITAL) {
+        const d3 V = ld(v64, w), AV = ld(w64, w);
+        P = add(P, muls(V, dt));
+        const d3 dw = muls(AV, dt);
+        const d3 Ox = rotate_around(ld(ox, w), dw), Oz = rotate_around(ld(oz, w), dw);
+        st(ox, w, Ox, 0.0);
+        st(oz, w, Oz, 0.0);
+        const double lz = len(Oz), lx = len(Ox);
+        bool ok = lz > 0.0;
+        if (M.shape == SHAPE_PLATE) ok = ok && lx > 0.0 && fabs(dot(Ox, Oz)) <= 1e-9 * lx * lz;
+        wall32[w] = ok ? make_float4((float)(Oz.x / lz), (float)(Oz.y / lz), (float)(Oz.z / lz), 1.0f)
+                       : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+    }
+    st(xB, w, P, 0.0);
+    v32B[w] = v32A[w];
+    w32B[w] = w32A[w];
+}
+
+// ---- broad phase -------------------------------------------------------------------------
+__global__ void __launch_bounds__(TPB) k_bounds(uint32_t n, const uint32_t* __restrict__ model_of,
+                                                const ModelDev* __restrict__ models, const double4_32a* __restrict__ x,
+                                                d3 origin, float4* __restrict__ pos32, unsigned* __restrict__ red) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    // red: [0..2] min (ordered float bits), [3..5] max, [6] max radius
+    unsigned mn[3] = {0xffffffffu, 0xffffffffu, 0xffffffffu}, mx[3] = {0, 0, 0}, rm = 0;
+    if (i < n) {
+        const ModelDev& M = models[model_of[i]];
+        const d3 p = ld(x, i);
+        const float4 q = make_float4((float)(p.x - origin.x), (float)(p.y - origin.y), (float)(p.z - origin.z), 0.0f);
+        pos32[i] = q;
+        if (M.scope == SCOPE_LOCAL) {
+            auto ordf = [](float f) {
+                unsigned b = __float_as_uint(f);
+                return (b >> 31) ? ~b : (b | 0x80000000u);
+            };
+            mn[0] = mx[0] = ordf(q.x);
+            mn[1] = mx[1] = ordf(q.y);
+            mn[2] = mx[2] = ordf(q.z);
+            rm = __float_as_uint((float)M.range);
+        }
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+#pragma unroll
+        for (int k = 0; k < 3; ++k) {
+            mn[k] = min(mn[k], __shfl_xor_sync(0xffffffffu, mn[k], o));
+            mx[k] = max(mx[k], __shfl_xor_sync(0xffffffffu, mx[k], o));
+        }
+        rm = max(rm, __shfl_xor_sync(0xffffffffu, rm, o));
+    }
+    if ((threadIdx.x & 31) == 0) {
+        for (int k = 0; k < 3; ++k) {
+            atomicMin(&red[k], mn[k]);
+            atomicMax(&red[3 + k], mx[k]);
+        }
+        atomicMax(&red[6], rm);
+    }
+}
+
+__global__ void __launch_bounds__(TPB) k_keys(uint32_t n, const uint32_t* __restrict__ model_of,
+                                              const ModelDev* __restrict__ models, const float4* __restrict__ pos32,
+                                              float3 lo, float inv_h, uint32_t nx, uint32_t ny, uint32_t nz,
+                                              uint64_t sentinel, uint64_t* __restrict__ key, uint32_t* __restrict__ sid) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    uint64_t k = sentinel;
+    if (models[model_of[i]].scope == SCOPE_LOCAL) {
+        const float4 p = pos32[i];
+        const uint32_t cx = min((uint32_t)fmaxf((p.x - lo.x) * inv_h, 0.0f), nx - 1);
+        const uint32_t cy = min((uint32_t)fmaxf((p.y - lo.y) * inv_h, 0.0f), ny - 1);
+        const uint32_t cz = min((uint32_t)fmaxf((p.z - lo.z) * inv_h, 0.0f), nz - 1);
+        k = ((uint64_t)cx * ny + cy) * nz + cz;
+    }
+    key[i] = k;
+    sid[i] = i;
+}
+
+__global__ void __launch_bounds__(TPB) k_cells(uint32_t nloc, const uint64_t* __restrict__ key,
+                                               uint32_t* __restrict__ grid_start, uint32_t* __restrict__ grid_end) {
+    const uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= nloc) return;
+    const uint64_t k = key[p];
+    if (p == 0 || key[p - 1] != k) grid_start[k] = p;
+    if (p == nloc - 1 || key[p + 1] != k) grid_end[k] = p + 1;
+}
+
+// Full neighbour list of every local sphere: 27 cells in a fixed order, j ascending within a
+// cell, then the walls; candidate when the pair may come within reach + skin (conservative).
+template <bool FILL>
+__global__ void __launch_bounds__(TPB) k_nbr(uint32_t nloc, const uint32_t* __restrict__ sid,
+                                             const uint64_t* __restrict__ key, const uint32_t* __restrict__ grid_start,
+                                             const uint32_t* __restrict__ grid_end, uint32_t nx, uint32_t ny, uint32_t nz,
+                                             const uint32_t* __restrict__ glob, uint32_t nglob,
+                                             const uint32_t* __restrict__ model_of, const ModelDev* __restrict__ models,
+                                             const PairParam* __restrict__ params, const float* __restrict__ reach,
+                                             uint32_t nm, const float4* __restrict__ pos32,
+                                             const float4* __restrict__ wall32, float skin,
+                                             uint32_t* __restrict__ cnt_or_ptr, uint32_t* __restrict__ ent) {
+    const uint32_t P = blockIdx.x * blockDim.x + threadIdx.x;
+    if (P >= nloc) return;
+    const uint32_t i = sid[P];
+    const uint64_t k = key[P];
+    const uint32_t cz = (uint32_t)(k % nz), cy = (uint32_t)((k / nz) % ny), cx = (uint32_t)(k / ((uint64_t)nz * ny));
+    const uint32_t mi = model_of[i];
+    const float4 pi = pos32[i];
+    uint32_t c = 0;
+    uint32_t off = FILL ? cnt_or_ptr[i] : 0u;
+    for (int dx = -1; dx <= 1; ++dx) {
+        if ((dx < 0 && cx == 0) || (dx > 0 && cx + 1 >= nx)) continue;
+        for (int dy = -1; dy <= 1; ++dy) {
+            if ((dy < 0 && cy == 0) || (dy > 0 && cy + 1 >= ny)) continue;
+            for (int dz = -1; dz <= 1; ++dz) {
+                if ((dz < 0 && cz == 0) || (dz > 0 && cz + 1 >= nz)) continue;
+                const uint64_t nk = ((uint64_t)(cx + dx) * ny + (cy + dy)) * nz + (cz + dz);
+                const uint32_t b = grid_start[nk], e = grid_end[nk];
+                for (uint32_t q = b; q < e; ++q) {
+                    const uint32_t j = sid[q];
+                    if (j == i) continue;
+                    const uint32_t mj = model_of[j];
+                    const uint32_t pa = mi * nm + mj, pb = mj * nm + mi;
+                    if (params[pa].cd == 0 && params[pb].cd == 0) continue;
+                    const float r = fmaxf(reach[pa], reach[pb]);
+                    float err;
+                    const float d = dist32(pi, pos32[j], err);
+                    if (d - err > (r + skin) * (1.0f + 4.0f * PF_ARITH_EPS)) continue;
+                    if (FILL) ent[off + c] = j;
+                    ++c;
+                }
+            }
+        }
+    }
+    for (uint32_t q = 0; q < nglob; ++q) {
+        const uint32_t w = glob[q];
+        const uint32_t pw = mi * nm + model_of[w];
+        const int cd = params[pw].cd;
+        if (cd == 0) continue;
+        const float4 wl = wall32[w];
+        if (wl.w != 0.0f) {
+            float err;
+            const float d = cd == CD_SP ? plane_dist32(pi, pos32[w], wl, err) : line_dist32(pi, pos32[w], wl, err);
+            if (d - err > (reach[pw] + skin) * (1.0f + 4.0f * PF_ARITH_EPS)) continue;
+        }
+        if (FILL) ent[off + c] = w | WALL_BIT;
+        ++c;
+    }
+    if (!FILL) cnt_or_ptr[i] = c;
+}
+
+// History slot of every entry: the entry itself for the owner (lower index, or a wall
+// entry), else the owner's entry for the same pair in the neighbour's list.
+__global__ void __launch_bounds__(TPB) k_slots(uint32_t n, const uint32_t* __restrict__ ptr,
+                                               const uint32_t* __restrict__ ent, uint32_t* __restrict__ slot,
+                                               int* __restrict__ err) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    for (uint32_t e = ptr[i]; e < ptr[i + 1]; ++e) {
+        const uint32_t v = ent[e];
+        if ((v & WALL_BIT) || i < v) {
+            slot[e] = e;
+            continue;
+        }
+        const uint32_t j = v;
+        uint32_t found = 0xffffffffu;
+        for (uint32_t q = ptr[j]; q < ptr[j + 1]; ++q)
+            if (ent[q] == i) { found = q; break; }
+        if (found == 0xffffffffu) atomicOr(err, 1);
+        slot[e] = found == 0xffffffffu ? e : found;
+    }
+}
+
+// New owner entries take the status of the same pair in the old list (if it was listed).
+__global__ void __launch_bounds__(TPB) k_carry(uint32_t n, const uint32_t* __restrict__ ptr,
+                                               const uint32_t* __restrict__ ent, const uint32_t* __restrict__ slot,
+                                               const uint32_t* __restrict__ optr, const uint32_t* __restrict__ oent,
+                                               const uint32_t* __restrict__ oslot, const float4* __restrict__ oh,
+                                               const uint8_t* __restrict__ of, float4* __restrict__ h,
+                                               uint8_t* __restrict__ f, float4* __restrict__ h2,
+                                               uint8_t* __restrict__ f2, int have_old) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    for (uint32_t e = ptr[i]; e < ptr[i + 1]; ++e) {
+        if (slot[e] != e) continue;
+        const uint32_t v = ent[e];
+        float4 hv = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+        uint8_t fv = HF_LAST_CONTACT | HF_LAST_BOND;       // default-constructed ImpactStatus
+        if (have_old) {
+            for (uint32_t q = optr[i]; q < optr[i + 1]; ++q)
+                if (oent[q] == v) {
+                    const uint32_t os = oslot[q];
+                    hv = oh[os];
+                    fv = of[os] & (uint8_t)15;
+                    break;
+                }
+        }
+        h[e] = hv;
+        f[e] = fv;
+        h2[e] = hv;
+        f2[e] = fv;
+    }
+}
+
+// Wall entries of every sphere, in ascending entry order, keyed by the wall's global index.
+__global__ void __launch_bounds__(TPB) k_wall_count(uint32_t n, const uint32_t* __restrict__ ptr,
+                                                    const uint32_t* __restrict__ ent, uint32_t* __restrict__ cnt) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    uint32_t c = 0;
+    for (uint32_t e = ptr[i]; e < ptr[i + 1]; ++e) c += (ent[e] & WALL_BIT) ? 1u : 0u;
+    cnt[i] = c;
+}
+__global__ void __launch_bounds__(TPB) k_wall_fill(uint32_t n, const uint32_t* __restrict__ ptr,
+                                                   const uint32_t* __restrict__ ent, const uint32_t* __restrict__ off,
+                                                   const uint32_t* __restrict__ gidx, uint32_t* __restrict__ key,
+                                                   uint32_t* __restrict__ val) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    uint32_t o = off[i];
+    for (uint32_t e = ptr[i]; e < ptr[i + 1]; ++e)
+        if (ent[e] & WALL_BIT) {
+            key[o] = gidx[ent[e] & ~WALL_BIT];
+            val[o] = e;
+            ++o;
+        }
+}
+__global__ void __launch_bounds__(TPB) k_wall_ptr(uint32_t nglob, const uint32_t* __restrict__ key, uint32_t m,
+                                                  uint32_t* __restrict__ wptr) {
+    const uint32_t q = blockIdx.x * blockDim.x + threadIdx.x;
+    if (q > nglob) return;
+    uint32_t lo = 0, hi = m;
+    while (lo < hi) {
+        const uint32_t mid = (lo + hi) >> 1;
+        if (key[mid] < q) lo = mid + 1; else hi = mid;
+    }
+    wptr[q] = lo;
+}
+// One warp per wall: its contact impulses in entry order (ordered shuffle sum, FP64), plus the
+// field and external impulses, as DOStatus::GetImpact holds them after ClearImpact.
+__global__ void k_wall_sum(uint32_t nglob, const uint32_t* __restrict__ glob, const uint32_t* __restrict__ wptr,
+                           const uint32_t* __restrict__ wval, const float* __restrict__ wimp,
+                           const uint32_t* __restrict__ model_of, const ModelDev* __restrict__ models, double dt, d3 fimp,
+                           double4_32a* __restrict__ imp, double4_32a* __restrict__ aimp) {
+    const uint32_t q = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int lane = threadIdx.x & 31;
+    if (q >= nglob) return;
+    d3 J = mk(0.0, 0.0, 0.0), JA = mk(0.0, 0.0, 0.0);
+    for (uint32_t b = wptr[q]; b < wptr[q + 1]; b += 32) {
+        float v[6] = {0, 0, 0, 0, 0, 0};
+        if (b + lane < wptr[q + 1]) {
+            const float* o = wimp + 6 * (size_t)wval[b + lane];
+            for (int k = 0; k < 6; ++k) v[k] = o[k];
+        }
+        const uint32_t c = min(32u, wptr[q + 1] - b);
+        for (uint32_t l = 0; l < c; ++l) {
+            float x[6];
+            for (int k = 0; k < 6; ++k) x[k] = __shfl_sync(0xffffffffu, v[k], l);
+            J = add(J, mk(x[0], x[1], x[2]));
+            JA = add(JA, mk(x[3], x[4], x[5]));
+        }
+    }
+    if (lane == 0) {
+        const uint32_t w = glob[q];
+        const ModelDev& M = models[model_of[w]];
+        J = add(J, muls(fimp, M.sudo));
+        J = add(J, smul(dt, mk(M.ext[0], M.ext[1], M.ext[2])));
+        st(imp, w, J, 0.0);
+        st(aimp, w, JA, 0.0);
+    }
+}
+
+// Contact activity of every owner entry at the current positions (for queries).
+__global__ void __launch_bounds__(TPB) k_active(uint32_t n, TickArgs a, uint8_t* __restrict__ act) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const uint32_t mi = a.model_of[i];
+    for (uint32_t e = a.nptr[i]; e < a.nptr[i + 1]; ++e) {
+        act[e] = 0;
+        if (a.nslot[e] != e) continue;
+        const uint32_t ent = a.nent[e];
+        const uint32_t j = ent & ~WALL_BIT;
+        const bool wall = ent & WALL_BIT;
+        const uint32_t mj = a.model_of[j];
+        bool i_slave = true;
+        if (!wall) {
+            const ModelDev& M = a.models[mi];
+            const ModelDev& N = a.models[mj];
+            if (M.density == 0.0 && N.density != 0.0) i_slave = false;
+            else if (N.density == 0.0 && M.density != 0.0) i_slave = true;
+            else i_slave = i < j;
+        }
+        const uint32_t s = i_slave ? i : j, m = i_slave ? j : i;
+        const uint32_t pi = (i_slave ? mi : mj) * a.nm + (i_slave ? mj : mi);
+        const PairParam& P = a.params[pi];
+        if (P.cd == 0) continue;
+        const double4_32a gg = a.geom[pi];
+        const d3 Ps = ld(a.xA, s), Pm = ld(a.xA, m);
+        double depth;
+        if (P.cd == CD_SS) {
+            depth = __dsub_rn(__dadd_rn(gg.x, gg.y), xlen(xsub(Pm, Ps)));
+        } else {
+            d3 nd, pt;
+            depth = wall_detect(P.cd, gg.x, gg.y, gg.z, gg.w, Ps, Pm, ld(a.ox, m), ld(a.oz, m), nd, pt);
+        }
+        act[e] = depth > 0.0 ? PF_ACTIVE_BIT : 0;
+    }
+}
+
+__global__ void __launch_bounds__(TPB) k_pack3m(uint32_t n, const double* __restrict__ src, double4_32a* __restrict__ dst) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) dst[i] = make_double4_32a(src[3 * (size_t)i], src[3 * (size_t)i + 1], src[3 * (size_t)i + 2], 0.0);
+}
+__global__ void __launch_bounds__(TPB) k_unpack3m(uint32_t n, const double4_32a* __restrict__ src, double* __restrict__ dst) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) {
+        const double4_32a v = src[i];
+        dst[3 * (size_t)i] = v.x;
+        dst[3 * (size_t)i + 1] = v.y;
+        dst[3 * (size_t)i + 2] = v.z;
+    }
+}
+__global__ void __launch_bounds__(TPB) k_copy32(uint32_t n, const double4_32a* __restrict__ v, float4* __restrict__ o) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) {
+        const double4_32a q = v[i];
+        o[i] = make_float4((float)q.x, (float)q.y, (float)q.z, 0.0f);
+    }
+}
+__global__ void __launch_bounds__(TPB) k_wall32(uint32_t n, const uint32_t* __restrict__ model_of,
+                                                const ModelDev* __restrict__ models, const double4_32a* __restrict__ ox,
+                                                const double4_32a* __restrict__ oz, float4* __restrict__ wall32) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const ModelDev& M = models[model_of[i]];
+    if (M.shape == SHAPE_SPHERE) {
+        wall32[i] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+        return;
+    }
+    const d3 Ox = ld(ox, i), Oz = ld(oz, i);
+    const double lz = len(Oz), lx = len(Ox);
+    bool ok = lz > 0.0;
+    if (M.shape == SHAPE_PLATE) ok = ok && lx > 0.0 && fabs(dot(Ox, Oz)) <= 1e-9 * lx * lz;
+    wall32[i] = ok ? make_float4((float)(Oz.x / lz), (float)(Oz.y / lz), (float)(Oz.z / lz), 1.0f)
+                   : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+}
+
+}  // namespace
+
+// ==========================================================================================
+class MixedEngine : public EngineBase {
+public:
+    ~MixedEngine() override;
+    int init(const HScene& scene, const vedo_engine_opts& opts) override;
+    int run(uint32_t nsteps, int* keep_running) override;
+    int get_state(const vedo_state_view& v) override;
+    int set_state(const vedo_state_view& v) override;
+    int num_interactions(uint32_t* n) override;
+    int get_interactions(const vedo_contact_view& v) override;
+    int get_observables(double out[13]) override;
+    int write_ido(const char* path) override;
+    double time() const override { return t_; }
+    uint64_t steps() const override { return round_; }
+    uint32_t num_objects() const override { return n_; }
+    uint64_t last_profile(double out[4]) const override {
+        for (int k = 0; k < 4; ++k) out[k] = prof_[k];
+        return launches_;
+    }
+    void set_profiling(bool on) override { profiling_ = on; }
+    const std::string& error() const override { return err_; }
+
+private:
+    struct NList {
+        uint32_t cap = 0, ne = 0;
+        uint32_t* ptr = nullptr;   // [n+1]
+        uint32_t* ent = nullptr;
+        uint32_t* slot = nullptr;
+        float4* h[2] = {nullptr, nullptr};
+        uint8_t* f[2] = {nullptr, nullptr};
+    };
+    int fail(int c, const std::string& m) { err_ = m; return c; }
+    int cuda_fail(cudaError_t e, const char* where) {
+        err_ = std::string("CUDA error ") + cudaGetErrorString(e) + " at " + where;
+        return e == cudaErrorMemoryAllocation ? VEDO_ERR_OUT_OF_MEMORY : VEDO_ERR_CUDA;
+    }
+    int rebuild();
+    int ensure_nlist(NList& L, uint32_t cap);
+    void free_nlist(NList& L);
+    TickArgs args(bool write_imp);
+
+    HScene host_;
+    Tables tab_;
+    vedo_engine_opts opts_{};
+    std::string err_;
+    uint32_t n_ = 0, nm_ = 0, nloc_ = 0;
+    double dt_ = 0, t_ = 0, t_stop_ = 0, g_[3] = {0, 0, 0}, origin_[3] = {0, 0, 0};
+    float skin_abs_ = 0.0f;
+    uint64_t round_ = 0;
+    int cur_ = 0;                   // which of the A/B buffers is "A" (current)
+    bool need_rebuild_ = true;
+    bool profiling_ = false;
+    double prof_[4] = {0, 0, 0, 0};
+    uint64_t launches_ = 0;
+    uint64_t rebuilds_ = 0;
+    uint64_t since_rebuild_ = 0;
+    int law_ = 0;                   // the single equation type of the scene, or 0 (mixed laws)
+    cudaStream_t stream_ = nullptr;
+    cudaEvent_t ev_[4] = {};
+
+    ModelDev* d_models_ = nullptr;
+    PairParam* d_params_ = nullptr;
+    float* d_pc32_ = nullptr;
+    double4_32a* d_geom_ = nullptr;
+    double4_32a* d_rr_ = nullptr;
+    float4* d_mf_ = nullptr;
+    float* d_reach_ = nullptr;
+    uint32_t* d_model_of_ = nullptr;
+    uint32_t* d_glob_ = nullptr;
+    std::vector<uint32_t> glob_;
+    double4_32a* d_x_[2] = {nullptr, nullptr};
+    double4_32a *d_v64_ = nullptr, *d_w64_ = nullptr, *d_ox_ = nullptr, *d_oz_ = nullptr;
+    double4_32a *d_imp_ = nullptr, *d_aimp_ = nullptr;
+    float4* d_v32_[2] = {nullptr, nullptr};
+    float4* d_w32_[2] = {nullptr, nullptr};
+    float4 *d_pos32_ = nullptr, *d_wall32_ = nullptr;
+    unsigned* d_red_ = nullptr;     // [0..6] bounds, [8] vmax bits
+    float* d_disp_ = nullptr;
+    int* d_err_ = nullptr;
+    NList nl_[2];
+    int nlc_ = 0;                   // current neighbour list
+    Scratch scratch_;
+    uint64_t *d_key_ = nullptr, *d_key_alt_ = nullptr;
+    uint32_t *d_sid_ = nullptr, *d_sid_alt_ = nullptr, *d_cnt_ = nullptr;
+    uint32_t *d_gs_ = nullptr, *d_ge_ = nullptr;
+    uint64_t grid_cap_ = 0;
+    uint8_t* d_act_ = nullptr;
+    uint32_t act_cap_ = 0;
+    // wall impulse output: per-wall entry lists (rebuilt with the neighbour list) and the
+    // per-entry wall share written on output steps
+    uint32_t* d_gidx_ = nullptr;
+    uint32_t *d_wkey_ = nullptr, *d_wval_ = nullptr, *d_wkey_alt_ = nullptr, *d_wval_alt_ = nullptr, *d_wptr_ = nullptr;
+    uint32_t wcap_ = 0, nwall_ent_ = 0;
+    float* d_wimp_ = nullptr;
+    uint32_t wimp_cap_ = 0;
+    double* d_stage_ = nullptr;
+    double* d_obs_ = nullptr;
+};
+
+#define MCK(call)                                                 \
+    do {                                                          \
+        cudaError_t _e = (call);                                  \
+        if (_e != cudaSuccess) return cuda_fail(_e, #call);       \
+    } while (0)
+
+template <class T>
+static cudaError_t mal(T** p, size_t count) {
+    *p = nullptr;
+    return cudaMalloc((void**)p, sizeof(T) * (count ? count : 1));
+}
+
+void MixedEngine::free_nlist(NList& L) {
+    cudaFree(L.ptr); cudaFree(L.ent); cudaFree(L.slot);
+    for (int b = 0; b < 2; ++b) { cudaFree(L.h[b]); cudaFree(L.f[b]); }
+    L = NList{};
+}
+
+int MixedEngine::ensure_nlist(NList& L, uint32_t cap) {
+    if (!L.ptr) MCK(mal(&L.ptr, (size_t)n_ + 1));
+    if (cap <= L.cap && L.ent) return VEDO_OK;
+    uint32_t* ptr = L.ptr;
+    L.ptr = nullptr;
+    free_nlist(L);
+    L.ptr = ptr;
+    uint64_t c = std::max<uint64_t>(1024, (uint64_t)cap + cap / 4);
+    L.cap = (uint32_t)std::min<uint64_t>(c, 0x7fffffffull);
+    MCK(mal(&L.ent, L.cap));
+    MCK(mal(&L.slot, L.cap));
+    for (int b = 0; b < 2; ++b) {
+        MCK(mal(&L.h[b], L.cap));
+        MCK(mal(&L.f[b], L.cap));
+    }
+    return VEDO_OK;
+}
+
+MixedEngine::~MixedEngine() {
+    if (stream_) cudaStreamSynchronize(stream_);
+    free_nlist(nl_[0]);
+    free_nlist(nl_[1]);
+    void* ptrs[] = {d_models_, d_params_, d_pc32_, d_geom_, d_rr_, d_mf_, d_reach_, d_model_of_, d_glob_, d_x_[0], d_x_[1], d_v64_,
+                    d_w64_, d_ox_, d_oz_, d_imp_, d_aimp_, d_v32_[0], d_v32_[1], d_w32_[0], d_w32_[1], d_pos32_,
+                    d_wall32_, d_red_, d_disp_, d_err_, d_key_, d_key_alt_, d_sid_, d_sid_alt_, d_cnt_, d_gs_, d_ge_,
+                    d_act_, d_stage_, d_obs_, d_gidx_, d_wkey_, d_wval_, d_wkey_alt_, d_wval_alt_, d_wptr_,
+                    d_wimp_};
+    for (void* p : ptrs) if (p) cudaFree(p);
+    for (auto& e : ev_) if (e) cudaEventDestroy(e);
+    if (stream_) cudaStreamDestroy(stream_);
+}
+
+int MixedEngine::init(const HScene& scene, const vedo_engine_opts& opts) {
+    host_ = scene;
+    opts_ = opts;
+    std::string msg;
+    int rc = build_tables(host_, tab_, msg);
+    if (rc != VEDO_OK) return fail(rc, msg);
+    n_ = host_.n;
+    nm_ = (uint32_t)tab_.models.size();
+    dt_ = host_.time_interval;
+    t_ = host_.time_current;
+    t_stop_ = host_.time_stop;
+    for (int k = 0; k < 3; ++k) g_[k] = host_.g[k];
+    double rmax = 0.0;
+    for (uint32_t i = 0; i < n_; ++i) {
+        const ModelDev& M = tab_.models[host_.model_of[i]];
+        if (M.scope == SCOPE_LOCAL) {
+            if (M.shape != SHAPE_SPHERE)
+                return fail(VEDO_ERR_UNSUPPORTED_MODEL, "mixed form: local (scope) objects must be spheres");
+            rmax = std::max(rmax, M.a0);
+            ++nloc_;
+        } else {
+            if (M.behavior != BEH_FIXED && M.behavior != BEH_ORBITAL)
+                return fail(VEDO_ERR_UNSUPPORTED_MODEL, "mixed form: walls must be fixed or orbital");
+            glob_.push_back(i);
+        }
+    }
+    skin_abs_ = (float)((opts.skin > 0 ? opts.skin : 0.15f) * rmax);
+    if (opts_.check_interval == 0) opts_.check_interval = 10;
+    MCK(cudaSetDevice(opts.device));
+    MCK(cudaStreamCreateWithFlags(&stream_, cudaStreamNonBlocking));
+    for (auto& e : ev_) MCK(cudaEventCreate(&e));
+    MCK(mal(&d_models_, nm_));
+    MCK(cudaMemcpy(d_models_, tab_.models.data(), sizeof(ModelDev) * nm_, cudaMemcpyHostToDevice));
+    MCK(mal(&d_params_, (size_t)nm_ * nm_));
+    MCK(cudaMemcpy(d_params_, tab_.params.data(), sizeof(PairParam) * nm_ * nm_, cudaMemcpyHostToDevice));
+    std::vector<float> pc((size_t)nm_ * nm_ * 8);
+    std::vector<double4_32a> geo((size_t)nm_ * nm_);
+    std::vector<float> reach((size_t)nm_ * nm_);
+    for (size_t q = 0; q < geo.size(); ++q) {
+        for (int k = 0; k < 8; ++k) pc[8 * q + k] = (float)tab_.params[q].c[k];
+        const double* g = &tab_.geom[4 * q];
+        geo[q] = make_double4_32a(g[0], g[1], g[2], g[3]);
+        double r = 0.0;
+        if (tab_.params[q].cd == CD_SS) r = g[0] + g[1];
+        else if (tab_.params[q].cd == CD_SP) r = g[0] + 0.5 * g[2];
+        else if (tab_.params[q].cd == CD_SC) r = g[0] + g[1];
+        reach[q] = (float)r * (1.0f + 1e-6f);
+    }
+    {
+        int law = -1;
+        for (const PairParam& P : tab_.params)
+            if (P.cd) law = (law == -1 || law == P.is) ? P.is : 0;
+        law_ = law < 0 ? 0 : law;
+    }
+    MCK(mal(&d_pc32_, pc.size()));
+    MCK(cudaMemcpy(d_pc32_, pc.data(), 4 * pc.size(), cudaMemcpyHostToDevice));
+    MCK(mal(&d_geom_, geo.size()));
+    MCK(cudaMemcpy(d_geom_, geo.data(), sizeof(double4_32a) * geo.size(), cudaMemcpyHostToDevice));
+    MCK(mal(&d_reach_, reach.size()));
+    MCK(cudaMemcpy(d_reach_, reach.data(), 4 * reach.size(), cudaMemcpyHostToDevice));
+    {
+        std::vector<double4_32a> rr(geo.size());
+        for (size_t q = 0; q < geo.size(); ++q) {
+            const double R = tab_.geom[4 * q] + tab_.geom[4 * q + 1];
+            rr[q] = make_double4_32a(R, R * R, 1e-9 * R * R, 0.0);
+        }
+        MCK(mal(&d_rr_, rr.size()));
+        MCK(cudaMemcpy(d_rr_, rr.data(), sizeof(double4_32a) * rr.size(), cudaMemcpyHostToDevice));
+        std::vector<float4> mf(2 * (size_t)nm_);
+        for (uint32_t k = 0; k < nm_; ++k) {
+            const ModelDev& M = tab_.models[k];
+            double gi[3];
+            for (int q = 0; q < 3; ++q) gi[q] = host_.g[q] * dt_ * M.sudo + dt_ * M.ext[q];
+            mf[2 * k] = make_float4((float)gi[0], (float)gi[1], (float)gi[2], (float)M.inv_sudo);
+            mf[2 * k + 1] = make_float4((float)M.rot_coef, 0.0f, 0.0f, 0.0f);
+        }
+        MCK(mal(&d_mf_, mf.size()));
+        MCK(cudaMemcpy(d_mf_, mf.data(), sizeof(float4) * mf.size(), cudaMemcpyHostToDevice));
+    }
+    MCK(mal(&d_model_of_, n_));
+    MCK(cudaMemcpy(d_model_of_, host_.model_of.data(), 4 * n_, cudaMemcpyHostToDevice));
+    MCK(mal(&d_glob_, glob_.size()));
+    if (!glob_.empty()) MCK(cudaMemcpy(d_glob_, glob_.data(), 4 * glob_.size(), cudaMemcpyHostToDevice));
+    {
+        std::vector<uint32_t> gidx(n_, 0xffffffffu);
+        for (uint32_t q = 0; q < glob_.size(); ++q) gidx[glob_[q]] = q;
+        MCK(mal(&d_gidx_, n_));
+        MCK(cudaMemcpy(d_gidx_, gidx.data(), 4 * n_, cudaMemcpyHostToDevice));
+        MCK(mal(&d_wptr_, glob_.size() + 1));
+    }
+    for (int b = 0; b < 2; ++b) {
+        MCK(mal(&d_x_[b], n_));
+        MCK(mal(&d_v32_[b], n_));
+        MCK(mal(&d_w32_[b], n_));
+    }
+    MCK(mal(&d_v64_, n_)); MCK(mal(&d_w64_, n_)); MCK(mal(&d_ox_, n_)); MCK(mal(&d_oz_, n_));
+    MCK(mal(&d_imp_, n_)); MCK(mal(&d_aimp_, n_)); MCK(mal(&d_pos32_, n_)); MCK(mal(&d_wall32_, n_));
+    MCK(mal(&d_red_, 16)); MCK(mal(&d_disp_, 1)); MCK(mal(&d_err_, 1));
+    MCK(mal(&d_key_, n_)); MCK(mal(&d_key_alt_, n_)); MCK(mal(&d_sid_, n_)); MCK(mal(&d_sid_alt_, n_));
+    MCK(mal(&d_cnt_, (size_t)n_ + 1));
+    MCK(mal(&d_stage_, 7 * 3 * (size_t)n_));
+    MCK(mal(&d_obs_, (size_t)(nblk(n_) + 2) * 16 + 64));
+    MCK(cudaMemset(d_red_, 0, 64));
+    MCK(cudaMemset(d_disp_, 0, 4));
+    // bounding box centre as FP32 origin
+    double lo[3] = {DBL_MAX, DBL_MAX, DBL_MAX}, hi[3] = {-DBL_MAX, -DBL_MAX, -DBL_MAX};
+    for (uint32_t i = 0; i < n_; ++i)
+        for (int k = 0; k < 3; ++k) {
+            lo[k] = std::min(lo[k], host_.pos[3 * i + k]);
+            hi[k] = std::max(hi[k], host_.pos[3 * i + k]);
+        }
+    for (int k = 0; k < 3; ++k) origin_[k] = 0.5 * (lo[k] + hi[k]);
+    vedo_state_view v{host_.pos.data(), host_.vel.data(), host_.av.data(), host_.ox.data(), host_.oz.data(),
+                      host_.imp.data(), host_.aimp.data()};
+    rc = set_state(v);
+    if (rc != VEDO_OK) return rc;
+    // history from the scene's records: carried into the first list by key
+    // (IactRecordTab::GetImpactStatus); stored temporarily as an "old list" of owner entries.
+    if (host_.rec.size()) {
+        std::vector<std::vector<std::pair<uint32_t, uint32_t>>> per(n_);
+        for (uint32_t q = 0; q < host_.rec.size(); ++q) {
+            uint32_t a = host_.rec.first[q], b = host_.rec.second[q];
+            if (a >= n_ || b >= n_) continue;
+            const bool bw = tab_.models[host_.model_of[b]].scope != SCOPE_LOCAL;
+            const bool aw = tab_.models[host_.model_of[a]].scope != SCOPE_LOCAL;
+            if (aw && !bw) std::swap(a, b);     // wall pairs are owned by the sphere
+            per[a].push_back({bw || aw ? (b | WALL_BIT) : b, q});
+        }
+        std::vector<uint32_t> optr(n_ + 1, 0), oent, oslot;
+        std::vector<float4> oh;
+        std::vector<uint8_t> of;
+        for (uint32_t i = 0; i < n_; ++i) {
+            optr[i] = (uint32_t)oent.size();
+            for (auto& pq : per[i]) {
+                const uint32_t q = pq.second;
+                oslot.push_back((uint32_t)oent.size());
+                oent.push_back(pq.first);
+                oh.push_back(make_float4((float)host_.rec.shear[3 * q], (float)host_.rec.shear[3 * q + 1],
+                                         (float)host_.rec.shear[3 * q + 2], (float)host_.rec.kn[q]));
+                of.push_back((uint8_t)(HF_LAST_CONTACT | HF_LAST_BOND | (host_.rec.contact[q] ? HF_CONTACT : 0) |
+                                       (host_.rec.bond[q] ? HF_BOND : 0)));
+            }
+        }
+        optr[n_] = (uint32_t)oent.size();
+        NList& O = nl_[1];
+        rc = ensure_nlist(O, (uint32_t)oent.size());
+        if (rc != VEDO_OK) return rc;
+        O.ne = (uint32_t)oent.size();
+        MCK(cudaMemcpy(O.ptr, optr.data(), 4 * (n_ + 1), cudaMemcpyHostToDevice));
+        MCK(cudaMemcpy(O.ent, oent.data(), 4 * oent.size(), cudaMemcpyHostToDevice));
+        MCK(cudaMemcpy(O.slot, oslot.data(), 4 * oslot.size(), cudaMemcpyHostToDevice));
+        MCK(cudaMemcpy(O.h[cur_], oh.data(), sizeof(float4) * oh.size(), cudaMemcpyHostToDevice));
+        MCK(cudaMemcpy(O.f[cur_], of.data(), of.size(), cudaMemcpyHostToDevice));
+        nlc_ = 1;   // the records play the role of the previous list
+    }
+    rc = rebuild();
+    if (rc != VEDO_OK) return rc;
+    MCK(cudaStreamSynchronize(stream_));
+    return VEDO_OK;
+}
+
+TickArgs MixedEngine::args(bool write_imp) {
+    NList& L = nl_[nlc_];
+    TickArgs a;
+    a.n = n_;
+    a.nm = nm_;
+    a.model_of = d_model_of_;
+    a.models = d_models_;
+    a.params = d_params_;
+    a.pc32 = d_pc32_;
+    a.geom = d_geom_;
+    a.xA = d_x_[cur_];
+    a.xB = d_x_[cur_ ^ 1];
+    a.v64 = d_v64_;
+    a.w64 = d_w64_;
+    a.v32A = d_v32_[cur_];
+    a.v32B = d_v32_[cur_ ^ 1];
+    a.w32A = d_w32_[cur_];
+    a.w32B = d_w32_[cur_ ^ 1];
+    a.ox = d_ox_;
+    a.oz = d_oz_;
+    a.nptr = L.ptr;
+    a.nent = L.ent;
+    a.nslot = L.slot;
+    a.hA = L.h[cur_];
+    a.hB = L.h[cur_ ^ 1];
+    a.fA = L.f[cur_];
+    a.fB = L.f[cur_ ^ 1];
+    a.imp = d_imp_;
+    a.aimp = d_aimp_;
+    a.write_imp = write_imp ? 1 : 0;
+    a.dt = dt_;
+    a.fimp = muls(mk(g_[0], g_[1], g_[2]), dt_);
+    a.vmax_bits = d_red_ + 8;
+    a.pos32 = d_pos32_;
+    a.disp = d_disp_;
+    a.reach = d_reach_;
+    a.wall32 = d_wall32_;
+    a.wimp = d_wimp_;
+    a.rr = d_rr_;
+    a.mf = d_mf_;
+    return a;
+}
+
+int MixedEngine::rebuild() {
+    const uint64_t l0 = g_sort_scan_launches;
+    uint64_t own = 0;
+    const d3 org = mk(origin_[0], origin_[1], origin_[2]);
+    unsigned red0[8] = {0xffffffffu, 0xffffffffu, 0xffffffffu, 0, 0, 0, 0, 0};
+    MCK(cudaMemcpyAsync(d_red_, red0, sizeof(red0), cudaMemcpyHostToDevice, stream_));
+    k_bounds<<<nblk(n_), TPB, 0, stream_>>>(n_, d_model_of_, d_models_, d_x_[cur_], org, d_pos32_, d_red_);
+    k_wall32<<<nblk(n_), TPB, 0, stream_>>>(n_, d_model_of_, d_models_, d_ox_, d_oz_, d_wall32_);
+    own += 2;
+    unsigned red[8];
+    MCK(cudaMemcpyAsync(red, d_red_, sizeof(red), cudaMemcpyDeviceToHost, stream_));
+    MCK(cudaStreamSynchronize(stream_));
+    auto unord = [](unsigned o) {
+        unsigned b = (o >> 31) ? (o & 0x7fffffffu) : ~o;
+        float f;
+        memcpy(&f, &b, 4);
+        return f;
+    };
+    float lo[3], hi[3];
+    for (int k = 0; k < 3; ++k) {
+        lo[k] = nloc_ ? unord(red[k]) : 0.0f;
+        hi[k] = nloc_ ? unord(red[3 + k]) : 0.0f;
+    }
+    float rmax;
+    memcpy(&rmax, &red[6], 4);
+    float h = (2.0f * rmax + skin_abs_) * (1.0f + 1e-5f);
+    uint32_t nc[3];
+    uint64_t cells = 0;
+    const uint64_t cell_budget = std::max<uint64_t>(8ull * n_, 1ull << 22);
+    for (int pass = 0; pass < 8; ++pass) {
+        for (int k = 0; k < 3; ++k) nc[k] = std::max<uint32_t>(1, (uint32_t)std::floor((hi[k] - lo[k]) / h) + 1);
+        cells = (uint64_t)nc[0] * nc[1] * nc[2];
+        if (cells <= cell_budget) break;
+        // sparse scene: a coarser grid still finds every neighbour within one cell
+        h *= (float)std::cbrt((double)cells / cell_budget) * 1.01f;
+    }
+    if (cells > grid_cap_) {
+        if (d_gs_) cudaFree(d_gs_);
+        if (d_ge_) cudaFree(d_ge_);
+        grid_cap_ = cells + cells / 4;
+        MCK(mal(&d_gs_, grid_cap_));
+        MCK(mal(&d_ge_, grid_cap_));
+    }
+    MCK(cudaMemsetAsync(d_gs_, 0, 4 * cells, stream_));
+    MCK(cudaMemsetAsync(d_ge_, 0, 4 * cells, stream_));
+    k_keys<<<nblk(n_), TPB, 0, stream_>>>(n_, d_model_of_, d_models_, d_pos32_, make_float3(lo[0], lo[1], lo[2]),
+                                          1.0f / h, nc[0], nc[1], nc[2], cells, d_key_, d_sid_);
+    ++own;
+    int bits = 1;
+    while (bits < 64 && (cells >> bits)) ++bits;
+    MCK(radix_sort_u64(d_key_, d_sid_, d_key_alt_, d_sid_alt_, n_, 0, bits, scratch_, stream_));
+    if (nloc_) {
+        k_cells<<<nblk(nloc_), TPB, 0, stream_>>>(nloc_, d_key_, d_gs_, d_ge_);
+        ++own;
+    }
+    // count, scan, fill
+    const int newl = nlc_ ^ 1;
+    NList& L = nl_[newl];
+    NList& O = nl_[nlc_];
+    if (!L.ptr) MCK(mal(&L.ptr, (size_t)n_ + 1));
+    MCK(cudaMemsetAsync(d_cnt_, 0, 4 * ((size_t)n_ + 1), stream_));
+    if (nloc_) {
+        k_nbr<false><<<nblk(nloc_), TPB, 0, stream_>>>(nloc_, d_sid_, d_key_, d_gs_, d_ge_, nc[0], nc[1], nc[2],
+                                                       d_glob_, (uint32_t)glob_.size(), d_model_of_, d_models_,
+                                                       d_params_, d_reach_, nm_, d_pos32_, d_wall32_, skin_abs_,
+                                                       d_cnt_, nullptr);
+        ++own;
+    }
+    MCK(exclusive_scan_u32(d_cnt_, L.ptr, n_ + 1, d_red_ + 9, scratch_, stream_));
+    uint32_t ne = 0;
+    MCK(cudaMemcpyAsync(&ne, d_red_ + 9, 4, cudaMemcpyDeviceToHost, stream_));
+    MCK(cudaStreamSynchronize(stream_));
+    int rc = ensure_nlist(L, ne);
+    if (rc != VEDO_OK) return rc;
+    L.ne = ne;
+    if (nloc_) {
+        k_nbr<true><<<nblk(nloc_), TPB, 0, stream_>>>(nloc_, d_sid_, d_key_, d_gs_, d_ge_, nc[0], nc[1], nc[2], d_glob_,
+                                                      (uint32_t)glob_.size(), d_model_of_, d_models_, d_params_,
+                                                      d_reach_, nm_, d_pos32_, d_wall32_, skin_abs_, L.ptr, L.ent);
+        ++own;
+    }
+    MCK(cudaMemsetAsync(d_err_, 0, 4, stream_));
+    k_slots<<<nblk(n_), TPB, 0, stream_>>>(n_, L.ptr, L.ent, L.slot, d_err_);
+    k_carry<<<nblk(n_), TPB, 0, stream_>>>(n_, L.ptr, L.ent, L.slot, O.ptr, O.ent, O.slot, O.h[cur_], O.f[cur_],
+                                           L.h[cur_], L.f[cur_], L.h[cur_ ^ 1], L.f[cur_ ^ 1],
+                                           O.ent != nullptr ? 1 : 0);
+    own += 2;
+    // per-wall entry lists for the wall impulse output
+    if (!glob_.empty()) {
+        k_wall_count<<<nblk(n_), TPB, 0, stream_>>>(n_, L.ptr, L.ent, d_cnt_);
+        MCK(exclusive_scan_u32(d_cnt_, d_cnt_, n_ + 1, d_red_ + 10, scratch_, stream_));
+        uint32_t nw = 0;
+        MCK(cudaMemcpyAsync(&nw, d_red_ + 10, 4, cudaMemcpyDeviceToHost, stream_));
+        MCK(cudaStreamSynchronize(stream_));
+        if (nw > wcap_) {
+            for (uint32_t** p : {&d_wkey_, &d_wval_, &d_wkey_alt_, &d_wval_alt_}) {
+                if (*p) cudaFree(*p);
+                *p = nullptr;
+            }
+            wcap_ = nw + nw / 4 + 64;
+            MCK(mal(&d_wkey_, wcap_)); MCK(mal(&d_wval_, wcap_)); MCK(mal(&d_wkey_alt_, wcap_)); MCK(mal(&d_wval_alt_, wcap_));
+        }
+        nwall_ent_ = nw;
+        k_wall_fill<<<nblk(n_), TPB, 0, stream_>>>(n_, L.ptr, L.ent, d_cnt_, d_gidx_, d_wkey_, d_wval_);
+        int wb = 1;
+        while (wb < 32 && (((uint32_t)glob_.size() - 1) >> wb)) ++wb;
+        MCK(radix_sort_u32(d_wkey_, d_wval_, d_wkey_alt_, d_wval_alt_, nw, 0, wb, scratch_, stream_));
+        k_wall_ptr<<<nblk(glob_.size() + 1), TPB, 0, stream_>>>((uint32_t)glob_.size(), d_wkey_, nw, d_wptr_);
+        own += 3;
+        if (6ull * ne > wimp_cap_) {
+            if (d_wimp_) cudaFree(d_wimp_);
+            wimp_cap_ = (uint32_t)std::min<uint64_t>(6ull * (ne + ne / 4 + 64), 0xffffffffull);
+            MCK(mal(&d_wimp_, wimp_cap_));
+        }
+    }
+    int herr = 0;
+    MCK(cudaMemcpyAsync(&herr, d_err_, 4, cudaMemcpyDeviceToHost, stream_));
+    MCK(cudaMemsetAsync(d_disp_, 0, 4, stream_));
+    MCK(cudaStreamSynchronize(stream_));
+    MCK(cudaGetLastError());
+    if (herr) return fail(VEDO_ERR_CUDA, "mixed form: asymmetric neighbour lists");
+    nlc_ = newl;
+    need_rebuild_ = false;
+    since_rebuild_ = 0;
+    ++rebuilds_;
+    launches_ += own + (g_sort_scan_launches - l0);
+    return VEDO_OK;
+}
+
+int MixedEngine::run(uint32_t nsteps, int* keep_running) {
+    prof_[0] = prof_[1] = prof_[2] = prof_[3] = 0;
+    launches_ = 0;
+    MCK(cudaSetDevice(opts_.device));
+    MCK(cudaEventRecord(ev_[0], stream_));
+    const float half_skin = 0.5f * skin_abs_;
+    for (uint32_t s = 0; s < nsteps; ++s) {
+        if (need_rebuild_) {
+            int rc = rebuild();
+            if (rc != VEDO_OK) return rc;
+        }
+        TickArgs a = args(s + 1 == nsteps);
+        switch (law_) {
+        case IS_BSDBF: k_tick<IS_BSDBF><<<nblk(n_), TPB, 0, stream_>>>(a); break;
+        case IS_BTSDBF: k_tick<IS_BTSDBF><<<nblk(n_), TPB, 0, stream_>>>(a); break;
+        case IS_BSDB2F: k_tick<IS_BSDB2F><<<nblk(n_), TPB, 0, stream_>>>(a); break;
+        case IS_HERTZ: k_tick<IS_HERTZ><<<nblk(n_), TPB, 0, stream_>>>(a); break;
+        case IS_H: k_tick<IS_H><<<nblk(n_), TPB, 0, stream_>>>(a); break;
+        default: k_tick<0><<<nblk(n_), TPB, 0, stream_>>>(a); break;
+        }
+        ++launches_;
+        if (a.write_imp && !glob_.empty()) {
+            k_wall_sum<<<nblk((uint64_t)glob_.size() * 32), TPB, 0, stream_>>>(
+                (uint32_t)glob_.size(), d_glob_, d_wptr_, d_wval_, d_wimp_, d_model_of_, d_models_, dt_, a.fimp,
+                d_imp_, d_aimp_);
+            ++launches_;
+        }
+        // walls move; thread 0 also adds dt * max|v| of the step to the displacement bound
+        k_walls<<<nblk(std::max<size_t>(glob_.size(), 1)), TPB, 0, stream_>>>(
+            (uint32_t)glob_.size(), d_glob_, d_model_of_, d_models_, a.xA, a.xB, d_v64_, d_w64_, a.v32A, a.v32B,
+            a.w32A, a.w32B, d_ox_, d_oz_, dt_, d_red_ + 8, d_disp_, d_wall32_);
+        ++launches_;
+        cur_ ^= 1;
+        ++round_;
+        ++since_rebuild_;
+        t_ += dt_;
+        if (since_rebuild_ % opts_.check_interval == 0) {
+            // Rebuild before any sphere can have moved half the skin: the bound so far plus
+            // twice its mean growth per step over the next check interval.
+            float disp = 0.0f;
+            MCK(cudaMemcpyAsync(&disp, d_disp_, 4, cudaMemcpyDeviceToHost, stream_));
+            MCK(cudaStreamSynchronize(stream_));
+            const float growth = disp / (float)since_rebuild_;
+            if (disp + 2.0f * growth * (float)opts_.check_interval > half_skin) need_rebuild_ = true;
+        }
+    }
+    MCK(cudaEventRecord(ev_[1], stream_));
+    MCK(cudaStreamSynchronize(stream_));
+    MCK(cudaGetLastError());
+    float ms = 0;
+    cudaEventElapsedTime(&ms, ev_[0], ev_[1]);
+    prof_[3] = ms;
+    if (keep_running) *keep_running = t_ < t_stop_ ? 1 : 0;
+    return VEDO_OK;
+}
+
+int MixedEngine::get_state(const vedo_state_view& v) {
+    double* dst[] = {v.position, v.velocity, v.angular_velocity, v.orientation_x, v.orientation_z, v.impact,
+                     v.angular_impact};
+    const double4_32a* src[] = {d_x_[cur_], d_v64_, d_w64_, d_ox_, d_oz_, d_imp_, d_aimp_};
+    for (int k = 0; k < 7; ++k) {
+        if (!dst[k]) continue;
+        double* st = d_stage_ + (size_t)k * 3 * n_;
+        k_unpack3m<<<nblk(n_), TPB, 0, stream_>>>(n_, src[k], st);
+        MCK(cudaMemcpyAsync(dst[k], st, 24 * (size_t)n_, cudaMemcpyDeviceToHost, stream_));
+    }
+    MCK(cudaStreamSynchronize(stream_));
+    MCK(cudaGetLastError());
+    return VEDO_OK;
+}
+
+int MixedEngine::set_state(const vedo_state_view& v) {
+    const double* srcs[] = {v.position, v.velocity, v.angular_velocity, v.orientation_x, v.orientation_z, v.impact,
+                            v.angular_impact};
+    double4_32a* dst[] = {d_x_[cur_], d_v64_, d_w64_, d_ox_, d_oz_, d_imp_, d_aimp_};
+    for (int k = 0; k < 7; ++k) {
+        if (!srcs[k]) continue;
+        double* st = d_stage_ + (size_t)k * 3 * n_;
+        MCK(cudaMemcpyAsync(st, srcs[k], 24 * (size_t)n_, cudaMemcpyHostToDevice, stream_));
+        k_pack3m<<<nblk(n_), TPB, 0, stream_>>>(n_, st, dst[k]);
+    }
+    k_copy32<<<nblk(n_), TPB, 0, stream_>>>(n_, d_v64_, d_v32_[cur_]);
+    k_copy32<<<nblk(n_), TPB, 0, stream_>>>(n_, d_w64_, d_w32_[cur_]);
+    MCK(cudaStreamSynchronize(stream_));
+    MCK(cudaGetLastError());
+    need_rebuild_ = true;
+    return VEDO_OK;
+}
+
+int MixedEngine::num_interactions(uint32_t* n) {
+    if (need_rebuild_) {
+        int rc = rebuild();
+        if (rc != VEDO_OK) return rc;
+    }
+    // owner entries only
+    NList& L = nl_[nlc_];
+    std::vector<uint32_t> slot(L.ne);
+    if (L.ne) {
+        MCK(cudaMemcpy(slot.data(), L.slot, 4 * L.ne, cudaMemcpyDeviceToHost));
+    }
+    uint32_t c = 0;
+    for (uint32_t e = 0; e < L.ne; ++e) c += slot[e] == e;
+    *n = c;
+    return VEDO_OK;
+}
+
+int MixedEngine::get_interactions(const vedo_contact_view& v) {
+    if (need_rebuild_) {
+        int rc = rebuild();
+        if (rc != VEDO_OK) return rc;
+    }
+    NList& L = nl_[nlc_];
+    const uint32_t ne = L.ne;
+    if (ne > act_cap_) {
+        if (d_act_) cudaFree(d_act_);
+        act_cap_ = ne + ne / 4 + 16;
+        MCK(mal(&d_act_, act_cap_));
+    }
+    if (ne) {
+        k_active<<<nblk(n_), TPB, 0, stream_>>>(n_, args(false), d_act_);
+    }
+    std::vector<uint32_t> ptr(n_ + 1), ent(ne), slot(ne);
+    std::vector<uint8_t> act(ne), fl(ne);
+    std::vector<float4> h(ne);
+    MCK(cudaMemcpyAsync(ptr.data(), L.ptr, 4 * (n_ + 1), cudaMemcpyDeviceToHost, stream_));
+    if (ne) {
+        MCK(cudaMemcpyAsync(ent.data(), L.ent, 4 * ne, cudaMemcpyDeviceToHost, stream_));
+        MCK(cudaMemcpyAsync(slot.data(), L.slot, 4 * ne, cudaMemcpyDeviceToHost, stream_));
+        MCK(cudaMemcpyAsync(act.data(), d_act_, ne, cudaMemcpyDeviceToHost, stream_));
+        MCK(cudaMemcpyAsync(fl.data(), L.f[cur_], ne, cudaMemcpyDeviceToHost, stream_));
+        MCK(cudaMemcpyAsync(h.data(), L.h[cur_], sizeof(float4) * ne, cudaMemcpyDeviceToHost, stream_));
+    }
+    MCK(cudaStreamSynchronize(stream_));
+    // owner entries sorted by (first, second)
+    struct Row { uint32_t a, b, sl, ms; uint32_t e; };
+    std::vector<Row> rows;
+    for (uint32_t i = 0; i < n_; ++i)
+        for (uint32_t e = ptr[i]; e < ptr[i + 1]; ++e) {
+            if (slot[e] != e) continue;
+            const uint32_t j = ent[e] & ~WALL_BIT;
+            const bool wall = ent[e] & WALL_BIT;
+            Row r;
+            r.a = std::min(i, j);
+            r.b = std::max(i, j);
+            r.sl = wall ? i : std::min(i, j);
+            r.ms = wall ? j : std::max(i, j);
+            r.e = e;
+            rows.push_back(r);
+        }
+    std::sort(rows.begin(), rows.end(), [](const Row& x, const Row& y) { return x.a != y.a ? x.a < y.a : x.b < y.b; });
+    for (size_t k = 0; k < rows.size(); ++k) {
+        const Row& r = rows[k];
+        if (v.first) v.first[k] = r.a;
+        if (v.second) v.second[k] = r.b;
+        if (v.slave) v.slave[k] = r.sl;
+        if (v.master) v.master[k] = r.ms;
+        if (v.active) v.active[k] = act[r.e] ? 1 : 0;
+        if (v.contact) v.contact[k] = (fl[r.e] & HF_CONTACT) ? 1 : 0;
+        if (v.kn) v.kn[k] = h[r.e].w;
+        if (v.shear) {
+            v.shear[3 * k] = h[r.e].x;
+            v.shear[3 * k + 1] = h[r.e].y;
+            v.shear[3 * k + 2] = h[r.e].z;
+        }
+    }
+    return VEDO_OK;
+}
+
+int MixedEngine::get_observables(double out[13]) {
+    NList& L = nl_[nlc_];
+    if (L.ne > act_cap_) {
+        if (d_act_) cudaFree(d_act_);
+        act_cap_ = L.ne + L.ne / 4 + 16;
+        MCK(mal(&d_act_, act_cap_));
+    }
+    if (L.ne) k_active<<<nblk(n_), TPB, 0, stream_>>>(n_, args(false), d_act_);
+    const unsigned nb = std::max(1u, nblk(n_));
+    double* part = d_obs_;
+    double* res = d_obs_ + (size_t)nb * 16 + 16;
+    const d3 g = mk(g_[0], g_[1], g_[2]);
+    obs::k_obs_a<<<nb, TPB, 0, stream_>>>(n_, d_model_of_, d_models_, d_x_[cur_], d_v64_, d_w64_, g, part);
+    obs::k_obs_reduce<<<1, 32, 0, stream_>>>(nb, 16, part, res, 12);
+    obs::k_obs_b<<<nb, TPB, 0, stream_>>>(n_, d_model_of_, d_models_, d_x_[cur_], d_v64_, d_w64_, res, 0, d_act_,
+                                          L.ne, part);
+    obs::k_obs_reduce<<<1, 32, 0, stream_>>>(nb, 6, part, res + 16, 6);
+    double r[22];
+    MCK(cudaMemcpyAsync(r, res, sizeof(r), cudaMemcpyDeviceToHost, stream_));
+    MCK(cudaStreamSynchronize(stream_));
+    const bool any = r[9] > 0;
+    out[0] = r[0]; out[1] = r[1]; out[2] = r[2];
+    out[3] = any ? r[12] : 0.0; out[4] = any ? r[13] : 0.0; out[5] = any ? r[14] : 0.0; out[6] = any ? r[15] : 0.0;
+    out[7] = r[16]; out[8] = r[17]; out[9] = r[21];
+    const double msum = r[10];
+    out[10] = msum > 0 ? r[18] / msum : 0.0;
+    out[11] = msum > 0 ? r[19] / msum : 0.0;
+    out[12] = msum > 0 ? r[20] / msum : 0.0;
+    return VEDO_OK;
+}
+
+int MixedEngine::write_ido(const char* path) {
+    vedo_state_view v{host_.pos.data(), host_.vel.data(), host_.av.data(), host_.ox.data(), host_.oz.data(),
+                      host_.imp.data(), host_.aimp.data()};
+    int rc = get_state(v);
+    if (rc != VEDO_OK) return rc;
+    host_.time_current = t_;
+    uint32_t np = 0;
+    rc = num_interactions(&np);
+    if (rc != VEDO_OK) return rc;
+    std::vector<uint32_t> a(np), b(np);
+    std::vector<uint8_t> act(np), con(np);
+    std::vector<double> sh(3 * (size_t)np), kn(np);
+    vedo_contact_view cv{a.data(), b.data(), nullptr, nullptr, act.data(), sh.data(), kn.data(), con.data()};
+    rc = get_interactions(cv);
+    if (rc != VEDO_OK) return rc;
+    HRecords R;
+    for (uint32_t k = 0; k < np; ++k) {
+        if (!act[k]) continue;
+        R.first.push_back(a[k]); R.second.push_back(b[k]);
+        R.contact.push_back(con[k]); R.bond.push_back(0);
+        R.kn.push_back(kn[k]); R.v0.push_back(0.0);
+        for (int q = 0; q < 3; ++q) {
+            R.shear.push_back(sh[3 * k + q]);
+            R.point.push_back(0.0); R.dirn.push_back(0.0); R.imp.push_back(0.0); R.aimp.push_back(0.0);
+        }
+        R.overlap.push_back(0.0);
+    }
+    HScene s = host_;
+    s.rec = R;
+    std::string msg;
+    if (!vedo::write_ido(path, s, msg)) return fail(VEDO_ERR_IO, msg);
+    return VEDO_OK;
+}
+
+EngineBase* make_mixed_engine() { return new (std::nothrow) MixedEngine(); }
+
+}  // namespace vedo

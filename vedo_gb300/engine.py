@@ -78,11 +78,16 @@ class GpuEngine:
     """
 
     def __init__(self, scene, up_iact: int = 1, record: int = 0, precision: int = _abi.PRECISION_FP64,
-                 device: int = 0, output_prefix: Optional[str] = None):
+                 device: int = 0, output_prefix: Optional[str] = None, skin: Optional[float] = None,
+                 check_interval: Optional[int] = None):
         L = lib()
         opts = EngineOpts()
         L.vedo_gpu_default_opts(C.byref(opts))
         opts.up_iact, opts.record, opts.precision, opts.device = up_iact, record, precision, device
+        if skin is not None:
+            opts.skin = skin
+        if check_interval is not None:
+            opts.check_interval = check_interval
         self._prefix = output_prefix.encode() if output_prefix else None
         opts.output_prefix = self._prefix
         h = C.c_void_p()

@@ -228,7 +228,7 @@ def hertz_drum(n: int = 1_000_000, seed: int = 2024, steps: int = 10000, dt: flo
                median_r: float = 1e-3, sigma_log: float = 0.2, r_lo: float = 0.5e-3, r_hi: float = 2e-3,
                E: float = 70e9, nu: float = 0.25, restitution: float = 0.7, mu: float = 0.4,
                density: float = 2500.0, R: float = 0.15, L: float = 0.3, rpm: float = 30.0,
-               facets: int = 64, gap: float = 0.01, solver: str = "ISwH") -> Scene:
+               facets: int = 64, gap: float = 0.01, solver: str = "ISwH", vel_sigma: float = 0.0) -> Scene:
     """Polydisperse Hertz drum.
 
     Radii are lognormal(median_r, sigma_log) clipped to [r_lo, r_hi] and binned into K
@@ -238,7 +238,8 @@ def hertz_drum(n: int = 1_000_000, seed: int = 2024, steps: int = 10000, dt: flo
     two end plates are orbital plates spinning at `rpm` about x.  The spheres fill the drum
     from the bottom in horizontal lattice layers, largest first, each layer's spacing set by
     its largest sphere plus a `gap` fraction, which leaves no initial overlap and packs the
-    1,000,000 default spheres into about 40 % of the drum volume."""
+    1,000,000 default spheres into about 40 % of the drum volume.  Initial velocities are zero
+    unless `vel_sigma` (m/s, per component) is given."""
     rng = np.random.default_rng(seed)
     edges = np.exp(np.linspace(math.log(r_lo), math.log(r_hi), K + 1))
     centres = np.sqrt(edges[:-1] * edges[1:])
@@ -270,7 +271,7 @@ def hertz_drum(n: int = 1_000_000, seed: int = 2024, steps: int = 10000, dt: flo
     pos += rng.uniform(-0.25 * gap, 0.25 * gap, size=pos.shape) * radii[:, None]
     perm = rng.permutation(n)                  # object order independent of the layer order
     pos, cls = pos[perm], cls[perm]
-    vel = np.zeros_like(pos)
+    vel = rng.normal(0.0, vel_sigma, size=pos.shape) if vel_sigma > 0 else np.zeros_like(pos)
     models: List[DOModel] = []
     for k in range(K):
         models.append(DOModel(f"B{k:03d}", f"B{k:03d}", MOBILE, LOCAL, density, 1.0, SPHERE, (float(centres[k]),)))
