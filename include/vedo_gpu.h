@@ -237,6 +237,25 @@ void vedo_gpu_destroy(vedo_gpu_engine* e);
 /* Library version string. */
 const char* vedo_gpu_version(void);
 
+/* ---- batches of scenes (MIXED form) -------------------------------------
+ * No counterpart in the reference, which runs one DOWorld per anne process
+ * (Anne.cpp:83-119).  One engine advances many independent scenes with one
+ * fused launch per step: objects are numbered scene after scene (scene s owns
+ * objects [first, first + count) of every state and contact array), objects of
+ * different scenes never interact, and each scene keeps its own time step, field
+ * acceleration, models and interaction models.  A scene's results do not depend
+ * on the other scenes of the batch: they are bit-identical to the same scene run
+ * alone in the MIXED form.  vedo_gpu_run advances every scene by nsteps steps;
+ * *keep_running refers to scene 0.  vedo_gpu_get_observables sums over all
+ * scenes with scene 0's field acceleration; vedo_gpu_write_ido needs a
+ * single-scene engine. */
+int vedo_gpu_create_batch(const vedo_scene_desc* const* scenes, uint32_t num_scenes, const vedo_engine_opts* opts,
+                          vedo_gpu_engine** out);
+uint32_t vedo_gpu_num_scenes(const vedo_gpu_engine* e);
+/* Object range and simulated time of one scene of a batch (scene 0 of a plain engine). */
+int vedo_gpu_scene_range(const vedo_gpu_engine* e, uint32_t scene, uint32_t* first_object, uint32_t* num_objects,
+                         double* time);
+
 #ifdef __cplusplus
 }
 #endif

@@ -15,30 +15,9 @@ from vedo_gb300 import scenes
 pytestmark = pytest.mark.gpu
 
 
-def _settled(engine_lib, tmp_path, scene, steps, name):
-    e = engine_lib.GpuEngine(scene, up_iact=20)
-    e.run(steps)
-    p = str(tmp_path / f"{name}.ido")
-    e.write_ido(p)
-    e.close()
-    return p
-
-
 def _active_set(it):
     a = it["active"] == 1
     return set(zip(it["first"][a].tolist(), it["second"][a].tolist()))
-
-
-@pytest.fixture(scope="module")
-def box_ido(engine_lib, tmp_path_factory):
-    sc = scenes.lsd_box(n_side=12, vel_sigma=0.3, spacing=2.05e-3)
-    return _settled(engine_lib, tmp_path_factory.mktemp("mx"), sc, 4000, "box")
-
-
-@pytest.fixture(scope="module")
-def drum_ido(engine_lib, tmp_path_factory):
-    sc = scenes.hertz_drum(n=40000, seed=3, steps=100, gap=0.002, vel_sigma=0.05)
-    return _settled(engine_lib, tmp_path_factory.mktemp("mx"), sc, 3000, "drum")
 
 
 @pytest.mark.parametrize("which", ["box", "drum"])
@@ -88,16 +67,16 @@ def test_mixed_deterministic(drum_ido, engine_lib):
         assert np.array_equal(r[0][k], r[1][k]), k
 
 
-def test_mixed_rebuilds_keep_history(box_ido, engine_lib):
-    """A tiny skin forces a rebuild every few steps; the shear history must survive them
-    (results stay within the FP32 tolerance of a run with a large skin)."""
-    a = engine_lib.GpuEngine(box_ido, precision=1)
+def test_mixed_results_independent_of_rebuilds(box_ido, engine_lib):
+    """Neighbour lists are kept in canonical order and histories are carried, so a tiny skin
+    (a rebuild every step or two) and a wide one (rare rebuilds) give bit-identical results."""
+    a = engine_lib.GpuEngine(box_ido, precision=1, skin=0.5)
     b = engine_lib.GpuEngine(box_ido, precision=1, skin=0.002, check_interval=1)
     a.run(400)
     b.run(400)
     sa, sb = a.state(), b.state()
-    err = np.linalg.norm(sa["velocity"] - sb["velocity"]) / np.linalg.norm(sa["velocity"])
-    assert err < 1e-4, err
+    for k in ("position", "velocity", "angular_velocity", "impact", "angular_impact"):
+        assert np.array_equal(sa[k], sb[k]), k
 
 
 def test_mixed_matches_oracle_trajectory_start(engine_lib, port_lib):

@@ -2,9 +2,10 @@
 
     python -m vedo_gb300.build          # -> vedo_gb300/_build/libvedogpu.so, vedo_gb300/_build/anne-gpu
 
-Every translation unit with FP64 physics is compiled with -fmad=false and the host
-compiler with -ffp-contract=off, so that no multiply-add is contracted: the engine's
-plain-FP64 form then evaluates the reference's IEEE operation sequence exactly.
+Every translation unit with physics is compiled with -fmad=false and the host compiler
+with -ffp-contract=off, so that no multiply-add is contracted behind the source's back:
+the plain-FP64 form then evaluates the reference's IEEE operation sequence exactly, and
+the mixed form's fused multiply-adds are the explicit fma/fmaf calls of its source.
 """
 from __future__ import annotations
 
@@ -34,7 +35,7 @@ def _nvcc() -> str:
 # source -> (compiler, extra flags)
 SOURCES = {
     "engine.cu": ("nvcc", ["-fmad=false"]),
-    "mixed.cu": ("nvcc", []),
+    "mixed.cu": ("nvcc", ["-fmad=false"]),
     "sort_scan.cu": ("nvcc", []),
     "scene_host.cpp": ("cxx", []),
     "capi.cpp": ("cxx", []),

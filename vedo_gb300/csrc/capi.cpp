@@ -2,6 +2,7 @@
 #include <cstring>
 #include <new>
 #include <string>
+#include <vector>
 
 #include "../../include/vedo_gpu.h"
 #include "engine_base.h"
@@ -137,5 +138,56 @@ const char* vedo_gpu_last_error(const vedo_gpu_engine* e) {
 void vedo_gpu_destroy(vedo_gpu_engine* e) { delete e; }
 
 const char* vedo_gpu_version(void) { return "vedo-gb300 0.1.0 (sm_103a)"; }
+
+int vedo_gpu_create_batch(const vedo_scene_desc* const* scenes, uint32_t num_scenes, const vedo_engine_opts* opts,
+                          vedo_gpu_engine** out) {
+    if (!scenes || !out || num_scenes == 0) return VEDO_ERR_INVALID_ARGUMENT;
+    *out = nullptr;
+    vedo_engine_opts o;
+    vedo_gpu_default_opts(&o);
+    if (opts) o = *opts;
+    if (o.precision != VEDO_PRECISION_MIXED) {
+        g_create_error = "batches run in the MIXED form only";
+        return VEDO_ERR_INVALID_ARGUMENT;
+    }
+    std::vector<vedo::HScene> hs(num_scenes);
+    std::vector<const vedo::HScene*> ptrs(num_scenes);
+    for (uint32_t k = 0; k < num_scenes; ++k) {
+        std::string err;
+        if (!scenes[k] || !vedo::scene_from_desc(scenes[k], hs[k], err)) {
+            g_create_error = "scene " + std::to_string(k) + ": " + (scenes[k] ? err : std::string("NULL"));
+            return scenes[k] ? VEDO_ERR_INVALID_SCENE : VEDO_ERR_INVALID_ARGUMENT;
+        }
+        ptrs[k] = &hs[k];
+    }
+    vedo_gpu_engine* e = new (std::nothrow) vedo_gpu_engine();
+    if (!e) return VEDO_ERR_OUT_OF_MEMORY;
+    int rc = VEDO_OK;
+    std::string err;
+    e->p = vedo::make_mixed_batch(ptrs, o, &rc, &err);
+    if (!e->p) {
+        g_create_error = err;
+        delete e;
+        return rc;
+    }
+    *out = e;
+    return VEDO_OK;
+}
+
+uint32_t vedo_gpu_num_scenes(const vedo_gpu_engine* e) { return e ? vedo::mixed_num_scenes(e->p) : 0u; }
+
+int vedo_gpu_scene_range(const vedo_gpu_engine* e, uint32_t scene, uint32_t* first_object, uint32_t* num_objects,
+                         double* time) {
+    if (!e || !first_object || !num_objects) return VEDO_ERR_INVALID_ARGUMENT;
+    int rc = vedo::mixed_scene_range(e->p, scene, first_object, num_objects, time);
+    if (rc == VEDO_ERR_INVALID_ARGUMENT && scene == 0 && vedo::mixed_num_scenes(e->p) == 1) {
+        // a single-scene FP64 engine
+        *first_object = 0;
+        *num_objects = e->p->num_objects();
+        if (time) *time = e->p->time();
+        return VEDO_OK;
+    }
+    return rc;
+}
 
 }  // extern "C"

@@ -3,6 +3,7 @@
 
 #include <cstdint>
 #include <string>
+#include <vector>
 
 #include "../../include/vedo_gpu.h"
 #include "scene_host.h"
@@ -30,5 +31,11 @@ public:
 
 EngineBase* make_fp64_engine();
 EngineBase* make_mixed_engine();
+// MIXED-form engine over several scenes (vedo_gpu_create_batch); nullptr with *rc / *err on failure.
+EngineBase* make_mixed_batch(const std::vector<const HScene*>& scenes, const vedo_engine_opts& opts, int* rc,
+                             std::string* err);
+// Scene count and per-scene object range / time of a batch engine (1 scene for any other engine).
+uint32_t mixed_num_scenes(EngineBase* e);
+int mixed_scene_range(EngineBase* e, uint32_t s, uint32_t* off, uint32_t* n, double* t);
 
 }  // namespace vedo

@@ -20,8 +20,14 @@
 //
 // Broad phase: uniform cell list of edge 2 r_max + skin, stable radix sort on cell key,
 // full neighbour lists within r_i + r_j + skin (a conservative FP32 test: a superset), walls
-// by a plane/axis lower bound.  The list is rebuilt when the accumulated bound on any
-// sphere's displacement, sum over steps of dt * max|v|, may exceed half the skin.
+// by a plane/axis lower bound.  The list is complete while every sphere and every wall plane
+// or axis has moved less than half the skin since the rebuild; the bound on that displacement,
+// the sum over steps of dt * max(max|v| of the spheres, the walls' plane speed), is kept on the
+// device.  A step that starts with the bound above half the skin is not taken: the tick and
+// wall kernels copy the state unchanged (an identity step) and count it, and the host, which
+// reads the bound and the count every few steps, rebuilds and takes the step again.  Contacts
+// are therefore never missed, and the results do not depend on the skin or on when the list
+// is rebuilt.
 #include <algorithm>
 #include <cfloat>
 #include <cmath>
@@ -107,14 +113,17 @@ __device__ __forceinline__ f3 operator+(f3 a, f3 b) { return fm(a.x + b.x, a.y +
 __device__ __forceinline__ f3 operator-(f3 a, f3 b) { return fm(a.x - b.x, a.y - b.y, a.z - b.z); }
 __device__ __forceinline__ f3 operator*(float s, f3 a) { return fm(s * a.x, s * a.y, s * a.z); }
 __device__ __forceinline__ f3 operator-(f3 a) { return fm(-a.x, -a.y, -a.z); }
-__device__ __forceinline__ float fdot(f3 a, f3 b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
+// Every multiply-add below is written out (fmaf) and the file is compiled with -fmad=false, so
+// the FP32 sequence is fixed by the source and does not change with the surrounding code (the
+// single-law and the multi-law kernels give bit-identical results).
+__device__ __forceinline__ float fdot(f3 a, f3 b) { return fmaf(a.z, b.z, fmaf(a.y, b.y, a.x * b.x)); }
 __device__ __forceinline__ float flen(f3 a) { return sqrtf(fdot(a, a)); }
 __device__ __forceinline__ f3 fdir(f3 a) {
     const float l = flen(a);
     return l != 0.0f ? (1.0f / l) * a : fm(0.0f, 0.0f, 0.0f);
 }
 __device__ __forceinline__ f3 fcross(f3 a, f3 b) {
-    return fm(a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x);
+    return fm(fmaf(a.y, b.z, -a.z * b.y), fmaf(a.z, b.x, -a.x * b.z), fmaf(a.x, b.y, -a.y * b.x));
 }
 __device__ __forceinline__ f3 f4to3(float4 v) { return fm(v.x, v.y, v.z); }
 
@@ -230,9 +239,27 @@ __device__ __forceinline__ int solve32(int is_rt, const float* __restrict__ c, b
     return 2;
 }
 
+// ---- scenes of a batch -----------------------------------------------------------------
+// Every scene of a batch keeps its own model/parameter block, cell grid, wall range and time
+// step; object indices are the scene's own shifted by its offset, so a scene's results do not
+// depend on the other scenes it is batched with.
+struct SceneDev {
+    uint32_t model_off, nm, pbase, wall_beg, wall_end, obj_off, nobj, pad;
+    uint64_t cell_base;
+    uint32_t nc[3];
+    float lo[3], inv_h;
+    double dt;
+};
+
+__device__ __forceinline__ uint32_t pidx(const SceneDev& S, uint32_t mg_slave, uint32_t mg_master) {
+    return S.pbase + (mg_slave - S.model_off) * S.nm + (mg_master - S.model_off);
+}
+
 // ---- tick ------------------------------------------------------------------------------
 struct TickArgs {
-    uint32_t n, nm;
+    uint32_t n;
+    const SceneDev* scenes;
+    const uint32_t* scene_of;
     const uint32_t* model_of;
     const ModelDev* models;
     const PairParam* params;
@@ -258,11 +285,10 @@ struct TickArgs {
     double4_32a* imp;
     double4_32a* aimp;
     int write_imp;
-    double dt;
-    d3 fimp;
     unsigned* vmax_bits;
     const float4* pos32;           // positions at the last rebuild (FP32 offsets)
     const float* disp;             // bound on any sphere's displacement since the last rebuild
+    float half_skin;               // a step starting with *disp above this is an identity step
     const float* reach;
     const float4* wall32;
     float* wimp;                   // [ne][6] impulse and angular impulse on the wall of a wall entry
@@ -270,16 +296,36 @@ struct TickArgs {
     const float4* mf;              // [nm][2]: field + external impulse per step, 1/m~; 2.5/(m~ r^2)
 };
 
+// identity step: the next buffers receive the current state and history unchanged
+__device__ __forceinline__ void hold_state(const TickArgs& a, uint32_t i) {
+    if (i >= a.n || a.models[a.model_of[i]].scope != SCOPE_LOCAL) return;
+    a.xB[i] = a.xA[i];
+    a.v32B[i] = a.v32A[i];
+    a.w32B[i] = a.w32A[i];
+    const uint32_t e1 = a.nptr[i + 1];
+    for (uint32_t e = a.nptr[i]; e < e1; ++e)
+        if (a.nslot[e] == e) {
+            a.hB[e] = a.hA[e];
+            a.fB[e] = a.fA[e];
+        }
+}
+
 template <int LAW>
 __global__ void __launch_bounds__(TPB) k_tick(TickArgs a) {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (*a.disp > a.half_skin) {     // the same value for every thread: the whole launch returns
+        hold_state(a, i);
+        return;
+    }
     float vmax_local = 0.0f;
     if (i < a.n) {
         const uint32_t mi = a.model_of[i];
         const ModelDev& M = a.models[mi];
         if (M.scope == SCOPE_LOCAL) {
+            const SceneDev& S = a.scenes[a.scene_of[i]];
+            const double dt = S.dt;
             const d3 Pi = ld(a.xA, i);
-            const float dtf = (float)a.dt;
+            const float dtf = (float)dt;
             const float disp = *a.disp;
             K3 J, JA;
             const uint32_t e1 = a.nptr[i + 1];
@@ -299,7 +345,7 @@ __global__ void __launch_bounds__(TPB) k_tick(TickArgs a) {
                     else i_slave = i < j;
                 }
                 const uint32_t s = i_slave ? i : j, m = i_slave ? j : i;
-                const uint32_t pi = (i_slave ? mi : mj) * a.nm + (i_slave ? mj : mi);
+                const uint32_t pi = pidx(S, i_slave ? mi : mj, i_slave ? mj : mi);
                 const PairParam& P = a.params[pi];
                 if (P.cd == 0) continue;
                 const uint32_t slot = a.nslot[e];
@@ -408,8 +454,8 @@ __global__ void __launch_bounds__(TPB) k_tick(TickArgs a) {
                 const f3 dv = mf0.w * Jf, dw = mf1.x * JAf;
                 const d3 V = ld(a.v64, i), W = ld(a.w64, i);
                 const d3 dvd = mk((double)dv.x, (double)dv.y, (double)dv.z);
-                const d3 P2 = mk(fma(a.dt, fma(0.5, dvd.x, V.x), Pi.x), fma(a.dt, fma(0.5, dvd.y, V.y), Pi.y),
-                                 fma(a.dt, fma(0.5, dvd.z, V.z), Pi.z));
+                const d3 P2 = mk(fma(dt, fma(0.5, dvd.x, V.x), Pi.x), fma(dt, fma(0.5, dvd.y, V.y), Pi.y),
+                                 fma(dt, fma(0.5, dvd.z, V.z), Pi.z));
                 const d3 V2 = add(V, dvd);
                 const d3 W2 = add(W, mk((double)dw.x, (double)dw.y, (double)dw.z));
                 st(a.xB, i, P2, 0.0);
@@ -434,23 +480,41 @@ __global__ void __launch_bounds__(TPB) k_tick(TickArgs a) {
 }
 
 // Scope-global objects (walls): fixed ones keep their state, orbital ones move with their
-// prescribed V and omega (DOOrbitalQuasiPlate.cpp:18-34).  Thread 0 also accumulates the
-// displacement bound of the step.
+// prescribed V and omega (DOOrbitalQuasiPlate.cpp:18-34).  Thread 0 also writes the
+// displacement bound after the step into the other parity slot (disp_out), or, when the step
+// is an identity step, carries the bound over and counts the step in *held.
 __global__ void k_walls(uint32_t nglob, const uint32_t* __restrict__ glob, const uint32_t* __restrict__ model_of,
-                        const ModelDev* __restrict__ models, const double4_32a* __restrict__ xA,
+                        const ModelDev* __restrict__ models, const SceneDev* __restrict__ scenes,
+                        const uint32_t* __restrict__ scene_of, const double4_32a* __restrict__ xA,
                         double4_32a* __restrict__ xB, const double4_32a* __restrict__ v64,
                         const double4_32a* __restrict__ w64, const float4* __restrict__ v32A,
                         float4* __restrict__ v32B, const float4* __restrict__ w32A, float4* __restrict__ w32B,
-                        double4_32a* __restrict__ ox, double4_32a* __restrict__ oz, double dt,
-                        unsigned* __restrict__ vmax_bits, float* __restrict__ disp_bound, float4* __restrict__ wall32) {
+                        double4_32a* __restrict__ ox, double4_32a* __restrict__ oz, float dt_max,
+                        unsigned* __restrict__ vmax_bits, const float* __restrict__ disp_in,
+                        float* __restrict__ disp_out, float half_skin, const unsigned* __restrict__ wall_speed_bits,
+                        unsigned* __restrict__ held, float4* __restrict__ wall32) {
     const uint32_t q = blockIdx.x * blockDim.x + threadIdx.x;
+    const float disp = *disp_in;
+    const bool hold = disp > half_skin;
     if (q == 0) {
-        *disp_bound += (float)dt * __uint_as_float(*vmax_bits);
+        if (hold) {
+            *disp_out = disp;
+            *held += 1u;
+        } else {
+            *disp_out = disp + dt_max * fmaxf(__uint_as_float(*vmax_bits), __uint_as_float(*wall_speed_bits));
+        }
         *vmax_bits = 0u;
     }
     if (q >= nglob) return;
     const uint32_t w = glob[q];
+    if (hold) {
+        xB[w] = xA[w];
+        v32B[w] = v32A[w];
+        w32B[w] = w32A[w];
+        return;
+    }
     const ModelDev& M = models[model_of[w]];
+    const double dt = scenes[scene_of[w]].dt;
     d3 P = ld(xA, w);
     if (M.behavior == BEH_ORBITAL) {
         const d3 V = ld(v64, w), AV = ld(w64, w);
@@ -472,11 +536,13 @@ __global__ void k_walls(uint32_t nglob, const uint32_t* __restrict__ glob, const
 
 // ---- broad phase -------------------------------------------------------------------------
 __global__ void __launch_bounds__(TPB) k_bounds(uint32_t n, const uint32_t* __restrict__ model_of,
-                                                const ModelDev* __restrict__ models, const double4_32a* __restrict__ x,
+                                                const ModelDev* __restrict__ models,
+                                                const uint32_t* __restrict__ scene_of, const double4_32a* __restrict__ x,
                                                 d3 origin, float4* __restrict__ pos32, unsigned* __restrict__ red) {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-    // red: [0..2] min (ordered float bits), [3..5] max, [6] max radius
+    // red[8 * scene + k]: [0..2] min (ordered float bits), [3..5] max, [6] max radius
     unsigned mn[3] = {0xffffffffu, 0xffffffffu, 0xffffffffu}, mx[3] = {0, 0, 0}, rm = 0;
+    const uint32_t sc = i < n ? scene_of[i] : 0xffffffffu;
     if (i < n) {
         const ModelDev& M = models[model_of[i]];
         const d3 p = ld(x, i);
@@ -493,37 +559,50 @@ __global__ void __launch_bounds__(TPB) k_bounds(uint32_t n, const uint32_t* __re
             rm = __float_as_uint((float)M.range);
         }
     }
+    const uint32_t sc0 = __shfl_sync(0xffffffffu, sc, 0);
+    if (__all_sync(0xffffffffu, sc == sc0 || sc == 0xffffffffu)) {   // one scene in this warp
 #pragma unroll
-    for (int o = 16; o > 0; o >>= 1) {
+        for (int o = 16; o > 0; o >>= 1) {
 #pragma unroll
-        for (int k = 0; k < 3; ++k) {
-            mn[k] = min(mn[k], __shfl_xor_sync(0xffffffffu, mn[k], o));
-            mx[k] = max(mx[k], __shfl_xor_sync(0xffffffffu, mx[k], o));
+            for (int k = 0; k < 3; ++k) {
+                mn[k] = min(mn[k], __shfl_xor_sync(0xffffffffu, mn[k], o));
+                mx[k] = max(mx[k], __shfl_xor_sync(0xffffffffu, mx[k], o));
+            }
+            rm = max(rm, __shfl_xor_sync(0xffffffffu, rm, o));
         }
-        rm = max(rm, __shfl_xor_sync(0xffffffffu, rm, o));
-    }
-    if ((threadIdx.x & 31) == 0) {
-        for (int k = 0; k < 3; ++k) {
-            atomicMin(&red[k], mn[k]);
-            atomicMax(&red[3 + k], mx[k]);
+        if ((threadIdx.x & 31) == 0 && sc0 != 0xffffffffu) {
+            unsigned* r = red + 8 * (size_t)sc0;
+            for (int k = 0; k < 3; ++k) {
+                atomicMin(&r[k], mn[k]);
+                atomicMax(&r[3 + k], mx[k]);
+            }
+            atomicMax(&r[6], rm);
         }
-        atomicMax(&red[6], rm);
+    } else if (sc != 0xffffffffu) {                                  // scene boundary inside the warp
+        unsigned* r = red + 8 * (size_t)sc;
+        for (int k = 0; k < 3; ++k) {
+            atomicMin(&r[k], mn[k]);
+            atomicMax(&r[3 + k], mx[k]);
+        }
+        atomicMax(&r[6], rm);
     }
 }
 
 __global__ void __launch_bounds__(TPB) k_keys(uint32_t n, const uint32_t* __restrict__ model_of,
-                                              const ModelDev* __restrict__ models, const float4* __restrict__ pos32,
-                                              float3 lo, float inv_h, uint32_t nx, uint32_t ny, uint32_t nz,
-                                              uint64_t sentinel, uint64_t* __restrict__ key, uint32_t* __restrict__ sid) {
+                                              const ModelDev* __restrict__ models,
+                                              const uint32_t* __restrict__ scene_of, const SceneDev* __restrict__ scenes,
+                                              const float4* __restrict__ pos32, uint64_t sentinel,
+                                              uint64_t* __restrict__ key, uint32_t* __restrict__ sid) {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     uint64_t k = sentinel;
     if (models[model_of[i]].scope == SCOPE_LOCAL) {
+        const SceneDev& S = scenes[scene_of[i]];
         const float4 p = pos32[i];
-        const uint32_t cx = min((uint32_t)fmaxf((p.x - lo.x) * inv_h, 0.0f), nx - 1);
-        const uint32_t cy = min((uint32_t)fmaxf((p.y - lo.y) * inv_h, 0.0f), ny - 1);
-        const uint32_t cz = min((uint32_t)fmaxf((p.z - lo.z) * inv_h, 0.0f), nz - 1);
-        k = ((uint64_t)cx * ny + cy) * nz + cz;
+        const uint32_t cx = min((uint32_t)fmaxf((p.x - S.lo[0]) * S.inv_h, 0.0f), S.nc[0] - 1);
+        const uint32_t cy = min((uint32_t)fmaxf((p.y - S.lo[1]) * S.inv_h, 0.0f), S.nc[1] - 1);
+        const uint32_t cz = min((uint32_t)fmaxf((p.z - S.lo[2]) * S.inv_h, 0.0f), S.nc[2] - 1);
+        k = S.cell_base + ((uint64_t)cx * S.nc[1] + cy) * S.nc[2] + cz;
     }
     key[i] = k;
     sid[i] = i;
@@ -543,17 +622,20 @@ __global__ void __launch_bounds__(TPB) k_cells(uint32_t nloc, const uint64_t* __
 template <bool FILL>
 __global__ void __launch_bounds__(TPB) k_nbr(uint32_t nloc, const uint32_t* __restrict__ sid,
                                              const uint64_t* __restrict__ key, const uint32_t* __restrict__ grid_start,
-                                             const uint32_t* __restrict__ grid_end, uint32_t nx, uint32_t ny, uint32_t nz,
-                                             const uint32_t* __restrict__ glob, uint32_t nglob,
+                                             const uint32_t* __restrict__ grid_end,
+                                             const uint32_t* __restrict__ scene_of, const SceneDev* __restrict__ scenes,
+                                             const uint32_t* __restrict__ glob,
                                              const uint32_t* __restrict__ model_of, const ModelDev* __restrict__ models,
                                              const PairParam* __restrict__ params, const float* __restrict__ reach,
-                                             uint32_t nm, const float4* __restrict__ pos32,
+                                             const float4* __restrict__ pos32,
                                              const float4* __restrict__ wall32, float skin,
                                              uint32_t* __restrict__ cnt_or_ptr, uint32_t* __restrict__ ent) {
     const uint32_t P = blockIdx.x * blockDim.x + threadIdx.x;
     if (P >= nloc) return;
     const uint32_t i = sid[P];
-    const uint64_t k = key[P];
+    const SceneDev& S = scenes[scene_of[i]];
+    const uint32_t nx = S.nc[0], ny = S.nc[1], nz = S.nc[2];
+    const uint64_t k = key[P] - S.cell_base;
     const uint32_t cz = (uint32_t)(k % nz), cy = (uint32_t)((k / nz) % ny), cx = (uint32_t)(k / ((uint64_t)nz * ny));
     const uint32_t mi = model_of[i];
     const float4 pi = pos32[i];
@@ -565,13 +647,13 @@ __global__ void __launch_bounds__(TPB) k_nbr(uint32_t nloc, const uint32_t* __re
             if ((dy < 0 && cy == 0) || (dy > 0 && cy + 1 >= ny)) continue;
             for (int dz = -1; dz <= 1; ++dz) {
                 if ((dz < 0 && cz == 0) || (dz > 0 && cz + 1 >= nz)) continue;
-                const uint64_t nk = ((uint64_t)(cx + dx) * ny + (cy + dy)) * nz + (cz + dz);
+                const uint64_t nk = S.cell_base + ((uint64_t)(cx + dx) * ny + (cy + dy)) * nz + (cz + dz);
                 const uint32_t b = grid_start[nk], e = grid_end[nk];
                 for (uint32_t q = b; q < e; ++q) {
                     const uint32_t j = sid[q];
                     if (j == i) continue;
                     const uint32_t mj = model_of[j];
-                    const uint32_t pa = mi * nm + mj, pb = mj * nm + mi;
+                    const uint32_t pa = pidx(S, mi, mj), pb = pidx(S, mj, mi);
                     if (params[pa].cd == 0 && params[pb].cd == 0) continue;
                     const float r = fmaxf(reach[pa], reach[pb]);
                     float err;
@@ -583,9 +665,9 @@ __global__ void __launch_bounds__(TPB) k_nbr(uint32_t nloc, const uint32_t* __re
             }
         }
     }
-    for (uint32_t q = 0; q < nglob; ++q) {
+    for (uint32_t q = S.wall_beg; q < S.wall_end; ++q) {
         const uint32_t w = glob[q];
-        const uint32_t pw = mi * nm + model_of[w];
+        const uint32_t pw = pidx(S, mi, model_of[w]);
         const int cd = params[pw].cd;
         if (cd == 0) continue;
         const float4 wl = wall32[w];
@@ -597,7 +679,22 @@ __global__ void __launch_bounds__(TPB) k_nbr(uint32_t nloc, const uint32_t* __re
         if (FILL) ent[off + c] = w | WALL_BIT;
         ++c;
     }
-    if (!FILL) cnt_or_ptr[i] = c;
+    if (!FILL) {
+        cnt_or_ptr[i] = c;
+        return;
+    }
+    // Canonical order: spheres by index, then walls by index.  Every per-sphere sum then runs
+    // in an order that depends neither on the cell grid nor on when the list was rebuilt, nor
+    // on where the scene sits in a batch (indices only shift by the scene's offset).
+    for (uint32_t q = 1; q < c; ++q) {
+        const uint32_t v = ent[off + q];
+        uint32_t r = q;
+        while (r > 0 && ent[off + r - 1] > v) {
+            ent[off + r] = ent[off + r - 1];
+            --r;
+        }
+        ent[off + r] = v;
+    }
 }
 
 // History slot of every entry: the entry itself for the owner (lower index, or a wall
@@ -691,8 +788,10 @@ __global__ void __launch_bounds__(TPB) k_wall_ptr(uint32_t nglob, const uint32_t
 // field and external impulses, as DOStatus::GetImpact holds them after ClearImpact.
 __global__ void k_wall_sum(uint32_t nglob, const uint32_t* __restrict__ glob, const uint32_t* __restrict__ wptr,
                            const uint32_t* __restrict__ wval, const float* __restrict__ wimp,
-                           const uint32_t* __restrict__ model_of, const ModelDev* __restrict__ models, double dt, d3 fimp,
-                           double4_32a* __restrict__ imp, double4_32a* __restrict__ aimp) {
+                           const uint32_t* __restrict__ model_of, const ModelDev* __restrict__ models,
+                           const SceneDev* __restrict__ scenes, const uint32_t* __restrict__ scene_of,
+                           const double* __restrict__ gfield, double4_32a* __restrict__ imp,
+                           double4_32a* __restrict__ aimp) {
     const uint32_t q = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const int lane = threadIdx.x & 31;
     if (q >= nglob) return;
@@ -714,6 +813,9 @@ __global__ void k_wall_sum(uint32_t nglob, const uint32_t* __restrict__ glob, co
     if (lane == 0) {
         const uint32_t w = glob[q];
         const ModelDev& M = models[model_of[w]];
+        const uint32_t sc = scene_of[w];
+        const double dt = scenes[sc].dt;
+        const d3 fimp = muls(mk(gfield[3 * sc], gfield[3 * sc + 1], gfield[3 * sc + 2]), dt);
         J = add(J, muls(fimp, M.sudo));
         J = add(J, smul(dt, mk(M.ext[0], M.ext[1], M.ext[2])));
         st(imp, w, J, 0.0);
@@ -742,7 +844,7 @@ __global__ void __launch_bounds__(TPB) k_active(uint32_t n, TickArgs a, uint8_t*
             else i_slave = i < j;
         }
         const uint32_t s = i_slave ? i : j, m = i_slave ? j : i;
-        const uint32_t pi = (i_slave ? mi : mj) * a.nm + (i_slave ? mj : mi);
+        const uint32_t pi = pidx(a.scenes[a.scene_of[i]], i_slave ? mi : mj, i_slave ? mj : mi);
         const PairParam& P = a.params[pi];
         if (P.cd == 0) continue;
         const double4_32a gg = a.geom[pi];
@@ -778,6 +880,35 @@ __global__ void __launch_bounds__(TPB) k_copy32(uint32_t n, const double4_32a* _
         o[i] = make_float4((float)q.x, (float)q.y, (float)q.z, 0.0f);
     }
 }
+// Bound on how fast an orbital wall's plane (plate) or axis line (cylinder) can move towards
+// a sphere that may touch it: |V| + |omega| R, R = half the wall's diagonal + 2 r_max.  A
+// wall spinning about its own normal (plate) or axis (cylinder) keeps its plane or line: only
+// the normal (plate) or transverse (cylinder) part of V counts.  V and omega of an orbital
+// wall are prescribed, so the bound holds until the state is set again.
+__global__ void k_wall_speed(uint32_t nglob, const uint32_t* __restrict__ glob, const uint32_t* __restrict__ model_of,
+                             const ModelDev* __restrict__ models, const double4_32a* __restrict__ v64,
+                             const double4_32a* __restrict__ w64, const double4_32a* __restrict__ oz, float reach,
+                             unsigned* __restrict__ out_bits) {
+    const uint32_t q = blockIdx.x * blockDim.x + threadIdx.x;
+    if (q >= nglob) return;
+    const uint32_t w = glob[q];
+    const ModelDev& M = models[model_of[w]];
+    if (M.behavior != BEH_ORBITAL) return;
+    const d3 V = ld(v64, w), W = ld(w64, w), Oz = ld(oz, w);
+    const double lz = len(Oz);
+    const double R = 0.5 * sqrt(M.a0 * M.a0 + M.a1 * M.a1 + M.a2 * M.a2) + (double)reach;
+    double sp = len(V) + len(W) * R;
+    if (lz > 0.0) {
+        const d3 u = muls(Oz, 1.0 / lz);
+        const d3 c = cross(W, u);
+        if (len(c) <= 1e-12 * len(W)) {                 // spins about its own normal / axis
+            const double vn = dot(V, u);
+            sp = (M.shape == SHAPE_PLATE) ? fabs(vn) : len(sub(V, muls(u, vn)));
+        }
+    }
+    atomicMax(out_bits, __float_as_uint((float)(sp * 1.0001) + 1e-30f));
+}
+
 __global__ void __launch_bounds__(TPB) k_wall32(uint32_t n, const uint32_t* __restrict__ model_of,
                                                 const ModelDev* __restrict__ models, const double4_32a* __restrict__ ox,
                                                 const double4_32a* __restrict__ oz, float4* __restrict__ wall32) {
@@ -802,7 +933,10 @@ __global__ void __launch_bounds__(TPB) k_wall32(uint32_t n, const uint32_t* __re
 class MixedEngine : public EngineBase {
 public:
     ~MixedEngine() override;
-    int init(const HScene& scene, const vedo_engine_opts& opts) override;
+    int init(const HScene& scene, const vedo_engine_opts& opts) override {
+        return init_batch(std::vector<const HScene*>{&scene}, opts);
+    }
+    int init_batch(const std::vector<const HScene*>& scenes, const vedo_engine_opts& opts);
     int run(uint32_t nsteps, int* keep_running) override;
     int get_state(const vedo_state_view& v) override;
     int set_state(const vedo_state_view& v) override;
@@ -810,7 +944,7 @@ public:
     int get_interactions(const vedo_contact_view& v) override;
     int get_observables(double out[13]) override;
     int write_ido(const char* path) override;
-    double time() const override { return t_; }
+    double time() const override { return sc_.empty() ? 0.0 : sc_[0].t; }
     uint64_t steps() const override { return round_; }
     uint32_t num_objects() const override { return n_; }
     uint64_t last_profile(double out[4]) const override {
@@ -819,6 +953,15 @@ public:
     }
     void set_profiling(bool on) override { profiling_ = on; }
     const std::string& error() const override { return err_; }
+    // batch accessors
+    uint32_t num_scenes() const { return (uint32_t)sc_.size(); }
+    int scene_range(uint32_t s, uint32_t* off, uint32_t* n) const {
+        if (s >= sc_.size()) return VEDO_ERR_INVALID_ARGUMENT;
+        *off = sc_[s].obj_off;
+        *n = sc_[s].nobj;
+        return VEDO_OK;
+    }
+    double scene_time(uint32_t s) const { return s < sc_.size() ? sc_[s].t : 0.0; }
 
 private:
     struct NList {
@@ -828,6 +971,11 @@ private:
         uint32_t* slot = nullptr;
         float4* h[2] = {nullptr, nullptr};
         uint8_t* f[2] = {nullptr, nullptr};
+    };
+    struct SceneHost {
+        uint32_t obj_off = 0, nobj = 0, model_off = 0, nm = 0, pbase = 0, wall_beg = 0, wall_end = 0, nloc = 0;
+        double dt = 0, t = 0, t_stop = 0, g[3] = {0, 0, 0};
+        float skin = 0;
     };
     int fail(int c, const std::string& m) { err_ = m; return c; }
     int cuda_fail(cudaError_t e, const char* where) {
@@ -839,13 +987,16 @@ private:
     void free_nlist(NList& L);
     TickArgs args(bool write_imp);
 
-    HScene host_;
-    Tables tab_;
+    std::vector<HScene> host_;      // per scene (states refreshed for IDO output)
+    std::vector<SceneHost> sc_;
+    std::vector<SceneDev> sdev_;
+    std::vector<ModelDev> models_;
+    std::vector<PairParam> params_;
     vedo_engine_opts opts_{};
     std::string err_;
-    uint32_t n_ = 0, nm_ = 0, nloc_ = 0;
-    double dt_ = 0, t_ = 0, t_stop_ = 0, g_[3] = {0, 0, 0}, origin_[3] = {0, 0, 0};
-    float skin_abs_ = 0.0f;
+    uint32_t n_ = 0, nm_ = 0, nloc_ = 0, np_ = 0;
+    double origin_[3] = {0, 0, 0};
+    float dt_max_ = 0.0f, skin_min_ = 0.0f;
     uint64_t round_ = 0;
     int cur_ = 0;                   // which of the A/B buffers is "A" (current)
     bool need_rebuild_ = true;
@@ -854,7 +1005,7 @@ private:
     uint64_t launches_ = 0;
     uint64_t rebuilds_ = 0;
     uint64_t since_rebuild_ = 0;
-    int law_ = 0;                   // the single equation type of the scene, or 0 (mixed laws)
+    int law_ = 0;                   // the single equation type of the batch, or 0 (several laws)
     cudaStream_t stream_ = nullptr;
     cudaEvent_t ev_[4] = {};
 
@@ -866,6 +1017,9 @@ private:
     float4* d_mf_ = nullptr;
     float* d_reach_ = nullptr;
     uint32_t* d_model_of_ = nullptr;
+    uint32_t* d_scene_of_ = nullptr;
+    SceneDev* d_scenes_ = nullptr;
+    double* d_gfield_ = nullptr;
     uint32_t* d_glob_ = nullptr;
     std::vector<uint32_t> glob_;
     double4_32a* d_x_[2] = {nullptr, nullptr};
@@ -874,8 +1028,9 @@ private:
     float4* d_v32_[2] = {nullptr, nullptr};
     float4* d_w32_[2] = {nullptr, nullptr};
     float4 *d_pos32_ = nullptr, *d_wall32_ = nullptr;
-    unsigned* d_red_ = nullptr;     // [0..6] bounds, [8] vmax bits
-    float* d_disp_ = nullptr;
+    unsigned* d_red_ = nullptr;     // [8] vmax bits, [9], [10] scan totals, [11] identity steps, [12] wall speed
+    unsigned* d_sred_ = nullptr;    // [scenes][8] per-scene bounds
+    float* d_disp_ = nullptr;       // [2] displacement bound, by step parity (cur_)
     int* d_err_ = nullptr;
     NList nl_[2];
     int nlc_ = 0;                   // current neighbour list
@@ -886,8 +1041,6 @@ private:
     uint64_t grid_cap_ = 0;
     uint8_t* d_act_ = nullptr;
     uint32_t act_cap_ = 0;
-    // wall impulse output: per-wall entry lists (rebuilt with the neighbour list) and the
-    // per-entry wall share written on output steps
     uint32_t* d_gidx_ = nullptr;
     uint32_t *d_wkey_ = nullptr, *d_wval_ = nullptr, *d_wkey_alt_ = nullptr, *d_wval_alt_ = nullptr, *d_wptr_ = nullptr;
     uint32_t wcap_ = 0, nwall_ent_ = 0;
@@ -937,106 +1090,149 @@ MixedEngine::~MixedEngine() {
     if (stream_) cudaStreamSynchronize(stream_);
     free_nlist(nl_[0]);
     free_nlist(nl_[1]);
-    void* ptrs[] = {d_models_, d_params_, d_pc32_, d_geom_, d_rr_, d_mf_, d_reach_, d_model_of_, d_glob_, d_x_[0], d_x_[1], d_v64_,
-                    d_w64_, d_ox_, d_oz_, d_imp_, d_aimp_, d_v32_[0], d_v32_[1], d_w32_[0], d_w32_[1], d_pos32_,
-                    d_wall32_, d_red_, d_disp_, d_err_, d_key_, d_key_alt_, d_sid_, d_sid_alt_, d_cnt_, d_gs_, d_ge_,
-                    d_act_, d_stage_, d_obs_, d_gidx_, d_wkey_, d_wval_, d_wkey_alt_, d_wval_alt_, d_wptr_,
-                    d_wimp_};
+    void* ptrs[] = {d_models_, d_params_, d_pc32_, d_geom_, d_rr_, d_mf_, d_reach_, d_model_of_, d_scene_of_,
+                    d_scenes_, d_gfield_, d_glob_, d_x_[0], d_x_[1], d_v64_, d_w64_, d_ox_, d_oz_, d_imp_, d_aimp_,
+                    d_v32_[0], d_v32_[1], d_w32_[0], d_w32_[1], d_pos32_, d_wall32_, d_red_, d_sred_, d_disp_, d_err_,
+                    d_key_, d_key_alt_, d_sid_, d_sid_alt_, d_cnt_, d_gs_, d_ge_, d_act_, d_stage_, d_obs_, d_gidx_,
+                    d_wkey_, d_wval_, d_wkey_alt_, d_wval_alt_, d_wptr_, d_wimp_};
     for (void* p : ptrs) if (p) cudaFree(p);
     for (auto& e : ev_) if (e) cudaEventDestroy(e);
     if (stream_) cudaStreamDestroy(stream_);
 }
 
-int MixedEngine::init(const HScene& scene, const vedo_engine_opts& opts) {
-    host_ = scene;
+int MixedEngine::init_batch(const std::vector<const HScene*>& scenes, const vedo_engine_opts& opts) {
     opts_ = opts;
-    std::string msg;
-    int rc = build_tables(host_, tab_, msg);
-    if (rc != VEDO_OK) return fail(rc, msg);
-    n_ = host_.n;
-    nm_ = (uint32_t)tab_.models.size();
-    dt_ = host_.time_interval;
-    t_ = host_.time_current;
-    t_stop_ = host_.time_stop;
-    for (int k = 0; k < 3; ++k) g_[k] = host_.g[k];
-    double rmax = 0.0;
-    for (uint32_t i = 0; i < n_; ++i) {
-        const ModelDev& M = tab_.models[host_.model_of[i]];
-        if (M.scope == SCOPE_LOCAL) {
-            if (M.shape != SHAPE_SPHERE)
-                return fail(VEDO_ERR_UNSUPPORTED_MODEL, "mixed form: local (scope) objects must be spheres");
-            rmax = std::max(rmax, M.a0);
-            ++nloc_;
-        } else {
-            if (M.behavior != BEH_FIXED && M.behavior != BEH_ORBITAL)
-                return fail(VEDO_ERR_UNSUPPORTED_MODEL, "mixed form: walls must be fixed or orbital");
-            glob_.push_back(i);
-        }
-    }
-    skin_abs_ = (float)((opts.skin > 0 ? opts.skin : 0.15f) * rmax);
     if (opts_.check_interval == 0) opts_.check_interval = 10;
+    if (scenes.empty()) return fail(VEDO_ERR_INVALID_SCENE, "empty batch");
+    // ---- per-scene tables, concatenated
+    std::vector<uint32_t> model_of, scene_of;
+    std::vector<double> pos, vel, av, ox, oz, imp, aimp;
+    std::vector<double4_32a> geo, rr;
+    std::vector<float> pc, reach;
+    std::vector<float4> mf;
+    std::vector<double> gfield;
+    struct Rec { uint32_t a, b; float4 h; uint8_t f; };
+    std::vector<std::vector<Rec>> recs;
+    int law = -1;
+    for (const HScene* hp : scenes) {
+        const HScene& h = *hp;
+        host_.push_back(h);
+        Tables t;
+        std::string msg;
+        int rc = build_tables(h, t, msg);
+        if (rc != VEDO_OK) return fail(rc, msg);
+        SceneHost S;
+        S.obj_off = n_;
+        S.nobj = h.n;
+        S.model_off = nm_;
+        S.nm = (uint32_t)t.models.size();
+        S.pbase = np_;
+        S.dt = h.time_interval;
+        S.t = h.time_current;
+        S.t_stop = h.time_stop;
+        for (int k = 0; k < 3; ++k) S.g[k] = h.g[k];
+        double rmax = 0.0;
+        S.wall_beg = (uint32_t)glob_.size();
+        for (uint32_t i = 0; i < h.n; ++i) {
+            const ModelDev& M = t.models[h.model_of[i]];
+            if (M.scope == SCOPE_LOCAL) {
+                if (M.shape != SHAPE_SPHERE)
+                    return fail(VEDO_ERR_UNSUPPORTED_MODEL, "mixed form: local (scope) objects must be spheres");
+                rmax = std::max(rmax, M.a0);
+                ++S.nloc;
+            } else {
+                if (M.behavior != BEH_FIXED && M.behavior != BEH_ORBITAL)
+                    return fail(VEDO_ERR_UNSUPPORTED_MODEL, "mixed form: walls must be fixed or orbital");
+                glob_.push_back(n_ + i);
+            }
+            model_of.push_back(S.model_off + h.model_of[i]);
+            scene_of.push_back((uint32_t)sc_.size());
+        }
+        S.wall_end = (uint32_t)glob_.size();
+        S.skin = (float)((opts.skin > 0 ? opts.skin : 0.15f) * rmax);
+        for (auto* pr : {&pos, &vel, &av, &ox, &oz, &imp, &aimp}) (void)pr;
+        pos.insert(pos.end(), h.pos.begin(), h.pos.end());
+        vel.insert(vel.end(), h.vel.begin(), h.vel.end());
+        av.insert(av.end(), h.av.begin(), h.av.end());
+        ox.insert(ox.end(), h.ox.begin(), h.ox.end());
+        oz.insert(oz.end(), h.oz.begin(), h.oz.end());
+        imp.insert(imp.end(), h.imp.begin(), h.imp.end());
+        aimp.insert(aimp.end(), h.aimp.begin(), h.aimp.end());
+        for (const ModelDev& M : t.models) models_.push_back(M);
+        const size_t nq = (size_t)S.nm * S.nm;
+        for (size_t q = 0; q < nq; ++q) {
+            const PairParam& P = t.params[q];
+            params_.push_back(P);
+            if (P.cd) law = (law == -1 || law == P.is) ? P.is : 0;
+            for (int k = 0; k < 8; ++k) pc.push_back((float)P.c[k]);
+            const double* g = &t.geom[4 * q];
+            geo.push_back(make_double4_32a(g[0], g[1], g[2], g[3]));
+            const double R = g[0] + g[1];
+            rr.push_back(make_double4_32a(R, R * R, 1e-9 * R * R, 0.0));
+            double r = 0.0;
+            if (P.cd == CD_SS) r = g[0] + g[1];
+            else if (P.cd == CD_SP) r = g[0] + 0.5 * g[2];
+            else if (P.cd == CD_SC) r = g[0] + g[1];
+            reach.push_back((float)r * (1.0f + 1e-6f));
+        }
+        for (const ModelDev& M : t.models) {
+            double gi[3];
+            for (int q = 0; q < 3; ++q) gi[q] = h.g[q] * S.dt * M.sudo + S.dt * M.ext[q];
+            mf.push_back(make_float4((float)gi[0], (float)gi[1], (float)gi[2], (float)M.inv_sudo));
+            mf.push_back(make_float4((float)M.rot_coef, 0.0f, 0.0f, 0.0f));
+        }
+        for (int k = 0; k < 3; ++k) gfield.push_back(h.g[k]);
+        // IactRecordTab records of this scene, owned by the lower sphere (or the sphere of a wall pair)
+        std::vector<Rec> rv;
+        for (uint32_t q = 0; q < h.rec.size(); ++q) {
+            uint32_t a = h.rec.first[q], b = h.rec.second[q];
+            if (a >= h.n || b >= h.n) continue;
+            const bool aw = t.models[h.model_of[a]].scope != SCOPE_LOCAL;
+            const bool bw = t.models[h.model_of[b]].scope != SCOPE_LOCAL;
+            if (aw && !bw) std::swap(a, b);
+            Rec r;
+            r.a = n_ + a;
+            r.b = (n_ + b) | ((aw || bw) ? WALL_BIT : 0u);
+            r.h = make_float4((float)h.rec.shear[3 * q], (float)h.rec.shear[3 * q + 1], (float)h.rec.shear[3 * q + 2],
+                              (float)h.rec.kn[q]);
+            r.f = (uint8_t)(HF_LAST_CONTACT | HF_LAST_BOND | (h.rec.contact[q] ? HF_CONTACT : 0) |
+                            (h.rec.bond[q] ? HF_BOND : 0));
+            rv.push_back(r);
+        }
+        recs.push_back(rv);
+        n_ += h.n;
+        nm_ += S.nm;
+        np_ += (uint32_t)nq;
+        nloc_ += S.nloc;
+        dt_max_ = std::max(dt_max_, (float)S.dt);
+        skin_min_ = sc_.empty() ? S.skin : std::min(skin_min_, S.skin);
+        sc_.push_back(S);
+    }
+    law_ = law < 0 ? 0 : law;
+    // ---- device
     MCK(cudaSetDevice(opts.device));
     MCK(cudaStreamCreateWithFlags(&stream_, cudaStreamNonBlocking));
     for (auto& e : ev_) MCK(cudaEventCreate(&e));
-    MCK(mal(&d_models_, nm_));
-    MCK(cudaMemcpy(d_models_, tab_.models.data(), sizeof(ModelDev) * nm_, cudaMemcpyHostToDevice));
-    MCK(mal(&d_params_, (size_t)nm_ * nm_));
-    MCK(cudaMemcpy(d_params_, tab_.params.data(), sizeof(PairParam) * nm_ * nm_, cudaMemcpyHostToDevice));
-    std::vector<float> pc((size_t)nm_ * nm_ * 8);
-    std::vector<double4_32a> geo((size_t)nm_ * nm_);
-    std::vector<float> reach((size_t)nm_ * nm_);
-    for (size_t q = 0; q < geo.size(); ++q) {
-        for (int k = 0; k < 8; ++k) pc[8 * q + k] = (float)tab_.params[q].c[k];
-        const double* g = &tab_.geom[4 * q];
-        geo[q] = make_double4_32a(g[0], g[1], g[2], g[3]);
-        double r = 0.0;
-        if (tab_.params[q].cd == CD_SS) r = g[0] + g[1];
-        else if (tab_.params[q].cd == CD_SP) r = g[0] + 0.5 * g[2];
-        else if (tab_.params[q].cd == CD_SC) r = g[0] + g[1];
-        reach[q] = (float)r * (1.0f + 1e-6f);
-    }
-    {
-        int law = -1;
-        for (const PairParam& P : tab_.params)
-            if (P.cd) law = (law == -1 || law == P.is) ? P.is : 0;
-        law_ = law < 0 ? 0 : law;
-    }
-    MCK(mal(&d_pc32_, pc.size()));
-    MCK(cudaMemcpy(d_pc32_, pc.data(), 4 * pc.size(), cudaMemcpyHostToDevice));
-    MCK(mal(&d_geom_, geo.size()));
-    MCK(cudaMemcpy(d_geom_, geo.data(), sizeof(double4_32a) * geo.size(), cudaMemcpyHostToDevice));
-    MCK(mal(&d_reach_, reach.size()));
-    MCK(cudaMemcpy(d_reach_, reach.data(), 4 * reach.size(), cudaMemcpyHostToDevice));
-    {
-        std::vector<double4_32a> rr(geo.size());
-        for (size_t q = 0; q < geo.size(); ++q) {
-            const double R = tab_.geom[4 * q] + tab_.geom[4 * q + 1];
-            rr[q] = make_double4_32a(R, R * R, 1e-9 * R * R, 0.0);
-        }
-        MCK(mal(&d_rr_, rr.size()));
-        MCK(cudaMemcpy(d_rr_, rr.data(), sizeof(double4_32a) * rr.size(), cudaMemcpyHostToDevice));
-        std::vector<float4> mf(2 * (size_t)nm_);
-        for (uint32_t k = 0; k < nm_; ++k) {
-            const ModelDev& M = tab_.models[k];
-            double gi[3];
-            for (int q = 0; q < 3; ++q) gi[q] = host_.g[q] * dt_ * M.sudo + dt_ * M.ext[q];
-            mf[2 * k] = make_float4((float)gi[0], (float)gi[1], (float)gi[2], (float)M.inv_sudo);
-            mf[2 * k + 1] = make_float4((float)M.rot_coef, 0.0f, 0.0f, 0.0f);
-        }
-        MCK(mal(&d_mf_, mf.size()));
-        MCK(cudaMemcpy(d_mf_, mf.data(), sizeof(float4) * mf.size(), cudaMemcpyHostToDevice));
-    }
-    MCK(mal(&d_model_of_, n_));
-    MCK(cudaMemcpy(d_model_of_, host_.model_of.data(), 4 * n_, cudaMemcpyHostToDevice));
-    MCK(mal(&d_glob_, glob_.size()));
-    if (!glob_.empty()) MCK(cudaMemcpy(d_glob_, glob_.data(), 4 * glob_.size(), cudaMemcpyHostToDevice));
+    auto up = [&](auto** d, const auto& v) -> int {
+        MCK(mal(d, v.size()));
+        if (!v.empty()) MCK(cudaMemcpy(*d, v.data(), sizeof(v[0]) * v.size(), cudaMemcpyHostToDevice));
+        return VEDO_OK;
+    };
+    int rc;
+    if ((rc = up(&d_models_, models_)) || (rc = up(&d_params_, params_)) || (rc = up(&d_pc32_, pc)) ||
+        (rc = up(&d_geom_, geo)) || (rc = up(&d_rr_, rr)) || (rc = up(&d_mf_, mf)) || (rc = up(&d_reach_, reach)) ||
+        (rc = up(&d_model_of_, model_of)) || (rc = up(&d_scene_of_, scene_of)) || (rc = up(&d_gfield_, gfield)) ||
+        (rc = up(&d_glob_, glob_)))
+        return rc;
     {
         std::vector<uint32_t> gidx(n_, 0xffffffffu);
         for (uint32_t q = 0; q < glob_.size(); ++q) gidx[glob_[q]] = q;
-        MCK(mal(&d_gidx_, n_));
-        MCK(cudaMemcpy(d_gidx_, gidx.data(), 4 * n_, cudaMemcpyHostToDevice));
+        if ((rc = up(&d_gidx_, gidx))) return rc;
         MCK(mal(&d_wptr_, glob_.size() + 1));
     }
+    sdev_.resize(sc_.size());
+    MCK(mal(&d_scenes_, sc_.size()));
+    MCK(mal(&d_sred_, 8 * sc_.size()));
     for (int b = 0; b < 2; ++b) {
         MCK(mal(&d_x_[b], n_));
         MCK(mal(&d_v32_[b], n_));
@@ -1044,50 +1240,40 @@ int MixedEngine::init(const HScene& scene, const vedo_engine_opts& opts) {
     }
     MCK(mal(&d_v64_, n_)); MCK(mal(&d_w64_, n_)); MCK(mal(&d_ox_, n_)); MCK(mal(&d_oz_, n_));
     MCK(mal(&d_imp_, n_)); MCK(mal(&d_aimp_, n_)); MCK(mal(&d_pos32_, n_)); MCK(mal(&d_wall32_, n_));
-    MCK(mal(&d_red_, 16)); MCK(mal(&d_disp_, 1)); MCK(mal(&d_err_, 1));
+    MCK(mal(&d_red_, 16)); MCK(mal(&d_disp_, 2)); MCK(mal(&d_err_, 1));
     MCK(mal(&d_key_, n_)); MCK(mal(&d_key_alt_, n_)); MCK(mal(&d_sid_, n_)); MCK(mal(&d_sid_alt_, n_));
     MCK(mal(&d_cnt_, (size_t)n_ + 1));
     MCK(mal(&d_stage_, 7 * 3 * (size_t)n_));
     MCK(mal(&d_obs_, (size_t)(nblk(n_) + 2) * 16 + 64));
     MCK(cudaMemset(d_red_, 0, 64));
-    MCK(cudaMemset(d_disp_, 0, 4));
-    // bounding box centre as FP32 origin
+    MCK(cudaMemset(d_disp_, 0, 8));
     double lo[3] = {DBL_MAX, DBL_MAX, DBL_MAX}, hi[3] = {-DBL_MAX, -DBL_MAX, -DBL_MAX};
     for (uint32_t i = 0; i < n_; ++i)
         for (int k = 0; k < 3; ++k) {
-            lo[k] = std::min(lo[k], host_.pos[3 * i + k]);
-            hi[k] = std::max(hi[k], host_.pos[3 * i + k]);
+            lo[k] = std::min(lo[k], pos[3 * i + k]);
+            hi[k] = std::max(hi[k], pos[3 * i + k]);
         }
     for (int k = 0; k < 3; ++k) origin_[k] = 0.5 * (lo[k] + hi[k]);
-    vedo_state_view v{host_.pos.data(), host_.vel.data(), host_.av.data(), host_.ox.data(), host_.oz.data(),
-                      host_.imp.data(), host_.aimp.data()};
+    vedo_state_view v{pos.data(), vel.data(), av.data(), ox.data(), oz.data(), imp.data(), aimp.data()};
     rc = set_state(v);
     if (rc != VEDO_OK) return rc;
-    // history from the scene's records: carried into the first list by key
-    // (IactRecordTab::GetImpactStatus); stored temporarily as an "old list" of owner entries.
-    if (host_.rec.size()) {
-        std::vector<std::vector<std::pair<uint32_t, uint32_t>>> per(n_);
-        for (uint32_t q = 0; q < host_.rec.size(); ++q) {
-            uint32_t a = host_.rec.first[q], b = host_.rec.second[q];
-            if (a >= n_ || b >= n_) continue;
-            const bool bw = tab_.models[host_.model_of[b]].scope != SCOPE_LOCAL;
-            const bool aw = tab_.models[host_.model_of[a]].scope != SCOPE_LOCAL;
-            if (aw && !bw) std::swap(a, b);     // wall pairs are owned by the sphere
-            per[a].push_back({bw || aw ? (b | WALL_BIT) : b, q});
-        }
+    // records play the role of the previous neighbour list for the first history carry
+    size_t nrec = 0;
+    for (auto& r : recs) nrec += r.size();
+    if (nrec) {
+        std::vector<std::vector<Rec*>> per(n_);
+        for (auto& rv : recs)
+            for (auto& r : rv) per[r.a].push_back(&r);
         std::vector<uint32_t> optr(n_ + 1, 0), oent, oslot;
         std::vector<float4> oh;
         std::vector<uint8_t> of;
         for (uint32_t i = 0; i < n_; ++i) {
             optr[i] = (uint32_t)oent.size();
-            for (auto& pq : per[i]) {
-                const uint32_t q = pq.second;
+            for (Rec* r : per[i]) {
                 oslot.push_back((uint32_t)oent.size());
-                oent.push_back(pq.first);
-                oh.push_back(make_float4((float)host_.rec.shear[3 * q], (float)host_.rec.shear[3 * q + 1],
-                                         (float)host_.rec.shear[3 * q + 2], (float)host_.rec.kn[q]));
-                of.push_back((uint8_t)(HF_LAST_CONTACT | HF_LAST_BOND | (host_.rec.contact[q] ? HF_CONTACT : 0) |
-                                       (host_.rec.bond[q] ? HF_BOND : 0)));
+                oent.push_back(r->b);
+                oh.push_back(r->h);
+                of.push_back(r->f);
             }
         }
         optr[n_] = (uint32_t)oent.size();
@@ -1100,7 +1286,7 @@ int MixedEngine::init(const HScene& scene, const vedo_engine_opts& opts) {
         MCK(cudaMemcpy(O.slot, oslot.data(), 4 * oslot.size(), cudaMemcpyHostToDevice));
         MCK(cudaMemcpy(O.h[cur_], oh.data(), sizeof(float4) * oh.size(), cudaMemcpyHostToDevice));
         MCK(cudaMemcpy(O.f[cur_], of.data(), of.size(), cudaMemcpyHostToDevice));
-        nlc_ = 1;   // the records play the role of the previous list
+        nlc_ = 1;
     }
     rc = rebuild();
     if (rc != VEDO_OK) return rc;
@@ -1112,7 +1298,8 @@ TickArgs MixedEngine::args(bool write_imp) {
     NList& L = nl_[nlc_];
     TickArgs a;
     a.n = n_;
-    a.nm = nm_;
+    a.scenes = d_scenes_;
+    a.scene_of = d_scene_of_;
     a.model_of = d_model_of_;
     a.models = d_models_;
     a.params = d_params_;
@@ -1138,11 +1325,10 @@ TickArgs MixedEngine::args(bool write_imp) {
     a.imp = d_imp_;
     a.aimp = d_aimp_;
     a.write_imp = write_imp ? 1 : 0;
-    a.dt = dt_;
-    a.fimp = muls(mk(g_[0], g_[1], g_[2]), dt_);
     a.vmax_bits = d_red_ + 8;
     a.pos32 = d_pos32_;
-    a.disp = d_disp_;
+    a.disp = d_disp_ + cur_;
+    a.half_skin = 0.5f * skin_min_;
     a.reach = d_reach_;
     a.wall32 = d_wall32_;
     a.wimp = d_wimp_;
@@ -1154,14 +1340,17 @@ TickArgs MixedEngine::args(bool write_imp) {
 int MixedEngine::rebuild() {
     const uint64_t l0 = g_sort_scan_launches;
     uint64_t own = 0;
+    const uint32_t S = (uint32_t)sc_.size();
     const d3 org = mk(origin_[0], origin_[1], origin_[2]);
-    unsigned red0[8] = {0xffffffffu, 0xffffffffu, 0xffffffffu, 0, 0, 0, 0, 0};
-    MCK(cudaMemcpyAsync(d_red_, red0, sizeof(red0), cudaMemcpyHostToDevice, stream_));
-    k_bounds<<<nblk(n_), TPB, 0, stream_>>>(n_, d_model_of_, d_models_, d_x_[cur_], org, d_pos32_, d_red_);
+    std::vector<unsigned> red0(8 * (size_t)S, 0u);
+    for (uint32_t s = 0; s < S; ++s) red0[8 * s] = red0[8 * s + 1] = red0[8 * s + 2] = 0xffffffffu;
+    MCK(cudaMemcpyAsync(d_sred_, red0.data(), 4 * red0.size(), cudaMemcpyHostToDevice, stream_));
+    k_bounds<<<nblk(n_), TPB, 0, stream_>>>(n_, d_model_of_, d_models_, d_scene_of_, d_x_[cur_], org, d_pos32_,
+                                            d_sred_);
     k_wall32<<<nblk(n_), TPB, 0, stream_>>>(n_, d_model_of_, d_models_, d_ox_, d_oz_, d_wall32_);
     own += 2;
-    unsigned red[8];
-    MCK(cudaMemcpyAsync(red, d_red_, sizeof(red), cudaMemcpyDeviceToHost, stream_));
+    std::vector<unsigned> red(8 * (size_t)S);
+    MCK(cudaMemcpyAsync(red.data(), d_sred_, 4 * red.size(), cudaMemcpyDeviceToHost, stream_));
     MCK(cudaStreamSynchronize(stream_));
     auto unord = [](unsigned o) {
         unsigned b = (o >> 31) ? (o & 0x7fffffffu) : ~o;
@@ -1169,24 +1358,47 @@ int MixedEngine::rebuild() {
         memcpy(&f, &b, 4);
         return f;
     };
-    float lo[3], hi[3];
-    for (int k = 0; k < 3; ++k) {
-        lo[k] = nloc_ ? unord(red[k]) : 0.0f;
-        hi[k] = nloc_ ? unord(red[3 + k]) : 0.0f;
-    }
-    float rmax;
-    memcpy(&rmax, &red[6], 4);
-    float h = (2.0f * rmax + skin_abs_) * (1.0f + 1e-5f);
-    uint32_t nc[3];
+    // per-scene cell grids (edge 2 r_max + skin), packed one after the other
     uint64_t cells = 0;
-    const uint64_t cell_budget = std::max<uint64_t>(8ull * n_, 1ull << 22);
-    for (int pass = 0; pass < 8; ++pass) {
-        for (int k = 0; k < 3; ++k) nc[k] = std::max<uint32_t>(1, (uint32_t)std::floor((hi[k] - lo[k]) / h) + 1);
-        cells = (uint64_t)nc[0] * nc[1] * nc[2];
-        if (cells <= cell_budget) break;
-        // sparse scene: a coarser grid still finds every neighbour within one cell
-        h *= (float)std::cbrt((double)cells / cell_budget) * 1.01f;
+    for (uint32_t s = 0; s < S; ++s) {
+        SceneDev& D = sdev_[s];
+        const SceneHost& H = sc_[s];
+        D.model_off = H.model_off;
+        D.nm = H.nm;
+        D.pbase = H.pbase;
+        D.wall_beg = H.wall_beg;
+        D.wall_end = H.wall_end;
+        D.obj_off = H.obj_off;
+        D.nobj = H.nobj;
+        D.pad = 0;
+        D.dt = H.dt;
+        float lo[3] = {0, 0, 0}, hi[3] = {0, 0, 0};
+        if (H.nloc)
+            for (int k = 0; k < 3; ++k) {
+                lo[k] = unord(red[8 * s + k]);
+                hi[k] = unord(red[8 * s + 3 + k]);
+            }
+        float rmax;
+        memcpy(&rmax, &red[8 * s + 6], 4);
+        float h = (2.0f * rmax + H.skin) * (1.0f + 1e-5f);
+        if (!(h > 0.0f)) h = 1.0f;
+        const uint64_t budget = std::max<uint64_t>(8ull * std::max<uint32_t>(H.nobj, 1), 1ull << 12);
+        uint32_t nc[3] = {1, 1, 1};
+        for (int pass = 0; pass < 8; ++pass) {
+            for (int k = 0; k < 3; ++k) nc[k] = std::max<uint32_t>(1, (uint32_t)std::floor((hi[k] - lo[k]) / h) + 1);
+            const uint64_t c = (uint64_t)nc[0] * nc[1] * nc[2];
+            if (c <= budget) break;
+            h *= (float)std::cbrt((double)c / budget) * 1.01f;   // sparse scene: coarser cells
+        }
+        for (int k = 0; k < 3; ++k) {
+            D.nc[k] = nc[k];
+            D.lo[k] = lo[k];
+        }
+        D.inv_h = 1.0f / h;
+        D.cell_base = cells;
+        cells += (uint64_t)nc[0] * nc[1] * nc[2];
     }
+    MCK(cudaMemcpyAsync(d_scenes_, sdev_.data(), sizeof(SceneDev) * S, cudaMemcpyHostToDevice, stream_));
     if (cells > grid_cap_) {
         if (d_gs_) cudaFree(d_gs_);
         if (d_ge_) cudaFree(d_ge_);
@@ -1196,8 +1408,8 @@ int MixedEngine::rebuild() {
     }
     MCK(cudaMemsetAsync(d_gs_, 0, 4 * cells, stream_));
     MCK(cudaMemsetAsync(d_ge_, 0, 4 * cells, stream_));
-    k_keys<<<nblk(n_), TPB, 0, stream_>>>(n_, d_model_of_, d_models_, d_pos32_, make_float3(lo[0], lo[1], lo[2]),
-                                          1.0f / h, nc[0], nc[1], nc[2], cells, d_key_, d_sid_);
+    k_keys<<<nblk(n_), TPB, 0, stream_>>>(n_, d_model_of_, d_models_, d_scene_of_, d_scenes_, d_pos32_, cells,
+                                          d_key_, d_sid_);
     ++own;
     int bits = 1;
     while (bits < 64 && (cells >> bits)) ++bits;
@@ -1213,10 +1425,9 @@ int MixedEngine::rebuild() {
     if (!L.ptr) MCK(mal(&L.ptr, (size_t)n_ + 1));
     MCK(cudaMemsetAsync(d_cnt_, 0, 4 * ((size_t)n_ + 1), stream_));
     if (nloc_) {
-        k_nbr<false><<<nblk(nloc_), TPB, 0, stream_>>>(nloc_, d_sid_, d_key_, d_gs_, d_ge_, nc[0], nc[1], nc[2],
-                                                       d_glob_, (uint32_t)glob_.size(), d_model_of_, d_models_,
-                                                       d_params_, d_reach_, nm_, d_pos32_, d_wall32_, skin_abs_,
-                                                       d_cnt_, nullptr);
+        k_nbr<false><<<nblk(nloc_), TPB, 0, stream_>>>(nloc_, d_sid_, d_key_, d_gs_, d_ge_, d_scene_of_, d_scenes_,
+                                                       d_glob_, d_model_of_, d_models_, d_params_, d_reach_,
+                                                       d_pos32_, d_wall32_, skin_min_, d_cnt_, nullptr);
         ++own;
     }
     MCK(exclusive_scan_u32(d_cnt_, L.ptr, n_ + 1, d_red_ + 9, scratch_, stream_));
@@ -1227,9 +1438,9 @@ int MixedEngine::rebuild() {
     if (rc != VEDO_OK) return rc;
     L.ne = ne;
     if (nloc_) {
-        k_nbr<true><<<nblk(nloc_), TPB, 0, stream_>>>(nloc_, d_sid_, d_key_, d_gs_, d_ge_, nc[0], nc[1], nc[2], d_glob_,
-                                                      (uint32_t)glob_.size(), d_model_of_, d_models_, d_params_,
-                                                      d_reach_, nm_, d_pos32_, d_wall32_, skin_abs_, L.ptr, L.ent);
+        k_nbr<true><<<nblk(nloc_), TPB, 0, stream_>>>(nloc_, d_sid_, d_key_, d_gs_, d_ge_, d_scene_of_, d_scenes_,
+                                                      d_glob_, d_model_of_, d_models_, d_params_, d_reach_, d_pos32_,
+                                                      d_wall32_, skin_min_, L.ptr, L.ent);
         ++own;
     }
     MCK(cudaMemsetAsync(d_err_, 0, 4, stream_));
@@ -1251,7 +1462,8 @@ int MixedEngine::rebuild() {
                 *p = nullptr;
             }
             wcap_ = nw + nw / 4 + 64;
-            MCK(mal(&d_wkey_, wcap_)); MCK(mal(&d_wval_, wcap_)); MCK(mal(&d_wkey_alt_, wcap_)); MCK(mal(&d_wval_alt_, wcap_));
+            MCK(mal(&d_wkey_, wcap_)); MCK(mal(&d_wval_, wcap_)); MCK(mal(&d_wkey_alt_, wcap_));
+            MCK(mal(&d_wval_alt_, wcap_));
         }
         nwall_ent_ = nw;
         k_wall_fill<<<nblk(n_), TPB, 0, stream_>>>(n_, L.ptr, L.ent, d_cnt_, d_gidx_, d_wkey_, d_wval_);
@@ -1266,9 +1478,22 @@ int MixedEngine::rebuild() {
             MCK(mal(&d_wimp_, wimp_cap_));
         }
     }
+    // orbital walls' plane speed (the spheres' speed is measured every step)
+    float rmax_all = 0.0f;
+    for (uint32_t s = 0; s < S; ++s) {
+        float r;
+        memcpy(&r, &red[8 * s + 6], 4);
+        rmax_all = std::max(rmax_all, r);
+    }
+    MCK(cudaMemsetAsync(d_red_ + 11, 0, 8, stream_));
+    if (!glob_.empty()) {
+        k_wall_speed<<<nblk(glob_.size()), TPB, 0, stream_>>>((uint32_t)glob_.size(), d_glob_, d_model_of_, d_models_,
+                                                             d_v64_, d_w64_, d_oz_, 2.0f * rmax_all, d_red_ + 12);
+        ++own;
+    }
     int herr = 0;
     MCK(cudaMemcpyAsync(&herr, d_err_, 4, cudaMemcpyDeviceToHost, stream_));
-    MCK(cudaMemsetAsync(d_disp_, 0, 4, stream_));
+    MCK(cudaMemsetAsync(d_disp_, 0, 8, stream_));
     MCK(cudaStreamSynchronize(stream_));
     MCK(cudaGetLastError());
     if (herr) return fail(VEDO_ERR_CUDA, "mixed form: asymmetric neighbour lists");
@@ -1285,45 +1510,61 @@ int MixedEngine::run(uint32_t nsteps, int* keep_running) {
     launches_ = 0;
     MCK(cudaSetDevice(opts_.device));
     MCK(cudaEventRecord(ev_[0], stream_));
-    const float half_skin = 0.5f * skin_abs_;
-    for (uint32_t s = 0; s < nsteps; ++s) {
+    const float half_skin = 0.5f * skin_min_;
+    const uint32_t ci = opts_.check_interval;
+    uint32_t done = 0;
+    while (done < nsteps) {
         if (need_rebuild_) {
             int rc = rebuild();
             if (rc != VEDO_OK) return rc;
         }
-        TickArgs a = args(s + 1 == nsteps);
-        switch (law_) {
-        case IS_BSDBF: k_tick<IS_BSDBF><<<nblk(n_), TPB, 0, stream_>>>(a); break;
-        case IS_BTSDBF: k_tick<IS_BTSDBF><<<nblk(n_), TPB, 0, stream_>>>(a); break;
-        case IS_BSDB2F: k_tick<IS_BSDB2F><<<nblk(n_), TPB, 0, stream_>>>(a); break;
-        case IS_HERTZ: k_tick<IS_HERTZ><<<nblk(n_), TPB, 0, stream_>>>(a); break;
-        case IS_H: k_tick<IS_H><<<nblk(n_), TPB, 0, stream_>>>(a); break;
-        default: k_tick<0><<<nblk(n_), TPB, 0, stream_>>>(a); break;
-        }
-        ++launches_;
-        if (a.write_imp && !glob_.empty()) {
-            k_wall_sum<<<nblk((uint64_t)glob_.size() * 32), TPB, 0, stream_>>>(
-                (uint32_t)glob_.size(), d_glob_, d_wptr_, d_wval_, d_wimp_, d_model_of_, d_models_, dt_, a.fimp,
-                d_imp_, d_aimp_);
+        // up to the next displacement check
+        const uint32_t chunk = std::min<uint32_t>(nsteps - done, ci - (uint32_t)(since_rebuild_ % ci));
+        for (uint32_t k = 0; k < chunk; ++k) {
+            TickArgs a = args(done + k + 1 == nsteps);
+            switch (law_) {
+            case IS_BSDBF: k_tick<IS_BSDBF><<<nblk(n_), TPB, 0, stream_>>>(a); break;
+            case IS_BTSDBF: k_tick<IS_BTSDBF><<<nblk(n_), TPB, 0, stream_>>>(a); break;
+            case IS_BSDB2F: k_tick<IS_BSDB2F><<<nblk(n_), TPB, 0, stream_>>>(a); break;
+            case IS_HERTZ: k_tick<IS_HERTZ><<<nblk(n_), TPB, 0, stream_>>>(a); break;
+            case IS_H: k_tick<IS_H><<<nblk(n_), TPB, 0, stream_>>>(a); break;
+            default: k_tick<0><<<nblk(n_), TPB, 0, stream_>>>(a); break;
+            }
             ++launches_;
+            if (a.write_imp && !glob_.empty()) {
+                k_wall_sum<<<nblk((uint64_t)glob_.size() * 32), TPB, 0, stream_>>>(
+                    (uint32_t)glob_.size(), d_glob_, d_wptr_, d_wval_, d_wimp_, d_model_of_, d_models_, d_scenes_,
+                    d_scene_of_, d_gfield_, d_imp_, d_aimp_);
+                ++launches_;
+            }
+            // walls move; thread 0 writes the displacement bound after the step
+            k_walls<<<nblk(std::max<size_t>(glob_.size(), 1)), TPB, 0, stream_>>>(
+                (uint32_t)glob_.size(), d_glob_, d_model_of_, d_models_, d_scenes_, d_scene_of_, a.xA, a.xB, d_v64_,
+                d_w64_, a.v32A, a.v32B, a.w32A, a.w32B, d_ox_, d_oz_, dt_max_, d_red_ + 8, d_disp_ + cur_,
+                d_disp_ + (cur_ ^ 1), half_skin, d_red_ + 12, d_red_ + 11, d_wall32_);
+            ++launches_;
+            cur_ ^= 1;
         }
-        // walls move; thread 0 also adds dt * max|v| of the step to the displacement bound
-        k_walls<<<nblk(std::max<size_t>(glob_.size(), 1)), TPB, 0, stream_>>>(
-            (uint32_t)glob_.size(), d_glob_, d_model_of_, d_models_, a.xA, a.xB, d_v64_, d_w64_, a.v32A, a.v32B,
-            a.w32A, a.w32B, d_ox_, d_oz_, dt_, d_red_ + 8, d_disp_, d_wall32_);
-        ++launches_;
-        cur_ ^= 1;
-        ++round_;
-        ++since_rebuild_;
-        t_ += dt_;
-        if (since_rebuild_ % opts_.check_interval == 0) {
-            // Rebuild before any sphere can have moved half the skin: the bound so far plus
-            // twice its mean growth per step over the next check interval.
-            float disp = 0.0f;
-            MCK(cudaMemcpyAsync(&disp, d_disp_, 4, cudaMemcpyDeviceToHost, stream_));
-            MCK(cudaStreamSynchronize(stream_));
+        float disp = 0.0f;
+        unsigned held = 0;
+        MCK(cudaMemcpyAsync(&disp, d_disp_ + cur_, 4, cudaMemcpyDeviceToHost, stream_));
+        MCK(cudaMemcpyAsync(&held, d_red_ + 11, 4, cudaMemcpyDeviceToHost, stream_));
+        MCK(cudaStreamSynchronize(stream_));
+        const uint32_t taken = chunk - std::min(held, chunk);
+        done += taken;
+        round_ += taken;
+        since_rebuild_ += taken;
+        for (auto& S : sc_)
+            for (uint32_t k = 0; k < taken; ++k) S.t += S.dt;     // SystemParameter::NextStep (SystemParameter.h:113-116), once per step
+        if (held || disp > half_skin) {
+            // held steps are taken again after the rebuild; a bound already past half the skin
+            // would hold the next step, and contact queries need a complete list too
+            need_rebuild_ = true;
+        } else if (since_rebuild_ % ci == 0) {
+            // Rebuild before the bound can reach half the skin: the bound so far plus twice its
+            // mean growth per step over the next check interval.
             const float growth = disp / (float)since_rebuild_;
-            if (disp + 2.0f * growth * (float)opts_.check_interval > half_skin) need_rebuild_ = true;
+            if (disp + 2.0f * growth * (float)ci > half_skin) need_rebuild_ = true;
         }
     }
     MCK(cudaEventRecord(ev_[1], stream_));
@@ -1332,7 +1573,7 @@ int MixedEngine::run(uint32_t nsteps, int* keep_running) {
     float ms = 0;
     cudaEventElapsedTime(&ms, ev_[0], ev_[1]);
     prof_[3] = ms;
-    if (keep_running) *keep_running = t_ < t_stop_ ? 1 : 0;
+    if (keep_running) *keep_running = sc_[0].t < sc_[0].t_stop ? 1 : 0;
     return VEDO_OK;
 }
 
@@ -1374,12 +1615,9 @@ int MixedEngine::num_interactions(uint32_t* n) {
         int rc = rebuild();
         if (rc != VEDO_OK) return rc;
     }
-    // owner entries only
     NList& L = nl_[nlc_];
     std::vector<uint32_t> slot(L.ne);
-    if (L.ne) {
-        MCK(cudaMemcpy(slot.data(), L.slot, 4 * L.ne, cudaMemcpyDeviceToHost));
-    }
+    if (L.ne) MCK(cudaMemcpy(slot.data(), L.slot, 4 * L.ne, cudaMemcpyDeviceToHost));
     uint32_t c = 0;
     for (uint32_t e = 0; e < L.ne; ++e) c += slot[e] == e;
     *n = c;
@@ -1398,9 +1636,7 @@ int MixedEngine::get_interactions(const vedo_contact_view& v) {
         act_cap_ = ne + ne / 4 + 16;
         MCK(mal(&d_act_, act_cap_));
     }
-    if (ne) {
-        k_active<<<nblk(n_), TPB, 0, stream_>>>(n_, args(false), d_act_);
-    }
+    if (ne) k_active<<<nblk(n_), TPB, 0, stream_>>>(n_, args(false), d_act_);
     std::vector<uint32_t> ptr(n_ + 1), ent(ne), slot(ne);
     std::vector<uint8_t> act(ne), fl(ne);
     std::vector<float4> h(ne);
@@ -1413,7 +1649,6 @@ int MixedEngine::get_interactions(const vedo_contact_view& v) {
         MCK(cudaMemcpyAsync(h.data(), L.h[cur_], sizeof(float4) * ne, cudaMemcpyDeviceToHost, stream_));
     }
     MCK(cudaStreamSynchronize(stream_));
-    // owner entries sorted by (first, second)
     struct Row { uint32_t a, b, sl, ms; uint32_t e; };
     std::vector<Row> rows;
     for (uint32_t i = 0; i < n_; ++i)
@@ -1449,6 +1684,10 @@ int MixedEngine::get_interactions(const vedo_contact_view& v) {
 }
 
 int MixedEngine::get_observables(double out[13]) {
+    if (need_rebuild_) {
+        int rc = rebuild();
+        if (rc != VEDO_OK) return rc;
+    }
     NList& L = nl_[nlc_];
     if (L.ne > act_cap_) {
         if (d_act_) cudaFree(d_act_);
@@ -1459,7 +1698,7 @@ int MixedEngine::get_observables(double out[13]) {
     const unsigned nb = std::max(1u, nblk(n_));
     double* part = d_obs_;
     double* res = d_obs_ + (size_t)nb * 16 + 16;
-    const d3 g = mk(g_[0], g_[1], g_[2]);
+    const d3 g = mk(sc_[0].g[0], sc_[0].g[1], sc_[0].g[2]);
     obs::k_obs_a<<<nb, TPB, 0, stream_>>>(n_, d_model_of_, d_models_, d_x_[cur_], d_v64_, d_w64_, g, part);
     obs::k_obs_reduce<<<1, 32, 0, stream_>>>(nb, 16, part, res, 12);
     obs::k_obs_b<<<nb, TPB, 0, stream_>>>(n_, d_model_of_, d_models_, d_x_[cur_], d_v64_, d_w64_, res, 0, d_act_,
@@ -1480,11 +1719,13 @@ int MixedEngine::get_observables(double out[13]) {
 }
 
 int MixedEngine::write_ido(const char* path) {
-    vedo_state_view v{host_.pos.data(), host_.vel.data(), host_.av.data(), host_.ox.data(), host_.oz.data(),
-                      host_.imp.data(), host_.aimp.data()};
+    if (sc_.size() != 1) return fail(VEDO_ERR_INVALID_ARGUMENT, "write_ido needs a single-scene engine");
+    HScene& hs = host_[0];
+    vedo_state_view v{hs.pos.data(), hs.vel.data(), hs.av.data(), hs.ox.data(), hs.oz.data(), hs.imp.data(),
+                      hs.aimp.data()};
     int rc = get_state(v);
     if (rc != VEDO_OK) return rc;
-    host_.time_current = t_;
+    hs.time_current = sc_[0].t;
     uint32_t np = 0;
     rc = num_interactions(&np);
     if (rc != VEDO_OK) return rc;
@@ -1506,7 +1747,7 @@ int MixedEngine::write_ido(const char* path) {
         }
         R.overlap.push_back(0.0);
     }
-    HScene s = host_;
+    HScene s = hs;
     s.rec = R;
     std::string msg;
     if (!vedo::write_ido(path, s, msg)) return fail(VEDO_ERR_IO, msg);
@@ -1514,5 +1755,35 @@ int MixedEngine::write_ido(const char* path) {
 }
 
 EngineBase* make_mixed_engine() { return new (std::nothrow) MixedEngine(); }
+
+// batch construction for the C ABI (capi.cpp)
+EngineBase* make_mixed_batch(const std::vector<const HScene*>& scenes, const vedo_engine_opts& opts, int* rc,
+                             std::string* err) {
+    MixedEngine* e = new (std::nothrow) MixedEngine();
+    if (!e) {
+        *rc = VEDO_ERR_OUT_OF_MEMORY;
+        return nullptr;
+    }
+    *rc = e->init_batch(scenes, opts);
+    if (*rc != VEDO_OK) {
+        *err = e->error();
+        delete e;
+        return nullptr;
+    }
+    return e;
+}
+
+int mixed_scene_range(EngineBase* e, uint32_t s, uint32_t* off, uint32_t* n, double* t) {
+    MixedEngine* m = dynamic_cast<MixedEngine*>(e);
+    if (!m) return VEDO_ERR_INVALID_ARGUMENT;
+    int rc = m->scene_range(s, off, n);
+    if (rc == VEDO_OK && t) *t = m->scene_time(s);
+    return rc;
+}
+
+uint32_t mixed_num_scenes(EngineBase* e) {
+    MixedEngine* m = dynamic_cast<MixedEngine*>(e);
+    return m ? m->num_scenes() : 1u;
+}
 
 }  // namespace vedo

@@ -61,12 +61,30 @@ def lib() -> C.CDLL:
         L.vedo_gpu_last_error.restype = C.c_char_p
         L.vedo_gpu_destroy.argtypes = [vp]
         L.vedo_gpu_version.restype = C.c_char_p
+        L.vedo_gpu_create_batch.argtypes = [C.POINTER(C.POINTER(_abi.SceneDesc)), C.c_uint32,
+                                            C.POINTER(EngineOpts), C.POINTER(vp)]
+        L.vedo_gpu_num_scenes.argtypes = [vp]
+        L.vedo_gpu_num_scenes.restype = C.c_uint32
+        L.vedo_gpu_scene_range.argtypes = [vp, C.c_uint32, C.POINTER(C.c_uint32), C.POINTER(C.c_uint32),
+                                           C.POINTER(C.c_double)]
         _lib = L
     return _lib
 
 
 STATE_FIELDS = ("position", "velocity", "angular_velocity", "orientation_x", "orientation_z", "impact",
                 "angular_impact")
+
+
+def _opts(up_iact, record, precision, device, prefix, skin, check_interval) -> EngineOpts:
+    opts = EngineOpts()
+    lib().vedo_gpu_default_opts(C.byref(opts))
+    opts.up_iact, opts.record, opts.precision, opts.device = up_iact, record, precision, device
+    if skin is not None:
+        opts.skin = skin
+    if check_interval is not None:
+        opts.check_interval = check_interval
+    opts.output_prefix = prefix
+    return opts
 
 
 class GpuEngine:
@@ -81,15 +99,8 @@ class GpuEngine:
                  device: int = 0, output_prefix: Optional[str] = None, skin: Optional[float] = None,
                  check_interval: Optional[int] = None):
         L = lib()
-        opts = EngineOpts()
-        L.vedo_gpu_default_opts(C.byref(opts))
-        opts.up_iact, opts.record, opts.precision, opts.device = up_iact, record, precision, device
-        if skin is not None:
-            opts.skin = skin
-        if check_interval is not None:
-            opts.check_interval = check_interval
         self._prefix = output_prefix.encode() if output_prefix else None
-        opts.output_prefix = self._prefix
+        opts = _opts(up_iact, record, precision, device, self._prefix, skin, check_interval)
         h = C.c_void_p()
         if isinstance(scene, (str, bytes, os.PathLike)):
             rc = L.vedo_gpu_create_from_ido(os.fsencode(scene), C.byref(opts), C.byref(h))
@@ -192,3 +203,44 @@ class GpuEngine:
 
     def __exit__(self, *a):
         self.close()
+
+
+class BatchEngine(GpuEngine):
+    """Many independent scenes advanced together by one MIXED-form engine.
+
+    Objects are numbered scene after scene; :meth:`scene_range` gives a scene's
+    ``(first, count, time)`` and :meth:`scene_state` its slice of the state.  Each
+    scene's results are bit-identical to the same scene run alone in the MIXED form.
+    """
+
+    def __init__(self, scene_list, device: int = 0, skin: Optional[float] = None,
+                 check_interval: Optional[int] = None):
+        L = lib()
+        self._prefix = None
+        opts = _opts(1, 0, _abi.PRECISION_MIXED, device, None, skin, check_interval)
+        descs, keeps = [], []
+        for sc in scene_list:
+            if isinstance(sc, (str, bytes, os.PathLike)):
+                sc = Scene.from_ido(sc)
+            d, k = scene_to_desc(sc)
+            descs.append(d)
+            keeps.append(k)
+        arr = (C.POINTER(_abi.SceneDesc) * max(1, len(descs)))(*[C.pointer(d) for d in descs])
+        h = C.c_void_p()
+        rc = L.vedo_gpu_create_batch(arr, len(descs), C.byref(opts), C.byref(h))
+        del keeps
+        if rc != 0:
+            raise EngineError(rc, L.vedo_gpu_last_error(None).decode())
+        self.h = h
+        self.n = L.vedo_gpu_num_objects(h)
+        self.num_scenes = L.vedo_gpu_num_scenes(h)
+
+    def scene_range(self, s: int):
+        f, c, t = C.c_uint32(0), C.c_uint32(0), C.c_double(0)
+        self._check(lib().vedo_gpu_scene_range(self.h, s, C.byref(f), C.byref(c), C.byref(t)))
+        return int(f.value), int(c.value), float(t.value)
+
+    def scene_state(self, s: int, fields=STATE_FIELDS, state: Optional[Dict[str, np.ndarray]] = None):
+        f, c, _ = self.scene_range(s)
+        st = state if state is not None else self.state(fields)
+        return {k: st[k][f:f + c] for k in fields}

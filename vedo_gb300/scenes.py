@@ -239,7 +239,13 @@ def hertz_drum(n: int = 1_000_000, seed: int = 2024, steps: int = 10000, dt: flo
     from the bottom in horizontal lattice layers, largest first, each layer's spacing set by
     its largest sphere plus a `gap` fraction, which leaves no initial overlap and packs the
     1,000,000 default spheres into about 40 % of the drum volume.  Initial velocities are zero
-    unless `vel_sigma` (m/s, per component) is given."""
+    unless `vel_sigma` (m/s, per component) is given.
+
+    Object order is a seeded permutation with one sphere of the largest class moved to the end
+    of the sphere block.  The reference's NBS broad phase takes its cell size from the radius of
+    the last local object, not the largest (NBSConsultant.cpp:140); with a small sphere last,
+    contacts between large spheres are missed, they interpenetrate and the packing heats up.
+    With the largest radius last that cell size is the correct one."""
     rng = np.random.default_rng(seed)
     edges = np.exp(np.linspace(math.log(r_lo), math.log(r_hi), K + 1))
     centres = np.sqrt(edges[:-1] * edges[1:])
@@ -270,6 +276,8 @@ def hertz_drum(n: int = 1_000_000, seed: int = 2024, steps: int = 10000, dt: flo
         z += a
     pos += rng.uniform(-0.25 * gap, 0.25 * gap, size=pos.shape) * radii[:, None]
     perm = rng.permutation(n)                  # object order independent of the layer order
+    last = int(np.flatnonzero(cls[perm] == cls.max())[-1])
+    perm[[last, n - 1]] = perm[[n - 1, last]]  # a largest-class sphere last: see the docstring
     pos, cls = pos[perm], cls[perm]
     vel = rng.normal(0.0, vel_sigma, size=pos.shape) if vel_sigma > 0 else np.zeros_like(pos)
     models: List[DOModel] = []
