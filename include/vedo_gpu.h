@@ -256,6 +256,33 @@ uint32_t vedo_gpu_num_scenes(const vedo_gpu_engine* e);
 int vedo_gpu_scene_range(const vedo_gpu_engine* e, uint32_t scene, uint32_t* first_object, uint32_t* num_objects,
                          double* time);
 
+/* ---- allocation-free system energy --------------------------------------
+ * No counterpart in the reference.
+ * For callers that cannot let a library allocate device memory: a coupled solver or a
+ * framework whose own allocator already holds most of HBM (a new cudaMalloc would fail or
+ * fragment its pool), or a hook on a time-critical loop (cudaFree, and often cudaMalloc,
+ * synchronise the whole device).  The same quantities as vedo_gpu_get_observables, over
+ * object state that the caller keeps in its own device buffers:
+ *   position, velocity, angular_velocity, inertia: [n][3] doubles (principal moments);
+ *   mass: [n] doubles; mobile: [n] bytes, nonzero = counted (NULL counts every object);
+ *   field_acceleration: 3 doubles in host memory;
+ *   out: 12 doubles in device memory, written when the stream reaches the call:
+ *   out[0..8] as vedo_gpu_get_observables out[0..8], out[9..11] the mass-weighted centre.
+ * stream is a cudaStream_t (NULL = the legacy default stream); the call does not wait.
+ * The reduction's partial sums live in a fixed 1 MiB array that the library declares in
+ * device memory, which every GPU that loads the library holds until the process exits.
+ * The call allocates nothing.  At most VEDO_NOALLOC_MAX_OBJECTS objects; larger counts
+ * return VEDO_ERR_INVALID_ARGUMENT with a message (vedo_gpu_last_error(NULL)).  The first
+ * call on each device, with that device current, looks up the array's device address
+ * (cudaGetSymbolAddress); make that first call before any stream capture.  All calls
+ * share the one array: calls that overlap on the GPU (on different streams, or from
+ * different threads without ordering) race and give wrong results. */
+#define VEDO_NOALLOC_MAX_OBJECTS 16777216u
+int vedo_gpu_system_energy_noalloc(const double* position, const double* velocity, const double* angular_velocity,
+                                   const double* mass, const double* inertia, const uint8_t* mobile,
+                                   uint32_t num_objects, const double field_acceleration[3], double* out,
+                                   void* stream);
+
 #ifdef __cplusplus
 }
 #endif

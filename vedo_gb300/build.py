@@ -37,6 +37,7 @@ SOURCES = {
     "engine.cu": ("nvcc", ["-fmad=false"]),
     "mixed.cu": ("nvcc", ["-fmad=false"]),
     "sort_scan.cu": ("nvcc", []),
+    "noalloc.cu": ("nvcc", []),
     "scene_host.cpp": ("cxx", []),
     "capi.cpp": ("cxx", []),
 }

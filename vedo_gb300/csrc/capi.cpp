@@ -42,6 +42,10 @@ int create_common(const vedo::HScene& s, const vedo_engine_opts* opts, vedo_gpu_
 }
 }  // namespace
 
+namespace vedo {
+void set_last_error(const std::string& msg) { g_create_error = msg; }
+}  // namespace vedo
+
 extern "C" {
 
 void vedo_gpu_default_opts(vedo_engine_opts* o) {
