@@ -141,12 +141,23 @@ typedef struct vedo_engine_opts {
                                  largest sphere radius (default 0.15); the list is rebuilt
                                  when any sphere may have moved half of it             */
     uint32_t check_interval;  /* MIXED only: steps between displacement checks (10)   */
-    uint32_t reserved[2];
+    uint32_t tick_block;      /* MIXED only: threads per block of the tick kernel, 32..256,
+                                 a multiple of 32 (0 = 256)                            */
+    float cell_scale;         /* MIXED only: cell edge as a multiple of 2 r_max + skin,
+                                 >= 1 (0 = 1)                                          */
+    uint32_t autotune;        /* MIXED only: 1 = the first steps of the run choose the tick
+                                 block, the skin and the cell scale by timing (results do
+                                 not depend on them); read the choice with
+                                 vedo_gpu_get_tuning                                    */
+    uint32_t graphs;          /* MIXED only: 1 = each check interval of steps is replayed
+                                 as one CUDA graph, captured once per neighbour list (default) */
+    uint32_t reserved[4];
 } vedo_engine_opts;
 
 typedef struct vedo_gpu_engine vedo_gpu_engine;
 
-/* Default options: up_iact 1, record 0, FP64, device 0, no files. */
+/* Default options: up_iact 1, record 0, FP64, device 0, no files; MIXED: skin 0.15,
+ * check_interval 10, tick_block 256, cell_scale 1, no autotuning, graphs on. */
 void vedo_gpu_default_opts(vedo_engine_opts* opts);
 
 /* Build an engine from a scene.  Replaces DOWorld + NBSConsultant +
@@ -233,6 +244,10 @@ void vedo_gpu_set_profiling(vedo_gpu_engine* e, int on);
  * on this thread. */
 const char* vedo_gpu_last_error(const vedo_gpu_engine* e);
 void vedo_gpu_destroy(vedo_gpu_engine* e);
+
+/* Skin (fraction of r_max), cell scale and tick block size in use by a MIXED-form engine,
+ * after autotuning when it was asked for.  No counterpart in the reference. */
+int vedo_gpu_get_tuning(const vedo_gpu_engine* e, float* skin, float* cell_scale, uint32_t* tick_block);
 
 /* Library version string. */
 const char* vedo_gpu_version(void);

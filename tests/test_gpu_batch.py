@@ -79,3 +79,27 @@ def test_batch_rejects_fp64_and_empty(engine_lib, mix):
     arr[0] = C.pointer(d)
     assert L.vedo_gpu_create_batch(arr, 1, C.byref(opts), C.byref(h)) == 1     # FP64 form
     assert not h.value
+
+
+def test_autotuned_graph_batch_equals_plain_alone(engine_lib):
+    """Hoppers of uneven sizes in one autotuned batch whose check intervals replay as CUDA
+    graphs, against each hopper alone with fixed settings and direct launches: bit-identical,
+    because neither the tuned skin, cell scale and block size nor graph replay change a result."""
+    steps = 300
+    hs = [scenes.hopper(n=n, seed=s, friction=mu, restitution=e, orifice=w, steps=steps)
+          for n, s, mu, e, w in scenes.hopper_params(4, seed=7, n_lo=1000, n_hi=6000)]
+    b = engine_lib.BatchEngine(hs, autotune=True)
+    b.run(steps)
+    tune = b.tuning()
+    assert tune["tick_block"] in (64, 128, 256) and tune["cell_scale"] >= 1.0 and tune["skin"] > 0
+    st = b.state(FIELDS)
+    for s, sc in enumerate(hs):
+        e = engine_lib.GpuEngine(sc, precision=1, graphs=False, skin=0.15, tick_block=256)
+        e.run(steps)
+        ref = e.state(FIELDS)
+        e.close()
+        f, c, t = b.scene_range(s)
+        for k in FIELDS:
+            assert np.array_equal(st[k][f:f + c], ref[k]), (s, k)
+    # the spheres are falling: the discharge is under way
+    assert (st["velocity"][:, 2] < -0.01).sum() > 0

@@ -58,6 +58,10 @@ void vedo_gpu_default_opts(vedo_engine_opts* o) {
     o->output_prefix = nullptr;
     o->skin = 0.15f;
     o->check_interval = 10;
+    o->tick_block = 256;
+    o->cell_scale = 1.0f;
+    o->autotune = 0;
+    o->graphs = 1;
 }
 
 int vedo_gpu_create(const vedo_scene_desc* scene, const vedo_engine_opts* opts, vedo_gpu_engine** out) {
@@ -140,6 +144,17 @@ const char* vedo_gpu_last_error(const vedo_gpu_engine* e) {
 }
 
 void vedo_gpu_destroy(vedo_gpu_engine* e) { delete e; }
+
+int vedo_gpu_get_tuning(const vedo_gpu_engine* e, float* skin, float* cell_scale, uint32_t* tick_block) {
+    if (!e || !skin || !cell_scale || !tick_block) return VEDO_ERR_INVALID_ARGUMENT;
+    float t[3];
+    const int rc = e->p->tuning(t);
+    if (rc != VEDO_OK) return rc;
+    *skin = t[0];
+    *cell_scale = t[1];
+    *tick_block = (uint32_t)t[2];
+    return VEDO_OK;
+}
 
 const char* vedo_gpu_version(void) { return "vedo-gb300 0.1.0 (sm_103a)"; }
 

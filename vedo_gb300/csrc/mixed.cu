@@ -962,6 +962,12 @@ public:
         return VEDO_OK;
     }
     double scene_time(uint32_t s) const { return s < sc_.size() ? sc_[s].t : 0.0; }
+    int tuning(float out[3]) const override {
+        out[0] = skin_frac_;
+        out[1] = cell_scale_;
+        out[2] = (float)tpb_;
+        return VEDO_OK;
+    }
 
 private:
     struct NList {
@@ -975,7 +981,7 @@ private:
     struct SceneHost {
         uint32_t obj_off = 0, nobj = 0, model_off = 0, nm = 0, pbase = 0, wall_beg = 0, wall_end = 0, nloc = 0;
         double dt = 0, t = 0, t_stop = 0, g[3] = {0, 0, 0};
-        float skin = 0;
+        float skin = 0, rmax = 0;
     };
     int fail(int c, const std::string& m) { err_ = m; return c; }
     int cuda_fail(cudaError_t e, const char* where) {
@@ -983,6 +989,11 @@ private:
         return e == cudaErrorMemoryAllocation ? VEDO_ERR_OUT_OF_MEMORY : VEDO_ERR_CUDA;
     }
     int rebuild();
+    void launch_step(bool write_imp);
+    int step_chunk(uint32_t chunk, bool imp_last, float* disp_after);
+    int autotune(uint32_t max_steps, uint32_t* taken);
+    void set_skin(float frac);
+    void drop_graphs();
     int ensure_nlist(NList& L, uint32_t cap);
     void free_nlist(NList& L);
     TickArgs args(bool write_imp);
@@ -997,6 +1008,11 @@ private:
     uint32_t n_ = 0, nm_ = 0, nloc_ = 0, np_ = 0;
     double origin_[3] = {0, 0, 0};
     float dt_max_ = 0.0f, skin_min_ = 0.0f;
+    float skin_frac_ = 0.15f;       // skin as a fraction of each scene's largest radius
+    float cell_scale_ = 1.0f;       // cell edge = cell_scale * (2 r_max + skin)
+    int tpb_ = TPB;                 // threads per block of the tick kernel
+    bool tune_pending_ = false;
+    cudaGraphExec_t graph_[2] = {nullptr, nullptr};   // one check interval of steps, by start parity
     uint64_t round_ = 0;
     int cur_ = 0;                   // which of the A/B buffers is "A" (current)
     bool need_rebuild_ = true;
@@ -1096,13 +1112,35 @@ MixedEngine::~MixedEngine() {
                     d_key_, d_key_alt_, d_sid_, d_sid_alt_, d_cnt_, d_gs_, d_ge_, d_act_, d_stage_, d_obs_, d_gidx_,
                     d_wkey_, d_wval_, d_wkey_alt_, d_wval_alt_, d_wptr_, d_wimp_};
     for (void* p : ptrs) if (p) cudaFree(p);
+    drop_graphs();
     for (auto& e : ev_) if (e) cudaEventDestroy(e);
     if (stream_) cudaStreamDestroy(stream_);
+}
+
+void MixedEngine::drop_graphs() {
+    for (auto& g : graph_) {
+        if (g) cudaGraphExecDestroy(g);
+        g = nullptr;
+    }
+}
+
+void MixedEngine::set_skin(float frac) {
+    skin_frac_ = frac;
+    for (size_t k = 0; k < sc_.size(); ++k) {
+        sc_[k].skin = frac * sc_[k].rmax;
+        skin_min_ = k == 0 ? sc_[k].skin : std::min(skin_min_, sc_[k].skin);
+    }
+    need_rebuild_ = true;
 }
 
 int MixedEngine::init_batch(const std::vector<const HScene*>& scenes, const vedo_engine_opts& opts) {
     opts_ = opts;
     if (opts_.check_interval == 0) opts_.check_interval = 10;
+    skin_frac_ = opts.skin > 0 ? opts.skin : 0.15f;
+    cell_scale_ = opts.cell_scale >= 1.0f ? opts.cell_scale : 1.0f;
+    tpb_ = opts.tick_block ? (int)opts.tick_block : TPB;
+    if (tpb_ < 32 || tpb_ > TPB || tpb_ % 32) return fail(VEDO_ERR_INVALID_ARGUMENT, "tick_block must be 32..256, a multiple of 32");
+    tune_pending_ = opts.autotune != 0;
     if (scenes.empty()) return fail(VEDO_ERR_INVALID_SCENE, "empty batch");
     // ---- per-scene tables, concatenated
     std::vector<uint32_t> model_of, scene_of;
@@ -1149,7 +1187,8 @@ int MixedEngine::init_batch(const std::vector<const HScene*>& scenes, const vedo
             scene_of.push_back((uint32_t)sc_.size());
         }
         S.wall_end = (uint32_t)glob_.size();
-        S.skin = (float)((opts.skin > 0 ? opts.skin : 0.15f) * rmax);
+        S.rmax = (float)rmax;
+        S.skin = skin_frac_ * S.rmax;
         for (auto* pr : {&pos, &vel, &av, &ox, &oz, &imp, &aimp}) (void)pr;
         pos.insert(pos.end(), h.pos.begin(), h.pos.end());
         vel.insert(vel.end(), h.vel.begin(), h.vel.end());
@@ -1338,6 +1377,7 @@ TickArgs MixedEngine::args(bool write_imp) {
 }
 
 int MixedEngine::rebuild() {
+    drop_graphs();   // the captured launches name this list's buffers
     const uint64_t l0 = g_sort_scan_launches;
     uint64_t own = 0;
     const uint32_t S = (uint32_t)sc_.size();
@@ -1380,7 +1420,7 @@ int MixedEngine::rebuild() {
             }
         float rmax;
         memcpy(&rmax, &red[8 * s + 6], 4);
-        float h = (2.0f * rmax + H.skin) * (1.0f + 1e-5f);
+        float h = (2.0f * rmax + H.skin) * (1.0f + 1e-5f) * cell_scale_;
         if (!(h > 0.0f)) h = 1.0f;
         const uint64_t budget = std::max<uint64_t>(8ull * std::max<uint32_t>(H.nobj, 1), 1ull << 12);
         uint32_t nc[3] = {1, 1, 1};
@@ -1505,67 +1545,190 @@ int MixedEngine::rebuild() {
     return VEDO_OK;
 }
 
+// One time step's launches: the fused tick, the wall impulse sums on the last step of a call,
+// and the wall kernel (wall motion and the displacement bound after the step).
+void MixedEngine::launch_step(bool write_imp) {
+    TickArgs a = args(write_imp);
+    const unsigned nb = (unsigned)((n_ + tpb_ - 1) / tpb_);
+    switch (law_) {
+    case IS_BSDBF: k_tick<IS_BSDBF><<<nb, tpb_, 0, stream_>>>(a); break;
+    case IS_BTSDBF: k_tick<IS_BTSDBF><<<nb, tpb_, 0, stream_>>>(a); break;
+    case IS_BSDB2F: k_tick<IS_BSDB2F><<<nb, tpb_, 0, stream_>>>(a); break;
+    case IS_HERTZ: k_tick<IS_HERTZ><<<nb, tpb_, 0, stream_>>>(a); break;
+    case IS_H: k_tick<IS_H><<<nb, tpb_, 0, stream_>>>(a); break;
+    default: k_tick<0><<<nb, tpb_, 0, stream_>>>(a); break;
+    }
+    ++launches_;
+    if (write_imp && !glob_.empty()) {
+        k_wall_sum<<<nblk((uint64_t)glob_.size() * 32), TPB, 0, stream_>>>(
+            (uint32_t)glob_.size(), d_glob_, d_wptr_, d_wval_, d_wimp_, d_model_of_, d_models_, d_scenes_, d_scene_of_,
+            d_gfield_, d_imp_, d_aimp_);
+        ++launches_;
+    }
+    k_walls<<<nblk(std::max<size_t>(glob_.size(), 1)), TPB, 0, stream_>>>(
+        (uint32_t)glob_.size(), d_glob_, d_model_of_, d_models_, d_scenes_, d_scene_of_, a.xA, a.xB, d_v64_, d_w64_,
+        a.v32A, a.v32B, a.w32A, a.w32B, d_ox_, d_oz_, dt_max_, d_red_ + 8, d_disp_ + cur_, d_disp_ + (cur_ ^ 1),
+        0.5f * skin_min_, d_red_ + 12, d_red_ + 11, d_wall32_);
+    ++launches_;
+    cur_ ^= 1;
+}
+
+// `chunk` steps, then one read of the displacement bound and of the held-step count.  A full
+// check interval without impulse output replays a CUDA graph captured once per list.
+int MixedEngine::step_chunk(uint32_t chunk, bool imp_last, float* disp_after) {
+    const uint32_t ci = opts_.check_interval;
+    if (opts_.graphs && chunk == ci && !imp_last) {
+        const int c0 = cur_;
+        if (!graph_[c0]) {
+            cudaGraph_t g = nullptr;
+            const uint64_t l0 = launches_;
+            MCK(cudaStreamBeginCapture(stream_, cudaStreamCaptureModeThreadLocal));
+            for (uint32_t k = 0; k < chunk; ++k) launch_step(false);
+            const cudaError_t ce = cudaStreamEndCapture(stream_, &g);
+            launches_ = l0;
+            cur_ = c0;
+            if (ce != cudaSuccess) return cuda_fail(ce, "cudaStreamEndCapture");
+            const cudaError_t ie = cudaGraphInstantiate(&graph_[c0], g, 0);
+            cudaGraphDestroy(g);
+            if (ie != cudaSuccess) return cuda_fail(ie, "cudaGraphInstantiate");
+        }
+        MCK(cudaGraphLaunch(graph_[c0], stream_));
+        launches_ += (uint64_t)chunk * 2;
+        if (chunk & 1) cur_ ^= 1;
+    } else {
+        for (uint32_t k = 0; k < chunk; ++k) launch_step(imp_last && k + 1 == chunk);
+    }
+    float disp = 0.0f;
+    unsigned held = 0;
+    MCK(cudaMemcpyAsync(&disp, d_disp_ + cur_, 4, cudaMemcpyDeviceToHost, stream_));
+    MCK(cudaMemcpyAsync(&held, d_red_ + 11, 4, cudaMemcpyDeviceToHost, stream_));
+    MCK(cudaStreamSynchronize(stream_));
+    const uint32_t taken = chunk - std::min(held, chunk);
+    round_ += taken;
+    since_rebuild_ += taken;
+    for (auto& S : sc_)
+        for (uint32_t k = 0; k < taken; ++k) S.t += S.dt;     // SystemParameter::NextStep (SystemParameter.h:113-116), once per step
+    const float half_skin = 0.5f * skin_min_;
+    if (held || disp > half_skin) {
+        // held steps are taken again after the rebuild; a bound already past half the skin
+        // would hold the next step, and contact queries need a complete list too
+        need_rebuild_ = true;
+    } else if (since_rebuild_ % ci == 0) {
+        // Rebuild before the bound can reach half the skin: the bound so far plus twice its
+        // mean growth per step over the next check interval.
+        const float growth = disp / (float)since_rebuild_;
+        if (disp + 2.0f * growth * (float)ci > half_skin) need_rebuild_ = true;
+    }
+    if (disp_after) *disp_after = disp;
+    return (int)taken == (int)chunk ? VEDO_OK : -(int)(chunk - taken);
+}
+
+// Online tuning of the tick block size, the skin and the cell scale.  The trials are ordinary
+// steps of the run: results do not depend on any of the three (the list is complete for any
+// skin and rebuild schedule, and the per-sphere sums follow the canonical list order), so the
+// run's results are those of an untuned run.  Costs are CUDA-event device times: the tick
+// per step, and for the skin the rebuild time spread over the steps a list of that skin is
+// expected to last at the displacement growth just measured.
+int MixedEngine::autotune(uint32_t max_steps, uint32_t* taken) {
+    *taken = 0;
+    const uint32_t ci = opts_.check_interval;
+    const int blocks[] = {64, 128, 256};
+    const float skins[] = {0.05f, 0.1f, 0.15f, 0.25f, 0.4f};
+    const float cells[] = {1.0f, 1.25f, 1.5f};
+    const uint32_t need = ci * (uint32_t)(3 + 5);
+    if (max_steps < need) return VEDO_OK;            // too short a call: tune in a later one
+    cudaEvent_t e0 = ev_[2], e1 = ev_[3];
+    auto timed_rebuild = [&](float* ms) -> int {
+        MCK(cudaEventRecord(e0, stream_));
+        int rc = rebuild();
+        if (rc != VEDO_OK) return rc;
+        MCK(cudaEventRecord(e1, stream_));
+        MCK(cudaEventSynchronize(e1));
+        MCK(cudaEventElapsedTime(ms, e0, e1));
+        return VEDO_OK;
+    };
+    auto timed_chunk = [&](float* ms_per_step, float* growth) -> int {
+        const uint64_t r0 = round_;
+        float disp = 0.0f;
+        MCK(cudaEventRecord(e0, stream_));
+        int rc = step_chunk(ci, false, &disp);
+        if (rc > 0) return rc;
+        MCK(cudaEventRecord(e1, stream_));
+        MCK(cudaEventSynchronize(e1));
+        float ms = 0.0f;
+        MCK(cudaEventElapsedTime(&ms, e0, e1));
+        *ms_per_step = ms / (float)ci;
+        if (growth) *growth = since_rebuild_ ? disp / (float)since_rebuild_ : 0.0f;
+        *taken += (uint32_t)(round_ - r0);
+        return VEDO_OK;
+    };
+    int rc;
+    if (need_rebuild_ && (rc = rebuild()) != VEDO_OK) return rc;
+    // 1. tick block size (the list is unchanged, the tick time alone decides)
+    float best = FLT_MAX;
+    int best_tpb = tpb_;
+    for (int b : blocks) {
+        tpb_ = b;
+        drop_graphs();
+        float t = 0.0f;
+        if ((rc = timed_chunk(&t, nullptr)) != VEDO_OK) return rc;
+        if (need_rebuild_ && (rc = rebuild()) != VEDO_OK) return rc;
+        if (t < best) { best = t; best_tpb = b; }
+    }
+    tpb_ = best_tpb;
+    // 2. skin: tick time per step plus the amortised rebuild
+    best = FLT_MAX;
+    float best_skin = skin_frac_;
+    for (float f : skins) {
+        set_skin(f);
+        float trb = 0.0f, t = 0.0f, growth = 0.0f;
+        if ((rc = timed_rebuild(&trb)) != VEDO_OK) return rc;
+        if ((rc = timed_chunk(&t, &growth)) != VEDO_OK) return rc;
+        // steps until the bound nears half the skin at this growth (the rebuild rule's margin)
+        const float life = growth > 0.0f ? std::max((float)ci, 0.5f * skin_min_ / growth - 2.0f * (float)ci) : 1e6f;
+        const float cost = t + trb / life;
+        if (cost < best) { best = cost; best_skin = f; }
+    }
+    set_skin(best_skin);
+    // 3. cell scale: the rebuild time alone (the list does not depend on it)
+    best = FLT_MAX;
+    float best_cell = cell_scale_;
+    for (float c : cells) {
+        cell_scale_ = c;
+        float trb = 0.0f;
+        if ((rc = timed_rebuild(&trb)) != VEDO_OK) return rc;
+        if (trb < best) { best = trb; best_cell = c; }
+    }
+    cell_scale_ = best_cell;
+    need_rebuild_ = true;
+    tune_pending_ = false;
+    return VEDO_OK;
+}
+
 int MixedEngine::run(uint32_t nsteps, int* keep_running) {
     prof_[0] = prof_[1] = prof_[2] = prof_[3] = 0;
     launches_ = 0;
     MCK(cudaSetDevice(opts_.device));
     MCK(cudaEventRecord(ev_[0], stream_));
-    const float half_skin = 0.5f * skin_min_;
     const uint32_t ci = opts_.check_interval;
     uint32_t done = 0;
+    if (tune_pending_ && nsteps > 1) {
+        // the tuner's steps are steps of this call; the last one stays for the impulse output
+        uint32_t t = 0;
+        int rc = autotune(nsteps - 1, &t);
+        if (rc != VEDO_OK) return rc;
+        done += t;
+    }
     while (done < nsteps) {
         if (need_rebuild_) {
             int rc = rebuild();
             if (rc != VEDO_OK) return rc;
         }
-        // up to the next displacement check
         const uint32_t chunk = std::min<uint32_t>(nsteps - done, ci - (uint32_t)(since_rebuild_ % ci));
-        for (uint32_t k = 0; k < chunk; ++k) {
-            TickArgs a = args(done + k + 1 == nsteps);
-            switch (law_) {
-            case IS_BSDBF: k_tick<IS_BSDBF><<<nblk(n_), TPB, 0, stream_>>>(a); break;
-            case IS_BTSDBF: k_tick<IS_BTSDBF><<<nblk(n_), TPB, 0, stream_>>>(a); break;
-            case IS_BSDB2F: k_tick<IS_BSDB2F><<<nblk(n_), TPB, 0, stream_>>>(a); break;
-            case IS_HERTZ: k_tick<IS_HERTZ><<<nblk(n_), TPB, 0, stream_>>>(a); break;
-            case IS_H: k_tick<IS_H><<<nblk(n_), TPB, 0, stream_>>>(a); break;
-            default: k_tick<0><<<nblk(n_), TPB, 0, stream_>>>(a); break;
-            }
-            ++launches_;
-            if (a.write_imp && !glob_.empty()) {
-                k_wall_sum<<<nblk((uint64_t)glob_.size() * 32), TPB, 0, stream_>>>(
-                    (uint32_t)glob_.size(), d_glob_, d_wptr_, d_wval_, d_wimp_, d_model_of_, d_models_, d_scenes_,
-                    d_scene_of_, d_gfield_, d_imp_, d_aimp_);
-                ++launches_;
-            }
-            // walls move; thread 0 writes the displacement bound after the step
-            k_walls<<<nblk(std::max<size_t>(glob_.size(), 1)), TPB, 0, stream_>>>(
-                (uint32_t)glob_.size(), d_glob_, d_model_of_, d_models_, d_scenes_, d_scene_of_, a.xA, a.xB, d_v64_,
-                d_w64_, a.v32A, a.v32B, a.w32A, a.w32B, d_ox_, d_oz_, dt_max_, d_red_ + 8, d_disp_ + cur_,
-                d_disp_ + (cur_ ^ 1), half_skin, d_red_ + 12, d_red_ + 11, d_wall32_);
-            ++launches_;
-            cur_ ^= 1;
-        }
-        float disp = 0.0f;
-        unsigned held = 0;
-        MCK(cudaMemcpyAsync(&disp, d_disp_ + cur_, 4, cudaMemcpyDeviceToHost, stream_));
-        MCK(cudaMemcpyAsync(&held, d_red_ + 11, 4, cudaMemcpyDeviceToHost, stream_));
-        MCK(cudaStreamSynchronize(stream_));
-        const uint32_t taken = chunk - std::min(held, chunk);
-        done += taken;
-        round_ += taken;
-        since_rebuild_ += taken;
-        for (auto& S : sc_)
-            for (uint32_t k = 0; k < taken; ++k) S.t += S.dt;     // SystemParameter::NextStep (SystemParameter.h:113-116), once per step
-        if (held || disp > half_skin) {
-            // held steps are taken again after the rebuild; a bound already past half the skin
-            // would hold the next step, and contact queries need a complete list too
-            need_rebuild_ = true;
-        } else if (since_rebuild_ % ci == 0) {
-            // Rebuild before the bound can reach half the skin: the bound so far plus twice its
-            // mean growth per step over the next check interval.
-            const float growth = disp / (float)since_rebuild_;
-            if (disp + 2.0f * growth * (float)ci > half_skin) need_rebuild_ = true;
-        }
+        const uint64_t r0 = round_;
+        int rc = step_chunk(chunk, done + chunk == nsteps, nullptr);
+        if (rc > 0) return rc;
+        done += (uint32_t)(round_ - r0);
     }
     MCK(cudaEventRecord(ev_[1], stream_));
     MCK(cudaStreamSynchronize(stream_));

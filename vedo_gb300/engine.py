@@ -67,6 +67,7 @@ def lib() -> C.CDLL:
         L.vedo_gpu_num_scenes.restype = C.c_uint32
         L.vedo_gpu_scene_range.argtypes = [vp, C.c_uint32, C.POINTER(C.c_uint32), C.POINTER(C.c_uint32),
                                            C.POINTER(C.c_double)]
+        L.vedo_gpu_get_tuning.argtypes = [vp, C.POINTER(C.c_float), C.POINTER(C.c_float), C.POINTER(C.c_uint32)]
         _lib = L
     return _lib
 
@@ -75,7 +76,8 @@ STATE_FIELDS = ("position", "velocity", "angular_velocity", "orientation_x", "or
                 "angular_impact")
 
 
-def _opts(up_iact, record, precision, device, prefix, skin, check_interval) -> EngineOpts:
+def _opts(up_iact, record, precision, device, prefix, skin, check_interval, tick_block=None, cell_scale=None,
+          autotune=False, graphs=True) -> EngineOpts:
     opts = EngineOpts()
     lib().vedo_gpu_default_opts(C.byref(opts))
     opts.up_iact, opts.record, opts.precision, opts.device = up_iact, record, precision, device
@@ -83,6 +85,12 @@ def _opts(up_iact, record, precision, device, prefix, skin, check_interval) -> E
         opts.skin = skin
     if check_interval is not None:
         opts.check_interval = check_interval
+    if tick_block is not None:
+        opts.tick_block = tick_block
+    if cell_scale is not None:
+        opts.cell_scale = cell_scale
+    opts.autotune = 1 if autotune else 0
+    opts.graphs = 1 if graphs else 0
     opts.output_prefix = prefix
     return opts
 
@@ -97,10 +105,12 @@ class GpuEngine:
 
     def __init__(self, scene, up_iact: int = 1, record: int = 0, precision: int = _abi.PRECISION_FP64,
                  device: int = 0, output_prefix: Optional[str] = None, skin: Optional[float] = None,
-                 check_interval: Optional[int] = None):
+                 check_interval: Optional[int] = None, tick_block: Optional[int] = None,
+                 cell_scale: Optional[float] = None, autotune: bool = False, graphs: bool = True):
         L = lib()
         self._prefix = output_prefix.encode() if output_prefix else None
-        opts = _opts(up_iact, record, precision, device, self._prefix, skin, check_interval)
+        opts = _opts(up_iact, record, precision, device, self._prefix, skin, check_interval, tick_block, cell_scale,
+                     autotune, graphs)
         h = C.c_void_p()
         if isinstance(scene, (str, bytes, os.PathLike)):
             rc = L.vedo_gpu_create_from_ido(os.fsencode(scene), C.byref(opts), C.byref(h))
@@ -178,6 +188,12 @@ class GpuEngine:
     def write_ido(self, path: str):
         self._check(lib().vedo_gpu_write_ido(self.h, os.fsencode(path)))
 
+    def tuning(self):
+        """Skin (fraction of r_max), cell scale and tick block size in use (MIXED form)."""
+        sk, cs, tb = C.c_float(0), C.c_float(0), C.c_uint32(0)
+        self._check(lib().vedo_gpu_get_tuning(self.h, C.byref(sk), C.byref(cs), C.byref(tb)))
+        return {"skin": float(sk.value), "cell_scale": float(cs.value), "tick_block": int(tb.value)}
+
     def set_profiling(self, on: bool):
         lib().vedo_gpu_set_profiling(self.h, 1 if on else 0)
 
@@ -214,10 +230,12 @@ class BatchEngine(GpuEngine):
     """
 
     def __init__(self, scene_list, device: int = 0, skin: Optional[float] = None,
-                 check_interval: Optional[int] = None):
+                 check_interval: Optional[int] = None, tick_block: Optional[int] = None,
+                 cell_scale: Optional[float] = None, autotune: bool = False, graphs: bool = True):
         L = lib()
         self._prefix = None
-        opts = _opts(1, 0, _abi.PRECISION_MIXED, device, None, skin, check_interval)
+        opts = _opts(1, 0, _abi.PRECISION_MIXED, device, None, skin, check_interval, tick_block, cell_scale,
+                     autotune, graphs)
         descs, keeps = [], []
         for sc in scene_list:
             if isinstance(sc, (str, bytes, os.PathLike)):

@@ -15,6 +15,11 @@ code, the C oracle and the GPU engine.
   whose shell is a static polygon of fixed plates and whose two end plates are
   orbital plates turning at 30 rpm; 35 % fill by seeded random sequential
   placement.
+* :func:`hopper` / :func:`hopper_batch` - flat-bottomed hoppers discharging through a
+  rectangular orifice (a box of fixed plates whose floor is four plates around the
+  orifice), monodisperse r = 1 mm Hertz spheres with friction (``ISwH``); the batch
+  draws sphere counts log-uniform on [1e3, 5e4], friction U(0.2, 0.6), restitution
+  U(0.5, 0.9) and orifice width U(6, 12) mm per scene.
 * :func:`cluster` - small random clusters used by the parity tests (every
   solver, plates, cylinders, orbital walls).
 """
@@ -338,3 +343,76 @@ def _hertz_mech(solver, E, nu, ra, rb, m_of, zeta, mu):
     return [("HertzNormalStiffness", kn), ("EquivalentMass", meff),
             ("ShearStiffnessCoefficient1", 8.0 * Gs), ("ShearStiffnessCoefficient2", 3.0 * Rs / (4.0 * Es)),
             ("DampingRatio", zeta), ("KineticFrictionCoefficient", mu)]
+
+
+def hopper(n: int = 10000, seed: int = 0, friction: float = 0.4, restitution: float = 0.7, orifice: float = 8e-3,
+           steps: int = 5000, dt: float = 5e-7, radius: float = 1e-3, density: float = 2500.0, E: float = 70e9,
+           nu: float = 0.25, spacing_factor: float = 1.1, vel_sigma: float = 0.01) -> Scene:
+    """Flat-bottomed hopper discharging through a square orifice of side `orifice`.
+
+    The spheres start on a jittered square-prism lattice (spacing `spacing_factor` x 2r),
+    about twice as tall as wide, resting 0.05 r above the floor.  Walls: four fixed side
+    plates and a floor of four fixed plates that leave the orifice open in its centre (the
+    reference's only holed plate has a circular hole, so the rectangular orifice is built from
+    plain plates).  Contact: ``ISwH`` (Hertz normal stiffness with friction) from E, nu,
+    restitution and friction, for sphere-sphere and sphere-wall."""
+    rng = np.random.default_rng(seed)
+    a = 2.0 * radius * spacing_factor
+    m = max(2, int(math.ceil((n / 2.0) ** (1.0 / 3.0))))
+    nz = int(math.ceil(n / (m * m)))
+    g = np.stack(np.meshgrid(np.arange(m), np.arange(m), np.arange(nz), indexing="ij"), -1).reshape(-1, 3)[:n]
+    pos = np.empty((n, 3))
+    pos[:, 0] = (g[:, 0] - 0.5 * (m - 1)) * a
+    pos[:, 1] = (g[:, 1] - 0.5 * (m - 1)) * a
+    pos[:, 2] = g[:, 2] * a + 1.05 * radius
+    pos += rng.uniform(-0.02 * radius, 0.02 * radius, size=pos.shape)
+    vel = rng.normal(0.0, vel_sigma, size=pos.shape)
+    W = m * a + 2.0 * radius                       # inner width of the box
+    H = nz * a + 4.0 * radius                      # side wall height
+    t = 2e-3                                       # plate thickness
+    w = min(orifice, W - 4.0 * radius)
+    models = [DOModel("Ball", "Ball", MOBILE, LOCAL, density, 1.0, SPHERE, (radius,)),
+              DOModel("Side", "Wall", FIXED, GLOBAL, 0.0, 1.0, QUASI_PLATE, (H, t, W + 2 * t)),
+              DOModel("FloorLR", "Wall", FIXED, GLOBAL, 0.0, 1.0, QUASI_PLATE, (0.5 * (W - w), t, W)),
+              DOModel("FloorFB", "Wall", FIXED, GLOBAL, 0.0, 1.0, QUASI_PLATE, (w, t, 0.5 * (W - w)))]
+    wp, wox, woz, widx = [], [], [], []
+    for sx, sy in ((1, 0), (-1, 0), (0, 1), (0, -1)):   # sides: normal points inwards
+        wp.append((sx * (0.5 * W + 0.5 * t), sy * (0.5 * W + 0.5 * t), 0.5 * H))
+        wox.append((0.0, 0.0, 1.0))
+        woz.append((-float(sx), -float(sy), 0.0))
+        widx.append(1)
+    q = 0.25 * (W + w)                             # centre of a floor strip beside the orifice
+    for sx in (1, -1):                             # left/right strips, full depth
+        wp.append((sx * q, 0.0, -0.5 * t)); wox.append((1.0, 0.0, 0.0)); woz.append((0.0, 0.0, 1.0)); widx.append(2)
+    for sy in (1, -1):                             # front/back strips between them
+        wp.append((0.0, sy * q, -0.5 * t)); wox.append((1.0, 0.0, 0.0)); woz.append((0.0, 0.0, 1.0)); widx.append(3)
+    zeta = damping_ratio(restitution)
+    m_of = lambda rr: density * 4.0 / 3.0 * math.pi * rr ** 3
+    iacts = [IactModel("Ball", "Ball", "ISwH", _hertz_mech("ISwH", E, nu, radius, radius, m_of, zeta, friction)),
+             IactModel("Wall", "Ball", "ISwH", _hertz_mech("ISwH", E, nu, radius, None, m_of, zeta, friction))]
+    k = len(widx)
+    midx = np.concatenate([np.zeros(n, np.uint32), np.array(widx, np.uint32)])
+    P = np.concatenate([pos, np.array(wp)])
+    V = np.concatenate([vel, np.zeros((k, 3))])
+    OX = np.concatenate([np.tile([1.0, 0, 0], (n, 1)), np.array(wox)])
+    OZ = np.concatenate([np.tile([0, 0, 1.0], (n, 1)), np.array(woz)])
+    AV = np.zeros((n + k, 3))
+    return Scene(time_control(steps, dt), models, iacts, midx, P, V, OX, OZ, AV)
+
+
+def hopper_params(num_scenes: int = 256, seed: int = 2025, n_lo: int = 1000, n_hi: int = 50000):
+    """Per-scene draws of the hopper batch: (n, seed, friction, restitution, orifice)."""
+    rng = np.random.default_rng(seed)
+    n = np.exp(rng.uniform(math.log(n_lo), math.log(n_hi), num_scenes)).astype(np.int64)
+    mu = rng.uniform(0.2, 0.6, num_scenes)
+    e = rng.uniform(0.5, 0.9, num_scenes)
+    w = rng.uniform(6e-3, 12e-3, num_scenes)
+    seeds = rng.integers(0, 2**31 - 1, num_scenes)
+    return [(int(n[k]), int(seeds[k]), float(mu[k]), float(e[k]), float(w[k])) for k in range(num_scenes)]
+
+
+def hopper_batch(num_scenes: int = 256, seed: int = 2025, steps: int = 5000, n_lo: int = 1000,
+                 n_hi: int = 50000) -> List[Scene]:
+    """The batched hopper workload: `num_scenes` independent hoppers of uneven sizes."""
+    return [hopper(n=n, seed=sd, friction=mu, restitution=e, orifice=w, steps=steps)
+            for n, sd, mu, e, w in hopper_params(num_scenes, seed, n_lo, n_hi)]
