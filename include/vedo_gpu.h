@@ -271,6 +271,55 @@ uint32_t vedo_gpu_num_scenes(const vedo_gpu_engine* e);
 int vedo_gpu_scene_range(const vedo_gpu_engine* e, uint32_t scene, uint32_t* first_object, uint32_t* num_objects,
                          double* time);
 
+/* ---- serving: continuous batching of DEM jobs (MIXED form) -------------
+ * No counterpart in the reference (anne runs one scene per process).  A server owns one
+ * GPU and a thread that advances every live job's scene in the same fused launches.  Jobs
+ * (a scene and a step count) are submitted from any thread at any time; each waits in a
+ * FIFO queue until admission, which counts an estimate of the job's device memory
+ * (VEDO_SRV_BYTES_PER_OBJECT per object) against the HBM budget.  The live set is kept at
+ * or below half the budget, because adding or removing jobs builds the next batch on the
+ * device while the current one still exists.  Admitted jobs join the batch at the next
+ * check interval, with their state and contact history resident on the device from then
+ * on; a job stops after exactly its step count and its final state is copied to the host.
+ * A job's result equals the same scene run alone in the MIXED form for the same number
+ * of steps, bit for bit. */
+#define VEDO_SRV_BYTES_PER_OBJECT 2048u
+enum { VEDO_JOB_QUEUED = 0, VEDO_JOB_RUNNING = 1, VEDO_JOB_DONE = 2, VEDO_JOB_CANCELLED = 3, VEDO_JOB_FAILED = 4 };
+
+typedef struct vedo_job_info {
+    uint32_t status;          /* VEDO_JOB_*                                              */
+    uint32_t num_objects;
+    uint64_t steps;           /* requested                                               */
+    uint64_t steps_done;
+    double submit_s;          /* seconds since the server started: submission,          */
+    double admit_s;           /*   admission (joined the batch) and completion; -1 = not */
+    double done_s;            /*   yet                                                   */
+} vedo_job_info;
+
+typedef struct vedo_server vedo_server;
+
+/* opts: engine options of the batch (precision must be MIXED); hbm_budget_bytes: device
+ * memory the server may hold. */
+int vedo_srv_create(const vedo_engine_opts* opts, uint64_t hbm_budget_bytes, vedo_server** out);
+/* Queue a job: the scene is copied; steps >= 1.  Fails (and queues nothing) when the scene is
+ * invalid or the job alone would not fit the budget. */
+int vedo_srv_submit(vedo_server* s, const vedo_scene_desc* scene, uint64_t steps, uint64_t* job_id);
+int vedo_srv_poll(vedo_server* s, uint64_t job_id, vedo_job_info* info);
+/* Block until the job is done, cancelled or failed, or timeout_s passes (then
+ * VEDO_ERR_DEVICE_TIMEOUT); info may be NULL. */
+int vedo_srv_wait(vedo_server* s, uint64_t job_id, double timeout_s, vedo_job_info* info);
+/* Final state of a done job ([n][3] host arrays, any pointer may be NULL). */
+int vedo_srv_result(vedo_server* s, uint64_t job_id, const vedo_state_view* out);
+/* Cancel a queued or running job (a running one stops at the next check interval). */
+int vedo_srv_cancel(vedo_server* s, uint64_t job_id);
+/* out[0] jobs done, [1] particle-steps of done jobs, [2] seconds the batch was stepping,
+ * [3] batches built, [4] objects in the current batch, [5] bytes committed to live jobs,
+ * [6] jobs queued, [7] jobs running. */
+int vedo_srv_stats(vedo_server* s, double out[8]);
+const char* vedo_srv_last_error(const vedo_server* s);
+/* Stops the server thread (running jobs are abandoned) and frees the GPU. */
+void vedo_srv_destroy(vedo_server* s);
+
 /* ---- allocation-free system energy --------------------------------------
  * No counterpart in the reference.
  * For callers that cannot let a library allocate device memory: a coupled solver or a

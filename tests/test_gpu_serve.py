@@ -1,0 +1,87 @@
+"""GPU tests of the job server (vedo_srv_*): continuous batching of DEM jobs.
+
+Bar: a job's result through the server equals the same scene run alone in the MIXED form for
+the same steps, bit for bit, although the job joins a batch that is already running, other
+jobs join and leave while it runs, and the batch is rebuilt each time."""
+import time
+
+import numpy as np
+import pytest
+
+from vedo_gb300 import scenes
+
+pytestmark = pytest.mark.gpu
+
+FIELDS = ("position", "velocity", "angular_velocity", "impact", "angular_impact")
+
+
+def _alone(engine_lib, sc, steps):
+    e = engine_lib.GpuEngine(sc, precision=1)
+    e.run(steps)
+    st = e.state(FIELDS)
+    e.close()
+    return st
+
+
+def _wait_running(srv, job, min_steps=1, timeout=60.0):
+    t0 = time.time()
+    while time.time() - t0 < timeout:
+        i = srv.poll(job)
+        if i["status"] != "queued" and i["steps_done"] >= min_steps:
+            return i
+        time.sleep(0.001)
+    raise AssertionError("job did not start")
+
+
+def test_served_jobs_equal_alone(engine_lib):
+    from vedo_gb300.serve import Server
+    jobs = [(scenes.hopper(n=3000, seed=1, steps=10), 400),
+            (scenes.serving_job("projectile", 2500, "lsd", 3), 250),
+            (scenes.serving_job("settle", 2000, "hertz", 4), 333),
+            (scenes.cluster(n=64, solver="ISwBSDBF", seed=21), 150)]
+    with Server(hbm_budget_bytes=8 * 10**9) as srv:
+        ids = [srv.submit(*jobs[0])]
+        _wait_running(srv, ids[0], 20)            # the others join a running batch
+        for sc, st in jobs[1:]:
+            ids.append(srv.submit(sc, st))
+            time.sleep(0.002)
+        infos = [srv.wait(j, 120.0) for j in ids]
+        assert all(i["status"] == "done" for i in infos), infos
+        assert all(i["steps_done"] == st for i, (_, st) in zip(infos, jobs))
+        res = [srv.result(j, FIELDS) for j in ids]
+        stats = srv.stats()
+    assert stats["jobs_done"] == len(jobs) and stats["batches"] >= 2
+    for (sc, st), r in zip(jobs, res):
+        ref = _alone(engine_lib, sc, st)
+        for k in FIELDS:
+            assert np.array_equal(r[k], ref[k]), k
+
+
+def test_admission_respects_the_hbm_budget(engine_lib):
+    from vedo_gb300.serve import BYTES_PER_OBJECT, Server
+    scs = [scenes.serving_job("settle", 2000, "lsd", s) for s in range(3)]
+    one = max(sc.num_objects for sc in scs) * BYTES_PER_OBJECT
+    with Server(hbm_budget_bytes=3 * one) as srv:      # half the budget holds one job, not two
+        ids = [srv.submit(sc, 200) for sc in scs]
+        infos = [srv.wait(j, 120.0) for j in ids]
+        res = [srv.result(j, ("position",)) for j in ids]
+    assert all(i["status"] == "done" for i in infos)
+    for a, b in zip(infos, infos[1:]):
+        assert b["admit_s"] >= a["done_s"]            # one at a time
+    for sc, r in zip(scs, res):
+        assert np.array_equal(r["position"], _alone(engine_lib, sc, 200)["position"])
+
+
+def test_cancel_and_oversized_jobs(engine_lib):
+    from vedo_gb300.serve import Server
+    with Server(hbm_budget_bytes=2 * 10**8) as srv:
+        big = scenes.serving_job("settle", 60000, "lsd", 1)
+        with pytest.raises(engine_lib.EngineError) as ex:
+            srv.submit(big, 10)                       # 60k objects x 2 KiB > half of 200 MB
+        assert ex.value.code == 4
+        j = srv.submit(scenes.serving_job("settle", 3000, "lsd", 2), 10**6)
+        _wait_running(srv, j, 1)
+        srv.cancel(j)
+        assert srv.wait(j, 60.0)["status"] == "cancelled"
+        k = srv.submit(scenes.cluster(n=64, seed=3), 50)
+        assert srv.wait(k, 60.0)["status"] == "done"

@@ -40,6 +40,7 @@ SOURCES = {
     "noalloc.cu": ("nvcc", []),
     "scene_host.cpp": ("cxx", []),
     "capi.cpp": ("cxx", []),
+    "serve.cpp": ("cxx", ["-pthread"]),
 }
 
 
@@ -71,7 +72,7 @@ def build(verbose: bool = False, force: bool = False) -> str:
     with cf.ThreadPoolExecutor(max_workers=min(8, len(srcs))) as ex:
         objs = list(ex.map(lambda kv: _compile(kv[0], kv[1][0], kv[1][1], verbose), srcs.items()))
     tmp = LIB + ".tmp"
-    cmd = [_nvcc(), *ARCH, "-shared", "-o", tmp, *objs, "-Xcompiler", "-fPIC", "-Xlinker", "--no-undefined"]
+    cmd = [_nvcc(), *ARCH, "-shared", "-o", tmp, *objs, "-Xcompiler", "-fPIC,-pthread", "-Xlinker", "--no-undefined"]
     if verbose:
         print(" ".join(cmd), flush=True)
     r = subprocess.run(cmd, capture_output=True, text=True)

@@ -38,6 +38,13 @@ EngineBase* make_mixed_batch(const std::vector<const HScene*>& scenes, const ved
                              std::string* err);
 // Scene count and per-scene object range / time of a batch engine (1 scene for any other engine).
 uint32_t mixed_num_scenes(EngineBase* e);
+// Continuous batching: a new MIXED engine from scenes `keep` of `prev` (moved on the device,
+// state and contact history) followed by the host scenes `add`; nullptr with *rc / *err.
+EngineBase* mixed_repack(EngineBase* prev, const std::vector<uint32_t>& keep, const std::vector<const HScene*>& add,
+                         const vedo_engine_opts& opts, int* rc, std::string* err);
+int mixed_set_scene_active(EngineBase* e, uint32_t s, bool on);
+int mixed_get_state_slice(EngineBase* e, uint32_t off, uint32_t cnt, const vedo_state_view& v);
+uint64_t mixed_scene_steps(EngineBase* e, uint32_t s);
 int mixed_scene_range(EngineBase* e, uint32_t s, uint32_t* off, uint32_t* n, double* t);
 
 }  // namespace vedo

@@ -33,6 +33,7 @@
 #include <cmath>
 #include <cstdio>
 #include <cstring>
+#include <memory>
 #include <new>
 #include <string>
 #include <vector>
@@ -244,7 +245,8 @@ __device__ __forceinline__ int solve32(int is_rt, const float* __restrict__ c, b
 // step; object indices are the scene's own shifted by its offset, so a scene's results do not
 // depend on the other scenes it is batched with.
 struct SceneDev {
-    uint32_t model_off, nm, pbase, wall_beg, wall_end, obj_off, nobj, pad;
+    uint32_t model_off, nm, pbase, wall_beg, wall_end, obj_off, nobj;
+    uint32_t active;               // 0: the scene's job is finished; its objects stay as they are
     uint64_t cell_base;
     uint32_t nc[3];
     float lo[3], inv_h;
@@ -321,8 +323,8 @@ __global__ void __launch_bounds__(TPB) k_tick(TickArgs a) {
     if (i < a.n) {
         const uint32_t mi = a.model_of[i];
         const ModelDev& M = a.models[mi];
-        if (M.scope == SCOPE_LOCAL) {
-            const SceneDev& S = a.scenes[a.scene_of[i]];
+        const SceneDev& S = a.scenes[a.scene_of[i]];
+        if (M.scope == SCOPE_LOCAL && S.active) {
             const double dt = S.dt;
             const d3 Pi = ld(a.xA, i);
             const float dtf = (float)dt;
@@ -472,6 +474,8 @@ __global__ void __launch_bounds__(TPB) k_tick(TickArgs a) {
                 a.v32B[i] = a.v32A[i];
                 a.w32B[i] = a.w32A[i];
             }
+        } else if (M.scope == SCOPE_LOCAL) {
+            hold_state(a, i);                      // a finished scene waits, unchanged
         }
     }
 #pragma unroll
@@ -507,7 +511,7 @@ __global__ void k_walls(uint32_t nglob, const uint32_t* __restrict__ glob, const
     }
     if (q >= nglob) return;
     const uint32_t w = glob[q];
-    if (hold) {
+    if (hold || !scenes[scene_of[w]].active) {
         xB[w] = xA[w];
         v32B[w] = v32A[w];
         w32B[w] = w32A[w];
@@ -927,6 +931,97 @@ __global__ void __launch_bounds__(TPB) k_wall32(uint32_t n, const uint32_t* __re
                    : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
 }
 
+// ---- moving scenes into a new engine (continuous batching) --------------------------------
+// One entry per scene of the new engine, in object order: its objects come from the previous
+// engine's device arrays (kind 0) or from host data staged on the device (kind 1).
+struct MoveScene {
+    uint32_t new_off, nobj, src_off, kind;
+};
+
+__device__ __forceinline__ const MoveScene& find_move(const MoveScene* __restrict__ mv, uint32_t nmv, uint32_t i) {
+    uint32_t lo = 0, hi = nmv;                      // last entry with new_off <= i
+    while (hi - lo > 1) {
+        const uint32_t mid = (lo + hi) >> 1;
+        if (mv[mid].new_off <= i) lo = mid; else hi = mid;
+    }
+    return mv[lo];
+}
+
+struct StateArrays {
+    const double4_32a *x, *v, *w, *ox, *oz, *imp, *aimp;
+};
+
+__global__ void __launch_bounds__(TPB) k_move_state(uint32_t n, const MoveScene* __restrict__ mv, uint32_t nmv,
+                                                    StateArrays prev, const double* __restrict__ stage,
+                                                    size_t stage_stride, double4_32a* __restrict__ x,
+                                                    double4_32a* __restrict__ v, double4_32a* __restrict__ w,
+                                                    double4_32a* __restrict__ ox, double4_32a* __restrict__ oz,
+                                                    double4_32a* __restrict__ imp, double4_32a* __restrict__ aimp,
+                                                    float4* __restrict__ v32, float4* __restrict__ w32) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const MoveScene& m = find_move(mv, nmv, i);
+    const uint32_t j = m.src_off + (i - m.new_off);
+    double4_32a* dst[7] = {x, v, w, ox, oz, imp, aimp};
+    if (m.kind == 0) {
+        const double4_32a* src[7] = {prev.x, prev.v, prev.w, prev.ox, prev.oz, prev.imp, prev.aimp};
+        for (int k = 0; k < 7; ++k) dst[k][i] = src[k][j];
+    } else {
+        for (int k = 0; k < 7; ++k) {
+            const double* q = stage + (size_t)k * stage_stride + 3 * (size_t)j;
+            dst[k][i] = make_double4_32a(q[0], q[1], q[2], 0.0);
+        }
+    }
+    const double4_32a vv = v[i], ww = w[i];
+    v32[i] = make_float4((float)vv.x, (float)vv.y, (float)vv.z, 0.0f);
+    w32[i] = make_float4((float)ww.x, (float)ww.y, (float)ww.z, 0.0f);
+}
+
+// A neighbour list (CSR rows, history at the same entry positions) that the first rebuild
+// of the new engine carries histories from: rows of kept scenes are copied from the previous
+// engine's current list with object and entry indices shifted; rows of new scenes come from
+// their IactRecordTab records, staged on the device.
+struct ListArrays {
+    const uint32_t *ptr, *ent, *slot;
+    const float4* h;
+    const uint8_t* f;
+};
+
+__global__ void __launch_bounds__(TPB) k_row_count(uint32_t n, const MoveScene* __restrict__ mv, uint32_t nmv,
+                                                   ListArrays prev, ListArrays stage, uint32_t* __restrict__ cnt) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i > n) return;
+    if (i == n) { cnt[n] = 0u; return; }
+    const MoveScene& m = find_move(mv, nmv, i);
+    const uint32_t j = m.src_off + (i - m.new_off);
+    const ListArrays& L = m.kind == 0 ? prev : stage;
+    cnt[i] = L.ptr ? L.ptr[j + 1] - L.ptr[j] : 0u;
+}
+
+__global__ void __launch_bounds__(TPB) k_row_fill(uint32_t n, const MoveScene* __restrict__ mv, uint32_t nmv,
+                                                  ListArrays prev, ListArrays stage, const uint32_t* __restrict__ ptr,
+                                                  uint32_t* __restrict__ ent, uint32_t* __restrict__ slot,
+                                                  float4* __restrict__ h, uint8_t* __restrict__ f) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const MoveScene& m = find_move(mv, nmv, i);
+    const uint32_t j = m.src_off + (i - m.new_off);
+    const ListArrays& L = m.kind == 0 ? prev : stage;
+    if (!L.ptr) return;
+    // object indices of a kept scene move by the scene's shift; staged rows already use the
+    // new indices.  Entry indices (slots) move by the shift of the scene's first row.
+    const uint32_t dobj = m.kind == 0 ? m.new_off - m.src_off : 0u;
+    const uint32_t dent = ptr[m.new_off] - L.ptr[m.src_off];
+    const uint32_t b = L.ptr[j], e1 = L.ptr[j + 1], o = ptr[i];
+    for (uint32_t q = b; q < e1; ++q) {
+        const uint32_t v = L.ent[q];
+        ent[o + (q - b)] = (v & WALL_BIT) | ((v & ~WALL_BIT) + dobj);
+        slot[o + (q - b)] = L.slot[q] + dent;
+        h[o + (q - b)] = L.h[q];
+        f[o + (q - b)] = L.f[q];
+    }
+}
+
 }  // namespace
 
 // ==========================================================================================
@@ -936,7 +1031,24 @@ public:
     int init(const HScene& scene, const vedo_engine_opts& opts) override {
         return init_batch(std::vector<const HScene*>{&scene}, opts);
     }
-    int init_batch(const std::vector<const HScene*>& scenes, const vedo_engine_opts& opts);
+    int init_batch(const std::vector<const HScene*>& scenes, const vedo_engine_opts& opts) {
+        std::vector<SceneSource> src;
+        for (const HScene* h : scenes) src.push_back(SceneSource{h, -1});
+        return init_from(src, nullptr, opts);
+    }
+    // A scene of a new engine: a host scene (prev_scene < 0) or scene prev_scene of `prev`,
+    // whose state and contact history move over on the device.
+    struct SceneSource {
+        const HScene* host;
+        int prev_scene;
+    };
+    int init_from(const std::vector<SceneSource>& src, const MixedEngine* prev, const vedo_engine_opts& opts);
+    // Freeze (or resume) one scene: a frozen scene's objects keep their state and its time stops.
+    int set_scene_active(uint32_t s, bool on);
+    bool scene_active(uint32_t s) const { return s < sc_.size() && sc_[s].active; }
+    // State of objects [off, off + cnt) into [cnt][3] host arrays.
+    int get_state_slice(uint32_t off, uint32_t cnt, const vedo_state_view& v);
+    uint64_t steps_of_scene(uint32_t s) const { return s < sc_.size() ? sc_[s].steps : 0; }
     int run(uint32_t nsteps, int* keep_running) override;
     int get_state(const vedo_state_view& v) override;
     int set_state(const vedo_state_view& v) override;
@@ -982,6 +1094,8 @@ private:
         uint32_t obj_off = 0, nobj = 0, model_off = 0, nm = 0, pbase = 0, wall_beg = 0, wall_end = 0, nloc = 0;
         double dt = 0, t = 0, t_stop = 0, g[3] = {0, 0, 0};
         float skin = 0, rmax = 0;
+        bool active = true;
+        uint64_t steps = 0;         // steps this scene has taken (in this engine and before)
     };
     int fail(int c, const std::string& m) { err_ = m; return c; }
     int cuda_fail(cudaError_t e, const char* where) {
@@ -998,7 +1112,7 @@ private:
     void free_nlist(NList& L);
     TickArgs args(bool write_imp);
 
-    std::vector<HScene> host_;      // per scene (states refreshed for IDO output)
+    std::vector<std::shared_ptr<const HScene>> host_;   // per scene: models, interactions, initial state
     std::vector<SceneHost> sc_;
     std::vector<SceneDev> sdev_;
     std::vector<ModelDev> models_;
@@ -1133,7 +1247,8 @@ void MixedEngine::set_skin(float frac) {
     need_rebuild_ = true;
 }
 
-int MixedEngine::init_batch(const std::vector<const HScene*>& scenes, const vedo_engine_opts& opts) {
+int MixedEngine::init_from(const std::vector<SceneSource>& src, const MixedEngine* prev,
+                           const vedo_engine_opts& opts) {
     opts_ = opts;
     if (opts_.check_interval == 0) opts_.check_interval = 10;
     skin_frac_ = opts.skin > 0 ? opts.skin : 0.15f;
@@ -1141,20 +1256,32 @@ int MixedEngine::init_batch(const std::vector<const HScene*>& scenes, const vedo
     tpb_ = opts.tick_block ? (int)opts.tick_block : TPB;
     if (tpb_ < 32 || tpb_ > TPB || tpb_ % 32) return fail(VEDO_ERR_INVALID_ARGUMENT, "tick_block must be 32..256, a multiple of 32");
     tune_pending_ = opts.autotune != 0;
-    if (scenes.empty()) return fail(VEDO_ERR_INVALID_SCENE, "empty batch");
+    if (prev) {                    // a repacked engine keeps the tuning of the one it replaces
+        skin_frac_ = prev->skin_frac_;
+        cell_scale_ = prev->cell_scale_;
+        tpb_ = prev->tpb_;
+        tune_pending_ = prev->tune_pending_;
+    }
+    if (src.empty()) return fail(VEDO_ERR_INVALID_SCENE, "empty batch");
     // ---- per-scene tables, concatenated
     std::vector<uint32_t> model_of, scene_of;
-    std::vector<double> pos, vel, av, ox, oz, imp, aimp;
+    std::vector<double> st[7];                 // staged host state of the new scenes
     std::vector<double4_32a> geo, rr;
     std::vector<float> pc, reach;
     std::vector<float4> mf;
     std::vector<double> gfield;
+    std::vector<MoveScene> moves;
     struct Rec { uint32_t a, b; float4 h; uint8_t f; };
-    std::vector<std::vector<Rec>> recs;
+    std::vector<std::vector<Rec>> recs;        // per new-scene object offset in staging order
+    uint32_t n_stage = 0;
     int law = -1;
-    for (const HScene* hp : scenes) {
+    for (const SceneSource& so : src) {
+        const bool kept = so.prev_scene >= 0;
+        if (kept && (!prev || (size_t)so.prev_scene >= prev->sc_.size()))
+            return fail(VEDO_ERR_INVALID_ARGUMENT, "scene source out of range");
+        std::shared_ptr<const HScene> hp = kept ? prev->host_[so.prev_scene] : std::make_shared<HScene>(*so.host);
         const HScene& h = *hp;
-        host_.push_back(h);
+        host_.push_back(hp);
         Tables t;
         std::string msg;
         int rc = build_tables(h, t, msg);
@@ -1166,7 +1293,8 @@ int MixedEngine::init_batch(const std::vector<const HScene*>& scenes, const vedo
         S.nm = (uint32_t)t.models.size();
         S.pbase = np_;
         S.dt = h.time_interval;
-        S.t = h.time_current;
+        S.t = kept ? prev->sc_[so.prev_scene].t : h.time_current;
+        S.steps = kept ? prev->sc_[so.prev_scene].steps : 0;
         S.t_stop = h.time_stop;
         for (int k = 0; k < 3; ++k) S.g[k] = h.g[k];
         double rmax = 0.0;
@@ -1189,14 +1317,31 @@ int MixedEngine::init_batch(const std::vector<const HScene*>& scenes, const vedo
         S.wall_end = (uint32_t)glob_.size();
         S.rmax = (float)rmax;
         S.skin = skin_frac_ * S.rmax;
-        for (auto* pr : {&pos, &vel, &av, &ox, &oz, &imp, &aimp}) (void)pr;
-        pos.insert(pos.end(), h.pos.begin(), h.pos.end());
-        vel.insert(vel.end(), h.vel.begin(), h.vel.end());
-        av.insert(av.end(), h.av.begin(), h.av.end());
-        ox.insert(ox.end(), h.ox.begin(), h.ox.end());
-        oz.insert(oz.end(), h.oz.begin(), h.oz.end());
-        imp.insert(imp.end(), h.imp.begin(), h.imp.end());
-        aimp.insert(aimp.end(), h.aimp.begin(), h.aimp.end());
+        if (kept) {
+            moves.push_back(MoveScene{n_, h.n, prev->sc_[so.prev_scene].obj_off, 0u});
+        } else {
+            moves.push_back(MoveScene{n_, h.n, n_stage, 1u});
+            const std::vector<double>* a[7] = {&h.pos, &h.vel, &h.av, &h.ox, &h.oz, &h.imp, &h.aimp};
+            for (int k = 0; k < 7; ++k) st[k].insert(st[k].end(), a[k]->begin(), a[k]->end());
+            // IactRecordTab records, owned by the lower sphere (or the sphere of a wall pair)
+            recs.resize((size_t)n_stage + h.n);
+            for (uint32_t q = 0; q < h.rec.size(); ++q) {
+                uint32_t ra = h.rec.first[q], rb = h.rec.second[q];
+                if (ra >= h.n || rb >= h.n) continue;
+                const bool aw = t.models[h.model_of[ra]].scope != SCOPE_LOCAL;
+                const bool bw = t.models[h.model_of[rb]].scope != SCOPE_LOCAL;
+                if (aw && !bw) std::swap(ra, rb);
+                Rec r;
+                r.a = n_stage + ra;
+                r.b = (n_ + rb) | ((aw || bw) ? WALL_BIT : 0u);
+                r.h = make_float4((float)h.rec.shear[3 * q], (float)h.rec.shear[3 * q + 1],
+                                  (float)h.rec.shear[3 * q + 2], (float)h.rec.kn[q]);
+                r.f = (uint8_t)(HF_LAST_CONTACT | HF_LAST_BOND | (h.rec.contact[q] ? HF_CONTACT : 0) |
+                                (h.rec.bond[q] ? HF_BOND : 0));
+                recs[r.a].push_back(r);
+            }
+            n_stage += h.n;
+        }
         for (const ModelDev& M : t.models) models_.push_back(M);
         const size_t nq = (size_t)S.nm * S.nm;
         for (size_t q = 0; q < nq; ++q) {
@@ -1221,24 +1366,6 @@ int MixedEngine::init_batch(const std::vector<const HScene*>& scenes, const vedo
             mf.push_back(make_float4((float)M.rot_coef, 0.0f, 0.0f, 0.0f));
         }
         for (int k = 0; k < 3; ++k) gfield.push_back(h.g[k]);
-        // IactRecordTab records of this scene, owned by the lower sphere (or the sphere of a wall pair)
-        std::vector<Rec> rv;
-        for (uint32_t q = 0; q < h.rec.size(); ++q) {
-            uint32_t a = h.rec.first[q], b = h.rec.second[q];
-            if (a >= h.n || b >= h.n) continue;
-            const bool aw = t.models[h.model_of[a]].scope != SCOPE_LOCAL;
-            const bool bw = t.models[h.model_of[b]].scope != SCOPE_LOCAL;
-            if (aw && !bw) std::swap(a, b);
-            Rec r;
-            r.a = n_ + a;
-            r.b = (n_ + b) | ((aw || bw) ? WALL_BIT : 0u);
-            r.h = make_float4((float)h.rec.shear[3 * q], (float)h.rec.shear[3 * q + 1], (float)h.rec.shear[3 * q + 2],
-                              (float)h.rec.kn[q]);
-            r.f = (uint8_t)(HF_LAST_CONTACT | HF_LAST_BOND | (h.rec.contact[q] ? HF_CONTACT : 0) |
-                            (h.rec.bond[q] ? HF_BOND : 0));
-            rv.push_back(r);
-        }
-        recs.push_back(rv);
         n_ += h.n;
         nm_ += S.nm;
         np_ += (uint32_t)nq;
@@ -1286,50 +1413,116 @@ int MixedEngine::init_batch(const std::vector<const HScene*>& scenes, const vedo
     MCK(mal(&d_obs_, (size_t)(nblk(n_) + 2) * 16 + 64));
     MCK(cudaMemset(d_red_, 0, 64));
     MCK(cudaMemset(d_disp_, 0, 8));
-    double lo[3] = {DBL_MAX, DBL_MAX, DBL_MAX}, hi[3] = {-DBL_MAX, -DBL_MAX, -DBL_MAX};
-    for (uint32_t i = 0; i < n_; ++i)
-        for (int k = 0; k < 3; ++k) {
-            lo[k] = std::min(lo[k], pos[3 * i + k]);
-            hi[k] = std::max(hi[k], pos[3 * i + k]);
-        }
-    for (int k = 0; k < 3; ++k) origin_[k] = 0.5 * (lo[k] + hi[k]);
-    vedo_state_view v{pos.data(), vel.data(), av.data(), ox.data(), oz.data(), imp.data(), aimp.data()};
-    rc = set_state(v);
-    if (rc != VEDO_OK) return rc;
-    // records play the role of the previous neighbour list for the first history carry
+    if (prev) {
+        for (int k = 0; k < 3; ++k) origin_[k] = prev->origin_[k];
+    } else {
+        double lo[3] = {DBL_MAX, DBL_MAX, DBL_MAX}, hi[3] = {-DBL_MAX, -DBL_MAX, -DBL_MAX};
+        for (uint32_t i = 0; i < n_stage; ++i)
+            for (int k = 0; k < 3; ++k) {
+                lo[k] = std::min(lo[k], st[0][3 * (size_t)i + k]);
+                hi[k] = std::max(hi[k], st[0][3 * (size_t)i + k]);
+            }
+        for (int k = 0; k < 3; ++k) origin_[k] = n_stage ? 0.5 * (lo[k] + hi[k]) : 0.0;
+    }
+    // state: staged host scenes and scenes moved from the previous engine, one kernel
+    const size_t stride = 3 * (size_t)n_;
+    for (int k = 0; k < 7; ++k)
+        if (n_stage) MCK(cudaMemcpy(d_stage_ + k * stride, st[k].data(), 8 * st[k].size(), cudaMemcpyHostToDevice));
+    MoveScene* d_moves = nullptr;
+    MCK(mal(&d_moves, moves.size()));
+    MCK(cudaMemcpy(d_moves, moves.data(), sizeof(MoveScene) * moves.size(), cudaMemcpyHostToDevice));
+    StateArrays ps{};
+    ListArrays pl{}, sl{};
+    if (prev) {
+        const int pc_ = prev->cur_;
+        ps = StateArrays{prev->d_x_[pc_], prev->d_v64_, prev->d_w64_, prev->d_ox_, prev->d_oz_, prev->d_imp_,
+                         prev->d_aimp_};
+        const NList& PL = prev->nl_[prev->nlc_];
+        if (PL.ent) pl = ListArrays{PL.ptr, PL.ent, PL.slot, PL.h[pc_], PL.f[pc_]};
+    }
+    k_move_state<<<nblk(n_), TPB, 0, stream_>>>(n_, d_moves, (uint32_t)moves.size(), ps, d_stage_, stride,
+                                                d_x_[cur_], d_v64_, d_w64_, d_ox_, d_oz_, d_imp_, d_aimp_,
+                                                d_v32_[cur_], d_w32_[cur_]);
+    // histories to carry: the previous engine's list rows and the new scenes' records
+    uint32_t* s_buf = nullptr;
+    float4* s_h = nullptr;
+    uint8_t* s_f = nullptr;
     size_t nrec = 0;
     for (auto& r : recs) nrec += r.size();
     if (nrec) {
-        std::vector<std::vector<Rec*>> per(n_);
-        for (auto& rv : recs)
-            for (auto& r : rv) per[r.a].push_back(&r);
-        std::vector<uint32_t> optr(n_ + 1, 0), oent, oslot;
-        std::vector<float4> oh;
-        std::vector<uint8_t> of;
-        for (uint32_t i = 0; i < n_; ++i) {
-            optr[i] = (uint32_t)oent.size();
-            for (Rec* r : per[i]) {
-                oslot.push_back((uint32_t)oent.size());
-                oent.push_back(r->b);
-                oh.push_back(r->h);
-                of.push_back(r->f);
+        std::vector<uint32_t> sptr(n_stage + 1, 0), sent, sslot;
+        std::vector<float4> shv;
+        std::vector<uint8_t> sfv;
+        for (uint32_t i = 0; i < n_stage; ++i) {
+            sptr[i] = (uint32_t)sent.size();
+            for (const Rec& r : recs[i]) {
+                sslot.push_back((uint32_t)sent.size());
+                sent.push_back(r.b);
+                shv.push_back(r.h);
+                sfv.push_back(r.f);
             }
         }
-        optr[n_] = (uint32_t)oent.size();
+        sptr[n_stage] = (uint32_t)sent.size();
+        MCK(mal(&s_buf, sptr.size() + 2 * sent.size()));
+        MCK(mal(&s_h, sent.size()));
+        MCK(mal(&s_f, sent.size()));
+        MCK(cudaMemcpy(s_buf, sptr.data(), 4 * sptr.size(), cudaMemcpyHostToDevice));
+        MCK(cudaMemcpy(s_buf + sptr.size(), sent.data(), 4 * sent.size(), cudaMemcpyHostToDevice));
+        MCK(cudaMemcpy(s_buf + sptr.size() + sent.size(), sslot.data(), 4 * sslot.size(), cudaMemcpyHostToDevice));
+        MCK(cudaMemcpy(s_h, shv.data(), sizeof(float4) * shv.size(), cudaMemcpyHostToDevice));
+        MCK(cudaMemcpy(s_f, sfv.data(), sfv.size(), cudaMemcpyHostToDevice));
+        sl = ListArrays{s_buf, s_buf + sptr.size(), s_buf + sptr.size() + sent.size(), s_h, s_f};
+    }
+    if (pl.ent || sl.ent) {
         NList& O = nl_[1];
-        rc = ensure_nlist(O, (uint32_t)oent.size());
-        if (rc != VEDO_OK) return rc;
-        O.ne = (uint32_t)oent.size();
-        MCK(cudaMemcpy(O.ptr, optr.data(), 4 * (n_ + 1), cudaMemcpyHostToDevice));
-        MCK(cudaMemcpy(O.ent, oent.data(), 4 * oent.size(), cudaMemcpyHostToDevice));
-        MCK(cudaMemcpy(O.slot, oslot.data(), 4 * oslot.size(), cudaMemcpyHostToDevice));
-        MCK(cudaMemcpy(O.h[cur_], oh.data(), sizeof(float4) * oh.size(), cudaMemcpyHostToDevice));
-        MCK(cudaMemcpy(O.f[cur_], of.data(), of.size(), cudaMemcpyHostToDevice));
+        if (!O.ptr) MCK(mal(&O.ptr, (size_t)n_ + 1));
+        k_row_count<<<nblk((size_t)n_ + 1), TPB, 0, stream_>>>(n_, d_moves, (uint32_t)moves.size(), pl, sl, d_cnt_);
+        MCK(exclusive_scan_u32(d_cnt_, O.ptr, n_ + 1, d_red_ + 9, scratch_, stream_));
+        uint32_t ne = 0;
+        MCK(cudaMemcpyAsync(&ne, d_red_ + 9, 4, cudaMemcpyDeviceToHost, stream_));
+        MCK(cudaStreamSynchronize(stream_));
+        if ((rc = ensure_nlist(O, ne)) != VEDO_OK) return rc;
+        O.ne = ne;
+        k_row_fill<<<nblk(n_), TPB, 0, stream_>>>(n_, d_moves, (uint32_t)moves.size(), pl, sl, O.ptr, O.ent, O.slot,
+                                                  O.h[cur_], O.f[cur_]);
         nlc_ = 1;
     }
+    MCK(cudaStreamSynchronize(stream_));
+    MCK(cudaGetLastError());
+    cudaFree(d_moves);
+    if (s_buf) cudaFree(s_buf);
+    if (s_h) cudaFree(s_h);
+    if (s_f) cudaFree(s_f);
+    need_rebuild_ = true;
     rc = rebuild();
     if (rc != VEDO_OK) return rc;
     MCK(cudaStreamSynchronize(stream_));
+    return VEDO_OK;
+}
+
+int MixedEngine::set_scene_active(uint32_t s, bool on) {
+    if (s >= sc_.size()) return fail(VEDO_ERR_INVALID_ARGUMENT, "scene index out of range");
+    sc_[s].active = on;
+    sdev_[s].active = on ? 1u : 0u;
+    MCK(cudaMemcpyAsync(d_scenes_ + s, &sdev_[s], sizeof(SceneDev), cudaMemcpyHostToDevice, stream_));
+    MCK(cudaStreamSynchronize(stream_));
+    drop_graphs();
+    return VEDO_OK;
+}
+
+int MixedEngine::get_state_slice(uint32_t off, uint32_t cnt, const vedo_state_view& v) {
+    if ((uint64_t)off + cnt > n_) return fail(VEDO_ERR_INVALID_ARGUMENT, "object range out of bounds");
+    double* dst[] = {v.position, v.velocity, v.angular_velocity, v.orientation_x, v.orientation_z, v.impact,
+                     v.angular_impact};
+    const double4_32a* src[] = {d_x_[cur_], d_v64_, d_w64_, d_ox_, d_oz_, d_imp_, d_aimp_};
+    for (int k = 0; k < 7; ++k) {
+        if (!dst[k] || !cnt) continue;
+        double* stg = d_stage_ + (size_t)k * 3 * n_;
+        k_unpack3m<<<nblk(cnt), TPB, 0, stream_>>>(cnt, src[k] + off, stg);
+        MCK(cudaMemcpyAsync(dst[k], stg, 24 * (size_t)cnt, cudaMemcpyDeviceToHost, stream_));
+    }
+    MCK(cudaStreamSynchronize(stream_));
+    MCK(cudaGetLastError());
     return VEDO_OK;
 }
 
@@ -1410,7 +1603,7 @@ int MixedEngine::rebuild() {
         D.wall_end = H.wall_end;
         D.obj_off = H.obj_off;
         D.nobj = H.nobj;
-        D.pad = 0;
+        D.active = H.active ? 1u : 0u;
         D.dt = H.dt;
         float lo[3] = {0, 0, 0}, hi[3] = {0, 0, 0};
         if (H.nloc)
@@ -1606,8 +1799,11 @@ int MixedEngine::step_chunk(uint32_t chunk, bool imp_last, float* disp_after) {
     const uint32_t taken = chunk - std::min(held, chunk);
     round_ += taken;
     since_rebuild_ += taken;
-    for (auto& S : sc_)
+    for (auto& S : sc_) {
+        if (!S.active) continue;
         for (uint32_t k = 0; k < taken; ++k) S.t += S.dt;     // SystemParameter::NextStep (SystemParameter.h:113-116), once per step
+        S.steps += taken;
+    }
     const float half_skin = 0.5f * skin_min_;
     if (held || disp > half_skin) {
         // held steps are taken again after the rebuild; a bound already past half the skin
@@ -1883,7 +2079,7 @@ int MixedEngine::get_observables(double out[13]) {
 
 int MixedEngine::write_ido(const char* path) {
     if (sc_.size() != 1) return fail(VEDO_ERR_INVALID_ARGUMENT, "write_ido needs a single-scene engine");
-    HScene& hs = host_[0];
+    HScene hs = *host_[0];
     vedo_state_view v{hs.pos.data(), hs.vel.data(), hs.av.data(), hs.ox.data(), hs.oz.data(), hs.imp.data(),
                       hs.aimp.data()};
     int rc = get_state(v);
@@ -1942,6 +2138,48 @@ int mixed_scene_range(EngineBase* e, uint32_t s, uint32_t* off, uint32_t* n, dou
     int rc = m->scene_range(s, off, n);
     if (rc == VEDO_OK && t) *t = m->scene_time(s);
     return rc;
+}
+
+// Continuous batching (serve.cpp): a new engine from scenes `keep` of `prev` (their device
+// state and histories move over) followed by the host scenes `add`.
+EngineBase* mixed_repack(EngineBase* prev, const std::vector<uint32_t>& keep, const std::vector<const HScene*>& add,
+                         const vedo_engine_opts& opts, int* rc, std::string* err) {
+    MixedEngine* p = prev ? dynamic_cast<MixedEngine*>(prev) : nullptr;
+    if (prev && !p) {
+        *rc = VEDO_ERR_INVALID_ARGUMENT;
+        *err = "repack needs a MIXED-form engine";
+        return nullptr;
+    }
+    std::vector<MixedEngine::SceneSource> src;
+    for (uint32_t k : keep) src.push_back(MixedEngine::SceneSource{nullptr, (int)k});
+    for (const HScene* h : add) src.push_back(MixedEngine::SceneSource{h, -1});
+    MixedEngine* e = new (std::nothrow) MixedEngine();
+    if (!e) {
+        *rc = VEDO_ERR_OUT_OF_MEMORY;
+        return nullptr;
+    }
+    *rc = e->init_from(src, p, opts);
+    if (*rc != VEDO_OK) {
+        *err = e->error();
+        delete e;
+        return nullptr;
+    }
+    return e;
+}
+
+int mixed_set_scene_active(EngineBase* e, uint32_t s, bool on) {
+    MixedEngine* m = dynamic_cast<MixedEngine*>(e);
+    return m ? m->set_scene_active(s, on) : VEDO_ERR_INVALID_ARGUMENT;
+}
+
+int mixed_get_state_slice(EngineBase* e, uint32_t off, uint32_t cnt, const vedo_state_view& v) {
+    MixedEngine* m = dynamic_cast<MixedEngine*>(e);
+    return m ? m->get_state_slice(off, cnt, v) : VEDO_ERR_INVALID_ARGUMENT;
+}
+
+uint64_t mixed_scene_steps(EngineBase* e, uint32_t s) {
+    MixedEngine* m = dynamic_cast<MixedEngine*>(e);
+    return m ? m->steps_of_scene(s) : 0;
 }
 
 uint32_t mixed_num_scenes(EngineBase* e) {

@@ -20,6 +20,9 @@ code, the C oracle and the GPU engine.
   orifice), monodisperse r = 1 mm Hertz spheres with friction (``ISwH``); the batch
   draws sphere counts log-uniform on [1e3, 5e4], friction U(0.2, 0.6), restitution
   U(0.5, 0.9) and orifice width U(6, 12) mm per scene.
+* :func:`serving_job` - the serving stream's jobs: a settling box or a projectile
+  impact on a bed, lognormal radii (median 1 mm, sigma_log 0.15) in 8 classes, linear
+  spring-dashpot or Hertz (``ISwH``, E = 0.5 GPa) contact.
 * :func:`cluster` - small random clusters used by the parity tests (every
   solver, plates, cylinders, orbital walls).
 """
@@ -416,3 +419,78 @@ def hopper_batch(num_scenes: int = 256, seed: int = 2025, steps: int = 5000, n_l
     """The batched hopper workload: `num_scenes` independent hoppers of uneven sizes."""
     return [hopper(n=n, seed=sd, friction=mu, restitution=e, orifice=w, steps=steps)
             for n, sd, mu, e, w in hopper_params(num_scenes, seed, n_lo, n_hi)]
+
+
+def serving_job(kind: str, n: int, model: str, seed: int, steps: int = 1000, K: int = 8,
+                median_r: float = 1e-3, sigma_log: float = 0.15, dt: float = 1e-6) -> Scene:
+    """A job of the serving stream.
+
+    kind 'settle': n spheres on a jittered lattice (spacing 2.2 r_max) fall into an open box
+    of 5 fixed plates with velocities N(0, 0.05 m/s).  kind 'projectile': the same lattice
+    rests just above the floor and one sphere of radius 3 mm, 1 m/s downwards, hits its
+    centre.  Radii are lognormal(median_r, sigma_log) clipped to [0.6, 1.6] mm and binned
+    into K classes, one DOModel per class.  model 'lsd': ``ISwBSDBF`` with kn = 1e4 N/m,
+    ks = 0.8 kn, restitution 0.8, friction 0.5; 'hertz': ``ISwH`` with E = 0.5 GPa, nu = 0.3,
+    restitution 0.7, friction 0.4 (a stiffness for which dt = 1e-6 s is about 0.13 of the
+    smallest sphere's Rayleigh time)."""
+    rng = np.random.default_rng(seed)
+    edges = np.exp(np.linspace(math.log(0.6e-3), math.log(1.6e-3), K + 1))
+    centres = np.sqrt(edges[:-1] * edges[1:])
+    r = np.clip(median_r * np.exp(sigma_log * rng.standard_normal(n)), edges[0], edges[-1] * (1 - 1e-12))
+    cls = np.clip(np.searchsorted(edges, r, side="right") - 1, 0, K - 1).astype(np.uint32)
+    rmax = float(centres[cls].max())
+    a = 2.2 * rmax
+    m = max(2, int(math.ceil((n / 2.0) ** (1.0 / 3.0))))
+    nz = int(math.ceil(n / (m * m)))
+    g = np.stack(np.meshgrid(np.arange(m), np.arange(m), np.arange(nz), indexing="ij"), -1).reshape(-1, 3)[:n]
+    pos = np.empty((n, 3))
+    pos[:, 0] = (g[:, 0] - 0.5 * (m - 1)) * a
+    pos[:, 1] = (g[:, 1] - 0.5 * (m - 1)) * a
+    pos[:, 2] = g[:, 2] * a + 1.05 * rmax
+    pos += rng.uniform(-0.02 * rmax, 0.02 * rmax, size=pos.shape)
+    vel = rng.normal(0.0, 0.05, size=pos.shape) if kind == "settle" else np.zeros((n, 3))
+    width = m * a + 4.0 * rmax
+    density = 2500.0
+    models = [DOModel(f"B{k}", f"B{k}", MOBILE, LOCAL, density, 1.0, SPHERE, (float(centres[k]),)) for k in range(K)]
+    groups = [f"B{k}" for k in range(K)]
+    P, V, midx = [pos], [vel], [cls]
+    if kind == "projectile":
+        rp = 3e-3
+        models.append(DOModel("Proj", "Proj", MOBILE, LOCAL, density, 1.0, SPHERE, (rp,)))
+        groups.append("Proj")
+        P.append(np.array([[0.0, 0.0, nz * a + rmax + rp + 2e-4]]))
+        V.append(np.array([[0.0, 0.0, -1.0]]))
+        midx.append(np.array([K], np.uint32))
+    base = len(models)
+    wm, widx, wp, wox, woz = box_walls(width, nz * a + 12e-3, 1e-3)
+    models += wm
+    nball = sum(len(x) for x in P)
+    midx = np.concatenate(midx + [base + np.array(widx, np.uint32)])
+    P = np.concatenate(P + [wp])
+    V = np.concatenate(V + [np.zeros_like(wp)])
+    nt = len(midx)
+    OX = np.concatenate([np.tile([1.0, 0, 0], (nball, 1)), wox])
+    OZ = np.concatenate([np.tile([0, 0, 1.0], (nball, 1)), woz])
+    AV = np.zeros((nt, 3))
+    radius_of = {gname: float(models[k].attrs[0]) for k, gname in enumerate(groups)}
+    m_of = lambda rr: density * 4.0 / 3.0 * math.pi * rr ** 3
+    iacts = []
+    if model == "lsd":
+        zeta = damping_ratio(0.8)
+        mech = lambda wall: lsd_mechanisms(1e4, 8e3, zeta if wall else zeta / math.sqrt(2.0),
+                                           zeta if wall else zeta / math.sqrt(2.0), 0.5)
+        for i, ga in enumerate(groups):
+            for gb in groups[i:]:
+                iacts.append(IactModel(ga, gb, "ISwBSDBF", mech(False)))
+        for gb in groups:
+            iacts.append(IactModel("Wall", gb, "ISwBSDBF", mech(True)))
+    else:
+        zeta = damping_ratio(0.7)
+        for i, ga in enumerate(groups):
+            for gb in groups[i:]:
+                iacts.append(IactModel(ga, gb, "ISwH", _hertz_mech("ISwH", 0.5e9, 0.3, radius_of[ga], radius_of[gb],
+                                                                    m_of, zeta, 0.4)))
+        for gb in groups:
+            iacts.append(IactModel("Wall", gb, "ISwH", _hertz_mech("ISwH", 0.5e9, 0.3, radius_of[gb], None, m_of,
+                                                                    zeta, 0.4)))
+    return Scene(time_control(steps, dt), models, iacts, midx, P, V, OX, OZ, AV)
