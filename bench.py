@@ -47,6 +47,13 @@ def parse():
     ap.add_argument("--cpu-sample-steps", type=int, default=20)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-profile-pass", action="store_true")
+    ap.add_argument("--profile-steps", type=int, default=20, help="steps of the per-kernel timing pass")
+    ap.add_argument("--batch-scenes", type=int, default=256, help="hopper scenes of the batched workload")
+    ap.add_argument("--batch-steps", type=int, default=300, help="timed steps of the batched workload")
+    ap.add_argument("--serve-duration", type=float, default=0.25, help="seconds of Poisson arrivals (200/s)")
+    ap.add_argument("--serve-steps-scale", type=float, default=0.1, help="job step counts x this factor")
+    ap.add_argument("--no-batch", action="store_true")
+    ap.add_argument("--no-serve", action="store_true")
     return ap.parse_args()
 
 
@@ -278,13 +285,14 @@ def ours(args, dist):
             b.close()
     f64.close()
 
-    # per-kernel split of the mixed form (tick = fused detect-force-integrate) from one
-    # profiled window
+    # per-kernel times of the mixed form from one profiled window: every tick launch (the
+    # fused detect-force-integrate kernel) is timed alone with CUDA events on the engine stream
     kern = None
     if not args.no_profile_pass:
         eng.set_profiling(True)
-        eng.run(args.up_iact)
+        eng.run(args.profile_steps)
         kern = eng.last_run_profile()
+        kern["steps"] = args.profile_steps
         eng.set_profiling(False)
     # e2e through the C ABI with pinned host buffers
     fields = ("position", "velocity", "angular_velocity", "orientation_x", "orientation_z")
@@ -314,13 +322,18 @@ def ours(args, dist):
     b_alg = 2 * s_state + z_pp * (2 * s_hist + 8) + 8
     peak, peak_kind = peaks()
     roof = None
-    if kern and kern["total_ms"] > 0:
-        t_step = t_ms / args.steps
-        ach = b_alg * n / (t_step * 1e-3) / 1e9
+    if kern and kern["pair_ms"] > 0:
+        t_tick = kern["pair_ms"] / kern["steps"]            # average duration of one tick launch
+        ach = b_alg * n / (t_tick * 1e-3) / 1e9
+        traffic = ncu_traffic_per_particle_step()
         roof = {"kernel": "k_tick (fused narrow phase + forces + integration, one launch per step)",
                 "bound": "hbm", "achieved": ach, "peak": peak, "unit": "GB/s", "frac": ach / peak,
-                "peak_source": peak_kind, "traffic": None, "ms_per_step": t_step,
-                "alg_bytes_per_step": b_alg * n}
+                "peak_source": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)" if peak_kind == "measured" else peak_kind,
+                "traffic": traffic * n if traffic else None,
+                "traffic_source": "profiles/k_tick_mixed_drum200k_ncu.md, dram bytes per particle-step x particles"
+                if traffic else None,
+                "tick_ms": t_tick, "walls_ms": kern["object_ms"] / kern["steps"],
+                "share_of_step": t_tick / (t_ms / args.steps), "alg_bytes_per_launch": b_alg * n}
     res = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": dist.world, "steps": args.steps,
            "warmup": args.warmup, "ms_per_step": t_ms / args.steps, "higher_is_better": True, "scaling": "weak",
            "vs_baseline": None, "dtype": "f32 forces + f64 state (mixed)",
@@ -344,8 +357,90 @@ def ours(args, dist):
                            f"{args.sync} steps, pinned host buffers, mixed form"},
            "roofline": roof, "cpu_baseline": cpu}
     eng.close()
+    if not args.no_batch:
+        res["batch"] = batch_workload(args, dist, dev)
+    if not args.no_serve and dist.world == 1:
+        res["serving"] = serving_workload(args, dev)
     if dist.rank == 0:
         emit(res)
+
+
+def ncu_traffic_per_particle_step():
+    """DRAM bytes per particle-step of the tick kernel from the committed ncu summary."""
+    try:
+        for line in open(os.path.join(ROOT, "profiles", "k_tick_mixed_drum200k_ncu.md")):
+            if line.startswith("dram_bytes_per_particle_step:"):
+                return float(line.split(":", 1)[1].split()[0])
+    except OSError:
+        pass
+    return None
+
+
+def batch_workload(args, dist, dev):
+    """The batched workload: hopper scenes of 1e3..5e4 spheres in one autotuned engine whose
+    check intervals replay as CUDA graphs (one fused tick launch per step over all scenes)."""
+    import torch
+    from vedo_gb300 import scenes
+    from vedo_gb300.engine import BatchEngine
+    hs = scenes.hopper_batch(args.batch_scenes, seed=2025 + dist.rank, steps=5000)
+    n = sum(scene_particles(h) for h in hs)
+    b = BatchEngine(hs, device=dev, autotune=True)
+    del hs
+    b.run(100)                       # autotuning (80 steps) + warm-up; the tuned settings stay
+    dist.barrier()
+    torch.cuda.synchronize()
+    b.run(args.batch_steps)
+    prof = b.last_run_profile()
+    t = dist.reduce(prof["total_ms"], "max")
+    total = dist.reduce(float(n), "sum")
+    out = {"workload": f"hopper_batch_{args.batch_scenes}", "scenes": args.batch_scenes, "particles": n,
+           "value": total * args.batch_steps / (t * 1e-3), "unit": UNIT, "ms_per_step": t / args.batch_steps,
+           "steps": args.batch_steps, "gpu_launches": prof["launches"], "tuning": b.tuning(),
+           "note": f"steps 100..{100 + args.batch_steps} of the configured 5000-step run; mixed form, "
+                   "CUDA-graph check intervals, autotuned tick block, skin and cell scale"}
+    b.close()
+    return out
+
+
+def serving_workload(args, dev):
+    """The serving stream, scaled: Poisson arrivals at 200 jobs/s for `--serve-duration` s,
+    sphere counts 2e3..2e5, step counts 1e3..2e4 scaled by `--serve-steps-scale`.  Served by
+    the continuous-batching server (mixed form) and, for comparison, one job at a time on the
+    plain FP64 engine with the same arrival times (latency = completion - arrival)."""
+    import numpy as np
+    from vedo_gb300 import serve
+    from vedo_gb300.engine import GpuEngine
+    sl, sh = max(1, int(1000 * args.serve_steps_scale)), max(2, int(20000 * args.serve_steps_scale))
+    stream = serve.job_stream(rate=200.0, duration=args.serve_duration, seed=4242, steps_lo=sl, steps_hi=sh)
+    if not stream:
+        return None
+    built = [serve.job_scene(k, n, m, sd, st) for (_, k, n, st, m, sd) in stream]
+    with serve.Server(hbm_budget_bytes=150 * 10**9, device=dev) as srv:
+        r = serve.serve_stream(srv, stream, built)
+        st = srv.stats()
+    # the same stream one job at a time on the FP64 engine
+    parts = [scene_particles(sc) for sc in built]
+    t_free, lat64, busy = 0.0, [], 0.0
+    for (ta, _, _, steps, _, _), sc in zip(stream, built):
+        t0 = time.perf_counter()
+        e = GpuEngine(sc, up_iact=20, device=dev)
+        e.run(steps)
+        e.close()
+        d = time.perf_counter() - t0
+        busy += d
+        start = max(ta, t_free)
+        t_free = start + d
+        lat64.append(t_free - ta)
+    ps = sum(p * s for p, (_, _, _, s, _, _) in zip(parts, stream))
+    p64 = serve.latency_percentiles(lat64)
+    return {"workload": f"serving stream, 200 jobs/s x {args.serve_duration} s ({len(stream)} jobs), "
+                        f"steps {sl}..{sh} (x{args.serve_steps_scale} of 1e3..2e4), 2e3..2e5 spheres",
+            "p50_ms": r["p50_ms"], "p99_ms": r["p99_ms"], "jobs_done": r["done"], "jobs": r["jobs"],
+            "served_particle_steps_per_s": r["served_particle_steps_per_s"],
+            "offered_particle_steps_per_s": r["offered_particle_steps_per_s"], "wall_s": r["wall_s"],
+            "batches_built": st["batches"], "hbm_budget_gb": 150,
+            "fp64_one_at_a_time": {"p50_ms": p64["p50_ms"], "p99_ms": p64["p99_ms"],
+                                   "particle_steps_per_s": ps / max(t_free, 1e-9), "busy_s": busy}}
 
 
 def main():

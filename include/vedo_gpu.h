@@ -231,9 +231,11 @@ int vedo_gpu_write_ido(vedo_gpu_engine* e, const char* path);
 
 /* Device time of the last vedo_gpu_run call in milliseconds, from CUDA events on
  * the engine's stream: out[3] = the whole call; with profiling on (see
- * vedo_gpu_set_profiling) also out[0] = pair kernel (detect + impact solve),
- * out[1] = object kernels (gather + integrate), out[2] = broad-phase rebuilds.
- * Returns the number of kernel launches the call issued. */
+ * vedo_gpu_set_profiling) also, FP64 form: out[0] = pair kernel (detect + impact
+ * solve), out[1] = object kernels (gather + integrate); MIXED form: out[0] = the
+ * fused tick kernel (every launch timed alone), out[1] = the wall kernels; both:
+ * out[2] = broad-phase rebuilds.  Returns the number of kernel launches the call
+ * issued. */
 uint64_t vedo_gpu_last_run_profile(const vedo_gpu_engine* e, double out[4]);
 
 /* Enable per-phase CUDA-event timing for vedo_gpu_last_run_profile (adds one host

@@ -1127,11 +1127,14 @@ private:
     int tpb_ = TPB;                 // threads per block of the tick kernel
     bool tune_pending_ = false;
     cudaGraphExec_t graph_[2] = {nullptr, nullptr};   // one check interval of steps, by start parity
+    std::vector<cudaEvent_t> pev_;  // profiling: per step, events before the tick, after it, after the walls
+    uint32_t pev_used_ = 0;
     uint64_t round_ = 0;
     int cur_ = 0;                   // which of the A/B buffers is "A" (current)
     bool need_rebuild_ = true;
     bool profiling_ = false;
     double prof_[4] = {0, 0, 0, 0};
+    uint64_t prof_ticks_ = 0;       // tick launches timed in the last run (profiling on)
     uint64_t launches_ = 0;
     uint64_t rebuilds_ = 0;
     uint64_t since_rebuild_ = 0;
@@ -1227,6 +1230,7 @@ MixedEngine::~MixedEngine() {
                     d_wkey_, d_wval_, d_wkey_alt_, d_wval_alt_, d_wptr_, d_wimp_};
     for (void* p : ptrs) if (p) cudaFree(p);
     drop_graphs();
+    for (auto& e : pev_) cudaEventDestroy(e);
     for (auto& e : ev_) if (e) cudaEventDestroy(e);
     if (stream_) cudaStreamDestroy(stream_);
 }
@@ -1743,6 +1747,12 @@ int MixedEngine::rebuild() {
 void MixedEngine::launch_step(bool write_imp) {
     TickArgs a = args(write_imp);
     const unsigned nb = (unsigned)((n_ + tpb_ - 1) / tpb_);
+    cudaEvent_t* pe = nullptr;
+    if (profiling_ && pev_used_ + 3 <= pev_.size()) {
+        pe = &pev_[pev_used_];
+        pev_used_ += 3;
+        cudaEventRecord(pe[0], stream_);
+    }
     switch (law_) {
     case IS_BSDBF: k_tick<IS_BSDBF><<<nb, tpb_, 0, stream_>>>(a); break;
     case IS_BTSDBF: k_tick<IS_BTSDBF><<<nb, tpb_, 0, stream_>>>(a); break;
@@ -1752,6 +1762,7 @@ void MixedEngine::launch_step(bool write_imp) {
     default: k_tick<0><<<nb, tpb_, 0, stream_>>>(a); break;
     }
     ++launches_;
+    if (pe) cudaEventRecord(pe[1], stream_);
     if (write_imp && !glob_.empty()) {
         k_wall_sum<<<nblk((uint64_t)glob_.size() * 32), TPB, 0, stream_>>>(
             (uint32_t)glob_.size(), d_glob_, d_wptr_, d_wval_, d_wimp_, d_model_of_, d_models_, d_scenes_, d_scene_of_,
@@ -1763,6 +1774,7 @@ void MixedEngine::launch_step(bool write_imp) {
         a.v32A, a.v32B, a.w32A, a.w32B, d_ox_, d_oz_, dt_max_, d_red_ + 8, d_disp_ + cur_, d_disp_ + (cur_ ^ 1),
         0.5f * skin_min_, d_red_ + 12, d_red_ + 11, d_wall32_);
     ++launches_;
+    if (pe) cudaEventRecord(pe[2], stream_);
     cur_ ^= 1;
 }
 
@@ -1770,7 +1782,15 @@ void MixedEngine::launch_step(bool write_imp) {
 // check interval without impulse output replays a CUDA graph captured once per list.
 int MixedEngine::step_chunk(uint32_t chunk, bool imp_last, float* disp_after) {
     const uint32_t ci = opts_.check_interval;
-    if (opts_.graphs && chunk == ci && !imp_last) {
+    if (profiling_ && pev_.size() < 3 * (size_t)ci) {
+        while (pev_.size() < 3 * (size_t)ci) {
+            cudaEvent_t e = nullptr;
+            MCK(cudaEventCreate(&e));
+            pev_.push_back(e);
+        }
+    }
+    pev_used_ = 0;
+    if (opts_.graphs && !profiling_ && chunk == ci && !imp_last) {
         const int c0 = cur_;
         if (!graph_[c0]) {
             cudaGraph_t g = nullptr;
@@ -1796,6 +1816,15 @@ int MixedEngine::step_chunk(uint32_t chunk, bool imp_last, float* disp_after) {
     MCK(cudaMemcpyAsync(&disp, d_disp_ + cur_, 4, cudaMemcpyDeviceToHost, stream_));
     MCK(cudaMemcpyAsync(&held, d_red_ + 11, 4, cudaMemcpyDeviceToHost, stream_));
     MCK(cudaStreamSynchronize(stream_));
+    for (uint32_t q = 0; q + 3 <= pev_used_; q += 3) {   // profiling: tick and wall kernel times
+        float a = 0.0f, b = 0.0f;
+        cudaEventElapsedTime(&a, pev_[q], pev_[q + 1]);
+        cudaEventElapsedTime(&b, pev_[q + 1], pev_[q + 2]);
+        prof_[0] += a;
+        prof_[1] += b;
+        prof_ticks_ += 1;
+    }
+    pev_used_ = 0;
     const uint32_t taken = chunk - std::min(held, chunk);
     round_ += taken;
     since_rebuild_ += taken;
@@ -1903,6 +1932,7 @@ int MixedEngine::autotune(uint32_t max_steps, uint32_t* taken) {
 
 int MixedEngine::run(uint32_t nsteps, int* keep_running) {
     prof_[0] = prof_[1] = prof_[2] = prof_[3] = 0;
+    prof_ticks_ = 0;
     launches_ = 0;
     MCK(cudaSetDevice(opts_.device));
     MCK(cudaEventRecord(ev_[0], stream_));
@@ -1917,8 +1947,16 @@ int MixedEngine::run(uint32_t nsteps, int* keep_running) {
     }
     while (done < nsteps) {
         if (need_rebuild_) {
+            if (profiling_) MCK(cudaEventRecord(ev_[2], stream_));
             int rc = rebuild();
             if (rc != VEDO_OK) return rc;
+            if (profiling_) {
+                MCK(cudaEventRecord(ev_[3], stream_));
+                MCK(cudaEventSynchronize(ev_[3]));
+                float ms = 0.0f;
+                cudaEventElapsedTime(&ms, ev_[2], ev_[3]);
+                prof_[2] += ms;
+            }
         }
         const uint32_t chunk = std::min<uint32_t>(nsteps - done, ci - (uint32_t)(since_rebuild_ % ci));
         const uint64_t r0 = round_;
