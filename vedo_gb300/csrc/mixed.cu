@@ -54,6 +54,15 @@ constexpr int TPB = 256;
 inline unsigned nblk(uint64_t n, int tpb = TPB) { return (unsigned)((n + tpb - 1) / tpb); }
 
 constexpr uint32_t WALL_BIT = 0x80000000u;
+// Per-entry facts fixed at rebuild (k_meta), so that the tick reads one word instead of both
+// objects' models and the pair's parameters: the pair-parameter index (bits 0-23), the
+// contact detector (bits 24-25), "bondable law" (the FP32 prefilter may not skip the pair),
+// "history owner" (the entry holds the pair's history) and "this sphere is the slave".
+constexpr uint32_t META_PI = 0x00ffffffu;
+constexpr int META_CD_SHIFT = 24;
+constexpr uint32_t META_BOND = 1u << 26;
+constexpr uint32_t META_OWNER = 1u << 27;
+constexpr uint32_t META_SLAVE = 1u << 28;
 constexpr uint8_t PF_ACTIVE_BIT = 64;
 // history flag bit: the status just became clean and the other buffer still holds the old one
 constexpr uint8_t HF_PENDING = 16;
@@ -280,6 +289,7 @@ struct TickArgs {
     const uint32_t* nptr;
     const uint32_t* nent;
     const uint32_t* nslot;
+    const uint32_t* nmeta;
     const float4* hA;
     float4* hB;
     const uint8_t* fA;
@@ -329,51 +339,46 @@ __global__ void __launch_bounds__(TPB) k_tick(TickArgs a) {
             const d3 Pi = ld(a.xA, i);
             const float dtf = (float)dt;
             const float disp = *a.disp;
+            const float4 p32i = a.pos32[i];
             K3 J, JA;
             const uint32_t e1 = a.nptr[i + 1];
             for (uint32_t e = a.nptr[i]; e < e1; ++e) {
                 const uint32_t ent = a.nent[e];
+                const uint32_t meta = a.nmeta[e];
+                const int cd = (int)((meta >> META_CD_SHIFT) & 3u);
+                if (cd == 0) continue;
                 const uint32_t j = ent & ~WALL_BIT;
                 const bool wall = ent & WALL_BIT;
-                const uint32_t mj = a.model_of[j];
-                // canonical orientation (Assembler.cpp:43-67); sphere-wall: the sphere is the slave
-                bool i_slave;
-                if (wall) {
-                    i_slave = true;
-                } else {
-                    const ModelDev& N = a.models[mj];
-                    if (M.density == 0.0 && N.density != 0.0) i_slave = false;
-                    else if (N.density == 0.0 && M.density != 0.0) i_slave = true;
-                    else i_slave = i < j;
-                }
+                // canonical orientation (Assembler.cpp:43-67), fixed at rebuild; sphere-wall: the sphere is the slave
+                const bool i_slave = meta & META_SLAVE;
+                const bool owner = meta & META_OWNER;
                 const uint32_t s = i_slave ? i : j, m = i_slave ? j : i;
-                const uint32_t pi = pidx(S, i_slave ? mi : mj, i_slave ? mj : mi);
-                const PairParam& P = a.params[pi];
-                if (P.cd == 0) continue;
-                const uint32_t slot = a.nslot[e];
-                const int is = LAW ? LAW : P.is;
-                const bool bondable = (is == IS_BSDBF || is == IS_BTSDBF || is == IS_BSDB2F) && P.c[4] != 0.0;
-                if (!bondable) {
+                const uint32_t pi = meta & META_PI;
+                if (!(meta & META_BOND)) {
                     // certainly apart: rebuild-time distance minus both spheres' travel since then
-                    const float4 ws = wall ? a.wall32[m] : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
-                    if (certainly_apart(P.cd, a.pos32[s], a.pos32[m], ws, a.reach[pi] + 2.0f * disp)) {
+                    const float4 ws = wall ? a.wall32[j] : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+                    const float4 p32j = a.pos32[j];
+                    if (certainly_apart(cd, i_slave ? p32i : p32j, i_slave ? p32j : p32i, ws,
+                                        a.reach[pi] + 2.0f * disp)) {
                         if (wall && a.write_imp) {
                             float* o = a.wimp + 6 * (size_t)e;
                             o[0] = o[1] = o[2] = o[3] = o[4] = o[5] = 0.0f;
                         }
-                        if (e == slot) {
-                            const uint8_t f0 = a.fA[slot];
+                        if (owner) {
+                            const uint8_t f0 = a.fA[e];
                             if (f0 & 15) {                 // ImpactStatus::Clean
-                                a.hB[slot] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
-                                a.fB[slot] = HF_PENDING;
+                                a.hB[e] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+                                a.fB[e] = HF_PENDING;
                             } else if (f0 & HF_PENDING) {
-                                a.hB[slot] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
-                                a.fB[slot] = 0;
+                                a.hB[e] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+                                a.fB[e] = 0;
                             }
                         }
                         continue;
                     }
                 }
+                const uint32_t slot = owner ? e : a.nslot[e];
+                const PairParam& P = a.params[pi];
                 const double4_32a gg = a.geom[pi];
                 const d3 Pj = ld(a.xA, j);
                 const d3 Ps = i_slave ? Pi : Pj, Pm = i_slave ? Pj : Pi;
@@ -723,6 +728,44 @@ __global__ void __launch_bounds__(TPB) k_slots(uint32_t n, const uint32_t* __res
     }
 }
 
+// Per-entry facts for the tick (META_*): orientation by the Assembler's rule
+// (Assembler.cpp:43-67: the density-0 object is the master, else the lower index is the
+// slave; a wall is always the master), the oriented pair's parameter index, its contact
+// detector, whether its law may bond (then the FP32 prefilter may not skip it), and
+// whether the entry holds the pair's history.
+__global__ void __launch_bounds__(TPB) k_meta(uint32_t n, const uint32_t* __restrict__ ptr,
+                                              const uint32_t* __restrict__ ent, const uint32_t* __restrict__ slot,
+                                              const uint32_t* __restrict__ model_of,
+                                              const ModelDev* __restrict__ models,
+                                              const uint32_t* __restrict__ scene_of,
+                                              const SceneDev* __restrict__ scenes,
+                                              const PairParam* __restrict__ params, uint32_t* __restrict__ meta) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const uint32_t mi = model_of[i];
+    const ModelDev& M = models[mi];
+    const SceneDev& S = scenes[scene_of[i]];
+    for (uint32_t e = ptr[i]; e < ptr[i + 1]; ++e) {
+        const uint32_t v = ent[e];
+        const uint32_t j = v & ~WALL_BIT;
+        const uint32_t mj = model_of[j];
+        bool i_slave;
+        if (v & WALL_BIT) {
+            i_slave = true;
+        } else {
+            const ModelDev& N = models[mj];
+            if (M.density == 0.0 && N.density != 0.0) i_slave = false;
+            else if (N.density == 0.0 && M.density != 0.0) i_slave = true;
+            else i_slave = i < j;
+        }
+        const uint32_t pi = pidx(S, i_slave ? mi : mj, i_slave ? mj : mi);
+        const PairParam& P = params[pi];
+        const bool bond = (P.is == IS_BSDBF || P.is == IS_BTSDBF || P.is == IS_BSDB2F) && P.c[4] != 0.0;
+        meta[e] = (pi & META_PI) | ((uint32_t)(P.cd & 3) << META_CD_SHIFT) | (bond ? META_BOND : 0u) |
+                  (slot[e] == e ? META_OWNER : 0u) | (i_slave ? META_SLAVE : 0u);
+    }
+}
+
 // New owner entries take the status of the same pair in the old list (if it was listed).
 __global__ void __launch_bounds__(TPB) k_carry(uint32_t n, const uint32_t* __restrict__ ptr,
                                                const uint32_t* __restrict__ ent, const uint32_t* __restrict__ slot,
@@ -753,6 +796,8 @@ __global__ void __launch_bounds__(TPB) k_carry(uint32_t n, const uint32_t* __res
         f2[e] = fv;
     }
 }
+
+
 
 // Wall entries of every sphere, in ascending entry order, keyed by the wall's global index.
 __global__ void __launch_bounds__(TPB) k_wall_count(uint32_t n, const uint32_t* __restrict__ ptr,
@@ -788,43 +833,69 @@ __global__ void __launch_bounds__(TPB) k_wall_ptr(uint32_t nglob, const uint32_t
     }
     wptr[q] = lo;
 }
-// One warp per wall: its contact impulses in entry order (ordered shuffle sum, FP64), plus the
-// field and external impulses, as DOStatus::GetImpact holds them after ClearImpact.
-__global__ void k_wall_sum(uint32_t nglob, const uint32_t* __restrict__ glob, const uint32_t* __restrict__ wptr,
-                           const uint32_t* __restrict__ wval, const float* __restrict__ wimp,
-                           const uint32_t* __restrict__ model_of, const ModelDev* __restrict__ models,
-                           const SceneDev* __restrict__ scenes, const uint32_t* __restrict__ scene_of,
-                           const double* __restrict__ gfield, double4_32a* __restrict__ imp,
-                           double4_32a* __restrict__ aimp) {
-    const uint32_t q = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    const int lane = threadIdx.x & 31;
+
+// Impulse on each wall, summed exactly: the six components of every wall entry are scaled by a
+// power of two fixed by the wall's largest entry (|x| 2^s <= 2^42) and added as 64-bit integers.
+// Integer addition is associative, so the sum is the same in any order and in parallel, and
+// entries that carry zero (spheres near the wall but not touching it) change nothing: the
+// result does not depend on the skin, on the list's rebuilds or on the scene's place in a
+// batch.  Relative resolution 2^-42 of the largest term, far below the FP32 inputs' rounding.
+__device__ __forceinline__ int wall_scale(unsigned maxbits) {
+    const float m = __uint_as_float(maxbits);
+    return m > 0.0f ? 42 - ilogbf(m) : 0;
+}
+
+__global__ void __launch_bounds__(TPB) k_wall_max(uint32_t nw, const uint32_t* __restrict__ wkey,
+                                                  const uint32_t* __restrict__ wval, const float* __restrict__ wimp,
+                                                  unsigned* __restrict__ wmax) {
+    const uint32_t e = blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= nw) return;
+    const float* o = wimp + 6 * (size_t)wval[e];
+    const float a = fmaxf(fmaxf(fabsf(o[0]), fabsf(o[1])), fabsf(o[2]));
+    const float b = fmaxf(fmaxf(fabsf(o[3]), fabsf(o[4])), fabsf(o[5]));
+    if (a > 0.0f) atomicMax(wmax + 2 * wkey[e], __float_as_uint(a));
+    if (b > 0.0f) atomicMax(wmax + 2 * wkey[e] + 1, __float_as_uint(b));
+}
+
+__global__ void __launch_bounds__(TPB) k_wall_acc(uint32_t nw, const uint32_t* __restrict__ wkey,
+                                                  const uint32_t* __restrict__ wval, const float* __restrict__ wimp,
+                                                  const unsigned* __restrict__ wmax,
+                                                  unsigned long long* __restrict__ wacc) {
+    const uint32_t e = blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= nw) return;
+    const uint32_t q = wkey[e];
+    const float* o = wimp + 6 * (size_t)wval[e];
+    const int s0 = wall_scale(wmax[2 * q]), s1 = wall_scale(wmax[2 * q + 1]);
+    for (int k = 0; k < 6; ++k) {
+        const float x = o[k];
+        if (x == 0.0f) continue;
+        const long long v = __double2ll_rn(ldexp((double)x, k < 3 ? s0 : s1));
+        atomicAdd(wacc + 6 * (size_t)q + k, (unsigned long long)v);
+    }
+}
+
+__global__ void k_wall_fin(uint32_t nglob, const uint32_t* __restrict__ glob, const unsigned* __restrict__ wmax,
+                           const unsigned long long* __restrict__ wacc, const uint32_t* __restrict__ model_of,
+                           const ModelDev* __restrict__ models, const SceneDev* __restrict__ scenes,
+                           const uint32_t* __restrict__ scene_of, const double* __restrict__ gfield,
+                           double4_32a* __restrict__ imp, double4_32a* __restrict__ aimp) {
+    const uint32_t q = blockIdx.x * blockDim.x + threadIdx.x;
     if (q >= nglob) return;
-    d3 J = mk(0.0, 0.0, 0.0), JA = mk(0.0, 0.0, 0.0);
-    for (uint32_t b = wptr[q]; b < wptr[q + 1]; b += 32) {
-        float v[6] = {0, 0, 0, 0, 0, 0};
-        if (b + lane < wptr[q + 1]) {
-            const float* o = wimp + 6 * (size_t)wval[b + lane];
-            for (int k = 0; k < 6; ++k) v[k] = o[k];
-        }
-        const uint32_t c = min(32u, wptr[q + 1] - b);
-        for (uint32_t l = 0; l < c; ++l) {
-            float x[6];
-            for (int k = 0; k < 6; ++k) x[k] = __shfl_sync(0xffffffffu, v[k], l);
-            J = add(J, mk(x[0], x[1], x[2]));
-            JA = add(JA, mk(x[3], x[4], x[5]));
-        }
-    }
-    if (lane == 0) {
-        const uint32_t w = glob[q];
-        const ModelDev& M = models[model_of[w]];
-        const uint32_t sc = scene_of[w];
-        const double dt = scenes[sc].dt;
-        const d3 fimp = muls(mk(gfield[3 * sc], gfield[3 * sc + 1], gfield[3 * sc + 2]), dt);
-        J = add(J, muls(fimp, M.sudo));
-        J = add(J, smul(dt, mk(M.ext[0], M.ext[1], M.ext[2])));
-        st(imp, w, J, 0.0);
-        st(aimp, w, JA, 0.0);
-    }
+    const int s0 = wall_scale(wmax[2 * q]), s1 = wall_scale(wmax[2 * q + 1]);
+    const unsigned long long* a = wacc + 6 * (size_t)q;
+    d3 J = mk(ldexp((double)(long long)a[0], -s0), ldexp((double)(long long)a[1], -s0),
+              ldexp((double)(long long)a[2], -s0));
+    const d3 JA = mk(ldexp((double)(long long)a[3], -s1), ldexp((double)(long long)a[4], -s1),
+                     ldexp((double)(long long)a[5], -s1));
+    const uint32_t w = glob[q];
+    const ModelDev& M = models[model_of[w]];
+    const uint32_t sc = scene_of[w];
+    const double dt = scenes[sc].dt;
+    const d3 fimp = muls(mk(gfield[3 * sc], gfield[3 * sc + 1], gfield[3 * sc + 2]), dt);
+    J = add(J, muls(fimp, M.sudo));
+    J = add(J, smul(dt, mk(M.ext[0], M.ext[1], M.ext[2])));
+    st(imp, w, J, 0.0);
+    st(aimp, w, JA, 0.0);
 }
 
 // Contact activity of every owner entry at the current positions (for queries).
@@ -1087,6 +1158,7 @@ private:
         uint32_t* ptr = nullptr;   // [n+1]
         uint32_t* ent = nullptr;
         uint32_t* slot = nullptr;
+        uint32_t* meta = nullptr;
         float4* h[2] = {nullptr, nullptr};
         uint8_t* f[2] = {nullptr, nullptr};
     };
@@ -1178,6 +1250,7 @@ private:
     uint32_t *d_wkey_ = nullptr, *d_wval_ = nullptr, *d_wkey_alt_ = nullptr, *d_wval_alt_ = nullptr, *d_wptr_ = nullptr;
     uint32_t wcap_ = 0, nwall_ent_ = 0;
     float* d_wimp_ = nullptr;
+    unsigned long long* d_wred_ = nullptr;   // per wall: 6 integer sums, then 2 maxima (as 32-bit)
     uint32_t wimp_cap_ = 0;
     double* d_stage_ = nullptr;
     double* d_obs_ = nullptr;
@@ -1196,7 +1269,7 @@ static cudaError_t mal(T** p, size_t count) {
 }
 
 void MixedEngine::free_nlist(NList& L) {
-    cudaFree(L.ptr); cudaFree(L.ent); cudaFree(L.slot);
+    cudaFree(L.ptr); cudaFree(L.ent); cudaFree(L.slot); cudaFree(L.meta);
     for (int b = 0; b < 2; ++b) { cudaFree(L.h[b]); cudaFree(L.f[b]); }
     L = NList{};
 }
@@ -1212,6 +1285,7 @@ int MixedEngine::ensure_nlist(NList& L, uint32_t cap) {
     L.cap = (uint32_t)std::min<uint64_t>(c, 0x7fffffffull);
     MCK(mal(&L.ent, L.cap));
     MCK(mal(&L.slot, L.cap));
+    MCK(mal(&L.meta, L.cap));
     for (int b = 0; b < 2; ++b) {
         MCK(mal(&L.h[b], L.cap));
         MCK(mal(&L.f[b], L.cap));
@@ -1227,7 +1301,7 @@ MixedEngine::~MixedEngine() {
                     d_scenes_, d_gfield_, d_glob_, d_x_[0], d_x_[1], d_v64_, d_w64_, d_ox_, d_oz_, d_imp_, d_aimp_,
                     d_v32_[0], d_v32_[1], d_w32_[0], d_w32_[1], d_pos32_, d_wall32_, d_red_, d_sred_, d_disp_, d_err_,
                     d_key_, d_key_alt_, d_sid_, d_sid_alt_, d_cnt_, d_gs_, d_ge_, d_act_, d_stage_, d_obs_, d_gidx_,
-                    d_wkey_, d_wval_, d_wkey_alt_, d_wval_alt_, d_wptr_, d_wimp_};
+                    d_wkey_, d_wval_, d_wkey_alt_, d_wval_alt_, d_wptr_, d_wimp_, d_wred_};
     for (void* p : ptrs) if (p) cudaFree(p);
     drop_graphs();
     for (auto& e : pev_) cudaEventDestroy(e);
@@ -1379,6 +1453,7 @@ int MixedEngine::init_from(const std::vector<SceneSource>& src, const MixedEngin
         sc_.push_back(S);
     }
     law_ = law < 0 ? 0 : law;
+    if (np_ > META_PI) return fail(VEDO_ERR_INVALID_SCENE, "too many interaction-model pairs in one batch (2^24)");
     // ---- device
     MCK(cudaSetDevice(opts.device));
     MCK(cudaStreamCreateWithFlags(&stream_, cudaStreamNonBlocking));
@@ -1399,6 +1474,7 @@ int MixedEngine::init_from(const std::vector<SceneSource>& src, const MixedEngin
         for (uint32_t q = 0; q < glob_.size(); ++q) gidx[glob_[q]] = q;
         if ((rc = up(&d_gidx_, gidx))) return rc;
         MCK(mal(&d_wptr_, glob_.size() + 1));
+        MCK(mal(&d_wred_, 7 * glob_.size()));
     }
     sdev_.resize(sc_.size());
     MCK(mal(&d_scenes_, sc_.size()));
@@ -1554,6 +1630,7 @@ TickArgs MixedEngine::args(bool write_imp) {
     a.nptr = L.ptr;
     a.nent = L.ent;
     a.nslot = L.slot;
+    a.nmeta = L.meta;
     a.hA = L.h[cur_];
     a.hB = L.h[cur_ ^ 1];
     a.fA = L.f[cur_];
@@ -1682,6 +1759,9 @@ int MixedEngine::rebuild() {
     }
     MCK(cudaMemsetAsync(d_err_, 0, 4, stream_));
     k_slots<<<nblk(n_), TPB, 0, stream_>>>(n_, L.ptr, L.ent, L.slot, d_err_);
+    k_meta<<<nblk(n_), TPB, 0, stream_>>>(n_, L.ptr, L.ent, L.slot, d_model_of_, d_models_, d_scene_of_, d_scenes_,
+                                          d_params_, L.meta);
+    ++own;
     k_carry<<<nblk(n_), TPB, 0, stream_>>>(n_, L.ptr, L.ent, L.slot, O.ptr, O.ent, O.slot, O.h[cur_], O.f[cur_],
                                            L.h[cur_], L.f[cur_], L.h[cur_ ^ 1], L.f[cur_ ^ 1],
                                            O.ent != nullptr ? 1 : 0);
@@ -1764,9 +1844,16 @@ void MixedEngine::launch_step(bool write_imp) {
     ++launches_;
     if (pe) cudaEventRecord(pe[1], stream_);
     if (write_imp && !glob_.empty()) {
-        k_wall_sum<<<nblk((uint64_t)glob_.size() * 32), TPB, 0, stream_>>>(
-            (uint32_t)glob_.size(), d_glob_, d_wptr_, d_wval_, d_wimp_, d_model_of_, d_models_, d_scenes_, d_scene_of_,
-            d_gfield_, d_imp_, d_aimp_);
+        const uint32_t ng = (uint32_t)glob_.size();
+        cudaMemsetAsync(d_wred_, 0, (size_t)ng * (8 + 48), stream_);
+        unsigned* wmax = reinterpret_cast<unsigned*>(d_wred_ + 6 * (size_t)ng);
+        if (nwall_ent_) {
+            k_wall_max<<<nblk(nwall_ent_), TPB, 0, stream_>>>(nwall_ent_, d_wkey_, d_wval_, d_wimp_, wmax);
+            k_wall_acc<<<nblk(nwall_ent_), TPB, 0, stream_>>>(nwall_ent_, d_wkey_, d_wval_, d_wimp_, wmax, d_wred_);
+            launches_ += 2;
+        }
+        k_wall_fin<<<nblk(ng), TPB, 0, stream_>>>(ng, d_glob_, wmax, d_wred_, d_model_of_, d_models_, d_scenes_,
+                                                  d_scene_of_, d_gfield_, d_imp_, d_aimp_);
         ++launches_;
     }
     k_walls<<<nblk(std::max<size_t>(glob_.size(), 1)), TPB, 0, stream_>>>(
