@@ -63,6 +63,7 @@ constexpr int META_CD_SHIFT = 24;
 constexpr uint32_t META_BOND = 1u << 26;
 constexpr uint32_t META_OWNER = 1u << 27;
 constexpr uint32_t META_SLAVE = 1u << 28;
+constexpr int TICK_GROUP = 4;    // list entries the tick loads and prefilters together
 constexpr uint8_t PF_ACTIVE_BIT = 64;
 // history flag bit: the status just became clean and the other buffer still holds the old one
 constexpr uint8_t HF_PENDING = 16;
@@ -340,13 +341,67 @@ __global__ void __launch_bounds__(TPB) k_tick(TickArgs a) {
             const float dtf = (float)dt;
             const float disp = *a.disp;
             const float4 p32i = a.pos32[i];
+            const float pad = 2.0f * disp;
             K3 J, JA;
             const uint32_t e1 = a.nptr[i + 1];
-            for (uint32_t e = a.nptr[i]; e < e1; ++e) {
-                const uint32_t ent = a.nent[e];
+            for (uint32_t base = a.nptr[i]; base < e1; base += TICK_GROUP) {
+                // Phase 1: the group's entries and neighbour positions are loaded together (the
+                // loads overlap) and the FP32 prefilter settles the pairs that are certainly
+                // apart: rebuild-time distance minus both spheres' travel since then.  The rest
+                // are flagged for the exact path.
+                uint32_t ge[TICK_GROUP], gm[TICK_GROUP];
+                float4 gp[TICK_GROUP];
+#pragma unroll
+                for (int k = 0; k < TICK_GROUP; ++k) {
+                    const bool ok = base + k < e1;
+                    ge[k] = ok ? a.nent[base + k] : 0u;
+                    gm[k] = ok ? a.nmeta[base + k] : 0u;     // cd 0: nothing to do
+                }
+#pragma unroll
+                for (int k = 0; k < TICK_GROUP; ++k)
+                    gp[k] = (gm[k] >> META_CD_SHIFT) & 3u ? a.pos32[ge[k] & ~WALL_BIT] : p32i;
+                uint32_t exact = 0;
+#pragma unroll
+                for (int k = 0; k < TICK_GROUP; ++k) {
+                    const uint32_t meta = gm[k];
+                    const int cd = (int)((meta >> META_CD_SHIFT) & 3u);
+                    if (cd == 0) continue;
+                    const uint32_t e = base + k;
+                    const uint32_t j = ge[k] & ~WALL_BIT;
+                    const bool wall = ge[k] & WALL_BIT;
+                    const bool i_slave = meta & META_SLAVE;
+                    if (meta & META_BOND) {
+                        exact |= 1u << k;
+                        continue;
+                    }
+                    const float4 ws = wall ? a.wall32[j] : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+                    if (!certainly_apart(cd, i_slave ? p32i : gp[k], i_slave ? gp[k] : p32i, ws,
+                                         a.reach[meta & META_PI] + pad)) {
+                        exact |= 1u << k;
+                        continue;
+                    }
+                    if (wall && a.write_imp) {
+                        float* o = a.wimp + 6 * (size_t)e;
+                        o[0] = o[1] = o[2] = o[3] = o[4] = o[5] = 0.0f;
+                    }
+                    if (meta & META_OWNER) {
+                        const uint8_t f0 = a.fA[e];
+                        if (f0 & 15) {                     // ImpactStatus::Clean
+                            a.hB[e] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+                            a.fB[e] = HF_PENDING;
+                        } else if (f0 & HF_PENDING) {
+                            a.hB[e] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+                            a.fB[e] = 0;
+                        }
+                    }
+                }
+                // Phase 2: the exact path for the flagged entries, in entry order
+                while (exact) {
+                const int k = __ffs(exact) - 1;
+                exact &= exact - 1;
+                const uint32_t e = base + k;
+                const uint32_t ent = a.nent[e];            // (reloaded: a register array indexed by k would spill)
                 const uint32_t meta = a.nmeta[e];
-                const int cd = (int)((meta >> META_CD_SHIFT) & 3u);
-                if (cd == 0) continue;
                 const uint32_t j = ent & ~WALL_BIT;
                 const bool wall = ent & WALL_BIT;
                 // canonical orientation (Assembler.cpp:43-67), fixed at rebuild; sphere-wall: the sphere is the slave
@@ -354,29 +409,6 @@ __global__ void __launch_bounds__(TPB) k_tick(TickArgs a) {
                 const bool owner = meta & META_OWNER;
                 const uint32_t s = i_slave ? i : j, m = i_slave ? j : i;
                 const uint32_t pi = meta & META_PI;
-                if (!(meta & META_BOND)) {
-                    // certainly apart: rebuild-time distance minus both spheres' travel since then
-                    const float4 ws = wall ? a.wall32[j] : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
-                    const float4 p32j = a.pos32[j];
-                    if (certainly_apart(cd, i_slave ? p32i : p32j, i_slave ? p32j : p32i, ws,
-                                        a.reach[pi] + 2.0f * disp)) {
-                        if (wall && a.write_imp) {
-                            float* o = a.wimp + 6 * (size_t)e;
-                            o[0] = o[1] = o[2] = o[3] = o[4] = o[5] = 0.0f;
-                        }
-                        if (owner) {
-                            const uint8_t f0 = a.fA[e];
-                            if (f0 & 15) {                 // ImpactStatus::Clean
-                                a.hB[e] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
-                                a.fB[e] = HF_PENDING;
-                            } else if (f0 & HF_PENDING) {
-                                a.hB[e] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
-                                a.fB[e] = 0;
-                            }
-                        }
-                        continue;
-                    }
-                }
                 const uint32_t slot = owner ? e : a.nslot[e];
                 const PairParam& P = a.params[pi];
                 const double4_32a gg = a.geom[pi];
@@ -445,6 +477,7 @@ __global__ void __launch_bounds__(TPB) k_tick(TickArgs a) {
                     float* o = a.wimp + 6 * (size_t)e;
                     o[0] = app ? -Jp.x : 0.0f; o[1] = app ? -Jp.y : 0.0f; o[2] = app ? -Jp.z : 0.0f;
                     o[3] = app == 2 ? tB.x : 0.0f; o[4] = app == 2 ? tB.y : 0.0f; o[5] = app == 2 ? tB.z : 0.0f;
+                }
                 }
             }
             // field and external impulse (DOContainer.cpp:20-27, DiscreteObject.cpp:160-163) join the
