@@ -157,6 +157,24 @@ struct K3 {
     }
 };
 
+// The tick's prefilter: certainly_apart (prefilter.cuh) with the positions' rounding bounds
+// precomputed in pos32.w and, for spheres and rods, squared distances (no square root): the
+// squared test carries the same error allowance as the distance test, so it is as conservative.
+__device__ __forceinline__ bool apart32(int cd, const float4& s, const float4& m, const float4& wall, float reach) {
+    const float dx = m.x - s.x, dy = m.y - s.y, dz = m.z - s.z;
+    const float lim = reach * (1.0f + 4.0f * PF_ARITH_EPS) + s.w + m.w;
+    if (cd == CD_SS) {
+        const float d2 = fmaf(dz, dz, fmaf(dy, dy, dx * dx));
+        return d2 > lim * lim * (1.0f + 4.0f * PF_ARITH_EPS);
+    }
+    if (wall.w == 0.0f) return false;
+    const float lim2 = lim + PF_ARITH_EPS * (fabsf(dx) + fabsf(dy) + fabsf(dz));
+    if (cd == CD_SP) return fabsf(fmaf(dz, wall.z, fmaf(dy, wall.y, dx * wall.x))) > lim2;
+    const float cx = fmaf(dy, wall.z, -dz * wall.y), cy = fmaf(dz, wall.x, -dx * wall.z),
+                cz = fmaf(dx, wall.y, -dy * wall.x);
+    return fmaf(cz, cz, fmaf(cy, cy, cx * cx)) > lim2 * lim2 * (1.0f + 4.0f * PF_ARITH_EPS);
+}
+
 // ---- the five laws in FP32 (same control flow as the reference's NextStep) -------------
 enum : uint8_t { HF_CONTACT = 1, HF_LAST_CONTACT = 2, HF_BOND = 4, HF_LAST_BOND = 8 };
 
@@ -332,30 +350,40 @@ __global__ void __launch_bounds__(TPB) k_tick(TickArgs a) {
     }
     float vmax_local = 0.0f;
     if (i < a.n) {
+        // every load that depends on the index alone is issued here, together, so that their
+        // latencies overlap; the model- and list-dependent ones follow
         const uint32_t mi = a.model_of[i];
+        const uint32_t si = a.scene_of[i];
+        const uint32_t e0 = a.nptr[i], e1 = a.nptr[i + 1];
+        const d3 Pi = ld(a.xA, i);
+        const d3 V = ld(a.v64, i);
+        const float4 p32i = a.pos32[i];
+        const float4 vo = a.v32A[i];
+        const float4 wo = a.w32A[i];
+        const float disp = *a.disp;
         const ModelDev& M = a.models[mi];
-        const SceneDev& S = a.scenes[a.scene_of[i]];
+        const SceneDev& S = a.scenes[si];
         if (M.scope == SCOPE_LOCAL && S.active) {
             const double dt = S.dt;
-            const d3 Pi = ld(a.xA, i);
             const float dtf = (float)dt;
-            const float disp = *a.disp;
-            const float4 p32i = a.pos32[i];
             const float pad = 2.0f * disp;
+            const float4 mf0 = a.mf[2 * mi], mf1 = a.mf[2 * mi + 1];
+            const bool mobile = M.behavior == BEH_MOBILE;
             K3 J, JA;
-            const uint32_t e1 = a.nptr[i + 1];
-            for (uint32_t base = a.nptr[i]; base < e1; base += TICK_GROUP) {
+            for (uint32_t base = e0; base < e1; base += TICK_GROUP) {
                 // Phase 1: the group's entries and neighbour positions are loaded together (the
                 // loads overlap) and the FP32 prefilter settles the pairs that are certainly
                 // apart: rebuild-time distance minus both spheres' travel since then.  The rest
                 // are flagged for the exact path.
                 uint32_t ge[TICK_GROUP], gm[TICK_GROUP];
+                uint8_t gf[TICK_GROUP];
                 float4 gp[TICK_GROUP];
 #pragma unroll
                 for (int k = 0; k < TICK_GROUP; ++k) {
                     const bool ok = base + k < e1;
                     ge[k] = ok ? a.nent[base + k] : 0u;
                     gm[k] = ok ? a.nmeta[base + k] : 0u;     // cd 0: nothing to do
+                    gf[k] = ok ? a.fA[base + k] : (uint8_t)0;
                 }
 #pragma unroll
                 for (int k = 0; k < TICK_GROUP; ++k)
@@ -375,8 +403,8 @@ __global__ void __launch_bounds__(TPB) k_tick(TickArgs a) {
                         continue;
                     }
                     const float4 ws = wall ? a.wall32[j] : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
-                    if (!certainly_apart(cd, i_slave ? p32i : gp[k], i_slave ? gp[k] : p32i, ws,
-                                         a.reach[meta & META_PI] + pad)) {
+                    if (!apart32(cd, i_slave ? p32i : gp[k], i_slave ? gp[k] : p32i, ws,
+                                 a.reach[meta & META_PI] + pad)) {
                         exact |= 1u << k;
                         continue;
                     }
@@ -385,7 +413,7 @@ __global__ void __launch_bounds__(TPB) k_tick(TickArgs a) {
                         o[0] = o[1] = o[2] = o[3] = o[4] = o[5] = 0.0f;
                     }
                     if (meta & META_OWNER) {
-                        const uint8_t f0 = a.fA[e];
+                        const uint8_t f0 = gf[k];
                         if (f0 & 15) {                     // ImpactStatus::Clean
                             a.hB[e] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
                             a.fB[e] = HF_PENDING;
@@ -482,35 +510,36 @@ __global__ void __launch_bounds__(TPB) k_tick(TickArgs a) {
             }
             // field and external impulse (DOContainer.cpp:20-27, DiscreteObject.cpp:160-163) join the
             // compensated sum; the increments dv, dw are FP32, the state update FP64
-            const float4 mf0 = a.mf[2 * mi], mf1 = a.mf[2 * mi + 1];
             J.add(fm(mf0.x, mf0.y, mf0.z));
             if (a.write_imp) {
                 st(a.imp, i, J.value(), 0.0);
                 st(a.aimp, i, JA.value(), 0.0);
             }
-            if (M.behavior == BEH_MOBILE) {
+            if (mobile) {
                 const f3 Jf = fm(J.s.x - J.c.x, J.s.y - J.c.y, J.s.z - J.c.z);
                 const f3 JAf = fm(JA.s.x - JA.c.x, JA.s.y - JA.c.y, JA.s.z - JA.c.z);
                 const f3 dv = mf0.w * Jf, dw = mf1.x * JAf;
-                const d3 V = ld(a.v64, i), W = ld(a.w64, i);
                 const d3 dvd = mk((double)dv.x, (double)dv.y, (double)dv.z);
                 const d3 P2 = mk(fma(dt, fma(0.5, dvd.x, V.x), Pi.x), fma(dt, fma(0.5, dvd.y, V.y), Pi.y),
                                  fma(dt, fma(0.5, dvd.z, V.z), Pi.z));
                 const d3 V2 = add(V, dvd);
-                const d3 W2 = add(W, mk((double)dw.x, (double)dw.y, (double)dw.z));
                 st(a.xB, i, P2, 0.0);
                 st(a.v64, i, V2, 0.0);
-                st(a.w64, i, W2, 0.0);
-                const float4 vo = a.v32A[i];
+                if (dw.x != 0.0f || dw.y != 0.0f || dw.z != 0.0f) {
+                    const d3 W2 = add(ld(a.w64, i), mk((double)dw.x, (double)dw.y, (double)dw.z));
+                    st(a.w64, i, W2, 0.0);
+                    a.w32B[i] = make_float4((float)W2.x, (float)W2.y, (float)W2.z, 0.0f);
+                } else {                                   // no torque: omega + 0 is omega
+                    a.w32B[i] = wo;
+                }
                 const float4 vn = make_float4((float)V2.x, (float)V2.y, (float)V2.z, 0.0f);
                 a.v32B[i] = vn;
-                a.w32B[i] = make_float4((float)W2.x, (float)W2.y, (float)W2.z, 0.0f);
-                vmax_local = fmaxf(sqrtf(vo.x * vo.x + vo.y * vo.y + vo.z * vo.z),
-                                   sqrtf(vn.x * vn.x + vn.y * vn.y + vn.z * vn.z));
+                vmax_local = sqrtf(fmaxf(fmaf(vo.z, vo.z, fmaf(vo.y, vo.y, vo.x * vo.x)),
+                                         fmaf(vn.z, vn.z, fmaf(vn.y, vn.y, vn.x * vn.x))));
             } else {
                 st(a.xB, i, Pi, 0.0);
-                a.v32B[i] = a.v32A[i];
-                a.w32B[i] = a.w32A[i];
+                a.v32B[i] = vo;
+                a.w32B[i] = wo;
             }
         } else if (M.scope == SCOPE_LOCAL) {
             hold_state(a, i);                      // a finished scene waits, unchanged
@@ -588,7 +617,8 @@ __global__ void __launch_bounds__(TPB) k_bounds(uint32_t n, const uint32_t* __re
     if (i < n) {
         const ModelDev& M = models[model_of[i]];
         const d3 p = ld(x, i);
-        const float4 q = make_float4((float)(p.x - origin.x), (float)(p.y - origin.y), (float)(p.z - origin.z), 0.0f);
+        float4 q = make_float4((float)(p.x - origin.x), (float)(p.y - origin.y), (float)(p.z - origin.z), 0.0f);
+        q.w = PF_POS_EPS * (fabsf(q.x) + fabsf(q.y) + fabsf(q.z));   // bound on this copy's rounding
         pos32[i] = q;
         if (M.scope == SCOPE_LOCAL) {
             auto ordf = [](float f) {

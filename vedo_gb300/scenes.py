@@ -20,6 +20,10 @@ code, the C oracle and the GPU engine.
   orifice), monodisperse r = 1 mm Hertz spheres with friction (``ISwH``); the batch
   draws sphere counts log-uniform on [1e3, 5e4], friction U(0.2, 0.6), restitution
   U(0.5, 0.9) and orifice width U(6, 12) mm per scene.
+* :func:`compressed_bed` - a large monodisperse Hertz bed (16,000,000 spheres of
+  r = 0.5 mm by default, E = 10 GPa, friction 0.5) at solid fraction 0.55 in a
+  0.4 x 0.4 m box of plates with 32 fixed vertical cylinders (r = 5 mm) on a jittered
+  grid, compressed by an orbital top plate moving down at 0.05 m/s.
 * :func:`serving_job` - the serving stream's jobs: a settling box or a projectile
   impact on a bed, lognormal radii (median 1 mm, sigma_log 0.15) in 8 classes, linear
   spring-dashpot or Hertz (``ISwH``, E = 0.5 GPa) contact.
@@ -493,4 +497,78 @@ def serving_job(kind: str, n: int, model: str, seed: int, steps: int = 1000, K: 
         for gb in groups:
             iacts.append(IactModel("Wall", gb, "ISwH", _hertz_mech("ISwH", 0.5e9, 0.3, radius_of[gb], None, m_of,
                                                                     zeta, 0.4)))
+    return Scene(time_control(steps, dt), models, iacts, midx, P, V, OX, OZ, AV)
+
+
+def compressed_bed(n: int = 16_000_000, seed: int = 5, steps: int = 2000, dt: float = 2e-7, radius: float = 5e-4,
+                   box: float = 0.4, E: float = 10e9, nu: float = 0.25, restitution: float = 0.7,
+                   friction: float = 0.5, density: float = 2500.0, solid_fraction: float = 0.55,
+                   cylinders: int = 32, cyl_radius: float = 5e-3, plate_speed: float = 0.05) -> Scene:
+    """A bed of n spheres at `solid_fraction` (a jittered face-centred cubic lattice: at 0.55
+    the nearest-neighbour gap is 0.2 r, so nothing overlaps) filling a `box` x `box` floor to the
+    height that holds n, with `cylinders` fixed vertical rods on a jittered grid (spheres that
+    would overlap a rod are not placed) and an orbital top plate just above the bed moving at
+    (0, 0, -plate_speed).  Walls: floor and four sides (fixed plates).  Contact ``ISwH`` (Hertz
+    normal stiffness with friction) for sphere-sphere, sphere-plate and sphere-rod."""
+    rng = np.random.default_rng(seed)
+    vs = 4.0 / 3.0 * math.pi * radius ** 3
+    a = (4.0 * vs / solid_fraction) ** (1.0 / 3.0)          # FCC cell edge (4 spheres per cell)
+    c = 1.1 * radius                                       # centre-to-wall distance of the outermost spheres
+    m = int((box - 2.0 * c) / a + 0.5)                     # cells across the box
+    inner = (m - 0.5) * a + 2.0 * c                        # lattice points span (m - 1/2) a
+    # rods on a jittered grid
+    g = int(math.ceil(math.sqrt(cylinders)))
+    rods = []
+    for k in range(cylinders):
+        gx, gy = k % g, k // g
+        cx = (gx + 0.5) / g * inner - 0.5 * inner + rng.uniform(-0.2, 0.2) * inner / g
+        cy = (gy + 0.5) / g * inner - 0.5 * inner + rng.uniform(-0.2, 0.2) * inner / g
+        rods.append((cx, cy))
+    rods = np.array(rods)
+    basis = np.array([[0.25, 0.25, 0.25], [0.75, 0.75, 0.25], [0.75, 0.25, 0.75], [0.25, 0.75, 0.75]]) * a
+    layer = np.stack(np.meshgrid(np.arange(m), np.arange(m), indexing="ij"), -1).reshape(-1, 2) * a
+    per_cell_layer = (layer[:, None, :] + basis[None, :, :2]).reshape(-1, 2) - 0.25 * a + c - 0.5 * inner
+    zoff = np.tile(basis[:, 2], len(layer)) - 0.25 * a + c
+    keep = np.ones(len(per_cell_layer), bool)
+    for cx, cy in rods:
+        d2 = (per_cell_layer[:, 0] - cx) ** 2 + (per_cell_layer[:, 1] - cy) ** 2
+        keep &= d2 > (cyl_radius + radius * 1.2) ** 2
+    xy = per_cell_layer[keep]
+    zo = zoff[keep]
+    per_layer = len(xy)
+    nl = int(math.ceil(n / per_layer))
+    pos = np.empty((nl * per_layer, 3))
+    for L in range(nl):
+        pos[L * per_layer:(L + 1) * per_layer, :2] = xy
+        pos[L * per_layer:(L + 1) * per_layer, 2] = zo + L * a
+    pos = pos[:n]
+    pos += rng.uniform(-0.05 * radius, 0.05 * radius, size=pos.shape)
+    top = float(pos[:, 2].max()) + radius
+    height = top + 0.02
+    t = 2e-3
+    models = [DOModel("Ball", "Ball", MOBILE, LOCAL, density, 1.0, SPHERE, (radius,)),
+              DOModel("Floor", "Wall", FIXED, GLOBAL, 0.0, 1.0, QUASI_PLATE, (inner + 2 * t, t, inner + 2 * t)),
+              DOModel("Side", "Wall", FIXED, GLOBAL, 0.0, 1.0, QUASI_PLATE, (height, t, inner + 2 * t)),
+              DOModel("Rod", "Wall", FIXED, GLOBAL, 0.0, 1.0, QUASI_CYLINDER, (cyl_radius, height)),
+              DOModel("Top", "Wall", ORBITAL, GLOBAL, 0.0, 1.0, QUASI_PLATE, (inner, t, inner))]
+    wp, wox, woz, wv, widx = [(0.0, 0.0, -0.5 * t)], [(1.0, 0.0, 0.0)], [(0.0, 0.0, 1.0)], [(0.0, 0.0, 0.0)], [1]
+    for sx, sy in ((1, 0), (-1, 0), (0, 1), (0, -1)):
+        wp.append((sx * (0.5 * inner + 0.5 * t), sy * (0.5 * inner + 0.5 * t), 0.5 * height))
+        wox.append((0.0, 0.0, 1.0)); woz.append((-float(sx), -float(sy), 0.0)); wv.append((0.0, 0.0, 0.0)); widx.append(2)
+    for cx, cy in rods:
+        wp.append((cx, cy, 0.5 * height)); wox.append((1.0, 0.0, 0.0)); woz.append((0.0, 0.0, 1.0))
+        wv.append((0.0, 0.0, 0.0)); widx.append(3)
+    wp.append((0.0, 0.0, top + 1e-5 + 0.5 * t)); wox.append((1.0, 0.0, 0.0)); woz.append((0.0, 0.0, -1.0))
+    wv.append((0.0, 0.0, -plate_speed)); widx.append(4)
+    zeta = damping_ratio(restitution)
+    m_of = lambda rr: density * 4.0 / 3.0 * math.pi * rr ** 3
+    iacts = [IactModel("Ball", "Ball", "ISwH", _hertz_mech("ISwH", E, nu, radius, radius, m_of, zeta, friction)),
+             IactModel("Wall", "Ball", "ISwH", _hertz_mech("ISwH", E, nu, radius, None, m_of, zeta, friction))]
+    k = len(widx)
+    midx = np.concatenate([np.zeros(n, np.uint32), np.array(widx, np.uint32)])
+    P = np.concatenate([pos, np.array(wp)])
+    V = np.concatenate([np.zeros((n, 3)), np.array(wv)])
+    OX = np.concatenate([np.tile([1.0, 0, 0], (n, 1)), np.array(wox)])
+    OZ = np.concatenate([np.tile([0, 0, 1.0], (n, 1)), np.array(woz)])
+    AV = np.zeros((n + k, 3))
     return Scene(time_control(steps, dt), models, iacts, midx, P, V, OX, OZ, AV)
