@@ -550,6 +550,34 @@ __global__ void __launch_bounds__(TPB) k_tick(TickArgs a) {
     if ((threadIdx.x & 31) == 0 && vmax_local > 0.0f) atomicMax(a.vmax_bits, __float_as_uint(vmax_local * 1.0001f));
 }
 
+// Vector3d::rotate_around (Vector3d.h:152-178) split in two: the half-angle terms of the turn
+// omega dt (v = axis sin(a/2), s = cos(a/2)), fixed for an orbital wall (prescribed omega, fixed
+// dt), and the rotation of a vector with them, in rotate_around's operation order.
+__device__ __forceinline__ double4_32a turn_terms(d3 va) {
+    const d3 u = dir(va);
+    const double ang = len(va);
+    const double c = cos(0.5 * ang), sn = sin(0.5 * ang);
+    const d3 v = muls(u, sn);
+    return make_double4_32a(v.x, v.y, v.z, c);
+}
+__device__ __forceinline__ d3 rotate_quat(d3 p, const double4_32a& R) {
+    const d3 v = mk(R.x, R.y, R.z);
+    const double s = R.w;
+    d3 r = add(smul(s * s, p), smul(dot(p, v), v));
+    r = add(r, smul(2.0 * s, cross(v, p)));
+    return add(r, cross(v, cross(v, p)));
+}
+__global__ void k_wall_rot(uint32_t nglob, const uint32_t* __restrict__ glob, const uint32_t* __restrict__ model_of,
+                           const ModelDev* __restrict__ models, const SceneDev* __restrict__ scenes,
+                           const uint32_t* __restrict__ scene_of, const double4_32a* __restrict__ w64,
+                           double4_32a* __restrict__ wrot) {
+    const uint32_t q = blockIdx.x * blockDim.x + threadIdx.x;
+    if (q >= nglob) return;
+    const uint32_t w = glob[q];
+    wrot[q] = models[model_of[w]].behavior == BEH_ORBITAL ? turn_terms(muls(ld(w64, w), scenes[scene_of[w]].dt))
+                                                           : make_double4_32a(0.0, 0.0, 0.0, 1.0);
+}
+
 // Scope-global objects (walls): fixed ones keep their state, orbital ones move with their
 // prescribed V and omega (DOOrbitalQuasiPlate.cpp:18-34).  Thread 0 also writes the
 // displacement bound after the step into the other parity slot (disp_out), or, when the step
@@ -563,6 +591,7 @@ __global__ void k_walls(uint32_t nglob, const uint32_t* __restrict__ glob, const
                         double4_32a* __restrict__ ox, double4_32a* __restrict__ oz, float dt_max,
                         unsigned* __restrict__ vmax_bits, const float* __restrict__ disp_in,
                         float* __restrict__ disp_out, float half_skin, const unsigned* __restrict__ wall_speed_bits,
+                        const double4_32a* __restrict__ wrot,
                         unsigned* __restrict__ held, float4* __restrict__ wall32) {
     const uint32_t q = blockIdx.x * blockDim.x + threadIdx.x;
     const float disp = *disp_in;
@@ -588,10 +617,11 @@ __global__ void k_walls(uint32_t nglob, const uint32_t* __restrict__ glob, const
     const double dt = scenes[scene_of[w]].dt;
     d3 P = ld(xA, w);
     if (M.behavior == BEH_ORBITAL) {
-        const d3 V = ld(v64, w), AV = ld(w64, w);
+        const d3 V = ld(v64, w);
         P = add(P, muls(V, dt));
-        const d3 dw = muls(AV, dt);
-        const d3 Ox = rotate_around(ld(ox, w), dw), Oz = rotate_around(ld(oz, w), dw);
+        // rotate_around(O, omega dt) with its cos/sin terms computed once per list (k_wall_rot)
+        const double4_32a R = wrot[q];
+        const d3 Ox = rotate_quat(ld(ox, w), R), Oz = rotate_quat(ld(oz, w), R);
         st(ox, w, Ox, 0.0);
         st(oz, w, Oz, 0.0);
         const double lz = len(Oz), lx = len(Ox);
@@ -1313,7 +1343,8 @@ private:
     uint32_t *d_wkey_ = nullptr, *d_wval_ = nullptr, *d_wkey_alt_ = nullptr, *d_wval_alt_ = nullptr, *d_wptr_ = nullptr;
     uint32_t wcap_ = 0, nwall_ent_ = 0;
     float* d_wimp_ = nullptr;
-    unsigned long long* d_wred_ = nullptr;   // per wall: 6 integer sums, then 2 maxima (as 32-bit)
+    unsigned long long* d_wred_ = nullptr;
+    double4_32a* d_wrot_ = nullptr;          // per wall: half-angle terms of its turn per step   // per wall: 6 integer sums, then 2 maxima (as 32-bit)
     uint32_t wimp_cap_ = 0;
     double* d_stage_ = nullptr;
     double* d_obs_ = nullptr;
@@ -1364,7 +1395,7 @@ MixedEngine::~MixedEngine() {
                     d_scenes_, d_gfield_, d_glob_, d_x_[0], d_x_[1], d_v64_, d_w64_, d_ox_, d_oz_, d_imp_, d_aimp_,
                     d_v32_[0], d_v32_[1], d_w32_[0], d_w32_[1], d_pos32_, d_wall32_, d_red_, d_sred_, d_disp_, d_err_,
                     d_key_, d_key_alt_, d_sid_, d_sid_alt_, d_cnt_, d_gs_, d_ge_, d_act_, d_stage_, d_obs_, d_gidx_,
-                    d_wkey_, d_wval_, d_wkey_alt_, d_wval_alt_, d_wptr_, d_wimp_, d_wred_};
+                    d_wkey_, d_wval_, d_wkey_alt_, d_wval_alt_, d_wptr_, d_wimp_, d_wred_, d_wrot_};
     for (void* p : ptrs) if (p) cudaFree(p);
     drop_graphs();
     for (auto& e : pev_) cudaEventDestroy(e);
@@ -1538,6 +1569,7 @@ int MixedEngine::init_from(const std::vector<SceneSource>& src, const MixedEngin
         if ((rc = up(&d_gidx_, gidx))) return rc;
         MCK(mal(&d_wptr_, glob_.size() + 1));
         MCK(mal(&d_wred_, 7 * glob_.size()));
+        MCK(mal(&d_wrot_, glob_.size()));
     }
     sdev_.resize(sc_.size());
     MCK(mal(&d_scenes_, sc_.size()));
@@ -1867,6 +1899,9 @@ int MixedEngine::rebuild() {
     }
     MCK(cudaMemsetAsync(d_red_ + 11, 0, 8, stream_));
     if (!glob_.empty()) {
+        k_wall_rot<<<nblk(glob_.size()), TPB, 0, stream_>>>((uint32_t)glob_.size(), d_glob_, d_model_of_, d_models_,
+                                                           d_scenes_, d_scene_of_, d_w64_, d_wrot_);
+        ++own;
         k_wall_speed<<<nblk(glob_.size()), TPB, 0, stream_>>>((uint32_t)glob_.size(), d_glob_, d_model_of_, d_models_,
                                                              d_v64_, d_w64_, d_oz_, 2.0f * rmax_all, d_red_ + 12);
         ++own;
@@ -1922,7 +1957,7 @@ void MixedEngine::launch_step(bool write_imp) {
     k_walls<<<nblk(std::max<size_t>(glob_.size(), 1)), TPB, 0, stream_>>>(
         (uint32_t)glob_.size(), d_glob_, d_model_of_, d_models_, d_scenes_, d_scene_of_, a.xA, a.xB, d_v64_, d_w64_,
         a.v32A, a.v32B, a.w32A, a.w32B, d_ox_, d_oz_, dt_max_, d_red_ + 8, d_disp_ + cur_, d_disp_ + (cur_ ^ 1),
-        0.5f * skin_min_, d_red_ + 12, d_red_ + 11, d_wall32_);
+        0.5f * skin_min_, d_red_ + 12, d_wrot_, d_red_ + 11, d_wall32_);
     ++launches_;
     if (pe) cudaEventRecord(pe[2], stream_);
     cur_ ^= 1;
