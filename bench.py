@@ -32,7 +32,7 @@ sys.path.insert(0, ROOT)
 METRIC = "particle-steps/s on 1 GB300 (mixed vs FP64 at stated error); serving p50/p99 ms"
 UNIT = "particle-steps/s"
 WORKLOAD = "hertz_drum_1M"
-TUNE_STEPS = 100
+TUNE_STEPS = 250
 
 
 def parse():
@@ -56,6 +56,8 @@ def parse():
     ap.add_argument("--bed-n", type=int, default=16_000_000, help="spheres of the compressed-bed workload")
     ap.add_argument("--bed-steps", type=int, default=100, help="timed steps of the compressed-bed workload")
     ap.add_argument("--no-bed", action="store_true")
+    ap.add_argument("--dense-n", type=int, default=1_000_000, help="spheres of the contact-dense workload")
+    ap.add_argument("--no-dense", action="store_true")
     ap.add_argument("--no-batch", action="store_true")
     ap.add_argument("--no-serve", action="store_true")
     return ap.parse_args()
@@ -370,6 +372,8 @@ def ours(args, dist):
         res["batch"] = batch_workload(args, dist, dev)
     if not args.no_bed:
         res["bed"] = bed_workload(args, dist, dev)
+    if not args.no_dense:
+        res["dense"] = dense_workload(args, dist, dev)
     if not args.no_serve and dist.world == 1:
         res["serving"] = serving_workload(args, dev)
     if dist.rank == 0:
@@ -397,7 +401,7 @@ def batch_workload(args, dist, dev):
     n = sum(scene_particles(h) for h in hs)
     b = BatchEngine(hs, device=dev, autotune=True)
     del hs
-    b.run(100)                       # autotuning (80 steps) + warm-up; the tuned settings stay
+    b.run(TUNE_STEPS)                # autotuning + warm-up; the tuned settings stay
     dist.barrier()
     torch.cuda.synchronize()
     b.run(args.batch_steps)
@@ -407,7 +411,7 @@ def batch_workload(args, dist, dev):
     out = {"workload": f"hopper_batch_{args.batch_scenes}", "scenes": args.batch_scenes, "particles": n,
            "value": total * args.batch_steps / (t * 1e-3), "unit": UNIT, "ms_per_step": t / args.batch_steps,
            "steps": args.batch_steps, "gpu_launches": prof["launches"], "tuning": b.tuning(),
-           "note": f"steps 100..{100 + args.batch_steps} of the configured 5000-step run; mixed form, "
+           "note": f"steps {TUNE_STEPS}..{TUNE_STEPS + args.batch_steps} of the configured 5000-step run; mixed form, "
                    "CUDA-graph check intervals, autotuned tick block, skin and cell scale"}
     b.close()
     return out
@@ -423,7 +427,7 @@ def bed_workload(args, dist, dev):
     n = scene_particles(sc)
     e = GpuEngine(sc, device=dev, precision=1, autotune=True)
     del sc
-    e.run(100)                       # autotuning + warm-up
+    e.run(TUNE_STEPS)                # autotuning + warm-up
     dist.barrier()
     torch.cuda.synchronize()
     e.run(args.bed_steps)
@@ -445,9 +449,77 @@ def bed_workload(args, dist, dev):
            "steps": args.bed_steps, "gpu_launches": prof["launches"], "tuning": e.tuning(), "z_pp": z,
            "tick_roofline": {"achieved": ach, "peak": peak, "unit": "GB/s", "frac": ach / peak, "tick_ms": t_tick,
                              "alg_bytes_per_particle_step": b_alg},
-           "note": f"steps 100..{100 + args.bed_steps} of the configured 2000-step run (dt 2e-7 s); mixed form"}
+           "note": f"steps {TUNE_STEPS}..{TUNE_STEPS + args.bed_steps} of the configured 2000-step run (dt 2e-7 s); "
+                   "mixed form"}
     e.close()
     return out
+
+
+def dense_workload(args, dist, dev):
+    """Contact-dense stress case (FCC lattice in contact, ~6 contacts per sphere): both forms'
+    throughput, the mixed form's per-step impulse error from identical state, its energy after
+    200 steps against the FP64 form's, and the tick-kernel roofline with contacts present."""
+    import numpy as np
+    import torch
+    from vedo_gb300 import scenes
+    from vedo_gb300.engine import GpuEngine
+    sc = scenes.dense_pack(n=args.dense_n, seed=9 + dist.rank)
+    n = scene_particles(sc)
+    f = "impact", "angular_impact"
+    a = GpuEngine(sc, up_iact=20, device=dev)
+    b = GpuEngine(sc, device=dev, precision=1)
+    a.run(1)
+    b.run(1)
+    sa, sb = a.state(f), b.state(f)
+    err = {k: float(np.linalg.norm(sa[k] - sb[k]) / max(np.linalg.norm(sa[k]), 1e-300)) for k in f}
+    ia, ib = a.interactions(), b.interactions()
+    A = set(zip(ia["first"][ia["active"] == 1].tolist(), ia["second"][ia["active"] == 1].tolist()))
+    B = set(zip(ib["first"][ib["active"] == 1].tolist(), ib["second"][ib["active"] == 1].tolist()))
+    z = len(A) / n
+    a.run(199)
+    b.run(199)
+    oa, ob = a.observables(), b.observables()
+    ea, eb = oa[0] + oa[1] + oa[2], ob[0] + ob[1] + ob[2]
+    # timing: FP64 form over the next steps, mixed form after tuning
+    a.run(args.warmup)
+    torch.cuda.synchronize()
+    a.run(args.steps)
+    t64 = dist.reduce(a.last_run_profile()["total_ms"], "max")
+    a.close()
+    b.close()
+    e = GpuEngine(sc, device=dev, precision=1, autotune=True)
+    del sc
+    e.run(TUNE_STEPS)
+    e.run(args.warmup)
+    dist.barrier()
+    torch.cuda.synchronize()
+    e.run(args.steps)
+    prof = e.last_run_profile()
+    t = dist.reduce(prof["total_ms"], "max")
+    e.set_profiling(True)
+    e.run(args.profile_steps)
+    kp = e.last_run_profile()
+    e.set_profiling(False)
+    tune = e.tuning()
+    e.close()
+    total = dist.reduce(float(n), "sum")
+    b_alg = 2 * 72 + z * (2 * 16 + 8)                # monodisperse: no per-particle radius
+    t_tick = kp["pair_ms"] / args.profile_steps
+    peak, _ = peaks()
+    ach = b_alg * n / (t_tick * 1e-3) / 1e9
+    mixed = total * args.steps / (t * 1e-3)
+    fp64 = total * args.steps / (t64 * 1e-3)
+    return {"workload": f"dense_fcc_{args.dense_n // 1000}k", "particles": n, "z_pp": z,
+            "value": mixed, "unit": UNIT, "ms_per_step": t / args.steps, "fp64_value": fp64,
+            "fp64_ms_per_step": t64 / args.steps, "mixed_over_fp64": mixed / fp64, "tuning": tune,
+            "errors_mixed_vs_fp64": {"step_impact_rel_l2": err["impact"],
+                                     "step_angular_impact_rel_l2": err["angular_impact"],
+                                     "contact_set_identical": A == B, "contacts": len(A),
+                                     "energy_rel_after_200_steps": abs(ea - eb) / max(abs(ea), 1e-300)},
+            "tick_roofline": {"achieved": ach, "peak": peak, "unit": "GB/s", "frac": ach / peak, "tick_ms": t_tick,
+                              "alg_bytes_per_particle_step": b_alg},
+            "note": "FCC lattice with neighbours overlapping by 1e-6 of the diameter (every pair in contact from "
+                    "step 0), ISwH E 70 GPa, dt 5e-7; per-step impulse error from identical state after one step"}
 
 
 def serving_workload(args, dev):

@@ -151,7 +151,10 @@ typedef struct vedo_engine_opts {
                                  vedo_gpu_get_tuning                                    */
     uint32_t graphs;          /* MIXED only: 1 = each check interval of steps is replayed
                                  as one CUDA graph, captured once per neighbour list (default) */
-    uint32_t reserved[4];
+    uint32_t stored_splits;   /* MIXED only: 1 = the hi/lo FP32 splits of the positions used by
+                                 the sphere-pair overlap test are stored once per step; 0 = formed
+                                 per pair (identical results; the autotuner chooses)       */
+    uint32_t reserved[3];
 } vedo_engine_opts;
 
 typedef struct vedo_gpu_engine vedo_gpu_engine;
@@ -247,9 +250,10 @@ void vedo_gpu_set_profiling(vedo_gpu_engine* e, int on);
 const char* vedo_gpu_last_error(const vedo_gpu_engine* e);
 void vedo_gpu_destroy(vedo_gpu_engine* e);
 
-/* Skin (fraction of r_max), cell scale and tick block size in use by a MIXED-form engine,
+/* Skin (fraction of r_max), cell scale, tick block size and split storage (may be NULL) in use by a MIXED-form engine,
  * after autotuning when it was asked for.  No counterpart in the reference. */
-int vedo_gpu_get_tuning(const vedo_gpu_engine* e, float* skin, float* cell_scale, uint32_t* tick_block);
+int vedo_gpu_get_tuning(const vedo_gpu_engine* e, float* skin, float* cell_scale, uint32_t* tick_block,
+                        uint32_t* stored_splits);
 
 /* Library version string. */
 const char* vedo_gpu_version(void);

@@ -102,3 +102,19 @@ def test_mixed_rejects_mobile_walls(engine_lib):
     with pytest.raises(engine_lib.EngineError) as ex:
         engine_lib.GpuEngine(sc, precision=1)
     assert ex.value.code == 3
+
+
+@pytest.mark.parametrize("which", ["dense", "box"])
+def test_stored_and_formed_position_splits_agree(which, box_ido, engine_lib):
+    """The sphere-pair overlap test's hi/lo position splits, stored once per step or formed per
+    pair, give bit-identical results (the autotuner may pick either)."""
+    sc = scenes.dense_pack(n=20000) if which == "dense" else box_ido
+    a = engine_lib.GpuEngine(sc, precision=1, stored_splits=False)
+    b = engine_lib.GpuEngine(sc, precision=1, stored_splits=True)
+    assert b.tuning()["stored_splits"] and not a.tuning()["stored_splits"]
+    a.run(300)
+    b.run(300)
+    sa, sb = a.state(), b.state()
+    for k in ("position", "velocity", "angular_velocity", "impact", "angular_impact"):
+        assert np.array_equal(sa[k], sb[k]), k
+    assert (a.interactions()["active"] == 1).sum() > 1000 if which == "dense" else True

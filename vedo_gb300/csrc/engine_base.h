@@ -27,8 +27,8 @@ public:
     virtual uint64_t last_profile(double out[4]) const = 0;
     virtual void set_profiling(bool on) = 0;
     virtual const std::string& error() const = 0;
-    // skin fraction, cell scale, tick block size in use (MIXED form only)
-    virtual int tuning(float out[3]) const { (void)out; return VEDO_ERR_INVALID_ARGUMENT; }
+    // skin fraction, cell scale, tick block size, stored position splits in use (MIXED form only)
+    virtual int tuning(float out[4]) const { (void)out; return VEDO_ERR_INVALID_ARGUMENT; }
 };
 
 EngineBase* make_fp64_engine();

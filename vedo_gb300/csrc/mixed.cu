@@ -138,6 +138,56 @@ __device__ __forceinline__ f3 fcross(f3 a, f3 b) {
 }
 __device__ __forceinline__ f3 f4to3(float4 v) { return fm(v.x, v.y, v.z); }
 
+// Double-float (hi + lo, ~48 bits) arithmetic from error-free FP32 transforms (Knuth's two-sum,
+// the FMA two-product).  Both spheres' positions are split into hi/lo FP32 pairs (split32 below),
+// then the relative displacement, |d|^2 and the overlap numerator R^2 - |d|^2 need no FP64 work.
+// The splits are either stored once per step (xs arrays) or formed when a pair needs them: the
+// same function on the same FP64 positions, so the two ways give identical bits.
+struct dfl { float hi, lo; };
+__device__ __forceinline__ dfl two_sum(float a, float b) {
+    const float s = a + b, bb = s - a;
+    return dfl{s, (a - (s - bb)) + (b - bb)};
+}
+__device__ __forceinline__ dfl df_add(dfl a, dfl b) {
+    const dfl s = two_sum(a.hi, b.hi);
+    return two_sum(s.hi, s.lo + (a.lo + b.lo));
+}
+// (hm + lm) - (hs + ls)
+__device__ __forceinline__ dfl df_diff(float hm, float lm, float hs, float ls) {
+    const dfl d = two_sum(hm, -hs);
+    return two_sum(d.hi, d.lo + (lm - ls));
+}
+__device__ __forceinline__ dfl df_sq(dfl a) {
+    const float p = a.hi * a.hi;
+    return two_sum(p, fmaf(a.hi, a.hi, -p) + 2.0f * a.hi * a.lo);
+}
+
+// x = hi + lo with hi = x rounded to FP32 (nearest, ties to even) and lo = (x - hi) rounded to
+// FP32, from the bits of x with integer operations (GB300's FP64 pipe is its scarcest): for
+// 2^-70 <= |x| < 2^101; zero, tiny and huge values take the FP64 conversions.
+__device__ __forceinline__ void split32(double x, float& hi, float& lo) {
+    const unsigned long long u = (unsigned long long)__double_as_longlong(x);
+    const int e = (int)((u >> 52) & 0x7ff) - 1023;           // unbiased exponent
+    if (e < -70 || e > 100) {                                  // 2^(e-52) below stays a normal FP32
+        hi = (float)x;
+        lo = (float)(x - (double)hi);
+        return;
+    }
+    const unsigned long long mant = u & 0xfffffffffffffull;   // 52 bits
+    const unsigned sign = (unsigned)(u >> 63) << 31;
+    const unsigned m23 = (unsigned)(mant >> 29);
+    const unsigned rem = (unsigned)(mant & 0x1fffffffu);      // 29 bits below FP32's mantissa
+    const bool up = rem > 0x10000000u || (rem == 0x10000000u && (m23 & 1u));
+    // exponent and mantissa as one integer: a carry out of the mantissa bumps the exponent
+    const unsigned body = (((unsigned)(e + 127)) << 23) + m23 + (up ? 1u : 0u);
+    hi = __uint_as_float(sign | body);
+    // x - hi = (rem or rem - 2^29) units of 2^(e - 52), exactly; its FP32 rounding
+    const int r = up ? (int)rem - (int)0x20000000 : (int)rem;
+    const float unit = __uint_as_float((unsigned)(e - 52 + 127) << 23);   // 2^(e-52)
+    const float lr = __int2float_rn(r) * unit;
+    lo = r == 0 ? 0.0f : (sign ? -lr : lr);                     // x - hi = +0 when exact
+}
+
 // Kahan-compensated FP32 sum of 3-vectors
 struct K3 {
     f3 s{0.0f, 0.0f, 0.0f}, c{0.0f, 0.0f, 0.0f};
@@ -324,6 +374,10 @@ struct TickArgs {
     const float4* wall32;
     float* wimp;                   // [ne][6] impulse and angular impulse on the wall of a wall entry
     const double4_32a* rr;         // [nm*nm] sphere-sphere: R = ra + rb, R^2, tie-band half width 1e-9 R^2
+    const float4* rr32;            // [nm*nm] the same for the double-float test: R^2 hi, R^2 lo, band, R
+    const float4* xsA;             // [n][2] hi/lo position splits of this step (xs_stored)
+    float4* xsB;                   // ... after the step
+    int xs_stored;                 // 1: splits stored once per step; 0: formed per pair
     const float4* mf;              // [nm][2]: field + external impulse per step, 1/m~; 2.5/(m~ r^2)
 };
 
@@ -331,6 +385,10 @@ struct TickArgs {
 __device__ __forceinline__ void hold_state(const TickArgs& a, uint32_t i) {
     if (i >= a.n || a.models[a.model_of[i]].scope != SCOPE_LOCAL) return;
     a.xB[i] = a.xA[i];
+    if (a.xs_stored) {
+        a.xsB[2 * i] = a.xsA[2 * i];
+        a.xsB[2 * i + 1] = a.xsA[2 * i + 1];
+    }
     a.v32B[i] = a.v32A[i];
     a.w32B[i] = a.w32A[i];
     const uint32_t e1 = a.nptr[i + 1];
@@ -341,7 +399,7 @@ __device__ __forceinline__ void hold_state(const TickArgs& a, uint32_t i) {
         }
 }
 
-template <int LAW>
+template <int LAW, bool XS>
 __global__ void __launch_bounds__(TPB) k_tick(TickArgs a) {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (*a.disp > a.half_skin) {     // the same value for every thread: the whole launch returns
@@ -440,32 +498,52 @@ __global__ void __launch_bounds__(TPB) k_tick(TickArgs a) {
                 const uint32_t slot = owner ? e : a.nslot[e];
                 const PairParam& P = a.params[pi];
                 const double4_32a gg = a.geom[pi];
-                const d3 Pj = ld(a.xA, j);
-                const d3 Ps = i_slave ? Pi : Pj, Pm = i_slave ? Pj : Pi;
                 bool active;
                 float depth;
                 f3 n, rA, rB;
                 if (P.cd == CD_SS) {
-                    const d3 d = sub(Pm, Ps);
-                    const double s2 = fma(d.z, d.z, fma(d.y, d.y, d.x * d.x));
-                    const double4_32a rq = a.rr[pi];          // R, R^2, band
-                    const double num = rq.y - s2;
-                    if (num < -rq.z) {
-                        active = false;
-                        depth = (float)num / ((float)rq.x + sqrtf((float)s2));
-                    } else if (num > rq.z) {
-                        active = true;
-                        depth = (float)num / ((float)rq.x + sqrtf((float)s2));
+                    // d = x_master - x_slave, |d|^2 and R^2 - |d|^2 in double-float from the two
+                    // positions' hi/lo splits; where the numerator is within 1e-9 R^2 of zero the
+                    // reference's FP64 formula decides
+                    float4 hi_i, lo_i, hj, lj;
+                    if (XS) {
+                        hj = a.xsA[2 * j];
+                        lj = a.xsA[2 * j + 1];
+                        hi_i = a.xsA[2 * i];
+                        lo_i = a.xsA[2 * i + 1];
+                    } else {
+                        const d3 Pj = ld(a.xA, j);
+                        split32(Pj.x, hj.x, lj.x);
+                        split32(Pj.y, hj.y, lj.y);
+                        split32(Pj.z, hj.z, lj.z);
+                        split32(Pi.x, hi_i.x, lo_i.x);
+                        split32(Pi.y, hi_i.y, lo_i.y);
+                        split32(Pi.z, hi_i.z, lo_i.z);
+                    }
+                    const float4 hs = i_slave ? hi_i : hj, ls = i_slave ? lo_i : lj;
+                    const float4 hm = i_slave ? hj : hi_i, lm = i_slave ? lj : lo_i;
+                    const dfl dx = df_diff(hm.x, lm.x, hs.x, ls.x), dy = df_diff(hm.y, lm.y, hs.y, ls.y),
+                              dz = df_diff(hm.z, lm.z, hs.z, ls.z);
+                    const dfl s2 = df_add(df_add(df_sq(dx), df_sq(dy)), df_sq(dz));
+                    const float4 rq = a.rr32[pi];                // R^2 hi, R^2 lo, band, R
+                    const dfl num = df_add(dfl{rq.x, rq.y}, dfl{-s2.hi, -s2.lo});
+                    if (num.hi < -rq.z || num.hi > rq.z) {
+                        active = num.hi > 0.0f;
+                        depth = (num.hi + num.lo) / (rq.w + sqrtf(s2.hi));
                     } else {                               // tie band: the reference's formula decides
+                        const d3 Pj = ld(a.xA, j);
+                        const d3 d = i_slave ? sub(Pj, Pi) : sub(Pi, Pj);
                         const double dex = __dsub_rn(__dadd_rn(gg.x, gg.y), xlen(d));
                         active = dex > 0.0;
                         depth = (float)dex;
                     }
-                    const f3 df = fm((float)d.x, (float)d.y, (float)d.z);
+                    const f3 df = fm(dx.hi + dx.lo, dy.hi + dy.lo, dz.hi + dz.lo);
                     n = fdir(df);
                     rA = ((float)gg.x - 0.5f * depth) * n;
                     rB = rA - df;
                 } else {
+                    const d3 Pj = ld(a.xA, j);
+                    const d3 Ps = i_slave ? Pi : Pj, Pm = i_slave ? Pj : Pi;
                     d3 nd, pt;
                     const double dex = wall_detect(P.cd, gg.x, gg.y, gg.z, gg.w, Ps, Pm, ld(a.ox, m), ld(a.oz, m), nd,
                                                    pt);
@@ -525,6 +603,15 @@ __global__ void __launch_bounds__(TPB) k_tick(TickArgs a) {
                 const d3 V2 = add(V, dvd);
                 st(a.xB, i, P2, 0.0);
                 st(a.v64, i, V2, 0.0);
+                if (XS) {
+                    float4 h2, l2;
+                    split32(P2.x, h2.x, l2.x);
+                    split32(P2.y, h2.y, l2.y);
+                    split32(P2.z, h2.z, l2.z);
+                    h2.w = l2.w = 0.0f;
+                    a.xsB[2 * i] = h2;
+                    a.xsB[2 * i + 1] = l2;
+                }
                 if (dw.x != 0.0f || dw.y != 0.0f || dw.z != 0.0f) {
                     const d3 W2 = add(ld(a.w64, i), mk((double)dw.x, (double)dw.y, (double)dw.z));
                     st(a.w64, i, W2, 0.0);
@@ -538,6 +625,10 @@ __global__ void __launch_bounds__(TPB) k_tick(TickArgs a) {
                                          fmaf(vn.z, vn.z, fmaf(vn.y, vn.y, vn.x * vn.x))));
             } else {
                 st(a.xB, i, Pi, 0.0);
+                if (XS) {
+                    a.xsB[2 * i] = a.xsA[2 * i];
+                    a.xsB[2 * i + 1] = a.xsA[2 * i + 1];
+                }
                 a.v32B[i] = vo;
                 a.w32B[i] = wo;
             }
@@ -1041,6 +1132,19 @@ __global__ void __launch_bounds__(TPB) k_unpack3m(uint32_t n, const double4_32a*
         dst[3 * (size_t)i + 2] = v.z;
     }
 }
+// positions as hi/lo FP32 splits, for the stored way of the double-float pair test
+__global__ void __launch_bounds__(TPB) k_split(uint32_t n, const double4_32a* __restrict__ x, float4* __restrict__ xs) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const double4_32a p = x[i];
+    float4 h, l;
+    split32(p.x, h.x, l.x);
+    split32(p.y, h.y, l.y);
+    split32(p.z, h.z, l.z);
+    h.w = l.w = 0.0f;
+    xs[2 * (size_t)i] = h;
+    xs[2 * (size_t)i + 1] = l;
+}
 __global__ void __launch_bounds__(TPB) k_copy32(uint32_t n, const double4_32a* __restrict__ v, float4* __restrict__ o) {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i < n) {
@@ -1238,10 +1342,11 @@ public:
         return VEDO_OK;
     }
     double scene_time(uint32_t s) const { return s < sc_.size() ? sc_[s].t : 0.0; }
-    int tuning(float out[3]) const override {
+    int tuning(float out[4]) const override {
         out[0] = skin_frac_;
         out[1] = cell_scale_;
         out[2] = (float)tpb_;
+        out[3] = xs_stored_ ? 1.0f : 0.0f;
         return VEDO_OK;
     }
 
@@ -1326,6 +1431,9 @@ private:
     float4* d_v32_[2] = {nullptr, nullptr};
     float4* d_w32_[2] = {nullptr, nullptr};
     float4 *d_pos32_ = nullptr, *d_wall32_ = nullptr;
+    float4* d_rr32_ = nullptr;
+    float4* d_xs_[2] = {nullptr, nullptr};        // hi/lo position splits by step parity (stored way)
+    bool xs_stored_ = false;
     unsigned* d_red_ = nullptr;     // [8] vmax bits, [9], [10] scan totals, [11] identity steps, [12] wall speed
     unsigned* d_sred_ = nullptr;    // [scenes][8] per-scene bounds
     float* d_disp_ = nullptr;       // [2] displacement bound, by step parity (cur_)
@@ -1393,7 +1501,7 @@ MixedEngine::~MixedEngine() {
     free_nlist(nl_[1]);
     void* ptrs[] = {d_models_, d_params_, d_pc32_, d_geom_, d_rr_, d_mf_, d_reach_, d_model_of_, d_scene_of_,
                     d_scenes_, d_gfield_, d_glob_, d_x_[0], d_x_[1], d_v64_, d_w64_, d_ox_, d_oz_, d_imp_, d_aimp_,
-                    d_v32_[0], d_v32_[1], d_w32_[0], d_w32_[1], d_pos32_, d_wall32_, d_red_, d_sred_, d_disp_, d_err_,
+                    d_v32_[0], d_v32_[1], d_w32_[0], d_w32_[1], d_rr32_, d_xs_[0], d_xs_[1], d_pos32_, d_wall32_, d_red_, d_sred_, d_disp_, d_err_,
                     d_key_, d_key_alt_, d_sid_, d_sid_alt_, d_cnt_, d_gs_, d_ge_, d_act_, d_stage_, d_obs_, d_gidx_,
                     d_wkey_, d_wval_, d_wkey_alt_, d_wval_alt_, d_wptr_, d_wimp_, d_wred_, d_wrot_};
     for (void* p : ptrs) if (p) cudaFree(p);
@@ -1428,10 +1536,12 @@ int MixedEngine::init_from(const std::vector<SceneSource>& src, const MixedEngin
     tpb_ = opts.tick_block ? (int)opts.tick_block : TPB;
     if (tpb_ < 32 || tpb_ > TPB || tpb_ % 32) return fail(VEDO_ERR_INVALID_ARGUMENT, "tick_block must be 32..256, a multiple of 32");
     tune_pending_ = opts.autotune != 0;
+    xs_stored_ = opts.stored_splits != 0;
     if (prev) {                    // a repacked engine keeps the tuning of the one it replaces
         skin_frac_ = prev->skin_frac_;
         cell_scale_ = prev->cell_scale_;
         tpb_ = prev->tpb_;
+        xs_stored_ = prev->xs_stored_;
         tune_pending_ = prev->tune_pending_;
     }
     if (src.empty()) return fail(VEDO_ERR_INVALID_SCENE, "empty batch");
@@ -1439,6 +1549,7 @@ int MixedEngine::init_from(const std::vector<SceneSource>& src, const MixedEngin
     std::vector<uint32_t> model_of, scene_of;
     std::vector<double> st[7];                 // staged host state of the new scenes
     std::vector<double4_32a> geo, rr;
+    std::vector<float4> rr32;
     std::vector<float> pc, reach;
     std::vector<float4> mf;
     std::vector<double> gfield;
@@ -1525,6 +1636,9 @@ int MixedEngine::init_from(const std::vector<SceneSource>& src, const MixedEngin
             geo.push_back(make_double4_32a(g[0], g[1], g[2], g[3]));
             const double R = g[0] + g[1];
             rr.push_back(make_double4_32a(R, R * R, 1e-9 * R * R, 0.0));
+            const double R2 = R * R;
+            const float R2h = (float)R2;
+            rr32.push_back(make_float4(R2h, (float)(R2 - (double)R2h), (float)(1e-9 * R2), (float)R));
             double r = 0.0;
             if (P.cd == CD_SS) r = g[0] + g[1];
             else if (P.cd == CD_SP) r = g[0] + 0.5 * g[2];
@@ -1559,7 +1673,7 @@ int MixedEngine::init_from(const std::vector<SceneSource>& src, const MixedEngin
     };
     int rc;
     if ((rc = up(&d_models_, models_)) || (rc = up(&d_params_, params_)) || (rc = up(&d_pc32_, pc)) ||
-        (rc = up(&d_geom_, geo)) || (rc = up(&d_rr_, rr)) || (rc = up(&d_mf_, mf)) || (rc = up(&d_reach_, reach)) ||
+        (rc = up(&d_geom_, geo)) || (rc = up(&d_rr_, rr)) || (rc = up(&d_rr32_, rr32)) || (rc = up(&d_mf_, mf)) || (rc = up(&d_reach_, reach)) ||
         (rc = up(&d_model_of_, model_of)) || (rc = up(&d_scene_of_, scene_of)) || (rc = up(&d_gfield_, gfield)) ||
         (rc = up(&d_glob_, glob_)))
         return rc;
@@ -1575,6 +1689,7 @@ int MixedEngine::init_from(const std::vector<SceneSource>& src, const MixedEngin
     MCK(mal(&d_scenes_, sc_.size()));
     MCK(mal(&d_sred_, 8 * sc_.size()));
     for (int b = 0; b < 2; ++b) {
+        MCK(mal(&d_xs_[b], 2 * (size_t)n_));
         MCK(mal(&d_x_[b], n_));
         MCK(mal(&d_v32_[b], n_));
         MCK(mal(&d_w32_[b], n_));
@@ -1741,6 +1856,10 @@ TickArgs MixedEngine::args(bool write_imp) {
     a.wall32 = d_wall32_;
     a.wimp = d_wimp_;
     a.rr = d_rr_;
+    a.rr32 = d_rr32_;
+    a.xsA = d_xs_[cur_];
+    a.xsB = d_xs_[cur_ ^ 1];
+    a.xs_stored = xs_stored_ ? 1 : 0;
     a.mf = d_mf_;
     return a;
 }
@@ -1912,6 +2031,10 @@ int MixedEngine::rebuild() {
     MCK(cudaStreamSynchronize(stream_));
     MCK(cudaGetLastError());
     if (herr) return fail(VEDO_ERR_CUDA, "mixed form: asymmetric neighbour lists");
+    if (xs_stored_) {              // the stored splits follow the positions from here on
+        k_split<<<nblk(n_), TPB, 0, stream_>>>(n_, d_x_[cur_], d_xs_[cur_]);
+        ++own;
+    }
     nlc_ = newl;
     need_rebuild_ = false;
     since_rebuild_ = 0;
@@ -1931,14 +2054,17 @@ void MixedEngine::launch_step(bool write_imp) {
         pev_used_ += 3;
         cudaEventRecord(pe[0], stream_);
     }
+#define VEDO_TICK(L)                                                         \
+    (xs_stored_ ? k_tick<L, true><<<nb, tpb_, 0, stream_>>>(a) : k_tick<L, false><<<nb, tpb_, 0, stream_>>>(a))
     switch (law_) {
-    case IS_BSDBF: k_tick<IS_BSDBF><<<nb, tpb_, 0, stream_>>>(a); break;
-    case IS_BTSDBF: k_tick<IS_BTSDBF><<<nb, tpb_, 0, stream_>>>(a); break;
-    case IS_BSDB2F: k_tick<IS_BSDB2F><<<nb, tpb_, 0, stream_>>>(a); break;
-    case IS_HERTZ: k_tick<IS_HERTZ><<<nb, tpb_, 0, stream_>>>(a); break;
-    case IS_H: k_tick<IS_H><<<nb, tpb_, 0, stream_>>>(a); break;
-    default: k_tick<0><<<nb, tpb_, 0, stream_>>>(a); break;
+    case IS_BSDBF: VEDO_TICK(IS_BSDBF); break;
+    case IS_BTSDBF: VEDO_TICK(IS_BTSDBF); break;
+    case IS_BSDB2F: VEDO_TICK(IS_BSDB2F); break;
+    case IS_HERTZ: VEDO_TICK(IS_HERTZ); break;
+    case IS_H: VEDO_TICK(IS_H); break;
+    default: VEDO_TICK(0); break;
     }
+#undef VEDO_TICK
     ++launches_;
     if (pe) cudaEventRecord(pe[1], stream_);
     if (write_imp && !glob_.empty()) {
@@ -2045,7 +2171,7 @@ int MixedEngine::autotune(uint32_t max_steps, uint32_t* taken) {
     const int blocks[] = {64, 128, 256};
     const float skins[] = {0.05f, 0.1f, 0.15f, 0.25f, 0.4f};
     const float cells[] = {1.0f, 1.25f, 1.5f};
-    const uint32_t need = ci * (uint32_t)(3 + 5);
+    const uint32_t need = ci * (uint32_t)(2 * (3 + 2 + 5));
     if (max_steps < need) return VEDO_OK;            // too short a call: tune in a later one
     cudaEvent_t e0 = ev_[2], e1 = ev_[3];
     auto timed_rebuild = [&](float* ms) -> int {
@@ -2060,6 +2186,10 @@ int MixedEngine::autotune(uint32_t max_steps, uint32_t* taken) {
     auto timed_chunk = [&](float* ms_per_step, float* growth) -> int {
         const uint64_t r0 = round_;
         float disp = 0.0f;
+        // an untimed chunk first: it captures the graph of this configuration
+        int wrc = step_chunk(ci, false, nullptr);
+        if (wrc > 0) return wrc;
+        if (need_rebuild_ && (wrc = rebuild()) != VEDO_OK) return wrc;
         MCK(cudaEventRecord(e0, stream_));
         int rc = step_chunk(ci, false, &disp);
         if (rc > 0) return rc;
@@ -2086,7 +2216,22 @@ int MixedEngine::autotune(uint32_t max_steps, uint32_t* taken) {
         if (t < best) { best = t; best_tpb = b; }
     }
     tpb_ = best_tpb;
-    // 2. skin: tick time per step plus the amortised rebuild
+    // 2. the pair test's hi/lo position splits: formed per pair, or stored once per step (the
+    //    two ways give identical bits)
+    {
+        float t_form = 0.0f, t_store = 0.0f;
+        xs_stored_ = false;
+        drop_graphs();
+        if ((rc = timed_chunk(&t_form, nullptr)) != VEDO_OK) return rc;
+        xs_stored_ = true;
+        drop_graphs();
+        k_split<<<nblk(n_), TPB, 0, stream_>>>(n_, d_x_[cur_], d_xs_[cur_]);
+        if ((rc = timed_chunk(&t_store, nullptr)) != VEDO_OK) return rc;
+        if (need_rebuild_ && (rc = rebuild()) != VEDO_OK) return rc;
+        xs_stored_ = t_store < t_form;
+        drop_graphs();
+    }
+    // 3. skin: tick time per step plus the amortised rebuild
     best = FLT_MAX;
     float best_skin = skin_frac_;
     for (float f : skins) {
@@ -2100,7 +2245,7 @@ int MixedEngine::autotune(uint32_t max_steps, uint32_t* taken) {
         if (cost < best) { best = cost; best_skin = f; }
     }
     set_skin(best_skin);
-    // 3. cell scale: the rebuild time alone (the list does not depend on it)
+    // 4. cell scale: the rebuild time alone (the list does not depend on it)
     best = FLT_MAX;
     float best_cell = cell_scale_;
     for (float c : cells) {

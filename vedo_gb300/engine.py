@@ -67,7 +67,8 @@ def lib() -> C.CDLL:
         L.vedo_gpu_num_scenes.restype = C.c_uint32
         L.vedo_gpu_scene_range.argtypes = [vp, C.c_uint32, C.POINTER(C.c_uint32), C.POINTER(C.c_uint32),
                                            C.POINTER(C.c_double)]
-        L.vedo_gpu_get_tuning.argtypes = [vp, C.POINTER(C.c_float), C.POINTER(C.c_float), C.POINTER(C.c_uint32)]
+        L.vedo_gpu_get_tuning.argtypes = [vp, C.POINTER(C.c_float), C.POINTER(C.c_float), C.POINTER(C.c_uint32),
+                                          C.POINTER(C.c_uint32)]
         _lib = L
     return _lib
 
@@ -77,7 +78,7 @@ STATE_FIELDS = ("position", "velocity", "angular_velocity", "orientation_x", "or
 
 
 def _opts(up_iact, record, precision, device, prefix, skin, check_interval, tick_block=None, cell_scale=None,
-          autotune=False, graphs=True) -> EngineOpts:
+          autotune=False, graphs=True, stored_splits=False) -> EngineOpts:
     opts = EngineOpts()
     lib().vedo_gpu_default_opts(C.byref(opts))
     opts.up_iact, opts.record, opts.precision, opts.device = up_iact, record, precision, device
@@ -91,6 +92,7 @@ def _opts(up_iact, record, precision, device, prefix, skin, check_interval, tick
         opts.cell_scale = cell_scale
     opts.autotune = 1 if autotune else 0
     opts.graphs = 1 if graphs else 0
+    opts.stored_splits = 1 if stored_splits else 0
     opts.output_prefix = prefix
     return opts
 
@@ -106,11 +108,12 @@ class GpuEngine:
     def __init__(self, scene, up_iact: int = 1, record: int = 0, precision: int = _abi.PRECISION_FP64,
                  device: int = 0, output_prefix: Optional[str] = None, skin: Optional[float] = None,
                  check_interval: Optional[int] = None, tick_block: Optional[int] = None,
-                 cell_scale: Optional[float] = None, autotune: bool = False, graphs: bool = True):
+                 cell_scale: Optional[float] = None, autotune: bool = False, graphs: bool = True,
+                 stored_splits: bool = False):
         L = lib()
         self._prefix = output_prefix.encode() if output_prefix else None
         opts = _opts(up_iact, record, precision, device, self._prefix, skin, check_interval, tick_block, cell_scale,
-                     autotune, graphs)
+                     autotune, graphs, stored_splits)
         h = C.c_void_p()
         if isinstance(scene, (str, bytes, os.PathLike)):
             rc = L.vedo_gpu_create_from_ido(os.fsencode(scene), C.byref(opts), C.byref(h))
@@ -190,9 +193,10 @@ class GpuEngine:
 
     def tuning(self):
         """Skin (fraction of r_max), cell scale and tick block size in use (MIXED form)."""
-        sk, cs, tb = C.c_float(0), C.c_float(0), C.c_uint32(0)
-        self._check(lib().vedo_gpu_get_tuning(self.h, C.byref(sk), C.byref(cs), C.byref(tb)))
-        return {"skin": float(sk.value), "cell_scale": float(cs.value), "tick_block": int(tb.value)}
+        sk, cs, tb, ss = C.c_float(0), C.c_float(0), C.c_uint32(0), C.c_uint32(0)
+        self._check(lib().vedo_gpu_get_tuning(self.h, C.byref(sk), C.byref(cs), C.byref(tb), C.byref(ss)))
+        return {"skin": float(sk.value), "cell_scale": float(cs.value), "tick_block": int(tb.value),
+                "stored_splits": bool(ss.value)}
 
     def set_profiling(self, on: bool):
         lib().vedo_gpu_set_profiling(self.h, 1 if on else 0)

@@ -24,6 +24,8 @@ code, the C oracle and the GPU engine.
   r = 0.5 mm by default, E = 10 GPa, friction 0.5) at solid fraction 0.55 in a
   0.4 x 0.4 m box of plates with 32 fixed vertical cylinders (r = 5 mm) on a jittered
   grid, compressed by an orbital top plate moving down at 0.05 m/s.
+* :func:`dense_pack` - a contact-dense stress case: spheres on a face-centred cubic lattice
+  whose neighbours overlap by a hair (12 contacts per sphere from the first step).
 * :func:`serving_job` - the serving stream's jobs: a settling box or a projectile
   impact on a bed, lognormal radii (median 1 mm, sigma_log 0.15) in 8 classes, linear
   spring-dashpot or Hertz (``ISwH``, E = 0.5 GPa) contact.
@@ -571,4 +573,45 @@ def compressed_bed(n: int = 16_000_000, seed: int = 5, steps: int = 2000, dt: fl
     OX = np.concatenate([np.tile([1.0, 0, 0], (n, 1)), np.array(wox)])
     OZ = np.concatenate([np.tile([0, 0, 1.0], (n, 1)), np.array(woz)])
     AV = np.zeros((n + k, 3))
+    return Scene(time_control(steps, dt), models, iacts, midx, P, V, OX, OZ, AV)
+
+
+def dense_pack(n: int = 1_000_000, seed: int = 9, steps: int = 1000, dt: float = 5e-7, radius: float = 1e-3,
+               overlap: float = 1e-6, E: float = 70e9, nu: float = 0.25, restitution: float = 0.7,
+               friction: float = 0.4, density: float = 2500.0) -> Scene:
+    """n spheres on a face-centred cubic lattice (a cube of cells) whose nearest neighbours
+    overlap by `overlap` x 2r, so every sphere has up to 12 contacts from the first step: the
+    contact path of every kernel runs for every pair.  The lattice sits on the floor of an open
+    box of fixed plates that touch its outer spheres; ISwH with Hertz stiffness from E and nu,
+    restitution and friction; small seeded velocities N(0, 1 mm/s)."""
+    rng = np.random.default_rng(seed)
+    d = 2.0 * radius * (1.0 - overlap)              # nearest-neighbour distance
+    a = d * math.sqrt(2.0)                          # FCC cell edge
+    m = max(1, int(math.ceil((n / 4.0) ** (1.0 / 3.0))))
+    basis = np.array([[0.0, 0.0, 0.0], [0.5, 0.5, 0.0], [0.5, 0.0, 0.5], [0.0, 0.5, 0.5]]) * a
+    g = np.stack(np.meshgrid(np.arange(m), np.arange(m), np.arange(m), indexing="ij"), -1).reshape(-1, 3) * a
+    pos = (g[:, None, :] + basis[None, :, :]).reshape(-1, 3)
+    pos = pos[np.lexsort((pos[:, 0], pos[:, 1], pos[:, 2]))][:n]   # fill from the bottom layer up
+    lo = pos.min(0) - radius
+    hi = pos.max(0) + radius
+    ctr = 0.5 * (lo + hi)
+    pos = pos - np.array([ctr[0], ctr[1], lo[2]])
+    vel = rng.normal(0.0, 1e-3, size=pos.shape)
+    half = 0.5 * (hi - lo)
+    width = 2.0 * float(max(half[0], half[1]))
+    height = float(hi[2] - lo[2]) + 4.0 * radius
+    wm, widx, wp, wox, woz = box_walls(width, height, 1e-3)
+    models = [DOModel("Ball", "Ball", MOBILE, LOCAL, density, 1.0, SPHERE, (radius,))] + wm
+    zeta = damping_ratio(restitution)
+    m_of = lambda rr: density * 4.0 / 3.0 * math.pi * rr ** 3
+    iacts = [IactModel("Ball", "Ball", "ISwH", _hertz_mech("ISwH", E, nu, radius, radius, m_of, zeta, friction)),
+             IactModel("Wall", "Ball", "ISwH", _hertz_mech("ISwH", E, nu, radius, None, m_of, zeta, friction))]
+    k = len(widx)
+    nn = len(pos)
+    midx = np.concatenate([np.zeros(nn, np.uint32), 1 + np.array(widx, np.uint32)])
+    P = np.concatenate([pos, wp])
+    V = np.concatenate([vel, np.zeros((k, 3))])
+    OX = np.concatenate([np.tile([1.0, 0, 0], (nn, 1)), wox])
+    OZ = np.concatenate([np.tile([0, 0, 1.0], (nn, 1)), woz])
+    AV = np.zeros((nn + k, 3))
     return Scene(time_control(steps, dt), models, iacts, midx, P, V, OX, OZ, AV)
