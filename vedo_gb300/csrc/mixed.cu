@@ -232,6 +232,14 @@ __device__ __forceinline__ f3 shear_rot(f3 F, f3 vs) {                    // ISw
     return fdot(F, vs) <= 0.0f ? (-flen(F)) * fdir(vs) : flen(F) * fdir(vs);
 }
 
+// ISwH's stiffness fixed at first contact from the normal approach speed (ISwH.cpp:79-110):
+// coef |vn|^0.4, where coef = (0.957832746294131 / (1 - beta^2), or 479.155951122633 when
+// beta >= 0.99) Meff^0.2 knH^0.8 is a constant of the interaction model, computed once in FP64
+// on the host (pc32 slot 6).  Out of line: it runs when a contact forms, not on every pass.
+__device__ __noinline__ float ish_first_kn(float knH, float coef, float vnl) {
+    return vnl == 0.0f ? knH : coef * powf(vnl, 0.4f);
+}
+
 // returns 0 (nothing added), 1 (impulse only) or 2 (impulse + torques).  LAW != 0 fixes the
 // equation type at compile time (scenes with a single law), LAW == 0 dispatches on `is`.
 template <int LAW>
@@ -269,13 +277,7 @@ __device__ __forceinline__ int solve32(int is_rt, const float* __restrict__ c, b
             const float knH = c[0], Meff = c[1], ksc1 = c[2], ksc2 = c[3], betan = c[4], fk = c[5];
             float kn;
             if (!(f & HF_CONTACT)) {
-                const float vnl = flen(vRn);
-                if (vnl == 0.0f) kn = knH;
-                else if (betan < 0.99f)
-                    kn = 0.957832746294131f / (1.0f - betan * betan) * powf(Meff, 0.2f) * powf(knH, 0.8f) *
-                         powf(vnl, 0.4f);
-                else
-                    kn = 479.155951122633f * powf(Meff, 0.2f) * powf(knH, 0.8f) * powf(vnl, 0.4f);
+                kn = ish_first_kn(knH, c[6], flen(vRn));
                 f |= HF_CONTACT;
             } else {
                 kn = h.w;
@@ -1632,6 +1634,11 @@ int MixedEngine::init_from(const std::vector<SceneSource>& src, const MixedEngin
             params_.push_back(P);
             if (P.cd) law = (law == -1 || law == P.is) ? P.is : 0;
             for (int k = 0; k < 8; ++k) pc.push_back((float)P.c[k]);
+            if (P.is == IS_H) {        // ISwH first-contact stiffness coefficient (see ish_first_kn)
+                const double knH = P.c[0], Meff = P.c[1], betan = P.c[4];
+                const double k0 = betan < 0.99 ? 0.957832746294131 / (1.0 - betan * betan) : 479.155951122633;
+                pc[pc.size() - 2] = (float)(k0 * std::pow(Meff, 0.2) * std::pow(knH, 0.8));
+            }
             const double* g = &t.geom[4 * q];
             geo.push_back(make_double4_32a(g[0], g[1], g[2], g[3]));
             const double R = g[0] + g[1];
