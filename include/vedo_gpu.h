@@ -227,6 +227,10 @@ int vedo_gpu_get_observables(vedo_gpu_engine* e, double out[13]);
 /* Simulated time (SystemParameter::GetTimeCurrent) and step counter. */
 double vedo_gpu_time(const vedo_gpu_engine* e);
 uint64_t vedo_gpu_step_count(const vedo_gpu_engine* e);
+/* Steps left until SimMediator::Run would return false (t >= t_stop, with the same FP
+ * accumulation t += dt; SimMediator.cpp:839-841), so that a caller can advance to the end in
+ * a few vedo_gpu_run calls.  For a batch: scene 0. */
+uint64_t vedo_gpu_steps_remaining(const vedo_gpu_engine* e);
 
 /* Write world + active-contact records as a reference .ido
  * (DOWorld::WriteIDO, DOWorld_RWIDO.cpp:149-202). */

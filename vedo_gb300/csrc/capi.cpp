@@ -125,6 +125,8 @@ double vedo_gpu_time(const vedo_gpu_engine* e) { return e ? e->p->time() : 0.0; 
 
 uint64_t vedo_gpu_step_count(const vedo_gpu_engine* e) { return e ? e->p->steps() : 0u; }
 
+uint64_t vedo_gpu_steps_remaining(const vedo_gpu_engine* e) { return e ? e->p->steps_remaining() : 0u; }
+
 int vedo_gpu_write_ido(vedo_gpu_engine* e, const char* path) {
     if (!e || !path) return VEDO_ERR_INVALID_ARGUMENT;
     return e->p->write_ido(path);

@@ -54,6 +54,7 @@ public:
 
     double time() const override { return t_; }
     uint64_t steps() const override { return round_; }
+    uint64_t steps_remaining() const override { return count_steps(t_, dt_, t_stop_); }
     uint32_t num_objects() const override { return n_; }
     uint64_t last_profile(double out[4]) const override;
     void set_profiling(bool on) override { profiling_ = on; }

@@ -23,6 +23,8 @@ public:
     virtual int write_ido(const char* path) = 0;
     virtual double time() const = 0;
     virtual uint64_t steps() const = 0;
+    // SimMediator::Run calls left before t >= t_stop, with the same accumulation t += dt
+    virtual uint64_t steps_remaining() const = 0;
     virtual uint32_t num_objects() const = 0;
     virtual uint64_t last_profile(double out[4]) const = 0;
     virtual void set_profiling(bool on) = 0;
@@ -30,6 +32,17 @@ public:
     // skin fraction, cell scale, tick block size, stored position splits in use (MIXED form only)
     virtual int tuning(float out[4]) const { (void)out; return VEDO_ERR_INVALID_ARGUMENT; }
 };
+
+// count of t += dt steps from t until t >= t_stop (SystemParameter::NextStep, SimMediator.cpp:839-841)
+inline uint64_t count_steps(double t, double dt, double t_stop) {
+    uint64_t k = 0;
+    if (!(dt > 0.0)) return 0;
+    while (t < t_stop) {
+        t += dt;
+        ++k;
+    }
+    return k;
+}
 
 EngineBase* make_fp64_engine();
 EngineBase* make_mixed_engine();

@@ -1328,6 +1328,9 @@ public:
     int write_ido(const char* path) override;
     double time() const override { return sc_.empty() ? 0.0 : sc_[0].t; }
     uint64_t steps() const override { return round_; }
+    uint64_t steps_remaining() const override {
+        return sc_.empty() ? 0 : count_steps(sc_[0].t, sc_[0].dt, sc_[0].t_stop);
+    }
     uint32_t num_objects() const override { return n_; }
     uint64_t last_profile(double out[4]) const override {
         for (int k = 0; k < 4; ++k) out[k] = prof_[k];

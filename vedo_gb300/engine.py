@@ -53,6 +53,8 @@ def lib() -> C.CDLL:
         L.vedo_gpu_time.restype = C.c_double
         L.vedo_gpu_step_count.argtypes = [vp]
         L.vedo_gpu_step_count.restype = C.c_uint64
+        L.vedo_gpu_steps_remaining.argtypes = [vp]
+        L.vedo_gpu_steps_remaining.restype = C.c_uint64
         L.vedo_gpu_write_ido.argtypes = [vp, C.c_char_p]
         L.vedo_gpu_last_run_profile.argtypes = [vp, C.POINTER(C.c_double)]
         L.vedo_gpu_last_run_profile.restype = C.c_uint64
@@ -187,6 +189,10 @@ class GpuEngine:
 
     def step_count(self) -> int:
         return lib().vedo_gpu_step_count(self.h)
+
+    def steps_remaining(self) -> int:
+        """Run() calls left before t >= t_stop."""
+        return lib().vedo_gpu_steps_remaining(self.h)
 
     def write_ido(self, path: str):
         self._check(lib().vedo_gpu_write_ido(self.h, os.fsencode(path)))
