@@ -174,6 +174,16 @@ int vedo_gpu_create(const vedo_scene_desc* scene, const vedo_engine_opts* opts, 
 /* Same, reading a reference .ido file (DOWorld::ReadIDO, DOWorld_RWIDO.cpp:9-55). */
 int vedo_gpu_create_from_ido(const char* path, const vedo_engine_opts* opts, vedo_gpu_engine** out);
 
+/* Same, reading a DOWorldSchema XML scene (DOWorld::ReadXML, DOWorld_ReadXML.cpp:592-660; the
+ * reference parses it with boost::property_tree, the engine with its own reader).  As the
+ * reference reader does, only a SimConstant named "SafetyFactor" sets the safety factor. */
+int vedo_gpu_create_from_xml(const char* path, const vedo_engine_opts* opts, vedo_gpu_engine** out);
+
+/* Convert a scene file between .ido and .xml by the names' extensions, without a GPU (the
+ * reference's DOWorld::ReadIDO/WriteIDO and ReadXML/WriteXML; XML values are written with 17
+ * significant digits). */
+int vedo_convert_scene(const char* in_path, const char* out_path);
+
 /* Advance nsteps time steps, each one SimMediator::Run() (SimMediator.cpp:714-842).
  * *keep_running (may be NULL) receives the last step's return value,
  * t_current < t_stop (SimMediator.cpp:839-841). */

@@ -179,6 +179,7 @@ class RefWorld(_World):
             L.vref_time.restype = C.c_double
             L.vref_energy.argtypes = [C.c_void_p, _dp]
             L.vref_write_ido.argtypes = [C.c_void_p, C.c_char_p]
+            L.vref_write_xml.argtypes = [C.c_void_p, C.c_char_p]
             L.vref_close.argtypes = [C.c_void_p]
             cls._lib = L
         return cls._lib
@@ -236,6 +237,10 @@ class RefWorld(_World):
 
     def write_ido(self, path: str):
         self.lib().vref_write_ido(self.h, path.encode())
+
+    def write_xml(self, path: str):
+        """The reference's own DOWorld::WriteXML (6 significant digits, as it writes them)."""
+        self.lib().vref_write_xml(self.h, path.encode())
 
     def close(self):
         if getattr(self, "h", None):

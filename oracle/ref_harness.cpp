@@ -190,6 +190,12 @@ void vref_write_ido(void* hp, const char* path) {
     h->world->WriteIDO(path, h->irt);
 }
 
+/* The reference's XML writer (DOWorld::WriteXML with the IactRecordTab, DOWorld_WriteXML.cpp). */
+void vref_write_xml(void* hp, const char* path) {
+    RefHandle* h = static_cast<RefHandle*>(hp);
+    h->world->WriteXML(path, h->irt);
+}
+
 /* The reference's destructors release memory they do not own (the process aborts with
  * "free(): invalid pointer" when SimMediator, the consultant and DOWorld are deleted in
  * turn), so a closed handle's reference objects are deliberately leaked. */

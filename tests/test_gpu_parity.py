@@ -198,3 +198,18 @@ def test_engine_native_library_is_the_one_loaded(engine_lib):
     prof = e.last_run_profile()
     assert prof["launches"] >= 4
     del ctypes
+
+
+def test_engine_from_xml_equals_engine_from_ido(engine_lib, tmp_path):
+    """DOWorldSchema XML input (vedo_gpu_create_from_xml) runs exactly as the same scene's .ido."""
+    sc = scenes.cluster(n=64, solver="ISwBSDBF", steps=300, seed=12)
+    ido, xml = str(tmp_path / "s.ido"), str(tmp_path / "s.xml")
+    sc.to_ido(ido)
+    engine_lib.convert_scene(ido, xml)
+    a = engine_lib.GpuEngine(ido, up_iact=5)
+    b = engine_lib.GpuEngine(xml, up_iact=5)
+    a.run(200)
+    b.run(200)
+    sa, sb = a.state(), b.state()
+    for k in sa:
+        assert np.array_equal(sa[k], sb[k]), k

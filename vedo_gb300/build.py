@@ -40,6 +40,7 @@ SOURCES = {
     "noalloc.cu": ("nvcc", []),
     "scene_host.cpp": ("cxx", []),
     "capi.cpp": ("cxx", []),
+    "xml_io.cpp": ("cxx", []),
     "serve.cpp": ("cxx", ["-pthread"]),
 }
 

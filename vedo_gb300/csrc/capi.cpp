@@ -89,6 +89,45 @@ int vedo_gpu_create_from_ido(const char* path, const vedo_engine_opts* opts, ved
     return create_common(s, opts, out);
 }
 
+int vedo_gpu_create_from_xml(const char* path, const vedo_engine_opts* opts, vedo_gpu_engine** out) {
+    if (!path || !out) return VEDO_ERR_INVALID_ARGUMENT;
+    *out = nullptr;
+    vedo::HScene s;
+    std::string err;
+    if (!vedo::read_xml(path, s, err)) {
+        g_create_error = err;
+        return VEDO_ERR_INVALID_SCENE;
+    }
+    return create_common(s, opts, out);
+}
+
+int vedo_convert_scene(const char* in_path, const char* out_path) {
+    if (!in_path || !out_path) return VEDO_ERR_INVALID_ARGUMENT;
+    auto ends = [](const std::string& a, const char* b) {
+        const size_t n = std::strlen(b);
+        return a.size() >= n && a.compare(a.size() - n, n, b) == 0;
+    };
+    const std::string in(in_path), out(out_path);
+    vedo::HScene s;
+    std::string err;
+    bool ok;
+    if (ends(in, ".ido")) ok = vedo::read_ido(in, s, err);
+    else if (ends(in, ".xml")) ok = vedo::read_xml(in, s, err);
+    else { g_create_error = "input must be .ido or .xml"; return VEDO_ERR_INVALID_ARGUMENT; }
+    if (!ok) {
+        g_create_error = err;
+        return ends(in, ".ido") ? VEDO_ERR_BAD_IDO : VEDO_ERR_INVALID_SCENE;
+    }
+    if (ends(out, ".ido")) ok = vedo::write_ido(out, s, err);
+    else if (ends(out, ".xml")) ok = vedo::write_xml(out, s, err);
+    else { g_create_error = "output must be .ido or .xml"; return VEDO_ERR_INVALID_ARGUMENT; }
+    if (!ok) {
+        g_create_error = err;
+        return VEDO_ERR_IO;
+    }
+    return VEDO_OK;
+}
+
 int vedo_gpu_run(vedo_gpu_engine* e, uint32_t nsteps, int* keep_running) {
     if (!e) return VEDO_ERR_INVALID_ARGUMENT;
     return e->p->run(nsteps, keep_running);

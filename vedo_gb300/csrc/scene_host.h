@@ -53,6 +53,9 @@ struct HScene {
 bool read_ido(const std::string& path, HScene& s, std::string& err);
 bool write_ido(const std::string& path, const HScene& s, std::string& err);
 bool scene_from_desc(const vedo_scene_desc* d, HScene& s, std::string& err);
+// DOWorldSchema XML (DOWorld_ReadXML.cpp / DOWorld_WriteXML.cpp layout); xml_io.cpp
+bool read_xml(const std::string& path, HScene& s, std::string& err);
+bool write_xml(const std::string& path, const HScene& s, std::string& err);
 
 // Flattened constants for the device.
 struct Tables {

@@ -41,6 +41,8 @@ def lib() -> C.CDLL:
         L.vedo_gpu_default_opts.argtypes = [C.POINTER(EngineOpts)]
         L.vedo_gpu_create.argtypes = [C.POINTER(_abi.SceneDesc), C.POINTER(EngineOpts), C.POINTER(vp)]
         L.vedo_gpu_create_from_ido.argtypes = [C.c_char_p, C.POINTER(EngineOpts), C.POINTER(vp)]
+        L.vedo_gpu_create_from_xml.argtypes = [C.c_char_p, C.POINTER(EngineOpts), C.POINTER(vp)]
+        L.vedo_convert_scene.argtypes = [C.c_char_p, C.c_char_p]
         L.vedo_gpu_run.argtypes = [vp, C.c_uint32, C.POINTER(C.c_int)]
         L.vedo_gpu_num_objects.argtypes = [vp]
         L.vedo_gpu_num_objects.restype = C.c_uint32
@@ -118,7 +120,9 @@ class GpuEngine:
                      autotune, graphs, stored_splits)
         h = C.c_void_p()
         if isinstance(scene, (str, bytes, os.PathLike)):
-            rc = L.vedo_gpu_create_from_ido(os.fsencode(scene), C.byref(opts), C.byref(h))
+            path = os.fsencode(scene)
+            make = L.vedo_gpu_create_from_xml if path.endswith(b".xml") else L.vedo_gpu_create_from_ido
+            rc = make(path, C.byref(opts), C.byref(h))
         else:
             desc, keep = scene_to_desc(scene)
             rc = L.vedo_gpu_create(C.byref(desc), C.byref(opts), C.byref(h))
@@ -229,6 +233,14 @@ class GpuEngine:
 
     def __exit__(self, *a):
         self.close()
+
+
+def convert_scene(src: str, dst: str):
+    """Convert a scene file between .ido and DOWorldSchema .xml (by extension); no GPU needed."""
+    L = lib()
+    rc = L.vedo_convert_scene(os.fsencode(src), os.fsencode(dst))
+    if rc != 0:
+        raise EngineError(rc, L.vedo_gpu_last_error(None).decode())
 
 
 class BatchEngine(GpuEngine):
