@@ -154,7 +154,11 @@ typedef struct vedo_engine_opts {
     uint32_t stored_splits;   /* MIXED only: 1 = the hi/lo FP32 splits of the positions used by
                                  the sphere-pair overlap test are stored once per step; 0 = formed
                                  per pair (identical results; the autotuner chooses)       */
-    uint32_t reserved[3];
+    uint32_t split_tick;      /* MIXED only: 1 = a light tick (prefilter only, high occupancy)
+                                 finishes the spheres without a pair on the exact path and
+                                 defers the rest to the full tick; 0 = one full tick
+                                 (identical results; the autotuner chooses)                 */
+    uint32_t reserved[2];
 } vedo_engine_opts;
 
 typedef struct vedo_gpu_engine vedo_gpu_engine;
@@ -264,10 +268,11 @@ void vedo_gpu_set_profiling(vedo_gpu_engine* e, int on);
 const char* vedo_gpu_last_error(const vedo_gpu_engine* e);
 void vedo_gpu_destroy(vedo_gpu_engine* e);
 
-/* Skin (fraction of r_max), cell scale, tick block size and split storage (may be NULL) in use by a MIXED-form engine,
+/* Skin (fraction of r_max), cell scale, tick block size, split storage and split tick (the last
+ * two may be NULL) in use by a MIXED-form engine,
  * after autotuning when it was asked for.  No counterpart in the reference. */
 int vedo_gpu_get_tuning(const vedo_gpu_engine* e, float* skin, float* cell_scale, uint32_t* tick_block,
-                        uint32_t* stored_splits);
+                        uint32_t* stored_splits, uint32_t* split_tick);
 
 /* Library version string. */
 const char* vedo_gpu_version(void);

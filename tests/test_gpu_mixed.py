@@ -118,3 +118,18 @@ def test_stored_and_formed_position_splits_agree(which, box_ido, engine_lib):
     for k in ("position", "velocity", "angular_velocity", "impact", "angular_impact"):
         assert np.array_equal(sa[k], sb[k]), k
     assert (a.interactions()["active"] == 1).sum() > 1000 if which == "dense" else True
+
+
+@pytest.mark.parametrize("which", ["dense", "box", "drum"])
+def test_split_tick_agrees_with_one_tick(which, box_ido, drum_ido, engine_lib):
+    """The split tick (light prefilter tick at full occupancy + the full tick over the deferred
+    spheres) gives the single tick's results bit for bit."""
+    sc = {"dense": lambda: scenes.dense_pack(n=20000), "box": lambda: box_ido, "drum": lambda: drum_ido}[which]()
+    a = engine_lib.GpuEngine(sc, precision=1, split_tick=False)
+    b = engine_lib.GpuEngine(sc, precision=1, split_tick=True, stored_splits=True)
+    assert b.tuning()["split_tick"] and not a.tuning()["split_tick"]
+    a.run(300)
+    b.run(300)
+    sa, sb = a.state(), b.state()
+    for k in ("position", "velocity", "angular_velocity", "impact", "angular_impact"):
+        assert np.array_equal(sa[k], sb[k]), k

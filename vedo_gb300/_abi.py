@@ -54,7 +54,8 @@ class EngineOpts(C.Structure):
     _fields_ = [("up_iact", C.c_uint32), ("record", C.c_uint32), ("precision", C.c_uint32), ("device", C.c_int32),
                 ("output_prefix", C.c_char_p), ("skin", C.c_float), ("check_interval", C.c_uint32),
                 ("tick_block", C.c_uint32), ("cell_scale", C.c_float), ("autotune", C.c_uint32),
-                ("graphs", C.c_uint32), ("stored_splits", C.c_uint32), ("reserved", C.c_uint32 * 3)]
+                ("graphs", C.c_uint32), ("stored_splits", C.c_uint32), ("split_tick", C.c_uint32),
+                ("reserved", C.c_uint32 * 2)]
 
 
 class StateView(C.Structure):

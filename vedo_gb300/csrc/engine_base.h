@@ -29,8 +29,8 @@ public:
     virtual uint64_t last_profile(double out[4]) const = 0;
     virtual void set_profiling(bool on) = 0;
     virtual const std::string& error() const = 0;
-    // skin fraction, cell scale, tick block size, stored position splits in use (MIXED form only)
-    virtual int tuning(float out[4]) const { (void)out; return VEDO_ERR_INVALID_ARGUMENT; }
+    // skin fraction, cell scale, tick block size, stored position splits, split tick (MIXED only)
+    virtual int tuning(float out[5]) const { (void)out; return VEDO_ERR_INVALID_ARGUMENT; }
 };
 
 // count of t += dt steps from t until t >= t_stop (SystemParameter::NextStep, SimMediator.cpp:839-841)

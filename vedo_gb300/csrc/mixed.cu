@@ -380,6 +380,8 @@ struct TickArgs {
     const float4* xsA;             // [n][2] hi/lo position splits of this step (xs_stored)
     float4* xsB;                   // ... after the step
     int xs_stored;                 // 1: splits stored once per step; 0: formed per pair
+    uint32_t* work;                // split tick: spheres deferred to the full tick (else nullptr)
+    uint32_t* nwork;
     const float4* mf;              // [nm][2]: field + external impulse per step, 1/m~; 2.5/(m~ r^2)
 };
 
@@ -401,11 +403,126 @@ __device__ __forceinline__ void hold_state(const TickArgs& a, uint32_t i) {
         }
 }
 
+// Phase 1 of a sphere's neighbour walk, for the group of entries at `base`: the entries and
+// neighbour positions are loaded together (the loads overlap) and the FP32 prefilter settles
+// the pairs that are certainly apart (rebuild-time distance minus both spheres' travel since
+// then): their history is cleaned and their wall-impulse share zeroed.  Returns the mask of
+// entries that need the exact path.  The side effects are idempotent, so a walk that is
+// abandoned and redone (the split tick) leaves the same state.
+__device__ __forceinline__ uint32_t prefilter_group(const TickArgs& a, uint32_t base, uint32_t e1, const float4& p32i,
+                                                    float pad) {
+    uint32_t ge[TICK_GROUP], gm[TICK_GROUP];
+    uint8_t gf[TICK_GROUP];
+    float4 gp[TICK_GROUP];
+#pragma unroll
+    for (int k = 0; k < TICK_GROUP; ++k) {
+        const bool ok = base + k < e1;
+        ge[k] = ok ? a.nent[base + k] : 0u;
+        gm[k] = ok ? a.nmeta[base + k] : 0u;     // cd 0: nothing to do
+        gf[k] = ok ? a.fA[base + k] : (uint8_t)0;
+    }
+#pragma unroll
+    for (int k = 0; k < TICK_GROUP; ++k)
+        gp[k] = (gm[k] >> META_CD_SHIFT) & 3u ? a.pos32[ge[k] & ~WALL_BIT] : p32i;
+    uint32_t exact = 0;
+#pragma unroll
+    for (int k = 0; k < TICK_GROUP; ++k) {
+        const uint32_t meta = gm[k];
+        const int cd = (int)((meta >> META_CD_SHIFT) & 3u);
+        if (cd == 0) continue;
+        const uint32_t e = base + k;
+        const uint32_t j = ge[k] & ~WALL_BIT;
+        const bool wall = ge[k] & WALL_BIT;
+        const bool i_slave = meta & META_SLAVE;
+        if (meta & META_BOND) {
+            exact |= 1u << k;
+            continue;
+        }
+        const float4 ws = wall ? a.wall32[j] : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+        if (!apart32(cd, i_slave ? p32i : gp[k], i_slave ? gp[k] : p32i, ws, a.reach[meta & META_PI] + pad)) {
+            exact |= 1u << k;
+            continue;
+        }
+        if (wall && a.write_imp) {
+            float* o = a.wimp + 6 * (size_t)e;
+            o[0] = o[1] = o[2] = o[3] = o[4] = o[5] = 0.0f;
+        }
+        if (meta & META_OWNER) {
+            const uint8_t f0 = gf[k];
+            if (f0 & 15) {                     // ImpactStatus::Clean
+                a.hB[e] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+                a.fB[e] = HF_PENDING;
+            } else if (f0 & HF_PENDING) {
+                a.hB[e] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+                a.fB[e] = 0;
+            }
+        }
+    }
+    return exact;
+}
+
+// The end of a sphere's step: field and external impulse join the compensated sum (the
+// increments dv, dw are FP32, the state update FP64), the impulses are recorded on the last
+// step of a call, and the sphere is integrated.  Returns the sphere's speed bound of the step.
+template <bool XS>
+__device__ __forceinline__ float finish_sphere(const TickArgs& a, uint32_t i, bool mobile, double dt, const d3& Pi,
+                                               const d3& V, const float4& vo, const float4& wo, const float4& mf0,
+                                               const float4& mf1, K3& J, K3& JA) {
+    // DOContainer.cpp:20-27, DiscreteObject.cpp:160-163
+    J.add(fm(mf0.x, mf0.y, mf0.z));
+    if (a.write_imp) {
+        st(a.imp, i, J.value(), 0.0);
+        st(a.aimp, i, JA.value(), 0.0);
+    }
+    if (mobile) {
+        const f3 Jf = fm(J.s.x - J.c.x, J.s.y - J.c.y, J.s.z - J.c.z);
+        const f3 JAf = fm(JA.s.x - JA.c.x, JA.s.y - JA.c.y, JA.s.z - JA.c.z);
+        const f3 dv = mf0.w * Jf, dw = mf1.x * JAf;
+        const d3 dvd = mk((double)dv.x, (double)dv.y, (double)dv.z);
+        const d3 P2 = mk(fma(dt, fma(0.5, dvd.x, V.x), Pi.x), fma(dt, fma(0.5, dvd.y, V.y), Pi.y),
+                         fma(dt, fma(0.5, dvd.z, V.z), Pi.z));
+        const d3 V2 = add(V, dvd);
+        st(a.xB, i, P2, 0.0);
+        st(a.v64, i, V2, 0.0);
+        if (XS) {
+            float4 h2, l2;
+            split32(P2.x, h2.x, l2.x);
+            split32(P2.y, h2.y, l2.y);
+            split32(P2.z, h2.z, l2.z);
+            h2.w = l2.w = 0.0f;
+            a.xsB[2 * i] = h2;
+            a.xsB[2 * i + 1] = l2;
+        }
+        if (dw.x != 0.0f || dw.y != 0.0f || dw.z != 0.0f) {
+            const d3 W2 = add(ld(a.w64, i), mk((double)dw.x, (double)dw.y, (double)dw.z));
+            st(a.w64, i, W2, 0.0);
+            a.w32B[i] = make_float4((float)W2.x, (float)W2.y, (float)W2.z, 0.0f);
+        } else {                                   // no torque: omega + 0 is omega
+            a.w32B[i] = wo;
+        }
+        const float4 vn = make_float4((float)V2.x, (float)V2.y, (float)V2.z, 0.0f);
+        a.v32B[i] = vn;
+        return sqrtf(fmaxf(fmaf(vo.z, vo.z, fmaf(vo.y, vo.y, vo.x * vo.x)),
+                           fmaf(vn.z, vn.z, fmaf(vn.y, vn.y, vn.x * vn.x))));
+    }
+    st(a.xB, i, Pi, 0.0);
+    if (XS) {
+        a.xsB[2 * i] = a.xsA[2 * i];
+        a.xsB[2 * i + 1] = a.xsA[2 * i + 1];
+    }
+    a.v32B[i] = vo;
+    a.w32B[i] = wo;
+    return 0.0f;
+}
+
 template <int LAW, bool XS>
 __global__ void __launch_bounds__(TPB) k_tick(TickArgs a) {
-    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (*a.disp > a.half_skin) {     // the same value for every thread: the whole launch returns
-        hold_state(a, i);
+    const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
+    const bool hold = *a.disp > a.half_skin;     // the same value for every thread of the launch
+    // split tick: this launch takes the spheres the light kernel deferred (none in a held step)
+    const uint32_t i = a.work ? (!hold && t < *a.nwork ? a.work[t] : a.n) : t;
+    if (hold) {
+        if (!a.work) hold_state(a, i);
         return;
     }
     float vmax_local = 0.0f;
@@ -431,58 +548,7 @@ __global__ void __launch_bounds__(TPB) k_tick(TickArgs a) {
             const bool mobile = M.behavior == BEH_MOBILE;
             K3 J, JA;
             for (uint32_t base = e0; base < e1; base += TICK_GROUP) {
-                // Phase 1: the group's entries and neighbour positions are loaded together (the
-                // loads overlap) and the FP32 prefilter settles the pairs that are certainly
-                // apart: rebuild-time distance minus both spheres' travel since then.  The rest
-                // are flagged for the exact path.
-                uint32_t ge[TICK_GROUP], gm[TICK_GROUP];
-                uint8_t gf[TICK_GROUP];
-                float4 gp[TICK_GROUP];
-#pragma unroll
-                for (int k = 0; k < TICK_GROUP; ++k) {
-                    const bool ok = base + k < e1;
-                    ge[k] = ok ? a.nent[base + k] : 0u;
-                    gm[k] = ok ? a.nmeta[base + k] : 0u;     // cd 0: nothing to do
-                    gf[k] = ok ? a.fA[base + k] : (uint8_t)0;
-                }
-#pragma unroll
-                for (int k = 0; k < TICK_GROUP; ++k)
-                    gp[k] = (gm[k] >> META_CD_SHIFT) & 3u ? a.pos32[ge[k] & ~WALL_BIT] : p32i;
-                uint32_t exact = 0;
-#pragma unroll
-                for (int k = 0; k < TICK_GROUP; ++k) {
-                    const uint32_t meta = gm[k];
-                    const int cd = (int)((meta >> META_CD_SHIFT) & 3u);
-                    if (cd == 0) continue;
-                    const uint32_t e = base + k;
-                    const uint32_t j = ge[k] & ~WALL_BIT;
-                    const bool wall = ge[k] & WALL_BIT;
-                    const bool i_slave = meta & META_SLAVE;
-                    if (meta & META_BOND) {
-                        exact |= 1u << k;
-                        continue;
-                    }
-                    const float4 ws = wall ? a.wall32[j] : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
-                    if (!apart32(cd, i_slave ? p32i : gp[k], i_slave ? gp[k] : p32i, ws,
-                                 a.reach[meta & META_PI] + pad)) {
-                        exact |= 1u << k;
-                        continue;
-                    }
-                    if (wall && a.write_imp) {
-                        float* o = a.wimp + 6 * (size_t)e;
-                        o[0] = o[1] = o[2] = o[3] = o[4] = o[5] = 0.0f;
-                    }
-                    if (meta & META_OWNER) {
-                        const uint8_t f0 = gf[k];
-                        if (f0 & 15) {                     // ImpactStatus::Clean
-                            a.hB[e] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
-                            a.fB[e] = HF_PENDING;
-                        } else if (f0 & HF_PENDING) {
-                            a.hB[e] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
-                            a.fB[e] = 0;
-                        }
-                    }
-                }
+                uint32_t exact = prefilter_group(a, base, e1, p32i, pad);
                 // Phase 2: the exact path for the flagged entries, in entry order
                 while (exact) {
                 const int k = __ffs(exact) - 1;
@@ -588,55 +654,61 @@ __global__ void __launch_bounds__(TPB) k_tick(TickArgs a) {
                 }
                 }
             }
-            // field and external impulse (DOContainer.cpp:20-27, DiscreteObject.cpp:160-163) join the
-            // compensated sum; the increments dv, dw are FP32, the state update FP64
-            J.add(fm(mf0.x, mf0.y, mf0.z));
-            if (a.write_imp) {
-                st(a.imp, i, J.value(), 0.0);
-                st(a.aimp, i, JA.value(), 0.0);
-            }
-            if (mobile) {
-                const f3 Jf = fm(J.s.x - J.c.x, J.s.y - J.c.y, J.s.z - J.c.z);
-                const f3 JAf = fm(JA.s.x - JA.c.x, JA.s.y - JA.c.y, JA.s.z - JA.c.z);
-                const f3 dv = mf0.w * Jf, dw = mf1.x * JAf;
-                const d3 dvd = mk((double)dv.x, (double)dv.y, (double)dv.z);
-                const d3 P2 = mk(fma(dt, fma(0.5, dvd.x, V.x), Pi.x), fma(dt, fma(0.5, dvd.y, V.y), Pi.y),
-                                 fma(dt, fma(0.5, dvd.z, V.z), Pi.z));
-                const d3 V2 = add(V, dvd);
-                st(a.xB, i, P2, 0.0);
-                st(a.v64, i, V2, 0.0);
-                if (XS) {
-                    float4 h2, l2;
-                    split32(P2.x, h2.x, l2.x);
-                    split32(P2.y, h2.y, l2.y);
-                    split32(P2.z, h2.z, l2.z);
-                    h2.w = l2.w = 0.0f;
-                    a.xsB[2 * i] = h2;
-                    a.xsB[2 * i + 1] = l2;
-                }
-                if (dw.x != 0.0f || dw.y != 0.0f || dw.z != 0.0f) {
-                    const d3 W2 = add(ld(a.w64, i), mk((double)dw.x, (double)dw.y, (double)dw.z));
-                    st(a.w64, i, W2, 0.0);
-                    a.w32B[i] = make_float4((float)W2.x, (float)W2.y, (float)W2.z, 0.0f);
-                } else {                                   // no torque: omega + 0 is omega
-                    a.w32B[i] = wo;
-                }
-                const float4 vn = make_float4((float)V2.x, (float)V2.y, (float)V2.z, 0.0f);
-                a.v32B[i] = vn;
-                vmax_local = sqrtf(fmaxf(fmaf(vo.z, vo.z, fmaf(vo.y, vo.y, vo.x * vo.x)),
-                                         fmaf(vn.z, vn.z, fmaf(vn.y, vn.y, vn.x * vn.x))));
-            } else {
-                st(a.xB, i, Pi, 0.0);
-                if (XS) {
-                    a.xsB[2 * i] = a.xsA[2 * i];
-                    a.xsB[2 * i + 1] = a.xsA[2 * i + 1];
-                }
-                a.v32B[i] = vo;
-                a.w32B[i] = wo;
-            }
+            vmax_local = finish_sphere<XS>(a, i, mobile, dt, Pi, V, vo, wo, mf0, mf1, J, JA);
         } else if (M.scope == SCOPE_LOCAL) {
             hold_state(a, i);                      // a finished scene waits, unchanged
         }
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) vmax_local = fmaxf(vmax_local, __shfl_xor_sync(0xffffffffu, vmax_local, o));
+    if ((threadIdx.x & 31) == 0 && vmax_local > 0.0f) atomicMax(a.vmax_bits, __float_as_uint(vmax_local * 1.0001f));
+}
+
+// The light half of the split tick: every sphere's neighbour walk in FP32 prefilter form only,
+// at a register count that keeps the SM full.  A sphere whose pairs are all certainly apart is
+// finished here (its sums hold the field impulse alone); a sphere with any pair that needs the
+// exact path is deferred, whole, to k_tick over the worklist.  Either way one thread computes
+// the sphere with the same operations, so results are those of the single tick.
+template <bool XS>
+__global__ void __launch_bounds__(TPB, 5) k_tick_light(TickArgs a) {   // 5 blocks of 256 per SM
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    const bool hold = *a.disp > a.half_skin;
+    float vmax_local = 0.0f;
+    bool defer = false;
+    if (hold) {
+        hold_state(a, i);
+    } else if (i < a.n) {
+        const uint32_t mi = a.model_of[i];
+        const uint32_t si = a.scene_of[i];
+        const uint32_t e0 = a.nptr[i], e1 = a.nptr[i + 1];
+        const float4 p32i = a.pos32[i];
+        const float disp = *a.disp;
+        const ModelDev& M = a.models[mi];
+        const SceneDev& S = a.scenes[si];
+        if (M.scope == SCOPE_LOCAL && S.active) {
+            const float pad = 2.0f * disp;
+            for (uint32_t base = e0; base < e1 && !defer; base += TICK_GROUP)
+                defer = prefilter_group(a, base, e1, p32i, pad) != 0u;
+            if (!defer) {                          // state loaded after the walk: fewer live registers
+                const d3 Pi = ld(a.xA, i);
+                const d3 V = ld(a.v64, i);
+                const float4 vo = a.v32A[i];
+                const float4 wo = a.w32A[i];
+                const float4 mf0 = a.mf[2 * mi], mf1 = a.mf[2 * mi + 1];
+                K3 J, JA;
+                vmax_local = finish_sphere<XS>(a, i, M.behavior == BEH_MOBILE, S.dt, Pi, V, vo, wo, mf0, mf1, J, JA);
+            }
+        } else if (M.scope == SCOPE_LOCAL) {
+            hold_state(a, i);
+        }
+    }
+    const unsigned dm = __ballot_sync(0xffffffffu, defer);
+    if (dm) {                                      // warp-aggregated append to the worklist
+        const int lane = threadIdx.x & 31, lead = __ffs(dm) - 1;
+        uint32_t at = 0;
+        if (lane == lead) at = atomicAdd(a.nwork, (uint32_t)__popc(dm));
+        at = __shfl_sync(0xffffffffu, at, lead);
+        if (defer) a.work[at + __popc(dm & ((1u << lane) - 1u))] = i;
     }
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) vmax_local = fmaxf(vmax_local, __shfl_xor_sync(0xffffffffu, vmax_local, o));
@@ -1347,11 +1419,12 @@ public:
         return VEDO_OK;
     }
     double scene_time(uint32_t s) const { return s < sc_.size() ? sc_[s].t : 0.0; }
-    int tuning(float out[4]) const override {
+    int tuning(float out[5]) const override {
         out[0] = skin_frac_;
         out[1] = cell_scale_;
         out[2] = (float)tpb_;
         out[3] = xs_stored_ ? 1.0f : 0.0f;
+        out[4] = split_tick_ ? 1.0f : 0.0f;
         return VEDO_OK;
     }
 
@@ -1439,6 +1512,8 @@ private:
     float4* d_rr32_ = nullptr;
     float4* d_xs_[2] = {nullptr, nullptr};        // hi/lo position splits by step parity (stored way)
     bool xs_stored_ = false;
+    bool split_tick_ = false;                     // light + deferred full tick (identical results)
+    uint32_t* d_work_ = nullptr;                  // [n] spheres deferred by the light tick
     unsigned* d_red_ = nullptr;     // [8] vmax bits, [9], [10] scan totals, [11] identity steps, [12] wall speed
     unsigned* d_sred_ = nullptr;    // [scenes][8] per-scene bounds
     float* d_disp_ = nullptr;       // [2] displacement bound, by step parity (cur_)
@@ -1506,7 +1581,7 @@ MixedEngine::~MixedEngine() {
     free_nlist(nl_[1]);
     void* ptrs[] = {d_models_, d_params_, d_pc32_, d_geom_, d_rr_, d_mf_, d_reach_, d_model_of_, d_scene_of_,
                     d_scenes_, d_gfield_, d_glob_, d_x_[0], d_x_[1], d_v64_, d_w64_, d_ox_, d_oz_, d_imp_, d_aimp_,
-                    d_v32_[0], d_v32_[1], d_w32_[0], d_w32_[1], d_rr32_, d_xs_[0], d_xs_[1], d_pos32_, d_wall32_, d_red_, d_sred_, d_disp_, d_err_,
+                    d_v32_[0], d_v32_[1], d_w32_[0], d_w32_[1], d_rr32_, d_xs_[0], d_xs_[1], d_work_, d_pos32_, d_wall32_, d_red_, d_sred_, d_disp_, d_err_,
                     d_key_, d_key_alt_, d_sid_, d_sid_alt_, d_cnt_, d_gs_, d_ge_, d_act_, d_stage_, d_obs_, d_gidx_,
                     d_wkey_, d_wval_, d_wkey_alt_, d_wval_alt_, d_wptr_, d_wimp_, d_wred_, d_wrot_};
     for (void* p : ptrs) if (p) cudaFree(p);
@@ -1542,11 +1617,13 @@ int MixedEngine::init_from(const std::vector<SceneSource>& src, const MixedEngin
     if (tpb_ < 32 || tpb_ > TPB || tpb_ % 32) return fail(VEDO_ERR_INVALID_ARGUMENT, "tick_block must be 32..256, a multiple of 32");
     tune_pending_ = opts.autotune != 0;
     xs_stored_ = opts.stored_splits != 0;
+    split_tick_ = opts.split_tick != 0;
     if (prev) {                    // a repacked engine keeps the tuning of the one it replaces
         skin_frac_ = prev->skin_frac_;
         cell_scale_ = prev->cell_scale_;
         tpb_ = prev->tpb_;
         xs_stored_ = prev->xs_stored_;
+        split_tick_ = prev->split_tick_;
         tune_pending_ = prev->tune_pending_;
     }
     if (src.empty()) return fail(VEDO_ERR_INVALID_SCENE, "empty batch");
@@ -1698,6 +1775,7 @@ int MixedEngine::init_from(const std::vector<SceneSource>& src, const MixedEngin
     sdev_.resize(sc_.size());
     MCK(mal(&d_scenes_, sc_.size()));
     MCK(mal(&d_sred_, 8 * sc_.size()));
+    MCK(mal(&d_work_, n_));
     for (int b = 0; b < 2; ++b) {
         MCK(mal(&d_xs_[b], 2 * (size_t)n_));
         MCK(mal(&d_x_[b], n_));
@@ -1870,6 +1948,8 @@ TickArgs MixedEngine::args(bool write_imp) {
     a.xsA = d_xs_[cur_];
     a.xsB = d_xs_[cur_ ^ 1];
     a.xs_stored = xs_stored_ ? 1 : 0;
+    a.work = split_tick_ ? d_work_ : nullptr;
+    a.nwork = d_red_ + 14;
     a.mf = d_mf_;
     return a;
 }
@@ -2064,6 +2144,12 @@ void MixedEngine::launch_step(bool write_imp) {
         pev_used_ += 3;
         cudaEventRecord(pe[0], stream_);
     }
+    if (split_tick_) {              // light tick over all spheres, then the full tick over the deferred
+        cudaMemsetAsync(a.nwork, 0, 4, stream_);
+        if (xs_stored_) k_tick_light<true><<<nblk(n_), TPB, 0, stream_>>>(a);
+        else k_tick_light<false><<<nblk(n_), TPB, 0, stream_>>>(a);
+        ++launches_;
+    }
 #define VEDO_TICK(L)                                                         \
     (xs_stored_ ? k_tick<L, true><<<nb, tpb_, 0, stream_>>>(a) : k_tick<L, false><<<nb, tpb_, 0, stream_>>>(a))
     switch (law_) {
@@ -2127,7 +2213,7 @@ int MixedEngine::step_chunk(uint32_t chunk, bool imp_last, float* disp_after) {
             if (ie != cudaSuccess) return cuda_fail(ie, "cudaGraphInstantiate");
         }
         MCK(cudaGraphLaunch(graph_[c0], stream_));
-        launches_ += (uint64_t)chunk * 2;
+        launches_ += (uint64_t)chunk * (split_tick_ ? 3 : 2);
         if (chunk & 1) cur_ ^= 1;
     } else {
         for (uint32_t k = 0; k < chunk; ++k) launch_step(imp_last && k + 1 == chunk);
@@ -2181,7 +2267,7 @@ int MixedEngine::autotune(uint32_t max_steps, uint32_t* taken) {
     const int blocks[] = {64, 128, 256};
     const float skins[] = {0.05f, 0.1f, 0.15f, 0.25f, 0.4f};
     const float cells[] = {1.0f, 1.25f, 1.5f};
-    const uint32_t need = ci * (uint32_t)(2 * (3 + 2 + 5));
+    const uint32_t need = ci * (uint32_t)(2 * (3 + 2 + 2 + 5));
     if (max_steps < need) return VEDO_OK;            // too short a call: tune in a later one
     cudaEvent_t e0 = ev_[2], e1 = ev_[3];
     auto timed_rebuild = [&](float* ms) -> int {
@@ -2239,6 +2325,20 @@ int MixedEngine::autotune(uint32_t max_steps, uint32_t* taken) {
         if ((rc = timed_chunk(&t_store, nullptr)) != VEDO_OK) return rc;
         if (need_rebuild_ && (rc = rebuild()) != VEDO_OK) return rc;
         xs_stored_ = t_store < t_form;
+        drop_graphs();
+    }
+    // 2b. one full tick, or the split tick (a light tick at full occupancy, the full tick over the
+    //     spheres with a pair on the exact path); identical results
+    {
+        float t_one = 0.0f, t_split = 0.0f;
+        split_tick_ = false;
+        drop_graphs();
+        if ((rc = timed_chunk(&t_one, nullptr)) != VEDO_OK) return rc;
+        split_tick_ = true;
+        drop_graphs();
+        if ((rc = timed_chunk(&t_split, nullptr)) != VEDO_OK) return rc;
+        if (need_rebuild_ && (rc = rebuild()) != VEDO_OK) return rc;
+        split_tick_ = t_split < t_one;
         drop_graphs();
     }
     // 3. skin: tick time per step plus the amortised rebuild

@@ -72,7 +72,7 @@ def lib() -> C.CDLL:
         L.vedo_gpu_scene_range.argtypes = [vp, C.c_uint32, C.POINTER(C.c_uint32), C.POINTER(C.c_uint32),
                                            C.POINTER(C.c_double)]
         L.vedo_gpu_get_tuning.argtypes = [vp, C.POINTER(C.c_float), C.POINTER(C.c_float), C.POINTER(C.c_uint32),
-                                          C.POINTER(C.c_uint32)]
+                                          C.POINTER(C.c_uint32), C.POINTER(C.c_uint32)]
         _lib = L
     return _lib
 
@@ -82,7 +82,7 @@ STATE_FIELDS = ("position", "velocity", "angular_velocity", "orientation_x", "or
 
 
 def _opts(up_iact, record, precision, device, prefix, skin, check_interval, tick_block=None, cell_scale=None,
-          autotune=False, graphs=True, stored_splits=False) -> EngineOpts:
+          autotune=False, graphs=True, stored_splits=False, split_tick=False) -> EngineOpts:
     opts = EngineOpts()
     lib().vedo_gpu_default_opts(C.byref(opts))
     opts.up_iact, opts.record, opts.precision, opts.device = up_iact, record, precision, device
@@ -97,6 +97,7 @@ def _opts(up_iact, record, precision, device, prefix, skin, check_interval, tick
     opts.autotune = 1 if autotune else 0
     opts.graphs = 1 if graphs else 0
     opts.stored_splits = 1 if stored_splits else 0
+    opts.split_tick = 1 if split_tick else 0
     opts.output_prefix = prefix
     return opts
 
@@ -113,11 +114,11 @@ class GpuEngine:
                  device: int = 0, output_prefix: Optional[str] = None, skin: Optional[float] = None,
                  check_interval: Optional[int] = None, tick_block: Optional[int] = None,
                  cell_scale: Optional[float] = None, autotune: bool = False, graphs: bool = True,
-                 stored_splits: bool = False):
+                 stored_splits: bool = False, split_tick: bool = False):
         L = lib()
         self._prefix = output_prefix.encode() if output_prefix else None
         opts = _opts(up_iact, record, precision, device, self._prefix, skin, check_interval, tick_block, cell_scale,
-                     autotune, graphs, stored_splits)
+                     autotune, graphs, stored_splits, split_tick)
         h = C.c_void_p()
         if isinstance(scene, (str, bytes, os.PathLike)):
             path = os.fsencode(scene)
@@ -203,10 +204,11 @@ class GpuEngine:
 
     def tuning(self):
         """Skin (fraction of r_max), cell scale and tick block size in use (MIXED form)."""
-        sk, cs, tb, ss = C.c_float(0), C.c_float(0), C.c_uint32(0), C.c_uint32(0)
-        self._check(lib().vedo_gpu_get_tuning(self.h, C.byref(sk), C.byref(cs), C.byref(tb), C.byref(ss)))
+        sk, cs, tb, ss, st = C.c_float(0), C.c_float(0), C.c_uint32(0), C.c_uint32(0), C.c_uint32(0)
+        self._check(lib().vedo_gpu_get_tuning(self.h, C.byref(sk), C.byref(cs), C.byref(tb), C.byref(ss),
+                                              C.byref(st)))
         return {"skin": float(sk.value), "cell_scale": float(cs.value), "tick_block": int(tb.value),
-                "stored_splits": bool(ss.value)}
+                "stored_splits": bool(ss.value), "split_tick": bool(st.value)}
 
     def set_profiling(self, on: bool):
         lib().vedo_gpu_set_profiling(self.h, 1 if on else 0)

@@ -1,6 +1,6 @@
 """Run one workload of the engine, for a profiler or a quick timing.
 
-    python -m vedo_gb300.profile_case <drum|dense|bed|hopper> <spheres> <steps> [--fp64] [--block B] [--stored]
+    python -m vedo_gb300.profile_case <drum|dense|bed|hopper> <spheres> <steps> [--fp64] [--block B] [--stored] [--split]
 
 Builds the seeded scene, creates the engine (mixed form unless --fp64; fixed settings, no
 autotuning, no graph replay, so that every step is one set of plain launches), runs 5 warm-up
@@ -37,12 +37,13 @@ def main(argv=None):
     ap.add_argument("--fp64", action="store_true")
     ap.add_argument("--block", type=int, default=64)
     ap.add_argument("--stored", action="store_true", help="store the hi/lo position splits once per step")
+    ap.add_argument("--split", action="store_true", help="light tick + full tick over the deferred spheres")
     a = ap.parse_args(argv)
     sc = make(a.kind, a.n)
     if a.fp64:
         e = GpuEngine(sc, up_iact=20)
     else:
-        e = GpuEngine(sc, precision=1, tick_block=a.block, graphs=False, stored_splits=a.stored)
+        e = GpuEngine(sc, precision=1, tick_block=a.block, graphs=False, stored_splits=a.stored, split_tick=a.split)
     e.run(5)
     e.run(a.steps)
     p = e.last_run_profile()
