@@ -335,7 +335,10 @@ def ours(args, dist):
         t_tick = kern["pair_ms"] / kern["steps"]            # average duration of one tick launch
         ach = b_alg * n / (t_tick * 1e-3) / 1e9
         traffic = ncu_traffic_per_particle_step()
-        roof = {"kernel": "k_tick (fused narrow phase + forces + integration, one launch per step)",
+        tuned = eng.tuning()
+        roof = {"kernel": ("k_tick_light + k_tick (split tick: prefilter walk and integration at high occupancy, "
+                           "the full fused tick over the spheres with a pair on the exact path)")
+                if tuned.get("split_tick") else "k_tick (fused narrow phase + forces + integration, one launch per step)",
                 "bound": "hbm", "achieved": ach, "peak": peak, "unit": "GB/s", "frac": ach / peak,
                 "peak_source": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)" if peak_kind == "measured" else peak_kind,
                 "traffic": traffic * n if traffic else None,
