@@ -38,7 +38,7 @@ TUNE_STEPS = 250
 def parse():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=100)
+    ap.add_argument("--steps", type=int, default=2000)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--n", type=int, default=1_000_000, help="spheres in the drum")
@@ -48,7 +48,7 @@ def parse():
     ap.add_argument("--cpu-sample-steps", type=int, default=20)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-profile-pass", action="store_true")
-    ap.add_argument("--profile-steps", type=int, default=20, help="steps of the per-kernel timing pass")
+    ap.add_argument("--profile-steps", type=int, default=200, help="steps of the per-kernel timing pass")
     ap.add_argument("--batch-scenes", type=int, default=256, help="hopper scenes of the batched workload")
     ap.add_argument("--batch-steps", type=int, default=300, help="timed steps of the batched workload")
     ap.add_argument("--serve-duration", type=float, default=0.25, help="seconds of Poisson arrivals (200/s)")
@@ -93,8 +93,10 @@ class Dist:
 
 
 class Clocks:
-    """nvidia-smi samples during the timed region (clocks, power, throttle reasons)."""
-    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+    """nvidia-smi samples (clocks, power, throttle reasons) kept for the timed region: the sampler
+    runs every 50 ms from before the warm-up, and only samples stamped between the region's start
+    and end are used (the nearest ones around it when the region is shorter than one interval)."""
+    FIELDS = ("timestamp,index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
               "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
               "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
 
@@ -102,6 +104,7 @@ class Clocks:
         self.gpu = gpu
         self.proc = None
         self.path = None
+        self.t0 = self.t1 = None
 
     def start(self):
         try:
@@ -109,37 +112,54 @@ class Clocks:
             os.close(fd)
             self.f = open(self.path, "w")
             self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.FIELDS}",
-                                          "--format=csv,noheader,nounits", "-lms", "200"], stdout=self.f,
+                                          "--format=csv,noheader,nounits", "-lms", "50"], stdout=self.f,
                                          stderr=subprocess.DEVNULL)
+            deadline = time.time() + 5.0                  # wait for the sampler's first line
+            while time.time() < deadline and os.path.getsize(self.path) == 0:
+                time.sleep(0.02)
         except Exception:
             self.proc = None
+
+    def begin(self):
+        self.t0 = time.time()
+
+    def end(self):
+        self.t1 = time.time()
 
     def stop(self):
         if not self.proc:
             return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        time.sleep(0.1)                                   # one more sample after the region
         self.proc.terminate()
         try:
             self.proc.wait(timeout=5)
         except Exception:
             self.proc.kill()
         self.f.close()
-        sm, mx, reasons = [], [], set()
+        rows = []
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
         for line in open(self.path):
             p = [x.strip() for x in line.split(",")]
-            if len(p) < 9:
+            if len(p) < 10:
                 continue
             try:
-                sm.append(float(p[1]))
-                mx.append(float(p[2]))
-            except ValueError:
+                ts = time.mktime(time.strptime(p[0].split(".")[0], "%Y/%m/%d %H:%M:%S")) + float("0." + p[0].split(".")[1])
+                rows.append((ts, float(p[2]), float(p[3]), [nm for k, nm in enumerate(names)
+                                                            if p[6 + k].lower().startswith("active")]))
+            except (ValueError, IndexError):
                 continue
-            for k, nm in enumerate(names):
-                if p[5 + k].lower().startswith("active"):
-                    reasons.add(nm)
         os.unlink(self.path)
-        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
-                "reasons": sorted(reasons), "samples": len(sm)}
+        t0, t1 = self.t0 or 0.0, self.t1 or 0.0
+        inside = [r for r in rows if t0 <= r[0] <= t1]
+        where = "inside the timed region"
+        if not inside and rows:                           # region shorter than the interval
+            inside = sorted(rows, key=lambda r: min(abs(r[0] - t0), abs(r[0] - t1)))[:2]
+            where = "nearest to the timed region"
+        sm = [r[1] for r in inside]
+        return {"sm_mhz": statistics.median(sm) if sm else None,
+                "sm_max_mhz": max(r[2] for r in inside) if inside else None,
+                "reasons": sorted({nm for r in inside for nm in r[3]}), "samples": len(sm), "where": where,
+                "region_s": round(t1 - t0, 4)}
 
 
 def peaks():
@@ -215,13 +235,17 @@ def time_form(eng, args, dist, clocks=None):
     """W warm-up steps, then exactly K timed steps (CUDA events on the engine stream, max over
     ranks); returns (ms for K steps, kernel launches in the timed region)."""
     import torch
+    if clocks:
+        clocks.start()
     eng.run(args.warmup)
     dist.barrier()
     torch.cuda.synchronize()
     if clocks:
-        clocks.start()
+        clocks.begin()
     eng.run(args.steps)
     prof = eng.last_run_profile()
+    if clocks:
+        clocks.end()
     rec = clocks.stop() if clocks else None
     dist.barrier()
     return dist.reduce(prof["total_ms"], "max"), prof["launches"], rec
@@ -334,16 +358,17 @@ def ours(args, dist):
     if kern and kern["pair_ms"] > 0:
         t_tick = kern["pair_ms"] / kern["steps"]            # average duration of one tick launch
         ach = b_alg * n / (t_tick * 1e-3) / 1e9
-        traffic = ncu_traffic_per_particle_step()
+        traffic = ncu_traffic("k_tick_light_drum1M_dram.md") if n == 1_000_000 else None
         tuned = eng.tuning()
         roof = {"kernel": ("k_tick_light + k_tick (split tick: prefilter walk and integration at high occupancy, "
                            "the full fused tick over the spheres with a pair on the exact path)")
                 if tuned.get("split_tick") else "k_tick (fused narrow phase + forces + integration, one launch per step)",
                 "bound": "hbm", "achieved": ach, "peak": peak, "unit": "GB/s", "frac": ach / peak,
                 "peak_source": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)" if peak_kind == "measured" else peak_kind,
-                "traffic": traffic * n if traffic else None,
-                "traffic_source": "profiles/k_tick_mixed_drum200k_ncu.md, dram bytes per particle-step x particles"
+                "traffic": traffic,
+                "traffic_source": "profiles/k_tick_light_drum1M_dram.md (ncu, the same workload at full size)"
                 if traffic else None,
+                "dram_frac": traffic / (t_tick * 1e-3) / 1e9 / peak if traffic else None,
                 "tick_ms": t_tick, "walls_ms": kern["object_ms"] / kern["steps"],
                 "share_of_step": t_tick / (t_ms / args.steps), "alg_bytes_per_launch": b_alg * n}
     res = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": dist.world, "steps": args.steps,
@@ -383,11 +408,12 @@ def ours(args, dist):
         emit(res)
 
 
-def ncu_traffic_per_particle_step():
-    """DRAM bytes per particle-step of the tick kernel from the committed ncu summary."""
+def ncu_traffic(name):
+    """DRAM bytes (read + write) of one step's tick launches from a committed ncu summary of the
+    same workload at full size."""
     try:
-        for line in open(os.path.join(ROOT, "profiles", "k_tick_mixed_drum200k_ncu.md")):
-            if line.startswith("dram_bytes_per_particle_step:"):
+        for line in open(os.path.join(ROOT, "profiles", name)):
+            if line.startswith("dram_bytes_per_launch:"):
                 return float(line.split(":", 1)[1].split()[0])
     except OSError:
         pass
@@ -446,12 +472,15 @@ def bed_workload(args, dist, dev):
     t_tick = kp["pair_ms"] / args.profile_steps
     peak, _ = peaks()
     ach = b_alg * n / (t_tick * 1e-3) / 1e9
+    traffic = ncu_traffic("k_tick_light_bed16M_dram.md") if args.bed_n == 16_000_000 else None
     total = dist.reduce(float(n), "sum")
     out = {"workload": f"compressed_bed_{args.bed_n // 1_000_000}M", "particles": n,
            "value": total * args.bed_steps / (t * 1e-3), "unit": UNIT, "ms_per_step": t / args.bed_steps,
            "steps": args.bed_steps, "gpu_launches": prof["launches"], "tuning": e.tuning(), "z_pp": z,
            "tick_roofline": {"achieved": ach, "peak": peak, "unit": "GB/s", "frac": ach / peak, "tick_ms": t_tick,
-                             "alg_bytes_per_particle_step": b_alg},
+                             "alg_bytes_per_particle_step": b_alg, "traffic": traffic,
+                             "dram_frac": traffic / (t_tick * 1e-3) / 1e9 / peak if traffic else None,
+                             "traffic_source": "profiles/k_tick_light_bed16M_dram.md" if traffic else None},
            "note": f"steps {TUNE_STEPS}..{TUNE_STEPS + args.bed_steps} of the configured 2000-step run (dt 2e-7 s); "
                    "mixed form"}
     e.close()

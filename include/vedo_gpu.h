@@ -139,7 +139,10 @@ typedef struct vedo_engine_opts {
                                  (NBSConsultant.cpp:63-76) do; NULL writes nothing  */
     float skin;               /* MIXED only: neighbour-list skin as a fraction of the
                                  largest sphere radius (default 0.15); the list is rebuilt
-                                 when any sphere may have moved half of it             */
+                                 when any sphere may have moved half of it.  Entries with
+                                 orbital walls are gathered with 8 times the skin and the
+                                 list is also rebuilt when a sphere's and an orbital wall's
+                                 travel together may have used that up                  */
     uint32_t check_interval;  /* MIXED only: steps between displacement checks (10)   */
     uint32_t tick_block;      /* MIXED only: threads per block of the tick kernel, 32..256,
                                  a multiple of 32 (0 = 256)                            */
@@ -158,7 +161,11 @@ typedef struct vedo_engine_opts {
                                  finishes the spheres without a pair on the exact path and
                                  defers the rest to the full tick; 0 = one full tick
                                  (identical results; the autotuner chooses)                 */
-    uint32_t reserved[2];
+    uint32_t full_walks;      /* MIXED only: 1 = every sphere walks its neighbour list every
+                                 step; 0 = a sphere whose pairs are all certainly apart since
+                                 the rebuild, with clean history, skips the walk (default;
+                                 identical results)                                     */
+    uint32_t reserved[1];
 } vedo_engine_opts;
 
 typedef struct vedo_gpu_engine vedo_gpu_engine;
@@ -245,6 +252,11 @@ uint64_t vedo_gpu_step_count(const vedo_gpu_engine* e);
  * accumulation t += dt; SimMediator.cpp:839-841), so that a caller can advance to the end in
  * a few vedo_gpu_run calls.  For a batch: scene 0. */
 uint64_t vedo_gpu_steps_remaining(const vedo_gpu_engine* e);
+
+/* MIXED form: the number of spheres whose next step skips the neighbour-list walk (every pair
+ * certainly apart since the last rebuild and its history clean; results are those of a full
+ * walk).  A measure of how much of the list the skin keeps idle.  FP64 form: 0. */
+int vedo_gpu_quiet_spheres(vedo_gpu_engine* e, uint64_t* count);
 
 /* Write world + active-contact records as a reference .ido
  * (DOWorld::WriteIDO, DOWorld_RWIDO.cpp:149-202). */

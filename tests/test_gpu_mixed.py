@@ -133,3 +133,82 @@ def test_split_tick_agrees_with_one_tick(which, box_ido, drum_ido, engine_lib):
     sa, sb = a.state(), b.state()
     for k in ("position", "velocity", "angular_velocity", "impact", "angular_impact"):
         assert np.array_equal(sa[k], sb[k]), k
+
+
+def _active_history(e):
+    it = e.interactions()
+    a = np.nonzero(it["active"] == 1)[0]
+    return {(int(it["first"][q]), int(it["second"][q])): (tuple(it["shear"][q]), float(it["kn"][q])) for q in a}
+
+
+def _same_run(a, b):
+    sa, sb = a.state(), b.state()
+    for k in ("position", "velocity", "angular_velocity", "impact", "angular_impact"):
+        assert np.array_equal(sa[k], sb[k]), k
+    ia, ib = a.interactions(), b.interactions()
+    for k in ia:
+        assert np.array_equal(ia[k], ib[k]), k
+
+
+@pytest.mark.parametrize("which,split", [("fresh_drum", True), ("fresh_drum", False), ("drum", True),
+                                         ("hopper", True), ("hopper", False), ("box", True)])
+def test_quiet_spheres_skip_the_walk_with_identical_results(which, split, box_ido, drum_ido, engine_lib):
+    """A sphere whose pairs have all been certainly apart since the rebuild, with clean history,
+    skips its neighbour-list walk; state, impulses and contact history equal those of full walks
+    bit for bit, over calls of uneven length (impulses written on each call's last step),
+    rebuilds, and contacts that form and break."""
+    sc = {"fresh_drum": lambda: scenes.hertz_drum(n=20000), "drum": lambda: drum_ido,
+          "hopper": lambda: scenes.hopper(n=6000), "box": lambda: box_ido}[which]()
+    a = engine_lib.GpuEngine(sc, precision=1, split_tick=split, full_walks=True)
+    b = engine_lib.GpuEngine(sc, precision=1, split_tick=split)
+    quiet = 0
+    for n in (7, 1, 33, 100, 2, 157, 60):
+        a.run(n)
+        b.run(n)
+        _same_run(a, b)
+        assert a.quiet_spheres() == 0
+        quiet = max(quiet, b.quiet_spheres())
+    if which in ("fresh_drum", "hopper"):       # free fall: most spheres are quiet
+        assert quiet > b.n // 2, quiet
+
+
+def test_orbital_wall_closing_in_independent_of_skin(engine_lib):
+    """A fast orbital top plate closing on a bed: its entries are gathered with the wider wall
+    skin and tested with their own displacement bound.  A tiny skin (rebuilds every few steps), a
+    wide one, and full walks give bit-identical results, the plate does reach the bed, and its
+    impulse agrees with the FP64 engine's."""
+    sc = scenes.compressed_bed(n=20000, box=0.03, cylinders=1, plate_speed=0.5)
+    plate = sc.position.shape[0] - 1
+    wide = engine_lib.GpuEngine(sc, precision=1, skin=0.5)
+    tiny = engine_lib.GpuEngine(sc, precision=1, skin=0.002, check_interval=1)
+    full = engine_lib.GpuEngine(sc, precision=1, skin=0.5, split_tick=True, full_walks=True)
+    f64 = engine_lib.GpuEngine(sc, up_iact=1)
+    touched = 0
+    for n in (50, 1, 99, 150):
+        for e in (wide, tiny, full, f64):
+            e.run(n)
+        _same_run(wide, full)
+        sa, sb = wide.state(), tiny.state()
+        for k in ("position", "velocity", "angular_velocity", "impact", "angular_impact"):
+            assert np.array_equal(sa[k], sb[k]), k
+        assert _active_history(wide) == _active_history(tiny)      # the candidate lists differ
+        jm, jf = sa["impact"][plate], f64.state(("impact",))["impact"][plate]
+        if jf[2] != 0.0:
+            touched += 1
+            assert np.linalg.norm(jm - jf) <= 1e-3 * np.linalg.norm(jf)
+    assert touched >= 2
+
+
+def test_profiled_graph_replay_times_kernels_without_changing_results(engine_lib):
+    """Per-kernel timing events ride inside the replayed graphs: the tick and wall times are
+    reported, and the results are those of an unprofiled run."""
+    sc = scenes.hertz_drum(n=20000)
+    a = engine_lib.GpuEngine(sc, precision=1, split_tick=True)
+    b = engine_lib.GpuEngine(sc, precision=1, split_tick=True)
+    b.set_profiling(True)
+    for n in (40, 100):
+        a.run(n)
+        b.run(n)
+    p = b.last_run_profile()
+    assert p["pair_ms"] > 0.0 and p["object_ms"] > 0.0 and p["pair_ms"] + p["object_ms"] <= p["total_ms"]
+    _same_run(a, b)

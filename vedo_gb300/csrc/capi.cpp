@@ -64,6 +64,7 @@ void vedo_gpu_default_opts(vedo_engine_opts* o) {
     o->graphs = 1;
     o->stored_splits = 0;
     o->split_tick = 0;
+    o->full_walks = 0;
 }
 
 int vedo_gpu_create(const vedo_scene_desc* scene, const vedo_engine_opts* opts, vedo_gpu_engine** out) {
@@ -166,6 +167,11 @@ double vedo_gpu_time(const vedo_gpu_engine* e) { return e ? e->p->time() : 0.0; 
 uint64_t vedo_gpu_step_count(const vedo_gpu_engine* e) { return e ? e->p->steps() : 0u; }
 
 uint64_t vedo_gpu_steps_remaining(const vedo_gpu_engine* e) { return e ? e->p->steps_remaining() : 0u; }
+
+int vedo_gpu_quiet_spheres(vedo_gpu_engine* e, uint64_t* count) {
+    if (!e || !count) return VEDO_ERR_INVALID_ARGUMENT;
+    return e->p->quiet_spheres(count);
+}
 
 int vedo_gpu_write_ido(vedo_gpu_engine* e, const char* path) {
     if (!e || !path) return VEDO_ERR_INVALID_ARGUMENT;

@@ -31,6 +31,10 @@ public:
     virtual const std::string& error() const = 0;
     // skin fraction, cell scale, tick block size, stored position splits, split tick (MIXED only)
     virtual int tuning(float out[5]) const { (void)out; return VEDO_ERR_INVALID_ARGUMENT; }
+    virtual int quiet_spheres(uint64_t* count) {
+        *count = 0;
+        return VEDO_OK;
+    }
 };
 
 // count of t += dt steps from t until t >= t_stop (SystemParameter::NextStep, SimMediator.cpp:839-841)

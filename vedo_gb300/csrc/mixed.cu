@@ -63,6 +63,11 @@ constexpr int META_CD_SHIFT = 24;
 constexpr uint32_t META_BOND = 1u << 26;
 constexpr uint32_t META_OWNER = 1u << 27;
 constexpr uint32_t META_SLAVE = 1u << 28;
+constexpr uint32_t META_MOVING = 1u << 29;   // the entry's other object is an orbital wall
+// Orbital walls move on their own schedule (a drum's end plates turn at a fixed rate), so their
+// entries are gathered with a wider skin and carry their own displacement bound; sphere pairs
+// and fixed walls keep the sphere bound alone.
+constexpr float WALL_SKIN = 8.0f;
 constexpr int TICK_GROUP = 4;    // list entries the tick loads and prefilters together
 constexpr uint8_t PF_ACTIVE_BIT = 64;
 // history flag bit: the status just became clean and the other buffer still holds the old one
@@ -370,8 +375,8 @@ struct TickArgs {
     int write_imp;
     unsigned* vmax_bits;
     const float4* pos32;           // positions at the last rebuild (FP32 offsets)
-    const float* disp;             // bound on any sphere's displacement since the last rebuild
-    float half_skin;               // a step starting with *disp above this is an identity step
+    const float* disp;             // [2]: bounds on any sphere's and any orbital wall's displacement since the rebuild
+    float skin, skin_w;            // list skins: sphere pairs and fixed walls; orbital walls
     const float* reach;
     const float4* wall32;
     float* wimp;                   // [ne][6] impulse and angular impulse on the wall of a wall entry
@@ -383,11 +388,23 @@ struct TickArgs {
     uint32_t* work;                // split tick: spheres deferred to the full tick (else nullptr)
     uint32_t* nwork;
     const float4* mf;              // [nm][2]: field + external impulse per step, 1/m~; 2.5/(m~ r^2)
+    const float* clear;            // [n] per sphere: every prefilter test of its list says "apart" for pad <= clear
+    uint8_t* qcnt;                 // [n] consecutive clean walks (0..2) since the last rebuild
 };
+
+// A step whose list may be incomplete is an identity step: a sphere pair may have closed by
+// both spheres' travel, a sphere-wall pair by the sphere's and an orbital wall's.
+__host__ __device__ __forceinline__ bool list_spent(float ds, float dw, float skin, float skin_w) {
+    return 2.0f * ds > skin || ds + dw > skin_w;
+}
+__device__ __forceinline__ bool held_step(const TickArgs& a) {
+    return list_spent(a.disp[0], a.disp[1], a.skin, a.skin_w);
+}
 
 // identity step: the next buffers receive the current state and history unchanged
 __device__ __forceinline__ void hold_state(const TickArgs& a, uint32_t i) {
     if (i >= a.n || a.models[a.model_of[i]].scope != SCOPE_LOCAL) return;
+    if (a.qcnt[i]) a.qcnt[i] = 0;          // the copy below makes both history buffers alike
     a.xB[i] = a.xA[i];
     if (a.xs_stored) {
         a.xsB[2 * i] = a.xsA[2 * i];
@@ -410,7 +427,7 @@ __device__ __forceinline__ void hold_state(const TickArgs& a, uint32_t i) {
 // entries that need the exact path.  The side effects are idempotent, so a walk that is
 // abandoned and redone (the split tick) leaves the same state.
 __device__ __forceinline__ uint32_t prefilter_group(const TickArgs& a, uint32_t base, uint32_t e1, const float4& p32i,
-                                                    float pad) {
+                                                    float pad, bool& dirty) {
     uint32_t ge[TICK_GROUP], gm[TICK_GROUP];
     uint8_t gf[TICK_GROUP];
     float4 gp[TICK_GROUP];
@@ -439,7 +456,8 @@ __device__ __forceinline__ uint32_t prefilter_group(const TickArgs& a, uint32_t 
             continue;
         }
         const float4 ws = wall ? a.wall32[j] : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
-        if (!apart32(cd, i_slave ? p32i : gp[k], i_slave ? gp[k] : p32i, ws, a.reach[meta & META_PI] + pad)) {
+        const float pk = (meta & META_MOVING) ? a.disp[0] + a.disp[1] : pad;
+        if (!apart32(cd, i_slave ? p32i : gp[k], i_slave ? gp[k] : p32i, ws, a.reach[meta & META_PI] + pk)) {
             exact |= 1u << k;
             continue;
         }
@@ -452,6 +470,7 @@ __device__ __forceinline__ uint32_t prefilter_group(const TickArgs& a, uint32_t 
             if (f0 & 15) {                     // ImpactStatus::Clean
                 a.hB[e] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
                 a.fB[e] = HF_PENDING;
+                dirty = true;
             } else if (f0 & HF_PENDING) {
                 a.hB[e] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
                 a.fB[e] = 0;
@@ -461,13 +480,30 @@ __device__ __forceinline__ uint32_t prefilter_group(const TickArgs& a, uint32_t 
     return exact;
 }
 
+// Quiet spheres.  Between rebuilds a sphere's list, the rebuild-time positions and the fixed
+// walls' normals do not change, and the prefilter's "apart" is monotone in the pad, so one
+// number per sphere (`clear`, k_clear) settles the whole walk: with pad <= clear every entry is
+// apart.  Such a walk writes history only to clean it: an owned entry whose status is set is
+// cleaned to HF_PENDING, and a HF_PENDING one clears the other buffer.  After two consecutive
+// walks that cleaned nothing (`qcnt` = 2) both buffers of every owned entry hold a clean status
+// that a further walk rewrites with the same values, so the walk is skipped and the sphere is
+// finished with its field impulse alone: the state is the walk's, bit for bit.  A walk that
+// cleans a status or needs the exact path resets the count; so do rebuilds and identity steps.
+__device__ __forceinline__ void note_walk(const TickArgs& a, uint32_t i, uint32_t qc, bool reset) {
+    const uint32_t q2 = reset ? 0u : (qc < 2u ? qc + 1u : 2u);
+    if (q2 != qc) a.qcnt[i] = (uint8_t)q2;
+}
+
 // The end of a sphere's step: field and external impulse join the compensated sum (the
 // increments dv, dw are FP32, the state update FP64), the impulses are recorded on the last
 // step of a call, and the sphere is integrated.  Returns the sphere's speed bound of the step.
+// The FP32 velocity copy is always the rounding of the FP64 velocity, so the old speed comes
+// from V.  A quiet sphere had no torque in its last two steps, so both buffers of its FP32
+// angular velocity already hold the value the copy would write.
 template <bool XS>
-__device__ __forceinline__ float finish_sphere(const TickArgs& a, uint32_t i, bool mobile, double dt, const d3& Pi,
-                                               const d3& V, const float4& vo, const float4& wo, const float4& mf0,
-                                               const float4& mf1, K3& J, K3& JA) {
+__device__ __forceinline__ float finish_sphere(const TickArgs& a, uint32_t i, bool mobile, bool quiet, double dt,
+                                               const d3& Pi, const d3& V, const float4& mf0, const float4& mf1, K3& J,
+                                               K3& JA) {
     // DOContainer.cpp:20-27, DiscreteObject.cpp:160-163
     J.add(fm(mf0.x, mf0.y, mf0.z));
     if (a.write_imp) {
@@ -497,36 +533,30 @@ __device__ __forceinline__ float finish_sphere(const TickArgs& a, uint32_t i, bo
             const d3 W2 = add(ld(a.w64, i), mk((double)dw.x, (double)dw.y, (double)dw.z));
             st(a.w64, i, W2, 0.0);
             a.w32B[i] = make_float4((float)W2.x, (float)W2.y, (float)W2.z, 0.0f);
-        } else {                                   // no torque: omega + 0 is omega
-            a.w32B[i] = wo;
+        } else if (!quiet) {                       // no torque: omega + 0 is omega
+            a.w32B[i] = a.w32A[i];
         }
         const float4 vn = make_float4((float)V2.x, (float)V2.y, (float)V2.z, 0.0f);
         a.v32B[i] = vn;
-        return sqrtf(fmaxf(fmaf(vo.z, vo.z, fmaf(vo.y, vo.y, vo.x * vo.x)),
-                           fmaf(vn.z, vn.z, fmaf(vn.y, vn.y, vn.x * vn.x))));
+        const float vx = (float)V.x, vy = (float)V.y, vz = (float)V.z;
+        return sqrtf(fmaxf(fmaf(vz, vz, fmaf(vy, vy, vx * vx)), fmaf(vn.z, vn.z, fmaf(vn.y, vn.y, vn.x * vn.x))));
     }
     st(a.xB, i, Pi, 0.0);
     if (XS) {
         a.xsB[2 * i] = a.xsA[2 * i];
         a.xsB[2 * i + 1] = a.xsA[2 * i + 1];
     }
-    a.v32B[i] = vo;
-    a.w32B[i] = wo;
+    a.v32B[i] = a.v32A[i];
+    a.w32B[i] = a.w32A[i];
     return 0.0f;
 }
 
+// One sphere's step: neighbour walk (prefilter, then the exact path in entry order), sums,
+// integration.  Returns the sphere's speed bound of the step.
 template <int LAW, bool XS>
-__global__ void __launch_bounds__(TPB) k_tick(TickArgs a) {
-    const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
-    const bool hold = *a.disp > a.half_skin;     // the same value for every thread of the launch
-    // split tick: this launch takes the spheres the light kernel deferred (none in a held step)
-    const uint32_t i = a.work ? (!hold && t < *a.nwork ? a.work[t] : a.n) : t;
-    if (hold) {
-        if (!a.work) hold_state(a, i);
-        return;
-    }
+__device__ __forceinline__ float tick_sphere(const TickArgs& a, uint32_t i) {
     float vmax_local = 0.0f;
-    if (i < a.n) {
+    {
         // every load that depends on the index alone is issued here, together, so that their
         // latencies overlap; the model- and list-dependent ones follow
         const uint32_t mi = a.model_of[i];
@@ -535,9 +565,7 @@ __global__ void __launch_bounds__(TPB) k_tick(TickArgs a) {
         const d3 Pi = ld(a.xA, i);
         const d3 V = ld(a.v64, i);
         const float4 p32i = a.pos32[i];
-        const float4 vo = a.v32A[i];
-        const float4 wo = a.w32A[i];
-        const float disp = *a.disp;
+        const float disp = a.disp[0];
         const ModelDev& M = a.models[mi];
         const SceneDev& S = a.scenes[si];
         if (M.scope == SCOPE_LOCAL && S.active) {
@@ -546,9 +574,14 @@ __global__ void __launch_bounds__(TPB) k_tick(TickArgs a) {
             const float pad = 2.0f * disp;
             const float4 mf0 = a.mf[2 * mi], mf1 = a.mf[2 * mi + 1];
             const bool mobile = M.behavior == BEH_MOBILE;
+            // the clean-walk count is kept by the light tick when there is one
+            const uint32_t qc = a.work ? 0u : a.qcnt[i];
+            const bool quiet = qc >= 2u && !a.write_imp && pad <= a.clear[i];
+            bool dirty = false, any_exact = false;
             K3 J, JA;
-            for (uint32_t base = e0; base < e1; base += TICK_GROUP) {
-                uint32_t exact = prefilter_group(a, base, e1, p32i, pad);
+            for (uint32_t base = e0; base < e1 && !quiet; base += TICK_GROUP) {
+                uint32_t exact = prefilter_group(a, base, e1, p32i, pad, dirty);
+                any_exact |= exact != 0u;
                 // Phase 2: the exact path for the flagged entries, in entry order
                 while (exact) {
                 const int k = __ffs(exact) - 1;
@@ -654,10 +687,43 @@ __global__ void __launch_bounds__(TPB) k_tick(TickArgs a) {
                 }
                 }
             }
-            vmax_local = finish_sphere<XS>(a, i, mobile, dt, Pi, V, vo, wo, mf0, mf1, J, JA);
+            if (!a.work && !quiet) note_walk(a, i, qc, dirty || any_exact);
+            vmax_local = finish_sphere<XS>(a, i, mobile, quiet, dt, Pi, V, mf0, mf1, J, JA);
         } else if (M.scope == SCOPE_LOCAL) {
             hold_state(a, i);                      // a finished scene waits, unchanged
         }
+    }
+    return vmax_local;
+}
+
+__device__ __forceinline__ void reduce_vmax(const TickArgs& a, float vmax_local) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) vmax_local = fmaxf(vmax_local, __shfl_xor_sync(0xffffffffu, vmax_local, o));
+    if ((threadIdx.x & 31) == 0 && vmax_local > 0.0f) atomicMax(a.vmax_bits, __float_as_uint(vmax_local * 1.0001f));
+}
+
+// The full tick, one thread per sphere.
+template <int LAW, bool XS>
+__global__ void __launch_bounds__(TPB) k_tick(TickArgs a) {
+    const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
+    float vmax_local = 0.0f;
+    if (held_step(a)) {                          // the same value for every thread of the launch
+        hold_state(a, t);
+    } else if (t < a.n) {
+        vmax_local = tick_sphere<LAW, XS>(a, t);
+    }
+    reduce_vmax(a, vmax_local);
+}
+
+// The full tick of the split tick: a grid sized to the resident threads strides over the
+// spheres the light kernel deferred (none in a held step).
+template <int LAW, bool XS>
+__global__ void __launch_bounds__(TPB) k_tick_work(TickArgs a) {
+    float vmax_local = 0.0f;
+    if (!held_step(a)) {
+        const uint32_t nw = *a.nwork;
+        for (uint32_t q = blockIdx.x * blockDim.x + threadIdx.x; q < nw; q += gridDim.x * blockDim.x)
+            vmax_local = fmaxf(vmax_local, tick_sphere<LAW, XS>(a, a.work[q]));
     }
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) vmax_local = fmaxf(vmax_local, __shfl_xor_sync(0xffffffffu, vmax_local, o));
@@ -672,31 +738,41 @@ __global__ void __launch_bounds__(TPB) k_tick(TickArgs a) {
 template <bool XS>
 __global__ void __launch_bounds__(TPB, 5) k_tick_light(TickArgs a) {   // 5 blocks of 256 per SM
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-    const bool hold = *a.disp > a.half_skin;
+    const bool hold = held_step(a);
     float vmax_local = 0.0f;
     bool defer = false;
     if (hold) {
         hold_state(a, i);
     } else if (i < a.n) {
+        // the state is read after the quiet test (or the walk): start bringing it to L2 now
+        asm volatile("prefetch.global.L2 [%0];" ::"l"(a.xA + i));
+        asm volatile("prefetch.global.L2 [%0];" ::"l"(a.v64 + i));
         const uint32_t mi = a.model_of[i];
         const uint32_t si = a.scene_of[i];
-        const uint32_t e0 = a.nptr[i], e1 = a.nptr[i + 1];
-        const float4 p32i = a.pos32[i];
-        const float disp = *a.disp;
+        const uint32_t qc = a.qcnt[i];
+        const float clear = a.clear[i];
+        const float disp = a.disp[0];
         const ModelDev& M = a.models[mi];
         const SceneDev& S = a.scenes[si];
         if (M.scope == SCOPE_LOCAL && S.active) {
             const float pad = 2.0f * disp;
-            for (uint32_t base = e0; base < e1 && !defer; base += TICK_GROUP)
-                defer = prefilter_group(a, base, e1, p32i, pad) != 0u;
+            const bool quiet = qc >= 2u && !a.write_imp && pad <= clear;
+            if (!quiet) {                          // walk the list
+                const uint32_t e0 = a.nptr[i], e1 = a.nptr[i + 1];
+                const float4 p32i = a.pos32[i];
+                bool dirty = false;
+                for (uint32_t base = e0; base < e1 && !defer; base += TICK_GROUP)
+                    defer = prefilter_group(a, base, e1, p32i, pad, dirty) != 0u;
+                note_walk(a, i, a.qcnt[i], dirty || defer);    // (reread: fewer live registers in the walk)
+            }
             if (!defer) {                          // state loaded after the walk: fewer live registers
                 const d3 Pi = ld(a.xA, i);
                 const d3 V = ld(a.v64, i);
-                const float4 vo = a.v32A[i];
-                const float4 wo = a.w32A[i];
-                const float4 mf0 = a.mf[2 * mi], mf1 = a.mf[2 * mi + 1];
+                const uint32_t mj = a.model_of[i];     // (reread: fewer live registers in the walk)
+                const float4 mf0 = a.mf[2 * mj], mf1 = a.mf[2 * mj + 1];
                 K3 J, JA;
-                vmax_local = finish_sphere<XS>(a, i, M.behavior == BEH_MOBILE, S.dt, Pi, V, vo, wo, mf0, mf1, J, JA);
+                vmax_local = finish_sphere<XS>(a, i, a.models[mj].behavior == BEH_MOBILE, quiet,
+                                               a.scenes[a.scene_of[i]].dt, Pi, V, mf0, mf1, J, JA);
             }
         } else if (M.scope == SCOPE_LOCAL) {
             hold_state(a, i);
@@ -755,18 +831,22 @@ __global__ void k_walls(uint32_t nglob, const uint32_t* __restrict__ glob, const
                         float4* __restrict__ v32B, const float4* __restrict__ w32A, float4* __restrict__ w32B,
                         double4_32a* __restrict__ ox, double4_32a* __restrict__ oz, float dt_max,
                         unsigned* __restrict__ vmax_bits, const float* __restrict__ disp_in,
-                        float* __restrict__ disp_out, float half_skin, const unsigned* __restrict__ wall_speed_bits,
+                        float* __restrict__ disp_out, float skin, float skin_w,
+                        const unsigned* __restrict__ wall_speed_bits,
                         const double4_32a* __restrict__ wrot,
-                        unsigned* __restrict__ held, float4* __restrict__ wall32) {
+                        unsigned* __restrict__ held, float4* __restrict__ wall32, unsigned* __restrict__ nwork) {
     const uint32_t q = blockIdx.x * blockDim.x + threadIdx.x;
-    const float disp = *disp_in;
-    const bool hold = disp > half_skin;
+    const float ds = disp_in[0], dw = disp_in[1];
+    const bool hold = list_spent(ds, dw, skin, skin_w);
     if (q == 0) {
+        *nwork = 0u;                               // the split tick's worklist, empty for the next step
         if (hold) {
-            *disp_out = disp;
+            disp_out[0] = ds;
+            disp_out[1] = dw;
             *held += 1u;
         } else {
-            *disp_out = disp + dt_max * fmaxf(__uint_as_float(*vmax_bits), __uint_as_float(*wall_speed_bits));
+            disp_out[0] = ds + dt_max * __uint_as_float(*vmax_bits);
+            disp_out[1] = dw + dt_max * __uint_as_float(*wall_speed_bits);
         }
         *vmax_bits = 0u;
     }
@@ -941,7 +1021,8 @@ __global__ void __launch_bounds__(TPB) k_nbr(uint32_t nloc, const uint32_t* __re
         if (wl.w != 0.0f) {
             float err;
             const float d = cd == CD_SP ? plane_dist32(pi, pos32[w], wl, err) : line_dist32(pi, pos32[w], wl, err);
-            if (d - err > (reach[pw] + skin) * (1.0f + 4.0f * PF_ARITH_EPS)) continue;
+            const float sk = models[model_of[w]].behavior == BEH_ORBITAL ? WALL_SKIN * skin : skin;
+            if (d - err > (reach[pw] + sk) * (1.0f + 4.0f * PF_ARITH_EPS)) continue;
         }
         if (FILL) ent[off + c] = w | WALL_BIT;
         ++c;
@@ -1019,8 +1100,9 @@ __global__ void __launch_bounds__(TPB) k_meta(uint32_t n, const uint32_t* __rest
         const uint32_t pi = pidx(S, i_slave ? mi : mj, i_slave ? mj : mi);
         const PairParam& P = params[pi];
         const bool bond = (P.is == IS_BSDBF || P.is == IS_BTSDBF || P.is == IS_BSDB2F) && P.c[4] != 0.0;
+        const bool moving = (v & WALL_BIT) && models[mj].behavior == BEH_ORBITAL;
         meta[e] = (pi & META_PI) | ((uint32_t)(P.cd & 3) << META_CD_SHIFT) | (bond ? META_BOND : 0u) |
-                  (slot[e] == e ? META_OWNER : 0u) | (i_slave ? META_SLAVE : 0u);
+                  (slot[e] == e ? META_OWNER : 0u) | (i_slave ? META_SLAVE : 0u) | (moving ? META_MOVING : 0u);
     }
 }
 
@@ -1056,6 +1138,74 @@ __global__ void __launch_bounds__(TPB) k_carry(uint32_t n, const uint32_t* __res
 }
 
 
+
+// Per sphere, the largest pad (the prefilter's allowance for both spheres' travel since the
+// rebuild) at which every entry of its new list is still certainly apart, checked with the
+// prefilter itself: an estimate from the rebuild-time gap, backed off until apart32 confirms it.
+// -1 (never quiet) for a sphere with a bondable entry, an entry that failed the check, or an
+// entry with an orbital wall (its normal is recomputed every step).  Resets the clean-walk count.
+__global__ void __launch_bounds__(TPB) k_clear(uint32_t n, const uint32_t* __restrict__ ptr,
+                                               const uint32_t* __restrict__ ent, const uint32_t* __restrict__ meta,
+                                               const uint32_t* __restrict__ model_of,
+                                               const ModelDev* __restrict__ models, const float4* __restrict__ pos32,
+                                               const float4* __restrict__ wall32, const float* __restrict__ reach,
+                                               float* __restrict__ clear, uint8_t* __restrict__ qcnt, int enable) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    qcnt[i] = 0;
+    float c = -1.0f;
+    if (enable && models[model_of[i]].scope == SCOPE_LOCAL) {
+        c = 3.0e38f;
+        const float4 pi = pos32[i];
+        for (uint32_t e = ptr[i]; e < ptr[i + 1]; ++e) {
+            const uint32_t m = meta[e];
+            const int cd = (int)((m >> META_CD_SHIFT) & 3u);
+            if (cd == 0) continue;
+            const uint32_t j = ent[e] & ~WALL_BIT;
+            const bool wall = ent[e] & WALL_BIT;
+            if ((m & META_BOND) || (wall && models[model_of[j]].behavior == BEH_ORBITAL)) {
+                c = -1.0f;
+                break;
+            }
+            const float4 pj = pos32[j];
+            const float4 ws = wall ? wall32[j] : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+            const float4 ps = (m & META_SLAVE) ? pi : pj, pm = (m & META_SLAVE) ? pj : pi;
+            const float dx = pm.x - ps.x, dy = pm.y - ps.y, dz = pm.z - ps.z;
+            float gap;
+            if (cd == CD_SS) {
+                gap = sqrtf(dx * dx + dy * dy + dz * dz);
+            } else if (cd == CD_SP) {
+                gap = fabsf(dx * ws.x + dy * ws.y + dz * ws.z);
+            } else {
+                const float cx = dy * ws.z - dz * ws.y, cy = dz * ws.x - dx * ws.z, cz = dx * ws.y - dy * ws.x;
+                gap = sqrtf(cx * cx + cy * cy + cz * cz);
+            }
+            const float r = reach[m & META_PI];
+            float t = (gap - ps.w - pm.w - PF_ARITH_EPS * (fabsf(dx) + fabsf(dy) + fabsf(dz))) * (1.0f - 1e-4f) - r;
+            bool ok = false;
+            for (int k = 0; k < 4 && t >= 0.0f && !ok; ++k) {
+                ok = apart32(cd, ps, pm, ws, r + t);
+                if (!ok) t = k < 2 ? 0.5f * t : 0.0f;
+            }
+            if (!ok) {
+                c = -1.0f;
+                break;
+            }
+            c = fminf(c, t);
+        }
+    }
+    clear[i] = c;
+}
+
+// Spheres whose next step skips the walk: the tick's own test, with the current bound.
+__global__ void __launch_bounds__(TPB) k_quiet_count(uint32_t n, const float* __restrict__ clear,
+                                                     const uint8_t* __restrict__ qcnt, const float* __restrict__ disp,
+                                                     unsigned* __restrict__ count) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    const bool q = i < n && qcnt[i] >= 2u && 2.0f * disp[0] <= clear[i];
+    const unsigned m = __ballot_sync(0xffffffffu, q);
+    if ((threadIdx.x & 31) == 0 && m) atomicAdd(count, (unsigned)__popc(m));
+}
 
 // Wall entries of every sphere, in ascending entry order, keyed by the wall's global index.
 __global__ void __launch_bounds__(TPB) k_wall_count(uint32_t n, const uint32_t* __restrict__ ptr,
@@ -1419,6 +1569,7 @@ public:
         return VEDO_OK;
     }
     double scene_time(uint32_t s) const { return s < sc_.size() ? sc_[s].t : 0.0; }
+    int quiet_spheres(uint64_t* count) override;
     int tuning(float out[5]) const override {
         out[0] = skin_frac_;
         out[1] = cell_scale_;
@@ -1452,7 +1603,7 @@ private:
     }
     int rebuild();
     void launch_step(bool write_imp);
-    int step_chunk(uint32_t chunk, bool imp_last, float* disp_after);
+    int step_chunk(uint32_t chunk, bool imp_last, float* use_after);
     int autotune(uint32_t max_steps, uint32_t* taken);
     void set_skin(float frac);
     void drop_graphs();
@@ -1474,7 +1625,10 @@ private:
     float cell_scale_ = 1.0f;       // cell edge = cell_scale * (2 r_max + skin)
     int tpb_ = TPB;                 // threads per block of the tick kernel
     bool tune_pending_ = false;
-    cudaGraphExec_t graph_[2] = {nullptr, nullptr};   // one check interval of steps, by start parity
+    // one check interval of steps, by start parity: [0..1] plain, [2..3] with the per-kernel
+    // timing events of profiling
+    cudaGraphExec_t graph_[4] = {nullptr, nullptr, nullptr, nullptr};
+    unsigned ev_flags_ = cudaEventRecordDefault;      // cudaEventRecordExternal while capturing
     std::vector<cudaEvent_t> pev_;  // profiling: per step, events before the tick, after it, after the walls
     uint32_t pev_used_ = 0;
     uint64_t round_ = 0;
@@ -1514,9 +1668,13 @@ private:
     bool xs_stored_ = false;
     bool split_tick_ = false;                     // light + deferred full tick (identical results)
     uint32_t* d_work_ = nullptr;                  // [n] spheres deferred by the light tick
+    bool quiet_ok_ = true;                        // quiet spheres skip their walk (identical results)
+    int sms_ = 1;                                 // streaming multiprocessors of the device
+    float* d_clear_ = nullptr;                    // [n] quiet-sphere pad limit of the current list
+    uint8_t* d_qcnt_ = nullptr;                   // [n] clean walks since the rebuild (0..2)
     unsigned* d_red_ = nullptr;     // [8] vmax bits, [9], [10] scan totals, [11] identity steps, [12] wall speed
     unsigned* d_sred_ = nullptr;    // [scenes][8] per-scene bounds
-    float* d_disp_ = nullptr;       // [2] displacement bound, by step parity (cur_)
+    float* d_disp_ = nullptr;       // [2][2] sphere and orbital-wall displacement bounds, by step parity (cur_)
     int* d_err_ = nullptr;
     NList nl_[2];
     int nlc_ = 0;                   // current neighbour list
@@ -1581,7 +1739,7 @@ MixedEngine::~MixedEngine() {
     free_nlist(nl_[1]);
     void* ptrs[] = {d_models_, d_params_, d_pc32_, d_geom_, d_rr_, d_mf_, d_reach_, d_model_of_, d_scene_of_,
                     d_scenes_, d_gfield_, d_glob_, d_x_[0], d_x_[1], d_v64_, d_w64_, d_ox_, d_oz_, d_imp_, d_aimp_,
-                    d_v32_[0], d_v32_[1], d_w32_[0], d_w32_[1], d_rr32_, d_xs_[0], d_xs_[1], d_work_, d_pos32_, d_wall32_, d_red_, d_sred_, d_disp_, d_err_,
+                    d_v32_[0], d_v32_[1], d_w32_[0], d_w32_[1], d_rr32_, d_xs_[0], d_xs_[1], d_work_, d_clear_, d_qcnt_, d_pos32_, d_wall32_, d_red_, d_sred_, d_disp_, d_err_,
                     d_key_, d_key_alt_, d_sid_, d_sid_alt_, d_cnt_, d_gs_, d_ge_, d_act_, d_stage_, d_obs_, d_gidx_,
                     d_wkey_, d_wval_, d_wkey_alt_, d_wval_alt_, d_wptr_, d_wimp_, d_wred_, d_wrot_};
     for (void* p : ptrs) if (p) cudaFree(p);
@@ -1618,12 +1776,14 @@ int MixedEngine::init_from(const std::vector<SceneSource>& src, const MixedEngin
     tune_pending_ = opts.autotune != 0;
     xs_stored_ = opts.stored_splits != 0;
     split_tick_ = opts.split_tick != 0;
+    quiet_ok_ = opts.full_walks == 0;
     if (prev) {                    // a repacked engine keeps the tuning of the one it replaces
         skin_frac_ = prev->skin_frac_;
         cell_scale_ = prev->cell_scale_;
         tpb_ = prev->tpb_;
         xs_stored_ = prev->xs_stored_;
         split_tick_ = prev->split_tick_;
+        quiet_ok_ = prev->quiet_ok_;
         tune_pending_ = prev->tune_pending_;
     }
     if (src.empty()) return fail(VEDO_ERR_INVALID_SCENE, "empty batch");
@@ -1751,6 +1911,7 @@ int MixedEngine::init_from(const std::vector<SceneSource>& src, const MixedEngin
     if (np_ > META_PI) return fail(VEDO_ERR_INVALID_SCENE, "too many interaction-model pairs in one batch (2^24)");
     // ---- device
     MCK(cudaSetDevice(opts.device));
+    MCK(cudaDeviceGetAttribute(&sms_, cudaDevAttrMultiProcessorCount, opts.device));
     MCK(cudaStreamCreateWithFlags(&stream_, cudaStreamNonBlocking));
     for (auto& e : ev_) MCK(cudaEventCreate(&e));
     auto up = [&](auto** d, const auto& v) -> int {
@@ -1776,6 +1937,9 @@ int MixedEngine::init_from(const std::vector<SceneSource>& src, const MixedEngin
     MCK(mal(&d_scenes_, sc_.size()));
     MCK(mal(&d_sred_, 8 * sc_.size()));
     MCK(mal(&d_work_, n_));
+    MCK(mal(&d_clear_, n_));
+    MCK(mal(&d_qcnt_, n_));
+    MCK(cudaMemset(d_qcnt_, 0, n_));
     for (int b = 0; b < 2; ++b) {
         MCK(mal(&d_xs_[b], 2 * (size_t)n_));
         MCK(mal(&d_x_[b], n_));
@@ -1784,13 +1948,13 @@ int MixedEngine::init_from(const std::vector<SceneSource>& src, const MixedEngin
     }
     MCK(mal(&d_v64_, n_)); MCK(mal(&d_w64_, n_)); MCK(mal(&d_ox_, n_)); MCK(mal(&d_oz_, n_));
     MCK(mal(&d_imp_, n_)); MCK(mal(&d_aimp_, n_)); MCK(mal(&d_pos32_, n_)); MCK(mal(&d_wall32_, n_));
-    MCK(mal(&d_red_, 16)); MCK(mal(&d_disp_, 2)); MCK(mal(&d_err_, 1));
+    MCK(mal(&d_red_, 16)); MCK(mal(&d_disp_, 4)); MCK(mal(&d_err_, 1));
     MCK(mal(&d_key_, n_)); MCK(mal(&d_key_alt_, n_)); MCK(mal(&d_sid_, n_)); MCK(mal(&d_sid_alt_, n_));
     MCK(mal(&d_cnt_, (size_t)n_ + 1));
     MCK(mal(&d_stage_, 7 * 3 * (size_t)n_));
     MCK(mal(&d_obs_, (size_t)(nblk(n_) + 2) * 16 + 64));
     MCK(cudaMemset(d_red_, 0, 64));
-    MCK(cudaMemset(d_disp_, 0, 8));
+    MCK(cudaMemset(d_disp_, 0, 16));
     if (prev) {
         for (int k = 0; k < 3; ++k) origin_[k] = prev->origin_[k];
     } else {
@@ -1938,8 +2102,9 @@ TickArgs MixedEngine::args(bool write_imp) {
     a.write_imp = write_imp ? 1 : 0;
     a.vmax_bits = d_red_ + 8;
     a.pos32 = d_pos32_;
-    a.disp = d_disp_ + cur_;
-    a.half_skin = 0.5f * skin_min_;
+    a.disp = d_disp_ + 2 * cur_;
+    a.skin = skin_min_;
+    a.skin_w = WALL_SKIN * skin_min_;
     a.reach = d_reach_;
     a.wall32 = d_wall32_;
     a.wimp = d_wimp_;
@@ -1951,6 +2116,8 @@ TickArgs MixedEngine::args(bool write_imp) {
     a.work = split_tick_ ? d_work_ : nullptr;
     a.nwork = d_red_ + 14;
     a.mf = d_mf_;
+    a.clear = d_clear_;
+    a.qcnt = d_qcnt_;
     return a;
 }
 
@@ -2069,7 +2236,9 @@ int MixedEngine::rebuild() {
     k_carry<<<nblk(n_), TPB, 0, stream_>>>(n_, L.ptr, L.ent, L.slot, O.ptr, O.ent, O.slot, O.h[cur_], O.f[cur_],
                                            L.h[cur_], L.f[cur_], L.h[cur_ ^ 1], L.f[cur_ ^ 1],
                                            O.ent != nullptr ? 1 : 0);
-    own += 2;
+    k_clear<<<nblk(n_), TPB, 0, stream_>>>(n_, L.ptr, L.ent, L.meta, d_model_of_, d_models_, d_pos32_, d_wall32_,
+                                           d_reach_, d_clear_, d_qcnt_, quiet_ok_ ? 1 : 0);
+    own += 3;
     // per-wall entry lists for the wall impulse output
     if (!glob_.empty()) {
         k_wall_count<<<nblk(n_), TPB, 0, stream_>>>(n_, L.ptr, L.ent, d_cnt_);
@@ -2117,7 +2286,7 @@ int MixedEngine::rebuild() {
     }
     int herr = 0;
     MCK(cudaMemcpyAsync(&herr, d_err_, 4, cudaMemcpyDeviceToHost, stream_));
-    MCK(cudaMemsetAsync(d_disp_, 0, 8, stream_));
+    MCK(cudaMemsetAsync(d_disp_, 0, 16, stream_));
     MCK(cudaStreamSynchronize(stream_));
     MCK(cudaGetLastError());
     if (herr) return fail(VEDO_ERR_CUDA, "mixed form: asymmetric neighbour lists");
@@ -2142,16 +2311,23 @@ void MixedEngine::launch_step(bool write_imp) {
     if (profiling_ && pev_used_ + 3 <= pev_.size()) {
         pe = &pev_[pev_used_];
         pev_used_ += 3;
-        cudaEventRecord(pe[0], stream_);
+        // external records while capturing (the flag is valid only then): a captured step keeps
+        // them as event nodes
+        cudaEventRecordWithFlags(pe[0], stream_, ev_flags_);
     }
+    unsigned nb_full = nb;
     if (split_tick_) {              // light tick over all spheres, then the full tick over the deferred
-        cudaMemsetAsync(a.nwork, 0, 4, stream_);
+        // (the worklist count is zeroed by k_walls at the end of every step)
         if (xs_stored_) k_tick_light<true><<<nblk(n_), TPB, 0, stream_>>>(a);
         else k_tick_light<false><<<nblk(n_), TPB, 0, stream_>>>(a);
         ++launches_;
+        // the full tick at its residency (128 registers: 16 warps per SM) strides over the worklist
+        nb_full = std::min<unsigned>(nb, (unsigned)sms_ * 512u / (unsigned)tpb_);
     }
-#define VEDO_TICK(L)                                                         \
-    (xs_stored_ ? k_tick<L, true><<<nb, tpb_, 0, stream_>>>(a) : k_tick<L, false><<<nb, tpb_, 0, stream_>>>(a))
+#define VEDO_TICK(L)                                                                                        \
+    (split_tick_ ? (xs_stored_ ? k_tick_work<L, true><<<nb_full, tpb_, 0, stream_>>>(a)                     \
+                               : k_tick_work<L, false><<<nb_full, tpb_, 0, stream_>>>(a))                   \
+                 : (xs_stored_ ? k_tick<L, true><<<nb, tpb_, 0, stream_>>>(a) : k_tick<L, false><<<nb, tpb_, 0, stream_>>>(a)))
     switch (law_) {
     case IS_BSDBF: VEDO_TICK(IS_BSDBF); break;
     case IS_BTSDBF: VEDO_TICK(IS_BTSDBF); break;
@@ -2162,7 +2338,7 @@ void MixedEngine::launch_step(bool write_imp) {
     }
 #undef VEDO_TICK
     ++launches_;
-    if (pe) cudaEventRecord(pe[1], stream_);
+    if (pe) cudaEventRecordWithFlags(pe[1], stream_, ev_flags_);
     if (write_imp && !glob_.empty()) {
         const uint32_t ng = (uint32_t)glob_.size();
         cudaMemsetAsync(d_wred_, 0, (size_t)ng * (8 + 48), stream_);
@@ -2178,16 +2354,16 @@ void MixedEngine::launch_step(bool write_imp) {
     }
     k_walls<<<nblk(std::max<size_t>(glob_.size(), 1)), TPB, 0, stream_>>>(
         (uint32_t)glob_.size(), d_glob_, d_model_of_, d_models_, d_scenes_, d_scene_of_, a.xA, a.xB, d_v64_, d_w64_,
-        a.v32A, a.v32B, a.w32A, a.w32B, d_ox_, d_oz_, dt_max_, d_red_ + 8, d_disp_ + cur_, d_disp_ + (cur_ ^ 1),
-        0.5f * skin_min_, d_red_ + 12, d_wrot_, d_red_ + 11, d_wall32_);
+        a.v32A, a.v32B, a.w32A, a.w32B, d_ox_, d_oz_, dt_max_, d_red_ + 8, d_disp_ + 2 * cur_,
+        d_disp_ + 2 * (cur_ ^ 1), skin_min_, WALL_SKIN * skin_min_, d_red_ + 12, d_wrot_, d_red_ + 11, d_wall32_, d_red_ + 14);
     ++launches_;
-    if (pe) cudaEventRecord(pe[2], stream_);
+    if (pe) cudaEventRecordWithFlags(pe[2], stream_, ev_flags_);
     cur_ ^= 1;
 }
 
 // `chunk` steps, then one read of the displacement bound and of the held-step count.  A full
 // check interval without impulse output replays a CUDA graph captured once per list.
-int MixedEngine::step_chunk(uint32_t chunk, bool imp_last, float* disp_after) {
+int MixedEngine::step_chunk(uint32_t chunk, bool imp_last, float* use_after) {
     const uint32_t ci = opts_.check_interval;
     if (profiling_ && pev_.size() < 3 * (size_t)ci) {
         while (pev_.size() < 3 * (size_t)ci) {
@@ -2197,30 +2373,35 @@ int MixedEngine::step_chunk(uint32_t chunk, bool imp_last, float* disp_after) {
         }
     }
     pev_used_ = 0;
-    if (opts_.graphs && !profiling_ && chunk == ci && !imp_last) {
+    if (opts_.graphs && chunk == ci && !imp_last) {
         const int c0 = cur_;
-        if (!graph_[c0]) {
+        const int gi = c0 + (profiling_ ? 2 : 0);
+        if (!graph_[gi]) {
             cudaGraph_t g = nullptr;
             const uint64_t l0 = launches_;
             MCK(cudaStreamBeginCapture(stream_, cudaStreamCaptureModeThreadLocal));
+            ev_flags_ = cudaEventRecordExternal;
             for (uint32_t k = 0; k < chunk; ++k) launch_step(false);
+            ev_flags_ = cudaEventRecordDefault;
             const cudaError_t ce = cudaStreamEndCapture(stream_, &g);
             launches_ = l0;
             cur_ = c0;
             if (ce != cudaSuccess) return cuda_fail(ce, "cudaStreamEndCapture");
-            const cudaError_t ie = cudaGraphInstantiate(&graph_[c0], g, 0);
+            pev_used_ = 0;
+            const cudaError_t ie = cudaGraphInstantiate(&graph_[gi], g, 0);
             cudaGraphDestroy(g);
             if (ie != cudaSuccess) return cuda_fail(ie, "cudaGraphInstantiate");
         }
-        MCK(cudaGraphLaunch(graph_[c0], stream_));
+        MCK(cudaGraphLaunch(graph_[gi], stream_));
+        if (profiling_) pev_used_ = 3 * chunk;           // the graph records every step's events
         launches_ += (uint64_t)chunk * (split_tick_ ? 3 : 2);
         if (chunk & 1) cur_ ^= 1;
     } else {
         for (uint32_t k = 0; k < chunk; ++k) launch_step(imp_last && k + 1 == chunk);
     }
-    float disp = 0.0f;
+    float dd[2] = {0.0f, 0.0f};
     unsigned held = 0;
-    MCK(cudaMemcpyAsync(&disp, d_disp_ + cur_, 4, cudaMemcpyDeviceToHost, stream_));
+    MCK(cudaMemcpyAsync(dd, d_disp_ + 2 * cur_, 8, cudaMemcpyDeviceToHost, stream_));
     MCK(cudaMemcpyAsync(&held, d_red_ + 11, 4, cudaMemcpyDeviceToHost, stream_));
     MCK(cudaStreamSynchronize(stream_));
     for (uint32_t q = 0; q + 3 <= pev_used_; q += 3) {   // profiling: tick and wall kernel times
@@ -2240,18 +2421,19 @@ int MixedEngine::step_chunk(uint32_t chunk, bool imp_last, float* disp_after) {
         for (uint32_t k = 0; k < taken; ++k) S.t += S.dt;     // SystemParameter::NextStep (SystemParameter.h:113-116), once per step
         S.steps += taken;
     }
-    const float half_skin = 0.5f * skin_min_;
-    if (held || disp > half_skin) {
+    // the share of the list's life used so far: 1 = the next step would be an identity step
+    const float use = std::max(2.0f * dd[0] / skin_min_, (dd[0] + dd[1]) / (WALL_SKIN * skin_min_));
+    if (held || list_spent(dd[0], dd[1], skin_min_, WALL_SKIN * skin_min_) || use > 1.0f) {
         // held steps are taken again after the rebuild; a bound already past half the skin
         // would hold the next step, and contact queries need a complete list too
         need_rebuild_ = true;
     } else if (since_rebuild_ % ci == 0) {
         // Rebuild before the bound can reach half the skin: the bound so far plus twice its
         // mean growth per step over the next check interval.
-        const float growth = disp / (float)since_rebuild_;
-        if (disp + 2.0f * growth * (float)ci > half_skin) need_rebuild_ = true;
+        const float growth = use / (float)since_rebuild_;
+        if (use + 2.0f * growth * (float)ci > 1.0f) need_rebuild_ = true;
     }
-    if (disp_after) *disp_after = disp;
+    if (use_after) *use_after = use;
     return (int)taken == (int)chunk ? VEDO_OK : -(int)(chunk - taken);
 }
 
@@ -2281,20 +2463,20 @@ int MixedEngine::autotune(uint32_t max_steps, uint32_t* taken) {
     };
     auto timed_chunk = [&](float* ms_per_step, float* growth) -> int {
         const uint64_t r0 = round_;
-        float disp = 0.0f;
+        float use = 0.0f;
         // an untimed chunk first: it captures the graph of this configuration
         int wrc = step_chunk(ci, false, nullptr);
         if (wrc > 0) return wrc;
         if (need_rebuild_ && (wrc = rebuild()) != VEDO_OK) return wrc;
         MCK(cudaEventRecord(e0, stream_));
-        int rc = step_chunk(ci, false, &disp);
+        int rc = step_chunk(ci, false, &use);
         if (rc > 0) return rc;
         MCK(cudaEventRecord(e1, stream_));
         MCK(cudaEventSynchronize(e1));
         float ms = 0.0f;
         MCK(cudaEventElapsedTime(&ms, e0, e1));
         *ms_per_step = ms / (float)ci;
-        if (growth) *growth = since_rebuild_ ? disp / (float)since_rebuild_ : 0.0f;
+        if (growth) *growth = since_rebuild_ ? use / (float)since_rebuild_ : 0.0f;
         *taken += (uint32_t)(round_ - r0);
         return VEDO_OK;
     };
@@ -2349,8 +2531,8 @@ int MixedEngine::autotune(uint32_t max_steps, uint32_t* taken) {
         float trb = 0.0f, t = 0.0f, growth = 0.0f;
         if ((rc = timed_rebuild(&trb)) != VEDO_OK) return rc;
         if ((rc = timed_chunk(&t, &growth)) != VEDO_OK) return rc;
-        // steps until the bound nears half the skin at this growth (the rebuild rule's margin)
-        const float life = growth > 0.0f ? std::max((float)ci, 0.5f * skin_min_ / growth - 2.0f * (float)ci) : 1e6f;
+        // steps until the list's life is used up at this growth (the rebuild rule's margin)
+        const float life = growth > 0.0f ? std::max((float)ci, 1.0f / growth - 2.0f * (float)ci) : 1e6f;
         const float cost = t + trb / life;
         if (cost < best) { best = cost; best_skin = f; }
     }
@@ -2426,6 +2608,18 @@ int MixedEngine::get_state(const vedo_state_view& v) {
     }
     MCK(cudaStreamSynchronize(stream_));
     MCK(cudaGetLastError());
+    return VEDO_OK;
+}
+
+int MixedEngine::quiet_spheres(uint64_t* count) {
+    *count = 0;
+    if (need_rebuild_ || !n_) return VEDO_OK;         // the next step starts with a new list
+    unsigned c = 0;
+    MCK(cudaMemsetAsync(d_red_ + 15, 0, 4, stream_));
+    k_quiet_count<<<nblk(n_), TPB, 0, stream_>>>(n_, d_clear_, d_qcnt_, d_disp_ + 2 * cur_, d_red_ + 15);
+    MCK(cudaMemcpyAsync(&c, d_red_ + 15, 4, cudaMemcpyDeviceToHost, stream_));
+    MCK(cudaStreamSynchronize(stream_));
+    *count = c;
     return VEDO_OK;
 }
 

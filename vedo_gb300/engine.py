@@ -82,7 +82,7 @@ STATE_FIELDS = ("position", "velocity", "angular_velocity", "orientation_x", "or
 
 
 def _opts(up_iact, record, precision, device, prefix, skin, check_interval, tick_block=None, cell_scale=None,
-          autotune=False, graphs=True, stored_splits=False, split_tick=False) -> EngineOpts:
+          autotune=False, graphs=True, stored_splits=False, split_tick=False, full_walks=False) -> EngineOpts:
     opts = EngineOpts()
     lib().vedo_gpu_default_opts(C.byref(opts))
     opts.up_iact, opts.record, opts.precision, opts.device = up_iact, record, precision, device
@@ -98,6 +98,7 @@ def _opts(up_iact, record, precision, device, prefix, skin, check_interval, tick
     opts.graphs = 1 if graphs else 0
     opts.stored_splits = 1 if stored_splits else 0
     opts.split_tick = 1 if split_tick else 0
+    opts.full_walks = 1 if full_walks else 0
     opts.output_prefix = prefix
     return opts
 
@@ -114,11 +115,11 @@ class GpuEngine:
                  device: int = 0, output_prefix: Optional[str] = None, skin: Optional[float] = None,
                  check_interval: Optional[int] = None, tick_block: Optional[int] = None,
                  cell_scale: Optional[float] = None, autotune: bool = False, graphs: bool = True,
-                 stored_splits: bool = False, split_tick: bool = False):
+                 stored_splits: bool = False, split_tick: bool = False, full_walks: bool = False):
         L = lib()
         self._prefix = output_prefix.encode() if output_prefix else None
         opts = _opts(up_iact, record, precision, device, self._prefix, skin, check_interval, tick_block, cell_scale,
-                     autotune, graphs, stored_splits, split_tick)
+                     autotune, graphs, stored_splits, split_tick, full_walks)
         h = C.c_void_p()
         if isinstance(scene, (str, bytes, os.PathLike)):
             path = os.fsencode(scene)
@@ -210,6 +211,12 @@ class GpuEngine:
         return {"skin": float(sk.value), "cell_scale": float(cs.value), "tick_block": int(tb.value),
                 "stored_splits": bool(ss.value), "split_tick": bool(st.value)}
 
+    def quiet_spheres(self) -> int:
+        """Spheres whose next step skips the neighbour-list walk (MIXED form; 0 for FP64)."""
+        c = C.c_uint64(0)
+        self._check(lib().vedo_gpu_quiet_spheres(self.h, C.byref(c)))
+        return int(c.value)
+
     def set_profiling(self, on: bool):
         lib().vedo_gpu_set_profiling(self.h, 1 if on else 0)
 
@@ -255,11 +262,12 @@ class BatchEngine(GpuEngine):
 
     def __init__(self, scene_list, device: int = 0, skin: Optional[float] = None,
                  check_interval: Optional[int] = None, tick_block: Optional[int] = None,
-                 cell_scale: Optional[float] = None, autotune: bool = False, graphs: bool = True):
+                 cell_scale: Optional[float] = None, autotune: bool = False, graphs: bool = True,
+                 full_walks: bool = False):
         L = lib()
         self._prefix = None
         opts = _opts(1, 0, _abi.PRECISION_MIXED, device, None, skin, check_interval, tick_block, cell_scale,
-                     autotune, graphs)
+                     autotune, graphs, full_walks=full_walks)
         descs, keeps = [], []
         for sc in scene_list:
             if isinstance(sc, (str, bytes, os.PathLike)):
