@@ -32,7 +32,7 @@ sys.path.insert(0, ROOT)
 METRIC = "particle-steps/s on 1 GB300 (mixed vs FP64 at stated error); serving p50/p99 ms"
 UNIT = "particle-steps/s"
 WORKLOAD = "hertz_drum_1M"
-TUNE_STEPS = 250
+TUNE_STEPS = 400
 
 
 def parse():
@@ -370,6 +370,9 @@ def ours(args, dist):
                 if traffic else None,
                 "dram_frac": traffic / (t_tick * 1e-3) / 1e9 / peak if traffic else None,
                 "tick_ms": t_tick, "walls_ms": kern["object_ms"] / kern["steps"],
+                "profile_pass": {"steps": kern["steps"], "launches": kern["launches"],
+                                 "ms_per_step": kern["total_ms"] / kern["steps"], "rebuild_ms": kern["rebuild_ms"],
+                                 "note": "graph replay with per-kernel event nodes (they add about 13 us per step)"},
                 "share_of_step": t_tick / (t_ms / args.steps), "alg_bytes_per_launch": b_alg * n}
     res = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": dist.world, "steps": args.steps,
            "warmup": args.warmup, "ms_per_step": t_ms / args.steps, "higher_is_better": True, "scaling": "weak",
@@ -420,6 +423,42 @@ def ncu_traffic(name):
     return None
 
 
+def form_errors(scene, dev, pre_steps, post_steps=200, up_iact=20):
+    """The mixed form against the FP64 engine on one scene: the FP64 engine runs `pre_steps`, both
+    forms restart from its .ido (identical positions, velocities and contact history), and after
+    one step their impulses and active contact sets are compared; after `post_steps` more steps,
+    their total energies."""
+    import numpy as np
+    from vedo_gb300.engine import GpuEngine
+    f64 = GpuEngine(scene, up_iact=up_iact, device=dev)
+    f64.run(pre_steps)
+    with tempfile.TemporaryDirectory() as td:
+        path = os.path.join(td, "w.ido")
+        f64.write_ido(path)
+        f64.close()
+        a = GpuEngine(path, up_iact=up_iact, device=dev)
+        b = GpuEngine(path, up_iact=up_iact, device=dev, precision=1)
+    a.run(1)
+    b.run(1)
+    f = ("impact", "angular_impact")
+    sa, sb = a.state(f), b.state(f)
+    out = {f"step_{k}_rel_l2": float(np.linalg.norm(sa[k] - sb[k]) / max(np.linalg.norm(sa[k]), 1e-300)) for k in f}
+    ia, ib = a.interactions(), b.interactions()
+    A = set(zip(ia["first"][ia["active"] == 1].tolist(), ia["second"][ia["active"] == 1].tolist()))
+    B = set(zip(ib["first"][ib["active"] == 1].tolist(), ib["second"][ib["active"] == 1].tolist()))
+    out["contact_set_identical"] = A == B
+    out["contacts"] = len(A)
+    a.run(post_steps)
+    b.run(post_steps)
+    oa, ob = a.observables(), b.observables()
+    ea, eb = oa[0] + oa[1] + oa[2], ob[0] + ob[1] + ob[2]
+    out[f"energy_rel_after_{post_steps}_steps"] = abs(ea - eb) / max(abs(ea), 1e-300)
+    out["from_step"] = pre_steps
+    a.close()
+    b.close()
+    return out
+
+
 def batch_workload(args, dist, dev):
     """The batched workload: hopper scenes of 1e3..5e4 spheres in one autotuned engine whose
     check intervals replay as CUDA graphs (one fused tick launch per step over all scenes)."""
@@ -428,6 +467,9 @@ def batch_workload(args, dist, dev):
     from vedo_gb300.engine import BatchEngine
     hs = scenes.hopper_batch(args.batch_scenes, seed=2025 + dist.rank, steps=5000)
     n = sum(scene_particles(h) for h in hs)
+    # errors against the FP64 engine on four of the scenes (a scene's results in the batch are
+    # those of the scene alone, bit for bit), from step 1000 of the run
+    errs = [] if args.no_profile_pass else [form_errors(hs[q], dev, 1000) for q in (0, 1, 2, 3)]
     b = BatchEngine(hs, device=dev, autotune=True)
     del hs
     b.run(TUNE_STEPS)                # autotuning + warm-up; the tuned settings stay
@@ -440,8 +482,14 @@ def batch_workload(args, dist, dev):
     out = {"workload": f"hopper_batch_{args.batch_scenes}", "scenes": args.batch_scenes, "particles": n,
            "value": total * args.batch_steps / (t * 1e-3), "unit": UNIT, "ms_per_step": t / args.batch_steps,
            "steps": args.batch_steps, "gpu_launches": prof["launches"], "tuning": b.tuning(),
+           "errors_mixed_vs_fp64": {"scenes": errs,
+                                    "max_step_impact_rel_l2": max((e["step_impact_rel_l2"] for e in errs), default=None),
+                                    "all_contact_sets_identical": all(e["contact_set_identical"] for e in errs),
+                                    "max_energy_rel": max((e["energy_rel_after_200_steps"] for e in errs),
+                                                          default=None)},
            "note": f"steps {TUNE_STEPS}..{TUNE_STEPS + args.batch_steps} of the configured 5000-step run; mixed form, "
-                   "CUDA-graph check intervals, autotuned tick block, skin and cell scale"}
+                   "CUDA-graph check intervals, autotuned tick block, skin and cell scale; errors on scenes 0-3 "
+                   "alone (bit-identical to their batch slices)"}
     b.close()
     return out
 
@@ -452,6 +500,12 @@ def bed_workload(args, dist, dev):
     import torch
     from vedo_gb300 import scenes
     from vedo_gb300.engine import GpuEngine
+    errs = None
+    if not args.no_profile_pass:
+        small = scenes.compressed_bed(n=1_000_000, box=0.1, cylinders=2, seed=5 + dist.rank)
+        errs = form_errors(small, dev, 1500)          # the top plate reaches the bed near step 1000
+        errs["scene"] = "compressed_bed of 1M spheres (same construction and depth; 0.1 x 0.1 m floor, 2 rods)"
+        del small
     sc = scenes.compressed_bed(n=args.bed_n, seed=5 + dist.rank)
     n = scene_particles(sc)
     e = GpuEngine(sc, device=dev, precision=1, autotune=True)
@@ -477,6 +531,7 @@ def bed_workload(args, dist, dev):
     out = {"workload": f"compressed_bed_{args.bed_n // 1_000_000}M", "particles": n,
            "value": total * args.bed_steps / (t * 1e-3), "unit": UNIT, "ms_per_step": t / args.bed_steps,
            "steps": args.bed_steps, "gpu_launches": prof["launches"], "tuning": e.tuning(), "z_pp": z,
+           "errors_mixed_vs_fp64": errs,
            "tick_roofline": {"achieved": ach, "peak": peak, "unit": "GB/s", "frac": ach / peak, "tick_ms": t_tick,
                              "alg_bytes_per_particle_step": b_alg, "traffic": traffic,
                              "dram_frac": traffic / (t_tick * 1e-3) / 1e9 / peak if traffic else None,

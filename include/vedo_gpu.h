@@ -258,6 +258,13 @@ uint64_t vedo_gpu_steps_remaining(const vedo_gpu_engine* e);
  * walk).  A measure of how much of the list the skin keeps idle.  FP64 form: 0. */
 int vedo_gpu_quiet_spheres(vedo_gpu_engine* e, uint64_t* count);
 
+/* MIXED form: the neighbour list's state.  out[0] = steps since its rebuild, out[1] = rebuilds
+ * so far, out[2] = bound on any sphere's displacement relative to its scene's drifting frame
+ * (free fall from the spheres' velocity midrange at the rebuild), out[3] = bound on any
+ * sphere's displacement, out[4] = bound on any orbital wall's approach, out[5] = the share of
+ * the list's life used (1 = the next step rebuilds).  FP64 form: zeros. */
+int vedo_gpu_list_status(vedo_gpu_engine* e, double out[6]);
+
 /* Write world + active-contact records as a reference .ido
  * (DOWorld::WriteIDO, DOWorld_RWIDO.cpp:149-202). */
 int vedo_gpu_write_ido(vedo_gpu_engine* e, const char* path);

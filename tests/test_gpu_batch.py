@@ -85,7 +85,7 @@ def test_autotuned_graph_batch_equals_plain_alone(engine_lib):
     """Hoppers of uneven sizes in one autotuned batch whose check intervals replay as CUDA
     graphs, against each hopper alone with fixed settings and direct launches: bit-identical,
     because neither the tuned skin, cell scale and block size nor graph replay change a result."""
-    steps = 300
+    steps = 500                                   # the tuner needs about 400 steps of the call
     hs = [scenes.hopper(n=n, seed=s, friction=mu, restitution=e, orifice=w, steps=steps)
           for n, s, mu, e, w in scenes.hopper_params(4, seed=7, n_lo=1000, n_hi=6000)]
     b = engine_lib.BatchEngine(hs, autotune=True)

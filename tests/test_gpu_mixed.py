@@ -212,3 +212,48 @@ def test_profiled_graph_replay_times_kernels_without_changing_results(engine_lib
     p = b.last_run_profile()
     assert p["pair_ms"] > 0.0 and p["object_ms"] > 0.0 and p["pair_ms"] + p["object_ms"] <= p["total_ms"]
     _same_run(a, b)
+
+
+def test_set_state_keeps_the_list_when_the_bound_absorbs_the_jump(engine_lib):
+    """vedo_gpu_set_state adds the spheres' largest jump to the displacement bound instead of
+    rebuilding (a moved wall, or a jump the skin cannot absorb, still rebuilds).  A wide-skin
+    engine that keeps its list and a tiny-skin one that rebuilds every step or two stay
+    bit-identical through unchanged, slightly moved and far moved states."""
+    sc = scenes.hopper(n=4000, steps=3000)
+    a = engine_lib.GpuEngine(sc, precision=1, skin=0.5, split_tick=True)
+    c = engine_lib.GpuEngine(sc, precision=1, skin=0.002, check_interval=1)
+    fields = ("position", "velocity", "angular_velocity")
+    for jump in (0.0, 2e-7, 3e-4):
+        a.run(37)
+        c.run(37)
+        sa, sc_ = a.state(fields), c.state(fields)
+        for k in fields:
+            assert np.array_equal(sa[k], sc_[k]), (jump, k)
+        sa["position"][5] += jump
+        sa["velocity"][7] *= 1.5
+        a.set_state(**sa)
+        c.set_state(**sa)
+        a.run(25)
+        c.run(25)
+        ra, rc = a.state(), c.state()
+        for k in ("position", "velocity", "angular_velocity", "impact", "angular_impact"):
+            assert np.array_equal(ra[k], rc[k]), (jump, k)
+        assert _active_history(a) == _active_history(c)
+
+
+def test_spinning_plate_corners_reach_spheres_beyond_its_list(engine_lib):
+    """A plate spinning in its own plane keeps its plane but sweeps its corners: spheres near the
+    plane outside its inscribed circle make the wall's approach bound the full |omega| R, so a
+    moderate skin (spheres first listed late) and a tiny one (rebuilt every step or two) stay
+    bit-identical, and the corners do hit the spheres."""
+    sc = scenes.spinning_plate()
+    a = engine_lib.GpuEngine(sc, precision=1, skin=0.05, split_tick=True)
+    b = engine_lib.GpuEngine(sc, precision=1, skin=0.002, check_interval=1)
+    for n in (1000, 700, 700, 599):
+        a.run(n)
+        b.run(n)
+        sa, sb = a.state(), b.state()
+        for k in ("position", "velocity", "angular_velocity", "impact", "angular_impact"):
+            assert np.array_equal(sa[k], sb[k]), (n, k)
+    v = a.state(("velocity",))["velocity"][:8]
+    assert (np.linalg.norm(v, axis=1) > 0.1).sum() >= 4          # the first four were struck

@@ -173,6 +173,11 @@ int vedo_gpu_quiet_spheres(vedo_gpu_engine* e, uint64_t* count) {
     return e->p->quiet_spheres(count);
 }
 
+int vedo_gpu_list_status(vedo_gpu_engine* e, double out[6]) {
+    if (!e || !out) return VEDO_ERR_INVALID_ARGUMENT;
+    return e->p->list_status(out);
+}
+
 int vedo_gpu_write_ido(vedo_gpu_engine* e, const char* path) {
     if (!e || !path) return VEDO_ERR_INVALID_ARGUMENT;
     return e->p->write_ido(path);

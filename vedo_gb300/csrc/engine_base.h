@@ -35,6 +35,10 @@ public:
         *count = 0;
         return VEDO_OK;
     }
+    virtual int list_status(double out[6]) {
+        for (int k = 0; k < 6; ++k) out[k] = 0.0;
+        return VEDO_OK;
+    }
 };
 
 // count of t += dt steps from t until t >= t_stop (SystemParameter::NextStep, SimMediator.cpp:839-841)

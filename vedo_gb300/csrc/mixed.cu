@@ -64,6 +64,10 @@ constexpr uint32_t META_BOND = 1u << 26;
 constexpr uint32_t META_OWNER = 1u << 27;
 constexpr uint32_t META_SLAVE = 1u << 28;
 constexpr uint32_t META_MOVING = 1u << 29;   // the entry's other object is an orbital wall
+// A wall entry whose sphere projects inside the plate (or along the rod's segment) with a
+// margin that outlasts the list: its distance is the distance to the plane (or axis), which
+// only the normal (or transverse) part of the sphere's displacement changes.
+constexpr uint32_t META_INTERIOR = 1u << 30;
 // Orbital walls move on their own schedule (a drum's end plates turn at a fixed rate), so their
 // entries are gathered with a wider skin and carry their own displacement bound; sphere pairs
 // and fixed walls keep the sphere bound alone.
@@ -336,6 +340,9 @@ struct SceneDev {
     uint32_t nc[3];
     float lo[3], inv_h;
     double dt;
+    // The scene's drifting frame since the last rebuild: velocity u0 + gdt (k + 1/2) in step k
+    // (free fall under the scene's field from the spheres' velocity midrange at the rebuild)
+    float u0[3], gdt[3];
 };
 
 __device__ __forceinline__ uint32_t pidx(const SceneDev& S, uint32_t mg_slave, uint32_t mg_master) {
@@ -375,7 +382,10 @@ struct TickArgs {
     int write_imp;
     unsigned* vmax_bits;
     const float4* pos32;           // positions at the last rebuild (FP32 offsets)
-    const float* disp;             // [2]: bounds on any sphere's and any orbital wall's displacement since the rebuild
+    // [4]: bounds since the rebuild on any sphere's displacement relative to its scene's frame,
+    // on any sphere's displacement, on any orbital wall's displacement; steps since the rebuild
+    // (integer bits)
+    const float* disp;
     float skin, skin_w;            // list skins: sphere pairs and fixed walls; orbital walls
     const float* reach;
     const float4* wall32;
@@ -388,17 +398,21 @@ struct TickArgs {
     uint32_t* work;                // split tick: spheres deferred to the full tick (else nullptr)
     uint32_t* nwork;
     const float4* mf;              // [nm][2]: field + external impulse per step, 1/m~; 2.5/(m~ r^2)
-    const float* clear;            // [n] per sphere: every prefilter test of its list says "apart" for pad <= clear
+    unsigned* vrel_bits;           // max over spheres of the speed relative to the scene's frame
+    const float2* clear;           // [n] per sphere: every prefilter test of its list says "apart" for
+                                   // sphere-pair pads <= x and fixed-wall pads <= y
     uint8_t* qcnt;                 // [n] consecutive clean walks (0..2) since the last rebuild
 };
 
-// A step whose list may be incomplete is an identity step: a sphere pair may have closed by
-// both spheres' travel, a sphere-wall pair by the sphere's and an orbital wall's.
-__host__ __device__ __forceinline__ bool list_spent(float ds, float dw, float skin, float skin_w) {
-    return 2.0f * ds > skin || ds + dw > skin_w;
+// A step whose list may be incomplete is an identity step.  A sphere pair may have closed by
+// both spheres' displacements relative to their scene's frame (the frame's own motion moves
+// both alike), a sphere and a fixed wall by the sphere's displacement, a sphere and an orbital
+// wall by that and the wall's.
+__host__ __device__ __forceinline__ bool list_spent(float drel, float dabs, float dw, float skin, float skin_w) {
+    return 2.0f * drel > skin || dabs > skin || dabs + dw > skin_w;
 }
 __device__ __forceinline__ bool held_step(const TickArgs& a) {
-    return list_spent(a.disp[0], a.disp[1], a.skin, a.skin_w);
+    return list_spent(a.disp[0], a.disp[1], a.disp[2], a.skin, a.skin_w);
 }
 
 // identity step: the next buffers receive the current state and history unchanged
@@ -456,7 +470,14 @@ __device__ __forceinline__ uint32_t prefilter_group(const TickArgs& a, uint32_t 
             continue;
         }
         const float4 ws = wall ? a.wall32[j] : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
-        const float pk = (meta & META_MOVING) ? a.disp[0] + a.disp[1] : pad;
+        // a wall entry: the sphere's whole displacement, or for an interior one (the smaller of the
+        // two bounds) the part across the wall: the frame's drift across it (the wall's w,
+        // k_walls) plus the deviation from the frame; an orbital wall's approach adds
+        float pk = pad;
+        if (wall) {
+            pk = (meta & META_INTERIOR) ? fminf(a.disp[1], a.disp[0] + ws.w) : a.disp[1];
+            if (meta & META_MOVING) pk += a.disp[2];
+        }
         if (!apart32(cd, i_slave ? p32i : gp[k], i_slave ? gp[k] : p32i, ws, a.reach[meta & META_PI] + pk)) {
             exact |= 1u << k;
             continue;
@@ -481,9 +502,9 @@ __device__ __forceinline__ uint32_t prefilter_group(const TickArgs& a, uint32_t 
 }
 
 // Quiet spheres.  Between rebuilds a sphere's list, the rebuild-time positions and the fixed
-// walls' normals do not change, and the prefilter's "apart" is monotone in the pad, so one
-// number per sphere (`clear`, k_clear) settles the whole walk: with pad <= clear every entry is
-// apart.  Such a walk writes history only to clean it: an owned entry whose status is set is
+// walls' normals do not change, and the prefilter's "apart" is monotone in the pad, so two
+// numbers per sphere (`clear`, k_clear: sphere pairs, fixed walls) settle the whole walk: with
+// the pads at or below them every entry is apart.  Such a walk writes history only to clean it: an owned entry whose status is set is
 // cleaned to HF_PENDING, and a HF_PENDING one clears the other buffer.  After two consecutive
 // walks that cleaned nothing (`qcnt` = 2) both buffers of every owned entry hold a clean status
 // that a further walk rewrites with the same values, so the walk is skipped and the sphere is
@@ -496,14 +517,20 @@ __device__ __forceinline__ void note_walk(const TickArgs& a, uint32_t i, uint32_
 
 // The end of a sphere's step: field and external impulse join the compensated sum (the
 // increments dv, dw are FP32, the state update FP64), the impulses are recorded on the last
-// step of a call, and the sphere is integrated.  Returns the sphere's speed bound of the step.
-// The FP32 velocity copy is always the rounding of the FP64 velocity, so the old speed comes
-// from V.  A quiet sphere had no torque in its last two steps, so both buffers of its FP32
-// angular velocity already hold the value the copy would write.
+// step of a call, and the sphere is integrated.  Returns the squared speed bounds of the step
+// (the square roots are taken once per warp):
+//  x: the step moves the sphere by dt (V + dv/2), at most max(|V|, |V + dv|), formed in FP32
+//     from the new velocity and the increment, |V| as |vn - dv| (the margin covers roundings);
+//  y: the frame's velocity in this step is u = u0 + gdt (k + 1/2), and the sphere's step
+//     velocity vmid = vn - dv/2 is compared with it in FP32 with an allowance s for the
+//     roundings: 2 |vmid - u|^2 + 2 s^2 >= (|vmid - u| + s)^2.
+// A quiet sphere had no torque in its last two steps, so both buffers of its FP32 angular
+// velocity already hold the value the copy would write.
 template <bool XS>
-__device__ __forceinline__ float finish_sphere(const TickArgs& a, uint32_t i, bool mobile, bool quiet, double dt,
-                                               const d3& Pi, const d3& V, const float4& mf0, const float4& mf1, K3& J,
-                                               K3& JA) {
+__device__ __forceinline__ float2 finish_sphere(const TickArgs& a, uint32_t i, bool mobile, bool quiet,
+                                                const SceneDev& S, const d3& Pi, const d3& V, const float4& mf0,
+                                                const float4& mf1, K3& J, K3& JA) {
+    const double dt = S.dt;
     // DOContainer.cpp:20-27, DiscreteObject.cpp:160-163
     J.add(fm(mf0.x, mf0.y, mf0.z));
     if (a.write_imp) {
@@ -538,8 +565,15 @@ __device__ __forceinline__ float finish_sphere(const TickArgs& a, uint32_t i, bo
         }
         const float4 vn = make_float4((float)V2.x, (float)V2.y, (float)V2.z, 0.0f);
         a.v32B[i] = vn;
-        const float vx = (float)V.x, vy = (float)V.y, vz = (float)V.z;
-        return sqrtf(fmaxf(fmaf(vz, vz, fmaf(vy, vy, vx * vx)), fmaf(vn.z, vn.z, fmaf(vn.y, vn.y, vn.x * vn.x))));
+        const float ox = vn.x - dv.x, oy = vn.y - dv.y, oz = vn.z - dv.z;
+        const float vabs2 = fmaxf(fmaf(oz, oz, fmaf(oy, oy, ox * ox)), fmaf(vn.z, vn.z, fmaf(vn.y, vn.y, vn.x * vn.x)));
+        const float kh = (float)__float_as_uint(a.disp[3]) + 0.5f;
+        const float ux = fmaf(S.gdt[0], kh, S.u0[0]), uy = fmaf(S.gdt[1], kh, S.u0[1]), uz = fmaf(S.gdt[2], kh, S.u0[2]);
+        const float rx = fmaf(-0.5f, dv.x, vn.x) - ux, ry = fmaf(-0.5f, dv.y, vn.y) - uy,
+                    rz = fmaf(-0.5f, dv.z, vn.z) - uz;
+        const float sl = 1e-6f * (fabsf(vn.x) + fabsf(vn.y) + fabsf(vn.z) + fabsf(dv.x) + fabsf(dv.y) + fabsf(dv.z) +
+                                  fabsf(ux) + fabsf(uy) + fabsf(uz));
+        return make_float2(vabs2, 2.0f * fmaf(rz, rz, fmaf(ry, ry, fmaf(rx, rx, sl * sl))));
     }
     st(a.xB, i, Pi, 0.0);
     if (XS) {
@@ -548,14 +582,14 @@ __device__ __forceinline__ float finish_sphere(const TickArgs& a, uint32_t i, bo
     }
     a.v32B[i] = a.v32A[i];
     a.w32B[i] = a.w32A[i];
-    return 0.0f;
+    return make_float2(0.0f, 0.0f);
 }
 
 // One sphere's step: neighbour walk (prefilter, then the exact path in entry order), sums,
-// integration.  Returns the sphere's speed bound of the step.
+// integration.  Returns its squared speed bounds of the step.
 template <int LAW, bool XS>
-__device__ __forceinline__ float tick_sphere(const TickArgs& a, uint32_t i) {
-    float vmax_local = 0.0f;
+__device__ __forceinline__ float2 tick_sphere(const TickArgs& a, uint32_t i) {
+    float2 vmax_local = make_float2(0.0f, 0.0f);
     {
         // every load that depends on the index alone is issued here, together, so that their
         // latencies overlap; the model- and list-dependent ones follow
@@ -576,7 +610,8 @@ __device__ __forceinline__ float tick_sphere(const TickArgs& a, uint32_t i) {
             const bool mobile = M.behavior == BEH_MOBILE;
             // the clean-walk count is kept by the light tick when there is one
             const uint32_t qc = a.work ? 0u : a.qcnt[i];
-            const bool quiet = qc >= 2u && !a.write_imp && pad <= a.clear[i];
+            const float2 cl = a.clear[i];
+            const bool quiet = qc >= 2u && !a.write_imp && pad <= cl.x && a.disp[1] <= cl.y;
             bool dirty = false, any_exact = false;
             K3 J, JA;
             for (uint32_t base = e0; base < e1 && !quiet; base += TICK_GROUP) {
@@ -688,7 +723,7 @@ __device__ __forceinline__ float tick_sphere(const TickArgs& a, uint32_t i) {
                 }
             }
             if (!a.work && !quiet) note_walk(a, i, qc, dirty || any_exact);
-            vmax_local = finish_sphere<XS>(a, i, mobile, quiet, dt, Pi, V, mf0, mf1, J, JA);
+            vmax_local = finish_sphere<XS>(a, i, mobile, quiet, S, Pi, V, mf0, mf1, J, JA);
         } else if (M.scope == SCOPE_LOCAL) {
             hold_state(a, i);                      // a finished scene waits, unchanged
         }
@@ -696,17 +731,29 @@ __device__ __forceinline__ float tick_sphere(const TickArgs& a, uint32_t i) {
     return vmax_local;
 }
 
-__device__ __forceinline__ void reduce_vmax(const TickArgs& a, float vmax_local) {
+// the warp's squared speed bounds (absolute, relative to the frame): their square roots, with
+// a margin for the roundings, join the step's maxima
+__device__ __forceinline__ void reduce_vmax(const TickArgs& a, float2 v) {
 #pragma unroll
-    for (int o = 16; o > 0; o >>= 1) vmax_local = fmaxf(vmax_local, __shfl_xor_sync(0xffffffffu, vmax_local, o));
-    if ((threadIdx.x & 31) == 0 && vmax_local > 0.0f) atomicMax(a.vmax_bits, __float_as_uint(vmax_local * 1.0001f));
+    for (int o = 16; o > 0; o >>= 1) {
+        v.x = fmaxf(v.x, __shfl_xor_sync(0xffffffffu, v.x, o));
+        v.y = fmaxf(v.y, __shfl_xor_sync(0xffffffffu, v.y, o));
+    }
+    if ((threadIdx.x & 31) == 0) {
+        // the maxima only grow within a step, so a value at or below one already read (from L2)
+        // needs no atomic: most warps skip it
+        const unsigned bx = __float_as_uint(sqrtf(v.x) * 1.0001f), by = __float_as_uint(sqrtf(v.y) * 1.0001f);
+        if (v.x > 0.0f && bx > __ldcg(a.vmax_bits)) atomicMax(a.vmax_bits, bx);
+        if (v.y > 0.0f && by > __ldcg(a.vrel_bits)) atomicMax(a.vrel_bits, by);
+    }
 }
+__device__ __forceinline__ float2 fmax2(float2 a, float2 b) { return make_float2(fmaxf(a.x, b.x), fmaxf(a.y, b.y)); }
 
 // The full tick, one thread per sphere.
 template <int LAW, bool XS>
 __global__ void __launch_bounds__(TPB) k_tick(TickArgs a) {
     const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
-    float vmax_local = 0.0f;
+    float2 vmax_local = make_float2(0.0f, 0.0f);
     if (held_step(a)) {                          // the same value for every thread of the launch
         hold_state(a, t);
     } else if (t < a.n) {
@@ -719,15 +766,13 @@ __global__ void __launch_bounds__(TPB) k_tick(TickArgs a) {
 // spheres the light kernel deferred (none in a held step).
 template <int LAW, bool XS>
 __global__ void __launch_bounds__(TPB) k_tick_work(TickArgs a) {
-    float vmax_local = 0.0f;
+    float2 vmax_local = make_float2(0.0f, 0.0f);
     if (!held_step(a)) {
         const uint32_t nw = *a.nwork;
         for (uint32_t q = blockIdx.x * blockDim.x + threadIdx.x; q < nw; q += gridDim.x * blockDim.x)
-            vmax_local = fmaxf(vmax_local, tick_sphere<LAW, XS>(a, a.work[q]));
+            vmax_local = fmax2(vmax_local, tick_sphere<LAW, XS>(a, a.work[q]));
     }
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) vmax_local = fmaxf(vmax_local, __shfl_xor_sync(0xffffffffu, vmax_local, o));
-    if ((threadIdx.x & 31) == 0 && vmax_local > 0.0f) atomicMax(a.vmax_bits, __float_as_uint(vmax_local * 1.0001f));
+    reduce_vmax(a, vmax_local);
 }
 
 // The light half of the split tick: every sphere's neighbour walk in FP32 prefilter form only,
@@ -739,7 +784,7 @@ template <bool XS>
 __global__ void __launch_bounds__(TPB, 5) k_tick_light(TickArgs a) {   // 5 blocks of 256 per SM
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     const bool hold = held_step(a);
-    float vmax_local = 0.0f;
+    float2 vmax_local = make_float2(0.0f, 0.0f);
     bool defer = false;
     if (hold) {
         hold_state(a, i);
@@ -750,13 +795,13 @@ __global__ void __launch_bounds__(TPB, 5) k_tick_light(TickArgs a) {   // 5 bloc
         const uint32_t mi = a.model_of[i];
         const uint32_t si = a.scene_of[i];
         const uint32_t qc = a.qcnt[i];
-        const float clear = a.clear[i];
+        const float2 clear = a.clear[i];
         const float disp = a.disp[0];
         const ModelDev& M = a.models[mi];
         const SceneDev& S = a.scenes[si];
         if (M.scope == SCOPE_LOCAL && S.active) {
             const float pad = 2.0f * disp;
-            const bool quiet = qc >= 2u && !a.write_imp && pad <= clear;
+            const bool quiet = qc >= 2u && !a.write_imp && pad <= clear.x && a.disp[1] <= clear.y;
             if (!quiet) {                          // walk the list
                 const uint32_t e0 = a.nptr[i], e1 = a.nptr[i + 1];
                 const float4 p32i = a.pos32[i];
@@ -772,7 +817,7 @@ __global__ void __launch_bounds__(TPB, 5) k_tick_light(TickArgs a) {   // 5 bloc
                 const float4 mf0 = a.mf[2 * mj], mf1 = a.mf[2 * mj + 1];
                 K3 J, JA;
                 vmax_local = finish_sphere<XS>(a, i, a.models[mj].behavior == BEH_MOBILE, quiet,
-                                               a.scenes[a.scene_of[i]].dt, Pi, V, mf0, mf1, J, JA);
+                                               a.scenes[a.scene_of[i]], Pi, V, mf0, mf1, J, JA);
             }
         } else if (M.scope == SCOPE_LOCAL) {
             hold_state(a, i);
@@ -786,9 +831,29 @@ __global__ void __launch_bounds__(TPB, 5) k_tick_light(TickArgs a) {   // 5 bloc
         at = __shfl_sync(0xffffffffu, at, lead);
         if (defer) a.work[at + __popc(dm & ((1u << lane) - 1u))] = i;
     }
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) vmax_local = fmaxf(vmax_local, __shfl_xor_sync(0xffffffffu, vmax_local, o));
-    if ((threadIdx.x & 31) == 0 && vmax_local > 0.0f) atomicMax(a.vmax_bits, __float_as_uint(vmax_local * 1.0001f));
+    reduce_vmax(a, vmax_local);
+}
+
+// A wall's FP32 record carries in w the drift of its scene's frame across it after k steps
+// since the rebuild: |D . n| for a plate, |D x a| for a rod, D = dt k (u0 + gdt k / 2), with an
+// allowance for the roundings of the frame's per-step velocities, of this closed form and of
+// the FP32 normal; w = 0 marks a wall without a usable normal, so a valid one keeps w > 0.
+__device__ __forceinline__ float frame_drift_across(const SceneDev& S, uint32_t k, int shape, float nx, float ny,
+                                                    float nz) {
+    const float kf = (float)k, dtk = (float)S.dt * kf, hk = 0.5f * kf;
+    const float Dx = dtk * fmaf(S.gdt[0], hk, S.u0[0]), Dy = dtk * fmaf(S.gdt[1], hk, S.u0[1]),
+                Dz = dtk * fmaf(S.gdt[2], hk, S.u0[2]);
+    float across;
+    if (shape == SHAPE_PLATE) {
+        across = fabsf(fmaf(Dz, nz, fmaf(Dy, ny, Dx * nx)));
+    } else {
+        const float cx = fmaf(Dy, nz, -Dz * ny), cy = fmaf(Dz, nx, -Dx * nz), cz = fmaf(Dx, ny, -Dy * nx);
+        across = sqrtf(fmaf(cz, cz, fmaf(cy, cy, cx * cx)));
+    }
+    const float slack = 1e-6f * (fabsf(Dx) + fabsf(Dy) + fabsf(Dz) +
+                                 dtk * (fabsf(S.u0[0]) + fabsf(S.u0[1]) + fabsf(S.u0[2]) +
+                                        kf * (fabsf(S.gdt[0]) + fabsf(S.gdt[1]) + fabsf(S.gdt[2]))));
+    return fmaxf(across + slack, 1e-30f);
 }
 
 // Vector3d::rotate_around (Vector3d.h:152-178) split in two: the half-angle terms of the turn
@@ -830,25 +895,28 @@ __global__ void k_walls(uint32_t nglob, const uint32_t* __restrict__ glob, const
                         const double4_32a* __restrict__ w64, const float4* __restrict__ v32A,
                         float4* __restrict__ v32B, const float4* __restrict__ w32A, float4* __restrict__ w32B,
                         double4_32a* __restrict__ ox, double4_32a* __restrict__ oz, float dt_max,
-                        unsigned* __restrict__ vmax_bits, const float* __restrict__ disp_in,
-                        float* __restrict__ disp_out, float skin, float skin_w,
-                        const unsigned* __restrict__ wall_speed_bits,
+                        unsigned* __restrict__ vmax_bits, unsigned* __restrict__ vrel_bits,
+                        const float* __restrict__ disp_in, float* __restrict__ disp_out, float skin, float skin_w,
+                        float pos_eps, const unsigned* __restrict__ wall_speed_bits,
                         const double4_32a* __restrict__ wrot,
                         unsigned* __restrict__ held, float4* __restrict__ wall32, unsigned* __restrict__ nwork) {
     const uint32_t q = blockIdx.x * blockDim.x + threadIdx.x;
-    const float ds = disp_in[0], dw = disp_in[1];
-    const bool hold = list_spent(ds, dw, skin, skin_w);
+    const float drel = disp_in[0], dabs = disp_in[1], dw = disp_in[2];
+    const bool hold = list_spent(drel, dabs, dw, skin, skin_w);
     if (q == 0) {
         *nwork = 0u;                               // the split tick's worklist, empty for the next step
         if (hold) {
-            disp_out[0] = ds;
-            disp_out[1] = dw;
+            for (int k = 0; k < 4; ++k) disp_out[k] = disp_in[k];
             *held += 1u;
         } else {
-            disp_out[0] = ds + dt_max * __uint_as_float(*vmax_bits);
-            disp_out[1] = dw + dt_max * __uint_as_float(*wall_speed_bits);
+            // pos_eps: the FP64 rounding of a position update, which the speeds do not see
+            disp_out[0] = drel + dt_max * __uint_as_float(*vrel_bits) + pos_eps;
+            disp_out[1] = dabs + dt_max * __uint_as_float(*vmax_bits) + pos_eps;
+            disp_out[2] = dw + dt_max * __uint_as_float(*wall_speed_bits) + pos_eps;
+            disp_out[3] = __uint_as_float(__float_as_uint(disp_in[3]) + 1u);
         }
         *vmax_bits = 0u;
+        *vrel_bits = 0u;
     }
     if (q >= nglob) return;
     const uint32_t w = glob[q];
@@ -859,9 +927,17 @@ __global__ void k_walls(uint32_t nglob, const uint32_t* __restrict__ glob, const
         return;
     }
     const ModelDev& M = models[model_of[w]];
-    const double dt = scenes[scene_of[w]].dt;
+    const SceneDev& S = scenes[scene_of[w]];
+    const double dt = S.dt;
+    const uint32_t k1 = __float_as_uint(disp_in[3]) + 1u;     // steps since the rebuild, after this one
     d3 P = ld(xA, w);
-    if (M.behavior == BEH_ORBITAL) {
+    if (M.behavior != BEH_ORBITAL) {
+        float4 ws = wall32[w];
+        if (ws.w != 0.0f) {
+            ws.w = frame_drift_across(S, k1, M.shape, ws.x, ws.y, ws.z);
+            wall32[w] = ws;
+        }
+    } else {
         const d3 V = ld(v64, w);
         P = add(P, muls(V, dt));
         // rotate_around(O, omega dt) with its cos/sin terms computed once per list (k_wall_rot)
@@ -872,7 +948,8 @@ __global__ void k_walls(uint32_t nglob, const uint32_t* __restrict__ glob, const
         const double lz = len(Oz), lx = len(Ox);
         bool ok = lz > 0.0;
         if (M.shape == SHAPE_PLATE) ok = ok && lx > 0.0 && fabs(dot(Ox, Oz)) <= 1e-9 * lx * lz;
-        wall32[w] = ok ? make_float4((float)(Oz.x / lz), (float)(Oz.y / lz), (float)(Oz.z / lz), 1.0f)
+        const float nx = (float)(Oz.x / lz), ny = (float)(Oz.y / lz), nz = (float)(Oz.z / lz);
+        wall32[w] = ok ? make_float4(nx, ny, nz, frame_drift_across(S, k1, M.shape, nx, ny, nz))
                        : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
     }
     st(xB, w, P, 0.0);
@@ -881,6 +958,44 @@ __global__ void k_walls(uint32_t nglob, const uint32_t* __restrict__ glob, const
 }
 
 // ---- broad phase -------------------------------------------------------------------------
+// Per scene, the componentwise range of its mobile spheres' velocities (ordered float bits in
+// vred[6 * scene + k]: [0..2] min, [3..5] max): its midrange is the frame velocity of the list.
+__global__ void __launch_bounds__(TPB) k_vrange(uint32_t n, const uint32_t* __restrict__ model_of,
+                                                const ModelDev* __restrict__ models,
+                                                const uint32_t* __restrict__ scene_of,
+                                                const double4_32a* __restrict__ v, unsigned* __restrict__ vred) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    unsigned mn[3] = {0xffffffffu, 0xffffffffu, 0xffffffffu}, mx[3] = {0, 0, 0};
+    uint32_t sc = 0xffffffffu;
+    if (i < n && models[model_of[i]].scope == SCOPE_LOCAL && models[model_of[i]].behavior == BEH_MOBILE) {
+        sc = scene_of[i];
+        const d3 q = ld(v, i);
+        const float f[3] = {(float)q.x, (float)q.y, (float)q.z};
+        for (int k = 0; k < 3; ++k) {
+            const unsigned b = __float_as_uint(f[k]);
+            mn[k] = mx[k] = (b >> 31) ? ~b : (b | 0x80000000u);
+        }
+    }
+    const uint32_t sc0 = __shfl_sync(0xffffffffu, sc, 0);
+    const bool one = __all_sync(0xffffffffu, sc == sc0 || sc == 0xffffffffu) && sc0 != 0xffffffffu;
+    if (one) {
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1)
+#pragma unroll
+            for (int k = 0; k < 3; ++k) {
+                mn[k] = min(mn[k], __shfl_xor_sync(0xffffffffu, mn[k], o));
+                mx[k] = max(mx[k], __shfl_xor_sync(0xffffffffu, mx[k], o));
+            }
+    }
+    if ((one && (threadIdx.x & 31) == 0) || (!one && sc != 0xffffffffu)) {
+        unsigned* r = vred + 6 * (size_t)(one ? sc0 : sc);
+        for (int k = 0; k < 3; ++k) {
+            atomicMin(&r[k], mn[k]);
+            atomicMax(&r[3 + k], mx[k]);
+        }
+    }
+}
+
 __global__ void __launch_bounds__(TPB) k_bounds(uint32_t n, const uint32_t* __restrict__ model_of,
                                                 const ModelDev* __restrict__ models,
                                                 const uint32_t* __restrict__ scene_of, const double4_32a* __restrict__ x,
@@ -1139,23 +1254,24 @@ __global__ void __launch_bounds__(TPB) k_carry(uint32_t n, const uint32_t* __res
 
 
 
-// Per sphere, the largest pad (the prefilter's allowance for both spheres' travel since the
-// rebuild) at which every entry of its new list is still certainly apart, checked with the
-// prefilter itself: an estimate from the rebuild-time gap, backed off until apart32 confirms it.
-// -1 (never quiet) for a sphere with a bondable entry, an entry that failed the check, or an
-// entry with an orbital wall (its normal is recomputed every step).  Resets the clean-walk count.
+// Per sphere, the largest pads (the prefilter's allowance for the travel since the rebuild:
+// sphere pairs in x, fixed walls in y) at which every entry of its new list is still certainly
+// apart, checked with the prefilter itself: an estimate from the rebuild-time gap, backed off
+// until apart32 confirms it.  -1 (never quiet) for a sphere with a bondable entry, an entry that
+// failed the check, or an entry with an orbital wall (its normal is recomputed every step).
+// Resets the clean-walk count.
 __global__ void __launch_bounds__(TPB) k_clear(uint32_t n, const uint32_t* __restrict__ ptr,
                                                const uint32_t* __restrict__ ent, const uint32_t* __restrict__ meta,
                                                const uint32_t* __restrict__ model_of,
                                                const ModelDev* __restrict__ models, const float4* __restrict__ pos32,
                                                const float4* __restrict__ wall32, const float* __restrict__ reach,
-                                               float* __restrict__ clear, uint8_t* __restrict__ qcnt, int enable) {
+                                               float2* __restrict__ clear, uint8_t* __restrict__ qcnt, int enable) {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     qcnt[i] = 0;
-    float c = -1.0f;
+    float c = -1.0f, cw = -1.0f;                   // sphere pairs, fixed walls
     if (enable && models[model_of[i]].scope == SCOPE_LOCAL) {
-        c = 3.0e38f;
+        c = cw = 3.0e38f;
         const float4 pi = pos32[i];
         for (uint32_t e = ptr[i]; e < ptr[i + 1]; ++e) {
             const uint32_t m = meta[e];
@@ -1164,7 +1280,7 @@ __global__ void __launch_bounds__(TPB) k_clear(uint32_t n, const uint32_t* __res
             const uint32_t j = ent[e] & ~WALL_BIT;
             const bool wall = ent[e] & WALL_BIT;
             if ((m & META_BOND) || (wall && models[model_of[j]].behavior == BEH_ORBITAL)) {
-                c = -1.0f;
+                c = cw = -1.0f;
                 break;
             }
             const float4 pj = pos32[j];
@@ -1188,21 +1304,60 @@ __global__ void __launch_bounds__(TPB) k_clear(uint32_t n, const uint32_t* __res
                 if (!ok) t = k < 2 ? 0.5f * t : 0.0f;
             }
             if (!ok) {
-                c = -1.0f;
+                c = cw = -1.0f;
                 break;
             }
-            c = fminf(c, t);
+            if (wall) cw = fminf(cw, t);
+            else c = fminf(c, t);
         }
     }
-    clear[i] = c;
+    clear[i] = make_float2(c, cw);
+}
+
+// Interior wall entries of the new list (META_INTERIOR): the sphere's projection lies inside
+// the plate's rectangle (or within the rod's length) by more than any in-plane travel before
+// the list is spent: the sphere's (at most the skin) and, for an orbital wall, the wall's own
+// (together at most the wall skin).
+__global__ void __launch_bounds__(TPB) k_interior(uint32_t n, const uint32_t* __restrict__ ptr,
+                                                  const uint32_t* __restrict__ ent, uint32_t* __restrict__ meta,
+                                                  const uint32_t* __restrict__ model_of,
+                                                  const ModelDev* __restrict__ models,
+                                                  const double4_32a* __restrict__ x, const double4_32a* __restrict__ ox,
+                                                  const double4_32a* __restrict__ oz, float skin, float skin_w) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n || models[model_of[i]].scope != SCOPE_LOCAL) return;
+    const d3 P = ld(x, i);
+    for (uint32_t e = ptr[i]; e < ptr[i + 1]; ++e) {
+        const uint32_t v = ent[e];
+        if (!(v & WALL_BIT)) continue;
+        const uint32_t w = v & ~WALL_BIT;
+        const ModelDev& W = models[model_of[w]];
+        const d3 Oz = ld(oz, w);
+        const double lz = len(Oz);
+        if (!(lz > 0.0)) continue;
+        const d3 d = sub(P, ld(x, w));
+        const double m = (W.behavior == BEH_ORBITAL ? skin_w : skin) + 1e-9 * (len(d) + 1.0);
+        const d3 uz = muls(Oz, 1.0 / lz);
+        bool in;
+        if (W.shape == SHAPE_PLATE) {
+            const d3 Ox = ld(ox, w);
+            const double lx = len(Ox);
+            if (!(lx > 0.0)) continue;
+            const d3 ux = muls(Ox, 1.0 / lx), uy = cross(uz, ux);
+            in = fabs(dot(d, ux)) <= 0.5 * W.a0 - m && fabs(dot(d, uy)) <= 0.5 * W.a2 - m;
+        } else {
+            in = fabs(dot(d, uz)) <= 0.5 * W.a1 - m;
+        }
+        if (in) meta[e] |= META_INTERIOR;
+    }
 }
 
 // Spheres whose next step skips the walk: the tick's own test, with the current bound.
-__global__ void __launch_bounds__(TPB) k_quiet_count(uint32_t n, const float* __restrict__ clear,
+__global__ void __launch_bounds__(TPB) k_quiet_count(uint32_t n, const float2* __restrict__ clear,
                                                      const uint8_t* __restrict__ qcnt, const float* __restrict__ disp,
                                                      unsigned* __restrict__ count) {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-    const bool q = i < n && qcnt[i] >= 2u && 2.0f * disp[0] <= clear[i];
+    const bool q = i < n && qcnt[i] >= 2u && 2.0f * disp[0] <= clear[i].x && disp[1] <= clear[i].y;
     const unsigned m = __ballot_sync(0xffffffffu, q);
     if ((threadIdx.x & 31) == 0 && m) atomicAdd(count, (unsigned)__popc(m));
 }
@@ -1347,6 +1502,37 @@ __global__ void __launch_bounds__(TPB) k_pack3m(uint32_t n, const double* __rest
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i < n) dst[i] = make_double4_32a(src[3 * (size_t)i], src[3 * (size_t)i + 1], src[3 * (size_t)i + 2], 0.0);
 }
+// vedo_gpu_set_state: one field of every object from the staged host copy.  With `jump`, the
+// field is the position and each sphere's jump (rounded up) joins a maximum, so that the list
+// can stay when the displacement bound absorbs it; any change to a wall's position, velocity,
+// angular velocity or orientation is flagged (its cached motion terms need a rebuild).
+__global__ void __launch_bounds__(TPB) k_place(uint32_t n, const double* __restrict__ src, double4_32a* __restrict__ dst,
+                                               const uint32_t* __restrict__ model_of,
+                                               const ModelDev* __restrict__ models, int wall_field,
+                                               unsigned* __restrict__ jump, unsigned* __restrict__ wall_moved) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    float d = 0.0f;
+    if (i < n) {
+        const double nx = src[3 * (size_t)i], ny = src[3 * (size_t)i + 1], nz = src[3 * (size_t)i + 2];
+        const double4_32a o = dst[i];
+        if (models[model_of[i]].scope == SCOPE_LOCAL) {
+            if (jump) {
+                const double dx = __dsub_rn(nx, o.x), dy = __dsub_rn(ny, o.y), dz = __dsub_rn(nz, o.z);
+                const double l = __dsqrt_rn(__dadd_rn(__dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy)), __dmul_rn(dz, dz)));
+                d = __fmul_ru(__double2float_ru(l), 1.000001f);
+                if (!(d == d)) d = 3.0e38f;            // a NaN jump spends the list
+            }
+        } else if (wall_field && (nx != o.x || ny != o.y || nz != o.z)) {
+            atomicOr(wall_moved, 1u);
+        }
+        dst[i] = make_double4_32a(nx, ny, nz, 0.0);
+    }
+    if (jump) {
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) d = fmaxf(d, __shfl_xor_sync(0xffffffffu, d, o));
+        if ((threadIdx.x & 31) == 0 && d > 0.0f) atomicMax(jump, __float_as_uint(d));
+    }
+}
 __global__ void __launch_bounds__(TPB) k_unpack3m(uint32_t n, const double4_32a* __restrict__ src, double* __restrict__ dst) {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i < n) {
@@ -1376,15 +1562,51 @@ __global__ void __launch_bounds__(TPB) k_copy32(uint32_t n, const double4_32a* _
         o[i] = make_float4((float)q.x, (float)q.y, (float)q.z, 0.0f);
     }
 }
+// Spinning orbital plates whose sweeping edges may meet a sphere: edge[q] is set when a sphere
+// lies within reach + skin_w of the plate's plane (the band it can reach before the list is
+// spent) but outside the plate's inscribed circle shrunk by skin_w.  Inside that circle the
+// plate covers the sphere's projection whatever its turn, so a plate turning about its own
+// normal changes no distance there.
+__global__ void __launch_bounds__(TPB) k_wall_edge(uint32_t n, const uint32_t* __restrict__ model_of,
+                                                   const ModelDev* __restrict__ models,
+                                                   const uint32_t* __restrict__ scene_of,
+                                                   const SceneDev* __restrict__ scenes,
+                                                   const uint32_t* __restrict__ glob,
+                                                   const double4_32a* __restrict__ x,
+                                                   const double4_32a* __restrict__ oz, float skin_w,
+                                                   unsigned* __restrict__ edge) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const ModelDev& M = models[model_of[i]];
+    if (M.scope != SCOPE_LOCAL) return;
+    const SceneDev& S = scenes[scene_of[i]];
+    const d3 P = ld(x, i);
+    for (uint32_t q = S.wall_beg; q < S.wall_end; ++q) {
+        const uint32_t w = glob[q];
+        const ModelDev& W = models[model_of[w]];
+        if (W.behavior != BEH_ORBITAL || W.shape != SHAPE_PLATE) continue;
+        const d3 Oz = ld(oz, w);
+        const double lz = len(Oz);
+        if (!(lz > 0.0)) continue;
+        const d3 d = sub(P, ld(x, w));
+        const double sd = dot(d, Oz) / lz;
+        const double tol = 1e-9 * (len(d) + 1.0);
+        if (fabs(sd) > M.range + 0.5 * W.a1 + skin_w + tol) continue;
+        const double rho = sqrt(fmax(dot(d, d) - sd * sd, 0.0));
+        if (rho > 0.5 * fmin(W.a0, W.a2) - skin_w - tol) atomicOr(&edge[q], 1u);
+    }
+}
+
 // Bound on how fast an orbital wall's plane (plate) or axis line (cylinder) can move towards
-// a sphere that may touch it: |V| + |omega| R, R = half the wall's diagonal + 2 r_max.  A
-// wall spinning about its own normal (plate) or axis (cylinder) keeps its plane or line: only
-// the normal (plate) or transverse (cylinder) part of V counts.  V and omega of an orbital
-// wall are prescribed, so the bound holds until the state is set again.
+// a sphere that may touch it: |V| + |omega| R, R = half the wall's diagonal + 2 r_max.  A rod
+// spinning about its own axis keeps its surface, and a plate spinning about its own normal
+// keeps its plane and, where no sphere is near its sweeping edges (k_wall_edge), every
+// distance: then only the normal (plate) or transverse (rod) part of V counts.  V and omega of
+// an orbital wall are prescribed, so the bound holds until the state is set again.
 __global__ void k_wall_speed(uint32_t nglob, const uint32_t* __restrict__ glob, const uint32_t* __restrict__ model_of,
                              const ModelDev* __restrict__ models, const double4_32a* __restrict__ v64,
                              const double4_32a* __restrict__ w64, const double4_32a* __restrict__ oz, float reach,
-                             unsigned* __restrict__ out_bits) {
+                             const unsigned* __restrict__ edge, unsigned* __restrict__ out_bits) {
     const uint32_t q = blockIdx.x * blockDim.x + threadIdx.x;
     if (q >= nglob) return;
     const uint32_t w = glob[q];
@@ -1397,7 +1619,7 @@ __global__ void k_wall_speed(uint32_t nglob, const uint32_t* __restrict__ glob, 
     if (lz > 0.0) {
         const d3 u = muls(Oz, 1.0 / lz);
         const d3 c = cross(W, u);
-        if (len(c) <= 1e-12 * len(W)) {                 // spins about its own normal / axis
+        if (len(c) <= 1e-12 * len(W) && !(M.shape == SHAPE_PLATE && edge[q])) {   // spins about its normal / axis
             const double vn = dot(V, u);
             sp = (M.shape == SHAPE_PLATE) ? fabs(vn) : len(sub(V, muls(u, vn)));
         }
@@ -1419,7 +1641,7 @@ __global__ void __launch_bounds__(TPB) k_wall32(uint32_t n, const uint32_t* __re
     const double lz = len(Oz), lx = len(Ox);
     bool ok = lz > 0.0;
     if (M.shape == SHAPE_PLATE) ok = ok && lx > 0.0 && fabs(dot(Ox, Oz)) <= 1e-9 * lx * lz;
-    wall32[i] = ok ? make_float4((float)(Oz.x / lz), (float)(Oz.y / lz), (float)(Oz.z / lz), 1.0f)
+    wall32[i] = ok ? make_float4((float)(Oz.x / lz), (float)(Oz.y / lz), (float)(Oz.z / lz), 1e-30f)   // no drift yet
                    : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
 }
 
@@ -1570,6 +1792,7 @@ public:
     }
     double scene_time(uint32_t s) const { return s < sc_.size() ? sc_[s].t : 0.0; }
     int quiet_spheres(uint64_t* count) override;
+    int list_status(double out[6]) override;
     int tuning(float out[5]) const override {
         out[0] = skin_frac_;
         out[1] = cell_scale_;
@@ -1670,11 +1893,13 @@ private:
     uint32_t* d_work_ = nullptr;                  // [n] spheres deferred by the light tick
     bool quiet_ok_ = true;                        // quiet spheres skip their walk (identical results)
     int sms_ = 1;                                 // streaming multiprocessors of the device
-    float* d_clear_ = nullptr;                    // [n] quiet-sphere pad limit of the current list
+    float2* d_clear_ = nullptr;                   // [n] quiet-sphere pad limits of the current list
+    unsigned* d_vred_ = nullptr;                  // [scenes][6] velocity ranges at the rebuild
+    float pos_eps_ = 0.0f;                        // FP64 rounding of a position update (bound)
     uint8_t* d_qcnt_ = nullptr;                   // [n] clean walks since the rebuild (0..2)
     unsigned* d_red_ = nullptr;     // [8] vmax bits, [9], [10] scan totals, [11] identity steps, [12] wall speed
     unsigned* d_sred_ = nullptr;    // [scenes][8] per-scene bounds
-    float* d_disp_ = nullptr;       // [2][2] sphere and orbital-wall displacement bounds, by step parity (cur_)
+    float* d_disp_ = nullptr;       // [2][4] displacement bounds and steps since the rebuild, by step parity (cur_)
     int* d_err_ = nullptr;
     NList nl_[2];
     int nlc_ = 0;                   // current neighbour list
@@ -1690,7 +1915,8 @@ private:
     uint32_t wcap_ = 0, nwall_ent_ = 0;
     float* d_wimp_ = nullptr;
     unsigned long long* d_wred_ = nullptr;
-    double4_32a* d_wrot_ = nullptr;          // per wall: half-angle terms of its turn per step   // per wall: 6 integer sums, then 2 maxima (as 32-bit)
+    double4_32a* d_wrot_ = nullptr;          // per wall: half-angle terms of its turn per step
+    unsigned* d_wedge_ = nullptr;            // per wall: a sphere is near a spinning plate's sweeping edges
     uint32_t wimp_cap_ = 0;
     double* d_stage_ = nullptr;
     double* d_obs_ = nullptr;
@@ -1739,9 +1965,9 @@ MixedEngine::~MixedEngine() {
     free_nlist(nl_[1]);
     void* ptrs[] = {d_models_, d_params_, d_pc32_, d_geom_, d_rr_, d_mf_, d_reach_, d_model_of_, d_scene_of_,
                     d_scenes_, d_gfield_, d_glob_, d_x_[0], d_x_[1], d_v64_, d_w64_, d_ox_, d_oz_, d_imp_, d_aimp_,
-                    d_v32_[0], d_v32_[1], d_w32_[0], d_w32_[1], d_rr32_, d_xs_[0], d_xs_[1], d_work_, d_clear_, d_qcnt_, d_pos32_, d_wall32_, d_red_, d_sred_, d_disp_, d_err_,
+                    d_v32_[0], d_v32_[1], d_w32_[0], d_w32_[1], d_rr32_, d_xs_[0], d_xs_[1], d_work_, d_clear_, d_vred_, d_qcnt_, d_pos32_, d_wall32_, d_red_, d_sred_, d_disp_, d_err_,
                     d_key_, d_key_alt_, d_sid_, d_sid_alt_, d_cnt_, d_gs_, d_ge_, d_act_, d_stage_, d_obs_, d_gidx_,
-                    d_wkey_, d_wval_, d_wkey_alt_, d_wval_alt_, d_wptr_, d_wimp_, d_wred_, d_wrot_};
+                    d_wkey_, d_wval_, d_wkey_alt_, d_wval_alt_, d_wptr_, d_wimp_, d_wred_, d_wrot_, d_wedge_};
     for (void* p : ptrs) if (p) cudaFree(p);
     drop_graphs();
     for (auto& e : pev_) cudaEventDestroy(e);
@@ -1932,10 +2158,12 @@ int MixedEngine::init_from(const std::vector<SceneSource>& src, const MixedEngin
         MCK(mal(&d_wptr_, glob_.size() + 1));
         MCK(mal(&d_wred_, 7 * glob_.size()));
         MCK(mal(&d_wrot_, glob_.size()));
+        MCK(mal(&d_wedge_, glob_.size()));
     }
     sdev_.resize(sc_.size());
     MCK(mal(&d_scenes_, sc_.size()));
     MCK(mal(&d_sred_, 8 * sc_.size()));
+    MCK(mal(&d_vred_, 6 * sc_.size()));
     MCK(mal(&d_work_, n_));
     MCK(mal(&d_clear_, n_));
     MCK(mal(&d_qcnt_, n_));
@@ -1948,13 +2176,13 @@ int MixedEngine::init_from(const std::vector<SceneSource>& src, const MixedEngin
     }
     MCK(mal(&d_v64_, n_)); MCK(mal(&d_w64_, n_)); MCK(mal(&d_ox_, n_)); MCK(mal(&d_oz_, n_));
     MCK(mal(&d_imp_, n_)); MCK(mal(&d_aimp_, n_)); MCK(mal(&d_pos32_, n_)); MCK(mal(&d_wall32_, n_));
-    MCK(mal(&d_red_, 16)); MCK(mal(&d_disp_, 4)); MCK(mal(&d_err_, 1));
+    MCK(mal(&d_red_, 16)); MCK(mal(&d_disp_, 8)); MCK(mal(&d_err_, 1));
     MCK(mal(&d_key_, n_)); MCK(mal(&d_key_alt_, n_)); MCK(mal(&d_sid_, n_)); MCK(mal(&d_sid_alt_, n_));
     MCK(mal(&d_cnt_, (size_t)n_ + 1));
     MCK(mal(&d_stage_, 7 * 3 * (size_t)n_));
     MCK(mal(&d_obs_, (size_t)(nblk(n_) + 2) * 16 + 64));
     MCK(cudaMemset(d_red_, 0, 64));
-    MCK(cudaMemset(d_disp_, 0, 16));
+    MCK(cudaMemset(d_disp_, 0, 32));
     if (prev) {
         for (int k = 0; k < 3; ++k) origin_[k] = prev->origin_[k];
     } else {
@@ -2044,6 +2272,8 @@ int MixedEngine::init_from(const std::vector<SceneSource>& src, const MixedEngin
 
 int MixedEngine::set_scene_active(uint32_t s, bool on) {
     if (s >= sc_.size()) return fail(VEDO_ERR_INVALID_ARGUMENT, "scene index out of range");
+    // a resumed scene rebuilds: its spheres stood still while its frame moved on
+    if (on && !sc_[s].active) need_rebuild_ = true;
     sc_[s].active = on;
     sdev_[s].active = on ? 1u : 0u;
     MCK(cudaMemcpyAsync(d_scenes_ + s, &sdev_[s], sizeof(SceneDev), cudaMemcpyHostToDevice, stream_));
@@ -2102,7 +2332,8 @@ TickArgs MixedEngine::args(bool write_imp) {
     a.write_imp = write_imp ? 1 : 0;
     a.vmax_bits = d_red_ + 8;
     a.pos32 = d_pos32_;
-    a.disp = d_disp_ + 2 * cur_;
+    a.disp = d_disp_ + 4 * cur_;
+    a.vrel_bits = d_red_ + 2;
     a.skin = skin_min_;
     a.skin_w = WALL_SKIN * skin_min_;
     a.reach = d_reach_;
@@ -2133,9 +2364,14 @@ int MixedEngine::rebuild() {
     k_bounds<<<nblk(n_), TPB, 0, stream_>>>(n_, d_model_of_, d_models_, d_scene_of_, d_x_[cur_], org, d_pos32_,
                                             d_sred_);
     k_wall32<<<nblk(n_), TPB, 0, stream_>>>(n_, d_model_of_, d_models_, d_ox_, d_oz_, d_wall32_);
-    own += 2;
-    std::vector<unsigned> red(8 * (size_t)S);
+    std::vector<unsigned> vred0(6 * (size_t)S, 0u);
+    for (uint32_t s = 0; s < S; ++s) vred0[6 * s] = vred0[6 * s + 1] = vred0[6 * s + 2] = 0xffffffffu;
+    MCK(cudaMemcpyAsync(d_vred_, vred0.data(), 4 * vred0.size(), cudaMemcpyHostToDevice, stream_));
+    k_vrange<<<nblk(n_), TPB, 0, stream_>>>(n_, d_model_of_, d_models_, d_scene_of_, d_v64_, d_vred_);
+    own += 3;
+    std::vector<unsigned> red(8 * (size_t)S), vred(6 * (size_t)S);
     MCK(cudaMemcpyAsync(red.data(), d_sred_, 4 * red.size(), cudaMemcpyDeviceToHost, stream_));
+    MCK(cudaMemcpyAsync(vred.data(), d_vred_, 4 * vred.size(), cudaMemcpyDeviceToHost, stream_));
     MCK(cudaStreamSynchronize(stream_));
     auto unord = [](unsigned o) {
         unsigned b = (o >> 31) ? (o & 0x7fffffffu) : ~o;
@@ -2145,6 +2381,7 @@ int MixedEngine::rebuild() {
     };
     // per-scene cell grids (edge 2 r_max + skin), packed one after the other
     uint64_t cells = 0;
+    float pos_eps = 0.0f;
     for (uint32_t s = 0; s < S; ++s) {
         SceneDev& D = sdev_[s];
         const SceneHost& H = sc_[s];
@@ -2157,11 +2394,20 @@ int MixedEngine::rebuild() {
         D.nobj = H.nobj;
         D.active = H.active ? 1u : 0u;
         D.dt = H.dt;
+        // the frame: free fall under the scene's field from its spheres' velocity midrange
+        const bool moving = vred[6 * s] != 0xffffffffu;
+        for (int k = 0; k < 3; ++k) {
+            D.u0[k] = moving ? 0.5f * (unord(vred[6 * s + k]) + unord(vred[6 * s + 3 + k])) : 0.0f;
+            D.gdt[k] = (float)(H.g[k] * H.dt);
+        }
         float lo[3] = {0, 0, 0}, hi[3] = {0, 0, 0};
         if (H.nloc)
             for (int k = 0; k < 3; ++k) {
                 lo[k] = unord(red[8 * s + k]);
                 hi[k] = unord(red[8 * s + 3 + k]);
+                // a position update's FP64 rounding is at most half an ulp of the coordinate
+                const double m = std::max(std::fabs(origin_[k] + lo[k]), std::fabs(origin_[k] + hi[k])) + 1.0;
+                pos_eps = std::max(pos_eps, (float)std::ldexp(m, -50));
             }
         float rmax;
         memcpy(&rmax, &red[8 * s + 6], 4);
@@ -2183,6 +2429,7 @@ int MixedEngine::rebuild() {
         D.cell_base = cells;
         cells += (uint64_t)nc[0] * nc[1] * nc[2];
     }
+    pos_eps_ = pos_eps;
     MCK(cudaMemcpyAsync(d_scenes_, sdev_.data(), sizeof(SceneDev) * S, cudaMemcpyHostToDevice, stream_));
     if (cells > grid_cap_) {
         if (d_gs_) cudaFree(d_gs_);
@@ -2236,6 +2483,8 @@ int MixedEngine::rebuild() {
     k_carry<<<nblk(n_), TPB, 0, stream_>>>(n_, L.ptr, L.ent, L.slot, O.ptr, O.ent, O.slot, O.h[cur_], O.f[cur_],
                                            L.h[cur_], L.f[cur_], L.h[cur_ ^ 1], L.f[cur_ ^ 1],
                                            O.ent != nullptr ? 1 : 0);
+    k_interior<<<nblk(n_), TPB, 0, stream_>>>(n_, L.ptr, L.ent, L.meta, d_model_of_, d_models_, d_x_[cur_], d_ox_,
+                                              d_oz_, skin_min_, WALL_SKIN * skin_min_);
     k_clear<<<nblk(n_), TPB, 0, stream_>>>(n_, L.ptr, L.ent, L.meta, d_model_of_, d_models_, d_pos32_, d_wall32_,
                                            d_reach_, d_clear_, d_qcnt_, quiet_ok_ ? 1 : 0);
     own += 3;
@@ -2280,13 +2529,17 @@ int MixedEngine::rebuild() {
         k_wall_rot<<<nblk(glob_.size()), TPB, 0, stream_>>>((uint32_t)glob_.size(), d_glob_, d_model_of_, d_models_,
                                                            d_scenes_, d_scene_of_, d_w64_, d_wrot_);
         ++own;
+        MCK(cudaMemsetAsync(d_wedge_, 0, 4 * glob_.size(), stream_));
+        k_wall_edge<<<nblk(n_), TPB, 0, stream_>>>(n_, d_model_of_, d_models_, d_scene_of_, d_scenes_, d_glob_,
+                                                   d_x_[cur_], d_oz_, WALL_SKIN * skin_min_, d_wedge_);
         k_wall_speed<<<nblk(glob_.size()), TPB, 0, stream_>>>((uint32_t)glob_.size(), d_glob_, d_model_of_, d_models_,
-                                                             d_v64_, d_w64_, d_oz_, 2.0f * rmax_all, d_red_ + 12);
-        ++own;
+                                                             d_v64_, d_w64_, d_oz_, 2.0f * rmax_all, d_wedge_,
+                                                             d_red_ + 12);
+        own += 2;
     }
     int herr = 0;
     MCK(cudaMemcpyAsync(&herr, d_err_, 4, cudaMemcpyDeviceToHost, stream_));
-    MCK(cudaMemsetAsync(d_disp_, 0, 16, stream_));
+    MCK(cudaMemsetAsync(d_disp_, 0, 32, stream_));
     MCK(cudaStreamSynchronize(stream_));
     MCK(cudaGetLastError());
     if (herr) return fail(VEDO_ERR_CUDA, "mixed form: asymmetric neighbour lists");
@@ -2354,8 +2607,8 @@ void MixedEngine::launch_step(bool write_imp) {
     }
     k_walls<<<nblk(std::max<size_t>(glob_.size(), 1)), TPB, 0, stream_>>>(
         (uint32_t)glob_.size(), d_glob_, d_model_of_, d_models_, d_scenes_, d_scene_of_, a.xA, a.xB, d_v64_, d_w64_,
-        a.v32A, a.v32B, a.w32A, a.w32B, d_ox_, d_oz_, dt_max_, d_red_ + 8, d_disp_ + 2 * cur_,
-        d_disp_ + 2 * (cur_ ^ 1), skin_min_, WALL_SKIN * skin_min_, d_red_ + 12, d_wrot_, d_red_ + 11, d_wall32_, d_red_ + 14);
+        a.v32A, a.v32B, a.w32A, a.w32B, d_ox_, d_oz_, dt_max_, d_red_ + 8, d_red_ + 2,
+        d_disp_ + 4 * cur_, d_disp_ + 4 * (cur_ ^ 1), skin_min_, WALL_SKIN * skin_min_, pos_eps_, d_red_ + 12, d_wrot_, d_red_ + 11, d_wall32_, d_red_ + 14);
     ++launches_;
     if (pe) cudaEventRecordWithFlags(pe[2], stream_, ev_flags_);
     cur_ ^= 1;
@@ -2399,9 +2652,9 @@ int MixedEngine::step_chunk(uint32_t chunk, bool imp_last, float* use_after) {
     } else {
         for (uint32_t k = 0; k < chunk; ++k) launch_step(imp_last && k + 1 == chunk);
     }
-    float dd[2] = {0.0f, 0.0f};
+    float dd[4] = {0.0f, 0.0f, 0.0f, 0.0f};
     unsigned held = 0;
-    MCK(cudaMemcpyAsync(dd, d_disp_ + 2 * cur_, 8, cudaMemcpyDeviceToHost, stream_));
+    MCK(cudaMemcpyAsync(dd, d_disp_ + 4 * cur_, 16, cudaMemcpyDeviceToHost, stream_));
     MCK(cudaMemcpyAsync(&held, d_red_ + 11, 4, cudaMemcpyDeviceToHost, stream_));
     MCK(cudaStreamSynchronize(stream_));
     for (uint32_t q = 0; q + 3 <= pev_used_; q += 3) {   // profiling: tick and wall kernel times
@@ -2422,8 +2675,8 @@ int MixedEngine::step_chunk(uint32_t chunk, bool imp_last, float* use_after) {
         S.steps += taken;
     }
     // the share of the list's life used so far: 1 = the next step would be an identity step
-    const float use = std::max(2.0f * dd[0] / skin_min_, (dd[0] + dd[1]) / (WALL_SKIN * skin_min_));
-    if (held || list_spent(dd[0], dd[1], skin_min_, WALL_SKIN * skin_min_) || use > 1.0f) {
+    const float use = std::max(std::max(2.0f * dd[0], dd[1]) / skin_min_, (dd[1] + dd[2]) / (WALL_SKIN * skin_min_));
+    if (held || list_spent(dd[0], dd[1], dd[2], skin_min_, WALL_SKIN * skin_min_) || use > 1.0f) {
         // held steps are taken again after the rebuild; a bound already past half the skin
         // would hold the next step, and contact queries need a complete list too
         need_rebuild_ = true;
@@ -2449,7 +2702,8 @@ int MixedEngine::autotune(uint32_t max_steps, uint32_t* taken) {
     const int blocks[] = {64, 128, 256};
     const float skins[] = {0.05f, 0.1f, 0.15f, 0.25f, 0.4f};
     const float cells[] = {1.0f, 1.25f, 1.5f};
-    const uint32_t need = ci * (uint32_t)(2 * (3 + 2 + 2 + 5));
+    // at most four chunks per timed trial (a rebuild between may add two), two per skin trial
+    const uint32_t need = ci * (uint32_t)(4 * (3 + 2 + 2) + 2 * 5);
     if (max_steps < need) return VEDO_OK;            // too short a call: tune in a later one
     cudaEvent_t e0 = ev_[2], e1 = ev_[3];
     auto timed_rebuild = [&](float* ms) -> int {
@@ -2464,10 +2718,16 @@ int MixedEngine::autotune(uint32_t max_steps, uint32_t* taken) {
     auto timed_chunk = [&](float* ms_per_step, float* growth) -> int {
         const uint64_t r0 = round_;
         float use = 0.0f;
-        // an untimed chunk first: it captures the graph of this configuration
+        // an untimed chunk first: it captures the graph of this configuration (after a rebuild,
+        // another, so that the clean-walk counts have settled when the timing starts)
         int wrc = step_chunk(ci, false, nullptr);
         if (wrc > 0) return wrc;
-        if (need_rebuild_ && (wrc = rebuild()) != VEDO_OK) return wrc;
+        if (need_rebuild_) {
+            if ((wrc = rebuild()) != VEDO_OK) return wrc;
+            wrc = step_chunk(ci, false, nullptr);
+            if (wrc > 0) return wrc;
+            if (need_rebuild_ && (wrc = rebuild()) != VEDO_OK) return wrc;
+        }
         MCK(cudaEventRecord(e0, stream_));
         int rc = step_chunk(ci, false, &use);
         if (rc > 0) return rc;
@@ -2528,9 +2788,38 @@ int MixedEngine::autotune(uint32_t max_steps, uint32_t* taken) {
     float best_skin = skin_frac_;
     for (float f : skins) {
         set_skin(f);
+        // what a rebuild costs: the rebuild, then the first chunk of the new list (its steps walk
+        // every list while the clean-walk counts settle, and its graph is captured)
         float trb = 0.0f, t = 0.0f, growth = 0.0f;
-        if ((rc = timed_rebuild(&trb)) != VEDO_OK) return rc;
-        if ((rc = timed_chunk(&t, &growth)) != VEDO_OK) return rc;
+        {
+            const uint64_t r0 = round_;
+            MCK(cudaEventRecord(e0, stream_));
+            if ((rc = rebuild()) != VEDO_OK) return rc;
+            int wrc = step_chunk(ci, false, nullptr);
+            if (wrc > 0) return wrc;
+            MCK(cudaEventRecord(e1, stream_));
+            MCK(cudaEventSynchronize(e1));
+            MCK(cudaEventElapsedTime(&trb, e0, e1));
+            *taken += (uint32_t)(round_ - r0);
+        }
+        if (need_rebuild_) {                           // the list did not last one chunk
+            if ((rc = rebuild()) != VEDO_OK) return rc;
+            continue;
+        }
+        {                                              // a settled chunk of the same list
+            const uint64_t r0 = round_;
+            float use = 0.0f, ms = 0.0f;
+            MCK(cudaEventRecord(e0, stream_));
+            int wrc = step_chunk(ci, false, &use);
+            if (wrc > 0) return wrc;
+            MCK(cudaEventRecord(e1, stream_));
+            MCK(cudaEventSynchronize(e1));
+            MCK(cudaEventElapsedTime(&ms, e0, e1));
+            t = ms / (float)ci;
+            growth = since_rebuild_ ? use / (float)since_rebuild_ : 0.0f;
+            *taken += (uint32_t)(round_ - r0);
+        }
+        trb = std::max(0.0f, trb - t * (float)ci);
         // steps until the list's life is used up at this growth (the rebuild rule's margin)
         const float life = growth > 0.0f ? std::max((float)ci, 1.0f / growth - 2.0f * (float)ci) : 1e6f;
         const float cost = t + trb / life;
@@ -2611,12 +2900,29 @@ int MixedEngine::get_state(const vedo_state_view& v) {
     return VEDO_OK;
 }
 
+int MixedEngine::list_status(double out[6]) {
+    float dd[4] = {0.0f, 0.0f, 0.0f, 0.0f};
+    MCK(cudaMemcpyAsync(dd, d_disp_ + 4 * cur_, 16, cudaMemcpyDeviceToHost, stream_));
+    MCK(cudaStreamSynchronize(stream_));
+    uint32_t k;
+    memcpy(&k, &dd[3], 4);
+    out[0] = (double)k;
+    out[1] = (double)rebuilds_;
+    out[2] = dd[0];
+    out[3] = dd[1];
+    out[4] = dd[2];
+    out[5] = skin_min_ > 0.0f ? std::max(std::max(2.0 * dd[0], (double)dd[1]) / skin_min_,
+                                          ((double)dd[1] + dd[2]) / (WALL_SKIN * skin_min_))
+                              : 0.0;
+    return VEDO_OK;
+}
+
 int MixedEngine::quiet_spheres(uint64_t* count) {
     *count = 0;
     if (need_rebuild_ || !n_) return VEDO_OK;         // the next step starts with a new list
     unsigned c = 0;
     MCK(cudaMemsetAsync(d_red_ + 15, 0, 4, stream_));
-    k_quiet_count<<<nblk(n_), TPB, 0, stream_>>>(n_, d_clear_, d_qcnt_, d_disp_ + 2 * cur_, d_red_ + 15);
+    k_quiet_count<<<nblk(n_), TPB, 0, stream_>>>(n_, d_clear_, d_qcnt_, d_disp_ + 4 * cur_, d_red_ + 15);
     MCK(cudaMemcpyAsync(&c, d_red_ + 15, 4, cudaMemcpyDeviceToHost, stream_));
     MCK(cudaStreamSynchronize(stream_));
     *count = c;
@@ -2627,17 +2933,43 @@ int MixedEngine::set_state(const vedo_state_view& v) {
     const double* srcs[] = {v.position, v.velocity, v.angular_velocity, v.orientation_x, v.orientation_z, v.impact,
                             v.angular_impact};
     double4_32a* dst[] = {d_x_[cur_], d_v64_, d_w64_, d_ox_, d_oz_, d_imp_, d_aimp_};
+    // The list survives new state when no wall changed and the spheres' largest jump fits the
+    // displacement bound: the jump is added to the bound (every pair may have closed by it).
+    MCK(cudaMemsetAsync(d_red_, 0, 8, stream_));      // [0] largest sphere jump, [1] a wall changed
     for (int k = 0; k < 7; ++k) {
         if (!srcs[k]) continue;
         double* st = d_stage_ + (size_t)k * 3 * n_;
         MCK(cudaMemcpyAsync(st, srcs[k], 24 * (size_t)n_, cudaMemcpyHostToDevice, stream_));
-        k_pack3m<<<nblk(n_), TPB, 0, stream_>>>(n_, st, dst[k]);
+        k_place<<<nblk(n_), TPB, 0, stream_>>>(n_, st, dst[k], d_model_of_, d_models_, k < 5 ? 1 : 0,
+                                               k == 0 ? d_red_ : nullptr, d_red_ + 1);
     }
     k_copy32<<<nblk(n_), TPB, 0, stream_>>>(n_, d_v64_, d_v32_[cur_]);
     k_copy32<<<nblk(n_), TPB, 0, stream_>>>(n_, d_w64_, d_w32_[cur_]);
+    unsigned jw[2] = {0u, 0u};
+    float dd[4] = {0.0f, 0.0f, 0.0f, 0.0f};
+    MCK(cudaMemcpyAsync(jw, d_red_, 8, cudaMemcpyDeviceToHost, stream_));
+    MCK(cudaMemcpyAsync(dd, d_disp_ + 4 * cur_, 16, cudaMemcpyDeviceToHost, stream_));
     MCK(cudaStreamSynchronize(stream_));
     MCK(cudaGetLastError());
-    need_rebuild_ = true;
+    if (need_rebuild_ || jw[1]) {
+        need_rebuild_ = true;
+        return VEDO_OK;
+    }
+    if (jw[0]) {
+        float j;
+        memcpy(&j, &jw[0], 4);
+        // the jump moves a sphere against its frame and absolutely (roundings of the sums: up)
+        dd[0] = std::nextafter(dd[0] + j, FLT_MAX);
+        dd[1] = std::nextafter(dd[1] + j, FLT_MAX);
+        if (list_spent(dd[0], dd[1], dd[2], skin_min_, WALL_SKIN * skin_min_)) {
+            need_rebuild_ = true;
+            return VEDO_OK;
+        }
+        MCK(cudaMemcpyAsync(d_disp_ + 4 * cur_, dd, 8, cudaMemcpyHostToDevice, stream_));
+        if (xs_stored_) k_split<<<nblk(n_), TPB, 0, stream_>>>(n_, d_x_[cur_], d_xs_[cur_]);
+        MCK(cudaStreamSynchronize(stream_));
+        MCK(cudaGetLastError());
+    }
     return VEDO_OK;
 }
 

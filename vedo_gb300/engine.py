@@ -211,6 +211,15 @@ class GpuEngine:
         return {"skin": float(sk.value), "cell_scale": float(cs.value), "tick_block": int(tb.value),
                 "stored_splits": bool(ss.value), "split_tick": bool(st.value)}
 
+    def list_status(self) -> Dict[str, float]:
+        """Neighbour-list state (MIXED form): steps since the rebuild, rebuilds, displacement
+        bounds (relative to the scene frame, absolute, orbital walls) and the share of the
+        list's life used."""
+        o = np.zeros(6)
+        self._check(lib().vedo_gpu_list_status(self.h, dptr(o)))
+        return {"steps": int(o[0]), "rebuilds": int(o[1]), "rel": float(o[2]), "abs": float(o[3]),
+                "wall": float(o[4]), "use": float(o[5])}
+
     def quiet_spheres(self) -> int:
         """Spheres whose next step skips the neighbour-list walk (MIXED form; 0 for FP64)."""
         c = C.c_uint64(0)

@@ -409,6 +409,36 @@ def hopper(n: int = 10000, seed: int = 0, friction: float = 0.4, restitution: fl
     return Scene(time_control(steps, dt), models, iacts, midx, P, V, OX, OZ, AV)
 
 
+def spinning_plate(omega: float = 500.0, steps: int = 3000, dt: float = 2e-7, radius: float = 1e-3,
+                   half: float = 10e-3, E: float = 70e9, nu: float = 0.25, restitution: float = 0.7,
+                   friction: float = 0.4, density: float = 2500.0) -> Scene:
+    """A square orbital plate (side 2 `half`, 2 mm thick, normal +z) spinning in its own plane at
+    `omega` rad/s about its centre, with spheres at rest in that plane just outside it, no field:
+    the turning corners sweep into the spheres (four spheres sit 15 degrees ahead of a corner,
+    four 25 degrees, all within the rounded corners' reach by 5 % of r, and clear of the plate
+    at the start).  A check of how the list handles
+    a wall whose plane never moves while its edges do.  ISwH contact."""
+    rho = half * math.sqrt(2.0) + 1e-3 + 0.95 * radius   # the rounded corners' reach + 0.95 r
+    ang = [math.radians(45.0 + 15.0 + 90.0 * q) for q in range(4)] + \
+          [math.radians(45.0 + 25.0 + 90.0 * q) for q in range(4)]
+    pos = np.array([[rho * math.cos(a), rho * math.sin(a), 0.0] for a in ang])
+    n = pos.shape[0]
+    models = [DOModel("Ball", "Ball", MOBILE, LOCAL, density, 1.0, SPHERE, (radius,)),
+              DOModel("Plate", "Wall", ORBITAL, GLOBAL, 0.0, 1.0, QUASI_PLATE, (2 * half, 2e-3, 2 * half))]
+    zeta = damping_ratio(restitution)
+    m_of = lambda rr: density * 4.0 / 3.0 * math.pi * rr ** 3
+    iacts = [IactModel("Ball", "Ball", "ISwH", _hertz_mech("ISwH", E, nu, radius, radius, m_of, zeta, friction)),
+             IactModel("Wall", "Ball", "ISwH", _hertz_mech("ISwH", E, nu, radius, None, m_of, zeta, friction))]
+    sp = time_control(steps, dt)
+    sp.field_acceleration = (0.0, 0.0, 0.0)
+    midx = np.concatenate([np.zeros(n, np.uint32), np.array([1], np.uint32)])
+    P = np.concatenate([pos, np.zeros((1, 3))])
+    OX = np.concatenate([np.tile([1.0, 0, 0], (n, 1)), np.array([[1.0, 0.0, 0.0]])])
+    OZ = np.concatenate([np.tile([0, 0, 1.0], (n, 1)), np.array([[0.0, 0.0, 1.0]])])
+    AV = np.concatenate([np.zeros((n, 3)), np.array([[0.0, 0.0, omega]])])
+    return Scene(sp, models, iacts, midx, P, np.zeros((n + 1, 3)), OX, OZ, AV)
+
+
 def hopper_params(num_scenes: int = 256, seed: int = 2025, n_lo: int = 1000, n_hi: int = 50000):
     """Per-scene draws of the hopper batch: (n, seed, friction, restitution, orifice)."""
     rng = np.random.default_rng(seed)
