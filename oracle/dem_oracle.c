@@ -739,6 +739,73 @@ static void sort_records(record_t* r, unsigned* n) {
     *n = m;
 }
 
+/* What SimMediator's constructor does once before the first step (SimMediator.cpp:125-134):
+   Consultant::CleanUp (Consultant.cpp:264-319) with the zone of interest as Boundary::Correct
+   leaves it (Boundary.cpp:79-128: bounds sorted per axis, an axis on where they differ).
+   Mobile objects outside the zone are erased; ElementMappingJump holds minus the number erased
+   up to and including each object (unsigned); IactRecordTab::ModifyPair (IactRecordTab.cpp:41-69)
+   moves every record whose key changes to its new key, in key order, overwriting what is there;
+   the survivors keep their order. */
+static int zoi_cleanup(dp_world* w, const vedo_scene_desc* sc) {
+    double lo[3], hi[3];
+    int sw[3], active = 0;
+    for (int k = 0; k < 3; ++k) {
+        lo[k] = sc->zoi_lower[k] < sc->zoi_upper[k] ? sc->zoi_lower[k] : sc->zoi_upper[k];
+        hi[k] = sc->zoi_lower[k] < sc->zoi_upper[k] ? sc->zoi_upper[k] : sc->zoi_lower[k];
+        sw[k] = lo[k] != hi[k];
+        active |= sw[k];
+    }
+    if (!active) return 0;
+    const unsigned n = w->n;
+    unsigned* jump = (unsigned*)malloc(sizeof(unsigned) * (n ? n : 1));
+    char* gone = (char*)calloc(n ? n : 1, 1);
+    unsigned dead = 0, nerased = 0;
+    for (unsigned u = 0; u < n; ++u) {
+        int out = 0;
+        for (int k = 0; k < 3; ++k) {
+            const double p = w->pos[3 * (size_t)u + k];
+            if (sw[k] && (p < lo[k] || p > hi[k])) out = 1;       /* Boundary::InBoundary */
+        }
+        if (w->models[w->model_of[u]].behavior == VEDO_MOBILE && out) { gone[u] = 1; --dead; ++nerased; }
+        jump[u] = dead;
+    }
+    if (nerased) {
+        /* ModifyPair on the records (sorted by key): unchanged keys stay; moved ones take their new
+           key, the last moved onto a key (in key order) over earlier ones and over a record there */
+        record_t* all = (record_t*)calloc(w->nrec ? w->nrec : 1, sizeof(record_t));
+        unsigned moved = 0, total = 0;
+        for (unsigned q = 0; q < w->nrec; ++q) {
+            record_t r = w->rec[q];
+            const unsigned na = r.a + (r.a < n ? jump[r.a] : 0u), nb = r.b + (r.b < n ? jump[r.b] : 0u);
+            if (na != r.a || nb != r.b) { r.a = na; r.b = nb; r.ord = w->nrec - 1 - moved; ++moved; }
+            else r.ord = w->nrec + q;
+            all[total++] = r;
+        }
+        qsort(all, total, sizeof(record_t), rec_cmp);
+        unsigned m = 0;
+        for (unsigned k = 0; k < total; ++k)
+            if (m == 0 || rec_key_cmp(&all[k], &all[m - 1]) != 0) all[m++] = all[k];
+        free(w->rec);
+        w->rec = all;
+        w->nrec = m;
+        /* DOContainer::Erase, DOWorld::EraseDOStatus */
+        double* arrs[9] = {w->pos, w->vel, w->av, w->ox, w->oz, w->imp, w->aimp, w->J, w->JA};
+        unsigned v = 0;
+        for (unsigned u = 0; u < n; ++u) {
+            if (gone[u]) continue;
+            w->model_of[v] = w->model_of[u];
+            w->sudo[v] = w->sudo[u];
+            for (int a = 0; a < 9; ++a)
+                for (int k = 0; k < 3; ++k) arrs[a][3 * (size_t)v + k] = arrs[a][3 * (size_t)u + k];
+            ++v;
+        }
+        w->n = v;
+    }
+    free(jump);
+    free(gone);
+    return (int)nerased;
+}
+
 static const record_t* find_record(const dp_world* w, unsigned a, unsigned b) {  /* IactRecordTab.cpp:20-25 */
     record_t key;
     key.a = a; key.b = b;
@@ -782,11 +849,10 @@ static int rebuild_records(dp_world* w) {
 /* ------------------------------------------------------------------------ */
 dp_world* dp_create(const vedo_scene_desc* sc, unsigned up_iact, char* err, size_t errlen) {
     if (!sc || !sc->num_objects) { set_err(err, errlen, "empty scene"); return NULL; }
-    if (sc->pbc_switch[0] || sc->pbc_switch[1] || sc->pbc_switch[2]) {
+    /* Boundary::Correct (Boundary.cpp:79-128): an axis is on where its bounds differ */
+    if (sc->pbc_lower[0] != sc->pbc_upper[0] || sc->pbc_lower[1] != sc->pbc_upper[1] ||
+        sc->pbc_lower[2] != sc->pbc_upper[2]) {
         set_err(err, errlen, "periodic boundary not supported"); return NULL;
-    }
-    if (sc->zoi_switch[0] || sc->zoi_switch[1] || sc->zoi_switch[2]) {
-        set_err(err, errlen, "zone of interest not supported"); return NULL;
     }
     dp_world* w = (dp_world*)calloc(1, sizeof(dp_world));
     w->t_start = sc->time_start; w->t_stop = sc->time_stop; w->dt = sc->time_interval; w->t = sc->time_current;
@@ -877,6 +943,7 @@ dp_world* dp_create(const vedo_scene_desc* sc, unsigned up_iact, char* err, size
         if (sc->record_shear) R->st.shear = ld3(sc->record_shear + 3 * r);
     }
     sort_records(w->rec, &w->nrec);
+    zoi_cleanup(w, sc);
     int rc = nbs_reset(w);
     if (rc == 0) rc = initiate(w);
     if (rc != 0) {

@@ -7,7 +7,7 @@ reference reads it (.ido bytes), the run parameters and the reference's results:
 final object state, candidate list (IactPairTab order), interaction list
 (slave/master, active flag, shear history, kn, contact flag) and energies.
 
-    python tests/golden/make_golden.py
+    python tests/golden/make_golden.py [case ...]      # all cases, or the named ones
 """
 import os
 import sys
@@ -29,13 +29,40 @@ def cases():
     yield "cluster_poly_orbital_cyl", scenes.cluster(n=48, solver="ISwH", polydisperse=True, orbital=True,
                                                      cylinders=3, steps=300, seed=9), 200, 3
     yield "cluster_bsdbf_upiact1", scenes.cluster(n=27, solver="ISwBSDBF", steps=200, seed=2), 150, 1
+    yield "cluster_zoi", zoi_scene(), 200, 5
+
+
+def zoi_scene():
+    """A settled LSD cluster (the reference's own .ido after 150 steps, with contact records)
+    given a zone of interest in z that leaves about a quarter of the spheres outside: the
+    reference erases them before the first step (Consultant::CleanUp) and re-keys the records
+    (IactRecordTab::ModifyPair), walls included, since they follow the spheres."""
+    import tempfile
+    from oracle import RefWorld
+    from vedo_gb300.scene import Boundary, Scene
+    sc = scenes.cluster(n=48, solver="ISwBSDBF", steps=400, seed=5)
+    w = RefWorld(sc, up_iact=5)
+    w.run(150)
+    with tempfile.TemporaryDirectory() as td:
+        path = os.path.join(td, "w.ido")
+        w.write_ido(path)
+        w.close()
+        out = Scene.from_ido(path)
+    mobile = [k for k, m in enumerate(out.model_index) if out.models[m].behavior == 3]
+    z = np.sort(out.position[mobile, 2])
+    cut = 0.5 * (z[3 * len(z) // 4 - 1] + z[3 * len(z) // 4])
+    out.sp.zoi = Boundary(switch=(False, False, True), lower=(0.0, 0.0, float(z[0]) - 1.0), upper=(0.0, 0.0, cut))
+    return out
 
 
 def main():
     import oracle
     oracle.build_ref()
     from oracle import RefWorld
+    only = set(sys.argv[1:])
     for name, sc, steps, up in cases():
+        if only and name not in only:
+            continue
         ido = sc.to_ido()
         w = RefWorld(sc, up_iact=up)
         cf0, cs0 = w.candidates()

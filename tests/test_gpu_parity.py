@@ -19,7 +19,8 @@ pytestmark = pytest.mark.gpu
 
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 GOLDEN = sorted(glob.glob(os.path.join(ROOT, "tests", "golden", "*.npz")))
-EXACT_CASES = ("box_lsd", "cluster_ISwBSDBF", "cluster_ISwBtSDBF", "cluster_ISwBSDB2F", "cluster_bsdbf_upiact1")
+EXACT_CASES = ("box_lsd", "cluster_ISwBSDBF", "cluster_ISwBtSDBF", "cluster_ISwBSDB2F", "cluster_bsdbf_upiact1",
+               "cluster_zoi")
 STATE = ("position", "velocity", "angular_velocity", "impact", "angular_impact", "orientation_x", "orientation_z")
 
 
@@ -213,3 +214,18 @@ def test_engine_from_xml_equals_engine_from_ido(engine_lib, tmp_path):
     sa, sb = a.state(), b.state()
     for k in sa:
         assert np.array_equal(sa[k], sb[k]), k
+
+
+def test_zone_of_interest_cleanup_in_both_forms(engine_lib):
+    """A world with a zone of interest loses its mobile objects outside the zone before the first
+    step, in both forms, and the survivors' contact sets agree."""
+    g = np.load(os.path.join(ROOT, "tests", "golden", "cluster_zoi.npz"))
+    sc = Scene.from_ido(g["ido"].tobytes())
+    a = engine_lib.GpuEngine(sc, up_iact=int(g["up_iact"]))
+    b = engine_lib.GpuEngine(sc, up_iact=int(g["up_iact"]), precision=1)
+    assert a.n == b.n == g["state_position"].shape[0] < sc.num_objects
+    ia, ib = a.interactions(), b.interactions()
+    A = set(zip(ia["first"][ia["active"] == 1].tolist(), ia["second"][ia["active"] == 1].tolist()))
+    B = set(zip(ib["first"][ib["active"] == 1].tolist(), ib["second"][ib["active"] == 1].tolist()))
+    assert A == B
+    np.testing.assert_array_equal(a.state(("position",))["position"], b.state(("position",))["position"])

@@ -13,7 +13,8 @@ from vedo_gb300.scene import Scene
 
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 GOLDEN = sorted(glob.glob(os.path.join(ROOT, "tests", "golden", "*.npz")))
-EXACT_CASES = ("box_lsd", "cluster_ISwBSDBF", "cluster_ISwBtSDBF", "cluster_ISwBSDB2F", "cluster_bsdbf_upiact1")
+EXACT_CASES = ("box_lsd", "cluster_ISwBSDBF", "cluster_ISwBtSDBF", "cluster_ISwBSDB2F", "cluster_bsdbf_upiact1",
+               "cluster_zoi")
 
 
 def _name(p):
@@ -80,12 +81,32 @@ def test_ido_roundtrip_bytes():
 
 def test_golden_ido_parses():
     """Every fixture's .ido (written by our writer, read by the reference when the fixtures were
-    made) parses back into the same object count and models."""
+    made) parses back into the same object count and models (less the objects a zone of interest
+    erased before the first step)."""
     for p in GOLDEN:
         g = np.load(p)
         sc = Scene.from_ido(g["ido"].tobytes())
-        assert sc.num_objects == g["state_position"].shape[0]
+        if not sc.sp.zoi.active:
+            assert sc.num_objects == g["state_position"].shape[0]
+        else:
+            assert sc.num_objects > g["state_position"].shape[0]
         assert sc.to_ido() == g["ido"].tobytes()
+
+
+def test_zoi_cleanup_erases_and_rekeys_like_the_reference(port_lib):
+    """The zone-of-interest fixture: the reference erased the mobile objects above the zone
+    before its first step and re-keyed the contact records; the oracle does the same (its
+    candidate list at step 0 equals the reference's, record aliasing included)."""
+    from oracle import PortWorld
+    g = np.load(os.path.join(ROOT, "tests", "golden", "cluster_zoi.npz"))
+    sc = Scene.from_ido(g["ido"].tobytes())
+    mobile = [k for k, m in enumerate(sc.model_index) if sc.models[m].behavior == 3]
+    above = [k for k in mobile if sc.position[k, 2] > sc.sp.zoi.upper[2]]
+    assert len(above) > 0 and any(a in above or b in above for a, b in zip(sc.records.first, sc.records.second))
+    w = PortWorld(sc, up_iact=int(g["up_iact"]))
+    assert w.n == sc.num_objects - len(above) == g["state_position"].shape[0]
+    f0, s0 = w.candidates()
+    assert np.array_equal(f0, g["cand0_first"]) and np.array_equal(s0, g["cand0_second"])
 
 
 def test_truncated_ido_rejected():

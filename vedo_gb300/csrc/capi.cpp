@@ -15,7 +15,8 @@ struct vedo_gpu_engine {
 namespace {
 thread_local std::string g_create_error;
 
-int create_common(const vedo::HScene& s, const vedo_engine_opts* opts, vedo_gpu_engine** out) {
+int create_common(vedo::HScene& s, const vedo_engine_opts* opts, vedo_gpu_engine** out) {
+    vedo::prepare_scene(s);
     vedo_engine_opts o;
     vedo_gpu_default_opts(&o);
     if (opts) o = *opts;
@@ -234,6 +235,7 @@ int vedo_gpu_create_batch(const vedo_scene_desc* const* scenes, uint32_t num_sce
             g_create_error = "scene " + std::to_string(k) + ": " + (scenes[k] ? err : std::string("NULL"));
             return scenes[k] ? VEDO_ERR_INVALID_SCENE : VEDO_ERR_INVALID_ARGUMENT;
         }
+        vedo::prepare_scene(hs[k]);
         ptrs[k] = &hs[k];
     }
     vedo_gpu_engine* e = new (std::nothrow) vedo_gpu_engine();

@@ -2,6 +2,7 @@
 // DOModel / IactModel flattening into device tables.
 #include "scene_host.h"
 
+#include <algorithm>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -340,13 +341,101 @@ bool scene_from_desc(const vedo_scene_desc* d, HScene& s, std::string& err) {
 }
 
 // ------------------------------------------------------------------------------------
+namespace {
+void correct_boundary(uint8_t sw[3], double lo[3], double hi[3]) {
+    for (int k = 0; k < 3; ++k) {
+        const double a = std::min(lo[k], hi[k]), b = std::max(lo[k], hi[k]);
+        lo[k] = a;
+        hi[k] = b;
+        sw[k] = a != b ? 1 : 0;
+    }
+}
+}  // namespace
+
+uint32_t prepare_scene(HScene& s) {
+    correct_boundary(s.zoi_switch, s.zoi_lower, s.zoi_upper);
+    correct_boundary(s.pbc_switch, s.pbc_lower, s.pbc_upper);
+    if (!(s.zoi_switch[0] || s.zoi_switch[1] || s.zoi_switch[2])) return 0;
+    // Boundary::InBoundary (Boundary.cpp:161-190): outside when below or above a switched axis
+    auto inside = [&](uint32_t i) {
+        for (int k = 0; k < 3; ++k) {
+            const double p = s.pos[3 * (size_t)i + k];
+            if (s.zoi_switch[k] && (p < s.zoi_lower[k] || p > s.zoi_upper[k])) return false;
+        }
+        return true;
+    };
+    // ElementMappingJump: minus the number of erased objects up to and including this one
+    // (unsigned, as the reference's _uint_t arithmetic)
+    std::vector<uint32_t> jump(s.n), erased;
+    uint32_t dead = 0;
+    for (uint32_t i = 0; i < s.n; ++i) {
+        const uint32_t m = s.model_of[i];
+        if (m < s.models.size() && s.models[m].behavior == VEDO_MOBILE && !inside(i)) {
+            erased.push_back(i);
+            --dead;
+        }
+        jump[i] = dead;
+    }
+    if (erased.empty()) return 0;
+    // ModifyPair: every record whose key changes is moved to its new key, overwriting whatever
+    // is there (in key order); records of erased objects are re-keyed the same way
+    HRecords& R = s.rec;
+    using Key = std::pair<uint32_t, uint32_t>;
+    std::map<Key, size_t> tab;
+    for (size_t q = 0; q < R.size(); ++q) tab[Key(R.first[q], R.second[q])] = q;
+    auto j = [&](uint32_t id) { return id < s.n ? jump[id] : 0u; };   // std::map::operator[] default
+    std::vector<Key> gone;
+    std::map<Key, size_t> extra;
+    for (const auto& kv : tab) {
+        const Key nk(kv.first.first + j(kv.first.first), kv.first.second + j(kv.first.second));
+        if (nk != kv.first) {
+            gone.push_back(kv.first);
+            extra[nk] = kv.second;
+        }
+    }
+    for (const Key& k : gone) tab.erase(k);
+    for (const auto& kv : extra) tab[kv.first] = kv.second;
+    HRecords N;
+    for (const auto& kv : tab) {
+        const size_t q = kv.second;
+        N.first.push_back(kv.first.first);
+        N.second.push_back(kv.first.second);
+        N.contact.push_back(R.contact[q]);
+        N.bond.push_back(R.bond[q]);
+        N.kn.push_back(R.kn[q]);
+        N.v0.push_back(R.v0[q]);
+        N.overlap.push_back(R.overlap[q]);
+        for (int k = 0; k < 3; ++k) {
+            N.shear.push_back(R.shear[3 * q + k]);
+            N.point.push_back(R.point[3 * q + k]);
+            N.dirn.push_back(R.dirn[3 * q + k]);
+            N.imp.push_back(R.imp[3 * q + k]);
+            N.aimp.push_back(R.aimp[3 * q + k]);
+        }
+    }
+    R = std::move(N);
+    // DOWorld::EraseDOStatus / DOContainer::Erase: the survivors keep their order
+    std::vector<uint8_t> keep(s.n, 1);
+    for (uint32_t i : erased) keep[i] = 0;
+    uint32_t w = 0;
+    for (uint32_t i = 0; i < s.n; ++i) {
+        if (!keep[i]) continue;
+        s.model_of[w] = s.model_of[i];
+        if (i < s.ids.size() && w < s.ids.size()) s.ids[w] = s.ids[i];
+        for (std::vector<double>* v : {&s.pos, &s.vel, &s.ox, &s.oz, &s.av, &s.imp, &s.aimp})
+            for (int k = 0; k < 3; ++k) (*v)[3 * (size_t)w + k] = (*v)[3 * (size_t)i + k];
+        ++w;
+    }
+    s.n = w;
+    s.model_of.resize(w);
+    if (s.ids.size() > w) s.ids.resize(w);
+    for (std::vector<double>* v : {&s.pos, &s.vel, &s.ox, &s.oz, &s.av, &s.imp, &s.aimp}) v->resize(3 * (size_t)w);
+    return (uint32_t)erased.size();
+}
+
 int build_tables(const HScene& s, Tables& t, std::string& err) {
     if (s.pbc_switch[0] || s.pbc_switch[1] || s.pbc_switch[2]) {
         err = "periodic boundary conditions are not implemented";
-        return VEDO_ERR_UNSUPPORTED_MODEL;
-    }
-    if (s.zoi_switch[0] || s.zoi_switch[1] || s.zoi_switch[2]) {
-        err = "zone-of-interest clean-up is not implemented";
         return VEDO_ERR_UNSUPPORTED_MODEL;
     }
     if (s.n == 0) { err = "empty world"; return VEDO_ERR_INVALID_SCENE; }

@@ -56,6 +56,13 @@ bool scene_from_desc(const vedo_scene_desc* d, HScene& s, std::string& err);
 // DOWorldSchema XML (DOWorld_ReadXML.cpp / DOWorld_WriteXML.cpp layout); xml_io.cpp
 bool read_xml(const std::string& path, HScene& s, std::string& err);
 bool write_xml(const std::string& path, const HScene& s, std::string& err);
+// What the reference does to a world before its first step: Boundary::Correct on the zone of
+// interest and the periodic boundary (Boundary.cpp:79-128), then Consultant::CleanUp
+// (Consultant.cpp:264-319), which SimMediator's constructor runs once (SimMediator.cpp:125-134):
+// mobile objects outside an active zone of interest are erased, the others renumbered, and the
+// pair records re-keyed as IactRecordTab::ModifyPair does (IactRecordTab.cpp:41-69).  Returns
+// the number of erased objects.
+uint32_t prepare_scene(HScene& s);
 
 // Flattened constants for the device.
 struct Tables {

@@ -309,6 +309,7 @@ int vedo_srv_submit(vedo_server* s, const vedo_scene_desc* scene, uint64_t steps
         s->err = err;
         return VEDO_ERR_INVALID_SCENE;
     }
+    vedo::prepare_scene(j->scene);
     j->num_objects = j->scene.n;
     for (uint32_t i = 0; i < j->scene.n; ++i) {
         const uint32_t m = j->scene.model_of[i];
