@@ -253,6 +253,15 @@ uint64_t vedo_gpu_step_count(const vedo_gpu_engine* e);
  * a few vedo_gpu_run calls.  For a batch: scene 0. */
 uint64_t vedo_gpu_steps_remaining(const vedo_gpu_engine* e);
 
+/* One time step with an external impulse and angular impulse for every object, as
+ * SimMediator::Run(external impacts) (SimMediator.cpp:987-1119, the coupling entry): they are
+ * added after the field and constrained impulses (DOContainer::AddImpact), before the response.
+ * impulse, angular_impulse: host [n][3] arrays in object order (NULL = zeros).  keep_running as
+ * vedo_gpu_run.  In the MIXED form they join the spheres' FP32 compensated sums; fixed and
+ * orbital walls do not respond to impulses in either form. */
+int vedo_gpu_run_with_impulses(vedo_gpu_engine* e, const double* impulse, const double* angular_impulse,
+                               int* keep_running);
+
 /* MIXED form: the number of spheres whose next step skips the neighbour-list walk (every pair
  * certainly apart since the last rebuild and its history clean; results are those of a full
  * walk).  A measure of how much of the list the skin keeps idle.  FP64 form: 0. */

@@ -229,3 +229,32 @@ def test_zone_of_interest_cleanup_in_both_forms(engine_lib):
     B = set(zip(ib["first"][ib["active"] == 1].tolist(), ib["second"][ib["active"] == 1].tolist()))
     assert A == B
     np.testing.assert_array_equal(a.state(("position",))["position"], b.state(("position",))["position"])
+
+
+@pytest.mark.parametrize("precision", [0, 1])
+def test_external_impulses_equal_a_constant_external_force(precision, engine_lib):
+    """vedo_gpu_run_with_impulses (SimMediator::Run with external impacts): a step that adds
+    F dt to every sphere equals a step of the same world whose sphere model carries the external
+    force F (DiscreteObject::AddConstrainedImpact adds dt F just before): bit for bit in the
+    FP64 form (the same sums in the same order), within FP32 roundings in the MIXED form."""
+    import copy
+    F = np.array([0.02, -0.01, 0.005])
+    sa = scenes.cluster(n=48, solver="ISwBSDBF", steps=400, seed=5)
+    sb = copy.deepcopy(sa)
+    sa.models[0].external_force = tuple(F)
+    dt = sa.sp.time_interval
+    a = engine_lib.GpuEngine(sa, up_iact=5, precision=precision)
+    b = engine_lib.GpuEngine(sb, up_iact=5, precision=precision)
+    imp = np.zeros((b.n, 3))
+    imp[sb.model_index == 0] = F * dt
+    for _ in range(120 if precision == 0 else 3):   # FP32 roundings grow along a chaotic trajectory
+        a.run(1)
+        b.run_with_impulses(imp, None)
+    ra, rb = a.state(), b.state()
+    for k in ("position", "velocity", "angular_velocity", "impact", "angular_impact"):
+        if precision == 0:
+            np.testing.assert_array_equal(ra[k], rb[k], err_msg=k)
+        else:
+            np.testing.assert_allclose(ra[k], rb[k], rtol=1e-5, atol=1e-7 * (np.abs(ra[k]).max() + 1e-30),
+                                       err_msg=k)
+    assert np.abs(ra["velocity"] - scenes.cluster(n=48, solver="ISwBSDBF", steps=400, seed=5).velocity).max() > 0

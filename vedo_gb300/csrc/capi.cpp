@@ -174,6 +174,12 @@ int vedo_gpu_quiet_spheres(vedo_gpu_engine* e, uint64_t* count) {
     return e->p->quiet_spheres(count);
 }
 
+int vedo_gpu_run_with_impulses(vedo_gpu_engine* e, const double* impulse, const double* angular_impulse,
+                               int* keep_running) {
+    if (!e) return VEDO_ERR_INVALID_ARGUMENT;
+    return e->p->run_with_impulses(impulse, angular_impulse, keep_running);
+}
+
 int vedo_gpu_list_status(vedo_gpu_engine* e, double out[6]) {
     if (!e || !out) return VEDO_ERR_INVALID_ARGUMENT;
     return e->p->list_status(out);

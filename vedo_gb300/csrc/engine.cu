@@ -170,9 +170,14 @@ __device__ __forceinline__ void finish_object(uint32_t i, const ModelDev& m, d3 
                                               double4_32a* __restrict__ av, double4_32a* __restrict__ ox,
                                               double4_32a* __restrict__ oz, double4_32a* __restrict__ imp,
                                               double4_32a* __restrict__ aimp, int write_imp, d3 origin,
-                                              float4* __restrict__ pos32, float4* __restrict__ wall32) {
+                                              float4* __restrict__ pos32, float4* __restrict__ wall32,
+                                              const double* __restrict__ ext_imp, const double* __restrict__ ext_aimp) {
     J = add(J, muls(fimp, m.sudo));                           // DOContainer::AddFieldImpact (DOContainer.cpp:25)
     J = add(J, smul(dt, mk(m.ext[0], m.ext[1], m.ext[2])));   // DiscreteObject::AddConstrainedImpact (:160-163)
+    if (ext_imp) {                 // SimMediator::Run(external impacts): DOContainer::AddImpact (SimMediator.cpp:1015-1018)
+        J = add(J, mk(ext_imp[3 * (size_t)i], ext_imp[3 * (size_t)i + 1], ext_imp[3 * (size_t)i + 2]));
+        JA = add(JA, mk(ext_aimp[3 * (size_t)i], ext_aimp[3 * (size_t)i + 1], ext_aimp[3 * (size_t)i + 2]));
+    }
     if (m.behavior != BEH_FIXED) {
         d3 P = ld(pos, i), V = ld(vel, i), AV = ld(av, i), Ox = ld(ox, i), Oz = ld(oz, i);
         respond_object(m, dt, J, JA, P, V, AV, Ox, Oz);
@@ -199,7 +204,8 @@ __global__ void __launch_bounds__(TPB) k_obj(uint32_t n, const uint32_t* __restr
                                              const uint32_t* __restrict__ csr_ptr, const uint32_t* __restrict__ csr_ent,
                                              const uint8_t* __restrict__ flags, const double* __restrict__ out,
                                              double dt, d3 fimp, int write_imp, d3 origin, float4* __restrict__ pos32,
-                                             float4* __restrict__ wall32) {
+                                             float4* __restrict__ wall32, const double* __restrict__ ext_imp,
+                                             const double* __restrict__ ext_aimp) {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     const ModelDev& m = models[model_of[i]];
@@ -210,7 +216,8 @@ __global__ void __launch_bounds__(TPB) k_obj(uint32_t n, const uint32_t* __restr
         const uint32_t ent = csr_ent[e];
         add_entry(ent, flags[ent >> 1], out, J, JA);
     }
-    finish_object(i, m, J, JA, dt, fimp, pos, vel, av, ox, oz, imp, aimp, write_imp, origin, pos32, wall32);
+    finish_object(i, m, J, JA, dt, fimp, pos, vel, av, ox, oz, imp, aimp, write_imp, origin, pos32, wall32, ext_imp,
+                  ext_aimp);
 }
 
 // One warp per scope-global object: lanes load 32 entries at a time, then every lane adds
@@ -221,14 +228,15 @@ __global__ void k_obj_global(uint32_t nglob, const uint32_t* __restrict__ glob, 
                              double4_32a* __restrict__ oz, double4_32a* __restrict__ imp, double4_32a* __restrict__ aimp,
                              const uint32_t* __restrict__ csr_ptr, const uint32_t* __restrict__ csr_ent,
                              const uint8_t* __restrict__ flags, const double* __restrict__ out, double dt, d3 fimp,
-                             int write_imp, d3 origin, float4* __restrict__ pos32, float4* __restrict__ wall32) {
+                             int write_imp, d3 origin, float4* __restrict__ pos32, float4* __restrict__ wall32,
+                             const double* __restrict__ ext_imp, const double* __restrict__ ext_aimp) {
     const uint32_t w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const int lane = threadIdx.x & 31;
     if (w >= nglob) return;
     const uint32_t i = glob[w];
     const ModelDev& m = models[model_of[i]];
     d3 J = mk(0.0, 0.0, 0.0), JA = mk(0.0, 0.0, 0.0);
-    const bool need_sum = write_imp || m.behavior == BEH_MOBILE || m.behavior == BEH_CONSTRAINED;
+    const bool need_sum = write_imp || m.behavior == BEH_MOBILE || m.behavior == BEH_CONSTRAINED || ext_imp;
     if (need_sum) {
         const uint32_t e0 = csr_ptr[i], e1 = csr_ptr[i + 1];
         for (uint32_t base = e0; base < e1; base += 32) {
@@ -263,7 +271,8 @@ __global__ void k_obj_global(uint32_t nglob, const uint32_t* __restrict__ glob, 
         }
     }
     if (lane == 0)
-        finish_object(i, m, J, JA, dt, fimp, pos, vel, av, ox, oz, imp, aimp, write_imp, origin, pos32, wall32);
+        finish_object(i, m, J, JA, dt, fimp, pos, vel, av, ox, oz, imp, aimp, write_imp, origin, pos32, wall32,
+                      ext_imp, ext_aimp);
 }
 
 // Narrow phase only: PF_ACTIVE of every pair at the current positions (the IsActive()
@@ -695,7 +704,7 @@ Engine::~Engine() {
                     d_oz_, d_imp_, d_aimp_, d_global_, d_safe_, d_red_, d_key_, d_key_alt_, d_cell_key_, d_sid_,
                     d_sid_alt_, d_cell_start_, d_cellof_, d_flag_, d_task_, d_total_, d_ck_, d_cv_, d_ck_alt_,
                     d_cv_alt_, d_cnt_, d_rec_key_, d_rec_hist_, d_rec_v0_, d_rec_flags_, d_obs_, d_stage_,
-                    d_pos32_, d_wall32_, d_reach_, d_grid_};
+                    d_pos32_, d_wall32_, d_reach_, d_grid_, d_ext_};
     for (void* p : ptrs) if (p) cudaFree(p);
     for (auto& e : ev_) if (e) cudaEventDestroy(e);
     if (stream_) cudaStreamDestroy(stream_);
@@ -989,13 +998,13 @@ int Engine::step_once(bool write_impulses) {
     const d3 org = mk(origin_[0], origin_[1], origin_[2]);
     k_obj<<<blocks_for(n_), TPB, 0, stream_>>>(n_, d_model_of_, d_models_, d_pos_, d_vel_, d_av_, d_ox_, d_oz_,
                                                d_imp_, d_aimp_, cur_.csr_ptr, cur_.csr_ent, cur_.flags, cur_.out, dt,
-                                               fimp, write_impulses ? 1 : 0, org, d_pos32_, d_wall32_);
+                                               fimp, write_impulses ? 1 : 0, org, d_pos32_, d_wall32_, ext_imp_, ext_aimp_);
     ++launches_;
     if (!global_ids_.empty()) {
         k_obj_global<<<blocks_for((uint64_t)global_ids_.size() * 32), TPB, 0, stream_>>>(
             (uint32_t)global_ids_.size(), d_global_, d_model_of_, d_models_, d_pos_, d_vel_, d_av_, d_ox_, d_oz_,
             d_imp_, d_aimp_, cur_.csr_ptr, cur_.csr_ent, cur_.flags, cur_.out, dt, fimp, write_impulses ? 1 : 0, org,
-            d_pos32_, d_wall32_);
+            d_pos32_, d_wall32_, ext_imp_, ext_aimp_);
         ++launches_;
     }
     if (prof) CK(cudaEventRecord(ev_[2], stream_));
@@ -1054,6 +1063,24 @@ int Engine::run(uint32_t nsteps, int* keep_running) {
     prof_ms_[3] = tot;
     if (keep_running) *keep_running = t_ < t_stop_ ? 1 : 0;   // SimMediator.cpp:839-841
     return VEDO_OK;
+}
+
+// One step with per-object external impulses (SimMediator::Run(external impacts),
+// SimMediator.cpp:987-1119): host [n][3] arrays, NULL adds zeros as the reference adds them.
+int Engine::run_with_impulses(const double* impulse, const double* angular_impulse, int* keep_running) {
+    CK(cudaSetDevice(device_));
+    if (!d_ext_) CK(cudaMalloc(&d_ext_, 2 * 24 * (size_t)n_));
+    const double* src[2] = {impulse, angular_impulse};
+    for (int k = 0; k < 2; ++k) {
+        double* dst = d_ext_ + (size_t)k * 3 * n_;
+        if (src[k]) CK(cudaMemcpyAsync(dst, src[k], 24 * (size_t)n_, cudaMemcpyHostToDevice, stream_));
+        else CK(cudaMemsetAsync(dst, 0, 24 * (size_t)n_, stream_));
+    }
+    ext_imp_ = d_ext_;
+    ext_aimp_ = d_ext_ + 3 * (size_t)n_;
+    const int rc = run(1, keep_running);
+    ext_imp_ = ext_aimp_ = nullptr;
+    return rc;
 }
 
 uint64_t Engine::last_profile(double out[4]) const {

@@ -45,6 +45,7 @@ public:
 
     int init(const HScene& scene, const vedo_engine_opts& opts) override;
     int run(uint32_t nsteps, int* keep_running) override;
+    int run_with_impulses(const double* impulse, const double* angular_impulse, int* keep_running) override;
     int get_state(const vedo_state_view& v) override;
     int set_state(const vedo_state_view& v) override;
     int num_interactions(uint32_t* n) override;
@@ -67,6 +68,8 @@ private:
     int ensure_list(PairList& L, uint32_t cap);
     void free_list(PairList& L);
     int step_once(bool write_impulses);
+    double* d_ext_ = nullptr;                        // [2][n][3] external impulses of run_with_impulses
+    const double *ext_imp_ = nullptr, *ext_aimp_ = nullptr;
     int record_ido();
     int sync_host_state();
     int ensure_stage();

@@ -35,6 +35,7 @@ public:
         *count = 0;
         return VEDO_OK;
     }
+    virtual int run_with_impulses(const double* impulse, const double* angular_impulse, int* keep_running) = 0;
     virtual int list_status(double out[6]) {
         for (int k = 0; k < 6; ++k) out[k] = 0.0;
         return VEDO_OK;

@@ -399,6 +399,7 @@ struct TickArgs {
     uint32_t* nwork;
     const float4* mf;              // [nm][2]: field + external impulse per step, 1/m~; 2.5/(m~ r^2)
     unsigned* vrel_bits;           // max over spheres of the speed relative to the scene's frame
+    const double* ext;             // [2][n][3] external impulse, angular impulse of this step (or nullptr)
     const float2* clear;           // [n] per sphere: every prefilter test of its list says "apart" for
                                    // sphere-pair pads <= x and fixed-wall pads <= y
     uint8_t* qcnt;                 // [n] consecutive clean walks (0..2) since the last rebuild
@@ -533,6 +534,12 @@ __device__ __forceinline__ float2 finish_sphere(const TickArgs& a, uint32_t i, b
     const double dt = S.dt;
     // DOContainer.cpp:20-27, DiscreteObject.cpp:160-163
     J.add(fm(mf0.x, mf0.y, mf0.z));
+    if (a.ext) {                   // SimMediator::Run(external impacts): DOContainer::AddImpact (SimMediator.cpp:1015-1018)
+        const double* e = a.ext + 3 * (size_t)i;
+        const double* ea = a.ext + 3 * ((size_t)a.n + i);
+        J.add(fm((float)e[0], (float)e[1], (float)e[2]));
+        JA.add(fm((float)ea[0], (float)ea[1], (float)ea[2]));
+    }
     if (a.write_imp) {
         st(a.imp, i, J.value(), 0.0);
         st(a.aimp, i, JA.value(), 0.0);
@@ -1792,6 +1799,7 @@ public:
     }
     double scene_time(uint32_t s) const { return s < sc_.size() ? sc_[s].t : 0.0; }
     int quiet_spheres(uint64_t* count) override;
+    int run_with_impulses(const double* impulse, const double* angular_impulse, int* keep_running) override;
     int list_status(double out[6]) override;
     int tuning(float out[5]) const override {
         out[0] = skin_frac_;
@@ -1894,6 +1902,8 @@ private:
     bool quiet_ok_ = true;                        // quiet spheres skip their walk (identical results)
     int sms_ = 1;                                 // streaming multiprocessors of the device
     float2* d_clear_ = nullptr;                   // [n] quiet-sphere pad limits of the current list
+    double* d_ext_ = nullptr;                     // [2][n][3] external impulses of run_with_impulses
+    bool ext_on_ = false;
     unsigned* d_vred_ = nullptr;                  // [scenes][6] velocity ranges at the rebuild
     float pos_eps_ = 0.0f;                        // FP64 rounding of a position update (bound)
     uint8_t* d_qcnt_ = nullptr;                   // [n] clean walks since the rebuild (0..2)
@@ -1965,7 +1975,7 @@ MixedEngine::~MixedEngine() {
     free_nlist(nl_[1]);
     void* ptrs[] = {d_models_, d_params_, d_pc32_, d_geom_, d_rr_, d_mf_, d_reach_, d_model_of_, d_scene_of_,
                     d_scenes_, d_gfield_, d_glob_, d_x_[0], d_x_[1], d_v64_, d_w64_, d_ox_, d_oz_, d_imp_, d_aimp_,
-                    d_v32_[0], d_v32_[1], d_w32_[0], d_w32_[1], d_rr32_, d_xs_[0], d_xs_[1], d_work_, d_clear_, d_vred_, d_qcnt_, d_pos32_, d_wall32_, d_red_, d_sred_, d_disp_, d_err_,
+                    d_v32_[0], d_v32_[1], d_w32_[0], d_w32_[1], d_rr32_, d_xs_[0], d_xs_[1], d_work_, d_clear_, d_vred_, d_ext_, d_qcnt_, d_pos32_, d_wall32_, d_red_, d_sred_, d_disp_, d_err_,
                     d_key_, d_key_alt_, d_sid_, d_sid_alt_, d_cnt_, d_gs_, d_ge_, d_act_, d_stage_, d_obs_, d_gidx_,
                     d_wkey_, d_wval_, d_wkey_alt_, d_wval_alt_, d_wptr_, d_wimp_, d_wred_, d_wrot_, d_wedge_};
     for (void* p : ptrs) if (p) cudaFree(p);
@@ -2349,6 +2359,7 @@ TickArgs MixedEngine::args(bool write_imp) {
     a.mf = d_mf_;
     a.clear = d_clear_;
     a.qcnt = d_qcnt_;
+    a.ext = ext_on_ ? d_ext_ : nullptr;
     return a;
 }
 
@@ -2898,6 +2909,24 @@ int MixedEngine::get_state(const vedo_state_view& v) {
     MCK(cudaStreamSynchronize(stream_));
     MCK(cudaGetLastError());
     return VEDO_OK;
+}
+
+// One step with per-object external impulses (SimMediator::Run(external impacts),
+// SimMediator.cpp:987-1119): added to each sphere's compensated sums after the field and
+// constrained impulses (walls, fixed or orbital, do not respond to impulses).
+int MixedEngine::run_with_impulses(const double* impulse, const double* angular_impulse, int* keep_running) {
+    MCK(cudaSetDevice(opts_.device));
+    if (!d_ext_) MCK(cudaMalloc(&d_ext_, 2 * 24 * (size_t)n_));
+    const double* src[2] = {impulse, angular_impulse};
+    for (int k = 0; k < 2; ++k) {
+        double* dst = d_ext_ + (size_t)k * 3 * n_;
+        if (src[k]) MCK(cudaMemcpyAsync(dst, src[k], 24 * (size_t)n_, cudaMemcpyHostToDevice, stream_));
+        else MCK(cudaMemsetAsync(dst, 0, 24 * (size_t)n_, stream_));
+    }
+    ext_on_ = true;
+    const int rc = run(1, keep_running);
+    ext_on_ = false;
+    return rc;
 }
 
 int MixedEngine::list_status(double out[6]) {

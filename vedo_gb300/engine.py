@@ -211,6 +211,22 @@ class GpuEngine:
         return {"skin": float(sk.value), "cell_scale": float(cs.value), "tick_block": int(tb.value),
                 "stored_splits": bool(ss.value), "split_tick": bool(st.value)}
 
+    def run_with_impulses(self, impulse=None, angular_impulse=None) -> bool:
+        """One step with an external impulse and angular impulse per object ([n, 3] arrays in
+        object order; None = zeros), as the reference's SimMediator::Run(external impacts)."""
+        keep = C.c_int(0)
+        args = []
+        for a in (impulse, angular_impulse):
+            if a is None:
+                args.append(None)
+            else:
+                a = np.ascontiguousarray(a, dtype=np.float64).reshape(self.n, 3)
+                args.append(a)
+        self._check(lib().vedo_gpu_run_with_impulses(self.h, dptr(args[0]) if args[0] is not None else None,
+                                                     dptr(args[1]) if args[1] is not None else None,
+                                                     C.byref(keep)))
+        return bool(keep.value)
+
     def list_status(self) -> Dict[str, float]:
         """Neighbour-list state (MIXED form): steps since the rebuild, rebuilds, displacement
         bounds (relative to the scene frame, absolute, orbital walls) and the share of the
