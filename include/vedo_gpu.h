@@ -52,7 +52,8 @@ enum {
 };
 
 /* ---- enums mirrored from DOModel.h:25-27 (C++11 build) ------------------ */
-enum { VEDO_SHAPE_SPHERE = 1, VEDO_SHAPE_QUASI_CYLINDER = 6, VEDO_SHAPE_QUASI_PLATE = 7 };
+enum { VEDO_SHAPE_SPHERE = 1, VEDO_SHAPE_QUASI_CYLINDER = 6, VEDO_SHAPE_QUASI_PLATE = 7,
+       VEDO_SHAPE_QUASI_PLATE_WITH_CIRCULAR_HOLE = 8 };
 enum { VEDO_CONSTRAINED = 1, VEDO_FIXED = 2, VEDO_MOBILE = 3, VEDO_ORBITAL = 4 };
 enum { VEDO_SCOPE_GLOBAL = 1, VEDO_SCOPE_LOCAL = 2 };
 

@@ -58,7 +58,7 @@ static v3 rotate_around(v3 p, v3 va) {                                          
 }
 
 /* ------------------------------------------------------------------------ */
-enum { CD_NONE = 0, CD_SS = 1, CD_SP = 2, CD_SC = 3 };
+enum { CD_NONE = 0, CD_SS = 1, CD_SP = 2, CD_SC = 3, CD_SHP = 4 };
 enum { IS_NONE = 0, IS_BSDBF = 1, IS_BTSDBF = 2, IS_BSDB2F = 3, IS_HERTZ = 4, IS_H = 5 };
 
 typedef struct {
@@ -191,6 +191,23 @@ static int analyse(model_t* m) {
         m->inertia = smul(k, V3(h * h + l * l, w * w + l * l, h * h + w * w));
         return 1;
     }
+    case VEDO_SHAPE_QUASI_PLATE_WITH_CIRCULAR_HOLE: {      /* DOModel.cpp:90-119 */
+        w = m->a[0]; h = m->a[1]; l = m->a[2];
+        const double hr = m->a[3], hxo = m->a[4], hyo = m->a[5];
+        if (m->scope == VEDO_SCOPE_LOCAL) {
+            double mx = (w > h) ? w : h;
+            mx = (mx > l) ? mx : l;
+            m->range = 0.5 * mx;
+        } else {
+            m->range = 0.5 * h;
+        }
+        if (!((fabs(hxo) <= (0.5 * w - hr)) && (fabs(hyo) <= (0.5 * l - hr)))) return 0;   /* the reference exits */
+        m->volume = w * h * l - hr * hr * PI * h;
+        m->mass = m->density * m->volume;
+        m->sudo_model = m->dfac * m->mass;
+        m->inertia = V3(0.0, 0.0, 0.0);
+        return 1;
+    }
     default:
         return 0;
     }
@@ -204,6 +221,10 @@ static int object_sudo_mass(const model_t* m, double* out) {
     if (m->shape == VEDO_SHAPE_SPHERE) {
         if (m->behavior == VEDO_MOBILE || m->behavior == VEDO_FIXED) { *out = m->sudo_model; return 0; }
         return -1;
+    }
+    if (m->shape == VEDO_SHAPE_QUASI_PLATE_WITH_CIRCULAR_HOLE) {   /* DOFixedQuasiPlateWithCircularHole.cpp:16-19 */
+        if (m->behavior == VEDO_FIXED) { *out = 0.0; return 0; }
+        return -1;           /* the mobile one (DOQuasiPlateWithCircularHole) is not restated */
     }
     if (m->shape == VEDO_SHAPE_QUASI_PLATE || m->shape == VEDO_SHAPE_QUASI_CYLINDER) {
         switch (m->behavior) {
@@ -254,7 +275,8 @@ static int cal_distance(const dp_world* w, unsigned i, unsigned j, double* out) 
         *out = len(sub(pi, pj));
         return 0;
     }
-    if (mi->shape == VEDO_SHAPE_SPHERE && mj->shape == VEDO_SHAPE_QUASI_PLATE) {     /* :294-334 */
+    if (mi->shape == VEDO_SHAPE_SPHERE && (mj->shape == VEDO_SHAPE_QUASI_PLATE ||
+                                           mj->shape == VEDO_SHAPE_QUASI_PLATE_WITH_CIRCULAR_HOLE)) {   /* :294-370 */
         v3 Ca = pi, Cb = pj, Oz = ld3(w->oz + 3 * j), Ox = ld3(w->ox + 3 * j);
         v3 Oy = cross(Oz, Ox);
         v3 Cap = sub(Ca, project_on(sub(Ca, Cb), Oz));
@@ -447,6 +469,7 @@ static int create_interaction(const dp_world* w, unsigned p1, unsigned p2, iactn
     if (ms->shape == VEDO_SHAPE_SPHERE && mm->shape == VEDO_SHAPE_SPHERE) cd = CD_SS;
     else if (ms->shape == VEDO_SHAPE_SPHERE && mm->shape == VEDO_SHAPE_QUASI_PLATE) cd = CD_SP;
     else if (ms->shape == VEDO_SHAPE_SPHERE && mm->shape == VEDO_SHAPE_QUASI_CYLINDER) cd = CD_SC;
+    else if (ms->shape == VEDO_SHAPE_SPHERE && mm->shape == VEDO_SHAPE_QUASI_PLATE_WITH_CIRCULAR_HOLE) cd = CD_SHP;
     const iact_t* im = &w->iacts[ia];
     if (cd == CD_NONE || im->eq == IS_NONE) return 2;
     for (int k = 0; MECH_NAMES[im->eq][k]; ++k)
@@ -501,6 +524,29 @@ static void detect(const dp_world* w, iactn_t* I) {
         v3 Caps = add(add(muls(Ox, dx), muls(Oy, dy)), Pm);
         v3 vIm = sub(Caps, Ps);
         ci->depth = ra + hh - len(vIm);
+        ci->dirn = dir(vIm);
+    } else if (I->cd == CD_SHP) {                            /* CDSphere2QuasiPlateWithCircularHole.cpp:15-133 */
+        v3 Oz = ld3(w->oz + 3 * m), Ox = ld3(w->ox + 3 * m);
+        v3 Oy = cross(Oz, Ox);
+        v3 Cap = sub(Ps, project_on(sub(Ps, Pm), Oz));
+        double hh = 0.5 * mm->a[1], hw = 0.5 * mm->a[0], hl = 0.5 * mm->a[2];
+        double hr = mm->a[3], hxo = mm->a[4], hyo = mm->a[5];
+        v3 Ch = add(Pm, V3(hxo, hyo, 0.0));          /* world-frame offsets, as the reference adds them */
+        v3 Cha = sub(Ps, Ch);
+        double dx = dot(sub(Cap, Pm), Ox);
+        if (dx < -hw) dx = -hw; else if (dx > hw) dx = hw;
+        double dy = dot(sub(Cap, Pm), Oy);
+        if (dy < -hl) dy = -hl; else if (dy > hl) dy = hl;
+        double dahx = dot(Cha, Ox), dahy = dot(Cha, Oy);
+        double dah = sqrt(dahx * dahx + dahy * dahy);
+        if (dah < hr) {
+            if (dah == 0.0) { dx = hxo; dy = hyo; }
+            else { dx = hxo + dahx / dah * hr; dy = hyo + dahy / dah * hr; }
+        }
+        v3 Caps = add(add(muls(Ox, dx), muls(Oy, dy)), Pm);
+        v3 vIm = sub(Caps, Ps);
+        if (dah == 0.0) ci->depth = ra + hh - sqrt(len(vIm) * len(vIm) + hr * hr);
+        else ci->depth = ra + hh - len(vIm);
         ci->dirn = dir(vIm);
     } else {                                                 /* CDSphere2QuasiCylinder.cpp:16-80 */
         double hh = 0.5 * mm->a[1];

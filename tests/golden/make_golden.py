@@ -30,6 +30,7 @@ def cases():
                                                      cylinders=3, steps=300, seed=9), 200, 3
     yield "cluster_bsdbf_upiact1", scenes.cluster(n=27, solver="ISwBSDBF", steps=200, seed=2), 150, 1
     yield "cluster_zoi", zoi_scene(), 200, 5
+    yield "holed_plate_lsd", scenes.holed_plate_drop(steps=500), 400, 5
 
 
 def zoi_scene():

@@ -257,3 +257,23 @@ def test_spinning_plate_corners_reach_spheres_beyond_its_list(engine_lib):
             assert np.array_equal(sa[k], sb[k]), (n, k)
     v = a.state(("velocity",))["velocity"][:8]
     assert (np.linalg.norm(v, axis=1) > 0.1).sum() >= 4          # the first four were struck
+
+
+def test_plate_with_circular_hole_mixed_against_fp64(engine_lib, tmp_path):
+    """Spheres on a plate with an off-centre circular hole (the reference's
+    QuasiPlateWithCircularHole): from identical state, the mixed form's contact set equals the
+    FP64 form's (pinned to the reference by the golden fixture) and its one-step impulses agree
+    within 1e-5."""
+    sc = scenes.holed_plate_drop(steps=2000)
+    f64 = engine_lib.GpuEngine(sc, up_iact=5)
+    f64.run(150)
+    path = str(tmp_path / "h.ido")
+    f64.write_ido(path)
+    a = engine_lib.GpuEngine(path, up_iact=5)
+    b = engine_lib.GpuEngine(path, up_iact=5, precision=1)
+    A, B = _active_set(a.interactions()), _active_set(b.interactions())
+    assert len(A) >= 4 and A == B
+    a.run(1)
+    b.run(1)
+    sa, sb = a.state(("impact",)), b.state(("impact",))
+    assert np.linalg.norm(sa["impact"] - sb["impact"]) <= 1e-5 * np.linalg.norm(sa["impact"])

@@ -20,7 +20,7 @@ pytestmark = pytest.mark.gpu
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 GOLDEN = sorted(glob.glob(os.path.join(ROOT, "tests", "golden", "*.npz")))
 EXACT_CASES = ("box_lsd", "cluster_ISwBSDBF", "cluster_ISwBtSDBF", "cluster_ISwBSDB2F", "cluster_bsdbf_upiact1",
-               "cluster_zoi")
+               "cluster_zoi", "holed_plate_lsd")
 STATE = ("position", "velocity", "angular_velocity", "impact", "angular_impact", "orientation_x", "orientation_z")
 
 

@@ -14,7 +14,7 @@ from vedo_gb300.scene import Scene
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 GOLDEN = sorted(glob.glob(os.path.join(ROOT, "tests", "golden", "*.npz")))
 EXACT_CASES = ("box_lsd", "cluster_ISwBSDBF", "cluster_ISwBtSDBF", "cluster_ISwBSDB2F", "cluster_bsdbf_upiact1",
-               "cluster_zoi")
+               "cluster_zoi", "holed_plate_lsd")
 
 
 def _name(p):
@@ -182,3 +182,15 @@ def test_abi_bad_ido_is_reported(engine_lib, tmp_path):
     rc = lib.vedo_gpu_create_from_ido(str(p).encode(), None, ctypes.byref(h))
     assert rc == 7
     assert b"truncated" in lib.vedo_gpu_last_error(None)
+
+
+def test_holed_plate_model_analysis():
+    """DOModel::Analysis of a plate with a circular hole (DOModel.cpp:90-119): the range of a
+    plate, the hole's volume taken out, no inertia; a hole outside the plate is an error."""
+    from vedo_gb300.scene import DOModel, FIXED, GLOBAL, QUASI_PLATE_WITH_CIRCULAR_HOLE
+    m = DOModel("H", "W", FIXED, GLOBAL, 7800.0, 1.0, QUASI_PLATE_WITH_CIRCULAR_HOLE, (0.1, 0.01, 0.2, 0.02, 0.01, -0.03))
+    rng, vol, mass, sm, inertia = m.analysis()
+    assert rng == 0.5 * 0.01 and vol == 0.1 * 0.01 * 0.2 - 0.02 * 0.02 * np.pi * 0.01 and inertia == (0.0, 0.0, 0.0)
+    bad = DOModel("H", "W", FIXED, GLOBAL, 7800.0, 1.0, QUASI_PLATE_WITH_CIRCULAR_HOLE, (0.1, 0.01, 0.2, 0.04, 0.02, 0.0))
+    with pytest.raises(ValueError):
+        bad.analysis()

@@ -14,6 +14,7 @@ namespace vedo {
 struct PairGeom {
     double ra;               // slave sphere radius
     double b0, b1, b2;       // master attributes (sphere r | cylinder r, h | plate w, h, l)
+    double hr, hxo, hyo;     // holed plate: hole radius and offsets (CD_SHP only)
 };
 
 struct PairParamFull {
@@ -41,6 +42,37 @@ __device__ __forceinline__ void detect_pair(int cd, const PairGeom& g, d3 Ps, d3
         d3 Caps = add(add(muls(Ox, dx), muls(Oy, dy)), Pm);
         d3 vIm = sub(Caps, Ps);
         depth = g.ra + hh - len(vIm);
+        n = dir(vIm);
+    } else if (cd == CD_SHP) {                                // CDSphere2QuasiPlateWithCircularHole.cpp:15-133
+        d3 Oz = ld(oz, m), Ox = ld(ox, m);
+        d3 Oy = cross(Oz, Ox);
+        d3 Cap = sub(Ps, project_on(sub(Ps, Pm), Oz));
+        double hh = 0.5 * g.b1, hw = 0.5 * g.b0, hl = 0.5 * g.b2;
+        // the hole's centre: the offsets are added in world coordinates, as the reference does
+        d3 Cha = sub(Ps, add(Pm, mk(g.hxo, g.hyo, 0.0)));
+        double dx = dot(sub(Cap, Pm), Ox);
+        if (dx < -hw) dx = -hw; else if (dx > hw) dx = hw;
+        double dy = dot(sub(Cap, Pm), Oy);
+        if (dy < -hl) dy = -hl; else if (dy > hl) dy = hl;
+        double dahx = dot(Cha, Ox), dahy = dot(Cha, Oy);
+        double dah = sqrt(dahx * dahx + dahy * dahy);
+        if (dah < g.hr) {
+            if (dah == 0.0) {
+                dx = g.hxo;
+                dy = g.hyo;
+            } else {
+                dx = g.hxo + dahx / dah * g.hr;
+                dy = g.hyo + dahy / dah * g.hr;
+            }
+        }
+        d3 Caps = add(add(muls(Ox, dx), muls(Oy, dy)), Pm);
+        d3 vIm = sub(Caps, Ps);
+        if (dah == 0.0) {
+            const double lv = len(vIm);
+            depth = g.ra + hh - sqrt(lv * lv + g.hr * g.hr);
+        } else {
+            depth = g.ra + hh - len(vIm);
+        }
         n = dir(vIm);
     } else {                                                  // CDSphere2QuasiCylinder.cpp:16-80
         double hh = 0.5 * g.b1;
@@ -246,7 +278,8 @@ __device__ __forceinline__ double cal_distance(const ModelDev& mi_, const ModelD
     ok = true;
     d3 pi = ld(pos, i), pj = ld(pos, j);
     if (mi->shape == SHAPE_SPHERE && mj->shape == SHAPE_SPHERE) return len(sub(pi, pj));
-    if (mi->shape == SHAPE_SPHERE && mj->shape == SHAPE_PLATE) {
+    // sphere - plate, and sphere - plate with a hole (DOMap.cpp:336-370: the hole is ignored)
+    if (mi->shape == SHAPE_SPHERE && (mj->shape == SHAPE_PLATE || mj->shape == SHAPE_HOLED)) {
         d3 Oz = ld(oz, j), Ox = ld(ox, j);
         d3 Oy = cross(Oz, Ox);
         d3 Cap = sub(pi, project_on(sub(pi, pj), Oz));

@@ -61,7 +61,8 @@ __host__ __device__ inline double dbl_of(unsigned long long o) {
 // time step
 __global__ void __launch_bounds__(TPB) k_pair(uint32_t np, const uint2* __restrict__ sm,
                                               const uint32_t* __restrict__ param, const PairParam* __restrict__ params,
-                                              const double4_32a* __restrict__ geom, const float* __restrict__ reach,
+                                              const double4_32a* __restrict__ geom, const double4_32a* __restrict__ hole,
+                                              const float* __restrict__ reach,
                                               const double4_32a* __restrict__ pos,
                                               const double4_32a* __restrict__ vel, const double4_32a* __restrict__ av,
                                               const double4_32a* __restrict__ ox, const double4_32a* __restrict__ oz,
@@ -86,7 +87,11 @@ __global__ void __launch_bounds__(TPB) k_pair(uint32_t np, const uint2* __restri
         return;
     }
     const double4_32a gg = geom[pi];
-    const PairGeom g{gg.x, gg.y, gg.z, gg.w};
+    PairGeom g{gg.x, gg.y, gg.z, gg.w, 0.0, 0.0, 0.0};
+    if (cd == CD_SHP) {
+        const double4_32a hh = hole[pi];
+        g.hr = hh.x; g.hxo = hh.y; g.hyo = hh.z;
+    }
     const d3 Ps = ld(pos, p.x), Pm = ld(pos, p.y);
     double depth;
     d3 n, point;
@@ -159,7 +164,7 @@ __device__ __forceinline__ void write32(uint32_t i, int shape, d3 P, d3 Ox, d3 O
     if (shape != SHAPE_SPHERE) {
         const double lz = len(Oz), lx = len(Ox);
         bool ok = lz > 0.0;
-        if (shape == SHAPE_PLATE) ok = ok && lx > 0.0 && fabs(dot(Ox, Oz)) <= 1e-9 * lx * lz;
+        if (shape == SHAPE_PLATE || shape == SHAPE_HOLED) ok = ok && lx > 0.0 && fabs(dot(Ox, Oz)) <= 1e-9 * lx * lz;
         wall32[i] = ok ? make_float4((float)(Oz.x / lz), (float)(Oz.y / lz), (float)(Oz.z / lz), 1.0f)
                        : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
     }
@@ -281,6 +286,7 @@ __global__ void __launch_bounds__(TPB) k_detect_active(uint32_t np, const uint2*
                                                        const uint32_t* __restrict__ param,
                                                        const PairParam* __restrict__ params,
                                                        const double4_32a* __restrict__ geom,
+                                                       const double4_32a* __restrict__ hole,
                                                        const float* __restrict__ reach,
                                                        const double4_32a* __restrict__ pos, const double4_32a* __restrict__ ox,
                                                        const double4_32a* __restrict__ oz,
@@ -294,7 +300,11 @@ __global__ void __launch_bounds__(TPB) k_detect_active(uint32_t np, const uint2*
     double depth = -1.0;
     if (!certainly_apart(params[pi].cd, pos32[p.x], pos32[p.y], wall32[p.y], reach[pi])) {
         const double4_32a gg = geom[pi];
-        const PairGeom g{gg.x, gg.y, gg.z, gg.w};
+        PairGeom g{gg.x, gg.y, gg.z, gg.w, 0.0, 0.0, 0.0};
+        if (params[pi].cd == CD_SHP) {
+            const double4_32a hh = hole[pi];
+            g.hr = hh.x; g.hxo = hh.y; g.hyo = hh.z;
+        }
         d3 n, point;
         detect_pair(params[pi].cd, g, ld(pos, p.x), ld(pos, p.y), ox, oz, p.y, depth, n, point);
     }
@@ -404,10 +414,10 @@ __device__ __forceinline__ bool candidate(const ModelDev& mi, const ModelDev& mj
         const uint32_t w = ip ? i : j, sp = ip ? j : i;
         const int wshape = ip ? mi.shape : mj.shape;
         const float4 wl = wall32[w];
-        if (wl.w != 0.0f && (wshape == SHAPE_PLATE || wshape == SHAPE_CYL) &&
+        if (wl.w != 0.0f && (wshape == SHAPE_PLATE || wshape == SHAPE_HOLED || wshape == SHAPE_CYL) &&
             (ip ? mj.shape : mi.shape) == SHAPE_SPHERE) {
             float e;
-            const float d = wshape == SHAPE_PLATE ? plane_dist32(pos32[sp], pos32[w], wl, e)
+            const float d = wshape != SHAPE_CYL ? plane_dist32(pos32[sp], pos32[w], wl, e)
                                                   : line_dist32(pos32[sp], pos32[w], wl, e);
             if (d - e > thi) return false;
         }
@@ -704,7 +714,7 @@ Engine::~Engine() {
                     d_oz_, d_imp_, d_aimp_, d_global_, d_safe_, d_red_, d_key_, d_key_alt_, d_cell_key_, d_sid_,
                     d_sid_alt_, d_cell_start_, d_cellof_, d_flag_, d_task_, d_total_, d_ck_, d_cv_, d_ck_alt_,
                     d_cv_alt_, d_cnt_, d_rec_key_, d_rec_hist_, d_rec_v0_, d_rec_flags_, d_obs_, d_stage_,
-                    d_pos32_, d_wall32_, d_reach_, d_grid_, d_ext_};
+                    d_pos32_, d_wall32_, d_reach_, d_grid_, d_ext_, d_hole_};
     for (void* p : ptrs) if (p) cudaFree(p);
     for (auto& e : ev_) if (e) cudaEventDestroy(e);
     if (stream_) cudaStreamDestroy(stream_);
@@ -744,6 +754,10 @@ int Engine::init(const HScene& scene, const vedo_engine_opts& opts) {
         geo[q] = make_double4_32a(tab_.geom[4 * q], tab_.geom[4 * q + 1], tab_.geom[4 * q + 2], tab_.geom[4 * q + 3]);
     CK(dalloc(&d_geom_, geo.size()));
     CK(cudaMemcpy(d_geom_, geo.data(), sizeof(double4_32a) * geo.size(), cudaMemcpyHostToDevice));
+    for (size_t q = 0; q < geo.size(); ++q)
+        geo[q] = make_double4_32a(tab_.hole[4 * q], tab_.hole[4 * q + 1], tab_.hole[4 * q + 2], 0.0);
+    CK(dalloc(&d_hole_, geo.size()));
+    CK(cudaMemcpy(d_hole_, geo.data(), sizeof(double4_32a) * geo.size(), cudaMemcpyHostToDevice));
     const int G = tab_.ngroups;
     CK(dalloc(&d_group_iact_, (size_t)G * G));
     CK(cudaMemcpy(d_group_iact_, tab_.group_iact.data(), sizeof(int) * G * G, cudaMemcpyHostToDevice));
@@ -779,7 +793,7 @@ int Engine::init(const HScene& scene, const vedo_engine_opts& opts) {
             const double* gq = &tab_.geom[4 * q];   // ra, b0, b1, b2
             double r = 0.0;
             if (tab_.params[q].cd == CD_SS) r = gq[0] + gq[1];
-            else if (tab_.params[q].cd == CD_SP) r = gq[0] + 0.5 * gq[2];
+            else if (cd_plane(tab_.params[q].cd) == CD_SP) r = gq[0] + 0.5 * gq[2];
             else if (tab_.params[q].cd == CD_SC) r = gq[0] + gq[1];
             reach[q] = (float)r * (1.0f + 1e-6f);
         }
@@ -840,7 +854,7 @@ int Engine::rebuild(bool from_records) {
     // IsActive() of the current interactions at the current positions
     if (!from_records && cur_.np) {
         k_detect_active<<<blocks_for(cur_.np), TPB, 0, stream_>>>(cur_.np, cur_.sm, cur_.param, d_params_, d_geom_,
-                                                                  d_reach_, d_pos_, d_ox_, d_oz_, d_pos32_,
+                                                                  d_hole_, d_reach_, d_pos_, d_ox_, d_oz_, d_pos32_,
                                                                   d_wall32_, cur_.flags);
         ++own;
     }
@@ -986,7 +1000,8 @@ int Engine::step_once(bool write_impulses) {
     // CalculateImpact
     if (prof) CK(cudaEventRecord(ev_[0], stream_));
     if (cur_.np) {
-        k_pair<<<blocks_for(cur_.np), TPB, 0, stream_>>>(cur_.np, cur_.sm, cur_.param, d_params_, d_geom_, d_reach_,
+        k_pair<<<blocks_for(cur_.np), TPB, 0, stream_>>>(cur_.np, cur_.sm, cur_.param, d_params_, d_geom_, d_hole_,
+                                                         d_reach_,
                                                          d_pos_, d_vel_, d_av_, d_ox_, d_oz_, d_pos32_, d_wall32_,
                                                          cur_.hist, cur_.v0, cur_.flags, cur_.out, dt,
                                                          backup_pending_ ? 1 : 0);
@@ -1158,8 +1173,8 @@ int Engine::get_interactions(const vedo_contact_view& v) {
     const uint32_t np = cur_.np;
     if (!np) return VEDO_OK;
     // ContactInfo::bActive of the last narrow phase = detection at the current positions
-    k_detect_active<<<blocks_for(np), TPB, 0, stream_>>>(np, cur_.sm, cur_.param, d_params_, d_geom_, d_reach_, d_pos_,
-                                                         d_ox_, d_oz_, d_pos32_, d_wall32_, cur_.flags);
+    k_detect_active<<<blocks_for(np), TPB, 0, stream_>>>(np, cur_.sm, cur_.param, d_params_, d_geom_, d_hole_, d_reach_,
+                                                         d_pos_, d_ox_, d_oz_, d_pos32_, d_wall32_, cur_.flags);
     std::vector<uint2> sm(np);
     std::vector<uint8_t> fl(np);
     std::vector<double4_32a> h(np);
@@ -1194,7 +1209,7 @@ int Engine::get_observables(double out[13]) {
     obs::k_obs_reduce<<<1, 32, 0, stream_>>>(nb, 16, part, res, 12);
     if (cur_.np)
         k_detect_active<<<blocks_for(cur_.np), TPB, 0, stream_>>>(cur_.np, cur_.sm, cur_.param, d_params_, d_geom_,
-                                                                  d_reach_, d_pos_, d_ox_, d_oz_, d_pos32_,
+                                                                  d_hole_, d_reach_, d_pos_, d_ox_, d_oz_, d_pos32_,
                                                                   d_wall32_, cur_.flags);
     obs::k_obs_b<<<nb, TPB, 0, stream_>>>(n_, d_model_of_, d_models_, d_pos_, d_vel_, d_av_, res, 0, cur_.flags, cur_.np,
                                      part);

@@ -93,6 +93,7 @@ private:
     ModelDev* d_models_ = nullptr;
     PairParam* d_params_ = nullptr;
     double4_32a* d_geom_ = nullptr;     // per (slave model, master model): ra, b0, b1, b2
+    double4_32a* d_hole_ = nullptr;     // per (slave model, master model): hole radius, offsets (CD_SHP)
     int* d_group_iact_ = nullptr;
     uint32_t* d_model_of_ = nullptr;
     int* d_err_ = nullptr;

@@ -96,12 +96,41 @@ __device__ __forceinline__ d3 xcross(d3 a, d3 b) {
 }
 __device__ __forceinline__ d3 xproject_on(d3 a, d3 v) { return xsmul(__ddiv_rn(xdot(a, v), xlen(v)), xdir(v)); }
 
-// The reference's sphere-plate / sphere-cylinder detectors (CDSphere2QuasiPlate.cpp:15-97,
-// CDSphere2QuasiCylinder.cpp:16-80) in exact FP64: depth, unit normal, impact point.
+// The reference's sphere-plate / sphere-plate-with-hole / sphere-cylinder detectors
+// (CDSphere2QuasiPlate.cpp:15-97, CDSphere2QuasiPlateWithCircularHole.cpp:15-133,
+// CDSphere2QuasiCylinder.cpp:16-80) in exact FP64: depth, unit normal, impact point.  `hole`:
+// hole radius and offsets (the offsets are added to the plate's centre in world coordinates).
 __device__ __forceinline__ double wall_detect(int cd, double ra, double b0, double b1, double b2, d3 Ps, d3 Pm, d3 Ox,
-                                              d3 Oz, d3& n, d3& point) {
+                                              d3 Oz, d3& n, d3& point, const double4_32a& hole) {
     double depth;
-    if (cd == CD_SP) {
+    if (cd == CD_SHP) {
+        const d3 Oy = xcross(Oz, Ox);
+        const d3 Cap = xsub(Ps, xproject_on(xsub(Ps, Pm), Oz));
+        const double hh = __dmul_rn(0.5, b1), hw = __dmul_rn(0.5, b0), hl = __dmul_rn(0.5, b2);
+        const double hr = hole.x, hxo = hole.y, hyo = hole.z;
+        const d3 Cha = xsub(Ps, xadd(Pm, mk(hxo, hyo, 0.0)));
+        double dx = xdot(xsub(Cap, Pm), Ox);
+        if (dx < -hw) dx = -hw; else if (dx > hw) dx = hw;
+        double dy = xdot(xsub(Cap, Pm), Oy);
+        if (dy < -hl) dy = -hl; else if (dy > hl) dy = hl;
+        const double dahx = xdot(Cha, Ox), dahy = xdot(Cha, Oy);
+        const double dah = __dsqrt_rn(__dadd_rn(__dmul_rn(dahx, dahx), __dmul_rn(dahy, dahy)));
+        if (dah < hr) {
+            if (dah == 0.0) {
+                dx = hxo;
+                dy = hyo;
+            } else {
+                dx = __dadd_rn(hxo, __dmul_rn(__ddiv_rn(dahx, dah), hr));
+                dy = __dadd_rn(hyo, __dmul_rn(__ddiv_rn(dahy, dah), hr));
+            }
+        }
+        const d3 Caps = xadd(xadd(xsmul(dx, Ox), xsmul(dy, Oy)), Pm);
+        const d3 vIm = xsub(Caps, Ps);
+        const double lv = xlen(vIm);
+        depth = dah == 0.0 ? __dsub_rn(__dadd_rn(ra, hh), __dsqrt_rn(__dadd_rn(__dmul_rn(lv, lv), __dmul_rn(hr, hr))))
+                           : __dsub_rn(__dadd_rn(ra, hh), lv);
+        n = xdir(vIm);
+    } else if (cd == CD_SP) {
         const d3 Oy = xcross(Oz, Ox);
         const d3 Cap = xsub(Ps, xproject_on(xsub(Ps, Pm), Oz));
         const double hh = __dmul_rn(0.5, b1), hw = __dmul_rn(0.5, b0), hl = __dmul_rn(0.5, b2);
@@ -359,6 +388,7 @@ struct TickArgs {
     const PairParam* params;
     const float* pc32;             // [nm*nm][8] float constants
     const double4_32a* geom;       // [nm*nm]: ra, b0, b1, b2
+    const double4_32a* hole;       // [nm*nm]: hole radius, offsets (sphere - plate with a hole)
     const double4_32a* xA;
     double4_32a* xB;
     double4_32a* v64;
@@ -689,7 +719,7 @@ __device__ __forceinline__ float2 tick_sphere(const TickArgs& a, uint32_t i) {
                     const d3 Ps = i_slave ? Pi : Pj, Pm = i_slave ? Pj : Pi;
                     d3 nd, pt;
                     const double dex = wall_detect(P.cd, gg.x, gg.y, gg.z, gg.w, Ps, Pm, ld(a.ox, m), ld(a.oz, m), nd,
-                                                   pt);
+                                                   pt, P.cd == CD_SHP ? a.hole[pi] : make_double4_32a(0, 0, 0, 0));
                     active = dex > 0.0;
                     depth = (float)dex;
                     n = fm((float)nd.x, (float)nd.y, (float)nd.z);
@@ -851,7 +881,7 @@ __device__ __forceinline__ float frame_drift_across(const SceneDev& S, uint32_t 
     const float Dx = dtk * fmaf(S.gdt[0], hk, S.u0[0]), Dy = dtk * fmaf(S.gdt[1], hk, S.u0[1]),
                 Dz = dtk * fmaf(S.gdt[2], hk, S.u0[2]);
     float across;
-    if (shape == SHAPE_PLATE) {
+    if (shape == SHAPE_PLATE || shape == SHAPE_HOLED) {
         across = fabsf(fmaf(Dz, nz, fmaf(Dy, ny, Dx * nx)));
     } else {
         const float cx = fmaf(Dy, nz, -Dz * ny), cy = fmaf(Dz, nx, -Dx * nz), cz = fmaf(Dx, ny, -Dy * nx);
@@ -954,7 +984,7 @@ __global__ void k_walls(uint32_t nglob, const uint32_t* __restrict__ glob, const
         st(oz, w, Oz, 0.0);
         const double lz = len(Oz), lx = len(Ox);
         bool ok = lz > 0.0;
-        if (M.shape == SHAPE_PLATE) ok = ok && lx > 0.0 && fabs(dot(Ox, Oz)) <= 1e-9 * lx * lz;
+        if (M.shape == SHAPE_PLATE || M.shape == SHAPE_HOLED) ok = ok && lx > 0.0 && fabs(dot(Ox, Oz)) <= 1e-9 * lx * lz;
         const float nx = (float)(Oz.x / lz), ny = (float)(Oz.y / lz), nz = (float)(Oz.z / lz);
         wall32[w] = ok ? make_float4(nx, ny, nz, frame_drift_across(S, k1, M.shape, nx, ny, nz))
                        : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
@@ -1137,7 +1167,7 @@ __global__ void __launch_bounds__(TPB) k_nbr(uint32_t nloc, const uint32_t* __re
     for (uint32_t q = S.wall_beg; q < S.wall_end; ++q) {
         const uint32_t w = glob[q];
         const uint32_t pw = pidx(S, mi, model_of[w]);
-        const int cd = params[pw].cd;
+        const int cd = cd_plane(params[pw].cd);
         if (cd == 0) continue;
         const float4 wl = wall32[w];
         if (wl.w != 0.0f) {
@@ -1223,7 +1253,7 @@ __global__ void __launch_bounds__(TPB) k_meta(uint32_t n, const uint32_t* __rest
         const PairParam& P = params[pi];
         const bool bond = (P.is == IS_BSDBF || P.is == IS_BTSDBF || P.is == IS_BSDB2F) && P.c[4] != 0.0;
         const bool moving = (v & WALL_BIT) && models[mj].behavior == BEH_ORBITAL;
-        meta[e] = (pi & META_PI) | ((uint32_t)(P.cd & 3) << META_CD_SHIFT) | (bond ? META_BOND : 0u) |
+        meta[e] = (pi & META_PI) | ((uint32_t)(cd_plane(P.cd) & 3) << META_CD_SHIFT) | (bond ? META_BOND : 0u) |
                   (slot[e] == e ? META_OWNER : 0u) | (i_slave ? META_SLAVE : 0u) | (moving ? META_MOVING : 0u);
     }
 }
@@ -1345,14 +1375,14 @@ __global__ void __launch_bounds__(TPB) k_interior(uint32_t n, const uint32_t* __
         const d3 d = sub(P, ld(x, w));
         const double m = (W.behavior == BEH_ORBITAL ? skin_w : skin) + 1e-9 * (len(d) + 1.0);
         const d3 uz = muls(Oz, 1.0 / lz);
-        bool in;
+        bool in = false;                           // a holed plate's hole edge is not modelled here
         if (W.shape == SHAPE_PLATE) {
             const d3 Ox = ld(ox, w);
             const double lx = len(Ox);
             if (!(lx > 0.0)) continue;
             const d3 ux = muls(Ox, 1.0 / lx), uy = cross(uz, ux);
             in = fabs(dot(d, ux)) <= 0.5 * W.a0 - m && fabs(dot(d, uy)) <= 0.5 * W.a2 - m;
-        } else {
+        } else if (W.shape == SHAPE_CYL) {
             in = fabs(dot(d, uz)) <= 0.5 * W.a1 - m;
         }
         if (in) meta[e] |= META_INTERIOR;
@@ -1499,7 +1529,8 @@ __global__ void __launch_bounds__(TPB) k_active(uint32_t n, TickArgs a, uint8_t*
             depth = __dsub_rn(__dadd_rn(gg.x, gg.y), xlen(xsub(Pm, Ps)));
         } else {
             d3 nd, pt;
-            depth = wall_detect(P.cd, gg.x, gg.y, gg.z, gg.w, Ps, Pm, ld(a.ox, m), ld(a.oz, m), nd, pt);
+            depth = wall_detect(P.cd, gg.x, gg.y, gg.z, gg.w, Ps, Pm, ld(a.ox, m), ld(a.oz, m), nd, pt,
+                                P.cd == CD_SHP ? a.hole[pi] : make_double4_32a(0, 0, 0, 0));
         }
         act[e] = depth > 0.0 ? PF_ACTIVE_BIT : 0;
     }
@@ -1647,7 +1678,7 @@ __global__ void __launch_bounds__(TPB) k_wall32(uint32_t n, const uint32_t* __re
     const d3 Ox = ld(ox, i), Oz = ld(oz, i);
     const double lz = len(Oz), lx = len(Ox);
     bool ok = lz > 0.0;
-    if (M.shape == SHAPE_PLATE) ok = ok && lx > 0.0 && fabs(dot(Ox, Oz)) <= 1e-9 * lx * lz;
+    if (M.shape == SHAPE_PLATE || M.shape == SHAPE_HOLED) ok = ok && lx > 0.0 && fabs(dot(Ox, Oz)) <= 1e-9 * lx * lz;
     wall32[i] = ok ? make_float4((float)(Oz.x / lz), (float)(Oz.y / lz), (float)(Oz.z / lz), 1e-30f)   // no drift yet
                    : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
 }
@@ -1879,6 +1910,7 @@ private:
     PairParam* d_params_ = nullptr;
     float* d_pc32_ = nullptr;
     double4_32a* d_geom_ = nullptr;
+    double4_32a* d_hole_ = nullptr;                // [nm*nm] hole radius and offsets (CD_SHP pairs)
     double4_32a* d_rr_ = nullptr;
     float4* d_mf_ = nullptr;
     float* d_reach_ = nullptr;
@@ -1973,7 +2005,7 @@ MixedEngine::~MixedEngine() {
     if (stream_) cudaStreamSynchronize(stream_);
     free_nlist(nl_[0]);
     free_nlist(nl_[1]);
-    void* ptrs[] = {d_models_, d_params_, d_pc32_, d_geom_, d_rr_, d_mf_, d_reach_, d_model_of_, d_scene_of_,
+    void* ptrs[] = {d_models_, d_params_, d_pc32_, d_geom_, d_hole_, d_rr_, d_mf_, d_reach_, d_model_of_, d_scene_of_,
                     d_scenes_, d_gfield_, d_glob_, d_x_[0], d_x_[1], d_v64_, d_w64_, d_ox_, d_oz_, d_imp_, d_aimp_,
                     d_v32_[0], d_v32_[1], d_w32_[0], d_w32_[1], d_rr32_, d_xs_[0], d_xs_[1], d_work_, d_clear_, d_vred_, d_ext_, d_qcnt_, d_pos32_, d_wall32_, d_red_, d_sred_, d_disp_, d_err_,
                     d_key_, d_key_alt_, d_sid_, d_sid_alt_, d_cnt_, d_gs_, d_ge_, d_act_, d_stage_, d_obs_, d_gidx_,
@@ -2026,7 +2058,7 @@ int MixedEngine::init_from(const std::vector<SceneSource>& src, const MixedEngin
     // ---- per-scene tables, concatenated
     std::vector<uint32_t> model_of, scene_of;
     std::vector<double> st[7];                 // staged host state of the new scenes
-    std::vector<double4_32a> geo, rr;
+    std::vector<double4_32a> geo, rr, hole;
     std::vector<float4> rr32;
     std::vector<float> pc, reach;
     std::vector<float4> mf;
@@ -2117,6 +2149,7 @@ int MixedEngine::init_from(const std::vector<SceneSource>& src, const MixedEngin
             }
             const double* g = &t.geom[4 * q];
             geo.push_back(make_double4_32a(g[0], g[1], g[2], g[3]));
+            hole.push_back(make_double4_32a(t.hole[4 * q], t.hole[4 * q + 1], t.hole[4 * q + 2], 0.0));
             const double R = g[0] + g[1];
             rr.push_back(make_double4_32a(R, R * R, 1e-9 * R * R, 0.0));
             const double R2 = R * R;
@@ -2124,7 +2157,7 @@ int MixedEngine::init_from(const std::vector<SceneSource>& src, const MixedEngin
             rr32.push_back(make_float4(R2h, (float)(R2 - (double)R2h), (float)(1e-9 * R2), (float)R));
             double r = 0.0;
             if (P.cd == CD_SS) r = g[0] + g[1];
-            else if (P.cd == CD_SP) r = g[0] + 0.5 * g[2];
+            else if (cd_plane(P.cd) == CD_SP) r = g[0] + 0.5 * g[2];
             else if (P.cd == CD_SC) r = g[0] + g[1];
             reach.push_back((float)r * (1.0f + 1e-6f));
         }
@@ -2157,7 +2190,7 @@ int MixedEngine::init_from(const std::vector<SceneSource>& src, const MixedEngin
     };
     int rc;
     if ((rc = up(&d_models_, models_)) || (rc = up(&d_params_, params_)) || (rc = up(&d_pc32_, pc)) ||
-        (rc = up(&d_geom_, geo)) || (rc = up(&d_rr_, rr)) || (rc = up(&d_rr32_, rr32)) || (rc = up(&d_mf_, mf)) || (rc = up(&d_reach_, reach)) ||
+        (rc = up(&d_geom_, geo)) || (rc = up(&d_hole_, hole)) || (rc = up(&d_rr_, rr)) || (rc = up(&d_rr32_, rr32)) || (rc = up(&d_mf_, mf)) || (rc = up(&d_reach_, reach)) ||
         (rc = up(&d_model_of_, model_of)) || (rc = up(&d_scene_of_, scene_of)) || (rc = up(&d_gfield_, gfield)) ||
         (rc = up(&d_glob_, glob_)))
         return rc;
@@ -2319,6 +2352,7 @@ TickArgs MixedEngine::args(bool write_imp) {
     a.params = d_params_;
     a.pc32 = d_pc32_;
     a.geom = d_geom_;
+    a.hole = d_hole_;
     a.xA = d_x_[cur_];
     a.xB = d_x_[cur_ ^ 1];
     a.v64 = d_v64_;

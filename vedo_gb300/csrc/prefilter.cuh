@@ -49,7 +49,7 @@ __device__ __forceinline__ float line_dist32(const float4& a, const float4& b, c
     return d;
 }
 
-// cd: 1 sphere-sphere, 2 sphere-plate, 3 sphere-cylinder.  `reach` bounds the distance at
+// cd: 1 sphere-sphere, 2 sphere-plate (4, with a hole: tested as the full plate), 3 sphere-cylinder.  `reach` bounds the distance at
 // which the pair can be in contact (radius sum, or radius + plate half-thickness, or sphere
 // + cylinder radius), already rounded up.  True when the pair is certainly apart.
 __device__ __forceinline__ bool certainly_apart(int cd, const float4& s, const float4& m, const float4& wall,
@@ -57,7 +57,7 @@ __device__ __forceinline__ bool certainly_apart(int cd, const float4& s, const f
     float e, d;
     if (cd == 1) {
         d = dist32(s, m, e);
-    } else if (cd == 2) {
+    } else if (cd == 2 || cd == 4) {
         if (wall.w == 0.0f) return false;
         d = plane_dist32(s, m, wall, e);
     } else {

@@ -75,6 +75,18 @@ bool analyse(const HModel& m, ModelDev& o) {
         double mmi = mass * (3.0 * r * r + h * h) / 12.0;
         o.ix = o.iy = mmi;
         o.iz = 0.5 * mass * r * r;
+    } else if (m.shape == SHAPE_HOLED) {                  // DOModel.cpp:90-119
+        const double w = m.attrs[0], h = m.attrs[1], l = m.attrs[2], hr = m.attrs[3], hxo = m.attrs[4],
+                     hyo = m.attrs[5];
+        o.range = (m.scope == SCOPE_LOCAL) ? 0.5 * std::max(std::max(w, h), l) : 0.5 * h;
+        if (!((std::abs(hxo) <= (0.5 * w - hr)) && (std::abs(hyo) <= (0.5 * l - hr)))) return false;   // the reference exits
+        vol = w * h * l - hr * hr * PI * h;
+        mass = m.density * vol;
+        sudo_model = m.density_factor * mass;
+        o.ix = o.iy = o.iz = 0.0;                        // "Need to be modified."
+        // the only factories: fixed and mobile (ModuleList.h:50,56); a mobile one moves as an
+        // orbital plate does (DOQuasiPlateWithCircularHole.cpp:22-38), which is not restated
+        if (m.behavior != BEH_FIXED) return false;
     } else if (m.shape == SHAPE_PLATE) {
         double w = m.attrs[0], h = m.attrs[1], l = m.attrs[2];
         o.range = (m.scope == SCOPE_LOCAL) ? 0.5 * std::max(std::max(w, h), l) : 0.5 * h;
@@ -473,6 +485,7 @@ int build_tables(const HScene& s, Tables& t, std::string& err) {
                 }
     t.params.assign(nm * nm, PairParam{});
     t.geom.assign(nm * nm * 4, 0.0);
+    t.hole.assign(nm * nm * 4, 0.0);
     for (size_t ms = 0; ms < nm; ++ms) {
         for (size_t mm = 0; mm < nm; ++mm) {
             const ModelDev& S = t.models[ms];
@@ -480,7 +493,8 @@ int build_tables(const HScene& s, Tables& t, std::string& err) {
             PairParam& P = t.params[ms * nm + mm];
             int ia = t.group_iact[(size_t)S.group * G + M.group];
             if (ia < 0 || S.shape != SHAPE_SPHERE) continue;
-            int cd = M.shape == SHAPE_SPHERE ? CD_SS : M.shape == SHAPE_PLATE ? CD_SP : M.shape == SHAPE_CYL ? CD_SC : 0;
+            int cd = M.shape == SHAPE_SPHERE ? CD_SS : M.shape == SHAPE_PLATE ? CD_SP : M.shape == SHAPE_CYL ? CD_SC
+                     : M.shape == SHAPE_HOLED ? CD_SHP : 0;
             const HIact& im = s.iacts[ia];
             int is = eq_of(im.equation_type);
             if (!cd || !is) continue;                      // the factories return null (Assembler.cpp:72-85)
@@ -489,6 +503,8 @@ int build_tables(const HScene& s, Tables& t, std::string& err) {
             P.iact = ia;
             double* geo = &t.geom[(ms * nm + mm) * 4];
             geo[0] = S.a0; geo[1] = M.a0; geo[2] = M.a1; geo[3] = M.a2;
+            if (cd == CD_SHP)
+                for (int k = 0; k < 3; ++k) t.hole[(ms * nm + mm) * 4 + k] = s.models[mm].attrs[3 + k];
             auto need = [&](const char* name, double& v) {
                 if (!mech(im, name, v)) {
                     err = "interaction " + im.master_group + "/" + im.slave_group + " has no mechanism " + name;

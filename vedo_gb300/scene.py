@@ -113,6 +113,14 @@ class DOModel:
             sm = self.density_factor * m
             k = m / 12.0
             return rng, vol, m, sm, (k * (h * h + l * l), k * (w * w + l * l), k * (h * h + w * w))
+        if self.shape == QUASI_PLATE_WITH_CIRCULAR_HOLE:
+            w, h, l, hr, hxo, hyo = a[0], a[1], a[2], a[3], a[4], a[5]
+            rng = 0.5 * max(max(w, h), l) if self.scope == LOCAL else 0.5 * h
+            if not (abs(hxo) <= 0.5 * w - hr and abs(hyo) <= 0.5 * l - hr):
+                raise ValueError(f"model {self.name!r}: the hole does not lie inside the plate")
+            vol = w * h * l - hr * hr * PI * h
+            m = self.density * vol
+            return rng, vol, m, self.density_factor * m, (0.0, 0.0, 0.0)
         raise ValueError(f"shape type {self.shape} of model {self.name!r} is not supported")
 
 

@@ -39,7 +39,8 @@ from typing import List, Optional, Sequence, Tuple
 
 import numpy as np
 
-from .scene import (CONSTRAINED, FIXED, GLOBAL, LOCAL, MOBILE, ORBITAL, QUASI_CYLINDER, QUASI_PLATE, SPHERE,
+from .scene import (CONSTRAINED, FIXED, GLOBAL, LOCAL, MOBILE, ORBITAL, QUASI_CYLINDER, QUASI_PLATE,
+                    QUASI_PLATE_WITH_CIRCULAR_HOLE, SPHERE,
                     Boundary, DOModel, IactModel, Scene, SystemParameter)
 
 
@@ -437,6 +438,47 @@ def spinning_plate(omega: float = 500.0, steps: int = 3000, dt: float = 2e-7, ra
     OZ = np.concatenate([np.tile([0, 0, 1.0], (n, 1)), np.array([[0.0, 0.0, 1.0]])])
     AV = np.concatenate([np.zeros((n, 3)), np.array([[0.0, 0.0, omega]])])
     return Scene(sp, models, iacts, midx, P, np.zeros((n + 1, 3)), OX, OZ, AV)
+
+
+def holed_plate_drop(n_side: int = 6, seed: int = 4, steps: int = 600, dt: float = 1e-6, radius: float = 1e-3,
+                     hole: float = 2.6e-3, hole_offset: Tuple[float, float] = (1.2e-3, -0.7e-3),
+                     solver: str = "ISwBSDBF") -> Scene:
+    """Spheres on a jittered square grid moving down onto a fixed square plate with a circular
+    hole (the reference's QuasiPlateWithCircularHole, offset from the plate's centre): some
+    fall through the hole, some land on its rim, one moves straight down the hole's axis (the
+    detector's zero-offset branch), the rest land on the flat part.  LSD (ISwBSDBF) for
+    bit-exact comparisons by default."""
+    rng = np.random.default_rng(seed)
+    sp = 2.3 * radius
+    side = 14 * radius
+    xs = (np.arange(n_side) - 0.5 * (n_side - 1)) * sp
+    X, Y = np.meshgrid(xs, xs, indexing="ij")
+    pos = np.stack([X.ravel(), Y.ravel(), np.full(X.size, radius + 0.5e-3 + 5e-6)], 1)   # just above the plate
+    pos[:, :2] += rng.uniform(-0.2 * radius, 0.2 * radius, size=(pos.shape[0], 2))
+    pos[:, 2] += rng.uniform(0.0, 0.02 * radius, size=pos.shape[0])
+    pos[0, :2] = hole_offset                              # exactly over the hole's centre
+    n = pos.shape[0]
+    kn, ks = 2e4, 1.6e4
+    zeta = damping_ratio(0.6)
+    models = [DOModel("Ball", "Ball", MOBILE, LOCAL, 2500.0, 1.0, SPHERE, (radius,)),
+              DOModel("Holed", "Wall", FIXED, GLOBAL, 0.0, 1.0, QUASI_PLATE_WITH_CIRCULAR_HOLE,
+                      (side, 1e-3, side, hole, hole_offset[0], hole_offset[1]))]
+    if solver == "ISwBSDBF":
+        mech = lambda b: lsd_mechanisms(kn, ks, b, b, 0.4)
+        iacts = [IactModel("Ball", "Ball", solver, mech(zeta / math.sqrt(2.0))),
+                 IactModel("Wall", "Ball", solver, mech(zeta))]
+    else:
+        m_of = lambda rr: 2500.0 * 4.0 / 3.0 * math.pi * rr ** 3
+        iacts = [IactModel("Ball", "Ball", solver, _hertz_mech(solver, 70e9, 0.25, radius, radius, m_of, zeta, 0.4)),
+                 IactModel("Wall", "Ball", solver, _hertz_mech(solver, 70e9, 0.25, radius, None, m_of, zeta, 0.4))]
+    midx = np.concatenate([np.zeros(n, np.uint32), np.array([1], np.uint32)])
+    P = np.concatenate([pos, np.zeros((1, 3))])
+    V = np.concatenate([rng.normal(0.0, 0.02, size=(n, 3)) * np.array([1.0, 1.0, 0.0]), np.zeros((1, 3))])
+    V[:n, 2] = -0.2
+    V[0, :2] = 0.0
+    OX = np.concatenate([np.tile([1.0, 0, 0], (n, 1)), np.array([[1.0, 0.0, 0.0]])])
+    OZ = np.concatenate([np.tile([0, 0, 1.0], (n, 1)), np.array([[0.0, 0.0, 1.0]])])
+    return Scene(time_control(steps, dt), models, iacts, midx, P, V, OX, OZ, np.zeros((n + 1, 3)))
 
 
 def hopper_params(num_scenes: int = 256, seed: int = 2025, n_lo: int = 1000, n_hi: int = 50000):
