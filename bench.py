@@ -327,8 +327,9 @@ def ours(args, dist):
         kern = eng.last_run_profile()
         kern["steps"] = args.profile_steps
         eng.set_profiling(False)
-    # e2e through the C ABI with pinned host buffers
-    fields = ("position", "velocity", "angular_velocity", "orientation_x", "orientation_z")
+    # e2e through the C ABI with pinned host buffers: the state that the step changes (sphere
+    # orientations are not integrated in this form)
+    fields = ("position", "velocity", "angular_velocity")
     pinned = {f: torch.empty((eng.n, 3), dtype=torch.float64, pin_memory=True) for f in fields}
     host = {f: pinned[f].numpy() for f in fields}
     eng.state(fields, out=host)
@@ -395,8 +396,9 @@ def ours(args, dist):
            "clocks": clocks_rec, "gpu_launches": launches,
            "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": xfer / args.sync,
                    "d2h_bytes_per_step": xfer / args.sync,
-                   "note": f"vedo_gpu_set_state + vedo_gpu_run({args.sync}) + vedo_gpu_get_state per "
-                           f"{args.sync} steps, pinned host buffers, mixed form"},
+                   "note": f"vedo_gpu_set_state + vedo_gpu_run({args.sync}) + vedo_gpu_get_state of position, "
+                           f"velocity and angular velocity (FP64) of every object per {args.sync} steps, pinned "
+                           f"host buffers, mixed form"},
            "roofline": roof, "cpu_baseline": cpu}
     eng.close()
     if not args.no_batch:

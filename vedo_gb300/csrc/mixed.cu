@@ -1887,9 +1887,10 @@ private:
     float cell_scale_ = 1.0f;       // cell edge = cell_scale * (2 r_max + skin)
     int tpb_ = TPB;                 // threads per block of the tick kernel
     bool tune_pending_ = false;
-    // one check interval of steps, by start parity: [0..1] plain, [2..3] with the per-kernel
-    // timing events of profiling
-    cudaGraphExec_t graph_[4] = {nullptr, nullptr, nullptr, nullptr};
+    // one check interval of steps, by start parity (+1), with the per-kernel timing events of
+    // profiling (+2), with the impulse output of a call's last step (+4)
+    cudaGraphExec_t graph_[8] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
+    uint64_t graph_launches_[8] = {0, 0, 0, 0, 0, 0, 0, 0};
     unsigned ev_flags_ = cudaEventRecordDefault;      // cudaEventRecordExternal while capturing
     std::vector<cudaEvent_t> pev_;  // profiling: per step, events before the tick, after it, after the walls
     uint32_t pev_used_ = 0;
@@ -2671,17 +2672,18 @@ int MixedEngine::step_chunk(uint32_t chunk, bool imp_last, float* use_after) {
         }
     }
     pev_used_ = 0;
-    if (opts_.graphs && chunk == ci && !imp_last) {
+    if (opts_.graphs && chunk == ci) {
         const int c0 = cur_;
-        const int gi = c0 + (profiling_ ? 2 : 0);
+        const int gi = c0 + (profiling_ ? 2 : 0) + (imp_last ? 4 : 0);
         if (!graph_[gi]) {
             cudaGraph_t g = nullptr;
             const uint64_t l0 = launches_;
             MCK(cudaStreamBeginCapture(stream_, cudaStreamCaptureModeThreadLocal));
             ev_flags_ = cudaEventRecordExternal;
-            for (uint32_t k = 0; k < chunk; ++k) launch_step(false);
+            for (uint32_t k = 0; k < chunk; ++k) launch_step(imp_last && k + 1 == chunk);
             ev_flags_ = cudaEventRecordDefault;
             const cudaError_t ce = cudaStreamEndCapture(stream_, &g);
+            graph_launches_[gi] = launches_ - l0;
             launches_ = l0;
             cur_ = c0;
             if (ce != cudaSuccess) return cuda_fail(ce, "cudaStreamEndCapture");
@@ -2692,7 +2694,7 @@ int MixedEngine::step_chunk(uint32_t chunk, bool imp_last, float* use_after) {
         }
         MCK(cudaGraphLaunch(graph_[gi], stream_));
         if (profiling_) pev_used_ = 3 * chunk;           // the graph records every step's events
-        launches_ += (uint64_t)chunk * (split_tick_ ? 3 : 2);
+        launches_ += graph_launches_[gi];
         if (chunk & 1) cur_ ^= 1;
     } else {
         for (uint32_t k = 0; k < chunk; ++k) launch_step(imp_last && k + 1 == chunk);
