@@ -11,23 +11,24 @@
 // in FP64 (positions, velocities, angular velocities).
 //
 // Precision split (per pair): the relative displacement d = x_master - x_slave and the
-// overlap numerator R^2 - |d|^2 are FP64 (the overlap of stiff contacts is 1e-9..1e-6 of the
-// radius, beyond FP32's reach); the overlap itself, the normal, relative velocities, forces
-// and torques are FP32 in pair-local coordinates.  The contact decision (overlap > 0) is the
+// overlap numerator R^2 - |d|^2 are double-float (hi/lo FP32 splits of the FP64 positions;
+// the overlap of stiff contacts is 1e-9..1e-6 of the radius, beyond FP32's reach); the overlap
+// itself, the normal, relative velocities, forces and torques are FP32 in pair-local
+// coordinates.  The contact decision (overlap > 0) is the
 // FP64 decision: where |R^2 - |d|^2| is within 1e-9 R^2 the reference's own FP64 formula
 // (rounded intrinsics, no contraction) decides, so contact sets equal the FP64 engine's.
 // Sphere-wall pairs use the reference's FP64 detectors for the geometry.
 //
 // Broad phase: uniform cell list of edge 2 r_max + skin, stable radix sort on cell key,
 // full neighbour lists within r_i + r_j + skin (a conservative FP32 test: a superset), walls
-// by a plane/axis lower bound.  The list is complete while every sphere and every wall plane
-// or axis has moved less than half the skin since the rebuild; the bound on that displacement,
-// the sum over steps of dt * max(max|v| of the spheres, the walls' plane speed), is kept on the
-// device.  A step that starts with the bound above half the skin is not taken: the tick and
-// wall kernels copy the state unchanged (an identity step) and count it, and the host, which
-// reads the bound and the count every few steps, rebuilds and takes the step again.  Contacts
-// are therefore never missed, and the results do not depend on the skin or on when the list
-// is rebuilt.
+// by a plane/axis lower bound (orbital walls with 8 skins).  The device keeps bounds on the
+// spheres' displacement since the rebuild relative to their scene's free-falling frame, on
+// their displacement itself and on the orbital walls' approach (list_spent); a step that
+// starts with the list possibly incomplete is not taken: the tick and wall kernels copy the
+// state unchanged (an identity step) and count it, and the host, which reads the bounds and
+// the count every few steps, rebuilds and takes the step again.  Contacts are therefore never
+// missed, and the results do not depend on the skin or on when the list is rebuilt.  Spheres
+// whose pairs have all been certainly apart since the rebuild skip their walk (quiet spheres).
 #include <algorithm>
 #include <cfloat>
 #include <cmath>
@@ -923,8 +924,9 @@ __global__ void k_wall_rot(uint32_t nglob, const uint32_t* __restrict__ glob, co
 
 // Scope-global objects (walls): fixed ones keep their state, orbital ones move with their
 // prescribed V and omega (DOOrbitalQuasiPlate.cpp:18-34).  Thread 0 also writes the
-// displacement bound after the step into the other parity slot (disp_out), or, when the step
-// is an identity step, carries the bound over and counts the step in *held.
+// displacement bounds and the step count after the step into the other parity slot
+// (disp_out), or, when the step is an identity step, carries them over and counts the step in
+// *held; every wall's FP32 record gets the frame's drift across it for the next step.
 __global__ void k_walls(uint32_t nglob, const uint32_t* __restrict__ glob, const uint32_t* __restrict__ model_of,
                         const ModelDev* __restrict__ models, const SceneDev* __restrict__ scenes,
                         const uint32_t* __restrict__ scene_of, const double4_32a* __restrict__ xA,
