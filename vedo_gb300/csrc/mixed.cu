@@ -819,7 +819,7 @@ __global__ void __launch_bounds__(TPB) k_tick_work(TickArgs a) {
 // exact path is deferred, whole, to k_tick over the worklist.  Either way one thread computes
 // the sphere with the same operations, so results are those of the single tick.
 template <bool XS>
-__global__ void __launch_bounds__(TPB, 5) k_tick_light(TickArgs a) {   // 5 blocks of 256 per SM
+__global__ void __launch_bounds__(TPB, 6) k_tick_light(TickArgs a) {   // 6 blocks of 256 per SM (40 registers; the rare walk spills a little)
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     const bool hold = held_step(a);
     float2 vmax_local = make_float2(0.0f, 0.0f);
