@@ -106,6 +106,9 @@ struct dp_world {
     double sf;
     unsigned up_iact;
     unsigned long long round;
+    /* periodic boundary after Boundary::Correct: switched axes, bounds, ranges */
+    int pbc_on, pbc_sw[3];
+    double pbc_lo[3], pbc_hi[3], pbc_r[3];
     /* models */
     int nmodels, ngroups, niact;
     model_t* models;
@@ -147,6 +150,38 @@ static void status_clean_contact(status_t* s) {              /* ImpactStatus.cpp
     s->last_contact = s->contact; s->contact = 0;
     s->last_bond = s->bond; s->bond = 0;
     s->shear = V3(0, 0, 0); s->imp_master = V3(0, 0, 0); s->aimp_master = V3(0, 0, 0);
+}
+
+/* ------------------------------------------------------------------------ */
+/* Boundary::DifferenceBoundaryConditions (vedo/framework/Boundary.cpp:306-345): the minimum
+   image of a difference on every switched axis */
+static v3 min_image(const dp_world* w, v3 d) {
+    double c[3] = {d.x, d.y, d.z};
+    for (int k = 0; k < 3; ++k) {
+        if (!w->pbc_sw[k]) continue;
+        if (c[k] >= 0.5 * w->pbc_r[k]) c[k] -= w->pbc_r[k];
+        if (c[k] < -0.5 * w->pbc_r[k]) c[k] += w->pbc_r[k];
+    }
+    return V3(c[0], c[1], c[2]);
+}
+
+/* Boundary::EnforceBoundaryConditions (Boundary.cpp:225-304): a position on a switched axis
+   is brought back into [lower, upper), one range at a time and by fmod beyond that */
+static void wrap_position(const dp_world* w, double* p) {
+    for (int k = 0; k < 3; ++k) {
+        if (!w->pbc_sw[k]) continue;
+        const double lo = w->pbc_lo[k], hi = w->pbc_hi[k], r = w->pbc_r[k];
+        double x = p[k];
+        if (x >= hi) {
+            x -= r;
+            if (x >= hi) x = lo + fmod(x - lo, r);
+        }
+        if (x < lo) {
+            x += r;
+            if (x < lo) x = lo + fmod(x - lo, r) + r;
+        }
+        p[k] = x;
+    }
 }
 
 /* ------------------------------------------------------------------------ */
@@ -509,6 +544,7 @@ static void detect(const dp_world* w, iactn_t* I) {
     cinfo_t* ci = &I->ci;
     if (I->cd == CD_SS) {                                    /* CDSphere2Sphere.cpp:14-60 */
         v3 vIm = sub(Pm, Ps);
+        if (w->pbc_on) vIm = min_image(w, vIm);              /* :19-22, pBC set when active */
         double rb = mm->a[0];
         ci->depth = ra + rb - len(vIm);
         ci->dirn = dir(vIm);
@@ -614,6 +650,11 @@ static void solve(dp_world* w, iactn_t* I, double dt) {
     if (depth > 0.0) {
         rA = sub(ci->point, ld3(w->pos + 3 * A));
         rB = sub(ci->point, ld3(w->pos + 3 * B));
+        if (w->pbc_on) {          /* every law: ISwBSDBF.cpp:69-73, ISwBtSDBF.cpp:69-73, ISwBSDB2F.cpp:72-76,
+                                     ISwHertz.cpp:59-63, ISwH.cpp:68-72 */
+            rA = min_image(w, rA);
+            rB = min_image(w, rB);
+        }
         vRel = sub(add(sub(Va, Vb), cross(AVa, rA)), cross(AVb, rB));
         vRn = smul(dot(vRel, n), n);
         vRs = sub(vRel, vRn);
@@ -858,7 +899,8 @@ static const record_t* find_record(const dp_world* w, unsigned a, unsigned b) { 
     return (const record_t*)bsearch(&key, w->rec, w->nrec, sizeof(record_t), rec_key_cmp);
 }
 
-/* SimMediator::Initiate without periodic boundary (SimMediator.cpp:640-712) */
+/* SimMediator::Initiate (SimMediator.cpp:640-712); with an active periodic boundary the
+   detectors and solvers see it (pbc_on) */
 static int initiate(dp_world* w) {
     free(w->it);
     w->it = (iactn_t*)calloc(w->ncand ? w->ncand : 1, sizeof(iactn_t));
@@ -895,12 +937,16 @@ static int rebuild_records(dp_world* w) {
 /* ------------------------------------------------------------------------ */
 dp_world* dp_create(const vedo_scene_desc* sc, unsigned up_iact, char* err, size_t errlen) {
     if (!sc || !sc->num_objects) { set_err(err, errlen, "empty scene"); return NULL; }
-    /* Boundary::Correct (Boundary.cpp:79-128): an axis is on where its bounds differ */
-    if (sc->pbc_lower[0] != sc->pbc_upper[0] || sc->pbc_lower[1] != sc->pbc_upper[1] ||
-        sc->pbc_lower[2] != sc->pbc_upper[2]) {
-        set_err(err, errlen, "periodic boundary not supported"); return NULL;
-    }
     dp_world* w = (dp_world*)calloc(1, sizeof(dp_world));
+    /* Boundary::Correct (Boundary.cpp:79-128): an axis is on where its bounds differ */
+    for (int k = 0; k < 3; ++k) {
+        const double a = sc->pbc_lower[k], b = sc->pbc_upper[k];
+        w->pbc_lo[k] = a < b ? a : b;
+        w->pbc_hi[k] = a < b ? b : a;
+        w->pbc_r[k] = w->pbc_hi[k] - w->pbc_lo[k];
+        w->pbc_sw[k] = a != b;
+        w->pbc_on |= w->pbc_sw[k];
+    }
     w->t_start = sc->time_start; w->t_stop = sc->time_stop; w->dt = sc->time_interval; w->t = sc->time_current;
     w->g = ld3(sc->field_acceleration);
     w->sf = sc->safety_factor;
@@ -1013,6 +1059,8 @@ int dp_run(dp_world* w, unsigned nsteps) {
             add_impact(w, o, smul(dt, w->models[w->model_of[o]].ext), 0);
         }
         for (unsigned o = 0; o < w->n; ++o) respond(w, o, dt);                 /* DOContainer::Response */
+        if (w->pbc_on)                                                         /* SimMediator.cpp:746 */
+            for (unsigned o = 0; o < w->n; ++o) wrap_position(w, w->pos + 3 * o);
         for (unsigned k = 0; k < w->ncand; ++k) detect(w, &w->it[k]);         /* CheckContactStatus */
         w->round++;                                                            /* NBSConsultant::NextStep */
         w->t += dt;

@@ -481,6 +481,61 @@ def holed_plate_drop(n_side: int = 6, seed: int = 4, steps: int = 600, dt: float
     return Scene(time_control(steps, dt), models, iacts, midx, P, V, OX, OZ, np.zeros((n + 1, 3)))
 
 
+def periodic_layer(nx: int = 4, ny: int = 4, layers: int = 3, seed: int = 6, steps: int = 400, dt: float = 1e-6,
+                   radius: float = 1e-3, solver: str = "ISwBSDBF", periodic_y: bool = True,
+                   drift: Tuple[float, float] = (3.0, -2.0), floor_spin: float = 0.0,
+                   side_walls: bool = False) -> Scene:
+    """Spheres tiling a box that is periodic in x (and y) on a floor plate, drifting across the
+    periodic faces.  The lattice is placed so that the spheres of one column start 0.1 mm short
+    of the upper x face (and one row 0.1 mm above the lower y face), so they wrap within the
+    first few dozen steps, while a pair in contact is still a candidate (with no drift the
+    lattice sits 1 mm clear of the faces instead).  The floor's centre is
+    off the box centre (lever arms to it cross half a period); `floor_spin` makes it an orbital
+    plate turning about its normal.  `side_walls` (with y not periodic) adds two fixed plates
+    normal to y whose centres lie outside the box in x: the periodic wrap moves them after the
+    first step, as it moves every object."""
+    rng = np.random.default_rng(seed)
+    sp = 2.05 * radius
+    Lx, Ly = nx * sp, ny * sp
+    h = 1e-3
+    i, j, k = np.meshgrid(np.arange(nx), np.arange(ny), np.arange(layers), indexing="ij")
+    ox0, oy0 = (0.95, 0.05) if drift[0] or drift[1] else (0.5, 0.5)     # no drift: 1 mm clear of the faces
+    pos = np.stack([-0.5 * Lx + (i.ravel() + ox0) * sp, -0.5 * Ly + (j.ravel() + oy0) * sp,
+                    radius + 5e-6 + k.ravel() * sp], 1)
+    pos += rng.uniform(-0.01 * sp, 0.01 * sp, size=pos.shape) * np.array([1.0, 1.0, 0.0])
+    n = pos.shape[0]
+    vel = rng.normal(0.0, 0.3, size=pos.shape)
+    vel[:, 0] += drift[0]
+    vel[:, 1] += drift[1] if periodic_y else 0.0
+    avel = rng.normal(0.0, 20.0, size=pos.shape)
+    floor_beh = ORBITAL if floor_spin else FIXED
+    models = [DOModel("Ball", "Ball", MOBILE, LOCAL, 2500.0, 1.0, SPHERE, (radius,)),
+              DOModel("Floor", "Wall", floor_beh, GLOBAL, 0.0, 1.0, QUASI_PLATE, (4 * Lx, h, 4 * Ly))]
+    midx = [np.zeros(n, np.uint32), np.array([1], np.uint32)]
+    P = [pos, np.array([[-0.3 * Lx, -0.3 * Ly if periodic_y else 0.0, -0.5 * h]])]
+    OX, OZ = [np.tile([1.0, 0, 0], (n, 1)), np.array([[1.0, 0.0, 0.0]])], [np.tile([0, 0, 1.0], (n, 1)),
+                                                                          np.array([[0.0, 0.0, 1.0]])]
+    AV = [avel, np.array([[0.0, 0.0, floor_spin]])]
+    if side_walls and not periodic_y:
+        models.append(DOModel("Side", "Wall", FIXED, GLOBAL, 0.0, 1.0, QUASI_PLATE, (4 * Lx, h, 4 * layers * sp)))
+        midx.append(np.array([2, 2], np.uint32))
+        P.append(np.array([[0.75 * Lx, 0.5 * Ly + 0.5 * h, 2 * layers * sp],
+                           [0.8 * Lx, -0.5 * Ly - 0.5 * h, 2 * layers * sp]]))
+        OX.append(np.tile([1.0, 0.0, 0.0], (2, 1)))
+        OZ.append(np.array([[0.0, 1.0, 0.0], [0.0, -1.0, 0.0]]))
+        AV.append(np.zeros((2, 3)))
+    zeta = damping_ratio(0.7)
+    iacts = [IactModel("Ball", "Ball", solver, _mechanisms(solver, zeta / math.sqrt(2.0), 0.5)),
+             IactModel("Wall", "Ball", solver, _mechanisms(solver, zeta, 0.5))]
+    P = np.concatenate(P)
+    sc = Scene(time_control(steps, dt), models, iacts, np.concatenate(midx), P,
+               np.concatenate([vel, np.zeros((P.shape[0] - n, 3))]), np.concatenate(OX), np.concatenate(OZ),
+               np.concatenate(AV))
+    sc.sp.pbc = Boundary(switch=(True, periodic_y, False), lower=(-0.5 * Lx, -0.5 * Ly if periodic_y else 0.0, 0.0),
+                         upper=(0.5 * Lx, 0.5 * Ly if periodic_y else 0.0, 0.0))
+    return sc
+
+
 def hopper_params(num_scenes: int = 256, seed: int = 2025, n_lo: int = 1000, n_hi: int = 50000):
     """Per-scene draws of the hopper batch: (n, seed, friction, restitution, orifice)."""
     rng = np.random.default_rng(seed)
