@@ -42,8 +42,9 @@ enum {
     VEDO_ERR_INVALID_SCENE = 2,     /* unknown model, bad index, empty world          */
     VEDO_ERR_UNSUPPORTED_MODEL = 3, /* no detector/solver for a shape pair or
                                        equation type (the factories' null result,
-                                       Assembler.cpp:72-85), or a feature the engine
-                                       does not implement (e.g. periodic boundary)   */
+                                       Assembler.cpp:72-85), or a feature the chosen
+                                       form does not implement (e.g. a periodic
+                                       boundary in the mixed form)                    */
     VEDO_ERR_OUT_OF_MEMORY = 4,     /* device allocation failed / admission rejected  */
     VEDO_ERR_CUDA = 5,              /* any other CUDA runtime error                   */
     VEDO_ERR_DEVICE_TIMEOUT = 6,    /* a bounded device wait gave up                  */
@@ -90,7 +91,9 @@ typedef struct vedo_scene_desc {
     uint8_t zoi_switch[3], pbc_switch[3];
     uint8_t reserved[2];
     double zoi_lower[3], zoi_upper[3];
-    double pbc_lower[3], pbc_upper[3];
+    double pbc_lower[3], pbc_upper[3];       /* periodic boundary (Boundary.cpp:225-345):
+                                                an axis is periodic where its bounds
+                                                differ; FP64 form only                 */
     uint32_t max_id_of_do;
     /* models */
     uint32_t num_models;

@@ -651,7 +651,7 @@ static void solve(dp_world* w, iactn_t* I, double dt) {
         rA = sub(ci->point, ld3(w->pos + 3 * A));
         rB = sub(ci->point, ld3(w->pos + 3 * B));
         if (w->pbc_on) {          /* every law: ISwBSDBF.cpp:69-73, ISwBtSDBF.cpp:69-73, ISwBSDB2F.cpp:72-76,
-                                     ISwHertz.cpp:59-63, ISwH.cpp:68-72 */
+                                     ISwHertz.cpp:59-63, ISwH.cpp:69-73 */
             rA = min_image(w, rA);
             rB = min_image(w, rB);
         }

@@ -31,6 +31,14 @@ def cases():
     yield "cluster_bsdbf_upiact1", scenes.cluster(n=27, solver="ISwBSDBF", steps=200, seed=2), 150, 1
     yield "cluster_zoi", zoi_scene(), 200, 5
     yield "holed_plate_lsd", scenes.holed_plate_drop(steps=500), 400, 5
+    # periodic boundary: spheres drift across the faces (wrap, minimum image in the detector and
+    # in every law's lever arms); ISwH with an orbital floor and side walls that the wrap moves
+    yield "periodic_lsd", scenes.periodic_layer(solver="ISwBSDBF"), 400, 5
+    yield "periodic_hertz", scenes.periodic_layer(solver="ISwHertz", seed=8), 400, 5
+    yield "periodic_far_lsd", scenes.periodic_layer(solver="ISwBSDBF", nx=3, ny=3, layers=2, seed=12,
+                                                    outside=True), 200, 4
+    yield "periodic_h", scenes.periodic_layer(solver="ISwH", periodic_y=False, floor_spin=40.0, side_walls=True,
+                                              seed=9, drift=(0.0, 0.0)), 400, 5
 
 
 def zoi_scene():

@@ -20,7 +20,8 @@ pytestmark = pytest.mark.gpu
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 GOLDEN = sorted(glob.glob(os.path.join(ROOT, "tests", "golden", "*.npz")))
 EXACT_CASES = ("box_lsd", "cluster_ISwBSDBF", "cluster_ISwBtSDBF", "cluster_ISwBSDB2F", "cluster_bsdbf_upiact1",
-               "cluster_zoi", "holed_plate_lsd")
+               "cluster_zoi", "holed_plate_lsd", "periodic_lsd",
+               "periodic_far_lsd")
 STATE = ("position", "velocity", "angular_velocity", "impact", "angular_impact", "orientation_x", "orientation_z")
 
 
@@ -258,3 +259,40 @@ def test_external_impulses_equal_a_constant_external_force(precision, engine_lib
             np.testing.assert_allclose(ra[k], rb[k], rtol=1e-5, atol=1e-7 * (np.abs(ra[k]).max() + 1e-30),
                                        err_msg=k)
     assert np.abs(ra["velocity"] - scenes.cluster(n=48, solver="ISwBSDBF", steps=400, seed=5).velocity).max() > 0
+
+
+def test_periodic_layer_at_size_bitexact(engine_lib, port_lib):
+    """A 12 x 12 x 4 layer drifting across both periodic faces: 300 steps with rebuilds every 5,
+    the FP64 form bit for bit against the oracle (the wrap after Response, the minimum image in
+    the sphere detector and in the lever arms, the FP32 prefilter's periodic distance bound)."""
+    from oracle import PortWorld
+    sc = scenes.periodic_layer(nx=12, ny=12, layers=4, seed=21, steps=400)
+    e = engine_lib.GpuEngine(sc, up_iact=5)
+    p = PortWorld(sc, up_iact=5)
+    x0 = sc.position[:, 0].copy()
+    for _ in range(3):
+        e.run(100)
+        p.run(100)
+        a, b = e.state(), p.state()
+        for k in ("position", "velocity", "angular_velocity", "impact", "angular_impact"):
+            np.testing.assert_array_equal(a[k], b[k], err_msg=k)
+        ia = e.interactions()
+        f, s = p.candidates()
+        assert np.array_equal(ia["first"], f) and np.array_equal(ia["second"], s)
+        assert np.array_equal(ia["active"].astype(bool), p.interactions()["active"].astype(bool))
+    lo, hi = sc.sp.pbc.lower[0], sc.sp.pbc.upper[0]
+    x = a["position"][:-1, 0]
+    assert np.all((x >= lo) & (x < hi))
+    assert np.sum(x < x0[:-1] - 0.5 * (hi - lo)) > 10          # spheres that went out at the upper face
+
+
+def test_periodic_boundary_is_rejected_by_the_mixed_form(engine_lib):
+    """The mixed form (and so batches and serving) does not implement the periodic boundary: a
+    periodic scene is refused with VEDO_ERR_UNSUPPORTED_MODEL rather than run without it."""
+    sc = scenes.periodic_layer()
+    with pytest.raises(engine_lib.EngineError) as ex:
+        engine_lib.GpuEngine(sc, precision=1)
+    assert ex.value.code == 3
+    with pytest.raises(engine_lib.EngineError) as ex:
+        engine_lib.BatchEngine([sc])
+    assert ex.value.code == 3

@@ -73,6 +73,49 @@ __host__ __device__ __forceinline__ d3 cross(d3 a, d3 b) {
     return mk(a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x);
 }
 __host__ __device__ __forceinline__ d3 project_on(d3 a, d3 v) { return smul(dot(a, v) / len(v), dir(v)); }
+
+// The periodic boundary after Boundary::Correct (Boundary.cpp:79-128): an axis is switched on
+// where its bounds differ, `on` is Boundary::Active, range = upper - lower.
+struct Periodic {
+    int on;
+    int sw[3];
+    double lo[3], hi[3], range[3];
+    float range32[3];    // FP32 copies of the switched ranges for the prefilter, 0 where off
+};
+
+// Boundary::DifferenceBoundaryConditions (Boundary.cpp:306-345): the minimum image of a
+// difference vector on every switched axis.
+__host__ __device__ __forceinline__ double min_image1(double d, double r) {
+    if (d >= 0.5 * r) d -= r;
+    if (d < -0.5 * r) d += r;
+    return d;
+}
+__host__ __device__ __forceinline__ d3 min_image(const Periodic& b, d3 v) {
+    if (b.sw[0]) v.x = min_image1(v.x, b.range[0]);
+    if (b.sw[1]) v.y = min_image1(v.y, b.range[1]);
+    if (b.sw[2]) v.z = min_image1(v.z, b.range[2]);
+    return v;
+}
+
+// Boundary::EnforceBoundaryConditions (Boundary.cpp:225-304): a coordinate on a switched axis
+// goes back into [lower, upper) by one range, or by fmod (exact in IEEE arithmetic) beyond that.
+__host__ __device__ __forceinline__ double wrap1(double p, double lo, double hi, double r) {
+    if (p >= hi) {
+        p -= r;
+        if (p >= hi) p = lo + fmod(p - lo, r);
+    }
+    if (p < lo) {
+        p += r;
+        if (p < lo) p = lo + fmod(p - lo, r) + r;
+    }
+    return p;
+}
+__host__ __device__ __forceinline__ d3 wrap_position(const Periodic& b, d3 p) {
+    if (b.sw[0]) p.x = wrap1(p.x, b.lo[0], b.hi[0], b.range[0]);
+    if (b.sw[1]) p.y = wrap1(p.y, b.lo[1], b.hi[1], b.range[1]);
+    if (b.sw[2]) p.z = wrap1(p.z, b.lo[2], b.hi[2], b.range[2]);
+    return p;
+}
 #ifdef __CUDACC__
 // Vector3d::rotate_around (Vector3d.h:152-178)
 __device__ __forceinline__ d3 rotate_around(d3 p, d3 va) {

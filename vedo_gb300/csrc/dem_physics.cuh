@@ -23,11 +23,14 @@ struct PairParamFull {
 };
 
 // ContactDetector::Detect of the three shape pairs: depth, direction, impact point.
+// With an active periodic boundary the sphere-sphere detector takes the minimum image of the
+// centre difference (CDSphere2Sphere.cpp:19-22); the wall detectors do not.
 __device__ __forceinline__ void detect_pair(int cd, const PairGeom& g, d3 Ps, d3 Pm, const double4_32a* __restrict__ ox,
-                                            const double4_32a* __restrict__ oz, uint32_t m, double& depth, d3& n,
-                                            d3& point) {
+                                            const double4_32a* __restrict__ oz, uint32_t m, const Periodic& pb,
+                                            double& depth, d3& n, d3& point) {
     if (cd == CD_SS) {                                        // CDSphere2Sphere.cpp:14-41
         d3 vIm = sub(Pm, Ps);
+        if (pb.on) vIm = min_image(pb, vIm);
         depth = g.ra + g.b0 - len(vIm);
         n = dir(vIm);
     } else if (cd == CD_SP) {                                 // CDSphere2QuasiPlate.cpp:15-97
@@ -114,10 +117,12 @@ struct PairStatus {
 };
 
 // ImpactSolver::NextStep of the five laws for one pair; returns the PF_APPLIED/PF_ANGULAR bits
-// and the impulse J on the slave, angular impulses tA (slave) and tB (master).
+// and the impulse J on the slave, angular impulses tA (slave) and tB (master).  With an active
+// periodic boundary every law takes the minimum image of both lever arms (ISwBSDBF.cpp:69-73,
+// ISwBtSDBF.cpp:69-73, ISwBSDB2F.cpp:72-76, ISwHertz.cpp:59-63, ISwH.cpp:69-73).
 __device__ __forceinline__ uint8_t solve_pair(int is, const double* __restrict__ c, bool active, double depth, d3 n,
                                               d3 point, d3 Ps, d3 Pm, d3 Va, d3 Vb, d3 AVa, d3 AVb, double dt,
-                                              PairStatus& st, d3& J, d3& tA, d3& tB) {
+                                              const Periodic& pb, PairStatus& st, d3& J, d3& tA, d3& tB) {
     const d3 Z = mk(0.0, 0.0, 0.0);
     if (is == IS_HERTZ || is == IS_H) {
         if (!active) {                                        // ISwHertz.cpp:26-30, ISwH.cpp:132-136
@@ -133,6 +138,10 @@ __device__ __forceinline__ uint8_t solve_pair(int is, const double* __restrict__
     if (depth > 0.0) {
         rA = sub(point, Ps);
         rB = sub(point, Pm);
+        if (pb.on) {
+            rA = min_image(pb, rA);
+            rB = min_image(pb, rB);
+        }
         vRel = sub(add(sub(Va, Vb), cross(AVa, rA)), cross(AVb, rB));
         vRn = smul(dot(vRel, n), n);
         vRs = sub(vRel, vRn);

@@ -69,7 +69,7 @@ __global__ void __launch_bounds__(TPB) k_pair(uint32_t np, const uint2* __restri
                                               const float4* __restrict__ pos32, const float4* __restrict__ wall32,
                                               double4_32a* __restrict__ hist, double* __restrict__ v0,
                                               uint8_t* __restrict__ flags, double* __restrict__ out, double dt,
-                                              int backup) {
+                                              int backup, Periodic pb) {
     const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
     if (k >= np) return;
     const uint2 p = sm[k];
@@ -77,7 +77,7 @@ __global__ void __launch_bounds__(TPB) k_pair(uint32_t np, const uint2* __restri
     const int cd = params[pi].cd, is = params[pi].is;
     // Pairs that are certainly apart and carry no normal bond: ImpactStatus::Clean, no impulse.
     const bool bondable = (is == IS_BSDBF || is == IS_BTSDBF || is == IS_BSDB2F) && params[pi].c[4] != 0.0;
-    if (!bondable && certainly_apart(cd, pos32[p.x], pos32[p.y], wall32[p.y], reach[pi])) {
+    if (!bondable && certainly_apart(cd, pos32[p.x], pos32[p.y], wall32[p.y], reach[pi], pb.on ? pb.range32 : nullptr)) {
         const uint8_t f0 = flags[k];
         if (f0 & PF_NONZERO) {
             hist[k] = make_double4_32a(0.0, 0.0, 0.0, 0.0);
@@ -95,7 +95,7 @@ __global__ void __launch_bounds__(TPB) k_pair(uint32_t np, const uint2* __restri
     const d3 Ps = ld(pos, p.x), Pm = ld(pos, p.y);
     double depth;
     d3 n, point;
-    detect_pair(cd, g, Ps, Pm, ox, oz, p.y, depth, n, point);
+    detect_pair(cd, g, Ps, Pm, ox, oz, p.y, pb, depth, n, point);
     const bool active = depth > 0.0;
     const uint8_t f0 = flags[k];
     PairStatus st;
@@ -128,7 +128,7 @@ __global__ void __launch_bounds__(TPB) k_pair(uint32_t np, const uint2* __restri
     }
     const d3 Va = ld(vel, p.x), Vb = ld(vel, p.y), AVa = ld(av, p.x), AVb = ld(av, p.y);
     d3 J, tA, tB;
-    const uint8_t app = solve_pair(is, c, active, depth, n, point, Ps, Pm, Va, Vb, AVa, AVb, dt, st, J, tA, tB);
+    const uint8_t app = solve_pair(is, c, active, depth, n, point, Ps, Pm, Va, Vb, AVa, AVb, dt, pb, st, J, tA, tB);
     if (st.f & PF_NONZERO) {
         hist[k] = make_double4_32a(st.shear.x, st.shear.y, st.shear.z, st.kn);
         v0[k] = st.v0;
@@ -176,7 +176,8 @@ __device__ __forceinline__ void finish_object(uint32_t i, const ModelDev& m, d3 
                                               double4_32a* __restrict__ oz, double4_32a* __restrict__ imp,
                                               double4_32a* __restrict__ aimp, int write_imp, d3 origin,
                                               float4* __restrict__ pos32, float4* __restrict__ wall32,
-                                              const double* __restrict__ ext_imp, const double* __restrict__ ext_aimp) {
+                                              const double* __restrict__ ext_imp, const double* __restrict__ ext_aimp,
+                                              const Periodic& pb) {
     J = add(J, muls(fimp, m.sudo));                           // DOContainer::AddFieldImpact (DOContainer.cpp:25)
     J = add(J, smul(dt, mk(m.ext[0], m.ext[1], m.ext[2])));   // DiscreteObject::AddConstrainedImpact (:160-163)
     if (ext_imp) {                 // SimMediator::Run(external impacts): DOContainer::AddImpact (SimMediator.cpp:1015-1018)
@@ -186,6 +187,7 @@ __device__ __forceinline__ void finish_object(uint32_t i, const ModelDev& m, d3 
     if (m.behavior != BEH_FIXED) {
         d3 P = ld(pos, i), V = ld(vel, i), AV = ld(av, i), Ox = ld(ox, i), Oz = ld(oz, i);
         respond_object(m, dt, J, JA, P, V, AV, Ox, Oz);
+        if (pb.on) P = wrap_position(pb, P);                 // DOContainer::EnforcePeriodicBoundaryConditions
         st(pos, i, P, 0.0);
         st(ox, i, Ox, 0.0);
         st(oz, i, Oz, 0.0);
@@ -194,6 +196,12 @@ __device__ __forceinline__ void finish_object(uint32_t i, const ModelDev& m, d3 
             st(av, i, AV, 0.0);
         }
         write32(i, m.shape, P, Ox, Oz, origin, pos32, wall32);
+    } else if (pb.on) {            // the wrap moves every object, fixed ones included (SimMediator.cpp:746)
+        const d3 P = ld(pos, i), W = wrap_position(pb, P);
+        if (W.x != P.x || W.y != P.y || W.z != P.z) {
+            st(pos, i, W, 0.0);
+            write32(i, m.shape, W, ld(ox, i), ld(oz, i), origin, pos32, wall32);
+        }
     }
     if (write_imp) {                                          // DiscreteObject::ClearImpact (:141-147)
         st(imp, i, J, 0.0);
@@ -210,7 +218,7 @@ __global__ void __launch_bounds__(TPB) k_obj(uint32_t n, const uint32_t* __restr
                                              const uint8_t* __restrict__ flags, const double* __restrict__ out,
                                              double dt, d3 fimp, int write_imp, d3 origin, float4* __restrict__ pos32,
                                              float4* __restrict__ wall32, const double* __restrict__ ext_imp,
-                                             const double* __restrict__ ext_aimp) {
+                                             const double* __restrict__ ext_aimp, Periodic pb) {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     const ModelDev& m = models[model_of[i]];
@@ -222,7 +230,7 @@ __global__ void __launch_bounds__(TPB) k_obj(uint32_t n, const uint32_t* __restr
         add_entry(ent, flags[ent >> 1], out, J, JA);
     }
     finish_object(i, m, J, JA, dt, fimp, pos, vel, av, ox, oz, imp, aimp, write_imp, origin, pos32, wall32, ext_imp,
-                  ext_aimp);
+                  ext_aimp, pb);
 }
 
 // One warp per scope-global object: lanes load 32 entries at a time, then every lane adds
@@ -234,7 +242,7 @@ __global__ void k_obj_global(uint32_t nglob, const uint32_t* __restrict__ glob, 
                              const uint32_t* __restrict__ csr_ptr, const uint32_t* __restrict__ csr_ent,
                              const uint8_t* __restrict__ flags, const double* __restrict__ out, double dt, d3 fimp,
                              int write_imp, d3 origin, float4* __restrict__ pos32, float4* __restrict__ wall32,
-                             const double* __restrict__ ext_imp, const double* __restrict__ ext_aimp) {
+                             const double* __restrict__ ext_imp, const double* __restrict__ ext_aimp, Periodic pb) {
     const uint32_t w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const int lane = threadIdx.x & 31;
     if (w >= nglob) return;
@@ -277,7 +285,7 @@ __global__ void k_obj_global(uint32_t nglob, const uint32_t* __restrict__ glob, 
     }
     if (lane == 0)
         finish_object(i, m, J, JA, dt, fimp, pos, vel, av, ox, oz, imp, aimp, write_imp, origin, pos32, wall32,
-                      ext_imp, ext_aimp);
+                      ext_imp, ext_aimp, pb);
 }
 
 // Narrow phase only: PF_ACTIVE of every pair at the current positions (the IsActive()
@@ -291,14 +299,15 @@ __global__ void __launch_bounds__(TPB) k_detect_active(uint32_t np, const uint2*
                                                        const double4_32a* __restrict__ pos, const double4_32a* __restrict__ ox,
                                                        const double4_32a* __restrict__ oz,
                                                        const float4* __restrict__ pos32,
-                                                       const float4* __restrict__ wall32, uint8_t* __restrict__ flags) {
+                                                       const float4* __restrict__ wall32, uint8_t* __restrict__ flags,
+                                                       Periodic pb) {
     const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
     if (k >= np) return;
     const uint2 p = sm[k];
     const uint32_t pi = param[k];
     const uint8_t f = flags[k];
     double depth = -1.0;
-    if (!certainly_apart(params[pi].cd, pos32[p.x], pos32[p.y], wall32[p.y], reach[pi])) {
+    if (!certainly_apart(params[pi].cd, pos32[p.x], pos32[p.y], wall32[p.y], reach[pi], pb.on ? pb.range32 : nullptr)) {
         const double4_32a gg = geom[pi];
         PairGeom g{gg.x, gg.y, gg.z, gg.w, 0.0, 0.0, 0.0};
         if (params[pi].cd == CD_SHP) {
@@ -306,7 +315,7 @@ __global__ void __launch_bounds__(TPB) k_detect_active(uint32_t np, const uint2*
             g.hr = hh.x; g.hxo = hh.y; g.hyo = hh.z;
         }
         d3 n, point;
-        detect_pair(params[pi].cd, g, ld(pos, p.x), ld(pos, p.y), ox, oz, p.y, depth, n, point);
+        detect_pair(params[pi].cd, g, ld(pos, p.x), ld(pos, p.y), ox, oz, p.y, pb, depth, n, point);
     }
     const uint8_t nf = depth > 0.0 ? (uint8_t)(f | PF_ACTIVE) : (uint8_t)(f & ~PF_ACTIVE);
     if (nf != f) flags[k] = nf;
@@ -582,7 +591,8 @@ __global__ void __launch_bounds__(TPB) k_history_old(uint32_t np, const uint32_t
                                                      const uint8_t* __restrict__ o_flags,
                                                      const double4_32a* __restrict__ o_hist,
                                                      const double* __restrict__ o_v0, double4_32a* __restrict__ hist,
-                                                     double* __restrict__ v0, uint8_t* __restrict__ flags) {
+                                                     double* __restrict__ v0, uint8_t* __restrict__ flags,
+                                                     Periodic pb) {
     const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
     if (k >= np) return;
     const uint32_t a = first[k], b = second[k];
@@ -592,7 +602,8 @@ __global__ void __launch_bounds__(TPB) k_history_old(uint32_t np, const uint32_t
     const uint2 p = sm[k];
     const uint32_t pi = param[k];
     // a pair certainly apart now was not active at this position in the old list either
-    const bool maybe = !certainly_apart(params[pi].cd, pos32[p.x], pos32[p.y], wall32[p.y], reach[pi]);
+    const bool maybe = !certainly_apart(params[pi].cd, pos32[p.x], pos32[p.y], wall32[p.y], reach[pi],
+                                        pb.on ? pb.range32 : nullptr);
     const uint32_t e1 = maybe ? o_ptr[a + 1] : 0u;
     for (uint32_t e = maybe ? o_ptr[a] : 0u; e < e1; ++e) {
         const uint32_t ko = o_ent[e] >> 1;
@@ -855,7 +866,7 @@ int Engine::rebuild(bool from_records) {
     if (!from_records && cur_.np) {
         k_detect_active<<<blocks_for(cur_.np), TPB, 0, stream_>>>(cur_.np, cur_.sm, cur_.param, d_params_, d_geom_,
                                                                   d_hole_, d_reach_, d_pos_, d_ox_, d_oz_, d_pos32_,
-                                                                  d_wall32_, cur_.flags);
+                                                                  d_wall32_, cur_.flags, tab_.pbc);
         ++own;
     }
     std::swap(cur_, old_);
@@ -956,7 +967,7 @@ int Engine::rebuild(bool from_records) {
             k_history_old<<<blocks_for(np), TPB, 0, stream_>>>(np, cur_.first, cur_.second, cur_.sm, cur_.param,
                                                                d_params_, d_reach_, d_pos32_, d_wall32_, old_.csr_ptr,
                                                                old_.csr_ent, old_.first, old_.second, old_.flags,
-                                                               old_.hist, old_.v0, cur_.hist, cur_.v0, cur_.flags);
+                                                               old_.hist, old_.v0, cur_.hist, cur_.v0, cur_.flags, tab_.pbc);
         }
         ++own;
     }
@@ -1004,7 +1015,7 @@ int Engine::step_once(bool write_impulses) {
                                                          d_reach_,
                                                          d_pos_, d_vel_, d_av_, d_ox_, d_oz_, d_pos32_, d_wall32_,
                                                          cur_.hist, cur_.v0, cur_.flags, cur_.out, dt,
-                                                         backup_pending_ ? 1 : 0);
+                                                         backup_pending_ ? 1 : 0, tab_.pbc);
         ++launches_;
     }
     if (prof) CK(cudaEventRecord(ev_[1], stream_));
@@ -1013,13 +1024,14 @@ int Engine::step_once(bool write_impulses) {
     const d3 org = mk(origin_[0], origin_[1], origin_[2]);
     k_obj<<<blocks_for(n_), TPB, 0, stream_>>>(n_, d_model_of_, d_models_, d_pos_, d_vel_, d_av_, d_ox_, d_oz_,
                                                d_imp_, d_aimp_, cur_.csr_ptr, cur_.csr_ent, cur_.flags, cur_.out, dt,
-                                               fimp, write_impulses ? 1 : 0, org, d_pos32_, d_wall32_, ext_imp_, ext_aimp_);
+                                               fimp, write_impulses ? 1 : 0, org, d_pos32_, d_wall32_, ext_imp_, ext_aimp_,
+                                               tab_.pbc);
     ++launches_;
     if (!global_ids_.empty()) {
         k_obj_global<<<blocks_for((uint64_t)global_ids_.size() * 32), TPB, 0, stream_>>>(
             (uint32_t)global_ids_.size(), d_global_, d_model_of_, d_models_, d_pos_, d_vel_, d_av_, d_ox_, d_oz_,
             d_imp_, d_aimp_, cur_.csr_ptr, cur_.csr_ent, cur_.flags, cur_.out, dt, fimp, write_impulses ? 1 : 0, org,
-            d_pos32_, d_wall32_, ext_imp_, ext_aimp_);
+            d_pos32_, d_wall32_, ext_imp_, ext_aimp_, tab_.pbc);
         ++launches_;
     }
     if (prof) CK(cudaEventRecord(ev_[2], stream_));
@@ -1174,7 +1186,7 @@ int Engine::get_interactions(const vedo_contact_view& v) {
     if (!np) return VEDO_OK;
     // ContactInfo::bActive of the last narrow phase = detection at the current positions
     k_detect_active<<<blocks_for(np), TPB, 0, stream_>>>(np, cur_.sm, cur_.param, d_params_, d_geom_, d_hole_, d_reach_,
-                                                         d_pos_, d_ox_, d_oz_, d_pos32_, d_wall32_, cur_.flags);
+                                                         d_pos_, d_ox_, d_oz_, d_pos32_, d_wall32_, cur_.flags, tab_.pbc);
     std::vector<uint2> sm(np);
     std::vector<uint8_t> fl(np);
     std::vector<double4_32a> h(np);
@@ -1210,7 +1222,7 @@ int Engine::get_observables(double out[13]) {
     if (cur_.np)
         k_detect_active<<<blocks_for(cur_.np), TPB, 0, stream_>>>(cur_.np, cur_.sm, cur_.param, d_params_, d_geom_,
                                                                   d_hole_, d_reach_, d_pos_, d_ox_, d_oz_, d_pos32_,
-                                                                  d_wall32_, cur_.flags);
+                                                                  d_wall32_, cur_.flags, tab_.pbc);
     obs::k_obs_b<<<nb, TPB, 0, stream_>>>(n_, d_model_of_, d_models_, d_pos_, d_vel_, d_av_, res, 0, cur_.flags, cur_.np,
                                      part);
     obs::k_obs_reduce<<<1, 32, 0, stream_>>>(nb, 6, part, res + 16, 6);

@@ -2082,6 +2082,8 @@ int MixedEngine::init_from(const std::vector<SceneSource>& src, const MixedEngin
         std::string msg;
         int rc = build_tables(h, t, msg);
         if (rc != VEDO_OK) return fail(rc, msg);
+        if (t.pbc.on)        // the plain FP64 form runs periodic scenes
+            return fail(VEDO_ERR_UNSUPPORTED_MODEL, "periodic boundary conditions: the mixed form does not implement them");
         SceneHost S;
         S.obj_off = n_;
         S.nobj = h.n;

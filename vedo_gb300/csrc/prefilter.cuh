@@ -49,14 +49,32 @@ __device__ __forceinline__ float line_dist32(const float4& a, const float4& b, c
     return d;
 }
 
+// Lower-bounded sphere centre distance under a periodic boundary: per axis the least of |d|,
+// |d - L|, |d + L| (L = the axis' range, 0 where off), which is at most the minimum-image
+// difference the detector takes, whichever image it picks; the shifted differences add the
+// rounding of L and of one more subtraction to the error.
+__device__ __forceinline__ float dist32_periodic(const float4& a, const float4& b, const float* L, float& err) {
+    float d[3] = {b.x - a.x, b.y - a.y, b.z - a.z};
+    float ext = 0.0f;
+    for (int k = 0; k < 3; ++k) {
+        if (L[k] == 0.0f) continue;
+        ext += 4.0f * PF_POS_EPS * (fabsf(d[k]) + L[k]);
+        d[k] = fminf(fabsf(d[k]), fminf(fabsf(d[k] - L[k]), fabsf(d[k] + L[k])));
+    }
+    const float l = sqrtf(d[0] * d[0] + d[1] * d[1] + d[2] * d[2]);
+    err = PF_POS_EPS * (l1(a) + l1(b)) + ext + PF_ARITH_EPS * l;
+    return l;
+}
+
 // cd: 1 sphere-sphere, 2 sphere-plate (4, with a hole: tested as the full plate), 3 sphere-cylinder.  `reach` bounds the distance at
 // which the pair can be in contact (radius sum, or radius + plate half-thickness, or sphere
-// + cylinder radius), already rounded up.  True when the pair is certainly apart.
+// + cylinder radius), already rounded up.  `periodic`: the FP32 ranges of an active periodic
+// boundary (sphere pairs only).  True when the pair is certainly apart.
 __device__ __forceinline__ bool certainly_apart(int cd, const float4& s, const float4& m, const float4& wall,
-                                                float reach) {
+                                                float reach, const float* periodic = nullptr) {
     float e, d;
     if (cd == 1) {
-        d = dist32(s, m, e);
+        d = periodic ? dist32_periodic(s, m, periodic, e) : dist32(s, m, e);
     } else if (cd == 2 || cd == 4) {
         if (wall.w == 0.0f) return false;
         d = plane_dist32(s, m, wall, e);

@@ -446,9 +446,17 @@ uint32_t prepare_scene(HScene& s) {
 }
 
 int build_tables(const HScene& s, Tables& t, std::string& err) {
-    if (s.pbc_switch[0] || s.pbc_switch[1] || s.pbc_switch[2]) {
-        err = "periodic boundary conditions are not implemented";
-        return VEDO_ERR_UNSUPPORTED_MODEL;
+    // Boundary::Correct (Boundary.cpp:79-128) as prepare_scene applied it: switched where the
+    // bounds differ; range = upper - lower
+    t.pbc = Periodic{};
+    for (int k = 0; k < 3; ++k) {
+        const double a = std::min(s.pbc_lower[k], s.pbc_upper[k]), b = std::max(s.pbc_lower[k], s.pbc_upper[k]);
+        t.pbc.lo[k] = a;
+        t.pbc.hi[k] = b;
+        t.pbc.range[k] = b - a;
+        t.pbc.sw[k] = a != b ? 1 : 0;
+        t.pbc.range32[k] = a != b ? (float)(b - a) : 0.0f;
+        t.pbc.on |= t.pbc.sw[k];
     }
     if (s.n == 0) { err = "empty world"; return VEDO_ERR_INVALID_SCENE; }
     const size_t nm = s.models.size();

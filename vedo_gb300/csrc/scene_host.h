@@ -72,6 +72,7 @@ struct Tables {
     std::vector<PairParam> params;        // [nmodels*nmodels], (slave model, master model)
     std::vector<double> geom;             // [nmodels*nmodels][4]: slave radius, master attrs a0..a2
     std::vector<double> hole;             // [nmodels*nmodels][4]: hole radius, x and y offsets (CD_SHP pairs)
+    Periodic pbc{};                       // the periodic boundary (on = 0: none)
 };
 
 // DOModel::Analysis + DOcf selection + ImpactSolver constructor constants.  Fails with

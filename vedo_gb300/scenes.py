@@ -484,7 +484,7 @@ def holed_plate_drop(n_side: int = 6, seed: int = 4, steps: int = 600, dt: float
 def periodic_layer(nx: int = 4, ny: int = 4, layers: int = 3, seed: int = 6, steps: int = 400, dt: float = 1e-6,
                    radius: float = 1e-3, solver: str = "ISwBSDBF", periodic_y: bool = True,
                    drift: Tuple[float, float] = (3.0, -2.0), floor_spin: float = 0.0,
-                   side_walls: bool = False) -> Scene:
+                   side_walls: bool = False, outside: bool = False) -> Scene:
     """Spheres tiling a box that is periodic in x (and y) on a floor plate, drifting across the
     periodic faces.  The lattice is placed so that the spheres of one column start 0.1 mm short
     of the upper x face (and one row 0.1 mm above the lower y face), so they wrap within the
@@ -493,7 +493,8 @@ def periodic_layer(nx: int = 4, ny: int = 4, layers: int = 3, seed: int = 6, ste
     off the box centre (lever arms to it cross half a period); `floor_spin` makes it an orbital
     plate turning about its normal.  `side_walls` (with y not periodic) adds two fixed plates
     normal to y whose centres lie outside the box in x: the periodic wrap moves them after the
-    first step, as it moves every object."""
+    first step, as it moves every object.  `outside` adds two spheres above the lattice placed
+    more than one range beyond the box in x (the wrap's fmod branch brings them back)."""
     rng = np.random.default_rng(seed)
     sp = 2.05 * radius
     Lx, Ly = nx * sp, ny * sp
@@ -503,6 +504,9 @@ def periodic_layer(nx: int = 4, ny: int = 4, layers: int = 3, seed: int = 6, ste
     pos = np.stack([-0.5 * Lx + (i.ravel() + ox0) * sp, -0.5 * Ly + (j.ravel() + oy0) * sp,
                     radius + 5e-6 + k.ravel() * sp], 1)
     pos += rng.uniform(-0.01 * sp, 0.01 * sp, size=pos.shape) * np.array([1.0, 1.0, 0.0])
+    if outside:
+        ztop = radius + 5e-6 + (layers + 1) * sp
+        pos = np.concatenate([pos, [[0.5 * Lx + 2.2 * Lx, 0.1 * Ly, ztop], [-0.5 * Lx - 3.4 * Lx, -0.2 * Ly, ztop]]])
     n = pos.shape[0]
     vel = rng.normal(0.0, 0.3, size=pos.shape)
     vel[:, 0] += drift[0]
