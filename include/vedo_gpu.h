@@ -196,7 +196,8 @@ int vedo_gpu_create_from_xml(const char* path, const vedo_engine_opts* opts, ved
 
 /* Convert a scene file between .ido and .xml by the names' extensions, without a GPU (the
  * reference's DOWorld::ReadIDO/WriteIDO and ReadXML/WriteXML; XML values are written with 17
- * significant digits). */
+ * significant digits); a .vtu output is the world as the post-processing tool's conversion
+ * writes it (DOWorld::WriteVTK<NullExternalFieldVTKWriter>, DOWorld_WriteVTK.h:148-243). */
 int vedo_convert_scene(const char* in_path, const char* out_path);
 
 /* Advance nsteps time steps, each one SimMediator::Run() (SimMediator.cpp:714-842).
@@ -281,6 +282,25 @@ int vedo_gpu_list_status(vedo_gpu_engine* e, double out[6]);
 /* Write world + active-contact records as a reference .ido
  * (DOWorld::WriteIDO, DOWorld_RWIDO.cpp:149-202). */
 int vedo_gpu_write_ido(vedo_gpu_engine* e, const char* path);
+
+/* Coordination numbers of the post-processing tool (CalcCoordinateNum.cpp, replaces
+ * CalcCoordinateNum::computeAvgCoordinateNum :8-77 and outputCoordinateNumVTK :79-126), computed
+ * on the device from the current state: per object, the number of other spheres whose centre
+ * distance is below (`below`) or at most (`touching`) the radius sum, 0 for other shapes (either
+ * array may be NULL, else num_objects long).  With `box` = {xmin, xmax, ymin, ymax, zmin, zmax}
+ * and `average`, *average = computeAvgCoordinateNum over the box: the `touching` counts of the
+ * spheres whose centre lies strictly inside the box widened by their radius, summed as an
+ * unsigned 32-bit integer and divided by their number (NaN when there is none).  Single-scene
+ * engines (VEDO_ERR_INVALID_ARGUMENT for a batch). */
+int vedo_gpu_coordination(vedo_gpu_engine* e, uint32_t* below, uint32_t* touching, const double* box,
+                          double* average);
+
+/* The current state as a VTK unstructured-grid file (DOWorld::WriteVTK, DOWorld_WriteVTK.h:148-243):
+ * every object a point with position, velocity, angular velocity, their magnitudes, radius (0 for
+ * other shapes) and granular temperatures (0); with_coordination != 0 adds the spheres'
+ * "CoordinateNumber" field (the `below` counts, spheres in object order) as
+ * CalcCoordinateNum::outputCoordinateNumVTK writes it.  Single-scene engines. */
+int vedo_gpu_write_vtk(vedo_gpu_engine* e, const char* path, int with_coordination);
 
 /* Device time of the last vedo_gpu_run call in milliseconds, from CUDA events on
  * the engine's stream: out[3] = the whole call; with profiling on (see

@@ -1174,6 +1174,39 @@ void dp_energy(const dp_world* w, double* out) {
     out[7] = mn; out[8] = amn;
 }
 
+/* CalcCoordinateNum (vedo/knight/CalcCoordinateNum.cpp).  outputCoordinateNumVTK (:79-126) counts
+   the pairs i < j of spheres with |p_i - p_j| < r_i + r_j; computeAvgCoordinateNum (:8-77) takes
+   the spheres whose centre lies strictly inside the box widened by their radius and counts, for
+   each, the other spheres with |p_i - p_j| <= r_i + r_j; the total is an unsigned 32-bit sum. */
+double dp_coordination(const dp_world* w, const double* box, unsigned* below, unsigned* touching) {
+    for (unsigned i = 0; i < w->n; ++i) { below[i] = 0; touching[i] = 0; }
+    for (unsigned i = 0; i < w->n; ++i) {
+        const model_t* mi = &w->models[w->model_of[i]];
+        if (mi->shape != VEDO_SHAPE_SPHERE) continue;
+        for (unsigned j = i + 1; j < w->n; ++j) {
+            const model_t* mj = &w->models[w->model_of[j]];
+            if (mj->shape != VEDO_SHAPE_SPHERE) continue;
+            const double d = len(sub(ld3(w->pos + 3 * i), ld3(w->pos + 3 * j)));
+            const double rs = mi->a[0] + mj->a[0];
+            if (d < rs) { below[i]++; below[j]++; }
+            if (d <= rs) { touching[i]++; touching[j]++; }
+        }
+    }
+    unsigned total = 0, count = 0;
+    for (unsigned i = 0; i < w->n; ++i) {
+        const model_t* m = &w->models[w->model_of[i]];
+        if (m->shape != VEDO_SHAPE_SPHERE) continue;
+        const double* p = w->pos + 3 * i;
+        const double r = m->a[0];
+        if (p[0] < box[1] + r && p[0] > box[0] - r && p[1] < box[3] + r && p[1] > box[2] - r &&
+            p[2] < box[5] + r && p[2] > box[4] - r) {
+            total += touching[i];
+            count++;
+        }
+    }
+    return total / (double)count;
+}
+
 void dp_destroy(dp_world* w) {
     if (!w) return;
     free(w->models); free(w->iacts); free(w->group_iact); free(w->model_of);

@@ -36,6 +36,10 @@ double dp_time(const dp_world* w);
 /* DOWorld::CalculateSystemEnergy over the current state (9 values, same
  * order as vedo_gpu_get_observables out[0..8]). */
 void dp_energy(const dp_world* w, double* out9);
+/* CalcCoordinateNum (vedo/knight/CalcCoordinateNum.cpp): per object the number of other spheres
+   whose centre distance is below (below) / at most (touching) the radius sum, 0 for other shapes;
+   returns computeAvgCoordinateNum over box = {xmin, xmax, ymin, ymax, zmin, zmax}. */
+double dp_coordination(const dp_world* w, const double* box, unsigned* below, unsigned* touching);
 void dp_destroy(dp_world* w);
 
 #ifdef __cplusplus

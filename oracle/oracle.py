@@ -86,6 +86,8 @@ class PortWorld(_World):
             L.dp_time.argtypes = [C.c_void_p]
             L.dp_time.restype = C.c_double
             L.dp_energy.argtypes = [C.c_void_p, _dp]
+            L.dp_coordination.argtypes = [C.c_void_p, _dp, _up, _up]
+            L.dp_coordination.restype = C.c_double
             L.dp_destroy.argtypes = [C.c_void_p]
             cls._lib = L
         return cls._lib
@@ -137,6 +139,14 @@ class PortWorld(_World):
         self.lib().dp_energy(self.h, _d(e))
         return e
 
+    def coordination(self, box=(0.0, 0.0, 0.0, 0.0, 0.0, 0.0)):
+        """(below, touching, average): CalcCoordinateNum's per-object counts and box average."""
+        below = np.zeros(self.n, np.uint32)
+        touching = np.zeros(self.n, np.uint32)
+        b = np.ascontiguousarray(box, dtype=np.float64)
+        avg = self.lib().dp_coordination(self.h, _d(b), below.ctypes.data_as(_up), touching.ctypes.data_as(_up))
+        return below, touching, avg
+
     def close(self):
         if getattr(self, "h", None):
             self.lib().dp_destroy(self.h)
@@ -147,6 +157,18 @@ class PortWorld(_World):
             self.close()
         except Exception:
             pass
+
+
+def ref_coordination(scene, box, coord_vtk: Optional[str] = None, world_vtk: Optional[str] = None) -> float:
+    """The reference's CalcCoordinateNum on `scene` (written as an IDO file): returns
+    computeAvgCoordinateNum over box = (xmin, xmax, ymin, ymax, zmin, zmax); writes the
+    coordination VTK file and the plain world VTK file when paths are given."""
+    L = RefWorld.lib()
+    with tempfile.TemporaryDirectory(prefix="vref_cn_") as td:
+        path = os.path.join(td, "scene.ido")
+        scene.to_ido(path)
+        b = np.ascontiguousarray(box, dtype=np.float64)
+        return L.vref_coordination(path.encode(), _d(b), (coord_vtk or "").encode(), (world_vtk or "").encode())
 
 
 class RefWorld(_World):
@@ -181,6 +203,8 @@ class RefWorld(_World):
             L.vref_write_ido.argtypes = [C.c_void_p, C.c_char_p]
             L.vref_write_xml.argtypes = [C.c_void_p, C.c_char_p]
             L.vref_close.argtypes = [C.c_void_p]
+            L.vref_coordination.argtypes = [C.c_char_p, _dp, C.c_char_p, C.c_char_p]
+            L.vref_coordination.restype = C.c_double
             cls._lib = L
         return cls._lib
 

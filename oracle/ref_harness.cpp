@@ -27,6 +27,8 @@
 #include <vedo/common/NBSConsultant.h>
 #include <vedo/common/SafeConsultant.h>
 #include <vedo/ModuleList.h>
+#include <vedo/framework/DOWorld_WriteVTK.h>
+#include <vedo/knight/CalcCoordinateNum.h>
 
 #include <unistd.h>
 #include <cstring>
@@ -194,6 +196,25 @@ void vref_write_ido(void* hp, const char* path) {
 void vref_write_xml(void* hp, const char* path) {
     RefHandle* h = static_cast<RefHandle*>(hp);
     h->world->WriteXML(path, h->irt);
+}
+
+/* The reference's post-processing observables on a world read from an IDO file (DOWorld::ReadIDO):
+ * returns CalcCoordinateNum::computeAvgCoordinateNum over box = {xmin, xmax, ymin, ymax, zmin,
+ * zmax} (CalcCoordinateNum.cpp:8-77); with coord_vtk, outputCoordinateNumVTK writes the
+ * per-sphere coordination numbers with the world (:79-126); with world_vtk, the world alone as
+ * the post-processing tool writes it (DOWorld::WriteVTK<NullExternalFieldVTKWriter>,
+ * Knight.cpp:711).  Returns -1 when the file cannot be read. */
+double vref_coordination(const char* ido_path, const double* box, const char* coord_vtk, const char* world_vtk) {
+    static std::ofstream devnull("/dev/null");
+    std::cout.rdbuf(devnull.rdbuf());
+    vedo::DOWorld* w = new vedo::DOWorld;
+    vedo::IactRecordTab* irt = new vedo::IactRecordTab();
+    if (!w->ReadIDO(ido_path, irt)) return -1.0;
+    CalcCoordinateNum c;
+    const double avg = c.computeAvgCoordinateNum(w, box[0], box[1], box[2], box[3], box[4], box[5]);
+    if (coord_vtk && coord_vtk[0]) c.outputCoordinateNumVTK(w, coord_vtk);
+    if (world_vtk && world_vtk[0]) w->WriteVTK<vedo::NullExternalFieldVTKWriter>(world_vtk);
+    return avg;   /* the world is leaked, as vref_close explains */
 }
 
 /* The reference's destructors release memory they do not own (the process aborts with

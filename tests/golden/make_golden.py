@@ -8,6 +8,9 @@ final object state, candidate list (IactPairTab order), interaction list
 (slave/master, active flag, shear history, kn, contact flag) and energies.
 
     python tests/golden/make_golden.py [case ...]      # all cases, or the named ones
+
+The observables' fixtures (tests/golden/observables/) hold the reference's coordination numbers
+(CalcCoordinateNum, compiled with the reference) and its VTK files for scenes with exact ties.
 """
 import os
 import sys
@@ -64,11 +67,38 @@ def zoi_scene():
     return out
 
 
+def observable_cases():
+    """(name, scene, box) of the coordination-number / VTK fixtures (tests/golden/observables/)."""
+    yield "touching_lattice", scenes.touching_lattice(), (0.0, 0.003, 0.0, 0.003, 0.0, 0.002)
+    yield "touching_lattice_whole", scenes.touching_lattice(seed=14, loose=80), (-1.0, 1.0, -1.0, 1.0, -1.0, 1.0)
+
+
+def make_observables(only):
+    """The reference's CalcCoordinateNum and DOWorld::WriteVTK on a scene read from its IDO file:
+    the box average, the coordination VTK file and the plain world VTK file, as written."""
+    import tempfile
+    from oracle import ref_coordination
+    out_dir = os.path.join(HERE, "observables")
+    os.makedirs(out_dir, exist_ok=True)
+    for name, sc, box in observable_cases():
+        if only and name not in only:
+            continue
+        with tempfile.TemporaryDirectory() as td:
+            cv, wv = os.path.join(td, "c.vtu"), os.path.join(td, "w.vtu")
+            avg = ref_coordination(sc, box, cv, wv)
+            coord_vtk, world_vtk = open(cv, "rb").read(), open(wv, "rb").read()
+        np.savez_compressed(os.path.join(out_dir, f"{name}.npz"), ido=np.frombuffer(sc.to_ido(), np.uint8),
+                            box=np.array(box), average=avg, coord_vtk=np.frombuffer(coord_vtk, np.uint8),
+                            world_vtk=np.frombuffer(world_vtk, np.uint8))
+        print(name, sc.num_objects, "objects, average coordination", avg)
+
+
 def main():
     import oracle
     oracle.build_ref()
     from oracle import RefWorld
     only = set(sys.argv[1:])
+    make_observables(only)
     for name, sc, steps, up in cases():
         if only and name not in only:
             continue

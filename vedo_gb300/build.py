@@ -38,6 +38,8 @@ SOURCES = {
     "mixed.cu": ("nvcc", ["-fmad=false"]),
     "sort_scan.cu": ("nvcc", []),
     "noalloc.cu": ("nvcc", []),
+    "coordination.cu": ("nvcc", ["-fmad=false"]),
+    "vtk_io.cpp": ("cxx", []),
     "scene_host.cpp": ("cxx", []),
     "capi.cpp": ("cxx", []),
     "xml_io.cpp": ("cxx", []),

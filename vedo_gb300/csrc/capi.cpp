@@ -5,6 +5,7 @@
 #include <vector>
 
 #include "../../include/vedo_gpu.h"
+#include "coordination.h"
 #include "engine_base.h"
 
 struct vedo_gpu_engine {
@@ -123,7 +124,8 @@ int vedo_convert_scene(const char* in_path, const char* out_path) {
     }
     if (ends(out, ".ido")) ok = vedo::write_ido(out, s, err);
     else if (ends(out, ".xml")) ok = vedo::write_xml(out, s, err);
-    else { g_create_error = "output must be .ido or .xml"; return VEDO_ERR_INVALID_ARGUMENT; }
+    else if (ends(out, ".vtu")) ok = vedo::write_world_vtk(out, s, s.pos.data(), s.vel.data(), s.av.data(), nullptr, err);
+    else { g_create_error = "output must be .ido, .xml or .vtu"; return VEDO_ERR_INVALID_ARGUMENT; }
     if (!ok) {
         g_create_error = err;
         return VEDO_ERR_IO;
@@ -183,6 +185,17 @@ int vedo_gpu_run_with_impulses(vedo_gpu_engine* e, const double* impulse, const 
 int vedo_gpu_list_status(vedo_gpu_engine* e, double out[6]) {
     if (!e || !out) return VEDO_ERR_INVALID_ARGUMENT;
     return e->p->list_status(out);
+}
+
+int vedo_gpu_coordination(vedo_gpu_engine* e, uint32_t* below, uint32_t* touching, const double* box,
+                          double* average) {
+    if (!e || (average && !box)) return VEDO_ERR_INVALID_ARGUMENT;
+    return e->p->coordination(below, touching, box, average);
+}
+
+int vedo_gpu_write_vtk(vedo_gpu_engine* e, const char* path, int with_coordination) {
+    if (!e || !path) return VEDO_ERR_INVALID_ARGUMENT;
+    return e->p->write_vtk(path, with_coordination);
 }
 
 int vedo_gpu_write_ido(vedo_gpu_engine* e, const char* path) {

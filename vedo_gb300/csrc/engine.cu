@@ -1247,6 +1247,24 @@ int Engine::sync_host_state() {
     return get_state(v);
 }
 
+int Engine::coordination(uint32_t* below, uint32_t* touching, const double* box, double* average) {
+    DeviceObjects d;
+    d.n = n_; d.model_of = d_model_of_; d.models = d_models_; d.pos = d_pos_;
+    d.stream = stream_; d.scratch = &scratch_; d.scene = &host_; d.launches = &launches_;
+    std::string m;
+    const int rc = coordination_host(d, below, touching, box, average, m);
+    return rc == VEDO_OK ? rc : fail(rc, m);
+}
+
+int Engine::write_vtk(const char* path, int with_coordination) {
+    DeviceObjects d;
+    d.n = n_; d.model_of = d_model_of_; d.models = d_models_; d.pos = d_pos_;
+    d.stream = stream_; d.scratch = &scratch_; d.scene = &host_; d.launches = &launches_;
+    std::string m;
+    const int rc = write_vtk_host(this, d, path, with_coordination, m);
+    return rc == VEDO_OK ? rc : fail(rc, m);
+}
+
 int Engine::write_ido(const char* path) {
     int rc = sync_host_state();
     if (rc != VEDO_OK) return rc;

@@ -52,6 +52,8 @@ public:
     int get_interactions(const vedo_contact_view& v) override;
     int get_observables(double out[13]) override;
     int write_ido(const char* path) override;
+    int coordination(uint32_t* below, uint32_t* touching, const double* box, double* average) override;
+    int write_vtk(const char* path, int with_coordination) override;
 
     double time() const override { return t_; }
     uint64_t steps() const override { return round_; }

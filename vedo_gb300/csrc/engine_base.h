@@ -10,6 +10,20 @@
 
 namespace vedo {
 
+struct Scratch;
+
+// The device arrays the observables read, objects in the engine's order (single-scene engines).
+struct DeviceObjects {
+    uint32_t n = 0;
+    const uint32_t* model_of = nullptr;
+    const ModelDev* models = nullptr;
+    const double4_32a* pos = nullptr;
+    cudaStream_t stream = nullptr;
+    Scratch* scratch = nullptr;
+    const HScene* scene = nullptr;       // the models and object order of the scene
+    uint64_t* launches = nullptr;        // the engine's kernel launch counter
+};
+
 class EngineBase {
 public:
     virtual ~EngineBase() = default;
@@ -40,7 +54,15 @@ public:
         for (int k = 0; k < 6; ++k) out[k] = 0.0;
         return VEDO_OK;
     }
+    // CalcCoordinateNum over the current state; the world (and coordination numbers) as VTK
+    virtual int coordination(uint32_t* below, uint32_t* touching, const double* box, double* average) = 0;
+    virtual int write_vtk(const char* path, int with_coordination) = 0;
 };
+
+// Shared implementations of the two observables over an engine's DeviceObjects.
+int coordination_host(const DeviceObjects& d, uint32_t* below, uint32_t* touching, const double* box,
+                      double* average, std::string& err);
+int write_vtk_host(EngineBase* e, const DeviceObjects& d, const char* path, int with_coordination, std::string& err);
 
 // count of t += dt steps from t until t >= t_stop (SystemParameter::NextStep, SimMediator.cpp:839-841)
 inline uint64_t count_steps(double t, double dt, double t_stop) {

@@ -1810,6 +1810,9 @@ public:
     int get_interactions(const vedo_contact_view& v) override;
     int get_observables(double out[13]) override;
     int write_ido(const char* path) override;
+    int coordination(uint32_t* below, uint32_t* touching, const double* box, double* average) override;
+    int write_vtk(const char* path, int with_coordination) override;
+    DeviceObjects objects();
     double time() const override { return sc_.empty() ? 0.0 : sc_[0].t; }
     uint64_t steps() const override { return round_; }
     uint64_t steps_remaining() const override {
@@ -3148,6 +3151,27 @@ int MixedEngine::get_observables(double out[13]) {
     out[11] = msum > 0 ? r[19] / msum : 0.0;
     out[12] = msum > 0 ? r[20] / msum : 0.0;
     return VEDO_OK;
+}
+
+// the observables' view of the state: positions of the current parity, single-scene engines only
+DeviceObjects MixedEngine::objects() {
+    DeviceObjects d;
+    d.n = n_; d.model_of = d_model_of_; d.models = d_models_; d.pos = d_x_[cur_];
+    d.stream = stream_; d.scratch = &scratch_; d.launches = &launches_;
+    d.scene = sc_.size() == 1 ? host_[0].get() : nullptr;
+    return d;
+}
+
+int MixedEngine::coordination(uint32_t* below, uint32_t* touching, const double* box, double* average) {
+    std::string m;
+    const int rc = coordination_host(objects(), below, touching, box, average, m);
+    return rc == VEDO_OK ? rc : fail(rc, m);
+}
+
+int MixedEngine::write_vtk(const char* path, int with_coordination) {
+    std::string m;
+    const int rc = write_vtk_host(this, objects(), path, with_coordination, m);
+    return rc == VEDO_OK ? rc : fail(rc, m);
 }
 
 int MixedEngine::write_ido(const char* path) {

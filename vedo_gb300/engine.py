@@ -58,6 +58,9 @@ def lib() -> C.CDLL:
         L.vedo_gpu_steps_remaining.argtypes = [vp]
         L.vedo_gpu_steps_remaining.restype = C.c_uint64
         L.vedo_gpu_write_ido.argtypes = [vp, C.c_char_p]
+        L.vedo_gpu_coordination.argtypes = [vp, C.POINTER(C.c_uint32), C.POINTER(C.c_uint32), C.POINTER(C.c_double),
+                                            C.POINTER(C.c_double)]
+        L.vedo_gpu_write_vtk.argtypes = [vp, C.c_char_p, C.c_int]
         L.vedo_gpu_last_run_profile.argtypes = [vp, C.POINTER(C.c_double)]
         L.vedo_gpu_last_run_profile.restype = C.c_uint64
         L.vedo_gpu_set_profiling.argtypes = [vp, C.c_int]
@@ -203,6 +206,28 @@ class GpuEngine:
     def write_ido(self, path: str):
         self._check(lib().vedo_gpu_write_ido(self.h, os.fsencode(path)))
 
+    def coordination(self, box=None):
+        """CalcCoordinateNum on the device: (below, touching, average) - per object the other
+        spheres whose centre distance is below / at most the radius sum (0 for walls), and with
+        box = (xmin, xmax, ymin, ymax, zmin, zmax) computeAvgCoordinateNum over it (else None)."""
+        below = np.zeros(self.n, np.uint32)
+        touching = np.zeros(self.n, np.uint32)
+        up = C.POINTER(C.c_uint32)
+        if box is None:
+            self._check(lib().vedo_gpu_coordination(self.h, below.ctypes.data_as(up), touching.ctypes.data_as(up),
+                                                     None, None))
+            return below, touching, None
+        b = np.ascontiguousarray(box, dtype=np.float64)
+        avg = C.c_double(0.0)
+        self._check(lib().vedo_gpu_coordination(self.h, below.ctypes.data_as(up), touching.ctypes.data_as(up),
+                                                 dptr(b), C.byref(avg)))
+        return below, touching, float(avg.value)
+
+    def write_vtk(self, path: str, with_coordination: bool = False):
+        """The current state as a VTK file (DOWorld::WriteVTK), with the spheres' coordination
+        numbers when asked (CalcCoordinateNum::outputCoordinateNumVTK)."""
+        self._check(lib().vedo_gpu_write_vtk(self.h, os.fsencode(path), 1 if with_coordination else 0))
+
     def tuning(self):
         """Skin (fraction of r_max), cell scale and tick block size in use (MIXED form)."""
         sk, cs, tb, ss, st = C.c_float(0), C.c_float(0), C.c_uint32(0), C.c_uint32(0), C.c_uint32(0)
@@ -270,7 +295,8 @@ class GpuEngine:
 
 
 def convert_scene(src: str, dst: str):
-    """Convert a scene file between .ido and DOWorldSchema .xml (by extension); no GPU needed."""
+    """Convert a scene file between .ido and DOWorldSchema .xml, or write it as a VTK .vtu file
+    (by extension); no GPU needed."""
     L = lib()
     rc = L.vedo_convert_scene(os.fsencode(src), os.fsencode(dst))
     if rc != 0:

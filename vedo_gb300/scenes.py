@@ -540,6 +540,42 @@ def periodic_layer(nx: int = 4, ny: int = 4, layers: int = 3, seed: int = 6, ste
     return sc
 
 
+def touching_lattice(seed: int = 13, nx: int = 5, ny: int = 5, nz: int = 3, loose: int = 40) -> Scene:
+    """Spheres at exactly touching distances, for the coordination number: a simple cubic lattice
+    of r = 2^-11 m spheres at spacing 2^-10 m (every axis neighbour at exactly the radius sum),
+    a few of them moved by +-2^-40 m along x (just overlapping or just apart), r = 2^-12 m
+    spheres at exactly the radius sum from a lattice sphere (and overlapping its next neighbour),
+    seeded loose spheres near the lattice, then a floor plate and a rod (walls are not counted).
+    Every lattice coordinate is exact in binary, so the tests meet exact ties."""
+    rng = np.random.default_rng(seed)
+    ra, rb = 2.0 ** -11, 2.0 ** -12
+    sp = 2.0 ** -10
+    i, j, k = np.meshgrid(np.arange(nx), np.arange(ny), np.arange(nz), indexing="ij")
+    A = np.stack([i.ravel(), j.ravel(), k.ravel()], 1).astype(float) * sp
+    move = rng.choice(len(A), size=len(A) // 5, replace=False)
+    A[move, 0] += rng.choice([-1.0, 1.0], size=len(move)) * 2.0 ** -40
+    host = rng.choice(len(A), size=6, replace=False)
+    B = A[host] + np.array([3.0 * 2.0 ** -12, 0.0, 0.0])
+    L = rng.uniform(-0.5 * sp, np.array([nx, ny, nz]) * sp, size=(loose, 3))
+    pos = np.concatenate([A, B, L])
+    midx = np.concatenate([np.zeros(len(A), np.uint32), np.ones(len(B), np.uint32), np.zeros(loose, np.uint32)])
+    n = len(pos)
+    models = [DOModel("BallA", "Ball", MOBILE, LOCAL, 2500.0, 1.0, SPHERE, (ra,)),
+              DOModel("BallB", "Ball", MOBILE, LOCAL, 2500.0, 1.0, SPHERE, (rb,)),
+              DOModel("Floor", "Wall", FIXED, GLOBAL, 0.0, 1.0, QUASI_PLATE, (0.02, 1e-3, 0.02)),
+              DOModel("Rod", "Wall", FIXED, GLOBAL, 0.0, 1.0, QUASI_CYLINDER, (1e-3, 0.01))]
+    P = np.concatenate([pos, [[0.002, 0.002, -ra - 0.5e-3], [0.009, 0.002, 0.002]]])
+    midx = np.concatenate([midx, np.array([2, 3], np.uint32)])
+    V = np.concatenate([rng.normal(0.0, 0.1, size=(n, 3)), np.zeros((2, 3))])
+    AV = np.concatenate([rng.normal(0.0, 5.0, size=(n, 3)), np.zeros((2, 3))])
+    OX = np.tile([1.0, 0.0, 0.0], (n + 2, 1))
+    OZ = np.tile([0.0, 0.0, 1.0], (n + 2, 1))
+    zeta = damping_ratio(0.7)
+    iacts = [IactModel("Ball", "Ball", "ISwBSDBF", lsd_mechanisms(1e4, 8e3, zeta, zeta, 0.5)),
+             IactModel("Wall", "Ball", "ISwBSDBF", lsd_mechanisms(1e4, 8e3, zeta, zeta, 0.5))]
+    return Scene(time_control(100, 1e-6), models, iacts, midx, P, V, OX, OZ, AV)
+
+
 def hopper_params(num_scenes: int = 256, seed: int = 2025, n_lo: int = 1000, n_hi: int = 50000):
     """Per-scene draws of the hopper batch: (n, seed, friction, restitution, orifice)."""
     rng = np.random.default_rng(seed)
