@@ -38,6 +38,8 @@ def cases():
     # in every law's lever arms); ISwH with an orbital floor and side walls that the wrap moves
     yield "periodic_lsd", scenes.periodic_layer(solver="ISwBSDBF"), 400, 5
     yield "periodic_hertz", scenes.periodic_layer(solver="ISwHertz", seed=8), 400, 5
+    yield "periodic_btsdbf", scenes.periodic_layer(solver="ISwBtSDBF", seed=15), 300, 5
+    yield "periodic_bsdb2f", scenes.periodic_layer(solver="ISwBSDB2F", seed=16), 300, 5
     yield "periodic_far_lsd", scenes.periodic_layer(solver="ISwBSDBF", nx=3, ny=3, layers=2, seed=12,
                                                     outside=True), 200, 4
     yield "periodic_h", scenes.periodic_layer(solver="ISwH", periodic_y=False, floor_spin=40.0, side_walls=True,
