@@ -121,8 +121,13 @@ __host__ __device__ __forceinline__ d3 wrap_position(const Periodic& b, d3 p) {
 __device__ __forceinline__ d3 rotate_around(d3 p, d3 va) {
     d3 u = dir(va);
     double a = len(va);
-    double s = cos(0.5 * a);
-    double t = sin(0.5 * a);
+    // cos(0) = 1 and sin(+0) = +0 exactly: a zero turn (an object not spinning) skips the two FP64
+    // transcendental calls, the largest cost of the per-object update on GB300's FP64 pipe
+    double s = 1.0, t = 0.0;
+    if (a != 0.0) {
+        s = cos(0.5 * a);
+        t = sin(0.5 * a);
+    }
     d3 v = muls(u, t);
     d3 r = add(smul(s * s, p), smul(dot(p, v), v));
     r = add(r, smul(2.0 * s, cross(v, p)));

@@ -69,7 +69,7 @@ __global__ void __launch_bounds__(TPB) k_pair(uint32_t np, const uint2* __restri
                                               const float4* __restrict__ pos32, const float4* __restrict__ wall32,
                                               double4_32a* __restrict__ hist, double* __restrict__ v0,
                                               uint8_t* __restrict__ flags, double* __restrict__ out, double dt,
-                                              int backup, Periodic pb) {
+                                              int backup, Periodic pb, uint8_t* __restrict__ touched) {
     const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
     if (k >= np) return;
     const uint2 p = sm[k];
@@ -139,6 +139,8 @@ __global__ void __launch_bounds__(TPB) k_pair(uint32_t np, const uint2* __restri
         o[0] = J.x; o[1] = J.y; o[2] = J.z;
         o[3] = tA.x; o[4] = tA.y; o[5] = tA.z;
         o[6] = tB.x; o[7] = tB.y; o[8] = tB.z;
+        touched[p.x] = 1;              // both objects have an impulse to gather this step
+        touched[p.y] = 1;
     }
 }
 
@@ -218,16 +220,21 @@ __global__ void __launch_bounds__(TPB) k_obj(uint32_t n, const uint32_t* __restr
                                              const uint8_t* __restrict__ flags, const double* __restrict__ out,
                                              double dt, d3 fimp, int write_imp, d3 origin, float4* __restrict__ pos32,
                                              float4* __restrict__ wall32, const double* __restrict__ ext_imp,
-                                             const double* __restrict__ ext_aimp, Periodic pb) {
+                                             const double* __restrict__ ext_aimp, Periodic pb,
+                                             uint8_t* __restrict__ touched) {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     const ModelDev& m = models[model_of[i]];
     if (m.scope == SCOPE_GLOBAL) return;
     d3 J = mk(0.0, 0.0, 0.0), JA = mk(0.0, 0.0, 0.0);
-    const uint32_t e1 = csr_ptr[i + 1];
-    for (uint32_t e = csr_ptr[i]; e < e1; ++e) {
-        const uint32_t ent = csr_ent[e];
-        add_entry(ent, flags[ent >> 1], out, J, JA);
+    // an object no pair applied an impulse to keeps zero sums: its ordered walk adds nothing
+    if (touched[i]) {
+        touched[i] = 0;
+        const uint32_t e1 = csr_ptr[i + 1];
+        for (uint32_t e = csr_ptr[i]; e < e1; ++e) {
+            const uint32_t ent = csr_ent[e];
+            add_entry(ent, flags[ent >> 1], out, J, JA);
+        }
     }
     finish_object(i, m, J, JA, dt, fimp, pos, vel, av, ox, oz, imp, aimp, write_imp, origin, pos32, wall32, ext_imp,
                   ext_aimp, pb);
@@ -242,11 +249,13 @@ __global__ void k_obj_global(uint32_t nglob, const uint32_t* __restrict__ glob, 
                              const uint32_t* __restrict__ csr_ptr, const uint32_t* __restrict__ csr_ent,
                              const uint8_t* __restrict__ flags, const double* __restrict__ out, double dt, d3 fimp,
                              int write_imp, d3 origin, float4* __restrict__ pos32, float4* __restrict__ wall32,
-                             const double* __restrict__ ext_imp, const double* __restrict__ ext_aimp, Periodic pb) {
+                             const double* __restrict__ ext_imp, const double* __restrict__ ext_aimp, Periodic pb,
+                             uint8_t* __restrict__ touched) {
     const uint32_t w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const int lane = threadIdx.x & 31;
     if (w >= nglob) return;
     const uint32_t i = glob[w];
+    if (lane == 0 && touched[i]) touched[i] = 0;
     const ModelDev& m = models[model_of[i]];
     d3 J = mk(0.0, 0.0, 0.0), JA = mk(0.0, 0.0, 0.0);
     const bool need_sum = write_imp || m.behavior == BEH_MOBILE || m.behavior == BEH_CONSTRAINED || ext_imp;
@@ -725,7 +734,7 @@ Engine::~Engine() {
                     d_oz_, d_imp_, d_aimp_, d_global_, d_safe_, d_red_, d_key_, d_key_alt_, d_cell_key_, d_sid_,
                     d_sid_alt_, d_cell_start_, d_cellof_, d_flag_, d_task_, d_total_, d_ck_, d_cv_, d_ck_alt_,
                     d_cv_alt_, d_cnt_, d_rec_key_, d_rec_hist_, d_rec_v0_, d_rec_flags_, d_obs_, d_stage_,
-                    d_pos32_, d_wall32_, d_reach_, d_grid_, d_ext_, d_hole_};
+                    d_pos32_, d_wall32_, d_reach_, d_grid_, d_ext_, d_hole_, d_touched_};
     for (void* p : ptrs) if (p) cudaFree(p);
     for (auto& e : ev_) if (e) cudaEventDestroy(e);
     if (stream_) cudaStreamDestroy(stream_);
@@ -798,6 +807,8 @@ int Engine::init(const HScene& scene, const vedo_engine_opts& opts) {
         for (int k = 0; k < 3; ++k) origin_[k] = 0.5 * (lo[k] + hi[k]);
         CK(dalloc(&d_pos32_, n_));
         CK(dalloc(&d_wall32_, n_));
+        CK(dalloc(&d_touched_, n_));
+        CK(cudaMemset(d_touched_, 0, n_));
         CK(cudaMemset(d_wall32_, 0, sizeof(float4) * n_));
         std::vector<float> reach((size_t)nm_ * nm_, 0.0f);
         for (size_t q = 0; q < reach.size(); ++q) {
@@ -1015,7 +1026,7 @@ int Engine::step_once(bool write_impulses) {
                                                          d_reach_,
                                                          d_pos_, d_vel_, d_av_, d_ox_, d_oz_, d_pos32_, d_wall32_,
                                                          cur_.hist, cur_.v0, cur_.flags, cur_.out, dt,
-                                                         backup_pending_ ? 1 : 0, tab_.pbc);
+                                                         backup_pending_ ? 1 : 0, tab_.pbc, d_touched_);
         ++launches_;
     }
     if (prof) CK(cudaEventRecord(ev_[1], stream_));
@@ -1025,13 +1036,13 @@ int Engine::step_once(bool write_impulses) {
     k_obj<<<blocks_for(n_), TPB, 0, stream_>>>(n_, d_model_of_, d_models_, d_pos_, d_vel_, d_av_, d_ox_, d_oz_,
                                                d_imp_, d_aimp_, cur_.csr_ptr, cur_.csr_ent, cur_.flags, cur_.out, dt,
                                                fimp, write_impulses ? 1 : 0, org, d_pos32_, d_wall32_, ext_imp_, ext_aimp_,
-                                               tab_.pbc);
+                                               tab_.pbc, d_touched_);
     ++launches_;
     if (!global_ids_.empty()) {
         k_obj_global<<<blocks_for((uint64_t)global_ids_.size() * 32), TPB, 0, stream_>>>(
             (uint32_t)global_ids_.size(), d_global_, d_model_of_, d_models_, d_pos_, d_vel_, d_av_, d_ox_, d_oz_,
             d_imp_, d_aimp_, cur_.csr_ptr, cur_.csr_ent, cur_.flags, cur_.out, dt, fimp, write_impulses ? 1 : 0, org,
-            d_pos32_, d_wall32_, ext_imp_, ext_aimp_, tab_.pbc);
+            d_pos32_, d_wall32_, ext_imp_, ext_aimp_, tab_.pbc, d_touched_);
         ++launches_;
     }
     if (prof) CK(cudaEventRecord(ev_[2], stream_));

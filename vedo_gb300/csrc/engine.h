@@ -126,6 +126,8 @@ private:
     // FP32 prefilter copies (prefilter.cuh): position offsets from origin_, unit wall axes,
     // and per (slave model, master model) the contact reach rounded up to float
     float4* d_pos32_ = nullptr;
+    // per object: 1 when a pair of this step applied an impulse to it (k_pair sets, k_obj clears)
+    uint8_t* d_touched_ = nullptr;
     float4* d_wall32_ = nullptr;
     float* d_reach_ = nullptr;
     double origin_[3] = {0, 0, 0};
