@@ -520,7 +520,11 @@ __global__ void __launch_bounds__(TPB) k_pairs(uint32_t nloc, const uint32_t* __
     const int gi = mi.group;
     uint32_t cnt = 0;
     const uint32_t off = FILL ? task[tid] : 0u;
-    for (uint32_t q = 0; q < jn; ++q) {
+    // the fill pass knows each task's count from the scanned offsets (the next task's offset, or
+    // the total after the last one): it stops at its last candidate and skips empty tasks
+    uint32_t want = 0xffffffffu;
+    if (FILL) want = ((uint64_t)tid + 1 < (uint64_t)nloc * NSLOT ? task[tid + 1] : ncells_p[1]) - off;
+    for (uint32_t q = 0; q < jn && cnt < want; ++q) {
         const uint32_t j = js[q];
         const ModelDev& mj = models[model_of[j]];
         if (group_iact[gi * G + mj.group] < 0) continue;
