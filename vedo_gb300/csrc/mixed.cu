@@ -1142,15 +1142,18 @@ __global__ void __launch_bounds__(TPB) k_nbr(uint32_t nloc, const uint32_t* __re
     const float4 pi = pos32[i];
     uint32_t c = 0;
     uint32_t off = FILL ? cnt_or_ptr[i] : 0u;
-    for (int dx = -1; dx <= 1; ++dx) {
+    // the fill pass knows the sphere's count from the scanned pointers: it stops once every entry
+    // is found (the entries are put in canonical order below, whatever order they were found in)
+    const uint32_t want = FILL ? cnt_or_ptr[i + 1] - off : 0xffffffffu;
+    for (int dx = -1; dx <= 1 && c < want; ++dx) {
         if ((dx < 0 && cx == 0) || (dx > 0 && cx + 1 >= nx)) continue;
-        for (int dy = -1; dy <= 1; ++dy) {
+        for (int dy = -1; dy <= 1 && c < want; ++dy) {
             if ((dy < 0 && cy == 0) || (dy > 0 && cy + 1 >= ny)) continue;
-            for (int dz = -1; dz <= 1; ++dz) {
+            for (int dz = -1; dz <= 1 && c < want; ++dz) {
                 if ((dz < 0 && cz == 0) || (dz > 0 && cz + 1 >= nz)) continue;
                 const uint64_t nk = S.cell_base + ((uint64_t)(cx + dx) * ny + (cy + dy)) * nz + (cz + dz);
                 const uint32_t b = grid_start[nk], e = grid_end[nk];
-                for (uint32_t q = b; q < e; ++q) {
+                for (uint32_t q = b; q < e && c < want; ++q) {
                     const uint32_t j = sid[q];
                     if (j == i) continue;
                     const uint32_t mj = model_of[j];
@@ -1166,7 +1169,7 @@ __global__ void __launch_bounds__(TPB) k_nbr(uint32_t nloc, const uint32_t* __re
             }
         }
     }
-    for (uint32_t q = S.wall_beg; q < S.wall_end; ++q) {
+    for (uint32_t q = S.wall_beg; q < S.wall_end && c < want; ++q) {
         const uint32_t w = glob[q];
         const uint32_t pw = pidx(S, mi, model_of[w]);
         const int cd = cd_plane(params[pw].cd);
