@@ -204,6 +204,9 @@ int vedo_convert_scene(const char* in_path, const char* out_path);
  * *keep_running (may be NULL) receives the last step's return value,
  * t_current < t_stop (SimMediator.cpp:839-841). */
 int vedo_gpu_run(vedo_gpu_engine* e, uint32_t nsteps, int* keep_running);
+/* The same under the name of the step contract: `while (sm.Run())` of Anne.cpp:128 becomes
+ * `do vedo_gpu_step(e, k, &keep); while (keep);`. */
+int vedo_gpu_step(vedo_gpu_engine* e, uint32_t nsteps, int* keep_running);
 
 /* Object state, [n][3] doubles per array; any pointer may be NULL.  impact /
  * angular_impact are the impulses the last Response consumed, as DOStatus
@@ -241,6 +244,9 @@ typedef struct vedo_contact_view {
 
 int vedo_gpu_num_interactions(vedo_gpu_engine* e, uint32_t* n);
 int vedo_gpu_get_interactions(vedo_gpu_engine* e, const vedo_contact_view* out);
+/* The same under the name of the contacts contract: pairs (first < second), active flag, shear
+ * and kn of every interaction, vedo_gpu_num_interactions long. */
+int vedo_gpu_get_contacts(vedo_gpu_engine* e, const vedo_contact_view* out);
 
 /* System observables as DOWorld::CalculateSystemEnergy computes them
  * (DOWorld.cpp:481-660) over the current state, mobile objects only:

@@ -296,3 +296,37 @@ def test_periodic_boundary_is_rejected_by_the_mixed_form(engine_lib):
     with pytest.raises(engine_lib.EngineError) as ex:
         engine_lib.BatchEngine([sc])
     assert ex.value.code == 3
+
+
+def test_step_and_contacts_entry_points_equal_run_and_interactions(engine_lib):
+    """vedo_gpu_step / vedo_gpu_get_contacts (the names of the step and contacts contract) do what
+    vedo_gpu_run / vedo_gpu_get_interactions do."""
+    import ctypes as C
+    from vedo_gb300.engine import lib
+    L = lib()
+    L.vedo_gpu_step.argtypes = [C.c_void_p, C.c_uint32, C.POINTER(C.c_int)]
+    L.vedo_gpu_get_contacts.argtypes = [C.c_void_p, C.POINTER(engine_lib.ContactView)]
+    sc = scenes.cluster(n=48, solver="ISwBSDBF", steps=400, seed=5)
+    a, b = engine_lib.GpuEngine(sc, up_iact=5), engine_lib.GpuEngine(sc, up_iact=5)
+    keep = C.c_int(0)
+    assert L.vedo_gpu_step(a.h, 150, C.byref(keep)) == 0 and keep.value == 1
+    b.run(150)
+    for k, v in a.state().items():
+        np.testing.assert_array_equal(v, b.state()[k], err_msg=k)
+    ib = b.interactions()
+    m = len(ib["first"])
+    first, second = np.zeros(m, np.uint32), np.zeros(m, np.uint32)
+    active = np.zeros(m, np.uint8)
+    shear = np.zeros((m, 3))
+    view = engine_lib.ContactView()
+    view.first = first.ctypes.data_as(C.POINTER(C.c_uint32))
+    view.second = second.ctypes.data_as(C.POINTER(C.c_uint32))
+    view.active = active.ctypes.data_as(C.POINTER(C.c_uint8))
+    view.shear = shear.ctypes.data_as(C.POINTER(C.c_double))
+    assert L.vedo_gpu_get_contacts(a.h, C.byref(view)) == 0
+    np.testing.assert_array_equal(first, ib["first"])
+    np.testing.assert_array_equal(second, ib["second"])
+    np.testing.assert_array_equal(active.astype(bool), ib["active"].astype(bool))
+    np.testing.assert_array_equal(shear, ib["shear"])
+    a.close()
+    b.close()

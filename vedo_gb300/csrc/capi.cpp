@@ -138,6 +138,8 @@ int vedo_gpu_run(vedo_gpu_engine* e, uint32_t nsteps, int* keep_running) {
     return e->p->run(nsteps, keep_running);
 }
 
+int vedo_gpu_step(vedo_gpu_engine* e, uint32_t nsteps, int* keep_running) { return vedo_gpu_run(e, nsteps, keep_running); }
+
 uint32_t vedo_gpu_num_objects(const vedo_gpu_engine* e) { return e ? e->p->num_objects() : 0u; }
 
 int vedo_gpu_get_state(vedo_gpu_engine* e, const vedo_state_view* out) {
@@ -159,6 +161,8 @@ int vedo_gpu_get_interactions(vedo_gpu_engine* e, const vedo_contact_view* out) 
     if (!e || !out) return VEDO_ERR_INVALID_ARGUMENT;
     return e->p->get_interactions(*out);
 }
+
+int vedo_gpu_get_contacts(vedo_gpu_engine* e, const vedo_contact_view* out) { return vedo_gpu_get_interactions(e, out); }
 
 int vedo_gpu_get_observables(vedo_gpu_engine* e, double out[13]) {
     if (!e || !out) return VEDO_ERR_INVALID_ARGUMENT;
