@@ -105,6 +105,7 @@ struct dp_world {
     v3 g;
     double sf;
     unsigned up_iact;
+    int leap;                          /* 1: LeapConsultant's candidate list, 0: NBSConsultant's */
     unsigned long long round;
     /* periodic boundary after Boundary::Correct: switched axes, bounds, ranges */
     int pbc_on, pbc_sw[3];
@@ -297,8 +298,9 @@ static int eq_of(const char* s) {                  /* IScf<IS>("name"), ModuleLi
 }
 
 /* ------------------------------------------------------------------------ */
-/* DOMap::CalDistance (vedo/framework/DOMap.cpp:142-414), no periodic boundary */
-static int cal_distance(const dp_world* w, unsigned i, unsigned j, double* out) {
+/* DOMap::CalDistance (vedo/framework/DOMap.cpp:142-414).  With `periodic` (the Leap consultant
+   passes the boundary) the difference vector takes the minimum image before its length. */
+static int cal_distance_pbc(const dp_world* w, unsigned i, unsigned j, int periodic, double* out) {
     const model_t* mi = &w->models[w->model_of[i]];
     const model_t* mj = &w->models[w->model_of[j]];
     if (mi->shape > mj->shape) {                    /* :144-147 swap */
@@ -307,7 +309,9 @@ static int cal_distance(const dp_world* w, unsigned i, unsigned j, double* out) 
     }
     v3 pi = ld3(w->pos + 3 * i), pj = ld3(w->pos + 3 * j);
     if (mi->shape == VEDO_SHAPE_SPHERE && mj->shape == VEDO_SHAPE_SPHERE) {          /* :149-157 */
-        *out = len(sub(pi, pj));
+        v3 Im = sub(pi, pj);
+        if (periodic) Im = min_image(w, Im);
+        *out = len(Im);
         return 0;
     }
     if (mi->shape == VEDO_SHAPE_SPHERE && (mj->shape == VEDO_SHAPE_QUASI_PLATE ||
@@ -322,7 +326,9 @@ static int cal_distance(const dp_world* w, unsigned i, unsigned j, double* out) 
         double dy = dot(sub(Cap, Cb), Oy);
         if (dy < -hl) dy = -hl; else if (dy > hl) dy = hl;
         v3 Caps = add(add(muls(Ox, dx), muls(Oy, dy)), Cb);
-        *out = len(sub(Caps, Ca));
+        v3 Im = sub(Caps, Ca);
+        if (periodic) Im = min_image(w, Im);
+        *out = len(Im);
         return 0;
     }
     if (mi->shape == VEDO_SHAPE_SPHERE && mj->shape == VEDO_SHAPE_QUASI_CYLINDER) {  /* :378-408 */
@@ -334,10 +340,15 @@ static int cal_distance(const dp_world* w, unsigned i, unsigned j, double* out) 
         if ((dap < hh) && (dap > -hh)) Im = sub(Cap, Ca);
         else if (dap >= hh) Im = sub(add(Cb, muls(ax, hh)), Ca);
         else Im = sub(sub(Cb, muls(ax, hh)), Ca);
+        if (periodic) Im = min_image(w, Im);
         *out = len(Im);
         return 0;
     }
     return -1;                                       /* :410-413 exit(-1) in the reference */
+}
+
+static int cal_distance(const dp_world* w, unsigned i, unsigned j, double* out) {
+    return cal_distance_pbc(w, i, j, 0, out);
 }
 
 /* ------------------------------------------------------------------------ */
@@ -368,20 +379,25 @@ static int push_cand(dp_world* w, unsigned a, unsigned b) {
     return 0;
 }
 
-static int build_tab(dp_world* w, const unsigned* v1, unsigned n1, const unsigned* v2, unsigned n2,
-                     int self, const double* safe) {                       /* :318-374 */
+static int build_tab_pbc(dp_world* w, const unsigned* v1, unsigned n1, const unsigned* v2, unsigned n2,
+                         int self, const double* safe, int periodic) {     /* :318-374 */
     for (unsigned i = 0; i < n1; ++i) {
         for (unsigned j = self ? i + 1 : 0; j < n2; ++j) {
             unsigned a = v1[i], b = v2[j];
             int ga = w->models[w->model_of[a]].group, gb = w->models[w->model_of[b]].group;
             if (w->group_iact[ga * w->ngroups + gb] < 0) continue;
             double d;
-            if (cal_distance(w, a, b, &d) != 0) return -2;
+            if (cal_distance_pbc(w, a, b, periodic, &d) != 0) return -2;
             if (d > (safe[a] + safe[b])) continue;
             if (push_cand(w, a, b) != 0) return -1;
         }
     }
     return 0;
+}
+
+static int build_tab(dp_world* w, const unsigned* v1, unsigned n1, const unsigned* v2, unsigned n2,
+                     int self, const double* safe) {
+    return build_tab_pbc(w, v1, n1, v2, n2, self, safe, 0);
 }
 
 static unsigned lookup_cell(const cellent_t* ents, const unsigned* starts, unsigned ncells, unsigned cx,
@@ -479,6 +495,171 @@ static int nbs_reset(dp_world* w) {
     free(safe); free(glob); free(ents); free(ids); free(starts);
     return rc;
 }
+
+/* ------------------------------------------------------------------------ */
+/* LeapConsultant::Reset + subReset (vedo/common/LeapConsultant.cpp:108-195, LeapConsultant.h:58-446).
+   The cell edge comes from the largest range and speed of the local objects; cells are visited
+   in the order of a comparator whose first key is the axis with the largest 2 %-98 % spread of
+   the local positions (TrirLeX/Y/Z, NBSConsultant.h:62-128); per cell the 13 half-shell
+   neighbours (each, when absent, replaced by its periodic image under the rule of
+   LeapConsultant.h:195-446), then the cell itself, then the scope-global objects; the candidate
+   distance takes the boundary's minimum image. */
+static int dcmp(const void* a, const void* b) {
+    double x = *(const double*)a, y = *(const double*)b;
+    return x < y ? -1 : (x > y ? 1 : 0);
+}
+
+static int g_leap_mode;                              /* comparator for qsort: 0 X, 1 Y, 2 Z */
+static void leap_keys(const cellent_t* e, unsigned k[3]) {
+    if (g_leap_mode == 0) { k[0] = e->cx; k[1] = e->cy; k[2] = e->cz; }       /* TrirLeX */
+    else if (g_leap_mode == 1) { k[0] = e->cy; k[1] = e->cx; k[2] = e->cz; }  /* TrirLeY */
+    else { k[0] = e->cz; k[1] = e->cx; k[2] = e->cy; }                         /* TrirLeZ */
+}
+static int leap_cmp(const void* a, const void* b) {
+    unsigned ka[3], kb[3];
+    leap_keys((const cellent_t*)a, ka);
+    leap_keys((const cellent_t*)b, kb);
+    for (int q = 0; q < 3; ++q)
+        if (ka[q] != kb[q]) return ka[q] < kb[q] ? -1 : 1;
+    unsigned ia = ((const cellent_t*)a)->id, ib = ((const cellent_t*)b)->id;   /* insertion order */
+    return ia < ib ? -1 : (ia > ib ? 1 : 0);
+}
+static unsigned leap_lookup(const cellent_t* ents, const unsigned* starts, unsigned ncells, unsigned cx, unsigned cy,
+                            unsigned cz, unsigned* cnt) {
+    cellent_t probe;
+    probe.cx = cx; probe.cy = cy; probe.cz = cz; probe.id = 0;
+    unsigned kp[3];
+    leap_keys(&probe, kp);
+    unsigned lo = 0, hi = ncells;
+    while (lo < hi) {
+        unsigned mid = (lo + hi) / 2;
+        unsigned km[3];
+        leap_keys(&ents[starts[mid]], km);
+        int c = 0;
+        for (int q = 0; q < 3 && c == 0; ++q)
+            if (km[q] != kp[q]) c = km[q] < kp[q] ? -1 : 1;
+        if (c == 0) { *cnt = starts[mid + 1] - starts[mid]; return starts[mid]; }
+        if (c < 0) lo = mid + 1; else hi = mid;
+    }
+    *cnt = 0;
+    return 0;
+}
+
+static int leap_reset(dp_world* w) {
+    unsigned n = w->n;
+    unsigned nl = 0;
+    for (unsigned u = 0; u < n; ++u) nl += w->models[w->model_of[u]].scope == VEDO_SCOPE_LOCAL;
+    if (nl == 0) return -3;                          /* the reference indexes an empty vector */
+    double* sx = (double*)malloc(sizeof(double) * nl * 5);
+    double* safe = (double*)malloc(sizeof(double) * (n ? n : 1));
+    unsigned* glob = (unsigned*)malloc(sizeof(unsigned) * (n ? n : 1));
+    cellent_t* ents = (cellent_t*)malloc(sizeof(cellent_t) * nl);
+    unsigned* ids = (unsigned*)malloc(sizeof(unsigned) * nl);
+    unsigned* starts = (unsigned*)malloc(sizeof(unsigned) * (nl + 1));
+    if (!sx || !safe || !glob || !ents || !ids || !starts) return -1;
+    double *sy = sx + nl, *sz = sx + 2 * nl, *sv = sx + 3 * nl, *sr = sx + 4 * nl;
+    unsigned k = 0;
+    for (unsigned u = 0; u < n; ++u) {                                       /* LeapConsultant.cpp:122-136 */
+        const model_t* m = &w->models[w->model_of[u]];
+        if (m->scope != VEDO_SCOPE_LOCAL) continue;
+        sx[k] = w->pos[3 * u]; sy[k] = w->pos[3 * u + 1]; sz[k] = w->pos[3 * u + 2];
+        sv[k] = len(ld3(w->vel + 3 * u)); sr[k] = m->range;
+        ++k;
+    }
+    qsort(sx, nl, sizeof(double), dcmp); qsort(sy, nl, sizeof(double), dcmp); qsort(sz, nl, sizeof(double), dcmp);
+    qsort(sv, nl, sizeof(double), dcmp); qsort(sr, nl, sizeof(double), dcmp);
+    const double xmin = sx[0], xmax = sx[nl - 1], ymin = sy[0], ymax = sy[nl - 1], zmin = sz[0], zmax = sz[nl - 1];
+    const double vmax = sv[nl - 1], rmax = sr[nl - 1];
+    const double discard = 0.02, keep = 1.0 - discard;                        /* :164-168 */
+    const double hi_d = keep * nl - 1, lo_d = discard * nl;
+    const size_t ih = hi_d < 0.0 ? 0 : (size_t)hi_d, il = (size_t)lo_d;
+    const double xs = sx[ih] - sx[il], ys = sy[ih] - sy[il], zs = sz[ih] - sz[il];
+    g_leap_mode = xs >= ys ? (xs >= zs ? 0 : 2) : (ys >= zs ? 1 : 2);         /* :170-193 */
+    double dtu = (double)w->up_iact * w->dt;                                  /* LeapConsultant.h:73 */
+    double glen = len(w->g);
+    for (unsigned u = 0; u < n; ++u) {                                        /* :116-136 */
+        const model_t* m = &w->models[w->model_of[u]];
+        safe[u] = w->sf * (2.0 * m->range + dtu * len(ld3(w->vel + 3 * u)) + 0.5 * dtu * dtu * glen);
+    }
+    double zone = w->sf * (2.0 * rmax + dtu * vmax + 0.5 * dtu * dtu * glen); /* :138 */
+    unsigned ncx = (unsigned)ceil((xmax - xmin) / zone); if (ncx < 1) ncx = 1;
+    unsigned ncy = (unsigned)ceil((ymax - ymin) / zone); if (ncy < 1) ncy = 1;
+    unsigned ncz = (unsigned)ceil((zmax - zmin) / zone); if (ncz < 1) ncz = 1;
+    const int px = w->pbc_sw[0] && (xmax - xmin) >= 0.5 * w->pbc_r[0];      /* :146-150 */
+    const int py = w->pbc_sw[1] && (ymax - ymin) >= 0.5 * w->pbc_r[1];
+    const int pz = w->pbc_sw[2] && (zmax - zmin) >= 0.5 * w->pbc_r[2];
+    const int has_pbc = px || py || pz;
+    const unsigned mx[3] = {ncx - 1, ncy - 1, ncz - 1};
+    const int pa[3] = {px, py, pz};
+    unsigned nloc = 0, nglob = 0;
+    for (unsigned u = 0; u < n; ++u) {                                        /* :160-179 */
+        const model_t* m = &w->models[w->model_of[u]];
+        if (m->scope == VEDO_SCOPE_LOCAL) {
+            const double* p = w->pos + 3 * u;
+            cellent_t e;
+            e.cx = (unsigned)((p[0] - xmin) / zone);
+            e.cy = (unsigned)((p[1] - ymin) / zone);
+            e.cz = (unsigned)((p[2] - zmin) / zone);
+            e.id = u;
+            ents[nloc++] = e;
+        } else {
+            glob[nglob++] = u;
+        }
+    }
+    qsort(ents, nloc, sizeof(cellent_t), leap_cmp);
+    unsigned ncells = 0;
+    for (unsigned q = 0; q < nloc; ++q) {
+        ids[q] = ents[q].id;
+        if (q == 0 || ents[q].cx != ents[q - 1].cx || ents[q].cy != ents[q - 1].cy || ents[q].cz != ents[q - 1].cz)
+            starts[ncells++] = q;
+    }
+    starts[ncells] = nloc;
+    w->ncand = 0;
+    static const int OFF[13][3] = {                                           /* :195-440 */
+        {-1, -1, -1}, {-1, -1, 0}, {-1, -1, 1}, {0, -1, -1}, {0, -1, 0}, {0, -1, 1}, {1, -1, -1}, {1, -1, 0},
+        {1, -1, 1}, {-1, 0, -1}, {-1, 0, 0}, {0, 0, -1}, {1, 0, -1}};
+    int rc = 0;
+    for (unsigned c = 0; c < ncells && rc == 0; ++c) {
+        const cellent_t* e = &ents[starts[c]];
+        const unsigned ic[3] = {e->cx, e->cy, e->cz};
+        const unsigned* v1 = ids + starts[c];
+        unsigned n1 = starts[c + 1] - starts[c];
+        for (int s = 0; s < 13 && rc == 0; ++s) {
+            unsigned nb[3];
+            for (int a = 0; a < 3; ++a) nb[a] = ic[a] + (unsigned)OFF[s][a];   /* unsigned, as _uint_t */
+            unsigned cnt, st = leap_lookup(ents, starts, ncells, nb[0], nb[1], nb[2], &cnt);
+            if (cnt) { rc = build_tab_pbc(w, v1, n1, ids + st, cnt, 0, safe, w->pbc_on); continue; }
+            if (!has_pbc) continue;
+            /* the periodic image: on an axis stepping down from zone 0 (up from the last zone)
+               the neighbour wraps when that axis is periodic; a wrapped id that names the
+               opposite neighbour is skipped (:199-216 and the twelve branches that follow) */
+            int at_edge = 0, dup = 0;
+            unsigned wi[3];
+            for (int a = 0; a < 3; ++a) {
+                if (OFF[s][a] < 0) {
+                    at_edge |= ic[a] == 0;
+                    wi[a] = pa[a] ? mx[a] : ic[a] - 1u;
+                    dup |= wi[a] == ic[a] + 1u;
+                } else if (OFF[s][a] > 0) {
+                    at_edge |= ic[a] == mx[a];
+                    wi[a] = pa[a] ? 0u : ic[a] + 1u;
+                    dup |= wi[a] == ic[a] - 1u;
+                } else {
+                    wi[a] = ic[a];
+                }
+            }
+            if (!at_edge || dup) continue;
+            st = leap_lookup(ents, starts, ncells, wi[0], wi[1], wi[2], &cnt);
+            if (cnt) rc = build_tab_pbc(w, v1, n1, ids + st, cnt, 0, safe, w->pbc_on);
+        }
+        if (rc == 0) rc = build_tab_pbc(w, v1, n1, v1, n1, 1, safe, w->pbc_on);          /* :442-443 */
+        if (rc == 0) rc = build_tab_pbc(w, v1, n1, glob, nglob, 0, safe, w->pbc_on);     /* :445-446 */
+    }
+    free(sx); free(safe); free(glob); free(ents); free(ids); free(starts);
+    return rc;
+}
+
+static int consultant_reset(dp_world* w) { return w->leap ? leap_reset(w) : nbs_reset(w); }
 
 /* ------------------------------------------------------------------------ */
 /* Assembler::CreateInteraction (vedo/framework/Assembler.cpp:15-87) with the
@@ -935,9 +1116,15 @@ static int rebuild_records(dp_world* w) {
 }
 
 /* ------------------------------------------------------------------------ */
-dp_world* dp_create(const vedo_scene_desc* sc, unsigned up_iact, char* err, size_t errlen) {
+dp_world* dp_create(const vedo_scene_desc* sc, unsigned up_iact, int consultant, char* err, size_t errlen) {
     if (!sc || !sc->num_objects) { set_err(err, errlen, "empty scene"); return NULL; }
+    if (consultant == 1 && (sc->zoi_lower[0] != sc->zoi_upper[0] || sc->zoi_lower[1] != sc->zoi_upper[1] ||
+                            sc->zoi_lower[2] != sc->zoi_upper[2])) {
+        /* LeapConsultant::NextStep erases objects outside the zone at every reset (:67) */
+        set_err(err, errlen, "a zone of interest with the Leap consultant is not supported"); return NULL;
+    }
     dp_world* w = (dp_world*)calloc(1, sizeof(dp_world));
+    w->leap = consultant == 1;
     /* Boundary::Correct (Boundary.cpp:79-128): an axis is on where its bounds differ */
     for (int k = 0; k < 3; ++k) {
         const double a = sc->pbc_lower[k], b = sc->pbc_upper[k];
@@ -1036,10 +1223,11 @@ dp_world* dp_create(const vedo_scene_desc* sc, unsigned up_iact, char* err, size
     }
     sort_records(w->rec, &w->nrec);
     zoi_cleanup(w, sc);
-    int rc = nbs_reset(w);
+    int rc = consultant_reset(w);
     if (rc == 0) rc = initiate(w);
     if (rc != 0) {
-        set_err(err, errlen, rc == -2 ? "unsupported interaction in candidate list" : "allocation failed");
+        set_err(err, errlen, rc == -2 ? "unsupported interaction in candidate list"
+                             : rc == -3 ? "the Leap consultant needs a local object" : "allocation failed");
         dp_destroy(w);
         return NULL;
     }
@@ -1067,7 +1255,7 @@ int dp_run(dp_world* w, unsigned nsteps) {
         int reset = (w->round % w->up_iact) == 0;
         if (reset) {
             rebuild_records(w);
-            nbs_reset(w);
+            consultant_reset(w);
         }
         for (unsigned k = 0; k < w->ncand && !reset; ++k) {                   /* BackupImpactStatus */
             w->it[k].st.last_contact = w->it[k].st.contact;

@@ -20,7 +20,8 @@ typedef struct dp_world dp_world;
 
 /* Build the world: NBS candidate list, SimMediator::Initiate, IDO history
  * re-attach.  Returns NULL and fills err on an unsupported/invalid scene. */
-dp_world* dp_create(const vedo_scene_desc* scene, unsigned up_iact, char* err, size_t errlen);
+/* consultant: 0 NBSConsultant, 1 LeapConsultant (the candidate list each builds) */
+dp_world* dp_create(const vedo_scene_desc* scene, unsigned up_iact, int consultant, char* err, size_t errlen);
 /* nsteps SimMediator::Run() calls; returns the last t_current < t_stop. */
 int dp_run(dp_world* w, unsigned nsteps);
 unsigned dp_num_objects(const dp_world* w);

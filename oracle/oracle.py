@@ -73,7 +73,7 @@ class PortWorld(_World):
                 build_port()
             L = C.CDLL(PORT_LIB)
             L.dp_create.restype = C.c_void_p
-            L.dp_create.argtypes = [C.c_void_p, C.c_uint, C.c_char_p, C.c_size_t]
+            L.dp_create.argtypes = [C.c_void_p, C.c_uint, C.c_int, C.c_char_p, C.c_size_t]
             L.dp_run.argtypes = [C.c_void_p, C.c_uint]
             L.dp_num_objects.argtypes = [C.c_void_p]
             L.dp_num_objects.restype = C.c_uint
@@ -92,12 +92,12 @@ class PortWorld(_World):
             cls._lib = L
         return cls._lib
 
-    def __init__(self, scene, up_iact: int = 1):
+    def __init__(self, scene, up_iact: int = 1, consultant: str = "nbs"):
         from vedo_gb300._abi import scene_to_desc
         L = self.lib()
         desc, keep = scene_to_desc(scene)
         err = C.create_string_buffer(256)
-        self.h = L.dp_create(C.byref(desc), up_iact, err, 256)
+        self.h = L.dp_create(C.byref(desc), up_iact, 1 if consultant == "leap" else 0, err, 256)
         if not self.h:
             raise ValueError("oracle rejected the scene: " + err.value.decode())
         self.n = L.dp_num_objects(self.h)
