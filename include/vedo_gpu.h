@@ -169,7 +169,11 @@ typedef struct vedo_engine_opts {
                                  step; 0 = a sphere whose pairs are all certainly apart since
                                  the rebuild, with clean history, skips the walk (default;
                                  identical results)                                     */
-    uint32_t reserved[1];
+    uint32_t consultant;      /* FP64 only: the candidate list of 0 = NBSConsultant (anne's
+                                 "nbs", NBSConsultant.cpp:85-374) or 1 = LeapConsultant
+                                 ("leap", LeapConsultant.cpp:108-195, LeapConsultant.h:58-446:
+                                 cells ordered along the widest axis, periodic neighbours);
+                                 the MIXED form's lists are complete by construction     */
 } vedo_engine_opts;
 
 typedef struct vedo_gpu_engine vedo_gpu_engine;

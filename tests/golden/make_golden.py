@@ -24,8 +24,11 @@ sys.path[:0] = [ROOT, os.path.join(ROOT, "oracle")]
 from vedo_gb300 import scenes  # noqa: E402
 
 
+LEAP = {"leap_cluster_poly", "leap_box_lsd", "leap_periodic_lsd", "leap_periodic_wide"}
+
+
 def cases():
-    """(name, scene, steps, up_iact) of every fixture."""
+    """(name, scene, steps, up_iact) of every fixture; the leap_* ones run the Leap consultant."""
     yield "box_lsd", scenes.lsd_box(n_side=5, steps=3000, vel_sigma=0.3, seed=11), 2500, 10
     for solver in ("ISwBSDBF", "ISwBtSDBF", "ISwBSDB2F", "ISwHertz", "ISwH"):
         yield f"cluster_{solver}", scenes.cluster(n=48, solver=solver, steps=400, seed=5), 300, 5
@@ -40,6 +43,13 @@ def cases():
     yield "periodic_hertz", scenes.periodic_layer(solver="ISwHertz", seed=8), 400, 5
     yield "periodic_btsdbf", scenes.periodic_layer(solver="ISwBtSDBF", seed=15), 300, 5
     yield "periodic_bsdb2f", scenes.periodic_layer(solver="ISwBSDB2F", seed=16), 300, 5
+    # the Leap consultant's candidate list: polydisperse (its cell edge takes the largest range),
+    # a box, and periodic layers (neighbour zones wrap across the faces)
+    yield "leap_cluster_poly", scenes.cluster(n=48, solver="ISwH", polydisperse=True, orbital=True, cylinders=3,
+                                              steps=300, seed=9), 200, 3
+    yield "leap_box_lsd", scenes.lsd_box(n_side=5, steps=3000, vel_sigma=0.3, seed=11), 600, 10
+    yield "leap_periodic_lsd", scenes.periodic_layer(solver="ISwBSDBF"), 400, 5
+    yield "leap_periodic_wide", scenes.periodic_layer(nx=8, ny=6, layers=2, solver="ISwBSDBF", seed=22), 400, 5
     yield "periodic_far_lsd", scenes.periodic_layer(solver="ISwBSDBF", nx=3, ny=3, layers=2, seed=12,
                                                     outside=True), 200, 4
     yield "periodic_h", scenes.periodic_layer(solver="ISwH", periodic_y=False, floor_spin=40.0, side_walls=True,
@@ -105,14 +115,15 @@ def main():
         if only and name not in only:
             continue
         ido = sc.to_ido()
-        w = RefWorld(sc, up_iact=up)
+        consultant = "leap" if name in LEAP else "nbs"
+        w = RefWorld(sc, up_iact=up, consultant=consultant)
         cf0, cs0 = w.candidates()
         w.run(steps)
         st = w.state()
         cf, cs = w.candidates()
         it = w.interactions()
         np.savez_compressed(os.path.join(HERE, f"{name}.npz"), ido=np.frombuffer(ido, np.uint8), steps=steps,
-                            up_iact=up, cand0_first=cf0, cand0_second=cs0, cand_first=cf, cand_second=cs,
+                            up_iact=up, consultant=consultant, cand0_first=cf0, cand0_second=cs0, cand_first=cf, cand_second=cs,
                             time=w.time(), energy=w.energy(),
                             **{f"state_{k}": v for k, v in st.items()},
                             **{f"iact_{k}": v for k, v in it.items()})

@@ -21,7 +21,8 @@ ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 GOLDEN = sorted(glob.glob(os.path.join(ROOT, "tests", "golden", "*.npz")))
 EXACT_CASES = ("box_lsd", "cluster_ISwBSDBF", "cluster_ISwBtSDBF", "cluster_ISwBSDB2F", "cluster_bsdbf_upiact1",
                "cluster_zoi", "holed_plate_lsd", "periodic_lsd",
-               "periodic_far_lsd", "periodic_btsdbf", "periodic_bsdb2f")
+               "periodic_far_lsd", "periodic_btsdbf", "periodic_bsdb2f", "leap_box_lsd",
+               "leap_periodic_lsd", "leap_periodic_wide")
 STATE = ("position", "velocity", "angular_velocity", "impact", "angular_impact", "orientation_x", "orientation_z")
 
 
@@ -33,7 +34,8 @@ def _name(p):
 def test_engine_matches_reference_golden(path, engine_lib):
     g = np.load(path)
     sc = Scene.from_ido(g["ido"].tobytes())
-    e = engine_lib.GpuEngine(sc, up_iact=int(g["up_iact"]))
+    e = engine_lib.GpuEngine(sc, up_iact=int(g["up_iact"]),
+                             consultant=str(g["consultant"]) if "consultant" in g else "nbs")
     it0 = e.interactions()
     assert np.array_equal(it0["first"], g["cand0_first"]) and np.array_equal(it0["second"], g["cand0_second"])
     e.run(int(g["steps"]))
@@ -330,3 +332,30 @@ def test_step_and_contacts_entry_points_equal_run_and_interactions(engine_lib):
     np.testing.assert_array_equal(shear, ib["shear"])
     a.close()
     b.close()
+
+
+@pytest.mark.parametrize("which", ["periodic", "box"])
+def test_leap_consultant_at_size_bitexact(which, engine_lib, port_lib):
+    """The Leap consultant's candidate list on the device: a 12 x 12 x 4 periodic layer (neighbour
+    zones wrapping across both periodic faces) and the 8,000-sphere box; candidate lists element
+    for element and states bit for bit against the oracle, with rebuilds every 5 / 20 steps."""
+    from oracle import PortWorld
+    if which == "periodic":
+        sc, up, steps = scenes.periodic_layer(nx=12, ny=12, layers=4, seed=21, steps=400), 5, 200
+    else:
+        sc, up, steps = scenes.lsd_box(), 20, 200
+    e = engine_lib.GpuEngine(sc, up_iact=up, consultant="leap")
+    p = PortWorld(sc, up_iact=up, consultant="leap")
+    for _ in range(2):
+        ia = e.interactions()
+        f, s = p.candidates()
+        assert np.array_equal(ia["first"], f) and np.array_equal(ia["second"], s)
+        e.run(steps // 2)
+        p.run(steps // 2)
+    a, b = e.state(), p.state()
+    for k in ("position", "velocity", "angular_velocity", "impact", "angular_impact"):
+        np.testing.assert_array_equal(a[k], b[k], err_msg=k)
+    nbs = engine_lib.GpuEngine(sc, up_iact=up)
+    assert len(nbs.interactions()["first"]) != len(e.interactions()["first"]) or which == "box"
+    e.close()
+    nbs.close()

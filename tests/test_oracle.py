@@ -15,7 +15,8 @@ ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 GOLDEN = sorted(glob.glob(os.path.join(ROOT, "tests", "golden", "*.npz")))
 EXACT_CASES = ("box_lsd", "cluster_ISwBSDBF", "cluster_ISwBtSDBF", "cluster_ISwBSDB2F", "cluster_bsdbf_upiact1",
                "cluster_zoi", "holed_plate_lsd", "periodic_lsd",
-               "periodic_far_lsd", "periodic_btsdbf", "periodic_bsdb2f")
+               "periodic_far_lsd", "periodic_btsdbf", "periodic_bsdb2f", "leap_box_lsd",
+               "leap_periodic_lsd", "leap_periodic_wide")
 
 
 def _name(p):
@@ -30,7 +31,7 @@ def test_port_matches_reference_golden(path, port_lib):
     from oracle import PortWorld
     g = np.load(path)
     sc = Scene.from_ido(g["ido"].tobytes())
-    w = PortWorld(sc, up_iact=int(g["up_iact"]))
+    w = PortWorld(sc, up_iact=int(g["up_iact"]), consultant=str(g["consultant"]) if "consultant" in g else "nbs")
     f0, s0 = w.candidates()
     assert np.array_equal(f0, g["cand0_first"]) and np.array_equal(s0, g["cand0_second"])
     w.run(int(g["steps"]))

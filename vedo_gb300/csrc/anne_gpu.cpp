@@ -4,9 +4,9 @@
 //
 // Same arguments and outputs as anne (Anne.cpp:24-36, 38-160): Mode `analysis` runs
 // SimMediator::Run until t >= t_stop; Type is accepted as anne accepts it (safe, near, nbs,
-// leap); the FP64 engine builds the NBS candidate list with UpIact as the rebuild interval (the
-// other consultants list more candidate pairs: the same contacts, while the order of the FP64
-// impulse sums, and so the last bits, are NBS's).
+// leap); the FP64 engine builds the NBS candidate list, or the Leap one for `leap`, with UpIact
+// as the rebuild interval (for safe and near, which list more candidate pairs, the contacts are
+// the same while the order of the FP64 impulse sums, and so the last bits, are NBS's).
 // Every Record steps <IDO>_NNNNNNN.ido is written and terminate.ido at the end
 // (Consultant::RecordIDO, NBSConsultant::NextStep).  --mixed runs the mixed-precision form
 // instead (UpIact is then ignored: its list is rebuilt by displacement).  Mode `redistribute`
@@ -56,6 +56,7 @@ int main(int argc, char** argv) {
     vedo_engine_opts o;
     vedo_gpu_default_opts(&o);
     o.up_iact = up_iact ? up_iact : 1;
+    o.consultant = type == "leap" ? 1u : 0u;
     o.precision = mixed ? VEDO_PRECISION_MIXED : VEDO_PRECISION_FP64;
     o.record = mixed ? 0 : record;           // the mixed form's records are written below
     o.output_prefix = mixed ? nullptr : ido.c_str();

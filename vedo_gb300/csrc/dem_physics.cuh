@@ -274,9 +274,11 @@ __device__ __forceinline__ void respond_object(const ModelDev& m, double dt, d3 
 
 // DOMap::CalDistance (DOMap.cpp:142-414) for the broad phase; i is the primary-cell object.
 // Returns a negative value for an unsupported shape pair.
+// pb (the Leap consultant): the difference vector takes the boundary's minimum image before its
+// length, as DOMap::CalDistance does when given the boundary (DOMap.cpp:152-155, 329-332, 371-374, 402-405).
 __device__ __forceinline__ double cal_distance(const ModelDev& mi_, const ModelDev& mj_, uint32_t i_, uint32_t j_,
                                                const double4_32a* __restrict__ pos, const double4_32a* __restrict__ ox,
-                                               const double4_32a* __restrict__ oz, bool& ok) {
+                                               const double4_32a* __restrict__ oz, const Periodic* pb, bool& ok) {
     const ModelDev* mi = &mi_;
     const ModelDev* mj = &mj_;
     uint32_t i = i_, j = j_;
@@ -286,7 +288,10 @@ __device__ __forceinline__ double cal_distance(const ModelDev& mi_, const ModelD
     }
     ok = true;
     d3 pi = ld(pos, i), pj = ld(pos, j);
-    if (mi->shape == SHAPE_SPHERE && mj->shape == SHAPE_SPHERE) return len(sub(pi, pj));
+    if (mi->shape == SHAPE_SPHERE && mj->shape == SHAPE_SPHERE) {
+        const d3 Im = sub(pi, pj);
+        return len(pb ? min_image(*pb, Im) : Im);
+    }
     // sphere - plate, and sphere - plate with a hole (DOMap.cpp:336-370: the hole is ignored)
     if (mi->shape == SHAPE_SPHERE && (mj->shape == SHAPE_PLATE || mj->shape == SHAPE_HOLED)) {
         d3 Oz = ld(oz, j), Ox = ld(ox, j);
@@ -298,7 +303,8 @@ __device__ __forceinline__ double cal_distance(const ModelDev& mi_, const ModelD
         double dy = dot(sub(Cap, pj), Oy);
         if (dy < -hl) dy = -hl; else if (dy > hl) dy = hl;
         d3 Caps = add(add(muls(Ox, dx), muls(Oy, dy)), pj);
-        return len(sub(Caps, pi));
+        const d3 Im = sub(Caps, pi);
+        return len(pb ? min_image(*pb, Im) : Im);
     }
     if (mi->shape == SHAPE_SPHERE && mj->shape == SHAPE_CYL) {
         double hh = 0.5 * (mj->a1);
@@ -309,7 +315,7 @@ __device__ __forceinline__ double cal_distance(const ModelDev& mi_, const ModelD
         if ((dap < hh) && (dap > -hh)) Im = sub(Cap, pi);
         else if (dap >= hh) Im = sub(add(pj, muls(ax, hh)), pi);
         else Im = sub(sub(pj, muls(ax, hh)), pi);
-        return len(Im);
+        return len(pb ? min_image(*pb, Im) : Im);
     }
     ok = false;
     return 0.0;

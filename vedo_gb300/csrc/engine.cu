@@ -43,6 +43,31 @@ __constant__ int c_slot[15][3] = {{-1, -1, -1}, {-1, -1, 0}, {-1, -1, 1}, {0, -1
 constexpr int SLOT_SELF = 12;
 constexpr int SLOT_GLOBAL = 13;
 constexpr int NSLOT = 15;
+// LeapConsultant::subReset (LeapConsultant.h:195-446): the 13 half-shell neighbours, then the
+// cell itself (13), then the scope-global objects (14).
+__constant__ int c_slot_leap[13][3] = {{-1, -1, -1}, {-1, -1, 0}, {-1, -1, 1}, {0, -1, -1}, {0, -1, 0},
+                                       {0, -1, 1},   {1, -1, -1}, {1, -1, 0},  {1, -1, 1},  {-1, 0, -1},
+                                       {-1, 0, 0},   {0, 0, -1},  {1, 0, -1}};
+
+// The broad phase's cell-key layout: the axis order of the key (the consultant's comparator:
+// NBS and TrirLeX x, y, z; TrirLeY y, x, z; TrirLeZ z, x, y, NBSConsultant.h:62-128), the key's
+// extent per axis, the number of zones per axis and, for the Leap consultant, its periodic axes.
+struct CellGrid {
+    int ord[3];                // axes from the most to the least significant
+    uint64_t dim[3];           // key extent per axis (x, y, z)
+    uint32_t ncel[3];          // zones per axis (x, y, z): the last zone is ncel - 1
+    int leap;                  // 1: LeapConsultant's traversal
+    int pbc[3], has_pbc;       // Leap: axes whose neighbours wrap (LeapConsultant.h:146-150)
+};
+__host__ __device__ inline uint64_t grid_key(const CellGrid& g, const uint64_t c[3]) {
+    return (c[g.ord[0]] * g.dim[g.ord[1]] + c[g.ord[1]]) * g.dim[g.ord[2]] + c[g.ord[2]];
+}
+__device__ inline void grid_cell(const CellGrid& g, uint64_t key, uint64_t c[3]) {
+    c[g.ord[2]] = key % g.dim[g.ord[2]];
+    const uint64_t rest = key / g.dim[g.ord[2]];
+    c[g.ord[1]] = rest % g.dim[g.ord[1]];
+    c[g.ord[0]] = rest / g.dim[g.ord[1]];
+}
 
 // order-preserving map of doubles to unsigned 64-bit integers (for exact atomic min/max)
 __host__ __device__ inline unsigned long long ord_of(double d) {
@@ -373,18 +398,34 @@ __global__ void __launch_bounds__(TPB) k_safe(uint32_t n, const uint32_t* __rest
 
 __global__ void __launch_bounds__(TPB) k_cellkey(uint32_t n, const uint32_t* __restrict__ model_of,
                                                  const ModelDev* __restrict__ models, const double4_32a* __restrict__ pos,
-                                                 double xmin, double ymin, double zmin, double zone, uint64_t ny1,
-                                                 uint64_t nz1, uint64_t sentinel, uint64_t* __restrict__ key,
+                                                 double xmin, double ymin, double zmin, double zone, CellGrid g,
+                                                 uint64_t sentinel, uint64_t* __restrict__ key,
                                                  uint32_t* __restrict__ sid) {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     uint64_t k = sentinel;
-    if (models[model_of[i]].scope == SCOPE_LOCAL) {          // :163-178
+    if (models[model_of[i]].scope == SCOPE_LOCAL) {          // NBS :163-178, Leap LeapConsultant.h:160-170
         const double4_32a p = pos[i];
-        const uint64_t cx = (uint32_t)((p.x - xmin) / zone);
-        const uint64_t cy = (uint32_t)((p.y - ymin) / zone);
-        const uint64_t cz = (uint32_t)((p.z - zmin) / zone);
-        k = (cx * ny1 + cy) * nz1 + cz;
+        const uint64_t c[3] = {(uint32_t)((p.x - xmin) / zone), (uint32_t)((p.y - ymin) / zone),
+                               (uint32_t)((p.z - zmin) / zone)};
+        k = grid_key(g, c);
+    }
+    key[i] = k;
+    sid[i] = i;
+}
+
+// One axis of the local objects' positions as sortable keys (others sort last): the Leap
+// consultant's spans come from the sorted positions (LeapConsultant.cpp:143-168).
+__global__ void __launch_bounds__(TPB) k_axis_key(uint32_t n, const uint32_t* __restrict__ model_of,
+                                                  const ModelDev* __restrict__ models,
+                                                  const double4_32a* __restrict__ pos, int axis,
+                                                  uint64_t* __restrict__ key, uint32_t* __restrict__ sid) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    uint64_t k = ~0ull;
+    if (models[model_of[i]].scope == SCOPE_LOCAL) {
+        const double4_32a p = pos[i];
+        k = ord_of(axis == 0 ? p.x : axis == 1 ? p.y : p.z);
     }
     key[i] = k;
     sid[i] = i;
@@ -415,14 +456,23 @@ __global__ void __launch_bounds__(TPB) k_cell_fill(uint32_t nloc, const uint64_t
 
 // Candidate test of BuildIactTab (NBSConsultant.cpp:318-345): DOMap::CalDistance <= safe_i +
 // safe_j, decided from FP32 bounds where they are conclusive and in exact FP64 otherwise.
+// pb: the Leap consultant's distance takes the boundary's minimum image (nullptr: NBS's does not)
 __device__ __forceinline__ bool candidate(const ModelDev& mi, const ModelDev& mj, uint32_t i, uint32_t j, double si,
                                           double sj, float si32, float sj32, const double4_32a* __restrict__ pos,
                                           const double4_32a* __restrict__ ox, const double4_32a* __restrict__ oz,
                                           const float4* __restrict__ pos32, const float4* __restrict__ wall32,
-                                          int* __restrict__ err) {
+                                          int* __restrict__ err, const Periodic* pb) {
     const float thr = si32 + sj32;                     // float sums of the rounded-to-float safe lengths
     const float tlo = thr * (1.0f - 4.0f * PF_ARITH_EPS), thi = thr * (1.0f + 4.0f * PF_ARITH_EPS);
-    if (mi.shape == SHAPE_SPHERE && mj.shape == SHAPE_SPHERE) {
+    if (pb) {
+        // periodic: the least distance over the images bounds the detector's from below (the
+        // certain-candidate shortcut is not taken: the image the reference picks may be another)
+        if (mi.shape == SHAPE_SPHERE && mj.shape == SHAPE_SPHERE) {
+            float e;
+            const float d = dist32_periodic(pos32[i], pos32[j], pb->range32, e);
+            if (d - e > thi) return false;
+        }
+    } else if (mi.shape == SHAPE_SPHERE && mj.shape == SHAPE_SPHERE) {
         float e;
         const float d = dist32(pos32[i], pos32[j], e);
         if (d - e > thi) return false;
@@ -441,7 +491,7 @@ __device__ __forceinline__ bool candidate(const ModelDev& mi, const ModelDev& mj
         }
     }
     bool ok;
-    const double d = cal_distance(mi, mj, i, j, pos, ox, oz, ok);
+    const double d = cal_distance(mi, mj, i, j, pos, ox, oz, pb, ok);
     if (!ok) {
         atomicOr(err, ERR_BAD_SHAPE_PAIR);
         return false;
@@ -464,7 +514,7 @@ __global__ void __launch_bounds__(TPB) k_pairs(uint32_t nloc, const uint32_t* __
                                                const double4_32a* __restrict__ pos, const double4_32a* __restrict__ ox,
                                                const double4_32a* __restrict__ oz, const float4* __restrict__ pos32,
                                                const float4* __restrict__ wall32, const double* __restrict__ safe,
-                                               uint32_t ncx, uint32_t ncy, uint32_t ncz, uint64_t ny1, uint64_t nz1,
+                                               CellGrid g, Periodic pbv,
                                                uint32_t* __restrict__ task, uint32_t* __restrict__ first,
                                                uint32_t* __restrict__ second, int* __restrict__ err) {
     const uint64_t t = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -472,45 +522,72 @@ __global__ void __launch_bounds__(TPB) k_pairs(uint32_t nloc, const uint32_t* __
     const int s = (int)(t / nloc);
     const uint32_t P = (uint32_t)(t % nloc);
     const uint32_t c = cellof[P];
-    const uint64_t key = cell_key[c];
-    const uint32_t cz = (uint32_t)(key % nz1);
-    const uint64_t rest = key / nz1;
-    const uint32_t cy = (uint32_t)(rest % ny1);
-    const uint32_t cx = (uint32_t)(rest / ny1);
+    uint64_t cc[3];
+    grid_cell(g, cell_key[c], cc);
     const uint32_t cs = cell_start[c], csize = cell_start[c + 1] - cs;
     const uint64_t tid = (uint64_t)cs * NSLOT + (uint64_t)s * csize + (P - cs);
-    if (cx >= ncx || cy >= ncy || cz >= ncz) {                // only cells inside the loops are primary (:186-190)
+    // NBS: only cells inside the loops are primary (:186-190); Leap visits every zone of its map
+    if (!g.leap && (cc[0] >= g.ncel[0] || cc[1] >= g.ncel[1] || cc[2] >= g.ncel[2])) {
         if (!FILL) task[tid] = 0;
         return;
     }
+    const int slot_self = g.leap ? 13 : SLOT_SELF, slot_global = g.leap ? 14 : SLOT_GLOBAL;
     const uint32_t* js = nullptr;
     uint32_t jn = 0;
-    if (s == SLOT_SELF) {                                     // BuildIactTab(v), :347-374
+    // the cell whose zone coordinates are w (its index, or none)
+    auto find_cell = [&](const uint64_t w[3]) -> uint32_t {
+        for (int a = 0; a < 3; ++a)
+            if (w[a] >= g.dim[a]) return 0xffffffffu;
+        const uint64_t nk = grid_key(g, w);
+        if (grid) return nk < grid_cells ? grid[nk] : 0xffffffffu;
+        const uint32_t nc = *ncells_p;
+        uint32_t lo = 0, hi = nc;
+        while (lo < hi) {
+            const uint32_t mid = (lo + hi) >> 1;
+            if (cell_key[mid] < nk) lo = mid + 1; else hi = mid;
+        }
+        return (lo < nc && cell_key[lo] == nk) ? lo : 0xffffffffu;
+    };
+    if (s == slot_self) {                                     // BuildIactTab(v), :347-374
         js = sid + P + 1;
         jn = cs + csize - (P + 1);
-    } else if (s == SLOT_GLOBAL) {                            // BuildIactTab(v, GlobalElement), :266
+    } else if (s == slot_global) {                            // BuildIactTab(v, GlobalElement), :266
         js = glob;
         jn = nglob;
-    } else {
-        const int dx = c_slot[s][0], dy = c_slot[s][1], dz = c_slot[s][2];
-        if (!((cx == 0 && dx < 0) || (cy == 0 && dy < 0) || (cz == 0 && dz < 0))) {
-            const uint64_t nk = ((uint64_t)(cx + dx) * ny1 + (uint64_t)(cy + dy)) * nz1 + (uint64_t)(cz + dz);
-            uint32_t c2 = 0xffffffffu;
-            if (grid) {
-                if (nk < grid_cells) c2 = grid[nk];
-            } else {
-                const uint32_t nc = *ncells_p;
-                uint32_t lo = 0, hi = nc;
-                while (lo < hi) {
-                    const uint32_t mid = (lo + hi) >> 1;
-                    if (cell_key[mid] < nk) lo = mid + 1; else hi = mid;
+    } else if (g.leap || s < NSLOT) {
+        int d[3];
+        for (int a = 0; a < 3; ++a) d[a] = g.leap ? c_slot_leap[s][a] : c_slot[s][a];
+        uint32_t c2 = 0xffffffffu;
+        if (!((cc[0] == 0 && d[0] < 0) || (cc[1] == 0 && d[1] < 0) || (cc[2] == 0 && d[2] < 0))) {
+            const uint64_t w[3] = {cc[0] + d[0], cc[1] + d[1], cc[2] + d[2]};
+            c2 = find_cell(w);
+        }
+        if (c2 == 0xffffffffu && g.leap && g.has_pbc) {
+            // the neighbour's periodic image (LeapConsultant.h:199-440): on an axis stepping down
+            // from zone 0 (up from the last zone) it wraps when that axis is periodic; ids are
+            // _uint_t, and an image that names the opposite neighbour is skipped
+            bool at_edge = false, dup = false, valid = true;
+            uint64_t w[3];
+            for (int a = 0; a < 3; ++a) {
+                const uint32_t ia = (uint32_t)cc[a], mx = g.ncel[a] - 1u;
+                uint32_t wa = ia;
+                if (d[a] < 0) {
+                    at_edge |= ia == 0u;
+                    wa = g.pbc[a] ? mx : ia - 1u;
+                    dup |= wa == ia + 1u;
+                } else if (d[a] > 0) {
+                    at_edge |= ia == mx;
+                    wa = g.pbc[a] ? 0u : ia + 1u;
+                    dup |= wa == ia - 1u;
                 }
-                if (lo < nc && cell_key[lo] == nk) c2 = lo;
+                valid &= wa != 0xffffffffu;
+                w[a] = wa;
             }
-            if (c2 != 0xffffffffu) {
-                js = sid + cell_start[c2];
-                jn = cell_start[c2 + 1] - cell_start[c2];
-            }
+            if (at_edge && !dup && valid) c2 = find_cell(w);
+        }
+        if (c2 != 0xffffffffu) {
+            js = sid + cell_start[c2];
+            jn = cell_start[c2 + 1] - cell_start[c2];
         }
     }
     const uint32_t i = sid[P];
@@ -529,7 +606,8 @@ __global__ void __launch_bounds__(TPB) k_pairs(uint32_t nloc, const uint32_t* __
         const ModelDev& mj = models[model_of[j]];
         if (group_iact[gi * G + mj.group] < 0) continue;
         const double sj = safe[j];
-        if (!candidate(mi, mj, i, j, si, sj, si32, (float)sj, pos, ox, oz, pos32, wall32, err)) continue;
+        if (!candidate(mi, mj, i, j, si, sj, si32, (float)sj, pos, ox, oz, pos32, wall32, err,
+                       g.leap && pbv.on ? &pbv : nullptr)) continue;
         if (FILL) {
             first[off + cnt] = i < j ? i : j;
             second[off + cnt] = i < j ? j : i;
@@ -753,10 +831,15 @@ int Engine::init(const HScene& scene, const vedo_engine_opts& opts) {
     host_ = scene;
     opts_ = opts;
     if (opts_.up_iact == 0) opts_.up_iact = 1;
+    if (opts_.consultant > 1) return fail(VEDO_ERR_INVALID_ARGUMENT, "unknown consultant");
+    leap_ = opts_.consultant == 1;
     out_prefix_ = opts.output_prefix ? opts.output_prefix : "";
     std::string msg;
     int rc = build_tables(host_, tab_, msg);
     if (rc != VEDO_OK) return fail(rc, msg);
+    if (leap_ && (host_.zoi_switch[0] || host_.zoi_switch[1] || host_.zoi_switch[2]))
+        return fail(VEDO_ERR_UNSUPPORTED_MODEL,      // LeapConsultant::NextStep erases objects at every reset (:67)
+                    "a zone of interest with the Leap consultant is not supported");
     n_ = host_.n;
     nm_ = (uint32_t)tab_.models.size();
     dt_ = host_.time_interval;
@@ -800,6 +883,9 @@ int Engine::init(const HScene& scene, const vedo_engine_opts& opts) {
     }
     for (uint32_t i = 0; i < n_; ++i)
         if (tab_.models[host_.model_of[i]].scope != SCOPE_LOCAL) global_ids_.push_back(i);
+        else leap_rmax_ = std::max(leap_rmax_, tab_.models[host_.model_of[i]].range);
+    if (leap_ && global_ids_.size() == n_)           // the reference indexes an empty vector
+        return fail(VEDO_ERR_INVALID_SCENE, "the Leap consultant needs a local object");
     // FP32 prefilter copies: origin at the centre of the initial bounding box
     {
         double lo[3] = {DBL_MAX, DBL_MAX, DBL_MAX}, hi[3] = {-DBL_MAX, -DBL_MAX, -DBL_MAX};
@@ -901,20 +987,57 @@ int Engine::rebuild(bool from_records) {
     const double zmin = dbl_of(red[4]), zmax = dbl_of(red[5]), vmax = dbl_of(red[6]);
     const uint32_t nloc = n_ - (uint32_t)global_ids_.size();
     double rmax = 0.0;
-    if (red[7]) rmax = tab_.models[host_.model_of[red[7] - 1]].range;     // the last local DO (:140)
-    const double zone = sf_ * (2.0 * rmax + dtu * vmax + 0.5 * dtu * dtu * glen);   // :146
+    CellGrid g{};
+    g.ord[0] = 0; g.ord[1] = 1; g.ord[2] = 2;
+    if (leap_) {
+        // LeapConsultant::Reset (LeapConsultant.cpp:108-195): the largest range of the local
+        // objects, and the comparator from the spans between the 2 % and 98 % quantiles of the
+        // local positions per axis (sorted on the device)
+        rmax = leap_rmax_;
+        const double keep = 1.0 - 0.02, hi_d = keep * nloc - 1, lo_d = 0.02 * nloc;
+        const uint32_t ih = hi_d < 0.0 ? 0u : (uint32_t)hi_d, il = (uint32_t)lo_d;
+        double span[3];
+        for (int a = 0; a < 3; ++a) {
+            k_axis_key<<<blocks_for(n_), TPB, 0, stream_>>>(n_, d_model_of_, d_models_, d_pos_, a, d_key_, d_sid_);
+            ++own;
+            CK(radix_sort_u64(d_key_, d_sid_, d_key_alt_, d_sid_alt_, n_, 0, 64, scratch_, stream_));
+            unsigned long long q[2];
+            CK(cudaMemcpyAsync(&q[0], d_key_ + ih, 8, cudaMemcpyDeviceToHost, stream_));
+            CK(cudaMemcpyAsync(&q[1], d_key_ + il, 8, cudaMemcpyDeviceToHost, stream_));
+            CK(cudaStreamSynchronize(stream_));
+            span[a] = dbl_of(q[0]) - dbl_of(q[1]);
+        }
+        const int mode = span[0] >= span[1] ? (span[0] >= span[2] ? 0 : 2) : (span[1] >= span[2] ? 1 : 2);
+        if (mode == 1) { g.ord[0] = 1; g.ord[1] = 0; g.ord[2] = 2; }        // TrirLeY
+        if (mode == 2) { g.ord[0] = 2; g.ord[1] = 0; g.ord[2] = 1; }        // TrirLeZ
+    } else if (red[7]) {
+        rmax = tab_.models[host_.model_of[red[7] - 1]].range;              // the last local DO (:140)
+    }
+    const double zone = sf_ * (2.0 * rmax + dtu * vmax + 0.5 * dtu * dtu * glen);   // :146, Leap :138
     auto ncel = [&](double lo, double hi) {
         uint32_t c = (uint32_t)std::ceil((hi - lo) / zone);
         return std::max(c, (uint32_t)1);
     };
     const uint32_t ncx = ncel(xmin, xmax), ncy = ncel(ymin, ymax), ncz = ncel(zmin, zmax);
-    const uint64_t ny1 = (uint64_t)ncy + 1, nz1 = (uint64_t)ncz + 1;
-    const uint64_t sentinel = ((uint64_t)ncx + 1) * ny1 * nz1;
+    g.ncel[0] = ncx; g.ncel[1] = ncy; g.ncel[2] = ncz;
+    g.leap = leap_ ? 1 : 0;
+    // key extents: zone ids reach ncel (a span that is a whole number of zones); Leap visits every
+    // zone, so its neighbours reach ncel + 1
+    const uint64_t pad = leap_ ? 2 : 1;
+    g.dim[0] = (uint64_t)ncx + pad; g.dim[1] = (uint64_t)ncy + pad; g.dim[2] = (uint64_t)ncz + pad;
+    if (leap_) {
+        const double lo3[3] = {xmin, ymin, zmin}, hi3[3] = {xmax, ymax, zmax};
+        for (int a = 0; a < 3; ++a) {                                      // LeapConsultant.h:146-150
+            g.pbc[a] = tab_.pbc.sw[a] && (hi3[a] - lo3[a]) >= 0.5 * tab_.pbc.range[a];
+            g.has_pbc |= g.pbc[a];
+        }
+    }
+    const uint64_t sentinel = g.dim[0] * g.dim[1] * g.dim[2];
     int bits = 1;
     while (bits < 64 && (sentinel >> bits)) ++bits;
-    // 2. cell keys, stable sort (locals by cell, ids ascending within a cell)
-    k_cellkey<<<blocks_for(n_), TPB, 0, stream_>>>(n_, d_model_of_, d_models_, d_pos_, xmin, ymin, zmin, zone, ny1,
-                                                   nz1, sentinel, d_key_, d_sid_);
+    // 2. cell keys, stable sort (locals by cell in the comparator's order, ids ascending within a cell)
+    k_cellkey<<<blocks_for(n_), TPB, 0, stream_>>>(n_, d_model_of_, d_models_, d_pos_, xmin, ymin, zmin, zone, g,
+                                                   sentinel, d_key_, d_sid_);
     ++own;
     CK(radix_sort_u64(d_key_, d_sid_, d_key_alt_, d_sid_alt_, n_, 0, bits, scratch_, stream_));
     // 3. cell ranges
@@ -951,7 +1074,7 @@ int Engine::rebuild(bool from_records) {
         k_pairs<false><<<blocks_for(ntask), TPB, 0, stream_>>>(
             nloc, d_sid_, d_cell_key_, d_cell_start_, d_total_, d_cellof_, grid, gcells, d_global_,
             (uint32_t)global_ids_.size(), d_model_of_, d_models_, d_group_iact_, tab_.ngroups, d_pos_, d_ox_, d_oz_,
-            d_pos32_, d_wall32_, d_safe_, ncx, ncy, ncz, ny1, nz1, d_task_, nullptr, nullptr, d_err_);
+            d_pos32_, d_wall32_, d_safe_, g, tab_.pbc, d_task_, nullptr, nullptr, d_err_);
         ++own;
         CK(exclusive_scan_u32(d_task_, d_task_, (uint32_t)ntask, d_total_ + 1, scratch_, stream_));
         CK(cudaMemcpyAsync(&np, d_total_ + 1, sizeof(uint32_t), cudaMemcpyDeviceToHost, stream_));
@@ -961,7 +1084,7 @@ int Engine::rebuild(bool from_records) {
         k_pairs<true><<<blocks_for(ntask), TPB, 0, stream_>>>(
             nloc, d_sid_, d_cell_key_, d_cell_start_, d_total_, d_cellof_, grid, gcells, d_global_,
             (uint32_t)global_ids_.size(), d_model_of_, d_models_, d_group_iact_, tab_.ngroups, d_pos_, d_ox_, d_oz_,
-            d_pos32_, d_wall32_, d_safe_, ncx, ncy, ncz, ny1, nz1, d_task_, cur_.first, cur_.second, d_err_);
+            d_pos32_, d_wall32_, d_safe_, g, tab_.pbc, d_task_, cur_.first, cur_.second, d_err_);
         ++own;
     } else {
         int rc = ensure_list(cur_, 0);

@@ -128,6 +128,9 @@ private:
     float4* d_pos32_ = nullptr;
     // per object: 1 when a pair of this step applied an impulse to it (k_pair sets, k_obj clears)
     uint8_t* d_touched_ = nullptr;
+    // the candidate list of LeapConsultant (else NBSConsultant), and its cell edge's largest range
+    bool leap_ = false;
+    double leap_rmax_ = 0.0;
     float4* d_wall32_ = nullptr;
     float* d_reach_ = nullptr;
     double origin_[3] = {0, 0, 0};

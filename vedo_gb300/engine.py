@@ -85,7 +85,8 @@ STATE_FIELDS = ("position", "velocity", "angular_velocity", "orientation_x", "or
 
 
 def _opts(up_iact, record, precision, device, prefix, skin, check_interval, tick_block=None, cell_scale=None,
-          autotune=False, graphs=True, stored_splits=False, split_tick=False, full_walks=False) -> EngineOpts:
+          autotune=False, graphs=True, stored_splits=False, split_tick=False, full_walks=False,
+          consultant="nbs") -> EngineOpts:
     opts = EngineOpts()
     lib().vedo_gpu_default_opts(C.byref(opts))
     opts.up_iact, opts.record, opts.precision, opts.device = up_iact, record, precision, device
@@ -102,6 +103,9 @@ def _opts(up_iact, record, precision, device, prefix, skin, check_interval, tick
     opts.stored_splits = 1 if stored_splits else 0
     opts.split_tick = 1 if split_tick else 0
     opts.full_walks = 1 if full_walks else 0
+    if consultant not in ("nbs", "leap"):
+        raise ValueError(f"consultant must be 'nbs' or 'leap', not {consultant!r}")
+    opts.consultant = 1 if consultant == "leap" else 0
     opts.output_prefix = prefix
     return opts
 
@@ -109,20 +113,22 @@ def _opts(up_iact, record, precision, device, prefix, skin, check_interval, tick
 class GpuEngine:
     """One scene on one GPU.
 
-    Parameters mirror ``anne analysis <ido> nbs <Record> <UpIact>`` (Anne.cpp:38-128):
+    Parameters mirror ``anne analysis <ido> <nbs|leap> <Record> <UpIact>`` (Anne.cpp:38-128):
     `up_iact` is the candidate-list rebuild interval, `record` the IDO record interval
-    (0 = never) and `output_prefix` where record/terminate IDO files go (None = none).
+    (0 = never), `output_prefix` where record/terminate IDO files go (None = none) and
+    `consultant` whose candidate list the FP64 form builds.
     """
 
     def __init__(self, scene, up_iact: int = 1, record: int = 0, precision: int = _abi.PRECISION_FP64,
                  device: int = 0, output_prefix: Optional[str] = None, skin: Optional[float] = None,
                  check_interval: Optional[int] = None, tick_block: Optional[int] = None,
                  cell_scale: Optional[float] = None, autotune: bool = False, graphs: bool = True,
-                 stored_splits: bool = False, split_tick: bool = False, full_walks: bool = False):
+                 stored_splits: bool = False, split_tick: bool = False, full_walks: bool = False,
+                 consultant: str = "nbs"):
         L = lib()
         self._prefix = output_prefix.encode() if output_prefix else None
         opts = _opts(up_iact, record, precision, device, self._prefix, skin, check_interval, tick_block, cell_scale,
-                     autotune, graphs, stored_splits, split_tick, full_walks)
+                     autotune, graphs, stored_splits, split_tick, full_walks, consultant)
         h = C.c_void_p()
         if isinstance(scene, (str, bytes, os.PathLike)):
             path = os.fsencode(scene)
