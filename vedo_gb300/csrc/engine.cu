@@ -53,20 +53,26 @@ __constant__ int c_slot_leap[13][3] = {{-1, -1, -1}, {-1, -1, 0}, {-1, -1, 1}, {
 // NBS and TrirLeX x, y, z; TrirLeY y, x, z; TrirLeZ z, x, y, NBSConsultant.h:62-128), the key's
 // extent per axis, the number of zones per axis and, for the Leap consultant, its periodic axes.
 struct CellGrid {
-    int ord[3];                // axes from the most to the least significant
+    int mode;                  // key order: 0 x, y, z (NBS, TrirLeX); 1 y, x, z (TrirLeY); 2 z, x, y (TrirLeZ)
     uint64_t dim[3];           // key extent per axis (x, y, z)
     uint32_t ncel[3];          // zones per axis (x, y, z): the last zone is ncel - 1
     int leap;                  // 1: LeapConsultant's traversal
     int pbc[3], has_pbc;       // Leap: axes whose neighbours wrap (LeapConsultant.h:146-150)
 };
+// (fixed indices per mode: the zone coordinates stay in registers)
 __host__ __device__ inline uint64_t grid_key(const CellGrid& g, const uint64_t c[3]) {
-    return (c[g.ord[0]] * g.dim[g.ord[1]] + c[g.ord[1]]) * g.dim[g.ord[2]] + c[g.ord[2]];
+    if (g.mode == 1) return (c[1] * g.dim[0] + c[0]) * g.dim[2] + c[2];
+    if (g.mode == 2) return (c[2] * g.dim[0] + c[0]) * g.dim[1] + c[1];
+    return (c[0] * g.dim[1] + c[1]) * g.dim[2] + c[2];
 }
 __device__ inline void grid_cell(const CellGrid& g, uint64_t key, uint64_t c[3]) {
-    c[g.ord[2]] = key % g.dim[g.ord[2]];
-    const uint64_t rest = key / g.dim[g.ord[2]];
-    c[g.ord[1]] = rest % g.dim[g.ord[1]];
-    c[g.ord[0]] = rest / g.dim[g.ord[1]];
+    if (g.mode == 1) {
+        c[2] = key % g.dim[2]; key /= g.dim[2]; c[0] = key % g.dim[0]; c[1] = key / g.dim[0];
+    } else if (g.mode == 2) {
+        c[1] = key % g.dim[1]; key /= g.dim[1]; c[0] = key % g.dim[0]; c[2] = key / g.dim[0];
+    } else {
+        c[2] = key % g.dim[2]; key /= g.dim[2]; c[1] = key % g.dim[1]; c[0] = key / g.dim[1];
+    }
 }
 
 // order-preserving map of doubles to unsigned 64-bit integers (for exact atomic min/max)
@@ -536,6 +542,7 @@ __global__ void __launch_bounds__(TPB) k_pairs(uint32_t nloc, const uint32_t* __
     uint32_t jn = 0;
     // the cell whose zone coordinates are w (its index, or none)
     auto find_cell = [&](const uint64_t w[3]) -> uint32_t {
+#pragma unroll
         for (int a = 0; a < 3; ++a)
             if (w[a] >= g.dim[a]) return 0xffffffffu;
         const uint64_t nk = grid_key(g, w);
@@ -556,6 +563,7 @@ __global__ void __launch_bounds__(TPB) k_pairs(uint32_t nloc, const uint32_t* __
         jn = nglob;
     } else if (g.leap || s < NSLOT) {
         int d[3];
+#pragma unroll
         for (int a = 0; a < 3; ++a) d[a] = g.leap ? c_slot_leap[s][a] : c_slot[s][a];
         uint32_t c2 = 0xffffffffu;
         if (!((cc[0] == 0 && d[0] < 0) || (cc[1] == 0 && d[1] < 0) || (cc[2] == 0 && d[2] < 0))) {
@@ -568,6 +576,7 @@ __global__ void __launch_bounds__(TPB) k_pairs(uint32_t nloc, const uint32_t* __
             // _uint_t, and an image that names the opposite neighbour is skipped
             bool at_edge = false, dup = false, valid = true;
             uint64_t w[3];
+#pragma unroll
             for (int a = 0; a < 3; ++a) {
                 const uint32_t ia = (uint32_t)cc[a], mx = g.ncel[a] - 1u;
                 uint32_t wa = ia;
@@ -988,7 +997,7 @@ int Engine::rebuild(bool from_records) {
     const uint32_t nloc = n_ - (uint32_t)global_ids_.size();
     double rmax = 0.0;
     CellGrid g{};
-    g.ord[0] = 0; g.ord[1] = 1; g.ord[2] = 2;
+    g.mode = 0;
     if (leap_) {
         // LeapConsultant::Reset (LeapConsultant.cpp:108-195): the largest range of the local
         // objects, and the comparator from the spans between the 2 % and 98 % quantiles of the
@@ -1007,9 +1016,7 @@ int Engine::rebuild(bool from_records) {
             CK(cudaStreamSynchronize(stream_));
             span[a] = dbl_of(q[0]) - dbl_of(q[1]);
         }
-        const int mode = span[0] >= span[1] ? (span[0] >= span[2] ? 0 : 2) : (span[1] >= span[2] ? 1 : 2);
-        if (mode == 1) { g.ord[0] = 1; g.ord[1] = 0; g.ord[2] = 2; }        // TrirLeY
-        if (mode == 2) { g.ord[0] = 2; g.ord[1] = 0; g.ord[2] = 1; }        // TrirLeZ
+        g.mode = span[0] >= span[1] ? (span[0] >= span[2] ? 0 : 2) : (span[1] >= span[2] ? 1 : 2);
     } else if (red[7]) {
         rmax = tab_.models[host_.model_of[red[7] - 1]].range;              // the last local DO (:140)
     }
