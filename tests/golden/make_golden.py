@@ -24,7 +24,8 @@ sys.path[:0] = [ROOT, os.path.join(ROOT, "oracle")]
 from vedo_gb300 import scenes  # noqa: E402
 
 
-LEAP = {"leap_cluster_poly", "leap_box_lsd", "leap_periodic_lsd", "leap_periodic_wide"}
+LEAP = {"leap_cluster_poly", "leap_box_lsd", "leap_periodic_lsd", "leap_periodic_wide", "leap_wide_y",
+        "leap_column_z"}
 
 
 def cases():
@@ -50,6 +51,10 @@ def cases():
     yield "leap_box_lsd", scenes.lsd_box(n_side=5, steps=3000, vel_sigma=0.3, seed=11), 600, 10
     yield "leap_periodic_lsd", scenes.periodic_layer(solver="ISwBSDBF"), 400, 5
     yield "leap_periodic_wide", scenes.periodic_layer(nx=8, ny=6, layers=2, solver="ISwBSDBF", seed=22), 400, 5
+    # the widest spread along y, then along z: the TrirLeY and TrirLeZ zone orders
+    yield "leap_wide_y", scenes.periodic_layer(nx=3, ny=10, layers=2, solver="ISwBSDBF", seed=23), 300, 5
+    yield "leap_column_z", scenes.periodic_layer(nx=3, ny=3, layers=12, solver="ISwBSDBF", seed=24,
+                                                 drift=(2.0, 1.0)), 300, 5
     yield "periodic_far_lsd", scenes.periodic_layer(solver="ISwBSDBF", nx=3, ny=3, layers=2, seed=12,
                                                     outside=True), 200, 4
     yield "periodic_h", scenes.periodic_layer(solver="ISwH", periodic_y=False, floor_spin=40.0, side_walls=True,
