@@ -787,9 +787,20 @@ __device__ __forceinline__ void reduce_vmax(const TickArgs& a, float2 v) {
 }
 __device__ __forceinline__ float2 fmax2(float2 a, float2 b) { return make_float2(fmaxf(a.x, b.x), fmaxf(a.y, b.y)); }
 
+// Programmatic dependent launch (sm_90 and later): the per-step kernels are launched so that the
+// next one may be scheduled while this one drains.  Each first waits until the grid before it
+// has finished and its writes are visible (a no-op for a plain launch), then lets the next grid
+// launch; that one is released only once every block of this grid has started, so its waiting
+// blocks never hold resources this grid still needs.
+__device__ __forceinline__ void step_order() {
+    asm volatile("griddepcontrol.wait;" ::: "memory");
+    asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+}
+
 // The full tick, one thread per sphere.
 template <int LAW, bool XS>
 __global__ void __launch_bounds__(TPB) k_tick(TickArgs a) {
+    step_order();
     const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
     float2 vmax_local = make_float2(0.0f, 0.0f);
     if (held_step(a)) {                          // the same value for every thread of the launch
@@ -804,6 +815,7 @@ __global__ void __launch_bounds__(TPB) k_tick(TickArgs a) {
 // spheres the light kernel deferred (none in a held step).
 template <int LAW, bool XS>
 __global__ void __launch_bounds__(TPB) k_tick_work(TickArgs a) {
+    step_order();
     float2 vmax_local = make_float2(0.0f, 0.0f);
     if (!held_step(a)) {
         const uint32_t nw = *a.nwork;
@@ -820,6 +832,7 @@ __global__ void __launch_bounds__(TPB) k_tick_work(TickArgs a) {
 // the sphere with the same operations, so results are those of the single tick.
 template <bool XS>
 __global__ void __launch_bounds__(TPB, 6) k_tick_light(TickArgs a) {   // 6 blocks of 256 per SM (40 registers; the rare walk spills a little)
+    step_order();
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     const bool hold = held_step(a);
     float2 vmax_local = make_float2(0.0f, 0.0f);
@@ -939,6 +952,7 @@ __global__ void k_walls(uint32_t nglob, const uint32_t* __restrict__ glob, const
                         float pos_eps, const unsigned* __restrict__ wall_speed_bits,
                         const double4_32a* __restrict__ wrot,
                         unsigned* __restrict__ held, float4* __restrict__ wall32, unsigned* __restrict__ nwork) {
+    step_order();
     const uint32_t q = blockIdx.x * blockDim.x + threadIdx.x;
     const float drel = disp_in[0], dabs = disp_in[1], dw = disp_in[2];
     const bool hold = list_spent(drel, dabs, dw, skin, skin_w);
@@ -1873,6 +1887,7 @@ private:
     }
     int rebuild();
     void launch_step(bool write_imp);
+    cudaError_t launch_err_ = cudaSuccess;   // the first failed launch of the step kernels
     int step_chunk(uint32_t chunk, bool imp_last, float* use_after);
     int autotune(uint32_t max_steps, uint32_t* taken);
     void set_skin(float frac);
@@ -2613,6 +2628,23 @@ int MixedEngine::rebuild() {
 
 // One time step's launches: the fused tick, the wall impulse sums on the last step of a call,
 // and the wall kernel (wall motion and the displacement bound after the step).
+// A per-step kernel launch; `dep`: with programmatic dependent launch (the kernel orders itself
+// after the previous one with step_order()).
+template <typename... P, typename... A>
+static cudaError_t step_launch(bool dep, void (*k)(P...), unsigned grid, unsigned block, cudaStream_t s, A... args) {
+    cudaLaunchConfig_t cfg{};
+    cfg.gridDim = dim3(grid);
+    cfg.blockDim = dim3(block);
+    cfg.dynamicSmemBytes = 0;
+    cfg.stream = s;
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    at[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = at;
+    cfg.numAttrs = dep ? 1 : 0;
+    return cudaLaunchKernelEx(&cfg, k, args...);
+}
+
 void MixedEngine::launch_step(bool write_imp) {
     TickArgs a = args(write_imp);
     const unsigned nb = (unsigned)((n_ + tpb_ - 1) / tpb_);
@@ -2624,19 +2656,23 @@ void MixedEngine::launch_step(bool write_imp) {
         // them as event nodes
         cudaEventRecordWithFlags(pe[0], stream_, ev_flags_);
     }
+    // dependent launches between the step's kernels, except where event records sit between them
+    const bool dep = pe == nullptr;
+    auto note = [&](cudaError_t e) {
+        if (e != cudaSuccess && launch_err_ == cudaSuccess) launch_err_ = e;
+    };
     unsigned nb_full = nb;
     if (split_tick_) {              // light tick over all spheres, then the full tick over the deferred
         // (the worklist count is zeroed by k_walls at the end of every step)
-        if (xs_stored_) k_tick_light<true><<<nblk(n_), TPB, 0, stream_>>>(a);
-        else k_tick_light<false><<<nblk(n_), TPB, 0, stream_>>>(a);
+        note(step_launch(dep, xs_stored_ ? k_tick_light<true> : k_tick_light<false>, nblk(n_), TPB, stream_, a));
         ++launches_;
         // the full tick at its residency (128 registers: 16 warps per SM) strides over the worklist
         nb_full = std::min<unsigned>(nb, (unsigned)sms_ * 512u / (unsigned)tpb_);
     }
 #define VEDO_TICK(L)                                                                                        \
-    (split_tick_ ? (xs_stored_ ? k_tick_work<L, true><<<nb_full, tpb_, 0, stream_>>>(a)                     \
-                               : k_tick_work<L, false><<<nb_full, tpb_, 0, stream_>>>(a))                   \
-                 : (xs_stored_ ? k_tick<L, true><<<nb, tpb_, 0, stream_>>>(a) : k_tick<L, false><<<nb, tpb_, 0, stream_>>>(a)))
+    note(step_launch(dep, split_tick_ ? (xs_stored_ ? k_tick_work<L, true> : k_tick_work<L, false>)          \
+                                      : (xs_stored_ ? k_tick<L, true> : k_tick<L, false>),                   \
+                     split_tick_ ? nb_full : nb, (unsigned)tpb_, stream_, a))
     switch (law_) {
     case IS_BSDBF: VEDO_TICK(IS_BSDBF); break;
     case IS_BTSDBF: VEDO_TICK(IS_BTSDBF); break;
@@ -2661,10 +2697,13 @@ void MixedEngine::launch_step(bool write_imp) {
                                                   d_scene_of_, d_gfield_, d_imp_, d_aimp_);
         ++launches_;
     }
-    k_walls<<<nblk(std::max<size_t>(glob_.size(), 1)), TPB, 0, stream_>>>(
-        (uint32_t)glob_.size(), d_glob_, d_model_of_, d_models_, d_scenes_, d_scene_of_, a.xA, a.xB, d_v64_, d_w64_,
-        a.v32A, a.v32B, a.w32A, a.w32B, d_ox_, d_oz_, dt_max_, d_red_ + 8, d_red_ + 2,
-        d_disp_ + 4 * cur_, d_disp_ + 4 * (cur_ ^ 1), skin_min_, WALL_SKIN * skin_min_, pos_eps_, d_red_ + 12, d_wrot_, d_red_ + 11, d_wall32_, d_red_ + 14);
+    note(step_launch(dep, k_walls, nblk(std::max<size_t>(glob_.size(), 1)), TPB, stream_,
+        (uint32_t)glob_.size(), (const uint32_t*)d_glob_, (const uint32_t*)d_model_of_, (const ModelDev*)d_models_,
+        (const SceneDev*)d_scenes_, (const uint32_t*)d_scene_of_, (const double4_32a*)a.xA, a.xB,
+        (const double4_32a*)d_v64_, (const double4_32a*)d_w64_, (const float4*)a.v32A, a.v32B, (const float4*)a.w32A,
+        a.w32B, d_ox_, d_oz_, dt_max_, d_red_ + 8, d_red_ + 2, (const float*)(d_disp_ + 4 * cur_),
+        d_disp_ + 4 * (cur_ ^ 1), skin_min_, WALL_SKIN * skin_min_, pos_eps_, (const unsigned*)(d_red_ + 12),
+        (const double4_32a*)d_wrot_, d_red_ + 11, d_wall32_, d_red_ + 14));
     ++launches_;
     if (pe) cudaEventRecordWithFlags(pe[2], stream_, ev_flags_);
     cur_ ^= 1;
@@ -2708,6 +2747,11 @@ int MixedEngine::step_chunk(uint32_t chunk, bool imp_last, float* use_after) {
         if (chunk & 1) cur_ ^= 1;
     } else {
         for (uint32_t k = 0; k < chunk; ++k) launch_step(imp_last && k + 1 == chunk);
+    }
+    if (launch_err_ != cudaSuccess) {
+        const cudaError_t le = launch_err_;
+        launch_err_ = cudaSuccess;
+        return cuda_fail(le, "kernel launch");
     }
     float dd[4] = {0.0f, 0.0f, 0.0f, 0.0f};
     unsigned held = 0;
