@@ -25,7 +25,7 @@ from vedo_gb300 import scenes  # noqa: E402
 
 
 LEAP = {"leap_cluster_poly", "leap_box_lsd", "leap_periodic_lsd", "leap_periodic_wide", "leap_wide_y",
-        "leap_column_z"}
+        "leap_column_z", "leap_single"}
 
 
 def cases():
@@ -55,6 +55,8 @@ def cases():
     yield "leap_wide_y", scenes.periodic_layer(nx=3, ny=10, layers=2, solver="ISwBSDBF", seed=23), 300, 5
     yield "leap_column_z", scenes.periodic_layer(nx=3, ny=3, layers=12, solver="ISwBSDBF", seed=24,
                                                  drift=(2.0, 1.0)), 300, 5
+    # one local sphere in a box: the 98 % quantile's index is negative before truncation
+    yield "leap_single", scenes.cluster(n=1, solver="ISwBSDBF", steps=300, seed=3, vel_sigma=2.0), 200, 5
     yield "periodic_far_lsd", scenes.periodic_layer(solver="ISwBSDBF", nx=3, ny=3, layers=2, seed=12,
                                                     outside=True), 200, 4
     yield "periodic_h", scenes.periodic_layer(solver="ISwH", periodic_y=False, floor_spin=40.0, side_walls=True,
