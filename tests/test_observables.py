@@ -61,3 +61,17 @@ def test_vtu_conversion_matches_reference_writer(path, engine_lib, tmp_path):
     ref = g["world_vtk"].tobytes().decode()
     assert mask_granular(ours) == mask_granular(ref)
     assert np.all(vtk_array(ours, "GranularTemperatureV") == 0.0)
+
+
+def test_vtu_from_xml_equals_vtu_from_ido(engine_lib, tmp_path):
+    """A scene read from DOWorldSchema XML writes the same VTK file as the same scene read from its
+    IDO file (the conversion runs on the host)."""
+    g = np.load(FIXTURES[0])
+    ido = tmp_path / "s.ido"
+    ido.write_bytes(g["ido"].tobytes())
+    xml = tmp_path / "s.xml"
+    engine_lib.convert_scene(str(ido), str(xml))
+    a, b = tmp_path / "a.vtu", tmp_path / "b.vtu"
+    engine_lib.convert_scene(str(ido), str(a))
+    engine_lib.convert_scene(str(xml), str(b))
+    assert a.read_text() == b.read_text()

@@ -196,3 +196,15 @@ def test_holed_plate_model_analysis():
     bad = DOModel("H", "W", FIXED, GLOBAL, 7800.0, 1.0, QUASI_PLATE_WITH_CIRCULAR_HOLE, (0.1, 0.01, 0.2, 0.04, 0.02, 0.0))
     with pytest.raises(ValueError):
         bad.analysis()
+
+
+def test_leap_with_a_zone_of_interest_is_refused(port_lib):
+    """The Leap consultant erases objects outside the zone at every reset (LeapConsultant.cpp:67),
+    which neither the oracle nor the engine does: the combination is refused, not run wrongly."""
+    from oracle import PortWorld
+    from vedo_gb300.scene import Boundary
+    sc = scenes.cluster(n=27, seed=2)
+    sc.sp.zoi = Boundary(switch=(False, False, True), lower=(0.0, 0.0, -1.0), upper=(0.0, 0.0, 1.0))
+    with pytest.raises(Exception, match="zone of interest"):
+        PortWorld(sc, consultant="leap")
+    PortWorld(sc, consultant="nbs")                 # the NBS consultant cleans up once, at the start
