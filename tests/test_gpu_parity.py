@@ -359,3 +359,15 @@ def test_leap_consultant_at_size_bitexact(which, engine_lib, port_lib):
     assert len(nbs.interactions()["first"]) != len(e.interactions()["first"]) or which == "box"
     e.close()
     nbs.close()
+
+
+def test_leap_self_pairs_are_refused_by_the_engine(engine_lib):
+    """A periodic axis one Leap zone wide gives the reference's list pairs (i, i): the engine refuses
+    the scene with VEDO_ERR_UNSUPPORTED_MODEL, as the oracle does, instead of building an
+    interaction of a sphere with itself."""
+    sc = scenes.periodic_layer(nx=6, ny=2, layers=3, solver="ISwBSDBF", seed=32, periodic_y=True,
+                               drift=(-0.74, -1.06))
+    with pytest.raises(engine_lib.EngineError) as ex:
+        engine_lib.GpuEngine(sc, up_iact=4, consultant="leap")
+    assert ex.value.code == 3
+    engine_lib.GpuEngine(sc, up_iact=4).close()     # the NBS list of the same layer is fine

@@ -208,3 +208,51 @@ def test_leap_with_a_zone_of_interest_is_refused(port_lib):
     with pytest.raises(Exception, match="zone of interest"):
         PortWorld(sc, consultant="leap")
     PortWorld(sc, consultant="nbs")                 # the NBS consultant cleans up once, at the start
+
+
+def _one_zone_periodic_layer():
+    """A layer whose periodic y axis is one Leap zone wide (two rows of spheres)."""
+    return scenes.periodic_layer(nx=6, ny=2, layers=3, solver="ISwBSDBF", seed=32, periodic_y=True,
+                                 drift=(-0.74, -1.06))
+
+
+def test_leap_self_pairs_are_refused(port_lib):
+    """With a periodic axis one zone wide, the reference's Leap consultant pairs a zone with its own
+    periodic image, so its list holds pairs (i, i); CreateInteraction drops them (Assembler.cpp:27-30)
+    and the pair table no longer lines up with the interactions.  The oracle refuses such a list."""
+    import oracle
+    from oracle import PortWorld
+    sc = _one_zone_periodic_layer()
+    with pytest.raises(ValueError, match="unsupported interaction"):
+        PortWorld(sc, up_iact=4, consultant="leap")
+    if oracle.ref_available() or oracle.build_ref() is not None:
+        from oracle import RefWorld
+        a, b = RefWorld(sc, up_iact=4, consultant="leap").candidates()
+        assert np.any(a == b)
+
+
+@pytest.mark.parametrize("seed", [31, 33, 34, 35])
+def test_leap_oracle_equals_the_reference_on_random_layouts(seed, port_lib):
+    """Seeded layouts (zone counts, periodic axes, drift) run by the reference's own Leap consultant
+    and by the oracle: candidate lists element for element at the start and after 120 steps,
+    states bit for bit.  Needs the reference compiled from its sources (skipped elsewhere)."""
+    import oracle
+    if not oracle.ref_available() and oracle.build_ref() is None:
+        pytest.skip("reference sources not available")
+    from oracle import PortWorld, RefWorld
+    rng = np.random.default_rng(seed)
+    # (at least three rows on each axis: a periodic axis one zone wide makes self pairs, above)
+    sc = scenes.periodic_layer(nx=int(rng.integers(3, 7)), ny=int(rng.integers(3, 7)), layers=int(rng.integers(1, 4)),
+                               solver="ISwBSDBF", seed=seed, periodic_y=bool(rng.integers(0, 2)),
+                               drift=(float(rng.uniform(-3, 3)), float(rng.uniform(-3, 3))))
+    r, p = RefWorld(sc, up_iact=4, consultant="leap"), PortWorld(sc, up_iact=4, consultant="leap")
+    for _ in range(2):
+        ra, rb = r.candidates()
+        pa, pb = p.candidates()
+        assert np.array_equal(ra, pa) and np.array_equal(rb, pb)
+        r.run(60)
+        p.run(60)
+    a, b = r.state(), p.state()
+    for k in ("position", "velocity", "angular_velocity"):
+        np.testing.assert_array_equal(a[k], b[k], err_msg=k)
+    r.close()

@@ -658,7 +658,10 @@ __global__ void __launch_bounds__(TPB) k_setup(uint32_t np, const uint32_t* __re
     const ModelDev& A = models[ma];
     const ModelDev& B = models[mb];
     uint32_t sl = a, ms = b;
-    bool bad = (B.density < 0.0 || A.density < 0.0) || (B.density == 0.0 && A.density == 0.0);
+    // no interaction of an object with itself (Assembler.cpp:27-30): the Leap consultant lists such
+    // pairs when a periodic axis is one zone wide, and the reference then drops them, leaving its
+    // pair table and interactions misaligned; here the list is refused
+    bool bad = a == b || (B.density < 0.0 || A.density < 0.0) || (B.density == 0.0 && A.density == 0.0);
     if (A.shape > B.shape) { sl = b; ms = a; }
     else if (A.shape < B.shape) { sl = a; ms = b; }
     else if (A.density == 0.0) { sl = b; ms = a; }
