@@ -124,7 +124,8 @@ typedef struct vedo_scene_desc {
 
 /* ---- engine options ---------------------------------------------------- */
 /* FP64: the drop-in; every FP64 operation in the reference's order, results bit-identical
- *       to the reference for the linear laws (see the design doc of the engine).
+ *       to the reference for the linear laws (Hertz-family laws and orbital walls within the
+ *       last-ulp differences of pow, sin and cos).
  * MIXED: contact forces in FP32 in pair-local coordinates, FP64 positions, velocities and
  *       overlap numerators, FP32 compensated sums per object; contact sets identical to
  *       FP64 at identical positions; sphere orientations are not integrated. */
