@@ -4,7 +4,7 @@
   restatement of the reference step (dem_oracle.c).  It builds on any host.
 * :class:`RefWorld` drives ``oracle/_ref/libvedoref.so``, the reference's own
   CPU code compiled from its sources by ``make -C oracle ref``.  Only available
-  where the reference sources are (never on the GPU host).
+  where the reference sources are.
 
 Both expose the same methods so that tests can compare them with each other
 and with the GPU engine.  Only tests/, __graft_entry__.smoke() and the CPU
