@@ -3,7 +3,10 @@
 Hertz drum (radii lognormal median 1 mm, sigma_log 0.2, clipped to [0.5, 2] mm, 32 classes;
 E = 70 GPa, nu = 0.25, e = 0.7, mu = 0.4 via the frictional Hertz-family law ISwH;
 drum R = 0.15 m, L = 0.3 m, polygon shell of 64 fixed plates, end plates at 30 rpm;
-dt = 5e-7 s).  Synthetic seeded scene (vedo_gb300.scenes.hertz_drum).
+dt = 5e-7 s; filled by random sequential placement).  Synthetic seeded scene
+(vedo_gb300.scenes.hertz_drum), settled on the GPU before the timed window
+(vedo_gb300.workloads.settled_drum: 300,000 steps of settling under gravity, untimed) so that
+the window times the contact step of a resting, rotating bed, not free fall.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
 
@@ -14,7 +17,7 @@ stepped, read back, every `--sync` steps).  Under torchrun (N > 1) every rank ru
 independent replica of the scene (no collective on the data path) and `value` is the
 particle-steps of all ranks over the slowest rank's time.  `--impl reference` times the
 reference algorithm on the host cores (the C restatement of the reference step; the
-reference's own build cannot run on this host).
+reference's own build cannot run on this host) on the same settled state.
 """
 import argparse
 import json
@@ -60,6 +63,12 @@ def parse():
     ap.add_argument("--no-dense", action="store_true")
     ap.add_argument("--no-batch", action="store_true")
     ap.add_argument("--no-serve", action="store_true")
+    ap.add_argument("--no-c1", action="store_true")
+    ap.add_argument("--settle-steps", type=int, default=300_000, help="drum settling steps before the window")
+    ap.add_argument("--c1-cpu-steps", type=int, default=20_000, help="C1 CPU baseline steps (full run: 20000)")
+    ap.add_argument("--cpu-job", default=None, help=argparse.SUPPRESS)
+    ap.add_argument("--cpu-out", default=None, help=argparse.SUPPRESS)
+    ap.add_argument("--cpu-scene", default=None, help=argparse.SUPPRESS)
     return ap.parse_args()
 
 
@@ -190,6 +199,46 @@ def cpu_rate(scene, up_iact, steps):
     return scene_particles(scene) * steps / (t1 - t0), t1 - t0
 
 
+def cpu_job(args):
+    """A CPU baseline in its own process (so that it runs beside the GPU sections): the C
+    restatement of the reference step over `--cpu-scene` (an .ido path, or "c1" for the
+    8,000-sphere box) for `--steps` steps; writes its rate to `--cpu-out`."""
+    from vedo_gb300 import scenes
+    from vedo_gb300.scene import Scene
+    if args.cpu_scene == "c1":
+        sc = scenes.lsd_box(steps=20000)
+    else:
+        sc = Scene.from_ido(args.cpu_scene)
+    rate, secs = cpu_rate(sc, args.up_iact, args.steps)
+    with open(args.cpu_out, "w") as f:
+        json.dump({"value": rate, "seconds": secs, "steps": args.steps, "particles": scene_particles(sc)}, f)
+
+
+class CpuJob:
+    """A cpu_job subprocess; result() waits for it and returns its JSON (None if it failed)."""
+    def __init__(self, scene_arg, steps, up_iact):
+        fd, self.out = tempfile.mkstemp(suffix=".json")
+        os.close(fd)
+        self.proc = subprocess.Popen([sys.executable, os.path.abspath(__file__), "--cpu-job", "1", "--cpu-scene",
+                                      scene_arg, "--steps", str(steps), "--up-iact", str(up_iact), "--cpu-out",
+                                      self.out], stdout=subprocess.DEVNULL, stderr=subprocess.PIPE)
+
+    def result(self, timeout=1800):
+        try:
+            _, err = self.proc.communicate(timeout=timeout)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+            return None
+        try:
+            with open(self.out) as f:
+                return json.load(f)
+        except (OSError, ValueError):
+            sys.stderr.write((err or b"").decode()[-2000:])
+            return None
+        finally:
+            os.unlink(self.out)
+
+
 def scene_particles(scene):
     from vedo_gb300.scene import SPHERE
     sph = [k for k, m in enumerate(scene.models) if m.shape == SPHERE]
@@ -197,11 +246,31 @@ def scene_particles(scene):
     return int(np.isin(scene.model_index, sph).sum())
 
 
+def settled_drum(args, dist, collective=True):
+    """The settled 1M-sphere drum of this rank (built and settled on its GPU once, then cached).
+    collective: every rank calls it (the build runs once per host, behind a barrier)."""
+    import torch
+    from vedo_gb300 import build as vbuild
+    from vedo_gb300 import workloads
+    if dist.local == 0 or dist.world == 1:
+        vbuild.build()
+    if collective:
+        dist.barrier()
+    vbuild.build()
+    torch.cuda.set_device(dist.local)
+    return workloads.settled_drum(n=args.n, seed=2024 + dist.rank, settle_steps=args.settle_steps,
+                                  device=dist.local)
+
+
 def reference_arm(args, dist):
+    """The C restatement of the reference step (single thread: the reference's step is
+    sequential) on the same settled drum as the GPU arm.  The settled state is made by the GPU
+    engine (untimed input preparation, cached on this host); the timed steps are CPU only."""
     if dist.rank != 0:
         return
-    from vedo_gb300 import scenes
-    scene = scenes.hertz_drum(n=args.n)
+    path, info = settled_drum(args, dist, collective=False)
+    from vedo_gb300.scene import Scene
+    scene = Scene.from_ido(path)
     n = scene_particles(scene)
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import oracle
@@ -221,12 +290,13 @@ def reference_arm(args, dist):
     value = n * k / dt
     emit({"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus, "steps": k, "warmup": args.warmup,
           "ms_per_step": 1e3 * dt / k, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-          "dtype": "f64", "data": "synthetic (seeded hertz_drum scene)", "impl": "reference",
-          "config": {"workload": WORKLOAD, "particles": n, "up_iact": args.up_iact,
-                     "steps_timed": k, "steps_requested": args.steps},
+          "dtype": "f64", "data": "synthetic (seeded hertz_drum scene, settled)", "impl": "reference",
+          "config": {"workload": WORKLOAD, "particles": n, "up_iact": args.up_iact, "steps_timed": k,
+                     "steps_requested": args.steps, "settle": info},
           "cpu_baseline": {"value": value, "unit": UNIT, "cores": 1, "kind": "port",
-                           "sample": f"{k} full time steps of the {n}-sphere drum after {args.warmup} warm-up "
-                                     f"steps, single thread (the reference step is sequential)"},
+                           "sample": f"{k} full time steps of the settled {n}-sphere drum ({info.get('contacts')} "
+                                     f"contacts) after {args.warmup} warm-up steps, single thread (the reference "
+                                     f"step is sequential)"},
           "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}})
 
 
@@ -254,40 +324,35 @@ def time_form(eng, args, dist, clocks=None):
 def ours(args, dist):
     import numpy as np
     import torch
-    from vedo_gb300 import build as vbuild
-    if dist.local == 0 or dist.world == 1:
-        vbuild.build()
-    dist.barrier()
-    vbuild.build()
-    from vedo_gb300 import scenes
     from vedo_gb300.engine import GpuEngine
+    from vedo_gb300.scene import Scene
 
     dev = dist.local
-    torch.cuda.set_device(dev)
-    scene = scenes.hertz_drum(n=args.n, seed=2024 + dist.rank)
+    # C1's full-run CPU baseline runs beside the GPU sections (single thread, its own process)
+    c1_cpu = CpuJob("c1", args.c1_cpu_steps, 20) if (dist.rank == 0 and dist.world == 1 and not args.no_c1
+                                                     and not args.no_cpu_baseline) else None
+    path, settle_info = settled_drum(args, dist)
+    scene = Scene.from_ido(path)
     n = scene_particles(scene)
-    cpu = None
+    cpu_job_c2 = None
     if dist.rank == 0 and dist.world == 1 and not args.no_cpu_baseline:
-        rate, secs = cpu_rate(scene, args.up_iact, args.cpu_sample_steps)
-        cpu = {"value": rate, "unit": UNIT, "cores": 1, "kind": "port",
-               "sample": f"first {args.cpu_sample_steps} time steps (one candidate-list rebuild) of the same "
-                         f"{n}-sphere drum, single thread, {secs:.1f} s"}
+        cpu_job_c2 = CpuJob(path, args.cpu_sample_steps, args.up_iact)
     total_particles = dist.reduce(float(n), "sum")
 
-    # plain FP64 form (the drop-in): same scene, same window
-    f64 = GpuEngine(scene, up_iact=args.up_iact, device=dev)
+    # plain FP64 form (the drop-in): same settled state, same window
+    f64 = GpuEngine(path, up_iact=args.up_iact, device=dev)
     t64, l64, _ = time_form(f64, args, dist)
     fp64_value = total_particles * args.steps / (t64 * 1e-3)
-    it64 = f64.interactions()
-    n_active = int(it64["active"].sum())
 
     # mixed form (the headline): FP32 pair forces, FP64 integration, compensated sums; the first
-    # TUNE_STEPS steps choose the tick block, skin and cell scale (results do not depend on them)
-    eng = GpuEngine(scene, up_iact=args.up_iact, device=dev, precision=1, autotune=True)
+    # TUNE_STEPS steps choose the tick shape, skin and cell scale (results do not depend on them)
+    eng = GpuEngine(path, up_iact=args.up_iact, device=dev, precision=1, autotune=True)
     eng.run(TUNE_STEPS)
     clocks = Clocks(dev)
     t_ms, launches, clocks_rec = time_form(eng, args, dist, clocks)
     value = total_particles * args.steps / (t_ms * 1e-3)
+    o_mx = eng.observables()
+    n_active = int(o_mx[9])                       # active contacts at the end of the window
 
     # error of the mixed form against the FP64 engine on this window: end-of-window energy and
     # the impulses of one step from the FP64 engine's state (restarted through an .ido so both
@@ -297,13 +362,14 @@ def ours(args, dist):
     e64, emx = o64[0] + o64[1] + o64[2], omx[0] + omx[1] + omx[2]
     errors = {"energy_rel": abs(e64 - emx) / max(abs(e64), 1e-300),
               "kinetic_rel": abs(o64[1] - omx[1]) / max(abs(o64[1]), 1e-300),
-              "contacts_fp64": int(o64[9]), "contacts_mixed": int(omx[9])}
+              "contacts_fp64": int(o64[9]), "contacts_mixed": int(omx[9]),
+              "after_steps": TUNE_STEPS + args.warmup + args.steps}
     if args.n <= 2_000_000 and not args.no_profile_pass:
         with tempfile.TemporaryDirectory() as td:
-            path = os.path.join(td, "w.ido")
-            f64.write_ido(path)
-            a = GpuEngine(path, up_iact=args.up_iact, device=dev)
-            b = GpuEngine(path, up_iact=args.up_iact, device=dev, precision=1)
+            p2 = os.path.join(td, "w.ido")
+            f64.write_ido(p2)
+            a = GpuEngine(p2, up_iact=args.up_iact, device=dev)
+            b = GpuEngine(p2, up_iact=args.up_iact, device=dev, precision=1)
             a.run(1)
             b.run(1)
             sa, sb = a.state(("impact", "angular_impact")), b.state(("impact", "angular_impact"))
@@ -314,6 +380,7 @@ def ours(args, dist):
                 d = sa[k] - sb[k]
                 errors[f"step_{k}_rel_l2"] = float(np.linalg.norm(d) / max(np.linalg.norm(sa[k]), 1e-300))
             errors["contact_set_identical"] = A == B
+            errors["contacts"] = len(A)
             a.close()
             b.close()
     f64.close()
@@ -359,15 +426,16 @@ def ours(args, dist):
     if kern and kern["pair_ms"] > 0:
         t_tick = kern["pair_ms"] / kern["steps"]            # average duration of one tick launch
         ach = b_alg * n / (t_tick * 1e-3) / 1e9
-        traffic = ncu_traffic("k_tick_light_drum1M_dram.md") if n == 1_000_000 else None
+        traffic = ncu_traffic("k_tick_drum1M_settled_dram.md") if n == 1_000_000 else None
         tuned = eng.tuning()
-        roof = {"kernel": ("k_tick_light + k_tick (split tick: prefilter walk and integration at high occupancy, "
-                           "the full fused tick over the spheres with a pair on the exact path)")
-                if tuned.get("split_tick") else "k_tick (fused narrow phase + forces + integration, one launch per step)",
+        roof = {"kernel": ("k_tick_light + k_tick_work (split tick: prefilter walk and integration at high "
+                           "occupancy, the warp-group contact tick over the spheres with a pair on the exact path)")
+                if tuned.get("split_tick") else "k_tick (warp-group contact tick: narrow phase + forces + "
+                                                "integration, one launch per step)",
                 "bound": "hbm", "achieved": ach, "peak": peak, "unit": "GB/s", "frac": ach / peak,
                 "peak_source": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)" if peak_kind == "measured" else peak_kind,
                 "traffic": traffic,
-                "traffic_source": "profiles/k_tick_light_drum1M_dram.md (ncu, the same workload at full size)"
+                "traffic_source": "profiles/k_tick_drum1M_settled_dram.md (ncu, the same workload at full size)"
                 if traffic else None,
                 "dram_frac": traffic / (t_tick * 1e-3) / 1e9 / peak if traffic else None,
                 "tick_ms": t_tick, "walls_ms": kern["object_ms"] / kern["steps"],
@@ -378,8 +446,10 @@ def ours(args, dist):
     res = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": dist.world, "steps": args.steps,
            "warmup": args.warmup, "ms_per_step": t_ms / args.steps, "higher_is_better": True, "scaling": "weak",
            "vs_baseline": None, "dtype": "f32 forces + f64 state (mixed)",
-           "data": "synthetic (seeded hertz_drum scene, no dataset)",
+           "data": "synthetic (seeded hertz_drum scene filled by random sequential placement and settled on the "
+                   "GPU, no dataset)",
            "config": {"workload": WORKLOAD, "particles_per_gpu": n, "objects_per_gpu": eng.n,
+                      "settle": settle_info,
                       "form": "mixed (FP32 pair-local forces, FP64 overlap numerator and integration, "
                               "Kahan sums; sphere orientation not integrated)",
                       "up_iact_fp64": args.up_iact, "active_contacts": n_active, "z_pp": z_pp,
@@ -387,8 +457,10 @@ def ours(args, dist):
                       "l2": "working set larger than L2 (state + lists > 129 MB)",
                       "parallelism": f"replicas x{dist.world}",
                       "tuning": eng.tuning(),
-                      "window": f"steps {TUNE_STEPS + args.warmup}..{TUNE_STEPS + args.warmup + args.steps} of the "
-                                f"configured 10000-step run (FP64 form: steps {args.warmup}..{args.warmup + args.steps})"},
+                      "window": f"steps {TUNE_STEPS + args.warmup}..{TUNE_STEPS + args.warmup + args.steps} after "
+                                f"{args.settle_steps} settling steps (FP64 form: steps "
+                                f"{args.warmup}..{args.warmup + args.steps} after them); z_pp counted at the "
+                                f"window's end"},
            "fp64": {"value": fp64_value, "ms_per_step": t64 / args.steps, "gpu_launches": l64,
                     "form": "plain FP64 drop-in, bit-exact operation order"},
            "mixed_over_fp64": value / fp64_value,
@@ -399,7 +471,7 @@ def ours(args, dist):
                    "note": f"vedo_gpu_set_state + vedo_gpu_run({args.sync}) + vedo_gpu_get_state of position, "
                            f"velocity and angular velocity (FP64) of every object per {args.sync} steps, pinned "
                            f"host buffers, mixed form"},
-           "roofline": roof, "cpu_baseline": cpu}
+           "roofline": roof, "cpu_baseline": None}
     eng.close()
     if not args.no_batch:
         res["batch"] = batch_workload(args, dist, dev)
@@ -407,10 +479,54 @@ def ours(args, dist):
         res["bed"] = bed_workload(args, dist, dev)
     if not args.no_dense:
         res["dense"] = dense_workload(args, dist, dev)
+    if not args.no_c1:
+        res["c1"] = c1_workload(args, dist, dev, c1_cpu)
     if not args.no_serve and dist.world == 1:
         res["serving"] = serving_workload(args, dev)
+    if cpu_job_c2:
+        r = cpu_job_c2.result()
+        if r:
+            res["cpu_baseline"] = {"value": r["value"], "unit": UNIT, "cores": 1, "kind": "port",
+                                   "sample": f"{r['steps']} time steps of the same settled {n}-sphere drum "
+                                             f"(the state the window starts from), single thread, "
+                                             f"{r['seconds']:.1f} s, run beside the GPU sections"}
     if dist.rank == 0:
         emit(res)
+
+
+def c1_workload(args, dist, dev, cpu_job_c1):
+    """C1: the 8,000-sphere linear spring-dashpot box, the whole 20,000-step run in the plain
+    FP64 form (bit for bit the reference's) and in the mixed form, beside the C restatement of
+    the reference's step over the same full run on one host core.  About 2 MB of state: the
+    step lives in L2 and is bound by launch latency, so its roofline fraction means nothing."""
+    import torch
+    from vedo_gb300 import scenes
+    from vedo_gb300.engine import GpuEngine
+    sc = scenes.lsd_box(steps=20000)
+    n = scene_particles(sc)
+    out = {"workload": "lsd_box_8k (20,000 steps, dt 1e-6 s, candidate list every 20 steps)", "particles": n}
+    for name, prec in (("fp64", 0), ("mixed", 1)):
+        e = GpuEngine(sc, up_iact=20, device=dev, precision=prec)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        e.run(20000)
+        wall = time.perf_counter() - t0
+        prof = e.last_run_profile()
+        o = e.observables()
+        out[name] = {"value": n * 20000 / (prof["total_ms"] * 1e-3), "unit": UNIT,
+                     "ms_per_step": prof["total_ms"] / 20000, "wall_s": wall, "gpu_launches": prof["launches"],
+                     "kinetic_energy_end": float(o[1] + o[2]), "contacts_end": int(o[9])}
+        e.close()
+    if cpu_job_c1:
+        r = cpu_job_c1.result()
+        if r:
+            out["cpu_baseline"] = {"value": r["value"], "unit": UNIT, "cores": 1, "kind": "port",
+                                   "sample": f"{r['steps']} steps of the same scene (the full run), single thread, "
+                                             f"{r['seconds']:.1f} s"}
+            out["fp64_over_cpu"] = out["fp64"]["value"] / r["value"]
+    out["note"] = ("L2-resident (state about 2 MB) and launch/latency-bound: one step is a few microseconds of "
+                   "kernels, so the rate measures launch overhead, not HBM")
+    return out
 
 
 def ncu_traffic(name):
@@ -654,6 +770,9 @@ def serving_workload(args, dev):
 
 def main():
     args = parse()
+    if args.cpu_job:
+        cpu_job(args)
+        return
     dist = Dist()
     try:
         if args.impl == "reference":

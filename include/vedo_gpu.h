@@ -55,6 +55,13 @@ enum {
 /* ---- enums mirrored from DOModel.h:25-27 (C++11 build) ------------------ */
 enum { VEDO_SHAPE_SPHERE = 1, VEDO_SHAPE_QUASI_CYLINDER = 6, VEDO_SHAPE_QUASI_PLATE = 7,
        VEDO_SHAPE_QUASI_PLATE_WITH_CIRCULAR_HOLE = 8 };
+/* No counterpart in the reference (its QuasiCylinder is the outside of a solid rod,
+ * CDSphere2QuasiCylinder.cpp:40-50): the inside of a hollow cylinder, a drum shell.  attrs
+ * {radius, length} about OrientationZ; global scope; fixed or orbital (a drum turning about its
+ * own axis).  A sphere inside touches it where its centre is farther than radius - r from the
+ * axis, within the length; beyond either end, the rim circle.  Scenes that use it cannot be
+ * read by the reference. */
+enum { VEDO_SHAPE_INNER_CYLINDER = 32 };
 enum { VEDO_CONSTRAINED = 1, VEDO_FIXED = 2, VEDO_MOBILE = 3, VEDO_ORBITAL = 4 };
 enum { VEDO_SCOPE_GLOBAL = 1, VEDO_SCOPE_LOCAL = 2 };
 
@@ -424,11 +431,29 @@ void vedo_srv_destroy(vedo_server* s);
  * The reduction's partial sums live in a fixed 1 MiB array that the library declares in
  * device memory, which every GPU that loads the library holds until the process exits.
  * The call allocates nothing.  At most VEDO_NOALLOC_MAX_OBJECTS objects; larger counts
- * return VEDO_ERR_INVALID_ARGUMENT with a message (vedo_gpu_last_error(NULL)).  The first
- * call on each device, with that device current, looks up the array's device address
- * (cudaGetSymbolAddress); make that first call before any stream capture.  All calls
- * share the one array: calls that overlap on the GPU (on different streams, or from
- * different threads without ordering) race and give wrong results. */
+ * return VEDO_ERR_INVALID_ARGUMENT with a message (vedo_gpu_last_error(NULL)), and so do
+ * buffers that are not device (or managed) memory of the current device.  The first call on
+ * each device, with that device current, looks up the array's device address
+ * (cudaGetSymbolAddress) and keeps it for the life of the process; with CUDA's lazy module
+ * loading that first call is also where the module is loaded and the array reserved, which
+ * can synchronise the device: make one warm-up call at set-up, before any stream capture and
+ * outside time-critical loops.  A cudaDeviceReset (or anything else that tears the primary
+ * context down) invalidates the kept address: do not call this entry point again in that
+ * process after such a reset.  All calls share the one array: calls that overlap on the GPU
+ * (on different streams, or from different threads without ordering) race and give wrong
+ * results. */
+/* ---- scene generation helper -----------------------------------------------
+ * No counterpart in the reference (it reads scenes from files; this seeds the synthetic
+ * workloads).  Random sequential placement, host only: sphere i (in the given order) is
+ * drawn uniformly, up to max_tries times, in the box [lo, hi] shrunk by its radius and, when
+ * cyl_radius > 0, inside the cylinder of that radius about the x axis shrunk by its radius;
+ * it is kept at the first draw that overlaps no sphere kept before.  out: [n][3] centres
+ * (NaN for a sphere not placed); *placed: the count kept.  The same seed gives the same
+ * spheres on every host. */
+int vedo_place_spheres(uint32_t n, const double* radii, const double lo[3], const double hi[3],
+                       double cyl_radius, uint64_t seed, uint32_t max_tries, double* out,
+                       uint32_t* placed);
+
 #define VEDO_NOALLOC_MAX_OBJECTS 16777216u
 int vedo_gpu_system_energy_noalloc(const double* position, const double* velocity, const double* angular_velocity,
                                    const double* mass, const double* inertia, const uint8_t* mobile,

@@ -58,7 +58,7 @@ static v3 rotate_around(v3 p, v3 va) {                                          
 }
 
 /* ------------------------------------------------------------------------ */
-enum { CD_NONE = 0, CD_SS = 1, CD_SP = 2, CD_SC = 3, CD_SHP = 4 };
+enum { CD_NONE = 0, CD_SS = 1, CD_SP = 2, CD_SC = 3, CD_SHP = 4, CD_SIC = 5 };
 enum { IS_NONE = 0, IS_BSDBF = 1, IS_BTSDBF = 2, IS_BSDB2F = 3, IS_HERTZ = 4, IS_H = 5 };
 
 typedef struct {
@@ -244,6 +244,16 @@ static int analyse(model_t* m) {
         m->inertia = V3(0.0, 0.0, 0.0);
         return 1;
     }
+    case VEDO_SHAPE_INNER_CYLINDER:
+        /* No counterpart in the reference (an extension the engine defines): the inside of a
+         * hollow cylinder, a shell of no thickness and no mass, global scope only. */
+        if (m->scope != VEDO_SCOPE_GLOBAL || !(m->a[0] > 0.0) || !(m->a[1] > 0.0)) return 0;
+        m->range = 0.0;
+        m->volume = 0.0;
+        m->mass = 0.0;
+        m->sudo_model = 0.0;
+        m->inertia = V3(0.0, 0.0, 0.0);
+        return 1;
     default:
         return 0;
     }
@@ -261,6 +271,10 @@ static int object_sudo_mass(const model_t* m, double* out) {
     if (m->shape == VEDO_SHAPE_QUASI_PLATE_WITH_CIRCULAR_HOLE) {   /* DOFixedQuasiPlateWithCircularHole.cpp:16-19 */
         if (m->behavior == VEDO_FIXED) { *out = 0.0; return 0; }
         return -1;           /* the mobile one (DOQuasiPlateWithCircularHole) is not restated */
+    }
+    if (m->shape == VEDO_SHAPE_INNER_CYLINDER) {               /* the engine's extension: fixed or orbital */
+        if (m->behavior == VEDO_FIXED || m->behavior == VEDO_ORBITAL) { *out = 0.0; return 0; }
+        return -1;
     }
     if (m->shape == VEDO_SHAPE_QUASI_PLATE || m->shape == VEDO_SHAPE_QUASI_CYLINDER) {
         switch (m->behavior) {
@@ -342,6 +356,19 @@ static int cal_distance_pbc(const dp_world* w, unsigned i, unsigned j, int perio
         else Im = sub(sub(Cb, muls(ax, hh)), Ca);
         if (periodic) Im = min_image(w, Im);
         *out = len(Im);
+        return 0;
+    }
+    if (mi->shape == VEDO_SHAPE_SPHERE && mj->shape == VEDO_SHAPE_INNER_CYLINDER) {
+        /* the engine's extension: centre to the nearest point of the shell (within its length
+         * the radial gap, beyond an end the rim circle); no minimum image */
+        const double hh = 0.5 * (mj->a[1]), R = mj->a[0];
+        v3 ax = ld3(w->oz + 3 * j);
+        v3 d = sub(pi, pj);
+        double t = dot(d, ax);
+        v3 rp = sub(d, muls(ax, t));
+        if (t <= hh && t >= -hh) { *out = fabs(R - len(rp)); return 0; }
+        v3 q = add(add(pj, muls(ax, t > 0.0 ? hh : -hh)), muls(dir(rp), R));
+        *out = len(sub(q, pi));
         return 0;
     }
     return -1;                                       /* :410-413 exit(-1) in the reference */
@@ -686,6 +713,7 @@ static int create_interaction(const dp_world* w, unsigned p1, unsigned p2, iactn
     else if (ms->shape == VEDO_SHAPE_SPHERE && mm->shape == VEDO_SHAPE_QUASI_PLATE) cd = CD_SP;
     else if (ms->shape == VEDO_SHAPE_SPHERE && mm->shape == VEDO_SHAPE_QUASI_CYLINDER) cd = CD_SC;
     else if (ms->shape == VEDO_SHAPE_SPHERE && mm->shape == VEDO_SHAPE_QUASI_PLATE_WITH_CIRCULAR_HOLE) cd = CD_SHP;
+    else if (ms->shape == VEDO_SHAPE_SPHERE && mm->shape == VEDO_SHAPE_INNER_CYLINDER) cd = CD_SIC;   /* extension */
     const iact_t* im = &w->iacts[ia];
     if (cd == CD_NONE || im->eq == IS_NONE) return 2;
     for (int k = 0; MECH_NAMES[im->eq][k]; ++k)
@@ -765,6 +793,26 @@ static void detect(const dp_world* w, iactn_t* I) {
         if (dah == 0.0) ci->depth = ra + hh - sqrt(len(vIm) * len(vIm) + hr * hr);
         else ci->depth = ra + hh - len(vIm);
         ci->dirn = dir(vIm);
+    } else if (I->cd == CD_SIC) {
+        /* The engine's extension, no reference counterpart: a sphere inside a hollow cylinder
+         * of radius a[0] and length a[1] about its unit OrientationZ.  Within the length the
+         * depth is how far the sphere passes the shell, the normal the outward radial direction;
+         * beyond an end, the nearest point of that end's rim circle. */
+        const double hh = 0.5 * mm->a[1], R = mm->a[0];
+        v3 ax = ld3(w->oz + 3 * m);
+        v3 d = sub(Ps, Pm);
+        double t = dot(d, ax);
+        v3 rp = sub(d, muls(ax, t));
+        v3 u = dir(rp);
+        if (t <= hh && t >= -hh) {
+            ci->depth = ra + len(rp) - R;
+            ci->dirn = u;
+        } else {
+            v3 q = add(add(Pm, muls(ax, t > 0.0 ? hh : -hh)), muls(u, R));
+            v3 vIm = sub(q, Ps);
+            ci->depth = ra - len(vIm);
+            ci->dirn = dir(vIm);
+        }
     } else {                                                 /* CDSphere2QuasiCylinder.cpp:16-80 */
         double hh = 0.5 * mm->a[1];
         v3 ax = ld3(w->oz + 3 * m);

@@ -60,5 +60,5 @@ def box_ido(engine_lib, tmp_path_factory):
 def drum_ido(engine_lib, tmp_path_factory):
     """A 40,000-sphere Hertz drum after 3,000 FP64 steps (dt 5e-7 s, E 70 GPa)."""
     from vedo_gb300 import scenes
-    sc = scenes.hertz_drum(n=40000, seed=3, steps=100, gap=0.002, vel_sigma=0.05)
+    sc = scenes.hertz_drum(n=40000, seed=3, steps=100, gap=0.002, vel_sigma=0.05, fill="lattice")
     return _settled(engine_lib, tmp_path_factory.mktemp("settled"), sc, 3000, "drum")

@@ -290,3 +290,27 @@ def test_oracle_equals_the_reference_on_random_clusters(seed, consultant, port_l
         else:
             np.testing.assert_allclose(a[k], b[k], rtol=1e-9, atol=1e-12 * (np.abs(a[k]).max() + 1e-300), err_msg=k)
     r.close()
+
+
+def test_port_matches_reference_whole_run_start(port_lib):
+    """The first 2,000 steps of the 8,000-sphere box's whole run: the C restatement's state has
+    the reference's SHA-256 after 100, 500, 1,000, 1,500 and 2,000 steps
+    (tests/golden/wholerun/lsd_box.npz, made by the reference itself)."""
+    import hashlib
+    from oracle import PortWorld
+    g = np.load(os.path.join(ROOT, "tests", "golden", "wholerun", "lsd_box.npz"))
+    want = {int(s): str(d) for s, d in zip(g["table"][:, 0], g["digests"])}
+    w = PortWorld(scenes.lsd_box(steps=int(g["steps"])), up_iact=int(g["up_iact"]))
+    done = 0
+    for target in (100, 500, 1000, 1500, 2000):
+        w.run(target - done)
+        done = target
+        st = w.state()
+        h = hashlib.sha256()
+        for k in ("position", "velocity", "angular_velocity"):
+            h.update(np.ascontiguousarray(st[k], dtype="<f8").tobytes())
+        assert h.hexdigest() == want[target], target
+        if target == 100:
+            for k in ("position", "velocity", "angular_velocity"):
+                np.testing.assert_array_equal(st[k], g[f"first100_{k}"], err_msg=k)
+    w.close()

@@ -9,7 +9,7 @@ import numpy as np
 import pytest
 
 from vedo_gb300 import scenes
-from vedo_gb300.scene import QUASI_CYLINDER, QUASI_PLATE, SPHERE
+from vedo_gb300.scene import INNER_CYLINDER, QUASI_CYLINDER, QUASI_PLATE, SPHERE
 
 spatial = pytest.importorskip("scipy.spatial")
 
@@ -46,6 +46,10 @@ def min_clearance(sc):
             t = np.clip((P - c) @ oz, -0.5 * h, 0.5 * h)
             closest = c + t[:, None] * oz
             gaps.append((np.linalg.norm(P - closest, axis=1) - r - rc).min())
+        elif m.shape == INNER_CYLINDER:              # inside the shell: R - axis distance - r
+            rc = m.attrs[0]
+            t = (P - c) @ oz
+            gaps.append((rc - np.linalg.norm((P - c) - t[:, None] * oz, axis=1) - r).min())
     return min(gaps)
 
 

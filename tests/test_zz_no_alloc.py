@@ -67,6 +67,55 @@ def test_noalloc_energy_equals_engine_observables_twice(engine_lib):
     e.close()
 
 
+@pytest.mark.gpu
+def test_noalloc_many_blocks_without_mobile_flags_and_no_new_memory(engine_lib):
+    """100,000 objects (more than 32 blocks of partial sums) with every object counted
+    (mobile = NULL), against a plain FP64 reduction of the same arrays; after a warm-up call,
+    a second call leaves the device's free memory unchanged."""
+    torch = pytest.importorskip("torch")
+    f = _entry(engine_lib)
+    rng = np.random.default_rng(11)
+    n = 100_000
+    p, v, w = rng.normal(0, 0.1, (n, 3)), rng.normal(0, 1.0, (n, 3)), rng.normal(0, 50.0, (n, 3))
+    m = rng.uniform(1e-6, 1e-5, n)
+    inertia = np.repeat((0.4 * m * 1e-6)[:, None], 3, axis=1)
+    x = {k: torch.from_numpy(np.ascontiguousarray(a)).cuda() for k, a in
+         (("p", p), ("v", v), ("w", w), ("m", m), ("i", inertia))}
+    out = torch.full((12,), float("nan"), dtype=torch.float64, device="cuda")
+    g = (C.c_double * 3)(0.0, 0.0, -9.81)
+    stream = torch.cuda.current_stream()
+    args = (x["p"].data_ptr(), x["v"].data_ptr(), x["w"].data_ptr(), x["m"].data_ptr(), x["i"].data_ptr(), None,
+            n, g, out.data_ptr(), stream.cuda_stream)
+    assert f(*args) == 0, engine_lib.lib().vedo_gpu_last_error(None)        # warm-up call
+    stream.synchronize()
+    free0 = torch.cuda.mem_get_info()[0]
+    assert f(*args) == 0, engine_lib.lib().vedo_gpu_last_error(None)
+    stream.synchronize()
+    assert torch.cuda.mem_get_info()[0] == free0
+    got = out.cpu().numpy()
+    ke_t = np.sum(0.5 * m * np.sum(v * v, axis=1))
+    ke_r = np.sum(0.5 * inertia * w * w)
+    pe = -np.sum(m * (p @ np.array([0.0, 0.0, -9.81])))
+    com = (m[:, None] * p).sum(axis=0) / m.sum()
+    for k, ref in ((0, pe), (1, ke_t), (2, ke_r)):
+        assert abs(got[k] - ref) <= 1e-12 * abs(ref), (k, got[k], ref)
+    speed, spin = np.linalg.norm(v, axis=1), np.linalg.norm(w, axis=1)
+    for k, ref in ((3, speed.min()), (4, speed.max()), (5, spin.min()), (6, spin.max())):
+        assert abs(got[k] - ref) <= 1e-15 * ref, (k, got[k], ref)        # one rounding of the norm
+    np.testing.assert_allclose(got[9:12], com, rtol=0, atol=1e-12 * np.abs(p).max())
+
+
+@pytest.mark.gpu
+def test_noalloc_rejects_host_buffers(engine_lib):
+    f = _entry(engine_lib)
+    g = (C.c_double * 3)(0.0, 0.0, -9.81)
+    host = np.zeros((4, 3))
+    hp = host.ctypes.data
+    rc = f(hp, hp, hp, hp, hp, None, 4, g, hp, None)
+    assert rc == 1
+    assert b"device memory" in engine_lib.lib().vedo_gpu_last_error(None)
+
+
 def test_noalloc_rejects_more_objects_than_its_scratch(engine_lib):
     """Refused before any CUDA call: runs without a GPU."""
     f = _entry(engine_lib)

@@ -44,6 +44,7 @@ SOURCES = {
     "capi.cpp": ("cxx", []),
     "xml_io.cpp": ("cxx", []),
     "serve.cpp": ("cxx", ["-pthread"]),
+    "scene_gen.cpp": ("cxx", []),
 }
 
 

@@ -14,9 +14,13 @@ namespace vedo {
 
 // ---- enums (DOModel.h:25-27) and engine-internal codes -------------------------------
 enum : int { SHAPE_SPHERE = 1, SHAPE_CYL = 6, SHAPE_PLATE = 7, SHAPE_HOLED = 8 };   // 8: QuasiPlateWithCircularHole
+// An engine extension with no counterpart in the reference: the inside of a hollow cylinder of
+// radius a0 and length a1 about its OrientationZ (a drum shell), global scope, fixed or orbital.
+enum : int { SHAPE_INNER_CYL = 32 };
 enum : int { BEH_CONSTRAINED = 1, BEH_FIXED = 2, BEH_MOBILE = 3, BEH_ORBITAL = 4 };
 enum : int { SCOPE_GLOBAL = 1, SCOPE_LOCAL = 2 };
-enum : int { CD_SS = 1, CD_SP = 2, CD_SC = 3, CD_SHP = 4 };   // CD_SHP: sphere - plate with a circular hole
+enum : int { CD_SS = 1, CD_SP = 2, CD_SC = 3, CD_SHP = 4, CD_SIC = 5 };   // CD_SHP: sphere - plate with a circular
+                                                                       // hole; CD_SIC: sphere inside a hollow cylinder
 // The holed plate is a plate without its hole: distances to it are at least those to the full
 // plate, so every conservative plate test (broad phase, prefilter) serves it unchanged.
 __host__ __device__ __forceinline__ int cd_plane(int cd) { return cd == CD_SHP ? CD_SP : cd; }

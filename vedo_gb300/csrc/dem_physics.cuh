@@ -77,6 +77,26 @@ __device__ __forceinline__ void detect_pair(int cd, const PairGeom& g, d3 Ps, d3
             depth = g.ra + hh - len(vIm);
         }
         n = dir(vIm);
+    } else if (cd == CD_SIC) {
+        // Engine extension, no reference counterpart: a sphere inside a hollow cylinder of radius
+        // b0 and length b1 about its unit OrientationZ (a drum shell).  Within the length the
+        // depth is how far the sphere's surface passes the shell, the normal the outward radial
+        // direction; beyond an end, the nearest point of that end's rim circle.
+        const double hh = 0.5 * g.b1, R = g.b0;
+        const d3 ax = ld(oz, m);
+        const d3 d = sub(Ps, Pm);
+        const double t = dot(d, ax);
+        const d3 rp = sub(d, muls(ax, t));
+        const d3 u = dir(rp);
+        if (t <= hh && t >= -hh) {
+            depth = g.ra + len(rp) - R;
+            n = u;
+        } else {
+            const d3 q = add(add(Pm, muls(ax, t > 0.0 ? hh : -hh)), muls(u, R));
+            const d3 vIm = sub(q, Ps);
+            depth = g.ra - len(vIm);
+            n = dir(vIm);
+        }
     } else {                                                  // CDSphere2QuasiCylinder.cpp:16-80
         double hh = 0.5 * g.b1;
         d3 ax = ld(oz, m);
@@ -316,6 +336,18 @@ __device__ __forceinline__ double cal_distance(const ModelDev& mi_, const ModelD
         else if (dap >= hh) Im = sub(add(pj, muls(ax, hh)), pi);
         else Im = sub(sub(pj, muls(ax, hh)), pi);
         return len(pb ? min_image(*pb, Im) : Im);
+    }
+    if (mi->shape == SHAPE_SPHERE && mj->shape == SHAPE_INNER_CYL) {
+        // engine extension: centre to the nearest point of the shell (within its length the
+        // radial gap, beyond an end the rim circle); the boundary's minimum image is not taken
+        const double hh = 0.5 * (mj->a1), R = mj->a0;
+        const d3 ax = ld(oz, j);
+        const d3 d = sub(pi, pj);
+        const double t = dot(d, ax);
+        const d3 rp = sub(d, muls(ax, t));
+        if (t <= hh && t >= -hh) return fabs(R - len(rp));
+        const d3 q = add(add(pj, muls(ax, t > 0.0 ? hh : -hh)), muls(dir(rp), R));
+        return len(sub(q, pi));
     }
     ok = false;
     return 0.0;

@@ -494,6 +494,12 @@ __device__ __forceinline__ bool candidate(const ModelDev& mi, const ModelDev& mj
             const float d = wshape != SHAPE_CYL ? plane_dist32(pos32[sp], pos32[w], wl, e)
                                                   : line_dist32(pos32[sp], pos32[w], wl, e);
             if (d - e > thi) return false;
+        } else if (wl.w != 0.0f && wshape == SHAPE_INNER_CYL && (ip ? mj.shape : mi.shape) == SHAPE_SPHERE) {
+            // the distance to the shell is at least R minus the axis distance (rim included)
+            float e;
+            const float d = line_dist32(pos32[sp], pos32[w], wl, e);
+            const float R = (float)(ip ? mi.a0 : mj.a0) * (1.0f - 4.0f * PF_ARITH_EPS);
+            if (R - (d + e) > thi) return false;
         }
     }
     bool ok;
@@ -919,7 +925,9 @@ int Engine::init(const HScene& scene, const vedo_engine_opts& opts) {
             if (tab_.params[q].cd == CD_SS) r = gq[0] + gq[1];
             else if (cd_plane(tab_.params[q].cd) == CD_SP) r = gq[0] + 0.5 * gq[2];
             else if (tab_.params[q].cd == CD_SC) r = gq[0] + gq[1];
-            reach[q] = (float)r * (1.0f + 1e-6f);
+            // inside a hollow cylinder: -(R - r), its magnitude rounded down (prefilter.cuh)
+            if (tab_.params[q].cd == CD_SIC) reach[q] = (float)(gq[0] - gq[1]) * (1.0f - 1e-6f);
+            else reach[q] = (float)r * (1.0f + 1e-6f);
         }
         CK(dalloc(&d_reach_, reach.size()));
         CK(cudaMemcpy(d_reach_, reach.data(), sizeof(float) * reach.size(), cudaMemcpyHostToDevice));

@@ -60,15 +60,16 @@ constexpr uint32_t WALL_BIT = 0x80000000u;
 // contact detector (bits 24-25), "bondable law" (the FP32 prefilter may not skip the pair),
 // "history owner" (the entry holds the pair's history) and "this sphere is the slave".
 constexpr uint32_t META_PI = 0x00ffffffu;
-constexpr int META_CD_SHIFT = 24;
-constexpr uint32_t META_BOND = 1u << 26;
-constexpr uint32_t META_OWNER = 1u << 27;
-constexpr uint32_t META_SLAVE = 1u << 28;
-constexpr uint32_t META_MOVING = 1u << 29;   // the entry's other object is an orbital wall
-// A wall entry whose sphere projects inside the plate (or along the rod's segment) with a
-// margin that outlasts the list: its distance is the distance to the plane (or axis), which
-// only the normal (or transverse) part of the sphere's displacement changes.
-constexpr uint32_t META_INTERIOR = 1u << 30;
+constexpr int META_CD_SHIFT = 24;            // bits 24-26
+constexpr uint32_t META_CD_MASK = 7u;
+constexpr uint32_t META_BOND = 1u << 27;
+constexpr uint32_t META_OWNER = 1u << 28;
+constexpr uint32_t META_SLAVE = 1u << 29;
+constexpr uint32_t META_MOVING = 1u << 30;   // the entry's other object is an orbital wall
+// A wall entry whose sphere projects inside the plate (or along the rod's or shell's length)
+// with a margin that outlasts the list: its distance is the distance to the plane (or axis),
+// which only the normal (or transverse) part of the sphere's displacement changes.
+constexpr uint32_t META_INTERIOR = 1u << 31;
 // Orbital walls move on their own schedule (a drum's end plates turn at a fixed rate), so their
 // entries are gathered with a wider skin and carry their own displacement bound; sphere pairs
 // and fixed walls keep the sphere bound alone.
@@ -143,6 +144,23 @@ __device__ __forceinline__ double wall_detect(int cd, double ra, double b0, doub
         const d3 vIm = xsub(Caps, Ps);
         depth = __dsub_rn(__dadd_rn(ra, hh), xlen(vIm));
         n = xdir(vIm);
+    } else if (cd == CD_SIC) {
+        // engine extension (the reference has no hollow cylinder): the inside of a shell of
+        // radius b0 and length b1 about Oz, as the FP64 form's detector computes it
+        const double hh = __dmul_rn(0.5, b1);
+        const d3 d = xsub(Ps, Pm);
+        const double t = xdot(d, Oz);
+        const d3 rp = xsub(d, xsmul(t, Oz));
+        const d3 u = xdir(rp);
+        if (t <= hh && t >= -hh) {
+            depth = __dsub_rn(__dadd_rn(ra, xlen(rp)), b0);
+            n = u;
+        } else {
+            const d3 q = xadd(xadd(Pm, xsmul(t > 0.0 ? hh : -hh, Oz)), xsmul(b0, u));
+            const d3 vIm = xsub(q, Ps);
+            depth = __dsub_rn(ra, xlen(vIm));
+            n = xdir(vIm);
+        }
     } else {
         const double hh = __dmul_rn(0.5, b1);
         double dap = xdot(xsub(Ps, Pm), Oz);
@@ -261,7 +279,15 @@ __device__ __forceinline__ bool apart32(int cd, const float4& s, const float4& m
     if (cd == CD_SP) return fabsf(fmaf(dz, wall.z, fmaf(dy, wall.y, dx * wall.x))) > lim2;
     const float cx = fmaf(dy, wall.z, -dz * wall.y), cy = fmaf(dz, wall.x, -dx * wall.z),
                 cz = fmaf(dx, wall.y, -dy * wall.x);
-    return fmaf(cz, cz, fmaf(cy, cy, cx * cx)) > lim2 * lim2 * (1.0f + 4.0f * PF_ARITH_EPS);
+    const float c2 = fmaf(cz, cz, fmaf(cy, cy, cx * cx));
+    if (cd == CD_SIC) {
+        // inside a hollow cylinder the reach is -(R - r) (plus the pad): clear while the centre
+        // stays nearer the axis than R - r - pad, less every rounding allowance
+        const float in = -reach * (1.0f - 4.0f * PF_ARITH_EPS) - s.w - m.w -
+                         PF_ARITH_EPS * (fabsf(dx) + fabsf(dy) + fabsf(dz));
+        return in > 0.0f && c2 < in * in * (1.0f - 4.0f * PF_ARITH_EPS);
+    }
+    return c2 > lim2 * lim2 * (1.0f + 4.0f * PF_ARITH_EPS);
 }
 
 // ---- the five laws in FP32 (same control flow as the reference's NextStep) -------------
@@ -434,6 +460,7 @@ struct TickArgs {
     const float2* clear;           // [n] per sphere: every prefilter test of its list says "apart" for
                                    // sphere-pair pads <= x and fixed-wall pads <= y
     uint8_t* qcnt;                 // [n] consecutive clean walks (0..2) since the last rebuild
+    const uint32_t* ext_of;        // [n] the caller's index of each object (storage order)
 };
 
 // A step whose list may be incomplete is an identity step.  A sphere pair may have closed by
@@ -486,12 +513,12 @@ __device__ __forceinline__ uint32_t prefilter_group(const TickArgs& a, uint32_t 
     }
 #pragma unroll
     for (int k = 0; k < TICK_GROUP; ++k)
-        gp[k] = (gm[k] >> META_CD_SHIFT) & 3u ? a.pos32[ge[k] & ~WALL_BIT] : p32i;
+        gp[k] = (gm[k] >> META_CD_SHIFT) & META_CD_MASK ? a.pos32[ge[k] & ~WALL_BIT] : p32i;
     uint32_t exact = 0;
 #pragma unroll
     for (int k = 0; k < TICK_GROUP; ++k) {
         const uint32_t meta = gm[k];
-        const int cd = (int)((meta >> META_CD_SHIFT) & 3u);
+        const int cd = (int)((meta >> META_CD_SHIFT) & META_CD_MASK);
         if (cd == 0) continue;
         const uint32_t e = base + k;
         const uint32_t j = ge[k] & ~WALL_BIT;
@@ -623,148 +650,269 @@ __device__ __forceinline__ float2 finish_sphere(const TickArgs& a, uint32_t i, b
     return make_float2(0.0f, 0.0f);
 }
 
-// One sphere's step: neighbour walk (prefilter, then the exact path in entry order), sums,
-// integration.  Returns its squared speed bounds of the step.
+// One list entry's prefilter: the per-entry form of prefilter_group (the same decisions, the
+// same history cleaning and wall-impulse writes).  Returns true when the entry needs the exact
+// path; `dirty` is set when a history was cleaned.
+__device__ __forceinline__ bool prefilter_entry(const TickArgs& a, uint32_t e, const float4& p32i, float pad,
+                                                bool& dirty) {
+    const uint32_t meta = a.nmeta[e];
+    const int cd = (int)((meta >> META_CD_SHIFT) & META_CD_MASK);
+    if (cd == 0) return false;
+    if (meta & META_BOND) return true;
+    const uint32_t ent = a.nent[e];
+    const uint32_t j = ent & ~WALL_BIT;
+    const bool wall = ent & WALL_BIT;
+    const bool i_slave = meta & META_SLAVE;
+    const float4 pj = a.pos32[j];
+    const float4 ws = wall ? a.wall32[j] : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+    float pk = pad;
+    if (wall) {
+        pk = (meta & META_INTERIOR) ? fminf(a.disp[1], a.disp[0] + ws.w) : a.disp[1];
+        if (meta & META_MOVING) pk += a.disp[2];
+    }
+    if (!apart32(cd, i_slave ? p32i : pj, i_slave ? pj : p32i, ws, a.reach[meta & META_PI] + pk)) return true;
+    if (wall && a.write_imp) {
+        float* o = a.wimp + 6 * (size_t)e;
+        o[0] = o[1] = o[2] = o[3] = o[4] = o[5] = 0.0f;
+    }
+    if (meta & META_OWNER) {
+        const uint8_t f0 = a.fA[e];
+        if (f0 & 15) {                         // ImpactStatus::Clean
+            a.hB[e] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+            a.fB[e] = HF_PENDING;
+            dirty = true;
+        } else if (f0 & HF_PENDING) {
+            a.hB[e] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+            a.fB[e] = 0;
+        }
+    }
+    return false;
+}
+
+// One list entry of sphere i on the exact path: the pair in canonical (slave, master)
+// orientation from the previous positions, the FP32 velocity copies and the pair's history
+// (identical inputs for both members, so both obtain the same impulse), the history update by
+// the entry that holds it, and the wall's share of the impulse.  Returns 0 (nothing added),
+// 1 (impulse) or 2 (impulse and torque) with sphere i's share of each in cj, ct.
 template <int LAW, bool XS>
-__device__ __forceinline__ float2 tick_sphere(const TickArgs& a, uint32_t i) {
+__device__ __forceinline__ int exact_entry(const TickArgs& a, uint32_t e, uint32_t i, float dtf, f3& cj, f3& ct) {
+    const uint32_t ent = a.nent[e];
+    const uint32_t meta = a.nmeta[e];
+    const uint32_t j = ent & ~WALL_BIT;
+    const bool wall = ent & WALL_BIT;
+    // canonical orientation (Assembler.cpp:43-67), fixed at rebuild; sphere-wall: the sphere is the slave
+    const bool i_slave = meta & META_SLAVE;
+    const bool owner = meta & META_OWNER;
+    const uint32_t s = i_slave ? i : j, m = i_slave ? j : i;
+    const uint32_t pi = meta & META_PI;
+    const uint32_t slot = owner ? e : a.nslot[e];
+    const PairParam& P = a.params[pi];
+    const double4_32a gg = a.geom[pi];
+    const d3 Pi = ld(a.xA, i);
+    bool active;
+    float depth;
+    f3 n, rA, rB;
+    if (P.cd == CD_SS) {
+        // d = x_master - x_slave, |d|^2 and R^2 - |d|^2 in double-float from the two
+        // positions' hi/lo splits; where the numerator is within 1e-9 R^2 of zero the
+        // reference's FP64 formula decides
+        float4 hi_i, lo_i, hj, lj;
+        if (XS) {
+            hj = a.xsA[2 * j];
+            lj = a.xsA[2 * j + 1];
+            hi_i = a.xsA[2 * i];
+            lo_i = a.xsA[2 * i + 1];
+        } else {
+            const d3 Pj = ld(a.xA, j);
+            split32(Pj.x, hj.x, lj.x);
+            split32(Pj.y, hj.y, lj.y);
+            split32(Pj.z, hj.z, lj.z);
+            split32(Pi.x, hi_i.x, lo_i.x);
+            split32(Pi.y, hi_i.y, lo_i.y);
+            split32(Pi.z, hi_i.z, lo_i.z);
+        }
+        const float4 hs = i_slave ? hi_i : hj, ls = i_slave ? lo_i : lj;
+        const float4 hm = i_slave ? hj : hi_i, lm = i_slave ? lj : lo_i;
+        const dfl dx = df_diff(hm.x, lm.x, hs.x, ls.x), dy = df_diff(hm.y, lm.y, hs.y, ls.y),
+                  dz = df_diff(hm.z, lm.z, hs.z, ls.z);
+        const dfl s2 = df_add(df_add(df_sq(dx), df_sq(dy)), df_sq(dz));
+        const float4 rq = a.rr32[pi];                // R^2 hi, R^2 lo, band, R
+        const dfl num = df_add(dfl{rq.x, rq.y}, dfl{-s2.hi, -s2.lo});
+        if (num.hi < -rq.z || num.hi > rq.z) {
+            active = num.hi > 0.0f;
+            depth = (num.hi + num.lo) / (rq.w + sqrtf(s2.hi));
+        } else {                               // tie band: the reference's formula decides
+            const d3 Pj = ld(a.xA, j);
+            const d3 d = i_slave ? sub(Pj, Pi) : sub(Pi, Pj);
+            const double dex = __dsub_rn(__dadd_rn(gg.x, gg.y), xlen(d));
+            active = dex > 0.0;
+            depth = (float)dex;
+        }
+        const f3 df = fm(dx.hi + dx.lo, dy.hi + dy.lo, dz.hi + dz.lo);
+        n = fdir(df);
+        rA = ((float)gg.x - 0.5f * depth) * n;
+        rB = rA - df;
+    } else {
+        const d3 Pj = ld(a.xA, j);
+        const d3 Ps = i_slave ? Pi : Pj, Pm = i_slave ? Pj : Pi;
+        d3 nd, pt;
+        const double dex = wall_detect(P.cd, gg.x, gg.y, gg.z, gg.w, Ps, Pm, ld(a.ox, m), ld(a.oz, m), nd, pt,
+                                       P.cd == CD_SHP ? a.hole[pi] : make_double4_32a(0, 0, 0, 0));
+        active = dex > 0.0;
+        depth = (float)dex;
+        n = fm((float)nd.x, (float)nd.y, (float)nd.z);
+        const d3 ra = sub(pt, Ps), rb = sub(pt, Pm);
+        rA = fm((float)ra.x, (float)ra.y, (float)ra.z);
+        rB = fm((float)rb.x, (float)rb.y, (float)rb.z);
+    }
+    const uint8_t f0 = a.fA[slot];
+    uint8_t f = f0 & 15;
+    float4 h = (f != 0 || active) ? a.hA[slot] : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+    f3 Jp = fm(0.0f, 0.0f, 0.0f), tA = Jp, tB = Jp;
+    const int app = solve32<LAW>(P.is, a.pc32 + 8 * (size_t)pi, active, depth, n, rA, rB, f4to3(a.v32A[s]),
+                                 f4to3(a.v32A[m]), f4to3(a.w32A[s]), f4to3(a.w32A[m]), dtf, f, h, Jp, tA, tB);
+    if (e == slot) {                           // history owner writes the new status
+        if (f != 0 || (f0 & 15) != 0) {
+            a.hB[slot] = h;
+            a.fB[slot] = (uint8_t)(f | ((f == 0) ? HF_PENDING : 0));
+        } else if (f0 & HF_PENDING) {
+            a.hB[slot] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+            a.fB[slot] = 0;
+        }
+    }
+    if (wall && a.write_imp) {                 // the wall's share, summed per wall later
+        float* o = a.wimp + 6 * (size_t)e;
+        o[0] = app ? -Jp.x : 0.0f; o[1] = app ? -Jp.y : 0.0f; o[2] = app ? -Jp.z : 0.0f;
+        o[3] = app == 2 ? tB.x : 0.0f; o[4] = app == 2 ? tB.y : 0.0f; o[5] = app == 2 ? tB.z : 0.0f;
+    }
+    cj = i_slave ? Jp : -Jp;
+    ct = i_slave ? tA : tB;
+    return app;
+}
+
+// ---- the contact tick: one warp per group of 32 spheres ---------------------------------
+// The group's list entries (its spheres' rows, concatenated) are walked in windows of TG_CAP:
+// the 32 lanes prefilter consecutive entries (coalesced list loads, every lane busy whatever
+// the rows' lengths), the entries on the exact path are queued and then computed by all 32
+// lanes together (no lane waits for a neighbour's long row), each entry's share of the impulse
+// lands in shared memory at its place in the row, and each lane sums its own sphere's row in
+// list order.  The per-sphere sums are therefore the sequence a single thread walking the row
+// would form (the same compensated additions in the same order), whatever the group.
+constexpr int TG_CAP = 128;                  // list entries a warp holds per window
+struct GroupSmem {
+    float4 cj[TG_CAP];                       // sphere's share of the impulse, per window entry
+    float4 ct[TG_CAP];                       // ... of the angular impulse
+    uint32_t row[33];                        // row k: window positions [row[k], row[k + 1])
+    uint32_t sid[32];
+    uint32_t e0[32];
+    float dtf[32];
+    uint32_t flags[32];                      // 1: a history was cleaned, 2: an entry took the exact path
+    uint16_t xq[TG_CAP];                     // exact-path queue of the window
+    uint8_t app[TG_CAP];
+};
+
+// the group row holding position q: the largest k with row[k] <= q (rows may be empty)
+__device__ __forceinline__ int group_row(const uint32_t* row, uint32_t q) {
+    int lo = 0, hi = 32;
+    while (hi - lo > 1) {
+        const int mid = (lo + hi) >> 1;
+        if (row[mid] <= q) lo = mid; else hi = mid;
+    }
+    return lo;
+}
+
+// Sphere i (or ~0u: this lane has none) of the warp's group; every lane of the warp calls it.
+template <int LAW, bool XS>
+__device__ __forceinline__ float2 tick_group(const TickArgs& a, uint32_t i, GroupSmem& g) {
+    const int lane = threadIdx.x & 31;
     float2 vmax_local = make_float2(0.0f, 0.0f);
-    {
-        // every load that depends on the index alone is issued here, together, so that their
-        // latencies overlap; the model- and list-dependent ones follow
-        const uint32_t mi = a.model_of[i];
-        const uint32_t si = a.scene_of[i];
-        const uint32_t e0 = a.nptr[i], e1 = a.nptr[i + 1];
-        const d3 Pi = ld(a.xA, i);
-        const d3 V = ld(a.v64, i);
-        const float4 p32i = a.pos32[i];
-        const float disp = a.disp[0];
+    uint32_t cnt = 0, qc = 0, mi = 0, si = 0;
+    bool local = false, quiet = false;
+    const float pad = 2.0f * a.disp[0];
+    if (i != 0xffffffffu) {
+        mi = a.model_of[i];
+        si = a.scene_of[i];
         const ModelDev& M = a.models[mi];
         const SceneDev& S = a.scenes[si];
         if (M.scope == SCOPE_LOCAL && S.active) {
-            const double dt = S.dt;
-            const float dtf = (float)dt;
-            const float pad = 2.0f * disp;
-            const float4 mf0 = a.mf[2 * mi], mf1 = a.mf[2 * mi + 1];
-            const bool mobile = M.behavior == BEH_MOBILE;
+            local = true;
             // the clean-walk count is kept by the light tick when there is one
-            const uint32_t qc = a.work ? 0u : a.qcnt[i];
+            qc = a.work ? 0u : a.qcnt[i];
             const float2 cl = a.clear[i];
-            const bool quiet = qc >= 2u && !a.write_imp && pad <= cl.x && a.disp[1] <= cl.y;
-            bool dirty = false, any_exact = false;
-            K3 J, JA;
-            for (uint32_t base = e0; base < e1 && !quiet; base += TICK_GROUP) {
-                uint32_t exact = prefilter_group(a, base, e1, p32i, pad, dirty);
-                any_exact |= exact != 0u;
-                // Phase 2: the exact path for the flagged entries, in entry order
-                while (exact) {
-                const int k = __ffs(exact) - 1;
-                exact &= exact - 1;
-                const uint32_t e = base + k;
-                const uint32_t ent = a.nent[e];            // (reloaded: a register array indexed by k would spill)
-                const uint32_t meta = a.nmeta[e];
-                const uint32_t j = ent & ~WALL_BIT;
-                const bool wall = ent & WALL_BIT;
-                // canonical orientation (Assembler.cpp:43-67), fixed at rebuild; sphere-wall: the sphere is the slave
-                const bool i_slave = meta & META_SLAVE;
-                const bool owner = meta & META_OWNER;
-                const uint32_t s = i_slave ? i : j, m = i_slave ? j : i;
-                const uint32_t pi = meta & META_PI;
-                const uint32_t slot = owner ? e : a.nslot[e];
-                const PairParam& P = a.params[pi];
-                const double4_32a gg = a.geom[pi];
-                bool active;
-                float depth;
-                f3 n, rA, rB;
-                if (P.cd == CD_SS) {
-                    // d = x_master - x_slave, |d|^2 and R^2 - |d|^2 in double-float from the two
-                    // positions' hi/lo splits; where the numerator is within 1e-9 R^2 of zero the
-                    // reference's FP64 formula decides
-                    float4 hi_i, lo_i, hj, lj;
-                    if (XS) {
-                        hj = a.xsA[2 * j];
-                        lj = a.xsA[2 * j + 1];
-                        hi_i = a.xsA[2 * i];
-                        lo_i = a.xsA[2 * i + 1];
-                    } else {
-                        const d3 Pj = ld(a.xA, j);
-                        split32(Pj.x, hj.x, lj.x);
-                        split32(Pj.y, hj.y, lj.y);
-                        split32(Pj.z, hj.z, lj.z);
-                        split32(Pi.x, hi_i.x, lo_i.x);
-                        split32(Pi.y, hi_i.y, lo_i.y);
-                        split32(Pi.z, hi_i.z, lo_i.z);
-                    }
-                    const float4 hs = i_slave ? hi_i : hj, ls = i_slave ? lo_i : lj;
-                    const float4 hm = i_slave ? hj : hi_i, lm = i_slave ? lj : lo_i;
-                    const dfl dx = df_diff(hm.x, lm.x, hs.x, ls.x), dy = df_diff(hm.y, lm.y, hs.y, ls.y),
-                              dz = df_diff(hm.z, lm.z, hs.z, ls.z);
-                    const dfl s2 = df_add(df_add(df_sq(dx), df_sq(dy)), df_sq(dz));
-                    const float4 rq = a.rr32[pi];                // R^2 hi, R^2 lo, band, R
-                    const dfl num = df_add(dfl{rq.x, rq.y}, dfl{-s2.hi, -s2.lo});
-                    if (num.hi < -rq.z || num.hi > rq.z) {
-                        active = num.hi > 0.0f;
-                        depth = (num.hi + num.lo) / (rq.w + sqrtf(s2.hi));
-                    } else {                               // tie band: the reference's formula decides
-                        const d3 Pj = ld(a.xA, j);
-                        const d3 d = i_slave ? sub(Pj, Pi) : sub(Pi, Pj);
-                        const double dex = __dsub_rn(__dadd_rn(gg.x, gg.y), xlen(d));
-                        active = dex > 0.0;
-                        depth = (float)dex;
-                    }
-                    const f3 df = fm(dx.hi + dx.lo, dy.hi + dy.lo, dz.hi + dz.lo);
-                    n = fdir(df);
-                    rA = ((float)gg.x - 0.5f * depth) * n;
-                    rB = rA - df;
-                } else {
-                    const d3 Pj = ld(a.xA, j);
-                    const d3 Ps = i_slave ? Pi : Pj, Pm = i_slave ? Pj : Pi;
-                    d3 nd, pt;
-                    const double dex = wall_detect(P.cd, gg.x, gg.y, gg.z, gg.w, Ps, Pm, ld(a.ox, m), ld(a.oz, m), nd,
-                                                   pt, P.cd == CD_SHP ? a.hole[pi] : make_double4_32a(0, 0, 0, 0));
-                    active = dex > 0.0;
-                    depth = (float)dex;
-                    n = fm((float)nd.x, (float)nd.y, (float)nd.z);
-                    const d3 ra = sub(pt, Ps), rb = sub(pt, Pm);
-                    rA = fm((float)ra.x, (float)ra.y, (float)ra.z);
-                    rB = fm((float)rb.x, (float)rb.y, (float)rb.z);
-                }
-                const uint8_t f0 = a.fA[slot];
-                uint8_t f = f0 & 15;
-                float4 h = (f != 0 || active) ? a.hA[slot] : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
-                f3 Jp = fm(0.0f, 0.0f, 0.0f), tA = Jp, tB = Jp;
-                const int app = solve32<LAW>(P.is, a.pc32 + 8 * (size_t)pi, active, depth, n, rA, rB,
-                                        f4to3(a.v32A[s]), f4to3(a.v32A[m]), f4to3(a.w32A[s]), f4to3(a.w32A[m]), dtf, f,
-                                        h, Jp, tA, tB);
-                if (e == slot) {                           // history owner writes the new status
-                    if (f != 0 || (f0 & 15) != 0) {
-                        a.hB[slot] = h;
-                        a.fB[slot] = (uint8_t)(f | ((f == 0) ? HF_PENDING : 0));
-                    } else if (f0 & HF_PENDING) {
-                        a.hB[slot] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
-                        a.fB[slot] = 0;
-                    }
-                }
+            quiet = qc >= 2u && !a.write_imp && pad <= cl.x && a.disp[1] <= cl.y;
+            if (!quiet) {
+                const uint32_t e0 = a.nptr[i];
+                cnt = a.nptr[i + 1] - e0;
+                g.e0[lane] = e0;
+            }
+            g.dtf[lane] = (float)S.dt;
+        } else if (M.scope == SCOPE_LOCAL) {
+            hold_state(a, i);                  // a finished scene waits, unchanged
+        }
+    }
+    g.sid[lane] = i;
+    g.flags[lane] = 0u;
+    uint32_t incl = cnt;                       // rows: exclusive scan of the walked counts
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const uint32_t v = __shfl_up_sync(0xffffffffu, incl, o);
+        if (lane >= o) incl += v;
+    }
+    g.row[lane] = incl - cnt;
+    if (lane == 31) g.row[32] = incl;
+    const uint32_t total = __shfl_sync(0xffffffffu, incl, 31);
+    __syncwarp();
+    K3 J, JA;
+    for (uint32_t w0 = 0; w0 < total; w0 += TG_CAP) {
+        const uint32_t w1 = min(total, w0 + (uint32_t)TG_CAP);
+        uint32_t nx = 0;
+        for (uint32_t q0 = w0; q0 < w1; q0 += 32) {
+            const uint32_t q = q0 + lane;
+            bool ex = false;
+            if (q < w1) {
+                const int k = group_row(g.row, q);
+                const uint32_t e = g.e0[k] + (q - g.row[k]);
+                bool dirty = false;
+                ex = prefilter_entry(a, e, a.pos32[g.sid[k]], pad, dirty);
+                if (dirty || ex) atomicOr(&g.flags[k], (dirty ? 1u : 0u) | (ex ? 2u : 0u));
+                g.app[q - w0] = 0;
+            }
+            const unsigned m = __ballot_sync(0xffffffffu, ex);
+            if (ex) g.xq[nx + __popc(m & ((1u << lane) - 1u))] = (uint16_t)(q - w0);
+            nx += (uint32_t)__popc(m);
+        }
+        __syncwarp();
+        for (uint32_t x = lane; x < nx; x += 32) {
+            const uint32_t qq = g.xq[x];
+            const uint32_t q = w0 + qq;
+            const int k = group_row(g.row, q);
+            f3 cj, ct;
+            const int app = exact_entry<LAW, XS>(a, g.e0[k] + (q - g.row[k]), g.sid[k], g.dtf[k], cj, ct);
+            g.app[qq] = (uint8_t)app;
+            g.cj[qq] = make_float4(cj.x, cj.y, cj.z, 0.0f);
+            g.ct[qq] = make_float4(ct.x, ct.y, ct.z, 0.0f);
+        }
+        __syncwarp();
+        if (cnt) {                             // this lane's row within the window, in list order
+            const uint32_t rb = g.row[lane];
+            const uint32_t r0 = max(rb, w0), r1 = min(rb + cnt, w1);
+            for (uint32_t q = r0; q < r1; ++q) {
+                const int app = g.app[q - w0];
                 if (app) {
-                    if (i_slave) {
-                        J.add(Jp);
-                        if (app == 2) JA.add(tA);
-                    } else {
-                        J.add(-Jp);
-                        if (app == 2) JA.add(tB);
-                    }
-                }
-                if (wall && a.write_imp) {                 // the wall's share, summed per wall later
-                    float* o = a.wimp + 6 * (size_t)e;
-                    o[0] = app ? -Jp.x : 0.0f; o[1] = app ? -Jp.y : 0.0f; o[2] = app ? -Jp.z : 0.0f;
-                    o[3] = app == 2 ? tB.x : 0.0f; o[4] = app == 2 ? tB.y : 0.0f; o[5] = app == 2 ? tB.z : 0.0f;
-                }
+                    J.add(f4to3(g.cj[q - w0]));
+                    if (app == 2) JA.add(f4to3(g.ct[q - w0]));
                 }
             }
-            if (!a.work && !quiet) note_walk(a, i, qc, dirty || any_exact);
-            vmax_local = finish_sphere<XS>(a, i, mobile, quiet, S, Pi, V, mf0, mf1, J, JA);
-        } else if (M.scope == SCOPE_LOCAL) {
-            hold_state(a, i);                      // a finished scene waits, unchanged
         }
+        __syncwarp();
+    }
+    if (local) {
+        if (!a.work && !quiet) note_walk(a, i, qc, g.flags[lane] != 0u);
+        const d3 Pi = ld(a.xA, i);
+        const d3 V = ld(a.v64, i);
+        const float4 mf0 = a.mf[2 * mi], mf1 = a.mf[2 * mi + 1];
+        vmax_local = finish_sphere<XS>(a, i, a.models[mi].behavior == BEH_MOBILE, quiet, a.scenes[si], Pi, V, mf0,
+                                       mf1, J, JA);
     }
     return vmax_local;
 }
@@ -797,30 +945,34 @@ __device__ __forceinline__ void step_order() {
     asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
 }
 
-// The full tick, one thread per sphere.
+// The full tick: one warp per group of 32 consecutive spheres.
 template <int LAW, bool XS>
 __global__ void __launch_bounds__(TPB) k_tick(TickArgs a) {
+    extern __shared__ GroupSmem tick_smem[];
     step_order();
     const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
     float2 vmax_local = make_float2(0.0f, 0.0f);
     if (held_step(a)) {                          // the same value for every thread of the launch
         hold_state(a, t);
-    } else if (t < a.n) {
-        vmax_local = tick_sphere<LAW, XS>(a, t);
+    } else {
+        vmax_local = tick_group<LAW, XS>(a, t < a.n ? t : 0xffffffffu, tick_smem[threadIdx.x >> 5]);
     }
     reduce_vmax(a, vmax_local);
 }
 
 // The full tick of the split tick: a grid sized to the resident threads strides over the
-// spheres the light kernel deferred (none in a held step).
+// spheres the light kernel deferred (none in a held step), 32 to a warp.
 template <int LAW, bool XS>
 __global__ void __launch_bounds__(TPB) k_tick_work(TickArgs a) {
+    extern __shared__ GroupSmem tick_smem[];
     step_order();
     float2 vmax_local = make_float2(0.0f, 0.0f);
     if (!held_step(a)) {
         const uint32_t nw = *a.nwork;
-        for (uint32_t q = blockIdx.x * blockDim.x + threadIdx.x; q < nw; q += gridDim.x * blockDim.x)
-            vmax_local = fmax2(vmax_local, tick_sphere<LAW, XS>(a, a.work[q]));
+        const uint32_t lane = threadIdx.x & 31u;
+        for (uint32_t g0 = blockIdx.x * blockDim.x + (threadIdx.x & ~31u); g0 < nw; g0 += gridDim.x * blockDim.x)
+            vmax_local = fmax2(vmax_local, tick_group<LAW, XS>(a, g0 + lane < nw ? a.work[g0 + lane] : 0xffffffffu,
+                                                               tick_smem[threadIdx.x >> 5]));
     }
     reduce_vmax(a, vmax_local);
 }
@@ -1144,6 +1296,7 @@ __global__ void __launch_bounds__(TPB) k_nbr(uint32_t nloc, const uint32_t* __re
                                              const PairParam* __restrict__ params, const float* __restrict__ reach,
                                              const float4* __restrict__ pos32,
                                              const float4* __restrict__ wall32, float skin,
+                                             const uint32_t* __restrict__ ext_of, const uint32_t* __restrict__ int_of,
                                              uint32_t* __restrict__ cnt_or_ptr, uint32_t* __restrict__ ent) {
     const uint32_t P = blockIdx.x * blockDim.x + threadIdx.x;
     if (P >= nloc) return;
@@ -1177,7 +1330,7 @@ __global__ void __launch_bounds__(TPB) k_nbr(uint32_t nloc, const uint32_t* __re
                     float err;
                     const float d = dist32(pi, pos32[j], err);
                     if (d - err > (r + skin) * (1.0f + 4.0f * PF_ARITH_EPS)) continue;
-                    if (FILL) ent[off + c] = j;
+                    if (FILL) ent[off + c] = ext_of[j];          // sorted below by the caller's index
                     ++c;
                 }
             }
@@ -1193,18 +1346,23 @@ __global__ void __launch_bounds__(TPB) k_nbr(uint32_t nloc, const uint32_t* __re
             float err;
             const float d = cd == CD_SP ? plane_dist32(pi, pos32[w], wl, err) : line_dist32(pi, pos32[w], wl, err);
             const float sk = models[model_of[w]].behavior == BEH_ORBITAL ? WALL_SKIN * skin : skin;
-            if (d - err > (reach[pw] + sk) * (1.0f + 4.0f * PF_ARITH_EPS)) continue;
+            if (cd == CD_SIC) {                        // clear of the shell by more than the skin
+                if (d + err < -(reach[pw] + sk) * (1.0f - 4.0f * PF_ARITH_EPS)) continue;
+            } else if (d - err > (reach[pw] + sk) * (1.0f + 4.0f * PF_ARITH_EPS)) {
+                continue;
+            }
         }
-        if (FILL) ent[off + c] = w | WALL_BIT;
+        if (FILL) ent[off + c] = ext_of[w] | WALL_BIT;
         ++c;
     }
     if (!FILL) {
         cnt_or_ptr[i] = c;
         return;
     }
-    // Canonical order: spheres by index, then walls by index.  Every per-sphere sum then runs
-    // in an order that depends neither on the cell grid nor on when the list was rebuilt, nor
-    // on where the scene sits in a batch (indices only shift by the scene's offset).
+    // Canonical order: spheres by the caller's index, then walls by the caller's index.  Every
+    // per-sphere sum then runs in an order that depends neither on the cell grid nor on when
+    // the list was rebuilt, nor on where the scene sits in a batch (indices only shift by the
+    // scene's offset), nor on the engine's storage order.
     for (uint32_t q = 1; q < c; ++q) {
         const uint32_t v = ent[off + q];
         uint32_t r = q;
@@ -1213,6 +1371,10 @@ __global__ void __launch_bounds__(TPB) k_nbr(uint32_t nloc, const uint32_t* __re
             --r;
         }
         ent[off + r] = v;
+    }
+    for (uint32_t q = 0; q < c; ++q) {                  // back to storage indices
+        const uint32_t v = ent[off + q];
+        ent[off + q] = (v & WALL_BIT) | int_of[v & ~WALL_BIT];
     }
 }
 
@@ -1249,7 +1411,8 @@ __global__ void __launch_bounds__(TPB) k_meta(uint32_t n, const uint32_t* __rest
                                               const ModelDev* __restrict__ models,
                                               const uint32_t* __restrict__ scene_of,
                                               const SceneDev* __restrict__ scenes,
-                                              const PairParam* __restrict__ params, uint32_t* __restrict__ meta) {
+                                              const PairParam* __restrict__ params, const uint32_t* __restrict__ ext_of,
+                                              uint32_t* __restrict__ meta) {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     const uint32_t mi = model_of[i];
@@ -1266,13 +1429,13 @@ __global__ void __launch_bounds__(TPB) k_meta(uint32_t n, const uint32_t* __rest
             const ModelDev& N = models[mj];
             if (M.density == 0.0 && N.density != 0.0) i_slave = false;
             else if (N.density == 0.0 && M.density != 0.0) i_slave = true;
-            else i_slave = i < j;
+            else i_slave = ext_of[i] < ext_of[j];
         }
         const uint32_t pi = pidx(S, i_slave ? mi : mj, i_slave ? mj : mi);
         const PairParam& P = params[pi];
         const bool bond = (P.is == IS_BSDBF || P.is == IS_BTSDBF || P.is == IS_BSDB2F) && P.c[4] != 0.0;
         const bool moving = (v & WALL_BIT) && models[mj].behavior == BEH_ORBITAL;
-        meta[e] = (pi & META_PI) | ((uint32_t)(cd_plane(P.cd) & 3) << META_CD_SHIFT) | (bond ? META_BOND : 0u) |
+        meta[e] = (pi & META_PI) | ((uint32_t)(cd_plane(P.cd) & META_CD_MASK) << META_CD_SHIFT) | (bond ? META_BOND : 0u) |
                   (slot[e] == e ? META_OWNER : 0u) | (i_slave ? META_SLAVE : 0u) | (moving ? META_MOVING : 0u);
     }
 }
@@ -1331,7 +1494,7 @@ __global__ void __launch_bounds__(TPB) k_clear(uint32_t n, const uint32_t* __res
         const float4 pi = pos32[i];
         for (uint32_t e = ptr[i]; e < ptr[i + 1]; ++e) {
             const uint32_t m = meta[e];
-            const int cd = (int)((m >> META_CD_SHIFT) & 3u);
+            const int cd = (int)((m >> META_CD_SHIFT) & META_CD_MASK);
             if (cd == 0) continue;
             const uint32_t j = ent[e] & ~WALL_BIT;
             const bool wall = ent[e] & WALL_BIT;
@@ -1353,7 +1516,10 @@ __global__ void __launch_bounds__(TPB) k_clear(uint32_t n, const uint32_t* __res
                 gap = sqrtf(cx * cx + cy * cy + cz * cz);
             }
             const float r = reach[m & META_PI];
-            float t = (gap - ps.w - pm.w - PF_ARITH_EPS * (fabsf(dx) + fabsf(dy) + fabsf(dz))) * (1.0f - 1e-4f) - r;
+            const float slack = ps.w + pm.w + PF_ARITH_EPS * (fabsf(dx) + fabsf(dy) + fabsf(dz));
+            // inside a hollow cylinder (r = -(R - r_s)): the room left between the centre's axis
+            // distance and R - r_s
+            float t = cd == CD_SIC ? (-r - gap - slack) * (1.0f - 1e-4f) : (gap - slack) * (1.0f - 1e-4f) - r;
             bool ok = false;
             for (int k = 0; k < 4 && t >= 0.0f && !ok; ++k) {
                 ok = apart32(cd, ps, pm, ws, r + t);
@@ -1401,7 +1567,7 @@ __global__ void __launch_bounds__(TPB) k_interior(uint32_t n, const uint32_t* __
             if (!(lx > 0.0)) continue;
             const d3 ux = muls(Ox, 1.0 / lx), uy = cross(uz, ux);
             in = fabs(dot(d, ux)) <= 0.5 * W.a0 - m && fabs(dot(d, uy)) <= 0.5 * W.a2 - m;
-        } else if (W.shape == SHAPE_CYL) {
+        } else if (W.shape == SHAPE_CYL || W.shape == SHAPE_INNER_CYL) {
             in = fabs(dot(d, uz)) <= 0.5 * W.a1 - m;
         }
         if (in) meta[e] |= META_INTERIOR;
@@ -1535,7 +1701,7 @@ __global__ void __launch_bounds__(TPB) k_active(uint32_t n, TickArgs a, uint8_t*
             const ModelDev& N = a.models[mj];
             if (M.density == 0.0 && N.density != 0.0) i_slave = false;
             else if (N.density == 0.0 && M.density != 0.0) i_slave = true;
-            else i_slave = i < j;
+            else i_slave = a.ext_of[i] < a.ext_of[j];
         }
         const uint32_t s = i_slave ? i : j, m = i_slave ? j : i;
         const uint32_t pi = pidx(a.scenes[a.scene_of[i]], i_slave ? mi : mj, i_slave ? mj : mi);
@@ -1564,13 +1730,15 @@ __global__ void __launch_bounds__(TPB) k_pack3m(uint32_t n, const double* __rest
 // can stay when the displacement bound absorbs it; any change to a wall's position, velocity,
 // angular velocity or orientation is flagged (its cached motion terms need a rebuild).
 __global__ void __launch_bounds__(TPB) k_place(uint32_t n, const double* __restrict__ src, double4_32a* __restrict__ dst,
+                                               const uint32_t* __restrict__ ext_of,
                                                const uint32_t* __restrict__ model_of,
                                                const ModelDev* __restrict__ models, int wall_field,
                                                unsigned* __restrict__ jump, unsigned* __restrict__ wall_moved) {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     float d = 0.0f;
     if (i < n) {
-        const double nx = src[3 * (size_t)i], ny = src[3 * (size_t)i + 1], nz = src[3 * (size_t)i + 2];
+        const size_t e = ext_of[i];                   // the caller's index of stored object i
+        const double nx = src[3 * e], ny = src[3 * e + 1], nz = src[3 * e + 2];
         const double4_32a o = dst[i];
         if (models[model_of[i]].scope == SCOPE_LOCAL) {
             if (jump) {
@@ -1590,14 +1758,37 @@ __global__ void __launch_bounds__(TPB) k_place(uint32_t n, const double* __restr
         if ((threadIdx.x & 31) == 0 && d > 0.0f) atomicMax(jump, __float_as_uint(d));
     }
 }
-__global__ void __launch_bounds__(TPB) k_unpack3m(uint32_t n, const double4_32a* __restrict__ src, double* __restrict__ dst) {
+// n objects of the caller's order starting at `off` into [n][3] doubles: object off + i is
+// stored at int_of[off + i]
+__global__ void __launch_bounds__(TPB) k_unpack3m(uint32_t n, uint32_t off, const uint32_t* __restrict__ int_of,
+                                                  const double4_32a* __restrict__ src, double* __restrict__ dst) {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i < n) {
-        const double4_32a v = src[i];
+        const double4_32a v = src[int_of[off + i]];
         dst[3 * (size_t)i] = v.x;
         dst[3 * (size_t)i + 1] = v.y;
         dst[3 * (size_t)i + 2] = v.z;
     }
+}
+// [n][3] doubles of the caller's order into storage order
+__global__ void __launch_bounds__(TPB) k_gather3(uint32_t n, const uint32_t* __restrict__ ext_of,
+                                                 const double* __restrict__ src, double* __restrict__ dst) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const size_t e = ext_of[i];
+    dst[3 * (size_t)i] = src[3 * e];
+    dst[3 * (size_t)i + 1] = src[3 * e + 1];
+    dst[3 * (size_t)i + 2] = src[3 * e + 2];
+}
+// positions and models in the caller's order, for the observables that list every object
+__global__ void __launch_bounds__(TPB) k_to_caller(uint32_t n, const uint32_t* __restrict__ int_of,
+                                                   const double4_32a* __restrict__ x, const uint32_t* __restrict__ model_of,
+                                                   double4_32a* __restrict__ xe, uint32_t* __restrict__ me) {
+    const uint32_t e = blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= n) return;
+    const uint32_t i = int_of[e];
+    xe[e] = x[i];
+    me[e] = model_of[i];
 }
 // positions as hi/lo FP32 splits, for the stored way of the double-float pair test
 __global__ void __launch_bounds__(TPB) k_split(uint32_t n, const double4_32a* __restrict__ x, float4* __restrict__ xs) {
@@ -1671,7 +1862,9 @@ __global__ void k_wall_speed(uint32_t nglob, const uint32_t* __restrict__ glob, 
     if (M.behavior != BEH_ORBITAL) return;
     const d3 V = ld(v64, w), W = ld(w64, w), Oz = ld(oz, w);
     const double lz = len(Oz);
-    const double R = 0.5 * sqrt(M.a0 * M.a0 + M.a1 * M.a1 + M.a2 * M.a2) + (double)reach;
+    // the wall's farthest point from its centre (a hollow cylinder: its rim), plus the reach
+    const double R = (M.shape == SHAPE_INNER_CYL ? sqrt(M.a0 * M.a0 + 0.25 * M.a1 * M.a1)
+                                                 : 0.5 * sqrt(M.a0 * M.a0 + M.a1 * M.a1 + M.a2 * M.a2)) + (double)reach;
     double sp = len(V) + len(W) * R;
     if (lz > 0.0) {
         const d3 u = muls(Oz, 1.0 / lz);
@@ -1793,6 +1986,56 @@ __global__ void __launch_bounds__(TPB) k_row_fill(uint32_t n, const MoveScene* _
     }
 }
 
+// Morton (Z-order) code of a cell triple, 21 bits per axis.
+inline uint64_t morton3(uint64_t x, uint64_t y, uint64_t z) {
+    auto spread = [](uint64_t v) {
+        v &= 0x1fffffull;
+        v = (v | v << 32) & 0x1f00000000ffffull;
+        v = (v | v << 16) & 0x1f0000ff0000ffull;
+        v = (v | v << 8) & 0x100f00f00f00f00full;
+        v = (v | v << 4) & 0x10c30c30c30c30c3ull;
+        v = (v | v << 2) & 0x1249249249249249ull;
+        return v;
+    };
+    return spread(x) | spread(y) << 1 | spread(z) << 2;
+}
+
+// The order in which the engine stores a scene's objects: its spheres by the Z-order code of
+// the cell of edge 2 r_max that holds their centre (ties by index), then its walls in their
+// own order.  Spheres near one another in space sit near one another in memory, so the
+// neighbours a warp gathers share cache lines whatever order the caller numbered them in.
+// Returns perm with perm[internal] = the caller's (scene-local) index.
+std::vector<uint32_t> spatial_order(const HScene& h, const Tables& t) {
+    std::vector<uint32_t> sph, wal;
+    double lo[3] = {DBL_MAX, DBL_MAX, DBL_MAX}, rmax = 0.0;
+    for (uint32_t i = 0; i < h.n; ++i) {
+        const ModelDev& M = t.models[h.model_of[i]];
+        if (M.scope == SCOPE_LOCAL) {
+            sph.push_back(i);
+            rmax = std::max(rmax, M.a0);
+            for (int k = 0; k < 3; ++k) lo[k] = std::min(lo[k], h.pos[3 * (size_t)i + k]);
+        } else {
+            wal.push_back(i);
+        }
+    }
+    const double cell = rmax > 0.0 ? 2.0 * rmax : 1.0;
+    std::vector<std::pair<uint64_t, uint32_t>> key(sph.size());
+    for (size_t q = 0; q < sph.size(); ++q) {
+        uint64_t c[3];
+        for (int k = 0; k < 3; ++k) {
+            const double f = std::floor((h.pos[3 * (size_t)sph[q] + k] - lo[k]) / cell);
+            c[k] = f > 0.0 ? (uint64_t)std::min(f, 2097151.0) : 0u;   // NaN and negative: cell 0
+        }
+        key[q] = {morton3(c[0], c[1], c[2]), sph[q]};
+    }
+    std::sort(key.begin(), key.end());
+    std::vector<uint32_t> perm;
+    perm.reserve(h.n);
+    for (const auto& kv : key) perm.push_back(kv.second);
+    perm.insert(perm.end(), wal.begin(), wal.end());
+    return perm;
+}
+
 }  // namespace
 
 // ==========================================================================================
@@ -1830,6 +2073,7 @@ public:
     int coordination(uint32_t* below, uint32_t* touching, const double* box, double* average) override;
     int write_vtk(const char* path, int with_coordination) override;
     DeviceObjects objects();
+    int caller_view();
     double time() const override { return sc_.empty() ? 0.0 : sc_[0].t; }
     uint64_t steps() const override { return round_; }
     uint64_t steps_remaining() const override {
@@ -1879,6 +2123,9 @@ private:
         float skin = 0, rmax = 0;
         bool active = true;
         uint64_t steps = 0;         // steps this scene has taken (in this engine and before)
+        // the scene's objects in the engine's storage order: perm[internal] = the caller's
+        // scene-local index (spatial_order)
+        std::shared_ptr<const std::vector<uint32_t>> perm;
     };
     int fail(int c, const std::string& m) { err_ = m; return c; }
     int cuda_fail(cudaError_t e, const char* where) {
@@ -1986,6 +2233,11 @@ private:
     uint32_t wimp_cap_ = 0;
     double* d_stage_ = nullptr;
     double* d_obs_ = nullptr;
+    // storage order: internal index -> the caller's (global) index, and back
+    uint32_t* d_ext_of_ = nullptr;
+    uint32_t* d_int_of_ = nullptr;
+    double4_32a* d_xe_ = nullptr;                 // positions in the caller's order (observables)
+    uint32_t* d_model_e_ = nullptr;               // models in the caller's order (observables)
 };
 
 #define MCK(call)                                                 \
@@ -2033,7 +2285,7 @@ MixedEngine::~MixedEngine() {
                     d_scenes_, d_gfield_, d_glob_, d_x_[0], d_x_[1], d_v64_, d_w64_, d_ox_, d_oz_, d_imp_, d_aimp_,
                     d_v32_[0], d_v32_[1], d_w32_[0], d_w32_[1], d_rr32_, d_xs_[0], d_xs_[1], d_work_, d_clear_, d_vred_, d_ext_, d_qcnt_, d_pos32_, d_wall32_, d_red_, d_sred_, d_disp_, d_err_,
                     d_key_, d_key_alt_, d_sid_, d_sid_alt_, d_cnt_, d_gs_, d_ge_, d_act_, d_stage_, d_obs_, d_gidx_,
-                    d_wkey_, d_wval_, d_wkey_alt_, d_wval_alt_, d_wptr_, d_wimp_, d_wred_, d_wrot_, d_wedge_};
+                    d_wkey_, d_wval_, d_wkey_alt_, d_wval_alt_, d_wptr_, d_wimp_, d_wred_, d_wrot_, d_wedge_, d_ext_of_, d_int_of_, d_xe_, d_model_e_};
     for (void* p : ptrs) if (p) cudaFree(p);
     drop_graphs();
     for (auto& e : pev_) cudaEventDestroy(e);
@@ -2080,7 +2332,7 @@ int MixedEngine::init_from(const std::vector<SceneSource>& src, const MixedEngin
     }
     if (src.empty()) return fail(VEDO_ERR_INVALID_SCENE, "empty batch");
     // ---- per-scene tables, concatenated
-    std::vector<uint32_t> model_of, scene_of;
+    std::vector<uint32_t> model_of, scene_of, ext_of;
     std::vector<double> st[7];                 // staged host state of the new scenes
     std::vector<double4_32a> geo, rr, hole;
     std::vector<float4> rr32;
@@ -2117,9 +2369,15 @@ int MixedEngine::init_from(const std::vector<SceneSource>& src, const MixedEngin
         S.t_stop = h.time_stop;
         for (int k = 0; k < 3; ++k) S.g[k] = h.g[k];
         double rmax = 0.0;
+        S.perm = kept ? prev->sc_[so.prev_scene].perm
+                      : std::make_shared<const std::vector<uint32_t>>(spatial_order(h, t));
+        const std::vector<uint32_t>& perm = *S.perm;
+        std::vector<uint32_t> inv(h.n);
+        for (uint32_t q = 0; q < h.n; ++q) inv[perm[q]] = q;
+        for (uint32_t q = 0; q < h.n; ++q) ext_of.push_back(n_ + perm[q]);
         S.wall_beg = (uint32_t)glob_.size();
         for (uint32_t i = 0; i < h.n; ++i) {
-            const ModelDev& M = t.models[h.model_of[i]];
+            const ModelDev& M = t.models[h.model_of[perm[i]]];
             if (M.scope == SCOPE_LOCAL) {
                 if (M.shape != SHAPE_SPHERE)
                     return fail(VEDO_ERR_UNSUPPORTED_MODEL, "mixed form: local (scope) objects must be spheres");
@@ -2130,7 +2388,7 @@ int MixedEngine::init_from(const std::vector<SceneSource>& src, const MixedEngin
                     return fail(VEDO_ERR_UNSUPPORTED_MODEL, "mixed form: walls must be fixed or orbital");
                 glob_.push_back(n_ + i);
             }
-            model_of.push_back(S.model_off + h.model_of[i]);
+            model_of.push_back(S.model_off + h.model_of[perm[i]]);
             scene_of.push_back((uint32_t)sc_.size());
         }
         S.wall_end = (uint32_t)glob_.size();
@@ -2141,15 +2399,21 @@ int MixedEngine::init_from(const std::vector<SceneSource>& src, const MixedEngin
         } else {
             moves.push_back(MoveScene{n_, h.n, n_stage, 1u});
             const std::vector<double>* a[7] = {&h.pos, &h.vel, &h.av, &h.ox, &h.oz, &h.imp, &h.aimp};
-            for (int k = 0; k < 7; ++k) st[k].insert(st[k].end(), a[k]->begin(), a[k]->end());
-            // IactRecordTab records, owned by the lower sphere (or the sphere of a wall pair)
+            for (int k = 0; k < 7; ++k)              // staged in storage order
+                for (uint32_t i = 0; i < h.n; ++i)
+                    st[k].insert(st[k].end(), a[k]->begin() + 3 * (size_t)perm[i], a[k]->begin() + 3 * (size_t)perm[i] + 3);
+            // IactRecordTab records, owned by the lower sphere (or the sphere of a wall pair),
+            // with their objects in storage order
             recs.resize((size_t)n_stage + h.n);
             for (uint32_t q = 0; q < h.rec.size(); ++q) {
                 uint32_t ra = h.rec.first[q], rb = h.rec.second[q];
                 if (ra >= h.n || rb >= h.n) continue;
-                const bool aw = t.models[h.model_of[ra]].scope != SCOPE_LOCAL;
-                const bool bw = t.models[h.model_of[rb]].scope != SCOPE_LOCAL;
+                ra = inv[ra];
+                rb = inv[rb];
+                const bool aw = t.models[h.model_of[perm[ra]]].scope != SCOPE_LOCAL;
+                const bool bw = t.models[h.model_of[perm[rb]]].scope != SCOPE_LOCAL;
                 if (aw && !bw) std::swap(ra, rb);
+                else if (!aw && !bw && rb < ra) std::swap(ra, rb);   // the row of the history owner
                 Rec r;
                 r.a = n_stage + ra;
                 r.b = (n_ + rb) | ((aw || bw) ? WALL_BIT : 0u);
@@ -2185,7 +2449,8 @@ int MixedEngine::init_from(const std::vector<SceneSource>& src, const MixedEngin
             if (P.cd == CD_SS) r = g[0] + g[1];
             else if (cd_plane(P.cd) == CD_SP) r = g[0] + 0.5 * g[2];
             else if (P.cd == CD_SC) r = g[0] + g[1];
-            reach.push_back((float)r * (1.0f + 1e-6f));
+            // inside a hollow cylinder: -(R - r), its magnitude rounded down (apart32)
+            reach.push_back(P.cd == CD_SIC ? (float)(g[0] - g[1]) * (1.0f - 1e-6f) : (float)r * (1.0f + 1e-6f));
         }
         for (const ModelDev& M : t.models) {
             double gi[3];
@@ -2218,8 +2483,13 @@ int MixedEngine::init_from(const std::vector<SceneSource>& src, const MixedEngin
     if ((rc = up(&d_models_, models_)) || (rc = up(&d_params_, params_)) || (rc = up(&d_pc32_, pc)) ||
         (rc = up(&d_geom_, geo)) || (rc = up(&d_hole_, hole)) || (rc = up(&d_rr_, rr)) || (rc = up(&d_rr32_, rr32)) || (rc = up(&d_mf_, mf)) || (rc = up(&d_reach_, reach)) ||
         (rc = up(&d_model_of_, model_of)) || (rc = up(&d_scene_of_, scene_of)) || (rc = up(&d_gfield_, gfield)) ||
-        (rc = up(&d_glob_, glob_)))
+        (rc = up(&d_glob_, glob_)) || (rc = up(&d_ext_of_, ext_of)))
         return rc;
+    {
+        std::vector<uint32_t> int_of(n_);
+        for (uint32_t i = 0; i < n_; ++i) int_of[ext_of[i]] = i;
+        if ((rc = up(&d_int_of_, int_of))) return rc;
+    }
     {
         std::vector<uint32_t> gidx(n_, 0xffffffffu);
         for (uint32_t q = 0; q < glob_.size(); ++q) gidx[glob_[q]] = q;
@@ -2359,7 +2629,7 @@ int MixedEngine::get_state_slice(uint32_t off, uint32_t cnt, const vedo_state_vi
     for (int k = 0; k < 7; ++k) {
         if (!dst[k] || !cnt) continue;
         double* stg = d_stage_ + (size_t)k * 3 * n_;
-        k_unpack3m<<<nblk(cnt), TPB, 0, stream_>>>(cnt, src[k] + off, stg);
+        k_unpack3m<<<nblk(cnt), TPB, 0, stream_>>>(cnt, off, d_int_of_, src[k], stg);
         MCK(cudaMemcpyAsync(dst[k], stg, 24 * (size_t)cnt, cudaMemcpyDeviceToHost, stream_));
     }
     MCK(cudaStreamSynchronize(stream_));
@@ -2420,6 +2690,7 @@ TickArgs MixedEngine::args(bool write_imp) {
     a.clear = d_clear_;
     a.qcnt = d_qcnt_;
     a.ext = ext_on_ ? d_ext_ : nullptr;
+    a.ext_of = d_ext_of_;
     return a;
 }
 
@@ -2530,7 +2801,8 @@ int MixedEngine::rebuild() {
     if (nloc_) {
         k_nbr<false><<<nblk(nloc_), TPB, 0, stream_>>>(nloc_, d_sid_, d_key_, d_gs_, d_ge_, d_scene_of_, d_scenes_,
                                                        d_glob_, d_model_of_, d_models_, d_params_, d_reach_,
-                                                       d_pos32_, d_wall32_, skin_min_, d_cnt_, nullptr);
+                                                       d_pos32_, d_wall32_, skin_min_, d_ext_of_, d_int_of_, d_cnt_,
+                                                       nullptr);
         ++own;
     }
     MCK(exclusive_scan_u32(d_cnt_, L.ptr, n_ + 1, d_red_ + 9, scratch_, stream_));
@@ -2543,13 +2815,13 @@ int MixedEngine::rebuild() {
     if (nloc_) {
         k_nbr<true><<<nblk(nloc_), TPB, 0, stream_>>>(nloc_, d_sid_, d_key_, d_gs_, d_ge_, d_scene_of_, d_scenes_,
                                                       d_glob_, d_model_of_, d_models_, d_params_, d_reach_, d_pos32_,
-                                                      d_wall32_, skin_min_, L.ptr, L.ent);
+                                                      d_wall32_, skin_min_, d_ext_of_, d_int_of_, L.ptr, L.ent);
         ++own;
     }
     MCK(cudaMemsetAsync(d_err_, 0, 4, stream_));
     k_slots<<<nblk(n_), TPB, 0, stream_>>>(n_, L.ptr, L.ent, L.slot, d_err_);
     k_meta<<<nblk(n_), TPB, 0, stream_>>>(n_, L.ptr, L.ent, L.slot, d_model_of_, d_models_, d_scene_of_, d_scenes_,
-                                          d_params_, L.meta);
+                                          d_params_, d_ext_of_, L.meta);
     ++own;
     k_carry<<<nblk(n_), TPB, 0, stream_>>>(n_, L.ptr, L.ent, L.slot, O.ptr, O.ent, O.slot, O.h[cur_], O.f[cur_],
                                            L.h[cur_], L.f[cur_], L.h[cur_ ^ 1], L.f[cur_ ^ 1],
@@ -2631,11 +2903,12 @@ int MixedEngine::rebuild() {
 // A per-step kernel launch; `dep`: with programmatic dependent launch (the kernel orders itself
 // after the previous one with step_order()).
 template <typename... P, typename... A>
-static cudaError_t step_launch(bool dep, void (*k)(P...), unsigned grid, unsigned block, cudaStream_t s, A... args) {
+static cudaError_t step_launch_smem(bool dep, void (*k)(P...), unsigned grid, unsigned block, size_t smem,
+                                    cudaStream_t s, A... args) {
     cudaLaunchConfig_t cfg{};
     cfg.gridDim = dim3(grid);
     cfg.blockDim = dim3(block);
-    cfg.dynamicSmemBytes = 0;
+    cfg.dynamicSmemBytes = smem;
     cfg.stream = s;
     cudaLaunchAttribute at[1];
     at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
@@ -2643,6 +2916,11 @@ static cudaError_t step_launch(bool dep, void (*k)(P...), unsigned grid, unsigne
     cfg.attrs = at;
     cfg.numAttrs = dep ? 1 : 0;
     return cudaLaunchKernelEx(&cfg, k, args...);
+}
+
+template <typename... P, typename... A>
+static cudaError_t step_launch(bool dep, void (*k)(P...), unsigned grid, unsigned block, cudaStream_t s, A... args) {
+    return step_launch_smem(dep, k, grid, block, 0, s, args...);
 }
 
 void MixedEngine::launch_step(bool write_imp) {
@@ -2670,9 +2948,10 @@ void MixedEngine::launch_step(bool write_imp) {
         nb_full = std::min<unsigned>(nb, (unsigned)sms_ * 512u / (unsigned)tpb_);
     }
 #define VEDO_TICK(L)                                                                                        \
-    note(step_launch(dep, split_tick_ ? (xs_stored_ ? k_tick_work<L, true> : k_tick_work<L, false>)          \
-                                      : (xs_stored_ ? k_tick<L, true> : k_tick<L, false>),                   \
-                     split_tick_ ? nb_full : nb, (unsigned)tpb_, stream_, a))
+    note(step_launch_smem(dep, split_tick_ ? (xs_stored_ ? k_tick_work<L, true> : k_tick_work<L, false>)     \
+                                           : (xs_stored_ ? k_tick<L, true> : k_tick<L, false>),              \
+                          split_tick_ ? nb_full : nb, (unsigned)tpb_, sizeof(GroupSmem) * (size_t)(tpb_ / 32),   \
+                          stream_, a))
     switch (law_) {
     case IS_BSDBF: VEDO_TICK(IS_BSDBF); break;
     case IS_BTSDBF: VEDO_TICK(IS_BTSDBF); break;
@@ -2993,7 +3272,7 @@ int MixedEngine::get_state(const vedo_state_view& v) {
     for (int k = 0; k < 7; ++k) {
         if (!dst[k]) continue;
         double* st = d_stage_ + (size_t)k * 3 * n_;
-        k_unpack3m<<<nblk(n_), TPB, 0, stream_>>>(n_, src[k], st);
+        k_unpack3m<<<nblk(n_), TPB, 0, stream_>>>(n_, 0u, d_int_of_, src[k], st);
         MCK(cudaMemcpyAsync(dst[k], st, 24 * (size_t)n_, cudaMemcpyDeviceToHost, stream_));
     }
     MCK(cudaStreamSynchronize(stream_));
@@ -3010,8 +3289,13 @@ int MixedEngine::run_with_impulses(const double* impulse, const double* angular_
     const double* src[2] = {impulse, angular_impulse};
     for (int k = 0; k < 2; ++k) {
         double* dst = d_ext_ + (size_t)k * 3 * n_;
-        if (src[k]) MCK(cudaMemcpyAsync(dst, src[k], 24 * (size_t)n_, cudaMemcpyHostToDevice, stream_));
-        else MCK(cudaMemsetAsync(dst, 0, 24 * (size_t)n_, stream_));
+        if (src[k]) {                              // the caller's order, gathered into storage order
+            double* stg = d_stage_ + (size_t)k * 3 * n_;
+            MCK(cudaMemcpyAsync(stg, src[k], 24 * (size_t)n_, cudaMemcpyHostToDevice, stream_));
+            k_gather3<<<nblk(n_), TPB, 0, stream_>>>(n_, d_ext_of_, stg, dst);
+        } else {
+            MCK(cudaMemsetAsync(dst, 0, 24 * (size_t)n_, stream_));
+        }
     }
     ext_on_ = true;
     const int rc = run(1, keep_running);
@@ -3059,7 +3343,7 @@ int MixedEngine::set_state(const vedo_state_view& v) {
         if (!srcs[k]) continue;
         double* st = d_stage_ + (size_t)k * 3 * n_;
         MCK(cudaMemcpyAsync(st, srcs[k], 24 * (size_t)n_, cudaMemcpyHostToDevice, stream_));
-        k_place<<<nblk(n_), TPB, 0, stream_>>>(n_, st, dst[k], d_model_of_, d_models_, k < 5 ? 1 : 0,
+        k_place<<<nblk(n_), TPB, 0, stream_>>>(n_, st, dst[k], d_ext_of_, d_model_of_, d_models_, k < 5 ? 1 : 0,
                                                k == 0 ? d_red_ : nullptr, d_red_ + 1);
     }
     k_copy32<<<nblk(n_), TPB, 0, stream_>>>(n_, d_v64_, d_v32_[cur_]);
@@ -3132,17 +3416,19 @@ int MixedEngine::get_interactions(const vedo_contact_view& v) {
     }
     MCK(cudaStreamSynchronize(stream_));
     struct Row { uint32_t a, b, sl, ms; uint32_t e; };
+    std::vector<uint32_t> ext(n_);
+    MCK(cudaMemcpy(ext.data(), d_ext_of_, 4 * (size_t)n_, cudaMemcpyDeviceToHost));
     std::vector<Row> rows;
     for (uint32_t i = 0; i < n_; ++i)
         for (uint32_t e = ptr[i]; e < ptr[i + 1]; ++e) {
             if (slot[e] != e) continue;
-            const uint32_t j = ent[e] & ~WALL_BIT;
+            const uint32_t ei = ext[i], ej = ext[ent[e] & ~WALL_BIT];   // the caller's indices
             const bool wall = ent[e] & WALL_BIT;
             Row r;
-            r.a = std::min(i, j);
-            r.b = std::max(i, j);
-            r.sl = wall ? i : std::min(i, j);
-            r.ms = wall ? j : std::max(i, j);
+            r.a = std::min(ei, ej);
+            r.b = std::max(ei, ej);
+            r.sl = wall ? ei : std::min(ei, ej);
+            r.ms = wall ? ej : std::max(ei, ej);
             r.e = e;
             rows.push_back(r);
         }
@@ -3201,21 +3487,37 @@ int MixedEngine::get_observables(double out[13]) {
 }
 
 // the observables' view of the state: positions of the current parity, single-scene engines only
+// Positions and models in the caller's object order (the coordination numbers and the VTK file
+// list objects in that order).
+int MixedEngine::caller_view() {
+    if (!d_xe_) {
+        MCK(mal(&d_xe_, n_));
+        MCK(mal(&d_model_e_, n_));
+    }
+    k_to_caller<<<nblk(n_), TPB, 0, stream_>>>(n_, d_int_of_, d_x_[cur_], d_model_of_, d_xe_, d_model_e_);
+    MCK(cudaGetLastError());
+    return VEDO_OK;
+}
+
 DeviceObjects MixedEngine::objects() {
     DeviceObjects d;
-    d.n = n_; d.model_of = d_model_of_; d.models = d_models_; d.pos = d_x_[cur_];
+    d.n = n_; d.model_of = d_model_e_; d.models = d_models_; d.pos = d_xe_;
     d.stream = stream_; d.scratch = &scratch_; d.launches = &launches_;
     d.scene = sc_.size() == 1 ? host_[0].get() : nullptr;
     return d;
 }
 
 int MixedEngine::coordination(uint32_t* below, uint32_t* touching, const double* box, double* average) {
+    const int vr = caller_view();
+    if (vr != VEDO_OK) return vr;
     std::string m;
     const int rc = coordination_host(objects(), below, touching, box, average, m);
     return rc == VEDO_OK ? rc : fail(rc, m);
 }
 
 int MixedEngine::write_vtk(const char* path, int with_coordination) {
+    const int vr = caller_view();
+    if (vr != VEDO_OK) return vr;
     std::string m;
     const int rc = write_vtk_host(this, objects(), path, with_coordination, m);
     return rc == VEDO_OK ? rc : fail(rc, m);

@@ -203,6 +203,31 @@ extern "C" int vedo_gpu_system_energy_noalloc(const double* position, const doub
         set_last_error("vedo_gpu_system_energy_noalloc: NULL argument");
         return VEDO_ERR_INVALID_ARGUMENT;
     }
+    int dev = -1;
+    if (cudaGetDevice(&dev) != cudaSuccess) {
+        set_last_error("vedo_gpu_system_energy_noalloc: no current CUDA device");
+        return VEDO_ERR_CUDA;
+    }
+    // every buffer the kernels touch must be device (or managed) memory of the current device:
+    // a host pointer or another GPU's would only fail later, as an asynchronous fault
+    const void* bufs[] = {position, velocity, angular_velocity, mass, inertia, mobile, out};
+    const char* names[] = {"position", "velocity", "angular_velocity", "mass", "inertia", "mobile", "out"};
+    for (int k = 0; k < 7; ++k) {
+        if (!bufs[k] || (k < 6 && !num_objects)) continue;
+        cudaPointerAttributes at{};
+        const cudaError_t pe = cudaPointerGetAttributes(&at, bufs[k]);
+        if (pe != cudaSuccess) {
+            cudaGetLastError();                       // clear the error the query left
+            set_last_error(std::string("vedo_gpu_system_energy_noalloc: ") + names[k] + ": " + cudaGetErrorString(pe));
+            return VEDO_ERR_INVALID_ARGUMENT;
+        }
+        const bool device_mem = at.type == cudaMemoryTypeDevice || at.type == cudaMemoryTypeManaged;
+        if (!device_mem || (at.type == cudaMemoryTypeDevice && at.device != dev)) {
+            set_last_error(std::string("vedo_gpu_system_energy_noalloc: ") + names[k] +
+                           " is not device memory of the current device");
+            return VEDO_ERR_INVALID_ARGUMENT;
+        }
+    }
     double* scratch = nullptr;
     const int rc = scratch_for_current_device(&scratch);
     if (rc != VEDO_OK) return rc;

@@ -66,10 +66,13 @@ __device__ __forceinline__ float dist32_periodic(const float4& a, const float4& 
     return l;
 }
 
-// cd: 1 sphere-sphere, 2 sphere-plate (4, with a hole: tested as the full plate), 3 sphere-cylinder.  `reach` bounds the distance at
-// which the pair can be in contact (radius sum, or radius + plate half-thickness, or sphere
-// + cylinder radius), already rounded up.  `periodic`: the FP32 ranges of an active periodic
-// boundary (sphere pairs only).  True when the pair is certainly apart.
+// cd: 1 sphere-sphere, 2 sphere-plate (4, with a hole: tested as the full plate), 3 sphere-cylinder,
+// 5 sphere inside a hollow cylinder.  `reach` bounds the distance at which the pair can be in
+// contact (radius sum, or radius + plate half-thickness, or sphere + cylinder radius), already
+// rounded up; for cd 5 it is stored negated, -(R - r) rounded towards zero: the sphere is clear
+// of the shell while its centre is nearer the axis than R - r (so that a pad added to the
+// reach narrows that radius).  `periodic`: the FP32 ranges of an active periodic boundary
+// (sphere pairs only).  True when the pair is certainly apart.
 __device__ __forceinline__ bool certainly_apart(int cd, const float4& s, const float4& m, const float4& wall,
                                                 float reach, const float* periodic = nullptr) {
     float e, d;
@@ -81,6 +84,7 @@ __device__ __forceinline__ bool certainly_apart(int cd, const float4& s, const f
     } else {
         if (wall.w == 0.0f) return false;
         d = line_dist32(s, m, wall, e);
+        if (cd == 5) return d + e < -reach * (1.0f - 4.0f * PF_ARITH_EPS);
     }
     return d - e > reach * (1.0f + 4.0f * PF_ARITH_EPS);
 }

@@ -87,6 +87,14 @@ bool analyse(const HModel& m, ModelDev& o) {
         // the only factories: fixed and mobile (ModuleList.h:50,56); a mobile one moves as an
         // orbital plate does (DOQuasiPlateWithCircularHole.cpp:22-38), which is not restated
         if (m.behavior != BEH_FIXED) return false;
+    } else if (m.shape == SHAPE_INNER_CYL) {
+        // engine extension (no reference counterpart): a shell of no thickness and no mass, range
+        // 0; only walls (global scope) that are fixed or turn about their own centre
+        if (m.scope != SCOPE_GLOBAL || (m.behavior != BEH_FIXED && m.behavior != BEH_ORBITAL)) return false;
+        if (!(m.attrs[0] > 0.0) || !(m.attrs[1] > 0.0)) return false;
+        o.range = 0.0;
+        vol = mass = sudo_model = 0.0;
+        o.ix = o.iy = o.iz = 0.0;
     } else if (m.shape == SHAPE_PLATE) {
         double w = m.attrs[0], h = m.attrs[1], l = m.attrs[2];
         o.range = (m.scope == SCOPE_LOCAL) ? 0.5 * std::max(std::max(w, h), l) : 0.5 * h;
@@ -502,7 +510,7 @@ int build_tables(const HScene& s, Tables& t, std::string& err) {
             int ia = t.group_iact[(size_t)S.group * G + M.group];
             if (ia < 0 || S.shape != SHAPE_SPHERE) continue;
             int cd = M.shape == SHAPE_SPHERE ? CD_SS : M.shape == SHAPE_PLATE ? CD_SP : M.shape == SHAPE_CYL ? CD_SC
-                     : M.shape == SHAPE_HOLED ? CD_SHP : 0;
+                     : M.shape == SHAPE_HOLED ? CD_SHP : M.shape == SHAPE_INNER_CYL ? CD_SIC : 0;
             const HIact& im = s.iacts[ia];
             int is = eq_of(im.equation_type);
             if (!cd || !is) continue;                      // the factories return null (Assembler.cpp:72-85)

@@ -30,6 +30,10 @@ import numpy as np
 # enum DOShapeType : _uint_t (DOModel.h:25, C++11 build)
 NO_SHAPE, SPHERE, DMSPHERE, ELLIPSOID, POLYHEDRA, POLYHEDRA_BREP, QUASI_CYLINDER, QUASI_PLATE, \
     QUASI_PLATE_WITH_CIRCULAR_HOLE, TRIANGLE = range(10)
+# No counterpart in the reference: the inside of a hollow cylinder (a drum shell), attrs
+# (radius, length) about OrientationZ, global scope, fixed or orbital.  An engine extension;
+# scenes that use it cannot be read by the reference.
+INNER_CYLINDER = 32
 # enum DOBehaviorType : _uint_t (DOModel.h:26)
 NO_BEHAVIOR, CONSTRAINED, FIXED, MOBILE, ORBITAL = range(5)
 # enum DOScopeType : _uint_t (DOModel.h:27)
@@ -105,6 +109,10 @@ class DOModel:
             sm = self.density_factor * m
             mmi = m * (3.0 * r * r + h * h) / 12.0
             return rng, vol, m, sm, (mmi, mmi, 0.5 * m * r * r)
+        if self.shape == INNER_CYLINDER:
+            if self.scope != GLOBAL:
+                raise ValueError(f"model {self.name!r}: an inner cylinder must have global scope")
+            return 0.0, 0.0, 0.0, 0.0, (0.0, 0.0, 0.0)
         if self.shape == QUASI_PLATE:
             w, h, l = a[0], a[1], a[2]
             rng = 0.5 * max(max(w, h), l) if self.scope == LOCAL else 0.5 * h

@@ -39,7 +39,7 @@ from typing import List, Optional, Sequence, Tuple
 
 import numpy as np
 
-from .scene import (CONSTRAINED, FIXED, GLOBAL, LOCAL, MOBILE, ORBITAL, QUASI_CYLINDER, QUASI_PLATE,
+from .scene import (CONSTRAINED, FIXED, GLOBAL, INNER_CYLINDER, LOCAL, MOBILE, ORBITAL, QUASI_CYLINDER, QUASI_PLATE,
                     QUASI_PLATE_WITH_CIRCULAR_HOLE, SPHERE,
                     Boundary, DOModel, IactModel, Scene, SystemParameter)
 
@@ -163,6 +163,37 @@ def _sequential_placement(rng, radii: np.ndarray, inside, lo: np.ndarray, hi: np
     return out[keep], keep
 
 
+def place_spheres(radii: np.ndarray, lo, hi, cyl_radius: float = 0.0, seed: int = 0, max_tries: int = 2000):
+    """Seeded random sequential placement through the engine library (vedo_place_spheres):
+    sphere i, in the given order, is drawn uniformly in the box [lo, hi] (and, for
+    cyl_radius > 0, inside that cylinder about the x axis), each wholly inside, and kept at
+    its first draw that overlaps no sphere kept before.  Returns ([n][3] centres with NaN for
+    spheres not placed, number placed)."""
+    import ctypes as C
+    from .engine import lib
+    L = lib()
+    dp = C.POINTER(C.c_double)
+    L.vedo_place_spheres.argtypes = [C.c_uint32, dp, dp, dp, C.c_double, C.c_uint64, C.c_uint32, dp,
+                                     C.POINTER(C.c_uint32)]
+    radii = np.ascontiguousarray(radii, np.float64)
+    lo = np.ascontiguousarray(lo, np.float64)
+    hi = np.ascontiguousarray(hi, np.float64)
+    out = np.empty((radii.shape[0], 3))
+    placed = C.c_uint32(0)
+    rc = L.vedo_place_spheres(radii.shape[0], radii.ctypes.data_as(dp), lo.ctypes.data_as(dp), hi.ctypes.data_as(dp),
+                              float(cyl_radius), int(seed) & (2**64 - 1), int(max_tries), out.ctypes.data_as(dp),
+                              C.byref(placed))
+    if rc != 0:
+        raise ValueError(f"vedo_place_spheres failed ({rc})")
+    return out, int(placed.value)
+
+
+def _circle_area_below(R: float, c: float) -> float:
+    """Area of the disc of radius R about the origin below the line z = c."""
+    c = min(max(c, -R), R)
+    return R * R * math.acos(-c / R) + c * math.sqrt(max(R * R - c * c, 0.0))
+
+
 def cluster(n: int = 64, seed: int = 7, solver: str = "ISwBSDBF", walls: str = "box", steps: int = 200,
             dt: float = 1e-6, radius: float = 1e-3, polydisperse: bool = False, density: float = 2500.0,
             vel_sigma: float = 0.2, orbital: bool = False, cylinders: int = 0, spacing: float = 2.05e-3,
@@ -243,18 +274,26 @@ def hertz_drum(n: int = 1_000_000, seed: int = 2024, steps: int = 10000, dt: flo
                median_r: float = 1e-3, sigma_log: float = 0.2, r_lo: float = 0.5e-3, r_hi: float = 2e-3,
                E: float = 70e9, nu: float = 0.25, restitution: float = 0.7, mu: float = 0.4,
                density: float = 2500.0, R: float = 0.15, L: float = 0.3, rpm: float = 30.0,
-               facets: int = 64, gap: float = 0.01, solver: str = "ISwH", vel_sigma: float = 0.0) -> Scene:
+               facets: int = 64, gap: float = 0.01, solver: str = "ISwH", vel_sigma: float = 0.0,
+               fill: str = "rsa", rsa_fraction: float = 0.30, shell: str = "cylinder") -> Scene:
     """Polydisperse Hertz drum.
 
     Radii are lognormal(median_r, sigma_log) clipped to [r_lo, r_hi] and binned into K
     log-spaced classes; each class is one DOModel and one group, with K(K+1)/2 sphere-sphere
     and K sphere-wall interaction models (Hertz stiffness from E, nu and the class radii).
-    The shell is `facets` fixed quasi-plates on a circle of radius R around the x axis; the
-    two end plates are orbital plates spinning at `rpm` about x.  The spheres fill the drum
-    from the bottom in horizontal lattice layers, largest first, each layer's spacing set by
-    its largest sphere plus a `gap` fraction, which leaves no initial overlap and packs the
-    1,000,000 default spheres into about 40 % of the drum volume.  Initial velocities are zero
-    unless `vel_sigma` (m/s, per component) is given.
+    shell="cylinder" (the default): the shell is one orbital hollow cylinder of radius R about
+    the x axis turning at `rpm` with the end plates (the engine's inner-cylinder extension; the
+    reference has no hollow cylinder, so such a scene runs on the engine and its oracle only).
+    shell="polygon": `facets` fixed quasi-plates on a circle of radius R, which the reference
+    can read.  The two end plates are orbital plates spinning at `rpm` about x.
+
+    fill="rsa" (the default): random sequential placement, largest spheres first, in the part
+    of the drum below the height at which the spheres make up `rsa_fraction` of its volume
+    (0.30: the 1,000,000 default spheres, about 5.0e-3 m^3 of solid, occupy the lower ~75 % of
+    the drum; settled under gravity they fill it to about 35-40 %).  fill="lattice": horizontal
+    lattice layers from the bottom, largest first, each layer's spacing set by its largest
+    sphere plus a `gap` fraction (no initial overlap, about 40 % of the drum volume).  Initial
+    velocities are zero unless `vel_sigma` (m/s, per component) is given.
 
     Object order is a seeded permutation with one sphere of the largest class moved to the end
     of the sphere block.  The reference's NBS broad phase takes its cell size from the radius of
@@ -266,11 +305,31 @@ def hertz_drum(n: int = 1_000_000, seed: int = 2024, steps: int = 10000, dt: flo
     centres = np.sqrt(edges[:-1] * edges[1:])
     r = np.clip(median_r * np.exp(sigma_log * rng.standard_normal(n)), r_lo, r_hi)
     cls = np.clip(np.searchsorted(edges, r, side="right") - 1, 0, K - 1).astype(np.uint32)
-    cls = np.sort(cls)[::-1].copy()            # largest classes first (bottom layers)
+    cls = np.sort(cls)[::-1].copy()            # largest classes first (bottom layers / placed first)
     radii = centres[cls]
     pos = np.zeros((n, 3))
     z = -R
     placed = 0
+    if fill == "rsa":
+        solid = float(np.sum(4.0 / 3.0 * math.pi * radii ** 3))
+        lo_z, hi_z = -R, R                     # height below which the drum holds solid / rsa_fraction
+        for _ in range(80):
+            mid = 0.5 * (lo_z + hi_z)
+            if _circle_area_below(R, mid) * L * rsa_fraction < solid:
+                lo_z = mid
+            else:
+                hi_z = mid
+        z_top = hi_z
+        for attempt in range(40):
+            top = min(z_top * 1.0 + attempt * 0.01 * R, R)
+            pos, placed = place_spheres(radii, (-0.5 * L, -R, -R), (0.5 * L, R, top), cyl_radius=R,
+                                        seed=seed * 1000003 + attempt)
+            if placed == n:
+                break
+        if placed != n:
+            raise ValueError(f"random sequential placement kept {placed} of {n} spheres")
+    elif fill != "lattice":
+        raise ValueError(f"unknown fill {fill!r}")
     while placed < n:
         rl = radii[placed]                       # largest radius of this layer (sorted descending)
         a = 2.0 * rl * (1.0 + gap)
@@ -289,7 +348,8 @@ def hertz_drum(n: int = 1_000_000, seed: int = 2024, steps: int = 10000, dt: flo
         pos[placed:placed + take] = sites[:take]
         placed += take
         z += a
-    pos += rng.uniform(-0.25 * gap, 0.25 * gap, size=pos.shape) * radii[:, None]
+    if fill == "lattice":
+        pos += rng.uniform(-0.25 * gap, 0.25 * gap, size=pos.shape) * radii[:, None]
     perm = rng.permutation(n)                  # object order independent of the layer order
     last = int(np.flatnonzero(cls[perm] == cls.max())[-1])
     perm[[last, n - 1]] = perm[[n - 1, last]]  # a largest-class sphere last: see the docstring
@@ -299,20 +359,32 @@ def hertz_drum(n: int = 1_000_000, seed: int = 2024, steps: int = 10000, dt: flo
     for k in range(K):
         models.append(DOModel(f"B{k:03d}", f"B{k:03d}", MOBILE, LOCAL, density, 1.0, SPHERE, (float(centres[k]),)))
     thick = 4e-3
-    fw = 2.0 * R * math.tan(math.pi / facets) * 1.02
-    shell = DOModel("Shell", "Wall", FIXED, GLOBAL, 0.0, 1.0, QUASI_PLATE, (L + 2 * thick, thick, fw))
-    endp = DOModel("EndPl", "Wall", ORBITAL, GLOBAL, 0.0, 1.0, QUASI_PLATE, (2.2 * R, thick, 2.2 * R))
-    models += [shell, endp]
-    wp, wox, woz, wav, widx = [], [], [], [], []
-    for f in range(facets):
-        th = 2.0 * math.pi * (f + 0.5) / facets
-        nrm = np.array([0.0, math.cos(th), math.sin(th)])
-        wp.append(nrm * (R + 0.5 * thick))
-        woz.append(-nrm)
-        wox.append([1.0, 0.0, 0.0])
-        wav.append([0.0, 0.0, 0.0])
-        widx.append(K)
     omega = rpm * 2.0 * math.pi / 60.0
+    if shell == "cylinder":
+        shell_m = DOModel("Shell", "Wall", ORBITAL, GLOBAL, 0.0, 1.0, INNER_CYLINDER, (R, L + 2 * thick))
+    elif shell == "polygon":
+        fw = 2.0 * R * math.tan(math.pi / facets) * 1.02
+        shell_m = DOModel("Shell", "Wall", FIXED, GLOBAL, 0.0, 1.0, QUASI_PLATE, (L + 2 * thick, thick, fw))
+    else:
+        raise ValueError(f"unknown shell {shell!r}")
+    endp = DOModel("EndPl", "Wall", ORBITAL, GLOBAL, 0.0, 1.0, QUASI_PLATE, (2.2 * R, thick, 2.2 * R))
+    models += [shell_m, endp]
+    wp, wox, woz, wav, widx = [], [], [], [], []
+    if shell == "cylinder":                    # axis x through the centre, turning about it
+        wp.append([0.0, 0.0, 0.0])
+        woz.append([1.0, 0.0, 0.0])
+        wox.append([0.0, 1.0, 0.0])
+        wav.append([omega, 0.0, 0.0])
+        widx.append(K)
+    else:
+        for f in range(facets):
+            th = 2.0 * math.pi * (f + 0.5) / facets
+            nrm = np.array([0.0, math.cos(th), math.sin(th)])
+            wp.append(nrm * (R + 0.5 * thick))
+            woz.append(-nrm)
+            wox.append([1.0, 0.0, 0.0])
+            wav.append([0.0, 0.0, 0.0])
+            widx.append(K)
     for sx in (-1.0, 1.0):
         wp.append([sx * (0.5 * L + 0.5 * thick), 0.0, 0.0])
         woz.append([-sx, 0.0, 0.0])
