@@ -371,3 +371,26 @@ def test_leap_self_pairs_are_refused_by_the_engine(engine_lib):
         engine_lib.GpuEngine(sc, up_iact=4, consultant="leap")
     assert ex.value.code == 3
     engine_lib.GpuEngine(sc, up_iact=4).close()     # the NBS list of the same layer is fine
+
+
+@pytest.mark.parametrize("case", ["box_lsd", "cluster_ISwH"])
+def test_system_status_csv_matches_reference(case, engine_lib, tmp_path):
+    """With an output prefix the FP64 form writes SystemStatus.csv as SimMediator does
+    (SimMediator.cpp:46-123): the same header, a line at creation and at every reset, the same
+    record and contact counts, and energies that print the same to the reference's 6 digits
+    (compared as numbers: the reductions add in another order)."""
+    g = np.load(os.path.join(ROOT, "tests", "golden", "status", f"{case}.npz"))
+    sc = Scene.from_ido(g["ido"].tobytes())
+    e = engine_lib.GpuEngine(sc, up_iact=int(g["up_iact"]), output_prefix=str(tmp_path / "w"))
+    e.run(int(g["steps"]))
+    e.close()
+    got = (tmp_path / "SystemStatus.csv").read_text().splitlines()
+    ref = g["csv"].tobytes().decode().splitlines()
+    assert got[0] == ref[0]
+    assert len(got) == len(ref)
+    for a, b in zip(got[1:], ref[1:]):
+        fa, fb = [x.strip() for x in a.split(",")], [x.strip() for x in b.split(",")]
+        assert len(fa) == len(fb)
+        assert fa[1:4] == fb[1:4], (a, b)                 # objects, records, contacts
+        np.testing.assert_allclose([float(x) for x in fa], [float(x) for x in fb], rtol=1e-5, atol=1e-300,
+                                   err_msg=f"{a} | {b}")

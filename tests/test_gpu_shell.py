@@ -1,0 +1,86 @@
+"""The hollow-cylinder (drum shell) extension on the GPU, in both engine forms.
+
+The reference cannot express a sphere inside a cylinder (its QuasiCylinder is the outside of a
+solid rod, CDSphere2QuasiCylinder.cpp:40-50), so parity here is against the analytic resting
+depth and against the C oracle, which carries the same extension: the FP64 form equals it bit
+for bit with the linear law and a fixed shell, and within the last-ulp differences of CUDA's
+pow/sin/cos (1e-9 relative) with ISwH and a turning shell; the mixed form keeps the FP64 form's
+contact set and its per-step impulses within 1e-5 relative."""
+import os
+import tempfile
+
+import numpy as np
+import pytest
+
+from vedo_gb300 import scenes
+
+pytestmark = pytest.mark.gpu
+
+M = 2500.0 * 4.0 / 3.0 * np.pi * 1e-9         # the shell_rest spheres' mass (r = 1 mm)
+
+
+@pytest.mark.parametrize("precision", [0, 1])
+def test_sphere_rests_at_the_analytic_depth(precision, engine_lib):
+    e = engine_lib.GpuEngine(scenes.shell_rest(), up_iact=1, precision=precision)
+    e.run(1)
+    J = e.state(("impact",))["impact"]
+    tol = 1e-9 if precision == 0 else 1e-5
+    assert np.abs(J[0]).max() <= tol * M * 9.81 * 1e-6, J[0]        # contact balances the field
+    np.testing.assert_allclose(J[1, 1], -1e4 * 1e-6 * 1e-6, rtol=tol)   # kn delta dt, outward normal
+    assert int(e.observables()[9]) == 2
+    e.close()
+
+
+def test_fp64_equals_oracle_with_fixed_shell_bit_for_bit(engine_lib, port_lib):
+    from oracle import PortWorld
+    sc = scenes.shell_drop()
+    e = engine_lib.GpuEngine(sc, up_iact=5)
+    p = PortWorld(sc, up_iact=5)
+    for _ in range(4):
+        e.run(250)
+        p.run(250)
+        a, b = e.state(), p.state()
+        for k in ("position", "velocity", "angular_velocity", "impact", "angular_impact"):
+            np.testing.assert_array_equal(a[k], b[k], err_msg=k)
+    ia, ib = e.interactions(), p.interactions()
+    f, s = p.candidates()
+    assert np.array_equal(ia["first"], f) and np.array_equal(ia["second"], s)
+    assert np.array_equal(ia["active"], ib["active"].astype(np.uint8))
+
+
+def test_fp64_equals_oracle_with_turning_shell(engine_lib, port_lib):
+    from oracle import PortWorld
+    sc = scenes.shell_drop(solver="ISwH", rpm=300.0, dt=2e-7, steps=5000)
+    e = engine_lib.GpuEngine(sc, up_iact=5)
+    p = PortWorld(sc, up_iact=5)
+    e.run(3000)
+    p.run(3000)
+    a, b = e.state(), p.state()
+    for k in ("position", "velocity", "angular_velocity"):
+        np.testing.assert_allclose(a[k], b[k], rtol=1e-9, atol=1e-12 * np.abs(b[k]).max(), err_msg=k)
+    ia, ib = e.interactions(), p.interactions()
+    assert np.array_equal(ia["active"], ib["active"].astype(np.uint8))
+
+
+def test_mixed_against_fp64_with_turning_shell(engine_lib):
+    sc = scenes.shell_drop(solver="ISwH", rpm=300.0, dt=2e-7, steps=5000)
+    f64 = engine_lib.GpuEngine(sc, up_iact=5)
+    f64.run(1500)
+    with tempfile.TemporaryDirectory() as td:
+        path = os.path.join(td, "s.ido")
+        f64.write_ido(path)
+        a = engine_lib.GpuEngine(path, up_iact=5)
+        b = engine_lib.GpuEngine(path, up_iact=5, precision=1)
+    A, B = a.interactions(), b.interactions()
+    sa = set(zip(A["first"][A["active"] == 1].tolist(), A["second"][A["active"] == 1].tolist()))
+    sb = set(zip(B["first"][B["active"] == 1].tolist(), B["second"][B["active"] == 1].tolist()))
+    assert sa == sb
+    a.run(1)
+    b.run(1)
+    ja, jb = a.state(("impact",))["impact"], b.state(("impact",))["impact"]
+    assert np.linalg.norm(ja - jb) <= 1e-5 * np.linalg.norm(ja)
+    for _ in range(6):
+        a.run(250)
+        b.run(250)
+    oa, ob = a.observables(), b.observables()
+    assert abs((oa[1] + oa[2]) - (ob[1] + ob[2])) <= 0.01 * (oa[1] + oa[2])

@@ -314,3 +314,40 @@ def test_port_matches_reference_whole_run_start(port_lib):
             for k in ("position", "velocity", "angular_velocity"):
                 np.testing.assert_array_equal(st[k], g[f"first100_{k}"], err_msg=k)
     w.close()
+
+
+def test_inner_cylinder_detector_analytic(port_lib):
+    """The hollow-cylinder extension (a drum shell; the reference has none): a sphere resting on
+    the bottom at the linear law's equilibrium depth m g / kn, and a sphere pressed 1 um into the
+    side.  Depths and outward radial normals are the analytic ones, and after one step the
+    resting sphere's total impulse (contact + field) vanishes to rounding."""
+    from oracle import PortWorld
+    sc = scenes.shell_rest()
+    m = 2500.0 * 4.0 / 3.0 * np.pi * 1e-9
+    w = PortWorld(sc, up_iact=1)
+    it = w.interactions()
+    assert list(it["master"]) == [2, 2] and list(it["active"]) == [1, 1]
+    np.testing.assert_allclose(it["depth"], [m * 9.81 / 1e4, 1e-6], rtol=1e-6)
+    np.testing.assert_allclose(it["normal"], [[0.0, 0.0, -1.0], [0.0, 1.0, 0.0]], atol=1e-12)
+    w.run(1)
+    J = w.state()["impact"]
+    assert np.abs(J[0]).max() <= 1e-9 * m * 9.81 * 1e-6
+    np.testing.assert_allclose(J[1, 1], -1e4 * 1e-6 * 1e-6, rtol=1e-6)
+    w.close()
+
+
+def test_inner_cylinder_scene_keeps_every_sphere_inside_and_reaches_the_shell(port_lib):
+    """shell_drop (the scene of the GPU shell tests): spheres start clear of the shell and of one
+    another, and within 1,000 steps of the oracle they reach it and bounce off it."""
+    from oracle import PortWorld
+    sc = scenes.shell_drop()
+    w = PortWorld(sc, up_iact=5)
+    hits = 0
+    for _ in range(10):
+        w.run(100)
+        it = w.interactions()
+        hits += int(it["active"][it["master"] == 150].sum())
+    assert hits > 10
+    v = w.state()["velocity"][:150]
+    assert np.abs(v).max() < 3.0
+    w.close()

@@ -827,6 +827,7 @@ int Engine::ensure_list(PairList& L, uint32_t cap) {
 }
 
 Engine::~Engine() {
+    if (status_) std::fclose(status_);
     if (stream_) cudaStreamSynchronize(stream_);
     free_list(cur_);
     free_list(old_);
@@ -977,7 +978,65 @@ int Engine::init(const HScene& scene, const vedo_engine_opts& opts) {
     if (rc != VEDO_OK) return rc;
     CK(cudaStreamSynchronize(stream_));
     backup_pending_ = false;
+    if (!out_prefix_.empty()) {
+        // SimMediator's constructor (SimMediator.cpp:103-123): the SystemStatus.csv header, then
+        // CalculateSystemEnergy with the IactRecordTab read from the file
+        std::string dir = out_prefix_;
+        const size_t slash = dir.find_last_of('/');
+        dir = slash == std::string::npos ? std::string() : dir.substr(0, slash + 1);
+        status_ = std::fopen((dir + "SystemStatus.csv").c_str(), "w");
+        if (!status_) return fail(VEDO_ERR_IO, "cannot write " + dir + "SystemStatus.csv");
+        std::fprintf(status_, "Simulated time, number of elements, number of interactions, Number of contacts, "
+                              "System energy, Potential energy, Kinetic energy, Kinetic energy (translation), "
+                              "Kinetic energy (rotation), Minimal velocity, Maximal velocity, "
+                              "Minimal angular velocity, Maximal angular velocity, Norm of momentum, "
+                              "Norm of angular momentum");
+        for (uint32_t u = 0; u < 2 * host_.num_udd_impact; ++u) std::fprintf(status_, ", User-defined Value %u", u + 1);
+        std::fprintf(status_, "\n");
+        uint64_t contacts = 0;
+        for (size_t q = 0; q < host_.rec.first.size(); ++q) contacts += host_.rec.contact[q] ? 1u : 0u;
+        rc = status_row(host_.rec.first.size(), contacts);
+        if (rc != VEDO_OK) return rc;
+    }
     return VEDO_OK;
+}
+
+// One line of SystemStatus.csv (SimMediator::CalculateSystemEnergy, SimMediator.cpp:46-81):
+// time, object count, IactRecordTab size and contact count, then the energies and extrema of
+// DOWorld::CalculateSystemEnergy, as the reference's ostream writes them (6 significant
+// digits).  The user-defined impact values, which the engine does not carry, are written as 0.
+int Engine::status_row(uint64_t records, uint64_t contacts) {
+    double o[13];
+    const int rc = get_observables(o);
+    if (rc != VEDO_OK) return rc;
+    std::fprintf(status_, "%g, %u, %llu, %llu, %g, %g, %g, %g, %g, %g, %g, %g, %g, %g, %g", t_, n_,
+                 (unsigned long long)records, (unsigned long long)contacts, o[0] + o[1] + o[2], o[0], o[1] + o[2],
+                 o[1], o[2], o[3], o[4], o[5], o[6], o[7], o[8]);
+    for (uint32_t u = 0; u < 2 * host_.num_udd_impact; ++u) std::fprintf(status_, ", 0");
+    std::fprintf(status_, "\n");
+    std::fflush(status_);
+    return VEDO_OK;
+}
+
+// The line SimMediator::Run writes at a reset or record step: the record table rebuilt from the
+// interactions that are active at the new positions (NBSConsultant::RebuildIactRecordTab,
+// NBSConsultant.cpp:376-389), and among them those whose status holds a contact.
+int Engine::status_row_now() {
+    uint64_t active = 0, contacts = 0;
+    if (cur_.np) {
+        k_detect_active<<<blocks_for(cur_.np), TPB, 0, stream_>>>(cur_.np, cur_.sm, cur_.param, d_params_, d_geom_,
+                                                                  d_hole_, d_reach_, d_pos_, d_ox_, d_oz_, d_pos32_,
+                                                                  d_wall32_, cur_.flags, tab_.pbc);
+        std::vector<uint8_t> f(cur_.np);
+        CK(cudaMemcpyAsync(f.data(), cur_.flags, cur_.np, cudaMemcpyDeviceToHost, stream_));
+        CK(cudaStreamSynchronize(stream_));
+        for (uint8_t b : f)
+            if (b & PF_ACTIVE) {
+                ++active;
+                contacts += (b & ST_CONTACT) ? 1u : 0u;
+            }
+    }
+    return status_row(active, contacts);
 }
 
 int Engine::rebuild(bool from_records) {
@@ -1217,6 +1276,10 @@ int Engine::step_once(bool write_impulses) {
     }
     if (opts_.record && round_ % opts_.record == 0 && !out_prefix_.empty()) {
         int rc = record_ido();
+        if (rc != VEDO_OK) return rc;
+    }
+    if (status_ && (round_ % opts_.up_iact == 0 || (opts_.record && round_ % opts_.record == 0))) {
+        int rc = status_row_now();                         // SimMediator.cpp:784-792
         if (rc != VEDO_OK) return rc;
     }
     if (t_ >= t_stop_ && !out_prefix_.empty()) {         // NBSConsultant.cpp:65-76

@@ -11,6 +11,7 @@
 #pragma once
 
 #include <cstdint>
+#include <cstdio>
 #include <string>
 #include <vector>
 
@@ -73,6 +74,9 @@ private:
     double* d_ext_ = nullptr;                        // [2][n][3] external impulses of run_with_impulses
     const double *ext_imp_ = nullptr, *ext_aimp_ = nullptr;
     int record_ido();
+    int status_row(uint64_t records, uint64_t contacts);   // one SystemStatus.csv line
+    int status_row_now();
+    std::FILE* status_ = nullptr;                    // <output dir>SystemStatus.csv, with an output prefix
     int sync_host_state();
     int ensure_stage();
 

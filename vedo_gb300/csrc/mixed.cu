@@ -222,12 +222,18 @@ __device__ __forceinline__ dfl df_sq(dfl a) {
 // x = hi + lo with hi = x rounded to FP32 (nearest, ties to even) and lo = (x - hi) rounded to
 // FP32, from the bits of x with integer operations (GB300's FP64 pipe is its scarcest): for
 // 2^-70 <= |x| < 2^101; zero, tiny and huge values take the FP64 conversions.
+// The FP64 conversions of the rare exponents, out of line: GB300 issues FP64 conversions on its
+// FP64 pipe (2 lanes per cycle per SM), and a short branch kept inline is predicated rather than
+// jumped over, so its FP64 instructions would be issued on every call.
+__device__ __noinline__ void split32_wide(double x, float& hi, float& lo) {
+    hi = (float)x;
+    lo = (float)(x - (double)hi);
+}
 __device__ __forceinline__ void split32(double x, float& hi, float& lo) {
     const unsigned long long u = (unsigned long long)__double_as_longlong(x);
     const int e = (int)((u >> 52) & 0x7ff) - 1023;           // unbiased exponent
     if (e < -70 || e > 100) {                                  // 2^(e-52) below stays a normal FP32
-        hi = (float)x;
-        lo = (float)(x - (double)hi);
+        split32_wide(x, hi, lo);
         return;
     }
     const unsigned long long mant = u & 0xfffffffffffffull;   // 52 bits
@@ -243,6 +249,32 @@ __device__ __forceinline__ void split32(double x, float& hi, float& lo) {
     const float unit = __uint_as_float((unsigned)(e - 52 + 127) << 23);   // 2^(e-52)
     const float lr = __int2float_rn(r) * unit;
     lo = r == 0 ? 0.0f : (sign ? -lr : lr);                     // x - hi = +0 when exact
+}
+
+// Exact FP32 <-> FP64 conversions from the bits, with integer operations: the same values as the
+// casts (round to nearest, ties to even), without GB300's FP64 pipe, which executes the casts.
+// Zero is handled inline; subnormal, huge and non-finite values take the casts out of line.
+__device__ __noinline__ double f2d_wide(float f) { return (double)f; }
+__device__ __noinline__ float d2f_wide(double x) { return (float)x; }
+__device__ __forceinline__ double f2d(float f) {
+    const unsigned b = __float_as_uint(f);
+    const unsigned ex = (b >> 23) & 0xffu;
+    if ((b << 1) == 0u) return __longlong_as_double((long long)((unsigned long long)b << 32));   // +-0
+    if (ex == 0u || ex == 0xffu) return f2d_wide(f);
+    const unsigned long long u = ((unsigned long long)(b >> 31) << 63) | ((unsigned long long)(ex + 896u) << 52) |
+                                 ((unsigned long long)(b & 0x7fffffu) << 29);
+    return __longlong_as_double((long long)u);
+}
+__device__ __forceinline__ float d2f(double x) {
+    const unsigned long long u = (unsigned long long)__double_as_longlong(x);
+    if ((u << 1) == 0ull) return __uint_as_float((unsigned)(u >> 32));                    // +-0
+    const int e = (int)((u >> 52) & 0x7ff) - 1023;
+    if (e < -126 || e > 126) return d2f_wide(x);
+    const unsigned long long mant = u & 0xfffffffffffffull;
+    const unsigned m23 = (unsigned)(mant >> 29);
+    const unsigned rem = (unsigned)(mant & 0x1fffffffu);
+    const bool up = rem > 0x10000000u || (rem == 0x10000000u && (m23 & 1u));
+    return __uint_as_float(((unsigned)(u >> 63) << 31) | ((((unsigned)(e + 127)) << 23) + m23 + (up ? 1u : 0u)));
 }
 
 // Kahan-compensated FP32 sum of 3-vectors
@@ -396,6 +428,7 @@ struct SceneDev {
     uint32_t nc[3];
     float lo[3], inv_h;
     double dt;
+    float dtf;                     // dt rounded to FP32 (the pair laws' time step)
     // The scene's drifting frame since the last rebuild: velocity u0 + gdt (k + 1/2) in step k
     // (free fall under the scene's field from the spheres' velocity midrange at the rebuild)
     float u0[3], gdt[3];
@@ -491,6 +524,32 @@ __device__ __forceinline__ void hold_state(const TickArgs& a, uint32_t i) {
             a.hB[e] = a.hA[e];
             a.fB[e] = a.fA[e];
         }
+}
+
+// The rare FP64 parts of the exact path, out of line: GB300 issues FP64 arithmetic, compares
+// and conversions on its FP64 pipe (2 lanes per cycle per SM), and a short branch kept inline is
+// predicated rather than jumped over, so its FP64 instructions would be issued for every pair.
+// Sphere pair in the tie band: the reference's formula, (ra + rb) - |x_m - x_s| in FP64.
+__device__ __noinline__ double tie_depth(const TickArgs& a, uint32_t pi, uint32_t s, uint32_t m) {
+    const double4_32a gg = a.geom[pi];
+    const d3 d = sub(ld(a.xA, m), ld(a.xA, s));
+    return __dsub_rn(__dadd_rn(gg.x, gg.y), xlen(d));
+}
+// Sphere-wall pair: the reference's detector in FP64 (wall_detect), the contact normal and
+// lever arms rounded to FP32.
+__device__ __noinline__ void wall_pair(const TickArgs& a, int cd, uint32_t pi, uint32_t s, uint32_t m, bool& active,
+                                       float& depth, f3& n, f3& rA, f3& rB) {
+    const double4_32a gg = a.geom[pi];
+    const d3 Ps = ld(a.xA, s), Pm = ld(a.xA, m);
+    d3 nd, pt;
+    const double dex = wall_detect(cd, gg.x, gg.y, gg.z, gg.w, Ps, Pm, ld(a.ox, m), ld(a.oz, m), nd, pt,
+                                   cd == CD_SHP ? a.hole[pi] : make_double4_32a(0, 0, 0, 0));
+    active = dex > 0.0;
+    depth = (float)dex;
+    n = fm((float)nd.x, (float)nd.y, (float)nd.z);
+    const d3 ra = sub(pt, Ps), rb = sub(pt, Pm);
+    rA = fm((float)ra.x, (float)ra.y, (float)ra.z);
+    rB = fm((float)rb.x, (float)rb.y, (float)rb.z);
 }
 
 // Phase 1 of a sphere's neighbour walk, for the group of entries at `base`: the entries and
@@ -606,7 +665,7 @@ __device__ __forceinline__ float2 finish_sphere(const TickArgs& a, uint32_t i, b
         const f3 Jf = fm(J.s.x - J.c.x, J.s.y - J.c.y, J.s.z - J.c.z);
         const f3 JAf = fm(JA.s.x - JA.c.x, JA.s.y - JA.c.y, JA.s.z - JA.c.z);
         const f3 dv = mf0.w * Jf, dw = mf1.x * JAf;
-        const d3 dvd = mk((double)dv.x, (double)dv.y, (double)dv.z);
+        const d3 dvd = mk(f2d(dv.x), f2d(dv.y), f2d(dv.z));
         const d3 P2 = mk(fma(dt, fma(0.5, dvd.x, V.x), Pi.x), fma(dt, fma(0.5, dvd.y, V.y), Pi.y),
                          fma(dt, fma(0.5, dvd.z, V.z), Pi.z));
         const d3 V2 = add(V, dvd);
@@ -622,13 +681,13 @@ __device__ __forceinline__ float2 finish_sphere(const TickArgs& a, uint32_t i, b
             a.xsB[2 * i + 1] = l2;
         }
         if (dw.x != 0.0f || dw.y != 0.0f || dw.z != 0.0f) {
-            const d3 W2 = add(ld(a.w64, i), mk((double)dw.x, (double)dw.y, (double)dw.z));
+            const d3 W2 = add(ld(a.w64, i), mk(f2d(dw.x), f2d(dw.y), f2d(dw.z)));
             st(a.w64, i, W2, 0.0);
-            a.w32B[i] = make_float4((float)W2.x, (float)W2.y, (float)W2.z, 0.0f);
+            a.w32B[i] = make_float4(d2f(W2.x), d2f(W2.y), d2f(W2.z), 0.0f);
         } else if (!quiet) {                       // no torque: omega + 0 is omega
             a.w32B[i] = a.w32A[i];
         }
-        const float4 vn = make_float4((float)V2.x, (float)V2.y, (float)V2.z, 0.0f);
+        const float4 vn = make_float4(d2f(V2.x), d2f(V2.y), d2f(V2.z), 0.0f);
         a.v32B[i] = vn;
         const float ox = vn.x - dv.x, oy = vn.y - dv.y, oz = vn.z - dv.z;
         const float vabs2 = fmaxf(fmaf(oz, oz, fmaf(oy, oy, ox * ox)), fmaf(vn.z, vn.z, fmaf(vn.y, vn.y, vn.x * vn.x)));
@@ -650,269 +709,135 @@ __device__ __forceinline__ float2 finish_sphere(const TickArgs& a, uint32_t i, b
     return make_float2(0.0f, 0.0f);
 }
 
-// One list entry's prefilter: the per-entry form of prefilter_group (the same decisions, the
-// same history cleaning and wall-impulse writes).  Returns true when the entry needs the exact
-// path; `dirty` is set when a history was cleaned.
-__device__ __forceinline__ bool prefilter_entry(const TickArgs& a, uint32_t e, const float4& p32i, float pad,
-                                                bool& dirty) {
-    const uint32_t meta = a.nmeta[e];
-    const int cd = (int)((meta >> META_CD_SHIFT) & META_CD_MASK);
-    if (cd == 0) return false;
-    if (meta & META_BOND) return true;
-    const uint32_t ent = a.nent[e];
-    const uint32_t j = ent & ~WALL_BIT;
-    const bool wall = ent & WALL_BIT;
-    const bool i_slave = meta & META_SLAVE;
-    const float4 pj = a.pos32[j];
-    const float4 ws = wall ? a.wall32[j] : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
-    float pk = pad;
-    if (wall) {
-        pk = (meta & META_INTERIOR) ? fminf(a.disp[1], a.disp[0] + ws.w) : a.disp[1];
-        if (meta & META_MOVING) pk += a.disp[2];
-    }
-    if (!apart32(cd, i_slave ? p32i : pj, i_slave ? pj : p32i, ws, a.reach[meta & META_PI] + pk)) return true;
-    if (wall && a.write_imp) {
-        float* o = a.wimp + 6 * (size_t)e;
-        o[0] = o[1] = o[2] = o[3] = o[4] = o[5] = 0.0f;
-    }
-    if (meta & META_OWNER) {
-        const uint8_t f0 = a.fA[e];
-        if (f0 & 15) {                         // ImpactStatus::Clean
-            a.hB[e] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
-            a.fB[e] = HF_PENDING;
-            dirty = true;
-        } else if (f0 & HF_PENDING) {
-            a.hB[e] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
-            a.fB[e] = 0;
-        }
-    }
-    return false;
-}
-
-// One list entry of sphere i on the exact path: the pair in canonical (slave, master)
-// orientation from the previous positions, the FP32 velocity copies and the pair's history
-// (identical inputs for both members, so both obtain the same impulse), the history update by
-// the entry that holds it, and the wall's share of the impulse.  Returns 0 (nothing added),
-// 1 (impulse) or 2 (impulse and torque) with sphere i's share of each in cj, ct.
+// One sphere's step: neighbour walk (prefilter, then the exact path in entry order), sums,
+// integration.  Returns its squared speed bounds of the step.
 template <int LAW, bool XS>
-__device__ __forceinline__ int exact_entry(const TickArgs& a, uint32_t e, uint32_t i, float dtf, f3& cj, f3& ct) {
-    const uint32_t ent = a.nent[e];
-    const uint32_t meta = a.nmeta[e];
-    const uint32_t j = ent & ~WALL_BIT;
-    const bool wall = ent & WALL_BIT;
-    // canonical orientation (Assembler.cpp:43-67), fixed at rebuild; sphere-wall: the sphere is the slave
-    const bool i_slave = meta & META_SLAVE;
-    const bool owner = meta & META_OWNER;
-    const uint32_t s = i_slave ? i : j, m = i_slave ? j : i;
-    const uint32_t pi = meta & META_PI;
-    const uint32_t slot = owner ? e : a.nslot[e];
-    const PairParam& P = a.params[pi];
-    const double4_32a gg = a.geom[pi];
-    const d3 Pi = ld(a.xA, i);
-    bool active;
-    float depth;
-    f3 n, rA, rB;
-    if (P.cd == CD_SS) {
-        // d = x_master - x_slave, |d|^2 and R^2 - |d|^2 in double-float from the two
-        // positions' hi/lo splits; where the numerator is within 1e-9 R^2 of zero the
-        // reference's FP64 formula decides
-        float4 hi_i, lo_i, hj, lj;
-        if (XS) {
-            hj = a.xsA[2 * j];
-            lj = a.xsA[2 * j + 1];
-            hi_i = a.xsA[2 * i];
-            lo_i = a.xsA[2 * i + 1];
-        } else {
-            const d3 Pj = ld(a.xA, j);
-            split32(Pj.x, hj.x, lj.x);
-            split32(Pj.y, hj.y, lj.y);
-            split32(Pj.z, hj.z, lj.z);
-            split32(Pi.x, hi_i.x, lo_i.x);
-            split32(Pi.y, hi_i.y, lo_i.y);
-            split32(Pi.z, hi_i.z, lo_i.z);
-        }
-        const float4 hs = i_slave ? hi_i : hj, ls = i_slave ? lo_i : lj;
-        const float4 hm = i_slave ? hj : hi_i, lm = i_slave ? lj : lo_i;
-        const dfl dx = df_diff(hm.x, lm.x, hs.x, ls.x), dy = df_diff(hm.y, lm.y, hs.y, ls.y),
-                  dz = df_diff(hm.z, lm.z, hs.z, ls.z);
-        const dfl s2 = df_add(df_add(df_sq(dx), df_sq(dy)), df_sq(dz));
-        const float4 rq = a.rr32[pi];                // R^2 hi, R^2 lo, band, R
-        const dfl num = df_add(dfl{rq.x, rq.y}, dfl{-s2.hi, -s2.lo});
-        if (num.hi < -rq.z || num.hi > rq.z) {
-            active = num.hi > 0.0f;
-            depth = (num.hi + num.lo) / (rq.w + sqrtf(s2.hi));
-        } else {                               // tie band: the reference's formula decides
-            const d3 Pj = ld(a.xA, j);
-            const d3 d = i_slave ? sub(Pj, Pi) : sub(Pi, Pj);
-            const double dex = __dsub_rn(__dadd_rn(gg.x, gg.y), xlen(d));
-            active = dex > 0.0;
-            depth = (float)dex;
-        }
-        const f3 df = fm(dx.hi + dx.lo, dy.hi + dy.lo, dz.hi + dz.lo);
-        n = fdir(df);
-        rA = ((float)gg.x - 0.5f * depth) * n;
-        rB = rA - df;
-    } else {
-        const d3 Pj = ld(a.xA, j);
-        const d3 Ps = i_slave ? Pi : Pj, Pm = i_slave ? Pj : Pi;
-        d3 nd, pt;
-        const double dex = wall_detect(P.cd, gg.x, gg.y, gg.z, gg.w, Ps, Pm, ld(a.ox, m), ld(a.oz, m), nd, pt,
-                                       P.cd == CD_SHP ? a.hole[pi] : make_double4_32a(0, 0, 0, 0));
-        active = dex > 0.0;
-        depth = (float)dex;
-        n = fm((float)nd.x, (float)nd.y, (float)nd.z);
-        const d3 ra = sub(pt, Ps), rb = sub(pt, Pm);
-        rA = fm((float)ra.x, (float)ra.y, (float)ra.z);
-        rB = fm((float)rb.x, (float)rb.y, (float)rb.z);
-    }
-    const uint8_t f0 = a.fA[slot];
-    uint8_t f = f0 & 15;
-    float4 h = (f != 0 || active) ? a.hA[slot] : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
-    f3 Jp = fm(0.0f, 0.0f, 0.0f), tA = Jp, tB = Jp;
-    const int app = solve32<LAW>(P.is, a.pc32 + 8 * (size_t)pi, active, depth, n, rA, rB, f4to3(a.v32A[s]),
-                                 f4to3(a.v32A[m]), f4to3(a.w32A[s]), f4to3(a.w32A[m]), dtf, f, h, Jp, tA, tB);
-    if (e == slot) {                           // history owner writes the new status
-        if (f != 0 || (f0 & 15) != 0) {
-            a.hB[slot] = h;
-            a.fB[slot] = (uint8_t)(f | ((f == 0) ? HF_PENDING : 0));
-        } else if (f0 & HF_PENDING) {
-            a.hB[slot] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
-            a.fB[slot] = 0;
-        }
-    }
-    if (wall && a.write_imp) {                 // the wall's share, summed per wall later
-        float* o = a.wimp + 6 * (size_t)e;
-        o[0] = app ? -Jp.x : 0.0f; o[1] = app ? -Jp.y : 0.0f; o[2] = app ? -Jp.z : 0.0f;
-        o[3] = app == 2 ? tB.x : 0.0f; o[4] = app == 2 ? tB.y : 0.0f; o[5] = app == 2 ? tB.z : 0.0f;
-    }
-    cj = i_slave ? Jp : -Jp;
-    ct = i_slave ? tA : tB;
-    return app;
-}
-
-// ---- the contact tick: one warp per group of 32 spheres ---------------------------------
-// The group's list entries (its spheres' rows, concatenated) are walked in windows of TG_CAP:
-// the 32 lanes prefilter consecutive entries (coalesced list loads, every lane busy whatever
-// the rows' lengths), the entries on the exact path are queued and then computed by all 32
-// lanes together (no lane waits for a neighbour's long row), each entry's share of the impulse
-// lands in shared memory at its place in the row, and each lane sums its own sphere's row in
-// list order.  The per-sphere sums are therefore the sequence a single thread walking the row
-// would form (the same compensated additions in the same order), whatever the group.
-constexpr int TG_CAP = 128;                  // list entries a warp holds per window
-struct GroupSmem {
-    float4 cj[TG_CAP];                       // sphere's share of the impulse, per window entry
-    float4 ct[TG_CAP];                       // ... of the angular impulse
-    uint32_t row[33];                        // row k: window positions [row[k], row[k + 1])
-    uint32_t sid[32];
-    uint32_t e0[32];
-    float dtf[32];
-    uint32_t flags[32];                      // 1: a history was cleaned, 2: an entry took the exact path
-    uint16_t xq[TG_CAP];                     // exact-path queue of the window
-    uint8_t app[TG_CAP];
-};
-
-// the group row holding position q: the largest k with row[k] <= q (rows may be empty)
-__device__ __forceinline__ int group_row(const uint32_t* row, uint32_t q) {
-    int lo = 0, hi = 32;
-    while (hi - lo > 1) {
-        const int mid = (lo + hi) >> 1;
-        if (row[mid] <= q) lo = mid; else hi = mid;
-    }
-    return lo;
-}
-
-// Sphere i (or ~0u: this lane has none) of the warp's group; every lane of the warp calls it.
-template <int LAW, bool XS>
-__device__ __forceinline__ float2 tick_group(const TickArgs& a, uint32_t i, GroupSmem& g) {
-    const int lane = threadIdx.x & 31;
+__device__ __forceinline__ float2 tick_sphere(const TickArgs& a, uint32_t i) {
     float2 vmax_local = make_float2(0.0f, 0.0f);
-    uint32_t cnt = 0, qc = 0, mi = 0, si = 0;
-    bool local = false, quiet = false;
-    const float pad = 2.0f * a.disp[0];
-    if (i != 0xffffffffu) {
-        mi = a.model_of[i];
-        si = a.scene_of[i];
+    {
+        // every load that depends on the index alone is issued here, together, so that their
+        // latencies overlap; the model- and list-dependent ones follow
+        const uint32_t mi = a.model_of[i];
+        const uint32_t si = a.scene_of[i];
+        const uint32_t e0 = a.nptr[i], e1 = a.nptr[i + 1];
+        const d3 Pi = ld(a.xA, i);
+        const d3 V = ld(a.v64, i);
+        const float4 p32i = a.pos32[i];
+        const float disp = a.disp[0];
         const ModelDev& M = a.models[mi];
         const SceneDev& S = a.scenes[si];
         if (M.scope == SCOPE_LOCAL && S.active) {
-            local = true;
+            const double dt = S.dt;
+            const float dtf = S.dtf;
+            const float pad = 2.0f * disp;
+            const float4 mf0 = a.mf[2 * mi], mf1 = a.mf[2 * mi + 1];
+            const bool mobile = M.behavior == BEH_MOBILE;
             // the clean-walk count is kept by the light tick when there is one
-            qc = a.work ? 0u : a.qcnt[i];
+            const uint32_t qc = a.work ? 0u : a.qcnt[i];
             const float2 cl = a.clear[i];
-            quiet = qc >= 2u && !a.write_imp && pad <= cl.x && a.disp[1] <= cl.y;
-            if (!quiet) {
-                const uint32_t e0 = a.nptr[i];
-                cnt = a.nptr[i + 1] - e0;
-                g.e0[lane] = e0;
-            }
-            g.dtf[lane] = (float)S.dt;
-        } else if (M.scope == SCOPE_LOCAL) {
-            hold_state(a, i);                  // a finished scene waits, unchanged
-        }
-    }
-    g.sid[lane] = i;
-    g.flags[lane] = 0u;
-    uint32_t incl = cnt;                       // rows: exclusive scan of the walked counts
-#pragma unroll
-    for (int o = 1; o < 32; o <<= 1) {
-        const uint32_t v = __shfl_up_sync(0xffffffffu, incl, o);
-        if (lane >= o) incl += v;
-    }
-    g.row[lane] = incl - cnt;
-    if (lane == 31) g.row[32] = incl;
-    const uint32_t total = __shfl_sync(0xffffffffu, incl, 31);
-    __syncwarp();
-    K3 J, JA;
-    for (uint32_t w0 = 0; w0 < total; w0 += TG_CAP) {
-        const uint32_t w1 = min(total, w0 + (uint32_t)TG_CAP);
-        uint32_t nx = 0;
-        for (uint32_t q0 = w0; q0 < w1; q0 += 32) {
-            const uint32_t q = q0 + lane;
-            bool ex = false;
-            if (q < w1) {
-                const int k = group_row(g.row, q);
-                const uint32_t e = g.e0[k] + (q - g.row[k]);
-                bool dirty = false;
-                ex = prefilter_entry(a, e, a.pos32[g.sid[k]], pad, dirty);
-                if (dirty || ex) atomicOr(&g.flags[k], (dirty ? 1u : 0u) | (ex ? 2u : 0u));
-                g.app[q - w0] = 0;
-            }
-            const unsigned m = __ballot_sync(0xffffffffu, ex);
-            if (ex) g.xq[nx + __popc(m & ((1u << lane) - 1u))] = (uint16_t)(q - w0);
-            nx += (uint32_t)__popc(m);
-        }
-        __syncwarp();
-        for (uint32_t x = lane; x < nx; x += 32) {
-            const uint32_t qq = g.xq[x];
-            const uint32_t q = w0 + qq;
-            const int k = group_row(g.row, q);
-            f3 cj, ct;
-            const int app = exact_entry<LAW, XS>(a, g.e0[k] + (q - g.row[k]), g.sid[k], g.dtf[k], cj, ct);
-            g.app[qq] = (uint8_t)app;
-            g.cj[qq] = make_float4(cj.x, cj.y, cj.z, 0.0f);
-            g.ct[qq] = make_float4(ct.x, ct.y, ct.z, 0.0f);
-        }
-        __syncwarp();
-        if (cnt) {                             // this lane's row within the window, in list order
-            const uint32_t rb = g.row[lane];
-            const uint32_t r0 = max(rb, w0), r1 = min(rb + cnt, w1);
-            for (uint32_t q = r0; q < r1; ++q) {
-                const int app = g.app[q - w0];
+            const bool quiet = qc >= 2u && !a.write_imp && pad <= cl.x && a.disp[1] <= cl.y;
+            bool dirty = false, any_exact = false;
+            K3 J, JA;
+            for (uint32_t base = e0; base < e1 && !quiet; base += TICK_GROUP) {
+                uint32_t exact = prefilter_group(a, base, e1, p32i, pad, dirty);
+                any_exact |= exact != 0u;
+                // Phase 2: the exact path for the flagged entries, in entry order
+                while (exact) {
+                const int k = __ffs(exact) - 1;
+                exact &= exact - 1;
+                const uint32_t e = base + k;
+                const uint32_t ent = a.nent[e];            // (reloaded: a register array indexed by k would spill)
+                const uint32_t meta = a.nmeta[e];
+                const uint32_t j = ent & ~WALL_BIT;
+                const bool wall = ent & WALL_BIT;
+                // canonical orientation (Assembler.cpp:43-67), fixed at rebuild; sphere-wall: the sphere is the slave
+                const bool i_slave = meta & META_SLAVE;
+                const bool owner = meta & META_OWNER;
+                const uint32_t s = i_slave ? i : j, m = i_slave ? j : i;
+                const uint32_t pi = meta & META_PI;
+                const uint32_t slot = owner ? e : a.nslot[e];
+                const PairParam& P = a.params[pi];
+                bool active;
+                float depth;
+                f3 n, rA, rB;
+                if (P.cd == CD_SS) {
+                    // d = x_master - x_slave, |d|^2 and R^2 - |d|^2 in double-float from the two
+                    // positions' hi/lo splits; where the numerator is within 1e-9 R^2 of zero the
+                    // reference's FP64 formula decides
+                    float4 hi_i, lo_i, hj, lj;
+                    if (XS) {
+                        hj = a.xsA[2 * j];
+                        lj = a.xsA[2 * j + 1];
+                        hi_i = a.xsA[2 * i];
+                        lo_i = a.xsA[2 * i + 1];
+                    } else {
+                        const d3 Pj = ld(a.xA, j);
+                        split32(Pj.x, hj.x, lj.x);
+                        split32(Pj.y, hj.y, lj.y);
+                        split32(Pj.z, hj.z, lj.z);
+                        split32(Pi.x, hi_i.x, lo_i.x);
+                        split32(Pi.y, hi_i.y, lo_i.y);
+                        split32(Pi.z, hi_i.z, lo_i.z);
+                    }
+                    const float4 hs = i_slave ? hi_i : hj, ls = i_slave ? lo_i : lj;
+                    const float4 hm = i_slave ? hj : hi_i, lm = i_slave ? lj : lo_i;
+                    const dfl dx = df_diff(hm.x, lm.x, hs.x, ls.x), dy = df_diff(hm.y, lm.y, hs.y, ls.y),
+                              dz = df_diff(hm.z, lm.z, hs.z, ls.z);
+                    const dfl s2 = df_add(df_add(df_sq(dx), df_sq(dy)), df_sq(dz));
+                    const float4 rq = a.rr32[pi];                // R^2 hi, R^2 lo, band, R
+                    const dfl num = df_add(dfl{rq.x, rq.y}, dfl{-s2.hi, -s2.lo});
+                    if (num.hi < -rq.z || num.hi > rq.z) {
+                        active = num.hi > 0.0f;
+                        depth = (num.hi + num.lo) / (rq.w + sqrtf(s2.hi));
+                    } else {                               // tie band: the reference's formula decides
+                        const double dex = tie_depth(a, pi, s, m);
+                        active = dex > 0.0;
+                        depth = (float)dex;
+                    }
+                    const f3 df = fm(dx.hi + dx.lo, dy.hi + dy.lo, dz.hi + dz.lo);
+                    n = fdir(df);
+                    rA = (a.pc32[8 * (size_t)pi + 7] - 0.5f * depth) * n;   // slot 7: the slave's radius
+                    rB = rA - df;
+                } else {
+                    wall_pair(a, P.cd, pi, s, m, active, depth, n, rA, rB);
+                }
+                const uint8_t f0 = a.fA[slot];
+                uint8_t f = f0 & 15;
+                float4 h = (f != 0 || active) ? a.hA[slot] : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+                f3 Jp = fm(0.0f, 0.0f, 0.0f), tA = Jp, tB = Jp;
+                const int app = solve32<LAW>(P.is, a.pc32 + 8 * (size_t)pi, active, depth, n, rA, rB,
+                                        f4to3(a.v32A[s]), f4to3(a.v32A[m]), f4to3(a.w32A[s]), f4to3(a.w32A[m]), dtf, f,
+                                        h, Jp, tA, tB);
+                if (e == slot) {                           // history owner writes the new status
+                    if (f != 0 || (f0 & 15) != 0) {
+                        a.hB[slot] = h;
+                        a.fB[slot] = (uint8_t)(f | ((f == 0) ? HF_PENDING : 0));
+                    } else if (f0 & HF_PENDING) {
+                        a.hB[slot] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+                        a.fB[slot] = 0;
+                    }
+                }
                 if (app) {
-                    J.add(f4to3(g.cj[q - w0]));
-                    if (app == 2) JA.add(f4to3(g.ct[q - w0]));
+                    if (i_slave) {
+                        J.add(Jp);
+                        if (app == 2) JA.add(tA);
+                    } else {
+                        J.add(-Jp);
+                        if (app == 2) JA.add(tB);
+                    }
+                }
+                if (wall && a.write_imp) {                 // the wall's share, summed per wall later
+                    float* o = a.wimp + 6 * (size_t)e;
+                    o[0] = app ? -Jp.x : 0.0f; o[1] = app ? -Jp.y : 0.0f; o[2] = app ? -Jp.z : 0.0f;
+                    o[3] = app == 2 ? tB.x : 0.0f; o[4] = app == 2 ? tB.y : 0.0f; o[5] = app == 2 ? tB.z : 0.0f;
+                }
                 }
             }
+            if (!a.work && !quiet) note_walk(a, i, qc, dirty || any_exact);
+            vmax_local = finish_sphere<XS>(a, i, mobile, quiet, S, Pi, V, mf0, mf1, J, JA);
+        } else if (M.scope == SCOPE_LOCAL) {
+            hold_state(a, i);                      // a finished scene waits, unchanged
         }
-        __syncwarp();
-    }
-    if (local) {
-        if (!a.work && !quiet) note_walk(a, i, qc, g.flags[lane] != 0u);
-        const d3 Pi = ld(a.xA, i);
-        const d3 V = ld(a.v64, i);
-        const float4 mf0 = a.mf[2 * mi], mf1 = a.mf[2 * mi + 1];
-        vmax_local = finish_sphere<XS>(a, i, a.models[mi].behavior == BEH_MOBILE, quiet, a.scenes[si], Pi, V, mf0,
-                                       mf1, J, JA);
     }
     return vmax_local;
 }
@@ -945,34 +870,30 @@ __device__ __forceinline__ void step_order() {
     asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
 }
 
-// The full tick: one warp per group of 32 consecutive spheres.
+// The full tick, one thread per sphere.
 template <int LAW, bool XS>
 __global__ void __launch_bounds__(TPB) k_tick(TickArgs a) {
-    extern __shared__ GroupSmem tick_smem[];
     step_order();
     const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
     float2 vmax_local = make_float2(0.0f, 0.0f);
     if (held_step(a)) {                          // the same value for every thread of the launch
         hold_state(a, t);
-    } else {
-        vmax_local = tick_group<LAW, XS>(a, t < a.n ? t : 0xffffffffu, tick_smem[threadIdx.x >> 5]);
+    } else if (t < a.n) {
+        vmax_local = tick_sphere<LAW, XS>(a, t);
     }
     reduce_vmax(a, vmax_local);
 }
 
 // The full tick of the split tick: a grid sized to the resident threads strides over the
-// spheres the light kernel deferred (none in a held step), 32 to a warp.
+// spheres the light kernel deferred (none in a held step).
 template <int LAW, bool XS>
 __global__ void __launch_bounds__(TPB) k_tick_work(TickArgs a) {
-    extern __shared__ GroupSmem tick_smem[];
     step_order();
     float2 vmax_local = make_float2(0.0f, 0.0f);
     if (!held_step(a)) {
         const uint32_t nw = *a.nwork;
-        const uint32_t lane = threadIdx.x & 31u;
-        for (uint32_t g0 = blockIdx.x * blockDim.x + (threadIdx.x & ~31u); g0 < nw; g0 += gridDim.x * blockDim.x)
-            vmax_local = fmax2(vmax_local, tick_group<LAW, XS>(a, g0 + lane < nw ? a.work[g0 + lane] : 0xffffffffu,
-                                                               tick_smem[threadIdx.x >> 5]));
+        for (uint32_t q = blockIdx.x * blockDim.x + threadIdx.x; q < nw; q += gridDim.x * blockDim.x)
+            vmax_local = fmax2(vmax_local, tick_sphere<LAW, XS>(a, a.work[q]));
     }
     reduce_vmax(a, vmax_local);
 }
@@ -2432,6 +2353,7 @@ int MixedEngine::init_from(const std::vector<SceneSource>& src, const MixedEngin
             params_.push_back(P);
             if (P.cd) law = (law == -1 || law == P.is) ? P.is : 0;
             for (int k = 0; k < 8; ++k) pc.push_back((float)P.c[k]);
+            pc[pc.size() - 1] = (float)t.geom[4 * q];   // slot 7: the slave sphere's radius (no law reads c[7])
             if (P.is == IS_H) {        // ISwH first-contact stiffness coefficient (see ish_first_kn)
                 const double knH = P.c[0], Meff = P.c[1], betan = P.c[4];
                 const double k0 = betan < 0.99 ? 0.957832746294131 / (1.0 - betan * betan) : 479.155951122633;
@@ -2736,6 +2658,7 @@ int MixedEngine::rebuild() {
         D.nobj = H.nobj;
         D.active = H.active ? 1u : 0u;
         D.dt = H.dt;
+        D.dtf = (float)H.dt;
         // the frame: free fall under the scene's field from its spheres' velocity midrange
         const bool moving = vred[6 * s] != 0xffffffffu;
         for (int k = 0; k < 3; ++k) {
@@ -2903,12 +2826,11 @@ int MixedEngine::rebuild() {
 // A per-step kernel launch; `dep`: with programmatic dependent launch (the kernel orders itself
 // after the previous one with step_order()).
 template <typename... P, typename... A>
-static cudaError_t step_launch_smem(bool dep, void (*k)(P...), unsigned grid, unsigned block, size_t smem,
-                                    cudaStream_t s, A... args) {
+static cudaError_t step_launch(bool dep, void (*k)(P...), unsigned grid, unsigned block, cudaStream_t s, A... args) {
     cudaLaunchConfig_t cfg{};
     cfg.gridDim = dim3(grid);
     cfg.blockDim = dim3(block);
-    cfg.dynamicSmemBytes = smem;
+    cfg.dynamicSmemBytes = 0;
     cfg.stream = s;
     cudaLaunchAttribute at[1];
     at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
@@ -2916,11 +2838,6 @@ static cudaError_t step_launch_smem(bool dep, void (*k)(P...), unsigned grid, un
     cfg.attrs = at;
     cfg.numAttrs = dep ? 1 : 0;
     return cudaLaunchKernelEx(&cfg, k, args...);
-}
-
-template <typename... P, typename... A>
-static cudaError_t step_launch(bool dep, void (*k)(P...), unsigned grid, unsigned block, cudaStream_t s, A... args) {
-    return step_launch_smem(dep, k, grid, block, 0, s, args...);
 }
 
 void MixedEngine::launch_step(bool write_imp) {
@@ -2948,10 +2865,9 @@ void MixedEngine::launch_step(bool write_imp) {
         nb_full = std::min<unsigned>(nb, (unsigned)sms_ * 512u / (unsigned)tpb_);
     }
 #define VEDO_TICK(L)                                                                                        \
-    note(step_launch_smem(dep, split_tick_ ? (xs_stored_ ? k_tick_work<L, true> : k_tick_work<L, false>)     \
-                                           : (xs_stored_ ? k_tick<L, true> : k_tick<L, false>),              \
-                          split_tick_ ? nb_full : nb, (unsigned)tpb_, sizeof(GroupSmem) * (size_t)(tpb_ / 32),   \
-                          stream_, a))
+    note(step_launch(dep, split_tick_ ? (xs_stored_ ? k_tick_work<L, true> : k_tick_work<L, false>)          \
+                                      : (xs_stored_ ? k_tick<L, true> : k_tick<L, false>),                   \
+                     split_tick_ ? nb_full : nb, (unsigned)tpb_, stream_, a))
     switch (law_) {
     case IS_BSDBF: VEDO_TICK(IS_BSDBF); break;
     case IS_BTSDBF: VEDO_TICK(IS_BTSDBF); break;

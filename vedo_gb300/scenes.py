@@ -512,6 +512,71 @@ def spinning_plate(omega: float = 500.0, steps: int = 3000, dt: float = 2e-7, ra
     return Scene(sp, models, iacts, midx, P, np.zeros((n + 1, 3)), OX, OZ, AV)
 
 
+def shell_drop(n: int = 150, seed: int = 6, steps: int = 600, dt: float = 1e-6, radius: float = 0.5e-3,
+               R: float = 8e-3, length: float = 12e-3, solver: str = "ISwBSDBF", rpm: float = 0.0,
+               speed: float = 3.0) -> Scene:
+    """Spheres inside a horizontal hollow cylinder (the engine's inner-cylinder extension, axis
+    x, radius R, closed by two fixed plates) placed by random sequential placement in its bottom
+    band and thrown outwards at `speed` m/s, so that most reach the shell within a few hundred
+    steps.  `rpm` turns the shell (orbital) about its axis.  LSD (ISwBSDBF) by default, for
+    bit-exact comparisons."""
+    rng = np.random.default_rng(seed)
+    radii = np.full(n, radius)
+    pos, placed = place_spheres(radii, (-0.5 * length, -R, -R), (0.5 * length, R, -0.55 * R), cyl_radius=R,
+                                seed=seed)
+    if placed != n:
+        raise ValueError(f"shell_drop: placed {placed} of {n}")
+    radial = pos.copy()
+    radial[:, 0] = 0.0
+    out = radial / np.maximum(np.linalg.norm(radial, axis=1), 1e-12)[:, None]
+    vel = speed * out + rng.normal(0.0, 0.05, size=pos.shape)
+    thick = 1e-3
+    behavior = ORBITAL if rpm else FIXED
+    models = [DOModel("Ball", "Ball", MOBILE, LOCAL, 2500.0, 1.0, SPHERE, (radius,)),
+              DOModel("Shell", "Wall", behavior, GLOBAL, 0.0, 1.0, INNER_CYLINDER, (R, length + 2 * thick)),
+              DOModel("End", "Wall", FIXED, GLOBAL, 0.0, 1.0, QUASI_PLATE, (2.2 * R, thick, 2.2 * R))]
+    zeta = damping_ratio(0.6)
+    if solver == "ISwBSDBF":
+        mech = lambda b: lsd_mechanisms(2e4, 1.6e4, b, b, 0.4)
+        iacts = [IactModel("Ball", "Ball", solver, mech(zeta / math.sqrt(2.0))),
+                 IactModel("Wall", "Ball", solver, mech(zeta))]
+    else:
+        m_of = lambda rr: 2500.0 * 4.0 / 3.0 * math.pi * rr ** 3
+        iacts = [IactModel("Ball", "Ball", solver, _hertz_mech(solver, 70e9, 0.25, radius, radius, m_of, zeta, 0.4)),
+                 IactModel("Wall", "Ball", solver, _hertz_mech(solver, 70e9, 0.25, radius, None, m_of, zeta, 0.4))]
+    omega = rpm * 2.0 * math.pi / 60.0
+    wp = [[0.0, 0.0, 0.0], [-0.5 * length - 0.5 * thick, 0.0, 0.0], [0.5 * length + 0.5 * thick, 0.0, 0.0]]
+    wox = [[0.0, 1.0, 0.0], [0.0, 1.0, 0.0], [0.0, 1.0, 0.0]]
+    woz = [[1.0, 0.0, 0.0], [1.0, 0.0, 0.0], [-1.0, 0.0, 0.0]]
+    wav = [[omega, 0.0, 0.0], [0.0, 0.0, 0.0], [0.0, 0.0, 0.0]]
+    midx = np.concatenate([np.zeros(n, np.uint32), np.array([1, 2, 2], np.uint32)])
+    P = np.concatenate([pos, np.array(wp)])
+    V = np.concatenate([vel, np.zeros((3, 3))])
+    OX = np.concatenate([np.tile([1.0, 0, 0], (n, 1)), np.array(wox)])
+    OZ = np.concatenate([np.tile([0, 0, 1.0], (n, 1)), np.array(woz)])
+    AV = np.concatenate([np.zeros((n, 3)), np.array(wav)])
+    return Scene(time_control(steps, dt), models, iacts, midx, P, V, OX, OZ, AV)
+
+
+def shell_rest(R: float = 8e-3, radius: float = 1e-3, kn: float = 1e4, length: float = 12e-3) -> Scene:
+    """One sphere resting on the bottom of a fixed horizontal hollow cylinder at the linear
+    law's equilibrium depth (kn delta = m g, ISwBSDBF), and a second sphere pressed 1 um into the
+    shell's side with the field off along its normal: the analytic checks of the inner-cylinder
+    detector (depth, outward radial normal, force balance)."""
+    m = 2500.0 * 4.0 / 3.0 * math.pi * radius ** 3
+    delta = m * 9.81 / kn
+    pos = np.array([[0.0, 0.0, -(R - radius + delta)], [2e-3, R - radius + 1e-6, 0.0]])
+    models = [DOModel("Ball", "Ball", MOBILE, LOCAL, 2500.0, 1.0, SPHERE, (radius,)),
+              DOModel("Shell", "Wall", FIXED, GLOBAL, 0.0, 1.0, INNER_CYLINDER, (R, length))]
+    iacts = [IactModel("Ball", "Ball", "ISwBSDBF", lsd_mechanisms(kn, 0.8 * kn, 0.1, 0.1, 0.5)),
+             IactModel("Wall", "Ball", "ISwBSDBF", lsd_mechanisms(kn, 0.8 * kn, 0.1, 0.1, 0.5))]
+    midx = np.array([0, 0, 1], np.uint32)
+    P = np.concatenate([pos, [[0.0, 0.0, 0.0]]])
+    OX = np.array([[1.0, 0, 0], [1.0, 0, 0], [0.0, 1.0, 0.0]])
+    OZ = np.array([[0, 0, 1.0], [0, 0, 1.0], [1.0, 0.0, 0.0]])
+    return Scene(time_control(10, 1e-6), models, iacts, midx, P, np.zeros((3, 3)), OX, OZ, np.zeros((3, 3)))
+
+
 def holed_plate_drop(n_side: int = 6, seed: int = 4, steps: int = 600, dt: float = 1e-6, radius: float = 1e-3,
                      hole: float = 2.6e-3, hole_offset: Tuple[float, float] = (1.2e-3, -0.7e-3),
                      solver: str = "ISwBSDBF") -> Scene:
