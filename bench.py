@@ -597,7 +597,9 @@ def batch_workload(args, dist, dev):
     prof = b.last_run_profile()
     t = dist.reduce(prof["total_ms"], "max")
     total = dist.reduce(float(n), "sum")
+    contacts = int(b.observables()[9])
     out = {"workload": f"hopper_batch_{args.batch_scenes}", "scenes": args.batch_scenes, "particles": n,
+           "active_contacts_end": contacts, "z_pp": contacts / n,
            "value": total * args.batch_steps / (t * 1e-3), "unit": UNIT, "ms_per_step": t / args.batch_steps,
            "steps": args.batch_steps, "gpu_launches": prof["launches"], "tuning": b.tuning(),
            "errors_mixed_vs_fp64": {"scenes": errs,
@@ -605,9 +607,10 @@ def batch_workload(args, dist, dev):
                                     "all_contact_sets_identical": all(e["contact_set_identical"] for e in errs),
                                     "max_energy_rel": max((e["energy_rel_after_200_steps"] for e in errs),
                                                           default=None)},
-           "note": f"steps {TUNE_STEPS}..{TUNE_STEPS + args.batch_steps} of the configured 5000-step run; mixed form, "
-                   "CUDA-graph check intervals, autotuned tick block, skin and cell scale; errors on scenes 0-3 "
-                   "alone (bit-identical to their batch slices)"}
+           "note": f"steps {TUNE_STEPS}..{TUNE_STEPS + args.batch_steps} of the configured 5000-step run, columns "
+                   "resting on touching lattices and draining through the orifice; mixed form, CUDA-graph check "
+                   "intervals, autotuned tick block, skin and cell scale; errors on scenes 0-3 alone "
+                   "(bit-identical to their batch slices)"}
     b.close()
     return out
 
@@ -622,7 +625,7 @@ def bed_workload(args, dist, dev):
     if not args.no_profile_pass:
         small = scenes.compressed_bed(n=1_000_000, box=0.1, cylinders=2, seed=5 + dist.rank)
         errs = form_errors(small, dev, 1500)          # the top plate reaches the bed near step 1000
-        errs["scene"] = "compressed_bed of 1M spheres (same construction and depth; 0.1 x 0.1 m floor, 2 rods)"
+        errs["scene"] = "compressed_bed of 1M spheres (same construction; 0.1 x 0.1 m floor, 2 rods)"
         del small
     sc = scenes.compressed_bed(n=args.bed_n, seed=5 + dist.rank)
     n = scene_particles(sc)
@@ -655,7 +658,8 @@ def bed_workload(args, dist, dev):
                              "dram_frac": traffic / (t_tick * 1e-3) / 1e9 / peak if traffic else None,
                              "traffic_source": "profiles/k_tick_light_bed16M_dram.md" if traffic else None},
            "note": f"steps {TUNE_STEPS}..{TUNE_STEPS + args.bed_steps} of the configured 2000-step run (dt 2e-7 s); "
-                   "mixed form"}
+                   "a simple cubic lattice whose neighbours, floor, walls and top plate touch (solid fraction 0.524, "
+                   "standing in for a random loose packing at 0.55); mixed form"}
     e.close()
     return out
 

@@ -370,15 +370,21 @@ int vedo_gpu_scene_range(const vedo_gpu_engine* e, uint32_t scene, uint32_t* fir
  * No counterpart in the reference (anne runs one scene per process).  A server owns one
  * GPU and a thread that advances every live job's scene in the same fused launches.  Jobs
  * (a scene and a step count) are submitted from any thread at any time; each waits in a
- * FIFO queue until admission, which counts an estimate of the job's device memory
- * (VEDO_SRV_BYTES_PER_OBJECT per object) against the HBM budget.  The live set is kept at
+ * FIFO queue until admission, which counts the job's device memory against the HBM
+ * budget: VEDO_SRV_BYTES_PER_OBJECT per object (state, FP32 copies, splits, sort and cell
+ * keys, staging) plus, per sphere, VEDO_SRV_ENTRIES_PER_SPHERE neighbour-list entries of
+ * VEDO_SRV_BYTES_PER_ENTRY (the current and previous list with their history and flags, the
+ * wall-impulse rows, all with the 25 % growth the engine allocates); a dense packing lists
+ * 12-14 neighbours per sphere within its skin.  The live set is kept at
  * or below half the budget, because adding or removing jobs builds the next batch on the
  * device while the current one still exists.  Admitted jobs join the batch at the next
  * check interval, with their state and contact history resident on the device from then
  * on; a job stops after exactly its step count and its final state is copied to the host.
  * A job's result equals the same scene run alone in the MIXED form for the same number
  * of steps, bit for bit. */
-#define VEDO_SRV_BYTES_PER_OBJECT 2048u
+#define VEDO_SRV_BYTES_PER_OBJECT 800u
+#define VEDO_SRV_ENTRIES_PER_SPHERE 18u
+#define VEDO_SRV_BYTES_PER_ENTRY 150u
 enum { VEDO_JOB_QUEUED = 0, VEDO_JOB_RUNNING = 1, VEDO_JOB_DONE = 2, VEDO_JOB_CANCELLED = 3, VEDO_JOB_FAILED = 4 };
 
 typedef struct vedo_job_info {
@@ -389,6 +395,7 @@ typedef struct vedo_job_info {
     double submit_s;          /* seconds since the server started: submission,          */
     double admit_s;           /*   admission (joined the batch) and completion; -1 = not */
     double done_s;            /*   yet                                                   */
+    uint64_t charged_bytes;   /* device memory the admission counts for the job          */
 } vedo_job_info;
 
 typedef struct vedo_server vedo_server;

@@ -58,9 +58,9 @@ def test_served_jobs_equal_alone(engine_lib):
 
 
 def test_admission_respects_the_hbm_budget(engine_lib):
-    from vedo_gb300.serve import BYTES_PER_OBJECT, Server
+    from vedo_gb300.serve import Server, job_charge
     scs = [scenes.serving_job("settle", 2000, "lsd", s) for s in range(3)]
-    one = max(sc.num_objects for sc in scs) * BYTES_PER_OBJECT
+    one = max(job_charge(sc.num_objects, 2000) for sc in scs)
     with Server(hbm_budget_bytes=3 * one) as srv:      # half the budget holds one job, not two
         ids = [srv.submit(sc, 200) for sc in scs]
         infos = [srv.wait(j, 120.0) for j in ids]
@@ -77,7 +77,7 @@ def test_cancel_and_oversized_jobs(engine_lib):
     with Server(hbm_budget_bytes=2 * 10**8) as srv:
         big = scenes.serving_job("settle", 60000, "lsd", 1)
         with pytest.raises(engine_lib.EngineError) as ex:
-            srv.submit(big, 10)                       # 60k objects x 2 KiB > half of 200 MB
+            srv.submit(big, 10)                       # 60k spheres' charge > half of 200 MB
         assert ex.value.code == 4
         j = srv.submit(scenes.serving_job("settle", 3000, "lsd", 2), 10**6)
         _wait_running(srv, j, 1)
@@ -85,3 +85,30 @@ def test_cancel_and_oversized_jobs(engine_lib):
         assert srv.wait(j, 60.0)["status"] == "cancelled"
         k = srv.submit(scenes.cluster(n=64, seed=3), 50)
         assert srv.wait(k, 60.0)["status"] == "done"
+
+
+@pytest.mark.parametrize("which", ["projectile", "dense"])
+def test_admission_charge_covers_the_engine_allocations(which, engine_lib):
+    """The charge a job is admitted against (objects and expected neighbour-list entries) is at
+    least the device memory a MIXED engine of that scene allocates once its list is built and
+    has been rebuilt (two lists alive), here measured as the drop in the device's free memory;
+    the dense pack (12 neighbours per sphere in contact) is the list's worst case."""
+    torch = pytest.importorskip("torch")
+    from vedo_gb300.scene import SPHERE
+    from vedo_gb300.serve import Server, job_charge
+    sc = scenes.serving_job("projectile", 40000, "hertz", 3) if which == "projectile" else scenes.dense_pack(n=40000)
+    nsph = int(sum(1 for m in sc.model_index if sc.models[m].shape == SPHERE))
+    charge = job_charge(sc.num_objects, nsph)
+    with Server(hbm_budget_bytes=10**10) as srv:            # the server reports the same charge
+        j = srv.submit(sc, 1)
+        assert srv.wait(j, 120.0)["charged_bytes"] == charge
+    torch.cuda.synchronize()
+    free0 = torch.cuda.mem_get_info()[0]
+    e = engine_lib.GpuEngine(sc, precision=1, skin=0.4)
+    e.run(200)
+    e.set_state(position=e.state(("position",))["position"] + 1.0)   # a jump past the skin: a rebuild
+    e.run(5)
+    torch.cuda.synchronize()
+    used = free0 - torch.cuda.mem_get_info()[0]
+    e.close()
+    assert 0 < used <= charge, (used, charge)

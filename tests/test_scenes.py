@@ -59,7 +59,7 @@ def min_clearance(sc):
     ("hopper", lambda: scenes.hopper(n=3000, seed=1)),
     ("settle_lsd", lambda: scenes.serving_job("settle", 3000, "lsd", 1)),
     ("projectile_hertz", lambda: scenes.serving_job("projectile", 3000, "hertz", 2)),
-    ("compressed_bed", lambda: scenes.compressed_bed(n=50000, box=0.06, cylinders=4)),
+    ("compressed_bed", lambda: scenes.compressed_bed(n=50000, box=0.06, cylinders=4, packing="fcc")),
 ])
 def test_scene_starts_without_overlaps(name, make):
     assert min_clearance(make()) > 0.0, name
@@ -72,3 +72,19 @@ def test_drum_has_a_largest_sphere_last():
     r = np.array([sc.models[m].attrs[0] if sc.models[m].shape == SPHERE else 0.0 for m in sc.model_index])
     last_sphere = np.flatnonzero(r > 0)[-1]
     assert r[last_sphere] == r.max()
+
+
+@pytest.mark.parametrize("name,make", [
+    ("compressed_bed", lambda: scenes.compressed_bed(n=50000, box=0.06, cylinders=4)),
+    ("hopper", lambda: scenes.hopper(n=3000, seed=1, touching=True)),
+])
+def test_touching_packings_touch_without_overlap(name, make):
+    """The contact-bearing stand-ins (a simple cubic lattice whose neighbours, floor and walls
+    touch): every sphere's nearest neighbour lies at 2 r to rounding, and no wall overlaps."""
+    sc = make()
+    sph = np.array([sc.models[m].shape == SPHERE for m in sc.model_index])
+    p = sc.position[sph]
+    r = sc.models[sc.model_index[np.flatnonzero(sph)[0]]].attrs[0]
+    d, _ = spatial.cKDTree(p).query(p, k=2)
+    np.testing.assert_allclose(d[:, 1], 2 * r, rtol=1e-12)
+    assert min_clearance(sc) > -1e-12 * r, name

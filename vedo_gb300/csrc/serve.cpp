@@ -263,6 +263,7 @@ void info_of(const Job& j, vedo_job_info* info) {
     info->submit_s = j.t_submit;
     info->admit_s = j.t_admit;
     info->done_s = j.t_done;
+    info->charged_bytes = j.bytes;
 }
 }  // namespace
 
@@ -316,7 +317,8 @@ int vedo_srv_submit(vedo_server* s, const vedo_scene_desc* scene, uint64_t steps
         if (m < j->scene.models.size() && j->scene.models[m].scope == VEDO_SCOPE_LOCAL) ++j->particles;
     }
     j->steps = steps;
-    j->bytes = (uint64_t)VEDO_SRV_BYTES_PER_OBJECT * j->scene.n;
+    j->bytes = (uint64_t)VEDO_SRV_BYTES_PER_OBJECT * j->scene.n +
+               (uint64_t)VEDO_SRV_ENTRIES_PER_SPHERE * VEDO_SRV_BYTES_PER_ENTRY * j->particles;
     std::lock_guard<std::mutex> lk(s->mu);
     if (j->bytes > s->budget / 2) {
         s->err = "job needs " + std::to_string(j->bytes) + " bytes, more than half the HBM budget";

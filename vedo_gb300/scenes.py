@@ -429,16 +429,20 @@ def _hertz_mech(solver, E, nu, ra, rb, m_of, zeta, mu):
 
 def hopper(n: int = 10000, seed: int = 0, friction: float = 0.4, restitution: float = 0.7, orifice: float = 8e-3,
            steps: int = 5000, dt: float = 5e-7, radius: float = 1e-3, density: float = 2500.0, E: float = 70e9,
-           nu: float = 0.25, spacing_factor: float = 1.1, vel_sigma: float = 0.01) -> Scene:
+           nu: float = 0.25, spacing_factor: float = 1.1, vel_sigma: float = 0.01, touching: bool = False) -> Scene:
     """Flat-bottomed hopper discharging through a square orifice of side `orifice`.
 
     The spheres start on a jittered square-prism lattice (spacing `spacing_factor` x 2r),
-    about twice as tall as wide, resting 0.05 r above the floor.  Walls: four fixed side
+    about twice as tall as wide, resting 0.05 r above the floor; with `touching` on a simple
+    cubic lattice whose neighbours and floor touch exactly (no jitter, at rest), so that the
+    column carries its contacts from the first step while it drains.  Walls: four fixed side
     plates and a floor of four fixed plates that leave the orifice open in its centre (the
     reference's only holed plate has a circular hole, so the rectangular orifice is built from
     plain plates).  Contact: ``ISwH`` (Hertz normal stiffness with friction) from E, nu,
     restitution and friction, for sphere-sphere and sphere-wall."""
     rng = np.random.default_rng(seed)
+    if touching:
+        spacing_factor = 1.0
     a = 2.0 * radius * spacing_factor
     m = max(2, int(math.ceil((n / 2.0) ** (1.0 / 3.0))))
     nz = int(math.ceil(n / (m * m)))
@@ -446,10 +450,14 @@ def hopper(n: int = 10000, seed: int = 0, friction: float = 0.4, restitution: fl
     pos = np.empty((n, 3))
     pos[:, 0] = (g[:, 0] - 0.5 * (m - 1)) * a
     pos[:, 1] = (g[:, 1] - 0.5 * (m - 1)) * a
-    pos[:, 2] = g[:, 2] * a + 1.05 * radius
-    pos += rng.uniform(-0.02 * radius, 0.02 * radius, size=pos.shape)
+    pos[:, 2] = g[:, 2] * a + (1.0 if touching else 1.05) * radius
+    jitter = rng.uniform(-0.02 * radius, 0.02 * radius, size=pos.shape)
     vel = rng.normal(0.0, vel_sigma, size=pos.shape)
-    W = m * a + 2.0 * radius                       # inner width of the box
+    if touching:
+        vel[:] = 0.0
+    else:
+        pos += jitter
+    W = m * a if touching else m * a + 2.0 * radius    # inner width of the box
     H = nz * a + 4.0 * radius                      # side wall height
     t = 2e-3                                       # plate thickness
     w = min(orifice, W - 4.0 * radius)
@@ -725,9 +733,10 @@ def hopper_params(num_scenes: int = 256, seed: int = 2025, n_lo: int = 1000, n_h
 
 
 def hopper_batch(num_scenes: int = 256, seed: int = 2025, steps: int = 5000, n_lo: int = 1000,
-                 n_hi: int = 50000) -> List[Scene]:
-    """The batched hopper workload: `num_scenes` independent hoppers of uneven sizes."""
-    return [hopper(n=n, seed=sd, friction=mu, restitution=e, orifice=w, steps=steps)
+                 n_hi: int = 50000, touching: bool = True) -> List[Scene]:
+    """The batched hopper workload: `num_scenes` independent hoppers of uneven sizes (touching
+    fills by default: the column rests on the floor and drains through the orifice)."""
+    return [hopper(n=n, seed=sd, friction=mu, restitution=e, orifice=w, steps=steps, touching=touching)
             for n, sd, mu, e, w in hopper_params(num_scenes, seed, n_lo, n_hi)]
 
 
@@ -809,13 +818,23 @@ def serving_job(kind: str, n: int, model: str, seed: int, steps: int = 1000, K: 
 def compressed_bed(n: int = 16_000_000, seed: int = 5, steps: int = 2000, dt: float = 2e-7, radius: float = 5e-4,
                    box: float = 0.4, E: float = 10e9, nu: float = 0.25, restitution: float = 0.7,
                    friction: float = 0.5, density: float = 2500.0, solid_fraction: float = 0.55,
-                   cylinders: int = 32, cyl_radius: float = 5e-3, plate_speed: float = 0.05) -> Scene:
-    """A bed of n spheres at `solid_fraction` (a jittered face-centred cubic lattice: at 0.55
-    the nearest-neighbour gap is 0.2 r, so nothing overlaps) filling a `box` x `box` floor to the
-    height that holds n, with `cylinders` fixed vertical rods on a jittered grid (spheres that
-    would overlap a rod are not placed) and an orbital top plate just above the bed moving at
-    (0, 0, -plate_speed).  Walls: floor and four sides (fixed plates).  Contact ``ISwH`` (Hertz
-    normal stiffness with friction) for sphere-sphere, sphere-plate and sphere-rod."""
+                   cylinders: int = 32, cyl_radius: float = 5e-3, plate_speed: float = 0.05,
+                   packing: str = "touching") -> Scene:
+    """A bed of n spheres filling a `box` x `box` floor to the height that holds n, with
+    `cylinders` fixed vertical rods on a jittered grid (spheres that would overlap a rod are not
+    placed) and an orbital top plate moving at (0, 0, -plate_speed).  Walls: floor and four
+    sides (fixed plates).  Contact ``ISwH`` (Hertz normal stiffness with friction) for
+    sphere-sphere, sphere-plate and sphere-rod.
+
+    packing="touching" (the default): a simple cubic lattice whose neighbours, floor, sides and
+    top plate touch exactly (solid fraction pi/6 = 0.524), so the bed carries its contacts from
+    the first step; it stands in for a random loose packing at 0.55, which only a long settle
+    of all n spheres would give.  packing="fcc": a jittered face-centred cubic lattice at
+    `solid_fraction` (at 0.55 the nearest-neighbour gap is 0.2 r: nothing touches) with the
+    plate 10 um above it."""
+    if packing == "touching":
+        return _touching_bed(n, seed, steps, dt, radius, box, E, nu, restitution, friction, density, cylinders,
+                             cyl_radius, plate_speed)
     rng = np.random.default_rng(seed)
     vs = 4.0 / 3.0 * math.pi * radius ** 3
     a = (4.0 * vs / solid_fraction) ** (1.0 / 3.0)          # FCC cell edge (4 spheres per cell)
@@ -865,6 +884,64 @@ def compressed_bed(n: int = 16_000_000, seed: int = 5, steps: int = 2000, dt: fl
         wp.append((cx, cy, 0.5 * height)); wox.append((1.0, 0.0, 0.0)); woz.append((0.0, 0.0, 1.0))
         wv.append((0.0, 0.0, 0.0)); widx.append(3)
     wp.append((0.0, 0.0, top + 1e-5 + 0.5 * t)); wox.append((1.0, 0.0, 0.0)); woz.append((0.0, 0.0, -1.0))
+    wv.append((0.0, 0.0, -plate_speed)); widx.append(4)
+    zeta = damping_ratio(restitution)
+    m_of = lambda rr: density * 4.0 / 3.0 * math.pi * rr ** 3
+    iacts = [IactModel("Ball", "Ball", "ISwH", _hertz_mech("ISwH", E, nu, radius, radius, m_of, zeta, friction)),
+             IactModel("Wall", "Ball", "ISwH", _hertz_mech("ISwH", E, nu, radius, None, m_of, zeta, friction))]
+    k = len(widx)
+    midx = np.concatenate([np.zeros(n, np.uint32), np.array(widx, np.uint32)])
+    P = np.concatenate([pos, np.array(wp)])
+    V = np.concatenate([np.zeros((n, 3)), np.array(wv)])
+    OX = np.concatenate([np.tile([1.0, 0, 0], (n, 1)), np.array(wox)])
+    OZ = np.concatenate([np.tile([0, 0, 1.0], (n, 1)), np.array(woz)])
+    AV = np.zeros((n + k, 3))
+    return Scene(time_control(steps, dt), models, iacts, midx, P, V, OX, OZ, AV)
+
+
+def _touching_bed(n, seed, steps, dt, radius, box, E, nu, restitution, friction, density, cylinders, cyl_radius,
+                  plate_speed) -> Scene:
+    rng = np.random.default_rng(seed)
+    a = 2.0 * radius
+    m = int(box / a)                                       # spheres across
+    inner = m * a                                          # the side walls touch the outer spheres
+    g = int(math.ceil(math.sqrt(cylinders)))
+    rods = []
+    for k in range(cylinders):
+        gx, gy = k % g, k // g
+        cx = (gx + 0.5) / g * inner - 0.5 * inner + rng.uniform(-0.2, 0.2) * inner / g
+        cy = (gy + 0.5) / g * inner - 0.5 * inner + rng.uniform(-0.2, 0.2) * inner / g
+        rods.append((cx, cy))
+    xs = (np.arange(m) + 0.5) * a - 0.5 * inner
+    X, Y = np.meshgrid(xs, xs, indexing="ij")
+    xy = np.stack([X.ravel(), Y.ravel()], 1)
+    keep = np.ones(len(xy), bool)
+    for cx, cy in rods:
+        keep &= (xy[:, 0] - cx) ** 2 + (xy[:, 1] - cy) ** 2 > (cyl_radius + radius * 1.001) ** 2
+    xy = xy[keep]
+    per_layer = len(xy)
+    nl = int(math.ceil(n / per_layer))
+    pos = np.empty((nl * per_layer, 3))
+    for L in range(nl):
+        pos[L * per_layer:(L + 1) * per_layer, :2] = xy
+        pos[L * per_layer:(L + 1) * per_layer, 2] = radius + L * a
+    pos = pos[:n]
+    top = float(pos[:, 2].max()) + radius
+    height = top + 0.02
+    t = 2e-3
+    models = [DOModel("Ball", "Ball", MOBILE, LOCAL, density, 1.0, SPHERE, (radius,)),
+              DOModel("Floor", "Wall", FIXED, GLOBAL, 0.0, 1.0, QUASI_PLATE, (inner + 2 * t, t, inner + 2 * t)),
+              DOModel("Side", "Wall", FIXED, GLOBAL, 0.0, 1.0, QUASI_PLATE, (height, t, inner + 2 * t)),
+              DOModel("Rod", "Wall", FIXED, GLOBAL, 0.0, 1.0, QUASI_CYLINDER, (cyl_radius, height)),
+              DOModel("Top", "Wall", ORBITAL, GLOBAL, 0.0, 1.0, QUASI_PLATE, (inner, t, inner))]
+    wp, wox, woz, wv, widx = [(0.0, 0.0, -0.5 * t)], [(1.0, 0.0, 0.0)], [(0.0, 0.0, 1.0)], [(0.0, 0.0, 0.0)], [1]
+    for sx, sy in ((1, 0), (-1, 0), (0, 1), (0, -1)):
+        wp.append((sx * (0.5 * inner + 0.5 * t), sy * (0.5 * inner + 0.5 * t), 0.5 * height))
+        wox.append((0.0, 0.0, 1.0)); woz.append((-float(sx), -float(sy), 0.0)); wv.append((0.0, 0.0, 0.0)); widx.append(2)
+    for cx, cy in rods:
+        wp.append((cx, cy, 0.5 * height)); wox.append((1.0, 0.0, 0.0)); woz.append((0.0, 0.0, 1.0))
+        wv.append((0.0, 0.0, 0.0)); widx.append(3)
+    wp.append((0.0, 0.0, top + 0.5 * t)); wox.append((1.0, 0.0, 0.0)); woz.append((0.0, 0.0, -1.0))
     wv.append((0.0, 0.0, -plate_speed)); widx.append(4)
     zeta = damping_ratio(restitution)
     m_of = lambda rr: density * 4.0 / 3.0 * math.pi * rr ** 3

@@ -21,13 +21,21 @@ from .engine import STATE_FIELDS, EngineError, _opts, lib
 
 JOB_QUEUED, JOB_RUNNING, JOB_DONE, JOB_CANCELLED, JOB_FAILED = range(5)
 STATUS = {0: "queued", 1: "running", 2: "done", 3: "cancelled", 4: "failed"}
-BYTES_PER_OBJECT = 2048
+# admission charge (include/vedo_gpu.h): per object, and per listed neighbour of a sphere
+BYTES_PER_OBJECT = 800
+ENTRIES_PER_SPHERE = 18
+BYTES_PER_ENTRY = 150
+
+
+def job_charge(num_objects: int, num_spheres: int) -> int:
+    """Device memory the server's admission counts for a job."""
+    return BYTES_PER_OBJECT * num_objects + ENTRIES_PER_SPHERE * BYTES_PER_ENTRY * num_spheres
 
 
 class JobInfo(C.Structure):
     _fields_ = [("status", C.c_uint32), ("num_objects", C.c_uint32), ("steps", C.c_uint64),
                 ("steps_done", C.c_uint64), ("submit_s", C.c_double), ("admit_s", C.c_double),
-                ("done_s", C.c_double)]
+                ("done_s", C.c_double), ("charged_bytes", C.c_uint64)]
 
 
 def _srv_lib():
@@ -50,7 +58,8 @@ def _srv_lib():
 
 def _info(ji: JobInfo) -> Dict:
     return {"status": STATUS[ji.status], "num_objects": ji.num_objects, "steps": ji.steps,
-            "steps_done": ji.steps_done, "submit_s": ji.submit_s, "admit_s": ji.admit_s, "done_s": ji.done_s}
+            "steps_done": ji.steps_done, "submit_s": ji.submit_s, "admit_s": ji.admit_s, "done_s": ji.done_s,
+            "charged_bytes": ji.charged_bytes}
 
 
 class Server:
