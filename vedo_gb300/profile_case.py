@@ -1,8 +1,10 @@
 """Run one workload of the engine, for a profiler or a quick timing.
 
-    python -m vedo_gb300.profile_case <drum|dense|bed|hopper> <spheres> <steps> [--fp64] [--block B] [--stored] [--split]
+    python -m vedo_gb300.profile_case <drum|settled|dense|bed|hopper> <spheres> <steps> [--fp64] [--block B]
+                                      [--stored] [--split] [--skin S]
 
-Builds the seeded scene, creates the engine (mixed form unless --fp64; fixed settings, no
+Builds the seeded scene (`settled`: the polydisperse drum after 300,000 steps of settling, made
+once per host by vedo_gb300.workloads.settled_drum and cached there), creates the engine (mixed form unless --fp64; fixed settings, no
 autotuning, no graph replay, so that every step is one set of plain launches), runs 5 warm-up
 steps and then <steps> steps, and prints the device time per step.  Under ncu, skip the warm-up
 launches with -s and capture the kernel of interest with -k / -c.
@@ -19,6 +21,9 @@ from .engine import GpuEngine
 def make(kind: str, n: int):
     if kind == "drum":
         return scenes.hertz_drum(n=n)
+    if kind == "settled":
+        from .workloads import settled_drum
+        return settled_drum(n=n)[0]
     if kind == "dense":
         return scenes.dense_pack(n=n)
     if kind == "bed":
@@ -38,12 +43,14 @@ def main(argv=None):
     ap.add_argument("--block", type=int, default=64)
     ap.add_argument("--stored", action="store_true", help="store the hi/lo position splits once per step")
     ap.add_argument("--split", action="store_true", help="light tick + full tick over the deferred spheres")
+    ap.add_argument("--skin", type=float, default=None, help="candidate-list skin (fraction of the cell)")
     a = ap.parse_args(argv)
     sc = make(a.kind, a.n)
     if a.fp64:
         e = GpuEngine(sc, up_iact=20)
     else:
-        e = GpuEngine(sc, precision=1, tick_block=a.block, graphs=False, stored_splits=a.stored, split_tick=a.split)
+        e = GpuEngine(sc, precision=1, tick_block=a.block, graphs=False, stored_splits=a.stored, split_tick=a.split,
+                      skin=a.skin)
     e.run(5)
     e.run(a.steps)
     p = e.last_run_profile()
