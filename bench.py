@@ -35,7 +35,7 @@ sys.path.insert(0, ROOT)
 METRIC = "particle-steps/s on 1 GB300 (mixed vs FP64 at stated error); serving p50/p99 ms"
 UNIT = "particle-steps/s"
 WORKLOAD = "hertz_drum_1M"
-TUNE_STEPS = 400
+TUNE_STEPS = 450
 
 
 def parse():
@@ -96,6 +96,14 @@ class Dist:
         t = torch.tensor([x], dtype=torch.float64)
         self.pg.all_reduce(t, op=self.pg.ReduceOp.MAX if op == "max" else self.pg.ReduceOp.SUM)
         return float(t.item())
+
+    def gather(self, obj) -> list:
+        """Every rank's `obj`, in rank order (the rank's own alone when there is one rank)."""
+        if not self.pg:
+            return [obj]
+        out = [None] * self.world
+        self.pg.all_gather_object(out, obj)
+        return out
 
     def close(self):
         if self.pg:
@@ -482,8 +490,8 @@ def ours(args, dist):
         res["dense"] = dense_workload(args, dist, dev)
     if not args.no_c1:
         res["c1"] = c1_workload(args, dist, dev, c1_cpu)
-    if not args.no_serve and dist.world == 1:
-        res["serving"] = serving_workload(args, dev)
+    if not args.no_serve:
+        res["serving"] = serving_workload(args, dist, dev)
     if cpu_job_c2:
         r = cpu_job_c2.result()
         if r:
@@ -580,15 +588,20 @@ def form_errors(scene, dev, pre_steps, post_steps=200, up_iact=20):
 
 def batch_workload(args, dist, dev):
     """The batched workload: hopper scenes of 1e3..5e4 spheres in one autotuned engine whose
-    check intervals replay as CUDA graphs (one fused tick launch per step over all scenes)."""
+    check intervals replay as CUDA graphs (one fused tick launch per step over all scenes).
+    On N GPUs the same scenes are placed whole on the GPUs (vedo_gb300.partition.pack_scenes,
+    by spheres x steps): a fixed job, so its scaling is strong."""
     import torch
-    from vedo_gb300 import scenes
+    from vedo_gb300 import partition, scenes
     from vedo_gb300.engine import BatchEngine
-    hs = scenes.hopper_batch(args.batch_scenes, seed=2025 + dist.rank, steps=5000)
+    hs = scenes.hopper_batch(args.batch_scenes, seed=2025, steps=5000)
+    weights = [scene_particles(h) * 5000 for h in hs]
+    mine = partition.pack_scenes(weights, dist.world)[dist.rank]
+    hs = [hs[q] for q in mine]
     n = sum(scene_particles(h) for h in hs)
     # errors against the FP64 engine on four of the scenes (a scene's results in the batch are
     # those of the scene alone, bit for bit), from step 1000 of the run
-    errs = [] if args.no_profile_pass else [form_errors(hs[q], dev, 1000) for q in (0, 1, 2, 3)]
+    errs = [] if args.no_profile_pass else [form_errors(hs[q], dev, 1000) for q in range(min(4, len(hs)))]
     b = BatchEngine(hs, device=dev, autotune=True)
     del hs
     b.run(TUNE_STEPS)                # autotuning + warm-up; the tuned settings stay
@@ -599,7 +612,10 @@ def batch_workload(args, dist, dev):
     t = dist.reduce(prof["total_ms"], "max")
     total = dist.reduce(float(n), "sum")
     contacts = int(b.observables()[9])
-    out = {"workload": f"hopper_batch_{args.batch_scenes}", "scenes": args.batch_scenes, "particles": n,
+    out = {"workload": f"hopper_batch_{args.batch_scenes}", "scenes": args.batch_scenes, "particles": int(total),
+           "scaling": "strong" if dist.world > 1 else None,
+           "placement": {"scenes_per_rank": [len(p) for p in dist.gather(mine)],
+                         "particles_per_rank": dist.gather(n), "rule": "longest first to the least-loaded GPU"},
            "active_contacts_end": contacts, "z_pp": contacts / n,
            "value": total * args.batch_steps / (t * 1e-3), "unit": UNIT, "ms_per_step": t / args.batch_steps,
            "steps": args.batch_steps, "gpu_launches": prof["launches"], "tuning": b.tuning(),
@@ -610,7 +626,7 @@ def batch_workload(args, dist, dev):
                                                           default=None)},
            "note": f"steps {TUNE_STEPS}..{TUNE_STEPS + args.batch_steps} of the configured 5000-step run, columns "
                    "resting on touching lattices and draining through the orifice; mixed form, CUDA-graph check "
-                   "intervals, autotuned tick block, skin and cell scale; errors on scenes 0-3 alone "
+                   "intervals, autotuned tick block, skin and cell scale; errors on the first four scenes of the GPU's share alone "
                    "(bit-identical to their batch slices)"}
     b.close()
     return out
@@ -732,29 +748,49 @@ def dense_workload(args, dist, dev):
                     "step 0), ISwH E 70 GPa, dt 5e-7; per-step impulse error from identical state after one step"}
 
 
-def serving_workload(args, dev):
+def serving_workload(args, dist, dev):
     """The serving stream: Poisson arrivals at 200 jobs/s for `--serve-duration` s, sphere
     counts 2e3..2e5, step counts 1e3..2e4 (x `--serve-steps-scale`).  Served by the
     continuous-batching server (mixed form), latency = completion - submission, over every job
-    including the drain after the last arrival.  For comparison the first `--serve-fp64-jobs`
-    jobs of the same stream run one at a time on the plain FP64 engine with the same arrival
-    times (the whole stream would take minutes in that form)."""
-    from vedo_gb300 import serve
+    including the drain after the last arrival.  On N GPUs one server per GPU takes the jobs
+    that vedo_gb300.partition.dispatch_stream hands it (in arrival order, to the GPU with the
+    least spheres x steps so far); latencies are pooled over all GPUs.  For comparison the
+    first `--serve-fp64-jobs` jobs of the stream run one at a time on the plain FP64 engine with
+    the same arrival times, on rank 0 (the whole stream would take minutes in that form)."""
+    from vedo_gb300 import partition, serve
     from vedo_gb300.engine import GpuEngine
     sl, sh = max(1, int(1000 * args.serve_steps_scale)), max(2, int(20000 * args.serve_steps_scale))
-    stream = serve.job_stream(rate=200.0, duration=args.serve_duration, seed=4242, steps_lo=sl, steps_hi=sh)
-    if not stream:
+    whole = serve.job_stream(rate=200.0, duration=args.serve_duration, seed=4242, steps_lo=sl, steps_hi=sh)
+    if not whole:
         return None
+    last_arrival = whole[-1][0]
+    ranks = partition.dispatch_stream([n * st for (_, _, n, st, _, _) in whole], dist.world)
+    mine = [q for q, r in enumerate(ranks) if r == dist.rank]
+    stream = [whole[q] for q in mine]
     built = [serve.job_scene(k, n, m, sd, st) for (_, k, n, st, m, sd) in stream]
+    offered = dist.reduce(float(sum(scene_particles(sc) * st for sc, (_, _, _, st, _, _) in zip(built, stream))),
+                          "sum") / max(last_arrival, 1e-9)
+    dist.barrier()
     with serve.Server(hbm_budget_bytes=150 * 10**9, device=dev) as srv:
-        r = serve.serve_stream(srv, stream, built)
-        st = srv.stats()
-    last_arrival = stream[-1][0]
+        r = serve.serve_stream(srv, stream, built) if stream else None
+        batches = srv.stats()["batches"]
+    del built
+    lat = {}
+    for part in dist.gather({q: i["done_s"] - i["submit_s"] for q, i in zip(mine, r["infos"] if r else [])
+                             if i["status"] == "done"}):
+        lat.update(part)
+    wall = dist.reduce(r["wall_s"] if r else 0.0, "max")
+    served = dist.reduce(float(r["particle_steps"]) if r else 0.0, "sum")
+    batches = int(dist.reduce(float(batches), "sum"))
+    jobs_per_rank = dist.gather(len(stream))
+    if dist.rank != 0:
+        return None
+    pooled = serve.latency_percentiles(list(lat.values()))
     # the first jobs of the same stream one at a time on the FP64 engine
-    k64 = min(args.serve_fp64_jobs, len(stream))
-    parts = [scene_particles(sc) for sc in built]
-    t_free, lat64, busy = 0.0, [], 0.0
-    for (ta, _, _, steps, _, _), sc in zip(stream[:k64], built[:k64]):
+    k64 = min(args.serve_fp64_jobs, len(whole))
+    t_free, lat64, busy, ps64 = 0.0, [], 0.0, 0
+    for ta, k, n, steps, m, sd in whole[:k64]:
+        sc = serve.job_scene(k, n, m, sd, steps)
         t0 = time.perf_counter()
         e = GpuEngine(sc, up_iact=20, device=dev)
         e.run(steps)
@@ -764,17 +800,17 @@ def serving_workload(args, dev):
         start = max(ta, t_free)
         t_free = start + d
         lat64.append(t_free - ta)
-    ps64 = sum(p * s_ for p, (_, _, _, s_, _, _) in zip(parts[:k64], stream[:k64]))
+        ps64 += scene_particles(sc) * steps
     p64 = serve.latency_percentiles(lat64)
-    lat_mixed_sample = [i["done_s"] - i["submit_s"] for i in r["infos"][:k64] if i["status"] == "done"]
-    pm = serve.latency_percentiles(lat_mixed_sample) if lat_mixed_sample else {}
-    return {"workload": f"serving stream, 200 jobs/s x {args.serve_duration} s ({len(stream)} jobs), "
+    same = [lat[q] for q in range(k64) if q in lat]
+    pm = serve.latency_percentiles(same) if same else {}
+    return {"workload": f"serving stream, 200 jobs/s x {args.serve_duration} s ({len(whole)} jobs), "
                         f"steps {sl}..{sh} (x{args.serve_steps_scale:g} of 1e3..2e4), 2e3..2e5 spheres",
-            "p50_ms": r["p50_ms"], "p99_ms": r["p99_ms"], "mean_ms": r["mean_ms"], "jobs_done": r["done"],
-            "jobs": r["jobs"], "served_particle_steps_per_s": r["served_particle_steps_per_s"],
-            "offered_particle_steps_per_s": r["offered_particle_steps_per_s"], "wall_s": r["wall_s"],
-            "last_arrival_s": last_arrival, "drain_s": r["wall_s"] - last_arrival,
-            "batches_built": st["batches"], "hbm_budget_gb": 150,
+            "p50_ms": pooled["p50_ms"], "p99_ms": pooled["p99_ms"], "mean_ms": pooled["mean_ms"],
+            "jobs_done": len(lat), "jobs": len(whole), "served_particle_steps_per_s": served / max(wall, 1e-9),
+            "offered_particle_steps_per_s": offered, "wall_s": wall,
+            "last_arrival_s": last_arrival, "drain_s": wall - last_arrival,
+            "batches_built": batches, "hbm_budget_gb_per_gpu": 150, "jobs_per_gpu": jobs_per_rank,
             "fp64_one_at_a_time": {"jobs": k64, "p50_ms": p64["p50_ms"], "p99_ms": p64["p99_ms"],
                                    "particle_steps_per_s": ps64 / max(busy, 1e-9), "busy_s": busy,
                                    "mixed_server_same_jobs_p50_ms": pm.get("p50_ms"),

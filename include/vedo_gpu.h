@@ -169,10 +169,14 @@ typedef struct vedo_engine_opts {
     uint32_t stored_splits;   /* MIXED only: 1 = the hi/lo FP32 splits of the positions used by
                                  the sphere-pair overlap test are stored once per step; 0 = formed
                                  per pair (identical results; the autotuner chooses)       */
-    uint32_t split_tick;      /* MIXED only: 1 = a light tick (prefilter only, high occupancy)
-                                 finishes the spheres without a pair on the exact path and
-                                 defers the rest to the full tick; 0 = one full tick
-                                 (identical results; the autotuner chooses)                 */
+    uint32_t split_tick;      /* MIXED only, the form of the tick: 0 = one full tick (each
+                                 sphere walks its list and evaluates its pairs); 1 = a light
+                                 tick (prefilter only, high occupancy) finishes the spheres
+                                 without a pair on the exact path and defers the rest to the
+                                 full tick; 2 = the pair pass (a prefilter pass lists the pairs
+                                 on the exact path, each is evaluated once, then every sphere
+                                 sums its pairs' records in list order).  Identical results;
+                                 the autotuner chooses                                     */
     uint32_t full_walks;      /* MIXED only: 1 = every sphere walks its neighbour list every
                                  step; 0 = a sphere whose pairs are all certainly apart since
                                  the rebuild, with clean history, skips the walk (default;
@@ -338,8 +342,8 @@ void vedo_gpu_set_profiling(vedo_gpu_engine* e, int on);
 const char* vedo_gpu_last_error(const vedo_gpu_engine* e);
 void vedo_gpu_destroy(vedo_gpu_engine* e);
 
-/* Skin (fraction of r_max), cell scale, tick block size, split storage and split tick (the last
- * two may be NULL) in use by a MIXED-form engine,
+/* Skin (fraction of r_max), cell scale, tick block size, split storage and the form of the tick
+ * (vedo_engine_opts.split_tick: 0, 1 or 2; the last two may be NULL) in use by a MIXED-form engine,
  * after autotuning when it was asked for.  No counterpart in the reference. */
 int vedo_gpu_get_tuning(const vedo_gpu_engine* e, float* skin, float* cell_scale, uint32_t* tick_block,
                         uint32_t* stored_splits, uint32_t* split_tick);
@@ -374,8 +378,10 @@ int vedo_gpu_scene_range(const vedo_gpu_engine* e, uint32_t scene, uint32_t* fir
  * budget: VEDO_SRV_BYTES_PER_OBJECT per object (state, FP32 copies, splits, sort and cell
  * keys, staging) plus, per sphere, VEDO_SRV_ENTRIES_PER_SPHERE neighbour-list entries of
  * VEDO_SRV_BYTES_PER_ENTRY (the current and previous list with their history and flags, the
- * wall-impulse rows, all with the 25 % growth the engine allocates); a dense packing lists
- * 12-14 neighbours per sphere within its skin.  The live set is kept at
+ * wall-impulse rows, all with the 25 % growth the engine allocates), and
+ * VEDO_SRV_BYTES_PER_ENTRY_PAIR_PASS more per entry when the server's options ask for the pair
+ * pass or for autotuning (the pair pass's worklist, marks and pair records); a dense packing
+ * lists 12-14 neighbours per sphere within its skin.  The live set is kept at
  * or below half the budget, because adding or removing jobs builds the next batch on the
  * device while the current one still exists.  Admitted jobs join the batch at the next
  * check interval, with their state and contact history resident on the device from then
@@ -385,6 +391,7 @@ int vedo_gpu_scene_range(const vedo_gpu_engine* e, uint32_t scene, uint32_t* fir
 #define VEDO_SRV_BYTES_PER_OBJECT 800u
 #define VEDO_SRV_ENTRIES_PER_SPHERE 18u
 #define VEDO_SRV_BYTES_PER_ENTRY 150u
+#define VEDO_SRV_BYTES_PER_ENTRY_PAIR_PASS 72u
 enum { VEDO_JOB_QUEUED = 0, VEDO_JOB_RUNNING = 1, VEDO_JOB_DONE = 2, VEDO_JOB_CANCELLED = 3, VEDO_JOB_FAILED = 4 };
 
 typedef struct vedo_job_info {

@@ -135,6 +135,51 @@ def test_split_tick_agrees_with_one_tick(which, box_ido, drum_ido, engine_lib):
         assert np.array_equal(sa[k], sb[k]), k
 
 
+@pytest.mark.parametrize("which", ["dense", "box", "drum", "hopper", "bed", "holed", "shell"])
+@pytest.mark.parametrize("stored", [False, True])
+def test_pair_pass_agrees_with_one_tick(which, stored, box_ido, drum_ido, engine_lib):
+    """The pair pass (prefilter pass, each pair on the exact path evaluated once, per-sphere sums
+    of the pair records in list order) gives the single tick's state, impulses and contact
+    history bit for bit, over calls of uneven length (impulses written on each call's last step),
+    rebuilds, walls (fixed plates, rods, a holed plate, an orbital top plate) and contacts that
+    form and break."""
+    sc = {"dense": lambda: scenes.dense_pack(n=20000), "box": lambda: box_ido, "drum": lambda: drum_ido,
+          "hopper": lambda: scenes.hopper(n=6000, touching=True),
+          "bed": lambda: scenes.compressed_bed(n=20000, box=0.03, cylinders=1, plate_speed=0.5),
+          "holed": lambda: scenes.holed_plate_drop(), "shell": lambda: scenes.shell_drop(rpm=30.0)}[which]()
+    a = engine_lib.GpuEngine(sc, precision=1, stored_splits=stored)
+    b = engine_lib.GpuEngine(sc, precision=1, stored_splits=stored, pair_pass=True)
+    assert b.tuning()["pair_pass"] and not a.tuning()["pair_pass"] and not b.tuning()["split_tick"]
+    for n in (7, 1, 33, 100, 2, 157):
+        a.run(n)
+        b.run(n)
+        _same_run(a, b)
+    if which in ("dense", "bed"):
+        assert (b.interactions()["active"] == 1).sum() > 100
+    elif which == "box":
+        assert (b.interactions()["active"] == 1).sum() > 10
+
+
+def test_pair_pass_batch_equals_alone(engine_lib):
+    """A scene's slice of a pair-pass batch equals the scene run alone in the single tick."""
+    hs = [scenes.hopper(n=n, seed=s, touching=True) for n, s in ((3000, 1), (5000, 2), (1200, 3))]
+    b = engine_lib.BatchEngine(hs, pair_pass=True)
+    b.run(250)
+    for q, h in enumerate(hs):
+        e = engine_lib.GpuEngine(h, precision=1)
+        e.run(250)
+        st, sb = e.state(), b.scene_state(q)
+        for k in ("position", "velocity", "angular_velocity"):
+            assert np.array_equal(st[k], sb[k]), (q, k)
+        e.close()
+    b.close()
+
+
+def test_split_tick_and_pair_pass_are_exclusive(engine_lib):
+    with pytest.raises(ValueError):
+        engine_lib.GpuEngine(scenes.dense_pack(n=2000), precision=1, split_tick=True, pair_pass=True)
+
+
 def _active_history(e):
     it = e.interactions()
     a = np.nonzero(it["active"] == 1)[0]

@@ -88,23 +88,25 @@ def test_cancel_and_oversized_jobs(engine_lib):
 
 
 @pytest.mark.parametrize("which", ["projectile", "dense"])
-def test_admission_charge_covers_the_engine_allocations(which, engine_lib):
-    """The charge a job is admitted against (objects and expected neighbour-list entries) is at
-    least the device memory a MIXED engine of that scene allocates once its list is built and
-    has been rebuilt (two lists alive), here measured as the drop in the device's free memory;
-    the dense pack (12 neighbours per sphere in contact) is the list's worst case."""
+@pytest.mark.parametrize("pair_pass", [False, True])
+def test_admission_charge_covers_the_engine_allocations(which, pair_pass, engine_lib):
+    """The charge a job is admitted against (objects and expected neighbour-list entries, plus
+    the pair pass's per-entry buffers when the server may run it) is at least the device memory
+    a MIXED engine of that scene allocates once its list is built and has been rebuilt (two
+    lists alive), here measured as the drop in the device's free memory; the dense pack (12
+    neighbours per sphere in contact) is the list's worst case."""
     torch = pytest.importorskip("torch")
     from vedo_gb300.scene import SPHERE
     from vedo_gb300.serve import Server, job_charge
     sc = scenes.serving_job("projectile", 40000, "hertz", 3) if which == "projectile" else scenes.dense_pack(n=40000)
     nsph = int(sum(1 for m in sc.model_index if sc.models[m].shape == SPHERE))
-    charge = job_charge(sc.num_objects, nsph)
-    with Server(hbm_budget_bytes=10**10) as srv:            # the server reports the same charge
+    charge = job_charge(sc.num_objects, nsph, pair_pass=pair_pass)
+    with Server(hbm_budget_bytes=10**10, pair_pass=pair_pass) as srv:    # the server reports the same charge
         j = srv.submit(sc, 1)
         assert srv.wait(j, 120.0)["charged_bytes"] == charge
     torch.cuda.synchronize()
     free0 = torch.cuda.mem_get_info()[0]
-    e = engine_lib.GpuEngine(sc, precision=1, skin=0.4)
+    e = engine_lib.GpuEngine(sc, precision=1, skin=0.4, pair_pass=pair_pass)
     e.run(200)
     e.set_state(position=e.state(("position",))["position"] + 1.0)   # a jump past the skin: a rebuild
     e.run(5)

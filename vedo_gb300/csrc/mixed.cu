@@ -486,7 +486,13 @@ struct TickArgs {
     float4* xsB;                   // ... after the step
     int xs_stored;                 // 1: splits stored once per step; 0: formed per pair
     uint32_t* work;                // split tick: spheres deferred to the full tick (else nullptr)
-    uint32_t* nwork;
+    uint32_t* nwork;               // split tick: spheres in `work`; pair pass: pairs in `pwork`
+    uint2* pwork;                  // pair pass: (owner entry, its sphere) of every pair on the exact path
+    uint8_t* xf;                   // pair pass: [ne] 1 = the entry is on the exact path this step
+    float4* prec;                  // pair pass: [ne][3] at the owner entry: (J, kind), torque on the
+                                   // slave, torque on the master
+    uint8_t* wk;                   // pair pass: [n] 1 = the sphere is quiet this step
+    uint32_t pcap;                 // pair pass: entries `pwork`, `xf` and `prec` hold
     const float4* mf;              // [nm][2]: field + external impulse per step, 1/m~; 2.5/(m~ r^2)
     unsigned* vrel_bits;           // max over spheres of the speed relative to the scene's frame
     const double* ext;             // [2][n][3] external impulse, angular impulse of this step (or nullptr)
@@ -559,7 +565,7 @@ __device__ __noinline__ void wall_pair(const TickArgs& a, int cd, uint32_t pi, u
 // entries that need the exact path.  The side effects are idempotent, so a walk that is
 // abandoned and redone (the split tick) leaves the same state.
 __device__ __forceinline__ uint32_t prefilter_group(const TickArgs& a, uint32_t base, uint32_t e1, const float4& p32i,
-                                                    float pad, bool& dirty) {
+                                                    float pad, bool& dirty, uint32_t& owned) {
     uint32_t ge[TICK_GROUP], gm[TICK_GROUP];
     uint8_t gf[TICK_GROUP];
     float4 gp[TICK_GROUP];
@@ -585,6 +591,7 @@ __device__ __forceinline__ uint32_t prefilter_group(const TickArgs& a, uint32_t 
         const bool i_slave = meta & META_SLAVE;
         if (meta & META_BOND) {
             exact |= 1u << k;
+            if (meta & META_OWNER) owned |= 1u << k;
             continue;
         }
         const float4 ws = wall ? a.wall32[j] : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
@@ -598,6 +605,7 @@ __device__ __forceinline__ uint32_t prefilter_group(const TickArgs& a, uint32_t 
         }
         if (!apart32(cd, i_slave ? p32i : gp[k], i_slave ? gp[k] : p32i, ws, a.reach[meta & META_PI] + pk)) {
             exact |= 1u << k;
+            if (meta & META_OWNER) owned |= 1u << k;
             continue;
         }
         if (wall && a.write_imp) {
@@ -709,6 +717,93 @@ __device__ __forceinline__ float2 finish_sphere(const TickArgs& a, uint32_t i, b
     return make_float2(0.0f, 0.0f);
 }
 
+// The exact path of one list entry e of sphere i (entry `meta`): the pair in canonical (slave,
+// master) orientation from the previous positions, FP32 velocity copies and the pair's history,
+// so both members of a sphere pair obtain the same bits; the history owner writes the new status
+// into the other buffer, a wall entry writes the wall's share of the impulse.  Returns 0 (nothing
+// added), 1 (impulse J only) or 2 (J and the torques tA on the slave, tB on the master).
+template <int LAW, bool XS>
+__device__ __forceinline__ int exact_pair(const TickArgs& a, uint32_t i, const d3& Pi, uint32_t e, uint32_t meta,
+                                          float dtf, f3& Jp, f3& tA, f3& tB) {
+    const uint32_t ent = a.nent[e];
+    const uint32_t j = ent & ~WALL_BIT;
+    const bool wall = ent & WALL_BIT;
+    // canonical orientation (Assembler.cpp:43-67), fixed at rebuild; sphere-wall: the sphere is the slave
+    const bool i_slave = meta & META_SLAVE;
+    const bool owner = meta & META_OWNER;
+    const uint32_t s = i_slave ? i : j, m = i_slave ? j : i;
+    const uint32_t pi = meta & META_PI;
+    const uint32_t slot = owner ? e : a.nslot[e];
+    const PairParam& P = a.params[pi];
+    bool active;
+    float depth;
+    f3 n, rA, rB;
+    if (P.cd == CD_SS) {
+        // d = x_master - x_slave, |d|^2 and R^2 - |d|^2 in double-float from the two
+        // positions' hi/lo splits; where the numerator is within 1e-9 R^2 of zero the
+        // reference's FP64 formula decides
+        float4 hi_i, lo_i, hj, lj;
+        if (XS) {
+            hj = a.xsA[2 * j];
+            lj = a.xsA[2 * j + 1];
+            hi_i = a.xsA[2 * i];
+            lo_i = a.xsA[2 * i + 1];
+        } else {
+            const d3 Pj = ld(a.xA, j);
+            split32(Pj.x, hj.x, lj.x);
+            split32(Pj.y, hj.y, lj.y);
+            split32(Pj.z, hj.z, lj.z);
+            split32(Pi.x, hi_i.x, lo_i.x);
+            split32(Pi.y, hi_i.y, lo_i.y);
+            split32(Pi.z, hi_i.z, lo_i.z);
+        }
+        const float4 hs = i_slave ? hi_i : hj, ls = i_slave ? lo_i : lj;
+        const float4 hm = i_slave ? hj : hi_i, lm = i_slave ? lj : lo_i;
+        const dfl dx = df_diff(hm.x, lm.x, hs.x, ls.x), dy = df_diff(hm.y, lm.y, hs.y, ls.y),
+                  dz = df_diff(hm.z, lm.z, hs.z, ls.z);
+        const dfl s2 = df_add(df_add(df_sq(dx), df_sq(dy)), df_sq(dz));
+        const float4 rq = a.rr32[pi];                // R^2 hi, R^2 lo, band, R
+        const dfl num = df_add(dfl{rq.x, rq.y}, dfl{-s2.hi, -s2.lo});
+        if (num.hi < -rq.z || num.hi > rq.z) {
+            active = num.hi > 0.0f;
+            depth = (num.hi + num.lo) / (rq.w + sqrtf(s2.hi));
+        } else {                               // tie band: the reference's formula decides
+            const double dex = tie_depth(a, pi, s, m);
+            active = dex > 0.0;
+            depth = (float)dex;
+        }
+        const f3 df = fm(dx.hi + dx.lo, dy.hi + dy.lo, dz.hi + dz.lo);
+        n = fdir(df);
+        rA = (a.pc32[8 * (size_t)pi + 7] - 0.5f * depth) * n;   // slot 7: the slave's radius
+        rB = rA - df;
+    } else {
+        wall_pair(a, P.cd, pi, s, m, active, depth, n, rA, rB);
+    }
+    const uint8_t f0 = a.fA[slot];
+    uint8_t f = f0 & 15;
+    float4 h = (f != 0 || active) ? a.hA[slot] : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+    Jp = fm(0.0f, 0.0f, 0.0f);
+    tA = Jp;
+    tB = Jp;
+    const int app = solve32<LAW>(P.is, a.pc32 + 8 * (size_t)pi, active, depth, n, rA, rB, f4to3(a.v32A[s]),
+                                 f4to3(a.v32A[m]), f4to3(a.w32A[s]), f4to3(a.w32A[m]), dtf, f, h, Jp, tA, tB);
+    if (e == slot) {                           // history owner writes the new status
+        if (f != 0 || (f0 & 15) != 0) {
+            a.hB[slot] = h;
+            a.fB[slot] = (uint8_t)(f | ((f == 0) ? HF_PENDING : 0));
+        } else if (f0 & HF_PENDING) {
+            a.hB[slot] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+            a.fB[slot] = 0;
+        }
+    }
+    if (wall && a.write_imp) {                 // the wall's share, summed per wall later
+        float* o = a.wimp + 6 * (size_t)e;
+        o[0] = app ? -Jp.x : 0.0f; o[1] = app ? -Jp.y : 0.0f; o[2] = app ? -Jp.z : 0.0f;
+        o[3] = app == 2 ? tB.x : 0.0f; o[4] = app == 2 ? tB.y : 0.0f; o[5] = app == 2 ? tB.z : 0.0f;
+    }
+    return app;
+}
+
 // One sphere's step: neighbour walk (prefilter, then the exact path in entry order), sums,
 // integration.  Returns its squared speed bounds of the step.
 template <int LAW, bool XS>
@@ -727,7 +822,6 @@ __device__ __forceinline__ float2 tick_sphere(const TickArgs& a, uint32_t i) {
         const ModelDev& M = a.models[mi];
         const SceneDev& S = a.scenes[si];
         if (M.scope == SCOPE_LOCAL && S.active) {
-            const double dt = S.dt;
             const float dtf = S.dtf;
             const float pad = 2.0f * disp;
             const float4 mf0 = a.mf[2 * mi], mf1 = a.mf[2 * mi + 1];
@@ -738,99 +832,34 @@ __device__ __forceinline__ float2 tick_sphere(const TickArgs& a, uint32_t i) {
             const bool quiet = qc >= 2u && !a.write_imp && pad <= cl.x && a.disp[1] <= cl.y;
             bool dirty = false, any_exact = false;
             K3 J, JA;
-            for (uint32_t base = e0; base < e1 && !quiet; base += TICK_GROUP) {
-                uint32_t exact = prefilter_group(a, base, e1, p32i, pad, dirty);
-                any_exact |= exact != 0u;
+            // The list is walked in chunks of 64 entries (one chunk for nearly every sphere):
+            // phase 1 prefilters the whole chunk into a mask, phase 2 runs the exact path over
+            // it.  A warp then iterates phase 2 as often as its busiest sphere has exact entries
+            // in the chunk, not as often as the busiest sphere of each group of entries has.
+            for (uint32_t c0 = e0; c0 < e1 && !quiet; c0 += 64) {
+                const uint32_t c1 = min(e1, c0 + 64);
+                unsigned long long exact = 0ull;
+                uint32_t owned = 0u;                   // (unused here)
+                for (uint32_t base = c0; base < c1; base += TICK_GROUP)
+                    exact |= (unsigned long long)prefilter_group(a, base, c1, p32i, pad, dirty, owned) << (base - c0);
+                any_exact |= exact != 0ull;
                 // Phase 2: the exact path for the flagged entries, in entry order
                 while (exact) {
-                const int k = __ffs(exact) - 1;
-                exact &= exact - 1;
-                const uint32_t e = base + k;
-                const uint32_t ent = a.nent[e];            // (reloaded: a register array indexed by k would spill)
-                const uint32_t meta = a.nmeta[e];
-                const uint32_t j = ent & ~WALL_BIT;
-                const bool wall = ent & WALL_BIT;
-                // canonical orientation (Assembler.cpp:43-67), fixed at rebuild; sphere-wall: the sphere is the slave
-                const bool i_slave = meta & META_SLAVE;
-                const bool owner = meta & META_OWNER;
-                const uint32_t s = i_slave ? i : j, m = i_slave ? j : i;
-                const uint32_t pi = meta & META_PI;
-                const uint32_t slot = owner ? e : a.nslot[e];
-                const PairParam& P = a.params[pi];
-                bool active;
-                float depth;
-                f3 n, rA, rB;
-                if (P.cd == CD_SS) {
-                    // d = x_master - x_slave, |d|^2 and R^2 - |d|^2 in double-float from the two
-                    // positions' hi/lo splits; where the numerator is within 1e-9 R^2 of zero the
-                    // reference's FP64 formula decides
-                    float4 hi_i, lo_i, hj, lj;
-                    if (XS) {
-                        hj = a.xsA[2 * j];
-                        lj = a.xsA[2 * j + 1];
-                        hi_i = a.xsA[2 * i];
-                        lo_i = a.xsA[2 * i + 1];
-                    } else {
-                        const d3 Pj = ld(a.xA, j);
-                        split32(Pj.x, hj.x, lj.x);
-                        split32(Pj.y, hj.y, lj.y);
-                        split32(Pj.z, hj.z, lj.z);
-                        split32(Pi.x, hi_i.x, lo_i.x);
-                        split32(Pi.y, hi_i.y, lo_i.y);
-                        split32(Pi.z, hi_i.z, lo_i.z);
+                    const int k = __ffsll(exact) - 1;
+                    exact &= exact - 1;
+                    const uint32_t e = c0 + k;
+                    const uint32_t meta = a.nmeta[e];
+                    f3 Jp, tA, tB;
+                    const int app = exact_pair<LAW, XS>(a, i, Pi, e, meta, dtf, Jp, tA, tB);
+                    if (app) {
+                        if (meta & META_SLAVE) {
+                            J.add(Jp);
+                            if (app == 2) JA.add(tA);
+                        } else {
+                            J.add(-Jp);
+                            if (app == 2) JA.add(tB);
+                        }
                     }
-                    const float4 hs = i_slave ? hi_i : hj, ls = i_slave ? lo_i : lj;
-                    const float4 hm = i_slave ? hj : hi_i, lm = i_slave ? lj : lo_i;
-                    const dfl dx = df_diff(hm.x, lm.x, hs.x, ls.x), dy = df_diff(hm.y, lm.y, hs.y, ls.y),
-                              dz = df_diff(hm.z, lm.z, hs.z, ls.z);
-                    const dfl s2 = df_add(df_add(df_sq(dx), df_sq(dy)), df_sq(dz));
-                    const float4 rq = a.rr32[pi];                // R^2 hi, R^2 lo, band, R
-                    const dfl num = df_add(dfl{rq.x, rq.y}, dfl{-s2.hi, -s2.lo});
-                    if (num.hi < -rq.z || num.hi > rq.z) {
-                        active = num.hi > 0.0f;
-                        depth = (num.hi + num.lo) / (rq.w + sqrtf(s2.hi));
-                    } else {                               // tie band: the reference's formula decides
-                        const double dex = tie_depth(a, pi, s, m);
-                        active = dex > 0.0;
-                        depth = (float)dex;
-                    }
-                    const f3 df = fm(dx.hi + dx.lo, dy.hi + dy.lo, dz.hi + dz.lo);
-                    n = fdir(df);
-                    rA = (a.pc32[8 * (size_t)pi + 7] - 0.5f * depth) * n;   // slot 7: the slave's radius
-                    rB = rA - df;
-                } else {
-                    wall_pair(a, P.cd, pi, s, m, active, depth, n, rA, rB);
-                }
-                const uint8_t f0 = a.fA[slot];
-                uint8_t f = f0 & 15;
-                float4 h = (f != 0 || active) ? a.hA[slot] : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
-                f3 Jp = fm(0.0f, 0.0f, 0.0f), tA = Jp, tB = Jp;
-                const int app = solve32<LAW>(P.is, a.pc32 + 8 * (size_t)pi, active, depth, n, rA, rB,
-                                        f4to3(a.v32A[s]), f4to3(a.v32A[m]), f4to3(a.w32A[s]), f4to3(a.w32A[m]), dtf, f,
-                                        h, Jp, tA, tB);
-                if (e == slot) {                           // history owner writes the new status
-                    if (f != 0 || (f0 & 15) != 0) {
-                        a.hB[slot] = h;
-                        a.fB[slot] = (uint8_t)(f | ((f == 0) ? HF_PENDING : 0));
-                    } else if (f0 & HF_PENDING) {
-                        a.hB[slot] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
-                        a.fB[slot] = 0;
-                    }
-                }
-                if (app) {
-                    if (i_slave) {
-                        J.add(Jp);
-                        if (app == 2) JA.add(tA);
-                    } else {
-                        J.add(-Jp);
-                        if (app == 2) JA.add(tB);
-                    }
-                }
-                if (wall && a.write_imp) {                 // the wall's share, summed per wall later
-                    float* o = a.wimp + 6 * (size_t)e;
-                    o[0] = app ? -Jp.x : 0.0f; o[1] = app ? -Jp.y : 0.0f; o[2] = app ? -Jp.z : 0.0f;
-                    o[3] = app == 2 ? tB.x : 0.0f; o[4] = app == 2 ? tB.y : 0.0f; o[5] = app == 2 ? tB.z : 0.0f;
-                }
                 }
             }
             if (!a.work && !quiet) note_walk(a, i, qc, dirty || any_exact);
@@ -930,8 +959,9 @@ __global__ void __launch_bounds__(TPB, 6) k_tick_light(TickArgs a) {   // 6 bloc
                 const uint32_t e0 = a.nptr[i], e1 = a.nptr[i + 1];
                 const float4 p32i = a.pos32[i];
                 bool dirty = false;
+                uint32_t owned = 0u;                   // (unused here)
                 for (uint32_t base = e0; base < e1 && !defer; base += TICK_GROUP)
-                    defer = prefilter_group(a, base, e1, p32i, pad, dirty) != 0u;
+                    defer = prefilter_group(a, base, e1, p32i, pad, dirty, owned) != 0u;
                 note_walk(a, i, a.qcnt[i], dirty || defer);    // (reread: fewer live registers in the walk)
             }
             if (!defer) {                          // state loaded after the walk: fewer live registers
@@ -954,6 +984,149 @@ __global__ void __launch_bounds__(TPB, 6) k_tick_light(TickArgs a) {   // 6 bloc
         if (lane == lead) at = atomicAdd(a.nwork, (uint32_t)__popc(dm));
         at = __shfl_sync(0xffffffffu, at, lead);
         if (defer) a.work[at + __popc(dm & ((1u << lane) - 1u))] = i;
+    }
+    reduce_vmax(a, vmax_local);
+}
+
+// ---- pair pass ------------------------------------------------------------------------------
+// The tick in three kernels, each pair on the exact path evaluated once:
+//  k_tick_pf     every sphere's list walk in prefilter form (with the single tick's history
+//                cleaning and clean-walk count), marking the entries on the exact path and
+//                appending each such pair once, at its history owner, to a worklist;
+//  k_tick_pairs  one thread per pair of the worklist: the exact path (exact_pair, the single
+//                tick's arithmetic) writes the pair's impulse and torques at its owner entry;
+//  k_tick_sum    one thread per sphere: the records of its marked entries in entry order join
+//                the compensated sums, then the sphere is integrated (finish_sphere).
+// Both members of a pair add the one evaluation that the single tick computes twice with
+// identical bits, in the same order, so results are the single tick's.  The pair kernel runs
+// with every lane on a pair, where the single tick's lanes wait for the sphere of their warp with
+// the most pairs.
+__global__ void __launch_bounds__(TPB, 4) k_tick_pf(TickArgs a) {     // 63 registers, no spills
+    step_order();
+    if (held_step(a)) return;                      // k_tick_sum holds the state (uniform branch)
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int lane = threadIdx.x & 31;
+    uint32_t c0 = 0u, e1 = 0u, qc = 0u;
+    float4 p32i = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+    float pad = 0.0f;
+    bool walk = false, dirty = false, any_exact = false;
+    if (i < a.n) {
+        const ModelDev& M = a.models[a.model_of[i]];
+        const SceneDev& S = a.scenes[a.scene_of[i]];
+        if (M.scope == SCOPE_LOCAL && S.active) {
+            qc = a.qcnt[i];
+            const float2 cl = a.clear[i];
+            pad = 2.0f * a.disp[0];
+            const bool quiet = qc >= 2u && !a.write_imp && pad <= cl.x && a.disp[1] <= cl.y;
+            a.wk[i] = quiet ? 1u : 0u;
+            if (!quiet) {
+                c0 = a.nptr[i];
+                e1 = a.nptr[i + 1];
+                p32i = a.pos32[i];
+                walk = true;
+            }
+        }
+    }
+    // the warp walks its spheres' lists 64 entries at a time, in step, so that every chunk's
+    // pairs are appended with one atomic per warp
+    bool more = walk && c0 < e1;
+    while (__any_sync(0xffffffffu, more)) {
+        unsigned long long own = 0ull;
+        if (more) {
+            const uint32_t c1 = min(e1, c0 + 64);
+            unsigned long long exact = 0ull;
+            for (uint32_t base = c0; base < c1; base += TICK_GROUP) {
+                uint32_t owned = 0u;
+                exact |= (unsigned long long)prefilter_group(a, base, c1, p32i, pad, dirty, owned) << (base - c0);
+                own |= (unsigned long long)owned << (base - c0);
+            }
+            any_exact |= exact != 0ull;
+            for (uint32_t e = c0; e < c1; ++e) a.xf[e] = (uint8_t)((exact >> (e - c0)) & 1ull);
+        }
+        const uint32_t cnt = (uint32_t)__popcll(own);
+        uint32_t incl = cnt;                       // inclusive prefix over the warp
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const uint32_t v = __shfl_up_sync(0xffffffffu, incl, o);
+            if (lane >= o) incl += v;
+        }
+        uint32_t at = 0u;
+        if (lane == 31 && incl) at = atomicAdd(a.nwork, incl);
+        at = __shfl_sync(0xffffffffu, at, 31) + incl - cnt;
+        while (own) {
+            const int k = __ffsll(own) - 1;
+            own &= own - 1;
+            if (at < a.pcap) a.pwork[at] = make_uint2(c0 + (uint32_t)k, i);   // (at most one per entry)
+            ++at;
+        }
+        if (more) {
+            c0 += 64;
+            more = c0 < e1;
+        }
+    }
+    if (walk) note_walk(a, i, qc, dirty || any_exact);
+}
+
+template <int LAW, bool XS>
+__global__ void __launch_bounds__(TPB) k_tick_pairs(TickArgs a) {
+    step_order();
+    if (held_step(a)) return;
+    const uint32_t nw = min(*a.nwork, a.pcap);
+    for (uint32_t q = blockIdx.x * blockDim.x + threadIdx.x; q < nw; q += gridDim.x * blockDim.x) {
+        const uint2 it = a.pwork[q];
+        const uint32_t e = it.x, i = it.y;
+        const uint32_t meta = a.nmeta[e];
+        const d3 Pi = XS ? mk(0.0, 0.0, 0.0) : ld(a.xA, i);
+        f3 Jp, tA, tB;
+        const int app = exact_pair<LAW, XS>(a, i, Pi, e, meta, a.scenes[a.scene_of[i]].dtf, Jp, tA, tB);
+        float4* r = a.prec + 3 * (size_t)e;
+        r[0] = make_float4(Jp.x, Jp.y, Jp.z, __int_as_float(app));
+        if (app == 2) {
+            r[1] = make_float4(tA.x, tA.y, tA.z, 0.0f);
+            r[2] = make_float4(tB.x, tB.y, tB.z, 0.0f);
+        }
+    }
+}
+
+template <bool XS>
+__global__ void __launch_bounds__(TPB, 4) k_tick_sum(TickArgs a) {
+    step_order();
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    float2 vmax_local = make_float2(0.0f, 0.0f);
+    if (held_step(a)) {
+        hold_state(a, i);
+    } else if (i < a.n) {
+        const uint32_t mi = a.model_of[i];
+        const uint32_t si = a.scene_of[i];
+        const uint32_t e0 = a.nptr[i], e1 = a.nptr[i + 1];
+        const d3 Pi = ld(a.xA, i);
+        const d3 V = ld(a.v64, i);
+        const ModelDev& M = a.models[mi];
+        const SceneDev& S = a.scenes[si];
+        if (M.scope == SCOPE_LOCAL && S.active) {
+            const bool quiet = a.wk[i] != 0u;
+            const float4 mf0 = a.mf[2 * mi], mf1 = a.mf[2 * mi + 1];
+            K3 J, JA;
+            for (uint32_t e = e0; e < e1 && !quiet; ++e) {
+                if (!a.xf[e]) continue;
+                const uint32_t meta = a.nmeta[e];
+                const uint32_t slot = (meta & META_OWNER) ? e : a.nslot[e];
+                const float4 r0 = a.prec[3 * (size_t)slot];
+                const int app = __float_as_int(r0.w);
+                if (app) {
+                    if (meta & META_SLAVE) {
+                        J.add(f4to3(r0));
+                        if (app == 2) JA.add(f4to3(a.prec[3 * (size_t)slot + 1]));
+                    } else {
+                        J.add(-f4to3(r0));
+                        if (app == 2) JA.add(f4to3(a.prec[3 * (size_t)slot + 2]));
+                    }
+                }
+            }
+            vmax_local = finish_sphere<XS>(a, i, M.behavior == BEH_MOBILE, quiet, S, Pi, V, mf0, mf1, J, JA);
+        } else if (M.scope == SCOPE_LOCAL) {
+            hold_state(a, i);
+        }
     }
     reduce_vmax(a, vmax_local);
 }
@@ -2024,7 +2197,7 @@ public:
         out[1] = cell_scale_;
         out[2] = (float)tpb_;
         out[3] = xs_stored_ ? 1.0f : 0.0f;
-        out[4] = split_tick_ ? 1.0f : 0.0f;
+        out[4] = pair_pass_ ? 2.0f : (split_tick_ ? 1.0f : 0.0f);
         return VEDO_OK;
     }
 
@@ -2123,6 +2296,29 @@ private:
     bool xs_stored_ = false;
     bool split_tick_ = false;                     // light + deferred full tick (identical results)
     uint32_t* d_work_ = nullptr;                  // [n] spheres deferred by the light tick
+    bool pair_pass_ = false;                      // prefilter pass, pair pass, per-sphere sums (identical results)
+    uint32_t pcap_ = 0;                           // entries the pair pass's buffers hold
+    uint2* d_pwork_ = nullptr;                    // [pcap] pairs on the exact path (owner entry, sphere)
+    uint8_t* d_xf_ = nullptr;                     // [pcap] entry on the exact path this step
+    float4* d_prec_ = nullptr;                    // [pcap][3] pair records at the owner entry
+    uint8_t* d_wk_ = nullptr;                     // [n] quiet this step (pair pass)
+    int ensure_pair_bufs(uint32_t ne);
+    void free_pair_bufs();
+    // blocks of tpb_ threads of kernel k resident on the whole GPU at once (cached per kernel
+    // and block size)
+    const void* grid_k_ = nullptr;
+    int grid_tpb_ = 0;
+    unsigned grid_blocks_ = 0;
+    unsigned resident_grid(const void* k) {
+        if (k != grid_k_ || tpb_ != grid_tpb_) {
+            int b = 0;
+            if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k, tpb_, 0) != cudaSuccess || b < 1) b = 1;
+            grid_k_ = k;
+            grid_tpb_ = tpb_;
+            grid_blocks_ = (unsigned)b * (unsigned)sms_;
+        }
+        return grid_blocks_;
+    }
     bool quiet_ok_ = true;                        // quiet spheres skip their walk (identical results)
     int sms_ = 1;                                 // streaming multiprocessors of the device
     float2* d_clear_ = nullptr;                   // [n] quiet-sphere pad limits of the current list
@@ -2179,6 +2375,27 @@ void MixedEngine::free_nlist(NList& L) {
     L = NList{};
 }
 
+// The pair pass's per-entry buffers, sized to the list (allocated only while the pair pass is
+// used or tried).
+int MixedEngine::ensure_pair_bufs(uint32_t ne) {
+    if (ne <= pcap_ && d_prec_) return VEDO_OK;
+    free_pair_bufs();
+    const uint64_t c = std::max<uint64_t>(1024, (uint64_t)ne + ne / 4);
+    pcap_ = (uint32_t)std::min<uint64_t>(c, 0x7fffffffull);
+    MCK(mal(&d_pwork_, pcap_));
+    MCK(mal(&d_xf_, pcap_));
+    MCK(mal(&d_prec_, 3 * (size_t)pcap_));
+    return VEDO_OK;
+}
+void MixedEngine::free_pair_bufs() {
+    for (void* p : {(void*)d_pwork_, (void*)d_xf_, (void*)d_prec_})
+        if (p) cudaFree(p);
+    d_pwork_ = nullptr;
+    d_xf_ = nullptr;
+    d_prec_ = nullptr;
+    pcap_ = 0;
+}
+
 int MixedEngine::ensure_nlist(NList& L, uint32_t cap) {
     if (!L.ptr) MCK(mal(&L.ptr, (size_t)n_ + 1));
     if (cap <= L.cap && L.ent) return VEDO_OK;
@@ -2204,10 +2421,11 @@ MixedEngine::~MixedEngine() {
     free_nlist(nl_[1]);
     void* ptrs[] = {d_models_, d_params_, d_pc32_, d_geom_, d_hole_, d_rr_, d_mf_, d_reach_, d_model_of_, d_scene_of_,
                     d_scenes_, d_gfield_, d_glob_, d_x_[0], d_x_[1], d_v64_, d_w64_, d_ox_, d_oz_, d_imp_, d_aimp_,
-                    d_v32_[0], d_v32_[1], d_w32_[0], d_w32_[1], d_rr32_, d_xs_[0], d_xs_[1], d_work_, d_clear_, d_vred_, d_ext_, d_qcnt_, d_pos32_, d_wall32_, d_red_, d_sred_, d_disp_, d_err_,
+                    d_v32_[0], d_v32_[1], d_w32_[0], d_w32_[1], d_rr32_, d_xs_[0], d_xs_[1], d_work_, d_wk_, d_clear_, d_vred_, d_ext_, d_qcnt_, d_pos32_, d_wall32_, d_red_, d_sred_, d_disp_, d_err_,
                     d_key_, d_key_alt_, d_sid_, d_sid_alt_, d_cnt_, d_gs_, d_ge_, d_act_, d_stage_, d_obs_, d_gidx_,
                     d_wkey_, d_wval_, d_wkey_alt_, d_wval_alt_, d_wptr_, d_wimp_, d_wred_, d_wrot_, d_wedge_, d_ext_of_, d_int_of_, d_xe_, d_model_e_};
     for (void* p : ptrs) if (p) cudaFree(p);
+    free_pair_bufs();
     drop_graphs();
     for (auto& e : pev_) cudaEventDestroy(e);
     for (auto& e : ev_) if (e) cudaEventDestroy(e);
@@ -2240,7 +2458,9 @@ int MixedEngine::init_from(const std::vector<SceneSource>& src, const MixedEngin
     if (tpb_ < 32 || tpb_ > TPB || tpb_ % 32) return fail(VEDO_ERR_INVALID_ARGUMENT, "tick_block must be 32..256, a multiple of 32");
     tune_pending_ = opts.autotune != 0;
     xs_stored_ = opts.stored_splits != 0;
-    split_tick_ = opts.split_tick != 0;
+    split_tick_ = opts.split_tick == 1;
+    pair_pass_ = opts.split_tick == 2;
+    if (opts.split_tick > 2) return fail(VEDO_ERR_INVALID_ARGUMENT, "split_tick must be 0, 1 or 2");
     quiet_ok_ = opts.full_walks == 0;
     if (prev) {                    // a repacked engine keeps the tuning of the one it replaces
         skin_frac_ = prev->skin_frac_;
@@ -2248,6 +2468,7 @@ int MixedEngine::init_from(const std::vector<SceneSource>& src, const MixedEngin
         tpb_ = prev->tpb_;
         xs_stored_ = prev->xs_stored_;
         split_tick_ = prev->split_tick_;
+        pair_pass_ = prev->pair_pass_;
         quiet_ok_ = prev->quiet_ok_;
         tune_pending_ = prev->tune_pending_;
     }
@@ -2426,6 +2647,7 @@ int MixedEngine::init_from(const std::vector<SceneSource>& src, const MixedEngin
     MCK(mal(&d_sred_, 8 * sc_.size()));
     MCK(mal(&d_vred_, 6 * sc_.size()));
     MCK(mal(&d_work_, n_));
+    MCK(mal(&d_wk_, n_));
     MCK(mal(&d_clear_, n_));
     MCK(mal(&d_qcnt_, n_));
     MCK(cudaMemset(d_qcnt_, 0, n_));
@@ -2608,6 +2830,11 @@ TickArgs MixedEngine::args(bool write_imp) {
     a.xs_stored = xs_stored_ ? 1 : 0;
     a.work = split_tick_ ? d_work_ : nullptr;
     a.nwork = d_red_ + 14;
+    a.pwork = d_pwork_;
+    a.xf = d_xf_;
+    a.prec = d_prec_;
+    a.wk = d_wk_;
+    a.pcap = pcap_;
     a.mf = d_mf_;
     a.clear = d_clear_;
     a.qcnt = d_qcnt_;
@@ -2735,6 +2962,7 @@ int MixedEngine::rebuild() {
     int rc = ensure_nlist(L, ne);
     if (rc != VEDO_OK) return rc;
     L.ne = ne;
+    if (pair_pass_ && (rc = ensure_pair_bufs(ne)) != VEDO_OK) return rc;
     if (nloc_) {
         k_nbr<true><<<nblk(nloc_), TPB, 0, stream_>>>(nloc_, d_sid_, d_key_, d_gs_, d_ge_, d_scene_of_, d_scenes_,
                                                       d_glob_, d_model_of_, d_models_, d_params_, d_reach_, d_pos32_,
@@ -2857,6 +3085,27 @@ void MixedEngine::launch_step(bool write_imp) {
         if (e != cudaSuccess && launch_err_ == cudaSuccess) launch_err_ = e;
     };
     unsigned nb_full = nb;
+    if (pair_pass_) {               // prefilter pass, pair pass over its worklist, per-sphere sums
+        // (the worklist count is zeroed by k_walls at the end of every step)
+        note(step_launch(dep, k_tick_pf, nblk(n_), TPB, stream_, a));
+        // the pair kernel strides over the worklist with the grid that is resident at once
+#define VEDO_PAIRS(L)                                                                                       \
+    {                                                                                                       \
+        auto kp = xs_stored_ ? k_tick_pairs<L, true> : k_tick_pairs<L, false>;                              \
+        note(step_launch(dep, kp, resident_grid((const void*)kp), (unsigned)tpb_, stream_, a));             \
+    }
+        switch (law_) {
+        case IS_BSDBF: VEDO_PAIRS(IS_BSDBF); break;
+        case IS_BTSDBF: VEDO_PAIRS(IS_BTSDBF); break;
+        case IS_BSDB2F: VEDO_PAIRS(IS_BSDB2F); break;
+        case IS_HERTZ: VEDO_PAIRS(IS_HERTZ); break;
+        case IS_H: VEDO_PAIRS(IS_H); break;
+        default: VEDO_PAIRS(0); break;
+        }
+#undef VEDO_PAIRS
+        note(step_launch(dep, xs_stored_ ? k_tick_sum<true> : k_tick_sum<false>, nblk(n_), TPB, stream_, a));
+        launches_ += 3;
+    } else {
     if (split_tick_) {              // light tick over all spheres, then the full tick over the deferred
         // (the worklist count is zeroed by k_walls at the end of every step)
         note(step_launch(dep, xs_stored_ ? k_tick_light<true> : k_tick_light<false>, nblk(n_), TPB, stream_, a));
@@ -2878,6 +3127,7 @@ void MixedEngine::launch_step(bool write_imp) {
     }
 #undef VEDO_TICK
     ++launches_;
+    }
     if (pe) cudaEventRecordWithFlags(pe[1], stream_, ev_flags_);
     if (write_imp && !glob_.empty()) {
         const uint32_t ng = (uint32_t)glob_.size();
@@ -2999,7 +3249,7 @@ int MixedEngine::autotune(uint32_t max_steps, uint32_t* taken) {
     const float skins[] = {0.05f, 0.1f, 0.15f, 0.25f, 0.4f};
     const float cells[] = {1.0f, 1.25f, 1.5f};
     // at most four chunks per timed trial (a rebuild between may add two), two per skin trial
-    const uint32_t need = ci * (uint32_t)(4 * (3 + 2 + 2) + 2 * 5);
+    const uint32_t need = ci * (uint32_t)(4 * (3 + 2 + 3) + 2 * 5);
     if (max_steps < need) return VEDO_OK;            // too short a call: tune in a later one
     cudaEvent_t e0 = ev_[2], e1 = ev_[3];
     auto timed_rebuild = [&](float* ms) -> int {
@@ -3065,18 +3315,28 @@ int MixedEngine::autotune(uint32_t max_steps, uint32_t* taken) {
         xs_stored_ = t_store < t_form;
         drop_graphs();
     }
-    // 2b. one full tick, or the split tick (a light tick at full occupancy, the full tick over the
-    //     spheres with a pair on the exact path); identical results
+    // 2b. one full tick, the split tick (a light tick at full occupancy, the full tick over the
+    //     spheres with a pair on the exact path) or the pair pass (each pair on the exact path
+    //     evaluated once); identical results
     {
-        float t_one = 0.0f, t_split = 0.0f;
+        float t_one = 0.0f, t_split = 0.0f, t_pair = 0.0f;
         split_tick_ = false;
+        pair_pass_ = false;
         drop_graphs();
         if ((rc = timed_chunk(&t_one, nullptr)) != VEDO_OK) return rc;
         split_tick_ = true;
         drop_graphs();
         if ((rc = timed_chunk(&t_split, nullptr)) != VEDO_OK) return rc;
         if (need_rebuild_ && (rc = rebuild()) != VEDO_OK) return rc;
-        split_tick_ = t_split < t_one;
+        split_tick_ = false;
+        pair_pass_ = true;
+        drop_graphs();
+        if ((rc = ensure_pair_bufs(nl_[nlc_].ne)) != VEDO_OK) return rc;
+        if ((rc = timed_chunk(&t_pair, nullptr)) != VEDO_OK) return rc;
+        if (need_rebuild_ && (rc = rebuild()) != VEDO_OK) return rc;
+        pair_pass_ = t_pair < t_one && t_pair < t_split;
+        split_tick_ = !pair_pass_ && t_split < t_one;
+        if (!pair_pass_) free_pair_bufs();
         drop_graphs();
     }
     // 3. skin: tick time per step plus the amortised rebuild

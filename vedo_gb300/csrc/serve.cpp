@@ -317,8 +317,12 @@ int vedo_srv_submit(vedo_server* s, const vedo_scene_desc* scene, uint64_t steps
         if (m < j->scene.models.size() && j->scene.models[m].scope == VEDO_SCOPE_LOCAL) ++j->particles;
     }
     j->steps = steps;
+    // an engine that may run the pair pass (asked for, or open to the autotuner) also holds its
+    // per-entry worklist, marks and pair records
+    const uint64_t per_entry = VEDO_SRV_BYTES_PER_ENTRY +
+                               ((s->opts.split_tick == 2 || s->opts.autotune) ? VEDO_SRV_BYTES_PER_ENTRY_PAIR_PASS : 0u);
     j->bytes = (uint64_t)VEDO_SRV_BYTES_PER_OBJECT * j->scene.n +
-               (uint64_t)VEDO_SRV_ENTRIES_PER_SPHERE * VEDO_SRV_BYTES_PER_ENTRY * j->particles;
+               (uint64_t)VEDO_SRV_ENTRIES_PER_SPHERE * per_entry * j->particles;
     std::lock_guard<std::mutex> lk(s->mu);
     if (j->bytes > s->budget / 2) {
         s->err = "job needs " + std::to_string(j->bytes) + " bytes, more than half the HBM budget";

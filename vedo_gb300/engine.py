@@ -86,7 +86,7 @@ STATE_FIELDS = ("position", "velocity", "angular_velocity", "orientation_x", "or
 
 def _opts(up_iact, record, precision, device, prefix, skin, check_interval, tick_block=None, cell_scale=None,
           autotune=False, graphs=True, stored_splits=False, split_tick=False, full_walks=False,
-          consultant="nbs") -> EngineOpts:
+          consultant="nbs", pair_pass=False) -> EngineOpts:
     opts = EngineOpts()
     lib().vedo_gpu_default_opts(C.byref(opts))
     opts.up_iact, opts.record, opts.precision, opts.device = up_iact, record, precision, device
@@ -101,7 +101,9 @@ def _opts(up_iact, record, precision, device, prefix, skin, check_interval, tick
     opts.autotune = 1 if autotune else 0
     opts.graphs = 1 if graphs else 0
     opts.stored_splits = 1 if stored_splits else 0
-    opts.split_tick = 1 if split_tick else 0
+    if split_tick and pair_pass:
+        raise ValueError("split_tick and pair_pass are two forms of the tick: choose one")
+    opts.split_tick = 2 if pair_pass else (1 if split_tick else 0)
     opts.full_walks = 1 if full_walks else 0
     if consultant not in ("nbs", "leap"):
         raise ValueError(f"consultant must be 'nbs' or 'leap', not {consultant!r}")
@@ -124,11 +126,11 @@ class GpuEngine:
                  check_interval: Optional[int] = None, tick_block: Optional[int] = None,
                  cell_scale: Optional[float] = None, autotune: bool = False, graphs: bool = True,
                  stored_splits: bool = False, split_tick: bool = False, full_walks: bool = False,
-                 consultant: str = "nbs"):
+                 consultant: str = "nbs", pair_pass: bool = False):
         L = lib()
         self._prefix = output_prefix.encode() if output_prefix else None
         opts = _opts(up_iact, record, precision, device, self._prefix, skin, check_interval, tick_block, cell_scale,
-                     autotune, graphs, stored_splits, split_tick, full_walks, consultant)
+                     autotune, graphs, stored_splits, split_tick, full_walks, consultant, pair_pass)
         h = C.c_void_p()
         if isinstance(scene, (str, bytes, os.PathLike)):
             path = os.fsencode(scene)
@@ -235,12 +237,13 @@ class GpuEngine:
         self._check(lib().vedo_gpu_write_vtk(self.h, os.fsencode(path), 1 if with_coordination else 0))
 
     def tuning(self):
-        """Skin (fraction of r_max), cell scale and tick block size in use (MIXED form)."""
+        """Skin (fraction of r_max), cell scale, tick block size, split storage and the form of
+        the tick (single, split or pair pass) in use (MIXED form)."""
         sk, cs, tb, ss, st = C.c_float(0), C.c_float(0), C.c_uint32(0), C.c_uint32(0), C.c_uint32(0)
         self._check(lib().vedo_gpu_get_tuning(self.h, C.byref(sk), C.byref(cs), C.byref(tb), C.byref(ss),
                                               C.byref(st)))
         return {"skin": float(sk.value), "cell_scale": float(cs.value), "tick_block": int(tb.value),
-                "stored_splits": bool(ss.value), "split_tick": bool(st.value)}
+                "stored_splits": bool(ss.value), "split_tick": st.value == 1, "pair_pass": st.value == 2}
 
     def run_with_impulses(self, impulse=None, angular_impulse=None) -> bool:
         """One step with an external impulse and angular impulse per object ([n, 3] arrays in
@@ -320,11 +323,11 @@ class BatchEngine(GpuEngine):
     def __init__(self, scene_list, device: int = 0, skin: Optional[float] = None,
                  check_interval: Optional[int] = None, tick_block: Optional[int] = None,
                  cell_scale: Optional[float] = None, autotune: bool = False, graphs: bool = True,
-                 full_walks: bool = False):
+                 full_walks: bool = False, split_tick: bool = False, pair_pass: bool = False):
         L = lib()
         self._prefix = None
         opts = _opts(1, 0, _abi.PRECISION_MIXED, device, None, skin, check_interval, tick_block, cell_scale,
-                     autotune, graphs, full_walks=full_walks)
+                     autotune, graphs, split_tick=split_tick, full_walks=full_walks, pair_pass=pair_pass)
         descs, keeps = [], []
         for sc in scene_list:
             if isinstance(sc, (str, bytes, os.PathLike)):

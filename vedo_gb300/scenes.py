@@ -12,9 +12,8 @@ code, the C oracle and the GPU engine.
   ks = 0.8 kn, restitution 0.8, friction 0.5; dt = 1e-6 s.
 * :func:`hertz_drum` - polydisperse Hertz spheres (lognormal radii binned into K
   classes, one DOModel per class) in a horizontal drum of R = 0.15 m, L = 0.3 m
-  whose shell is a static polygon of fixed plates and whose two end plates are
-  orbital plates turning at 30 rpm; 35 % fill by seeded random sequential
-  placement.
+  whose shell (one hollow cylinder, or a polygon of fixed plates) and two end plates
+  turn at 30 rpm; filled by seeded random sequential placement.
 * :func:`hopper` / :func:`hopper_batch` - flat-bottomed hoppers discharging through a
   rectangular orifice (a box of fixed plates whose floor is four plates around the
   orifice), monodisperse r = 1 mm Hertz spheres with friction (``ISwH``); the batch

@@ -25,11 +25,14 @@ STATUS = {0: "queued", 1: "running", 2: "done", 3: "cancelled", 4: "failed"}
 BYTES_PER_OBJECT = 800
 ENTRIES_PER_SPHERE = 18
 BYTES_PER_ENTRY = 150
+BYTES_PER_ENTRY_PAIR_PASS = 72
 
 
-def job_charge(num_objects: int, num_spheres: int) -> int:
-    """Device memory the server's admission counts for a job."""
-    return BYTES_PER_OBJECT * num_objects + ENTRIES_PER_SPHERE * BYTES_PER_ENTRY * num_spheres
+def job_charge(num_objects: int, num_spheres: int, pair_pass: bool = False) -> int:
+    """Device memory the server's admission counts for a job (`pair_pass`: the server's options
+    ask for the pair pass or for autotuning)."""
+    per_entry = BYTES_PER_ENTRY + (BYTES_PER_ENTRY_PAIR_PASS if pair_pass else 0)
+    return BYTES_PER_OBJECT * num_objects + ENTRIES_PER_SPHERE * per_entry * num_spheres
 
 
 class JobInfo(C.Structure):
@@ -69,7 +72,8 @@ class Server:
         L = _srv_lib()
         opts = _opts(1, 0, _abi.PRECISION_MIXED, device, None, engine_opts.get("skin"),
                      engine_opts.get("check_interval"), engine_opts.get("tick_block"), engine_opts.get("cell_scale"),
-                     engine_opts.get("autotune", False), engine_opts.get("graphs", True))
+                     engine_opts.get("autotune", False), engine_opts.get("graphs", True),
+                     split_tick=engine_opts.get("split_tick", False), pair_pass=engine_opts.get("pair_pass", False))
         h = C.c_void_p()
         rc = L.vedo_srv_create(C.byref(opts), int(hbm_budget_bytes), C.byref(h))
         if rc != 0:
