@@ -460,7 +460,7 @@ def ours(args, dist):
            "config": {"workload": WORKLOAD, "particles_per_gpu": n, "objects_per_gpu": eng.n,
                       "settle": settle_info,
                       "form": "mixed (FP32 pair-local forces, FP64 overlap numerator and integration, "
-                              "Kahan sums; sphere orientation not integrated)",
+                              "Kahan sums; sphere orientations not asked for, so not integrated)",
                       "up_iact_fp64": args.up_iact, "active_contacts": n_active, "z_pp": z_pp,
                       "alg_bytes_per_particle_step": b_alg,
                       "l2": "working set larger than L2 (state + lists > 129 MB)",

@@ -186,6 +186,12 @@ typedef struct vedo_engine_opts {
                                  ("leap", LeapConsultant.cpp:108-195, LeapConsultant.h:58-446:
                                  cells ordered along the widest axis, periodic neighbours);
                                  the MIXED form's lists are complete by construction     */
+    uint32_t orientations;    /* MIXED only: 1 = integrate the spheres' orientations (Ox, Oz
+                                 turned by dt (w + dw/2) each step in FP64, as
+                                 DOSphere::Response, DOSphere.cpp:40-44); 0 = leave them as
+                                 they are (default: no force or contact depends on a sphere's
+                                 orientation, and the turn costs FP64 sines and cosines per
+                                 spinning sphere per step).  The FP64 form always turns them */
 } vedo_engine_opts;
 
 typedef struct vedo_gpu_engine vedo_gpu_engine;

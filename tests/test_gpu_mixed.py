@@ -180,6 +180,37 @@ def test_split_tick_and_pair_pass_are_exclusive(engine_lib):
         engine_lib.GpuEngine(scenes.dense_pack(n=2000), precision=1, split_tick=True, pair_pass=True)
 
 
+def test_mixed_orientations_follow_the_fp64_form(box_ido, engine_lib):
+    """With `orientations` the mixed form turns every sphere's Ox, Oz by dt (w + dw/2) per step
+    as DOSphere::Response does: on the settled box (spheres rolling and spinning) they stay
+    within 1e-6 of the FP64 form's after 300 steps (the angular velocities themselves differ at
+    the mixed form's force error), stay unit and orthogonal, and are the same in every form of
+    the tick; without the option they are left as they were."""
+    f64 = engine_lib.GpuEngine(box_ido, up_iact=1)
+    mixed = [engine_lib.GpuEngine(box_ido, precision=1, orientations=True, **kw)
+             for kw in ({}, {"split_tick": True}, {"pair_pass": True})]
+    still = engine_lib.GpuEngine(box_ido, precision=1)
+    o0 = still.state(("orientation_x", "orientation_z"))
+    for e in [f64, still] + mixed:
+        e.run(300)
+    ref = f64.state(("orientation_x", "orientation_z", "angular_velocity"))
+    assert np.abs(ref["angular_velocity"]).max() > 1.0          # the spheres do spin
+    moved = np.abs(ref["orientation_x"] - o0["orientation_x"]).max()
+    assert moved > 1e-3
+    first = mixed[0].state(("orientation_x", "orientation_z"))
+    for e in mixed[1:]:
+        st = e.state(("orientation_x", "orientation_z"))
+        for k in st:
+            assert np.array_equal(st[k], first[k]), k
+    for k in ("orientation_x", "orientation_z"):
+        np.testing.assert_allclose(first[k], ref[k], rtol=0, atol=1e-6, err_msg=k)
+        assert np.allclose(np.linalg.norm(first[k], axis=1), 1.0, atol=1e-12)
+    assert np.abs(np.sum(first["orientation_x"] * first["orientation_z"], axis=1)).max() < 1e-12
+    left = still.state(("orientation_x", "orientation_z"))
+    for k in left:
+        assert np.array_equal(left[k], o0[k]), k
+
+
 def _active_history(e):
     it = e.interactions()
     a = np.nonzero(it["active"] == 1)[0]
@@ -222,7 +253,7 @@ def test_orbital_wall_closing_in_independent_of_skin(engine_lib):
     skin and tested with their own displacement bound.  A tiny skin (rebuilds every few steps), a
     wide one, and full walks give bit-identical results, the plate does reach the bed, and its
     impulse agrees with the FP64 engine's."""
-    sc = scenes.compressed_bed(n=20000, box=0.03, cylinders=1, plate_speed=0.5)
+    sc = scenes.compressed_bed(n=20000, box=0.03, cylinders=1, plate_speed=0.5, packing="fcc")
     plate = sc.position.shape[0] - 1
     wide = engine_lib.GpuEngine(sc, precision=1, skin=0.5)
     tiny = engine_lib.GpuEngine(sc, precision=1, skin=0.002, check_interval=1)

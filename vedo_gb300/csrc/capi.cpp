@@ -67,6 +67,7 @@ void vedo_gpu_default_opts(vedo_engine_opts* o) {
     o->stored_splits = 0;
     o->split_tick = 0;
     o->full_walks = 0;
+    o->orientations = 0;
 }
 
 int vedo_gpu_create(const vedo_scene_desc* scene, const vedo_engine_opts* opts, vedo_gpu_engine** out) {

@@ -487,10 +487,15 @@ struct TickArgs {
     int xs_stored;                 // 1: splits stored once per step; 0: formed per pair
     uint32_t* work;                // split tick: spheres deferred to the full tick (else nullptr)
     uint32_t* nwork;               // split tick: spheres in `work`; pair pass: pairs in `pwork`
-    uint2* pwork;                  // pair pass: (owner entry, its sphere) of every pair on the exact path
+    uint4* pwork;                  // pair pass: (owner entry, its sphere, entry word, meta word) of every
+                                   // pair on the exact path
     uint8_t* xf;                   // pair pass: [ne] 1 = the entry is on the exact path this step
-    float4* prec;                  // pair pass: [ne][3] at the owner entry: (J, kind), torque on the
-                                   // slave, torque on the master
+                                   // (entries after a sphere's first 64)
+    unsigned long long* xm;        // pair pass: [n] the same for a sphere's first 64 entries, as a mask
+    float4* prec;                  // pair pass: [ne][2] per entry, the pair's share of the entry's
+                                   // sphere: (impulse, kind), (torque, 0)
+    const uint32_t* pmir;          // pair pass: [ne] at an owner entry of a sphere pair, the
+                                   // partner's entry of the same pair
     uint8_t* wk;                   // pair pass: [n] 1 = the sphere is quiet this step
     uint32_t pcap;                 // pair pass: entries `pwork`, `xf` and `prec` hold
     const float4* mf;              // [nm][2]: field + external impulse per step, 1/m~; 2.5/(m~ r^2)
@@ -500,6 +505,9 @@ struct TickArgs {
                                    // sphere-pair pads <= x and fixed-wall pads <= y
     uint8_t* qcnt;                 // [n] consecutive clean walks (0..2) since the last rebuild
     const uint32_t* ext_of;        // [n] the caller's index of each object (storage order)
+    double4_32a* sox;              // the orientation arrays (ox, oz), written for spheres when
+    double4_32a* soz;              // `orient` is set (no kernel of the step reads a sphere's)
+    int orient;
 };
 
 // A step whose list may be incomplete is an identity step.  A sphere pair may have closed by
@@ -641,6 +649,18 @@ __device__ __forceinline__ void note_walk(const TickArgs& a, uint32_t i, uint32_
     if (q2 != qc) a.qcnt[i] = (uint8_t)q2;
 }
 
+// DOSphere::Response (DOSphere.cpp:40-44): the orientation turns by dw = dt (w + dav/2) with
+// the angular velocity w before the step and its increment dav (FP32, converted exactly), by
+// Vector3d::rotate_around in FP64 for both axes; a zero turn leaves them.  Out of line: it runs
+// only when the caller asks for orientations.
+__device__ __noinline__ void turn_sphere(const TickArgs& a, uint32_t i, double dt, f3 dav) {
+    const d3 W = ld(a.w64, i);
+    const d3 dwv = smul(dt, add(W, smul(0.5, mk(f2d(dav.x), f2d(dav.y), f2d(dav.z)))));
+    if (dwv.x == 0.0 && dwv.y == 0.0 && dwv.z == 0.0) return;
+    st(a.sox, i, rotate_around(ld(a.sox, i), dwv), 0.0);
+    st(a.soz, i, rotate_around(ld(a.soz, i), dwv), 0.0);
+}
+
 // The end of a sphere's step: field and external impulse join the compensated sum (the
 // increments dv, dw are FP32, the state update FP64), the impulses are recorded on the last
 // step of a call, and the sphere is integrated.  Returns the squared speed bounds of the step
@@ -688,6 +708,7 @@ __device__ __forceinline__ float2 finish_sphere(const TickArgs& a, uint32_t i, b
             a.xsB[2 * i] = h2;
             a.xsB[2 * i + 1] = l2;
         }
+        if (a.orient) turn_sphere(a, i, dt, dw);     // (with the angular velocity before the step)
         if (dw.x != 0.0f || dw.y != 0.0f || dw.z != 0.0f) {
             const d3 W2 = add(ld(a.w64, i), mk(f2d(dw.x), f2d(dw.y), f2d(dw.z)));
             st(a.w64, i, W2, 0.0);
@@ -723,9 +744,9 @@ __device__ __forceinline__ float2 finish_sphere(const TickArgs& a, uint32_t i, b
 // into the other buffer, a wall entry writes the wall's share of the impulse.  Returns 0 (nothing
 // added), 1 (impulse J only) or 2 (J and the torques tA on the slave, tB on the master).
 template <int LAW, bool XS>
-__device__ __forceinline__ int exact_pair(const TickArgs& a, uint32_t i, const d3& Pi, uint32_t e, uint32_t meta,
+__device__ __forceinline__ int exact_pair(const TickArgs& a, uint32_t i, const d3& Pi, uint32_t e, uint32_t ent,
+                                          uint32_t meta,
                                           float dtf, f3& Jp, f3& tA, f3& tB) {
-    const uint32_t ent = a.nent[e];
     const uint32_t j = ent & ~WALL_BIT;
     const bool wall = ent & WALL_BIT;
     // canonical orientation (Assembler.cpp:43-67), fixed at rebuild; sphere-wall: the sphere is the slave
@@ -850,7 +871,7 @@ __device__ __forceinline__ float2 tick_sphere(const TickArgs& a, uint32_t i) {
                     const uint32_t e = c0 + k;
                     const uint32_t meta = a.nmeta[e];
                     f3 Jp, tA, tB;
-                    const int app = exact_pair<LAW, XS>(a, i, Pi, e, meta, dtf, Jp, tA, tB);
+                    const int app = exact_pair<LAW, XS>(a, i, Pi, e, a.nent[e], meta, dtf, Jp, tA, tB);
                     if (app) {
                         if (meta & META_SLAVE) {
                             J.add(Jp);
@@ -994,8 +1015,9 @@ __global__ void __launch_bounds__(TPB, 6) k_tick_light(TickArgs a) {   // 6 bloc
 //                cleaning and clean-walk count), marking the entries on the exact path and
 //                appending each such pair once, at its history owner, to a worklist;
 //  k_tick_pairs  one thread per pair of the worklist: the exact path (exact_pair, the single
-//                tick's arithmetic) writes the pair's impulse and torques at its owner entry;
-//  k_tick_sum    one thread per sphere: the records of its marked entries in entry order join
+//                tick's arithmetic) writes each member's share of the impulse and torque at that
+//                member's own entry of the pair;
+//  k_tick_sum    one thread per sphere: the shares at its marked entries, in entry order, join
 //                the compensated sums, then the sphere is integrated (finish_sphere).
 // Both members of a pair add the one evaluation that the single tick computes twice with
 // identical bits, in the same order, so results are the single tick's.  The pair kernel runs
@@ -1006,7 +1028,7 @@ __global__ void __launch_bounds__(TPB, 4) k_tick_pf(TickArgs a) {     // 63 regi
     if (held_step(a)) return;                      // k_tick_sum holds the state (uniform branch)
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     const int lane = threadIdx.x & 31;
-    uint32_t c0 = 0u, e1 = 0u, qc = 0u;
+    uint32_t c0 = 0u, e0 = 0u, e1 = 0u, qc = 0u;
     float4 p32i = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
     float pad = 0.0f;
     bool walk = false, dirty = false, any_exact = false;
@@ -1020,10 +1042,12 @@ __global__ void __launch_bounds__(TPB, 4) k_tick_pf(TickArgs a) {     // 63 regi
             const bool quiet = qc >= 2u && !a.write_imp && pad <= cl.x && a.disp[1] <= cl.y;
             a.wk[i] = quiet ? 1u : 0u;
             if (!quiet) {
-                c0 = a.nptr[i];
+                e0 = a.nptr[i];
                 e1 = a.nptr[i + 1];
+                c0 = e0;
                 p32i = a.pos32[i];
                 walk = true;
+                if (e0 == e1) a.xm[i] = 0ull;      // an empty list: no chunk writes the mask
             }
         }
     }
@@ -1041,7 +1065,11 @@ __global__ void __launch_bounds__(TPB, 4) k_tick_pf(TickArgs a) {     // 63 regi
                 own |= (unsigned long long)owned << (base - c0);
             }
             any_exact |= exact != 0ull;
-            for (uint32_t e = c0; e < c1; ++e) a.xf[e] = (uint8_t)((exact >> (e - c0)) & 1ull);
+            if (c0 == e0) {
+                a.xm[i] = exact;
+            } else {
+                for (uint32_t e = c0; e < c1; ++e) a.xf[e] = (uint8_t)((exact >> (e - c0)) & 1ull);
+            }
         }
         const uint32_t cnt = (uint32_t)__popcll(own);
         uint32_t incl = cnt;                       // inclusive prefix over the warp
@@ -1056,7 +1084,8 @@ __global__ void __launch_bounds__(TPB, 4) k_tick_pf(TickArgs a) {     // 63 regi
         while (own) {
             const int k = __ffsll(own) - 1;
             own &= own - 1;
-            if (at < a.pcap) a.pwork[at] = make_uint2(c0 + (uint32_t)k, i);   // (at most one per entry)
+            const uint32_t e = c0 + (uint32_t)k;   // (its words are in L1 from the prefilter)
+            if (at < a.pcap) a.pwork[at] = make_uint4(e, i, a.nent[e], a.nmeta[e]);   // (at most one per entry)
             ++at;
         }
         if (more) {
@@ -1068,22 +1097,28 @@ __global__ void __launch_bounds__(TPB, 4) k_tick_pf(TickArgs a) {     // 63 regi
 }
 
 template <int LAW, bool XS>
-__global__ void __launch_bounds__(TPB) k_tick_pairs(TickArgs a) {
+__global__ void __launch_bounds__(TPB, 4) k_tick_pairs(TickArgs a) {     // 64 registers (a few spill)
     step_order();
     if (held_step(a)) return;
     const uint32_t nw = min(*a.nwork, a.pcap);
     for (uint32_t q = blockIdx.x * blockDim.x + threadIdx.x; q < nw; q += gridDim.x * blockDim.x) {
-        const uint2 it = a.pwork[q];
-        const uint32_t e = it.x, i = it.y;
-        const uint32_t meta = a.nmeta[e];
+        const uint4 it = a.pwork[q];
+        const uint32_t e = it.x, i = it.y, ent = it.z, meta = it.w;
         const d3 Pi = XS ? mk(0.0, 0.0, 0.0) : ld(a.xA, i);
         f3 Jp, tA, tB;
-        const int app = exact_pair<LAW, XS>(a, i, Pi, e, meta, a.scenes[a.scene_of[i]].dtf, Jp, tA, tB);
-        float4* r = a.prec + 3 * (size_t)e;
-        r[0] = make_float4(Jp.x, Jp.y, Jp.z, __int_as_float(app));
-        if (app == 2) {
-            r[1] = make_float4(tA.x, tA.y, tA.z, 0.0f);
-            r[2] = make_float4(tB.x, tB.y, tB.z, 0.0f);
+        const int app = exact_pair<LAW, XS>(a, i, Pi, e, ent, meta, a.scenes[a.scene_of[i]].dtf, Jp, tA, tB);
+        // each member's share at its own entry: the slave adds J and tA, the master -J and tB
+        // (the negation is exact, so the sums see the single tick's values)
+        const bool i_slave = meta & META_SLAVE;
+        const float kind = __int_as_float(app);
+        const f3 Ji = i_slave ? Jp : -Jp, ti = i_slave ? tA : tB;
+        a.prec[2 * (size_t)e] = make_float4(Ji.x, Ji.y, Ji.z, kind);
+        if (app == 2) a.prec[2 * (size_t)e + 1] = make_float4(ti.x, ti.y, ti.z, 0.0f);
+        if (!(ent & WALL_BIT)) {                   // a sphere pair: the partner's share at its entry
+            const uint32_t q2 = a.pmir[e];
+            const f3 Jj = i_slave ? -Jp : Jp, tj = i_slave ? tB : tA;
+            a.prec[2 * (size_t)q2] = make_float4(Jj.x, Jj.y, Jj.z, kind);
+            if (app == 2) a.prec[2 * (size_t)q2 + 1] = make_float4(tj.x, tj.y, tj.z, 0.0f);
         }
     }
 }
@@ -1107,21 +1142,19 @@ __global__ void __launch_bounds__(TPB, 4) k_tick_sum(TickArgs a) {
             const bool quiet = a.wk[i] != 0u;
             const float4 mf0 = a.mf[2 * mi], mf1 = a.mf[2 * mi + 1];
             K3 J, JA;
-            for (uint32_t e = e0; e < e1 && !quiet; ++e) {
-                if (!a.xf[e]) continue;
-                const uint32_t meta = a.nmeta[e];
-                const uint32_t slot = (meta & META_OWNER) ? e : a.nslot[e];
-                const float4 r0 = a.prec[3 * (size_t)slot];
+            auto add_pair = [&](uint32_t e) {
+                const float4 r0 = a.prec[2 * (size_t)e];
                 const int app = __float_as_int(r0.w);
                 if (app) {
-                    if (meta & META_SLAVE) {
-                        J.add(f4to3(r0));
-                        if (app == 2) JA.add(f4to3(a.prec[3 * (size_t)slot + 1]));
-                    } else {
-                        J.add(-f4to3(r0));
-                        if (app == 2) JA.add(f4to3(a.prec[3 * (size_t)slot + 2]));
-                    }
+                    J.add(f4to3(r0));
+                    if (app == 2) JA.add(f4to3(a.prec[2 * (size_t)e + 1]));
                 }
+            };
+            if (!quiet) {
+                for (unsigned long long m = a.xm[i]; m; m &= m - 1)
+                    add_pair(e0 + (uint32_t)(__ffsll(m) - 1));
+                for (uint32_t e = e0 + 64; e < e1; ++e)         // long lists: entries after the first 64
+                    if (a.xf[e]) add_pair(e);
             }
             vmax_local = finish_sphere<XS>(a, i, M.behavior == BEH_MOBILE, quiet, S, Pi, V, mf0, mf1, J, JA);
         } else if (M.scope == SCOPE_LOCAL) {
@@ -1491,6 +1524,24 @@ __global__ void __launch_bounds__(TPB) k_slots(uint32_t n, const uint32_t* __res
             if (ent[q] == i) { found = q; break; }
         if (found == 0xffffffffu) atomicOr(err, 1);
         slot[e] = found == 0xffffffffu ? e : found;
+    }
+}
+
+// Pair pass: at each owner entry of a sphere pair, the partner's entry of the same pair (every
+// entry first names itself, then, in a second launch, each non-owner entry names itself at its
+// owner entry; an entry without partner keeps its own index).
+template <bool PARTNER>
+__global__ void __launch_bounds__(TPB) k_mirror(uint32_t n, const uint32_t* __restrict__ ptr,
+                                                const uint32_t* __restrict__ slot, uint32_t* __restrict__ mir) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    for (uint32_t e = ptr[i]; e < ptr[i + 1]; ++e) {
+        if (!PARTNER) {
+            mir[e] = e;
+        } else {
+            const uint32_t o = slot[e];
+            if (o != e) mir[o] = e;
+        }
     }
 }
 
@@ -2298,12 +2349,18 @@ private:
     uint32_t* d_work_ = nullptr;                  // [n] spheres deferred by the light tick
     bool pair_pass_ = false;                      // prefilter pass, pair pass, per-sphere sums (identical results)
     uint32_t pcap_ = 0;                           // entries the pair pass's buffers hold
-    uint2* d_pwork_ = nullptr;                    // [pcap] pairs on the exact path (owner entry, sphere)
+    uint4* d_pwork_ = nullptr;                    // [pcap] pairs on the exact path (owner entry, sphere)
     uint8_t* d_xf_ = nullptr;                     // [pcap] entry on the exact path this step
-    float4* d_prec_ = nullptr;                    // [pcap][3] pair records at the owner entry
+    float4* d_prec_ = nullptr;                    // [pcap][2] each entry's share of its pair
+    uint32_t* d_pmir_ = nullptr;                  // [pcap] partner entry of an owner entry
     uint8_t* d_wk_ = nullptr;                     // [n] quiet this step (pair pass)
+    unsigned long long* d_xm_ = nullptr;          // [n] exact-path mask of the first 64 entries (pair pass)
     int ensure_pair_bufs(uint32_t ne);
     void free_pair_bufs();
+    void fill_mirror(const NList& L) {
+        k_mirror<false><<<nblk(n_), TPB, 0, stream_>>>(n_, L.ptr, L.slot, d_pmir_);
+        k_mirror<true><<<nblk(n_), TPB, 0, stream_>>>(n_, L.ptr, L.slot, d_pmir_);
+    }
     // blocks of tpb_ threads of kernel k resident on the whole GPU at once (cached per kernel
     // and block size)
     const void* grid_k_ = nullptr;
@@ -2320,6 +2377,7 @@ private:
         return grid_blocks_;
     }
     bool quiet_ok_ = true;                        // quiet spheres skip their walk (identical results)
+    bool orient_ = false;                         // integrate the spheres' orientations
     int sms_ = 1;                                 // streaming multiprocessors of the device
     float2* d_clear_ = nullptr;                   // [n] quiet-sphere pad limits of the current list
     double* d_ext_ = nullptr;                     // [2][n][3] external impulses of run_with_impulses
@@ -2378,21 +2436,28 @@ void MixedEngine::free_nlist(NList& L) {
 // The pair pass's per-entry buffers, sized to the list (allocated only while the pair pass is
 // used or tried).
 int MixedEngine::ensure_pair_bufs(uint32_t ne) {
+    if (!d_wk_) MCK(mal(&d_wk_, n_));
+    if (!d_xm_) MCK(mal(&d_xm_, n_));
     if (ne <= pcap_ && d_prec_) return VEDO_OK;
-    free_pair_bufs();
+    for (void* p : {(void*)d_pwork_, (void*)d_xf_, (void*)d_prec_, (void*)d_pmir_})
+        if (p) cudaFree(p);
     const uint64_t c = std::max<uint64_t>(1024, (uint64_t)ne + ne / 4);
     pcap_ = (uint32_t)std::min<uint64_t>(c, 0x7fffffffull);
     MCK(mal(&d_pwork_, pcap_));
     MCK(mal(&d_xf_, pcap_));
-    MCK(mal(&d_prec_, 3 * (size_t)pcap_));
+    MCK(mal(&d_prec_, 2 * (size_t)pcap_));
+    MCK(mal(&d_pmir_, pcap_));
     return VEDO_OK;
 }
 void MixedEngine::free_pair_bufs() {
-    for (void* p : {(void*)d_pwork_, (void*)d_xf_, (void*)d_prec_})
+    for (void* p : {(void*)d_pwork_, (void*)d_xf_, (void*)d_prec_, (void*)d_pmir_, (void*)d_wk_, (void*)d_xm_})
         if (p) cudaFree(p);
     d_pwork_ = nullptr;
     d_xf_ = nullptr;
     d_prec_ = nullptr;
+    d_pmir_ = nullptr;
+    d_wk_ = nullptr;
+    d_xm_ = nullptr;
     pcap_ = 0;
 }
 
@@ -2421,7 +2486,7 @@ MixedEngine::~MixedEngine() {
     free_nlist(nl_[1]);
     void* ptrs[] = {d_models_, d_params_, d_pc32_, d_geom_, d_hole_, d_rr_, d_mf_, d_reach_, d_model_of_, d_scene_of_,
                     d_scenes_, d_gfield_, d_glob_, d_x_[0], d_x_[1], d_v64_, d_w64_, d_ox_, d_oz_, d_imp_, d_aimp_,
-                    d_v32_[0], d_v32_[1], d_w32_[0], d_w32_[1], d_rr32_, d_xs_[0], d_xs_[1], d_work_, d_wk_, d_clear_, d_vred_, d_ext_, d_qcnt_, d_pos32_, d_wall32_, d_red_, d_sred_, d_disp_, d_err_,
+                    d_v32_[0], d_v32_[1], d_w32_[0], d_w32_[1], d_rr32_, d_xs_[0], d_xs_[1], d_work_, d_clear_, d_vred_, d_ext_, d_qcnt_, d_pos32_, d_wall32_, d_red_, d_sred_, d_disp_, d_err_,
                     d_key_, d_key_alt_, d_sid_, d_sid_alt_, d_cnt_, d_gs_, d_ge_, d_act_, d_stage_, d_obs_, d_gidx_,
                     d_wkey_, d_wval_, d_wkey_alt_, d_wval_alt_, d_wptr_, d_wimp_, d_wred_, d_wrot_, d_wedge_, d_ext_of_, d_int_of_, d_xe_, d_model_e_};
     for (void* p : ptrs) if (p) cudaFree(p);
@@ -2462,6 +2527,7 @@ int MixedEngine::init_from(const std::vector<SceneSource>& src, const MixedEngin
     pair_pass_ = opts.split_tick == 2;
     if (opts.split_tick > 2) return fail(VEDO_ERR_INVALID_ARGUMENT, "split_tick must be 0, 1 or 2");
     quiet_ok_ = opts.full_walks == 0;
+    orient_ = opts.orientations != 0;
     if (prev) {                    // a repacked engine keeps the tuning of the one it replaces
         skin_frac_ = prev->skin_frac_;
         cell_scale_ = prev->cell_scale_;
@@ -2647,7 +2713,7 @@ int MixedEngine::init_from(const std::vector<SceneSource>& src, const MixedEngin
     MCK(mal(&d_sred_, 8 * sc_.size()));
     MCK(mal(&d_vred_, 6 * sc_.size()));
     MCK(mal(&d_work_, n_));
-    MCK(mal(&d_wk_, n_));
+
     MCK(mal(&d_clear_, n_));
     MCK(mal(&d_qcnt_, n_));
     MCK(cudaMemset(d_qcnt_, 0, n_));
@@ -2833,13 +2899,18 @@ TickArgs MixedEngine::args(bool write_imp) {
     a.pwork = d_pwork_;
     a.xf = d_xf_;
     a.prec = d_prec_;
+    a.pmir = d_pmir_;
     a.wk = d_wk_;
+    a.xm = d_xm_;
     a.pcap = pcap_;
     a.mf = d_mf_;
     a.clear = d_clear_;
     a.qcnt = d_qcnt_;
     a.ext = ext_on_ ? d_ext_ : nullptr;
     a.ext_of = d_ext_of_;
+    a.sox = d_ox_;
+    a.soz = d_oz_;
+    a.orient = orient_ ? 1 : 0;
     return a;
 }
 
@@ -2971,6 +3042,10 @@ int MixedEngine::rebuild() {
     }
     MCK(cudaMemsetAsync(d_err_, 0, 4, stream_));
     k_slots<<<nblk(n_), TPB, 0, stream_>>>(n_, L.ptr, L.ent, L.slot, d_err_);
+    if (pair_pass_) {
+        fill_mirror(L);
+        own += 2;
+    }
     k_meta<<<nblk(n_), TPB, 0, stream_>>>(n_, L.ptr, L.ent, L.slot, d_model_of_, d_models_, d_scene_of_, d_scenes_,
                                           d_params_, d_ext_of_, L.meta);
     ++own;
@@ -3263,17 +3338,20 @@ int MixedEngine::autotune(uint32_t max_steps, uint32_t* taken) {
     };
     auto timed_chunk = [&](float* ms_per_step, float* growth) -> int {
         const uint64_t r0 = round_;
-        float use = 0.0f;
+        float use = 0.0f, use0 = 0.0f;
         // an untimed chunk first: it captures the graph of this configuration (after a rebuild,
-        // another, so that the clean-walk counts have settled when the timing starts)
-        int wrc = step_chunk(ci, false, nullptr);
+        // another, so that the clean-walk counts have settled when the timing starts).  A list
+        // past half its life is rebuilt first: a list that runs out inside the timed chunk makes
+        // its remaining steps identity steps, which would time the configuration far too fast.
+        int wrc = step_chunk(ci, false, &use0);
         if (wrc > 0) return wrc;
-        if (need_rebuild_) {
+        if (need_rebuild_ || use0 > 0.5f) {
             if ((wrc = rebuild()) != VEDO_OK) return wrc;
             wrc = step_chunk(ci, false, nullptr);
             if (wrc > 0) return wrc;
             if (need_rebuild_ && (wrc = rebuild()) != VEDO_OK) return wrc;
         }
+        const uint64_t rt = round_;
         MCK(cudaEventRecord(e0, stream_));
         int rc = step_chunk(ci, false, &use);
         if (rc > 0) return rc;
@@ -3281,7 +3359,9 @@ int MixedEngine::autotune(uint32_t max_steps, uint32_t* taken) {
         MCK(cudaEventSynchronize(e1));
         float ms = 0.0f;
         MCK(cudaEventElapsedTime(&ms, e0, e1));
-        *ms_per_step = ms / (float)ci;
+        // per step taken (should the list still have run out, its identity steps do not count
+        // as steps: an overestimate, never an underestimate)
+        *ms_per_step = ms / (float)std::max<uint64_t>(1, round_ - rt);
         if (growth) *growth = since_rebuild_ ? use / (float)since_rebuild_ : 0.0f;
         *taken += (uint32_t)(round_ - r0);
         return VEDO_OK;
@@ -3332,6 +3412,7 @@ int MixedEngine::autotune(uint32_t max_steps, uint32_t* taken) {
         pair_pass_ = true;
         drop_graphs();
         if ((rc = ensure_pair_bufs(nl_[nlc_].ne)) != VEDO_OK) return rc;
+        fill_mirror(nl_[nlc_]);
         if ((rc = timed_chunk(&t_pair, nullptr)) != VEDO_OK) return rc;
         if (need_rebuild_ && (rc = rebuild()) != VEDO_OK) return rc;
         pair_pass_ = t_pair < t_one && t_pair < t_split;
@@ -3373,7 +3454,12 @@ int MixedEngine::autotune(uint32_t max_steps, uint32_t* taken) {
             MCK(cudaEventElapsedTime(&ms, e0, e1));
             t = ms / (float)ci;
             growth = since_rebuild_ ? use / (float)since_rebuild_ : 0.0f;
+            const bool short_list = round_ - r0 < ci;   // identity steps: the list did not last
             *taken += (uint32_t)(round_ - r0);
+            if (short_list) {
+                if ((rc = rebuild()) != VEDO_OK) return rc;
+                continue;
+            }
         }
         trb = std::max(0.0f, trb - t * (float)ci);
         // steps until the list's life is used up at this growth (the rebuild rule's margin)

@@ -86,7 +86,7 @@ STATE_FIELDS = ("position", "velocity", "angular_velocity", "orientation_x", "or
 
 def _opts(up_iact, record, precision, device, prefix, skin, check_interval, tick_block=None, cell_scale=None,
           autotune=False, graphs=True, stored_splits=False, split_tick=False, full_walks=False,
-          consultant="nbs", pair_pass=False) -> EngineOpts:
+          consultant="nbs", pair_pass=False, orientations=False) -> EngineOpts:
     opts = EngineOpts()
     lib().vedo_gpu_default_opts(C.byref(opts))
     opts.up_iact, opts.record, opts.precision, opts.device = up_iact, record, precision, device
@@ -105,6 +105,7 @@ def _opts(up_iact, record, precision, device, prefix, skin, check_interval, tick
         raise ValueError("split_tick and pair_pass are two forms of the tick: choose one")
     opts.split_tick = 2 if pair_pass else (1 if split_tick else 0)
     opts.full_walks = 1 if full_walks else 0
+    opts.orientations = 1 if orientations else 0
     if consultant not in ("nbs", "leap"):
         raise ValueError(f"consultant must be 'nbs' or 'leap', not {consultant!r}")
     opts.consultant = 1 if consultant == "leap" else 0
@@ -126,11 +127,11 @@ class GpuEngine:
                  check_interval: Optional[int] = None, tick_block: Optional[int] = None,
                  cell_scale: Optional[float] = None, autotune: bool = False, graphs: bool = True,
                  stored_splits: bool = False, split_tick: bool = False, full_walks: bool = False,
-                 consultant: str = "nbs", pair_pass: bool = False):
+                 consultant: str = "nbs", pair_pass: bool = False, orientations: bool = False):
         L = lib()
         self._prefix = output_prefix.encode() if output_prefix else None
         opts = _opts(up_iact, record, precision, device, self._prefix, skin, check_interval, tick_block, cell_scale,
-                     autotune, graphs, stored_splits, split_tick, full_walks, consultant, pair_pass)
+                     autotune, graphs, stored_splits, split_tick, full_walks, consultant, pair_pass, orientations)
         h = C.c_void_p()
         if isinstance(scene, (str, bytes, os.PathLike)):
             path = os.fsencode(scene)
@@ -323,11 +324,13 @@ class BatchEngine(GpuEngine):
     def __init__(self, scene_list, device: int = 0, skin: Optional[float] = None,
                  check_interval: Optional[int] = None, tick_block: Optional[int] = None,
                  cell_scale: Optional[float] = None, autotune: bool = False, graphs: bool = True,
-                 full_walks: bool = False, split_tick: bool = False, pair_pass: bool = False):
+                 full_walks: bool = False, split_tick: bool = False, pair_pass: bool = False,
+                 orientations: bool = False):
         L = lib()
         self._prefix = None
         opts = _opts(1, 0, _abi.PRECISION_MIXED, device, None, skin, check_interval, tick_block, cell_scale,
-                     autotune, graphs, split_tick=split_tick, full_walks=full_walks, pair_pass=pair_pass)
+                     autotune, graphs, split_tick=split_tick, full_walks=full_walks, pair_pass=pair_pass,
+                     orientations=orientations)
         descs, keeps = [], []
         for sc in scene_list:
             if isinstance(sc, (str, bytes, os.PathLike)):

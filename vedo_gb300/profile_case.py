@@ -1,7 +1,7 @@
 """Run one workload of the engine, for a profiler or a quick timing.
 
     python -m vedo_gb300.profile_case <drum|settled|dense|bed|hopper> <spheres> <steps> [--fp64] [--block B]
-                                      [--stored] [--split] [--skin S]
+                                      [--stored] [--split | --pair] [--skin S]
 
 Builds the seeded scene (`settled`: the polydisperse drum after 300,000 steps of settling, made
 once per host by vedo_gb300.workloads.settled_drum and cached there), creates the engine (mixed form unless --fp64; fixed settings, no
@@ -43,14 +43,15 @@ def main(argv=None):
     ap.add_argument("--block", type=int, default=64)
     ap.add_argument("--stored", action="store_true", help="store the hi/lo position splits once per step")
     ap.add_argument("--split", action="store_true", help="light tick + full tick over the deferred spheres")
-    ap.add_argument("--skin", type=float, default=None, help="candidate-list skin (fraction of the cell)")
+    ap.add_argument("--pair", action="store_true", help="pair pass: prefilter pass, one evaluation per pair, sums")
+    ap.add_argument("--skin", type=float, default=None, help="candidate-list skin (fraction of r_max)")
     a = ap.parse_args(argv)
     sc = make(a.kind, a.n)
     if a.fp64:
         e = GpuEngine(sc, up_iact=20)
     else:
         e = GpuEngine(sc, precision=1, tick_block=a.block, graphs=False, stored_splits=a.stored, split_tick=a.split,
-                      skin=a.skin)
+                      pair_pass=a.pair, skin=a.skin)
     e.run(5)
     e.run(a.steps)
     p = e.last_run_profile()
