@@ -437,10 +437,17 @@ def ours(args, dist):
         ach = b_alg * n / (t_tick * 1e-3) / 1e9
         traffic = ncu_traffic("k_tick_drum1M_settled_dram.md") if n == 1_000_000 else None
         tuned = eng.tuning()
-        roof = {"kernel": ("k_tick_light + k_tick_work (split tick: prefilter walk and integration at high "
-                           "occupancy, the per-sphere contact tick over the spheres with a pair on the exact path)")
-                if tuned.get("split_tick") else "k_tick (per-sphere contact tick over the Z-order storage: narrow "
-                                                "phase + forces + integration, one launch per step)",
+        if tuned.get("pair_pass"):
+            kname = ("k_tick_pf + k_tick_pairs + k_tick_sum (pair pass: prefilter walk listing the pairs on the "
+                     "exact path, one thread per pair for narrow phase + forces, per-sphere ordered sums + "
+                     "integration)")
+        elif tuned.get("split_tick"):
+            kname = ("k_tick_light + k_tick_work (split tick: prefilter walk and integration at high occupancy, the "
+                     "per-sphere contact tick over the spheres with a pair on the exact path)")
+        else:
+            kname = ("k_tick (per-sphere contact tick over the Z-order storage: narrow phase + forces + "
+                     "integration, one launch per step)")
+        roof = {"kernel": kname,
                 "bound": "hbm", "achieved": ach, "peak": peak, "unit": "GB/s", "frac": ach / peak,
                 "peak_source": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)" if peak_kind == "measured" else peak_kind,
                 "traffic": traffic,

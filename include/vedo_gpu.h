@@ -243,6 +243,10 @@ typedef struct vedo_state_view {
     double* angular_impact;
 } vedo_state_view;
 
+/* Objects now (DOWorld's object count).  With the Leap consultant and an active zone of interest
+ * the mobile objects that leave the zone are erased at the next reset (LeapConsultant.cpp:61-68,
+ * Consultant::CleanUp), so the count, and the length of every state array, can shrink during a
+ * vedo_gpu_run call: read it after each call. */
 uint32_t vedo_gpu_num_objects(const vedo_gpu_engine* e);
 int vedo_gpu_get_state(vedo_gpu_engine* e, const vedo_state_view* out);
 /* Overwrite the object state (DOContainer::SetDOStatus, DOContainer.h:55-58). */

@@ -106,6 +106,8 @@ struct dp_world {
     double sf;
     unsigned up_iact;
     int leap;                          /* 1: LeapConsultant's candidate list, 0: NBSConsultant's */
+    double zoi_lo[3], zoi_hi[3];       /* the zone of interest after Boundary::Correct */
+    int zoi_sw[3], zoi_on;
     unsigned long long round;
     /* periodic boundary after Boundary::Correct: switched axes, bounds, ranges */
     int pbc_on, pbc_sw[3];
@@ -1062,16 +1064,11 @@ static void sort_records(record_t* r, unsigned* n) {
    up to and including each object (unsigned); IactRecordTab::ModifyPair (IactRecordTab.cpp:41-69)
    moves every record whose key changes to its new key, in key order, overwriting what is there;
    the survivors keep their order. */
-static int zoi_cleanup(dp_world* w, const vedo_scene_desc* sc) {
-    double lo[3], hi[3];
-    int sw[3], active = 0;
-    for (int k = 0; k < 3; ++k) {
-        lo[k] = sc->zoi_lower[k] < sc->zoi_upper[k] ? sc->zoi_lower[k] : sc->zoi_upper[k];
-        hi[k] = sc->zoi_lower[k] < sc->zoi_upper[k] ? sc->zoi_upper[k] : sc->zoi_lower[k];
-        sw[k] = lo[k] != hi[k];
-        active |= sw[k];
-    }
-    if (!active) return 0;
+static int zoi_cleanup(dp_world* w) {
+    const double* lo = w->zoi_lo;
+    const double* hi = w->zoi_hi;
+    const int* sw = w->zoi_sw;
+    if (!w->zoi_on) return 0;
     const unsigned n = w->n;
     unsigned* jump = (unsigned*)malloc(sizeof(unsigned) * (n ? n : 1));
     char* gone = (char*)calloc(n ? n : 1, 1);
@@ -1166,13 +1163,15 @@ static int rebuild_records(dp_world* w) {
 /* ------------------------------------------------------------------------ */
 dp_world* dp_create(const vedo_scene_desc* sc, unsigned up_iact, int consultant, char* err, size_t errlen) {
     if (!sc || !sc->num_objects) { set_err(err, errlen, "empty scene"); return NULL; }
-    if (consultant == 1 && (sc->zoi_lower[0] != sc->zoi_upper[0] || sc->zoi_lower[1] != sc->zoi_upper[1] ||
-                            sc->zoi_lower[2] != sc->zoi_upper[2])) {
-        /* LeapConsultant::NextStep erases objects outside the zone at every reset (:67) */
-        set_err(err, errlen, "a zone of interest with the Leap consultant is not supported"); return NULL;
-    }
     dp_world* w = (dp_world*)calloc(1, sizeof(dp_world));
     w->leap = consultant == 1;
+    for (int k = 0; k < 3; ++k) {                  /* Boundary::Correct for the zone of interest */
+        const double a = sc->zoi_lower[k], b = sc->zoi_upper[k];
+        w->zoi_lo[k] = a < b ? a : b;
+        w->zoi_hi[k] = a < b ? b : a;
+        w->zoi_sw[k] = a != b;
+        w->zoi_on |= w->zoi_sw[k];
+    }
     /* Boundary::Correct (Boundary.cpp:79-128): an axis is on where its bounds differ */
     for (int k = 0; k < 3; ++k) {
         const double a = sc->pbc_lower[k], b = sc->pbc_upper[k];
@@ -1270,7 +1269,7 @@ dp_world* dp_create(const vedo_scene_desc* sc, unsigned up_iact, int consultant,
         if (sc->record_shear) R->st.shear = ld3(sc->record_shear + 3 * r);
     }
     sort_records(w->rec, &w->nrec);
-    zoi_cleanup(w, sc);
+    zoi_cleanup(w);                                /* SimMediator's constructor (SimMediator.cpp:125-134) */
     int rc = consultant_reset(w);
     if (rc == 0) rc = initiate(w);
     if (rc != 0) {
@@ -1303,7 +1302,11 @@ int dp_run(dp_world* w, unsigned nsteps) {
         int reset = (w->round % w->up_iact) == 0;
         if (reset) {
             rebuild_records(w);
-            consultant_reset(w);
+            /* LeapConsultant::NextStep (LeapConsultant.cpp:61-68): SyncWorld, RebuildIactRecordTab,
+               CleanUp, Reset -- the Leap consultant erases the mobile objects outside the zone of
+               interest at every reset (NBSConsultant::NextStep does not) */
+            if (w->leap) zoi_cleanup(w);
+            if (consultant_reset(w) != 0) return -1;
         }
         for (unsigned k = 0; k < w->ncand && !reset; ++k) {                   /* BackupImpactStatus */
             w->it[k].st.last_contact = w->it[k].st.contact;

@@ -53,7 +53,10 @@ def _d(a):
 
 
 class _World:
-    n: int
+    @property
+    def n(self) -> int:
+        """Objects now (the Leap consultant's zone-of-interest clean-up erases some at resets)."""
+        return self._num_objects()
 
     def state(self) -> Dict[str, np.ndarray]:
         out = {k: np.zeros((self.n, 3)) for k in ("position", "velocity", "angular_velocity", "orientation_x",
@@ -100,7 +103,9 @@ class PortWorld(_World):
         self.h = L.dp_create(C.byref(desc), up_iact, 1 if consultant == "leap" else 0, err, 256)
         if not self.h:
             raise ValueError("oracle rejected the scene: " + err.value.decode())
-        self.n = L.dp_num_objects(self.h)
+
+    def _num_objects(self) -> int:
+        return self.lib().dp_num_objects(self.h)
 
     def run(self, nsteps: int) -> int:
         return self.lib().dp_run(self.h, nsteps)
@@ -220,7 +225,9 @@ class RefWorld(_World):
             os.chdir(cwd)
         if not self.h:
             raise ValueError("reference could not read the scene")
-        self.n = L.vref_num_do(self.h)
+
+    def _num_objects(self) -> int:
+        return self.lib().vref_num_do(self.h)
 
     def run(self, nsteps: int) -> int:
         cwd = os.getcwd()

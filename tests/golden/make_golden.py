@@ -25,7 +25,7 @@ from vedo_gb300 import scenes  # noqa: E402
 
 
 LEAP = {"leap_cluster_poly", "leap_box_lsd", "leap_periodic_lsd", "leap_periodic_wide", "leap_wide_y",
-        "leap_column_z", "leap_single"}
+        "leap_column_z", "leap_single", "leap_zoi", "leap_zoi_h"}
 
 
 def cases():
@@ -37,6 +37,10 @@ def cases():
                                                      cylinders=3, steps=300, seed=9), 200, 3
     yield "cluster_bsdbf_upiact1", scenes.cluster(n=27, solver="ISwBSDBF", steps=200, seed=2), 150, 1
     yield "cluster_zoi", zoi_scene(), 200, 5
+    # the Leap consultant erases the mobile objects that leave the zone at every reset
+    # (LeapConsultant.cpp:61-68), re-keying the contact records (IactRecordTab::ModifyPair)
+    yield "leap_zoi", leap_zoi_scene(), 1500, 5
+    yield "leap_zoi_h", leap_zoi_scene(solver="ISwH", seed=19), 1000, 5
     yield "holed_plate_lsd", scenes.holed_plate_drop(steps=500), 400, 5
     # periodic boundary: spheres drift across the faces (wrap, minimum image in the detector and
     # in every law's lever arms); ISwH with an orbital floor and side walls that the wrap moves
@@ -84,6 +88,19 @@ def zoi_scene():
     cut = 0.5 * (z[3 * len(z) // 4 - 1] + z[3 * len(z) // 4])
     out.sp.zoi = Boundary(switch=(False, False, True), lower=(0.0, 0.0, float(z[0]) - 1.0), upper=(0.0, 0.0, cut))
     return out
+
+
+def leap_zoi_scene(solver: str = "ISwBSDBF", seed: int = 13):
+    """Colliding spheres (0.5 m/s) in a box of plates with a zone of interest 0.05 mm beyond the
+    outermost spheres in x: over the run about half the spheres cross it and are erased at the
+    next reset, most erasures with contacts active (records re-keyed)."""
+    from vedo_gb300.scene import Boundary
+    sc = scenes.cluster(n=48, solver=solver, steps=3000, seed=seed, vel_sigma=0.5)
+    mobile = [k for k, m in enumerate(sc.model_index) if sc.models[m].behavior == 3]
+    x = sc.position[mobile, 0]
+    sc.sp.zoi = Boundary(switch=(True, False, False), lower=(float(x.min()) - 5e-5, 0.0, 0.0),
+                         upper=(float(x.max()) + 5e-5, 0.0, 0.0))
+    return sc
 
 
 def observable_cases():

@@ -22,7 +22,7 @@ GOLDEN = sorted(glob.glob(os.path.join(ROOT, "tests", "golden", "*.npz")))
 EXACT_CASES = ("box_lsd", "cluster_ISwBSDBF", "cluster_ISwBtSDBF", "cluster_ISwBSDB2F", "cluster_bsdbf_upiact1",
                "cluster_zoi", "holed_plate_lsd", "periodic_lsd",
                "periodic_far_lsd", "periodic_btsdbf", "periodic_bsdb2f", "leap_box_lsd",
-               "leap_periodic_lsd", "leap_periodic_wide", "leap_wide_y", "leap_column_z", "leap_single")
+               "leap_periodic_lsd", "leap_periodic_wide", "leap_wide_y", "leap_column_z", "leap_single", "leap_zoi")
 STATE = ("position", "velocity", "angular_velocity", "impact", "angular_impact", "orientation_x", "orientation_z")
 
 

@@ -198,16 +198,26 @@ def test_holed_plate_model_analysis():
         bad.analysis()
 
 
-def test_leap_with_a_zone_of_interest_is_refused(port_lib):
-    """The Leap consultant erases objects outside the zone at every reset (LeapConsultant.cpp:67),
-    which neither the oracle nor the engine does: the combination is refused, not run wrongly."""
+def test_leap_cleans_the_zone_at_every_reset(port_lib):
+    """The Leap consultant erases the mobile objects outside the zone of interest at every reset
+    (LeapConsultant.cpp:61-68), the NBS consultant only once, at the start (SimMediator.cpp:125-134):
+    with spheres flying out of the zone, the Leap world shrinks during the run and the NBS world
+    keeps its objects after the start (the golden fixtures leap_zoi*.npz pin the Leap run to the
+    reference's, records included)."""
     from oracle import PortWorld
     from vedo_gb300.scene import Boundary
-    sc = scenes.cluster(n=27, seed=2)
-    sc.sp.zoi = Boundary(switch=(False, False, True), lower=(0.0, 0.0, -1.0), upper=(0.0, 0.0, 1.0))
-    with pytest.raises(Exception, match="zone of interest"):
-        PortWorld(sc, consultant="leap")
-    PortWorld(sc, consultant="nbs")                 # the NBS consultant cleans up once, at the start
+    sc = scenes.cluster(n=27, seed=2, vel_sigma=1.0)
+    mobile = [k for k, m in enumerate(sc.model_index) if sc.models[m].behavior == 3]
+    x = sc.position[mobile, 0]
+    sc.sp.zoi = Boundary(switch=(True, False, False), lower=(float(x.min()) - 5e-5, 0.0, 0.0),
+                         upper=(float(x.max()) + 5e-5, 0.0, 0.0))
+    leap, nbs = PortWorld(sc, up_iact=5, consultant="leap"), PortWorld(sc, up_iact=5, consultant="nbs")
+    n0 = leap.n
+    assert n0 == nbs.n == sc.num_objects
+    leap.run(600)
+    nbs.run(600)
+    assert leap.n < n0 and nbs.n == n0
+    assert leap.state()["position"].shape == (leap.n, 3)
 
 
 def _one_zone_periodic_layer():

@@ -856,9 +856,7 @@ int Engine::init(const HScene& scene, const vedo_engine_opts& opts) {
     std::string msg;
     int rc = build_tables(host_, tab_, msg);
     if (rc != VEDO_OK) return fail(rc, msg);
-    if (leap_ && (host_.zoi_switch[0] || host_.zoi_switch[1] || host_.zoi_switch[2]))
-        return fail(VEDO_ERR_UNSUPPORTED_MODEL,      // LeapConsultant::NextStep erases objects at every reset (:67)
-                    "a zone of interest with the Leap consultant is not supported");
+    zoi_on_ = host_.zoi_switch[0] || host_.zoi_switch[1] || host_.zoi_switch[2];
     n_ = host_.n;
     nm_ = (uint32_t)tab_.models.size();
     dt_ = host_.time_interval;
@@ -965,13 +963,8 @@ int Engine::init(const HScene& scene, const vedo_engine_opts& opts) {
             // default-constructed ImpactStatus + setters (IactRecordTab.cpp:432-530)
             rf.push_back((uint8_t)(ST_DEFAULT | (R.contact[q] ? ST_CONTACT : 0) | (R.bond[q] ? ST_BOND : 0) | PF_NONZERO));
         }
-        nrec_ = (uint32_t)rk.size();
-        CK(dalloc(&d_rec_key_, nrec_)); CK(dalloc(&d_rec_hist_, nrec_)); CK(dalloc(&d_rec_v0_, nrec_));
-        CK(dalloc(&d_rec_flags_, nrec_));
-        CK(cudaMemcpy(d_rec_key_, rk.data(), 8 * nrec_, cudaMemcpyHostToDevice));
-        CK(cudaMemcpy(d_rec_hist_, rh.data(), sizeof(double4_32a) * nrec_, cudaMemcpyHostToDevice));
-        CK(cudaMemcpy(d_rec_v0_, rv.data(), 8 * nrec_, cudaMemcpyHostToDevice));
-        CK(cudaMemcpy(d_rec_flags_, rf.data(), nrec_, cudaMemcpyHostToDevice));
+        rc = upload_records(rk, rh, rv, rf);
+        if (rc != VEDO_OK) return rc;
     }
     // first candidate list (NBSConsultant constructor) + Initiate
     rc = rebuild(true);
@@ -998,6 +991,104 @@ int Engine::init(const HScene& scene, const vedo_engine_opts& opts) {
         rc = status_row(host_.rec.first.size(), contacts);
         if (rc != VEDO_OK) return rc;
     }
+    return VEDO_OK;
+}
+
+// The records the next list takes its history from (sorted by key).
+int Engine::upload_records(const std::vector<uint64_t>& rk, const std::vector<double4_32a>& rh,
+                           const std::vector<double>& rv, const std::vector<uint8_t>& rf) {
+    for (void** p : {(void**)&d_rec_key_, (void**)&d_rec_hist_, (void**)&d_rec_v0_, (void**)&d_rec_flags_}) {
+        if (*p) cudaFree(*p);
+        *p = nullptr;
+    }
+    nrec_ = (uint32_t)rk.size();
+    if (!nrec_) return VEDO_OK;
+    CK(dalloc(&d_rec_key_, nrec_)); CK(dalloc(&d_rec_hist_, nrec_)); CK(dalloc(&d_rec_v0_, nrec_));
+    CK(dalloc(&d_rec_flags_, nrec_));
+    CK(cudaMemcpy(d_rec_key_, rk.data(), 8 * nrec_, cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(d_rec_hist_, rh.data(), sizeof(double4_32a) * nrec_, cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(d_rec_v0_, rv.data(), 8 * nrec_, cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(d_rec_flags_, rf.data(), nrec_, cudaMemcpyHostToDevice));
+    return VEDO_OK;
+}
+
+// LeapConsultant::NextStep at a reset (LeapConsultant.cpp:61-68): SyncWorld,
+// RebuildIactRecordTab, then Consultant::CleanUp (Consultant.cpp:264-319).  The mobile objects
+// outside the zone of interest are erased and the others renumbered (their order kept); the
+// records of the interactions active at the current positions -- their statuses as the carry of
+// an ordinary reset takes them -- are re-keyed as IactRecordTab::ModifyPair does, and become the
+// records the reset's list takes its history from.  Host work, run only when an object leaves.
+int Engine::leap_cleanup(bool* erased_any) {
+    *erased_any = false;
+    int rc = sync_host_state();
+    if (rc != VEDO_OK) return rc;
+    std::vector<uint32_t> jump;
+    const std::vector<uint32_t> erased = zoi_outside(host_, jump);
+    if (erased.empty()) return VEDO_OK;
+    const uint32_t np = cur_.np;
+    std::vector<uint32_t> fa(np), fb(np);
+    std::vector<uint8_t> fl(np);
+    std::vector<double4_32a> hh(np);
+    std::vector<double> vv(np);
+    if (np) {
+        k_detect_active<<<blocks_for(np), TPB, 0, stream_>>>(np, cur_.sm, cur_.param, d_params_, d_geom_, d_hole_,
+                                                             d_reach_, d_pos_, d_ox_, d_oz_, d_pos32_, d_wall32_,
+                                                             cur_.flags, tab_.pbc);
+        ++launches_;
+        CK(cudaMemcpyAsync(fa.data(), cur_.first, 4 * (size_t)np, cudaMemcpyDeviceToHost, stream_));
+        CK(cudaMemcpyAsync(fb.data(), cur_.second, 4 * (size_t)np, cudaMemcpyDeviceToHost, stream_));
+        CK(cudaMemcpyAsync(fl.data(), cur_.flags, np, cudaMemcpyDeviceToHost, stream_));
+        CK(cudaMemcpyAsync(hh.data(), cur_.hist, sizeof(double4_32a) * np, cudaMemcpyDeviceToHost, stream_));
+        CK(cudaMemcpyAsync(vv.data(), cur_.v0, 8 * (size_t)np, cudaMemcpyDeviceToHost, stream_));
+        CK(cudaStreamSynchronize(stream_));
+    }
+    std::vector<std::pair<uint32_t, uint32_t>> keys;
+    std::vector<uint32_t> src;
+    for (uint32_t k = 0; k < np; ++k)
+        if (fl[k] & PF_ACTIVE) {
+            keys.push_back({fa[k], fb[k]});
+            src.push_back(k);
+        }
+    std::vector<uint64_t> rk;
+    std::vector<double4_32a> rh;
+    std::vector<double> rv;
+    std::vector<uint8_t> rf;
+    for (const auto& kv : modify_pair(keys, jump)) {
+        const uint32_t k = src[kv.second];
+        const bool nz = fl[k] & PF_NONZERO;
+        rk.push_back(((uint64_t)kv.first.first << 32) | kv.first.second);
+        rh.push_back(nz ? hh[k] : make_double4_32a(0.0, 0.0, 0.0, 0.0));
+        rv.push_back(nz ? vv[k] : 0.0);
+        rf.push_back((uint8_t)(fl[k] & (PF_STATUS | PF_NONZERO)));
+    }
+    erase_objects(host_, erased);
+    n_ = host_.n;
+    // the survivors' state and models (the buffers keep their larger capacity)
+    std::vector<double4_32a> tmp;
+    double4_32a* dst[] = {d_pos_, d_vel_, d_av_, d_ox_, d_oz_, d_imp_, d_aimp_};
+    const std::vector<double>* srcv[] = {&host_.pos, &host_.vel, &host_.av, &host_.ox, &host_.oz, &host_.imp,
+                                         &host_.aimp};
+    for (int k = 0; k < 7; ++k) {
+        upload3(tmp, *srcv[k], n_);
+        CK(cudaMemcpy(dst[k], tmp.data(), sizeof(double4_32a) * n_, cudaMemcpyHostToDevice));
+    }
+    CK(cudaMemcpy(d_model_of_, host_.model_of.data(), sizeof(uint32_t) * n_, cudaMemcpyHostToDevice));
+    global_ids_.clear();
+    leap_rmax_ = 0.0;                      // LeapConsultant::Reset takes the largest range anew
+    for (uint32_t i = 0; i < n_; ++i)
+        if (tab_.models[host_.model_of[i]].scope != SCOPE_LOCAL) global_ids_.push_back(i);
+        else leap_rmax_ = std::max(leap_rmax_, tab_.models[host_.model_of[i]].range);
+    if (global_ids_.size() == n_) return fail(VEDO_ERR_INVALID_SCENE, "the zone of interest erased every local object");
+    if (!global_ids_.empty())
+        CK(cudaMemcpy(d_global_, global_ids_.data(), sizeof(uint32_t) * global_ids_.size(), cudaMemcpyHostToDevice));
+    k_refresh32<<<blocks_for(n_), TPB, 0, stream_>>>(n_, d_model_of_, d_models_, d_pos_, d_ox_, d_oz_,
+                                                     mk(origin_[0], origin_[1], origin_[2]), d_pos32_, d_wall32_);
+    ++launches_;
+    CK(cudaMemsetAsync(d_touched_, 0, n_, stream_));
+    CK(cudaStreamSynchronize(stream_));
+    rc = upload_records(rk, rh, rv, rf);
+    if (rc != VEDO_OK) return rc;
+    *erased_any = true;
     return VEDO_OK;
 }
 
@@ -1256,7 +1347,12 @@ int Engine::step_once(bool write_impulses) {
     t_ += dt;                                              // SystemParameter::NextStep (SystemParameter.h:113-116)
     if (round_ % opts_.up_iact == 0) {
         if (prof) CK(cudaEventRecord(ev_[3], stream_));
-        int rc = rebuild(false);
+        bool erased = false;
+        if (leap_ && zoi_on_) {                            // LeapConsultant.cpp:61-68
+            int rc = leap_cleanup(&erased);
+            if (rc != VEDO_OK) return rc;
+        }
+        int rc = rebuild(erased);                          // after an erasure, from the re-keyed records
         if (rc != VEDO_OK) return rc;
         if (prof) {
             CK(cudaEventRecord(ev_[4], stream_));

@@ -79,6 +79,10 @@ private:
     std::FILE* status_ = nullptr;                    // <output dir>SystemStatus.csv, with an output prefix
     int sync_host_state();
     int ensure_stage();
+    int leap_cleanup(bool* erased);                  // LeapConsultant::NextStep's CleanUp at a reset
+    int upload_records(const std::vector<uint64_t>& key, const std::vector<double4_32a>& hist,
+                       const std::vector<double>& v0, const std::vector<uint8_t>& flags);
+    bool zoi_on_ = false;                            // an active zone of interest
 
     // scene and options
     HScene host_;

@@ -372,10 +372,10 @@ void correct_boundary(uint8_t sw[3], double lo[3], double hi[3]) {
 }
 }  // namespace
 
-uint32_t prepare_scene(HScene& s) {
-    correct_boundary(s.zoi_switch, s.zoi_lower, s.zoi_upper);
-    correct_boundary(s.pbc_switch, s.pbc_lower, s.pbc_upper);
-    if (!(s.zoi_switch[0] || s.zoi_switch[1] || s.zoi_switch[2])) return 0;
+std::vector<uint32_t> zoi_outside(const HScene& s, std::vector<uint32_t>& jump) {
+    std::vector<uint32_t> erased;
+    jump.assign(s.n, 0u);
+    if (!(s.zoi_switch[0] || s.zoi_switch[1] || s.zoi_switch[2])) return erased;
     // Boundary::InBoundary (Boundary.cpp:161-190): outside when below or above a switched axis
     auto inside = [&](uint32_t i) {
         for (int k = 0; k < 3; ++k) {
@@ -386,7 +386,6 @@ uint32_t prepare_scene(HScene& s) {
     };
     // ElementMappingJump: minus the number of erased objects up to and including this one
     // (unsigned, as the reference's _uint_t arithmetic)
-    std::vector<uint32_t> jump(s.n), erased;
     uint32_t dead = 0;
     for (uint32_t i = 0; i < s.n; ++i) {
         const uint32_t m = s.model_of[i];
@@ -396,14 +395,18 @@ uint32_t prepare_scene(HScene& s) {
         }
         jump[i] = dead;
     }
-    if (erased.empty()) return 0;
-    // ModifyPair: every record whose key changes is moved to its new key, overwriting whatever
-    // is there (in key order); records of erased objects are re-keyed the same way
-    HRecords& R = s.rec;
+    return erased;
+}
+
+std::vector<std::pair<std::pair<uint32_t, uint32_t>, size_t>> modify_pair(
+    const std::vector<std::pair<uint32_t, uint32_t>>& keys, const std::vector<uint32_t>& jump) {
+    // every record whose key changes is moved to its new key, overwriting whatever is there (in
+    // key order); records of erased objects are re-keyed the same way
     using Key = std::pair<uint32_t, uint32_t>;
+    const uint32_t n = (uint32_t)jump.size();
     std::map<Key, size_t> tab;
-    for (size_t q = 0; q < R.size(); ++q) tab[Key(R.first[q], R.second[q])] = q;
-    auto j = [&](uint32_t id) { return id < s.n ? jump[id] : 0u; };   // std::map::operator[] default
+    for (size_t q = 0; q < keys.size(); ++q) tab[keys[q]] = q;
+    auto j = [&](uint32_t id) { return id < n ? jump[id] : 0u; };   // std::map::operator[] default
     std::vector<Key> gone;
     std::map<Key, size_t> extra;
     for (const auto& kv : tab) {
@@ -415,8 +418,38 @@ uint32_t prepare_scene(HScene& s) {
     }
     for (const Key& k : gone) tab.erase(k);
     for (const auto& kv : extra) tab[kv.first] = kv.second;
+    return std::vector<std::pair<Key, size_t>>(tab.begin(), tab.end());
+}
+
+void erase_objects(HScene& s, const std::vector<uint32_t>& erased) {
+    std::vector<uint8_t> keep(s.n, 1);
+    for (uint32_t i : erased) keep[i] = 0;
+    uint32_t w = 0;
+    for (uint32_t i = 0; i < s.n; ++i) {
+        if (!keep[i]) continue;
+        s.model_of[w] = s.model_of[i];
+        if (i < s.ids.size() && w < s.ids.size()) s.ids[w] = s.ids[i];
+        for (std::vector<double>* v : {&s.pos, &s.vel, &s.ox, &s.oz, &s.av, &s.imp, &s.aimp})
+            for (int k = 0; k < 3; ++k) (*v)[3 * (size_t)w + k] = (*v)[3 * (size_t)i + k];
+        ++w;
+    }
+    s.n = w;
+    s.model_of.resize(w);
+    if (s.ids.size() > w) s.ids.resize(w);
+    for (std::vector<double>* v : {&s.pos, &s.vel, &s.ox, &s.oz, &s.av, &s.imp, &s.aimp}) v->resize(3 * (size_t)w);
+}
+
+uint32_t prepare_scene(HScene& s) {
+    correct_boundary(s.zoi_switch, s.zoi_lower, s.zoi_upper);
+    correct_boundary(s.pbc_switch, s.pbc_lower, s.pbc_upper);
+    std::vector<uint32_t> jump;
+    const std::vector<uint32_t> erased = zoi_outside(s, jump);
+    if (erased.empty()) return 0;
+    HRecords& R = s.rec;
+    std::vector<std::pair<uint32_t, uint32_t>> keys(R.size());
+    for (size_t q = 0; q < R.size(); ++q) keys[q] = {R.first[q], R.second[q]};
     HRecords N;
-    for (const auto& kv : tab) {
+    for (const auto& kv : modify_pair(keys, jump)) {
         const size_t q = kv.second;
         N.first.push_back(kv.first.first);
         N.second.push_back(kv.first.second);
@@ -434,22 +467,7 @@ uint32_t prepare_scene(HScene& s) {
         }
     }
     R = std::move(N);
-    // DOWorld::EraseDOStatus / DOContainer::Erase: the survivors keep their order
-    std::vector<uint8_t> keep(s.n, 1);
-    for (uint32_t i : erased) keep[i] = 0;
-    uint32_t w = 0;
-    for (uint32_t i = 0; i < s.n; ++i) {
-        if (!keep[i]) continue;
-        s.model_of[w] = s.model_of[i];
-        if (i < s.ids.size() && w < s.ids.size()) s.ids[w] = s.ids[i];
-        for (std::vector<double>* v : {&s.pos, &s.vel, &s.ox, &s.oz, &s.av, &s.imp, &s.aimp})
-            for (int k = 0; k < 3; ++k) (*v)[3 * (size_t)w + k] = (*v)[3 * (size_t)i + k];
-        ++w;
-    }
-    s.n = w;
-    s.model_of.resize(w);
-    if (s.ids.size() > w) s.ids.resize(w);
-    for (std::vector<double>* v : {&s.pos, &s.vel, &s.ox, &s.oz, &s.av, &s.imp, &s.aimp}) v->resize(3 * (size_t)w);
+    erase_objects(s, erased);
     return (uint32_t)erased.size();
 }
 

@@ -63,6 +63,17 @@ bool write_xml(const std::string& path, const HScene& s, std::string& err);
 // pair records re-keyed as IactRecordTab::ModifyPair does (IactRecordTab.cpp:41-69).  Returns
 // the number of erased objects.
 uint32_t prepare_scene(HScene& s);
+// The three steps of Consultant::CleanUp, for a world whose boundaries are corrected (the Leap
+// consultant runs it at every reset, LeapConsultant.cpp:61-68):
+//  zoi_outside    the mobile objects outside the zone of interest (ascending), and per object the
+//                 ElementMappingJump (minus the erased count up to and including it, unsigned);
+//  modify_pair    IactRecordTab::ModifyPair on record keys (later equal keys replace earlier
+//                 ones): the surviving (new key, index of its source record) in key order;
+//  erase_objects  DOContainer::Erase / DOWorld::EraseDOStatus: the survivors keep their order.
+std::vector<uint32_t> zoi_outside(const HScene& s, std::vector<uint32_t>& jump);
+std::vector<std::pair<std::pair<uint32_t, uint32_t>, size_t>> modify_pair(
+    const std::vector<std::pair<uint32_t, uint32_t>>& keys, const std::vector<uint32_t>& jump);
+void erase_objects(HScene& s, const std::vector<uint32_t>& erased);
 
 // Flattened constants for the device.
 struct Tables {

@@ -144,7 +144,12 @@ class GpuEngine:
         if rc != 0:
             raise EngineError(rc, L.vedo_gpu_last_error(None).decode())
         self.h = h
-        self.n = L.vedo_gpu_num_objects(h)
+
+    @property
+    def n(self) -> int:
+        """Objects now: the Leap consultant's zone-of-interest clean-up erases objects at resets
+        (LeapConsultant.cpp:61-68), so the count is read after every call that steps."""
+        return lib().vedo_gpu_num_objects(self.h)
 
     def _check(self, rc: int):
         if rc != 0:
@@ -345,7 +350,6 @@ class BatchEngine(GpuEngine):
         if rc != 0:
             raise EngineError(rc, L.vedo_gpu_last_error(None).decode())
         self.h = h
-        self.n = L.vedo_gpu_num_objects(h)
         self.num_scenes = L.vedo_gpu_num_scenes(h)
 
     def scene_range(self, s: int):
