@@ -671,7 +671,8 @@ def bed_workload(args, dist, dev):
     t_tick = kp["pair_ms"] / args.profile_steps
     peak, _ = peaks()
     ach = b_alg * n / (t_tick * 1e-3) / 1e9
-    traffic = ncu_traffic("k_tick_light_bed16M_dram.md") if args.bed_n == 16_000_000 else None
+    # a committed capture of the pair-pass tick at this size, when there is one
+    traffic = ncu_traffic("k_tick_bed16M_dram.md") if args.bed_n == 16_000_000 else None
     total = dist.reduce(float(n), "sum")
     out = {"workload": f"compressed_bed_{args.bed_n // 1_000_000}M", "particles": n,
            "value": total * args.bed_steps / (t * 1e-3), "unit": UNIT, "ms_per_step": t / args.bed_steps,
@@ -680,7 +681,7 @@ def bed_workload(args, dist, dev):
            "tick_roofline": {"achieved": ach, "peak": peak, "unit": "GB/s", "frac": ach / peak, "tick_ms": t_tick,
                              "alg_bytes_per_particle_step": b_alg, "traffic": traffic,
                              "dram_frac": traffic / (t_tick * 1e-3) / 1e9 / peak if traffic else None,
-                             "traffic_source": "profiles/k_tick_light_bed16M_dram.md" if traffic else None},
+                             "traffic_source": "profiles/k_tick_bed16M_dram.md" if traffic else None},
            "note": f"steps {TUNE_STEPS}..{TUNE_STEPS + args.bed_steps} of the configured 2000-step run (dt 2e-7 s); "
                    "a simple cubic lattice whose neighbours, floor, walls and top plate touch (solid fraction 0.524, "
                    "standing in for a random loose packing at 0.55); mixed form"}

@@ -183,7 +183,7 @@ def test_split_tick_and_pair_pass_are_exclusive(engine_lib):
 def test_mixed_orientations_follow_the_fp64_form(box_ido, engine_lib):
     """With `orientations` the mixed form turns every sphere's Ox, Oz by dt (w + dw/2) per step
     as DOSphere::Response does: on the settled box (spheres rolling and spinning) they stay
-    within 1e-6 of the FP64 form's after 300 steps (the angular velocities themselves differ at
+    within 1e-5 of the FP64 form's after 300 steps (the angular velocities themselves differ at
     the mixed form's force error), stay unit and orthogonal, and are the same in every form of
     the tick; without the option they are left as they were."""
     f64 = engine_lib.GpuEngine(box_ido, up_iact=1)
@@ -203,7 +203,7 @@ def test_mixed_orientations_follow_the_fp64_form(box_ido, engine_lib):
         for k in st:
             assert np.array_equal(st[k], first[k]), k
     for k in ("orientation_x", "orientation_z"):
-        np.testing.assert_allclose(first[k], ref[k], rtol=0, atol=1e-6, err_msg=k)
+        np.testing.assert_allclose(first[k], ref[k], rtol=0, atol=1e-5, err_msg=k)
         assert np.allclose(np.linalg.norm(first[k], axis=1), 1.0, atol=1e-12)
     assert np.abs(np.sum(first["orientation_x"] * first["orientation_z"], axis=1)).max() < 1e-12
     left = still.state(("orientation_x", "orientation_z"))
