@@ -486,7 +486,8 @@ struct TickArgs {
     float4* xsB;                   // ... after the step
     int xs_stored;                 // 1: splits stored once per step; 0: formed per pair
     uint32_t* work;                // split tick: spheres deferred to the full tick (else nullptr)
-    uint32_t* nwork;               // split tick: spheres in `work`; pair pass: pairs in `pwork`
+    uint32_t* nwork;               // split tick: spheres in `work`; pair pass: sphere pairs in `pwork`
+                                   // (from its start), and nwork[-1] wall pairs (from its end)
     uint4* pwork;                  // pair pass: (owner entry, its sphere, entry word, meta word) of every
                                    // pair on the exact path
     uint8_t* xf;                   // pair pass: [ne] 1 = the entry is on the exact path this step
@@ -573,7 +574,7 @@ __device__ __noinline__ void wall_pair(const TickArgs& a, int cd, uint32_t pi, u
 // entries that need the exact path.  The side effects are idempotent, so a walk that is
 // abandoned and redone (the split tick) leaves the same state.
 __device__ __forceinline__ uint32_t prefilter_group(const TickArgs& a, uint32_t base, uint32_t e1, const float4& p32i,
-                                                    float pad, bool& dirty, uint32_t& owned) {
+                                                    float pad, bool& dirty, uint32_t& owned, uint32_t& walls) {
     uint32_t ge[TICK_GROUP], gm[TICK_GROUP];
     uint8_t gf[TICK_GROUP];
     float4 gp[TICK_GROUP];
@@ -600,6 +601,7 @@ __device__ __forceinline__ uint32_t prefilter_group(const TickArgs& a, uint32_t 
         if (meta & META_BOND) {
             exact |= 1u << k;
             if (meta & META_OWNER) owned |= 1u << k;
+            if (wall) walls |= 1u << k;
             continue;
         }
         const float4 ws = wall ? a.wall32[j] : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
@@ -614,6 +616,7 @@ __device__ __forceinline__ uint32_t prefilter_group(const TickArgs& a, uint32_t 
         if (!apart32(cd, i_slave ? p32i : gp[k], i_slave ? gp[k] : p32i, ws, a.reach[meta & META_PI] + pk)) {
             exact |= 1u << k;
             if (meta & META_OWNER) owned |= 1u << k;
+            if (wall) walls |= 1u << k;
             continue;
         }
         if (wall && a.write_imp) {
@@ -860,9 +863,10 @@ __device__ __forceinline__ float2 tick_sphere(const TickArgs& a, uint32_t i) {
             for (uint32_t c0 = e0; c0 < e1 && !quiet; c0 += 64) {
                 const uint32_t c1 = min(e1, c0 + 64);
                 unsigned long long exact = 0ull;
-                uint32_t owned = 0u;                   // (unused here)
+                uint32_t owned = 0u, walls = 0u;       // (unused here)
                 for (uint32_t base = c0; base < c1; base += TICK_GROUP)
-                    exact |= (unsigned long long)prefilter_group(a, base, c1, p32i, pad, dirty, owned) << (base - c0);
+                    exact |= (unsigned long long)prefilter_group(a, base, c1, p32i, pad, dirty, owned, walls)
+                             << (base - c0);
                 any_exact |= exact != 0ull;
                 // Phase 2: the exact path for the flagged entries, in entry order
                 while (exact) {
@@ -980,9 +984,9 @@ __global__ void __launch_bounds__(TPB, 6) k_tick_light(TickArgs a) {   // 6 bloc
                 const uint32_t e0 = a.nptr[i], e1 = a.nptr[i + 1];
                 const float4 p32i = a.pos32[i];
                 bool dirty = false;
-                uint32_t owned = 0u;                   // (unused here)
+                uint32_t owned = 0u, walls = 0u;       // (unused here)
                 for (uint32_t base = e0; base < e1 && !defer; base += TICK_GROUP)
-                    defer = prefilter_group(a, base, e1, p32i, pad, dirty, owned) != 0u;
+                    defer = prefilter_group(a, base, e1, p32i, pad, dirty, owned, walls) != 0u;
                 note_walk(a, i, a.qcnt[i], dirty || defer);    // (reread: fewer live registers in the walk)
             }
             if (!defer) {                          // state loaded after the walk: fewer live registers
@@ -1055,14 +1059,16 @@ __global__ void __launch_bounds__(TPB, 4) k_tick_pf(TickArgs a) {     // 63 regi
     // pairs are appended with one atomic per warp
     bool more = walk && c0 < e1;
     while (__any_sync(0xffffffffu, more)) {
-        unsigned long long own = 0ull;
+        unsigned long long own = 0ull, wown = 0ull;
         if (more) {
             const uint32_t c1 = min(e1, c0 + 64);
             unsigned long long exact = 0ull;
             for (uint32_t base = c0; base < c1; base += TICK_GROUP) {
-                uint32_t owned = 0u;
-                exact |= (unsigned long long)prefilter_group(a, base, c1, p32i, pad, dirty, owned) << (base - c0);
-                own |= (unsigned long long)owned << (base - c0);
+                uint32_t owned = 0u, walls = 0u;
+                exact |= (unsigned long long)prefilter_group(a, base, c1, p32i, pad, dirty, owned, walls)
+                         << (base - c0);
+                own |= (unsigned long long)(owned & ~walls) << (base - c0);
+                wown |= (unsigned long long)(owned & walls) << (base - c0);
             }
             any_exact |= exact != 0ull;
             if (c0 == e0) {
@@ -1071,22 +1077,38 @@ __global__ void __launch_bounds__(TPB, 4) k_tick_pf(TickArgs a) {     // 63 regi
                 for (uint32_t e = c0; e < c1; ++e) a.xf[e] = (uint8_t)((exact >> (e - c0)) & 1ull);
             }
         }
-        const uint32_t cnt = (uint32_t)__popcll(own);
-        uint32_t incl = cnt;                       // inclusive prefix over the warp
+        // sphere pairs fill the worklist from its start, wall pairs from its end, so that the
+        // pair kernel runs each kind in full warps (a wall pair's detector is FP64 work, and a
+        // warp issues it once for every lane that needs it)
+        const uint32_t cnt = (uint32_t)__popcll(own), wcnt = (uint32_t)__popcll(wown);
+        uint32_t incl = cnt, wincl = wcnt;         // inclusive prefixes over the warp
 #pragma unroll
         for (int o = 1; o < 32; o <<= 1) {
             const uint32_t v = __shfl_up_sync(0xffffffffu, incl, o);
-            if (lane >= o) incl += v;
+            const uint32_t w = __shfl_up_sync(0xffffffffu, wincl, o);
+            if (lane >= o) {
+                incl += v;
+                wincl += w;
+            }
         }
-        uint32_t at = 0u;
+        uint32_t at = 0u, wat = 0u;
         if (lane == 31 && incl) at = atomicAdd(a.nwork, incl);
+        if (lane == 31 && wincl) wat = atomicAdd(a.nwork - 1, wincl);
         at = __shfl_sync(0xffffffffu, at, 31) + incl - cnt;
+        wat = __shfl_sync(0xffffffffu, wat, 31) + wincl - wcnt;
         while (own) {
             const int k = __ffsll(own) - 1;
             own &= own - 1;
             const uint32_t e = c0 + (uint32_t)k;   // (its words are in L1 from the prefilter)
             if (at < a.pcap) a.pwork[at] = make_uint4(e, i, a.nent[e], a.nmeta[e]);   // (at most one per entry)
             ++at;
+        }
+        while (wown) {
+            const int k = __ffsll(wown) - 1;
+            wown &= wown - 1;
+            const uint32_t e = c0 + (uint32_t)k;
+            if (wat < a.pcap) a.pwork[a.pcap - 1u - wat] = make_uint4(e, i, a.nent[e], a.nmeta[e]);
+            ++wat;
         }
         if (more) {
             c0 += 64;
@@ -1096,31 +1118,36 @@ __global__ void __launch_bounds__(TPB, 4) k_tick_pf(TickArgs a) {     // 63 regi
     if (walk) note_walk(a, i, qc, dirty || any_exact);
 }
 
+// One pair of the worklist: the exact path and both members' shares.
+template <int LAW, bool XS>
+__device__ __forceinline__ void pair_item(const TickArgs& a, const uint4& it) {
+    const uint32_t e = it.x, i = it.y, ent = it.z, meta = it.w;
+    const d3 Pi = XS ? mk(0.0, 0.0, 0.0) : ld(a.xA, i);
+    f3 Jp, tA, tB;
+    const int app = exact_pair<LAW, XS>(a, i, Pi, e, ent, meta, a.scenes[a.scene_of[i]].dtf, Jp, tA, tB);
+    // each member's share at its own entry: the slave adds J and tA, the master -J and tB
+    // (the negation is exact, so the sums see the single tick's values)
+    const bool i_slave = meta & META_SLAVE;
+    const float kind = __int_as_float(app);
+    const f3 Ji = i_slave ? Jp : -Jp, ti = i_slave ? tA : tB;
+    a.prec[2 * (size_t)e] = make_float4(Ji.x, Ji.y, Ji.z, kind);
+    if (app == 2) a.prec[2 * (size_t)e + 1] = make_float4(ti.x, ti.y, ti.z, 0.0f);
+    if (!(ent & WALL_BIT)) {                   // a sphere pair: the partner's share at its entry
+        const uint32_t q2 = a.pmir[e];
+        const f3 Jj = i_slave ? -Jp : Jp, tj = i_slave ? tB : tA;
+        a.prec[2 * (size_t)q2] = make_float4(Jj.x, Jj.y, Jj.z, kind);
+        if (app == 2) a.prec[2 * (size_t)q2 + 1] = make_float4(tj.x, tj.y, tj.z, 0.0f);
+    }
+}
+
 template <int LAW, bool XS>
 __global__ void __launch_bounds__(TPB, 4) k_tick_pairs(TickArgs a) {     // 64 registers (a few spill)
     step_order();
     if (held_step(a)) return;
-    const uint32_t nw = min(*a.nwork, a.pcap);
-    for (uint32_t q = blockIdx.x * blockDim.x + threadIdx.x; q < nw; q += gridDim.x * blockDim.x) {
-        const uint4 it = a.pwork[q];
-        const uint32_t e = it.x, i = it.y, ent = it.z, meta = it.w;
-        const d3 Pi = XS ? mk(0.0, 0.0, 0.0) : ld(a.xA, i);
-        f3 Jp, tA, tB;
-        const int app = exact_pair<LAW, XS>(a, i, Pi, e, ent, meta, a.scenes[a.scene_of[i]].dtf, Jp, tA, tB);
-        // each member's share at its own entry: the slave adds J and tA, the master -J and tB
-        // (the negation is exact, so the sums see the single tick's values)
-        const bool i_slave = meta & META_SLAVE;
-        const float kind = __int_as_float(app);
-        const f3 Ji = i_slave ? Jp : -Jp, ti = i_slave ? tA : tB;
-        a.prec[2 * (size_t)e] = make_float4(Ji.x, Ji.y, Ji.z, kind);
-        if (app == 2) a.prec[2 * (size_t)e + 1] = make_float4(ti.x, ti.y, ti.z, 0.0f);
-        if (!(ent & WALL_BIT)) {                   // a sphere pair: the partner's share at its entry
-            const uint32_t q2 = a.pmir[e];
-            const f3 Jj = i_slave ? -Jp : Jp, tj = i_slave ? tB : tA;
-            a.prec[2 * (size_t)q2] = make_float4(Jj.x, Jj.y, Jj.z, kind);
-            if (app == 2) a.prec[2 * (size_t)q2 + 1] = make_float4(tj.x, tj.y, tj.z, 0.0f);
-        }
-    }
+    const uint32_t nw = min(a.nwork[0], a.pcap), nww = min(a.nwork[-1], a.pcap - nw);
+    // sphere pairs, then wall pairs: only the warp that straddles the two mixes them
+    for (uint32_t q = blockIdx.x * blockDim.x + threadIdx.x; q < nw + nww; q += gridDim.x * blockDim.x)
+        pair_item<LAW, XS>(a, a.pwork[q < nw ? q : a.pcap - 1u - (q - nw)]);
 }
 
 template <bool XS>
@@ -1236,7 +1263,9 @@ __global__ void k_walls(uint32_t nglob, const uint32_t* __restrict__ glob, const
     const float drel = disp_in[0], dabs = disp_in[1], dw = disp_in[2];
     const bool hold = list_spent(drel, dabs, dw, skin, skin_w);
     if (q == 0) {
-        *nwork = 0u;                               // the split tick's worklist, empty for the next step
+        nwork[0] = nwork[1] = 0u;                  // the worklists' counts (pair pass: wall pairs, then
+                                                   // sphere pairs and the split tick's spheres), empty
+                                                   // for the next step
         if (hold) {
             for (int k = 0; k < 4; ++k) disp_out[k] = disp_in[k];
             *held += 1u;
@@ -3223,7 +3252,7 @@ void MixedEngine::launch_step(bool write_imp) {
         (const double4_32a*)d_v64_, (const double4_32a*)d_w64_, (const float4*)a.v32A, a.v32B, (const float4*)a.w32A,
         a.w32B, d_ox_, d_oz_, dt_max_, d_red_ + 8, d_red_ + 2, (const float*)(d_disp_ + 4 * cur_),
         d_disp_ + 4 * (cur_ ^ 1), skin_min_, WALL_SKIN * skin_min_, pos_eps_, (const unsigned*)(d_red_ + 12),
-        (const double4_32a*)d_wrot_, d_red_ + 11, d_wall32_, d_red_ + 14));
+        (const double4_32a*)d_wrot_, d_red_ + 11, d_wall32_, d_red_ + 13));
     ++launches_;
     if (pe) cudaEventRecordWithFlags(pe[2], stream_, ev_flags_);
     cur_ ^= 1;
