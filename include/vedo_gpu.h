@@ -398,6 +398,13 @@ int vedo_gpu_scene_range(const vedo_gpu_engine* e, uint32_t scene, uint32_t* fir
  * on; a job stops after exactly its step count and its final state is copied to the host.
  * A job's result equals the same scene run alone in the MIXED form for the same number
  * of steps, bit for bit. */
+/* Admission order: arrival (default), or the queued job with the least work (spheres x steps)
+ * first; with a cap on the live jobs' spheres (0: none), a job waits while admitting it would pass
+ * the cap (a job larger than the cap alone runs when nothing else does).  Shortest-first with a cap
+ * trades the long jobs' latency for the short ones' when the offered work exceeds the GPU's rate.
+ * No counterpart in the reference. */
+#define VEDO_SRV_FIFO 0u
+#define VEDO_SRV_SHORTEST_FIRST 1u
 #define VEDO_SRV_BYTES_PER_OBJECT 800u
 #define VEDO_SRV_ENTRIES_PER_SPHERE 18u
 #define VEDO_SRV_BYTES_PER_ENTRY 150u
@@ -422,6 +429,7 @@ typedef struct vedo_server vedo_server;
 int vedo_srv_create(const vedo_engine_opts* opts, uint64_t hbm_budget_bytes, vedo_server** out);
 /* Queue a job: the scene is copied; steps >= 1.  Fails (and queues nothing) when the scene is
  * invalid or the job alone would not fit the budget. */
+int vedo_srv_set_policy(vedo_server* s, uint32_t order, uint64_t max_live_spheres);
 int vedo_srv_submit(vedo_server* s, const vedo_scene_desc* scene, uint64_t steps, uint64_t* job_id);
 int vedo_srv_poll(vedo_server* s, uint64_t job_id, vedo_job_info* info);
 /* Block until the job is done, cancelled or failed, or timeout_s passes (then

@@ -57,6 +57,33 @@ def test_served_jobs_equal_alone(engine_lib):
             assert np.array_equal(r[k], ref[k]), k
 
 
+def test_shortest_first_with_a_live_cap(engine_lib):
+    """Shortest-work-first admission under a live-sphere cap: with a long job running, a short
+    job submitted after a second long one is admitted before it (and finishes first), the cap
+    holds the second long job back while the first runs, and every result still equals its scene
+    alone."""
+    from vedo_gb300.serve import Server
+    long1 = (scenes.serving_job("settle", 3000, "lsd", 5), 3000)
+    long2 = (scenes.serving_job("settle", 3000, "lsd", 6), 3000)
+    short = (scenes.serving_job("projectile", 2000, "lsd", 7), 100)
+    n1 = long1[0].num_objects
+    with Server(hbm_budget_bytes=8 * 10**9, order="shortest", max_live_spheres=n1 + short[0].num_objects) as srv:
+        a = srv.submit(*long1)
+        _wait_running(srv, a, 1)
+        b = srv.submit(*long2)
+        c = srv.submit(*short)
+        ib, ic = srv.wait(b, 120.0), srv.wait(c, 120.0)
+        ia = srv.wait(a, 120.0)
+        res = {j: srv.result(j, FIELDS) for j in (a, b, c)}
+    assert all(i["status"] == "done" for i in (ia, ib, ic))
+    assert ic["admit_s"] < ib["admit_s"] and ic["done_s"] < ib["done_s"]
+    assert ib["admit_s"] >= ia["done_s"] - 1e-6        # the cap: the second long job waits for the first
+    for j, (sc, st) in zip((a, b, c), (long1, long2, short)):
+        ref = _alone(engine_lib, sc, st)
+        for k in FIELDS:
+            assert np.array_equal(res[j][k], ref[k]), k
+
+
 def test_admission_respects_the_hbm_budget(engine_lib):
     from vedo_gb300.serve import Server, job_charge
     scs = [scenes.serving_job("settle", 2000, "lsd", s) for s in range(3)]

@@ -506,8 +506,9 @@ struct TickArgs {
                                    // sphere-pair pads <= x and fixed-wall pads <= y
     uint8_t* qcnt;                 // [n] consecutive clean walks (0..2) since the last rebuild
     const uint32_t* ext_of;        // [n] the caller's index of each object (storage order)
-    double4_32a* sox;              // the orientation arrays (ox, oz), written for spheres when
-    double4_32a* soz;              // `orient` is set (no kernel of the step reads a sphere's)
+    double4_32a* sox;              // the orientation arrays (ox, oz), turned for spheres by k_turn
+    double4_32a* soz;              // when `orient` is set (no kernel of the step reads a sphere's)
+    float4* tdav;                  // [n] the step's angular velocity increment, for k_turn
     int orient;
 };
 
@@ -567,6 +568,22 @@ __device__ __noinline__ void wall_pair(const TickArgs& a, int cd, uint32_t pi, u
     rB = fm((float)rb.x, (float)rb.y, (float)rb.z);
 }
 
+// The rare writes of an entry that is certainly apart, out of line: the wall's zero share on an
+// output step, and the cleaning of an owned history that is set or pending.
+__device__ __noinline__ void apart_wall_share(const TickArgs& a, uint32_t e) {
+    float* o = a.wimp + 6 * (size_t)e;
+    o[0] = o[1] = o[2] = o[3] = o[4] = o[5] = 0.0f;
+}
+__device__ __noinline__ bool clean_history(const TickArgs& a, uint32_t e, uint8_t f0) {
+    a.hB[e] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+    if (f0 & 15) {                             // ImpactStatus::Clean
+        a.fB[e] = HF_PENDING;
+        return true;
+    }
+    a.fB[e] = 0;                               // HF_PENDING: both buffers clean again
+    return false;
+}
+
 // Phase 1 of a sphere's neighbour walk, for the group of entries at `base`: the entries and
 // neighbour positions are loaded together (the loads overlap) and the FP32 prefilter settles
 // the pairs that are certainly apart (rebuild-time distance minus both spheres' travel since
@@ -619,21 +636,8 @@ __device__ __forceinline__ uint32_t prefilter_group(const TickArgs& a, uint32_t 
             if (wall) walls |= 1u << k;
             continue;
         }
-        if (wall && a.write_imp) {
-            float* o = a.wimp + 6 * (size_t)e;
-            o[0] = o[1] = o[2] = o[3] = o[4] = o[5] = 0.0f;
-        }
-        if (meta & META_OWNER) {
-            const uint8_t f0 = gf[k];
-            if (f0 & 15) {                     // ImpactStatus::Clean
-                a.hB[e] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
-                a.fB[e] = HF_PENDING;
-                dirty = true;
-            } else if (f0 & HF_PENDING) {
-                a.hB[e] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
-                a.fB[e] = 0;
-            }
-        }
+        if (wall && a.write_imp) apart_wall_share(a, e);
+        if ((meta & META_OWNER) && (gf[k] & (15 | HF_PENDING))) dirty |= clean_history(a, e, gf[k]);
     }
     return exact;
 }
@@ -650,18 +654,6 @@ __device__ __forceinline__ uint32_t prefilter_group(const TickArgs& a, uint32_t 
 __device__ __forceinline__ void note_walk(const TickArgs& a, uint32_t i, uint32_t qc, bool reset) {
     const uint32_t q2 = reset ? 0u : (qc < 2u ? qc + 1u : 2u);
     if (q2 != qc) a.qcnt[i] = (uint8_t)q2;
-}
-
-// DOSphere::Response (DOSphere.cpp:40-44): the orientation turns by dw = dt (w + dav/2) with
-// the angular velocity w before the step and its increment dav (FP32, converted exactly), by
-// Vector3d::rotate_around in FP64 for both axes; a zero turn leaves them.  Out of line: it runs
-// only when the caller asks for orientations.
-__device__ __noinline__ void turn_sphere(const TickArgs& a, uint32_t i, double dt, f3 dav) {
-    const d3 W = ld(a.w64, i);
-    const d3 dwv = smul(dt, add(W, smul(0.5, mk(f2d(dav.x), f2d(dav.y), f2d(dav.z)))));
-    if (dwv.x == 0.0 && dwv.y == 0.0 && dwv.z == 0.0) return;
-    st(a.sox, i, rotate_around(ld(a.sox, i), dwv), 0.0);
-    st(a.soz, i, rotate_around(ld(a.soz, i), dwv), 0.0);
 }
 
 // The end of a sphere's step: field and external impulse join the compensated sum (the
@@ -711,7 +703,7 @@ __device__ __forceinline__ float2 finish_sphere(const TickArgs& a, uint32_t i, b
             a.xsB[2 * i] = h2;
             a.xsB[2 * i + 1] = l2;
         }
-        if (a.orient) turn_sphere(a, i, dt, dw);     // (with the angular velocity before the step)
+        if (a.orient) a.tdav[i] = make_float4(dw.x, dw.y, dw.z, 0.0f);   // for k_turn
         if (dw.x != 0.0f || dw.y != 0.0f || dw.z != 0.0f) {
             const d3 W2 = add(ld(a.w64, i), mk(f2d(dw.x), f2d(dw.y), f2d(dw.z)));
             st(a.w64, i, W2, 0.0);
@@ -1013,6 +1005,25 @@ __global__ void __launch_bounds__(TPB, 6) k_tick_light(TickArgs a) {   // 6 bloc
     reduce_vmax(a, vmax_local);
 }
 
+// DOSphere::Response (DOSphere.cpp:40-44): the orientation turns by dw = dt (w + dav/2) with the
+// angular velocity w before the step and its increment dav, by Vector3d::rotate_around in FP64 for
+// both axes; a zero turn leaves them.  Run after the tick when the caller asks for orientations,
+// from the new angular velocity w + dav and the increment: dt (w + dav - dav/2).
+__global__ void __launch_bounds__(TPB) k_turn(TickArgs a) {
+    step_order();
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (held_step(a) || i >= a.n) return;
+    const ModelDev& M = a.models[a.model_of[i]];
+    const SceneDev& S = a.scenes[a.scene_of[i]];
+    if (M.scope != SCOPE_LOCAL || !S.active || M.behavior != BEH_MOBILE) return;
+    const float4 dav = a.tdav[i];
+    const d3 W2 = ld(a.w64, i);
+    const d3 dwv = smul(S.dt, sub(W2, smul(0.5, mk(f2d(dav.x), f2d(dav.y), f2d(dav.z)))));
+    if (dwv.x == 0.0 && dwv.y == 0.0 && dwv.z == 0.0) return;
+    st(a.sox, i, rotate_around(ld(a.sox, i), dwv), 0.0);
+    st(a.soz, i, rotate_around(ld(a.soz, i), dwv), 0.0);
+}
+
 // ---- pair pass ------------------------------------------------------------------------------
 // The tick in three kernels, each pair on the exact path evaluated once:
 //  k_tick_pf     every sphere's list walk in prefilter form (with the single tick's history
@@ -1151,7 +1162,7 @@ __global__ void __launch_bounds__(TPB, 4) k_tick_pairs(TickArgs a) {     // 64 r
 }
 
 template <bool XS>
-__global__ void __launch_bounds__(TPB, 4) k_tick_sum(TickArgs a) {
+__global__ void __launch_bounds__(TPB, 5) k_tick_sum(TickArgs a) {      // 48 registers: 5 blocks of 256 per SM
     step_order();
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     float2 vmax_local = make_float2(0.0f, 0.0f);
@@ -2407,6 +2418,7 @@ private:
     }
     bool quiet_ok_ = true;                        // quiet spheres skip their walk (identical results)
     bool orient_ = false;                         // integrate the spheres' orientations
+    float4* d_tdav_ = nullptr;                    // [n] angular velocity increments (orientations)
     int sms_ = 1;                                 // streaming multiprocessors of the device
     float2* d_clear_ = nullptr;                   // [n] quiet-sphere pad limits of the current list
     double* d_ext_ = nullptr;                     // [2][n][3] external impulses of run_with_impulses
@@ -2515,7 +2527,7 @@ MixedEngine::~MixedEngine() {
     free_nlist(nl_[1]);
     void* ptrs[] = {d_models_, d_params_, d_pc32_, d_geom_, d_hole_, d_rr_, d_mf_, d_reach_, d_model_of_, d_scene_of_,
                     d_scenes_, d_gfield_, d_glob_, d_x_[0], d_x_[1], d_v64_, d_w64_, d_ox_, d_oz_, d_imp_, d_aimp_,
-                    d_v32_[0], d_v32_[1], d_w32_[0], d_w32_[1], d_rr32_, d_xs_[0], d_xs_[1], d_work_, d_clear_, d_vred_, d_ext_, d_qcnt_, d_pos32_, d_wall32_, d_red_, d_sred_, d_disp_, d_err_,
+                    d_v32_[0], d_v32_[1], d_w32_[0], d_w32_[1], d_rr32_, d_xs_[0], d_xs_[1], d_work_, d_tdav_, d_clear_, d_vred_, d_ext_, d_qcnt_, d_pos32_, d_wall32_, d_red_, d_sred_, d_disp_, d_err_,
                     d_key_, d_key_alt_, d_sid_, d_sid_alt_, d_cnt_, d_gs_, d_ge_, d_act_, d_stage_, d_obs_, d_gidx_,
                     d_wkey_, d_wval_, d_wkey_alt_, d_wval_alt_, d_wptr_, d_wimp_, d_wred_, d_wrot_, d_wedge_, d_ext_of_, d_int_of_, d_xe_, d_model_e_};
     for (void* p : ptrs) if (p) cudaFree(p);
@@ -2742,6 +2754,7 @@ int MixedEngine::init_from(const std::vector<SceneSource>& src, const MixedEngin
     MCK(mal(&d_sred_, 8 * sc_.size()));
     MCK(mal(&d_vred_, 6 * sc_.size()));
     MCK(mal(&d_work_, n_));
+    if (orient_) MCK(mal(&d_tdav_, n_));
 
     MCK(mal(&d_clear_, n_));
     MCK(mal(&d_qcnt_, n_));
@@ -2939,6 +2952,7 @@ TickArgs MixedEngine::args(bool write_imp) {
     a.ext_of = d_ext_of_;
     a.sox = d_ox_;
     a.soz = d_oz_;
+    a.tdav = d_tdav_;
     a.orient = orient_ ? 1 : 0;
     return a;
 }
@@ -3231,6 +3245,10 @@ void MixedEngine::launch_step(bool write_imp) {
     }
 #undef VEDO_TICK
     ++launches_;
+    }
+    if (orient_) {                  // sphere orientations, from the tick's angular velocity increments
+        note(step_launch(dep, k_turn, nblk(n_), TPB, stream_, a));
+        ++launches_;
     }
     if (pe) cudaEventRecordWithFlags(pe[1], stream_, ev_flags_);
     if (write_imp && !glob_.empty()) {

@@ -58,6 +58,9 @@ struct vedo_server {
     std::deque<uint64_t> queue;
     uint64_t next_id = 1;
     uint64_t committed = 0;
+    uint32_t order = VEDO_SRV_FIFO;   // admission order (vedo_srv_set_policy)
+    uint64_t max_live = 0;            // cap on the live jobs' spheres (0: none)
+    uint64_t live_spheres = 0;        // spheres of the admitted, unfinished jobs
     bool stop = false;
     std::thread th;
     std::string err;
@@ -83,6 +86,7 @@ void vedo_server::fail_live(const std::string& msg) {
         j->error = msg;
         j->t_done = now();
         committed -= j->bytes;
+        live_spheres -= j->particles;
         --running;
         j = nullptr;
     }
@@ -159,24 +163,40 @@ void vedo_server::loop() {
                 j->status = VEDO_JOB_CANCELLED;
                 j->t_done = now();
                 committed -= j->bytes;
+                live_spheres -= j->particles;
                 --running;
                 live[s] = nullptr;
                 cv_done.notify_all();
             }
-            // FIFO admission against half the budget (the next batch is built beside the current one)
-            while (!queue.empty()) {
-                Job* j = jobs[queue.front()].get();
-                if (j->status != VEDO_JOB_QUEUED) {
-                    queue.pop_front();
-                    continue;
+            // admission against half the budget (the next batch is built beside the current one) and
+            // the live-sphere cap, in arrival order or shortest work (spheres x steps) first; a job
+            // alone larger than the cap is admitted when nothing else runs
+            for (;;) {
+                while (!queue.empty() && jobs[queue.front()]->status != VEDO_JOB_QUEUED) queue.pop_front();
+                if (queue.empty()) break;
+                size_t pick = 0;
+                if (order == VEDO_SRV_SHORTEST_FIRST) {
+                    double best = -1.0;
+                    for (size_t q = 0; q < queue.size(); ++q) {
+                        const Job* c = jobs[queue[q]].get();
+                        if (c->status != VEDO_JOB_QUEUED) continue;
+                        const double w = (double)c->particles * (double)c->steps;
+                        if (best < 0.0 || w < best) {
+                            best = w;
+                            pick = q;
+                        }
+                    }
                 }
+                Job* j = jobs[queue[pick]].get();
                 if (committed + j->bytes > budget / 2) break;
+                if (max_live && running > 0 && live_spheres + j->particles > max_live) break;
                 committed += j->bytes;
+                live_spheres += j->particles;
                 j->status = VEDO_JOB_RUNNING;
                 j->t_admit = now();
                 ++running;
                 admit.push_back(j);
-                queue.pop_front();
+                queue.erase(queue.begin() + (std::ptrdiff_t)pick);
             }
         }
         uint64_t frozen = 0;
@@ -235,6 +255,7 @@ void vedo_server::loop() {
             if (grc != VEDO_OK) j->error = eng->error();
             j->t_done = now();
             committed -= j->bytes;
+            live_spheres -= j->particles;
             --running;
             jobs_done += 1;
             ps_done += (double)j->particles * (double)j->steps;
@@ -298,6 +319,17 @@ int vedo_srv_create(const vedo_engine_opts* opts, uint64_t hbm_budget_bytes, ved
     s->t0 = Clock::now();
     s->th = std::thread([s] { s->loop(); });
     *out = s;
+    return VEDO_OK;
+}
+
+int vedo_srv_set_policy(vedo_server* s, uint32_t order, uint64_t max_live_spheres) {
+    if (!s || (order != VEDO_SRV_FIFO && order != VEDO_SRV_SHORTEST_FIRST)) return VEDO_ERR_INVALID_ARGUMENT;
+    {
+        std::lock_guard<std::mutex> lk(s->mu);
+        s->order = order;
+        s->max_live = max_live_spheres;
+    }
+    s->cv_work.notify_all();
     return VEDO_OK;
 }
 

@@ -47,6 +47,7 @@ def _srv_lib():
         vp = C.c_void_p
         L.vedo_srv_create.argtypes = [C.POINTER(EngineOpts), C.c_uint64, C.POINTER(vp)]
         L.vedo_srv_submit.argtypes = [vp, C.POINTER(_abi.SceneDesc), C.c_uint64, C.POINTER(C.c_uint64)]
+        L.vedo_srv_set_policy.argtypes = [vp, C.c_uint32, C.c_uint64]
         L.vedo_srv_poll.argtypes = [vp, C.c_uint64, C.POINTER(JobInfo)]
         L.vedo_srv_wait.argtypes = [vp, C.c_uint64, C.c_double, C.POINTER(JobInfo)]
         L.vedo_srv_result.argtypes = [vp, C.c_uint64, C.POINTER(StateView)]
@@ -66,9 +67,14 @@ def _info(ji: JobInfo) -> Dict:
 
 
 class Server:
-    """Continuous-batching DEM job server on one GPU (MIXED form)."""
+    """Continuous-batching DEM job server on one GPU (MIXED form).
 
-    def __init__(self, hbm_budget_bytes: int = 150 * 10**9, device: int = 0, **engine_opts):
+    `order` = "fifo" (admission in arrival order) or "shortest" (the queued job with the least
+    spheres x steps first); `max_live_spheres` caps the spheres of the running jobs (0: no cap
+    beyond the HBM budget)."""
+
+    def __init__(self, hbm_budget_bytes: int = 150 * 10**9, device: int = 0, order: str = "fifo",
+                 max_live_spheres: int = 0, **engine_opts):
         L = _srv_lib()
         opts = _opts(1, 0, _abi.PRECISION_MIXED, device, None, engine_opts.get("skin"),
                      engine_opts.get("check_interval"), engine_opts.get("tick_block"), engine_opts.get("cell_scale"),
@@ -81,6 +87,9 @@ class Server:
             raise EngineError(rc, L.vedo_srv_last_error(None).decode())
         self.h = h
         self.sizes: Dict[int, int] = {}
+        if order not in ("fifo", "shortest"):
+            raise ValueError(f"order must be 'fifo' or 'shortest', not {order!r}")
+        self._check(L.vedo_srv_set_policy(h, 1 if order == "shortest" else 0, int(max_live_spheres)))
 
     def _check(self, rc: int):
         if rc != 0:
