@@ -288,15 +288,18 @@ def test_periodic_layer_at_size_bitexact(engine_lib, port_lib):
     assert np.sum(x < x0[:-1] - 0.5 * (hi - lo)) > 10          # spheres that went out at the upper face
 
 
-def test_periodic_boundary_is_rejected_by_the_mixed_form(engine_lib):
-    """The mixed form (and so batches and serving) does not implement the periodic boundary: a
-    periodic scene is refused with VEDO_ERR_UNSUPPORTED_MODEL rather than run without it."""
-    sc = scenes.periodic_layer()
+def test_mixed_form_refuses_periodic_layouts_it_cannot_run(engine_lib):
+    """The mixed form runs periodic scenes (tests/test_gpu_periodic_mixed.py) but refuses, with
+    VEDO_ERR_UNSUPPORTED_MODEL, a periodic range shorter than three cells of 2 r_max + skin and
+    walls outside the periodic box (the reference's wrap would move them; the mixed form keeps
+    walls where they are)."""
+    small = scenes.periodic_layer(nx=3, ny=3, layers=2, seed=3)       # 3 spheres per period
     with pytest.raises(engine_lib.EngineError) as ex:
-        engine_lib.GpuEngine(sc, precision=1)
+        engine_lib.GpuEngine(small, precision=1, skin=0.5)
     assert ex.value.code == 3
+    walls_out = scenes.periodic_layer(nx=8, ny=8, layers=2, periodic_y=False, side_walls=True, seed=9)
     with pytest.raises(engine_lib.EngineError) as ex:
-        engine_lib.BatchEngine([sc])
+        engine_lib.BatchEngine([walls_out])
     assert ex.value.code == 3
 
 

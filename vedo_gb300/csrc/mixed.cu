@@ -218,6 +218,16 @@ __device__ __forceinline__ dfl df_sq(dfl a) {
     const float p = a.hi * a.hi;
     return two_sum(p, fmaf(a.hi, a.hi, -p) + 2.0f * a.hi * a.lo);
 }
+// The nearest periodic image of a double-float difference on an axis of range L (FP32, 0 = off;
+// Lhi + Llo = the FP64 range): one range off when the difference reaches half of it, as
+// Boundary::DifferenceBoundaryConditions does (pairs that can touch are far from that limit).
+__device__ __forceinline__ dfl df_image(dfl d, float L, float Lhi, float Llo) {
+    if (L == 0.0f) return d;
+    const float v = d.hi + d.lo;
+    if (v >= 0.5f * L) return df_add(d, dfl{-Lhi, -Llo});
+    if (v < -0.5f * L) return df_add(d, dfl{Lhi, Llo});
+    return d;
+}
 
 // x = hi + lo with hi = x rounded to FP32 (nearest, ties to even) and lo = (x - hi) rounded to
 // FP32, from the bits of x with integer operations (GB300's FP64 pipe is its scarcest): for
@@ -299,10 +309,26 @@ struct K3 {
 // The tick's prefilter: certainly_apart (prefilter.cuh) with the positions' rounding bounds
 // precomputed in pos32.w and, for spheres and rods, squared distances (no square root): the
 // squared test carries the same error allowance as the distance test, so it is as conservative.
-__device__ __forceinline__ bool apart32(int cd, const float4& s, const float4& m, const float4& wall, float reach) {
-    const float dx = m.x - s.x, dy = m.y - s.y, dz = m.z - s.z;
-    const float lim = reach * (1.0f + 4.0f * PF_ARITH_EPS) + s.w + m.w;
+// The minimum image of an FP32 difference on an axis of range L (0: no boundary), as a
+// magnitude, and the rounding it adds (the range's and one more subtraction's), as
+// dist32_periodic (prefilter.cuh) bounds it.
+__device__ __forceinline__ float min_image32(float d, float L, float& ext) {
+    if (L == 0.0f) return d;
+    ext += 4.0f * PF_POS_EPS * (fabsf(d) + L);
+    return fminf(fabsf(d), fminf(fabsf(d - L), fabsf(d + L)));
+}
+__device__ __forceinline__ bool apart32(int cd, const float4& s, const float4& m, const float4& wall, float reach,
+                                        const float* L = nullptr) {
+    float dx = m.x - s.x, dy = m.y - s.y, dz = m.z - s.z;
+    float lim = reach * (1.0f + 4.0f * PF_ARITH_EPS) + s.w + m.w;
     if (cd == CD_SS) {
+        if (L) {                                   // a periodic scene: the nearest image
+            float ext = 0.0f;
+            dx = min_image32(dx, L[0], ext);
+            dy = min_image32(dy, L[1], ext);
+            dz = min_image32(dz, L[2], ext);
+            lim += ext;
+        }
         const float d2 = fmaf(dz, dz, fmaf(dy, dy, dx * dx));
         return d2 > lim * lim * (1.0f + 4.0f * PF_ARITH_EPS);
     }
@@ -432,6 +458,11 @@ struct SceneDev {
     // The scene's drifting frame since the last rebuild: velocity u0 + gdt (k + 1/2) in step k
     // (free fall under the scene's field from the spheres' velocity midrange at the rebuild)
     float u0[3], gdt[3];
+    // An active periodic boundary (Boundary.cpp:225-345): the FP64 box for the wrap after each
+    // step and the tie band, its ranges in FP32 (0 where an axis is off) for the prefilter and
+    // the cell grid, and as double-float pairs for the exact path's minimum image
+    Periodic pb;
+    float pr_hi[3], pr_lo[3];
 };
 
 __device__ __forceinline__ uint32_t pidx(const SceneDev& S, uint32_t mg_slave, uint32_t mg_master) {
@@ -546,9 +577,10 @@ __device__ __forceinline__ void hold_state(const TickArgs& a, uint32_t i) {
 // and conversions on its FP64 pipe (2 lanes per cycle per SM), and a short branch kept inline is
 // predicated rather than jumped over, so its FP64 instructions would be issued for every pair.
 // Sphere pair in the tie band: the reference's formula, (ra + rb) - |x_m - x_s| in FP64.
-__device__ __noinline__ double tie_depth(const TickArgs& a, uint32_t pi, uint32_t s, uint32_t m) {
+__device__ __noinline__ double tie_depth(const TickArgs& a, uint32_t pi, uint32_t s, uint32_t m, const Periodic& pb) {
     const double4_32a gg = a.geom[pi];
-    const d3 d = sub(ld(a.xA, m), ld(a.xA, s));
+    d3 d = sub(ld(a.xA, m), ld(a.xA, s));
+    if (pb.on) d = min_image(pb, d);              // CDSphere2Sphere.cpp:19-22
     return __dsub_rn(__dadd_rn(gg.x, gg.y), xlen(d));
 }
 // Sphere-wall pair: the reference's detector in FP64 (wall_detect), the contact normal and
@@ -591,7 +623,8 @@ __device__ __noinline__ bool clean_history(const TickArgs& a, uint32_t e, uint8_
 // entries that need the exact path.  The side effects are idempotent, so a walk that is
 // abandoned and redone (the split tick) leaves the same state.
 __device__ __forceinline__ uint32_t prefilter_group(const TickArgs& a, uint32_t base, uint32_t e1, const float4& p32i,
-                                                    float pad, bool& dirty, uint32_t& owned, uint32_t& walls) {
+                                                    float pad, bool& dirty, uint32_t& owned, uint32_t& walls,
+                                                    const float* L) {
     uint32_t ge[TICK_GROUP], gm[TICK_GROUP];
     uint8_t gf[TICK_GROUP];
     float4 gp[TICK_GROUP];
@@ -630,7 +663,8 @@ __device__ __forceinline__ uint32_t prefilter_group(const TickArgs& a, uint32_t 
             pk = (meta & META_INTERIOR) ? fminf(a.disp[1], a.disp[0] + ws.w) : a.disp[1];
             if (meta & META_MOVING) pk += a.disp[2];
         }
-        if (!apart32(cd, i_slave ? p32i : gp[k], i_slave ? gp[k] : p32i, ws, a.reach[meta & META_PI] + pk)) {
+        if (!apart32(cd, i_slave ? p32i : gp[k], i_slave ? gp[k] : p32i, ws, a.reach[meta & META_PI] + pk,
+                     wall ? nullptr : L)) {
             exact |= 1u << k;
             if (meta & META_OWNER) owned |= 1u << k;
             if (wall) walls |= 1u << k;
@@ -739,9 +773,9 @@ __device__ __forceinline__ float2 finish_sphere(const TickArgs& a, uint32_t i, b
 // into the other buffer, a wall entry writes the wall's share of the impulse.  Returns 0 (nothing
 // added), 1 (impulse J only) or 2 (J and the torques tA on the slave, tB on the master).
 template <int LAW, bool XS>
-__device__ __forceinline__ int exact_pair(const TickArgs& a, uint32_t i, const d3& Pi, uint32_t e, uint32_t ent,
-                                          uint32_t meta,
-                                          float dtf, f3& Jp, f3& tA, f3& tB) {
+__device__ __forceinline__ int exact_pair(const TickArgs& a, const SceneDev& S, uint32_t i, const d3& Pi, uint32_t e,
+                                          uint32_t ent, uint32_t meta, f3& Jp, f3& tA, f3& tB) {
+    const float dtf = S.dtf;
     const uint32_t j = ent & ~WALL_BIT;
     const bool wall = ent & WALL_BIT;
     // canonical orientation (Assembler.cpp:43-67), fixed at rebuild; sphere-wall: the sphere is the slave
@@ -775,8 +809,13 @@ __device__ __forceinline__ int exact_pair(const TickArgs& a, uint32_t i, const d
         }
         const float4 hs = i_slave ? hi_i : hj, ls = i_slave ? lo_i : lj;
         const float4 hm = i_slave ? hj : hi_i, lm = i_slave ? lj : lo_i;
-        const dfl dx = df_diff(hm.x, lm.x, hs.x, ls.x), dy = df_diff(hm.y, lm.y, hs.y, ls.y),
-                  dz = df_diff(hm.z, lm.z, hs.z, ls.z);
+        dfl dx = df_diff(hm.x, lm.x, hs.x, ls.x), dy = df_diff(hm.y, lm.y, hs.y, ls.y),
+            dz = df_diff(hm.z, lm.z, hs.z, ls.z);
+        if (S.pb.on) {                             // a periodic scene: the nearest image
+            dx = df_image(dx, S.pb.range32[0], S.pr_hi[0], S.pr_lo[0]);
+            dy = df_image(dy, S.pb.range32[1], S.pr_hi[1], S.pr_lo[1]);
+            dz = df_image(dz, S.pb.range32[2], S.pr_hi[2], S.pr_lo[2]);
+        }
         const dfl s2 = df_add(df_add(df_sq(dx), df_sq(dy)), df_sq(dz));
         const float4 rq = a.rr32[pi];                // R^2 hi, R^2 lo, band, R
         const dfl num = df_add(dfl{rq.x, rq.y}, dfl{-s2.hi, -s2.lo});
@@ -784,7 +823,7 @@ __device__ __forceinline__ int exact_pair(const TickArgs& a, uint32_t i, const d
             active = num.hi > 0.0f;
             depth = (num.hi + num.lo) / (rq.w + sqrtf(s2.hi));
         } else {                               // tie band: the reference's formula decides
-            const double dex = tie_depth(a, pi, s, m);
+            const double dex = tie_depth(a, pi, s, m, S.pb);
             active = dex > 0.0;
             depth = (float)dex;
         }
@@ -838,7 +877,6 @@ __device__ __forceinline__ float2 tick_sphere(const TickArgs& a, uint32_t i) {
         const ModelDev& M = a.models[mi];
         const SceneDev& S = a.scenes[si];
         if (M.scope == SCOPE_LOCAL && S.active) {
-            const float dtf = S.dtf;
             const float pad = 2.0f * disp;
             const float4 mf0 = a.mf[2 * mi], mf1 = a.mf[2 * mi + 1];
             const bool mobile = M.behavior == BEH_MOBILE;
@@ -857,7 +895,8 @@ __device__ __forceinline__ float2 tick_sphere(const TickArgs& a, uint32_t i) {
                 unsigned long long exact = 0ull;
                 uint32_t owned = 0u, walls = 0u;       // (unused here)
                 for (uint32_t base = c0; base < c1; base += TICK_GROUP)
-                    exact |= (unsigned long long)prefilter_group(a, base, c1, p32i, pad, dirty, owned, walls)
+                    exact |= (unsigned long long)prefilter_group(a, base, c1, p32i, pad, dirty, owned, walls,
+                                                                 S.pb.on ? S.pb.range32 : nullptr)
                              << (base - c0);
                 any_exact |= exact != 0ull;
                 // Phase 2: the exact path for the flagged entries, in entry order
@@ -867,7 +906,7 @@ __device__ __forceinline__ float2 tick_sphere(const TickArgs& a, uint32_t i) {
                     const uint32_t e = c0 + k;
                     const uint32_t meta = a.nmeta[e];
                     f3 Jp, tA, tB;
-                    const int app = exact_pair<LAW, XS>(a, i, Pi, e, a.nent[e], meta, dtf, Jp, tA, tB);
+                    const int app = exact_pair<LAW, XS>(a, S, i, Pi, e, a.nent[e], meta, Jp, tA, tB);
                     if (app) {
                         if (meta & META_SLAVE) {
                             J.add(Jp);
@@ -978,7 +1017,8 @@ __global__ void __launch_bounds__(TPB, 6) k_tick_light(TickArgs a) {   // 6 bloc
                 bool dirty = false;
                 uint32_t owned = 0u, walls = 0u;       // (unused here)
                 for (uint32_t base = e0; base < e1 && !defer; base += TICK_GROUP)
-                    defer = prefilter_group(a, base, e1, p32i, pad, dirty, owned, walls) != 0u;
+                    defer = prefilter_group(a, base, e1, p32i, pad, dirty, owned, walls,
+                                            S.pb.on ? S.pb.range32 : nullptr) != 0u;
                 note_walk(a, i, a.qcnt[i], dirty || defer);    // (reread: fewer live registers in the walk)
             }
             if (!defer) {                          // state loaded after the walk: fewer live registers
@@ -1024,6 +1064,31 @@ __global__ void __launch_bounds__(TPB) k_turn(TickArgs a) {
     st(a.soz, i, rotate_around(ld(a.soz, i), dwv), 0.0);
 }
 
+// SimMediator.cpp:746: after the response every object of a periodic scene goes back into the
+// periodic box (Boundary::EnforceBoundaryConditions, wrap_position); run after the tick, only
+// when a scene is periodic, so that the tick itself carries no FP64 wrap.  A wrapped sphere's
+// position splits are formed anew.
+__global__ void __launch_bounds__(TPB) k_wrap(TickArgs a) {
+    step_order();
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (held_step(a) || i >= a.n) return;
+    const SceneDev& S = a.scenes[a.scene_of[i]];
+    if (!S.pb.on || !S.active || a.models[a.model_of[i]].scope != SCOPE_LOCAL) return;
+    const d3 P = ld(a.xB, i);
+    const d3 W = wrap_position(S.pb, P);
+    if (W.x == P.x && W.y == P.y && W.z == P.z) return;
+    st(a.xB, i, W, 0.0);
+    if (a.xs_stored) {
+        float4 h2, l2;
+        split32(W.x, h2.x, l2.x);
+        split32(W.y, h2.y, l2.y);
+        split32(W.z, h2.z, l2.z);
+        h2.w = l2.w = 0.0f;
+        a.xsB[2 * i] = h2;
+        a.xsB[2 * i + 1] = l2;
+    }
+}
+
 // ---- pair pass ------------------------------------------------------------------------------
 // The tick in three kernels, each pair on the exact path evaluated once:
 //  k_tick_pf     every sphere's list walk in prefilter form (with the single tick's history
@@ -1046,10 +1111,12 @@ __global__ void __launch_bounds__(TPB, 4) k_tick_pf(TickArgs a) {     // 63 regi
     uint32_t c0 = 0u, e0 = 0u, e1 = 0u, qc = 0u;
     float4 p32i = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
     float pad = 0.0f;
+    const float* L = nullptr;
     bool walk = false, dirty = false, any_exact = false;
     if (i < a.n) {
         const ModelDev& M = a.models[a.model_of[i]];
         const SceneDev& S = a.scenes[a.scene_of[i]];
+        if (S.pb.on) L = S.pb.range32;
         if (M.scope == SCOPE_LOCAL && S.active) {
             qc = a.qcnt[i];
             const float2 cl = a.clear[i];
@@ -1076,7 +1143,7 @@ __global__ void __launch_bounds__(TPB, 4) k_tick_pf(TickArgs a) {     // 63 regi
             unsigned long long exact = 0ull;
             for (uint32_t base = c0; base < c1; base += TICK_GROUP) {
                 uint32_t owned = 0u, walls = 0u;
-                exact |= (unsigned long long)prefilter_group(a, base, c1, p32i, pad, dirty, owned, walls)
+                exact |= (unsigned long long)prefilter_group(a, base, c1, p32i, pad, dirty, owned, walls, L)
                          << (base - c0);
                 own |= (unsigned long long)(owned & ~walls) << (base - c0);
                 wown |= (unsigned long long)(owned & walls) << (base - c0);
@@ -1135,7 +1202,7 @@ __device__ __forceinline__ void pair_item(const TickArgs& a, const uint4& it) {
     const uint32_t e = it.x, i = it.y, ent = it.z, meta = it.w;
     const d3 Pi = XS ? mk(0.0, 0.0, 0.0) : ld(a.xA, i);
     f3 Jp, tA, tB;
-    const int app = exact_pair<LAW, XS>(a, i, Pi, e, ent, meta, a.scenes[a.scene_of[i]].dtf, Jp, tA, tB);
+    const int app = exact_pair<LAW, XS>(a, a.scenes[a.scene_of[i]], i, Pi, e, ent, meta, Jp, tA, tB);
     // each member's share at its own entry: the slave adds J and tA, the master -J and tB
     // (the negation is exact, so the sums see the single tick's values)
     const bool i_slave = meta & META_SLAVE;
@@ -1433,10 +1500,17 @@ __global__ void __launch_bounds__(TPB) k_keys(uint32_t n, const uint32_t* __rest
     if (models[model_of[i]].scope == SCOPE_LOCAL) {
         const SceneDev& S = scenes[scene_of[i]];
         const float4 p = pos32[i];
-        const uint32_t cx = min((uint32_t)fmaxf((p.x - S.lo[0]) * S.inv_h, 0.0f), S.nc[0] - 1);
-        const uint32_t cy = min((uint32_t)fmaxf((p.y - S.lo[1]) * S.inv_h, 0.0f), S.nc[1] - 1);
-        const uint32_t cz = min((uint32_t)fmaxf((p.z - S.lo[2]) * S.inv_h, 0.0f), S.nc[2] - 1);
-        k = S.cell_base + ((uint64_t)cx * S.nc[1] + cy) * S.nc[2] + cz;
+        const float pc[3] = {p.x, p.y, p.z};
+        uint32_t c[3];
+        for (int a = 0; a < 3; ++a) {
+            float u = pc[a] - S.lo[a];
+            if (S.pb.sw[a]) {                      // periodic axis: the image inside the box
+                const float L = S.pb.range32[a];
+                u -= L * floorf(u / L);
+            }
+            c[a] = min((uint32_t)fmaxf(u * S.inv_h, 0.0f), S.nc[a] - 1);
+        }
+        k = S.cell_base + ((uint64_t)c[0] * S.nc[1] + c[1]) * S.nc[2] + c[2];
     }
     key[i] = k;
     sid[i] = i;
@@ -1479,13 +1553,24 @@ __global__ void __launch_bounds__(TPB) k_nbr(uint32_t nloc, const uint32_t* __re
     // the fill pass knows the sphere's count from the scanned pointers: it stops once every entry
     // is found (the entries are put in canonical order below, whatever order they were found in)
     const uint32_t want = FILL ? cnt_or_ptr[i + 1] - off : 0xffffffffu;
+    // a neighbour cell index on an axis, wrapping on a periodic one (at least three cells: the
+    // three are distinct); 0xffffffff outside a bounded grid
+    auto ncell = [&](int a, uint32_t cc, uint32_t nn, int d) -> uint32_t {
+        if (S.pb.sw[a]) return (cc + nn + (uint32_t)(d + 1) - 1u) % nn;
+        if ((d < 0 && cc == 0) || (d > 0 && cc + 1 >= nn)) return 0xffffffffu;
+        return cc + (uint32_t)d;
+    };
+    const float* L = S.pb.on ? S.pb.range32 : nullptr;
     for (int dx = -1; dx <= 1 && c < want; ++dx) {
-        if ((dx < 0 && cx == 0) || (dx > 0 && cx + 1 >= nx)) continue;
+        const uint32_t xx = ncell(0, cx, nx, dx);
+        if (xx == 0xffffffffu) continue;
         for (int dy = -1; dy <= 1 && c < want; ++dy) {
-            if ((dy < 0 && cy == 0) || (dy > 0 && cy + 1 >= ny)) continue;
+            const uint32_t yy = ncell(1, cy, ny, dy);
+            if (yy == 0xffffffffu) continue;
             for (int dz = -1; dz <= 1 && c < want; ++dz) {
-                if ((dz < 0 && cz == 0) || (dz > 0 && cz + 1 >= nz)) continue;
-                const uint64_t nk = S.cell_base + ((uint64_t)(cx + dx) * ny + (cy + dy)) * nz + (cz + dz);
+                const uint32_t zz = ncell(2, cz, nz, dz);
+                if (zz == 0xffffffffu) continue;
+                const uint64_t nk = S.cell_base + ((uint64_t)xx * ny + yy) * nz + zz;
                 const uint32_t b = grid_start[nk], e = grid_end[nk];
                 for (uint32_t q = b; q < e && c < want; ++q) {
                     const uint32_t j = sid[q];
@@ -1495,7 +1580,7 @@ __global__ void __launch_bounds__(TPB) k_nbr(uint32_t nloc, const uint32_t* __re
                     if (params[pa].cd == 0 && params[pb].cd == 0) continue;
                     const float r = fmaxf(reach[pa], reach[pb]);
                     float err;
-                    const float d = dist32(pi, pos32[j], err);
+                    const float d = L ? dist32_periodic(pi, pos32[j], L, err) : dist32(pi, pos32[j], err);
                     if (d - err > (r + skin) * (1.0f + 4.0f * PF_ARITH_EPS)) continue;
                     if (FILL) ent[off + c] = ext_of[j];          // sorted below by the caller's index
                     ++c;
@@ -1669,12 +1754,14 @@ __global__ void __launch_bounds__(TPB) k_clear(uint32_t n, const uint32_t* __res
                                                const uint32_t* __restrict__ model_of,
                                                const ModelDev* __restrict__ models, const float4* __restrict__ pos32,
                                                const float4* __restrict__ wall32, const float* __restrict__ reach,
-                                               float2* __restrict__ clear, uint8_t* __restrict__ qcnt, int enable) {
+                                               float2* __restrict__ clear, uint8_t* __restrict__ qcnt, int enable,
+                                               const uint32_t* __restrict__ scene_of, const SceneDev* __restrict__ scenes) {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     qcnt[i] = 0;
     float c = -1.0f, cw = -1.0f;                   // sphere pairs, fixed walls
-    if (enable && models[model_of[i]].scope == SCOPE_LOCAL) {
+    // (the spheres of a periodic scene always walk their lists: these limits use plain differences)
+    if (enable && models[model_of[i]].scope == SCOPE_LOCAL && !scenes[scene_of[i]].pb.on) {
         c = cw = 3.0e38f;
         const float4 pi = pos32[i];
         for (uint32_t e = ptr[i]; e < ptr[i + 1]; ++e) {
@@ -2311,6 +2398,7 @@ private:
         // the scene's objects in the engine's storage order: perm[internal] = the caller's
         // scene-local index (spatial_order)
         std::shared_ptr<const std::vector<uint32_t>> perm;
+        Periodic pb{};              // the scene's periodic boundary (on = 0: none)
     };
     int fail(int c, const std::string& m) { err_ = m; return c; }
     int cuda_fail(cudaError_t e, const char* where) {
@@ -2418,6 +2506,7 @@ private:
     }
     bool quiet_ok_ = true;                        // quiet spheres skip their walk (identical results)
     bool orient_ = false;                         // integrate the spheres' orientations
+    bool any_pbc_ = false;                        // a scene has a periodic boundary
     float4* d_tdav_ = nullptr;                    // [n] angular velocity increments (orientations)
     int sms_ = 1;                                 // streaming multiprocessors of the device
     float2* d_clear_ = nullptr;                   // [n] quiet-sphere pad limits of the current list
@@ -2604,9 +2693,31 @@ int MixedEngine::init_from(const std::vector<SceneSource>& src, const MixedEngin
         std::string msg;
         int rc = build_tables(h, t, msg);
         if (rc != VEDO_OK) return fail(rc, msg);
-        if (t.pbc.on)        // the plain FP64 form runs periodic scenes
-            return fail(VEDO_ERR_UNSUPPORTED_MODEL, "periodic boundary conditions: the mixed form does not implement them");
         SceneHost S;
+        S.pb = t.pbc;
+        if (t.pbc.on) {
+            // Periodic scenes: sphere pairs take the nearest image and mobile spheres go back into
+            // the box after every step.  Walls and spheres that do not move stay where they are,
+            // which the reference's wrap agrees with only inside the box: other layouts are refused.
+            for (uint32_t i = 0; i < h.n; ++i) {
+                const ModelDev& M = t.models[h.model_of[i]];
+                const bool moves = M.scope == SCOPE_LOCAL && M.behavior == BEH_MOBILE;
+                bool inside = true;
+                for (int k = 0; k < 3; ++k) {
+                    const double p = h.pos[3 * (size_t)i + k];
+                    if (t.pbc.sw[k] && (p < t.pbc.lo[k] || p >= t.pbc.hi[k])) inside = false;
+                }
+                if (!moves && !inside)
+                    return fail(VEDO_ERR_UNSUPPORTED_MODEL, "mixed form, periodic boundary: a wall or a sphere that does "
+                                                            "not move lies outside the periodic box");
+                if (M.scope != SCOPE_LOCAL && M.behavior == BEH_ORBITAL)
+                    for (int k = 0; k < 3; ++k)
+                        if (t.pbc.sw[k] && h.vel[3 * (size_t)i + k] != 0.0)
+                            return fail(VEDO_ERR_UNSUPPORTED_MODEL, "mixed form, periodic boundary: an orbital wall "
+                                                                    "moves along a periodic axis");
+            }
+            any_pbc_ = true;
+        }
         S.obj_off = n_;
         S.nobj = h.n;
         S.model_off = nm_;
@@ -3000,6 +3111,12 @@ int MixedEngine::rebuild() {
         D.active = H.active ? 1u : 0u;
         D.dt = H.dt;
         D.dtf = (float)H.dt;
+        D.pb = H.pb;
+        for (int k = 0; k < 3; ++k) {
+            const float hi = (float)H.pb.range[k];
+            D.pr_hi[k] = H.pb.sw[k] ? hi : 0.0f;
+            D.pr_lo[k] = H.pb.sw[k] ? (float)(H.pb.range[k] - (double)hi) : 0.0f;
+        }
         // the frame: free fall under the scene's field from its spheres' velocity midrange
         const bool moving = vred[6 * s] != 0xffffffffu;
         for (int k = 0; k < 3; ++k) {
@@ -3021,11 +3138,27 @@ int MixedEngine::rebuild() {
         if (!(h > 0.0f)) h = 1.0f;
         const uint64_t budget = std::max<uint64_t>(8ull * std::max<uint32_t>(H.nobj, 1), 1ull << 12);
         uint32_t nc[3] = {1, 1, 1};
+        // a periodic axis: the grid spans the box, ranges of at least one cell edge each, and the
+        // cells wrap around (k_keys, k_nbr)
+        for (int k = 0; k < 3; ++k)
+            if (H.pb.sw[k]) lo[k] = (float)(H.pb.lo[k] - origin_[k]);
+        // a periodic axis holds at least three cells (the three neighbour cells are then distinct):
+        // the cells may be made no wider than a third of the shortest periodic range
+        const float hmin = (2.0f * rmax + H.skin) * (1.0f + 1e-5f);
+        float hcap = 3.0e38f;
+        for (int k = 0; k < 3; ++k)
+            if (H.pb.sw[k]) hcap = std::min(hcap, H.pb.range32[k] / 3.0f);
+        if (hmin > hcap)
+            return fail(VEDO_ERR_UNSUPPORTED_MODEL, "mixed form, periodic boundary: a periodic range shorter than "
+                                                    "three times 2 r_max + skin");
+        h = std::min(h, hcap);
         for (int pass = 0; pass < 8; ++pass) {
-            for (int k = 0; k < 3; ++k) nc[k] = std::max<uint32_t>(1, (uint32_t)std::floor((hi[k] - lo[k]) / h) + 1);
+            for (int k = 0; k < 3; ++k)
+                nc[k] = H.pb.sw[k] ? std::max<uint32_t>(3, (uint32_t)std::floor(H.pb.range32[k] / h))
+                                   : std::max<uint32_t>(1, (uint32_t)std::floor((hi[k] - lo[k]) / h) + 1);
             const uint64_t c = (uint64_t)nc[0] * nc[1] * nc[2];
-            if (c <= budget) break;
-            h *= (float)std::cbrt((double)c / budget) * 1.01f;   // sparse scene: coarser cells
+            if (c <= budget || h >= hcap) break;
+            h = std::min(hcap, h * (float)std::cbrt((double)c / budget) * 1.01f);   // sparse scene: coarser cells
         }
         for (int k = 0; k < 3; ++k) {
             D.nc[k] = nc[k];
@@ -3098,7 +3231,7 @@ int MixedEngine::rebuild() {
     k_interior<<<nblk(n_), TPB, 0, stream_>>>(n_, L.ptr, L.ent, L.meta, d_model_of_, d_models_, d_x_[cur_], d_ox_,
                                               d_oz_, skin_min_, WALL_SKIN * skin_min_);
     k_clear<<<nblk(n_), TPB, 0, stream_>>>(n_, L.ptr, L.ent, L.meta, d_model_of_, d_models_, d_pos32_, d_wall32_,
-                                           d_reach_, d_clear_, d_qcnt_, quiet_ok_ ? 1 : 0);
+                                           d_reach_, d_clear_, d_qcnt_, quiet_ok_ ? 1 : 0, d_scene_of_, d_scenes_);
     own += 3;
     // per-wall entry lists for the wall impulse output
     if (!glob_.empty()) {
@@ -3245,6 +3378,10 @@ void MixedEngine::launch_step(bool write_imp) {
     }
 #undef VEDO_TICK
     ++launches_;
+    }
+    if (any_pbc_) {                 // periodic scenes: spheres back into the box
+        note(step_launch(dep, k_wrap, nblk(n_), TPB, stream_, a));
+        ++launches_;
     }
     if (orient_) {                  // sphere orientations, from the tick's angular velocity increments
         note(step_launch(dep, k_turn, nblk(n_), TPB, stream_, a));
@@ -3471,6 +3608,11 @@ int MixedEngine::autotune(uint32_t max_steps, uint32_t* taken) {
     best = FLT_MAX;
     float best_skin = skin_frac_;
     for (float f : skins) {
+        bool fits = true;                   // a periodic range must hold three cells of 2 r_max + skin
+        for (const SceneHost& H : sc_)
+            for (int k = 0; k < 3; ++k)
+                if (H.pb.sw[k] && (2.0f + f) * H.rmax * (1.0f + 1e-5f) > H.pb.range32[k] / 3.0f) fits = false;
+        if (!fits) continue;
         set_skin(f);
         // what a rebuild costs: the rebuild, then the first chunk of the new list (its steps walk
         // every list while the clean-walk counts settle, and its graph is captured)
