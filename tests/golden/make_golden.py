@@ -42,6 +42,10 @@ def cases():
     yield "leap_zoi", leap_zoi_scene(), 1500, 5
     yield "leap_zoi_h", leap_zoi_scene(solver="ISwH", seed=19), 1000, 5
     yield "holed_plate_lsd", scenes.holed_plate_drop(steps=500), 400, 5
+    # a lid on the cluster moved by its impulses: a mobile plate (translation and rotation,
+    # DOQuasiPlate.cpp:20-41) and a constrained one (along its normal, DOConstrainedQuasiPlate.cpp:18-35)
+    yield "piston_mobile_lsd", scenes.piston(behavior="mobile", solver="ISwBSDBF"), 600, 5
+    yield "piston_constrained_h", scenes.piston(behavior="constrained", solver="ISwH"), 600, 5
     # periodic boundary: spheres drift across the faces (wrap, minimum image in the detector and
     # in every law's lever arms); ISwH with an orbital floor and side walls that the wrap moves
     yield "periodic_lsd", scenes.periodic_layer(solver="ISwBSDBF"), 400, 5

@@ -257,6 +257,33 @@ def cluster(n: int = 64, seed: int = 7, solver: str = "ISwBSDBF", walls: str = "
     return sc
 
 
+def piston(n: int = 48, seed: int = 11, solver: str = "ISwBSDBF", behavior: str = "mobile", steps: int = 1000,
+           dt: float = 1e-6, speed: float = 0.5, spin: float = 4.0, lid_density: float = 2500.0) -> Scene:
+    """The colliding cluster of :func:`cluster` in its box of fixed plates, under a lid: a plate
+    (2 mm thick) that is a mobile quasi-plate (`behavior` "mobile": DOQuasiPlate, moved by its
+    impulses in translation and rotation) or a constrained one ("constrained":
+    DOConstrainedQuasiPlate, moved only along its normal), starting 0.2 mm above the top layer at
+    `speed` m/s downwards (and turning at `spin` rad/s about a horizontal axis when mobile), falling
+    under gravity onto the spheres and pushed back by them."""
+    sc = cluster(n=n, seed=seed, solver=solver, steps=steps, dt=dt)
+    sph = np.array([sc.models[m].shape == SPHERE for m in sc.model_index])
+    radius = sc.models[0].attrs[0]
+    top = float(sc.position[sph, 2].max()) + radius
+    side = int(math.ceil(n ** (1.0 / 3.0)))
+    inner = side * 2.05e-3 + 4 * radius
+    w = inner - 2.0 * radius                       # clear of the side plates
+    beh = {"mobile": MOBILE, "constrained": CONSTRAINED}[behavior]
+    models = list(sc.models) + [DOModel("Lid", "Lid", beh, GLOBAL, lid_density, 1.0, QUASI_PLATE, (w, 2e-3, w))]
+    lid = len(models) - 1
+    zeta = damping_ratio(0.7)
+    iacts = list(sc.iact_models) + [IactModel("Lid", "B0", solver, _mechanisms(solver, zeta, 0.5))]
+    app = lambda a, row: np.concatenate([a, np.asarray([row], dtype=np.float64)])   # noqa: E731
+    return Scene(sc.sp, models, iacts, np.concatenate([sc.model_index, np.array([lid], np.uint32)]),
+                 app(sc.position, [0.0, 0.0, top + 2e-4 + 1e-3]), app(sc.velocity, [0.0, 0.0, -speed]),
+                 app(sc.orientation_x, [1.0, 0.0, 0.0]), app(sc.orientation_z, [0.0, 0.0, 1.0]),
+                 app(sc.angular_velocity, [spin if behavior == "mobile" else 0.0, 0.0, 0.0]))
+
+
 def _mechanisms(solver: str, zeta: float, mu: float):
     if solver in ("ISwBSDBF", "ISwBtSDBF", "ISwBSDB2F"):
         return lsd_mechanisms(1e4, 8e3, zeta, zeta, mu)
