@@ -92,16 +92,48 @@ def test_mixed_matches_oracle_trajectory_start(engine_lib, port_lib):
     assert np.abs(a["position"] - b["position"]).max() <= 1e-9
 
 
-def test_mixed_rejects_mobile_walls(engine_lib):
-    from vedo_gb300.scene import MOBILE
-    sc = scenes.cluster(n=8)
-    for m in sc.models:
-        if m.group == "Wall":
-            m.behavior = MOBILE
-            m.density = 1000.0
-    with pytest.raises(engine_lib.EngineError) as ex:
-        engine_lib.GpuEngine(sc, precision=1)
-    assert ex.value.code == 3
+@pytest.mark.parametrize("behavior,solver", [("mobile", "ISwBSDBF"), ("constrained", "ISwH")])
+def test_mixed_mobile_and_constrained_walls_against_fp64(behavior, solver, engine_lib):
+    """A lid moved by its impulses (a mobile plate: translation and rotation; a constrained one:
+    along its normal) in the mixed form: the wall shares are summed exactly every step and the
+    lid responds as the FP64 form's respond_object.  From the FP64 form's state at step 150 (lid
+    in contact): identical contact sets, the lid's and the spheres' step impulses within 1e-5,
+    and after 300 more steps the lid within 1e-7 m and 1e-4 relative in velocity of the FP64
+    form's; every form of the tick gives the same bits."""
+    import os
+    import tempfile
+    sc = scenes.piston(behavior=behavior, solver=solver, steps=3000)
+    lid = sc.num_objects - 1
+    f64 = engine_lib.GpuEngine(sc, up_iact=5)
+    f64.run(150)
+    with tempfile.TemporaryDirectory() as td:
+        path = os.path.join(td, "p.ido")
+        f64.write_ido(path)
+        a = engine_lib.GpuEngine(path, up_iact=5)
+        forms = [engine_lib.GpuEngine(path, up_iact=5, precision=1, **kw)
+                 for kw in ({}, {"split_tick": True}, {"pair_pass": True}, {"skin": 0.02, "check_interval": 1})]
+    b = forms[0]
+    A, B = _active_set(a.interactions()), _active_set(b.interactions())
+    assert A == B and any(lid in p for p in A)
+    a.run(1)
+    for e in forms:
+        e.run(1)
+    sa, sb = a.state(), b.state()
+    for k in ("impact", "angular_impact"):
+        ref = np.linalg.norm(sa[k])
+        assert np.linalg.norm(sa[k] - sb[k]) <= 1e-5 * ref, k
+    assert np.linalg.norm(sa["impact"][lid] - sb["impact"][lid]) <= 1e-5 * np.linalg.norm(sa["impact"][lid])
+    a.run(300)
+    for e in forms:
+        e.run(300)
+    sa, sb = a.state(), b.state()
+    assert np.abs(sa["position"][lid] - sb["position"][lid]).max() <= 1e-7
+    assert np.linalg.norm(sa["velocity"][lid] - sb["velocity"][lid]) <= 1e-4 * np.linalg.norm(sa["velocity"][lid])
+    assert abs(sa["position"][lid][2] - sc.position[lid][2]) > 1e-5          # the lid did move
+    for e in forms[1:]:
+        st = e.state()
+        for k in ("position", "velocity", "angular_velocity", "orientation_x", "orientation_z"):
+            assert np.array_equal(st[k], sb[k]), k
 
 
 @pytest.mark.parametrize("which", ["dense", "box"])

@@ -501,6 +501,8 @@ struct TickArgs {
     double4_32a* imp;
     double4_32a* aimp;
     int write_imp;
+    int wimp_on;                   // write the wall shares (output steps, and every step of an engine
+                                   // with mobile or constrained walls)
     unsigned* vmax_bits;
     const float4* pos32;           // positions at the last rebuild (FP32 offsets)
     // [4]: bounds since the rebuild on any sphere's displacement relative to its scene's frame,
@@ -622,6 +624,7 @@ __device__ __noinline__ bool clean_history(const TickArgs& a, uint32_t e, uint8_
 // then): their history is cleaned and their wall-impulse share zeroed.  Returns the mask of
 // entries that need the exact path.  The side effects are idempotent, so a walk that is
 // abandoned and redone (the split tick) leaves the same state.
+template <bool PBC>
 __device__ __forceinline__ uint32_t prefilter_group(const TickArgs& a, uint32_t base, uint32_t e1, const float4& p32i,
                                                     float pad, bool& dirty, uint32_t& owned, uint32_t& walls,
                                                     const float* L) {
@@ -664,16 +667,25 @@ __device__ __forceinline__ uint32_t prefilter_group(const TickArgs& a, uint32_t 
             if (meta & META_MOVING) pk += a.disp[2];
         }
         if (!apart32(cd, i_slave ? p32i : gp[k], i_slave ? gp[k] : p32i, ws, a.reach[meta & META_PI] + pk,
-                     wall ? nullptr : L)) {
+                     PBC && !wall ? L : nullptr)) {
             exact |= 1u << k;
             if (meta & META_OWNER) owned |= 1u << k;
             if (wall) walls |= 1u << k;
             continue;
         }
-        if (wall && a.write_imp) apart_wall_share(a, e);
+        if (wall && a.wimp_on) apart_wall_share(a, e);
         if ((meta & META_OWNER) && (gf[k] & (15 | HF_PENDING))) dirty |= clean_history(a, e, gf[k]);
     }
     return exact;
+}
+
+// The group's prefilter with the periodic image only where the scene has a periodic boundary
+// (a separate instance: the common path carries none of it).
+__device__ __forceinline__ uint32_t prefilter_any(const TickArgs& a, uint32_t base, uint32_t e1, const float4& p32i,
+                                                  float pad, bool& dirty, uint32_t& owned, uint32_t& walls,
+                                                  const float* L) {
+    return L ? prefilter_group<true>(a, base, e1, p32i, pad, dirty, owned, walls, L)
+             : prefilter_group<false>(a, base, e1, p32i, pad, dirty, owned, walls, nullptr);
 }
 
 // Quiet spheres.  Between rebuilds a sphere's list, the rebuild-time positions and the fixed
@@ -851,7 +863,7 @@ __device__ __forceinline__ int exact_pair(const TickArgs& a, const SceneDev& S, 
             a.fB[slot] = 0;
         }
     }
-    if (wall && a.write_imp) {                 // the wall's share, summed per wall later
+    if (wall && a.wimp_on) {                   // the wall's share, summed per wall later
         float* o = a.wimp + 6 * (size_t)e;
         o[0] = app ? -Jp.x : 0.0f; o[1] = app ? -Jp.y : 0.0f; o[2] = app ? -Jp.z : 0.0f;
         o[3] = app == 2 ? tB.x : 0.0f; o[4] = app == 2 ? tB.y : 0.0f; o[5] = app == 2 ? tB.z : 0.0f;
@@ -895,8 +907,8 @@ __device__ __forceinline__ float2 tick_sphere(const TickArgs& a, uint32_t i) {
                 unsigned long long exact = 0ull;
                 uint32_t owned = 0u, walls = 0u;       // (unused here)
                 for (uint32_t base = c0; base < c1; base += TICK_GROUP)
-                    exact |= (unsigned long long)prefilter_group(a, base, c1, p32i, pad, dirty, owned, walls,
-                                                                 S.pb.on ? S.pb.range32 : nullptr)
+                    exact |= (unsigned long long)prefilter_any(a, base, c1, p32i, pad, dirty, owned, walls,
+                                                               S.pb.on ? S.pb.range32 : nullptr)
                              << (base - c0);
                 any_exact |= exact != 0ull;
                 // Phase 2: the exact path for the flagged entries, in entry order
@@ -1016,9 +1028,10 @@ __global__ void __launch_bounds__(TPB, 6) k_tick_light(TickArgs a) {   // 6 bloc
                 const float4 p32i = a.pos32[i];
                 bool dirty = false;
                 uint32_t owned = 0u, walls = 0u;       // (unused here)
+                // a periodic scene's spheres go to the full tick, whose prefilter takes the images
+                defer = S.pb.on != 0;
                 for (uint32_t base = e0; base < e1 && !defer; base += TICK_GROUP)
-                    defer = prefilter_group(a, base, e1, p32i, pad, dirty, owned, walls,
-                                            S.pb.on ? S.pb.range32 : nullptr) != 0u;
+                    defer = prefilter_group<false>(a, base, e1, p32i, pad, dirty, owned, walls, nullptr) != 0u;
                 note_walk(a, i, a.qcnt[i], dirty || defer);    // (reread: fewer live registers in the walk)
             }
             if (!defer) {                          // state loaded after the walk: fewer live registers
@@ -1143,7 +1156,7 @@ __global__ void __launch_bounds__(TPB, 4) k_tick_pf(TickArgs a) {     // 63 regi
             unsigned long long exact = 0ull;
             for (uint32_t base = c0; base < c1; base += TICK_GROUP) {
                 uint32_t owned = 0u, walls = 0u;
-                exact |= (unsigned long long)prefilter_group(a, base, c1, p32i, pad, dirty, owned, walls, L)
+                exact |= (unsigned long long)prefilter_any(a, base, c1, p32i, pad, dirty, owned, walls, L)
                          << (base - c0);
                 own |= (unsigned long long)(owned & ~walls) << (base - c0);
                 wown |= (unsigned long long)(owned & walls) << (base - c0);
@@ -1327,15 +1340,17 @@ __global__ void k_wall_rot(uint32_t nglob, const uint32_t* __restrict__ glob, co
 __global__ void k_walls(uint32_t nglob, const uint32_t* __restrict__ glob, const uint32_t* __restrict__ model_of,
                         const ModelDev* __restrict__ models, const SceneDev* __restrict__ scenes,
                         const uint32_t* __restrict__ scene_of, const double4_32a* __restrict__ xA,
-                        double4_32a* __restrict__ xB, const double4_32a* __restrict__ v64,
-                        const double4_32a* __restrict__ w64, const float4* __restrict__ v32A,
+                        double4_32a* __restrict__ xB, double4_32a* __restrict__ v64,
+                        double4_32a* __restrict__ w64, const float4* __restrict__ v32A,
                         float4* __restrict__ v32B, const float4* __restrict__ w32A, float4* __restrict__ w32B,
                         double4_32a* __restrict__ ox, double4_32a* __restrict__ oz, float dt_max,
                         unsigned* __restrict__ vmax_bits, unsigned* __restrict__ vrel_bits,
                         const float* __restrict__ disp_in, float* __restrict__ disp_out, float skin, float skin_w,
                         float pos_eps, const unsigned* __restrict__ wall_speed_bits,
                         const double4_32a* __restrict__ wrot,
-                        unsigned* __restrict__ held, float4* __restrict__ wall32, unsigned* __restrict__ nwork) {
+                        unsigned* __restrict__ held, float4* __restrict__ wall32, unsigned* __restrict__ nwork,
+                        const double4_32a* __restrict__ imp, const double4_32a* __restrict__ aimp,
+                        unsigned* __restrict__ dyn_bits) {
     step_order();
     const uint32_t q = blockIdx.x * blockDim.x + threadIdx.x;
     const float drel = disp_in[0], dabs = disp_in[1], dw = disp_in[2];
@@ -1370,12 +1385,55 @@ __global__ void k_walls(uint32_t nglob, const uint32_t* __restrict__ glob, const
     const double dt = S.dt;
     const uint32_t k1 = __float_as_uint(disp_in[3]) + 1u;     // steps since the rebuild, after this one
     d3 P = ld(xA, w);
-    if (M.behavior != BEH_ORBITAL) {
+    if (M.behavior == BEH_FIXED) {
         float4 ws = wall32[w];
         if (ws.w != 0.0f) {
             ws.w = frame_drift_across(S, k1, M.shape, ws.x, ws.y, ws.z);
             wall32[w] = ws;
         }
+    } else if (M.behavior != BEH_ORBITAL) {
+        // a mobile or constrained wall moved by its impulses this step (summed exactly by
+        // k_wall_max/acc/fin, field and external force included), as the FP64 form's
+        // respond_object: DOQuasiPlate.cpp:20-41 / DOConstrainedQuasiPlate.cpp:18-35
+        const d3 J = ld(imp, w), JA = ld(aimp, w);
+        d3 V = ld(v64, w), AV = ld(w64, w), Ox = ld(ox, w), Oz = ld(oz, w);
+        const d3 P0 = P;
+        d3 dw;
+        if (M.behavior == BEH_CONSTRAINED) {
+            const d3 dv = smul(M.inv_sudo, smul(dot(J, Oz), dir(Oz)));
+            P = add(P, smul(dt, add(V, smul(0.5, dv))));
+            dw = muls(AV, dt);
+            V = add(V, dv);
+        } else {
+            const d3 dv = smul(M.inv_sudo, J);
+            const d3 dav = mk(dot(JA, Ox) / M.ix, dot(JA, cross(Oz, Ox)) / M.iy, dot(JA, Oz) / M.iz);
+            P = add(P, smul(dt, add(V, smul(0.5, dv))));
+            dw = smul(dt, add(AV, smul(0.5, dav)));
+            V = add(V, dv);
+            AV = add(AV, dav);
+        }
+        Ox = rotate_around(Ox, dw);
+        Oz = rotate_around(Oz, dw);
+        st(ox, w, Ox, 0.0);
+        st(oz, w, Oz, 0.0);
+        st(v64, w, V, 0.0);
+        st(w64, w, AV, 0.0);
+        st(xB, w, P, 0.0);
+        v32B[w] = make_float4((float)V.x, (float)V.y, (float)V.z, 0.0f);
+        w32B[w] = make_float4((float)AV.x, (float)AV.y, (float)AV.z, 0.0f);
+        const double lz = len(Oz), lx = len(Ox);
+        bool ok = lz > 0.0;
+        if (M.shape == SHAPE_PLATE || M.shape == SHAPE_HOLED) ok = ok && lx > 0.0 && fabs(dot(Ox, Oz)) <= 1e-9 * lx * lz;
+        const float nx = (float)(Oz.x / lz), ny = (float)(Oz.y / lz), nz = (float)(Oz.z / lz);
+        wall32[w] = ok ? make_float4(nx, ny, nz, frame_drift_across(S, k1, M.shape, nx, ny, nz))
+                       : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+        // how far any point of the wall went this step: its centre's travel and the turn of its
+        // farthest point (k_wall_bound adds the largest to the walls' displacement bound)
+        const double R = M.shape == SHAPE_INNER_CYL ? sqrt(M.a0 * M.a0 + 0.25 * M.a1 * M.a1)
+                                                    : 0.5 * sqrt(M.a0 * M.a0 + M.a1 * M.a1 + M.a2 * M.a2);
+        const double d = len(sub(P, P0)) + len(dw) * R;
+        atomicMax(dyn_bits, __float_as_uint((float)(d * 1.0001) + 1e-30f));
+        return;
     } else {
         const d3 V = ld(v64, w);
         P = add(P, muls(V, dt));
@@ -1394,6 +1452,16 @@ __global__ void k_walls(uint32_t nglob, const uint32_t* __restrict__ glob, const
     st(xB, w, P, 0.0);
     v32B[w] = v32A[w];
     w32B[w] = w32A[w];
+}
+
+// After k_walls, when mobile or constrained walls move: the largest distance any point of such a
+// wall went this step joins the walls' displacement bound (not in a step that was held).
+__global__ void k_wall_bound(const float* __restrict__ disp_in, float* __restrict__ disp_out, float skin,
+                             float skin_w, unsigned* __restrict__ dyn_bits) {
+    step_order();
+    if (blockIdx.x != 0 || threadIdx.x != 0) return;
+    if (!list_spent(disp_in[0], disp_in[1], disp_in[2], skin, skin_w)) disp_out[2] += __uint_as_float(*dyn_bits);
+    *dyn_bits = 0u;
 }
 
 // ---- broad phase -------------------------------------------------------------------------
@@ -1597,7 +1665,7 @@ __global__ void __launch_bounds__(TPB) k_nbr(uint32_t nloc, const uint32_t* __re
         if (wl.w != 0.0f) {
             float err;
             const float d = cd == CD_SP ? plane_dist32(pi, pos32[w], wl, err) : line_dist32(pi, pos32[w], wl, err);
-            const float sk = models[model_of[w]].behavior == BEH_ORBITAL ? WALL_SKIN * skin : skin;
+            const float sk = models[model_of[w]].behavior != BEH_FIXED ? WALL_SKIN * skin : skin;
             if (cd == CD_SIC) {                        // clear of the shell by more than the skin
                 if (d + err < -(reach[pw] + sk) * (1.0f - 4.0f * PF_ARITH_EPS)) continue;
             } else if (d - err > (reach[pw] + sk) * (1.0f + 4.0f * PF_ARITH_EPS)) {
@@ -1704,7 +1772,7 @@ __global__ void __launch_bounds__(TPB) k_meta(uint32_t n, const uint32_t* __rest
         const uint32_t pi = pidx(S, i_slave ? mi : mj, i_slave ? mj : mi);
         const PairParam& P = params[pi];
         const bool bond = (P.is == IS_BSDBF || P.is == IS_BTSDBF || P.is == IS_BSDB2F) && P.c[4] != 0.0;
-        const bool moving = (v & WALL_BIT) && models[mj].behavior == BEH_ORBITAL;
+        const bool moving = (v & WALL_BIT) && models[mj].behavior != BEH_FIXED;
         meta[e] = (pi & META_PI) | ((uint32_t)(cd_plane(P.cd) & META_CD_MASK) << META_CD_SHIFT) | (bond ? META_BOND : 0u) |
                   (slot[e] == e ? META_OWNER : 0u) | (i_slave ? META_SLAVE : 0u) | (moving ? META_MOVING : 0u);
     }
@@ -1770,7 +1838,7 @@ __global__ void __launch_bounds__(TPB) k_clear(uint32_t n, const uint32_t* __res
             if (cd == 0) continue;
             const uint32_t j = ent[e] & ~WALL_BIT;
             const bool wall = ent[e] & WALL_BIT;
-            if ((m & META_BOND) || (wall && models[model_of[j]].behavior == BEH_ORBITAL)) {
+            if ((m & META_BOND) || (wall && models[model_of[j]].behavior != BEH_FIXED)) {
                 c = cw = -1.0f;
                 break;
             }
@@ -1830,7 +1898,7 @@ __global__ void __launch_bounds__(TPB) k_interior(uint32_t n, const uint32_t* __
         const double lz = len(Oz);
         if (!(lz > 0.0)) continue;
         const d3 d = sub(P, ld(x, w));
-        const double m = (W.behavior == BEH_ORBITAL ? skin_w : skin) + 1e-9 * (len(d) + 1.0);
+        const double m = (W.behavior != BEH_FIXED ? skin_w : skin) + 1e-9 * (len(d) + 1.0);
         const d3 uz = muls(Oz, 1.0 / lz);
         bool in = false;                           // a holed plate's hole edge is not modelled here
         if (W.shape == SHAPE_PLATE) {
@@ -1983,7 +2051,10 @@ __global__ void __launch_bounds__(TPB) k_active(uint32_t n, TickArgs a, uint8_t*
         const d3 Ps = ld(a.xA, s), Pm = ld(a.xA, m);
         double depth;
         if (P.cd == CD_SS) {
-            depth = __dsub_rn(__dadd_rn(gg.x, gg.y), xlen(xsub(Pm, Ps)));
+            d3 d = xsub(Pm, Ps);
+            const Periodic& pb = a.scenes[a.scene_of[i]].pb;
+            if (pb.on) d = min_image(pb, d);      // CDSphere2Sphere.cpp:19-22
+            depth = __dsub_rn(__dadd_rn(gg.x, gg.y), xlen(d));
         } else {
             d3 nd, pt;
             depth = wall_detect(P.cd, gg.x, gg.y, gg.z, gg.w, Ps, Pm, ld(a.ox, m), ld(a.oz, m), nd, pt,
@@ -2507,6 +2578,7 @@ private:
     bool quiet_ok_ = true;                        // quiet spheres skip their walk (identical results)
     bool orient_ = false;                         // integrate the spheres' orientations
     bool any_pbc_ = false;                        // a scene has a periodic boundary
+    bool dyn_walls_ = false;                      // a wall is mobile or constrained (moved by its impulses)
     float4* d_tdav_ = nullptr;                    // [n] angular velocity increments (orientations)
     int sms_ = 1;                                 // streaming multiprocessors of the device
     float2* d_clear_ = nullptr;                   // [n] quiet-sphere pad limits of the current list
@@ -2744,8 +2816,7 @@ int MixedEngine::init_from(const std::vector<SceneSource>& src, const MixedEngin
                 rmax = std::max(rmax, M.a0);
                 ++S.nloc;
             } else {
-                if (M.behavior != BEH_FIXED && M.behavior != BEH_ORBITAL)
-                    return fail(VEDO_ERR_UNSUPPORTED_MODEL, "mixed form: walls must be fixed or orbital");
+                if (M.behavior == BEH_MOBILE || M.behavior == BEH_CONSTRAINED) dyn_walls_ = true;
                 glob_.push_back(n_ + i);
             }
             model_of.push_back(S.model_off + h.model_of[perm[i]]);
@@ -3033,6 +3104,7 @@ TickArgs MixedEngine::args(bool write_imp) {
     a.imp = d_imp_;
     a.aimp = d_aimp_;
     a.write_imp = write_imp ? 1 : 0;
+    a.wimp_on = (write_imp || dyn_walls_) ? 1 : 0;
     a.vmax_bits = d_red_ + 8;
     a.pos32 = d_pos32_;
     a.disp = d_disp_ + 4 * cur_;
@@ -3388,7 +3460,7 @@ void MixedEngine::launch_step(bool write_imp) {
         ++launches_;
     }
     if (pe) cudaEventRecordWithFlags(pe[1], stream_, ev_flags_);
-    if (write_imp && !glob_.empty()) {
+    if ((write_imp || dyn_walls_) && !glob_.empty()) {      // the walls' impulses (every step when walls respond)
         const uint32_t ng = (uint32_t)glob_.size();
         cudaMemsetAsync(d_wred_, 0, (size_t)ng * (8 + 48), stream_);
         unsigned* wmax = reinterpret_cast<unsigned*>(d_wred_ + 6 * (size_t)ng);
@@ -3404,11 +3476,17 @@ void MixedEngine::launch_step(bool write_imp) {
     note(step_launch(dep, k_walls, nblk(std::max<size_t>(glob_.size(), 1)), TPB, stream_,
         (uint32_t)glob_.size(), (const uint32_t*)d_glob_, (const uint32_t*)d_model_of_, (const ModelDev*)d_models_,
         (const SceneDev*)d_scenes_, (const uint32_t*)d_scene_of_, (const double4_32a*)a.xA, a.xB,
-        (const double4_32a*)d_v64_, (const double4_32a*)d_w64_, (const float4*)a.v32A, a.v32B, (const float4*)a.w32A,
+        d_v64_, d_w64_, (const float4*)a.v32A, a.v32B, (const float4*)a.w32A,
         a.w32B, d_ox_, d_oz_, dt_max_, d_red_ + 8, d_red_ + 2, (const float*)(d_disp_ + 4 * cur_),
         d_disp_ + 4 * (cur_ ^ 1), skin_min_, WALL_SKIN * skin_min_, pos_eps_, (const unsigned*)(d_red_ + 12),
-        (const double4_32a*)d_wrot_, d_red_ + 11, d_wall32_, d_red_ + 13));
+        (const double4_32a*)d_wrot_, d_red_ + 11, d_wall32_, d_red_ + 13, (const double4_32a*)d_imp_,
+        (const double4_32a*)d_aimp_, d_red_ + 3));
     ++launches_;
+    if (dyn_walls_) {
+        note(step_launch(dep, k_wall_bound, 1u, 32u, stream_, (const float*)(d_disp_ + 4 * cur_),
+                         d_disp_ + 4 * (cur_ ^ 1), skin_min_, WALL_SKIN * skin_min_, d_red_ + 3));
+        ++launches_;
+    }
     if (pe) cudaEventRecordWithFlags(pe[2], stream_, ev_flags_);
     cur_ ^= 1;
 }
