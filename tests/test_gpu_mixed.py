@@ -96,16 +96,17 @@ def test_mixed_matches_oracle_trajectory_start(engine_lib, port_lib):
 def test_mixed_mobile_and_constrained_walls_against_fp64(behavior, solver, engine_lib):
     """A lid moved by its impulses (a mobile plate: translation and rotation; a constrained one:
     along its normal) in the mixed form: the wall shares are summed exactly every step and the
-    lid responds as the FP64 form's respond_object.  From the FP64 form's state at step 150 (lid
+    lid responds as the FP64 form's respond_object.  From the FP64 form's state at step 450 (lid
     in contact): identical contact sets, the lid's and the spheres' step impulses within 1e-5,
-    and after 300 more steps the lid within 1e-7 m and 1e-4 relative in velocity of the FP64
-    form's; every form of the tick gives the same bits."""
+    and after 100 more steps the lid within 1e-8 m and 1e-3 relative in velocity of the FP64
+    form's (the lid rests on many spheres: the force errors add up in its small sideways motion);
+    every form of the tick gives the same bits."""
     import os
     import tempfile
     sc = scenes.piston(behavior=behavior, solver=solver, steps=3000)
     lid = sc.num_objects - 1
     f64 = engine_lib.GpuEngine(sc, up_iact=5)
-    f64.run(150)
+    f64.run(450)                                   # the lid has reached the spheres
     with tempfile.TemporaryDirectory() as td:
         path = os.path.join(td, "p.ido")
         f64.write_ido(path)
@@ -123,12 +124,12 @@ def test_mixed_mobile_and_constrained_walls_against_fp64(behavior, solver, engin
         ref = np.linalg.norm(sa[k])
         assert np.linalg.norm(sa[k] - sb[k]) <= 1e-5 * ref, k
     assert np.linalg.norm(sa["impact"][lid] - sb["impact"][lid]) <= 1e-5 * np.linalg.norm(sa["impact"][lid])
-    a.run(300)
+    a.run(100)
     for e in forms:
-        e.run(300)
+        e.run(100)
     sa, sb = a.state(), b.state()
-    assert np.abs(sa["position"][lid] - sb["position"][lid]).max() <= 1e-7
-    assert np.linalg.norm(sa["velocity"][lid] - sb["velocity"][lid]) <= 1e-4 * np.linalg.norm(sa["velocity"][lid])
+    assert np.abs(sa["position"][lid] - sb["position"][lid]).max() <= 1e-8
+    assert np.linalg.norm(sa["velocity"][lid] - sb["velocity"][lid]) <= 1e-3 * np.linalg.norm(sa["velocity"][lid])
     assert abs(sa["position"][lid][2] - sc.position[lid][2]) > 1e-5          # the lid did move
     for e in forms[1:]:
         st = e.state()

@@ -588,7 +588,7 @@ __device__ __noinline__ double tie_depth(const TickArgs& a, uint32_t pi, uint32_
 // Sphere-wall pair: the reference's detector in FP64 (wall_detect), the contact normal and
 // lever arms rounded to FP32.
 __device__ __noinline__ void wall_pair(const TickArgs& a, int cd, uint32_t pi, uint32_t s, uint32_t m, bool& active,
-                                       float& depth, f3& n, f3& rA, f3& rB) {
+                                       float& depth, f3& n, f3& rA, f3& rB, const Periodic& pb) {
     const double4_32a gg = a.geom[pi];
     const d3 Ps = ld(a.xA, s), Pm = ld(a.xA, m);
     d3 nd, pt;
@@ -597,7 +597,11 @@ __device__ __noinline__ void wall_pair(const TickArgs& a, int cd, uint32_t pi, u
     active = dex > 0.0;
     depth = (float)dex;
     n = fm((float)nd.x, (float)nd.y, (float)nd.z);
-    const d3 ra = sub(pt, Ps), rb = sub(pt, Pm);
+    d3 ra = sub(pt, Ps), rb = sub(pt, Pm);
+    if (pb.on) {                               // both lever arms take the nearest image (ISwBSDBF.cpp:69-73)
+        ra = min_image(pb, ra);
+        rb = min_image(pb, rb);
+    }
     rA = fm((float)ra.x, (float)ra.y, (float)ra.z);
     rB = fm((float)rb.x, (float)rb.y, (float)rb.z);
 }
@@ -844,7 +848,7 @@ __device__ __forceinline__ int exact_pair(const TickArgs& a, const SceneDev& S, 
         rA = (a.pc32[8 * (size_t)pi + 7] - 0.5f * depth) * n;   // slot 7: the slave's radius
         rB = rA - df;
     } else {
-        wall_pair(a, P.cd, pi, s, m, active, depth, n, rA, rB);
+        wall_pair(a, P.cd, pi, s, m, active, depth, n, rA, rB, S.pb);
     }
     const uint8_t f0 = a.fA[slot];
     uint8_t f = f0 & 15;
