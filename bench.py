@@ -35,7 +35,7 @@ sys.path.insert(0, ROOT)
 METRIC = "particle-steps/s on 1 GB300 (mixed vs FP64 at stated error); serving p50/p99 ms"
 UNIT = "particle-steps/s"
 WORKLOAD = "hertz_drum_1M"
-TUNE_STEPS = 450
+TUNE_STEPS = 500
 
 
 def parse():
@@ -522,8 +522,8 @@ def c1_workload(args, dist, dev, cpu_job_c1):
     sc = scenes.lsd_box(steps=20000)
     n = scene_particles(sc)
     out = {"workload": "lsd_box_8k (20,000 steps, dt 1e-6 s, candidate list every 20 steps)", "particles": n}
-    for name, prec in (("fp64", 0), ("mixed", 1)):
-        e = GpuEngine(sc, up_iact=20, device=dev, precision=prec)
+    for name, prec, pers in (("fp64", 0, False), ("mixed", 1, False), ("mixed_persistent", 1, True)):
+        e = GpuEngine(sc, up_iact=20, device=dev, precision=prec, persistent=pers)
         torch.cuda.synchronize()
         t0 = time.perf_counter()
         e.run(20000)
@@ -542,7 +542,9 @@ def c1_workload(args, dist, dev, cpu_job_c1):
                                              f"{r['seconds']:.1f} s"}
             out["fp64_over_cpu"] = out["fp64"]["value"] / r["value"]
     out["note"] = ("L2-resident (state about 2 MB) and launch/latency-bound: one step is a few microseconds of "
-                   "kernels, so the rate measures launch overhead, not HBM")
+                   "kernels, so the rate measures launch overhead, not HBM; mixed: each check interval of 10 "
+                   "steps replayed as a CUDA graph of per-step kernels; mixed_persistent: each interval one "
+                   "cooperative launch with grid barriers between the stages (identical results)")
     return out
 
 
@@ -620,13 +622,32 @@ def batch_workload(args, dist, dev):
     t = dist.reduce(prof["total_ms"], "max")
     total = dist.reduce(float(n), "sum")
     contacts = int(b.observables()[9])
+    tune = b.tuning()
+    # the same window with the check intervals in the other schedule (a replayed graph of per-step
+    # kernels, or one persistent cooperative launch): the tuned settings otherwise, fresh engine
+    other = None
+    if not args.no_profile_pass:
+        hs2 = [scenes.hopper_batch(args.batch_scenes, seed=2025, steps=5000)[q] for q in mine]
+        b2 = BatchEngine(hs2, device=dev, skin=tune["skin"], cell_scale=tune["cell_scale"],
+                         tick_block=tune["tick_block"], stored_splits=tune["stored_splits"],
+                         split_tick=tune["split_tick"], pair_pass=tune["pair_pass"],
+                         persistent=not tune["persistent"])
+        del hs2
+        b2.run(TUNE_STEPS)
+        torch.cuda.synchronize()
+        b2.run(args.batch_steps)
+        p2 = b2.last_run_profile()
+        other = {"persistent": b2.tuning()["persistent"], "ms_per_step": p2["total_ms"] / args.batch_steps,
+                 "gpu_launches": p2["launches"]}
+        b2.close()
     out = {"workload": f"hopper_batch_{args.batch_scenes}", "scenes": args.batch_scenes, "particles": int(total),
            "scaling": "strong" if dist.world > 1 else None,
            "placement": {"scenes_per_rank": [len(p) for p in dist.gather(mine)],
                          "particles_per_rank": dist.gather(n), "rule": "longest first to the least-loaded GPU"},
            "active_contacts_end": contacts, "z_pp": contacts / n,
            "value": total * args.batch_steps / (t * 1e-3), "unit": UNIT, "ms_per_step": t / args.batch_steps,
-           "steps": args.batch_steps, "gpu_launches": prof["launches"], "tuning": b.tuning(),
+           "steps": args.batch_steps, "gpu_launches": prof["launches"], "tuning": tune,
+           "other_schedule": other,
            "errors_mixed_vs_fp64": {"scenes": errs,
                                     "max_step_impact_rel_l2": max((e["step_impact_rel_l2"] for e in errs), default=None),
                                     "all_contact_sets_identical": all(e["contact_set_identical"] for e in errs),

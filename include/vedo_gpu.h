@@ -192,6 +192,14 @@ typedef struct vedo_engine_opts {
                                  they are (default: no force or contact depends on a sphere's
                                  orientation, and the turn costs FP64 sines and cosines per
                                  spinning sphere per step).  The FP64 form always turns them */
+    uint32_t persistent;      /* MIXED only: 1 = a check interval of steps runs as ONE cooperative
+                                 launch (every block resident at once) whose stages are separated
+                                 by grid barriers, in place of a replayed graph of per-step
+                                 kernels; for the full tick and the pair pass (split_tick 0 or 2)
+                                 without mobile or constrained walls, other steps as before.  Each
+                                 barrier's wait is bounded (2 s): on expiry the call returns
+                                 VEDO_ERR_CUDA and the engine's state is undefined.  Identical
+                                 results; the autotuner chooses (default 0)              */
 } vedo_engine_opts;
 
 typedef struct vedo_gpu_engine vedo_gpu_engine;
@@ -352,11 +360,20 @@ void vedo_gpu_set_profiling(vedo_gpu_engine* e, int on);
 const char* vedo_gpu_last_error(const vedo_gpu_engine* e);
 void vedo_gpu_destroy(vedo_gpu_engine* e);
 
-/* Skin (fraction of r_max), cell scale, tick block size, split storage and the form of the tick
- * (vedo_engine_opts.split_tick: 0, 1 or 2; the last two may be NULL) in use by a MIXED-form engine,
+/* Skin (fraction of r_max), cell scale, tick block size, split storage, the form of the tick
+ * (vedo_engine_opts.split_tick: 0, 1 or 2) and whether a check interval runs as one persistent
+ * launch (vedo_engine_opts.persistent; the last three may be NULL) in use by a MIXED-form engine,
  * after autotuning when it was asked for.  No counterpart in the reference. */
 int vedo_gpu_get_tuning(const vedo_gpu_engine* e, float* skin, float* cell_scale, uint32_t* tick_block,
-                        uint32_t* stored_splits, uint32_t* split_tick);
+                        uint32_t* stored_splits, uint32_t* split_tick, uint32_t* persistent);
+
+/* The persistent tick's grid barrier on its own (no counterpart in the reference): `rounds`
+ * barriers over a cooperative grid of every block the device holds at once, where each barrier
+ * expects `extra` more arrivals than the grid has (0: a working barrier; > 0: one that nothing
+ * completes, whose wait must end after `limit_ns` nanoseconds with the expiry recorded).  out[0]:
+ * rounds completed; out[1]: blocks that saw a round's arrivals miscounted; out[2]: 1 = a wait
+ * expired; out[3]: the round whose barrier expired first.  The device stays usable either way. */
+int vedo_gpu_barrier_check(int32_t device, uint32_t rounds, uint32_t extra, uint64_t limit_ns, uint32_t out[4]);
 
 /* Library version string. */
 const char* vedo_gpu_version(void);

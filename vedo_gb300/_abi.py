@@ -55,7 +55,8 @@ class EngineOpts(C.Structure):
                 ("output_prefix", C.c_char_p), ("skin", C.c_float), ("check_interval", C.c_uint32),
                 ("tick_block", C.c_uint32), ("cell_scale", C.c_float), ("autotune", C.c_uint32),
                 ("graphs", C.c_uint32), ("stored_splits", C.c_uint32), ("split_tick", C.c_uint32),
-                ("full_walks", C.c_uint32), ("consultant", C.c_uint32), ("orientations", C.c_uint32)]
+                ("full_walks", C.c_uint32), ("consultant", C.c_uint32), ("orientations", C.c_uint32),
+                ("persistent", C.c_uint32)]
 
 
 class StateView(C.Structure):

@@ -68,6 +68,7 @@ void vedo_gpu_default_opts(vedo_engine_opts* o) {
     o->split_tick = 0;
     o->full_walks = 0;
     o->orientations = 0;
+    o->persistent = 0;
 }
 
 int vedo_gpu_create(const vedo_scene_desc* scene, const vedo_engine_opts* opts, vedo_gpu_engine** out) {
@@ -225,9 +226,9 @@ const char* vedo_gpu_last_error(const vedo_gpu_engine* e) {
 void vedo_gpu_destroy(vedo_gpu_engine* e) { delete e; }
 
 int vedo_gpu_get_tuning(const vedo_gpu_engine* e, float* skin, float* cell_scale, uint32_t* tick_block,
-                        uint32_t* stored_splits, uint32_t* split_tick) {
+                        uint32_t* stored_splits, uint32_t* split_tick, uint32_t* persistent) {
     if (!e || !skin || !cell_scale || !tick_block) return VEDO_ERR_INVALID_ARGUMENT;
-    float t[5];
+    float t[6];
     const int rc = e->p->tuning(t);
     if (rc != VEDO_OK) return rc;
     *skin = t[0];
@@ -235,6 +236,7 @@ int vedo_gpu_get_tuning(const vedo_gpu_engine* e, float* skin, float* cell_scale
     *tick_block = (uint32_t)t[2];
     if (stored_splits) *stored_splits = (uint32_t)t[3];
     if (split_tick) *split_tick = (uint32_t)t[4];
+    if (persistent) *persistent = (uint32_t)t[5];
     return VEDO_OK;
 }
 

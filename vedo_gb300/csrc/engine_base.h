@@ -43,8 +43,9 @@ public:
     virtual uint64_t last_profile(double out[4]) const = 0;
     virtual void set_profiling(bool on) = 0;
     virtual const std::string& error() const = 0;
-    // skin fraction, cell scale, tick block size, stored position splits, split tick (MIXED only)
-    virtual int tuning(float out[5]) const { (void)out; return VEDO_ERR_INVALID_ARGUMENT; }
+    // skin fraction, cell scale, tick block size, stored position splits, split tick, persistent
+    // tick (MIXED only)
+    virtual int tuning(float out[6]) const { (void)out; return VEDO_ERR_INVALID_ARGUMENT; }
     virtual int quiet_spheres(uint64_t* count) {
         *count = 0;
         return VEDO_OK;

@@ -1066,10 +1066,8 @@ __global__ void __launch_bounds__(TPB, 6) k_tick_light(TickArgs a) {   // 6 bloc
 // angular velocity w before the step and its increment dav, by Vector3d::rotate_around in FP64 for
 // both axes; a zero turn leaves them.  Run after the tick when the caller asks for orientations,
 // from the new angular velocity w + dav and the increment: dt (w + dav - dav/2).
-__global__ void __launch_bounds__(TPB) k_turn(TickArgs a) {
-    step_order();
-    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (held_step(a) || i >= a.n) return;
+__device__ __forceinline__ void turn_sphere(const TickArgs& a, uint32_t i) {
+    if (i >= a.n) return;
     const ModelDev& M = a.models[a.model_of[i]];
     const SceneDev& S = a.scenes[a.scene_of[i]];
     if (M.scope != SCOPE_LOCAL || !S.active || M.behavior != BEH_MOBILE) return;
@@ -1080,15 +1078,17 @@ __global__ void __launch_bounds__(TPB) k_turn(TickArgs a) {
     st(a.sox, i, rotate_around(ld(a.sox, i), dwv), 0.0);
     st(a.soz, i, rotate_around(ld(a.soz, i), dwv), 0.0);
 }
+__global__ void __launch_bounds__(TPB) k_turn(TickArgs a) {
+    step_order();
+    if (!held_step(a)) turn_sphere(a, blockIdx.x * blockDim.x + threadIdx.x);
+}
 
 // SimMediator.cpp:746: after the response every object of a periodic scene goes back into the
 // periodic box (Boundary::EnforceBoundaryConditions, wrap_position); run after the tick, only
 // when a scene is periodic, so that the tick itself carries no FP64 wrap.  A wrapped sphere's
 // position splits are formed anew.
-__global__ void __launch_bounds__(TPB) k_wrap(TickArgs a) {
-    step_order();
-    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (held_step(a) || i >= a.n) return;
+__device__ __forceinline__ void wrap_sphere(const TickArgs& a, uint32_t i) {
+    if (i >= a.n) return;
     const SceneDev& S = a.scenes[a.scene_of[i]];
     if (!S.pb.on || !S.active || a.models[a.model_of[i]].scope != SCOPE_LOCAL) return;
     const d3 P = ld(a.xB, i);
@@ -1105,6 +1105,10 @@ __global__ void __launch_bounds__(TPB) k_wrap(TickArgs a) {
         a.xsB[2 * i + 1] = l2;
     }
 }
+__global__ void __launch_bounds__(TPB) k_wrap(TickArgs a) {
+    step_order();
+    if (!held_step(a)) wrap_sphere(a, blockIdx.x * blockDim.x + threadIdx.x);
+}
 
 // ---- pair pass ------------------------------------------------------------------------------
 // The tick in three kernels, each pair on the exact path evaluated once:
@@ -1120,10 +1124,8 @@ __global__ void __launch_bounds__(TPB) k_wrap(TickArgs a) {
 // identical bits, in the same order, so results are the single tick's.  The pair kernel runs
 // with every lane on a pair, where the single tick's lanes wait for the sphere of their warp with
 // the most pairs.
-__global__ void __launch_bounds__(TPB, 4) k_tick_pf(TickArgs a) {     // 63 registers, no spills
-    step_order();
-    if (held_step(a)) return;                      // k_tick_sum holds the state (uniform branch)
-    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+// One sphere's prefilter walk (i >= n: a lane without a sphere); every lane of the warp calls it.
+__device__ __forceinline__ void pf_sphere(const TickArgs& a, uint32_t i) {
     const int lane = threadIdx.x & 31;
     uint32_t c0 = 0u, e0 = 0u, e1 = 0u, qc = 0u;
     float4 p32i = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
@@ -1212,6 +1214,11 @@ __global__ void __launch_bounds__(TPB, 4) k_tick_pf(TickArgs a) {     // 63 regi
     }
     if (walk) note_walk(a, i, qc, dirty || any_exact);
 }
+__global__ void __launch_bounds__(TPB, 4) k_tick_pf(TickArgs a) {
+    step_order();
+    if (held_step(a)) return;                      // k_tick_sum holds the state (uniform branch)
+    pf_sphere(a, blockIdx.x * blockDim.x + threadIdx.x);
+}
 
 // One pair of the worklist: the exact path and both members' shares.
 template <int LAW, bool XS>
@@ -1235,22 +1242,27 @@ __device__ __forceinline__ void pair_item(const TickArgs& a, const uint4& it) {
     }
 }
 
+// The worklist's pairs from `first` in strides of `stride`: sphere pairs, then wall pairs (only
+// the warp that straddles the two mixes them).
+template <int LAW, bool XS>
+__device__ __forceinline__ void pairs_from(const TickArgs& a, uint32_t first, uint32_t stride) {
+    const uint32_t nw = min(a.nwork[0], a.pcap), nww = min(a.nwork[-1], a.pcap - nw);
+    for (uint32_t q = first; q < nw + nww; q += stride)
+        pair_item<LAW, XS>(a, a.pwork[q < nw ? q : a.pcap - 1u - (q - nw)]);
+}
 template <int LAW, bool XS>
 __global__ void __launch_bounds__(TPB, 4) k_tick_pairs(TickArgs a) {     // 64 registers (a few spill)
     step_order();
     if (held_step(a)) return;
-    const uint32_t nw = min(a.nwork[0], a.pcap), nww = min(a.nwork[-1], a.pcap - nw);
-    // sphere pairs, then wall pairs: only the warp that straddles the two mixes them
-    for (uint32_t q = blockIdx.x * blockDim.x + threadIdx.x; q < nw + nww; q += gridDim.x * blockDim.x)
-        pair_item<LAW, XS>(a, a.pwork[q < nw ? q : a.pcap - 1u - (q - nw)]);
+    pairs_from<LAW, XS>(a, blockIdx.x * blockDim.x + threadIdx.x, gridDim.x * blockDim.x);
 }
 
+// One sphere's sums and integration (or, in an identity step, its state carried over); returns its
+// squared speed bounds.
 template <bool XS>
-__global__ void __launch_bounds__(TPB, 5) k_tick_sum(TickArgs a) {      // 48 registers: 5 blocks of 256 per SM
-    step_order();
-    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+__device__ __forceinline__ float2 sum_sphere(const TickArgs& a, uint32_t i, bool hold) {
     float2 vmax_local = make_float2(0.0f, 0.0f);
-    if (held_step(a)) {
+    if (hold) {
         hold_state(a, i);
     } else if (i < a.n) {
         const uint32_t mi = a.model_of[i];
@@ -1264,26 +1276,48 @@ __global__ void __launch_bounds__(TPB, 5) k_tick_sum(TickArgs a) {      // 48 re
             const bool quiet = a.wk[i] != 0u;
             const float4 mf0 = a.mf[2 * mi], mf1 = a.mf[2 * mi + 1];
             K3 J, JA;
-            auto add_pair = [&](uint32_t e) {
-                const float4 r0 = a.prec[2 * (size_t)e];
+            auto add_pair = [&](const float4& r0, const float4& t0) {
                 const int app = __float_as_int(r0.w);
                 if (app) {
                     J.add(f4to3(r0));
-                    if (app == 2) JA.add(f4to3(a.prec[2 * (size_t)e + 1]));
+                    if (app == 2) JA.add(f4to3(t0));
                 }
             };
             if (!quiet) {
-                for (unsigned long long m = a.xm[i]; m; m &= m - 1)
-                    add_pair(e0 + (uint32_t)(__ffsll(m) - 1));
+                // the records of two marked entries at a time are loaded together (both halves of an
+                // entry's record share one 32-byte sector), then summed in entry order
+                unsigned long long m = a.xm[i];
+                while (m) {
+                    float4 r[2], t[2];
+                    uint32_t cnt = 0;
+#pragma unroll
+                    for (int k = 0; k < 2; ++k) {
+                        if (m) {
+                            const size_t e = e0 + (uint32_t)(__ffsll(m) - 1);
+                            m &= m - 1;
+                            r[k] = a.prec[2 * e];
+                            t[k] = a.prec[2 * e + 1];
+                            cnt = (uint32_t)k + 1u;
+                        }
+                    }
+#pragma unroll
+                    for (int k = 0; k < 2; ++k)
+                        if ((uint32_t)k < cnt) add_pair(r[k], t[k]);
+                }
                 for (uint32_t e = e0 + 64; e < e1; ++e)         // long lists: entries after the first 64
-                    if (a.xf[e]) add_pair(e);
+                    if (a.xf[e]) add_pair(a.prec[2 * (size_t)e], a.prec[2 * (size_t)e + 1]);
             }
             vmax_local = finish_sphere<XS>(a, i, M.behavior == BEH_MOBILE, quiet, S, Pi, V, mf0, mf1, J, JA);
         } else if (M.scope == SCOPE_LOCAL) {
             hold_state(a, i);
         }
     }
-    reduce_vmax(a, vmax_local);
+    return vmax_local;
+}
+template <bool XS>
+__global__ void __launch_bounds__(TPB, 5) k_tick_sum(TickArgs a) {      // 48 registers: 5 blocks of 256 per SM
+    step_order();
+    reduce_vmax(a, sum_sphere<XS>(a, blockIdx.x * blockDim.x + threadIdx.x, held_step(a)));
 }
 
 // A wall's FP32 record carries in w the drift of its scene's frame across it after k steps
@@ -1341,22 +1375,69 @@ __global__ void k_wall_rot(uint32_t nglob, const uint32_t* __restrict__ glob, co
 // displacement bounds and the step count after the step into the other parity slot
 // (disp_out), or, when the step is an identity step, carries them over and counts the step in
 // *held; every wall's FP32 record gets the frame's drift across it for the next step.
-__global__ void k_walls(uint32_t nglob, const uint32_t* __restrict__ glob, const uint32_t* __restrict__ model_of,
-                        const ModelDev* __restrict__ models, const SceneDev* __restrict__ scenes,
-                        const uint32_t* __restrict__ scene_of, const double4_32a* __restrict__ xA,
-                        double4_32a* __restrict__ xB, double4_32a* __restrict__ v64,
-                        double4_32a* __restrict__ w64, const float4* __restrict__ v32A,
-                        float4* __restrict__ v32B, const float4* __restrict__ w32A, float4* __restrict__ w32B,
-                        double4_32a* __restrict__ ox, double4_32a* __restrict__ oz, float dt_max,
-                        unsigned* __restrict__ vmax_bits, unsigned* __restrict__ vrel_bits,
-                        const float* __restrict__ disp_in, float* __restrict__ disp_out, float skin, float skin_w,
-                        float pos_eps, const unsigned* __restrict__ wall_speed_bits,
-                        const double4_32a* __restrict__ wrot,
-                        unsigned* __restrict__ held, float4* __restrict__ wall32, unsigned* __restrict__ nwork,
-                        const double4_32a* __restrict__ imp, const double4_32a* __restrict__ aimp,
-                        unsigned* __restrict__ dyn_bits) {
-    step_order();
-    const uint32_t q = blockIdx.x * blockDim.x + threadIdx.x;
+struct WallArgs {
+    uint32_t nglob;
+    const uint32_t* glob;
+    const uint32_t* model_of;
+    const ModelDev* models;
+    const SceneDev* scenes;
+    const uint32_t* scene_of;
+    const double4_32a* xA;
+    double4_32a* xB;
+    double4_32a* v64;
+    double4_32a* w64;
+    const float4* v32A;
+    float4* v32B;
+    const float4* w32A;
+    float4* w32B;
+    double4_32a* ox;
+    double4_32a* oz;
+    float dt_max;
+    unsigned* vmax_bits;
+    unsigned* vrel_bits;
+    const float* disp_in;
+    float* disp_out;
+    float skin, skin_w, pos_eps;
+    const unsigned* wall_speed_bits;
+    const double4_32a* wrot;
+    unsigned* held;
+    float4* wall32;
+    unsigned* nwork;
+    const double4_32a* imp;
+    const double4_32a* aimp;
+    unsigned* dyn_bits;
+};
+__device__ __forceinline__ void walls_item(const WallArgs& W, uint32_t q) {
+    const uint32_t nglob = W.nglob;
+    const uint32_t* __restrict__ glob = W.glob;
+    const uint32_t* __restrict__ model_of = W.model_of;
+    const ModelDev* __restrict__ models = W.models;
+    const SceneDev* __restrict__ scenes = W.scenes;
+    const uint32_t* __restrict__ scene_of = W.scene_of;
+    const double4_32a* xA = W.xA;
+    double4_32a* xB = W.xB;
+    double4_32a* v64 = W.v64;
+    double4_32a* w64 = W.w64;
+    const float4* v32A = W.v32A;
+    float4* v32B = W.v32B;
+    const float4* w32A = W.w32A;
+    float4* w32B = W.w32B;
+    double4_32a* ox = W.ox;
+    double4_32a* oz = W.oz;
+    const float dt_max = W.dt_max;
+    unsigned* vmax_bits = W.vmax_bits;
+    unsigned* vrel_bits = W.vrel_bits;
+    const float* disp_in = W.disp_in;
+    float* disp_out = W.disp_out;
+    const float skin = W.skin, skin_w = W.skin_w, pos_eps = W.pos_eps;
+    const unsigned* wall_speed_bits = W.wall_speed_bits;
+    const double4_32a* __restrict__ wrot = W.wrot;
+    unsigned* held = W.held;
+    float4* wall32 = W.wall32;
+    unsigned* nwork = W.nwork;
+    const double4_32a* imp = W.imp;
+    const double4_32a* aimp = W.aimp;
+    unsigned* dyn_bits = W.dyn_bits;
     const float drel = disp_in[0], dabs = disp_in[1], dw = disp_in[2];
     const bool hold = list_spent(drel, dabs, dw, skin, skin_w);
     if (q == 0) {
@@ -1457,6 +1538,10 @@ __global__ void k_walls(uint32_t nglob, const uint32_t* __restrict__ glob, const
     v32B[w] = v32A[w];
     w32B[w] = w32A[w];
 }
+__global__ void k_walls(WallArgs W) {
+    step_order();
+    walls_item(W, blockIdx.x * blockDim.x + threadIdx.x);
+}
 
 // After k_walls, when mobile or constrained walls move: the largest distance any point of such a
 // wall went this step joins the walls' displacement bound (not in a step that was held).
@@ -1466,6 +1551,140 @@ __global__ void k_wall_bound(const float* __restrict__ disp_in, float* __restric
     if (blockIdx.x != 0 || threadIdx.x != 0) return;
     if (!list_spent(disp_in[0], disp_in[1], disp_in[2], skin, skin_w)) disp_out[2] += __uint_as_float(*dyn_bits);
     *dyn_bits = 0u;
+}
+
+// ---- persistent tick ------------------------------------------------------------------------
+// One cooperative launch runs a whole check interval: the steps' stages (the kernels above, as
+// device functions, with the same operations in the same order per sphere, pair and wall) are
+// separated by grid barriers instead of kernel boundaries.  A cooperative launch has every block
+// resident at once (the launch fails rather than start otherwise), so the barrier's wait always
+// ends; it is still bounded: a block that has waited `limit_ns` on the global timer, or polled
+// a bounded number of times, records the barrier's site and sets the expiry flag, and every block
+// that sees the flag leaves at its next barrier, so the kernel ends and the host reports the
+// error.  Words: [0] arrivals, [1] generation, [2] expired, [3] the site of the first expiry.
+struct GridBar {
+    unsigned* w;
+    uint32_t nblocks;
+    unsigned long long limit_ns;
+};
+__device__ __forceinline__ unsigned long long global_ns() {
+    unsigned long long t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
+__device__ __forceinline__ unsigned ld_acquire(const unsigned* p) {
+    unsigned v;
+    asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+    return v;
+}
+__device__ __forceinline__ bool grid_sync(const GridBar& g, unsigned site) {
+    __shared__ int ok_s;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        int ok = 0;
+        unsigned* w = g.w;
+        if (ld_acquire(w + 2) == 0u) {
+            const unsigned gen = ld_acquire(w + 1);
+            __threadfence();                       // this block's writes, before its arrival
+            if (atomicAdd(w, 1u) == g.nblocks - 1u) {
+                atomicExch(w, 0u);                 // the count is reset before the generation moves
+                __threadfence();
+                atomicAdd(w + 1, 1u);
+                ok = 1;
+            } else {
+                const unsigned long long t0 = global_ns();
+                const unsigned long long polls = g.limit_ns / 16u + 4096u;
+                for (unsigned long long k = 0;; ++k) {
+                    if (ld_acquire(w + 1) != gen) {
+                        ok = 1;
+                        break;
+                    }
+                    if (ld_acquire(w + 2) != 0u) break;
+                    if (k > polls || global_ns() - t0 > g.limit_ns) {
+                        atomicCAS(w + 3, 0u, site);
+                        atomicExch(w + 2, 1u);
+                        break;
+                    }
+                    __nanosleep(32);
+                }
+            }
+            __threadfence();                       // the other blocks' writes, after the barrier
+        }
+        ok_s = ok;
+    }
+    __syncthreads();
+    return ok_s != 0;
+}
+
+struct PersistArgs {
+    TickArgs t[2];                 // the steps that start from the first step's buffers, and the others
+    WallArgs w[2];
+    uint32_t steps;
+    int pbc;                       // a scene is periodic: spheres back into the box after each step
+    GridBar bar;
+};
+static_assert(sizeof(PersistArgs) <= 4096, "the persistent tick's arguments must fit the classic parameter space");
+
+// FORM 0: the full tick (one thread per sphere), then the walls; FORM 2: the pair pass's prefilter
+// pass, pair pass and sums, then the walls.  Spheres go to the warps of the whole grid in turn
+// (consecutive warps of a block on different SMs), so a small scene spreads over every SM.
+template <int FORM, int LAW, bool XS>
+__global__ void __launch_bounds__(FORM == 2 ? 1024 : 512, 1) k_persist(PersistArgs p) {
+    const uint32_t lane = threadIdx.x & 31u;
+    const uint32_t W = gridDim.x * (blockDim.x >> 5);
+    const uint32_t gw = (threadIdx.x >> 5) * gridDim.x + blockIdx.x;
+    uint32_t site = 1;
+    for (uint32_t k = 0; k < p.steps; ++k) {
+        const TickArgs& a = p.t[k & 1u];
+        const uint32_t n = a.n;
+        const bool hold = list_spent(__ldcg(a.disp), __ldcg(a.disp + 1), __ldcg(a.disp + 2), a.skin, a.skin_w);
+        float2 vm = make_float2(0.0f, 0.0f);
+        if (FORM == 2) {
+            if (!hold)
+                for (uint32_t s = gw; s * 32u < n; s += W) pf_sphere(a, s * 32u + lane);
+            if (!grid_sync(p.bar, site++)) return;
+            if (!hold) pairs_from<LAW, XS>(a, gw * 32u + lane, W * 32u);
+            if (!grid_sync(p.bar, site++)) return;
+            for (uint32_t s = gw; s * 32u < n; s += W) {
+                const uint32_t i = s * 32u + lane;
+                vm = fmax2(vm, sum_sphere<XS>(a, i, hold));
+                if (!hold && p.pbc) wrap_sphere(a, i);
+                if (!hold && a.orient) turn_sphere(a, i);
+            }
+        } else {
+            for (uint32_t s = gw; s * 32u < n; s += W) {
+                const uint32_t i = s * 32u + lane;
+                if (hold) {
+                    hold_state(a, i);
+                } else if (i < n) {
+                    vm = fmax2(vm, tick_sphere<LAW, XS>(a, i));
+                    if (p.pbc) wrap_sphere(a, i);
+                    if (a.orient) turn_sphere(a, i);
+                }
+            }
+        }
+        reduce_vmax(a, vm);
+        if (!grid_sync(p.bar, site++)) return;
+        const WallArgs& wa = p.w[k & 1u];
+        for (uint32_t q = blockIdx.x * blockDim.x + threadIdx.x; q < max(wa.nglob, 1u); q += gridDim.x * blockDim.x)
+            walls_item(wa, q);
+        if (k + 1u < p.steps && !grid_sync(p.bar, site++)) return;
+    }
+}
+
+// The barrier alone, for its check: `rounds` barriers over a cooperative grid that expects
+// `nblocks` arrivals (more than the grid has: a barrier that nothing completes, which must expire
+// and end the kernel).  Each block adds its round count; out[0] gets the rounds every block saw
+// complete, out[1] the blocks that saw a round's counts wrong.
+__global__ void k_bar_check(GridBar g, uint32_t rounds, unsigned* cnt, unsigned* out) {
+    for (uint32_t r = 0; r < rounds; ++r) {
+        if (threadIdx.x == 0) atomicAdd(cnt + (r & 1u), 1u);
+        if (!grid_sync(g, r + 1u)) return;
+        if (threadIdx.x == 0) {
+            if (__ldcg(cnt + (r & 1u)) != gridDim.x * (r / 2u + 1u)) atomicAdd(out + 1, 1u);
+            if (blockIdx.x == 0) atomicExch(out, r + 1u);
+        }
+    }
 }
 
 // ---- broad phase -------------------------------------------------------------------------
@@ -2445,12 +2664,13 @@ public:
     int quiet_spheres(uint64_t* count) override;
     int run_with_impulses(const double* impulse, const double* angular_impulse, int* keep_running) override;
     int list_status(double out[6]) override;
-    int tuning(float out[5]) const override {
+    int tuning(float out[6]) const override {
         out[0] = skin_frac_;
         out[1] = cell_scale_;
         out[2] = (float)tpb_;
         out[3] = xs_stored_ ? 1.0f : 0.0f;
         out[4] = pair_pass_ ? 2.0f : (split_tick_ ? 1.0f : 0.0f);
+        out[5] = persistent_ ? 1.0f : 0.0f;
         return VEDO_OK;
     }
 
@@ -2490,6 +2710,7 @@ private:
     int ensure_nlist(NList& L, uint32_t cap);
     void free_nlist(NList& L);
     TickArgs args(bool write_imp);
+    WallArgs wargs(int c);
 
     std::vector<std::shared_ptr<const HScene>> host_;   // per scene: models, interactions, initial state
     std::vector<SceneHost> sc_;
@@ -2580,6 +2801,14 @@ private:
         return grid_blocks_;
     }
     bool quiet_ok_ = true;                        // quiet spheres skip their walk (identical results)
+    // one cooperative launch per check interval (the full tick or the pair pass; identical results)
+    bool persistent_ = false;
+    const void* pk_ = nullptr;                    // the persistent kernel of the grid below
+    unsigned pk_grid_ = 0;
+    bool persist_usable() const {
+        return persistent_ && !split_tick_ && !dyn_walls_ && !profiling_;
+    }
+    int launch_persistent(uint32_t chunk);
     bool orient_ = false;                         // integrate the spheres' orientations
     bool any_pbc_ = false;                        // a scene has a periodic boundary
     bool dyn_walls_ = false;                      // a wall is mobile or constrained (moved by its impulses)
@@ -2734,6 +2963,8 @@ int MixedEngine::init_from(const std::vector<SceneSource>& src, const MixedEngin
     if (opts.split_tick > 2) return fail(VEDO_ERR_INVALID_ARGUMENT, "split_tick must be 0, 1 or 2");
     quiet_ok_ = opts.full_walks == 0;
     orient_ = opts.orientations != 0;
+    persistent_ = opts.persistent != 0;
+    if (opts.persistent > 1) return fail(VEDO_ERR_INVALID_ARGUMENT, "persistent must be 0 or 1");
     if (prev) {                    // a repacked engine keeps the tuning of the one it replaces
         skin_frac_ = prev->skin_frac_;
         cell_scale_ = prev->cell_scale_;
@@ -2742,6 +2973,7 @@ int MixedEngine::init_from(const std::vector<SceneSource>& src, const MixedEngin
         split_tick_ = prev->split_tick_;
         pair_pass_ = prev->pair_pass_;
         quiet_ok_ = prev->quiet_ok_;
+        persistent_ = prev->persistent_;
         tune_pending_ = prev->tune_pending_;
     }
     if (src.empty()) return fail(VEDO_ERR_INVALID_SCENE, "empty batch");
@@ -3073,6 +3305,44 @@ int MixedEngine::get_state_slice(uint32_t off, uint32_t cnt, const vedo_state_vi
     MCK(cudaStreamSynchronize(stream_));
     MCK(cudaGetLastError());
     return VEDO_OK;
+}
+
+// The wall kernel's arguments for a step that starts from buffer parity c.
+WallArgs MixedEngine::wargs(int c) {
+    WallArgs w;
+    w.nglob = (uint32_t)glob_.size();
+    w.glob = d_glob_;
+    w.model_of = d_model_of_;
+    w.models = d_models_;
+    w.scenes = d_scenes_;
+    w.scene_of = d_scene_of_;
+    w.xA = d_x_[c];
+    w.xB = d_x_[c ^ 1];
+    w.v64 = d_v64_;
+    w.w64 = d_w64_;
+    w.v32A = d_v32_[c];
+    w.v32B = d_v32_[c ^ 1];
+    w.w32A = d_w32_[c];
+    w.w32B = d_w32_[c ^ 1];
+    w.ox = d_ox_;
+    w.oz = d_oz_;
+    w.dt_max = dt_max_;
+    w.vmax_bits = d_red_ + 8;
+    w.vrel_bits = d_red_ + 2;
+    w.disp_in = d_disp_ + 4 * c;
+    w.disp_out = d_disp_ + 4 * (c ^ 1);
+    w.skin = skin_min_;
+    w.skin_w = WALL_SKIN * skin_min_;
+    w.pos_eps = pos_eps_;
+    w.wall_speed_bits = d_red_ + 12;
+    w.wrot = d_wrot_;
+    w.held = d_red_ + 11;
+    w.wall32 = d_wall32_;
+    w.nwork = d_red_ + 13;
+    w.imp = d_imp_;
+    w.aimp = d_aimp_;
+    w.dyn_bits = d_red_ + 3;
+    return w;
 }
 
 TickArgs MixedEngine::args(bool write_imp) {
@@ -3477,14 +3747,7 @@ void MixedEngine::launch_step(bool write_imp) {
                                                   d_scene_of_, d_gfield_, d_imp_, d_aimp_);
         ++launches_;
     }
-    note(step_launch(dep, k_walls, nblk(std::max<size_t>(glob_.size(), 1)), TPB, stream_,
-        (uint32_t)glob_.size(), (const uint32_t*)d_glob_, (const uint32_t*)d_model_of_, (const ModelDev*)d_models_,
-        (const SceneDev*)d_scenes_, (const uint32_t*)d_scene_of_, (const double4_32a*)a.xA, a.xB,
-        d_v64_, d_w64_, (const float4*)a.v32A, a.v32B, (const float4*)a.w32A,
-        a.w32B, d_ox_, d_oz_, dt_max_, d_red_ + 8, d_red_ + 2, (const float*)(d_disp_ + 4 * cur_),
-        d_disp_ + 4 * (cur_ ^ 1), skin_min_, WALL_SKIN * skin_min_, pos_eps_, (const unsigned*)(d_red_ + 12),
-        (const double4_32a*)d_wrot_, d_red_ + 11, d_wall32_, d_red_ + 13, (const double4_32a*)d_imp_,
-        (const double4_32a*)d_aimp_, d_red_ + 3));
+    note(step_launch(dep, k_walls, nblk(std::max<size_t>(glob_.size(), 1)), TPB, stream_, wargs(cur_)));
     ++launches_;
     if (dyn_walls_) {
         note(step_launch(dep, k_wall_bound, 1u, 32u, stream_, (const float*)(d_disp_ + 4 * cur_),
@@ -3495,8 +3758,65 @@ void MixedEngine::launch_step(bool write_imp) {
     cur_ ^= 1;
 }
 
+// `chunk` steps as one cooperative launch of the persistent tick; 0 = launched, -1 = the kernel
+// cannot have a block resident on every SM (the caller launches the steps one by one), > 0 an
+// error code.
+int MixedEngine::launch_persistent(uint32_t chunk) {
+    const unsigned block = pair_pass_ ? 1024u : 512u;
+    const void* k = nullptr;
+#define VEDO_PK(L)                                                                                     \
+    k = pair_pass_ ? (xs_stored_ ? (const void*)k_persist<2, L, true> : (const void*)k_persist<2, L, false>) \
+                   : (xs_stored_ ? (const void*)k_persist<0, L, true> : (const void*)k_persist<0, L, false>)
+    switch (law_) {
+    case IS_BSDBF: VEDO_PK(IS_BSDBF); break;
+    case IS_BTSDBF: VEDO_PK(IS_BTSDBF); break;
+    case IS_BSDB2F: VEDO_PK(IS_BSDB2F); break;
+    case IS_HERTZ: VEDO_PK(IS_HERTZ); break;
+    case IS_H: VEDO_PK(IS_H); break;
+    default: VEDO_PK(0); break;
+    }
+#undef VEDO_PK
+    if (k != pk_) {
+        int b = 0;
+        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k, (int)block, 0) != cudaSuccess) b = 0;
+        (void)cudaGetLastError();
+        pk_ = k;
+        pk_grid_ = (unsigned)std::max(b, 0) * (unsigned)sms_;
+    }
+    if (pk_grid_ == 0) return -1;
+    PersistArgs p;
+    const int c0 = cur_;
+    p.t[0] = args(false);
+    p.w[0] = wargs(c0);
+    cur_ = c0 ^ 1;
+    p.t[1] = args(false);
+    p.w[1] = wargs(c0 ^ 1);
+    cur_ = c0;
+    p.steps = chunk;
+    p.pbc = any_pbc_ ? 1 : 0;
+    p.bar.w = d_red_ + 4;
+    p.bar.nblocks = pk_grid_;
+    p.bar.limit_ns = 2000000000ull;
+    cudaLaunchConfig_t cfg{};
+    cfg.gridDim = dim3(pk_grid_);
+    cfg.blockDim = dim3(block);
+    cfg.dynamicSmemBytes = 0;
+    cfg.stream = stream_;
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeCooperative;
+    at[0].val.cooperative = 1;
+    cfg.attrs = at;
+    cfg.numAttrs = 1;
+    void* kargs[] = {&p};
+    MCK(cudaLaunchKernelExC(&cfg, k, kargs));
+    ++launches_;
+    if (chunk & 1) cur_ ^= 1;
+    return 0;
+}
+
 // `chunk` steps, then one read of the displacement bound and of the held-step count.  A full
-// check interval without impulse output replays a CUDA graph captured once per list.
+// check interval without impulse output replays a CUDA graph captured once per list, or runs as
+// one persistent launch.
 int MixedEngine::step_chunk(uint32_t chunk, bool imp_last, float* use_after) {
     const uint32_t ci = opts_.check_interval;
     if (profiling_ && pev_.size() < 3 * (size_t)ci) {
@@ -3507,7 +3827,14 @@ int MixedEngine::step_chunk(uint32_t chunk, bool imp_last, float* use_after) {
         }
     }
     pev_used_ = 0;
-    if (opts_.graphs && chunk == ci) {
+    int persisted = -1;
+    if (!imp_last && persist_usable()) {
+        persisted = launch_persistent(chunk);
+        if (persisted > 0) return persisted;
+    }
+    if (persisted == 0) {
+        // (launched)
+    } else if (opts_.graphs && chunk == ci) {
         const int c0 = cur_;
         const int gi = c0 + (profiling_ ? 2 : 0) + (imp_last ? 4 : 0);
         if (!graph_[gi]) {
@@ -3540,10 +3867,17 @@ int MixedEngine::step_chunk(uint32_t chunk, bool imp_last, float* use_after) {
         return cuda_fail(le, "kernel launch");
     }
     float dd[4] = {0.0f, 0.0f, 0.0f, 0.0f};
-    unsigned held = 0;
+    unsigned red[8] = {0, 0, 0, 0, 0, 0, 0, 0};    // [2], [3]: barrier expiry and its site; [7]: held steps
     MCK(cudaMemcpyAsync(dd, d_disp_ + 4 * cur_, 16, cudaMemcpyDeviceToHost, stream_));
-    MCK(cudaMemcpyAsync(&held, d_red_ + 11, 4, cudaMemcpyDeviceToHost, stream_));
+    MCK(cudaMemcpyAsync(red, d_red_ + 4, 32, cudaMemcpyDeviceToHost, stream_));
     MCK(cudaStreamSynchronize(stream_));
+    const unsigned held = red[7];
+    if (red[2]) {
+        MCK(cudaMemsetAsync(d_red_ + 4, 0, 16, stream_));
+        MCK(cudaStreamSynchronize(stream_));
+        return fail(VEDO_ERR_CUDA, "persistent tick: a grid barrier waited past its limit (barrier " +
+                                       std::to_string(red[3]) + " of the interval); the state is undefined");
+    }
     for (uint32_t q = 0; q + 3 <= pev_used_; q += 3) {   // profiling: tick and wall kernel times
         float a = 0.0f, b = 0.0f;
         cudaEventElapsedTime(&a, pev_[q], pev_[q + 1]);
@@ -3590,7 +3924,7 @@ int MixedEngine::autotune(uint32_t max_steps, uint32_t* taken) {
     const float skins[] = {0.05f, 0.1f, 0.15f, 0.25f, 0.4f};
     const float cells[] = {1.0f, 1.25f, 1.5f};
     // at most four chunks per timed trial (a rebuild between may add two), two per skin trial
-    const uint32_t need = ci * (uint32_t)(4 * (3 + 2 + 3) + 2 * 5);
+    const uint32_t need = ci * (uint32_t)(4 * (3 + 2 + 3 + 1) + 2 * 5);
     if (max_steps < need) return VEDO_OK;            // too short a call: tune in a later one
     cudaEvent_t e0 = ev_[2], e1 = ev_[3];
     auto timed_rebuild = [&](float* ms) -> int {
@@ -3685,6 +4019,17 @@ int MixedEngine::autotune(uint32_t max_steps, uint32_t* taken) {
         split_tick_ = !pair_pass_ && t_split < t_one;
         if (!pair_pass_) free_pair_bufs();
         drop_graphs();
+        // 2c. the chosen tick's check interval as one persistent launch, against the replayed
+        //     graph of per-step kernels just timed (the full tick and the pair pass)
+        persistent_ = false;
+        if (!split_tick_ && !dyn_walls_) {
+            const float t_graph = pair_pass_ ? t_pair : t_one;
+            float t_pers = 0.0f;
+            persistent_ = true;
+            if ((rc = timed_chunk(&t_pers, nullptr)) != VEDO_OK) return rc;
+            if (need_rebuild_ && (rc = rebuild()) != VEDO_OK) return rc;
+            persistent_ = pk_grid_ > 0 && t_pers < t_graph;
+        }
     }
     // 3. skin: tick time per step plus the amortised rebuild
     best = FLT_MAX;
@@ -4166,4 +4511,45 @@ uint32_t mixed_num_scenes(EngineBase* e) {
     return m ? m->num_scenes() : 1u;
 }
 
+// The persistent tick's grid barrier on its own (vedo_gpu_barrier_check).
+static int barrier_check(int device, uint32_t rounds, uint32_t extra, uint64_t limit_ns, uint32_t out[4]) {
+    if (cudaSetDevice(device) != cudaSuccess) return VEDO_ERR_CUDA;
+    int sms = 0, b = 0;
+    if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device) != cudaSuccess) return VEDO_ERR_CUDA;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_bar_check, 256, 0) != cudaSuccess || b < 1)
+        return VEDO_ERR_CUDA;
+    unsigned* d = nullptr;
+    if (cudaMalloc(&d, 8 * sizeof(unsigned)) != cudaSuccess) return VEDO_ERR_OUT_OF_MEMORY;
+    int rc = VEDO_OK;
+    unsigned h[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+    GridBar g;
+    g.w = d;
+    g.nblocks = (uint32_t)(sms * b) + extra;
+    g.limit_ns = limit_ns;
+    cudaLaunchConfig_t cfg{};
+    cfg.gridDim = dim3((unsigned)(sms * b));
+    cfg.blockDim = dim3(256);
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeCooperative;
+    at[0].val.cooperative = 1;
+    cfg.attrs = at;
+    cfg.numAttrs = 1;
+    if (cudaMemset(d, 0, 8 * sizeof(unsigned)) != cudaSuccess ||
+        cudaLaunchKernelEx(&cfg, k_bar_check, g, rounds, d + 4, d + 6) != cudaSuccess ||
+        cudaDeviceSynchronize() != cudaSuccess || cudaMemcpy(h, d, sizeof(h), cudaMemcpyDeviceToHost) != cudaSuccess)
+        rc = VEDO_ERR_CUDA;
+    cudaFree(d);
+    out[0] = h[6];
+    out[1] = h[7];
+    out[2] = h[2];
+    out[3] = h[3];
+    return rc;
+}
+
 }  // namespace vedo
+
+extern "C" int vedo_gpu_barrier_check(int32_t device, uint32_t rounds, uint32_t extra, uint64_t limit_ns,
+                                      uint32_t out[4]) {
+    if (!out || rounds == 0 || limit_ns == 0) return VEDO_ERR_INVALID_ARGUMENT;
+    return vedo::barrier_check(device, rounds, extra, limit_ns, out);
+}

@@ -75,7 +75,9 @@ def lib() -> C.CDLL:
         L.vedo_gpu_scene_range.argtypes = [vp, C.c_uint32, C.POINTER(C.c_uint32), C.POINTER(C.c_uint32),
                                            C.POINTER(C.c_double)]
         L.vedo_gpu_get_tuning.argtypes = [vp, C.POINTER(C.c_float), C.POINTER(C.c_float), C.POINTER(C.c_uint32),
-                                          C.POINTER(C.c_uint32), C.POINTER(C.c_uint32)]
+                                          C.POINTER(C.c_uint32), C.POINTER(C.c_uint32), C.POINTER(C.c_uint32)]
+        L.vedo_gpu_barrier_check.argtypes = [C.c_int32, C.c_uint32, C.c_uint32, C.c_uint64,
+                                             C.POINTER(C.c_uint32)]
         _lib = L
     return _lib
 
@@ -86,7 +88,7 @@ STATE_FIELDS = ("position", "velocity", "angular_velocity", "orientation_x", "or
 
 def _opts(up_iact, record, precision, device, prefix, skin, check_interval, tick_block=None, cell_scale=None,
           autotune=False, graphs=True, stored_splits=False, split_tick=False, full_walks=False,
-          consultant="nbs", pair_pass=False, orientations=False) -> EngineOpts:
+          consultant="nbs", pair_pass=False, orientations=False, persistent=False) -> EngineOpts:
     opts = EngineOpts()
     lib().vedo_gpu_default_opts(C.byref(opts))
     opts.up_iact, opts.record, opts.precision, opts.device = up_iact, record, precision, device
@@ -106,6 +108,7 @@ def _opts(up_iact, record, precision, device, prefix, skin, check_interval, tick
     opts.split_tick = 2 if pair_pass else (1 if split_tick else 0)
     opts.full_walks = 1 if full_walks else 0
     opts.orientations = 1 if orientations else 0
+    opts.persistent = 1 if persistent else 0
     if consultant not in ("nbs", "leap"):
         raise ValueError(f"consultant must be 'nbs' or 'leap', not {consultant!r}")
     opts.consultant = 1 if consultant == "leap" else 0
@@ -127,11 +130,13 @@ class GpuEngine:
                  check_interval: Optional[int] = None, tick_block: Optional[int] = None,
                  cell_scale: Optional[float] = None, autotune: bool = False, graphs: bool = True,
                  stored_splits: bool = False, split_tick: bool = False, full_walks: bool = False,
-                 consultant: str = "nbs", pair_pass: bool = False, orientations: bool = False):
+                 consultant: str = "nbs", pair_pass: bool = False, orientations: bool = False,
+                 persistent: bool = False):
         L = lib()
         self._prefix = output_prefix.encode() if output_prefix else None
         opts = _opts(up_iact, record, precision, device, self._prefix, skin, check_interval, tick_block, cell_scale,
-                     autotune, graphs, stored_splits, split_tick, full_walks, consultant, pair_pass, orientations)
+                     autotune, graphs, stored_splits, split_tick, full_walks, consultant, pair_pass, orientations,
+                     persistent)
         h = C.c_void_p()
         if isinstance(scene, (str, bytes, os.PathLike)):
             path = os.fsencode(scene)
@@ -243,13 +248,16 @@ class GpuEngine:
         self._check(lib().vedo_gpu_write_vtk(self.h, os.fsencode(path), 1 if with_coordination else 0))
 
     def tuning(self):
-        """Skin (fraction of r_max), cell scale, tick block size, split storage and the form of
-        the tick (single, split or pair pass) in use (MIXED form)."""
-        sk, cs, tb, ss, st = C.c_float(0), C.c_float(0), C.c_uint32(0), C.c_uint32(0), C.c_uint32(0)
+        """Skin (fraction of r_max), cell scale, tick block size, split storage, the form of the
+        tick (single, split or pair pass) and whether a check interval is one persistent launch,
+        in use (MIXED form)."""
+        sk, cs, tb, ss, st, pe = (C.c_float(0), C.c_float(0), C.c_uint32(0), C.c_uint32(0), C.c_uint32(0),
+                                  C.c_uint32(0))
         self._check(lib().vedo_gpu_get_tuning(self.h, C.byref(sk), C.byref(cs), C.byref(tb), C.byref(ss),
-                                              C.byref(st)))
+                                              C.byref(st), C.byref(pe)))
         return {"skin": float(sk.value), "cell_scale": float(cs.value), "tick_block": int(tb.value),
-                "stored_splits": bool(ss.value), "split_tick": st.value == 1, "pair_pass": st.value == 2}
+                "stored_splits": bool(ss.value), "split_tick": st.value == 1, "pair_pass": st.value == 2,
+                "persistent": bool(pe.value)}
 
     def run_with_impulses(self, impulse=None, angular_impulse=None) -> bool:
         """One step with an external impulse and angular impulse per object ([n, 3] arrays in
@@ -330,12 +338,12 @@ class BatchEngine(GpuEngine):
                  check_interval: Optional[int] = None, tick_block: Optional[int] = None,
                  cell_scale: Optional[float] = None, autotune: bool = False, graphs: bool = True,
                  full_walks: bool = False, split_tick: bool = False, pair_pass: bool = False,
-                 orientations: bool = False):
+                 orientations: bool = False, persistent: bool = False, stored_splits: bool = False):
         L = lib()
         self._prefix = None
         opts = _opts(1, 0, _abi.PRECISION_MIXED, device, None, skin, check_interval, tick_block, cell_scale,
-                     autotune, graphs, split_tick=split_tick, full_walks=full_walks, pair_pass=pair_pass,
-                     orientations=orientations)
+                     autotune, graphs, stored_splits=stored_splits, split_tick=split_tick, full_walks=full_walks,
+                     pair_pass=pair_pass, orientations=orientations, persistent=persistent)
         descs, keeps = [], []
         for sc in scene_list:
             if isinstance(sc, (str, bytes, os.PathLike)):

@@ -1,12 +1,13 @@
 """Run one workload of the engine, for a profiler or a quick timing.
 
     python -m vedo_gb300.profile_case <drum|settled|dense|bed|hopper> <spheres> <steps> [--fp64] [--block B]
-                                      [--stored] [--split | --pair] [--skin S]
+                                      [--stored] [--split | --pair] [--skin S] [--persistent]
 
 Builds the seeded scene (`settled`: the polydisperse drum after 300,000 steps of settling, made
 once per host by vedo_gb300.workloads.settled_drum and cached there), creates the engine (mixed form unless --fp64; fixed settings, no
-autotuning, no graph replay, so that every step is one set of plain launches), runs 5 warm-up
-steps and then <steps> steps, and prints the device time per step.  Under ncu, skip the warm-up
+autotuning, no graph replay, so that every step is one set of plain launches; --persistent: each
+check interval one cooperative launch instead), runs 5 warm-up steps and then <steps> steps, and
+prints the device time per step.  Under ncu, skip the warm-up
 launches with -s and capture the kernel of interest with -k / -c.
 """
 from __future__ import annotations
@@ -45,13 +46,14 @@ def main(argv=None):
     ap.add_argument("--split", action="store_true", help="light tick + full tick over the deferred spheres")
     ap.add_argument("--pair", action="store_true", help="pair pass: prefilter pass, one evaluation per pair, sums")
     ap.add_argument("--skin", type=float, default=None, help="candidate-list skin (fraction of r_max)")
+    ap.add_argument("--persistent", action="store_true", help="one cooperative launch per check interval")
     a = ap.parse_args(argv)
     sc = make(a.kind, a.n)
     if a.fp64:
         e = GpuEngine(sc, up_iact=20)
     else:
         e = GpuEngine(sc, precision=1, tick_block=a.block, graphs=False, stored_splits=a.stored, split_tick=a.split,
-                      pair_pass=a.pair, skin=a.skin)
+                      pair_pass=a.pair, skin=a.skin, persistent=a.persistent)
     e.run(5)
     e.run(a.steps)
     p = e.last_run_profile()

@@ -80,7 +80,8 @@ class Server:
                      engine_opts.get("check_interval"), engine_opts.get("tick_block"), engine_opts.get("cell_scale"),
                      engine_opts.get("autotune", False), engine_opts.get("graphs", True),
                      split_tick=engine_opts.get("split_tick", False), pair_pass=engine_opts.get("pair_pass", False),
-                     orientations=engine_opts.get("orientations", False))
+                     orientations=engine_opts.get("orientations", False),
+                     persistent=engine_opts.get("persistent", False))
         h = C.c_void_p()
         rc = L.vedo_srv_create(C.byref(opts), int(hbm_budget_bytes), C.byref(h))
         if rc != 0:
