@@ -106,6 +106,27 @@ def test_lsd_box_full_size_bitexact(engine_lib, port_lib):
     assert np.array_equal(ia["first"], f) and np.array_equal(ia["second"], s)
 
 
+def test_two_pass_pair_kernel_bitexact(engine_lib, port_lib):
+    """A box of 39,304 spheres thrown together (about 50,000 contacts after 200 steps), whose
+    candidate list is longer than the one-pass pair kernel takes: the prefilter pass compacts the pairs that may touch and the exact pass evaluates them in full
+    warps; 200 steps with rebuilds every 20, bit for bit against the oracle."""
+    from oracle import PortWorld
+    sc = scenes.lsd_box(n_side=34, box_width=0.08, box_height=0.1, steps=400, spacing=2.005e-3, vel_sigma=0.3)
+    e = engine_lib.GpuEngine(sc, up_iact=20)
+    p = PortWorld(sc, up_iact=20)
+    assert len(e.interactions()["first"]) > (1 << 17)
+    e.run(200)
+    p.run(200)
+    a, b = e.state(), p.state()
+    for k in ("position", "velocity", "angular_velocity", "impact", "angular_impact"):
+        np.testing.assert_array_equal(a[k], b[k], err_msg=k)
+    ia, ib = e.interactions(), p.interactions()
+    f, s = p.candidates()
+    assert np.array_equal(ia["first"], f) and np.array_equal(ia["second"], s)
+    assert np.array_equal(ia["active"], ib["active"].astype(np.uint8))
+    assert ia["active"].sum() > 10000
+
+
 def test_first_100_steps_pointwise_hertz_drum_small(engine_lib, port_lib):
     """Polydisperse ISwH drum (orbital end plates, polygon shell), 20k spheres: pointwise agreement
     for the first 100 steps (1e-9 relative), exact contact set."""

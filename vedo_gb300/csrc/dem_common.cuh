@@ -121,8 +121,14 @@ __host__ __device__ __forceinline__ d3 wrap_position(const Periodic& b, d3 p) {
     return p;
 }
 #ifdef __CUDACC__
-// Vector3d::rotate_around (Vector3d.h:152-178)
-__device__ __forceinline__ d3 rotate_around(d3 p, d3 va) {
+// Vector3d::rotate_around (Vector3d.h:152-178), in two parts: the turn's half-angle terms (its
+// axis scaled by sin(a/2), and cos(a/2)), then the rotation of a vector with them, so that an
+// object's two orientation vectors share one evaluation of the transcendentals.
+struct Turn {
+    d3 v;
+    double s;
+};
+__device__ __forceinline__ Turn turn_of(d3 va) {
     d3 u = dir(va);
     double a = len(va);
     // cos(0) = 1 and sin(+0) = +0 exactly: a zero turn (an object not spinning) skips the two FP64
@@ -132,11 +138,16 @@ __device__ __forceinline__ d3 rotate_around(d3 p, d3 va) {
         s = cos(0.5 * a);
         t = sin(0.5 * a);
     }
-    d3 v = muls(u, t);
+    return Turn{muls(u, t), s};
+}
+__device__ __forceinline__ d3 rotate_by(d3 p, const Turn& T) {
+    const d3 v = T.v;
+    const double s = T.s;
     d3 r = add(smul(s * s, p), smul(dot(p, v), v));
     r = add(r, smul(2.0 * s, cross(v, p)));
     return add(r, cross(v, cross(v, p)));
 }
+__device__ __forceinline__ d3 rotate_around(d3 p, d3 va) { return rotate_by(p, turn_of(va)); }
 
 __device__ __forceinline__ d3 ld(const double4_32a* p, uint32_t i) {
     double4_32a v = p[i];

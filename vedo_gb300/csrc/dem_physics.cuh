@@ -261,23 +261,26 @@ __device__ __forceinline__ void respond_object(const ModelDev& m, double dt, d3 
         d3 dp = smul(dt, add(V, smul(0.5, dv)));
         d3 dw = smul(dt, add(AV, smul(0.5, dav)));
         P = add(P, dp);
-        Ox = rotate_around(Ox, dw);
-        Oz = rotate_around(Oz, dw);
+        const Turn T = turn_of(dw);
+        Ox = rotate_by(Ox, T);
+        Oz = rotate_by(Oz, T);
         V = add(V, dv);
         AV = add(AV, dav);
     } else if (m.behavior == BEH_ORBITAL) {                   // DOOrbitalQuasiPlate.cpp:18-34
         d3 dp = muls(V, dt);
         d3 dw = muls(AV, dt);
         P = add(P, dp);
-        Ox = rotate_around(Ox, dw);
-        Oz = rotate_around(Oz, dw);
+        const Turn T = turn_of(dw);
+        Ox = rotate_by(Ox, T);
+        Oz = rotate_by(Oz, T);
     } else if (m.behavior == BEH_CONSTRAINED) {               // DOConstrainedQuasiPlate.cpp:18-35
         d3 dv = smul(m.inv_sudo, smul(dot(J, Oz), dir(Oz)));
         d3 dp = smul(dt, add(V, smul(0.5, dv)));
         d3 dw = muls(AV, dt);
         P = add(P, dp);
-        Ox = rotate_around(Ox, dw);
-        Oz = rotate_around(Oz, dw);
+        const Turn T = turn_of(dw);
+        Ox = rotate_by(Ox, T);
+        Oz = rotate_by(Oz, T);
         V = add(V, dv);
     } else {                                                  // DOQuasiPlate.cpp:20-41, DOQuasiCylinder.cpp
         d3 dv = smul(m.inv_sudo, J);
@@ -285,8 +288,9 @@ __device__ __forceinline__ void respond_object(const ModelDev& m, double dt, d3 
         d3 dp = smul(dt, add(V, smul(0.5, dv)));
         d3 dw = smul(dt, add(AV, smul(0.5, dav)));
         P = add(P, dp);
-        Ox = rotate_around(Ox, dw);
-        Oz = rotate_around(Oz, dw);
+        const Turn T = turn_of(dw);
+        Ox = rotate_by(Ox, T);
+        Oz = rotate_by(Oz, T);
         V = add(V, dv);
         AV = add(AV, dav);
     }

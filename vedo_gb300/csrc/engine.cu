@@ -3,10 +3,10 @@
 // Built with -fmad=false: the FP64 arithmetic below reproduces the reference's IEEE
 // operation sequence (see dem_physics.cuh).  Per time step (SimMediator::Run,
 // SimMediator.cpp:714-842) two kernels run:
-//   k_pair  - one thread per candidate pair: narrow phase at the current positions
-//             (the ContactInfo the reference computed at the end of the previous
-//             step) + impact solver + status update; the impulses go to a per-pair
-//             output record.
+//   k_pair_pf, k_pair_exact - the FP32 prefilter over every candidate pair, then for the
+//             pairs it leaves (in full warps): narrow phase at the current positions (the
+//             ContactInfo the reference computed at the end of the previous step) + impact
+//             solver + status update; the impulses go to a per-pair output record.
 //   k_obj   - one thread per local object: the pair impulses in candidate-list order
 //             (the reference's IactContainer order), the field impulse, the external
 //             force and DiscreteObject::Response.  Scope-global objects (walls) are
@@ -34,6 +34,8 @@ namespace {
 
 constexpr int TPB = 256;
 inline unsigned blocks_for(uint64_t n, int tpb = TPB) { return (unsigned)((n + tpb - 1) / tpb); }
+// Candidate lists up to this length take the one-pass pair kernel (the step is launch-bound there)
+constexpr uint32_t FUSED_PAIRS = 1u << 17;
 
 // Neighbour visiting order of NBSConsultant::Reset (NBSConsultant.cpp:202-270):
 // 12 = the cell itself (i < j), 13 = all scope-global objects.
@@ -90,33 +92,64 @@ __host__ __device__ inline double dbl_of(unsigned long long o) {
 
 // ------------------------------------------------------------------------------------
 // time step
-__global__ void __launch_bounds__(TPB) k_pair(uint32_t np, const uint2* __restrict__ sm,
-                                              const uint32_t* __restrict__ param, const PairParam* __restrict__ params,
-                                              const double4_32a* __restrict__ geom, const double4_32a* __restrict__ hole,
-                                              const float* __restrict__ reach,
-                                              const double4_32a* __restrict__ pos,
-                                              const double4_32a* __restrict__ vel, const double4_32a* __restrict__ av,
-                                              const double4_32a* __restrict__ ox, const double4_32a* __restrict__ oz,
-                                              const float4* __restrict__ pos32, const float4* __restrict__ wall32,
-                                              double4_32a* __restrict__ hist, double* __restrict__ v0,
-                                              uint8_t* __restrict__ flags, double* __restrict__ out, double dt,
-                                              int backup, Periodic pb, uint8_t* __restrict__ touched) {
+// CalculateImpact in two passes, so that the FP64 work runs in full warps (the FP64 pipe issues a
+// warp instruction at the same cost however few of its lanes are active, and most candidate pairs
+// are apart):
+//  k_pair_pf     one thread per candidate pair: the FP32 prefilter; a pair that is certainly apart
+//                and carries no normal bond gets ImpactStatus::Clean and no impulse, the others are
+//                appended to the worklist (warp-aggregated);
+//  k_pair_exact  the worklist's pairs: narrow phase at the current positions + impact solver +
+//                status update, each pair's operations exactly those of a single pass, written to
+//                the pair's own records (the order of the worklist does not matter).
+__global__ void __launch_bounds__(TPB) k_pair_pf(uint32_t np, const uint2* __restrict__ sm,
+                                                 const uint32_t* __restrict__ param,
+                                                 const PairParam* __restrict__ params, const float* __restrict__ reach,
+                                                 const float4* __restrict__ pos32, const float4* __restrict__ wall32,
+                                                 double4_32a* __restrict__ hist, double* __restrict__ v0,
+                                                 uint8_t* __restrict__ flags, Periodic pb, uint32_t* __restrict__ work,
+                                                 uint32_t* __restrict__ nwork) {
     const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
-    if (k >= np) return;
+    bool near = false;
+    if (k < np) {
+        const uint2 p = sm[k];
+        const uint32_t pi = param[k];
+        const int cd = params[pi].cd, is = params[pi].is;
+        // Pairs that are certainly apart and carry no normal bond: ImpactStatus::Clean, no impulse.
+        const bool bondable = (is == IS_BSDBF || is == IS_BTSDBF || is == IS_BSDB2F) && params[pi].c[4] != 0.0;
+        if (!bondable &&
+            certainly_apart(cd, pos32[p.x], pos32[p.y], wall32[p.y], reach[pi], pb.on ? pb.range32 : nullptr)) {
+            const uint8_t f0 = flags[k];
+            if (f0 & PF_NONZERO) {
+                hist[k] = make_double4_32a(0.0, 0.0, 0.0, 0.0);
+                v0[k] = 0.0;
+            }
+            if (f0 != 0) flags[k] = 0;
+        } else {
+            near = true;
+        }
+    }
+    const unsigned m = __ballot_sync(0xffffffffu, near);
+    if (m) {
+        const int lane = threadIdx.x & 31, lead = __ffs(m) - 1;
+        uint32_t at = 0;
+        if (lane == lead) at = atomicAdd(nwork, (uint32_t)__popc(m));
+        at = __shfl_sync(0xffffffffu, at, lead);
+        if (near) work[at + __popc(m & ((1u << lane) - 1u))] = k;
+    }
+}
+
+__device__ __forceinline__ void pair_exact(uint32_t k, const uint2* __restrict__ sm,
+                                           const uint32_t* __restrict__ param, const PairParam* __restrict__ params,
+                                           const double4_32a* __restrict__ geom, const double4_32a* __restrict__ hole,
+                                           const double4_32a* __restrict__ pos,
+                                           const double4_32a* __restrict__ vel, const double4_32a* __restrict__ av,
+                                           const double4_32a* __restrict__ ox, const double4_32a* __restrict__ oz,
+                                           double4_32a* __restrict__ hist, double* __restrict__ v0,
+                                           uint8_t* __restrict__ flags, double* __restrict__ out, double dt,
+                                           int backup, const Periodic& pb, uint8_t* __restrict__ touched) {
     const uint2 p = sm[k];
     const uint32_t pi = param[k];
     const int cd = params[pi].cd, is = params[pi].is;
-    // Pairs that are certainly apart and carry no normal bond: ImpactStatus::Clean, no impulse.
-    const bool bondable = (is == IS_BSDBF || is == IS_BTSDBF || is == IS_BSDB2F) && params[pi].c[4] != 0.0;
-    if (!bondable && certainly_apart(cd, pos32[p.x], pos32[p.y], wall32[p.y], reach[pi], pb.on ? pb.range32 : nullptr)) {
-        const uint8_t f0 = flags[k];
-        if (f0 & PF_NONZERO) {
-            hist[k] = make_double4_32a(0.0, 0.0, 0.0, 0.0);
-            v0[k] = 0.0;
-        }
-        if (f0 != 0) flags[k] = 0;
-        return;
-    }
     const double4_32a gg = geom[pi];
     PairGeom g{gg.x, gg.y, gg.z, gg.w, 0.0, 0.0, 0.0};
     if (cd == CD_SHP) {
@@ -173,6 +206,62 @@ __global__ void __launch_bounds__(TPB) k_pair(uint32_t np, const uint2* __restri
         touched[p.x] = 1;              // both objects have an impulse to gather this step
         touched[p.y] = 1;
     }
+}
+
+// Both passes in one thread per candidate pair, for short lists (one launch less per step where
+// the step is launch-bound; the same operations per pair).
+__global__ void __launch_bounds__(TPB) k_pair_fused(uint32_t np, const uint2* __restrict__ sm,
+                                                    const uint32_t* __restrict__ param,
+                                                    const PairParam* __restrict__ params,
+                                                    const double4_32a* __restrict__ geom,
+                                                    const double4_32a* __restrict__ hole,
+                                                    const float* __restrict__ reach,
+                                                    const double4_32a* __restrict__ pos,
+                                                    const double4_32a* __restrict__ vel,
+                                                    const double4_32a* __restrict__ av,
+                                                    const double4_32a* __restrict__ ox,
+                                                    const double4_32a* __restrict__ oz,
+                                                    const float4* __restrict__ pos32,
+                                                    const float4* __restrict__ wall32, double4_32a* __restrict__ hist,
+                                                    double* __restrict__ v0, uint8_t* __restrict__ flags,
+                                                    double* __restrict__ out, double dt, int backup, Periodic pb,
+                                                    uint8_t* __restrict__ touched) {
+    const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= np) return;
+    const uint2 p = sm[k];
+    const uint32_t pi = param[k];
+    const int cd = params[pi].cd, is = params[pi].is;
+    const bool bondable = (is == IS_BSDBF || is == IS_BTSDBF || is == IS_BSDB2F) && params[pi].c[4] != 0.0;
+    if (!bondable && certainly_apart(cd, pos32[p.x], pos32[p.y], wall32[p.y], reach[pi], pb.on ? pb.range32 : nullptr)) {
+        const uint8_t f0 = flags[k];
+        if (f0 & PF_NONZERO) {
+            hist[k] = make_double4_32a(0.0, 0.0, 0.0, 0.0);
+            v0[k] = 0.0;
+        }
+        if (f0 != 0) flags[k] = 0;
+        return;
+    }
+    pair_exact(k, sm, param, params, geom, hole, pos, vel, av, ox, oz, hist, v0, flags, out, dt, backup, pb, touched);
+}
+
+__global__ void __launch_bounds__(TPB) k_pair_exact(const uint32_t* __restrict__ work,
+                                                    const uint32_t* __restrict__ nwork, const uint2* __restrict__ sm,
+                                                    const uint32_t* __restrict__ param,
+                                                    const PairParam* __restrict__ params,
+                                                    const double4_32a* __restrict__ geom,
+                                                    const double4_32a* __restrict__ hole,
+                                                    const double4_32a* __restrict__ pos,
+                                                    const double4_32a* __restrict__ vel,
+                                                    const double4_32a* __restrict__ av,
+                                                    const double4_32a* __restrict__ ox,
+                                                    const double4_32a* __restrict__ oz, double4_32a* __restrict__ hist,
+                                                    double* __restrict__ v0, uint8_t* __restrict__ flags,
+                                                    double* __restrict__ out, double dt, int backup, Periodic pb,
+                                                    uint8_t* __restrict__ touched) {
+    const uint32_t nw = *nwork;
+    for (uint32_t q = blockIdx.x * blockDim.x + threadIdx.x; q < nw; q += gridDim.x * blockDim.x)
+        pair_exact(work[q], sm, param, params, geom, hole, pos, vel, av, ox, oz, hist, v0, flags, out, dt, backup, pb,
+                   touched);
 }
 
 __device__ __forceinline__ void add_entry(uint32_t ent, uint8_t f, const double* __restrict__ out, d3& J, d3& JA) {
@@ -252,8 +341,9 @@ __global__ void __launch_bounds__(TPB) k_obj(uint32_t n, const uint32_t* __restr
                                              double dt, d3 fimp, int write_imp, d3 origin, float4* __restrict__ pos32,
                                              float4* __restrict__ wall32, const double* __restrict__ ext_imp,
                                              const double* __restrict__ ext_aimp, Periodic pb,
-                                             uint8_t* __restrict__ touched) {
+                                             uint8_t* __restrict__ touched, uint32_t* __restrict__ nwork) {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i == 0) *nwork = 0u;                                   // the pair worklist, empty for the next step
     if (i >= n) return;
     const ModelDev& m = models[model_of[i]];
     if (m.scope == SCOPE_GLOBAL) return;
@@ -311,8 +401,10 @@ __global__ void k_obj_global(uint32_t nglob, const uint32_t* __restrict__ glob, 
                     }
                 }
             }
-            const uint32_t cnt = min(32u, e1 - base);
-            for (uint32_t q = 0; q < cnt; ++q) {
+            // only the entries that applied an impulse, in entry order (a wall's candidate list is
+            // long and few of its spheres touch it)
+            for (unsigned am = __ballot_sync(0xffffffffu, app != 0); am; am &= am - 1) {
+                const int q = __ffs(am) - 1;
                 const int a = __shfl_sync(0xffffffffu, app, q);
                 const double bx = __shfl_sync(0xffffffffu, jx, q), by = __shfl_sync(0xffffffffu, jy, q),
                              bz = __shfl_sync(0xffffffffu, jz, q);
@@ -806,7 +898,7 @@ static cudaError_t dalloc(T** p, size_t count) {
 
 void Engine::free_list(PairList& L) {
     cudaFree(L.first); cudaFree(L.second); cudaFree(L.sm); cudaFree(L.param); cudaFree(L.hist); cudaFree(L.v0);
-    cudaFree(L.flags); cudaFree(L.out); cudaFree(L.csr_ent); cudaFree(L.csr_ptr);
+    cudaFree(L.flags); cudaFree(L.out); cudaFree(L.csr_ent); cudaFree(L.csr_ptr); cudaFree(L.work);
     L = PairList{};
 }
 
@@ -823,6 +915,7 @@ int Engine::ensure_list(PairList& L, uint32_t cap) {
     CK(dalloc(&L.first, c)); CK(dalloc(&L.second, c)); CK(dalloc(&L.sm, c)); CK(dalloc(&L.param, c));
     CK(dalloc(&L.hist, c)); CK(dalloc(&L.v0, c)); CK(dalloc(&L.flags, c)); CK(dalloc(&L.out, 9 * c));
     CK(dalloc(&L.csr_ent, 2 * c));
+    CK(dalloc(&L.work, c));
     return VEDO_OK;
 }
 
@@ -835,7 +928,7 @@ Engine::~Engine() {
                     d_oz_, d_imp_, d_aimp_, d_global_, d_safe_, d_red_, d_key_, d_key_alt_, d_cell_key_, d_sid_,
                     d_sid_alt_, d_cell_start_, d_cellof_, d_flag_, d_task_, d_total_, d_ck_, d_cv_, d_ck_alt_,
                     d_cv_alt_, d_cnt_, d_rec_key_, d_rec_hist_, d_rec_v0_, d_rec_flags_, d_obs_, d_stage_,
-                    d_pos32_, d_wall32_, d_reach_, d_grid_, d_ext_, d_hole_, d_touched_};
+                    d_pos32_, d_wall32_, d_reach_, d_grid_, d_ext_, d_hole_, d_touched_, d_nwork_};
     for (void* p : ptrs) if (p) cudaFree(p);
     for (auto& e : ev_) if (e) cudaEventDestroy(e);
     if (stream_) cudaStreamDestroy(stream_);
@@ -916,6 +1009,8 @@ int Engine::init(const HScene& scene, const vedo_engine_opts& opts) {
         CK(dalloc(&d_wall32_, n_));
         CK(dalloc(&d_touched_, n_));
         CK(cudaMemset(d_touched_, 0, n_));
+        CK(dalloc(&d_nwork_, 1));
+        CK(cudaMemset(d_nwork_, 0, sizeof(uint32_t)));
         CK(cudaMemset(d_wall32_, 0, sizeof(float4) * n_));
         std::vector<float> reach((size_t)nm_ * nm_, 0.0f);
         for (size_t q = 0; q < reach.size(); ++q) {
@@ -1316,22 +1411,37 @@ int Engine::step_once(bool write_impulses) {
     const bool prof = profiling_;
     // CalculateImpact
     if (prof) CK(cudaEventRecord(ev_[0], stream_));
-    if (cur_.np) {
-        k_pair<<<blocks_for(cur_.np), TPB, 0, stream_>>>(cur_.np, cur_.sm, cur_.param, d_params_, d_geom_, d_hole_,
-                                                         d_reach_,
-                                                         d_pos_, d_vel_, d_av_, d_ox_, d_oz_, d_pos32_, d_wall32_,
-                                                         cur_.hist, cur_.v0, cur_.flags, cur_.out, dt,
-                                                         backup_pending_ ? 1 : 0, tab_.pbc, d_touched_);
+    if (cur_.np && cur_.np <= FUSED_PAIRS) {
+        k_pair_fused<<<blocks_for(cur_.np), TPB, 0, stream_>>>(cur_.np, cur_.sm, cur_.param, d_params_, d_geom_,
+                                                               d_hole_, d_reach_, d_pos_, d_vel_, d_av_, d_ox_, d_oz_,
+                                                               d_pos32_, d_wall32_, cur_.hist, cur_.v0, cur_.flags,
+                                                               cur_.out, dt, backup_pending_ ? 1 : 0, tab_.pbc,
+                                                               d_touched_);
         ++launches_;
+    } else if (cur_.np) {
+        k_pair_pf<<<blocks_for(cur_.np), TPB, 0, stream_>>>(cur_.np, cur_.sm, cur_.param, d_params_, d_reach_,
+                                                            d_pos32_, d_wall32_, cur_.hist, cur_.v0, cur_.flags,
+                                                            tab_.pbc, cur_.work, d_nwork_);
+        if (!pair_grid_) {                         // the exact pass strides with the grid resident at once
+            int b = 0;
+            if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_pair_exact, TPB, 0) != cudaSuccess || b < 1) b = 1;
+            int sms = 1;
+            cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, opts_.device);
+            pair_grid_ = (unsigned)(b * std::max(sms, 1));
+        }
+        k_pair_exact<<<std::min<unsigned>(pair_grid_, blocks_for(cur_.np)), TPB, 0, stream_>>>(
+            cur_.work, d_nwork_, cur_.sm, cur_.param, d_params_, d_geom_, d_hole_, d_pos_, d_vel_, d_av_, d_ox_,
+            d_oz_, cur_.hist, cur_.v0, cur_.flags, cur_.out, dt, backup_pending_ ? 1 : 0, tab_.pbc, d_touched_);
+        launches_ += 2;
     }
     if (prof) CK(cudaEventRecord(ev_[1], stream_));
-    // AddFieldImpact + AddConstrainedImpact + Response (+ CheckContactStatus in the next k_pair)
+    // AddFieldImpact + AddConstrainedImpact + Response (+ CheckContactStatus in the next k_pair_exact)
     const d3 fimp = muls(mk(g_[0], g_[1], g_[2]), dt);    // csp->GetFieldAcceleration() * dt (SimMediator.cpp:738)
     const d3 org = mk(origin_[0], origin_[1], origin_[2]);
     k_obj<<<blocks_for(n_), TPB, 0, stream_>>>(n_, d_model_of_, d_models_, d_pos_, d_vel_, d_av_, d_ox_, d_oz_,
                                                d_imp_, d_aimp_, cur_.csr_ptr, cur_.csr_ent, cur_.flags, cur_.out, dt,
                                                fimp, write_impulses ? 1 : 0, org, d_pos32_, d_wall32_, ext_imp_, ext_aimp_,
-                                               tab_.pbc, d_touched_);
+                                               tab_.pbc, d_touched_, d_nwork_);
     ++launches_;
     if (!global_ids_.empty()) {
         k_obj_global<<<blocks_for((uint64_t)global_ids_.size() * 32), TPB, 0, stream_>>>(

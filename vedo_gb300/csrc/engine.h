@@ -37,6 +37,7 @@ struct PairList {
     double* out = nullptr;       // [cap][9]: J, tA, tB of the last solve
     uint32_t* csr_ent = nullptr; // [2*cap]
     uint32_t* csr_ptr = nullptr; // [n+1]
+    uint32_t* work = nullptr;    // [cap]: the pairs the prefilter left this step (any order)
 };
 
 class Engine : public EngineBase {
@@ -134,8 +135,10 @@ private:
     // FP32 prefilter copies (prefilter.cuh): position offsets from origin_, unit wall axes,
     // and per (slave model, master model) the contact reach rounded up to float
     float4* d_pos32_ = nullptr;
-    // per object: 1 when a pair of this step applied an impulse to it (k_pair sets, k_obj clears)
+    // per object: 1 when a pair of this step applied an impulse to it (k_pair_exact sets, k_obj clears)
     uint8_t* d_touched_ = nullptr;
+    uint32_t* d_nwork_ = nullptr;   // pairs in the current list's worklist (k_obj empties it)
+    unsigned pair_grid_ = 0;        // blocks of k_pair_exact resident at once
     // the candidate list of LeapConsultant (else NBSConsultant), and its cell edge's largest range
     bool leap_ = false;
     double leap_rmax_ = 0.0;

@@ -1075,8 +1075,9 @@ __device__ __forceinline__ void turn_sphere(const TickArgs& a, uint32_t i) {
     const d3 W2 = ld(a.w64, i);
     const d3 dwv = smul(S.dt, sub(W2, smul(0.5, mk(f2d(dav.x), f2d(dav.y), f2d(dav.z)))));
     if (dwv.x == 0.0 && dwv.y == 0.0 && dwv.z == 0.0) return;
-    st(a.sox, i, rotate_around(ld(a.sox, i), dwv), 0.0);
-    st(a.soz, i, rotate_around(ld(a.soz, i), dwv), 0.0);
+    const Turn T = turn_of(dwv);
+    st(a.sox, i, rotate_by(ld(a.sox, i), T), 0.0);
+    st(a.soz, i, rotate_by(ld(a.soz, i), T), 0.0);
 }
 __global__ void __launch_bounds__(TPB) k_turn(TickArgs a) {
     step_order();
@@ -1497,8 +1498,9 @@ __device__ __forceinline__ void walls_item(const WallArgs& W, uint32_t q) {
             V = add(V, dv);
             AV = add(AV, dav);
         }
-        Ox = rotate_around(Ox, dw);
-        Oz = rotate_around(Oz, dw);
+        const Turn T = turn_of(dw);
+        Ox = rotate_by(Ox, T);
+        Oz = rotate_by(Oz, T);
         st(ox, w, Ox, 0.0);
         st(oz, w, Oz, 0.0);
         st(v64, w, V, 0.0);
