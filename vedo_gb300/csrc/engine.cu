@@ -351,8 +351,19 @@ __global__ void __launch_bounds__(TPB) k_obj(uint32_t n, const uint32_t* __restr
     // an object no pair applied an impulse to keeps zero sums: its ordered walk adds nothing
     if (touched[i]) {
         touched[i] = 0;
-        const uint32_t e1 = csr_ptr[i + 1];
-        for (uint32_t e = csr_ptr[i]; e < e1; ++e) {
+        const uint32_t e0 = csr_ptr[i], e1 = csr_ptr[i + 1];
+        // the entries that applied an impulse are marked first (integer work), then summed in entry
+        // order: a warp issues each FP64 add once per marked entry of its busiest object, not once
+        // per candidate entry (most candidates of an object apply nothing)
+        const uint32_t c1 = min(e1, e0 + 64u);
+        unsigned long long mark = 0ull;
+        for (uint32_t e = e0; e < c1; ++e)
+            if (flags[csr_ent[e] >> 1] & PF_APPLIED) mark |= 1ull << (e - e0);
+        for (; mark; mark &= mark - 1) {
+            const uint32_t ent = csr_ent[e0 + (uint32_t)(__ffsll(mark) - 1)];
+            add_entry(ent, flags[ent >> 1], out, J, JA);
+        }
+        for (uint32_t e = c1; e < e1; ++e) {                   // long lists: the entries after 64
             const uint32_t ent = csr_ent[e];
             add_entry(ent, flags[ent >> 1], out, J, JA);
         }
