@@ -788,7 +788,9 @@ __device__ __forceinline__ float2 finish_sphere(const TickArgs& a, uint32_t i, b
 // so both members of a sphere pair obtain the same bits; the history owner writes the new status
 // into the other buffer, a wall entry writes the wall's share of the impulse.  Returns 0 (nothing
 // added), 1 (impulse J only) or 2 (J and the torques tA on the slave, tB on the master).
-template <int LAW, bool XS>
+// KIND: 0 any entry; 1 a sphere pair, 2 a wall pair (the other branch is not compiled: a kernel
+// without the out-of-line wall detector's call keeps its locals in registers).
+template <int LAW, bool XS, int KIND = 0>
 __device__ __forceinline__ int exact_pair(const TickArgs& a, const SceneDev& S, uint32_t i, const d3& Pi, uint32_t e,
                                           uint32_t ent, uint32_t meta, f3& Jp, f3& tA, f3& tB) {
     const float dtf = S.dtf;
@@ -804,7 +806,7 @@ __device__ __forceinline__ int exact_pair(const TickArgs& a, const SceneDev& S, 
     bool active;
     float depth;
     f3 n, rA, rB;
-    if (P.cd == CD_SS) {
+    if (KIND == 1 || (KIND == 0 && P.cd == CD_SS)) {
         // d = x_master - x_slave, |d|^2 and R^2 - |d|^2 in double-float from the two
         // positions' hi/lo splits; where the numerator is within 1e-9 R^2 of zero the
         // reference's FP64 formula decides
@@ -847,7 +849,7 @@ __device__ __forceinline__ int exact_pair(const TickArgs& a, const SceneDev& S, 
         n = fdir(df);
         rA = (a.pc32[8 * (size_t)pi + 7] - 0.5f * depth) * n;   // slot 7: the slave's radius
         rB = rA - df;
-    } else {
+    } else if (KIND != 1) {
         wall_pair(a, P.cd, pi, s, m, active, depth, n, rA, rB, S.pb);
     }
     const uint8_t f0 = a.fA[slot];
@@ -1175,9 +1177,9 @@ __device__ __forceinline__ void pf_sphere(const TickArgs& a, uint32_t i) {
                 for (uint32_t e = c0; e < c1; ++e) a.xf[e] = (uint8_t)((exact >> (e - c0)) & 1ull);
             }
         }
-        // sphere pairs fill the worklist from its start, wall pairs from its end, so that the
-        // pair kernel runs each kind in full warps (a wall pair's detector is FP64 work, and a
-        // warp issues it once for every lane that needs it)
+        // sphere pairs fill the worklist from its start, wall pairs from its end, so that each
+        // kind has a pair kernel of its own, in full warps (a wall pair's detector is FP64 work,
+        // and a warp issues it once for every lane that needs it)
         const uint32_t cnt = (uint32_t)__popcll(own), wcnt = (uint32_t)__popcll(wown);
         uint32_t incl = cnt, wincl = wcnt;         // inclusive prefixes over the warp
 #pragma unroll
@@ -1222,12 +1224,12 @@ __global__ void __launch_bounds__(TPB, 4) k_tick_pf(TickArgs a) {
 }
 
 // One pair of the worklist: the exact path and both members' shares.
-template <int LAW, bool XS>
+template <int LAW, bool XS, int KIND>
 __device__ __forceinline__ void pair_item(const TickArgs& a, const uint4& it) {
     const uint32_t e = it.x, i = it.y, ent = it.z, meta = it.w;
     const d3 Pi = XS ? mk(0.0, 0.0, 0.0) : ld(a.xA, i);
     f3 Jp, tA, tB;
-    const int app = exact_pair<LAW, XS>(a, a.scenes[a.scene_of[i]], i, Pi, e, ent, meta, Jp, tA, tB);
+    const int app = exact_pair<LAW, XS, KIND>(a, a.scenes[a.scene_of[i]], i, Pi, e, ent, meta, Jp, tA, tB);
     // each member's share at its own entry: the slave adds J and tA, the master -J and tB
     // (the negation is exact, so the sums see the single tick's values)
     const bool i_slave = meta & META_SLAVE;
@@ -1243,19 +1245,23 @@ __device__ __forceinline__ void pair_item(const TickArgs& a, const uint4& it) {
     }
 }
 
-// The worklist's pairs from `first` in strides of `stride`: sphere pairs, then wall pairs (only
-// the warp that straddles the two mixes them).
-template <int LAW, bool XS>
+// The worklist's pairs from `first` in strides of `stride`: KIND 1 the sphere pairs (from the
+// worklist's start), KIND 2 the wall pairs (from its end).  Two kernels: the sphere-pair one
+// carries no call of the wall detector, and so no spills.
+template <int LAW, bool XS, int KIND>
 __device__ __forceinline__ void pairs_from(const TickArgs& a, uint32_t first, uint32_t stride) {
     const uint32_t nw = min(a.nwork[0], a.pcap), nww = min(a.nwork[-1], a.pcap - nw);
-    for (uint32_t q = first; q < nw + nww; q += stride)
-        pair_item<LAW, XS>(a, a.pwork[q < nw ? q : a.pcap - 1u - (q - nw)]);
+    if (KIND == 1) {
+        for (uint32_t q = first; q < nw; q += stride) pair_item<LAW, XS, 1>(a, a.pwork[q]);
+    } else {
+        for (uint32_t q = first; q < nww; q += stride) pair_item<LAW, XS, 2>(a, a.pwork[a.pcap - 1u - q]);
+    }
 }
-template <int LAW, bool XS>
-__global__ void __launch_bounds__(TPB, 4) k_tick_pairs(TickArgs a) {     // 64 registers (a few spill)
+template <int LAW, bool XS, int KIND>
+__global__ void __launch_bounds__(TPB, 4) k_tick_pairs(TickArgs a) {     // sphere pairs: 56 registers, no spills
     step_order();
     if (held_step(a)) return;
-    pairs_from<LAW, XS>(a, blockIdx.x * blockDim.x + threadIdx.x, gridDim.x * blockDim.x);
+    pairs_from<LAW, XS, KIND>(a, blockIdx.x * blockDim.x + threadIdx.x, gridDim.x * blockDim.x);
 }
 
 // One sphere's sums and integration (or, in an identity step, its state carried over); returns its
@@ -1645,7 +1651,10 @@ __global__ void __launch_bounds__(FORM == 2 ? 1024 : 512, 1) k_persist(PersistAr
             if (!hold)
                 for (uint32_t s = gw; s * 32u < n; s += W) pf_sphere(a, s * 32u + lane);
             if (!grid_sync(p.bar, site++)) return;
-            if (!hold) pairs_from<LAW, XS>(a, gw * 32u + lane, W * 32u);
+            if (!hold) {
+                pairs_from<LAW, XS, 1>(a, gw * 32u + lane, W * 32u);
+                pairs_from<LAW, XS, 2>(a, gw * 32u + lane, W * 32u);
+            }
             if (!grid_sync(p.bar, site++)) return;
             for (uint32_t s = gw; s * 32u < n; s += W) {
                 const uint32_t i = s * 32u + lane;
@@ -3690,8 +3699,13 @@ void MixedEngine::launch_step(bool write_imp) {
         // the pair kernel strides over the worklist with the grid that is resident at once
 #define VEDO_PAIRS(L)                                                                                       \
     {                                                                                                       \
-        auto kp = xs_stored_ ? k_tick_pairs<L, true> : k_tick_pairs<L, false>;                              \
+        auto kp = xs_stored_ ? k_tick_pairs<L, true, 1> : k_tick_pairs<L, false, 1>;                        \
+        auto kw = xs_stored_ ? k_tick_pairs<L, true, 2> : k_tick_pairs<L, false, 2>;                        \
         note(step_launch(dep, kp, resident_grid((const void*)kp), (unsigned)tpb_, stream_, a));             \
+        if (!glob_.empty()) {                                                                               \
+            note(step_launch(dep, kw, (unsigned)sms_ * 4u, (unsigned)tpb_, stream_, a));                     \
+            ++launches_;                                                                                    \
+        }                                                                                                   \
     }
         switch (law_) {
         case IS_BSDBF: VEDO_PAIRS(IS_BSDBF); break;
