@@ -1257,8 +1257,19 @@ __device__ __forceinline__ void pairs_from(const TickArgs& a, uint32_t first, ui
         for (uint32_t q = first; q < nww; q += stride) pair_item<LAW, XS, 2>(a, a.pwork[a.pcap - 1u - q]);
     }
 }
-template <int LAW, bool XS, int KIND>
+// AFTER_WALLS: launched after the wall-pair kernel, whose blocks all waited for the prefilter pass
+// before releasing this one, so the worklist is complete when it starts; it waits for the
+// wall-pair kernel only at its end, so that the two run side by side (the wall pairs' FP64 work
+// and the sphere pairs' gathers use different units), and the sum kernel after it, waiting for
+// it, then waits for both.
+template <int LAW, bool XS, int KIND, bool AFTER_WALLS>
 __global__ void __launch_bounds__(TPB, 4) k_tick_pairs(TickArgs a) {     // sphere pairs: 56 registers, no spills
+    if (AFTER_WALLS) {
+        asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+        if (!held_step(a)) pairs_from<LAW, XS, KIND>(a, blockIdx.x * blockDim.x + threadIdx.x, gridDim.x * blockDim.x);
+        asm volatile("griddepcontrol.wait;" ::: "memory");
+        return;
+    }
     step_order();
     if (held_step(a)) return;
     pairs_from<LAW, XS, KIND>(a, blockIdx.x * blockDim.x + threadIdx.x, gridDim.x * blockDim.x);
@@ -3699,12 +3710,19 @@ void MixedEngine::launch_step(bool write_imp) {
         // the pair kernel strides over the worklist with the grid that is resident at once
 #define VEDO_PAIRS(L)                                                                                       \
     {                                                                                                       \
-        auto kp = xs_stored_ ? k_tick_pairs<L, true, 1> : k_tick_pairs<L, false, 1>;                        \
-        auto kw = xs_stored_ ? k_tick_pairs<L, true, 2> : k_tick_pairs<L, false, 2>;                        \
-        note(step_launch(dep, kp, resident_grid((const void*)kp), (unsigned)tpb_, stream_, a));             \
-        if (!glob_.empty()) {                                                                               \
+        auto kw = xs_stored_ ? k_tick_pairs<L, true, 2, false> : k_tick_pairs<L, false, 2, false>;          \
+        if (!glob_.empty() && dep) {   /* the wall pairs, then the sphere pairs beside them */             \
+            auto kp = xs_stored_ ? k_tick_pairs<L, true, 1, true> : k_tick_pairs<L, false, 1, true>;        \
             note(step_launch(dep, kw, (unsigned)sms_ * 4u, (unsigned)tpb_, stream_, a));                     \
+            note(step_launch(dep, kp, resident_grid((const void*)kp), (unsigned)tpb_, stream_, a));         \
             ++launches_;                                                                                    \
+        } else {                                                                                            \
+            auto kp = xs_stored_ ? k_tick_pairs<L, true, 1, false> : k_tick_pairs<L, false, 1, false>;      \
+            note(step_launch(dep, kp, resident_grid((const void*)kp), (unsigned)tpb_, stream_, a));         \
+            if (!glob_.empty()) {                                                                           \
+                note(step_launch(dep, kw, (unsigned)sms_ * 4u, (unsigned)tpb_, stream_, a));                 \
+                ++launches_;                                                                                \
+            }                                                                                               \
         }                                                                                                   \
     }
         switch (law_) {
