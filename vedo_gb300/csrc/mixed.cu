@@ -1114,12 +1114,13 @@ __global__ void __launch_bounds__(TPB) k_wrap(TickArgs a) {
 }
 
 // ---- pair pass ------------------------------------------------------------------------------
-// The tick in three kernels, each pair on the exact path evaluated once:
+// The tick in three stages, each pair on the exact path evaluated once:
 //  k_tick_pf     every sphere's list walk in prefilter form (with the single tick's history
 //                cleaning and clean-walk count), marking the entries on the exact path and
 //                appending each such pair once, at its history owner, to a worklist;
-//  k_tick_pairs  one thread per pair of the worklist: the exact path (exact_pair, the single
-//                tick's arithmetic) writes each member's share of the impulse and torque at that
+//  k_tick_pairs  one thread per pair of the worklist, the wall pairs and the sphere pairs in two
+//                kernels that run side by side: the exact path (exact_pair, the single tick's
+//                arithmetic) writes each member's share of the impulse and torque at that
 //                member's own entry of the pair;
 //  k_tick_sum    one thread per sphere: the shares at its marked entries, in entry order, join
 //                the compensated sums, then the sphere is integrated (finish_sphere).
