@@ -4547,7 +4547,7 @@ uint32_t mixed_num_scenes(EngineBase* e) {
 }
 
 // The persistent tick's grid barrier on its own (vedo_gpu_barrier_check).
-static int barrier_check(int device, uint32_t rounds, uint32_t extra, uint64_t limit_ns, uint32_t out[4]) {
+static int barrier_check_on(int device, uint32_t rounds, uint32_t extra, uint64_t limit_ns, uint32_t out[4]) {
     if (cudaSetDevice(device) != cudaSuccess) return VEDO_ERR_CUDA;
     int sms = 0, b = 0;
     if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device) != cudaSuccess) return VEDO_ERR_CUDA;
@@ -4578,6 +4578,14 @@ static int barrier_check(int device, uint32_t rounds, uint32_t extra, uint64_t l
     out[1] = h[7];
     out[2] = h[2];
     out[3] = h[3];
+    return rc;
+}
+// (the caller's current device is left as it was)
+static int barrier_check(int device, uint32_t rounds, uint32_t extra, uint64_t limit_ns, uint32_t out[4]) {
+    int prev = 0;
+    if (cudaGetDevice(&prev) != cudaSuccess) return VEDO_ERR_CUDA;
+    const int rc = barrier_check_on(device, rounds, extra, limit_ns, out);
+    cudaSetDevice(prev);
     return rc;
 }
 
