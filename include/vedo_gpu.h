@@ -198,8 +198,10 @@ typedef struct vedo_engine_opts {
                                  kernels; for the full tick and the pair pass (split_tick 0 or 2)
                                  without mobile or constrained walls, other steps as before.  Each
                                  barrier's wait is bounded (2 s): on expiry the call returns
-                                 VEDO_ERR_CUDA and the engine's state is undefined.  Identical
-                                 results; the autotuner chooses (default 0)              */
+                                 VEDO_ERR_CUDA and the engine's state is undefined (kernels of
+                                 other streams or processes holding SMs for seconds delay its
+                                 blocks and can cause that).  Identical results; the autotuner
+                                 chooses (default 0)                                      */
 } vedo_engine_opts;
 
 typedef struct vedo_gpu_engine vedo_gpu_engine;
